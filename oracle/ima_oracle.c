@@ -1,0 +1,646 @@
+/*
+ * ima_oracle.c -- CPU restatement of IMa2p's hot-path arithmetic (FP64).
+ *
+ * TEST INFRASTRUCTURE ONLY: the parity checker for the GB300 kernels.  Only
+ * tests/, __graft_entry__.smoke() and bench.py's CPU legs load it; the
+ * product library never links or calls it.
+ *
+ * Each block names the reference function it restates (paths relative to
+ * the IMa2p tree).  The restatement is pinned against the compiled
+ * reference (oracle/_ref/imaref) by tests/test_oracle_vs_ref.py and against
+ * the committed fixtures in tests/golden/.
+ */
+#include "ima_oracle.h"
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORA_REJECT_IS (-1000000000.0) /* imamp.hpp:157 */
+#define ORA_BESSI_MIN (-1e+100)       /* imamp.hpp:173 */
+#define ORA_LOG2 0.69314718055994530941723212146
+#define ORA_LOG10 2.3025850929940456840
+
+/* ======================================================================
+ * Infinite sites.  labelgtree (calc_prob_data.cpp:537-581): starting at a
+ * tip, walk towards the root, merging the tip's 0/1 label into each parent
+ * according to the sister's label (-1 unset, 2 mixed); stop as soon as a
+ * parent's label is left unchanged.
+ * ==================================================================== */
+static void is_walk(int8_t *mut, const int *up0, const int *up1,
+                    const int *down, int e)
+{
+  for (;;) {
+    int p = down[e];
+    if (p < 0) return;
+    int sis = (up0[p] == e) ? up1[p] : up0[p];
+    int8_t me = mut[e], mp = mut[p], ms = mut[sis];
+    if (mp != me) {
+      if (me == 2)
+        mut[p] = (ms != -1) ? ms : 2;
+      else if (ms != -1 && ms != 2 && ms != me)
+        mut[p] = 2;
+      else
+        mut[p] = me;
+    } else if (mp == 2 && ms != -1 && ms != 2) {
+      mut[p] = ms;
+    } else {
+      return;
+    }
+    e = p;
+  }
+}
+
+static void is_label_site(int n, int S, int site, const int8_t *seq,
+                          const int *up0, const int *up1, const int *down,
+                          int8_t *mut)
+{
+  int nl = 2 * n - 1;
+  for (int j = 0; j < n; j++) mut[j] = seq[(size_t)j * S + site];
+  for (int j = n; j < nl; j++) mut[j] = -1;
+  for (int j = 0; j < n; j++) is_walk(mut, up0, up1, down, j);
+}
+
+static inline int is_split(const int8_t *mut, int a, int b)
+{
+  return (mut[a] == 0 && mut[b] == 1) || (mut[a] == 1 && mut[b] == 0);
+}
+
+static inline double branch_len(const int *up0, const double *time, int c)
+{
+  int u = up0[c];
+  return (u == -1) ? time[c] : time[c] - time[u];
+}
+
+int ora_is_sumlogk(int n, int S, const int8_t *seq, const int *up0,
+                   const int *up1, const int *down, double *sumlogk,
+                   int *counts)
+{
+  int nl = 2 * n - 1;
+  int8_t *mut = (int8_t *)malloc((size_t)nl);
+  memset(counts, 0, sizeof(int) * (size_t)(n - 1));
+  *sumlogk = 0.0;
+  for (int site = 0; site < S; site++) {
+    is_label_site(n, S, site, seq, up0, up1, down, mut);
+    int hit = -1;
+    for (int node = n; node < nl; node++) {
+      if (is_split(mut, up0[node], up1[node])) {
+        if (hit != -1) { free(mut); return 1; }
+        hit = node;
+        counts[node - n]++;
+      }
+    }
+    if (hit == -1) { free(mut); return 2; }
+  }
+  double sum = 0.0;
+  for (int i = 0; i < n - 1; i++) {
+    double f = 1.0;
+    for (int j = 1; j <= counts[i]; j++) f *= (double)j;
+    sum += log(f);
+  }
+  *sumlogk = sum;
+  free(mut);
+  return 0;
+}
+
+double ora_is_likelihood(int n, int S, const int8_t *seq, const int *up0,
+                         const int *up1, const int *down, const double *time,
+                         double length, double u, double sumlogk,
+                         int *site_node, int *status)
+{
+  int nl = 2 * n - 1;
+  int8_t *mut = (int8_t *)malloc((size_t)nl);
+  double p = -length * u;
+  *status = 0;
+  for (int site = 0; site < S; site++) {
+    is_label_site(n, S, site, seq, up0, up1, down, mut);
+    int hit = -1;
+    double t = 0.0;
+    for (int node = n; node < nl; node++) {
+      int a = up0[node], b = up1[node];
+      if (!is_split(mut, a, b)) continue;
+      if (hit != -1) {
+        free(mut);
+        *status = 1;
+        if (site_node) site_node[site] = -2;
+        return ORA_REJECT_IS;
+      }
+      if (down[node] == -1)
+        t = branch_len(up0, time, a) + branch_len(up0, time, b);
+      else if (mut[down[node]] == mut[a])
+        t = branch_len(up0, time, b);
+      else
+        t = branch_len(up0, time, a);
+      hit = node;
+    }
+    if (site_node) site_node[site] = hit;
+    if (hit == -1) { free(mut); *status = 2; return 0.0; }
+    p = p + log(t * u);
+  }
+  free(mut);
+  return p - sumlogk;
+}
+
+/* ======================================================================
+ * HKY85 pruning (makefrac, calc_prob_data.cpp:118-471; getstandfactor
+ * :473-493; likelihoodHKY :583-607).  P_jk(b) with Pi_k / A_k taken from
+ * the purine/pyrimidine class of the target state k.
+ * ==================================================================== */
+double ora_hky_standfactor(const double *pi, double kappa)
+{
+  double p = 0.0;
+  for (int i = 0; i < 4; i++)
+    for (int j = 0; j < 4; j++) {
+      if (i == j) continue;
+      if (i + j == 2 || i + j == 4) p += pi[i] * pi[j] * kappa;
+      else p += pi[i] * pi[j];
+    }
+  return p;
+}
+
+static void hky_pmatrix(const double *pi, double kappa, double b, double P[4][4])
+{
+  double e1 = exp(-b);
+  for (int k = 0; k < 4; k++) {
+    double Pk = (k == 0 || k == 2) ? pi[0] + pi[2] : pi[1] + pi[3];
+    double A = 1.0 + Pk * (kappa - 1.0);
+    double e2 = exp(-b * A);
+    for (int j = 0; j < 4; j++) {
+      if (j == k)
+        P[j][k] = pi[k] + pi[k] * e1 * (1.0 / Pk - 1.0) + e2 * ((Pk - pi[k]) / Pk);
+      else if (j + k == 2 || j + k == 4)
+        P[j][k] = pi[k] + pi[k] * e1 * (1.0 / Pk - 1.0) - (pi[k] / Pk) * e2;
+      else
+        P[j][k] = pi[k] * (1.0 - e1);
+    }
+  }
+}
+
+typedef struct {
+  int n, S;
+  const int8_t *seq;
+  const double *pi;
+  const int *up0, *up1;
+  const double *time;
+  double mu, kappa;
+  const int *e;
+  double *frac, *newfrac, *sf;
+} hky_job;
+
+/* returns 1 when `node` was recomputed or is itself on the dirty list */
+static int hky_visit(hky_job *J, int node)
+{
+  const int *e = J->e;
+  int ret = (node == e[0] || node == e[1] || node == e[2] || node == e[3] || e[0] == -1);
+  int c[2] = {J->up0[node], J->up1[node]};
+  if (c[0] == -1) return ret;
+  int fresh[2];
+  for (int k = 0; k < 2; k++) {
+    fresh[k] = hky_visit(J, c[k]);
+    if (fresh[k]) ret = 1;
+  }
+  if (!ret) return 0;
+  int S = J->S;
+  double P[2][4][4];
+  for (int k = 0; k < 2; k++)
+    hky_pmatrix(J->pi, J->kappa, J->mu * branch_len(J->up0, J->time, c[k]), P[k]);
+  for (int i = 0; i < S; i++) {
+    double v[2][4];
+    double scale = 0.0;
+    for (int k = 0; k < 2; k++) {
+      int ch = c[k];
+      if (J->up0[ch] == -1) {
+        int s = J->seq[(size_t)ch * S + i];
+        for (int j = 0; j < 4; j++) v[k][j] = P[k][j][s];
+      } else {
+        const double *L = (fresh[k] ? J->newfrac : J->frac) + ((size_t)ch * S + i) * 4;
+        for (int j = 0; j < 4; j++)
+          v[k][j] = P[k][j][0] * L[0] + P[k][j][1] * L[1] + P[k][j][2] * L[2] + P[k][j][3] * L[3];
+        scale += J->sf[(size_t)ch * S + i];
+      }
+    }
+    double *out = J->newfrac + ((size_t)node * S + i) * 4;
+    double mx = 0.0;
+    for (int j = 0; j < 4; j++) {
+      out[j] = v[0][j] * v[1][j];
+      if (out[j] > mx) mx = out[j];
+    }
+    for (int j = 0; j < 4; j++) out[j] /= mx;
+    J->sf[(size_t)node * S + i] = scale + log(mx);
+  }
+  return 1;
+}
+
+double ora_hky_likelihood(int n, int S, int totsites, const int8_t *seq,
+                          const int *mult, const double *pi, const int *up0,
+                          const int *up1, const int *down, int root,
+                          const double *time, double u, double kappa,
+                          const int *e, double *frac, double *newfrac,
+                          double *sf, double *oldsf)
+{
+  (void)down; (void)oldsf;
+  hky_job J;
+  J.n = n; J.S = S; J.seq = seq; J.pi = pi; J.up0 = up0; J.up1 = up1;
+  J.time = time; J.kappa = kappa; J.e = e;
+  J.frac = frac; J.newfrac = newfrac; J.sf = sf;
+  J.mu = u / ((double)totsites * ora_hky_standfactor(pi, kappa));
+  for (int i = n; i < 2 * n - 1; i++) newfrac[(size_t)i * S * 4] = -1.0;
+  hky_visit(&J, root);
+  double p = 0.0;
+  for (int i = 0; i < S; i++) {
+    const double *L = newfrac + ((size_t)root * S + i) * 4;
+    double f = 0.0;
+    for (int j = 0; j < 4; j++) f += pi[j] * L[j];
+    p += mult[i] * (log(f) + sf[(size_t)root * S + i]);
+  }
+  return p;
+}
+
+void ora_hky_copyfraclike(int n, int S, const double *newfrac, double *frac)
+{
+  for (int i = n; i < 2 * n - 1; i++) {
+    const double *src = newfrac + (size_t)i * S * 4;
+    if (src[0] != -1.0) memcpy(frac + (size_t)i * S * 4, src, sizeof(double) * 4 * (size_t)S);
+  }
+}
+
+void ora_hky_storescalefactors(int n, int S, const double *sf, double *oldsf)
+{
+  memcpy(oldsf + (size_t)n * S, sf + (size_t)n * S, sizeof(double) * (size_t)(n - 1) * S);
+}
+
+void ora_hky_restorescalefactors(int n, int S, double *sf, const double *oldsf)
+{
+  memcpy(sf + (size_t)n * S, oldsf + (size_t)n * S, sizeof(double) * (size_t)(n - 1) * S);
+}
+
+/* ======================================================================
+ * Bessel I_n as the reference evaluates it: Abramowitz & Stegun 9.8.1-9.8.4
+ * polynomials for n = 0, 1 (utilities.cpp:54-124) and Miller's downward
+ * recurrence from j = 2(n + floor(sqrt(40 n))) with 1e10 rescaling for
+ * n >= 2 (utilities.cpp:1449-1496).
+ * ==================================================================== */
+static const double AS_I0_SMALL[7] = {1.0, 3.5156229, 3.0899424, 1.2067492,
+                                      0.2659732, 0.360768e-1, 0.45813e-2};
+static const double AS_I0_LARGE[9] = {0.39894228, 0.1328592e-1, 0.225319e-2,
+                                      -0.157565e-2, 0.916281e-2, -0.2057706e-1,
+                                      0.2635537e-1, -0.1647633e-1, 0.392377e-2};
+static const double AS_I1_SMALL[7] = {0.5, 0.87890594, 0.51498869, 0.15084934,
+                                      0.2658733e-1, 0.301532e-2, 0.32411e-3};
+static const double AS_I1_LARGE[9] = {0.39894228, -0.3988024e-1, -0.362018e-2,
+                                      0.163801e-2, -0.1031555e-1, 0.2282967e-1,
+                                      -0.2895312e-1, 0.1787654e-1, -0.420059e-2};
+
+static double horner(const double *c, int m, double y)
+{
+  double r = c[m - 1];
+  for (int k = m - 2; k >= 0; k--) r = c[k] + y * r;
+  return r;
+}
+
+double ora_bessi0(double x)
+{
+  double ax = fabs(x);
+  if (ax < 3.75) {
+    double y = x / 3.75;
+    y *= y;
+    return horner(AS_I0_SMALL, 7, y);
+  }
+  double y = 3.75 / ax;
+  return (exp(ax) / sqrt(ax)) * horner(AS_I0_LARGE, 9, y);
+}
+
+double ora_bessi1(double x)
+{
+  double ax = fabs(x), ans;
+  if (ax < 3.75) {
+    double y = x / 3.75;
+    y *= y;
+    ans = ax * horner(AS_I1_SMALL, 7, y);
+  } else {
+    double y = 3.75 / ax;
+    /* the reference evaluates the tail (coefficients 5..8) first */
+    double tail = AS_I1_LARGE[5] + y * (AS_I1_LARGE[6] + y * (AS_I1_LARGE[7] + y * AS_I1_LARGE[8]));
+    ans = AS_I1_LARGE[0] + y * (AS_I1_LARGE[1] + y * (AS_I1_LARGE[2] + y * (AS_I1_LARGE[3] + y * (AS_I1_LARGE[4] + y * tail))));
+    ans *= (exp(ax) / sqrt(ax));
+  }
+  return x < 0.0 ? -ans : ans;
+}
+
+double ora_bessi(int n, double x)
+{
+  n = abs(n);
+  if (x > 700) return DBL_MAX / 1e10;
+  if (n == 0) return ora_bessi0(x);
+  if (n == 1) return ora_bessi1(x);
+  if (x == 0.0) return 0.0;
+  double tox = 2.0 / fabs(x);
+  double bip = 0.0, ans = 0.0, bi = 1.0;
+  for (int j = 2 * (n + (int)sqrt(40.0 * n)); j > 0; j--) {
+    double bim = bip + j * tox * bi;
+    bip = bi;
+    bi = bim;
+    if (fabs(bi) > 1.0e10) {
+      ans *= 1.0e-10;
+      bi *= 1.0e-10;
+      bip *= 1.0e-10;
+    }
+    if (j == n) ans = bip;
+  }
+  ans *= ora_bessi0(x) / bi;
+  return (x < 0.0 && (n & 1)) ? -ans : ans;
+}
+
+double ora_sw_branch_term(int d, double t, double u)
+{
+  double b = ora_bessi(d, t * u);
+  if (!(b > 0.0)) return ORA_BESSI_MIN;
+  return -(t * u) + log(b);
+}
+
+double ora_sw_likelihood(int n, const int *A, const int *down, const int *up0,
+                         const double *time, double u, double tr,
+                         double *dlikeA)
+{
+  int nl = 2 * n - 1, zero = 0;
+  double like = 0.0;
+  for (int i = 0; i < nl; i++) {
+    if (down[i] == -1) { if (dlikeA) dlikeA[i] = 0.0; continue; }
+    int d = A[i] - A[down[i]];
+    double t = (up0[i] == -1) ? time[i] * tr : tr * (time[i] - time[up0[i]]);
+    double b = ora_bessi(d, t * u);
+    double v;
+    if (!(b > 0.0)) { zero = 1; v = ORA_BESSI_MIN; }
+    else v = -(t * u) + log(b);
+    if (dlikeA) dlikeA[i] = v;
+    like += v;
+  }
+  return zero ? -DBL_MAX : like;
+}
+
+/* ======================================================================
+ * MT19937 (Matsumoto & Nishimura 1998), as vendored at utilities.cpp:323-427
+ * ==================================================================== */
+void ora_mt_seed(ora_mt *s, uint32_t seed)
+{
+  s->mt[0] = seed;
+  for (int i = 1; i < 624; i++)
+    s->mt[i] = 1812433253u * (s->mt[i - 1] ^ (s->mt[i - 1] >> 30)) + (uint32_t)i;
+  s->mti = 624;
+}
+
+uint32_t ora_mt_u32(ora_mt *s)
+{
+  if (s->mti >= 624) {
+    for (int k = 0; k < 624; k++) {
+      uint32_t y = (s->mt[k] & 0x80000000u) | (s->mt[(k + 1) % 624] & 0x7fffffffu);
+      s->mt[k] = s->mt[(k + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+    }
+    s->mti = 0;
+  }
+  uint32_t y = s->mt[s->mti++];
+  y ^= y >> 11;
+  y ^= (y << 7) & 0x9d2c5680u;
+  y ^= (y << 15) & 0xefc60000u;
+  y ^= y >> 18;
+  return y;
+}
+
+double ora_mt_uniform(ora_mt *s)
+{
+  return ((double)ora_mt_u32(s) + 0.5) * 2.32830643653869628906e-10;
+}
+
+void ora_mt_fill_u32(uint32_t seed, int count, uint32_t *out)
+{
+  ora_mt s;
+  ora_mt_seed(&s, seed);
+  for (int i = 0; i < count; i++) out[i] = ora_mt_u32(&s);
+}
+
+/* ======================================================================
+ * MC3 (setheat swapchains.cpp:71-178; swapchains :526-653; swapweight :12-34)
+ * ==================================================================== */
+int ora_setheat(int nchains, double h1, double h2, int heatmode, double *beta,
+                double *allbetas)
+{
+  int N = nchains;
+  if (N == 1) { beta[0] = allbetas[0] = 1.0; return 0; }
+  for (int i = 0; i < N; i++) {
+    if (heatmode == 0) allbetas[i] = 1.0 / (1.0 + h1 * i);
+    else if (heatmode == 1) allbetas[i] = 1 - (1 - h2) * (i) * pow(h1, (double)(N - 1 - i)) / (double)(N - 1);
+    else allbetas[i] = 1.0 - i * (1.0 / (N - 1));
+  }
+  double hl = (heatmode == 0 && h1 < 0.05) ? 0.05 : h1;
+  for (int i = 0; i < N; i++) {
+    if (heatmode == 0) beta[i] = 1.0 / (1.0 + hl * i);
+    else if (heatmode == 1) beta[i] = 1 - (1 - h2) * (i) * pow(h1, (double)(N - 1 - i)) / (double)(N - 1);
+    else beta[i] = 1.0 - i * (1.0 / (N - 1));
+    if (beta[i] <= 0.0 || beta[i] > 1.0) return 1;
+  }
+  return 0;
+}
+
+void ora_chain_sums(int nchains, int nloci, const double *pdg,
+                    const double *probg, int include_probg, double *S)
+{
+  for (int c = 0; c < nchains; c++) {
+    double s = 0.0;
+    for (int l = 0; l < nloci; l++) s += pdg[(size_t)c * nloci + l];
+    if (include_probg) s += probg[c];
+    S[c] = s;
+  }
+}
+
+static int beta_index(int N, const double *allbetas, double b)
+{
+  for (int p = 0; p < N; p++)
+    if (allbetas[p] == b) return p;
+  return -1;
+}
+
+int ora_swapchains(int nchains, int swaptries, const double *S, double *beta,
+                   const double *allbetas, const double *u, int *used,
+                   int *swapcount, int *tempcount, int *accepted_pairs)
+{
+  int n = nchains, k = 0, swap0ok = 0;
+  for (int t = 0; t < swaptries; t++) {
+    int ci, cj, cjmin, cjrange;
+    do { ci = (int)(u[k++] * n); } while (ci < 0 || ci >= n);
+    if (n < 2 * 7 + 3) { cjmin = 0; cjrange = n; }
+    else {
+      cjmin = ci - 7 > 0 ? ci - 7 : 0;
+      cjrange = (n < ci + 7 ? n : ci + 7) - cjmin;
+    }
+    do { cj = cjmin + (int)(u[k++] * cjrange); } while (cj == ci || cj < 0 || cj >= n);
+    int p = beta_index(n, allbetas, beta[ci]);
+    int q = beta_index(n, allbetas, beta[cj]);
+    int hi = ci > cj ? ci : cj, lo = ci > cj ? cj : ci;
+    int phi = p > q ? p : q, plo = p > q ? q : p;
+    if (p >= 0 && q >= 0) tempcount[phi * n + plo]++;
+    swapcount[hi * n + lo]++;
+    double w = exp((beta[ci] - beta[cj]) * (S[cj] - S[ci]));
+    int acc = 0;
+    if (w >= 1.0) acc = 1;
+    else if (w > u[k++]) acc = 1;
+    if (accepted_pairs) {
+      accepted_pairs[3 * t] = ci;
+      accepted_pairs[3 * t + 1] = cj;
+      accepted_pairs[3 * t + 2] = acc;
+    }
+    if (acc) {
+      double bt = beta[ci];
+      beta[ci] = beta[cj];
+      beta[cj] = bt;
+      swapcount[lo * n + hi]++;
+      if (p >= 0 && q >= 0) tempcount[plo * n + phi]++;
+      if (ci == 0 || cj == 0) swap0ok = 1;
+    }
+  }
+  *used = k;
+  return swap0ok;
+}
+
+/* ======================================================================
+ * L-mode surface (jointp, jointfind.cpp:885-1047; eexp utilities.cpp:1507-1540)
+ * ==================================================================== */
+void ora_gsamp_offsets(int np, int nm, int *ccp, int *fcp, int *hccp, int *mcp,
+                       int *fmp, int *qip, int *mip, int *pdgp, int *probgp)
+{
+  *ccp = 0;
+  *fcp = np;
+  *hccp = 2 * np;
+  *mcp = 3 * np;
+  *fmp = 3 * np + nm;
+  *qip = 3 * np + 2 * nm;
+  *mip = 4 * np + 2 * nm;
+  *pdgp = 4 * np + 3 * nm;
+  *probgp = *pdgp + 1;
+}
+
+void ora_surface_p(int G, int rowlen, const float *g, int np, int nm,
+                   int npops, int modeltype, const double *lognorm,
+                   const double *x, double *pout)
+{
+  int ccp, fcp, hccp, mcp, fmp, qip, mip, pdgp, probgp;
+  ora_gsamp_offsets(np, nm, &ccp, &fcp, &hccp, &mcp, &fmp, &qip, &mip, &pdgp, &probgp);
+  int lo = 0, hi = np + nm;
+  if (modeltype == 1) hi = np;
+  if (modeltype == 2) lo = np;
+  double logx[64], divx[64], l2d[64];
+  for (int i = 0; i < np; i++) l2d[i] = ORA_LOG2 - log(x[i]);
+  for (int i = lo; i < hi; i++) { logx[i] = log(x[i]); divx[i] = 1.0 / x[i]; }
+  for (int gi = 0; gi < G; gi++) {
+    const float *r = g + (size_t)gi * rowlen;
+    double p;
+    if (lognorm) p = lognorm[gi];
+    else if (npops == 2) p = -r[probgp];
+    else {
+      double s = 0.0;
+      if (modeltype == 1) for (int i = 0; i < np; i++) s += r[qip + i];
+      else for (int i = 0; i < nm; i++) s += r[mip + i];
+      p = -s;
+    }
+    for (int i = lo; i < hi; i++) {
+      if (i < np) {
+        double dg = 2.0 * r[fcp + i];
+        p += r[ccp + i] * l2d[i] - r[hccp + i] - dg * divx[i];
+      } else {
+        int i1 = i - np;
+        p += r[mcp + i1] * logx[i] - r[fmp + i1] * x[i];
+      }
+    }
+    pout[gi] = p;
+  }
+}
+
+double ora_jointp_exact(int G, int rowlen, const float *g, int np, int nm,
+                        int npops, int modeltype, const double *lognorm,
+                        const double *x, double *ess)
+{
+  double *p = (double *)malloc(sizeof(double) * (size_t)G);
+  ora_surface_p(G, rowlen, g, np, nm, npops, modeltype, lognorm, x, p);
+  double M = -INFINITY;
+  for (int i = 0; i < G; i++) if (p[i] > M) M = p[i];
+  long double s = 0.0L, s2 = 0.0L;
+  for (int i = 0; i < G; i++) {
+    long double w = expl((long double)(p[i] - M));
+    s += w;
+    s2 += w * w;
+  }
+  free(p);
+  if (ess) *ess = (double)(s * s / s2);
+  return log((double)G) - (M + (double)logl(s));
+}
+
+void ora_eexp(double x, double *m, int *z)
+{
+  static const double inv_fact[10] = {
+      1.0, 0.5, 0.16666666666666666666666666667, 0.04166666666666666666666666667,
+      0.00833333333333333333333333333, 0.001388888888888888888888888889,
+      0.000198412698412698412698412698, 0.000024801587301587301587301587301,
+      2.75573192239858906525573192239859e-6, 2.75573192239858906525573192239e-7};
+  const double log10_2 = 0.30102999566398119521;
+  int n = (int)floor(x / ORA_LOG2);
+  double zr = log10_2 * (double)n;
+  *z = (int)zr;
+  zr -= (double)*z;
+  double u = x - ((double)n) * ORA_LOG2;
+  double t = inv_fact[9];
+  for (int k = 8; k >= 0; k--) t = inv_fact[k] + u * t;
+  t = 1 + u * t;
+  *m = t * pow(10.0, zr);
+  if (fabs(*m) > 10) { *m = *m / 10.0; *z = *z + 1; }
+  if (fabs(*m) < 1) { *m = *m * 10.0; *z = *z - 1; }
+}
+
+static int cmp_desc(const void *a, const void *b)
+{
+  double x = *(const double *)a, y = *(const double *)b;
+  return (x < y) - (x > y);
+}
+
+double ora_jointp_compat(int G, int rowlen, const float *g, int np, int nm,
+                         int npops, int modeltype, const double *lognorm,
+                         const double *x, double *ess)
+{
+  double *p = (double *)malloc(sizeof(double) * (size_t)G);
+  double *list = (double *)malloc(sizeof(double) * (size_t)G);
+  ora_surface_p(G, rowlen, g, np, nm, npops, modeltype, lognorm, x, p);
+  /* list membership: the first value, then every value within 10 of the
+   * running maximum at the time it is seen */
+  int m = 0;
+  double runmax = p[0];
+  list[m++] = p[0];
+  for (int i = 1; i < G; i++) {
+    if (runmax - p[i] < 10) {
+      list[m++] = p[i];
+      if (p[i] > runmax) runmax = p[i];
+    }
+  }
+  qsort(list, (size_t)m, sizeof(double), cmp_desc);
+  int iin = m - 1;
+  int cnt = 0;
+  do { cnt++; } while (cnt < iin && list[0] - list[cnt] < 10);
+  double *mm = (double *)malloc(sizeof(double) * (size_t)cnt);
+  int *zz = (int *)malloc(sizeof(int) * (size_t)cnt);
+  int maxz = -10000000;
+  for (int i = 0; i < cnt; i++) {
+    ora_eexp(list[i], &mm[i], &zz[i]);
+    if (zz[i] > maxz) maxz = zz[i];
+  }
+  maxz -= 10;
+  double acc = 0.0, acc2 = 0.0;
+  for (int i = 0; i < cnt; i++) {
+    int zadj = zz[i] - maxz;
+    if (zadj > -308 && zadj < 308) mm[i] *= pow(10.0, (double)zadj);
+    else if (zadj <= -308) mm[i] = 0.0;
+    else mm[i] = DBL_MAX;
+    acc += mm[i];
+    acc2 += mm[i] * mm[i];
+  }
+  if (ess) *ess = acc * acc / acc2;
+  double q = log((double)G) - (log(acc) + maxz * ORA_LOG10);
+  free(mm); free(zz); free(p); free(list);
+  return q;
+}

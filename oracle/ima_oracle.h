@@ -1,0 +1,120 @@
+/*
+ * ima_oracle.h -- CPU restatement of IMa2p's hot-path arithmetic.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the parity checker for the
+ * GB300 kernels: only tests/, __graft_entry__.smoke() and bench.py's
+ * cpu_baseline / reference legs may load it.  The product path
+ * (ima2p_gb300/, libima2p_gb300.so) never calls it.
+ *
+ * Every function restates the reference algorithm cited beside it
+ * (paths relative to the IMa2p source tree).  The restatement is pinned
+ * against the compiled reference itself (oracle/_ref/imaref, built by
+ * oracle/Makefile from the untouched sources) by tests/test_oracle_vs_ref.py
+ * and by the committed fixtures under tests/golden/.
+ *
+ * Genealogy layout used throughout: numlines = 2n-1 nodes, tips 0..n-1,
+ * internal nodes n..2n-2; up0/up1 = daughter ids (-1 at tips), down =
+ * parent id (-1 at the root), time[c] = time at the lower end of edge c,
+ * so the branch length of c is time[c] (tip) or time[c]-time[up0[c]].
+ */
+#ifndef IMA_ORACLE_H
+#define IMA_ORACLE_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- infinite sites (calc_prob_data.cpp:537-836) ---------------------- */
+/* calc_sumlogk restated (calc_prob_data.cpp:609-719).  Returns 0 on success,
+ * 1 when a site maps to two mutation nodes (the reference returns early and
+ * leaves the constant at 0), 2 when a site maps to none (IM_err in the
+ * reference).  counts[n-1] receives the per-internal-node mutation counts. */
+int ora_is_sumlogk(int n, int S, const int8_t *seq, const int *up0,
+                   const int *up1, const int *down, double *sumlogk,
+                   int *counts);
+/* likelihoodIS restated (calc_prob_data.cpp:731-836).  site_node[S] gets the
+ * node whose daughters carry {0,1}.  *status: 0 ok, 1 = two mutation nodes
+ * (return value REJECTINFINITESITESCONSTANT), 2 = incompatible site. */
+double ora_is_likelihood(int n, int S, const int8_t *seq, const int *up0,
+                         const int *up1, const int *down, const double *time,
+                         double length, double u, double sumlogk,
+                         int *site_node, int *status);
+
+/* ---- HKY pruning (calc_prob_data.cpp:118-607, update_gtree_common.cpp:2140-2181) */
+/* Buffers: frac/newfrac [numlines][S][4], sf/oldsf [numlines][S] (only
+ * internal rows are used).  e[4] = dirty node ids, e[0] == -1 => full. */
+double ora_hky_likelihood(int n, int S, int totsites, const int8_t *seq,
+                          const int *mult, const double *pi, const int *up0,
+                          const int *up1, const int *down, int root,
+                          const double *time, double u, double kappa,
+                          const int *e, double *frac, double *newfrac,
+                          double *sf, double *oldsf);
+void ora_hky_copyfraclike(int n, int S, const double *newfrac, double *frac);
+void ora_hky_storescalefactors(int n, int S, const double *sf, double *oldsf);
+void ora_hky_restorescalefactors(int n, int S, double *sf, const double *oldsf);
+double ora_hky_standfactor(const double *pi, double kappa);
+
+/* ---- stepwise microsatellites (calc_prob_data.cpp:841-909, utilities.cpp:54-124, 1449-1496) */
+double ora_bessi0(double x);
+double ora_bessi1(double x);
+double ora_bessi(int n, double x);
+/* Returns the locus log-likelihood; dlikeA[numlines] receives the per-branch
+ * terms.  A[numlines] = allele states at the top of every edge. */
+double ora_sw_likelihood(int n, const int *A, const int *down, const int *up0,
+                         const double *time, double u, double tr,
+                         double *dlikeA);
+/* Rescore a list of branches with the per-branch term of likelihoodSW, as
+ * finishSWupdateA does for its 3-4 changed edges
+ * (update_gtree_common.cpp:2219-2362). */
+double ora_sw_branch_term(int d, double t, double u);
+
+/* ---- MT19937 (utilities.cpp:323-427) ----------------------------------- */
+typedef struct { uint32_t mt[624]; int mti; } ora_mt;
+void ora_mt_seed(ora_mt *s, uint32_t seed);
+uint32_t ora_mt_u32(ora_mt *s);
+double ora_mt_uniform(ora_mt *s);          /* genrand_real3: (k+0.5)/2^32 */
+void ora_mt_fill_u32(uint32_t seed, int count, uint32_t *out);
+
+/* ---- MC3 (swapchains.cpp:12-178, 526-662) ------------------------------ */
+/* setheat for one process (numprocesses=1): heatmode 0 linear, 1 geometric,
+ * 2 even (imamp.hpp heating enum order HLINEAR, HGEOMETRIC, HEVEN). */
+int ora_setheat(int nchains, double h1, double h2, int heatmode, double *beta,
+                double *allbetas);
+/* Serial swapchains with swapbetasonly=1.  S[c] = sum_loci pdg + probg
+ * (already reduced).  Uniforms come from u[] in order; *used returns how
+ * many were consumed.  swapcount/tempcount are nchains x nchains row-major
+ * and are incremented in place.  Returns swap0ok. */
+int ora_swapchains(int nchains, int swaptries, const double *S, double *beta,
+                   const double *allbetas, const double *u, int *used,
+                   int *swapcount, int *tempcount, int *accepted_pairs);
+/* S[c] = sum_li pdg[c*nloci+li] (in locus order) + probg[c] */
+void ora_chain_sums(int nchains, int nloci, const double *pdg,
+                    const double *probg, int include_probg, double *S);
+
+/* ---- L-mode surface (jointfind.cpp:885-1047) ---------------------------- */
+/* Column offsets of a gsampinf row (ginfo.cpp:288-316 / jointfind.cpp:914-926)
+ * for numpopsizeparams = np, nummigrateparams = nm. */
+void ora_gsamp_offsets(int np, int nm, int *ccp, int *fcp, int *hccp, int *mcp,
+                       int *fmp, int *qip, int *mip, int *pdgp, int *probgp);
+/* p_g for every genealogy at x.  modeltype 0 full (bias -probg), 1 theta
+ * only (bias -sum qi), 2 migration only (bias -sum mi); lognorm (optional,
+ * may be NULL) replaces the bias term with an FP64 per-genealogy value. */
+void ora_surface_p(int G, int rowlen, const float *g, int np, int nm,
+                   int npops, int modeltype, const double *lognorm,
+                   const double *x, double *p);
+/* Exact FP64 log-sum-exp form: q = log G - log sum_g exp(p_g) (+ESS). */
+double ora_jointp_exact(int G, int rowlen, const float *g, int np, int nm,
+                        int npops, int modeltype, const double *lognorm,
+                        const double *x, double *ess);
+/* The reference's truncated sum: linked list within PRANGELOG=10 of the
+ * running max, descending traversal with its off-by-one, eexp mantissa /
+ * decimal exponent accumulation. */
+double ora_jointp_compat(int G, int rowlen, const float *g, int np, int nm,
+                         int npops, int modeltype, const double *lognorm,
+                         const double *x, double *ess);
+void ora_eexp(double x, double *m, int *z);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

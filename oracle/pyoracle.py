@@ -1,0 +1,277 @@
+"""ctypes view of the CPU oracle (libima_oracle.so) and a runner for the
+compiled reference harness (_ref/imaref).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU legs, never by the product package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libima_oracle.so")
+REF_BIN = os.path.join(HERE, "_ref", "imaref")
+
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        _lib = C.CDLL(LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+P = C.c_void_p
+I = C.c_int
+D = C.c_double
+
+
+def _declare(L):
+    L.ora_is_sumlogk.argtypes = [I, I, P, P, P, P, P, P]
+    L.ora_is_sumlogk.restype = I
+    L.ora_is_likelihood.argtypes = [I, I, P, P, P, P, P, D, D, D, P, P]
+    L.ora_is_likelihood.restype = D
+    L.ora_hky_likelihood.argtypes = [I, I, I, P, P, P, P, P, P, I, P, D, D, P, P, P, P, P]
+    L.ora_hky_likelihood.restype = D
+    for f in ("ora_hky_copyfraclike", "ora_hky_storescalefactors", "ora_hky_restorescalefactors"):
+        getattr(L, f).argtypes = [I, I, P, P]
+        getattr(L, f).restype = None
+    L.ora_bessi.argtypes = [I, D]
+    L.ora_bessi.restype = D
+    L.ora_sw_likelihood.argtypes = [I, P, P, P, P, D, D, P]
+    L.ora_sw_likelihood.restype = D
+    L.ora_sw_branch_term.argtypes = [I, D, D]
+    L.ora_sw_branch_term.restype = D
+    L.ora_mt_fill_u32.argtypes = [C.c_uint32, I, P]
+    L.ora_mt_fill_u32.restype = None
+    L.ora_setheat.argtypes = [I, D, D, I, P, P]
+    L.ora_setheat.restype = I
+    L.ora_swapchains.argtypes = [I, I, P, P, P, P, P, P, P, P]
+    L.ora_swapchains.restype = I
+    L.ora_chain_sums.argtypes = [I, I, P, P, I, P]
+    L.ora_chain_sums.restype = None
+    L.ora_surface_p.argtypes = [I, I, P, I, I, I, I, P, P, P]
+    L.ora_surface_p.restype = None
+    for f in ("ora_jointp_exact", "ora_jointp_compat"):
+        getattr(L, f).argtypes = [I, I, P, I, I, I, I, P, P, P]
+        getattr(L, f).restype = D
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+# ----------------------------------------------------------------- IS
+def is_sumlogk(seq, g):
+    n, S = seq.shape
+    seq = np.ascontiguousarray(seq, np.int8)
+    out = np.zeros(1)
+    counts = np.zeros(n - 1, np.int32)
+    st = lib().ora_is_sumlogk(n, S, _p(seq), _p(_i32(g.up0)), _p(_i32(g.up1)),
+                              _p(_i32(g.down)), _p(out), _p(counts))
+    return st, float(out[0]), counts
+
+
+def is_likelihood(seq, g, length, u, sumlogk):
+    n, S = seq.shape
+    seq = np.ascontiguousarray(seq, np.int8)
+    node = np.zeros(max(S, 1), np.int32)
+    st = np.zeros(1, np.int32)
+    v = lib().ora_is_likelihood(n, S, _p(seq), _p(_i32(g.up0)), _p(_i32(g.up1)),
+                                _p(_i32(g.down)), _p(_f64(g.time)), length, u,
+                                sumlogk, _p(node), _p(st))
+    return v, int(st[0]), node[:S]
+
+
+# ---------------------------------------------------------------- HKY
+class HKYState:
+    """FP64 frac/newfrac/scalefactor buffers of one chain-locus."""
+
+    def __init__(self, n, S):
+        nl = 2 * n - 1
+        self.n, self.S = n, S
+        self.frac = np.zeros((nl, S, 4))
+        self.newfrac = np.zeros((nl, S, 4))
+        self.sf = np.zeros((nl, S))
+        self.oldsf = np.zeros((nl, S))
+
+    def likelihood(self, loc, g, u, kappa, e=(-1, -1, -1, -1)):
+        e = _i32(e)
+        return lib().ora_hky_likelihood(
+            self.n, self.S, loc.totsites, _p(np.ascontiguousarray(loc.seq, np.int8)),
+            _p(_i32(loc.mult)), _p(_f64(loc.pi)), _p(_i32(g.up0)), _p(_i32(g.up1)),
+            _p(_i32(g.down)), int(g.root), _p(_f64(g.time)), u, kappa, _p(e),
+            _p(self.frac), _p(self.newfrac), _p(self.sf), _p(self.oldsf))
+
+    def accept(self):
+        lib().ora_hky_copyfraclike(self.n, self.S, _p(self.newfrac), _p(self.frac))
+        lib().ora_hky_storescalefactors(self.n, self.S, _p(self.sf), _p(self.oldsf))
+
+    def reject(self):
+        lib().ora_hky_restorescalefactors(self.n, self.S, _p(self.sf), _p(self.oldsf))
+
+
+# ----------------------------------------------------------------- SW
+def sw_likelihood(A, g, u, tr=1.0):
+    n = g.n
+    dl = np.zeros(2 * n - 1)
+    v = lib().ora_sw_likelihood(n, _p(_i32(A)), _p(_i32(g.down)), _p(_i32(g.up0)),
+                                _p(_f64(g.time)), u, tr, _p(dl))
+    return v, dl
+
+
+def bessi(n, x):
+    return lib().ora_bessi(int(n), float(x))
+
+
+# ------------------------------------------------------------ MT / MC3
+def mt_u32(seed, count):
+    out = np.zeros(count, np.uint32)
+    lib().ora_mt_fill_u32(seed, count, _p(out))
+    return out
+
+
+def mt_uniforms(seed, count):
+    return (mt_u32(seed, count).astype(np.float64) + 0.5) * 2.32830643653869628906e-10
+
+
+def setheat(nchains, h1, h2, mode):
+    beta = np.zeros(nchains)
+    allb = np.zeros(nchains)
+    st = lib().ora_setheat(nchains, h1, h2, mode, _p(beta), _p(allb))
+    return st, beta, allb
+
+
+def chain_sums(pdg, probg, include_probg=True):
+    nch, nl = pdg.shape
+    S = np.zeros(nch)
+    lib().ora_chain_sums(nch, nl, _p(_f64(pdg)), _p(_f64(probg)), int(include_probg), _p(S))
+    return S
+
+
+def swapchains(S, beta, allbetas, swaptries, uniforms, swapcount, tempcount):
+    """Mutates beta, swapcount, tempcount in place; returns (swap0ok, used, decisions)."""
+    n = len(beta)
+    used = np.zeros(1, np.int32)
+    dec = np.zeros((swaptries, 3), np.int32)
+    ok = lib().ora_swapchains(n, swaptries, _p(_f64(S)), _p(beta), _p(_f64(allbetas)),
+                              _p(_f64(uniforms)), _p(used), _p(swapcount), _p(tempcount),
+                              _p(dec))
+    return ok, int(used[0]), dec
+
+
+# ------------------------------------------------------------ surface
+def surface_p(rows, np_, nm, npops, x, modeltype=0, lognorm=None):
+    G, rl = rows.shape
+    out = np.zeros(G)
+    rows = np.ascontiguousarray(rows, np.float32)
+    lib().ora_surface_p(G, rl, _p(rows), np_, nm, npops, modeltype,
+                        _p(_f64(lognorm)) if lognorm is not None else None,
+                        _p(_f64(x)), _p(out))
+    return out
+
+
+def jointp(rows, np_, nm, npops, x, modeltype=0, lognorm=None, compat=False):
+    G, rl = rows.shape
+    rows = np.ascontiguousarray(rows, np.float32)
+    ess = np.zeros(1)
+    f = lib().ora_jointp_compat if compat else lib().ora_jointp_exact
+    q = f(G, rl, _p(rows), np_, nm, npops, modeltype,
+          _p(_f64(lognorm)) if lognorm is not None else None, _p(_f64(x)), _p(ess))
+    return q, float(ess[0])
+
+
+# ------------------------------------------------- compiled reference
+def ref_available():
+    return os.path.exists(REF_BIN)
+
+
+def _tree_txt(g):
+    return " ".join(map(str, g.up0)) + "\n" + " ".join(map(str, g.up1)) + "\n" + \
+        " ".join(map(str, g.down)) + "\n" + " ".join("%.17g" % t for t in g.time) + "\n"
+
+
+def run_ref(mode, text):
+    with tempfile.NamedTemporaryFile("w", suffix=".txt", delete=False) as f:
+        f.write(text)
+        path = f.name
+    try:
+        out = subprocess.run([REF_BIN, mode, path], check=True, capture_output=True,
+                             text=True).stdout
+    finally:
+        os.unlink(path)
+    return out
+
+
+def ref_is(seq, trees, lengths, us):
+    n, S = seq.shape
+    t = [f"{n} {S}", " ".join(map(str, seq.ravel())), str(len(trees))]
+    for g, L, u in zip(trees, lengths, us):
+        t.append(_tree_txt(g) + "%.17g %.17g" % (L, u))
+    out = run_ref("is", "\n".join(t) + "\n")
+    return np.array([[float(v) for v in line.split()] for line in out.strip().splitlines()])
+
+
+def ref_hky(loc, items):
+    """items: list of (g, u, kappa, edits) where edits = [(g2, (e1..e4), accept)]."""
+    n, S = loc.seq.shape
+    t = [f"{n} {S} {loc.totsites}", " ".join(map(str, loc.seq.ravel())),
+         " ".join(map(str, loc.mult)), " ".join("%.17g" % p for p in loc.pi), str(len(items))]
+    for g, u, kappa, edits in items:
+        t.append(_tree_txt(g) + "%.17g %.17g %d" % (u, kappa, len(edits)))
+        for g2, e, acc in edits:
+            t.append(_tree_txt(g2) + " ".join(map(str, e)) + " %d" % acc)
+    out = run_ref("hky", "\n".join(t) + "\n")
+    return np.array([float(v) for v in out.split()])
+
+
+def ref_sw(trees, alleles, us, tr=1.0):
+    n = trees[0].n
+    t = [f"{n} {len(trees)}"]
+    for g, A, u in zip(trees, alleles, us):
+        t.append(_tree_txt(g) + " ".join(map(str, A)) + "\n%.17g %.17g" % (u, tr))
+    out = run_ref("sw", "\n".join(t) + "\n")
+    return np.array([[float(v) for v in line.split()] for line in out.strip().splitlines()])
+
+
+def ref_swap(pdg, probg, swaptries, nsteps, mode, h1, h2, seed):
+    nch, nl = pdg.shape
+    t = [f"{nch} {nl} {swaptries} {nsteps} {mode} %.17g %.17g {seed}" % (h1, h2),
+         " ".join("%.17g" % v for v in pdg.ravel()), " ".join("%.17g" % v for v in probg)]
+    out = run_ref("swap", "\n".join(t) + "\n").strip().splitlines()
+    steps = [line.split() for line in out[:nsteps]]
+    ok = np.array([int(s[0]) for s in steps])
+    betas = np.array([[float(v) for v in s[1:]] for s in steps])
+    sc = np.array([[int(v) for v in line.split()] for line in out[nsteps:nsteps + nch]])
+    tc = np.array([[int(v) for v in line.split()] for line in out[nsteps + nch:nsteps + 2 * nch]])
+    return ok, betas, sc, tc
+
+
+def ref_jointp(rows, np_, nm, npops, modeltype, points):
+    G, rl = rows.shape
+    t = [f"{G} {rl} {np_} {nm} {npops} {modeltype}",
+         "\n".join(" ".join("%.9g" % v for v in r) for r in rows), str(len(points))]
+    t += [" ".join("%.17g" % v for v in x) for x in points]
+    out = run_ref("jointp", "\n".join(t) + "\n")
+    return np.array([[float(v) for v in line.split()] for line in out.strip().splitlines()])

@@ -1,0 +1,7 @@
+/* ref_access.h -- accessors for reference file statics (test infrastructure). */
+#ifndef REF_ACCESS_H
+#define REF_ACCESS_H
+double refacc_sumlogk(int li);
+void refacc_jointp_setup(int nparams_total, int modeltype);
+double refacc_jointp(double *x, double *ess);
+#endif

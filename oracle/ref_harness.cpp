@@ -1,0 +1,251 @@
+/*
+ * ref_harness.cpp -- drives the UNMODIFIED IMa2p reference functions on
+ * dumped inputs, to pin the oracle restatement (oracle/ima_oracle.c) and to
+ * produce the golden fixtures under tests/golden/.
+ *
+ * TEST INFRASTRUCTURE ONLY.  oracle/Makefile compiles this file together with
+ * the reference sources where they lie (nothing is copied into this repo);
+ * the result, oracle/_ref/imaref, is git-ignored.
+ *
+ * The reference keeps some hot-path state in file statics (the sumlogk cache
+ * in calc_prob_data.cpp, jointp's list and model range in jointfind.cpp);
+ * ref_access_cpd.cpp and ref_access_jf.cpp include those two reference
+ * sources to reach them.  The other reference objects are linked unchanged.
+ *
+ * Usage:  imaref is|hky|sw|swap|jointp <input.txt>   (results on stdout)
+ */
+#undef GLOBVARS
+#include "imamp.hpp"
+#include "ref_access.h"
+#include <string>
+
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+static FILE *g_in;
+static int rd_i() { int v; if (fscanf(g_in, "%d", &v) != 1) { fprintf(stderr, "short input\n"); exit(3); } return v; }
+static double rd_d() { double v; if (fscanf(g_in, "%lf", &v) != 1) { fprintf(stderr, "short input\n"); exit(3); } return v; }
+
+static void alloc_chains(int nchains, int nl)
+{
+  numchains = nchains;
+  numprocesses = 1;
+  nloci = nl;
+  C = (struct chain **)calloc((size_t)nchains, sizeof(struct chain *));
+  for (int c = 0; c < nchains; c++) {
+    C[c] = (struct chain *)calloc(1, sizeof(struct chain));
+    C[c]->G = (struct genealogy *)calloc((size_t)nl, sizeof(struct genealogy));
+  }
+  L = (struct locus *)calloc((size_t)nl, sizeof(struct locus));
+}
+
+static struct edge *alloc_tree(int nlines)
+{
+  return (struct edge *)calloc((size_t)nlines, sizeof(struct edge));
+}
+
+/* reads up0[nl] up1[nl] down[nl] time[nl] into gtree */
+static void read_tree(struct edge *t, int nlines)
+{
+  for (int i = 0; i < nlines; i++) t[i].up[0] = rd_i();
+  for (int i = 0; i < nlines; i++) t[i].up[1] = rd_i();
+  for (int i = 0; i < nlines; i++) t[i].down = rd_i();
+  for (int i = 0; i < nlines; i++) t[i].time = rd_d();
+}
+
+static int find_root(struct edge *t, int nlines)
+{
+  for (int i = 0; i < nlines; i++) if (t[i].down == -1) return i;
+  return -1;
+}
+
+/* IS: n S seq[n*S] nitems {tree length u}*   ->  pdg sumlogk_cache own_sumlogk */
+static void run_is()
+{
+  int n = rd_i(), S = rd_i();
+  int nl = 2 * n - 1;
+  std::vector<int> seq((size_t)n * S);
+  for (auto &v : seq) v = rd_i();
+  int nitems = rd_i();
+  alloc_chains(nitems, 1);
+  L[0].numgenes = n;
+  L[0].numlines = nl;
+  L[0].numsites = S;
+  L[0].seq = (int **)malloc(sizeof(int *) * n);
+  for (int i = 0; i < n; i++) L[0].seq[i] = &seq[(size_t)i * S];
+  std::vector<double> us(nitems);
+  for (int c = 0; c < nitems; c++) {
+    C[c]->G[0].gtree = alloc_tree(nl);
+    read_tree(C[c]->G[0].gtree, nl);
+    C[c]->G[0].root = find_root(C[c]->G[0].gtree, nl);
+    C[c]->G[0].length = rd_d();
+    us[c] = rd_d();
+  }
+  for (int c = 0; c < nitems; c++) {
+    double pdg = likelihoodIS(c, 0, us[c]);
+    double own = 0.0;
+    calc_sumlogk(c, 0, &own);
+    printf("%.17g %.17g %.17g\n", pdg, refacc_sumlogk(0), own);
+  }
+}
+
+/* HKY: n S totsites seq mult pi[4] nitems
+ *   per item: tree u kappa nedits { tree e1 e2 e3 e4 accept }*
+ *   -> one line per evaluation */
+static void alloc_hky(struct edge *t, int n, int S)
+{
+  for (int i = n; i < 2 * n - 1; i++) {
+    t[i].hkyi.frac = (double **)malloc(sizeof(double *) * S);
+    t[i].hkyi.newfrac = (double **)malloc(sizeof(double *) * S);
+    for (int k = 0; k < S; k++) {
+      t[i].hkyi.frac[k] = (double *)calloc(4, sizeof(double));
+      t[i].hkyi.newfrac[k] = (double *)calloc(4, sizeof(double));
+    }
+    t[i].hkyi.scalefactor = (double *)calloc((size_t)S, sizeof(double));
+    t[i].hkyi.oldscalefactor = (double *)calloc((size_t)S, sizeof(double));
+  }
+}
+
+static void run_hky()
+{
+  int n = rd_i(), S = rd_i(), tots = rd_i();
+  int nl = 2 * n - 1;
+  std::vector<int> seq((size_t)n * S);
+  for (auto &v : seq) v = rd_i();
+  std::vector<int> mult(S);
+  for (auto &v : mult) v = rd_i();
+  double pi[4];
+  for (int j = 0; j < 4; j++) pi[j] = rd_d();
+  int nitems = rd_i();
+  alloc_chains(1, 1);
+  L[0].numgenes = n;
+  L[0].numlines = nl;
+  L[0].numsites = S;
+  L[0].totsites = tots;
+  L[0].mult = mult.data();
+  L[0].seq = (int **)malloc(sizeof(int *) * n);
+  for (int i = 0; i < n; i++) L[0].seq[i] = &seq[(size_t)i * S];
+  for (int j = 0; j < 4; j++) C[0]->G[0].pi[j] = pi[j];
+  struct edge *t = alloc_tree(nl);
+  alloc_hky(t, n, S);
+  C[0]->G[0].gtree = t;
+  for (int it = 0; it < nitems; it++) {
+    read_tree(t, nl);
+    C[0]->G[0].root = find_root(t, nl);
+    double u = rd_d(), kappa = rd_d();
+    double p = likelihoodHKY(0, 0, u, kappa, -1, -1, -1, -1);
+    printf("%.17g\n", p);
+    copyfraclike(0, 0);
+    storescalefactors(0, 0);
+    int nedits = rd_i();
+    for (int k = 0; k < nedits; k++) {
+      read_tree(t, nl);
+      C[0]->G[0].root = find_root(t, nl);
+      int e1 = rd_i(), e2 = rd_i(), e3 = rd_i(), e4 = rd_i(), acc = rd_i();
+      double pe = likelihoodHKY(0, 0, u, kappa, e1, e2, e3, e4);
+      printf("%.17g\n", pe);
+      if (acc) { copyfraclike(0, 0); storescalefactors(0, 0); }
+      else restorescalefactors(0, 0);
+    }
+  }
+}
+
+/* SW: n nitems {tree A[nl] u tr}*  ->  like dlikeA[nl] */
+static void run_sw()
+{
+  int n = rd_i();
+  int nl = 2 * n - 1;
+  int nitems = rd_i();
+  alloc_chains(1, 1);
+  L[0].numgenes = n;
+  L[0].numlines = nl;
+  L[0].minA[0] = -1000000;
+  L[0].maxA[0] = 1000000;
+  struct edge *t = alloc_tree(nl);
+  for (int i = 0; i < nl; i++) {
+    t[i].A = (int *)calloc(1, sizeof(int));
+    t[i].dlikeA = (double *)calloc(1, sizeof(double));
+  }
+  C[0]->G[0].gtree = t;
+  for (int it = 0; it < nitems; it++) {
+    read_tree(t, nl);
+    for (int i = 0; i < nl; i++) t[i].A[0] = rd_i();
+    double u = rd_d(), tr = rd_d();
+    double like = likelihoodSW(0, 0, 0, u, tr);
+    printf("%.17g", like);
+    for (int i = 0; i < nl; i++) printf(" %.17g", t[i].dlikeA[0]);
+    printf("\n");
+  }
+}
+
+/* SWAP: nchains nloci swaptries nsteps heatmode h1 h2 seed pdg[nchains*nloci] probg[nchains]
+ *   -> per step: beta[]; then swapcount and tempbasedswapcount rows */
+static void run_swap()
+{
+  int nch = rd_i(), nl = rd_i(), tries = rd_i(), nsteps = rd_i(), mode = rd_i();
+  double h1 = rd_d(), h2 = rd_d();
+  int seed = rd_i();
+  alloc_chains(nch, nl);
+  for (int c = 0; c < nch; c++)
+    for (int l = 0; l < nl; l++) C[c]->G[l].pdg = rd_d();
+  for (int c = 0; c < nch; c++) C[c]->allpcalc.probg = rd_d();
+  setseeds(seed);
+  setheat(h1, h2, mode, 0);
+  for (int s = 0; s < nsteps; s++) {
+    int ok = swapchains(tries, 1, 0, mode);
+    printf("%d", ok);
+    for (int c = 0; c < nch; c++) printf(" %.17g", beta[c]);
+    printf("\n");
+  }
+  for (int i = 0; i < nch; i++) {
+    for (int j = 0; j < nch; j++) printf("%d ", swapcount[i][j]);
+    printf("\n");
+  }
+  for (int i = 0; i < nch; i++) {
+    for (int j = 0; j < nch; j++) printf("%d ", tempbasedswapcount[i][j]);
+    printf("\n");
+  }
+}
+
+/* JOINTP: G rowlen np nm npops modeltype rows[G*rowlen] npoints points[npoints*(np+nm)]
+ *   -> q ess per point */
+static void run_jointp()
+{
+  int G = rd_i(), rowlen = rd_i(), np = rd_i(), nm = rd_i(), npp = rd_i(), mt = rd_i();
+  genealogiessaved = G;
+  numpopsizeparams = np;
+  nummigrateparams = nm;
+  npops = npp;
+  gsampinf = (float **)malloc(sizeof(float *) * G);
+  for (int g = 0; g < G; g++) {
+    gsampinf[g] = (float *)malloc(sizeof(float) * rowlen);
+    for (int k = 0; k < rowlen; k++) gsampinf[g][k] = (float)rd_d();
+  }
+  eexpsum = (struct extendnum *)malloc(sizeof(struct extendnum) * G);
+  refacc_jointp_setup(np + nm, mt);
+  int npts = rd_i();
+  std::vector<double> x(np + nm);
+  for (int p = 0; p < npts; p++) {
+    for (int k = 0; k < np + nm; k++) x[k] = rd_d();
+    double ess = 0.0;
+    double q = refacc_jointp(x.data(), &ess);
+    printf("%.17g %.17g\n", q, ess);
+  }
+}
+
+int main(int argc, char **argv)
+{
+  if (argc != 3) { fprintf(stderr, "usage: imaref is|hky|sw|swap|jointp <input>\n"); return 2; }
+  g_in = fopen(argv[2], "r");
+  if (!g_in) { perror(argv[2]); return 2; }
+  std::string mode = argv[1];
+  if (mode == "is") run_is();
+  else if (mode == "hky") run_hky();
+  else if (mode == "sw") run_sw();
+  else if (mode == "swap") run_swap();
+  else if (mode == "jointp") run_jointp();
+  else { fprintf(stderr, "unknown mode\n"); return 2; }
+  fclose(g_in);
+  return 0;
+}

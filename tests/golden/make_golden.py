@@ -1,0 +1,317 @@
+"""Generate the golden fixtures in this directory by running the UNMODIFIED
+IMa2p reference (oracle/_ref/imaref, built by ``make -C oracle ref`` from the
+reference source tree) on seeded inputs.
+
+Run from the repository root:  python tests/golden/make_golden.py
+
+Fixtures:
+  golden_is.npz     likelihoodIS + calc_sumlogk on synthetic 2-population loci
+                    and on loci of the reference's own Simulations/*.u files
+                    (genealogies built as perfect phylogenies of their IS data)
+  golden_hky.npz    likelihoodHKY full and dirty-node evaluations with
+                    copyfraclike/storescalefactors/restorescalefactors
+  golden_sw.npz     likelihoodSW totals and per-branch dlikeA, incl. zero-
+                    probability branches and x > 700
+  golden_swap.npz   setheat + swapchains (MT19937 seeded), betas and counts
+  golden_jointp.npz jointp (truncated, eexp) values and ESS
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from ima2p_gb300 import synth  # noqa: E402
+from oracle import pyoracle as O  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+SIMDIR = "/root/reference/Simulations"
+
+
+def pack_trees(trees):
+    return dict(up0=np.stack([t.up0 for t in trees]), up1=np.stack([t.up1 for t in trees]),
+                down=np.stack([t.down for t in trees]), time=np.stack([t.time for t in trees]),
+                root=np.array([t.root for t in trees], np.int32))
+
+
+# ------------------------------------------------------- .u IS loci
+def read_u_is_loci(path):
+    """Infinite-sites loci of a .u file as 0/1 matrices (readata.cpp:34-495:
+    sites with exactly two ACGT states, coded against the first sequence)."""
+    lines = [ln.rstrip("\n") for ln in open(path)]
+    i = 1
+    while lines[i].startswith("#"):
+        i += 1
+    i += 3  # npops, names, tree
+    nloci = int(lines[i].split()[0])
+    i += 1
+    loci = []
+    for _ in range(nloci):
+        hdr = lines[i].split()
+        n = int(hdr[1]) + int(hdr[2])
+        nb = int(hdr[3])
+        rows = [lines[i + 1 + k][10:].replace(" ", "")[:nb].lower() for k in range(n)]
+        i += 1 + n
+        cols = []
+        for s in range(nb):
+            col = [r[s] for r in rows]
+            if any(c not in "acgt" for c in col):
+                continue
+            states = sorted(set(col))
+            if len(states) != 2:
+                continue
+            cols.append([0 if c == col[0] else 1 for c in col])
+        if cols:
+            loci.append(np.array(cols, np.int8).T.copy())
+    return loci
+
+
+def perfect_phylogeny(rng, seq):
+    """A binary genealogy on which every 0/1 column is a single mutation;
+    polytomies are resolved at random, times are drawn to respect the nesting."""
+    n = seq.shape[0]
+    # columns are coded against the first sequence, so rooting on its side
+    # makes every derived set a clade (four-gamete compatible data)
+    splits = {frozenset(np.nonzero(c)[0]) for c in seq.T}
+    full = frozenset(range(n))
+    clades = sorted({s for s in splits if 1 < len(s) < n} | {full}, key=len)
+    # every clade's children: maximal proper sub-clades plus leftover tips
+    nl = 2 * n - 1
+    up0 = np.full(nl, -1, np.int32)
+    up1 = np.full(nl, -1, np.int32)
+    down = np.full(nl, -1, np.int32)
+    height = np.zeros(nl)
+    node_of = {frozenset([t]): t for t in range(n)}
+    nxt = [n]
+
+    def join(a, b, h):
+        k = nxt[0]
+        nxt[0] += 1
+        up0[k], up1[k] = a, b
+        down[a] = down[b] = k
+        height[k] = h
+        return k
+
+    for c in clades:
+        subs = [s for s in node_of if s < c and len(s) < len(c)]
+        maximal = [s for s in subs if not any(s < t for t in subs)]
+        parts = [node_of[s] for s in maximal]
+        covered = frozenset().union(*maximal) if maximal else frozenset()
+        parts += [t for t in c if t not in covered]
+        base = max(height[p] for p in parts)
+        while len(parts) > 1:
+            i, j = rng.choice(len(parts), 2, replace=False)
+            base += rng.exponential(0.2)
+            k = join(parts[i], parts[j], base)
+            parts = [p for q, p in enumerate(parts) if q not in (i, j)] + [k]
+        node_of[c] = parts[0]
+        for s in maximal:
+            del node_of[s]
+        for t in c:
+            node_of.pop(frozenset([t]), None)
+    root = node_of[full]
+    time = np.zeros(nl)
+    for c in range(nl):
+        time[c] = height[down[c]] if down[c] >= 0 else -1.0
+    return synth.Genealogy(up0, up1, down, time, int(root))
+
+
+def golden_is():
+    rng = np.random.default_rng(1001)
+    out = {}
+    cases = []
+    for k in range(3):
+        g0 = synth.two_pop_tree(rng, 10, 10, theta=5.0, mig=0.1, tsplit=1.0)
+        seq = synth.is_data(rng, g0, 1.0, min_sites=5)
+        trees = [g0] + [synth.jitter_times(rng, g0, 0.2) for _ in range(4)]
+        trees.append(synth.two_pop_tree(rng, 10, 10))  # mostly incompatible
+        cases.append(("syn%d" % k, seq, trees))
+    for fname in ("Sim1_5loci.u", "Sim2.u"):
+        path = os.path.join(SIMDIR, fname)
+        for li, seq in enumerate(read_u_is_loci(path)[:3]):
+            g0 = perfect_phylogeny(rng, seq)
+            trees = [g0] + [synth.jitter_times(rng, g0, 0.2) for _ in range(2)]
+            cases.append(("%s_L%d" % (fname.split(".")[0], li), seq, trees))
+    for ci, (name, seq, trees) in enumerate(cases):
+        lengths = np.array([t.length() for t in trees])
+        us = rng.lognormal(0.0, 0.5, len(trees))
+        ref = O.ref_is(seq, trees, lengths, us)
+        p = "c%d_" % ci
+        out[p + "name"] = np.array(name)
+        out[p + "seq"] = seq
+        for k, v in pack_trees(trees).items():
+            out[p + k] = v
+        out[p + "length"] = lengths
+        out[p + "u"] = us
+        out[p + "ref"] = ref
+    out["ncases"] = np.array(len(cases))
+    np.savez_compressed(os.path.join(OUT, "golden_is.npz"), **out)
+
+
+def time_edit(rng, g, k):
+    """Move the coalescence that creates internal node k inside its window."""
+    h = g.copy()
+    a, b = int(h.up0[k]), int(h.up1[k])
+    lo = max(h.time[h.up0[a]] if h.up0[a] >= 0 else 0.0, h.time[h.up0[b]] if h.up0[b] >= 0 else 0.0)
+    hi = h.time[k] if h.down[k] >= 0 else h.time[a] * 1.5
+    h.time[a] = h.time[b] = lo + (hi - lo) * rng.uniform(0.05, 0.95)
+    return h
+
+
+def tip_swap(rng, g):
+    """Exchange two tips that hang from different parents (a topology edit)."""
+    h = g.copy()
+    n = h.n
+    while True:
+        i, j = rng.choice(n, 2, replace=False)
+        if h.down[i] != h.down[j]:
+            break
+    pi, pj = int(h.down[i]), int(h.down[j])
+    for p, old, new in ((pi, i, j), (pj, j, i)):
+        if h.up0[p] == old:
+            h.up0[p] = new
+        else:
+            h.up1[p] = new
+    h.down[i], h.down[j] = pj, pi
+    h.time[i], h.time[j] = h.time[j], h.time[i]
+    return h, int(i), int(j)
+
+
+def golden_hky():
+    rng = np.random.default_rng(1002)
+    out = {}
+    cases = []
+    for k, (n1, nb) in enumerate(((6, 300), (10, 1000), (20, 1000))):
+        g = synth.two_pop_tree(rng, n1, n1, theta=10.0, mig=0.2, tsplit=1.5)
+        pi_sim = rng.dirichlet([5, 5, 5, 5])
+        kappa = rng.uniform(2, 8)
+        u = float(rng.lognormal(0, 0.5))
+        loc = synth.hky_data(rng, g, nb, u, kappa, pi_sim)
+        n = g.n
+        seqs = []  # (tree, e, accept)
+        cur = g
+        for step in range(6):
+            if step % 3 == 2:
+                h, i, j = tip_swap(rng, cur)
+                e = (i, j, -1, -1)
+            else:
+                kk = int(rng.integers(n, 2 * n - 1))
+                h = time_edit(rng, cur, kk)
+                e = (kk, -1, -1, -1)
+            acc = int(rng.uniform() < 0.5)
+            seqs.append((h, e, acc))
+            if acc:
+                cur = h
+        cases.append((loc, g, u, kappa, seqs))
+    for ci, (loc, g, u, kappa, seqs) in enumerate(cases):
+        ref = O.ref_hky(loc, [(g, u, kappa, seqs)])
+        p = "c%d_" % ci
+        out[p + "seq"] = loc.seq
+        out[p + "mult"] = loc.mult
+        out[p + "totsites"] = np.array(loc.totsites)
+        out[p + "pi"] = loc.pi
+        for kk, v in pack_trees([g] + [s[0] for s in seqs]).items():
+            out[p + kk] = v
+        out[p + "e"] = np.array([s[1] for s in seqs], np.int32)
+        out[p + "acc"] = np.array([s[2] for s in seqs], np.int32)
+        out[p + "u"] = np.array(u)
+        out[p + "kappa"] = np.array(kappa)
+        out[p + "ref"] = ref
+    out["ncases"] = np.array(len(cases))
+    np.savez_compressed(os.path.join(OUT, "golden_hky.npz"), **out)
+
+
+def golden_sw():
+    rng = np.random.default_rng(1003)
+    g = synth.three_pop_tree(rng, [10, 10, 10], theta=4.0, mig=0.05)
+    trees, alleles, us = [], [], []
+    for k in range(8):
+        h = synth.jitter_times(rng, g, 0.3)
+        A = synth.sw_alleles(rng, h, float(rng.lognormal(0, 0.5)))
+        if k == 5:  # a large jump across a short branch -> Miller recurrence
+            A = A.copy()
+            A[h.up0[h.root]] += 7
+        if k == 6:  # zero-length branch with an allele change -> I_d(0) = 0
+            A = A.copy()
+            h = h.copy()
+            c = int(h.up0[h.root])
+            if h.up0[c] >= 0:
+                h.time[h.up0[c]] = h.time[h.up1[c]] = h.time[c]
+                A[c] = A[h.root] + 2
+        trees.append(h)
+        alleles.append(A)
+        us.append(float(rng.lognormal(0, 0.5)) if k != 7 else 40.0)  # x > 700
+    ref = O.ref_sw(trees, alleles, us)
+    out = pack_trees(trees)
+    out["A"] = np.stack(alleles)
+    out["u"] = np.array(us)
+    out["ref"] = ref
+    np.savez_compressed(os.path.join(OUT, "golden_sw.npz"), **out)
+
+
+def golden_swap():
+    rng = np.random.default_rng(1004)
+    out = {}
+    cases = [(4, 5, 1, 200, 1, 0.9, 0.8, 0), (20, 10, 2, 200, 1, 0.96, 0.9, 7),
+             (24, 3, 3, 100, 0, 0.05, 0.0, 11), (128, 6, 12, 60, 1, 0.95, 0.8, 5)]
+    for ci, (nch, nl, tries, steps, mode, h1, h2, seed) in enumerate(cases):
+        pdg = rng.normal(-100, 3, (nch, nl))
+        probg = rng.normal(-30, 2, nch)
+        ok, betas, sc, tc = O.ref_swap(pdg, probg, tries, steps, mode, h1, h2, seed)
+        p = "c%d_" % ci
+        out[p + "params"] = np.array([nch, nl, tries, steps, mode, seed])
+        out[p + "h"] = np.array([h1, h2])
+        out[p + "pdg"] = pdg
+        out[p + "probg"] = probg
+        out[p + "ok"] = ok
+        out[p + "betas"] = betas
+        out[p + "swapcount"] = sc
+        out[p + "tempcount"] = tc
+    out["ncases"] = np.array(len(cases))
+    np.savez_compressed(os.path.join(OUT, "golden_swap.npz"), **out)
+
+
+def golden_jointp():
+    rng = np.random.default_rng(1005)
+    out = {}
+    # 2 populations (3 theta, 2 m), row width 21 as in a real .ti
+    off = synth.gsamp_layout(3, 2, 1)
+    G = 400
+    rows = np.zeros((G, off["rowlen"]), np.float32)
+    rows[:, 0:3] = rng.poisson(4, (G, 3))
+    rows[:, 3:6] = rng.gamma(3, 1, (G, 3))
+    rows[:, 6:9] = rng.normal(0, 1, (G, 3))
+    rows[:, 9:11] = rng.poisson(1, (G, 2))
+    rows[:, 11:13] = rng.gamma(2, 1, (G, 2))
+    rows[:, off["probg"]] = rng.normal(15, 6, G)
+    pts = np.concatenate([rng.uniform(0.1, 10, (12, 3)), rng.uniform(1e-3, 2, (12, 2))], 1)
+    out["a_rows"] = rows
+    out["a_pts"] = pts
+    out["a_ref"] = O.ref_jointp(rows, 3, 2, 2, 0, pts)
+    # 3 populations (5 theta, 8 m): theta-only and migration-only model types
+    rows5, _, off5 = synth.surface_stats(rng, 300, 5, 8, 2)
+    rows5[:, off5["qi"]:off5["qi"] + 5] = rng.normal(-4, 1, (300, 5))
+    rows5[:, off5["mi"]:off5["mi"] + 8] = rng.normal(-2, 1, (300, 8))
+    pts5 = synth.surface_points(rng, 8)
+    out["b_rows"] = rows5
+    out["b_pts"] = pts5
+    out["b_ref1"] = O.ref_jointp(rows5, 5, 8, 3, 1, pts5)
+    out["b_ref2"] = O.ref_jointp(rows5, 5, 8, 3, 2, pts5)
+    np.savez_compressed(os.path.join(OUT, "golden_jointp.npz"), **out)
+
+
+if __name__ == "__main__":
+    if not O.ref_available():
+        sys.exit("build the reference harness first: make -C oracle ref")
+    golden_is()
+    golden_hky()
+    golden_sw()
+    golden_swap()
+    golden_jointp()
+    for f in sorted(os.listdir(OUT)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(OUT, f)))
