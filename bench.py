@@ -1,0 +1,385 @@
+#!/usr/bin/env python3
+"""Throughput of the GB300 hot paths: chain-locus likelihood evaluations per
+second (and L-mode surface points per second with --workload surface).
+
+Default workload: 2 populations, 50 HKY loci x (20+20) copies x 1000 bp, 32
+heated chains -- every chain-locus fully re-evaluated each step (the batched
+form of changet_RY1's all-locus re-likelihood), FP32 pruning with exact
+power-of-two rescaling and FP64 sums.  One JSON line on stdout.
+
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--workload hky|sw|is|surface]
+  python bench.py --impl reference ...   # the CPU restatement of the reference
+
+value: inputs resident in HBM, device time (CUDA events) of K steps, L2
+flushed between steps.  e2e: the same steps through the public C ABI from
+host buffers (genealogies staged and copied host->device, results copied
+back) on the host clock.  Multi-GPU: independent replicas, one per rank.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "chain-locus likelihood evals/s"
+SURF_METRIC = "L-mode grid points/s"
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d["hbm_gbs"], d["bf16_tflops"], "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+def profile_traffic(kernel):
+    """dram bytes per launch from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f).get(kernel)
+    except Exception:
+        return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.out = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.out.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------- workloads
+def build_ctx(wl, api):
+    ctx = api.Context(0)
+    for spec in wl.loci:
+        if spec[0] == "is":
+            ctx.add_locus_is(spec[1])
+        elif spec[0] == "hky":
+            L = spec[1]
+            ctx.add_locus_hky(L.seq, L.mult, L.totsites)
+        else:
+            ctx.add_locus_sw(spec[1], spec[2])
+    ctx.set_chains(wl.nruns, wl.cpr)
+    wl.upload(ctx)
+    return ctx
+
+
+def algo_bytes(wl):
+    """Compulsory bytes of one full evaluation of every chain-locus."""
+    total = 0.0
+    for spec in wl.loci:
+        if spec[0] == "hky":
+            L = spec[1]
+            n, S = L.seq.shape
+            # partials (float4) + exponent written per internal node and pattern,
+            # tip states, multiplicities, topology and times read
+            total += (n - 1) * S * 20.0 + n * S + 4.0 * S + (2 * n - 1) * 16.0
+        elif spec[0] == "sw":
+            n = spec[1]
+            total += (2 * n - 1) * 28.0  # node + FF time + allele read, dlikeA write
+        else:
+            seq = spec[1]
+            n, S = seq.shape
+            total += (2 * n - 1) * 16.0 + n * S + 8.0
+    return total * wl.nchains
+
+
+def dominant_kind(wl, api):
+    kinds = {s[0] for s in wl.loci}
+    if "hky" in kinds:
+        return api.K_HKY_FAST, "k_hky_fast"
+    if "sw" in kinds:
+        return api.K_SW_FAST, "k_sw_fast"
+    return api.K_IS, "k_is"
+
+
+def run_ours(args):
+    from ima2p_gb300 import api, workloads
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist_mod.init_process_group("gloo")
+        dist = dist_mod
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("LOCAL_RANK", "0"))
+    wl = workloads.make(args.workload)
+    ctx = build_ctx(wl, api)
+    ci, li = wl.pairs()
+    u = wl.u.ravel()
+    par = wl.par.ravel()
+    units = len(ci)
+    prec = api.PREC_FAST
+    batch = ctx.batch_create(ci, li, u, par, precision=prec)
+    # warm-up (also initialises per-locus constants)
+    for _ in range(args.warmup):
+        batch.run(use_graph=True)
+    ctx.synchronize()
+    res_fast, st_fast = batch.results()
+
+    # ---------------- timed region: resident inputs, L2 flushed between steps
+    kind, kname = dominant_kind(wl, api)
+    ctx.set_profiling(True)
+    n0 = ctx.launch_count()
+    k0 = ctx.kernel_stats(kind)
+    times = []
+    if dist:
+        dist.barrier()
+    with Clocks(0) as clk:
+        for _ in range(args.steps):
+            ctx.flush_l2()
+            ctx.timer_begin()
+            batch.run(use_graph=False)
+            times.append(ctx.timer_end())
+    k1 = ctx.kernel_stats(kind)
+    n_launch = ctx.launch_count() - n0  # library kernels only (the L2 flush is a memset)
+    ctx.set_profiling(False)
+    total_ms = float(sum(times))
+    if dist:
+        import torch
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = units * args.steps * world / (total_ms / 1e3)
+
+    # ---------------- dominant kernel roofline
+    kl = k1[0] - k0[0]
+    kms = (k1[1] - k0[1]) / max(kl, 1)
+    kbytes = (k1[2] - k0[2]) / max(kl, 1)
+    hbm, bf16, src = measured_peaks()
+    achieved = kbytes / (kms / 1e3) / 1e9 if kms > 0 else 0.0
+    roof = {"kernel": kname, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm,
+            "unit": "GB/s", "frac": round(achieved / hbm, 4), "peak_source": src,
+            "traffic": profile_traffic(kname), "algorithmic_bytes_per_launch": kbytes,
+            "avg_launch_ms": round(kms, 5)}
+
+    # ---------------- plain FP64 per-chain form on the same GPU
+    b64 = ctx.batch_create(ci, li, u, par, precision=api.PREC_FP64)
+    for _ in range(2):
+        b64.run(use_graph=False)
+    t64 = []
+    for _ in range(max(3, min(args.steps, 10))):
+        ctx.flush_l2()
+        ctx.timer_begin()
+        b64.run(use_graph=False)
+        t64.append(ctx.timer_end())
+    res64, _ = b64.results()
+    v64 = units / (statistics.median(t64) / 1e3)
+    ok = (st_fast == 0)
+    err = np.abs(res_fast[ok] - res64[ok])
+
+    # ---------------- e2e through the C ABI from host buffers
+    pci, pli, up0, up1, down, tm = wl.packed()
+    nodes = len(up0)
+    ns = sum(2 * ((len(wl.trees[(int(c), int(l))].up0) + 1) // 2) + 2 for c, l in zip(ci, li))
+    # NodeRec + FP64 time + float-float time per node, level schedule, per-pair
+    # levels/length/pi, and the 40-byte request of each pair
+    h2d = nodes * 24 + ns * 2 + units * (4 + 8 + 32) + units * 40
+    d2h = units * (8 + 4)
+    e2e_t = []
+    for s in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        ctx.set_genealogies(pci, pli, up0, up1, down, tm)
+        r, _ = ctx.eval(ci, li, u, par, precision=prec)
+        t1 = time.perf_counter()
+        if s >= args.warmup:
+            e2e_t.append(t1 - t0)
+    e2e = units * world / statistics.median(e2e_t)
+
+    out = {
+        "metric": METRIC, "value": round(value, 1), "unit": "evals/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 5),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (seeded IM coalescent genealogies and simulated data, shapes of the named config)",
+        "config": {"workload": wl.describe, "global_batch": units * world, "chain_loci_per_step": units,
+                   "parallelism": "replicas%d" % world, "l2": "flushed between timed steps",
+                   "precision": "FP32 partials, exact power-of-two rescaling, FP64 root sums"},
+        "e2e": {"value": round(e2e, 1), "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "roofline": roof,
+        "fp64_form": {"value": round(v64, 1), "unit": "evals/s", "speedup": round(value / world / v64, 2)},
+        "error_vs_fp64": {"max_abs": float(err.max()) if len(err) else None,
+                          "median_abs": float(np.median(err)) if len(err) else None,
+                          "max_rel": float((err / np.abs(res64[ok])).max()) if len(err) else None},
+        "gpu_launches": int(n_launch),
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        out["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
+        print(json.dumps(out), flush=True)
+    batch.destroy()
+    b64.destroy()
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+# --------------------------------------------------------- CPU baselines
+def _oracle_items(wl):
+    from oracle import pyoracle as O
+
+    items = []
+    ci, li = wl.pairs()
+    for c, l in zip(ci, li):
+        spec = wl.loci[l]
+        g = wl.trees[(int(c), int(l))]
+        items.append((spec, g, float(wl.u[c, l]), float(wl.par[c, l]), wl.alleles.get((int(c), int(l)))))
+    return O, items
+
+
+def _eval_item(O, it, cache):
+    spec, g, u, par, A = it
+    if spec[0] == "hky":
+        L = spec[1]
+        st = cache.get(id(L))
+        if st is None:
+            st = cache[id(L)] = O.HKYState(*L.seq.shape)
+        return st.likelihood(L, g, u, par)
+    if spec[0] == "sw":
+        return O.sw_likelihood(A, g, u, par)[0]
+    seq = spec[1]
+    return O.is_likelihood(seq, g, g.length(), u, 0.0)[0]
+
+
+def cpu_baseline(wl, seconds):
+    """The oracle (a C restatement of the reference) on one host core over a
+    bounded sample of the workload's chain-loci."""
+    O, items = _oracle_items(wl)
+    cache = {}
+    n = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        _eval_item(O, items[n % len(items)], cache)
+        n += 1
+    dt = time.perf_counter() - t0
+    return {"value": round(n / dt, 1), "unit": "evals/s", "cores": 1, "kind": "port",
+            "sample": "%d chain-locus evaluations (%.1f s, cycling over the workload's %d chain-loci)"
+                      % (n, dt, len(items))}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from ima2p_gb300 import workloads
+
+    wl = workloads.make(args.workload)
+    O, items = _oracle_items(wl)
+    cores = os.cpu_count() or 1
+    chunks = [items[k::cores] for k in range(cores)]
+
+    def work(chunk):
+        cache = {}
+        for it in chunk:
+            _eval_item(O, it, cache)
+        return len(chunk)
+
+    # one step = a bounded sample: every core evaluates its share of at most
+    # `cap` chain-loci (ctypes calls release the GIL, so threads run in parallel)
+    cap = max(cores, min(len(items), args.ref_cap))
+    sample = [c[: max(1, cap // cores)] for c in chunks]
+    done = sum(len(c) for c in sample)
+    times = []
+    with ThreadPoolExecutor(cores) as ex:
+        for s in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            list(ex.map(work, sample))
+            if s >= args.warmup:
+                times.append(time.perf_counter() - t0)
+    v = done / statistics.median(times)
+    desc = "%d of the workload's %d chain-loci per step, %d threads" % (done, len(items), cores)
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": round(v, 1), "unit": "evals/s", "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * statistics.median(times), 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+        "data": "synthetic", "config": {"workload": wl.describe},
+        "cpu_baseline": {"value": round(v, 1), "unit": "evals/s", "cores": cores, "kind": "port",
+                         "sample": desc},
+        "e2e": {"value": round(v, 1), "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="hky", choices=["hky", "sw", "is", "mixed", "surface"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-cap", type=int, default=4096)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

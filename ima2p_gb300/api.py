@@ -1,0 +1,402 @@
+"""Python view of the C ABI in include/ima_gpu.h (libima2p_gb300.so).
+
+The method names mirror the reference functions they replace
+(likelihoodIS / likelihoodHKY / likelihoodSW, copyfraclike /
+storescalefactors / restorescalefactors, setheat / swapchains, jointp), with
+the same argument meaning, sentinels and error behaviour: a failing call
+raises ImaError carrying the library's status code and message, where the
+reference would print IM_err and exit.  There is no CPU fallback: without the
+compiled library every call fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libima2p_gb300.so")
+
+IMA_OK, IMA_ERR_ARG, IMA_ERR_CUDA, IMA_ERR_STATE, IMA_ERR_NOMEM, IMA_ERR_DATA = 0, -1, -2, -3, -4, -5
+MODEL_IS, MODEL_HKY, MODEL_SW = 0, 1, 2
+PREC_FAST, PREC_FP64 = 0, 1
+EVAL_OK, EVAL_IS_REJECT, EVAL_IS_FAIL, EVAL_SW_ZERO = 0, 1, 2, 3
+SURF_FAST, SURF_FP64, SURF_COMPAT = 0, 1, 2
+K_IS, K_IS_SUMLOGK, K_HKY_FAST, K_HKY_FP64, K_SW_FAST, K_SW_FP64, K_SWAP, K_SURF_FAST, \
+    K_SURF_FP64, K_SURF_COMPAT = range(10)
+KERNEL_NAMES = ["is", "is_sumlogk", "hky_fast", "hky_fp64", "sw_fast", "sw_fp64", "swap",
+                "surf_fast", "surf_fp64", "surf_compat"]
+REJECT_IS = -1000000000.0
+
+# every symbol the header declares (checked by tests/test_abi.py)
+EXPORTS = [
+    "ima_gpu_create", "ima_gpu_destroy", "ima_gpu_error", "ima_gpu_synchronize",
+    "ima_gpu_add_locus_is", "ima_gpu_add_locus_hky", "ima_gpu_add_locus_sw", "ima_gpu_set_chains",
+    "ima_gpu_set_genealogy", "ima_gpu_set_genealogies", "ima_gpu_set_pi", "ima_gpu_set_alleles", "ima_gpu_likelihoodIS",
+    "ima_gpu_likelihoodHKY", "ima_gpu_copyfraclike", "ima_gpu_storescalefactors",
+    "ima_gpu_restorescalefactors", "ima_gpu_likelihoodSW", "ima_gpu_get_dlikeA", "ima_gpu_eval",
+    "ima_gpu_commit", "ima_gpu_batch_create", "ima_gpu_batch_run", "ima_gpu_batch_results",
+    "ima_gpu_batch_destroy", "ima_gpu_flush_genealogies", "ima_gpu_setheat", "ima_gpu_get_betas",
+    "ima_gpu_set_betas", "ima_gpu_set_pdg", "ima_gpu_get_pdg", "ima_gpu_set_probg",
+    "ima_gpu_swapchains", "ima_gpu_get_swapcounts", "ima_gpu_surface_load",
+    "ima_gpu_surface_eval", "ima_gpu_jointp", "ima_gpu_timer_begin", "ima_gpu_timer_end",
+    "ima_gpu_set_profiling", "ima_gpu_kernel_stats", "ima_gpu_launch_count", "ima_gpu_flush_l2",
+    "ima_gpu_memory",
+]
+
+
+class ImaError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Loads the compiled library; fails loudly when it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImaError(IMA_ERR_STATE, f"{path} is missing: build it with ima2p_gb300.build "
+                                      "(python -c 'import __graft_entry__ as g; g.build()')")
+    lib = C.CDLL(path)
+    _declare(lib)
+    _lib = lib
+    return lib
+
+
+P = C.c_void_p
+I = C.c_int
+D = C.c_double
+
+
+def _declare(L):
+    sig = {
+        "ima_gpu_create": (I, [I, C.POINTER(P)]),
+        "ima_gpu_destroy": (None, [P]),
+        "ima_gpu_error": (C.c_char_p, [P]),
+        "ima_gpu_synchronize": (I, [P]),
+        "ima_gpu_add_locus_is": (I, [P, I, I, P, C.POINTER(I)]),
+        "ima_gpu_add_locus_hky": (I, [P, I, I, I, P, P, C.POINTER(I)]),
+        "ima_gpu_add_locus_sw": (I, [P, I, I, C.POINTER(I)]),
+        "ima_gpu_set_chains": (I, [P, I, I]),
+        "ima_gpu_set_genealogy": (I, [P, I, I, P, P, P, P, D]),
+        "ima_gpu_set_genealogies": (I, [P, I, P, P, P, P, P, P, P]),
+        "ima_gpu_set_pi": (I, [P, I, I, P]),
+        "ima_gpu_set_alleles": (I, [P, I, I, I, P]),
+        "ima_gpu_likelihoodIS": (I, [P, I, I, D, P]),
+        "ima_gpu_likelihoodHKY": (I, [P, I, I, D, D, I, I, I, I, P]),
+        "ima_gpu_copyfraclike": (I, [P, I, I]),
+        "ima_gpu_storescalefactors": (I, [P, I, I]),
+        "ima_gpu_restorescalefactors": (I, [P, I, I]),
+        "ima_gpu_likelihoodSW": (I, [P, I, I, I, D, D, P]),
+        "ima_gpu_get_dlikeA": (I, [P, I, I, I, P]),
+        "ima_gpu_eval": (I, [P, I, P, P, P, P, P, P, I, P, P]),
+        "ima_gpu_commit": (I, [P, I, P, P, P]),
+        "ima_gpu_batch_create": (I, [P, I, P, P, P, P, P, P, I, C.POINTER(I)]),
+        "ima_gpu_batch_run": (I, [P, I, I]),
+        "ima_gpu_batch_results": (I, [P, I, P, P]),
+        "ima_gpu_batch_destroy": (I, [P, I]),
+        "ima_gpu_flush_genealogies": (I, [P]),
+        "ima_gpu_setheat": (I, [P, D, D, I]),
+        "ima_gpu_get_betas": (I, [P, P]),
+        "ima_gpu_set_betas": (I, [P, P]),
+        "ima_gpu_set_pdg": (I, [P, P]),
+        "ima_gpu_get_pdg": (I, [P, P]),
+        "ima_gpu_set_probg": (I, [P, P]),
+        "ima_gpu_swapchains": (I, [P, I, I, P, I, C.c_uint64, P, P]),
+        "ima_gpu_get_swapcounts": (I, [P, I, P, P]),
+        "ima_gpu_surface_load": (I, [P, I, I, P, I, I, I, P]),
+        "ima_gpu_surface_eval": (I, [P, I, P, I, I, P, P]),
+        "ima_gpu_jointp": (I, [P, P, I, P, P]),
+        "ima_gpu_timer_begin": (I, [P]),
+        "ima_gpu_timer_end": (I, [P, C.POINTER(C.c_float)]),
+        "ima_gpu_set_profiling": (I, [P, I]),
+        "ima_gpu_kernel_stats": (I, [P, I, C.POINTER(C.c_longlong), C.POINTER(D), C.POINTER(D)]),
+        "ima_gpu_launch_count": (I, [P, C.POINTER(C.c_longlong)]),
+        "ima_gpu_flush_l2": (I, [P]),
+        "ima_gpu_memory": (I, [P, C.POINTER(C.c_size_t)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _i32(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Context:
+    """One device context: resident loci, chains, genealogies and surface."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = P()
+        rc = self.lib.ima_gpu_create(device, C.byref(h))
+        if rc != IMA_OK:
+            raise ImaError(rc, "ima_gpu_create failed (no usable CUDA device?)")
+        self.h = h
+        self.loci = []
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ima_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ck(self, rc):
+        if rc != IMA_OK:
+            raise ImaError(rc, self.lib.ima_gpu_error(self.h).decode())
+
+    # ------------------------------------------------------------ loci
+    def add_locus_is(self, seq):
+        seq = np.ascontiguousarray(seq, np.int8)
+        li = I()
+        self._ck(self.lib.ima_gpu_add_locus_is(self.h, seq.shape[0], seq.shape[1], _ptr(seq), C.byref(li)))
+        self.loci.append((MODEL_IS, seq.shape[0]))
+        return li.value
+
+    def add_locus_hky(self, seq, mult, totsites):
+        seq = np.ascontiguousarray(seq, np.int8)
+        mult = _i32(mult)
+        li = I()
+        self._ck(self.lib.ima_gpu_add_locus_hky(self.h, seq.shape[0], seq.shape[1], int(totsites),
+                                                 _ptr(seq), _ptr(mult), C.byref(li)))
+        self.loci.append((MODEL_HKY, seq.shape[0]))
+        return li.value
+
+    def add_locus_sw(self, numgenes, nlinked=1):
+        li = I()
+        self._ck(self.lib.ima_gpu_add_locus_sw(self.h, int(numgenes), int(nlinked), C.byref(li)))
+        self.loci.append((MODEL_SW, numgenes))
+        return li.value
+
+    def set_chains(self, nruns, chains_per_run):
+        self._ck(self.lib.ima_gpu_set_chains(self.h, int(nruns), int(chains_per_run)))
+        self.nruns, self.cpr = nruns, chains_per_run
+        self.nchains = nruns * chains_per_run
+
+    # -------------------------------------------------------- genealogy
+    def set_genealogy(self, ci, li, g, length=None):
+        self._ck(self.lib.ima_gpu_set_genealogy(
+            self.h, int(ci), int(li), _ptr(_i32(g.up0)), _ptr(_i32(g.up1)), _ptr(_i32(g.down)),
+            _ptr(_f64(g.time)), -1.0 if length is None else float(length)))
+
+    def set_genealogies(self, ci, li, up0, up1, down, time, length=None):
+        """Packed form: node arrays of all pairs concatenated in pair order."""
+        ci, li = _i32(ci), _i32(li)
+        self._ck(self.lib.ima_gpu_set_genealogies(
+            self.h, len(ci), _ptr(ci), _ptr(li), _ptr(_i32(up0)), _ptr(_i32(up1)), _ptr(_i32(down)),
+            _ptr(_f64(time)), _ptr(_f64(length))))
+
+    def set_pi(self, ci, li, pi):
+        self._ck(self.lib.ima_gpu_set_pi(self.h, int(ci), int(li), _ptr(_f64(pi))))
+
+    def set_alleles(self, ci, li, A, ai=0):
+        self._ck(self.lib.ima_gpu_set_alleles(self.h, int(ci), int(li), int(ai), _ptr(_i32(A))))
+
+    def flush_genealogies(self):
+        self._ck(self.lib.ima_gpu_flush_genealogies(self.h))
+
+    # -------------------------------------------- reference mirrors
+    def likelihoodIS(self, ci, li, mutrate):
+        out = np.zeros(1)
+        self._ck(self.lib.ima_gpu_likelihoodIS(self.h, int(ci), int(li), float(mutrate), _ptr(out)))
+        return float(out[0])
+
+    def likelihoodHKY(self, ci, li, mutrate, kappa, e1=-1, e2=-1, e3=-1, e4=-1):
+        out = np.zeros(1)
+        self._ck(self.lib.ima_gpu_likelihoodHKY(self.h, int(ci), int(li), float(mutrate), float(kappa),
+                                                 int(e1), int(e2), int(e3), int(e4), _ptr(out)))
+        return float(out[0])
+
+    def copyfraclike(self, ci, li):
+        self._ck(self.lib.ima_gpu_copyfraclike(self.h, int(ci), int(li)))
+
+    def storescalefactors(self, ci, li):
+        self._ck(self.lib.ima_gpu_storescalefactors(self.h, int(ci), int(li)))
+
+    def restorescalefactors(self, ci, li):
+        self._ck(self.lib.ima_gpu_restorescalefactors(self.h, int(ci), int(li)))
+
+    def likelihoodSW(self, ci, li, ai, u, tr=1.0):
+        out = np.zeros(1)
+        self._ck(self.lib.ima_gpu_likelihoodSW(self.h, int(ci), int(li), int(ai), float(u), float(tr), _ptr(out)))
+        return float(out[0])
+
+    def get_dlikeA(self, ci, li, ai=0):
+        n = self.loci[li][1]
+        out = np.zeros(2 * n - 1)
+        self._ck(self.lib.ima_gpu_get_dlikeA(self.h, int(ci), int(li), int(ai), _ptr(out)))
+        return out
+
+    # -------------------------------------------------------- batched
+    def eval(self, ci, li, u, kappa=None, edits=None, ai=None, precision=PREC_FAST):
+        ci, li, u = _i32(ci), _i32(li), _f64(u)
+        n = len(ci)
+        kappa, ai = _f64(kappa), _i32(ai)
+        edits = None if edits is None else _i32(edits).reshape(n, 4)
+        res = np.zeros(n)
+        st = np.zeros(n, np.int32)
+        self._ck(self.lib.ima_gpu_eval(self.h, n, _ptr(ci), _ptr(li), _ptr(u), _ptr(kappa), _ptr(edits),
+                                       _ptr(ai), int(precision), _ptr(res), _ptr(st)))
+        return res, st
+
+    def commit(self, ci, li, accept):
+        ci, li = _i32(ci), _i32(li)
+        acc = np.ascontiguousarray(accept, np.uint8)
+        self._ck(self.lib.ima_gpu_commit(self.h, len(ci), _ptr(ci), _ptr(li), _ptr(acc)))
+
+    def batch_create(self, ci, li, u, kappa=None, edits=None, ai=None, precision=PREC_FAST):
+        ci, li, u = _i32(ci), _i32(li), _f64(u)
+        n = len(ci)
+        kappa, ai = _f64(kappa), _i32(ai)
+        edits = None if edits is None else _i32(edits).reshape(n, 4)
+        b = I()
+        self._ck(self.lib.ima_gpu_batch_create(self.h, n, _ptr(ci), _ptr(li), _ptr(u), _ptr(kappa),
+                                               _ptr(edits), _ptr(ai), int(precision), C.byref(b)))
+        return Batch(self, b.value, n)
+
+    # ----------------------------------------------------------- MC3
+    def setheat(self, hval1, hval2, heatmode):
+        self._ck(self.lib.ima_gpu_setheat(self.h, float(hval1), float(hval2), int(heatmode)))
+
+    def get_betas(self):
+        out = np.zeros(self.nchains)
+        self._ck(self.lib.ima_gpu_get_betas(self.h, _ptr(out)))
+        return out
+
+    def set_betas(self, beta):
+        self._ck(self.lib.ima_gpu_set_betas(self.h, _ptr(_f64(beta))))
+
+    def set_pdg(self, pdg):
+        self._ck(self.lib.ima_gpu_set_pdg(self.h, _ptr(_f64(pdg))))
+
+    def get_pdg(self):
+        out = np.zeros((self.nchains, len(self.loci)))
+        self._ck(self.lib.ima_gpu_get_pdg(self.h, _ptr(out)))
+        return out
+
+    def set_probg(self, probg):
+        self._ck(self.lib.ima_gpu_set_probg(self.h, _ptr(_f64(probg))))
+
+    def swapchains(self, swaptries, include_probg=True, uniforms=None, seed=0):
+        """uniforms: [nruns, stride] per-run streams, or None for Philox."""
+        used = np.zeros(self.nruns, np.int32)
+        ok = np.zeros(self.nruns, np.int32)
+        if uniforms is not None:
+            uniforms = _f64(uniforms).reshape(self.nruns, -1)
+            stride = uniforms.shape[1]
+        else:
+            stride = 0
+        self._ck(self.lib.ima_gpu_swapchains(self.h, int(swaptries), int(include_probg), _ptr(uniforms),
+                                             int(stride), int(seed), _ptr(used), _ptr(ok)))
+        return ok, used
+
+    def get_swapcounts(self, run=0):
+        sc = np.zeros((self.cpr, self.cpr), np.int32)
+        tc = np.zeros((self.cpr, self.cpr), np.int32)
+        self._ck(self.lib.ima_gpu_get_swapcounts(self.h, int(run), _ptr(sc), _ptr(tc)))
+        return sc, tc
+
+    # ------------------------------------------------------- surface
+    def surface_load(self, rows, numpopsizeparams, nummigrateparams, npops, lognorm=None):
+        rows = np.ascontiguousarray(rows, np.float32)
+        self.surf_npar = numpopsizeparams + nummigrateparams
+        self._ck(self.lib.ima_gpu_surface_load(self.h, rows.shape[0], rows.shape[1], _ptr(rows),
+                                               int(numpopsizeparams), int(nummigrateparams), int(npops),
+                                               _ptr(_f64(lognorm))))
+
+    def surface_eval(self, x, modeltype=0, method=SURF_FAST):
+        x = _f64(x).reshape(-1, self.surf_npar)
+        q = np.zeros(len(x))
+        ess = np.zeros(len(x))
+        self._ck(self.lib.ima_gpu_surface_eval(self.h, len(x), _ptr(x), int(modeltype), int(method),
+                                               _ptr(q), _ptr(ess)))
+        return q, ess
+
+    def jointp(self, x, calc_ess=1):
+        q = np.zeros(1)
+        e = np.zeros(1)
+        self._ck(self.lib.ima_gpu_jointp(self.h, _ptr(_f64(x)), int(calc_ess), _ptr(e), _ptr(q)))
+        return float(q[0]), float(e[0])
+
+    # --------------------------------------------------- measurement
+    def synchronize(self):
+        self._ck(self.lib.ima_gpu_synchronize(self.h))
+
+    def timer_begin(self):
+        self._ck(self.lib.ima_gpu_timer_begin(self.h))
+
+    def timer_end(self):
+        ms = C.c_float()
+        self._ck(self.lib.ima_gpu_timer_end(self.h, C.byref(ms)))
+        return ms.value
+
+    def set_profiling(self, on):
+        self._ck(self.lib.ima_gpu_set_profiling(self.h, int(on)))
+
+    def kernel_stats(self, kind):
+        n = C.c_longlong()
+        ms = D()
+        by = D()
+        self._ck(self.lib.ima_gpu_kernel_stats(self.h, int(kind), C.byref(n), C.byref(ms), C.byref(by)))
+        return n.value, ms.value, by.value
+
+    def launch_count(self):
+        n = C.c_longlong()
+        self._ck(self.lib.ima_gpu_launch_count(self.h, C.byref(n)))
+        return n.value
+
+    def flush_l2(self):
+        self._ck(self.lib.ima_gpu_flush_l2(self.h))
+
+    def memory(self):
+        n = C.c_size_t()
+        self._ck(self.lib.ima_gpu_memory(self.h, C.byref(n)))
+        return n.value
+
+
+class Batch:
+    """Requests staged on the device; run() replays them (optionally as a graph)."""
+
+    def __init__(self, ctx, handle, n):
+        self.ctx, self.handle, self.n = ctx, handle, n
+
+    def run(self, use_graph=True):
+        self.ctx._ck(self.ctx.lib.ima_gpu_batch_run(self.ctx.h, self.handle, int(use_graph)))
+
+    def results(self):
+        res = np.zeros(self.n)
+        st = np.zeros(self.n, np.int32)
+        self.ctx._ck(self.ctx.lib.ima_gpu_batch_results(self.ctx.h, self.handle, _ptr(res), _ptr(st)))
+        return res, st
+
+    def destroy(self):
+        if self.handle is not None:
+            self.ctx._ck(self.ctx.lib.ima_gpu_batch_destroy(self.ctx.h, self.handle))
+            self.handle = None

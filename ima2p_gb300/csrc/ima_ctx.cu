@@ -1,0 +1,1311 @@
+// ima_ctx.cu -- the C ABI (include/ima_gpu.h): context, resident pools,
+// genealogy staging, request batching, commit/revert, swaps, surface, timing.
+//
+// Host-side genealogy edits land in a pinned mirror of the device pools and
+// are shipped, one contiguous copy per pool over the range of touched
+// chain-loci, before the next launch.  Requests of a batch are grouped by
+// mutation model (one kernel per model) and their results are returned in
+// the caller's order.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+int sw_init_tables();
+
+namespace {
+
+struct LocusHost {
+  LocusDev d;
+  std::vector<int8_t> seq;
+  std::vector<int32_t> mult;
+  bool sumlogk_done = false;
+};
+
+struct Batch {
+  bool live = false;
+  int n = 0, nis = 0, nhky = 0, nsw = 0, prec = IMA_PREC_FAST;
+  std::vector<int> order;  // grouped position -> caller index
+  ReqDev *d_req = nullptr;
+  double *d_res = nullptr;
+  int32_t *d_st = nullptr;
+  std::vector<ReqDev> h_req;
+  cudaGraphExec_t graph = nullptr;
+  int maxn_is = 0, maxs_is = 0, maxn_hky = 0, maxn_sw = 0;
+  int cap = 0;  // capacity of the device buffers
+};
+
+struct PendingTiming {
+  int kind;
+  cudaEvent_t a, b;
+  double bytes;
+};
+
+template <typename T>
+T *dev_alloc(size_t count, size_t &total)
+{
+  if (count == 0) count = 1;
+  void *p = nullptr;
+  if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) return nullptr;
+  cudaMemset(p, 0, count * sizeof(T));
+  total += count * sizeof(T);
+  return static_cast<T *>(p);
+}
+
+template <typename T>
+T *host_alloc(size_t count)
+{
+  if (count == 0) count = 1;
+  void *p = nullptr;
+  if (cudaMallocHost(&p, count * sizeof(T)) != cudaSuccess) return nullptr;
+  memset(p, 0, count * sizeof(T));
+  return static_cast<T *>(p);
+}
+
+}  // namespace
+
+struct ima_ctx {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  std::string err;
+  size_t dev_bytes = 0;
+  long long launches = 0;
+
+  // loci
+  std::vector<LocusHost> loci;
+  LocusDev *d_loci = nullptr;
+  int8_t *d_seq = nullptr;
+  int32_t *d_mult = nullptr;
+  double *d_sumlogk = nullptr;
+  int *d_flag = nullptr;
+
+  // chains x loci
+  int nruns = 0, cpr = 0, nchains = 0, nloci = 0, nitems = 0;
+  std::vector<ItemDev> items;
+  ItemDev *d_items = nullptr;
+  size_t nnodes = 0, nsched = 0, nal = 0, npart = 0, npart64 = 0;
+  // host mirrors (pinned)
+  NodeRec *h_nodes = nullptr;
+  double *h_t64 = nullptr;
+  float2 *h_tff = nullptr;
+  int16_t *h_sched = nullptr;
+  int32_t *h_nlev = nullptr;
+  double *h_len = nullptr;
+  double *h_pi = nullptr;
+  int32_t *h_al = nullptr;
+  int dirty_lo = INT32_MAX, dirty_hi = -1;
+  // device pools
+  NodeRec *d_nodes = nullptr;
+  double *d_t64 = nullptr;
+  float2 *d_tff = nullptr;
+  int16_t *d_sched = nullptr;
+  int32_t *d_nlev = nullptr;
+  double *d_len = nullptr;
+  double *d_pi = nullptr;
+  int32_t *d_al = nullptr;
+  double *d_dlike = nullptr;
+  std::vector<uint8_t> dl_fast;  // per item x marker: last SW evaluation was float-float
+  std::vector<uint8_t> has_tree; // per item: a genealogy was uploaded
+  float4 *d_part = nullptr;
+  int32_t *d_pexp = nullptr;
+  double *d_part64 = nullptr, *d_psf64 = nullptr;
+  uint8_t *d_slot32 = nullptr, *d_fresh32 = nullptr, *d_slot64 = nullptr, *d_fresh64 = nullptr;
+  double *d_pdg = nullptr, *d_pdg_new = nullptr;
+
+  // MC3
+  double *d_beta = nullptr, *d_allbetas = nullptr, *d_probg = nullptr, *d_S = nullptr;
+  int32_t *d_swapcount = nullptr, *d_tempcount = nullptr, *d_used = nullptr, *d_swap0ok = nullptr;
+  unsigned long long *d_ctr = nullptr;
+  double *d_uni = nullptr;
+  size_t uni_cap = 0;
+
+  // surface
+  int sG = 0, srowlen = 0, snp = 0, snm = 0, snpops = 0;
+  float *d_rows = nullptr;
+  double *d_lognorm = nullptr;
+  void *d_sscratch = nullptr;
+  size_t sscratch_cap = 0;
+  double *d_sx = nullptr, *d_sq = nullptr, *d_sess = nullptr;
+  size_t spts_cap = 0;
+
+  // batches
+  std::vector<Batch> batches;
+  Batch evb;  // buffers of ima_gpu_eval
+  int32_t *d_citems = nullptr;
+  uint8_t *d_cacc = nullptr;
+  size_t ccap = 0;
+
+  // timing
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  bool profiling = false;
+  std::vector<PendingTiming> pending;
+  long long k_launches[IMA_K_COUNT] = {0};
+  double k_ms[IMA_K_COUNT] = {0}, k_bytes[IMA_K_COUNT] = {0};
+  std::vector<cudaEvent_t> event_pool;
+  void *d_flush = nullptr;
+  size_t flush_bytes = 0;
+
+  int fail(int code, const char *fmt, ...)
+  {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    err = buf;
+    return code;
+  }
+  int cuda(cudaError_t e, const char *what)
+  {
+    if (e == cudaSuccess) return IMA_OK;
+    return fail(IMA_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  }
+  Pools pools() const
+  {
+    Pools P;
+    P.loci = d_loci;
+    P.items = d_items;
+    P.seq = d_seq;
+    P.mult = d_mult;
+    P.nodes = d_nodes;
+    P.t64 = d_t64;
+    P.tff = d_tff;
+    P.sched = d_sched;
+    P.nlev = d_nlev;
+    P.length = d_len;
+    P.pi = d_pi;
+    P.alleles = d_al;
+    P.dlike = d_dlike;
+    P.sumlogk = d_sumlogk;
+    P.pdg_new = d_pdg_new;
+    P.part = d_part;
+    P.pexp = d_pexp;
+    P.part64 = d_part64;
+    P.psf64 = d_psf64;
+    P.slot32 = d_slot32;
+    P.fresh32 = d_fresh32;
+    P.slot64 = d_slot64;
+    P.fresh64 = d_fresh64;
+    return P;
+  }
+  cudaEvent_t ev()
+  {
+    if (!event_pool.empty()) {
+      cudaEvent_t e = event_pool.back();
+      event_pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+  }
+  // bracket one kernel launch for accounting
+  template <typename F>
+  void launch(int kind, double bytes, F &&f)
+  {
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (profiling) {
+      a = ev();
+      b = ev();
+      cudaEventRecord(a, st);
+    }
+    f();
+    launches++;
+    k_launches[kind]++;
+    k_bytes[kind] += bytes;
+    if (profiling) {
+      cudaEventRecord(b, st);
+      pending.push_back({kind, a, b, bytes});
+    }
+  }
+  void resolve_timings()
+  {
+    if (pending.empty()) return;
+    cudaStreamSynchronize(st);
+    for (auto &p : pending) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, p.a, p.b);
+      k_ms[p.kind] += ms;
+      event_pool.push_back(p.a);
+      event_pool.push_back(p.b);
+    }
+    pending.clear();
+  }
+  int item_of(int ci, int li) const { return ci * nloci + li; }
+  bool valid(int ci, int li) const { return ci >= 0 && ci < nchains && li >= 0 && li < nloci; }
+};
+
+// ======================================================================
+// context
+extern "C" int ima_gpu_create(int device, ima_ctx **out)
+{
+  if (!out) return IMA_ERR_ARG;
+  *out = nullptr;
+  ima_ctx *c = new (std::nothrow) ima_ctx;
+  if (!c) return IMA_ERR_NOMEM;
+  c->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return IMA_ERR_CUDA;
+  }
+  cudaEventCreate(&c->t0);
+  cudaEventCreate(&c->t1);
+  if (sw_init_tables() != 0) {
+    delete c;
+    return IMA_ERR_CUDA;
+  }
+  c->d_flag = dev_alloc<int>(64, c->dev_bytes);
+  *out = c;
+  return IMA_OK;
+}
+
+extern "C" void ima_gpu_destroy(ima_ctx *c)
+{
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->st);
+  c->batches.push_back(c->evb);
+  for (auto &b : c->batches) {
+    if (b.graph) cudaGraphExecDestroy(b.graph);
+    cudaFree(b.d_req);
+    cudaFree(b.d_res);
+    cudaFree(b.d_st);
+  }
+  void *devs[] = {c->d_loci, c->d_seq, c->d_mult, c->d_sumlogk, c->d_flag, c->d_items,
+                  c->d_nodes, c->d_t64, c->d_tff, c->d_sched, c->d_nlev, c->d_len, c->d_pi,
+                  c->d_al, c->d_dlike, c->d_part, c->d_pexp, c->d_part64, c->d_psf64,
+                  c->d_slot32, c->d_fresh32, c->d_slot64, c->d_fresh64, c->d_pdg, c->d_pdg_new,
+                  c->d_beta, c->d_allbetas, c->d_probg, c->d_S, c->d_swapcount, c->d_tempcount,
+                  c->d_used, c->d_swap0ok, c->d_ctr, c->d_uni, c->d_rows, c->d_lognorm,
+                  c->d_sscratch, c->d_sx, c->d_sq, c->d_sess, c->d_citems, c->d_cacc, c->d_flush};
+  for (void *p : devs)
+    if (p) cudaFree(p);
+  void *hosts[] = {c->h_nodes, c->h_t64, c->h_tff, c->h_sched, c->h_nlev, c->h_len, c->h_pi, c->h_al};
+  for (void *p : hosts)
+    if (p) cudaFreeHost(p);
+  for (auto &p : c->pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+  for (auto e : c->event_pool) cudaEventDestroy(e);
+  if (c->t0) cudaEventDestroy(c->t0);
+  if (c->t1) cudaEventDestroy(c->t1);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+}
+
+extern "C" const char *ima_gpu_error(const ima_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+extern "C" int ima_gpu_synchronize(ima_ctx *c)
+{
+  if (!c) return IMA_ERR_ARG;
+  return c->cuda(cudaStreamSynchronize(c->st), "synchronize");
+}
+
+// ======================================================================
+// loci
+static int add_locus(ima_ctx *c, int model, int n, int S, int tots, const int8_t *seq,
+                     const int32_t *mult, int nlinked, int *li)
+{
+  if (!c || !li) return IMA_ERR_ARG;
+  if (c->nchains) return c->fail(IMA_ERR_STATE, "loci must be added before ima_gpu_set_chains");
+  if (n < 2 || n > 16000) return c->fail(IMA_ERR_ARG, "numgenes %d out of range", n);
+  if (S < 0 || (S > 0 && !seq && model != IMA_MODEL_SW)) return c->fail(IMA_ERR_ARG, "bad sites");
+  LocusHost L;
+  L.d.model = model;
+  L.d.n = n;
+  L.d.nsites = S;
+  L.d.totsites = tots;
+  L.d.nlinked = nlinked;
+  if (seq && S > 0) {
+    L.seq.assign(seq, seq + (size_t)n * S);
+    for (int8_t v : L.seq) {
+      if (model == IMA_MODEL_IS && (v < 0 || v > 1)) return c->fail(IMA_ERR_ARG, "IS states must be 0/1");
+      if (model == IMA_MODEL_HKY && (v < 0 || v > 3)) return c->fail(IMA_ERR_ARG, "HKY states must be 0..3");
+    }
+  }
+  if (mult) L.mult.assign(mult, mult + S);
+  *li = (int)c->loci.size();
+  c->loci.push_back(std::move(L));
+  return IMA_OK;
+}
+
+extern "C" int ima_gpu_add_locus_is(ima_ctx *c, int numgenes, int numsites, const int8_t *seq, int *li)
+{
+  return add_locus(c, IMA_MODEL_IS, numgenes, numsites, numsites, seq, nullptr, 1, li);
+}
+
+extern "C" int ima_gpu_add_locus_hky(ima_ctx *c, int numgenes, int numsites, int totsites,
+                                     const int8_t *seq, const int32_t *mult, int *li)
+{
+  if (!c || !mult || numsites < 1 || totsites < 1) return c ? c->fail(IMA_ERR_ARG, "bad HKY locus") : IMA_ERR_ARG;
+  return add_locus(c, IMA_MODEL_HKY, numgenes, numsites, totsites, seq, mult, 1, li);
+}
+
+extern "C" int ima_gpu_add_locus_sw(ima_ctx *c, int numgenes, int nlinked, int *li)
+{
+  if (nlinked < 1) return c ? c->fail(IMA_ERR_ARG, "nlinked must be >= 1") : IMA_ERR_ARG;
+  return add_locus(c, IMA_MODEL_SW, numgenes, 0, 0, nullptr, nullptr, nlinked, li);
+}
+
+extern "C" int ima_gpu_set_chains(ima_ctx *c, int nruns, int chains_per_run)
+{
+  if (!c) return IMA_ERR_ARG;
+  if (c->nchains) return c->fail(IMA_ERR_STATE, "chains already set");
+  if (nruns < 1 || chains_per_run < 1 || c->loci.empty())
+    return c->fail(IMA_ERR_ARG, "need >= 1 run, >= 1 chain and >= 1 locus");
+  cudaSetDevice(c->device);
+  c->nruns = nruns;
+  c->cpr = chains_per_run;
+  c->nchains = nruns * chains_per_run;
+  c->nloci = (int)c->loci.size();
+  c->nitems = c->nchains * c->nloci;
+  // locus tables
+  std::vector<int8_t> seq;
+  std::vector<int32_t> mult;
+  std::vector<LocusDev> ld;
+  for (auto &L : c->loci) {
+    L.d.seq_off = (int)seq.size();
+    L.d.mult_off = (int)mult.size();
+    seq.insert(seq.end(), L.seq.begin(), L.seq.end());
+    mult.insert(mult.end(), L.mult.begin(), L.mult.end());
+    ld.push_back(L.d);
+  }
+  // placement of every chain-locus
+  c->items.resize(c->nitems);
+  size_t nodes = 0, sched = 0, al = 0, part = 0, part64 = 0;
+  for (int ci = 0; ci < c->nchains; ci++)
+    for (int li = 0; li < c->nloci; li++) {
+      const LocusDev &L = ld[li];
+      ItemDev &it = c->items[c->item_of(ci, li)];
+      int nl = 2 * L.n - 1;
+      it.locus = li;
+      it.n = L.n;
+      it.node_off = (int)nodes;
+      it.sched_off = (int)sched;
+      it.al_off = (int)al;
+      it.dl_off = (int)al;
+      it.part_off = (long long)part;
+      it.part64_off = (long long)part64;
+      nodes += nl;
+      sched += 2 * L.n + 2;
+      if (L.model == IMA_MODEL_SW) al += (size_t)L.nlinked * nl;
+      if (L.model == IMA_MODEL_HKY) {
+        part += 2 * (size_t)(L.n - 1) * L.nsites;
+        part64 += 2 * (size_t)(L.n - 1) * L.nsites;
+      }
+    }
+  if (nodes > (size_t)INT32_MAX || sched > (size_t)INT32_MAX || al > (size_t)INT32_MAX)
+    return c->fail(IMA_ERR_ARG, "too many nodes for 32-bit offsets");
+  c->nnodes = nodes;
+  c->nsched = sched;
+  c->nal = al;
+  c->npart = part;
+  c->npart64 = part64;
+  size_t &B = c->dev_bytes;
+  c->d_loci = dev_alloc<LocusDev>(ld.size(), B);
+  c->d_seq = dev_alloc<int8_t>(seq.size(), B);
+  c->d_mult = dev_alloc<int32_t>(mult.size(), B);
+  c->d_sumlogk = dev_alloc<double>(c->nloci, B);
+  c->d_items = dev_alloc<ItemDev>(c->nitems, B);
+  c->d_nodes = dev_alloc<NodeRec>(nodes, B);
+  c->d_t64 = dev_alloc<double>(nodes, B);
+  c->d_tff = dev_alloc<float2>(nodes, B);
+  c->d_slot32 = dev_alloc<uint8_t>(nodes, B);
+  c->d_fresh32 = dev_alloc<uint8_t>(nodes, B);
+  c->d_sched = dev_alloc<int16_t>(sched, B);
+  c->d_nlev = dev_alloc<int32_t>(c->nitems, B);
+  c->d_len = dev_alloc<double>(c->nitems, B);
+  c->d_pi = dev_alloc<double>(4 * (size_t)c->nitems, B);
+  c->d_al = dev_alloc<int32_t>(al, B);
+  c->d_dlike = dev_alloc<double>(al, B);
+  c->d_part = dev_alloc<float4>(part, B);
+  c->d_pexp = dev_alloc<int32_t>(part, B);
+  c->d_pdg = dev_alloc<double>(c->nitems, B);
+  c->d_pdg_new = dev_alloc<double>(c->nitems, B);
+  c->d_beta = dev_alloc<double>(c->nchains, B);
+  c->d_allbetas = dev_alloc<double>(c->nchains, B);
+  c->d_probg = dev_alloc<double>(c->nchains, B);
+  c->d_S = dev_alloc<double>(c->nchains, B);
+  c->d_swapcount = dev_alloc<int32_t>((size_t)c->nruns * c->cpr * c->cpr, B);
+  c->d_tempcount = dev_alloc<int32_t>((size_t)c->nruns * c->cpr * c->cpr, B);
+  c->d_used = dev_alloc<int32_t>(c->nruns, B);
+  c->d_swap0ok = dev_alloc<int32_t>(c->nruns, B);
+  c->d_ctr = dev_alloc<unsigned long long>(c->nruns, B);
+  void *chk[] = {c->d_loci, c->d_seq, c->d_mult, c->d_sumlogk, c->d_items, c->d_nodes, c->d_t64,
+                 c->d_tff, c->d_slot32, c->d_fresh32, c->d_sched, c->d_nlev, c->d_len, c->d_pi,
+                 c->d_al, c->d_dlike, c->d_part, c->d_pexp, c->d_pdg, c->d_pdg_new, c->d_beta,
+                 c->d_allbetas, c->d_probg, c->d_S, c->d_swapcount, c->d_tempcount, c->d_used,
+                 c->d_swap0ok, c->d_ctr};
+  for (void *p : chk)
+    if (!p) return c->fail(IMA_ERR_NOMEM, "device allocation failed (%zu bytes so far)", B);
+  c->h_nodes = host_alloc<NodeRec>(nodes);
+  c->h_t64 = host_alloc<double>(nodes);
+  c->h_tff = host_alloc<float2>(nodes);
+  c->h_sched = host_alloc<int16_t>(sched);
+  c->h_nlev = host_alloc<int32_t>(c->nitems);
+  c->h_len = host_alloc<double>(c->nitems);
+  c->h_pi = host_alloc<double>(4 * (size_t)c->nitems);
+  c->h_al = host_alloc<int32_t>(al);
+  if (!c->h_nodes || !c->h_t64 || !c->h_tff || !c->h_sched || !c->h_nlev || !c->h_len || !c->h_pi || !c->h_al)
+    return c->fail(IMA_ERR_NOMEM, "pinned host allocation failed");
+  for (int i = 0; i < c->nitems; i++)
+    for (int j = 0; j < 4; j++) c->h_pi[4 * (size_t)i + j] = 0.25;
+  c->dl_fast.assign(al ? al : 1, 0);
+  c->has_tree.assign(c->nitems, 0);
+  int r = IMA_OK;
+  r = r ? r : c->cuda(cudaMemcpy(c->d_loci, ld.data(), ld.size() * sizeof(LocusDev), cudaMemcpyHostToDevice), "loci");
+  if (!seq.empty()) r = r ? r : c->cuda(cudaMemcpy(c->d_seq, seq.data(), seq.size(), cudaMemcpyHostToDevice), "seq");
+  if (!mult.empty()) r = r ? r : c->cuda(cudaMemcpy(c->d_mult, mult.data(), mult.size() * 4, cudaMemcpyHostToDevice), "mult");
+  r = r ? r : c->cuda(cudaMemcpy(c->d_items, c->items.data(), c->items.size() * sizeof(ItemDev), cudaMemcpyHostToDevice), "items");
+  r = r ? r : c->cuda(cudaMemcpy(c->d_pi, c->h_pi, 4 * sizeof(double) * c->nitems, cudaMemcpyHostToDevice), "pi");
+  return r;
+}
+
+// ======================================================================
+// genealogies
+static void mark(ima_ctx *c, int item)
+{
+  c->dirty_lo = std::min(c->dirty_lo, item);
+  c->dirty_hi = std::max(c->dirty_hi, item);
+}
+
+extern "C" int ima_gpu_set_genealogy(ima_ctx *c, int ci, int li, const int32_t *up0, const int32_t *up1,
+                                     const int32_t *down, const double *time, double length)
+{
+  if (!c || !up0 || !up1 || !down || !time) return IMA_ERR_ARG;
+  if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
+  if (!c->valid(ci, li)) return c->fail(IMA_ERR_ARG, "chain %d locus %d out of range", ci, li);
+  const int item = c->item_of(ci, li);
+  const ItemDev &it = c->items[item];
+  const int n = it.n, nl = 2 * n - 1;
+  // validate the topology: tips have no daughters, internal nodes two, one root
+  int root = -1;
+  for (int k = 0; k < nl; k++) {
+    bool tip = k < n;
+    if (tip != (up0[k] < 0) || tip != (up1[k] < 0)) return c->fail(IMA_ERR_ARG, "node %d: daughters do not match tip/internal numbering", k);
+    if (!tip) {
+      if (up0[k] >= nl || up1[k] >= nl || up0[k] == up1[k]) return c->fail(IMA_ERR_ARG, "node %d: bad daughters", k);
+      if (down[up0[k]] != k || down[up1[k]] != k) return c->fail(IMA_ERR_ARG, "node %d: parent links disagree", k);
+    }
+    if (down[k] < 0) {
+      if (root >= 0) return c->fail(IMA_ERR_ARG, "two roots (%d, %d)", root, k);
+      root = k;
+    } else if (down[k] < n || down[k] >= nl) {
+      return c->fail(IMA_ERR_ARG, "node %d: bad parent %d", k, down[k]);
+    }
+  }
+  if (root < n) return c->fail(IMA_ERR_ARG, "no internal root");
+  // heights by an explicit post-order from the root; levels = heights 1..H
+  std::vector<int> height(nl, 0), stack;
+  std::vector<uint8_t> seen(nl, 0);
+  stack.push_back(root);
+  int visited = 0;
+  while (!stack.empty()) {
+    int v = stack.back();
+    if (v < n) {
+      stack.pop_back();
+      visited++;
+      continue;
+    }
+    if (!seen[v]) {
+      seen[v] = 1;
+      stack.push_back(up0[v]);
+      stack.push_back(up1[v]);
+      if (stack.size() > (size_t)4 * nl) return c->fail(IMA_ERR_ARG, "genealogy has a cycle");
+      continue;
+    }
+    stack.pop_back();
+    height[v] = 1 + std::max(height[up0[v]], height[up1[v]]);
+    visited++;
+  }
+  if (visited != nl) return c->fail(IMA_ERR_ARG, "genealogy is not connected");
+  int H = height[root];
+  std::vector<int> cnt(H + 2, 0);
+  for (int k = n; k < nl; k++) cnt[height[k]]++;
+  int16_t *sch = c->h_sched + it.sched_off;
+  int16_t *order = sch, *lstart = sch + (n - 1);
+  std::vector<int> pos(H + 2, 0);
+  for (int h = 1; h <= H; h++) pos[h + 1] = pos[h] + cnt[h];
+  for (int h = 1; h <= H + 1; h++) lstart[h - 1] = (int16_t)pos[h];
+  for (int k = n; k < nl; k++) order[pos[height[k]]++] = (int16_t)k;
+  c->h_nlev[item] = H;
+  double L = 0.0;
+  for (int k = 0; k < nl; k++) {
+    NodeRec &r = c->h_nodes[it.node_off + k];
+    r.up0 = (int16_t)up0[k];
+    r.up1 = (int16_t)up1[k];
+    r.down = (int16_t)down[k];
+    r.pad = 0;
+    double t = time[k];
+    c->h_t64[it.node_off + k] = t;
+    float hi = (float)t;
+    c->h_tff[it.node_off + k] = make_float2(hi, (float)(t - (double)hi));
+    if (down[k] >= 0) L += (up0[k] < 0) ? t : t - time[up0[k]];
+  }
+  c->h_len[item] = (length >= 0.0) ? length : L;
+  c->has_tree[item] = 1;
+  mark(c, item);
+  return IMA_OK;
+}
+
+extern "C" int ima_gpu_set_genealogies(ima_ctx *c, int n, const int32_t *ci, const int32_t *li,
+                                       const int32_t *up0, const int32_t *up1, const int32_t *down,
+                                       const double *time, const double *length)
+{
+  if (!c || n < 0 || (n > 0 && (!ci || !li || !up0 || !up1 || !down || !time))) return IMA_ERR_ARG;
+  size_t off = 0;
+  for (int k = 0; k < n; k++) {
+    if (!c->valid(ci[k], li[k])) return c->fail(IMA_ERR_ARG, "pair %d: chain %d locus %d out of range", k, ci[k], li[k]);
+    int nl = 2 * c->loci[li[k]].d.n - 1;
+    int r = ima_gpu_set_genealogy(c, ci[k], li[k], up0 + off, up1 + off, down + off, time + off,
+                                  length ? length[k] : -1.0);
+    if (r) return r;
+    off += nl;
+  }
+  return IMA_OK;
+}
+
+extern "C" int ima_gpu_set_pi(ima_ctx *c, int ci, int li, const double *pi4)
+{
+  if (!c || !pi4) return IMA_ERR_ARG;
+  if (!c->valid(ci, li)) return c->fail(IMA_ERR_ARG, "chain %d locus %d out of range", ci, li);
+  int item = c->item_of(ci, li);
+  for (int j = 0; j < 4; j++) c->h_pi[4 * (size_t)item + j] = pi4[j];
+  mark(c, item);
+  return IMA_OK;
+}
+
+extern "C" int ima_gpu_set_alleles(ima_ctx *c, int ci, int li, int ai, const int32_t *A)
+{
+  if (!c || !A) return IMA_ERR_ARG;
+  if (!c->valid(ci, li)) return c->fail(IMA_ERR_ARG, "chain %d locus %d out of range", ci, li);
+  const LocusDev &L = c->loci[li].d;
+  if (L.model != IMA_MODEL_SW || ai < 0 || ai >= L.nlinked) return c->fail(IMA_ERR_ARG, "locus %d marker %d is not stepwise", li, ai);
+  int item = c->item_of(ci, li);
+  const ItemDev &it = c->items[item];
+  int nl = 2 * it.n - 1;
+  memcpy(c->h_al + it.al_off + (size_t)ai * nl, A, sizeof(int32_t) * nl);
+  mark(c, item);
+  return IMA_OK;
+}
+
+static int flush(ima_ctx *c)
+{
+  if (c->dirty_hi < 0) return IMA_OK;
+  int lo = c->dirty_lo, hi = c->dirty_hi;
+  const ItemDev &a = c->items[lo], &b = c->items[hi];
+  size_t n0 = a.node_off, n1 = (size_t)b.node_off + 2 * b.n - 1;
+  size_t s0 = a.sched_off, s1 = (size_t)b.sched_off + 2 * b.n + 2;
+  size_t a0 = a.al_off, a1 = (size_t)b.al_off;
+  a1 += (c->loci[b.locus].d.model == IMA_MODEL_SW) ? (size_t)c->loci[b.locus].d.nlinked * (2 * b.n - 1) : 0;
+  cudaStream_t st = c->st;
+  int r = IMA_OK;
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_nodes + n0, c->h_nodes + n0, (n1 - n0) * sizeof(NodeRec), cudaMemcpyHostToDevice, st), "nodes");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_t64 + n0, c->h_t64 + n0, (n1 - n0) * sizeof(double), cudaMemcpyHostToDevice, st), "times");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_tff + n0, c->h_tff + n0, (n1 - n0) * sizeof(float2), cudaMemcpyHostToDevice, st), "times");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_sched + s0, c->h_sched + s0, (s1 - s0) * sizeof(int16_t), cudaMemcpyHostToDevice, st), "sched");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_nlev + lo, c->h_nlev + lo, (hi - lo + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, st), "levels");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_len + lo, c->h_len + lo, (hi - lo + 1) * sizeof(double), cudaMemcpyHostToDevice, st), "length");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_pi + 4 * (size_t)lo, c->h_pi + 4 * (size_t)lo, 4 * (hi - lo + 1) * sizeof(double), cudaMemcpyHostToDevice, st), "pi");
+  if (a1 > a0) r = r ? r : c->cuda(cudaMemcpyAsync(c->d_al + a0, c->h_al + a0, (a1 - a0) * sizeof(int32_t), cudaMemcpyHostToDevice, st), "alleles");
+  c->dirty_lo = INT32_MAX;
+  c->dirty_hi = -1;
+  return r;
+}
+
+extern "C" int ima_gpu_flush_genealogies(ima_ctx *c)
+{
+  if (!c) return IMA_ERR_ARG;
+  return flush(c);
+}
+
+// ======================================================================
+// batches
+static int ensure_fp64_hky(ima_ctx *c)
+{
+  if (c->d_part64 || c->npart64 == 0) {
+    if (!c->d_slot64) {
+      c->d_slot64 = dev_alloc<uint8_t>(c->nnodes, c->dev_bytes);
+      c->d_fresh64 = dev_alloc<uint8_t>(c->nnodes, c->dev_bytes);
+    }
+    return IMA_OK;
+  }
+  c->d_part64 = dev_alloc<double>(4 * c->npart64, c->dev_bytes);
+  c->d_psf64 = dev_alloc<double>(c->npart64, c->dev_bytes);
+  c->d_slot64 = dev_alloc<uint8_t>(c->nnodes, c->dev_bytes);
+  c->d_fresh64 = dev_alloc<uint8_t>(c->nnodes, c->dev_bytes);
+  if (!c->d_part64 || !c->d_psf64 || !c->d_slot64 || !c->d_fresh64)
+    return c->fail(IMA_ERR_NOMEM, "FP64 partial likelihood pools (%zu doubles) do not fit", 5 * c->npart64);
+  return IMA_OK;
+}
+
+static int build_batch(ima_ctx *c, Batch &b, int n, const int32_t *ci, const int32_t *li, const double *u,
+                       const double *kappa, const int32_t *edits, const int32_t *ai, int prec)
+{
+  if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
+  if (n < 1 || !ci || !li || !u) return c->fail(IMA_ERR_ARG, "empty or null request list");
+  if (prec != IMA_PREC_FAST && prec != IMA_PREC_FP64) return c->fail(IMA_ERR_ARG, "bad precision");
+  std::vector<int> g[3];
+  for (int k = 0; k < n; k++) {
+    if (!c->valid(ci[k], li[k])) return c->fail(IMA_ERR_ARG, "request %d: chain %d locus %d out of range", k, ci[k], li[k]);
+    const LocusDev &L = c->loci[li[k]].d;
+    if (L.model == IMA_MODEL_SW && ai && (ai[k] < 0 || ai[k] >= L.nlinked)) return c->fail(IMA_ERR_ARG, "request %d: bad marker", k);
+    if (!(u[k] > 0.0)) return c->fail(IMA_ERR_ARG, "request %d: mutation rate must be > 0", k);
+    if (!c->has_tree[c->item_of(ci[k], li[k])]) return c->fail(IMA_ERR_STATE, "request %d: chain %d locus %d has no genealogy", k, ci[k], li[k]);
+    g[L.model].push_back(k);
+  }
+  b.n = n;
+  b.prec = prec;
+  b.nis = (int)g[0].size();
+  b.nhky = (int)g[1].size();
+  b.nsw = (int)g[2].size();
+  b.order.clear();
+  b.h_req.clear();
+  b.maxn_is = b.maxs_is = b.maxn_hky = b.maxn_sw = 0;
+  for (int m = 0; m < 3; m++)
+    for (int k : g[m]) {
+      ReqDev r;
+      r.item = c->item_of(ci[k], li[k]);
+      r.ai = ai ? ai[k] : 0;
+      for (int q = 0; q < 4; q++) r.e[q] = edits ? edits[4 * k + q] : -1;
+      r.u = u[k];
+      r.par = kappa ? kappa[k] : 1.0;
+      const LocusDev &L = c->loci[li[k]].d;
+      if (m == 0) { b.maxn_is = std::max(b.maxn_is, L.n); b.maxs_is = std::max(b.maxs_is, L.nsites); }
+      if (m == 1) b.maxn_hky = std::max(b.maxn_hky, L.n);
+      if (m == 2) b.maxn_sw = std::max(b.maxn_sw, L.n);
+      b.h_req.push_back(r);
+      b.order.push_back(k);
+    }
+  if (b.nhky && prec == IMA_PREC_FP64) {
+    int r = ensure_fp64_hky(c);
+    if (r) return r;
+  }
+  if (!c->d_slot64 && b.nhky) {
+    // the commit kernel touches both slot sets; keep the FP64 marks allocated
+    c->d_slot64 = dev_alloc<uint8_t>(c->nnodes, c->dev_bytes);
+    c->d_fresh64 = dev_alloc<uint8_t>(c->nnodes, c->dev_bytes);
+  }
+  if (b.cap < n) {
+    // the previous capacity may still be read by queued work
+    cudaStreamSynchronize(c->st);
+    cudaFree(b.d_req);
+    cudaFree(b.d_res);
+    cudaFree(b.d_st);
+    size_t &B = c->dev_bytes;
+    b.d_req = dev_alloc<ReqDev>(n, B);
+    b.d_res = dev_alloc<double>(n, B);
+    b.d_st = dev_alloc<int32_t>(n, B);
+    if (!b.d_req || !b.d_res || !b.d_st) {
+      b.cap = 0;
+      return c->fail(IMA_ERR_NOMEM, "batch buffers");
+    }
+    b.cap = n;
+  }
+  return c->cuda(cudaMemcpyAsync(b.d_req, b.h_req.data(), n * sizeof(ReqDev), cudaMemcpyHostToDevice, c->st), "requests");
+}
+
+static double hky_bytes(ima_ctx *c, const Batch &b)
+{
+  double s = 0;
+  for (int k = b.nis; k < b.nis + b.nhky; k++) {
+    const ItemDev &it = c->items[b.h_req[k].item];
+    const LocusDev &L = c->loci[it.locus].d;
+    double nodes = (double)(2 * it.n - 1);
+    s += (double)(it.n - 1) * L.nsites * 20.0 + (double)it.n * L.nsites + L.nsites * 4.0 + nodes * 16.0;
+  }
+  return b.prec == IMA_PREC_FP64 ? s * 2.0 : s;
+}
+
+static double sw_bytes(ima_ctx *c, const Batch &b)
+{
+  double s = 0;
+  for (int k = b.nis + b.nhky; k < b.n; k++) {
+    const ItemDev &it = c->items[b.h_req[k].item];
+    s += (double)(2 * it.n - 1) * 28.0;  // node + times + allele + dlikeA write
+  }
+  return s;
+}
+
+// kernels of a batch (no host work, graph-capturable once sumlogk is set)
+static void enqueue(ima_ctx *c, Batch &b)
+{
+  Pools P = c->pools();
+  cudaStream_t st = c->st;
+  if (b.nis)
+    c->launch(IMA_K_IS, 0.0, [&] { launch_is(P, b.d_req, b.nis, b.maxn_is, b.maxs_is, b.d_res, b.d_st, nullptr, st); });
+  if (b.nhky) {
+    const ReqDev *r = b.d_req + b.nis;
+    if (b.prec == IMA_PREC_FP64)
+      c->launch(IMA_K_HKY_FP64, hky_bytes(c, b), [&] { launch_hky_fp64(P, r, b.nhky, b.maxn_hky, b.d_res + b.nis, b.d_st + b.nis, st); });
+    else
+      c->launch(IMA_K_HKY_FAST, hky_bytes(c, b), [&] { launch_hky_fast(P, r, b.nhky, b.maxn_hky, b.d_res + b.nis, b.d_st + b.nis, st); });
+  }
+  if (b.nsw) {
+    const ReqDev *r = b.d_req + b.nis + b.nhky;
+    int off = b.nis + b.nhky;
+    if (b.prec == IMA_PREC_FP64)
+      c->launch(IMA_K_SW_FP64, sw_bytes(c, b), [&] { launch_sw_fp64(P, r, b.nsw, b.d_res + off, b.d_st + off, st); });
+    else
+      c->launch(IMA_K_SW_FAST, sw_bytes(c, b), [&] { launch_sw_fast(P, r, b.nsw, b.d_res + off, b.d_st + off, st); });
+  }
+}
+
+// the reference caches sum log k! from the first genealogy it evaluates per locus
+static int init_sumlogk(ima_ctx *c, Batch &b)
+{
+  bool any = false;
+  for (int k = 0; k < b.nis; k++) {
+    int li = c->items[b.h_req[k].item].locus;
+    if (!c->loci[li].sumlogk_done) any = true;
+  }
+  if (!any) return IMA_OK;
+  // first request of each uninitialised locus in the caller's order
+  std::vector<std::pair<int, int>> firsts;  // (caller index, grouped index)
+  for (int k = 0; k < b.nis; k++) firsts.push_back({b.order[k], k});
+  std::sort(firsts.begin(), firsts.end());
+  Pools P = c->pools();
+  std::vector<int> inited;
+  for (auto &f : firsts) {
+    int item = b.h_req[f.second].item;
+    int li = c->items[item].locus;
+    LocusHost &L = c->loci[li];
+    if (L.sumlogk_done) continue;
+    c->launch(IMA_K_IS_SUMLOGK, 0.0, [&] { launch_is_sumlogk(P, item, li, L.d.n, L.d.nsites, c->d_flag, c->st); });
+    int flag = 0;
+    int r = c->cuda(cudaMemcpyAsync(&flag, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->st), "sumlogk flag");
+    r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "sumlogk");
+    if (r) return r;
+    if (flag == 2) return c->fail(IMA_ERR_DATA, "Data incompatible with current genealogy, likelihood calculation failed, chain %d, locus %d", item / c->nloci, li);
+    L.sumlogk_done = true;
+  }
+  return IMA_OK;
+}
+
+static int fetch(ima_ctx *c, Batch &b, double *result, int32_t *status)
+{
+  std::vector<double> res(b.n);
+  std::vector<int32_t> sts(b.n);
+  int r = c->cuda(cudaMemcpyAsync(res.data(), b.d_res, b.n * sizeof(double), cudaMemcpyDeviceToHost, c->st), "results");
+  r = r ? r : c->cuda(cudaMemcpyAsync(sts.data(), b.d_st, b.n * sizeof(int32_t), cudaMemcpyDeviceToHost, c->st), "status");
+  r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "evaluation");
+  if (r) return r;
+  for (int k = 0; k < b.n; k++) {
+    if (result) result[b.order[k]] = res[k];
+    if (status) status[b.order[k]] = sts[k];
+  }
+  // remember the format of the per-branch SW terms
+  for (int k = b.nis + b.nhky; k < b.n; k++) {
+    const ItemDev &it = c->items[b.h_req[k].item];
+    c->dl_fast[it.al_off + (size_t)b.h_req[k].ai] = (b.prec == IMA_PREC_FAST);
+  }
+  return IMA_OK;
+}
+
+static void free_batch(Batch &b)
+{
+  if (b.graph) cudaGraphExecDestroy(b.graph);
+  cudaFree(b.d_req);
+  cudaFree(b.d_res);
+  cudaFree(b.d_st);
+  b = Batch();
+}
+
+extern "C" int ima_gpu_eval(ima_ctx *c, int n, const int32_t *ci, const int32_t *li, const double *u,
+                            const double *kappa, const int32_t *edits, const int32_t *ai, int precision,
+                            double *result, int32_t *status)
+{
+  if (!c) return IMA_ERR_ARG;
+  Batch &b = c->evb;  // reused request buffers: no allocation per call
+  int r = build_batch(c, b, n, ci, li, u, kappa, edits, ai, precision);
+  r = r ? r : flush(c);
+  r = r ? r : init_sumlogk(c, b);
+  if (!r) enqueue(c, b);
+  r = r ? r : c->cuda(cudaGetLastError(), "launch");
+  r = r ? r : fetch(c, b, result, status);
+  return r;
+}
+
+extern "C" int ima_gpu_batch_create(ima_ctx *c, int n, const int32_t *ci, const int32_t *li, const double *u,
+                                    const double *kappa, const int32_t *edits, const int32_t *ai,
+                                    int precision, int *batch)
+{
+  if (!c || !batch) return IMA_ERR_ARG;
+  Batch b;
+  int r = build_batch(c, b, n, ci, li, u, kappa, edits, ai, precision);
+  if (r) {
+    free_batch(b);
+    return r;
+  }
+  b.live = true;
+  for (size_t k = 0; k < c->batches.size(); k++)
+    if (!c->batches[k].live) {
+      c->batches[k] = b;
+      *batch = (int)k;
+      return IMA_OK;
+    }
+  c->batches.push_back(b);
+  *batch = (int)c->batches.size() - 1;
+  return IMA_OK;
+}
+
+extern "C" int ima_gpu_batch_run(ima_ctx *c, int batch, int use_graph)
+{
+  if (!c || batch < 0 || batch >= (int)c->batches.size() || !c->batches[batch].live) return IMA_ERR_ARG;
+  Batch &b = c->batches[batch];
+  int r = flush(c);
+  r = r ? r : init_sumlogk(c, b);
+  if (r) return r;
+  if (!use_graph || c->profiling) {
+    enqueue(c, b);
+    return c->cuda(cudaGetLastError(), "launch");
+  }
+  if (!b.graph) {
+    cudaGraph_t g;
+    r = c->cuda(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal), "capture");
+    if (r) return r;
+    long long before = c->launches;
+    enqueue(c, b);
+    long long nk = c->launches - before;
+    r = c->cuda(cudaStreamEndCapture(c->st, &g), "capture end");
+    if (r) return r;
+    r = c->cuda(cudaGraphInstantiate(&b.graph, g, 0), "graph instantiate");
+    cudaGraphDestroy(g);
+    if (r) return r;
+    c->launches -= nk;  // counted when replayed
+  }
+  r = c->cuda(cudaGraphLaunch(b.graph, c->st), "graph launch");
+  c->launches += (b.nis ? 1 : 0) + (b.nhky ? 1 : 0) + (b.nsw ? 1 : 0);
+  return r;
+}
+
+extern "C" int ima_gpu_batch_results(ima_ctx *c, int batch, double *result, int32_t *status)
+{
+  if (!c || batch < 0 || batch >= (int)c->batches.size() || !c->batches[batch].live) return IMA_ERR_ARG;
+  return fetch(c, c->batches[batch], result, status);
+}
+
+extern "C" int ima_gpu_batch_destroy(ima_ctx *c, int batch)
+{
+  if (!c || batch < 0 || batch >= (int)c->batches.size() || !c->batches[batch].live) return IMA_ERR_ARG;
+  cudaStreamSynchronize(c->st);
+  free_batch(c->batches[batch]);
+  return IMA_OK;
+}
+
+// ======================================================================
+// commit / revert
+static int commit(ima_ctx *c, int n, const int32_t *ci, const int32_t *li, const uint8_t *accept,
+                  bool partials, bool pdg)
+{
+  if (!c || n < 1 || !ci || !li || !accept) return IMA_ERR_ARG;
+  if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
+  std::vector<int32_t> items(n);
+  for (int k = 0; k < n; k++) {
+    if (!c->valid(ci[k], li[k])) return c->fail(IMA_ERR_ARG, "chain %d locus %d out of range", ci[k], li[k]);
+    items[k] = c->item_of(ci[k], li[k]);
+  }
+  if ((size_t)n > c->ccap) {
+    cudaStreamSynchronize(c->st);
+    cudaFree(c->d_citems);
+    cudaFree(c->d_cacc);
+    c->d_citems = dev_alloc<int32_t>(n, c->dev_bytes);
+    c->d_cacc = dev_alloc<uint8_t>(n, c->dev_bytes);
+    if (!c->d_citems || !c->d_cacc) return c->fail(IMA_ERR_NOMEM, "commit buffers");
+    c->ccap = n;
+  }
+  int r = c->cuda(cudaMemcpyAsync(c->d_citems, items.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, c->st), "commit");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_cacc, accept, n, cudaMemcpyHostToDevice, c->st), "commit");
+  if (r) return r;
+  Pools P = c->pools();
+  if (partials && c->d_slot64) launch_hky_commit(P, c->d_citems, c->d_cacc, n, c->st), c->launches++;
+  if (pdg) launch_pdg_commit(c->d_citems, c->d_cacc, c->d_pdg_new, c->d_pdg, n, c->st), c->launches++;
+  r = c->cuda(cudaGetLastError(), "commit launch");
+  // the host arrays are stack-owned: wait for the copies
+  return r ? r : c->cuda(cudaStreamSynchronize(c->st), "commit");
+}
+
+extern "C" int ima_gpu_commit(ima_ctx *c, int n, const int32_t *ci, const int32_t *li, const uint8_t *accept)
+{
+  return commit(c, n, ci, li, accept, true, true);
+}
+
+// ======================================================================
+// per-call reference mirrors
+extern "C" int ima_gpu_likelihoodIS(ima_ctx *c, int ci, int li, double mutrate, double *result)
+{
+  if (!c || !result) return IMA_ERR_ARG;
+  if (!c->valid(ci, li) || c->loci[li].d.model != IMA_MODEL_IS) return c->fail(IMA_ERR_ARG, "locus %d is not infinite-sites", li);
+  int32_t st = 0;
+  int r = ima_gpu_eval(c, 1, &ci, &li, &mutrate, nullptr, nullptr, nullptr, IMA_PREC_FP64, result, &st);
+  if (r) return r;
+  if (st == IMA_EVAL_IS_FAIL) return c->fail(IMA_ERR_DATA, "Data incompatible with current genealogy, likelihood calculation failed, chain %d, locus %d", ci, li);
+  return IMA_OK;
+}
+
+extern "C" int ima_gpu_likelihoodHKY(ima_ctx *c, int ci, int li, double mutrate, double kappa,
+                                     int e1, int e2, int e3, int e4, double *result)
+{
+  if (!c || !result) return IMA_ERR_ARG;
+  if (!c->valid(ci, li) || c->loci[li].d.model != IMA_MODEL_HKY) return c->fail(IMA_ERR_ARG, "locus %d is not HKY", li);
+  int32_t e[4] = {e1, e2, e3, e4};
+  return ima_gpu_eval(c, 1, &ci, &li, &mutrate, &kappa, e, nullptr, IMA_PREC_FAST, result, nullptr);
+}
+
+extern "C" int ima_gpu_copyfraclike(ima_ctx *c, int ci, int li)
+{
+  uint8_t a = 1;
+  return commit(c, 1, &ci, &li, &a, true, false);
+}
+
+extern "C" int ima_gpu_storescalefactors(ima_ctx *c, int ci, int li)
+{
+  // scale factors travel with their partial likelihoods: committed by copyfraclike
+  if (!c) return IMA_ERR_ARG;
+  if (!c->valid(ci, li)) return c->fail(IMA_ERR_ARG, "chain %d locus %d out of range", ci, li);
+  return IMA_OK;
+}
+
+extern "C" int ima_gpu_restorescalefactors(ima_ctx *c, int ci, int li)
+{
+  uint8_t a = 0;
+  return commit(c, 1, &ci, &li, &a, true, false);
+}
+
+extern "C" int ima_gpu_likelihoodSW(ima_ctx *c, int ci, int li, int ai, double u, double tr, double *result)
+{
+  if (!c || !result) return IMA_ERR_ARG;
+  if (!c->valid(ci, li) || c->loci[li].d.model != IMA_MODEL_SW) return c->fail(IMA_ERR_ARG, "locus %d is not stepwise", li);
+  return ima_gpu_eval(c, 1, &ci, &li, &u, &tr, nullptr, &ai, IMA_PREC_FAST, result, nullptr);
+}
+
+extern "C" int ima_gpu_get_dlikeA(ima_ctx *c, int ci, int li, int ai, double *dlikeA)
+{
+  if (!c || !dlikeA) return IMA_ERR_ARG;
+  if (!c->valid(ci, li) || c->loci[li].d.model != IMA_MODEL_SW) return c->fail(IMA_ERR_ARG, "locus %d is not stepwise", li);
+  const ItemDev &it = c->items[c->item_of(ci, li)];
+  if (ai < 0 || ai >= c->loci[li].d.nlinked) return c->fail(IMA_ERR_ARG, "bad marker");
+  int nl = 2 * it.n - 1;
+  std::vector<double> raw(nl);
+  int r = c->cuda(cudaMemcpyAsync(raw.data(), c->d_dlike + it.dl_off + (size_t)ai * nl, nl * sizeof(double), cudaMemcpyDeviceToHost, c->st), "dlikeA");
+  r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "dlikeA");
+  if (r) return r;
+  bool ffmt = c->dl_fast[it.al_off + (size_t)ai];
+  for (int k = 0; k < nl; k++) {
+    if (ffmt) {
+      float2 v;
+      memcpy(&v, &raw[k], sizeof(v));
+      dlikeA[k] = std::isinf(v.x) ? -1e100 : (double)v.x + (double)v.y;
+    } else {
+      dlikeA[k] = raw[k];
+    }
+  }
+  return IMA_OK;
+}
+
+// ======================================================================
+// MC3
+extern "C" int ima_gpu_setheat(ima_ctx *c, double h1, double h2, int heatmode)
+{
+  if (!c) return IMA_ERR_ARG;
+  if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
+  if (heatmode < 0 || heatmode > 2) return c->fail(IMA_ERR_ARG, "heatmode must be 0, 1 or 2");
+  const int N = c->cpr;
+  std::vector<double> beta(c->nchains), allb(c->nchains);
+  for (int r = 0; r < c->nruns; r++)
+    for (int i = 0; i < N; i++) {
+      double a, b;
+      if (N == 1) {
+        a = b = 1.0;
+      } else if (heatmode == 0) {
+        a = 1.0 / (1.0 + h1 * i);
+        b = 1.0 / (1.0 + (h1 < 0.05 ? 0.05 : h1) * i);
+      } else if (heatmode == 1) {
+        a = b = 1 - (1 - h2) * (i) * std::pow(h1, (double)(N - 1 - i)) / (double)(N - 1);
+      } else {
+        a = b = 1.0 - i * (1.0 / (N - 1));
+      }
+      if (N > 1 && (b <= 0.0 || b > 1.0))
+        return c->fail(IMA_ERR_ARG, "command line heating terms have caused a heating value out of range. chain %d beta %f", i, b);
+      allb[(size_t)r * N + i] = a;
+      beta[(size_t)r * N + i] = b;
+    }
+  int rr = c->cuda(cudaMemcpyAsync(c->d_beta, beta.data(), beta.size() * 8, cudaMemcpyHostToDevice, c->st), "beta");
+  rr = rr ? rr : c->cuda(cudaMemcpyAsync(c->d_allbetas, allb.data(), allb.size() * 8, cudaMemcpyHostToDevice, c->st), "allbetas");
+  return rr ? rr : c->cuda(cudaStreamSynchronize(c->st), "setheat");
+}
+
+static int copy_dev(ima_ctx *c, void *dst, const void *src, size_t bytes, cudaMemcpyKind k, const char *what)
+{
+  if (!c || !src || !dst) return IMA_ERR_ARG;
+  if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
+  int r = c->cuda(cudaMemcpyAsync(dst, src, bytes, k, c->st), what);
+  return r ? r : c->cuda(cudaStreamSynchronize(c->st), what);
+}
+
+extern "C" int ima_gpu_get_betas(ima_ctx *c, double *beta)
+{
+  return copy_dev(c, beta, c ? c->d_beta : nullptr, c ? c->nchains * 8 : 0, cudaMemcpyDeviceToHost, "betas");
+}
+extern "C" int ima_gpu_set_betas(ima_ctx *c, const double *beta)
+{
+  return copy_dev(c, c ? c->d_beta : nullptr, beta, c ? c->nchains * 8 : 0, cudaMemcpyHostToDevice, "betas");
+}
+extern "C" int ima_gpu_set_pdg(ima_ctx *c, const double *pdg)
+{
+  return copy_dev(c, c ? c->d_pdg : nullptr, pdg, c ? (size_t)c->nitems * 8 : 0, cudaMemcpyHostToDevice, "pdg");
+}
+extern "C" int ima_gpu_get_pdg(ima_ctx *c, double *pdg)
+{
+  return copy_dev(c, pdg, c ? c->d_pdg : nullptr, c ? (size_t)c->nitems * 8 : 0, cudaMemcpyDeviceToHost, "pdg");
+}
+extern "C" int ima_gpu_set_probg(ima_ctx *c, const double *probg)
+{
+  return copy_dev(c, c ? c->d_probg : nullptr, probg, c ? c->nchains * 8 : 0, cudaMemcpyHostToDevice, "probg");
+}
+
+extern "C" int ima_gpu_swapchains(ima_ctx *c, int swaptries, int include_probg, const double *uniforms,
+                                  int stride, uint64_t seed, int32_t *used, int32_t *swap0ok)
+{
+  if (!c) return IMA_ERR_ARG;
+  if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
+  if (swaptries < 0) return c->fail(IMA_ERR_ARG, "swaptries must be >= 0");
+  if (c->cpr < 2) return IMA_OK;  // the reference swaps only when numchains > 1
+  int r = IMA_OK;
+  if (uniforms) {
+    if (stride < 1) return c->fail(IMA_ERR_ARG, "stride must be >= 1");
+    size_t need = (size_t)stride * c->nruns;
+    if (need > c->uni_cap) {
+      cudaStreamSynchronize(c->st);
+      cudaFree(c->d_uni);
+      c->d_uni = dev_alloc<double>(need, c->dev_bytes);
+      if (!c->d_uni) return c->fail(IMA_ERR_NOMEM, "uniform buffer");
+      c->uni_cap = need;
+    }
+    r = c->cuda(cudaMemcpyAsync(c->d_uni, uniforms, need * 8, cudaMemcpyHostToDevice, c->st), "uniforms");
+    if (r) return r;
+  }
+  SwapArgs a;
+  a.nruns = c->nruns;
+  a.cpr = c->cpr;
+  a.nloci = c->nloci;
+  a.swaptries = swaptries;
+  a.include_probg = include_probg;
+  a.stride = stride;
+  a.pdg = c->d_pdg;
+  a.probg = c->d_probg;
+  a.beta = c->d_beta;
+  a.allbetas = c->d_allbetas;
+  a.uniforms = uniforms ? c->d_uni : nullptr;
+  a.seed = seed;
+  a.counter = c->d_ctr;
+  a.used = c->d_used;
+  a.swap0ok = c->d_swap0ok;
+  a.swapcount = c->d_swapcount;
+  a.tempcount = c->d_tempcount;
+  a.S = c->d_S;
+  c->launch(IMA_K_SWAP, (double)c->nitems * 8.0, [&] { launch_swap(a, c->st); });
+  r = c->cuda(cudaGetLastError(), "swap launch");
+  if (r) return r;
+  if (used) r = r ? r : c->cuda(cudaMemcpyAsync(used, c->d_used, c->nruns * 4, cudaMemcpyDeviceToHost, c->st), "used");
+  if (swap0ok) r = r ? r : c->cuda(cudaMemcpyAsync(swap0ok, c->d_swap0ok, c->nruns * 4, cudaMemcpyDeviceToHost, c->st), "swap0ok");
+  if (used || swap0ok || uniforms) r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "swap");
+  if (!r && used)
+    for (int k = 0; k < c->nruns; k++)
+      if (used[k] < 0) return c->fail(IMA_ERR_ARG, "run %d ran out of supplied uniforms", k);
+  return r;
+}
+
+extern "C" int ima_gpu_get_swapcounts(ima_ctx *c, int run, int32_t *swapcount, int32_t *tempcount)
+{
+  if (!c || run < 0 || run >= c->nruns) return IMA_ERR_ARG;
+  size_t nn = (size_t)c->cpr * c->cpr;
+  int r = IMA_OK;
+  if (swapcount) r = c->cuda(cudaMemcpyAsync(swapcount, c->d_swapcount + run * nn, nn * 4, cudaMemcpyDeviceToHost, c->st), "swapcount");
+  if (tempcount) r = r ? r : c->cuda(cudaMemcpyAsync(tempcount, c->d_tempcount + run * nn, nn * 4, cudaMemcpyDeviceToHost, c->st), "tempcount");
+  return r ? r : c->cuda(cudaStreamSynchronize(c->st), "swapcounts");
+}
+
+// ======================================================================
+// surface
+extern "C" int ima_gpu_surface_load(ima_ctx *c, int G, int rowlen, const float *rows, int np, int nm,
+                                    int npops, const double *lognorm)
+{
+  if (!c || !rows) return IMA_ERR_ARG;
+  if (G < 1 || np < 0 || nm < 0 || np + nm < 1 || np + nm > 32 || rowlen < 4 * np + 3 * nm + 2 || rowlen > 64)
+    return c->fail(IMA_ERR_ARG, "bad surface shape (G %d, rowlen %d, %d theta, %d m)", G, rowlen, np, nm);
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->st);
+  cudaFree(c->d_rows);
+  cudaFree(c->d_lognorm);
+  c->d_lognorm = nullptr;
+  c->d_rows = dev_alloc<float>((size_t)G * rowlen, c->dev_bytes);
+  if (!c->d_rows) return c->fail(IMA_ERR_NOMEM, "surface rows");
+  if (lognorm) {
+    c->d_lognorm = dev_alloc<double>(G, c->dev_bytes);
+    if (!c->d_lognorm) return c->fail(IMA_ERR_NOMEM, "surface normalisers");
+  }
+  c->sG = G;
+  c->srowlen = rowlen;
+  c->snp = np;
+  c->snm = nm;
+  c->snpops = npops;
+  int r = c->cuda(cudaMemcpyAsync(c->d_rows, rows, (size_t)G * rowlen * 4, cudaMemcpyHostToDevice, c->st), "rows");
+  if (lognorm) r = r ? r : c->cuda(cudaMemcpyAsync(c->d_lognorm, lognorm, (size_t)G * 8, cudaMemcpyHostToDevice, c->st), "lognorm");
+  return r ? r : c->cuda(cudaStreamSynchronize(c->st), "surface load");
+}
+
+static int surf_points(ima_ctx *c, int npoints)
+{
+  if ((size_t)npoints <= c->spts_cap) return IMA_OK;
+  cudaFree(c->d_sx);
+  cudaFree(c->d_sq);
+  cudaFree(c->d_sess);
+  c->d_sx = dev_alloc<double>((size_t)npoints * 32, c->dev_bytes);
+  c->d_sq = dev_alloc<double>(npoints, c->dev_bytes);
+  c->d_sess = dev_alloc<double>(npoints, c->dev_bytes);
+  if (!c->d_sx || !c->d_sq || !c->d_sess) return c->fail(IMA_ERR_NOMEM, "surface point buffers");
+  c->spts_cap = npoints;
+  return IMA_OK;
+}
+
+static int surf_scratch(ima_ctx *c, size_t bytes)
+{
+  if (bytes <= c->sscratch_cap) return IMA_OK;
+  cudaFree(c->d_sscratch);
+  c->d_sscratch = dev_alloc<char>(bytes, c->dev_bytes);
+  if (!c->d_sscratch) return c->fail(IMA_ERR_NOMEM, "surface scratch (%zu bytes)", bytes);
+  c->sscratch_cap = bytes;
+  return IMA_OK;
+}
+
+extern "C" int ima_gpu_surface_eval(ima_ctx *c, int npoints, const double *x, int modeltype, int method,
+                                    double *q, double *ess)
+{
+  if (!c || !x || !q || npoints < 1) return IMA_ERR_ARG;
+  if (!c->d_rows) return c->fail(IMA_ERR_STATE, "call ima_gpu_surface_load first");
+  if (modeltype < 0 || modeltype > 2) return c->fail(IMA_ERR_ARG, "modeltype must be 0, 1 or 2");
+  const int npar = c->snp + c->snm;
+  for (size_t k = 0; k < (size_t)npoints * npar; k++)
+    if (!(x[k] > 0.0)) return c->fail(IMA_ERR_ARG, "parameter values must be > 0 (point %zu)", k / npar);
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->st);
+  int r = surf_points(c, npoints);
+  if (r) return r;
+  SurfArgs a;
+  a.G = c->sG;
+  a.rowlen = c->srowlen;
+  a.np = c->snp;
+  a.nm = c->snm;
+  a.npops = c->snpops;
+  a.modeltype = modeltype;
+  a.npoints = npoints;
+  a.rows = c->d_rows;
+  a.lognorm = c->d_lognorm;
+  a.x = c->d_sx;
+  a.q = c->d_sq;
+  a.ess = c->d_sess;
+  r = c->cuda(cudaMemcpyAsync(c->d_sx, x, (size_t)npoints * npar * 8, cudaMemcpyHostToDevice, c->st), "points");
+  if (r) return r;
+  if (method == IMA_SURF_FAST) {
+    r = surf_scratch(c, surface_fast_scratch_bytes(a.G, npoints));
+    if (r) return r;
+    int lr = 0;
+    c->launch(IMA_K_SURF_FAST, (double)a.G * 27 * 4 + (double)npoints * 27 * 8,
+              [&] { lr = launch_surface_fast(a, c->d_sscratch, c->sscratch_cap, c->st); });
+    if (lr) return c->fail(IMA_ERR_ARG, "fast surface: unsupported shape (%d)", lr);
+  } else if (method == IMA_SURF_FP64) {
+    r = surf_scratch(c, surface_fp64_scratch_bytes(a.G, npoints));
+    if (r) return r;
+    c->launch(IMA_K_SURF_FP64, (double)a.G * a.rowlen * 4, [&] { launch_surface_fp64(a, (double *)c->d_sscratch, c->st); });
+  } else if (method == IMA_SURF_COMPAT) {
+    r = surf_scratch(c, surface_fp64_scratch_bytes(a.G, npoints));
+    if (r) return r;
+    c->launch(IMA_K_SURF_COMPAT, (double)a.G * a.rowlen * 4, [&] { launch_surface_compat(a, (double *)c->d_sscratch, c->st); });
+  } else {
+    return c->fail(IMA_ERR_ARG, "unknown surface method %d", method);
+  }
+  r = c->cuda(cudaGetLastError(), "surface launch");
+  r = r ? r : c->cuda(cudaMemcpyAsync(q, c->d_sq, npoints * 8, cudaMemcpyDeviceToHost, c->st), "q");
+  if (ess) r = r ? r : c->cuda(cudaMemcpyAsync(ess, c->d_sess, npoints * 8, cudaMemcpyDeviceToHost, c->st), "ess");
+  return r ? r : c->cuda(cudaStreamSynchronize(c->st), "surface");
+}
+
+extern "C" int ima_gpu_jointp(ima_ctx *c, const double *x, int calc_ess, double *effective_n, double *q)
+{
+  if (!c || !x || !q) return IMA_ERR_ARG;
+  double e = 0.0;
+  int r = ima_gpu_surface_eval(c, 1, x, 0, IMA_SURF_COMPAT, q, &e);
+  if (!r && calc_ess && effective_n) *effective_n = e;
+  return r;
+}
+
+// ======================================================================
+// measurement
+extern "C" int ima_gpu_timer_begin(ima_ctx *c)
+{
+  if (!c) return IMA_ERR_ARG;
+  return c->cuda(cudaEventRecord(c->t0, c->st), "timer");
+}
+
+extern "C" int ima_gpu_timer_end(ima_ctx *c, float *ms)
+{
+  if (!c || !ms) return IMA_ERR_ARG;
+  int r = c->cuda(cudaEventRecord(c->t1, c->st), "timer");
+  r = r ? r : c->cuda(cudaEventSynchronize(c->t1), "timer");
+  return r ? r : c->cuda(cudaEventElapsedTime(ms, c->t0, c->t1), "timer");
+}
+
+extern "C" int ima_gpu_set_profiling(ima_ctx *c, int on)
+{
+  if (!c) return IMA_ERR_ARG;
+  c->resolve_timings();
+  c->profiling = on != 0;
+  return IMA_OK;
+}
+
+extern "C" int ima_gpu_kernel_stats(ima_ctx *c, int kind, long long *launches, double *ms_total,
+                                    double *bytes_total)
+{
+  if (!c || kind < 0 || kind >= IMA_K_COUNT) return IMA_ERR_ARG;
+  c->resolve_timings();
+  if (launches) *launches = c->k_launches[kind];
+  if (ms_total) *ms_total = c->k_ms[kind];
+  if (bytes_total) *bytes_total = c->k_bytes[kind];
+  return IMA_OK;
+}
+
+extern "C" int ima_gpu_launch_count(ima_ctx *c, long long *n)
+{
+  if (!c || !n) return IMA_ERR_ARG;
+  *n = c->launches;
+  return IMA_OK;
+}
+
+extern "C" int ima_gpu_flush_l2(ima_ctx *c)
+{
+  if (!c) return IMA_ERR_ARG;
+  if (!c->d_flush) {
+    c->flush_bytes = (size_t)512 << 20;
+    if (cudaMalloc(&c->d_flush, c->flush_bytes) != cudaSuccess) {
+      c->d_flush = nullptr;
+      return c->fail(IMA_ERR_NOMEM, "L2 flush buffer");
+    }
+    c->dev_bytes += c->flush_bytes;
+  }
+  return c->cuda(cudaMemsetAsync(c->d_flush, c->launches & 0xff, c->flush_bytes, c->st), "flush");
+}
+
+extern "C" int ima_gpu_memory(ima_ctx *c, size_t *bytes)
+{
+  if (!c || !bytes) return IMA_ERR_ARG;
+  *bytes = c->dev_bytes;
+  return IMA_OK;
+}

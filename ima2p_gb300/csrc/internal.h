@@ -1,0 +1,119 @@
+// internal.h -- device data layout and launch interfaces shared by the
+// context (ima_ctx.cu) and the kernels (k_*.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "../../include/ima_gpu.h"
+
+// One genealogy node: the reference's struct edge (imamp.hpp:651-679) reduced
+// to its topology, packed into 8 bytes so a node is one load.
+struct NodeRec {
+  int16_t up0, up1, down, pad;
+};
+
+// Locus table entry (shared by every chain).
+struct LocusDev {
+  int model;      // IMA_MODEL_*
+  int n;          // gene copies (tips)
+  int nsites;     // IS segregating sites / HKY patterns
+  int totsites;   // HKY: columns before pattern compression
+  int nlinked;    // SW: linked markers
+  int seq_off;    // int8 [n][nsites] in the seq pool
+  int mult_off;   // int32 [nsites] in the mult pool
+  int pad;
+};
+
+// Static placement of one chain-locus in the resident pools.
+struct ItemDev {
+  int locus;
+  int n;
+  int node_off;            // nodes / times / slot / fresh pools
+  int sched_off;           // int16 [2n] level schedule
+  long long part_off;      // HKY: float4 index of slot 0 (slot 1 at + (n-1)*S)
+  long long part64_off;    // HKY FP64: double index (x4 per pattern) of slot 0
+  int al_off;              // SW: int32 [nlinked][2n-1] alleles
+  int dl_off;              // SW: double [nlinked][2n-1] dlikeA
+};
+
+// One evaluation request (a chain-locus with its parameters).
+struct ReqDev {
+  int item;
+  int ai;
+  int e[4];
+  double u;
+  double par;  // HKY: kappa; SW: branch-time scale tr
+};
+
+// Everything a kernel may read; passed by value.
+struct Pools {
+  const LocusDev *loci;
+  const ItemDev *items;
+  const int8_t *seq;
+  const int32_t *mult;
+  const NodeRec *nodes;
+  const double *t64;        // FP64 node times
+  const float2 *tff;        // float-float node times (hi, lo)
+  const int16_t *sched;     // per item: order[n-1] then level starts[nlev+1]
+  const int32_t *nlev;      // levels per item
+  const double *length;     // genealogy length per item (from treeweight)
+  const double *pi;         // [item][4]
+  const int32_t *alleles;
+  double *dlike;            // SW per-branch terms
+  double *sumlogk;          // IS per-locus constant
+  double *pdg_new;          // last evaluated log P(D|G) per item
+  // HKY state
+  float4 *part;             // FP32 partials
+  int32_t *pexp;            // FP32 partial power-of-two exponents
+  double *part64;           // FP64 partials (4 per pattern)
+  double *psf64;            // FP64 log scale factors
+  uint8_t *slot32, *fresh32, *slot64, *fresh64;
+};
+
+// Launch wrappers (k_*.cu).  All launch on `st`.
+void launch_is_sumlogk(const Pools &P, int item, int locus, int maxn, int maxS, int *d_flag,
+                       cudaStream_t st);
+void launch_is(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int maxS, double *result,
+               int32_t *status, int32_t *site_node, cudaStream_t st);
+void launch_hky_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, double *result,
+                     int32_t *status, cudaStream_t st);
+void launch_hky_fp64(const Pools &P, const ReqDev *reqs, int nreq, int maxn, double *result,
+                     int32_t *status, cudaStream_t st);
+void launch_hky_commit(const Pools &P, const int32_t *items, const uint8_t *accept, int n,
+                       cudaStream_t st);
+void launch_sw_fast(const Pools &P, const ReqDev *reqs, int nreq, double *result,
+                    int32_t *status, cudaStream_t st);
+void launch_sw_fp64(const Pools &P, const ReqDev *reqs, int nreq, double *result,
+                    int32_t *status, cudaStream_t st);
+
+// MC3
+struct SwapArgs {
+  int nruns, cpr, nloci, swaptries, include_probg, stride;
+  const double *pdg;        // [nchains][nloci]
+  const double *probg;      // [nchains]
+  double *beta;             // [nchains]
+  const double *allbetas;   // [nchains]
+  const double *uniforms;   // [nruns][stride] or null
+  unsigned long long seed;
+  unsigned long long *counter;  // per-run Philox counters
+  int32_t *used, *swap0ok;
+  int32_t *swapcount, *tempcount;  // [nruns][cpr][cpr]
+  double *S;                       // scratch [nchains]
+};
+void launch_swap(const SwapArgs &a, cudaStream_t st);
+void launch_pdg_commit(const int32_t *items, const uint8_t *accept, const double *pdg_new,
+                       double *pdg, int n, cudaStream_t st);
+
+// Surface
+struct SurfArgs {
+  int G, rowlen, np, nm, npops, modeltype, npoints;
+  const float *rows;        // [G][rowlen]
+  const double *lognorm;    // [G] or null
+  const double *x;          // [npoints][np+nm]
+  double *q, *ess;
+};
+void launch_surface_fp64(const SurfArgs &a, double *scratch, cudaStream_t st);
+void launch_surface_compat(const SurfArgs &a, double *scratch, cudaStream_t st);
+int launch_surface_fast(const SurfArgs &a, void *scratch, size_t scratch_bytes, cudaStream_t st);
+size_t surface_fast_scratch_bytes(int G, int npoints);
+size_t surface_fp64_scratch_bytes(int G, int npoints);

@@ -1,0 +1,436 @@
+// k_hky.cu -- HKY85 Felsenstein pruning over site patterns (makefrac,
+// calc_prob_data.cpp:118-471; likelihoodHKY :583-607) and the accept/reject of
+// its partial likelihoods (copyfraclike / storescalefactors /
+// restorescalefactors, update_gtree_common.cpp:2140-2181).
+//
+// One CTA per chain-locus.  Internal nodes are visited level by level (the
+// host supplies, with each genealogy, its internal nodes sorted by height);
+// inside a level every (node, pattern) pair is independent, so the CTA's
+// threads sweep them with one barrier per level.  A node is recomputed when
+// it is on the dirty list, when the list is -1 (full), or when a daughter is
+// dirty or recomputed -- the reference's propagation rule (:137-163).
+//
+// Partial likelihoods are resident state in two slots per node: slot[node]
+// names the committed one ("frac"), the other receives new values
+// ("newfrac").  Accept flips the slot of every recomputed node, reject keeps
+// it; this replaces the reference's buffer copies with a one-byte flip.
+//
+// FP32 form: partials are float4, rescaled after every node by an exact
+// power of two whose exponent is kept as an integer, so the log scale factor
+// carries no rounding; the root sum log(sum_j pi_j L_j) is formed from an
+// FP32 mantissa log and the integer exponent, accumulated in FP64.
+// FP64 form: the reference's arithmetic -- partials divided by their maximum,
+// log(max) accumulated into an FP64 scale factor.
+#include "internal.h"
+
+namespace {
+
+constexpr int HKY_BS = 128;
+constexpr double LN2 = 0.69314718055994530941723212146;
+
+__device__ __forceinline__ float branch_ff(const NodeRec *nd, const float2 *t, int c)
+{
+  int u = nd[c].up0;
+  if (u < 0) return t[c].x + t[c].y;
+  return (t[c].x - t[u].x) + (t[c].y - t[u].y);
+}
+
+__device__ __forceinline__ double branch_64(const NodeRec *nd, const double *t, int c)
+{
+  int u = nd[c].up0;
+  return (u < 0) ? t[c] : t[c] - t[u];
+}
+
+// HKY85 transition matrix P[j][k] = P(j -> k | b), Pi and A from the class
+// (purine / pyrimidine) of the target state k.
+template <typename T>
+__device__ __forceinline__ void hky_p(const T *pi, T kpa, T b, T *P)
+{
+  T e1 = exp(-b);
+  T PR = pi[0] + pi[2], PY = pi[1] + pi[3];
+  T eR = exp(-b * (T(1) + PR * kpa)), eY = exp(-b * (T(1) + PY * kpa));
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    T Pk = (k == 0 || k == 2) ? PR : PY;
+    T e2 = (k == 0 || k == 2) ? eR : eY;
+    T base = pi[k] + pi[k] * e1 * (T(1) / Pk - T(1));
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      T v;
+      if (j == k) v = base + e2 * ((Pk - pi[k]) / Pk);
+      else if (j + k == 2 || j + k == 4) v = base - (pi[k] / Pk) * e2;
+      else v = pi[k] * (T(1) - e1);
+      P[j * 4 + k] = v;
+    }
+  }
+}
+
+// Shared-memory carve-up, identical on host (sizing) and device.
+struct HkyLayout {
+  size_t nd, fresh, order, total;
+};
+__host__ __device__ inline HkyLayout hky_layout(int maxnl, size_t elem)
+{
+  HkyLayout l;
+  l.nd = elem * 16 * (size_t)maxnl;
+  l.fresh = l.nd + sizeof(NodeRec) * (size_t)maxnl;
+  l.order = (l.fresh + 3 * (size_t)maxnl + 15) & ~size_t(15);
+  l.total = (l.order + sizeof(int16_t) * (size_t)(maxnl + 3) + 15) & ~size_t(15);
+  return l;
+}
+
+// Per-CTA shared state common to both precisions.
+struct Tree {
+  NodeRec *nd;
+  uint8_t *fresh;
+  uint8_t *dirty;
+  uint8_t *slot;
+  int16_t *order;
+  int16_t *lstart;
+};
+
+__device__ double standfactor(const double *pi, double kappa)
+{
+  double p = 0.0;
+  for (int i = 0; i < 4; i++)
+    for (int j = 0; j < 4; j++) {
+      if (i == j) continue;
+      p += (i + j == 2 || i + j == 4) ? pi[i] * pi[j] * kappa : pi[i] * pi[j];
+    }
+  return p;
+}
+
+// Loads topology and schedule, marks dirty nodes and decides which internal
+// nodes are recomputed.  Returns after a barrier.
+__device__ void load_tree(const Pools &P, const ItemDev &it, const ReqDev &R, int nlev, Tree &T,
+                          const uint8_t *gslot)
+{
+  const int n = it.n, nl = 2 * n - 1;
+  for (int k = threadIdx.x; k < nl; k += blockDim.x) {
+    T.nd[k] = P.nodes[it.node_off + k];
+    T.dirty[k] = 0;
+    T.slot[k] = gslot[it.node_off + k];
+  }
+  for (int k = threadIdx.x; k < n - 1 + nlev + 1; k += blockDim.x)
+    T.order[k] = P.sched[it.sched_off + k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    bool full = (R.e[0] == -1);
+    for (int q = 0; q < 4; q++)
+      if (R.e[q] >= 0 && R.e[q] < nl) T.dirty[R.e[q]] = 1;
+    for (int k = 0; k < n - 1; k++) {
+      int node = T.order[k];
+      int a = T.nd[node].up0, b = T.nd[node].up1;
+      bool f = full || T.dirty[node] || T.dirty[a] || T.dirty[b] ||
+               (a >= n && T.fresh[a]) || (b >= n && T.fresh[b]);
+      T.fresh[node] = f ? 1 : 0;
+    }
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ float pow2f(int k)  // 2^k for -126 <= k <= 127
+{
+  return __int_as_float((127 + k) << 23);
+}
+
+__device__ __forceinline__ int expo_of(float m)  // floor(log2(m)) for normal m > 0
+{
+  return ((__float_as_int(m) >> 23) & 0xff) - 127;
+}
+
+// ------------------------------------------------------------------ FP32
+__global__ void __launch_bounds__(HKY_BS) k_hky_fast(Pools P, const ReqDev *reqs,
+                                                     double *result, int32_t *status, int maxnl)
+{
+  extern __shared__ __align__(16) char smem[];
+  const ReqDev R = reqs[blockIdx.x];
+  const ItemDev it = P.items[R.item];
+  const LocusDev L = P.loci[it.locus];
+  const int n = it.n, nl = 2 * n - 1, S = L.nsites, nint = n - 1;
+  const int nlev = P.nlev[R.item];
+  const HkyLayout lay = hky_layout(maxnl, sizeof(float));
+  float *Pm = reinterpret_cast<float *>(smem);               // [maxnl][16]
+  Tree T;
+  T.nd = reinterpret_cast<NodeRec *>(smem + lay.nd);
+  T.fresh = reinterpret_cast<uint8_t *>(smem + lay.fresh);
+  T.dirty = T.fresh + maxnl;
+  T.slot = T.dirty + maxnl;
+  T.order = reinterpret_cast<int16_t *>(smem + lay.order);
+  __shared__ double red_d[HKY_BS / 32];
+  __shared__ long long red_e[HKY_BS / 32];
+  __shared__ float spi[4];
+  __shared__ float smu;
+
+  load_tree(P, it, R, nlev, T, P.slot32);
+  T.lstart = T.order + nint;
+  if (threadIdx.x == 0) {
+    const double *pid = P.pi + 4 * (size_t)R.item;
+    double mu = R.u / ((double)L.totsites * standfactor(pid, R.par));
+    smu = (float)mu;
+    for (int j = 0; j < 4; j++) spi[j] = (float)pid[j];
+  }
+  __syncthreads();
+  // transition matrices of every branch that feeds a recomputed node
+  const float2 *tff = P.tff + it.node_off;
+  float kpa = (float)(R.par - 1.0);
+  for (int c = threadIdx.x; c < nl; c += blockDim.x) {
+    int d = T.nd[c].down;
+    if (d < 0 || !T.fresh[d]) continue;
+    float pil[4] = {spi[0], spi[1], spi[2], spi[3]};
+    hky_p<float>(pil, kpa, smu * branch_ff(T.nd, tff, c), Pm + 16 * c);
+  }
+  __syncthreads();
+
+  const size_t slot_stride = (size_t)nint * S;
+  float4 *part = P.part + it.part_off;
+  int32_t *pexp = P.pexp + it.part_off;
+  const int8_t *seq = P.seq + L.seq_off;
+  for (int lv = 0; lv < nlev; lv++) {
+    int beg = T.lstart[lv], cnt = T.lstart[lv + 1] - beg;
+    for (int w = threadIdx.x; w < cnt * S; w += blockDim.x) {
+      int node = T.order[beg + w / S];
+      int i = w - (w / S) * S;
+      if (!T.fresh[node]) continue;
+      float v[2][4];
+      int e = 0;
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        int c = h ? T.nd[node].up1 : T.nd[node].up0;
+        const float *Pc = Pm + 16 * c;
+        if (c < n) {
+          int s = seq[(size_t)c * S + i];
+#pragma unroll
+          for (int j = 0; j < 4; j++) v[h][j] = Pc[j * 4 + s];
+        } else {
+          int rs = T.fresh[c] ? 1 - T.slot[c] : T.slot[c];
+          size_t idx = rs * slot_stride + (size_t)(c - n) * S + i;
+          float4 Lc = part[idx];
+          e += pexp[idx];
+#pragma unroll
+          for (int j = 0; j < 4; j++)
+            v[h][j] = Pc[j * 4 + 0] * Lc.x + Pc[j * 4 + 1] * Lc.y + Pc[j * 4 + 2] * Lc.z +
+                      Pc[j * 4 + 3] * Lc.w;
+        }
+      }
+      float o0 = v[0][0] * v[1][0], o1 = v[0][1] * v[1][1];
+      float o2 = v[0][2] * v[1][2], o3 = v[0][3] * v[1][3];
+      float m = fmaxf(fmaxf(o0, o1), fmaxf(o2, o3));
+      if (m < 1e-30f) {  // keep the exponent extraction in the normal range
+        o0 *= 1.8446744e19f; o1 *= 1.8446744e19f; o2 *= 1.8446744e19f; o3 *= 1.8446744e19f;
+        m *= 1.8446744e19f;
+        e -= 64;
+      }
+      int k = expo_of(m);
+      float sc = pow2f(-k);
+      size_t widx = (1 - T.slot[node]) * slot_stride + (size_t)(node - n) * S + i;
+      part[widx] = make_float4(o0 * sc, o1 * sc, o2 * sc, o3 * sc);
+      pexp[widx] = e + k;
+    }
+    __syncthreads();
+  }
+
+  // root: sum_i mult_i * (log(sum_j pi_j L_j) + scale_i)
+  int root = T.order[nint - 1];
+  int rs = T.fresh[root] ? 1 - T.slot[root] : T.slot[root];
+  const int32_t *mult = P.mult + L.mult_off;
+  double acc = 0.0;
+  long long acce = 0;
+  for (int i = threadIdx.x; i < S; i += blockDim.x) {
+    size_t idx = rs * slot_stride + (size_t)(root - n) * S + i;
+    float4 Lr = part[idx];
+    float f = spi[0] * Lr.x + spi[1] * Lr.y + spi[2] * Lr.z + spi[3] * Lr.w;
+    int k = expo_of(f);
+    float mant = f * pow2f(-k);
+    int mlt = mult[i];
+    acc += (double)mlt * (double)logf(mant);
+    acce += (long long)mlt * (long long)(pexp[idx] + k);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    acce += __shfl_xor_sync(0xffffffffu, acce, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red_d[threadIdx.x >> 5] = acc;
+    red_e[threadIdx.x >> 5] = acce;
+  }
+  // recomputed flags for the commit step
+  for (int k = threadIdx.x; k < nl; k += blockDim.x)
+    P.fresh32[it.node_off + k] = (k >= n) ? T.fresh[k] : 0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    long long se = 0;
+    for (int w = 0; w < HKY_BS / 32; w++) { s += red_d[w]; se += red_e[w]; }
+    result[blockIdx.x] = s + (double)se * LN2;
+    P.pdg_new[R.item] = result[blockIdx.x];
+    status[blockIdx.x] = IMA_EVAL_OK;
+  }
+}
+
+// ------------------------------------------------------------------ FP64
+__global__ void __launch_bounds__(HKY_BS) k_hky_fp64(Pools P, const ReqDev *reqs,
+                                                     double *result, int32_t *status, int maxnl)
+{
+  extern __shared__ __align__(16) char smem[];
+  const ReqDev R = reqs[blockIdx.x];
+  const ItemDev it = P.items[R.item];
+  const LocusDev L = P.loci[it.locus];
+  const int n = it.n, nl = 2 * n - 1, S = L.nsites, nint = n - 1;
+  const int nlev = P.nlev[R.item];
+  const HkyLayout lay = hky_layout(maxnl, sizeof(double));
+  double *Pm = reinterpret_cast<double *>(smem);  // [maxnl][16]
+  Tree T;
+  T.nd = reinterpret_cast<NodeRec *>(smem + lay.nd);
+  T.fresh = reinterpret_cast<uint8_t *>(smem + lay.fresh);
+  T.dirty = T.fresh + maxnl;
+  T.slot = T.dirty + maxnl;
+  T.order = reinterpret_cast<int16_t *>(smem + lay.order);
+  __shared__ double red_d[HKY_BS / 32];
+  __shared__ double spi[4];
+  __shared__ double smu;
+
+  load_tree(P, it, R, nlev, T, P.slot64);
+  T.lstart = T.order + nint;
+  if (threadIdx.x == 0) {
+    const double *pid = P.pi + 4 * (size_t)R.item;
+    smu = R.u / ((double)L.totsites * standfactor(pid, R.par));
+    for (int j = 0; j < 4; j++) spi[j] = pid[j];
+  }
+  __syncthreads();
+  const double *t64 = P.t64 + it.node_off;
+  double kpa = R.par - 1.0;
+  for (int c = threadIdx.x; c < nl; c += blockDim.x) {
+    int d = T.nd[c].down;
+    if (d < 0 || !T.fresh[d]) continue;
+    double pil[4] = {spi[0], spi[1], spi[2], spi[3]};
+    hky_p<double>(pil, kpa, smu * branch_64(T.nd, t64, c), Pm + 16 * c);
+  }
+  __syncthreads();
+
+  const size_t slot_stride = (size_t)nint * S;
+  double *part = P.part64 + it.part64_off * 4;
+  double *psf = P.psf64 + it.part64_off;
+  const int8_t *seq = P.seq + L.seq_off;
+  for (int lv = 0; lv < nlev; lv++) {
+    int beg = T.lstart[lv], cnt = T.lstart[lv + 1] - beg;
+    for (int w = threadIdx.x; w < cnt * S; w += blockDim.x) {
+      int node = T.order[beg + w / S];
+      int i = w - (w / S) * S;
+      if (!T.fresh[node]) continue;
+      double v[2][4];
+      double sf = 0.0;
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        int c = h ? T.nd[node].up1 : T.nd[node].up0;
+        const double *Pc = Pm + 16 * c;
+        if (c < n) {
+          int s = seq[(size_t)c * S + i];
+#pragma unroll
+          for (int j = 0; j < 4; j++) v[h][j] = Pc[j * 4 + s];
+        } else {
+          int rs = T.fresh[c] ? 1 - T.slot[c] : T.slot[c];
+          size_t idx = rs * slot_stride + (size_t)(c - n) * S + i;
+          const double2 *Lp = reinterpret_cast<const double2 *>(part + 4 * idx);
+          double2 a = Lp[0], b = Lp[1];
+          sf += psf[idx];
+#pragma unroll
+          for (int j = 0; j < 4; j++)
+            v[h][j] = Pc[j * 4 + 0] * a.x + Pc[j * 4 + 1] * a.y + Pc[j * 4 + 2] * b.x +
+                      Pc[j * 4 + 3] * b.y;
+        }
+      }
+      double o[4];
+      double m = 0.0;
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        o[j] = v[0][j] * v[1][j];
+        if (o[j] > m) m = o[j];
+      }
+      size_t widx = (1 - T.slot[node]) * slot_stride + (size_t)(node - n) * S + i;
+      double2 *W = reinterpret_cast<double2 *>(part + 4 * widx);
+      W[0] = make_double2(o[0] / m, o[1] / m);
+      W[1] = make_double2(o[2] / m, o[3] / m);
+      psf[widx] = sf + log(m);
+    }
+    __syncthreads();
+  }
+
+  int root = T.order[nint - 1];
+  int rs = T.fresh[root] ? 1 - T.slot[root] : T.slot[root];
+  const int32_t *mult = P.mult + L.mult_off;
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < S; i += blockDim.x) {
+    size_t idx = rs * slot_stride + (size_t)(root - n) * S + i;
+    const double2 *Lp = reinterpret_cast<const double2 *>(part + 4 * idx);
+    double2 a = Lp[0], b = Lp[1];
+    double f = spi[0] * a.x + spi[1] * a.y + spi[2] * b.x + spi[3] * b.y;
+    acc += mult[i] * (log(f) + psf[idx]);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red_d[threadIdx.x >> 5] = acc;
+  for (int k = threadIdx.x; k < nl; k += blockDim.x)
+    P.fresh64[it.node_off + k] = (k >= n) ? T.fresh[k] : 0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < HKY_BS / 32; w++) s += red_d[w];
+    result[blockIdx.x] = s;
+    P.pdg_new[R.item] = s;
+    status[blockIdx.x] = IMA_EVAL_OK;
+  }
+}
+
+// accept: recomputed nodes' new slot becomes the committed one; reject: the
+// committed slot stays.  Either way the recomputed marks are cleared, so a
+// repeated accept is a no-op as the reference's repeated copy is.
+__global__ void k_hky_commit(Pools P, const int32_t *items, const uint8_t *accept)
+{
+  const ItemDev it = P.items[items[blockIdx.x]];
+  const bool acc = accept[blockIdx.x] != 0;
+  const int nl = 2 * it.n - 1;
+  for (int k = threadIdx.x; k < nl; k += blockDim.x) {
+    size_t g = (size_t)it.node_off + k;
+    if (P.fresh32[g]) {
+      if (acc) P.slot32[g] ^= 1;
+      P.fresh32[g] = 0;
+    }
+    if (P.slot64 && P.fresh64[g]) {
+      if (acc) P.slot64[g] ^= 1;
+      P.fresh64[g] = 0;
+    }
+  }
+}
+
+size_t hky_smem(int maxn, size_t elem) { return hky_layout(2 * maxn - 1, elem).total; }
+
+}  // namespace
+
+void launch_hky_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, double *result,
+                     int32_t *status, cudaStream_t st)
+{
+  if (nreq <= 0) return;
+  size_t sm = hky_smem(maxn, sizeof(float));
+  if (sm > 48 * 1024)
+    cudaFuncSetAttribute(k_hky_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_hky_fast<<<nreq, HKY_BS, sm, st>>>(P, reqs, result, status, 2 * maxn - 1);
+}
+
+void launch_hky_fp64(const Pools &P, const ReqDev *reqs, int nreq, int maxn, double *result,
+                     int32_t *status, cudaStream_t st)
+{
+  if (nreq <= 0) return;
+  size_t sm = hky_smem(maxn, sizeof(double));
+  if (sm > 48 * 1024)
+    cudaFuncSetAttribute(k_hky_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_hky_fp64<<<nreq, HKY_BS, sm, st>>>(P, reqs, result, status, 2 * maxn - 1);
+}
+
+void launch_hky_commit(const Pools &P, const int32_t *items, const uint8_t *accept, int n,
+                       cudaStream_t st)
+{
+  if (n <= 0) return;
+  k_hky_commit<<<n, 128, 0, st>>>(P, items, accept);
+}

@@ -1,0 +1,164 @@
+"""Seeded synthetic workloads with the shapes of the benchmark configurations.
+
+  is       2 populations, 5 IS loci x (10+10) copies, 4 geometric chains
+  hky      2 populations, 50 HKY loci x (20+20) x 1000 bp, 32 chains
+  sw       3 sampled populations (5-population tree), 100 SW loci x 30 copies
+           per population, 64 chains
+  mixed    300 loci (200 HKY of U(200,3000) bp, 100 SW), U(4,60) copies per
+           population x 3 populations, 128 chains x 8 runs
+  surface  G = 2^21 genealogy summaries, K = 48 row width, P = 2^16 points
+
+Every chain gets its own genealogy per locus: independent coalescent draws
+for the smaller configurations, time-rescaled copies of a per-locus draw
+(with perturbed internal microsatellite states) for the large ones.  Data
+and parameters follow the distributions the configurations name.
+"""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+
+from . import synth
+
+
+@dataclasses.dataclass
+class Workload:
+    name: str
+    describe: str
+    loci: list            # ("is", seq) | ("hky", HKYLocus) | ("sw", n, 1)
+    nruns: int
+    cpr: int
+    trees: dict            # (ci, li) -> Genealogy
+    u: np.ndarray          # [nchains, nloci]
+    par: np.ndarray        # [nchains, nloci] kappa (HKY) / tr (SW) / unused
+    pi: dict               # (ci, li) -> base frequencies
+    alleles: dict          # (ci, li) -> int32 [2n-1]
+
+    @property
+    def nchains(self):
+        return self.nruns * self.cpr
+
+    @property
+    def nloci(self):
+        return len(self.loci)
+
+    def pairs(self):
+        ci = np.repeat(np.arange(self.nchains), self.nloci).astype(np.int32)
+        li = np.tile(np.arange(self.nloci), self.nchains).astype(np.int32)
+        return ci, li
+
+    def packed(self):
+        """Node arrays of every chain-locus concatenated in pair order."""
+        ci, li = self.pairs()
+        gs = [self.trees[(int(c), int(l))] for c, l in zip(ci, li)]
+        cat = lambda f: np.concatenate([getattr(g, f) for g in gs])
+        return ci, li, cat("up0").astype(np.int32), cat("up1").astype(np.int32), \
+            cat("down").astype(np.int32), cat("time")
+
+    def upload(self, ctx):
+        ci, li, up0, up1, down, time = self.packed()
+        ctx.set_genealogies(ci, li, up0, up1, down, time)
+        for (c, l), p in self.pi.items():
+            ctx.set_pi(c, l, p)
+        for (c, l), A in self.alleles.items():
+            ctx.set_alleles(c, l, A)
+
+
+def _loci_u(rng, nloci):
+    u = rng.lognormal(0.0, 0.5, nloci)
+    return u / np.exp(np.mean(np.log(u)))  # product of the scalars = 1
+
+
+def make_is(seed=1001):
+    rng = np.random.default_rng(seed)
+    nloci, nch = 5, 4
+    loci, trees = [], {}
+    u = np.tile(_loci_u(rng, nloci), (nch, 1))
+    for li in range(nloci):
+        g0 = synth.two_pop_tree(rng, 10, 10, theta=5.0, mig=0.1, tsplit=1.0)
+        loci.append(("is", synth.is_data(rng, g0, u[0, li] * 1.0, min_sites=3)))
+        for ci in range(nch):
+            trees[(ci, li)] = g0 if ci == 0 else synth.jitter_times(rng, g0, 0.1)
+    return Workload("is", "config1-is: 2 pops, 5 IS loci x (10+10) copies, 500 bp, 4 chains",
+                    loci, 1, nch, trees, u, np.ones((nch, nloci)), {}, {})
+
+
+def make_hky(seed=1002, nloci=50, nch=32, ncopies=20, nbases=1000):
+    rng = np.random.default_rng(seed)
+    loci, trees, pis = [], {}, {}
+    ul = _loci_u(rng, nloci)
+    kap = rng.uniform(2.0, 8.0, nloci)
+    for li in range(nloci):
+        g0 = synth.two_pop_tree(rng, ncopies, ncopies, theta=10.0, mig=0.2, tsplit=1.5)
+        loc = synth.hky_data(rng, g0, nbases, float(ul[li]), float(kap[li]), rng.dirichlet([5, 5, 5, 5]))
+        loci.append(("hky", loc))
+        for ci in range(nch):
+            trees[(ci, li)] = g0 if ci == 0 else synth.two_pop_tree(rng, ncopies, ncopies, 10.0, 0.2, 1.5)
+            pis[(ci, li)] = loc.pi
+    return Workload("hky", "config2-hky-fp32: 2 pops, %d HKY loci x (%d+%d) x %d bp, %d chains, "
+                           "full re-evaluation of every chain-locus per step" % (nloci, ncopies, ncopies, nbases, nch),
+                    loci, 1, nch, trees, np.tile(ul, (nch, 1)), np.tile(kap, (nch, 1)), pis, {})
+
+
+def _perturb_alleles(rng, g, A, n):
+    B = A.copy()
+    internal = np.arange(n, 2 * n - 1)
+    flip = rng.uniform(size=len(internal)) < 0.2
+    B[internal[flip]] += rng.choice([-1, 1], size=int(flip.sum()))
+    return np.maximum(B, 4).astype(np.int32)
+
+
+def make_sw(seed=1003, nloci=100, nch=64, per_pop=30):
+    rng = np.random.default_rng(seed)
+    loci, trees, alleles = [], {}, {}
+    ul = _loci_u(rng, nloci)
+    n = 3 * per_pop
+    for li in range(nloci):
+        g0 = synth.three_pop_tree(rng, [per_pop] * 3, theta=4.0, mig=0.05)
+        A0 = synth.sw_alleles(rng, g0, float(ul[li]))
+        loci.append(("sw", n, 1))
+        for ci in range(nch):
+            trees[(ci, li)] = g0 if ci == 0 else synth.jitter_times(rng, g0, 0.15)
+            alleles[(ci, li)] = A0 if ci == 0 else _perturb_alleles(rng, g0, A0, n)
+    return Workload("sw", "config3-sw: 3 sampled pops (5-pop tree), %d SW loci x %d copies, %d chains, "
+                          "full evaluation of every chain-locus per step" % (nloci, n, nch),
+                    loci, 1, nch, trees, np.tile(ul, (nch, 1)), np.ones((nch, nloci)), {}, alleles)
+
+
+def make_mixed(seed=1004, n_hky=200, n_sw=100, nruns=8, cpr=128):
+    rng = np.random.default_rng(seed)
+    loci, base, pis, alleles = [], [], {}, {}
+    nloci = n_hky + n_sw
+    ul = _loci_u(rng, nloci)
+    kap = rng.uniform(2.0, 8.0, nloci)
+    for li in range(nloci):
+        samples = [int(v) for v in rng.integers(4, 61, 3)]
+        g0 = synth.three_pop_tree(rng, samples, theta=10.0 if li < n_hky else 4.0, mig=0.05)
+        base.append(g0)
+        if li < n_hky:
+            loc = synth.hky_data(rng, g0, int(rng.integers(200, 3001)), float(ul[li]), float(kap[li]),
+                                 rng.dirichlet([5, 5, 5, 5]))
+            loci.append(("hky", loc))
+        else:
+            loci.append(("sw", g0.n, 1))
+            base[-1] = (g0, synth.sw_alleles(rng, g0, float(ul[li])))
+    nch = nruns * cpr
+    trees = {}
+    for ci in range(nch):
+        for li in range(nloci):
+            if li < n_hky:
+                trees[(ci, li)] = synth.jitter_times(rng, base[li], 0.15)
+                pis[(ci, li)] = loci[li][1].pi
+            else:
+                g0, A0 = base[li]
+                trees[(ci, li)] = synth.jitter_times(rng, g0, 0.15)
+                alleles[(ci, li)] = _perturb_alleles(rng, g0, A0, g0.n)
+    par = np.tile(np.where(np.arange(nloci) < n_hky, kap, 1.0), (nch, 1))
+    return Workload("mixed", "config4-mixed: 300 loci (200 HKY U(200,3000) bp + 100 SW), U(4,60) copies "
+                             "x 3 pops, %d chains x %d runs" % (cpr, nruns),
+                    loci, nruns, cpr, trees, np.tile(ul, (nch, 1)), par, pis, alleles)
+
+
+def make(name):
+    return {"is": make_is, "hky": make_hky, "sw": make_sw, "mixed": make_mixed}[name]()

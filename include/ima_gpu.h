@@ -1,0 +1,231 @@
+/*
+ * ima_gpu.h -- C ABI of the GB300 implementation of IMa2p's data-parallel
+ * hot paths: the per-locus data likelihoods (infinite sites, HKY pruning,
+ * stepwise microsatellites), the MC3 temperature swaps and the L-mode
+ * joint-posterior surface.
+ *
+ * Conventions
+ *  - Plain C types only; every function returns an IMA_* status (never exits).
+ *    ima_gpu_error() returns the text of the last failure on a context.
+ *  - Host buffers are caller-owned; genealogies, partial likelihoods and chain
+ *    state are device-resident and owned by the context.
+ *  - One context = one CUDA stream on one device; call it from one host
+ *    thread at a time.
+ *  - Chains are numbered 0..nruns*chains_per_run-1 (run r owns chains
+ *    r*chains_per_run ..); loci 0..nloci-1 in the order they were added.
+ *    A (chain, locus) pair is a "chain-locus".
+ *  - Genealogy layout is the reference's struct edge (imamp.hpp:651-679):
+ *    numlines = 2n-1 nodes, tips 0..n-1, up0/up1 daughters (-1 at tips),
+ *    down parent (-1 at the root), time[c] = time at the lower end of edge c.
+ *
+ * Each entry point names the reference interface it replaces
+ * (paths relative to the IMa2p source tree, src/).
+ */
+#ifndef IMA_GPU_H
+#define IMA_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ima_ctx ima_ctx;
+
+/* status codes */
+#define IMA_OK 0
+#define IMA_ERR_ARG (-1)           /* bad argument (index, size, pointer)          */
+#define IMA_ERR_CUDA (-2)          /* a CUDA call failed                          */
+#define IMA_ERR_STATE (-3)         /* call out of order (e.g. no chains yet)       */
+#define IMA_ERR_NOMEM (-4)         /* device or host allocation failed            */
+#define IMA_ERR_DATA (-5)          /* data incompatible with a genealogy: the
+                                      reference's IM_err(IMERR_INFINITESITESFAIL) */
+#define IMA_ERR_TIMEOUT (-6)       /* a bounded device wait ran out               */
+
+/* mutation models, in the reference's enum order (imamp.hpp mutation models) */
+#define IMA_MODEL_IS 0
+#define IMA_MODEL_HKY 1
+#define IMA_MODEL_SW 2
+
+/* arithmetic of an evaluation */
+#define IMA_PREC_FAST 0            /* FP32 pruning / float-float Bessel, FP64 sums */
+#define IMA_PREC_FP64 1            /* plain FP64 per chain-locus                  */
+
+/* per chain-locus evaluation status */
+#define IMA_EVAL_OK 0
+#define IMA_EVAL_IS_REJECT 1       /* two mutation nodes: REJECTINFINITESITESCONSTANT */
+#define IMA_EVAL_IS_FAIL 2         /* no mutation node: data incompatible         */
+#define IMA_EVAL_SW_ZERO 3         /* a Bessel term was 0: result is -DBL_MAX     */
+
+/* ------------------------------------------------------------------ context */
+int ima_gpu_create(int device, ima_ctx **out);
+void ima_gpu_destroy(ima_ctx *ctx);
+const char *ima_gpu_error(const ima_ctx *ctx);
+int ima_gpu_synchronize(ima_ctx *ctx);
+
+/* ------------------------------------------------------------------- loci
+ * Locus tables shared by every chain; replace the L[li] arrays built by
+ * readseqIS / readseqHKY / readseqSW (readata.cpp:347-495, :247-345, :499-588).
+ * seq is [numgenes][numsites] row-major: 0/1 for IS (coded against the first
+ * sequence), 0..3 = A,C,G,T site patterns for HKY with their multiplicities. */
+int ima_gpu_add_locus_is(ima_ctx *ctx, int numgenes, int numsites, const int8_t *seq, int *li);
+int ima_gpu_add_locus_hky(ima_ctx *ctx, int numgenes, int numsites, int totsites,
+                          const int8_t *seq, const int32_t *mult, int *li);
+/* nlinked = number of linked stepwise markers (allele arrays per node). */
+int ima_gpu_add_locus_sw(ima_ctx *ctx, int numgenes, int nlinked, int *li);
+
+/* Allocate the resident state of nruns * chains_per_run chains over every
+ * locus added so far (replaces the per-chain allocations of setup,
+ * initialize.cpp:2074).  Loci cannot be added afterwards. */
+int ima_gpu_set_chains(ima_ctx *ctx, int nruns, int chains_per_run);
+
+/* -------------------------------------------------------------- genealogy
+ * Upload one genealogy (replaces writes to C[ci]->G[li].gtree).  length is the
+ * genealogy length from treeweight (update_gtree_common.cpp:1822-1840), used
+ * by the infinite-sites likelihood; pass a negative value to use the sum of
+ * branch lengths.  Edits are staged on the host and shipped to the device,
+ * as one copy per changed range, before the next evaluation. */
+int ima_gpu_set_genealogy(ima_ctx *ctx, int ci, int li, const int32_t *up0, const int32_t *up1,
+                          const int32_t *down, const double *time, double length);
+/* Many genealogies in one call: arrays of pair k start at offset
+ * sum_{j<k} numlines_j of the packed up0/up1/down/time arrays; length may be
+ * NULL (sum of branch lengths). */
+int ima_gpu_set_genealogies(ima_ctx *ctx, int npairs, const int32_t *ci, const int32_t *li,
+                            const int32_t *up0, const int32_t *up1, const int32_t *down,
+                            const double *time, const double *length);
+/* Base frequencies of an HKY chain-locus (C[ci]->G[li].pi). */
+int ima_gpu_set_pi(ima_ctx *ctx, int ci, int li, const double *pi4);
+/* Allele states of linked marker ai on every node (gtree[i].A[ai]). */
+int ima_gpu_set_alleles(ima_ctx *ctx, int ci, int li, int ai, const int32_t *A);
+
+/* --------------------------------------------- per-call reference mirrors
+ * Same names, argument meaning, return values and side effects as the
+ * reference functions, evaluated on the GPU from the resident state. */
+/* likelihoodIS (calc_prob_data.cpp:731-836): the per-locus constant sum log k!
+ * is taken from the first genealogy evaluated for the locus, as the reference's
+ * static sumlogk cache does (:760-765). */
+int ima_gpu_likelihoodIS(ima_ctx *ctx, int ci, int li, double mutrate, double *result);
+/* likelihoodHKY (calc_prob_data.cpp:583-607): e1..e4 are the dirty nodes
+ * (e1 == -1 recomputes every node). */
+int ima_gpu_likelihoodHKY(ima_ctx *ctx, int ci, int li, double mutrate, double kappa,
+                          int e1, int e2, int e3, int e4, double *result);
+/* copyfraclike / storescalefactors / restorescalefactors
+ * (update_gtree_common.cpp:2140-2181): accept or reject the partial
+ * likelihoods of the last HKY evaluation of (ci, li). */
+int ima_gpu_copyfraclike(ima_ctx *ctx, int ci, int li);
+int ima_gpu_storescalefactors(ima_ctx *ctx, int ci, int li);
+int ima_gpu_restorescalefactors(ima_ctx *ctx, int ci, int li);
+/* likelihoodSW (calc_prob_data.cpp:841-909): also refreshes the resident
+ * per-branch terms dlikeA of marker ai. */
+int ima_gpu_likelihoodSW(ima_ctx *ctx, int ci, int li, int ai, double u, double tr, double *result);
+/* Per-branch dlikeA terms of marker ai (gtree[i].dlikeA[ai]) after the last
+ * SW evaluation; dlikeA has numlines entries. */
+int ima_gpu_get_dlikeA(ima_ctx *ctx, int ci, int li, int ai, double *dlikeA);
+
+/* ------------------------------------------------------ batched likelihoods
+ * One launch over many chain-locus pairs of mixed models (the batched form
+ * of the calls above, as changet_RY1 / updategenealogy make them,
+ * update_t_RY.cpp:343-389, update_gtree.cpp:838-888).
+ *   ci, li     : chain-locus pairs (may repeat loci and mix models)
+ *   u          : mutation rate scalar per pair
+ *   kappa      : HKY kappa per pair; for SW pairs the branch-time scale tr
+ *                of likelihoodSW (ignored for IS; NULL = 1.0)
+ *   edits      : 4 dirty node ids per pair for HKY (NULL = full recompute)
+ *   ai         : SW marker per pair (NULL = 0)
+ *   precision  : IMA_PREC_FAST or IMA_PREC_FP64
+ *   result     : log P(D|G) per pair (host)
+ *   status     : IMA_EVAL_* per pair (host, may be NULL)
+ * Staged requests can be replayed without host copies through the batch
+ * handle functions below. */
+int ima_gpu_eval(ima_ctx *ctx, int npairs, const int32_t *ci, const int32_t *li, const double *u,
+                 const double *kappa, const int32_t *edits, const int32_t *ai, int precision,
+                 double *result, int32_t *status);
+/* accept[k] != 0 commits pair k (copyfraclike + storescalefactors and
+ * G.pdg = result), else reverts it (restorescalefactors). */
+int ima_gpu_commit(ima_ctx *ctx, int npairs, const int32_t *ci, const int32_t *li,
+                   const uint8_t *accept);
+
+/* Batches: stage requests once, run them from device memory (optionally as a
+ * CUDA graph replay), read the results when needed. */
+int ima_gpu_batch_create(ima_ctx *ctx, int npairs, const int32_t *ci, const int32_t *li,
+                         const double *u, const double *kappa, const int32_t *edits,
+                         const int32_t *ai, int precision, int *batch);
+int ima_gpu_batch_run(ima_ctx *ctx, int batch, int use_graph);
+int ima_gpu_batch_results(ima_ctx *ctx, int batch, double *result, int32_t *status);
+int ima_gpu_batch_destroy(ima_ctx *ctx, int batch);
+/* Copy every staged genealogy edit to the device now (normally implicit). */
+int ima_gpu_flush_genealogies(ima_ctx *ctx);
+
+/* -------------------------------------------------------------- MC3 swaps */
+/* setheat (swapchains.cpp:71-178) for every run (numprocesses = 1 within a
+ * run); heatmode 0 linear, 1 geometric, 2 even. */
+int ima_gpu_setheat(ima_ctx *ctx, double hval1, double hval2, int heatmode);
+int ima_gpu_get_betas(ima_ctx *ctx, double *beta);        /* nchains values */
+int ima_gpu_set_betas(ima_ctx *ctx, const double *beta);
+/* G.pdg of every chain-locus ([nchains][nloci]) and allpcalc.probg per chain. */
+int ima_gpu_set_pdg(ima_ctx *ctx, const double *pdg);
+int ima_gpu_get_pdg(ima_ctx *ctx, double *pdg);
+int ima_gpu_set_probg(ima_ctx *ctx, const double *probg);
+/* swapchains (swapchains.cpp:526-653) with swapbetasonly = 1 in every run.
+ * Uniform source: if uniforms != NULL, run r consumes uniforms[r*stride ...]
+ * in the reference's order (ci, cj rejection loop, then U only when w < 1)
+ * and used[r] returns how many it consumed; else a per-run Philox stream
+ * keyed by seed is used.  include_probg = 0 reproduces -c4.
+ * swap0ok[r] (may be NULL) as the reference returns it. */
+int ima_gpu_swapchains(ima_ctx *ctx, int swaptries, int include_probg, const double *uniforms,
+                       int stride, uint64_t seed, int32_t *used, int32_t *swap0ok);
+/* swapcount and tempbasedswapcount (imamp.hpp:1123-1129) of run r,
+ * chains_per_run^2 each, row-major. */
+int ima_gpu_get_swapcounts(ima_ctx *ctx, int run, int32_t *swapcount, int32_t *tempcount);
+
+/* --------------------------------------------------------- L-mode surface
+ * Load G saved genealogies (gsampinf rows, ginfo.cpp:288-316) for jointp.
+ * lognorm (may be NULL) replaces the per-genealogy bias -probg (or -sum qi,
+ * -sum mi) with an FP64 value. */
+int ima_gpu_surface_load(ima_ctx *ctx, int G, int rowlen, const float *gsampinf,
+                         int numpopsizeparams, int nummigrateparams, int npops,
+                         const double *lognorm);
+/* methods */
+#define IMA_SURF_FAST 0     /* split-precision contraction + online log-sum-exp */
+#define IMA_SURF_FP64 1     /* FP64 CUDA-core form, exact log-sum-exp           */
+#define IMA_SURF_COMPAT 2   /* the reference's truncated sum (PRANGELOG, eexp)   */
+/* q = log G - log sum_g exp(p_g(x)) at npoints points x[npoints][nparams];
+ * modeltype 0 full, 1 population sizes only, 2 migration only (jointp's
+ * nowmodeltype).  ess (may be NULL) = effective number of genealogies. */
+int ima_gpu_surface_eval(ima_ctx *ctx, int npoints, const double *x, int modeltype, int method,
+                         double *q, double *ess);
+/* jointp (jointfind.cpp:885-1047) at one point, reference semantics. */
+int ima_gpu_jointp(ima_ctx *ctx, const double *x, int calc_ess, double *effective_n, double *q);
+
+/* ------------------------------------------------------------ measurement */
+/* CUDA-event timer on the context stream. */
+int ima_gpu_timer_begin(ima_ctx *ctx);
+int ima_gpu_timer_end(ima_ctx *ctx, float *ms);
+/* Per-kernel accounting: when enabled, every launch of kernel `kind` is
+ * bracketed by events on its stream; totals are read with kernel_stats. */
+int ima_gpu_set_profiling(ima_ctx *ctx, int on);
+int ima_gpu_kernel_stats(ima_ctx *ctx, int kind, long long *launches, double *ms_total,
+                         double *bytes_total);
+/* kernel kinds for kernel_stats */
+#define IMA_K_IS 0
+#define IMA_K_IS_SUMLOGK 1
+#define IMA_K_HKY_FAST 2
+#define IMA_K_HKY_FP64 3
+#define IMA_K_SW_FAST 4
+#define IMA_K_SW_FP64 5
+#define IMA_K_SWAP 6
+#define IMA_K_SURF_FAST 7
+#define IMA_K_SURF_FP64 8
+#define IMA_K_SURF_COMPAT 9
+#define IMA_K_COUNT 10
+/* Total kernel launches issued by this library on the context. */
+int ima_gpu_launch_count(ima_ctx *ctx, long long *n);
+/* Write a device buffer larger than L2 (evicts resident data). */
+int ima_gpu_flush_l2(ima_ctx *ctx);
+/* Device bytes held by the context. */
+int ima_gpu_memory(ima_ctx *ctx, size_t *bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IMA_GPU_H */

@@ -1,0 +1,96 @@
+"""HKY pruning on the GPU: full and dirty-node evaluations with
+accept/reject of the partial likelihoods, against the reference's golden
+values.  FP64 form: 1e-12 relative.  FP32 form (FP32 partials, exact
+power-of-two rescaling, FP64 root sums): per-locus |error| within
+HKY_FP32_TOL below; its measured distribution is reported by bench.py."""
+import numpy as np
+import pytest
+
+from ima2p_gb300 import api, synth
+from ima2p_gb300.synth import HKYLocus
+from oracle import pyoracle as O
+from tests._golden import load, trees
+from tests._gpu import ctx_with
+
+pytestmark = pytest.mark.gpu
+
+# relative to |log L|: FP32 rounding of ~depth*10 operations per pattern
+HKY_FP32_RTOL = 2e-6
+
+
+def _run_golden(precision):
+    d = load("golden_hky.npz")
+    for c in range(int(d["ncases"])):
+        p = "c%d_" % c
+        loc = HKYLocus(d[p + "seq"], d[p + "mult"], int(d[p + "totsites"]), d[p + "pi"])
+        ts = trees(d, p)
+        u, kappa = float(d[p + "u"]), float(d[p + "kappa"])
+        ctx = ctx_with([("hky", loc)])
+        ctx.set_pi(0, 0, loc.pi)
+        ctx.set_genealogy(0, 0, ts[0])
+        got = [ctx.eval([0], [0], [u], [kappa], precision=precision)[0][0]]
+        ctx.commit([0], [0], [1])
+        for t, e, acc in zip(ts[1:], d[p + "e"], d[p + "acc"]):
+            ctx.set_genealogy(0, 0, t)
+            got.append(ctx.eval([0], [0], [u], [kappa], edits=[e], precision=precision)[0][0])
+            ctx.commit([0], [0], [acc])
+        ctx.close()
+        yield np.array(got), d[p + "ref"]
+
+
+def test_hky_fp64_golden():
+    for got, ref in _run_golden(api.PREC_FP64):
+        np.testing.assert_allclose(got, ref, rtol=1e-12, atol=0)
+
+
+def test_hky_fp32_golden():
+    for got, ref in _run_golden(api.PREC_FAST):
+        np.testing.assert_allclose(got, ref, rtol=HKY_FP32_RTOL, atol=0)
+
+
+def test_hky_reference_mirror_calls():
+    d = load("golden_hky.npz")
+    p = "c1_"
+    loc = HKYLocus(d[p + "seq"], d[p + "mult"], int(d[p + "totsites"]), d[p + "pi"])
+    ts = trees(d, p)
+    u, kappa = float(d[p + "u"]), float(d[p + "kappa"])
+    ctx = ctx_with([("hky", loc)])
+    ctx.set_pi(0, 0, loc.pi)
+    ctx.set_genealogy(0, 0, ts[0])
+    got = [ctx.likelihoodHKY(0, 0, u, kappa, -1, -1, -1, -1)]
+    ctx.copyfraclike(0, 0)
+    ctx.storescalefactors(0, 0)
+    for t, e, acc in zip(ts[1:], d[p + "e"], d[p + "acc"]):
+        ctx.set_genealogy(0, 0, t)
+        got.append(ctx.likelihoodHKY(0, 0, u, kappa, *[int(v) for v in e]))
+        if acc:
+            ctx.copyfraclike(0, 0)
+            ctx.storescalefactors(0, 0)
+        else:
+            ctx.restorescalefactors(0, 0)
+    np.testing.assert_allclose(got, d[p + "ref"], rtol=HKY_FP32_RTOL)
+
+
+def test_hky_batch_many_chains_vs_oracle():
+    rng = np.random.default_rng(11)
+    nloci, nch = 3, 5
+    locs, base = [], []
+    for li in range(nloci):
+        g = synth.two_pop_tree(rng, 8 + 4 * li, 8 + 4 * li, theta=10.0, mig=0.2, tsplit=1.5)
+        locs.append(synth.hky_data(rng, g, 400 + 300 * li, 1.0, rng.uniform(2, 8), rng.dirichlet([5] * 4)))
+        base.append(g)
+    ctx = ctx_with([("hky", L) for L in locs], 1, nch)
+    ci, li, u, kap, want = [], [], [], [], []
+    for c in range(nch):
+        for l in range(nloci):
+            t = synth.jitter_times(rng, base[l], 0.3)
+            ctx.set_genealogy(c, l, t)
+            ctx.set_pi(c, l, locs[l].pi)
+            uu, kk = float(rng.lognormal(0, 0.5)), float(rng.uniform(2, 8))
+            st = O.HKYState(*locs[l].seq.shape)
+            want.append(st.likelihood(locs[l], t, uu, kk))
+            ci.append(c), li.append(l), u.append(uu), kap.append(kk)
+    r64, _ = ctx.eval(ci, li, u, kap, precision=api.PREC_FP64)
+    r32, _ = ctx.eval(ci, li, u, kap, precision=api.PREC_FAST)
+    np.testing.assert_allclose(r64, want, rtol=1e-12)
+    np.testing.assert_allclose(r32, want, rtol=HKY_FP32_RTOL)

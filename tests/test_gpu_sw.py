@@ -1,0 +1,84 @@
+"""Stepwise-mutation likelihood on the GPU against the reference's golden
+values: per-locus totals and per-branch dlikeA, including a zero Bessel term
+(total -DBL_MAX) and x > 700.  The float-float form must stay within
+SW_FAST_ATOL of the reference per locus (the 1e-6 target, with margin); the
+FP64 form within 1e-12 relative."""
+import numpy as np
+import pytest
+
+from ima2p_gb300 import api, synth
+from oracle import pyoracle as O
+from tests._golden import load, trees
+from tests._gpu import ctx_with
+
+pytestmark = pytest.mark.gpu
+
+SW_FAST_ATOL = 1e-9      # per-locus |log L - reference|
+DBLMAX = np.finfo(np.float64).max
+
+
+@pytest.mark.parametrize("prec", [api.PREC_FAST, api.PREC_FP64])
+def test_sw_golden(prec):
+    d = load("golden_sw.npz")
+    ts = trees(d)
+    n = ts[0].n
+    ctx = ctx_with([("sw", n, 1)], 1, len(ts))
+    for ci, (t, A) in enumerate(zip(ts, d["A"])):
+        ctx.set_genealogy(ci, 0, t)
+        ctx.set_alleles(ci, 0, A)
+    res, st = ctx.eval(np.arange(len(ts)), np.zeros(len(ts)), d["u"], precision=prec)
+    for ci, r in enumerate(d["ref"]):
+        if r[0] == -DBLMAX:
+            assert res[ci] == -DBLMAX and st[ci] == api.EVAL_SW_ZERO
+            continue
+        if prec == api.PREC_FAST:
+            assert abs(res[ci] - r[0]) <= SW_FAST_ATOL, (ci, res[ci], r[0])
+        else:
+            assert abs(res[ci] - r[0]) <= 1e-12 * abs(r[0])
+        dl = ctx.get_dlikeA(ci, 0)
+        np.testing.assert_allclose(dl, r[1:], rtol=1e-11 if prec == api.PREC_FP64 else 1e-9, atol=1e-11)
+
+
+def test_sw_config3_shape_vs_oracle():
+    rng = np.random.default_rng(5)
+    nloci, nch = 6, 4
+    base = [synth.three_pop_tree(rng, [30, 30, 30], theta=4.0, mig=0.05) for _ in range(nloci)]
+    ctx = ctx_with([("sw", 90, 1)] * nloci, 1, nch)
+    ci, li, u, want = [], [], [], []
+    worst = 0.0
+    for c in range(nch):
+        for l in range(nloci):
+            t = synth.jitter_times(rng, base[l], 0.2)
+            A = synth.sw_alleles(rng, t, float(rng.lognormal(0, 0.5)))
+            ctx.set_genealogy(c, l, t)
+            ctx.set_alleles(c, l, A)
+            uu = float(rng.lognormal(0, 0.5))
+            want.append(O.sw_likelihood(A, t, uu)[0])
+            ci.append(c), li.append(l), u.append(uu)
+    fast, _ = ctx.eval(ci, li, u, precision=api.PREC_FAST)
+    slow, _ = ctx.eval(ci, li, u, precision=api.PREC_FP64)
+    np.testing.assert_allclose(slow, want, rtol=1e-12)
+    assert np.max(np.abs(fast - np.array(want))) <= SW_FAST_ATOL
+
+
+def test_sw_bessel_edge_terms():
+    """Single-branch genealogies sweep |d| and x across the A&S / Miller
+    regimes and the float-float fallbacks."""
+    cases = []
+    for d in (0, 1, 2, 3, 5, 9, 17, 30):
+        for x in (1e-12, 1e-6, 0.01, 0.3, 1.0, 3.7499, 3.75, 10.0, 80.0, 699.0, 701.0):
+            cases.append((d, x))
+    n = 2
+    ctx = ctx_with([("sw", n, 1)], 1, len(cases))
+    for ci, (d, x) in enumerate(cases):
+        g = synth.Genealogy(np.array([-1, -1, 0]), np.array([-1, -1, 1]), np.array([2, 2, -1]),
+                            np.array([x, x, -1.0]), 2)
+        ctx.set_genealogy(ci, 0, g)
+        ctx.set_alleles(ci, 0, np.array([20 + d, 20, 20]))
+    res, st = ctx.eval(np.arange(len(cases)), np.zeros(len(cases)), np.ones(len(cases)))
+    for k, (d, x) in enumerate(cases):
+        want = O.lib().ora_sw_branch_term(d, x, 1.0) + O.lib().ora_sw_branch_term(0, x, 1.0)
+        if want <= -1e99:
+            assert st[k] == api.EVAL_SW_ZERO
+        else:
+            assert abs(res[k] - want) <= 1e-9 * max(1.0, abs(want)), (d, x, res[k], want)
