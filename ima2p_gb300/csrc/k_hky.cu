@@ -65,6 +65,32 @@ __device__ __forceinline__ void hky_p(const T *pi, T kpa, T b, T *P)
   }
 }
 
+// The same matrix for FP32, rewritten with E1 = 1 - exp(-b), E2 = 1 - exp(-bA)
+// taken from expm1 so that short branches do not cancel:
+//   transversion  pi_k E1
+//   transition    (pi_k / Pi_k) (E2 - E1 (1 - Pi_k))
+//   identity      1 - E1 pi_k (1 - Pi_k) / Pi_k - E2 (Pi_k - pi_k) / Pi_k
+__device__ __forceinline__ void hky_p_fast(const float *pi, float kpa, float b, float *P)
+{
+  float E1 = -expm1f(-b);
+  float PR = pi[0] + pi[2], PY = pi[1] + pi[3];
+  float ER = -expm1f(-b * (1.0f + PR * kpa)), EY = -expm1f(-b * (1.0f + PY * kpa));
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    float Pk = (k == 0 || k == 2) ? PR : PY;
+    float E2 = (k == 0 || k == 2) ? ER : EY;
+    float r = pi[k] / Pk;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      float v;
+      if (j == k) v = 1.0f - E1 * r * (1.0f - Pk) - E2 * (1.0f - r);
+      else if (j + k == 2 || j + k == 4) v = r * (E2 - E1 * (1.0f - Pk));
+      else v = pi[k] * E1;
+      P[j * 4 + k] = v;
+    }
+  }
+}
+
 // Shared-memory carve-up, identical on host (sizing) and device.
 struct HkyLayout {
   size_t nd, fresh, order, total;
@@ -178,7 +204,7 @@ __global__ void __launch_bounds__(HKY_BS) k_hky_fast(Pools P, const ReqDev *reqs
     int d = T.nd[c].down;
     if (d < 0 || !T.fresh[d]) continue;
     float pil[4] = {spi[0], spi[1], spi[2], spi[3]};
-    hky_p<float>(pil, kpa, smu * branch_ff(T.nd, tff, c), Pm + 16 * c);
+    hky_p_fast(pil, kpa, smu * branch_ff(T.nd, tff, c), Pm + 16 * c);
   }
   __syncthreads();
 
