@@ -40,7 +40,8 @@ EXPORTS = [
     "ima_gpu_batch_destroy", "ima_gpu_flush_genealogies", "ima_gpu_setheat", "ima_gpu_get_betas",
     "ima_gpu_set_betas", "ima_gpu_set_pdg", "ima_gpu_get_pdg", "ima_gpu_set_probg",
     "ima_gpu_swapchains", "ima_gpu_get_swapcounts", "ima_gpu_surface_load",
-    "ima_gpu_surface_eval", "ima_gpu_jointp", "ima_gpu_timer_begin", "ima_gpu_timer_end",
+    "ima_gpu_surface_eval", "ima_gpu_jointp", "ima_gpu_surface_fp64_noalloc",
+    "ima_gpu_timer_begin", "ima_gpu_timer_end",
     "ima_gpu_set_profiling", "ima_gpu_kernel_stats", "ima_gpu_launch_count", "ima_gpu_flush_l2",
     "ima_gpu_memory",
 ]
@@ -113,6 +114,7 @@ def _declare(L):
         "ima_gpu_surface_load": (I, [P, I, I, P, I, I, I, P]),
         "ima_gpu_surface_eval": (I, [P, I, P, I, I, P, P]),
         "ima_gpu_jointp": (I, [P, P, I, P, P]),
+        "ima_gpu_surface_fp64_noalloc": (I, [P, I, I, I, I, I, P, P, I, I, P, P, P]),
         "ima_gpu_timer_begin": (I, [P]),
         "ima_gpu_timer_end": (I, [P, C.POINTER(C.c_float)]),
         "ima_gpu_set_profiling": (I, [P, I]),
@@ -379,6 +381,19 @@ class Context:
         n = C.c_size_t()
         self._ck(self.lib.ima_gpu_memory(self.h, C.byref(n)))
         return n.value
+
+
+IMA_ERR_TOO_LARGE = -7
+
+
+def surface_fp64_noalloc(rows_ptr, G, rowlen, np_, nm, npops, lognorm_ptr, x_ptr, npoints,
+                         modeltype, q_ptr, ess_ptr, stream=None):
+    """The allocation-free FP64 surface on caller-owned device pointers (ints);
+    returns the library status code.  For callers that cannot allocate device
+    memory; see include/ima_gpu.h for its scratch limit."""
+    lib = load_library()
+    return lib.ima_gpu_surface_fp64_noalloc(rows_ptr, G, rowlen, np_, nm, npops, lognorm_ptr, x_ptr,
+                                            npoints, modeltype, q_ptr, ess_ptr, stream)
 
 
 class Batch:

@@ -18,6 +18,7 @@
 // overall maximum and, when every listed value is in range, also the
 // smallest one -- and its eexp decimal-exponent accumulation.
 #include <cfloat>
+#include <mutex>
 
 #include "internal.h"
 
@@ -332,4 +333,80 @@ void launch_surface_compat(const SurfArgs &a, double *scratch, cudaStream_t st)
     uint8_t *listed = reinterpret_cast<uint8_t *>(scratch + (size_t)conc * a.G);
     k_surf_compat<<<np, CP_BS, 0, st>>>(a, p0, scratch, listed);
   }
+}
+
+// ======================================================================
+// Allocation-free variant of the FP64 surface, for callers that cannot call
+// cudaMalloc.  Its only scratch -- one (max, sum, sum of squares) triple per
+// point and genealogy chunk -- lives in the fixed device array below, which
+// every GPU that loads this library holds until the process exits.
+namespace {
+
+constexpr size_t NOALLOC_SCRATCH_DOUBLES = (size_t)1 << 19;  // 4 MiB
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+__device__ __align__(256) double g_surf_scratch[NOALLOC_SCRATCH_DOUBLES];
+
+std::mutex g_noalloc_mu;
+double *g_noalloc_addr[NOALLOC_MAX_DEVICES];
+
+// Device address of g_surf_scratch on the current device, looked up once per
+// device (host code cannot use the symbol itself as a device pointer).
+int noalloc_scratch(double **out)
+{
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return IMA_ERR_CUDA;
+  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return IMA_ERR_ARG;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    double *p = nullptr;
+    if (cudaGetSymbolAddress(reinterpret_cast<void **>(&p), g_surf_scratch) != cudaSuccess)
+      return IMA_ERR_CUDA;
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return IMA_OK;
+}
+
+}  // namespace
+
+extern "C" int ima_gpu_surface_fp64_noalloc(const float *rows, int G, int rowlen, int np, int nm,
+                                            int npops, const double *lognorm, const double *x,
+                                            int npoints, int modeltype, double *q, double *ess,
+                                            void *stream)
+{
+  if (!rows || !x || !q || G < 1 || npoints < 1 || np < 0 || nm < 0 || np + nm < 1 ||
+      np + nm > 32 || rowlen < 4 * np + 3 * nm + 2 || rowlen > 64 || modeltype < 0 || modeltype > 2)
+    return IMA_ERR_ARG;
+  // one triple per point and chunk: use as many chunks as the array allows
+  size_t per_point = 3;
+  if ((size_t)npoints * per_point > NOALLOC_SCRATCH_DOUBLES) return IMA_ERR_TOO_LARGE;
+  int nchunks = (G + 65535) / 65536;
+  if (nchunks > 64) nchunks = 64;
+  size_t fit = NOALLOC_SCRATCH_DOUBLES / ((size_t)npoints * per_point);
+  if ((size_t)nchunks > fit) nchunks = (int)fit;
+  double *scratch = nullptr;
+  int r = noalloc_scratch(&scratch);
+  if (r) return r;
+  SurfArgs a;
+  a.G = G;
+  a.rowlen = rowlen;
+  a.np = np;
+  a.nm = nm;
+  a.npops = npops;
+  a.modeltype = modeltype;
+  a.npoints = npoints;
+  a.rows = rows;
+  a.lognorm = lognorm;
+  a.x = x;
+  a.q = q;
+  a.ess = ess;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // every (point, chunk) triple is written before the merge reads it, so the
+  // contents left by an earlier call never leak into this one
+  int chunk = (G + nchunks - 1) / nchunks;
+  dim3 grid((npoints + F64_PTS - 1) / F64_PTS, nchunks);
+  k_surf_fp64<<<grid, F64_PTS, 0, st>>>(a, chunk, scratch);
+  k_surf_merge<<<(npoints + 127) / 128, 128, 0, st>>>(a, nchunks, scratch);
+  return cudaGetLastError() == cudaSuccess ? IMA_OK : IMA_ERR_CUDA;
 }

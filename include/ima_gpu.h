@@ -197,6 +197,26 @@ int ima_gpu_surface_eval(ima_ctx *ctx, int npoints, const double *x, int modelty
 /* jointp (jointfind.cpp:885-1047) at one point, reference semantics. */
 int ima_gpu_jointp(ima_ctx *ctx, const double *x, int calc_ess, double *effective_n, double *q);
 
+/* No counterpart in the reference.  The FP64 surface of ima_gpu_surface_eval
+ * (IMA_SURF_FP64) for callers that cannot allocate device memory -- code
+ * running inside a CUDA graph capture or under a host framework that owns
+ * every device allocation.  No context and no allocation: every pointer is
+ * caller-owned DEVICE memory (rows [G][rowlen] float, lognorm [G] or NULL,
+ * x [npoints][np+nm], q and ess [npoints], ess may be NULL); work is queued
+ * on `stream` (a cudaStream_t, NULL = legacy default stream) and results are
+ * ready when that stream is.  The kernel's scratch is a fixed 4 MiB device
+ * array inside this library, held on every GPU that loads it until the
+ * process exits; it bounds npoints at 174762 -- larger requests return
+ * IMA_ERR_TOO_LARGE without launching anything.  The first call on a device
+ * looks up the array's device address (make it before any stream capture).
+ * All calls share the array: calls that overlap on the GPU (different
+ * streams, or other threads) race, so serialise them. */
+#define IMA_ERR_TOO_LARGE (-7)
+int ima_gpu_surface_fp64_noalloc(const float *rows, int G, int rowlen, int numpopsizeparams,
+                                 int nummigrateparams, int npops, const double *lognorm,
+                                 const double *x, int npoints, int modeltype, double *q,
+                                 double *ess, void *stream);
+
 /* ------------------------------------------------------------ measurement */
 /* CUDA-event timer on the context stream. */
 int ima_gpu_timer_begin(ima_ctx *ctx);
