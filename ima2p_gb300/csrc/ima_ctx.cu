@@ -351,6 +351,7 @@ extern "C" int ima_gpu_add_locus_hky(ima_ctx *c, int numgenes, int numsites, int
 extern "C" int ima_gpu_add_locus_sw(ima_ctx *c, int numgenes, int nlinked, int *li)
 {
   if (nlinked < 1) return c ? c->fail(IMA_ERR_ARG, "nlinked must be >= 1") : IMA_ERR_ARG;
+  if (numgenes > 256) return c ? c->fail(IMA_ERR_ARG, "stepwise loci hold at most 256 gene copies") : IMA_ERR_ARG;
   return add_locus(c, IMA_MODEL_SW, numgenes, 0, 0, nullptr, nullptr, nlinked, li);
 }
 

@@ -98,69 +98,60 @@ __device__ __forceinline__ double term_64(int d, double x, bool *zero)
 }
 
 // --------------------------------------------------------- float-float
-// log(bessi0(x)) - x
-__device__ ff l0_ff(ff x)
+// Coefficient tables of the four |d| <= 1 regimes, zero-padded to 9 terms:
+// [d01 * 2 + small]: d=0 large, d=0 small, d=1 large, d=1 small.
+struct SwTables {
+  float2 c[4][9];
+};
+
+__device__ __forceinline__ ff ff_add_fast(ff a, ff b)  // no cancellation expected
 {
-  if (x.hi < 3.75f) {
-    ff y = ff_mul(x, ffc(c_ff.inv375));
-    y = ff_mul(y, y);
-    return ff_sub(ff_log(ff_horner(c_ff.i0s, 7, y), c_ff), x);
-  }
-  ff z = ff_div(ff_from(3.75f), x);
-  ff lx = ff_log(x, c_ff);
-  return ff_sub(ff_log(ff_horner(c_ff.i0l, 9, z), c_ff), ff_make(0.5f * lx.hi, 0.5f * lx.lo));
+  ff s = two_sum(a.hi, b.hi);
+  float e = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+  return fast_two_sum(s.hi, e);
 }
 
-// log(bessi1(x)) - x, x > 0
-__device__ ff l1_ff(ff x)
+// log(bessi(n, x)) - x for n <= 1 (and the log(bessi0) - x part for n >= 2),
+// one code path for every lane: the regime only selects the argument and
+// the coefficient table.
+//   x < 3.75:  bessi0 = P0(y), bessi1 = x P1(y), y = (x / 3.75)^2
+//   x >= 3.75: bessi_n = exp(x) / sqrt(x) Q_n(z), z = 3.75 / x
+__device__ __forceinline__ ff sw_core(ff x, int d01, const SwTables &T)
 {
-  if (x.hi < 3.75f) {
-    ff y = ff_mul(x, ffc(c_ff.inv375));
-    y = ff_mul(y, y);
-    return ff_sub(ff_add(ff_log(x, c_ff), ff_log(ff_horner(c_ff.i1s, 7, y), c_ff)), x);
-  }
-  ff z = ff_div(ff_from(3.75f), x);
-  ff lx = ff_log(x, c_ff);
-  return ff_sub(ff_log(ff_horner(c_ff.i1l, 9, z), c_ff), ff_make(0.5f * lx.hi, 0.5f * lx.lo));
+  const bool small = x.hi < 3.75f;
+  const ff xs = (x.hi > 0.f) ? x : ff_from(1.0f);
+  ff y = ff_mul(x, ffc(c_ff.inv375));
+  y = ff_mul(y, y);
+  ff z = ff_div(ff_from(3.75f), xs);
+  ff arg = small ? y : z;
+  const float2 *c = T.c[d01 * 2 + (small ? 1 : 0)];
+  ff acc = ffc(c[8]);
+#pragma unroll
+  for (int k = 7; k >= 0; k--) acc = ff_add_fast(ff_mul(acc, arg), ffc(c[k]));
+  ff lp = ff_log(acc, c_ff);
+  ff lx = ff_log(xs, c_ff);
+  ff tail = small ? (d01 ? ff_sub(lx, x) : ff_neg(x)) : ff_make(-0.5f * lx.hi, -0.5f * lx.lo);
+  return ff_add(lp, tail);
 }
 
-// Returns false when the branch must be evaluated in FP64.
-__device__ bool term_ff(int d, ff x, ff *out, bool *zero)
+// log(ans / bi) of the reference's Miller recurrence and its 1e10 rescaling
+// count; false when the value must come from the FP64 path.
+__device__ bool sw_miller(int n, ff x, ff *out)
 {
-  int n = abs(d);
-  if (x.hi > 700.0f || (x.hi == 700.0f && x.lo > 0.0f)) {
-    *out = ff_sub(ffc(c_ff.logmydblmax), x);
-    return true;
-  }
-  if (n == 0) {
-    *out = l0_ff(x);
-    return true;
-  }
-  if (x.hi == 0.0f) {
-    *zero = true;
-    *out = ff_from(0.0f);
-    return true;
-  }
-  if (n == 1) {
-    *out = l1_ff(x);
-    return true;
-  }
   if (x.hi < 1e-15f) return false;
-  // Miller recurrence; the reference's 1e10 rescaling of `ans` after it is
-  // captured is counted instead of applied, keeping it in float range
   ff tox = ff_div(ff_from(2.0f), x);
   ff bip = ff_from(0.0f), bi = ff_from(1.0f), ans = ff_from(0.0f);
-  const ff big = ffc(c_ff.e10m);  // 1e-10
+  const ff tiny = ffc(c_ff.e10m);  // 1e-10
   int scaled = 0;
   bool got = false;
   for (int j = 2 * (n + (int)sqrtf(40.0f * n)); j > 0; j--) {
-    ff bim = ff_add(bip, ff_mul(ff_mul_f(tox, (float)j), bi));
+    ff bim = ff_add_fast(bip, ff_mul_f(ff_mul(tox, bi), (float)j));
     bip = bi;
     bi = bim;
     if (bi.hi > 1.0e10f) {
       if (got) scaled++;
-      bi = ff_mul(bi, big);
-      bip = ff_mul(bip, big);
+      bi = ff_mul(bi, tiny);
+      bip = ff_mul(bip, tiny);
     }
     if (j == n) {
       ans = bip;
@@ -168,16 +159,14 @@ __device__ bool term_ff(int d, ff x, ff *out, bool *zero)
     }
   }
   // the reference's FP64 `ans` is ans * 1e-10^scaled: leave the range where
-  // that value is normal to the FP64 path
+  // that value is not a normal double to the FP64 path
   if (!(ans.hi > 0.0f) || __log10f(ans.hi) - 10.0f * scaled < -300.0f) return false;
-  // log(ans) - log(bi): the ratio itself may leave float range
   ff r = ff_sub(ff_log(ans, c_ff), ff_log(bi, c_ff));
-  ff s = ff_mul_f(ffc(c_ff.ln1e10), (float)scaled);
-  *out = ff_add(ff_sub(r, s), l0_ff(x));
+  *out = ff_sub(r, ff_mul_f(ffc(c_ff.ln1e10), (float)scaled));
   return true;
 }
 
-__device__ __forceinline__ ff branch_ff(const NodeRec &nd, const float2 *t, int c, ff tr)
+__device__ __forceinline__ ff branch_len_ff(const NodeRec &nd, const float2 *t, int c, ff tr)
 {
   ff a = ff_make(t[c].x, t[c].y);
   if (nd.up0 < 0) return ff_mul(a, tr);
@@ -203,63 +192,134 @@ __device__ __forceinline__ ff warp_sum_ff(ff v)
   return v;
 }
 
-__global__ void __launch_bounds__(SW_BS) k_sw_fast(Pools P, const ReqDev *reqs, double *result,
-                                                   int32_t *status)
+constexpr int SW_IPC = 8;        // chain-loci per CTA (one warp reduces each)
+constexpr int SW_FAST_BS = 256;
+constexpr int SW_MAXB = SW_IPC * 512;
+
+// Three phases per CTA of up to 8 chain-loci: (A) every branch through the
+// branch-free core, with |d| >= 2 branches queued; (B) the queued Miller
+// recurrences, packed onto consecutive threads; (C) one warp per chain-locus
+// sums its branch terms in float-float.
+__global__ void __launch_bounds__(SW_FAST_BS) k_sw_fast(Pools P, const ReqDev *reqs, int nreq,
+                                                        double *result, int32_t *status)
 {
-  const ReqDev R = reqs[blockIdx.x];
-  const double tr = R.par;
-  const ItemDev it = P.items[R.item];
-  const int nl = 2 * it.n - 1;
-  const NodeRec *nd = P.nodes + it.node_off;
-  const float2 *tff = P.tff + it.node_off;
-  const double *t64 = P.t64 + it.node_off;
-  const int32_t *A = P.alleles + it.al_off + (size_t)R.ai * nl;
-  float2 *dl = reinterpret_cast<float2 *>(P.dlike) + it.dl_off + (size_t)R.ai * nl;
-  const float uh = (float)R.u;
-  const ff u = ff_make(uh, (float)(R.u - (double)uh));
-  const float trh = (float)tr;
-  const ff trf = ff_make(trh, (float)(tr - (double)trh));
-  ff acc = ff_from(0.0f);
-  bool zero = false;
-  for (int c = threadIdx.x; c < nl; c += SW_BS) {
-    NodeRec r = nd[c];
-    if (r.down < 0) {
-      dl[c] = make_float2(0.f, 0.f);
-      continue;
-    }
-    int d = A[c] - A[r.down];
-    ff x = ff_mul(branch_ff(r, tff, c, trf), u);
-    ff v;
-    bool z = false;
-    if (!term_ff(d, x, &v, &z)) {  // rare: exact FP64 evaluation
-      double t = (r.up0 < 0) ? t64[c] * tr : tr * (t64[c] - t64[r.up0]);
-      double w = term_64(d, t * R.u, &z);
-      float wh = (float)w;
-      v = ff_make(wh, (float)(w - (double)wh));
-    }
-    if (z) {
-      zero = true;
-      v = ff_make(-1e30f, 0.f);  // placeholder: the total is -DBL_MAX anyway
-      dl[c] = make_float2(-INFINITY, 0.f);
-    } else {
-      dl[c] = make_float2(v.hi, v.lo);
-    }
-    acc = ff_add(acc, v);
+  __shared__ SwTables T;
+  __shared__ float2 vals[SW_MAXB];
+  __shared__ int16_t queue[SW_MAXB];
+  __shared__ int qn;
+  __shared__ int bstart[SW_IPC + 1];
+  __shared__ int zero[SW_IPC];
+  __shared__ float2 uff[SW_IPC], trff[SW_IPC];
+  const int r0 = blockIdx.x * SW_IPC;
+  const int nit = min(SW_IPC, nreq - r0);
+  const int tid = threadIdx.x;
+  if (tid < 36) {
+    int t = tid / 9, k = tid % 9;
+    int d01 = t >> 1, small = t & 1;
+    int m = small ? 7 : 9;
+    float2 v = make_float2(0.f, 0.f);
+    if (k < m) v = d01 ? (small ? c_ff.i1s[k] : c_ff.i1l[k]) : (small ? c_ff.i0s[k] : c_ff.i0l[k]);
+    T.c[t][k] = v;
   }
-  __shared__ float2 red[SW_BS / 32];
-  __shared__ int anyzero;
-  if (threadIdx.x == 0) anyzero = 0;
+  if (tid == 0) {
+    qn = 0;
+    int b = 0;
+    for (int i = 0; i < nit; i++) {
+      bstart[i] = b;
+      b += 2 * P.items[reqs[r0 + i].item].n - 1;
+    }
+    bstart[nit] = b;
+  }
+  if (tid < nit) {
+    const ReqDev R = reqs[r0 + tid];
+    float uh = (float)R.u, th = (float)R.par;
+    uff[tid] = make_float2(uh, (float)(R.u - (double)uh));
+    trff[tid] = make_float2(th, (float)(R.par - (double)th));
+    zero[tid] = 0;
+  }
   __syncthreads();
-  acc = warp_sum_ff(acc);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = make_float2(acc.hi, acc.lo);
-  if (zero) anyzero = 1;
+  const int total = bstart[nit];
+  // ---- phase A
+  for (int b = tid; b < total; b += SW_FAST_BS) {
+    int i = 0;
+    while (b >= bstart[i + 1]) i++;
+    const ReqDev &R = reqs[r0 + i];
+    const ItemDev it = P.items[R.item];
+    const int nl = 2 * it.n - 1, c = b - bstart[i];
+    const NodeRec nd = P.nodes[it.node_off + c];
+    float2 out = make_float2(0.f, 0.f);
+    if (nd.down >= 0) {
+      const int32_t *A = P.alleles + it.al_off + (size_t)R.ai * nl;
+      int n = abs(A[c] - A[nd.down]);
+      ff x = ff_mul(branch_len_ff(nd, P.tff + it.node_off, c, ffc(trff[i])), ffc(uff[i]));
+      ff v;
+      if (x.hi > 700.0f || (x.hi == 700.0f && x.lo > 0.0f)) {
+        v = ff_sub(ffc(c_ff.logmydblmax), x);
+      } else if (n >= 1 && x.hi == 0.0f) {
+        zero[i] = 1;
+        v = ff_make(-INFINITY, 0.f);
+      } else {
+        v = sw_core(x, n == 1 ? 1 : 0, T);
+        if (n >= 2) queue[atomicAdd(&qn, 1)] = (int16_t)b;
+      }
+      out = make_float2(v.hi, v.lo);
+    }
+    vals[b] = out;
+  }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    ff s = ff_from(0.0f);
-    for (int w = 0; w < SW_BS / 32; w++) s = ff_add(s, ff_make(red[w].x, red[w].y));
-    result[blockIdx.x] = anyzero ? -DBL_MAX : ff_to_double(s);
-    P.pdg_new[R.item] = result[blockIdx.x];
-    status[blockIdx.x] = anyzero ? IMA_EVAL_SW_ZERO : IMA_EVAL_OK;
+  // ---- phase B: |d| >= 2
+  for (int q = tid; q < qn; q += SW_FAST_BS) {
+    const int b = queue[q];
+    int i = 0;
+    while (b >= bstart[i + 1]) i++;
+    const ReqDev &R = reqs[r0 + i];
+    const ItemDev it = P.items[R.item];
+    const int nl = 2 * it.n - 1, c = b - bstart[i];
+    const NodeRec nd = P.nodes[it.node_off + c];
+    const int32_t *A = P.alleles + it.al_off + (size_t)R.ai * nl;
+    const int d = A[c] - A[nd.down];
+    ff x = ff_mul(branch_len_ff(nd, P.tff + it.node_off, c, ffc(trff[i])), ffc(uff[i]));
+    ff r;
+    float2 out;
+    if (sw_miller(abs(d), x, &r)) {
+      ff v = ff_add(ffc(vals[b]), r);
+      out = make_float2(v.hi, v.lo);
+    } else {  // rare: the reference's FP64 arithmetic
+      const double *t64 = P.t64 + it.node_off;
+      double t = (nd.up0 < 0) ? t64[c] * R.par : R.par * (t64[c] - t64[nd.up0]);
+      bool z = false;
+      double w = term_64(d, t * R.u, &z);
+      if (z) {
+        zero[i] = 1;
+        out = make_float2(-INFINITY, 0.f);
+      } else {
+        float wh = (float)w;
+        out = make_float2(wh, (float)(w - (double)wh));
+      }
+    }
+    vals[b] = out;
+  }
+  __syncthreads();
+  // ---- phase C: per chain-locus sums, dlikeA write-back
+  const int w = tid >> 5, lane = tid & 31;
+  if (w < nit) {
+    const ReqDev &R = reqs[r0 + w];
+    const ItemDev it = P.items[R.item];
+    const int nl = 2 * it.n - 1;
+    float2 *dl = reinterpret_cast<float2 *>(P.dlike) + it.dl_off + (size_t)R.ai * nl;
+    ff acc = ff_from(0.f);
+    for (int c = lane; c < nl; c += 32) {
+      float2 v = vals[bstart[w] + c];
+      dl[c] = v;
+      if (v.x != -INFINITY) acc = ff_add(acc, ffc(v));
+    }
+    acc = warp_sum_ff(acc);
+    if (lane == 0) {
+      double res = zero[w] ? -DBL_MAX : ff_to_double(acc);
+      result[r0 + w] = res;
+      status[r0 + w] = zero[w] ? IMA_EVAL_SW_ZERO : IMA_EVAL_OK;
+      P.pdg_new[R.item] = res;
+    }
   }
 }
 
@@ -350,7 +410,7 @@ void launch_sw_fast(const Pools &P, const ReqDev *reqs, int nreq, double *result
                     int32_t *status, cudaStream_t st)
 {
   if (nreq <= 0) return;
-  k_sw_fast<<<nreq, SW_BS, 0, st>>>(P, reqs, result, status);
+  k_sw_fast<<<(nreq + SW_IPC - 1) / SW_IPC, SW_FAST_BS, 0, st>>>(P, reqs, nreq, result, status);
 }
 
 void launch_sw_fp64(const Pools &P, const ReqDev *reqs, int nreq, double *result,

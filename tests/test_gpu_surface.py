@@ -40,3 +40,31 @@ def test_surface_fp64_exact_vs_oracle():
         qo, eo = O.jointp(rows, 5, 8, 3, pts[k], modeltype=0, lognorm=lognorm)
         assert abs(q[k] - qo) <= 1e-12 * abs(qo)
         assert abs(ess[k] - eo) <= 1e-9 * eo
+
+
+@pytest.mark.parametrize("mt", [0, 1, 2])
+def test_surface_fast_split_precision_vs_oracle(mt):
+    """Screen + exact float-float recomputation: within 2e-9 relative of the
+    exact FP64 log-sum-exp (the target is 1e-7); what remains is the FP32 exp
+    of each term's offset from the running maximum."""
+    rng = np.random.default_rng(31 + mt)
+    rows, lognorm, off = synth.surface_stats(rng, 20000, 5, 8, 2)
+    pts = synth.surface_points(rng, 150)
+    ctx = ctx_with([("sw", 2, 1)])
+    ln = lognorm if mt == 0 else None
+    ctx.surface_load(rows, 5, 8, 3, lognorm=ln)
+    q, ess = ctx.surface_eval(pts, modeltype=mt, method=api.SURF_FAST)
+    for k in range(0, len(pts), 7):
+        qo, eo = O.jointp(rows, 5, 8, 3, pts[k], modeltype=mt, lognorm=ln)
+        assert abs(q[k] - qo) <= 2e-9 * abs(qo), (k, q[k], qo)
+        assert abs(ess[k] - eo) <= 1e-4 * eo
+
+
+def test_surface_fast_two_populations_golden_rows():
+    d = load("golden_jointp.npz")
+    rows, pts = d["a_rows"], d["a_pts"]
+    ctx = ctx_with([("sw", 2, 1)])
+    ctx.surface_load(rows, 3, 2, 2)
+    q, _ = ctx.surface_eval(pts, modeltype=0, method=api.SURF_FAST)
+    want = [O.jointp(rows, 3, 2, 2, x)[0] for x in pts]
+    np.testing.assert_allclose(q, want, rtol=2e-9)
