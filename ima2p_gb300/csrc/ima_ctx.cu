@@ -38,7 +38,7 @@ struct Batch {
   int32_t *d_st = nullptr;
   std::vector<ReqDev> h_req;
   cudaGraphExec_t graph = nullptr;
-  int maxn_is = 0, maxs_is = 0, maxn_hky = 0, maxn_sw = 0;
+  int maxn_is = 0, maxs_is = 0, maxn_hky = 0, maxs_hky = 0, maxn_sw = 0;
   int cap = 0;  // capacity of the device buffers
 };
 
@@ -100,7 +100,8 @@ struct ima_ctx {
   double *h_len = nullptr;
   double *h_pi = nullptr;
   int32_t *h_al = nullptr;
-  int dirty_lo = INT32_MAX, dirty_hi = -1;
+  int dirty_lo = INT32_MAX, dirty_hi = -1;    // topology, schedule, pi, alleles
+  int tdirty_lo = INT32_MAX, tdirty_hi = -1;  // times and lengths only
   // device pools
   NodeRec *d_nodes = nullptr;
   double *d_t64 = nullptr;
@@ -486,6 +487,25 @@ extern "C" int ima_gpu_set_genealogy(ima_ctx *c, int ci, int li, const int32_t *
   const int item = c->item_of(ci, li);
   const ItemDev &it = c->items[item];
   const int n = it.n, nl = 2 * n - 1;
+  NodeRec *rec = c->h_nodes + it.node_off;
+  // same topology as the resident genealogy: only times and length change
+  bool same = c->has_tree[item] != 0;
+  for (int k = 0; same && k < nl; k++)
+    same = rec[k].up0 == up0[k] && rec[k].up1 == up1[k] && rec[k].down == down[k];
+  if (same) {
+    double L = 0.0;
+    for (int k = 0; k < nl; k++) {
+      double t = time[k];
+      c->h_t64[it.node_off + k] = t;
+      float hi = (float)t;
+      c->h_tff[it.node_off + k] = make_float2(hi, (float)(t - (double)hi));
+      if (down[k] >= 0) L += (up0[k] < 0) ? t : t - time[up0[k]];
+    }
+    c->h_len[item] = (length >= 0.0) ? length : L;
+    c->tdirty_lo = std::min(c->tdirty_lo, item);
+    c->tdirty_hi = std::max(c->tdirty_hi, item);
+    return IMA_OK;
+  }
   // validate the topology: tips have no daughters, internal nodes two, one root
   int root = -1;
   for (int k = 0; k < nl; k++) {
@@ -504,8 +524,11 @@ extern "C" int ima_gpu_set_genealogy(ima_ctx *c, int ci, int li, const int32_t *
   }
   if (root < n) return c->fail(IMA_ERR_ARG, "no internal root");
   // heights by an explicit post-order from the root; levels = heights 1..H
-  std::vector<int> height(nl, 0), stack;
-  std::vector<uint8_t> seen(nl, 0);
+  thread_local std::vector<int> height, stack, cnt, pos;
+  thread_local std::vector<uint8_t> seen;
+  height.assign(nl, 0);
+  seen.assign(nl, 0);
+  stack.clear();
   stack.push_back(root);
   int visited = 0;
   while (!stack.empty()) {
@@ -528,11 +551,11 @@ extern "C" int ima_gpu_set_genealogy(ima_ctx *c, int ci, int li, const int32_t *
   }
   if (visited != nl) return c->fail(IMA_ERR_ARG, "genealogy is not connected");
   int H = height[root];
-  std::vector<int> cnt(H + 2, 0);
+  cnt.assign(H + 2, 0);
   for (int k = n; k < nl; k++) cnt[height[k]]++;
   int16_t *sch = c->h_sched + it.sched_off;
   int16_t *order = sch, *lstart = sch + (n - 1);
-  std::vector<int> pos(H + 2, 0);
+  pos.assign(H + 2, 0);
   for (int h = 1; h <= H; h++) pos[h + 1] = pos[h] + cnt[h];
   for (int h = 1; h <= H + 1; h++) lstart[h - 1] = (int16_t)pos[h];
   for (int k = n; k < nl; k++) order[pos[height[k]]++] = (int16_t)k;
@@ -597,9 +620,32 @@ extern "C" int ima_gpu_set_alleles(ima_ctx *c, int ci, int li, int ai, const int
   return IMA_OK;
 }
 
+static int flush_times(ima_ctx *c)
+{
+  if (c->tdirty_hi < 0) return IMA_OK;
+  int lo = c->tdirty_lo, hi = c->tdirty_hi;
+  const ItemDev &a = c->items[lo], &b = c->items[hi];
+  size_t n0 = a.node_off, n1 = (size_t)b.node_off + 2 * b.n - 1;
+  cudaStream_t st = c->st;
+  int r = IMA_OK;
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_t64 + n0, c->h_t64 + n0, (n1 - n0) * sizeof(double), cudaMemcpyHostToDevice, st), "times");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_tff + n0, c->h_tff + n0, (n1 - n0) * sizeof(float2), cudaMemcpyHostToDevice, st), "times");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_len + lo, c->h_len + lo, (hi - lo + 1) * sizeof(double), cudaMemcpyHostToDevice, st), "length");
+  c->tdirty_lo = INT32_MAX;
+  c->tdirty_hi = -1;
+  return r;
+}
+
 static int flush(ima_ctx *c)
 {
-  if (c->dirty_hi < 0) return IMA_OK;
+  if (c->dirty_hi < 0) return flush_times(c);
+  // a topology range covers times too; widen it by the time-only range
+  if (c->tdirty_hi >= 0) {
+    c->dirty_lo = std::min(c->dirty_lo, c->tdirty_lo);
+    c->dirty_hi = std::max(c->dirty_hi, c->tdirty_hi);
+    c->tdirty_lo = INT32_MAX;
+    c->tdirty_hi = -1;
+  }
   int lo = c->dirty_lo, hi = c->dirty_hi;
   const ItemDev &a = c->items[lo], &b = c->items[hi];
   size_t n0 = a.node_off, n1 = (size_t)b.node_off + 2 * b.n - 1;
@@ -669,7 +715,7 @@ static int build_batch(ima_ctx *c, Batch &b, int n, const int32_t *ci, const int
   b.nsw = (int)g[2].size();
   b.order.clear();
   b.h_req.clear();
-  b.maxn_is = b.maxs_is = b.maxn_hky = b.maxn_sw = 0;
+  b.maxn_is = b.maxs_is = b.maxn_hky = b.maxs_hky = b.maxn_sw = 0;
   for (int m = 0; m < 3; m++)
     for (int k : g[m]) {
       ReqDev r;
@@ -680,7 +726,7 @@ static int build_batch(ima_ctx *c, Batch &b, int n, const int32_t *ci, const int
       r.par = kappa ? kappa[k] : 1.0;
       const LocusDev &L = c->loci[li[k]].d;
       if (m == 0) { b.maxn_is = std::max(b.maxn_is, L.n); b.maxs_is = std::max(b.maxs_is, L.nsites); }
-      if (m == 1) b.maxn_hky = std::max(b.maxn_hky, L.n);
+      if (m == 1) { b.maxn_hky = std::max(b.maxn_hky, L.n); b.maxs_hky = std::max(b.maxs_hky, L.nsites); }
       if (m == 2) b.maxn_sw = std::max(b.maxn_sw, L.n);
       b.h_req.push_back(r);
       b.order.push_back(k);
@@ -747,7 +793,7 @@ static void enqueue(ima_ctx *c, Batch &b)
     if (b.prec == IMA_PREC_FP64)
       c->launch(IMA_K_HKY_FP64, hky_bytes(c, b), [&] { launch_hky_fp64(P, r, b.nhky, b.maxn_hky, b.d_res + b.nis, b.d_st + b.nis, st); });
     else
-      c->launch(IMA_K_HKY_FAST, hky_bytes(c, b), [&] { launch_hky_fast(P, r, b.nhky, b.maxn_hky, b.d_res + b.nis, b.d_st + b.nis, st); });
+      c->launch(IMA_K_HKY_FAST, hky_bytes(c, b), [&] { launch_hky_fast(P, r, b.nhky, b.maxn_hky, b.maxs_hky, b.d_res + b.nis, b.d_st + b.nis, st); });
   }
   if (b.nsw) {
     const ReqDev *r = b.d_req + b.nis + b.nhky;

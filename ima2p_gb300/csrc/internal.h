@@ -75,8 +75,8 @@ void launch_is_sumlogk(const Pools &P, int item, int locus, int maxn, int maxS, 
                        cudaStream_t st);
 void launch_is(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int maxS, double *result,
                int32_t *status, int32_t *site_node, cudaStream_t st);
-void launch_hky_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, double *result,
-                     int32_t *status, cudaStream_t st);
+void launch_hky_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int maxS,
+                     double *result, int32_t *status, cudaStream_t st);
 void launch_hky_fp64(const Pools &P, const ReqDev *reqs, int nreq, int maxn, double *result,
                      int32_t *status, cudaStream_t st);
 void launch_hky_commit(const Pools &P, const int32_t *items, const uint8_t *accept, int n,

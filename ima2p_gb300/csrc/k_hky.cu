@@ -166,8 +166,15 @@ __device__ __forceinline__ int expo_of(float m)  // floor(log2(m)) for normal m 
 }
 
 // ------------------------------------------------------------------ FP32
-__global__ void __launch_bounds__(HKY_BS) k_hky_fast(Pools P, const ReqDev *reqs,
-                                                     double *result, int32_t *status, int maxnl)
+// Thread mapping: with S <= HKY_BS patterns, HKY_BS / S nodes of a level are
+// processed at once (pattern = tid % S), so no division runs per work item;
+// wider loci loop over pattern blocks.  With CACHE, the partials this launch
+// computes are also kept in shared memory ([internal node][pattern]) and
+// daughters are read from there instead of making an L2 round trip per level.
+template <bool CACHE>
+__global__ void __launch_bounds__(HKY_BS, 12) k_hky_fast(Pools P, const ReqDev *reqs,
+                                                     double *result, int32_t *status, int maxnl,
+                                                     int cache_S)
 {
   extern __shared__ __align__(16) char smem[];
   const ReqDev R = reqs[blockIdx.x];
@@ -183,24 +190,43 @@ __global__ void __launch_bounds__(HKY_BS) k_hky_fast(Pools P, const ReqDev *reqs
   T.dirty = T.fresh + maxnl;
   T.slot = T.dirty + maxnl;
   T.order = reinterpret_cast<int16_t *>(smem + lay.order);
+  float4 *cpart = reinterpret_cast<float4 *>(smem + lay.total);         // [nint][cache_S]
+  int32_t *cexp = reinterpret_cast<int32_t *>(cpart + (size_t)(maxnl / 2) * cache_S);
   __shared__ double red_d[HKY_BS / 32];
   __shared__ long long red_e[HKY_BS / 32];
   __shared__ float spi[4];
   __shared__ float smu;
 
-  load_tree(P, it, R, nlev, T, P.slot32);
+  const int tid = threadIdx.x;
+  const bool full = (R.e[0] == -1);
+  for (int k = tid; k < nl; k += HKY_BS) {
+    T.nd[k] = P.nodes[it.node_off + k];
+    T.slot[k] = P.slot32[it.node_off + k];
+    T.dirty[k] = 0;
+    T.fresh[k] = full ? 1 : 0;
+  }
+  for (int k = tid; k < nint + nlev + 1; k += HKY_BS) T.order[k] = P.sched[it.sched_off + k];
   T.lstart = T.order + nint;
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     const double *pid = P.pi + 4 * (size_t)R.item;
-    double mu = R.u / ((double)L.totsites * standfactor(pid, R.par));
-    smu = (float)mu;
+    smu = (float)(R.u / ((double)L.totsites * standfactor(pid, R.par)));
     for (int j = 0; j < 4; j++) spi[j] = (float)pid[j];
   }
   __syncthreads();
-  // transition matrices of every branch that feeds a recomputed node
+  if (!full && tid == 0) {  // the reference's propagation rule, bottom-up
+    for (int q = 0; q < 4; q++)
+      if (R.e[q] >= 0 && R.e[q] < nl) T.dirty[R.e[q]] = 1;
+    for (int k = 0; k < nint; k++) {
+      int node = T.order[k];
+      int a = T.nd[node].up0, b = T.nd[node].up1;
+      T.fresh[node] = (T.dirty[node] || T.dirty[a] || T.dirty[b] || (a >= n && T.fresh[a]) ||
+                       (b >= n && T.fresh[b])) ? 1 : 0;
+    }
+  }
+  if (!full) __syncthreads();
   const float2 *tff = P.tff + it.node_off;
-  float kpa = (float)(R.par - 1.0);
-  for (int c = threadIdx.x; c < nl; c += blockDim.x) {
+  const float kpa = (float)(R.par - 1.0);
+  for (int c = tid; c < nl; c += HKY_BS) {
     int d = T.nd[c].down;
     if (d < 0 || !T.fresh[d]) continue;
     float pil[4] = {spi[0], spi[1], spi[2], spi[3]};
@@ -212,80 +238,122 @@ __global__ void __launch_bounds__(HKY_BS) k_hky_fast(Pools P, const ReqDev *reqs
   float4 *part = P.part + it.part_off;
   int32_t *pexp = P.pexp + it.part_off;
   const int8_t *seq = P.seq + L.seq_off;
+  // (node slot, pattern) of this thread
+  const bool narrow = S <= HKY_BS;
+  const int jstep = narrow ? HKY_BS / S : 1;
+  const int js = narrow ? tid / S : 0;
+  const int is = narrow ? tid - js * S : tid;
+  const int istep = narrow ? S : HKY_BS;  // narrow: one pattern per thread
+  const bool active = !narrow || js < jstep;
   for (int lv = 0; lv < nlev; lv++) {
-    int beg = T.lstart[lv], cnt = T.lstart[lv + 1] - beg;
-    for (int w = threadIdx.x; w < cnt * S; w += blockDim.x) {
-      int node = T.order[beg + w / S];
-      int i = w - (w / S) * S;
-      if (!T.fresh[node]) continue;
-      float v[2][4];
-      int e = 0;
+    const int beg = T.lstart[lv], cnt = T.lstart[lv + 1] - beg;
+    if (active) {
+      for (int jj = js; jj < cnt; jj += jstep) {
+        const int node = T.order[beg + jj];
+        if (!T.fresh[node]) continue;
+        const int c0 = T.nd[node].up0, c1 = T.nd[node].up1;
+        const float4 *P0 = reinterpret_cast<const float4 *>(Pm + 16 * c0);
+        const float4 *P1 = reinterpret_cast<const float4 *>(Pm + 16 * c1);
+        for (int i = is; i < S; i += istep) {
+          float v[2][4];
+          int e = 0;
 #pragma unroll
-      for (int h = 0; h < 2; h++) {
-        int c = h ? T.nd[node].up1 : T.nd[node].up0;
-        const float *Pc = Pm + 16 * c;
-        if (c < n) {
-          int s = seq[(size_t)c * S + i];
+          for (int h = 0; h < 2; h++) {
+            const int c = h ? c1 : c0;
+            const float4 *Pc = h ? P1 : P0;
+            if (c < n) {
+              int st = seq[(size_t)c * S + i];
+              const float *Pf = reinterpret_cast<const float *>(Pc);
 #pragma unroll
-          for (int j = 0; j < 4; j++) v[h][j] = Pc[j * 4 + s];
-        } else {
-          int rs = T.fresh[c] ? 1 - T.slot[c] : T.slot[c];
-          size_t idx = rs * slot_stride + (size_t)(c - n) * S + i;
-          float4 Lc = part[idx];
-          e += pexp[idx];
+              for (int j = 0; j < 4; j++) v[h][j] = Pf[j * 4 + st];
+            } else {
+              float4 Lc;
+              if (CACHE && T.fresh[c]) {
+                size_t ci = (size_t)(c - n) * cache_S + i;
+                Lc = cpart[ci];
+                e += cexp[ci];
+              } else {
+                int rs = T.fresh[c] ? 1 - T.slot[c] : T.slot[c];
+                size_t idx = rs * slot_stride + (size_t)(c - n) * S + i;
+                Lc = part[idx];
+                e += pexp[idx];
+              }
 #pragma unroll
-          for (int j = 0; j < 4; j++)
-            v[h][j] = Pc[j * 4 + 0] * Lc.x + Pc[j * 4 + 1] * Lc.y + Pc[j * 4 + 2] * Lc.z +
-                      Pc[j * 4 + 3] * Lc.w;
+              for (int j = 0; j < 4; j++) {
+                float4 pr = Pc[j];
+                v[h][j] = pr.x * Lc.x + pr.y * Lc.y + pr.z * Lc.z + pr.w * Lc.w;
+              }
+            }
+          }
+          float4 ov = make_float4(v[0][0] * v[1][0], v[0][1] * v[1][1], v[0][2] * v[1][2],
+                                  v[0][3] * v[1][3]);
+          // rescale by an exact 2^40 only when the largest entry drops below
+          // 2^-40: products of two daughters then stay above 2^-80 (normal)
+          const float m = fmaxf(fmaxf(ov.x, ov.y), fmaxf(ov.z, ov.w));
+          if (m < 9.094947e-13f) {
+            const float up = 1.0995116e12f;  // 2^40
+            ov.x *= up; ov.y *= up; ov.z *= up; ov.w *= up;
+            e -= 40;
+            if (m * up < 9.094947e-13f) {  // very small value: normalise exactly
+              const float mm = m * up;
+              const int k = (mm > 0.f) ? expo_of(mm) : 0;
+              const float sc = pow2f(-k);
+              ov.x *= sc; ov.y *= sc; ov.z *= sc; ov.w *= sc;
+              e += k;
+            }
+          }
+          const size_t widx = (1 - T.slot[node]) * slot_stride + (size_t)(node - n) * S + i;
+          part[widx] = ov;
+          pexp[widx] = e;
+          if (CACHE) {
+            size_t ci = (size_t)(node - n) * cache_S + i;
+            cpart[ci] = ov;
+            cexp[ci] = e;
+          }
         }
       }
-      float o0 = v[0][0] * v[1][0], o1 = v[0][1] * v[1][1];
-      float o2 = v[0][2] * v[1][2], o3 = v[0][3] * v[1][3];
-      float m = fmaxf(fmaxf(o0, o1), fmaxf(o2, o3));
-      if (m < 1e-30f) {  // keep the exponent extraction in the normal range
-        o0 *= 1.8446744e19f; o1 *= 1.8446744e19f; o2 *= 1.8446744e19f; o3 *= 1.8446744e19f;
-        m *= 1.8446744e19f;
-        e -= 64;
-      }
-      int k = expo_of(m);
-      float sc = pow2f(-k);
-      size_t widx = (1 - T.slot[node]) * slot_stride + (size_t)(node - n) * S + i;
-      part[widx] = make_float4(o0 * sc, o1 * sc, o2 * sc, o3 * sc);
-      pexp[widx] = e + k;
     }
     __syncthreads();
   }
 
   // root: sum_i mult_i * (log(sum_j pi_j L_j) + scale_i)
-  int root = T.order[nint - 1];
-  int rs = T.fresh[root] ? 1 - T.slot[root] : T.slot[root];
+  const int root = T.order[nint - 1];
+  const int rs = T.fresh[root] ? 1 - T.slot[root] : T.slot[root];
   const int32_t *mult = P.mult + L.mult_off;
   double acc = 0.0;
   long long acce = 0;
-  for (int i = threadIdx.x; i < S; i += blockDim.x) {
-    size_t idx = rs * slot_stride + (size_t)(root - n) * S + i;
-    float4 Lr = part[idx];
+  for (int i = tid; i < S; i += HKY_BS) {
+    float4 Lr;
+    int er;
+    if (CACHE && T.fresh[root]) {
+      size_t ci = (size_t)(root - n) * cache_S + i;
+      Lr = cpart[ci];
+      er = cexp[ci];
+    } else {
+      size_t idx = rs * slot_stride + (size_t)(root - n) * S + i;
+      Lr = part[idx];
+      er = pexp[idx];
+    }
     float f = spi[0] * Lr.x + spi[1] * Lr.y + spi[2] * Lr.z + spi[3] * Lr.w;
     int k = expo_of(f);
     float mant = f * pow2f(-k);
     int mlt = mult[i];
     acc += (double)mlt * (double)logf(mant);
-    acce += (long long)mlt * (long long)(pexp[idx] + k);
+    acce += (long long)mlt * (long long)(er + k);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     acc += __shfl_xor_sync(0xffffffffu, acc, o);
     acce += __shfl_xor_sync(0xffffffffu, acce, o);
   }
-  if ((threadIdx.x & 31) == 0) {
-    red_d[threadIdx.x >> 5] = acc;
-    red_e[threadIdx.x >> 5] = acce;
+  if ((tid & 31) == 0) {
+    red_d[tid >> 5] = acc;
+    red_e[tid >> 5] = acce;
   }
-  // recomputed flags for the commit step
-  for (int k = threadIdx.x; k < nl; k += blockDim.x)
-    P.fresh32[it.node_off + k] = (k >= n) ? T.fresh[k] : 0;
+  // recomputed marks for the commit step
+  for (int k = tid; k < nl; k += HKY_BS) P.fresh32[it.node_off + k] = (k >= n) ? T.fresh[k] : 0;
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     double s = 0.0;
     long long se = 0;
     for (int w = 0; w < HKY_BS / 32; w++) { s += red_d[w]; se += red_e[w]; }
@@ -434,14 +502,27 @@ size_t hky_smem(int maxn, size_t elem) { return hky_layout(2 * maxn - 1, elem).t
 
 }  // namespace
 
-void launch_hky_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, double *result,
-                     int32_t *status, cudaStream_t st)
+// Partials stay in shared memory when the largest chain-locus of the batch
+// fits in this budget (keeps >= 3 CTAs per SM).
+constexpr size_t HKY_CACHE_BUDGET = 64 * 1024;
+
+void launch_hky_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int maxS,
+                     double *result, int32_t *status, cudaStream_t st)
 {
   if (nreq <= 0) return;
-  size_t sm = hky_smem(maxn, sizeof(float));
-  if (sm > 48 * 1024)
-    cudaFuncSetAttribute(k_hky_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_hky_fast<<<nreq, HKY_BS, sm, st>>>(P, reqs, result, status, 2 * maxn - 1);
+  const int maxnl = 2 * maxn - 1;
+  size_t base = hky_smem(maxn, sizeof(float));
+  size_t cache = (size_t)(maxnl / 2) * maxS * (sizeof(float4) + sizeof(int32_t));
+  if (cache <= HKY_CACHE_BUDGET) {
+    size_t sm = base + cache;
+    if (sm > 48 * 1024)
+      cudaFuncSetAttribute(k_hky_fast<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_hky_fast<true><<<nreq, HKY_BS, sm, st>>>(P, reqs, result, status, maxnl, maxS);
+  } else {
+    if (base > 48 * 1024)
+      cudaFuncSetAttribute(k_hky_fast<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)base);
+    k_hky_fast<false><<<nreq, HKY_BS, base, st>>>(P, reqs, result, status, maxnl, 0);
+  }
 }
 
 void launch_hky_fp64(const Pools &P, const ReqDev *reqs, int nreq, int maxn, double *result,

@@ -94,3 +94,31 @@ def test_hky_batch_many_chains_vs_oracle():
     r32, _ = ctx.eval(ci, li, u, kap, precision=api.PREC_FAST)
     np.testing.assert_allclose(r64, want, rtol=1e-12)
     np.testing.assert_allclose(r32, want, rtol=HKY_FP32_RTOL)
+
+
+def test_hky_large_locus_uses_global_partials():
+    """A chain-locus whose partials exceed the shared-memory cache (100 copies,
+    3000 bp) takes the global-memory path; full and dirty-node evaluations
+    agree with the oracle."""
+    rng = np.random.default_rng(13)
+    g = synth.two_pop_tree(rng, 50, 50, theta=10.0, mig=0.2, tsplit=1.5)
+    loc = synth.hky_data(rng, g, 3000, 1.0, 4.0, rng.dirichlet([5] * 4))
+    assert (loc.seq.shape[0] - 1) * loc.seq.shape[1] * 20 > 64 * 1024
+    ctx = ctx_with([("hky", loc)])
+    ctx.set_pi(0, 0, loc.pi)
+    ctx.set_genealogy(0, 0, g)
+    st = O.HKYState(*loc.seq.shape)
+    want = st.likelihood(loc, g, 1.0, 4.0)
+    st.accept()
+    got = ctx.eval([0], [0], [1.0], [4.0])[0][0]
+    ctx.commit([0], [0], [1])
+    assert abs(got - want) <= HKY_FP32_RTOL * abs(want)
+    k = g.n + 7
+    h = g.copy()
+    a, b = int(h.up0[k]), int(h.up1[k])
+    lo = max(h.time[h.up0[a]] if h.up0[a] >= 0 else 0.0, h.time[h.up0[b]] if h.up0[b] >= 0 else 0.0)
+    h.time[a] = h.time[b] = 0.5 * (lo + h.time[a])
+    ctx.set_genealogy(0, 0, h)
+    got = ctx.eval([0], [0], [1.0], [4.0], edits=[[k, -1, -1, -1]])[0][0]
+    want = st.likelihood(loc, h, 1.0, 4.0, (k, -1, -1, -1))
+    assert abs(got - want) <= HKY_FP32_RTOL * abs(want)
