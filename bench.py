@@ -282,15 +282,19 @@ def run_ours(args):
 
 
 # --------------------------------------------------------- CPU baselines
-def _oracle_items(wl):
+def _oracle_items(wl, limit=None):
+    """(locus spec, genealogy, u, kappa/tr, alleles) of the workload's chain-loci;
+    with `limit`, an even sample of that many."""
     from oracle import pyoracle as O
 
-    items = []
     ci, li = wl.pairs()
-    for c, l in zip(ci, li):
-        spec = wl.loci[l]
-        g = wl.trees[(int(c), int(l))]
-        items.append((spec, g, float(wl.u[c, l]), float(wl.par[c, l]), wl.alleles.get((int(c), int(l)))))
+    idx = np.arange(len(ci))
+    if limit is not None and limit < len(idx):
+        idx = np.linspace(0, len(idx) - 1, limit).astype(int)
+    items = []
+    for k in idx:
+        c, l = int(ci[k]), int(li[k])
+        items.append((wl.loci[l], wl.tree(c, l), float(wl.u[c, l]), float(wl.par[c, l]), wl.allele(c, l)))
     return O, items
 
 
@@ -311,7 +315,7 @@ def _eval_item(O, it, cache):
 def cpu_baseline(wl, seconds):
     """The oracle (a C restatement of the reference) on one host core over a
     bounded sample of the workload's chain-loci."""
-    O, items = _oracle_items(wl)
+    O, items = _oracle_items(wl, limit=20000)
     cache = {}
     n = 0
     t0 = time.perf_counter()
@@ -324,42 +328,72 @@ def cpu_baseline(wl, seconds):
                       % (n, dt, len(items))}
 
 
+_REF = {}
+
+
+def _ref_init(counter, workload, limit, ncores):
+    """Worker set-up: this worker's share of a bounded sample of the workload."""
+    from ima2p_gb300 import workloads
+
+    with counter.get_lock():
+        k = counter.value
+        counter.value += 1
+    wl = workloads.make(workload)
+    O, items = _oracle_items(wl, limit=limit)
+    _REF["O"], _REF["items"] = O, items[k::ncores]
+
+
+def _ref_step(min_seconds):
+    """Evaluate this worker's share, repeated until min_seconds have passed."""
+    cache = {}
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        for it in _REF["items"]:
+            _eval_item(_REF["O"], it, cache)
+        n += len(_REF["items"])
+        if not _REF["items"] or time.perf_counter() - t0 >= min_seconds:
+            return n
+
+
 def run_reference(args):
+    """The reference's CPU path on every host core: the oracle (a C
+    restatement of the reference functions) in one process per core, each on
+    its share of a bounded sample of the workload's chain-loci."""
+    import multiprocessing as mp
+
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     from ima2p_gb300 import workloads
 
-    wl = workloads.make(args.workload)
-    O, items = _oracle_items(wl)
+    if args.workload == "surface":
+        print(json.dumps({"impl": "reference", "unavailable": "surface reference arm not provided; "
+                          "see cpu_baseline of the surface line"}))
+        return
     cores = os.cpu_count() or 1
-    chunks = [items[k::cores] for k in range(cores)]
-
-    def work(chunk):
-        cache = {}
-        for it in chunk:
-            _eval_item(O, it, cache)
-        return len(chunk)
-
-    # one step = a bounded sample: every core evaluates its share of at most
-    # `cap` chain-loci (ctypes calls release the GIL, so threads run in parallel)
-    cap = max(cores, min(len(items), args.ref_cap))
-    sample = [c[: max(1, cap // cores)] for c in chunks]
-    done = sum(len(c) for c in sample)
-    times = []
-    with ThreadPoolExecutor(cores) as ex:
+    wl = workloads.make(args.workload)
+    nall = wl.nchains * wl.nloci
+    limit = min(nall, max(args.ref_cap, cores))
+    ctx = mp.get_context("spawn")
+    counter = ctx.Value("i", 0)
+    with ctx.Pool(cores, initializer=_ref_init, initargs=(counter, args.workload, limit, cores)) as pool:
+        times = []
+        done = 0
         for s in range(args.warmup + args.steps):
             t0 = time.perf_counter()
-            list(ex.map(work, sample))
+            done = sum(pool.map(_ref_step, [0.05] * cores, chunksize=1))
             if s >= args.warmup:
                 times.append(time.perf_counter() - t0)
     v = done / statistics.median(times)
-    desc = "%d of the workload's %d chain-loci per step, %d threads" % (done, len(items), cores)
+    wl_desc = wl.describe
+    desc = ("%d chain-locus evaluations per step (a %d-pair sample of the workload's %d, repeated "
+            "for >= 50 ms), %d processes" % (done, limit, nall, cores))
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": round(v, 1), "unit": "evals/s", "n_gpus": 0,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * statistics.median(times), 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
-        "data": "synthetic", "config": {"workload": wl.describe},
+        "data": "synthetic", "config": {"workload": wl_desc},
         "cpu_baseline": {"value": round(v, 1), "unit": "evals/s", "cores": cores, "kind": "port",
                          "sample": desc},
         "e2e": {"value": round(v, 1), "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

@@ -48,13 +48,20 @@ struct PendingTiming {
   double bytes;
 };
 
+// Zeroed device allocation.  The zeroing is queued on the context stream so
+// that it is ordered before every later copy or kernel on that stream (a
+// plain cudaMemset would run on the legacy stream, which a non-blocking
+// stream does not wait for).
 template <typename T>
-T *dev_alloc(size_t count, size_t &total)
+T *dev_alloc(size_t count, size_t &total, cudaStream_t st)
 {
   if (count == 0) count = 1;
   void *p = nullptr;
   if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) return nullptr;
-  cudaMemset(p, 0, count * sizeof(T));
+  if (cudaMemsetAsync(p, 0, count * sizeof(T), st) != cudaSuccess) {
+    cudaFree(p);
+    return nullptr;
+  }
   total += count * sizeof(T);
   return static_cast<T *>(p);
 }
@@ -264,7 +271,7 @@ extern "C" int ima_gpu_create(int device, ima_ctx **out)
     delete c;
     return IMA_ERR_CUDA;
   }
-  c->d_flag = dev_alloc<int>(64, c->dev_bytes);
+  c->d_flag = dev_alloc<int>(64, c->dev_bytes, c->st);
   *out = c;
   return IMA_OK;
 }
@@ -411,35 +418,35 @@ extern "C" int ima_gpu_set_chains(ima_ctx *c, int nruns, int chains_per_run)
   c->npart = part;
   c->npart64 = part64;
   size_t &B = c->dev_bytes;
-  c->d_loci = dev_alloc<LocusDev>(ld.size(), B);
-  c->d_seq = dev_alloc<int8_t>(seq.size(), B);
-  c->d_mult = dev_alloc<int32_t>(mult.size(), B);
-  c->d_sumlogk = dev_alloc<double>(c->nloci, B);
-  c->d_items = dev_alloc<ItemDev>(c->nitems, B);
-  c->d_nodes = dev_alloc<NodeRec>(nodes, B);
-  c->d_t64 = dev_alloc<double>(nodes, B);
-  c->d_tff = dev_alloc<float2>(nodes, B);
-  c->d_slot32 = dev_alloc<uint8_t>(nodes, B);
-  c->d_fresh32 = dev_alloc<uint8_t>(nodes, B);
-  c->d_sched = dev_alloc<int16_t>(sched, B);
-  c->d_nlev = dev_alloc<int32_t>(c->nitems, B);
-  c->d_len = dev_alloc<double>(c->nitems, B);
-  c->d_pi = dev_alloc<double>(4 * (size_t)c->nitems, B);
-  c->d_al = dev_alloc<int32_t>(al, B);
-  c->d_dlike = dev_alloc<double>(al, B);
-  c->d_part = dev_alloc<float4>(part, B);
-  c->d_pexp = dev_alloc<int32_t>(part, B);
-  c->d_pdg = dev_alloc<double>(c->nitems, B);
-  c->d_pdg_new = dev_alloc<double>(c->nitems, B);
-  c->d_beta = dev_alloc<double>(c->nchains, B);
-  c->d_allbetas = dev_alloc<double>(c->nchains, B);
-  c->d_probg = dev_alloc<double>(c->nchains, B);
-  c->d_S = dev_alloc<double>(c->nchains, B);
-  c->d_swapcount = dev_alloc<int32_t>((size_t)c->nruns * c->cpr * c->cpr, B);
-  c->d_tempcount = dev_alloc<int32_t>((size_t)c->nruns * c->cpr * c->cpr, B);
-  c->d_used = dev_alloc<int32_t>(c->nruns, B);
-  c->d_swap0ok = dev_alloc<int32_t>(c->nruns, B);
-  c->d_ctr = dev_alloc<unsigned long long>(c->nruns, B);
+  c->d_loci = dev_alloc<LocusDev>(ld.size(), B, c->st);
+  c->d_seq = dev_alloc<int8_t>(seq.size(), B, c->st);
+  c->d_mult = dev_alloc<int32_t>(mult.size(), B, c->st);
+  c->d_sumlogk = dev_alloc<double>(c->nloci, B, c->st);
+  c->d_items = dev_alloc<ItemDev>(c->nitems, B, c->st);
+  c->d_nodes = dev_alloc<NodeRec>(nodes, B, c->st);
+  c->d_t64 = dev_alloc<double>(nodes, B, c->st);
+  c->d_tff = dev_alloc<float2>(nodes, B, c->st);
+  c->d_slot32 = dev_alloc<uint8_t>(nodes, B, c->st);
+  c->d_fresh32 = dev_alloc<uint8_t>(nodes, B, c->st);
+  c->d_sched = dev_alloc<int16_t>(sched, B, c->st);
+  c->d_nlev = dev_alloc<int32_t>(c->nitems, B, c->st);
+  c->d_len = dev_alloc<double>(c->nitems, B, c->st);
+  c->d_pi = dev_alloc<double>(4 * (size_t)c->nitems, B, c->st);
+  c->d_al = dev_alloc<int32_t>(al, B, c->st);
+  c->d_dlike = dev_alloc<double>(al, B, c->st);
+  c->d_part = dev_alloc<float4>(part, B, c->st);
+  c->d_pexp = dev_alloc<int32_t>(part, B, c->st);
+  c->d_pdg = dev_alloc<double>(c->nitems, B, c->st);
+  c->d_pdg_new = dev_alloc<double>(c->nitems, B, c->st);
+  c->d_beta = dev_alloc<double>(c->nchains, B, c->st);
+  c->d_allbetas = dev_alloc<double>(c->nchains, B, c->st);
+  c->d_probg = dev_alloc<double>(c->nchains, B, c->st);
+  c->d_S = dev_alloc<double>(c->nchains, B, c->st);
+  c->d_swapcount = dev_alloc<int32_t>((size_t)c->nruns * c->cpr * c->cpr, B, c->st);
+  c->d_tempcount = dev_alloc<int32_t>((size_t)c->nruns * c->cpr * c->cpr, B, c->st);
+  c->d_used = dev_alloc<int32_t>(c->nruns, B, c->st);
+  c->d_swap0ok = dev_alloc<int32_t>(c->nruns, B, c->st);
+  c->d_ctr = dev_alloc<unsigned long long>(c->nruns, B, c->st);
   void *chk[] = {c->d_loci, c->d_seq, c->d_mult, c->d_sumlogk, c->d_items, c->d_nodes, c->d_t64,
                  c->d_tff, c->d_slot32, c->d_fresh32, c->d_sched, c->d_nlev, c->d_len, c->d_pi,
                  c->d_al, c->d_dlike, c->d_part, c->d_pexp, c->d_pdg, c->d_pdg_new, c->d_beta,
@@ -462,12 +469,13 @@ extern "C" int ima_gpu_set_chains(ima_ctx *c, int nruns, int chains_per_run)
   c->dl_fast.assign(al ? al : 1, 0);
   c->has_tree.assign(c->nitems, 0);
   int r = IMA_OK;
-  r = r ? r : c->cuda(cudaMemcpy(c->d_loci, ld.data(), ld.size() * sizeof(LocusDev), cudaMemcpyHostToDevice), "loci");
-  if (!seq.empty()) r = r ? r : c->cuda(cudaMemcpy(c->d_seq, seq.data(), seq.size(), cudaMemcpyHostToDevice), "seq");
-  if (!mult.empty()) r = r ? r : c->cuda(cudaMemcpy(c->d_mult, mult.data(), mult.size() * 4, cudaMemcpyHostToDevice), "mult");
-  r = r ? r : c->cuda(cudaMemcpy(c->d_items, c->items.data(), c->items.size() * sizeof(ItemDev), cudaMemcpyHostToDevice), "items");
-  r = r ? r : c->cuda(cudaMemcpy(c->d_pi, c->h_pi, 4 * sizeof(double) * c->nitems, cudaMemcpyHostToDevice), "pi");
-  return r;
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_loci, ld.data(), ld.size() * sizeof(LocusDev), cudaMemcpyHostToDevice, c->st), "loci");
+  if (!seq.empty()) r = r ? r : c->cuda(cudaMemcpyAsync(c->d_seq, seq.data(), seq.size(), cudaMemcpyHostToDevice, c->st), "seq");
+  if (!mult.empty()) r = r ? r : c->cuda(cudaMemcpyAsync(c->d_mult, mult.data(), mult.size() * 4, cudaMemcpyHostToDevice, c->st), "mult");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_items, c->items.data(), c->items.size() * sizeof(ItemDev), cudaMemcpyHostToDevice, c->st), "items");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_pi, c->h_pi, 4 * sizeof(double) * c->nitems, cudaMemcpyHostToDevice, c->st), "pi");
+  // the host vectors above are about to go out of scope
+  return r ? r : c->cuda(cudaStreamSynchronize(c->st), "set_chains");
 }
 
 // ======================================================================
@@ -679,15 +687,15 @@ static int ensure_fp64_hky(ima_ctx *c)
 {
   if (c->d_part64 || c->npart64 == 0) {
     if (!c->d_slot64) {
-      c->d_slot64 = dev_alloc<uint8_t>(c->nnodes, c->dev_bytes);
-      c->d_fresh64 = dev_alloc<uint8_t>(c->nnodes, c->dev_bytes);
+      c->d_slot64 = dev_alloc<uint8_t>(c->nnodes, c->dev_bytes, c->st);
+      c->d_fresh64 = dev_alloc<uint8_t>(c->nnodes, c->dev_bytes, c->st);
     }
     return IMA_OK;
   }
-  c->d_part64 = dev_alloc<double>(4 * c->npart64, c->dev_bytes);
-  c->d_psf64 = dev_alloc<double>(c->npart64, c->dev_bytes);
-  c->d_slot64 = dev_alloc<uint8_t>(c->nnodes, c->dev_bytes);
-  c->d_fresh64 = dev_alloc<uint8_t>(c->nnodes, c->dev_bytes);
+  c->d_part64 = dev_alloc<double>(4 * c->npart64, c->dev_bytes, c->st);
+  c->d_psf64 = dev_alloc<double>(c->npart64, c->dev_bytes, c->st);
+  c->d_slot64 = dev_alloc<uint8_t>(c->nnodes, c->dev_bytes, c->st);
+  c->d_fresh64 = dev_alloc<uint8_t>(c->nnodes, c->dev_bytes, c->st);
   if (!c->d_part64 || !c->d_psf64 || !c->d_slot64 || !c->d_fresh64)
     return c->fail(IMA_ERR_NOMEM, "FP64 partial likelihood pools (%zu doubles) do not fit", 5 * c->npart64);
   return IMA_OK;
@@ -708,6 +716,14 @@ static int build_batch(ima_ctx *c, Batch &b, int n, const int32_t *ci, const int
     if (!c->has_tree[c->item_of(ci[k], li[k])]) return c->fail(IMA_ERR_STATE, "request %d: chain %d locus %d has no genealogy", k, ci[k], li[k]);
     g[L.model].push_back(k);
   }
+  // largest chain-loci first inside each model (longest-processing-time
+  // order: the big ones start in the first wave, small ones fill the tail)
+  auto cost = [&](int k) {
+    const LocusDev &L = c->loci[li[k]].d;
+    return L.model == IMA_MODEL_HKY ? (long long)(L.n - 1) * L.nsites : (long long)L.n;
+  };
+  for (int m = 1; m < 3; m++)
+    std::stable_sort(g[m].begin(), g[m].end(), [&](int a, int b) { return cost(a) > cost(b); });
   b.n = n;
   b.prec = prec;
   b.nis = (int)g[0].size();
@@ -737,8 +753,8 @@ static int build_batch(ima_ctx *c, Batch &b, int n, const int32_t *ci, const int
   }
   if (!c->d_slot64 && b.nhky) {
     // the commit kernel touches both slot sets; keep the FP64 marks allocated
-    c->d_slot64 = dev_alloc<uint8_t>(c->nnodes, c->dev_bytes);
-    c->d_fresh64 = dev_alloc<uint8_t>(c->nnodes, c->dev_bytes);
+    c->d_slot64 = dev_alloc<uint8_t>(c->nnodes, c->dev_bytes, c->st);
+    c->d_fresh64 = dev_alloc<uint8_t>(c->nnodes, c->dev_bytes, c->st);
   }
   if (b.cap < n) {
     // the previous capacity may still be read by queued work
@@ -747,9 +763,9 @@ static int build_batch(ima_ctx *c, Batch &b, int n, const int32_t *ci, const int
     cudaFree(b.d_res);
     cudaFree(b.d_st);
     size_t &B = c->dev_bytes;
-    b.d_req = dev_alloc<ReqDev>(n, B);
-    b.d_res = dev_alloc<double>(n, B);
-    b.d_st = dev_alloc<int32_t>(n, B);
+    b.d_req = dev_alloc<ReqDev>(n, B, c->st);
+    b.d_res = dev_alloc<double>(n, B, c->st);
+    b.d_st = dev_alloc<int32_t>(n, B, c->st);
     if (!b.d_req || !b.d_res || !b.d_st) {
       b.cap = 0;
       return c->fail(IMA_ERR_NOMEM, "batch buffers");
@@ -963,8 +979,8 @@ static int commit(ima_ctx *c, int n, const int32_t *ci, const int32_t *li, const
     cudaStreamSynchronize(c->st);
     cudaFree(c->d_citems);
     cudaFree(c->d_cacc);
-    c->d_citems = dev_alloc<int32_t>(n, c->dev_bytes);
-    c->d_cacc = dev_alloc<uint8_t>(n, c->dev_bytes);
+    c->d_citems = dev_alloc<int32_t>(n, c->dev_bytes, c->st);
+    c->d_cacc = dev_alloc<uint8_t>(n, c->dev_bytes, c->st);
     if (!c->d_citems || !c->d_cacc) return c->fail(IMA_ERR_NOMEM, "commit buffers");
     c->ccap = n;
   }
@@ -1132,7 +1148,7 @@ extern "C" int ima_gpu_swapchains(ima_ctx *c, int swaptries, int include_probg, 
     if (need > c->uni_cap) {
       cudaStreamSynchronize(c->st);
       cudaFree(c->d_uni);
-      c->d_uni = dev_alloc<double>(need, c->dev_bytes);
+      c->d_uni = dev_alloc<double>(need, c->dev_bytes, c->st);
       if (!c->d_uni) return c->fail(IMA_ERR_NOMEM, "uniform buffer");
       c->uni_cap = need;
     }
@@ -1193,10 +1209,10 @@ extern "C" int ima_gpu_surface_load(ima_ctx *c, int G, int rowlen, const float *
   cudaFree(c->d_rows);
   cudaFree(c->d_lognorm);
   c->d_lognorm = nullptr;
-  c->d_rows = dev_alloc<float>((size_t)G * rowlen, c->dev_bytes);
+  c->d_rows = dev_alloc<float>((size_t)G * rowlen, c->dev_bytes, c->st);
   if (!c->d_rows) return c->fail(IMA_ERR_NOMEM, "surface rows");
   if (lognorm) {
-    c->d_lognorm = dev_alloc<double>(G, c->dev_bytes);
+    c->d_lognorm = dev_alloc<double>(G, c->dev_bytes, c->st);
     if (!c->d_lognorm) return c->fail(IMA_ERR_NOMEM, "surface normalisers");
   }
   c->sG = G;
@@ -1215,9 +1231,9 @@ static int surf_points(ima_ctx *c, int npoints)
   cudaFree(c->d_sx);
   cudaFree(c->d_sq);
   cudaFree(c->d_sess);
-  c->d_sx = dev_alloc<double>((size_t)npoints * 32, c->dev_bytes);
-  c->d_sq = dev_alloc<double>(npoints, c->dev_bytes);
-  c->d_sess = dev_alloc<double>(npoints, c->dev_bytes);
+  c->d_sx = dev_alloc<double>((size_t)npoints * 32, c->dev_bytes, c->st);
+  c->d_sq = dev_alloc<double>(npoints, c->dev_bytes, c->st);
+  c->d_sess = dev_alloc<double>(npoints, c->dev_bytes, c->st);
   if (!c->d_sx || !c->d_sq || !c->d_sess) return c->fail(IMA_ERR_NOMEM, "surface point buffers");
   c->spts_cap = npoints;
   return IMA_OK;
@@ -1227,7 +1243,7 @@ static int surf_scratch(ima_ctx *c, size_t bytes)
 {
   if (bytes <= c->sscratch_cap) return IMA_OK;
   cudaFree(c->d_sscratch);
-  c->d_sscratch = dev_alloc<char>(bytes, c->dev_bytes);
+  c->d_sscratch = dev_alloc<char>(bytes, c->dev_bytes, c->st);
   if (!c->d_sscratch) return c->fail(IMA_ERR_NOMEM, "surface scratch (%zu bytes)", bytes);
   c->sscratch_cap = bytes;
   return IMA_OK;

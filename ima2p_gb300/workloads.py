@@ -29,11 +29,12 @@ class Workload:
     loci: list            # ("is", seq) | ("hky", HKYLocus) | ("sw", n, 1)
     nruns: int
     cpr: int
-    trees: dict            # (ci, li) -> Genealogy
+    trees: dict            # (ci, li) -> Genealogy (or built on demand, see tree())
     u: np.ndarray          # [nchains, nloci]
     par: np.ndarray        # [nchains, nloci] kappa (HKY) / tr (SW) / unused
-    pi: dict               # (ci, li) -> base frequencies
+    pi: dict               # (ci, li) -> base frequencies (or per locus, see pi_of())
     alleles: dict          # (ci, li) -> int32 [2n-1]
+    lazy: object = None    # optional (base trees, time factors, allele fn) for big runs
 
     @property
     def nchains(self):
@@ -48,21 +49,55 @@ class Workload:
         li = np.tile(np.arange(self.nloci), self.nchains).astype(np.int32)
         return ci, li
 
+    def tree(self, c, l):
+        if self.lazy is None:
+            return self.trees[(c, l)]
+        base, fac, _ = self.lazy
+        g = base[l].copy()
+        keep = g.time >= 0
+        g.time[keep] *= fac[c, l]
+        return g
+
+    def allele(self, c, l):
+        if self.lazy is None:
+            return self.alleles.get((c, l))
+        return self.lazy[2](c, l)
+
     def packed(self):
         """Node arrays of every chain-locus concatenated in pair order."""
         ci, li = self.pairs()
-        gs = [self.trees[(int(c), int(l))] for c, l in zip(ci, li)]
-        cat = lambda f: np.concatenate([getattr(g, f) for g in gs])
-        return ci, li, cat("up0").astype(np.int32), cat("up1").astype(np.int32), \
-            cat("down").astype(np.int32), cat("time")
+        if self.lazy is None:
+            gs = [self.trees[(int(c), int(l))] for c, l in zip(ci, li)]
+            cat = lambda f: np.concatenate([getattr(g, f) for g in gs])
+            return ci, li, cat("up0").astype(np.int32), cat("up1").astype(np.int32), \
+                cat("down").astype(np.int32), cat("time")
+        base, fac, _ = self.lazy
+        nl = np.array([len(g.up0) for g in base])
+        rows = [np.tile(np.concatenate([base[l].up0 for l in range(self.nloci)]), self.nchains)]
+        up0 = rows[0].astype(np.int32)
+        up1 = np.tile(np.concatenate([g.up1 for g in base]), self.nchains).astype(np.int32)
+        down = np.tile(np.concatenate([g.down for g in base]), self.nchains).astype(np.int32)
+        bt = np.concatenate([g.time for g in base])
+        f = np.repeat(fac.reshape(-1), np.tile(nl, self.nchains))
+        t = np.tile(bt, self.nchains)
+        time = np.where(t >= 0, t * f, t)
+        return ci, li, up0, up1, down, time
 
     def upload(self, ctx):
         ci, li, up0, up1, down, time = self.packed()
         ctx.set_genealogies(ci, li, up0, up1, down, time)
-        for (c, l), p in self.pi.items():
-            ctx.set_pi(c, l, p)
-        for (c, l), A in self.alleles.items():
-            ctx.set_alleles(c, l, A)
+        if self.lazy is None:
+            for (c, l), p in self.pi.items():
+                ctx.set_pi(c, l, p)
+            for (c, l), A in self.alleles.items():
+                ctx.set_alleles(c, l, A)
+        else:
+            for l, spec in enumerate(self.loci):
+                for c in range(self.nchains):
+                    if spec[0] == "hky":
+                        ctx.set_pi(c, l, spec[1].pi)
+                    elif spec[0] == "sw":
+                        ctx.set_alleles(c, l, self.allele(c, l))
 
 
 def _loci_u(rng, nloci):
@@ -128,7 +163,7 @@ def make_sw(seed=1003, nloci=100, nch=64, per_pop=30):
 
 def make_mixed(seed=1004, n_hky=200, n_sw=100, nruns=8, cpr=128):
     rng = np.random.default_rng(seed)
-    loci, base, pis, alleles = [], [], {}, {}
+    loci, base, A0s = [], [], {}
     nloci = n_hky + n_sw
     ul = _loci_u(rng, nloci)
     kap = rng.uniform(2.0, 8.0, nloci)
@@ -142,22 +177,21 @@ def make_mixed(seed=1004, n_hky=200, n_sw=100, nruns=8, cpr=128):
             loci.append(("hky", loc))
         else:
             loci.append(("sw", g0.n, 1))
-            base[-1] = (g0, synth.sw_alleles(rng, g0, float(ul[li])))
+            A0s[li] = synth.sw_alleles(rng, g0, float(ul[li]))
     nch = nruns * cpr
-    trees = {}
-    for ci in range(nch):
-        for li in range(nloci):
-            if li < n_hky:
-                trees[(ci, li)] = synth.jitter_times(rng, base[li], 0.15)
-                pis[(ci, li)] = loci[li][1].pi
-            else:
-                g0, A0 = base[li]
-                trees[(ci, li)] = synth.jitter_times(rng, g0, 0.15)
-                alleles[(ci, li)] = _perturb_alleles(rng, g0, A0, g0.n)
+    fac = np.exp(rng.normal(0.0, 0.15, (nch, nloci)))
+
+    def allele(c, l):
+        if l not in A0s:
+            return None
+        r = np.random.default_rng(seed * 7919 + c * 1000 + l)
+        return _perturb_alleles(r, base[l], A0s[l], base[l].n)
+
     par = np.tile(np.where(np.arange(nloci) < n_hky, kap, 1.0), (nch, 1))
     return Workload("mixed", "config4-mixed: 300 loci (200 HKY U(200,3000) bp + 100 SW), U(4,60) copies "
                              "x 3 pops, %d chains x %d runs" % (cpr, nruns),
-                    loci, nruns, cpr, trees, np.tile(ul, (nch, 1)), par, pis, alleles)
+                    loci, nruns, cpr, {}, np.tile(ul, (nch, 1)), par, {}, {},
+                    lazy=(base, fac, allele))
 
 
 def make(name):
