@@ -112,6 +112,20 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def aggregate(total_ms, units, steps, dist=None):
+    """Replicas: every rank ran `units` per step on its own GPU; the job time
+    is the slowest rank's and the value counts every rank's units."""
+    world = 1
+    if dist is not None:
+        import torch
+
+        world = dist.get_world_size()
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    return total_ms, units * steps * world / (total_ms / 1e3)
+
+
 # ------------------------------------------------------------- workloads
 def build_ctx(wl, api):
     ctx = api.Context(0)
@@ -199,13 +213,7 @@ def run_ours(args):
     k1 = ctx.kernel_stats(kind)
     n_launch = ctx.launch_count() - n0  # library kernels only (the L2 flush is a memset)
     ctx.set_profiling(False)
-    total_ms = float(sum(times))
-    if dist:
-        import torch
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = units * args.steps * world / (total_ms / 1e3)
+    total_ms, value = aggregate(float(sum(times)), units, args.steps, dist)
 
     # ---------------- dominant kernel roofline
     kl = k1[0] - k0[0]
@@ -271,6 +279,24 @@ def run_ours(args):
         "gpu_launches": int(n_launch),
         "clocks": clk.summary(),
     }
+    # MC3 swap sweeps of every run on the resident sums (the reference's
+    # default swaptries = max(1, chains / 10)), committed likelihoods as pdg
+    ctx.commit(ci, li, np.ones(units, np.uint8))
+    ctx.set_probg(np.zeros(wl.nchains))
+    ctx.setheat(0.9, 0.8, 1)
+    tries = max(1, wl.cpr // 10)
+    for _ in range(3):
+        ctx.swapchains(tries, True, seed=7)
+    ctx.synchronize()
+    ctx.timer_begin()
+    nsw = 200
+    for _ in range(nsw):
+        ctx.swapchains(tries, True, seed=7)
+    sw_ms = ctx.timer_end() / nsw
+    out["swaps"] = {"runs": wl.nruns, "chains_per_run": wl.cpr, "swaptries": tries,
+                    "ms_per_sweep": round(sw_ms, 5),
+                    "attempts_per_s": round(wl.nruns * tries / (sw_ms / 1e3), 1),
+                    "note": "one launch per sweep: per-chain sums over loci + sequential attempts per run"}
     if rank == 0:
         out["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
         print(json.dumps(out), flush=True)
@@ -405,7 +431,7 @@ def run_surface(args):
     from ima2p_gb300 import api, synth
 
     rng = np.random.default_rng(1005)
-    G, P = 1 << 21, 1 << 16
+    G, P = 1 << args.surface_log2g, 1 << args.surface_log2p
     rows, lognorm, off = synth.surface_stats(rng, G, 5, 8, 2)
     pts = synth.surface_points(rng, P)
     ctx = api.Context(0)
@@ -445,8 +471,9 @@ def run_surface(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+ff",
         "data": "synthetic gsampinf rows with the configured distributions",
-        "config": {"workload": "config5-surface: G=2^21 genealogy summaries, K=48 row width "
-                               "(5 theta, 8 m), P=2^16 points, full model", "global_batch": P,
+        "config": {"workload": "config5-surface: G=2^%d genealogy summaries, K=48 row width "
+                               "(5 theta, 8 m), P=2^%d points, full model"
+                               % (args.surface_log2g, args.surface_log2p), "global_batch": P,
                    "l2": "flushed between timed steps"},
         "e2e": {"value": round(e2e, 1), "unit": "points/s", "h2d_bytes_per_step": int(P * 13 * 8),
                 "d2h_bytes_per_step": int(P * 16)},
@@ -467,7 +494,7 @@ def run_surface(args):
         n += 1
     dt = time.perf_counter() - t0
     out["cpu_baseline"] = {"value": round(n / dt, 3), "unit": "points/s", "cores": 1, "kind": "port",
-                           "sample": "%d points, exact log-sum-exp over all 2^21 genealogies" % n}
+                           "sample": "%d points, exact log-sum-exp over all %d genealogies" % (n, G)}
     print(json.dumps(out), flush=True)
     ctx.close()
 
@@ -481,6 +508,8 @@ def main():
     ap.add_argument("--workload", default="hky", choices=["hky", "sw", "is", "mixed", "surface"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-cap", type=int, default=4096)
+    ap.add_argument("--surface-log2g", type=int, default=21, help="log2 genealogies (config 5: 21)")
+    ap.add_argument("--surface-log2p", type=int, default=16, help="log2 points (config 5: 16)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
