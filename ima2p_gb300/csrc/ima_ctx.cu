@@ -817,7 +817,7 @@ static void enqueue(ima_ctx *c, Batch &b)
     if (b.prec == IMA_PREC_FP64)
       c->launch(IMA_K_SW_FP64, sw_bytes(c, b), [&] { launch_sw_fp64(P, r, b.nsw, b.d_res + off, b.d_st + off, st); });
     else
-      c->launch(IMA_K_SW_FAST, sw_bytes(c, b), [&] { launch_sw_fast(P, r, b.nsw, b.d_res + off, b.d_st + off, st); });
+      c->launch(IMA_K_SW_FAST, sw_bytes(c, b), [&] { launch_sw_fast(P, r, b.nsw, b.maxn_sw, b.d_res + off, b.d_st + off, st); });
   }
 }
 

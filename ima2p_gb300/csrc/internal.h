@@ -81,7 +81,7 @@ void launch_hky_fp64(const Pools &P, const ReqDev *reqs, int nreq, int maxn, dou
                      int32_t *status, cudaStream_t st);
 void launch_hky_commit(const Pools &P, const int32_t *items, const uint8_t *accept, int n,
                        cudaStream_t st);
-void launch_sw_fast(const Pools &P, const ReqDev *reqs, int nreq, double *result,
+void launch_sw_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, double *result,
                     int32_t *status, cudaStream_t st);
 void launch_sw_fp64(const Pools &P, const ReqDev *reqs, int nreq, double *result,
                     int32_t *status, cudaStream_t st);

@@ -194,18 +194,20 @@ __device__ __forceinline__ ff warp_sum_ff(ff v)
 
 constexpr int SW_IPC = 8;        // chain-loci per CTA (one warp reduces each)
 constexpr int SW_FAST_BS = 256;
-constexpr int SW_MAXB = SW_IPC * 512;
+// branch terms (float2) and the |d| >= 2 queue (int16) live in dynamic shared
+// memory sized for the batch's largest chain-locus
 
 // Three phases per CTA of up to 8 chain-loci: (A) every branch through the
 // branch-free core, with |d| >= 2 branches queued; (B) the queued Miller
 // recurrences, packed onto consecutive threads; (C) one warp per chain-locus
 // sums its branch terms in float-float.
 __global__ void __launch_bounds__(SW_FAST_BS) k_sw_fast(Pools P, const ReqDev *reqs, int nreq,
-                                                        double *result, int32_t *status)
+                                                        double *result, int32_t *status, int maxb)
 {
   __shared__ SwTables T;
-  __shared__ float2 vals[SW_MAXB];
-  __shared__ int16_t queue[SW_MAXB];
+  extern __shared__ __align__(16) char sw_smem[];
+  float2 *vals = reinterpret_cast<float2 *>(sw_smem);
+  int16_t *queue = reinterpret_cast<int16_t *>(vals + maxb);
   __shared__ int qn;
   __shared__ int bstart[SW_IPC + 1];
   __shared__ int zero[SW_IPC];
@@ -406,11 +408,15 @@ int sw_init_tables()
   return 0;
 }
 
-void launch_sw_fast(const Pools &P, const ReqDev *reqs, int nreq, double *result,
+void launch_sw_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, double *result,
                     int32_t *status, cudaStream_t st)
 {
   if (nreq <= 0) return;
-  k_sw_fast<<<(nreq + SW_IPC - 1) / SW_IPC, SW_FAST_BS, 0, st>>>(P, reqs, nreq, result, status);
+  const int maxb = SW_IPC * (2 * maxn - 1);
+  const size_t sm = (size_t)maxb * (sizeof(float2) + sizeof(int16_t));
+  if (sm > 48 * 1024)
+    cudaFuncSetAttribute(k_sw_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_sw_fast<<<(nreq + SW_IPC - 1) / SW_IPC, SW_FAST_BS, sm, st>>>(P, reqs, nreq, result, status, maxb);
 }
 
 void launch_sw_fp64(const Pools &P, const ReqDev *reqs, int nreq, double *result,
