@@ -22,11 +22,11 @@ IMA_OK, IMA_ERR_ARG, IMA_ERR_CUDA, IMA_ERR_STATE, IMA_ERR_NOMEM, IMA_ERR_DATA = 
 MODEL_IS, MODEL_HKY, MODEL_SW = 0, 1, 2
 PREC_FAST, PREC_FP64 = 0, 1
 EVAL_OK, EVAL_IS_REJECT, EVAL_IS_FAIL, EVAL_SW_ZERO = 0, 1, 2, 3
-SURF_FAST, SURF_FP64, SURF_COMPAT = 0, 1, 2
+SURF_FAST, SURF_FP64, SURF_COMPAT, SURF_TC = 0, 1, 2, 3
 K_IS, K_IS_SUMLOGK, K_HKY_FAST, K_HKY_FP64, K_SW_FAST, K_SW_FP64, K_SWAP, K_SURF_FAST, \
-    K_SURF_FP64, K_SURF_COMPAT = range(10)
+    K_SURF_FP64, K_SURF_COMPAT, K_SURF_TC = range(11)
 KERNEL_NAMES = ["is", "is_sumlogk", "hky_fast", "hky_fp64", "sw_fast", "sw_fp64", "swap",
-                "surf_fast", "surf_fp64", "surf_compat"]
+                "surf_fast", "surf_fp64", "surf_compat", "surf_tc"]
 REJECT_IS = -1000000000.0
 
 # every symbol the header declares (checked by tests/test_abi.py)
@@ -40,7 +40,7 @@ EXPORTS = [
     "ima_gpu_batch_destroy", "ima_gpu_flush_genealogies", "ima_gpu_setheat", "ima_gpu_get_betas",
     "ima_gpu_set_betas", "ima_gpu_set_pdg", "ima_gpu_get_pdg", "ima_gpu_set_probg",
     "ima_gpu_swapchains", "ima_gpu_get_swapcounts", "ima_gpu_surface_load",
-    "ima_gpu_surface_eval", "ima_gpu_jointp", "ima_gpu_surface_fp64_noalloc",
+    "ima_gpu_surface_eval", "ima_gpu_jointp", "ima_gpu_surface_fp64_noalloc", "ima_gpu_tc_selftest",
     "ima_gpu_timer_begin", "ima_gpu_timer_end",
     "ima_gpu_set_profiling", "ima_gpu_kernel_stats", "ima_gpu_launch_count", "ima_gpu_flush_l2",
     "ima_gpu_memory",
@@ -115,6 +115,7 @@ def _declare(L):
         "ima_gpu_surface_eval": (I, [P, I, P, I, I, P, P]),
         "ima_gpu_jointp": (I, [P, P, I, P, P]),
         "ima_gpu_surface_fp64_noalloc": (I, [P, I, I, I, I, I, P, P, I, I, P, P, P]),
+        "ima_gpu_tc_selftest": (I, [P, C.POINTER(I), C.POINTER(C.c_float)]),
         "ima_gpu_timer_begin": (I, [P]),
         "ima_gpu_timer_end": (I, [P, C.POINTER(C.c_float)]),
         "ima_gpu_set_profiling": (I, [P, I]),
@@ -340,6 +341,12 @@ class Context:
         self._ck(self.lib.ima_gpu_surface_eval(self.h, len(x), _ptr(x), int(modeltype), int(method),
                                                _ptr(q), _ptr(ess)))
         return q, ess
+
+    def tc_selftest(self):
+        bad = I()
+        err = C.c_float()
+        self._ck(self.lib.ima_gpu_tc_selftest(self.h, C.byref(bad), C.byref(err)))
+        return bad.value, err.value
 
     def jointp(self, x, calc_ess=1):
         q = np.zeros(1)

@@ -1284,6 +1284,20 @@ extern "C" int ima_gpu_surface_eval(ima_ctx *c, int npoints, const double *x, in
     c->launch(IMA_K_SURF_FAST, (double)a.G * 27 * 4 + (double)npoints * 27 * 8,
               [&] { lr = launch_surface_fast(a, c->d_sscratch, c->sscratch_cap, c->st); });
     if (lr) return c->fail(IMA_ERR_ARG, "fast surface: unsupported shape (%d)", lr);
+  } else if (method == IMA_SURF_TC) {
+    r = surf_scratch(c, surface_tc_scratch_bytes(a.G, npoints));
+    if (r) return r;
+    int lr = 0;
+    r = c->cuda(cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->st), "flag");
+    if (r) return r;
+    c->launch(IMA_K_SURF_TC, (double)a.G * 32 * 2 + (double)npoints * 27 * 8,
+              [&] { lr = launch_surface_tc(a, c->d_sscratch, c->sscratch_cap, c->d_flag, c->st); });
+    if (lr) return c->fail(IMA_ERR_ARG, "tensor-core surface: unsupported shape (%d)", lr);
+    int flag = 0;
+    r = c->cuda(cudaMemcpyAsync(&flag, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->st), "flag");
+    r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "tensor-core surface");
+    if (r) return r;
+    if (flag) return c->fail(IMA_ERR_TIMEOUT, "tensor-core surface: a pipeline wait ran out (stage %d)", flag);
   } else if (method == IMA_SURF_FP64) {
     r = surf_scratch(c, surface_fp64_scratch_bytes(a.G, npoints));
     if (r) return r;
@@ -1299,6 +1313,20 @@ extern "C" int ima_gpu_surface_eval(ima_ctx *c, int npoints, const double *x, in
   r = r ? r : c->cuda(cudaMemcpyAsync(q, c->d_sq, npoints * 8, cudaMemcpyDeviceToHost, c->st), "q");
   if (ess) r = r ? r : c->cuda(cudaMemcpyAsync(ess, c->d_sess, npoints * 8, cudaMemcpyDeviceToHost, c->st), "ess");
   return r ? r : c->cuda(cudaStreamSynchronize(c->st), "surface");
+}
+
+extern "C" int ima_gpu_tc_selftest(ima_ctx *c, int *mismatches, float *max_abs_err)
+{
+  if (!c || !mismatches || !max_abs_err) return IMA_ERR_ARG;
+  cudaSetDevice(c->device);
+  int r = surf_scratch(c, (size_t)256 << 10);
+  if (r) return r;
+  int tr = tc_selftest(c->st, c->d_sscratch, c->sscratch_cap, mismatches, max_abs_err);
+  c->launches += 3;
+  if (tr) return c->fail(IMA_ERR_CUDA, "tensor-core self-test failed to run (%d): %s", tr,
+                         cudaGetErrorString(cudaGetLastError()));
+  if (*mismatches < 0) return c->fail(IMA_ERR_TIMEOUT, "tensor-core self-test: a wait ran out (%d)", -*mismatches);
+  return IMA_OK;
 }
 
 extern "C" int ima_gpu_jointp(ima_ctx *c, const double *x, int calc_ess, double *effective_n, double *q)

@@ -142,23 +142,6 @@ __global__ void __launch_bounds__(BS) k_surf_screen_fp32(SurfPrep S, int npoints
   }
 }
 
-// exact maximum over an even sample of SURF_SEED genealogies, per point
-__global__ void k_surf_seed(SurfPrep S, int npoints)
-{
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= npoints) return;
-  float2 phi[SURF_K];
-  for (int k = 0; k < S.K; k++) phi[k] = S.phiff[(size_t)p * SURF_K + k];
-  float best = -INFINITY;
-  const int n = min(SURF_SEED, S.G);
-  for (int i = 0; i < n; i++) {
-    int g = (int)(((long long)i * S.G) / n);
-    ff y = surf_exact(S, g, S.sT + g, S.Gpad, phi);
-    best = fmaxf(best, y.hi);
-  }
-  S.seed[p] = best;
-}
-
 }  // namespace
 
 size_t surface_fast_scratch_bytes(int G, int npoints)
@@ -174,7 +157,7 @@ int launch_surface_fast(const SurfArgs &a, void *scratch, size_t scratch_bytes, 
   char *base = static_cast<char *>(scratch);
   SurfPart *part = surf_prep_carve(&S, base, a.G, a.npoints);
   surf_prep(a, S, false, st);
-  k_surf_seed<<<(a.npoints + 127) / 128, 128, 0, st>>>(S, a.npoints);
+  surf_seed(S, a.npoints, st);
   int nchunks = (a.G + 65535) / 65536;
   if (nchunks > SURF_MAX_CHUNKS) nchunks = SURF_MAX_CHUNKS;
   int chunk = (a.G + nchunks - 1) / nchunks;

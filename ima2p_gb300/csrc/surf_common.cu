@@ -3,6 +3,7 @@
 #include <cuda_bf16.h>
 
 #include "surf_common.cuh"
+#include "tc_ptx.cuh"
 
 namespace {
 
@@ -52,9 +53,10 @@ __global__ void k_prep_rows(SurfArgs a, SurfPrep S)
   }
   float bh = (float)bias;
   S.biasff[g] = make_float2(bh, (float)(bias - (double)bh));
-  if (S.sbf) {
-    __nv_bfloat16 *row = reinterpret_cast<__nv_bfloat16 *>(S.sbf + (size_t)g * SURF_KP);
-    for (int k = 0; k < SURF_KP; k++) row[k] = __float2bfloat16_rn(col[k]);
+  if (S.sbf) {  // the MMA's tile layout, 256 genealogies per tile
+    char *tile = reinterpret_cast<char *>(S.sbf) + (size_t)(g / SURF_TC_N) * SURF_TC_N * SURF_KP * 2;
+    for (int k = 0; k < SURF_KP; k++)
+      *reinterpret_cast<__nv_bfloat16 *>(tile + tc::tile_off(g % SURF_TC_N, k)) = __float2bfloat16_rn(col[k]);
   }
 }
 
@@ -89,7 +91,10 @@ __global__ void k_prep_points(SurfArgs a, SurfPrep S, int npad)
       if (k < SURF_K) S.phiff[(size_t)p * SURF_K + k] = make_float2(v, (float)(phi[k] - (double)v));
     }
     mag += __uint_as_float(S.colmax[k]) * fabsf(v);
-    if (S.pbf) reinterpret_cast<__nv_bfloat16 *>(S.pbf)[(size_t)p * SURF_KP + k] = __float2bfloat16_rn(v);
+    if (S.pbf) {  // the MMA's tile layout, 128 points per tile
+      char *tile = reinterpret_cast<char *>(S.pbf) + (size_t)(p / SURF_TC_M) * SURF_TC_M * SURF_KP * 2;
+      *reinterpret_cast<__nv_bfloat16 *>(tile + tc::tile_off(p % SURF_TC_M, k)) = __float2bfloat16_rn(v);
+    }
   }
   if (p < a.npoints) S.mag[p] = mag;
 }
@@ -169,6 +174,28 @@ void surf_prep(const SurfArgs &a, SurfPrep &S, bool bf16, cudaStream_t st)
   k_prep_rows<<<S.Gpad / 256, 256, 0, st>>>(a, S);
   int npad = (a.npoints + 255) / 256 * 256;
   k_prep_points<<<npad / 256, 256, 0, st>>>(a, S, npad);
+}
+
+// exact maximum over an even sample of SURF_SEED genealogies, per point
+__global__ void k_surf_seed(SurfPrep S, int npoints)
+{
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npoints) return;
+  float2 phi[SURF_K];
+  for (int k = 0; k < S.K; k++) phi[k] = S.phiff[(size_t)p * SURF_K + k];
+  float best = -INFINITY;
+  const int n = min(SURF_SEED, S.G);
+  for (int i = 0; i < n; i++) {
+    int g = (int)(((long long)i * S.G) / n);
+    ff y = surf_exact(S, g, S.sT + g, S.Gpad, phi);
+    best = fmaxf(best, y.hi);
+  }
+  S.seed[p] = best;
+}
+
+void surf_seed(const SurfPrep &S, int npoints, cudaStream_t st)
+{
+  k_surf_seed<<<(npoints + 127) / 128, 128, 0, st>>>(S, npoints);
 }
 
 void surf_merge(const SurfArgs &a, const SurfPart *part, int nchunks, cudaStream_t st)

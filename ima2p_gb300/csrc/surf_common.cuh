@@ -13,6 +13,8 @@ constexpr int SURF_KP = 32;         // screened columns: the terms, the bias, ze
 constexpr int SURF_MAX_CHUNKS = 64;
 constexpr float SURF_MARGIN = 32.0f;  // nats below the running max that still count
 constexpr int SURF_SEED = 256;      // genealogies sampled per point for the seed maximum
+constexpr int SURF_TC_M = 128;      // tensor-core screen: points per A tile
+constexpr int SURF_TC_N = 256;      // tensor-core screen: genealogies per B tile
 
 // Operands prepared once per evaluation (model type and points fixed).
 struct SurfPrep {
@@ -24,8 +26,8 @@ struct SurfPrep {
   float *mag;       // [npoints] sum_k colmax_k |phi_k|: scale of screening errors
   float *seed;      // [npoints] exact max over a sample of genealogies
   unsigned *colmax; // [SURF_KP] max |column| as float bits
-  uint16_t *sbf;    // [Gpad][SURF_KP] bf16 statistics (tensor-core screen)
-  uint16_t *pbf;    // [npoints_pad][SURF_KP] bf16 phi (tensor-core screen)
+  uint16_t *sbf;    // bf16 statistics in 256-row MMA tiles (tensor-core screen)
+  uint16_t *pbf;    // bf16 phi in 128-row MMA tiles (tensor-core screen)
 };
 
 // Per (point, chunk) partial of the online log-sum-exp.
@@ -141,3 +143,4 @@ size_t surf_prep_bytes(int G, int npoints);
 SurfPart *surf_prep_carve(SurfPrep *S, char *base, int G, int npoints);
 void surf_prep(const SurfArgs &a, SurfPrep &S, bool bf16, cudaStream_t st);
 void surf_merge(const SurfArgs &a, const SurfPart *part, int nchunks, cudaStream_t st);
+void surf_seed(const SurfPrep &S, int npoints, cudaStream_t st);

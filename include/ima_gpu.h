@@ -189,11 +189,17 @@ int ima_gpu_surface_load(ima_ctx *ctx, int G, int rowlen, const float *gsampinf,
 #define IMA_SURF_FAST 0     /* split-precision contraction + online log-sum-exp */
 #define IMA_SURF_FP64 1     /* FP64 CUDA-core form, exact log-sum-exp           */
 #define IMA_SURF_COMPAT 2   /* the reference's truncated sum (PRANGELOG, eexp)   */
+#define IMA_SURF_TC 3       /* IMA_SURF_FAST with its screen on the tensor cores  */
 /* q = log G - log sum_g exp(p_g(x)) at npoints points x[npoints][nparams];
  * modeltype 0 full, 1 population sizes only, 2 migration only (jointp's
  * nowmodeltype).  ess (may be NULL) = effective number of genealogies. */
 int ima_gpu_surface_eval(ima_ctx *ctx, int npoints, const double *x, int modeltype, int method,
                          double *q, double *ess);
+/* Checks the tensor-core path on this device: one 128 x 256 x 32 bf16 tile of
+ * small integers through TMA, tcgen05.mma and tcgen05.ld, compared element by
+ * element with CUDA cores.  *mismatches = 0 when every element matches. */
+int ima_gpu_tc_selftest(ima_ctx *ctx, int *mismatches, float *max_abs_err);
+
 /* jointp (jointfind.cpp:885-1047) at one point, reference semantics. */
 int ima_gpu_jointp(ima_ctx *ctx, const double *x, int calc_ess, double *effective_n, double *q);
 
@@ -237,7 +243,8 @@ int ima_gpu_kernel_stats(ima_ctx *ctx, int kind, long long *launches, double *ms
 #define IMA_K_SURF_FAST 7
 #define IMA_K_SURF_FP64 8
 #define IMA_K_SURF_COMPAT 9
-#define IMA_K_COUNT 10
+#define IMA_K_SURF_TC 10
+#define IMA_K_COUNT 11
 /* Total kernel launches issued by this library on the context. */
 int ima_gpu_launch_count(ima_ctx *ctx, long long *n);
 /* Write a device buffer larger than L2 (evicts resident data). */

@@ -1,0 +1,35 @@
+"""The tensor-core path: a bf16 tile through TMA, tcgen05.mma and tcgen05.ld
+checked element by element against CUDA cores, then the tensor-core-screened
+surface against the exact FP64 log-sum-exp of the oracle (2e-9 relative, the
+tolerance of the CUDA-core screen)."""
+import numpy as np
+import pytest
+
+from ima2p_gb300 import api, synth
+from oracle import pyoracle as O
+from tests._gpu import ctx_with
+
+pytestmark = pytest.mark.gpu
+
+
+def test_tcgen05_tile_is_exact():
+    ctx = ctx_with([("sw", 2, 1)])
+    bad, err = ctx.tc_selftest()
+    assert bad == 0 and err == 0.0, (bad, err)
+
+
+@pytest.mark.parametrize("mt", [0, 1, 2])
+def test_surface_tensor_core_screen_vs_oracle(mt):
+    rng = np.random.default_rng(41 + mt)
+    rows, lognorm, off = synth.surface_stats(rng, 30000, 5, 8, 2)
+    pts = synth.surface_points(rng, 300)
+    ctx = ctx_with([("sw", 2, 1)])
+    ln = lognorm if mt == 0 else None
+    ctx.surface_load(rows, 5, 8, 3, lognorm=ln)
+    q, ess = ctx.surface_eval(pts, modeltype=mt, method=api.SURF_TC)
+    q2, _ = ctx.surface_eval(pts, modeltype=mt, method=api.SURF_FAST)
+    np.testing.assert_allclose(q, q2, rtol=2e-9)
+    for k in range(0, len(pts), 13):
+        qo, eo = O.jointp(rows, 5, 8, 3, pts[k], modeltype=mt, lognorm=ln)
+        assert abs(q[k] - qo) <= 2e-9 * abs(qo), (k, q[k], qo)
+        assert abs(ess[k] - eo) <= 1e-4 * eo
