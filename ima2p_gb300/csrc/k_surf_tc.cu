@@ -1,14 +1,17 @@
 // k_surf_tc.cu -- tensor-core screen of the L-mode surface (tcgen05, sm_103a).
 //
-// The screen of the split-precision surface (see k_surf_fast.cu) as a bf16
-// GEMM on the 5th-generation tensor cores: D[point][genealogy] =
+// The screen of the split-precision surface (see k_surf_fast.cu) as a
+// split-bf16 GEMM on the 5th-generation tensor cores: D[point][genealogy] =
 // phi(x_point) . s_genealogy over 32 columns (26 statistics, the bias, zero
-// padding), accumulated in FP32 in tensor memory.
+// padding), with both operands split into bf16 hi + lo planes and
+// D = phi_hi s_hi + phi_lo s_hi + phi_hi s_lo accumulated in FP32 in tensor
+// memory (three K = 32 products, six tcgen05.mma per tile): about 16
+// significant bits per product, so few terms reach the exact recomputation.
 //
 // One CTA owns 128 points (the A operand, loaded once) and streams tiles of
 // 256 genealogies (the B operand) through a 4-stage shared-memory ring filled
 // by 1-D bulk copies (the TMA engine; the prepared operand is already in the
-// tile layout, so one copy per tile).  One thread issues two K=16 MMAs per
+// tile layout, so one copy per tile).  One thread issues six K=16 MMAs per
 // tile into one of two 256-column TMEM accumulators; eight epilogue warps
 // drain the other accumulator with tcgen05.ld -- warps 4-7 take genealogy
 // columns 0-127, warps 8-11 columns 128-255, each thread one point (its TMEM
@@ -31,17 +34,22 @@ namespace {
 constexpr int TC_M = SURF_TC_M;  // points per CTA (TMEM lanes)
 constexpr int TC_N = SURF_TC_N;  // genealogies per tile (accumulator columns)
 constexpr int TC_STAGES = 4;
-constexpr uint32_t A_BYTES = TC_M * SURF_KP * 2;   // 8 KB
-constexpr uint32_t B_BYTES = TC_N * SURF_KP * 2;   // 16 KB
+constexpr uint32_t A_PLANE = TC_M * SURF_KP * 2;   // 8 KB
+constexpr uint32_t B_PLANE = TC_N * SURF_KP * 2;   // 16 KB
+constexpr uint32_t A_BYTES = 2 * A_PLANE;          // hi + lo
+constexpr uint32_t B_BYTES = 2 * B_PLANE;
 // shared memory requested per CTA: more than half an SM's, so one CTA holds
 // an SM and its 512 TMEM columns at a time
-constexpr size_t TC_SMEM = 120 * 1024;
+constexpr size_t TC_SMEM = 152 * 1024;
 constexpr uint32_t WAIT_LIMIT = 1u << 24;          // polls before a wait gives up
 constexpr int TC_THREADS = 384;                    // warp 0 loads, warp 1 MMAs, 4-11 epilogue
 
-// bf16 screen error: both operands rounded to bf16 (2^-8 each), FP32
-// accumulation of 32 products; bounded by 0.0086 of sum_k colmax_k |phi_k|.
-constexpr float BF16_SCREEN_ERR = 0.0086f;
+// split-bf16 screen error, relative to sum_k colmax_k |phi_k| (u = 2^-8, the
+// bf16 unit roundoff): the dropped lo*lo product and the residuals of both
+// splits, <= 3 u^2 = 4.6e-5 per product, plus the FP32 accumulation of 96
+// products even if every addition truncates, <= 96 * 2^-23 = 1.1e-5;
+// bounded with margin by 1e-4.
+constexpr float BF16_SCREEN_ERR = 1e-4f;
 
 struct TcSmem {
   uint64_t full[TC_STAGES], empty[TC_STAGES], accfull[2], accempty[2], abar;
@@ -131,10 +139,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       tc::fence_after_sync();
       const uint32_t baddr = tc::smem_u32(bufB + s * B_BYTES);
       const uint32_t d = tmem + (uint32_t)(a * TC_N);
+      // phi_hi s_hi + phi_lo s_hi + phi_hi s_lo, each K = 32 as two K = 16
+      const uint32_t ap[3] = {aaddr, aaddr + A_PLANE, aaddr};
+      const uint32_t bp[3] = {baddr, baddr, baddr + B_PLANE};
 #pragma unroll
-      for (int kh = 0; kh < 2; kh++)  // K = 32 as two K = 16 instructions
-        tc::mma_bf16(d, tc::sdesc(aaddr + kh * 256, 128, 512), tc::sdesc(baddr + kh * 256, 128, 512),
-                     idesc, kh);
+      for (int t = 0; t < 3; t++)
+#pragma unroll
+        for (int kh = 0; kh < 2; kh++)
+          tc::mma_bf16(d, tc::sdesc(ap[t] + kh * 256, 128, 512), tc::sdesc(bp[t] + kh * 256, 128, 512),
+                       idesc, (t | kh) ? 1u : 0u);
       tc::mma_commit(&sh.empty[s]);   // stage s free once these MMAs have read it
       tc::mma_commit(&sh.accfull[a]); // accumulator a ready for the epilogue
       done = i + 1;
@@ -218,6 +231,7 @@ __global__ void k_tc_merge(SurfArgs a, const SurfPart *part, int nchunks)
 __global__ void __launch_bounds__(128, 1) k_tc_selftest(const uint16_t *A, const uint16_t *B, float *D,
                                                          int *err)
 {
+  constexpr uint32_t A_BYTES = A_PLANE, B_BYTES = B_PLANE;
   extern __shared__ __align__(1024) char smem[];
   char *bufA = smem, *bufB = smem + A_BYTES;
   __shared__ uint64_t bar, mbar;
@@ -342,6 +356,7 @@ int launch_surface_tc(const SurfArgs &a, void *scratch, size_t scratch_bytes, in
 
 int tc_selftest(cudaStream_t st, void *scratch, size_t bytes, int *h_bad, float *h_maxerr)
 {
+  constexpr uint32_t A_BYTES = A_PLANE, B_BYTES = B_PLANE;
   // scratch: A (8 KB) | B (16 KB) | D (128 KB) | bad, maxerr, err
   const size_t need = A_BYTES + B_BYTES + (size_t)TC_M * TC_N * 4 + 16;
   if (bytes < need) return 3;

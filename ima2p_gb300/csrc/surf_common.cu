@@ -53,10 +53,15 @@ __global__ void k_prep_rows(SurfArgs a, SurfPrep S)
   }
   float bh = (float)bias;
   S.biasff[g] = make_float2(bh, (float)(bias - (double)bh));
-  if (S.sbf) {  // the MMA's tile layout, 256 genealogies per tile
-    char *tile = reinterpret_cast<char *>(S.sbf) + (size_t)(g / SURF_TC_N) * SURF_TC_N * SURF_KP * 2;
-    for (int k = 0; k < SURF_KP; k++)
-      *reinterpret_cast<__nv_bfloat16 *>(tile + tc::tile_off(g % SURF_TC_N, k)) = __float2bfloat16_rn(col[k]);
+  if (S.sbf) {  // the MMA's tile layout, 256 genealogies per tile: hi plane, then lo plane
+    const size_t plane = (size_t)SURF_TC_N * SURF_KP * 2;
+    char *tile = reinterpret_cast<char *>(S.sbf) + (size_t)(g / SURF_TC_N) * 2 * plane;
+    for (int k = 0; k < SURF_KP; k++) {
+      __nv_bfloat16 hi = __float2bfloat16_rn(col[k]);
+      __nv_bfloat16 lo = __float2bfloat16_rn(col[k] - __bfloat162float(hi));
+      *reinterpret_cast<__nv_bfloat16 *>(tile + tc::tile_off(g % SURF_TC_N, k)) = hi;
+      *reinterpret_cast<__nv_bfloat16 *>(tile + plane + tc::tile_off(g % SURF_TC_N, k)) = lo;
+    }
   }
 }
 
@@ -91,9 +96,13 @@ __global__ void k_prep_points(SurfArgs a, SurfPrep S, int npad)
       if (k < SURF_K) S.phiff[(size_t)p * SURF_K + k] = make_float2(v, (float)(phi[k] - (double)v));
     }
     mag += __uint_as_float(S.colmax[k]) * fabsf(v);
-    if (S.pbf) {  // the MMA's tile layout, 128 points per tile
-      char *tile = reinterpret_cast<char *>(S.pbf) + (size_t)(p / SURF_TC_M) * SURF_TC_M * SURF_KP * 2;
-      *reinterpret_cast<__nv_bfloat16 *>(tile + tc::tile_off(p % SURF_TC_M, k)) = __float2bfloat16_rn(v);
+    if (S.pbf) {  // the MMA's tile layout, 128 points per tile: hi plane, then lo plane
+      const size_t plane = (size_t)SURF_TC_M * SURF_KP * 2;
+      char *tile = reinterpret_cast<char *>(S.pbf) + (size_t)(p / SURF_TC_M) * 2 * plane;
+      __nv_bfloat16 hi = __float2bfloat16_rn(v);
+      __nv_bfloat16 lo = __float2bfloat16_rn((float)(phi[k] - (double)__bfloat162float(hi)));
+      *reinterpret_cast<__nv_bfloat16 *>(tile + tc::tile_off(p % SURF_TC_M, k)) = hi;
+      *reinterpret_cast<__nv_bfloat16 *>(tile + plane + tc::tile_off(p % SURF_TC_M, k)) = lo;
     }
   }
   if (p < a.npoints) S.mag[p] = mag;
@@ -132,8 +141,8 @@ size_t surf_prep_bytes(int G, int npoints)
   b += align256(sizeof(float) * npad);
   b += align256(sizeof(float) * npad);
   b += align256(sizeof(unsigned) * SURF_KP);
-  b += align256(sizeof(uint16_t) * SURF_KP * Gpad);
-  b += align256(sizeof(uint16_t) * SURF_KP * npad);
+  b += align256(2 * sizeof(uint16_t) * SURF_KP * Gpad);
+  b += align256(2 * sizeof(uint16_t) * SURF_KP * npad);
   return b;
 }
 
@@ -156,8 +165,8 @@ SurfPart *surf_prep_carve(SurfPrep *S, char *base, int G, int npoints)
   S->mag = reinterpret_cast<float *>(take(sizeof(float) * npad));
   S->seed = reinterpret_cast<float *>(take(sizeof(float) * npad));
   S->colmax = reinterpret_cast<unsigned *>(take(sizeof(unsigned) * SURF_KP));
-  S->sbf = reinterpret_cast<uint16_t *>(take(sizeof(uint16_t) * SURF_KP * Gpad));
-  S->pbf = reinterpret_cast<uint16_t *>(take(sizeof(uint16_t) * SURF_KP * npad));
+  S->sbf = reinterpret_cast<uint16_t *>(take(2 * sizeof(uint16_t) * SURF_KP * Gpad));
+  S->pbf = reinterpret_cast<uint16_t *>(take(2 * sizeof(uint16_t) * SURF_KP * npad));
   return reinterpret_cast<SurfPart *>(base + o);
 }
 

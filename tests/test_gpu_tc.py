@@ -1,7 +1,8 @@
 """The tensor-core path: a bf16 tile through TMA, tcgen05.mma and tcgen05.ld
 checked element by element against CUDA cores, then the tensor-core-screened
 surface against the exact FP64 log-sum-exp of the oracle (2e-9 relative, the
-tolerance of the CUDA-core screen)."""
+tolerance of the CUDA-core screen, plus 3e-7 absolute: the weights
+exp(p - max) are FP32 exponentials, within 2 ulp)."""
 import numpy as np
 import pytest
 
@@ -28,8 +29,8 @@ def test_surface_tensor_core_screen_vs_oracle(mt):
     ctx.surface_load(rows, 5, 8, 3, lognorm=ln)
     q, ess = ctx.surface_eval(pts, modeltype=mt, method=api.SURF_TC)
     q2, _ = ctx.surface_eval(pts, modeltype=mt, method=api.SURF_FAST)
-    np.testing.assert_allclose(q, q2, rtol=2e-9)
+    np.testing.assert_allclose(q, q2, rtol=2e-9, atol=3e-7)
     for k in range(0, len(pts), 13):
         qo, eo = O.jointp(rows, 5, 8, 3, pts[k], modeltype=mt, lognorm=ln)
-        assert abs(q[k] - qo) <= 2e-9 * abs(qo), (k, q[k], qo)
+        assert abs(q[k] - qo) <= 2e-9 * abs(qo) + 3e-7, (k, q[k], qo)
         assert abs(ess[k] - eo) <= 1e-4 * eo
