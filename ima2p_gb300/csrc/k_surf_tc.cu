@@ -9,14 +9,28 @@
 // significant bits per product, so few terms reach the exact recomputation.
 //
 // One CTA owns 128 points (the A operand, loaded once) and streams tiles of
-// 256 genealogies (the B operand) through a 4-stage shared-memory ring filled
-// by 1-D bulk copies (the TMA engine; the prepared operand is already in the
-// tile layout, so one copy per tile).  One thread issues six K=16 MMAs per
-// tile into one of two 256-column TMEM accumulators; eight epilogue warps
-// drain the other accumulator with tcgen05.ld -- warps 4-7 take genealogy
-// columns 0-127, warps 8-11 columns 128-255, each thread one point (its TMEM
-// lane) -- and send every term within MARGIN + screen error of the point's
-// best maximum to the exact float-float recomputation.
+// 128 genealogies (the B operand) through an 8-stage shared-memory ring
+// filled by 1-D bulk copies (the TMA engine; the prepared operand is already
+// in the tile layout, so one copy per tile).  Warp roles:
+//   warp 0     one thread issues the bulk copies;
+//   warp 1     one thread issues six K=16 MMAs per tile into one of four
+//              128-column TMEM accumulators, so it can run three tiles ahead
+//              of the slowest draining warp;
+//   warps 4-19 drain the accumulators with tcgen05.ld -- warp w reads TMEM
+//              lane quarter w % 4 (32 points, one per thread) and 32
+//              genealogy columns -- and a max tree over each thread's 32
+//              values decides whether any lies within MARGIN + screen error
+//              of the point's best maximum; such candidates go to a ring;
+//   warps 2-3  take the rings' candidates 32 at a time, recompute them
+//              exactly (phi of every point is staged in shared memory) and
+//              fold them into per-point log-sum-exp states.
+// The drain never waits for the exact recomputation, so one warp's
+// candidates do not hold the accumulator.  The threshold is a lower bound on
+// the point's maximum less MARGIN and the screen error: a screened value less
+// its error bound is such a lower bound, so the threshold is tight from the
+// first tile without any exact work, and exact values raise it further.  The
+// bound is shared by the warps of the CTA (shared memory) and by all
+// genealogy chunks of the point (global memory).
 //
 // Every wait is bounded: a wait that runs out sets the error word, the CTA
 // stops issuing work, waits (bounded) for the copies and MMAs it started,
@@ -24,6 +38,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "surf_common.cuh"
@@ -33,16 +48,19 @@ namespace {
 
 constexpr int TC_M = SURF_TC_M;  // points per CTA (TMEM lanes)
 constexpr int TC_N = SURF_TC_N;  // genealogies per tile (accumulator columns)
-constexpr int TC_STAGES = 4;
+constexpr int NACC = 512 / TC_N;     // TMEM accumulators of TC_N columns
 constexpr uint32_t A_PLANE = TC_M * SURF_KP * 2;   // 8 KB
-constexpr uint32_t B_PLANE = TC_N * SURF_KP * 2;   // 16 KB
+constexpr uint32_t B_PLANE = TC_N * SURF_KP * 2;
 constexpr uint32_t A_BYTES = 2 * A_PLANE;          // hi + lo
 constexpr uint32_t B_BYTES = 2 * B_PLANE;
+constexpr int TC_STAGES = (128 * 1024) / B_BYTES;  // operand ring stages (128 KB of B tiles)
+static_assert(TC_STAGES >= NACC, "a stage's done barrier also marks its accumulator ready");
 // shared memory requested per CTA: more than half an SM's, so one CTA holds
-// an SM and its 512 TMEM columns at a time
-constexpr size_t TC_SMEM = 152 * 1024;
-constexpr uint32_t WAIT_LIMIT = 1u << 24;          // polls before a wait gives up
-constexpr int TC_THREADS = 384;                    // warp 0 loads, warp 1 MMAs, 4-11 epilogue
+// an SM and its 512 TMEM columns at a time (the operand ring, phi of the
+// CTA's points, the candidate rings and the per-point log-sum-exp states)
+constexpr size_t TC_SMEM = 212 * 1024;
+constexpr uint32_t WAIT_LIMIT = 1u << 24;          // try_wait rounds before a wait gives up
+constexpr int TC_THREADS = 640;                    // roles: see the file comment
 
 // split-bf16 screen error, relative to sum_k colmax_k |phi_k| (u = 2^-8, the
 // bf16 unit roundoff): the dropped lo*lo product and the residuals of both
@@ -51,10 +69,27 @@ constexpr int TC_THREADS = 384;                    // warp 0 loads, warp 1 MMAs,
 // bounded with margin by 1e-4.
 constexpr float BF16_SCREEN_ERR = 1e-4f;
 
+constexpr int PHI_STRIDE = SURF_K + 1;   // float2 per point row of staged phi (padded)
+constexpr int EPI_WARPS = 16;            // warps 4-19 drain the accumulators
+constexpr int COL_GROUPS = EPI_WARPS / 4;          // accumulator column groups (TMEM lane quarters x 4)
+constexpr int GROUP_COLS = TC_N / COL_GROUPS;      // columns per epilogue warp and tile
+constexpr int REF_WARPS = 2;             // warps 2-3 recompute candidates exactly
+constexpr int RING = 1024;               // candidate slots per refine warp
+
 struct TcSmem {
-  uint64_t full[TC_STAGES], empty[TC_STAGES], accfull[2], accempty[2], abar;
+  // full[s]: B tile of stage s landed; done[s]: the MMAs of the tile in stage
+  // s completed (stage free, accumulator ready); accempty[a]: accumulator a
+  // drained by every epilogue warp
+  uint64_t full[TC_STAGES], done[TC_STAGES], accempty[NACC], abar;
   uint32_t tmem;
   int err;
+  int epi_done;                       // epilogue warps that have finished
+  unsigned head[REF_WARPS];           // slots reserved so far in each ring
+  int ring[REF_WARPS][RING];          // candidates: genealogy << 7 | point; -1 = free
+  float2 res[REF_WARPS][32];          // exact values of one batch
+  SurfPart lse[TC_M];                 // log-sum-exp state per point
+  unsigned best[TC_M];                // best lower bound on the point's maximum (ordered bits)
+  float2 phi[TC_M * PHI_STRIDE];      // float-float phi of the CTA's points
 };
 
 __device__ __forceinline__ void set_err(int *err_shared, int *err_global, int code)
@@ -63,8 +98,84 @@ __device__ __forceinline__ void set_err(int *err_shared, int *err_global, int co
   atomicCAS(err_global, 0, code);
 }
 
+// hand one candidate (point pl, genealogy g) to the refine warp owning pl
+__device__ __forceinline__ void push_candidate(TcSmem &sh, int *gerr, int pl, int g)
+{
+  const int r = pl & 1;
+  const unsigned slot = atomicAdd(&sh.head[r], 1u);
+  volatile int *dst = &sh.ring[r][slot % RING];
+  // the slot is free once the refine warp has taken its previous occupant
+  for (uint32_t it = 0; *dst != -1; it++) {
+    if (it > WAIT_LIMIT || *(volatile int *)&sh.err) {
+      set_err(&sh.err, gerr, 6);
+      return;
+    }
+    __nanosleep(32);
+  }
+  *dst = (g << 7) | pl;
+}
+
+// Refine warp r: takes its ring's candidates 32 at a time, recomputes each
+// exactly (one per lane) and folds it into its point's log-sum-exp state --
+// lanes holding the same point form a group whose lowest lane folds the
+// group's values.  It stops when every epilogue warp has finished and the
+// ring is drained.
+__device__ void refine_loop(const SurfPrep &S, TcSmem &sh, int *gerr, int r, int lane, int ptile, int npoints)
+{
+  for (unsigned next = 0;; next += 32) {
+    const unsigned slot = next + lane;
+    volatile int *src = &sh.ring[r][slot % RING];
+    int e = -1;
+    for (uint32_t it = 0;; it++) {
+      e = *src;
+      if (e != -1) break;
+      if (*(volatile int *)&sh.epi_done == EPI_WARPS && slot >= *(volatile unsigned *)&sh.head[r]) break;
+      if (*(volatile int *)&sh.err) break;
+      if (it > WAIT_LIMIT) {
+        set_err(&sh.err, gerr, 7);
+        break;
+      }
+      __nanosleep(64);
+    }
+    const bool have = e != -1;
+    int owner = TC_M + lane;  // unique dummy for idle lanes
+    if (have) {
+      *src = -1;
+      owner = e & (TC_M - 1);
+      const int g = e >> 7;
+      ff y = surf_exact(S, g, S.sT + g, S.Gpad, &sh.phi[owner * PHI_STRIDE]);
+      sh.res[r][lane] = make_float2(y.hi, y.lo);
+    }
+    __syncwarp();
+    const unsigned grp = __match_any_sync(0xffffffffu, owner);
+    if (have && lane == __ffs(grp) - 1) {
+      LseState L;
+      L.unpack(sh.lse[owner]);
+      const float b0 = ord2f(*(volatile unsigned *)&sh.best[owner]);
+      float b = b0;
+      for (unsigned m = grp; m; m &= m - 1) {
+        const float2 v = sh.res[r][__ffs(m) - 1];
+        L.add(ff_make(v.x, v.y));
+        b = fmaxf(b, v.x);
+      }
+      sh.lse[owner] = L.pack();
+      // publish an improved maximum to the drain and the other chunks
+      if (b > b0) {
+        atomicMax(&sh.best[owner], f2ord(b));
+        atomicMax(&S.best[ptile * TC_M + owner], f2ord(b));
+      }
+    }
+    __syncwarp();
+    if (!__any_sync(0xffffffffu, have)) break;
+  }
+  (void)npoints;
+}
+
+// stride > 0: max-only pass over genealogy tiles 0, stride, 2 stride, ...
+// that only raises the shared per-point lower bounds (no candidates, no
+// partials); stride == 0: the full pass over every tile.
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    k_surf_tc(SurfPrep S, int npoints, int tiles_per_chunk, SurfPart *part, int *gerr)
+    k_surf_tc(SurfPrep S, int npoints, int tiles_per_chunk, int stride, SurfPart *part, int *gerr)
 {
   extern __shared__ __align__(1024) char smem[];
   char *bufA = smem;
@@ -72,22 +183,36 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   TcSmem &sh = *reinterpret_cast<TcSmem *>(smem + A_BYTES + TC_STAGES * B_BYTES);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ptile = blockIdx.x;
-  const int ntiles_all = S.Gpad / TC_N;
+  const bool maxonly = stride > 0;
+  const int step = maxonly ? stride : 1;
+  const int ntiles_all = (S.Gpad / TC_N + step - 1) / step;  // tiles of this pass
   const int t0 = blockIdx.y * tiles_per_chunk, t1 = min(ntiles_all, t0 + tiles_per_chunk);
   const int ntiles = max(0, t1 - t0);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < TC_STAGES; s++) {
       tc::mbar_init(&sh.full[s], 1);
-      tc::mbar_init(&sh.empty[s], 1);
+      tc::mbar_init(&sh.done[s], 1);
     }
-    for (int a = 0; a < 2; a++) {
-      tc::mbar_init(&sh.accfull[a], 1);
-      tc::mbar_init(&sh.accempty[a], 8);  // one arrival per epilogue warp
-    }
+    for (int a = 0; a < NACC; a++) tc::mbar_init(&sh.accempty[a], EPI_WARPS);  // one arrival per epilogue warp
     tc::mbar_init(&sh.abar, 1);
     sh.err = 0;
+    sh.epi_done = 0;
+    for (int r = 0; r < REF_WARPS; r++) sh.head[r] = 0;
     tc::fence_barrier_init();
+  }
+  // every thread stages phi, the rings and the per-point states
+  for (int i = threadIdx.x; i < TC_M * SURF_K; i += TC_THREADS) {
+    const int pl = i / SURF_K, k = i % SURF_K, p = ptile * TC_M + pl;
+    sh.phi[pl * PHI_STRIDE + k] = p < npoints ? S.phiff[(size_t)p * SURF_K + k] : make_float2(0.f, 0.f);
+  }
+  for (int i = threadIdx.x; i < REF_WARPS * RING; i += TC_THREADS) (&sh.ring[0][0])[i] = -1;
+  for (int pl = threadIdx.x; pl < TC_M; pl += TC_THREADS) {
+    LseState L;
+    L.init();
+    sh.lse[pl] = L.pack();
+    const int p = ptile * TC_M + pl;
+    sh.best[pl] = p < npoints ? S.best[p] : f2ord(-INFINITY);
   }
   if (warp == 1) {
     tc::tmem_alloc(&sh.tmem, 512);
@@ -105,13 +230,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     int issued = 0;
     for (int i = 0; i < ntiles; i++) {
       const int s = i % TC_STAGES;
-      if (i >= TC_STAGES && !tc::mbar_wait(&sh.empty[s], ((i / TC_STAGES) - 1) & 1, WAIT_LIMIT)) {
+      if (i >= TC_STAGES && !tc::mbar_wait(&sh.done[s], ((i / TC_STAGES) - 1) & 1, WAIT_LIMIT)) {
         set_err(&sh.err, gerr, 1);
         break;
       }
       if (*(volatile int *)&sh.err) break;
       tc::mbar_expect_tx(&sh.full[s], B_BYTES);
-      tc::bulk_g2s(bufB + s * B_BYTES, S.sbf + (size_t)(t0 + i) * (B_BYTES / 2), B_BYTES, &sh.full[s]);
+      tc::bulk_g2s(bufB + s * B_BYTES, S.sbf + (size_t)(t0 + i) * step * (B_BYTES / 2), B_BYTES, &sh.full[s]);
       issued = i + 1;
     }
     // copies this thread started must land before the CTA can leave
@@ -121,88 +246,138 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   } else if (warp == 1 && lane == 0) {
     // --------------------------------------------------------------- MMA
     const uint32_t idesc = tc::idesc_bf16_f32(TC_M, TC_N);
-    const uint32_t aaddr = tc::smem_u32(bufA);
+    // descriptors: the address field counts 16-byte units, so offsets add
+    const uint64_t ad = tc::sdesc(tc::smem_u32(bufA), 128, 512);
+    const uint64_t bd0 = tc::sdesc(tc::smem_u32(bufB), 128, 512);
     bool ok = tc::mbar_wait(&sh.abar, 0, WAIT_LIMIT);
     if (!ok) set_err(&sh.err, gerr, 2);
-    int done = 0;
+    int ndone = 0;
     for (int i = 0; ok && i < ntiles; i++) {
-      const int s = i % TC_STAGES, a = i & 1;
+      const int s = i % TC_STAGES, a = i % NACC;
       if (!tc::mbar_wait(&sh.full[s], (i / TC_STAGES) & 1, WAIT_LIMIT)) {
         set_err(&sh.err, gerr, 3);
         break;
       }
-      if (i >= 2 && !tc::mbar_wait(&sh.accempty[a], ((i >> 1) - 1) & 1, WAIT_LIMIT)) {
+      if (i >= NACC && !tc::mbar_wait(&sh.accempty[a], ((i / NACC) - 1) & 1, WAIT_LIMIT)) {
         set_err(&sh.err, gerr, 4);
         break;
       }
       if (*(volatile int *)&sh.err) break;
       tc::fence_after_sync();
-      const uint32_t baddr = tc::smem_u32(bufB + s * B_BYTES);
       const uint32_t d = tmem + (uint32_t)(a * TC_N);
+      const uint64_t bd = bd0 + (uint64_t)((s * B_BYTES) >> 4);
       // phi_hi s_hi + phi_lo s_hi + phi_hi s_lo, each K = 32 as two K = 16
-      const uint32_t ap[3] = {aaddr, aaddr + A_PLANE, aaddr};
-      const uint32_t bp[3] = {baddr, baddr, baddr + B_PLANE};
+      const uint64_t ap[3] = {ad, ad + (A_PLANE >> 4), ad};
+      const uint64_t bp[3] = {bd, bd, bd + (B_PLANE >> 4)};
 #pragma unroll
       for (int t = 0; t < 3; t++)
 #pragma unroll
         for (int kh = 0; kh < 2; kh++)
-          tc::mma_bf16(d, tc::sdesc(ap[t] + kh * 256, 128, 512), tc::sdesc(bp[t] + kh * 256, 128, 512),
-                       idesc, (t | kh) ? 1u : 0u);
-      tc::mma_commit(&sh.empty[s]);   // stage s free once these MMAs have read it
-      tc::mma_commit(&sh.accfull[a]); // accumulator a ready for the epilogue
-      done = i + 1;
+          tc::mma_bf16(d, ap[t] + kh * 16, bp[t] + kh * 16, idesc, (t | kh) ? 1u : 0u);
+      tc::mma_commit(&sh.done[s]);  // stage s free and accumulator a ready once these complete
+      ndone = i + 1;
     }
-    if (done > 0) tc::mbar_wait(&sh.accfull[(done - 1) & 1], ((done - 1) >> 1) & 1, WAIT_LIMIT);
+    if (ndone > 0) tc::mbar_wait(&sh.done[(ndone - 1) % TC_STAGES], ((ndone - 1) / TC_STAGES) & 1, WAIT_LIMIT);
+  } else if ((warp == 2 || warp == 3) && !maxonly) {
+    // ------------------------------------------------------------ refine
+    refine_loop(S, sh, gerr, warp - 2, lane, ptile, npoints);
   } else if (warp >= 4) {
     // ---------------------------------------------------------- epilogue
+    const int ew = warp - 4;            // epilogue warp
     const int q = warp & 3;             // TMEM lane quarter of this warp
-    const int half = (warp - 4) >> 2;   // genealogy columns [128 half, +128)
+    const int cg = ew >> 2;             // genealogy columns [GROUP_COLS cg, +GROUP_COLS)
     const int pl = q * 32 + lane;       // point within the tile = TMEM lane
     const int p = ptile * TC_M + pl;
     const bool live = p < npoints;
-    float2 phi[SURF_K];
-    float off = 0.f, best = -INFINITY;
-    if (live) {
-      for (int k = 0; k < S.K; k++) phi[k] = S.phiff[(size_t)p * SURF_K + k];
-      off = BF16_SCREEN_ERR * S.mag[p] + SURF_MARGIN;
-      best = S.seed[p];
-    }
-    LseState st;
-    st.init();
+    const float err = live ? BF16_SCREEN_ERR * S.mag[p] : 0.f;  // screen error bound
+    const float off = err + SURF_MARGIN;
+    // lb: a lower bound on the point's maximum -- exact values, and screened
+    // values less their error bound, from any warp of this CTA or any chunk
+    // (the global bound is read one tile ahead)
+    float lb = -INFINITY, published = -INFINITY;
+    unsigned pending = live ? *(volatile unsigned *)&S.best[p] : 0u;
     for (int i = 0; i < ntiles; i++) {
-      const int a = i & 1;
-      if (!tc::mbar_wait(&sh.accfull[a], (i >> 1) & 1, WAIT_LIMIT)) {
+      const int a = i % NACC;
+      if (!tc::mbar_wait(&sh.done[i % TC_STAGES], (i / TC_STAGES) & 1, WAIT_LIMIT)) {
         set_err(&sh.err, gerr, 5);
         break;
       }
       tc::fence_after_sync();
-      const int gbase = (t0 + i) * TC_N + half * 128;
-      const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * TC_N + half * 128);
-#pragma unroll 1
-      for (int c = 0; c < 4; c++) {
-        float v[32];
-        tc::tmem_ld32(tl + c * 32, v);
-        const float thr = best - off;
-        unsigned mask = 0;
+      if (live) {
+        lb = fmaxf(lb, ord2f(pending));
+        pending = *(volatile unsigned *)&S.best[p];
+        lb = fmaxf(lb, ord2f(*(volatile unsigned *)&sh.best[pl]));
+      }
+      const int gbase = (t0 + i) * step * TC_N + cg * GROUP_COLS;
+      const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * TC_N + cg * GROUP_COLS);
+      float mxv;
+      float v[32];
+      if constexpr (GROUP_COLS == 32) {
+        // one load and a max tree; the candidate masks come from the same
+        // registers
+        uint32_t r[32];
+        tc::tmem_ld32_nowait(tl, r);
+        tc::tmem_wait_ld(r);
 #pragma unroll
-        for (int j = 0; j < 32; j++)
-          if (v[j] > thr) mask |= 1u << j;
-        if (!live) mask = 0;
-        while (mask) {
-          const int j = __ffs(mask) - 1;
-          mask &= mask - 1;
-          const int g = gbase + c * 32 + j;
-          if (g >= S.G) continue;
-          ff y = surf_exact(S, g, S.sT + g, S.Gpad, phi);
-          st.add(y);
-          best = fmaxf(best, y.hi);
+        for (int j = 0; j < 32; j++) v[j] = __uint_as_float(r[j]);
+        float mx[16];
+#pragma unroll
+        for (int j = 0; j < 16; j++) mx[j] = fmaxf(v[j], v[j + 16]);
+#pragma unroll
+        for (int w = 8; w >= 1; w >>= 1)
+#pragma unroll
+          for (int j = 0; j < w; j++) mx[j] = fmaxf(mx[j], mx[j + w]);
+        mxv = mx[0];
+      } else {
+        // both loads in flight, one wait, a max tree in place; a passing
+        // value reloads the columns
+        static_assert(GROUP_COLS == 64, "one or two 32-column loads per warp and tile");
+        uint32_t r[64];
+        tc::tmem_ld32_nowait(tl, r);
+        tc::tmem_ld32_nowait(tl + 32, r + 32);
+        tc::tmem_wait_ld(r);
+        tc::reg_fence32(r + 32);
+        float w64[64];
+#pragma unroll
+        for (int j = 0; j < 64; j++) w64[j] = __uint_as_float(r[j]);
+#pragma unroll
+        for (int w = 32; w >= 1; w >>= 1)
+#pragma unroll
+          for (int j = 0; j < w; j++) w64[j] = fmaxf(w64[j], w64[j + w]);
+        mxv = w64[0];
+      }
+      // padded genealogies (g >= G) screen to 0 and must not raise lb
+      if (gbase + GROUP_COLS <= S.G) lb = fmaxf(lb, mxv - err);
+      const float thr = lb - off;
+      const bool hit = live && !maxonly && mxv > thr;
+      if (live && lb > published) {
+        published = lb;
+        atomicMax(&sh.best[pl], f2ord(lb));
+        atomicMax(&S.best[p], f2ord(lb));
+      }
+      if (__any_sync(0xffffffffu, hit)) {
+#pragma unroll 1
+        for (int c = 0; c < GROUP_COLS / 32; c++) {
+          if constexpr (GROUP_COLS != 32) tc::tmem_ld32(tl + c * 32, v);
+          unsigned mask = 0;
+#pragma unroll
+          for (int j = 0; j < 32; j++)
+            if (v[j] > thr) mask |= 1u << j;
+          const int gc = gbase + c * 32, nv = S.G - gc;
+          if (!hit) mask = 0;
+          else if (nv < 32) mask &= nv > 0 ? (1u << nv) - 1u : 0u;
+          for (; mask; mask &= mask - 1) push_candidate(sh, gerr, pl, gc + __ffs(mask) - 1);
         }
       }
       tc::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&sh.accempty[a]);
     }
-    if (live) part[((size_t)p * 2 + half) * gridDim.y + blockIdx.y] = st.pack();
+    __syncwarp();
+    if (lane == 0) {
+      __threadfence_block();
+      atomicAdd(&sh.epi_done, 1);
+    }
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -210,19 +385,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     tc::fence_after_sync();
     tc::tmem_dealloc(tmem, 512);
   }
-}
-
-__global__ void k_tc_merge(SurfArgs a, const SurfPart *part, int nchunks)
-{
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= a.npoints) return;
-  LseState m;
-  m.init();
-  for (int h = 0; h < 2; h++)
-    for (int c = 0; c < nchunks; c++) m.merge(part[((size_t)p * 2 + h) * nchunks + c]);
-  // the FP64 merge kernel reads one partial per (point, chunk)
-  SurfPart *out = const_cast<SurfPart *>(part) + (size_t)a.npoints * 2 * nchunks;
-  out[p] = m.pack();
+  if (threadIdx.x < TC_M && !maxonly) {
+    const int p = ptile * TC_M + threadIdx.x;
+    if (p < npoints) part[(size_t)p * gridDim.y + blockIdx.y] = sh.lse[threadIdx.x];
+  }
 }
 
 // ------------------------------------------------------------ self-test
@@ -326,31 +492,66 @@ __global__ void k_tc_selftest_check(const float *D, int *bad, float *maxerr)
 size_t surface_tc_scratch_bytes(int G, int npoints)
 {
   const int nchunks = SURF_MAX_CHUNKS;
-  return surf_prep_bytes(G, npoints) + ((size_t)npoints * 2 * nchunks + npoints) * sizeof(SurfPart) + 1024;
+  return surf_prep_bytes(G, npoints) + (size_t)npoints * nchunks * sizeof(SurfPart) + 1024;
 }
+
+namespace {
+
+constexpr int PRE_STRIDE = 8;  // tile stride of the max-only pre-pass
+
+// genealogy chunks for a pass over `ntiles` tiles: one CTA holds an SM, so
+// pick the chunk count whose CTA total fills its last wave best (at least
+// 8 tiles per CTA); returns the chunk count, tiles per chunk in *per
+int surf_tc_chunks(int ptiles, int ntiles, int nsm, int *per)
+{
+  const int maxch = std::max(1, std::min(SURF_MAX_CHUNKS, ntiles / 8));
+  int nchunks = 1;
+  *per = ntiles;
+  double best_eff = -1.0;
+  for (int c = 1; c <= maxch; c++) {
+    const int pc = (ntiles + c - 1) / c, cc = (ntiles + pc - 1) / pc;
+    const double waves = (double)ptiles * cc / nsm;
+    const double eff = waves / std::ceil(waves);
+    if (eff > best_eff + 0.02) {  // fewer chunks unless clearly better filled
+      best_eff = eff;
+      nchunks = cc;
+      *per = pc;
+    }
+  }
+  return nchunks;
+}
+
+}  // namespace
 
 int launch_surface_tc(const SurfArgs &a, void *scratch, size_t scratch_bytes, int *d_err, cudaStream_t st)
 {
   if (a.np + a.nm > SURF_K / 2) return 2;
   if (scratch_bytes < surface_tc_scratch_bytes(a.G, a.npoints)) return 3;
+  if (a.G >= (1 << 24)) return 4;  // candidate entries pack the genealogy index into 24 bits
   SurfPrep S;
   SurfPart *part = surf_prep_carve(&S, static_cast<char *>(scratch), a.G, a.npoints);
   surf_prep(a, S, true, st);
   surf_seed(S, a.npoints, st);
   const int ntiles = S.Gpad / TC_N;
   const int ptiles = (a.npoints + TC_M - 1) / TC_M;
-  // genealogy chunks: enough CTAs for every SM, at least 8 tiles per CTA
-  int nchunks = (2 * 152 + ptiles - 1) / ptiles;
-  nchunks = std::max(1, std::min(nchunks, std::min(SURF_MAX_CHUNKS, (ntiles + 7) / 8)));
-  const int per = (ntiles + nchunks - 1) / nchunks;
-  nchunks = (ntiles + per - 1) / per;
   static_assert(A_BYTES + TC_STAGES * B_BYTES + sizeof(TcSmem) + 1024 <= TC_SMEM, "smem");
   const size_t sm = TC_SMEM;
   cudaFuncSetAttribute(k_surf_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  dim3 grid(ptiles, nchunks);
-  k_surf_tc<<<grid, TC_THREADS, sm, st>>>(S, a.npoints, per, part, d_err);
-  k_tc_merge<<<(a.npoints + 127) / 128, 128, 0, st>>>(a, part, nchunks);
-  surf_merge(a, part + (size_t)a.npoints * 2 * nchunks, 1, st);
+  int nsm = 152;
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  }
+  // max-only pre-pass over every PRE_STRIDE-th tile: every point starts the
+  // full pass with a lower bound near its maximum
+  int per = 0;
+  int nchunks = surf_tc_chunks(ptiles, (ntiles + PRE_STRIDE - 1) / PRE_STRIDE, nsm, &per);
+  if (ntiles >= 4 * PRE_STRIDE)
+    k_surf_tc<<<dim3(ptiles, nchunks), TC_THREADS, sm, st>>>(S, a.npoints, per, PRE_STRIDE, part, d_err);
+  nchunks = surf_tc_chunks(ptiles, ntiles, nsm, &per);
+  k_surf_tc<<<dim3(ptiles, nchunks), TC_THREADS, sm, st>>>(S, a.npoints, per, 0, part, d_err);
+  surf_merge(a, part, nchunks, st);
   return 0;
 }
 

@@ -47,13 +47,16 @@ __global__ void k_prep_rows(SurfArgs a, SurfPrep S)
     }
     col[K] = (float)bias;
   }
+  // the grid covers Gpad (a multiple of 256) exactly, so every warp is full
+  const unsigned lane = threadIdx.x & 31;
   for (int k = 0; k < SURF_KP; k++) {
     S.sT[(size_t)k * S.Gpad + g] = col[k];
-    if (g < a.G) atomicMax(&S.colmax[k], __float_as_uint(fabsf(col[k])));
+    const unsigned m = __reduce_max_sync(0xffffffffu, g < a.G ? __float_as_uint(fabsf(col[k])) : 0u);
+    if (lane == 0 && m) atomicMax(&S.colmax[k], m);
   }
   float bh = (float)bias;
   S.biasff[g] = make_float2(bh, (float)(bias - (double)bh));
-  if (S.sbf) {  // the MMA's tile layout, 256 genealogies per tile: hi plane, then lo plane
+  if (S.sbf) {  // the MMA's tile layout, SURF_TC_N genealogies per tile: hi plane, then lo plane
     const size_t plane = (size_t)SURF_TC_N * SURF_KP * 2;
     char *tile = reinterpret_cast<char *>(S.sbf) + (size_t)(g / SURF_TC_N) * 2 * plane;
     for (int k = 0; k < SURF_KP; k++) {
@@ -140,6 +143,7 @@ size_t surf_prep_bytes(int G, int npoints)
   b += align256(sizeof(float) * SURF_KP * npad);
   b += align256(sizeof(float) * npad);
   b += align256(sizeof(float) * npad);
+  b += align256(sizeof(unsigned) * npad);
   b += align256(sizeof(unsigned) * SURF_KP);
   b += align256(2 * sizeof(uint16_t) * SURF_KP * Gpad);
   b += align256(2 * sizeof(uint16_t) * SURF_KP * npad);
@@ -164,6 +168,7 @@ SurfPart *surf_prep_carve(SurfPrep *S, char *base, int G, int npoints)
   S->phi32 = reinterpret_cast<float *>(take(sizeof(float) * SURF_KP * npad));
   S->mag = reinterpret_cast<float *>(take(sizeof(float) * npad));
   S->seed = reinterpret_cast<float *>(take(sizeof(float) * npad));
+  S->best = reinterpret_cast<unsigned *>(take(sizeof(unsigned) * npad));
   S->colmax = reinterpret_cast<unsigned *>(take(sizeof(unsigned) * SURF_KP));
   S->sbf = reinterpret_cast<uint16_t *>(take(2 * sizeof(uint16_t) * SURF_KP * Gpad));
   S->pbf = reinterpret_cast<uint16_t *>(take(2 * sizeof(uint16_t) * SURF_KP * npad));
@@ -185,26 +190,33 @@ void surf_prep(const SurfArgs &a, SurfPrep &S, bool bf16, cudaStream_t st)
   k_prep_points<<<npad / 256, 256, 0, st>>>(a, S, npad);
 }
 
-// exact maximum over an even sample of SURF_SEED genealogies, per point
+// exact maximum over an even sample of SURF_SEED genealogies, one warp per
+// point; also the starting value of the maximum shared by genealogy chunks
 __global__ void k_surf_seed(SurfPrep S, int npoints)
 {
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= npoints) return;
+  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (p >= npoints) return;  // warp-uniform
   float2 phi[SURF_K];
-  for (int k = 0; k < S.K; k++) phi[k] = S.phiff[(size_t)p * SURF_K + k];
+#pragma unroll
+  for (int k = 0; k < SURF_K; k++) phi[k] = S.phiff[(size_t)p * SURF_K + k];
   float best = -INFINITY;
   const int n = min(SURF_SEED, S.G);
-  for (int i = 0; i < n; i++) {
+  for (int i = lane; i < n; i += 32) {
     int g = (int)(((long long)i * S.G) / n);
     ff y = surf_exact(S, g, S.sT + g, S.Gpad, phi);
     best = fmaxf(best, y.hi);
   }
-  S.seed[p] = best;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) best = fmaxf(best, __shfl_xor_sync(0xffffffffu, best, o));
+  if (lane == 0) {
+    S.seed[p] = best;
+    S.best[p] = f2ord(best);
+  }
 }
 
 void surf_seed(const SurfPrep &S, int npoints, cudaStream_t st)
 {
-  k_surf_seed<<<(npoints + 127) / 128, 128, 0, st>>>(S, npoints);
+  k_surf_seed<<<(npoints * 32 + 255) / 256, 256, 0, st>>>(S, npoints);
 }
 
 void surf_merge(const SurfArgs &a, const SurfPart *part, int nchunks, cudaStream_t st)

@@ -12,7 +12,7 @@ constexpr int SURF_K = 30;          // exact terms: 2 (theta + migration paramet
 constexpr int SURF_KP = 32;         // screened columns: the terms, the bias, zero padding
 constexpr int SURF_MAX_CHUNKS = 64;
 constexpr float SURF_MARGIN = 32.0f;  // nats below the running max that still count
-constexpr int SURF_SEED = 256;      // genealogies sampled per point for the seed maximum
+constexpr int SURF_SEED = 1024;     // genealogies sampled per point for the seed maximum
 constexpr int SURF_TC_M = 128;      // tensor-core screen: points per A tile
 constexpr int SURF_TC_N = 256;      // tensor-core screen: genealogies per B tile
 
@@ -25,6 +25,7 @@ struct SurfPrep {
   float *phi32;     // [npoints][SURF_KP] phi rounded, 1 in the bias column
   float *mag;       // [npoints] sum_k colmax_k |phi_k|: scale of screening errors
   float *seed;      // [npoints] exact max over a sample of genealogies
+  unsigned *best;   // [npoints] best exact maximum found so far (ordered bits), shared by chunks
   unsigned *colmax; // [SURF_KP] max |column| as float bits
   uint16_t *sbf;    // bf16 statistics, hi and lo planes of 256-row MMA tiles (tensor-core screen)
   uint16_t *pbf;    // bf16 phi, hi and lo planes of 128-row MMA tiles (tensor-core screen)
@@ -46,7 +47,11 @@ __device__ __forceinline__ ff surf_exact(const SurfPrep &S, int g, const float *
 {
   float2 b = S.biasff[g];
   float sum = b.x, comp = b.y;
-  for (int k = 0; k < S.K; k++) {
+  // fully unrolled with a bound check: phi stays in registers and the
+  // column loads issue together
+#pragma unroll
+  for (int k = 0; k < SURF_K; k++) {
+    if (k >= S.K) break;
     float s = col[k * stride];
     float2 f = phi[k];
     float p = __fmul_rn(s, f.x);
@@ -100,6 +105,12 @@ struct LseState {
     p.s2 = s2;
     p.pad = 0.f;
     return p;
+  }
+  __device__ __forceinline__ void unpack(const SurfPart &o)
+  {
+    m = ff_make(o.mh, o.ml);
+    s = ff_make(o.sh, o.sl);
+    s2 = o.s2;
   }
   // fold another partial (same point) into this one
   __device__ __forceinline__ void merge(const SurfPart &o)
