@@ -140,6 +140,10 @@ struct ima_ctx {
   double *d_lognorm = nullptr;
   void *d_sscratch = nullptr;
   size_t sscratch_cap = 0;
+  // row-derived surface operands held in the scratch: 0 none, 1 FP32 (split
+  // precision screen), 2 FP32 + bf16 planes (tensor-core screen); for the
+  // model type srows_model
+  int srows_state = 0, srows_model = -1;
   double *d_sx = nullptr, *d_sq = nullptr, *d_sess = nullptr;
   size_t spts_cap = 0;
 
@@ -1215,6 +1219,7 @@ extern "C" int ima_gpu_surface_load(ima_ctx *c, int G, int rowlen, const float *
     c->d_lognorm = dev_alloc<double>(G, c->dev_bytes, c->st);
     if (!c->d_lognorm) return c->fail(IMA_ERR_NOMEM, "surface normalisers");
   }
+  c->srows_state = 0;
   c->sG = G;
   c->srowlen = rowlen;
   c->snp = np;
@@ -1242,6 +1247,7 @@ static int surf_points(ima_ctx *c, int npoints)
 static int surf_scratch(ima_ctx *c, size_t bytes)
 {
   if (bytes <= c->sscratch_cap) return IMA_OK;
+  c->srows_state = 0;
   cudaFree(c->d_sscratch);
   c->d_sscratch = dev_alloc<char>(bytes, c->dev_bytes, c->st);
   if (!c->d_sscratch) return c->fail(IMA_ERR_NOMEM, "surface scratch (%zu bytes)", bytes);
@@ -1282,8 +1288,11 @@ extern "C" int ima_gpu_surface_eval(ima_ctx *c, int npoints, const double *x, in
     if (r) return r;
     int lr = 0;
     c->launch(IMA_K_SURF_FAST, (double)a.G * 27 * 4 + (double)npoints * 27 * 8,
-              [&] { lr = launch_surface_fast(a, c->d_sscratch, c->sscratch_cap, c->st); });
+              [&] { lr = launch_surface_fast(a, c->d_sscratch, c->sscratch_cap,
+                                             c->srows_state >= 1 && c->srows_model == modeltype, c->st); });
     if (lr) return c->fail(IMA_ERR_ARG, "fast surface: unsupported shape (%d)", lr);
+    if (c->srows_state < 1 || c->srows_model != modeltype) c->srows_state = 1;
+    c->srows_model = modeltype;
   } else if (method == IMA_SURF_TC) {
     r = surf_scratch(c, surface_tc_scratch_bytes(a.G, npoints));
     if (r) return r;
@@ -1291,8 +1300,11 @@ extern "C" int ima_gpu_surface_eval(ima_ctx *c, int npoints, const double *x, in
     r = c->cuda(cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->st), "flag");
     if (r) return r;
     c->launch(IMA_K_SURF_TC, (double)a.G * 32 * 2 + (double)npoints * 27 * 8,
-              [&] { lr = launch_surface_tc(a, c->d_sscratch, c->sscratch_cap, c->d_flag, c->st); });
+              [&] { lr = launch_surface_tc(a, c->d_sscratch, c->sscratch_cap, c->d_flag,
+                                           c->srows_state == 2 && c->srows_model == modeltype, c->st); });
     if (lr) return c->fail(IMA_ERR_ARG, "tensor-core surface: unsupported shape (%d)", lr);
+    c->srows_state = 2;
+    c->srows_model = modeltype;
     int flag = 0;
     r = c->cuda(cudaMemcpyAsync(&flag, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->st), "flag");
     r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "tensor-core surface");
@@ -1301,10 +1313,12 @@ extern "C" int ima_gpu_surface_eval(ima_ctx *c, int npoints, const double *x, in
   } else if (method == IMA_SURF_FP64) {
     r = surf_scratch(c, surface_fp64_scratch_bytes(a.G, npoints));
     if (r) return r;
+    c->srows_state = 0;  // the FP64 form overwrites the scratch
     c->launch(IMA_K_SURF_FP64, (double)a.G * a.rowlen * 4, [&] { launch_surface_fp64(a, (double *)c->d_sscratch, c->st); });
   } else if (method == IMA_SURF_COMPAT) {
     r = surf_scratch(c, surface_fp64_scratch_bytes(a.G, npoints));
     if (r) return r;
+    c->srows_state = 0;
     c->launch(IMA_K_SURF_COMPAT, (double)a.G * a.rowlen * 4, [&] { launch_surface_compat(a, (double *)c->d_sscratch, c->st); });
   } else {
     return c->fail(IMA_ERR_ARG, "unknown surface method %d", method);
@@ -1321,6 +1335,7 @@ extern "C" int ima_gpu_tc_selftest(ima_ctx *c, int *mismatches, float *max_abs_e
   cudaSetDevice(c->device);
   int r = surf_scratch(c, (size_t)256 << 10);
   if (r) return r;
+  c->srows_state = 0;
   int tr = tc_selftest(c->st, c->d_sscratch, c->sscratch_cap, mismatches, max_abs_err);
   c->launches += 3;
   if (tr) return c->fail(IMA_ERR_CUDA, "tensor-core self-test failed to run (%d): %s", tr,

@@ -149,15 +149,15 @@ size_t surface_fast_scratch_bytes(int G, int npoints)
   return surf_prep_bytes(G, npoints) + (size_t)npoints * SURF_MAX_CHUNKS * sizeof(SurfPart) + 256;
 }
 
-int launch_surface_fast(const SurfArgs &a, void *scratch, size_t scratch_bytes, cudaStream_t st)
+int launch_surface_fast(const SurfArgs &a, void *scratch, size_t scratch_bytes, bool rows_ready, cudaStream_t st)
 {
   if (a.np + a.nm > SURF_K / 2) return 2;
   if (scratch_bytes < surface_fast_scratch_bytes(a.G, a.npoints)) return 3;
   SurfPrep S;
   char *base = static_cast<char *>(scratch);
   SurfPart *part = surf_prep_carve(&S, base, a.G, a.npoints);
-  surf_prep(a, S, false, st);
-  surf_seed(S, a.npoints, st);
+  surf_prep(a, S, false, rows_ready, st);
+  surf_seed(S, a.npoints, SURF_SEED, st);
   int nchunks = (a.G + 65535) / 65536;
   if (nchunks > SURF_MAX_CHUNKS) nchunks = SURF_MAX_CHUNKS;
   int chunk = (a.G + nchunks - 1) / nchunks;

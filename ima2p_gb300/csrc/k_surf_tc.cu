@@ -498,6 +498,7 @@ size_t surface_tc_scratch_bytes(int G, int npoints)
 namespace {
 
 constexpr int PRE_STRIDE = 8;  // tile stride of the max-only pre-pass
+constexpr int SEED_TC = 32;    // exact samples per point before the pre-pass (one per lane)
 
 // genealogy chunks for a pass over `ntiles` tiles: one CTA holds an SM, so
 // pick the chunk count whose CTA total fills its last wave best (at least
@@ -523,15 +524,16 @@ int surf_tc_chunks(int ptiles, int ntiles, int nsm, int *per)
 
 }  // namespace
 
-int launch_surface_tc(const SurfArgs &a, void *scratch, size_t scratch_bytes, int *d_err, cudaStream_t st)
+int launch_surface_tc(const SurfArgs &a, void *scratch, size_t scratch_bytes, int *d_err, bool rows_ready,
+                      cudaStream_t st)
 {
   if (a.np + a.nm > SURF_K / 2) return 2;
   if (scratch_bytes < surface_tc_scratch_bytes(a.G, a.npoints)) return 3;
   if (a.G >= (1 << 24)) return 4;  // candidate entries pack the genealogy index into 24 bits
   SurfPrep S;
   SurfPart *part = surf_prep_carve(&S, static_cast<char *>(scratch), a.G, a.npoints);
-  surf_prep(a, S, true, st);
-  surf_seed(S, a.npoints, st);
+  surf_prep(a, S, true, rows_ready, st);
+  surf_seed(S, a.npoints, SEED_TC, st);
   const int ntiles = S.Gpad / TC_N;
   const int ptiles = (a.npoints + TC_M - 1) / TC_M;
   static_assert(A_BYTES + TC_STAGES * B_BYTES + sizeof(TcSmem) + 1024 <= TC_SMEM, "smem");

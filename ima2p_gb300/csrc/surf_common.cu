@@ -162,20 +162,22 @@ SurfPart *surf_prep_carve(SurfPrep *S, char *base, int G, int npoints)
   };
   S->G = G;
   S->Gpad = (int)Gpad;
+  // operands derived from the rows alone come first, at offsets that do not
+  // depend on the number of points, so they survive between evaluations
   S->sT = reinterpret_cast<float *>(take(sizeof(float) * SURF_KP * Gpad));
   S->biasff = reinterpret_cast<float2 *>(take(sizeof(float2) * Gpad));
+  S->colmax = reinterpret_cast<unsigned *>(take(sizeof(unsigned) * SURF_KP));
+  S->sbf = reinterpret_cast<uint16_t *>(take(2 * sizeof(uint16_t) * SURF_KP * Gpad));
   S->phiff = reinterpret_cast<float2 *>(take(sizeof(float2) * SURF_K * npad));
   S->phi32 = reinterpret_cast<float *>(take(sizeof(float) * SURF_KP * npad));
   S->mag = reinterpret_cast<float *>(take(sizeof(float) * npad));
   S->seed = reinterpret_cast<float *>(take(sizeof(float) * npad));
   S->best = reinterpret_cast<unsigned *>(take(sizeof(unsigned) * npad));
-  S->colmax = reinterpret_cast<unsigned *>(take(sizeof(unsigned) * SURF_KP));
-  S->sbf = reinterpret_cast<uint16_t *>(take(2 * sizeof(uint16_t) * SURF_KP * Gpad));
   S->pbf = reinterpret_cast<uint16_t *>(take(2 * sizeof(uint16_t) * SURF_KP * npad));
   return reinterpret_cast<SurfPart *>(base + o);
 }
 
-void surf_prep(const SurfArgs &a, SurfPrep &S, bool bf16, cudaStream_t st)
+void surf_prep(const SurfArgs &a, SurfPrep &S, bool bf16, bool rows_ready, cudaStream_t st)
 {
   S.np = a.np;
   S.nm = a.nm;
@@ -184,15 +186,17 @@ void surf_prep(const SurfArgs &a, SurfPrep &S, bool bf16, cudaStream_t st)
     S.sbf = nullptr;
     S.pbf = nullptr;
   }
-  cudaMemsetAsync(S.colmax, 0, sizeof(unsigned) * SURF_KP, st);
-  k_prep_rows<<<S.Gpad / 256, 256, 0, st>>>(a, S);
+  if (!rows_ready) {
+    cudaMemsetAsync(S.colmax, 0, sizeof(unsigned) * SURF_KP, st);
+    k_prep_rows<<<S.Gpad / 256, 256, 0, st>>>(a, S);
+  }
   int npad = (a.npoints + 255) / 256 * 256;
   k_prep_points<<<npad / 256, 256, 0, st>>>(a, S, npad);
 }
 
-// exact maximum over an even sample of SURF_SEED genealogies, one warp per
+// exact maximum over an even sample of `samples` genealogies, one warp per
 // point; also the starting value of the maximum shared by genealogy chunks
-__global__ void k_surf_seed(SurfPrep S, int npoints)
+__global__ void k_surf_seed(SurfPrep S, int npoints, int samples)
 {
   const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (p >= npoints) return;  // warp-uniform
@@ -200,7 +204,7 @@ __global__ void k_surf_seed(SurfPrep S, int npoints)
 #pragma unroll
   for (int k = 0; k < SURF_K; k++) phi[k] = S.phiff[(size_t)p * SURF_K + k];
   float best = -INFINITY;
-  const int n = min(SURF_SEED, S.G);
+  const int n = min(samples, S.G);
   for (int i = lane; i < n; i += 32) {
     int g = (int)(((long long)i * S.G) / n);
     ff y = surf_exact(S, g, S.sT + g, S.Gpad, phi);
@@ -214,9 +218,9 @@ __global__ void k_surf_seed(SurfPrep S, int npoints)
   }
 }
 
-void surf_seed(const SurfPrep &S, int npoints, cudaStream_t st)
+void surf_seed(const SurfPrep &S, int npoints, int samples, cudaStream_t st)
 {
-  k_surf_seed<<<(npoints * 32 + 255) / 256, 256, 0, st>>>(S, npoints);
+  k_surf_seed<<<(npoints * 32 + 255) / 256, 256, 0, st>>>(S, npoints, samples);
 }
 
 void surf_merge(const SurfArgs &a, const SurfPart *part, int nchunks, cudaStream_t st)

@@ -12,7 +12,7 @@ constexpr int SURF_K = 30;          // exact terms: 2 (theta + migration paramet
 constexpr int SURF_KP = 32;         // screened columns: the terms, the bias, zero padding
 constexpr int SURF_MAX_CHUNKS = 64;
 constexpr float SURF_MARGIN = 32.0f;  // nats below the running max that still count
-constexpr int SURF_SEED = 1024;     // genealogies sampled per point for the seed maximum
+constexpr int SURF_SEED = 256;      // genealogies sampled per point for the seed maximum (FP32 screen)
 constexpr int SURF_TC_M = 128;      // tensor-core screen: points per A tile
 constexpr int SURF_TC_N = 256;      // tensor-core screen: genealogies per B tile
 
@@ -152,6 +152,8 @@ __device__ __forceinline__ float ord2f(unsigned u)
 
 size_t surf_prep_bytes(int G, int npoints);
 SurfPart *surf_prep_carve(SurfPrep *S, char *base, int G, int npoints);
-void surf_prep(const SurfArgs &a, SurfPrep &S, bool bf16, cudaStream_t st);
+// rows_ready: the row-derived operands (sT, biasff, colmax, sbf) are already
+// in place from an earlier evaluation of the same rows and model type
+void surf_prep(const SurfArgs &a, SurfPrep &S, bool bf16, bool rows_ready, cudaStream_t st);
 void surf_merge(const SurfArgs &a, const SurfPart *part, int nchunks, cudaStream_t st);
-void surf_seed(const SurfPrep &S, int npoints, cudaStream_t st);
+void surf_seed(const SurfPrep &S, int npoints, int samples, cudaStream_t st);
