@@ -1286,23 +1286,25 @@ extern "C" int ima_gpu_surface_eval(ima_ctx *c, int npoints, const double *x, in
   if (method == IMA_SURF_FAST) {
     r = surf_scratch(c, surface_fast_scratch_bytes(a.G, npoints));
     if (r) return r;
-    int lr = 0;
+    int lr = 0, nk = 1;
     c->launch(IMA_K_SURF_FAST, (double)a.G * 27 * 4 + (double)npoints * 27 * 8,
               [&] { lr = launch_surface_fast(a, c->d_sscratch, c->sscratch_cap,
-                                             c->srows_state >= 1 && c->srows_model == modeltype, c->st); });
+                                             c->srows_state >= 1 && c->srows_model == modeltype, &nk, c->st); });
     if (lr) return c->fail(IMA_ERR_ARG, "fast surface: unsupported shape (%d)", lr);
+    c->launches += nk - 1;  // one evaluation, several kernels
     if (c->srows_state < 1 || c->srows_model != modeltype) c->srows_state = 1;
     c->srows_model = modeltype;
   } else if (method == IMA_SURF_TC) {
     r = surf_scratch(c, surface_tc_scratch_bytes(a.G, npoints));
     if (r) return r;
-    int lr = 0;
+    int lr = 0, nk = 1;
     r = c->cuda(cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->st), "flag");
     if (r) return r;
     c->launch(IMA_K_SURF_TC, (double)a.G * 32 * 2 + (double)npoints * 27 * 8,
               [&] { lr = launch_surface_tc(a, c->d_sscratch, c->sscratch_cap, c->d_flag,
-                                           c->srows_state == 2 && c->srows_model == modeltype, c->st); });
+                                           c->srows_state == 2 && c->srows_model == modeltype, &nk, c->st); });
     if (lr) return c->fail(IMA_ERR_ARG, "tensor-core surface: unsupported shape (%d)", lr);
+    c->launches += nk - 1;
     c->srows_state = 2;
     c->srows_model = modeltype;
     int flag = 0;
@@ -1315,11 +1317,13 @@ extern "C" int ima_gpu_surface_eval(ima_ctx *c, int npoints, const double *x, in
     if (r) return r;
     c->srows_state = 0;  // the FP64 form overwrites the scratch
     c->launch(IMA_K_SURF_FP64, (double)a.G * a.rowlen * 4, [&] { launch_surface_fp64(a, (double *)c->d_sscratch, c->st); });
+    c->launches += 1;  // pass + merge
   } else if (method == IMA_SURF_COMPAT) {
     r = surf_scratch(c, surface_fp64_scratch_bytes(a.G, npoints));
     if (r) return r;
     c->srows_state = 0;
     c->launch(IMA_K_SURF_COMPAT, (double)a.G * a.rowlen * 4, [&] { launch_surface_compat(a, (double *)c->d_sscratch, c->st); });
+    c->launches += (npoints + SURF_COMPAT_CONCURRENT - 1) / SURF_COMPAT_CONCURRENT - 1;
   } else {
     return c->fail(IMA_ERR_ARG, "unknown surface method %d", method);
   }

@@ -114,10 +114,13 @@ struct SurfArgs {
 };
 void launch_surface_fp64(const SurfArgs &a, double *scratch, cudaStream_t st);
 void launch_surface_compat(const SurfArgs &a, double *scratch, cudaStream_t st);
-int launch_surface_fast(const SurfArgs &a, void *scratch, size_t scratch_bytes, bool rows_ready, cudaStream_t st);
+constexpr int SURF_COMPAT_CONCURRENT = 64;  // points per launch of the compat surface
+// the surface launchers report how many kernels they enqueued in *nkernels
+int launch_surface_fast(const SurfArgs &a, void *scratch, size_t scratch_bytes, bool rows_ready, int *nkernels,
+                        cudaStream_t st);
 size_t surface_fast_scratch_bytes(int G, int npoints);
 int launch_surface_tc(const SurfArgs &a, void *scratch, size_t scratch_bytes, int *d_err, bool rows_ready,
-                      cudaStream_t st);
+                      int *nkernels, cudaStream_t st);
 size_t surface_tc_scratch_bytes(int G, int npoints);
 int tc_selftest(cudaStream_t st, void *scratch, size_t bytes, int *h_bad, float *h_maxerr);
 size_t surface_fp64_scratch_bytes(int G, int npoints);

@@ -300,7 +300,6 @@ __global__ void __launch_bounds__(CP_BS) k_surf_compat(SurfArgs a, int pt0, doub
   }
 }
 
-constexpr int COMPAT_CONCURRENT = 64;
 
 }  // namespace
 
@@ -309,7 +308,7 @@ size_t surface_fp64_scratch_bytes(int G, int npoints)
   int nchunks = (G + 65535) / 65536;
   if (nchunks > 64) nchunks = 64;
   size_t f64 = (size_t)npoints * nchunks * 3 * sizeof(double);
-  size_t cp = (size_t)(npoints < COMPAT_CONCURRENT ? npoints : COMPAT_CONCURRENT) * G *
+  size_t cp = (size_t)(npoints < SURF_COMPAT_CONCURRENT ? npoints : SURF_COMPAT_CONCURRENT) * G *
               (sizeof(double) + 1);
   return f64 > cp ? f64 : cp;
 }
@@ -327,9 +326,9 @@ void launch_surface_fp64(const SurfArgs &a, double *scratch, cudaStream_t st)
 
 void launch_surface_compat(const SurfArgs &a, double *scratch, cudaStream_t st)
 {
-  for (int p0 = 0; p0 < a.npoints; p0 += COMPAT_CONCURRENT) {
-    int np = a.npoints - p0 < COMPAT_CONCURRENT ? a.npoints - p0 : COMPAT_CONCURRENT;
-    int conc = a.npoints < COMPAT_CONCURRENT ? a.npoints : COMPAT_CONCURRENT;
+  for (int p0 = 0; p0 < a.npoints; p0 += SURF_COMPAT_CONCURRENT) {
+    int np = a.npoints - p0 < SURF_COMPAT_CONCURRENT ? a.npoints - p0 : SURF_COMPAT_CONCURRENT;
+    int conc = a.npoints < SURF_COMPAT_CONCURRENT ? a.npoints : SURF_COMPAT_CONCURRENT;
     uint8_t *listed = reinterpret_cast<uint8_t *>(scratch + (size_t)conc * a.G);
     k_surf_compat<<<np, CP_BS, 0, st>>>(a, p0, scratch, listed);
   }

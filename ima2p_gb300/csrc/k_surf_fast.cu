@@ -149,7 +149,8 @@ size_t surface_fast_scratch_bytes(int G, int npoints)
   return surf_prep_bytes(G, npoints) + (size_t)npoints * SURF_MAX_CHUNKS * sizeof(SurfPart) + 256;
 }
 
-int launch_surface_fast(const SurfArgs &a, void *scratch, size_t scratch_bytes, bool rows_ready, cudaStream_t st)
+int launch_surface_fast(const SurfArgs &a, void *scratch, size_t scratch_bytes, bool rows_ready, int *nkernels,
+                        cudaStream_t st)
 {
   if (a.np + a.nm > SURF_K / 2) return 2;
   if (scratch_bytes < surface_fast_scratch_bytes(a.G, a.npoints)) return 3;
@@ -166,5 +167,6 @@ int launch_surface_fast(const SurfArgs &a, void *scratch, size_t scratch_bytes, 
   dim3 grid((a.npoints + TP - 1) / TP, nchunks);
   k_surf_screen_fp32<<<grid, BS, 0, st>>>(S, a.npoints, chunk, part);
   surf_merge(a, part, nchunks, st);
+  *nkernels = (rows_ready ? 0 : 1) + 4;  // rows, points, seed, screen, merge
   return 0;
 }

@@ -525,7 +525,7 @@ int surf_tc_chunks(int ptiles, int ntiles, int nsm, int *per)
 }  // namespace
 
 int launch_surface_tc(const SurfArgs &a, void *scratch, size_t scratch_bytes, int *d_err, bool rows_ready,
-                      cudaStream_t st)
+                      int *nkernels, cudaStream_t st)
 {
   if (a.np + a.nm > SURF_K / 2) return 2;
   if (scratch_bytes < surface_tc_scratch_bytes(a.G, a.npoints)) return 3;
@@ -549,11 +549,12 @@ int launch_surface_tc(const SurfArgs &a, void *scratch, size_t scratch_bytes, in
   // full pass with a lower bound near its maximum
   int per = 0;
   int nchunks = surf_tc_chunks(ptiles, (ntiles + PRE_STRIDE - 1) / PRE_STRIDE, nsm, &per);
-  if (ntiles >= 4 * PRE_STRIDE)
-    k_surf_tc<<<dim3(ptiles, nchunks), TC_THREADS, sm, st>>>(S, a.npoints, per, PRE_STRIDE, part, d_err);
+  const bool pre = ntiles >= 4 * PRE_STRIDE;
+  if (pre) k_surf_tc<<<dim3(ptiles, nchunks), TC_THREADS, sm, st>>>(S, a.npoints, per, PRE_STRIDE, part, d_err);
   nchunks = surf_tc_chunks(ptiles, ntiles, nsm, &per);
   k_surf_tc<<<dim3(ptiles, nchunks), TC_THREADS, sm, st>>>(S, a.npoints, per, 0, part, d_err);
   surf_merge(a, part, nchunks, st);
+  *nkernels = (rows_ready ? 0 : 1) + 4 + (pre ? 1 : 0);  // rows, points, seed, pre-pass, pass, merge
   return 0;
 }
 
