@@ -334,7 +334,7 @@ class Context:
                                                int(numpopsizeparams), int(nummigrateparams), int(npops),
                                                _ptr(_f64(lognorm))))
 
-    def surface_eval(self, x, modeltype=0, method=SURF_FAST):
+    def surface_eval(self, x, modeltype=0, method=SURF_TC):
         x = _f64(x).reshape(-1, self.surf_npar)
         q = np.zeros(len(x))
         ess = np.zeros(len(x))

@@ -192,7 +192,10 @@ int ima_gpu_surface_load(ima_ctx *ctx, int G, int rowlen, const float *gsampinf,
 #define IMA_SURF_TC 3       /* IMA_SURF_FAST with its screen on the tensor cores  */
 /* q = log G - log sum_g exp(p_g(x)) at npoints points x[npoints][nparams];
  * modeltype 0 full, 1 population sizes only, 2 migration only (jointp's
- * nowmodeltype).  ess (may be NULL) = effective number of genealogies. */
+ * nowmodeltype).  ess (may be NULL) = effective number of genealogies.
+ * IMA_SURF_TC is the fastest exact method (G < 2^24); IMA_SURF_FAST gives
+ * the same sum with its screen on CUDA cores.  Both keep the operands derived
+ * from the rows between calls while the rows and modeltype are unchanged. */
 int ima_gpu_surface_eval(ima_ctx *ctx, int npoints, const double *x, int modeltype, int method,
                          double *q, double *ess);
 /* Checks the tensor-core path on this device: one 128 x 256 x 32 bf16 tile of
