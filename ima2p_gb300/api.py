@@ -41,10 +41,24 @@ EXPORTS = [
     "ima_gpu_set_betas", "ima_gpu_set_pdg", "ima_gpu_get_pdg", "ima_gpu_set_probg",
     "ima_gpu_swapchains", "ima_gpu_get_swapcounts", "ima_gpu_surface_load",
     "ima_gpu_surface_eval", "ima_gpu_jointp", "ima_gpu_surface_fp64_noalloc", "ima_gpu_tc_selftest",
+    "ima_gpu_surface_info", "ima_mt19937_seed", "ima_mt19937_uniform", "ima_gpu_modelloop",
     "ima_gpu_timer_begin", "ima_gpu_timer_end",
     "ima_gpu_set_profiling", "ima_gpu_kernel_stats", "ima_gpu_launch_count", "ima_gpu_flush_l2",
     "ima_gpu_memory",
 ]
+
+
+class MT19937(C.Structure):
+    """The reference's MT19937 generator state (ima_mt19937)."""
+    _fields_ = [("mt", C.c_uint32 * 624), ("mti", C.c_int)]
+
+    def __init__(self, seed=None):
+        super().__init__()
+        if seed is not None:
+            load_library().ima_mt19937_seed(C.byref(self), int(seed))
+
+    def uniform(self):
+        return load_library().ima_mt19937_uniform(C.byref(self))
 
 
 class ImaError(RuntimeError):
@@ -114,6 +128,10 @@ def _declare(L):
         "ima_gpu_surface_load": (I, [P, I, I, P, I, I, I, P]),
         "ima_gpu_surface_eval": (I, [P, I, P, I, I, P, P]),
         "ima_gpu_jointp": (I, [P, P, I, P, P]),
+        "ima_gpu_surface_info": (I, [P, C.POINTER(I), C.POINTER(I), C.POINTER(I), C.POINTER(I)]),
+        "ima_mt19937_seed": (None, [P, C.c_uint32]),
+        "ima_mt19937_uniform": (D, [P]),
+        "ima_gpu_modelloop": (I, [P, I, P, I, P, I, I, P, P, P, C.POINTER(I), C.POINTER(I)]),
         "ima_gpu_surface_fp64_noalloc": (I, [P, I, I, I, I, I, P, P, I, I, P, P, P]),
         "ima_gpu_tc_selftest": (I, [P, C.POINTER(I), C.POINTER(C.c_float)]),
         "ima_gpu_timer_begin": (I, [P]),
@@ -353,6 +371,27 @@ class Context:
         e = np.zeros(1)
         self._ck(self.lib.ima_gpu_jointp(self.h, _ptr(_f64(x)), int(calc_ess), _ptr(e), _ptr(q)))
         return float(q[0]), float(e[0])
+
+    def surface_info(self):
+        G, np_, nm, npops = I(), I(), I(), I()
+        self._ck(self.lib.ima_gpu_surface_info(self.h, C.byref(G), C.byref(np_), C.byref(nm), C.byref(npops)))
+        return G.value, np_.value, nm.value, npops.value
+
+    def modelloop(self, upper, modeltype=0, rng=None, seed=1234, multiplier=100, xmap=None, nested=0,
+                  method=SURF_COMPAT):
+        """modelloop (jointfind.cpp:746-812): the DE peak search over the
+        loaded surface.  rng: an MT19937 state (continues across calls);
+        returns (best[n+1], ess, generations, restarts, rng)."""
+        rng = rng if rng is not None else MT19937(seed)
+        n = sum(self.surface_info()[1:3])
+        best = np.zeros(n + 1)
+        ess = np.zeros(1)
+        gens, runs = I(), I()
+        xm = _f64(xmap) if xmap is not None else None
+        self._ck(self.lib.ima_gpu_modelloop(self.h, int(modeltype), _ptr(_f64(upper)), int(multiplier),
+                                            _ptr(xm) if xm is not None else None, int(nested), int(method),
+                                            C.byref(rng), _ptr(best), _ptr(ess), C.byref(gens), C.byref(runs)))
+        return best, float(ess[0]), gens.value, runs.value, rng
 
     # --------------------------------------------------- measurement
     def synchronize(self):

@@ -1230,6 +1230,17 @@ extern "C" int ima_gpu_surface_load(ima_ctx *c, int G, int rowlen, const float *
   return r ? r : c->cuda(cudaStreamSynchronize(c->st), "surface load");
 }
 
+extern "C" int ima_gpu_surface_info(ima_ctx *c, int *G, int *np, int *nm, int *npops)
+{
+  if (!c) return IMA_ERR_ARG;
+  if (!c->d_rows) return c->fail(IMA_ERR_STATE, "call ima_gpu_surface_load first");
+  if (G) *G = c->sG;
+  if (np) *np = c->snp;
+  if (nm) *nm = c->snm;
+  if (npops) *npops = c->snpops;
+  return IMA_OK;
+}
+
 static int surf_points(ima_ctx *c, int npoints)
 {
   if ((size_t)npoints <= c->spts_cap) return IMA_OK;

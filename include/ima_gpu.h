@@ -205,6 +205,39 @@ int ima_gpu_tc_selftest(ima_ctx *ctx, int *mismatches, float *max_abs_err);
 
 /* jointp (jointfind.cpp:885-1047) at one point, reference semantics. */
 int ima_gpu_jointp(ima_ctx *ctx, const double *x, int calc_ess, double *effective_n, double *q);
+/* The loaded surface's shape (any pointer may be NULL). */
+int ima_gpu_surface_info(ima_ctx *ctx, int *G, int *numpopsizeparams, int *nummigrateparams, int *npops);
+
+/* ---------------------------------------------------- L-mode peak search
+ * MT19937 generator state (utilities.cpp:323-427, Matsumoto & Nishimura):
+ * the reference's global generator, carried by the caller so that a peak
+ * search continues the caller's stream. */
+typedef struct {
+  uint32_t mt[624];
+  int mti;
+} ima_mt19937;
+/* init_genrand, as setseeds (utilities.cpp:399-408) seeds the generator */
+void ima_mt19937_seed(ima_mt19937 *rng, uint32_t seed);
+/* genrand_real3, the reference's uniform() in (0,1) */
+double ima_mt19937_uniform(ima_mt19937 *rng);
+/* modelloop (jointfind.cpp:746-812): differential-evolution search for the
+ * peak of the loaded surface, for modeltype 0 (full), 1 (population sizes)
+ * or 2 (migration rates) -- findjointpeaks (:1089-1183) runs 0 for two
+ * populations, 1 and 2 otherwise.  Bounds are (MINPARAMVAL, upper[k]], the
+ * priors' maxima (setbounds :578-590).  xmap (NULL for the model itself)
+ * gives a nested model of `nested` parameters as setup_mapping does: entry k
+ * is the nested index of full parameter k, or -value for a constant;
+ * nested models of modeltype 2 are not accepted (the reference's bounds for
+ * them index past the mapped ones).  Each generation's popsizemultiplier *
+ * (model parameters) trial vectors are evaluated in one surface call with
+ * `method`; IMA_SURF_COMPAT (the reference's jointp) follows the reference's
+ * search exactly, draw for draw from *rng.  Out: best[np+nm] the peak in the
+ * full model's parameters and best[np+nm] its -log density; *ess the
+ * effective number of genealogies there; generations over all restarts; the
+ * number of searches run.  Any of ess, generations, restarts may be NULL. */
+int ima_gpu_modelloop(ima_ctx *ctx, int modeltype, const double *upper, int popsizemultiplier,
+                      const double *xmap, int nested, int method, ima_mt19937 *rng, double *best,
+                      double *ess, int *generations, int *restarts);
 
 /* No counterpart in the reference.  The FP64 surface of ima_gpu_surface_eval
  * (IMA_SURF_FP64) for callers that cannot allocate device memory -- code

@@ -644,3 +644,162 @@ double ora_jointp_compat(int G, int rowlen, const float *g, int np, int nm,
   free(mm); free(zz); free(p); free(list);
   return q;
 }
+
+/* ======================================================================
+ * L-mode peak search by differential evolution (jointfind.cpp:594-812)
+ * ==================================================================== */
+typedef struct {
+  int G, rowlen, np, nm, npops, modeltype, compat;
+  const float *g;
+  const double *lognorm;
+} de_obj;
+
+static double de_eval(const de_obj *o, const double *x, double *ess)
+{
+  double e = 0.0;
+  double q = o->compat ? ora_jointp_compat(o->G, o->rowlen, o->g, o->np, o->nm, o->npops,
+                                           o->modeltype, o->lognorm, x, &e)
+                       : ora_jointp_exact(o->G, o->rowlen, o->g, o->np, o->nm, o->npops,
+                                          o->modeltype, o->lognorm, x, &e);
+  if (ess) *ess = e;
+  return q;
+}
+
+#define DE_MINPARAMVAL 0.0000001 /* imamp.hpp:130 */
+#define DE_STARTHI 1E200         /* jointfind.cpp:136-142 */
+#define DE_STARTLOW -1E200
+#define DE_SPREADTOL 1.0e-7
+#define DE_PLOOPTOL 1.0e-6
+#define DE_LOOPMATCH 2
+#define DE_MAXRESTART 10
+#define DE_RECRATE 0.9 /* :145-146 */
+#define DE_FWEIGHT 0.8
+
+static int de_randposint(ora_mt *r, int n) { return (int)floor(ora_mt_uniform(r) * n); }
+
+/* the full parameter vector jointp sees for population member v */
+static void de_full(const double *v, const double *xmap, int n, double *full)
+{
+  if (!xmap) {
+    for (int i = 0; i < n; i++) full[i] = v[i];
+    return;
+  }
+  for (int i = 0; i < n; i++) full[i] = xmap[i] < 0 ? -xmap[i] : v[(int)xmap[i]];
+}
+
+int ora_modelloop(int G, int rowlen, const float *g, int np, int nm, int npops,
+                  const double *lognorm, int compat, int modeltype,
+                  const double *upper, int multiplier, const double *xmap,
+                  int nested, ora_mt *rng, double *best, double *ess,
+                  int *restarts)
+{
+  const int n = np + nm;
+  if (xmap && (nested < 1 || modeltype == 2)) return -1; /* see the header */
+  de_obj o = {G, rowlen, np, nm, npops, modeltype, compat, g, lognorm};
+  const int r0 = (modeltype == 2) ? np : 0;
+  int modelparams = modeltype == 0 ? n : (modeltype == 1 ? np : nm);
+  if (xmap) modelparams = nested;
+  const int jmax = r0 + modelparams;
+  const int dep = modelparams * multiplier;
+  double *lo = (double *)calloc(n, sizeof(double)), *hi = (double *)calloc(n, sizeof(double));
+  if (!xmap) {
+    for (int j = 0; j < n; j++) {
+      lo[j] = DE_MINPARAMVAL;
+      hi[j] = upper[j];
+    }
+  } else {
+    /* reversemapvals: the first full parameter mapped to each nested index */
+    for (int i = 0, k = 0; i < n; i++)
+      if (k == (int)xmap[i]) {
+        lo[k] = DE_MINPARAMVAL;
+        hi[k] = upper[i];
+        k++;
+      }
+  }
+  double *pop = (double *)calloc((size_t)dep * (n + 1), sizeof(double));
+  double *trial = (double *)calloc((size_t)dep * (n + 1), sizeof(double));
+  double *full = (double *)calloc(n, sizeof(double));
+  double *bestv = (double *)calloc(n + 1, sizeof(double));
+#define POP(i, j) pop[(size_t)(i) * (n + 1) + (j)]
+#define TRI(i, j) trial[(size_t)(i) * (n + 1) + (j)]
+  int gens = 0, nrun = 0;
+  double global_pd = DE_STARTHI;
+  /* startpop */
+  {
+    for (int i = 0; i < dep; i++) {
+      for (int j = 0; j < n; j++)
+        POP(i, j) = (j >= r0 && j < jmax) ? lo[j] + ora_mt_uniform(rng) * (hi[j] - lo[j]) : -1.0;
+      de_full(&POP(i, 0), xmap, n, full);
+      POP(i, n) = de_eval(&o, full, NULL);
+    }
+  }
+  for (int i = 0; i < dep; i++)
+    if (POP(i, n) < global_pd) global_pd = POP(i, n);
+  int newstart = 0, countloop = 0;
+  do {
+    if (newstart > 0) {
+      for (int i = 0; i < dep; i++) {
+        for (int j = 0; j < n; j++)
+          POP(i, j) = (j >= r0 && j < jmax) ? lo[j] + ora_mt_uniform(rng) * (hi[j] - lo[j]) : -1.0;
+        de_full(&POP(i, 0), xmap, n, full);
+        POP(i, n) = de_eval(&o, full, NULL);
+      }
+    }
+    /* difeloop: nextgen until the spread of the population's values is small */
+    double lowpd, hipd;
+    do {
+      lowpd = DE_STARTHI;
+      hipd = DE_STARTLOW;
+      for (int i = 0; i < dep; i++) {
+        int A = de_randposint(rng, dep), B = de_randposint(rng, dep), Cv = de_randposint(rng, dep);
+        for (int j = r0; j < jmax; j++) {
+          double u = ora_mt_uniform(rng);
+          if (u < DE_RECRATE) {
+            double t = POP(Cv, j) + DE_FWEIGHT * (POP(A, j) - POP(B, j));
+            if (t < lo[j]) t = POP(Cv, j) - ora_mt_uniform(rng) * (POP(Cv, j) - lo[j]);
+            if (t > hi[j]) t = POP(Cv, j) + ora_mt_uniform(rng) * (hi[j] - POP(Cv, j));
+            TRI(i, j) = t;
+          } else {
+            TRI(i, j) = POP(i, j);
+          }
+        }
+        de_full(&TRI(i, 0), xmap, n, full);
+        TRI(i, n) = de_eval(&o, full, NULL);
+      }
+      for (int i = 0; i < dep; i++) {
+        if (TRI(i, n) < POP(i, n))
+          for (int j = 0; j <= n; j++) POP(i, j) = TRI(i, j);
+        if (POP(i, n) < lowpd) lowpd = POP(i, n);
+        if (POP(i, n) > hipd) hipd = POP(i, n);
+      }
+      gens++;
+    } while (hipd - lowpd > DE_SPREADTOL);
+    double local_pd = lowpd;
+    nrun++;
+    if (fabs(local_pd - global_pd) < DE_PLOOPTOL) countloop++;
+    else if (local_pd < global_pd) countloop = 0;
+    if (local_pd < global_pd) {
+      /* copybest */
+      double t = DE_STARTHI;
+      int k = 0;
+      for (int i = 0; i < dep; i++)
+        if (POP(i, n) < t) {
+          t = POP(i, n);
+          k = i;
+        }
+      for (int j = 0; j <= n; j++) bestv[j] = POP(k, j);
+      bestv[n] = t;
+      global_pd = local_pd;
+    }
+    newstart++;
+  } while (countloop < DE_LOOPMATCH && newstart < DE_MAXRESTART);
+  de_full(bestv, xmap, n, full);
+  for (int j = 0; j < n; j++) best[j] = full[j];
+  best[n] = bestv[n];
+  de_eval(&o, full, ess);
+  if (restarts) *restarts = nrun;
+#undef POP
+#undef TRI
+  free(lo); free(hi); free(pop); free(trial); free(full); free(bestv);
+  return gens;
+}

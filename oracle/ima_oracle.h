@@ -114,6 +114,23 @@ double ora_jointp_compat(int G, int rowlen, const float *g, int np, int nm,
                          const double *x, double *ess);
 void ora_eexp(double x, double *m, int *z);
 
+/* L-mode peak search: modelloop (jointfind.cpp:746-812) with startpop
+ * (:658-702), nextgen (:594-656), difeloop (:705-720) and copybest
+ * (:723-738), for one model type, or a nested model given by xmap (nested > 0
+ * parameters; mapvals :555-566, reversemapvals :540-552).  Lower bounds are
+ * MINPARAMVAL, upper bounds the priors' maxima (setbounds :578-590).  The
+ * objective is jointp on the given rows, compat (the reference's truncated
+ * sum) or exact.  Uniforms come from *rng.  best[nparams+1] holds the peak's
+ * parameters (mapped to the full model) and -log density; returns the number
+ * of generations over all restarts, *restarts the number of DE runs; -1 for
+ * a nested model of modeltype 2, whose bounds the reference indexes past the
+ * mapped ones. */
+int ora_modelloop(int G, int rowlen, const float *g, int np, int nm, int npops,
+                  const double *lognorm, int compat, int modeltype,
+                  const double *upper, int multiplier, const double *xmap,
+                  int nested, ora_mt *rng, double *best, double *ess,
+                  int *restarts);
+
 #ifdef __cplusplus
 }
 #endif

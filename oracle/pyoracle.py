@@ -68,6 +68,12 @@ def _declare(L):
     for f in ("ora_jointp_exact", "ora_jointp_compat"):
         getattr(L, f).argtypes = [I, I, P, I, I, I, I, P, P, P]
         getattr(L, f).restype = D
+    L.ora_mt_seed.argtypes = [P, C.c_uint32]
+    L.ora_mt_seed.restype = None
+    L.ora_mt_uniform.argtypes = [P]
+    L.ora_mt_uniform.restype = D
+    L.ora_modelloop.argtypes = [I, I, P, I, I, I, P, I, I, P, I, P, I, P, P, P, P]
+    L.ora_modelloop.restype = I
 
 
 def _p(a):
@@ -275,3 +281,54 @@ def ref_jointp(rows, np_, nm, npops, modeltype, points):
     t += [" ".join("%.17g" % v for v in x) for x in points]
     out = run_ref("jointp", "\n".join(t) + "\n")
     return np.array([[float(v) for v in line.split()] for line in out.strip().splitlines()])
+
+
+# ------------------------------------------------------------ DE peak search
+class MT(C.Structure):
+    """MT19937 generator state (utilities.cpp:323-427): mt[624], mti."""
+    _fields_ = [("mt", C.c_uint32 * 624), ("mti", C.c_int)]
+
+    def __init__(self, seed):
+        super().__init__()
+        lib().ora_mt_seed(C.byref(self), seed)
+
+    def uniform(self):
+        return lib().ora_mt_uniform(C.byref(self))
+
+
+def modelloop(rows, np_, nm, npops, upper, modeltype=0, multiplier=100, seed=1234, rng=None,
+              xmap=None, nested=0, compat=True, lognorm=None):
+    """modelloop (jointfind.cpp:746-812) restated; returns (best[n+1], ess,
+    generations, restarts, rng)."""
+    G, rl = rows.shape
+    rows = np.ascontiguousarray(rows, np.float32)
+    n = np_ + nm
+    rng = rng if rng is not None else MT(seed)
+    best = np.zeros(n + 1)
+    ess = np.zeros(1)
+    nrun = np.zeros(1, np.int32)
+    gens = lib().ora_modelloop(G, rl, _p(rows), np_, nm, npops,
+                               _p(_f64(lognorm)) if lognorm is not None else None, int(compat), modeltype,
+                               _p(_f64(upper)), multiplier,
+                               _p(_f64(xmap)) if xmap is not None else None, nested,
+                               C.cast(C.pointer(rng), C.c_void_p), _p(best), _p(ess), _p(nrun))
+    return best, float(ess[0]), gens, int(nrun[0]), rng
+
+
+def ref_de(rows, np_, nm, npops, upper, modeltype=0, multiplier=100, seed=1234, xmap=None, nested=0):
+    """The reference's own modelloop through oracle/_ref/imaref (this
+    container only); returns (best[n+1], ess)."""
+    G, rl = rows.shape
+    lines = ["%d %d %d %d %d %d %d %d %d" % (G, rl, np_, nm, npops, modeltype, multiplier, seed, nested),
+             " ".join("%.9g" % v for v in np.asarray(rows, np.float32).ravel()),
+             " ".join("%.17g" % v for v in upper)]
+    if nested:
+        lines.append(" ".join("%.17g" % v for v in xmap))
+    out = run_ref("de", "\n".join(lines) + "\n")
+    best = ess = None
+    for ln in out.splitlines():
+        if ln.startswith("BEST"):
+            best = np.array([float(v) for v in ln.split()[1:]])
+        elif ln.startswith("ESS"):
+            ess = float(ln.split()[1])
+    return best, ess

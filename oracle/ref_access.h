@@ -4,4 +4,6 @@
 double refacc_sumlogk(int li);
 void refacc_jointp_setup(int nparams_total, int modeltype);
 double refacc_jointp(double *x, double *ess);
+void refacc_modelloop(int nparams_total, int modeltype, const double *upper, int multiplier,
+                      const double *xmap, int nested_params, double *best_out, double *ess_out);
 #endif

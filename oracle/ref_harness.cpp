@@ -12,7 +12,7 @@
  * ref_access_cpd.cpp and ref_access_jf.cpp include those two reference
  * sources to reach them.  The other reference objects are linked unchanged.
  *
- * Usage:  imaref is|hky|sw|swap|jointp <input.txt>   (results on stdout)
+ * Usage:  imaref is|hky|sw|swap|jointp|de <input.txt>   (results on stdout)
  */
 #undef GLOBVARS
 #include "imamp.hpp"
@@ -208,11 +208,8 @@ static void run_swap()
   }
 }
 
-/* JOINTP: G rowlen np nm npops modeltype rows[G*rowlen] npoints points[npoints*(np+nm)]
- *   -> q ess per point */
-static void run_jointp()
+static void load_gsampinf(int G, int rowlen, int np, int nm, int npp)
 {
-  int G = rd_i(), rowlen = rd_i(), np = rd_i(), nm = rd_i(), npp = rd_i(), mt = rd_i();
   genealogiessaved = G;
   numpopsizeparams = np;
   nummigrateparams = nm;
@@ -223,6 +220,14 @@ static void run_jointp()
     for (int k = 0; k < rowlen; k++) gsampinf[g][k] = (float)rd_d();
   }
   eexpsum = (struct extendnum *)malloc(sizeof(struct extendnum) * G);
+}
+
+/* JOINTP: G rowlen np nm npops modeltype rows[G*rowlen] npoints points[npoints*(np+nm)]
+ *   -> q ess per point */
+static void run_jointp()
+{
+  int G = rd_i(), rowlen = rd_i(), np = rd_i(), nm = rd_i(), npp = rd_i(), mt = rd_i();
+  load_gsampinf(G, rowlen, np, nm, npp);
   refacc_jointp_setup(np + nm, mt);
   int npts = rd_i();
   std::vector<double> x(np + nm);
@@ -234,9 +239,32 @@ static void run_jointp()
   }
 }
 
+/* DE: G rowlen np nm npops modeltype multiplier seed nested rows[G*rowlen]
+ *     upper[np+nm] [xmap[np+nm] when nested > 0]
+ *   -> "BEST" best[np+nm] objective; "ESS" ess  (modelloop's own progress
+ *      lines also go to stdout) */
+static void run_de()
+{
+  int G = rd_i(), rowlen = rd_i(), np = rd_i(), nm = rd_i(), npp = rd_i(), mt = rd_i();
+  int mult = rd_i(), seed = rd_i(), nested = rd_i();
+  load_gsampinf(G, rowlen, np, nm, npp);
+  int n = np + nm;
+  std::vector<double> upper(n), xmap(n), best(n + 1);
+  for (int k = 0; k < n; k++) upper[k] = rd_d();
+  if (nested > 0)
+    for (int k = 0; k < n; k++) xmap[k] = rd_d();
+  refacc_jointp_setup(n, mt);
+  setseeds(seed);
+  double ess = 0.0;
+  refacc_modelloop(n, mt, upper.data(), mult, nested > 0 ? xmap.data() : nullptr, nested, best.data(), &ess);
+  printf("BEST");
+  for (int k = 0; k <= n; k++) printf(" %.17g", best[k]);
+  printf("\nESS %.17g\n", ess);
+}
+
 int main(int argc, char **argv)
 {
-  if (argc != 3) { fprintf(stderr, "usage: imaref is|hky|sw|swap|jointp <input>\n"); return 2; }
+  if (argc != 3) { fprintf(stderr, "usage: imaref is|hky|sw|swap|jointp|de <input>\n"); return 2; }
   g_in = fopen(argv[2], "r");
   if (!g_in) { perror(argv[2]); return 2; }
   std::string mode = argv[1];
@@ -245,6 +273,7 @@ int main(int argc, char **argv)
   else if (mode == "sw") run_sw();
   else if (mode == "swap") run_swap();
   else if (mode == "jointp") run_jointp();
+  else if (mode == "de") run_de();
   else { fprintf(stderr, "unknown mode\n"); return 2; }
   fclose(g_in);
   return 0;

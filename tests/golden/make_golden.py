@@ -14,6 +14,11 @@ Fixtures:
                     probability branches and x > 700
   golden_swap.npz   setheat + swapchains (MT19937 seeded), betas and counts
   golden_jointp.npz jointp (truncated, eexp) values and ESS
+  golden_de.npz     modelloop (the L-mode differential-evolution peak search,
+                    MT19937 seeded) for the full model, theta-only and
+                    migration-only model types and a nested model
+
+Run with fixture names (is hky sw swap jointp de) to regenerate only those.
 """
 from __future__ import annotations
 
@@ -304,14 +309,43 @@ def golden_jointp():
     np.savez_compressed(os.path.join(OUT, "golden_jointp.npz"), **out)
 
 
+def de_rows(rng, G, np_, nm):
+    """gsampinf rows close to one another, so the posterior spreads over many
+    genealogies (a peak with an effective sample size in the hundreds)."""
+    rows, _, off = synth.surface_stats(rng, G, np_, nm, 1)
+    rows[:] = rows[0]
+    rows[:, off["fc"]:off["fc"] + np_] *= (1 + 0.05 * rng.standard_normal((G, np_))).astype(np.float32)
+    rows[:, off["fm"]:off["fm"] + nm] *= (1 + 0.05 * rng.standard_normal((G, nm))).astype(np.float32)
+    rows[:, off["probg"]] = (200 + rng.normal(0, 0.5, G)).astype(np.float32)
+    rows[:, off["qi"]:off["qi"] + np_] += rng.normal(0, 0.3, (G, np_)).astype(np.float32)
+    rows[:, off["mi"]:off["mi"] + nm] += rng.normal(0, 0.3, (G, nm)).astype(np.float32)
+    return rows
+
+
+def golden_de():
+    rng = np.random.default_rng(1006)
+    rows = de_rows(rng, 400, 3, 2)
+    upper = np.array([20.0, 20.0, 20.0, 2.0, 2.0])
+    # (name, npops, modeltype, seed, xmap, nested); DE population 30 x params
+    cases = [("full", 2, 0, 77, None, 0), ("theta", 3, 1, 78, None, 0), ("mig", 3, 2, 79, None, 0),
+             ("nested", 2, 0, 80, [0.0, 0.0, 1.0, 2.0, -1e-7], 3)]
+    out = {"rows": rows, "upper": upper, "multiplier": np.array(30)}
+    for name, npops, mt, seed, xmap, nested in cases:
+        best, ess = O.ref_de(rows, 3, 2, npops, upper, mt, 30, seed, xmap=xmap, nested=nested)
+        out[name + "_case"] = np.array([npops, mt, seed, nested])
+        out[name + "_xmap"] = np.array(xmap if xmap else [0.0] * 5)
+        out[name + "_best"] = best
+        out[name + "_ess"] = np.array(ess)
+    np.savez_compressed(os.path.join(OUT, "golden_de.npz"), **out)
+
+
 if __name__ == "__main__":
     if not O.ref_available():
         sys.exit("build the reference harness first: make -C oracle ref")
-    golden_is()
-    golden_hky()
-    golden_sw()
-    golden_swap()
-    golden_jointp()
+    gens = {"is": golden_is, "hky": golden_hky, "sw": golden_sw, "swap": golden_swap,
+            "jointp": golden_jointp, "de": golden_de}
+    for name in (sys.argv[1:] or list(gens)):
+        gens[name]()
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))
