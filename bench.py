@@ -509,6 +509,20 @@ def run_surface(args):
     dt = time.perf_counter() - t0
     out["cpu_baseline"] = {"value": round(n / dt, 3), "unit": "points/s", "cores": 1, "kind": "port",
                            "sample": "%d points, exact log-sum-exp over all %d genealogies" % (n, G)}
+    if not args.no_peak_search:
+        # the L-mode peak search (modelloop) on this surface: differential
+        # evolution with 100 x 13 trial points per generation, each generation
+        # one batched tensor-core surface evaluation
+        upper = [20.0] * 5 + [2.0] * 8
+        t0 = time.perf_counter()
+        best, ess_pk, gens, runs, _ = ctx.modelloop(upper, 0, seed=1234, multiplier=100, method=method)
+        dt = time.perf_counter() - t0
+        evals = (gens + runs) * 1300
+        out["peak_search"] = {"generations": gens, "restarts": runs, "seconds": round(dt, 3),
+                              "ms_per_generation": round(1e3 * dt / (gens + runs), 4),
+                              "points_per_s": round(evals / dt, 1), "population": 1300,
+                              "peak_neg_log_density": float(best[-1]), "ess": ess_pk,
+                              "cpu_seconds_per_generation_1core": round(1300 / out["cpu_baseline"]["value"], 1)}
     print(json.dumps(out), flush=True)
     ctx.close()
 
@@ -525,6 +539,7 @@ def main():
     ap.add_argument("--surface-log2g", type=int, default=21, help="log2 genealogies (config 5: 21)")
     ap.add_argument("--surface-log2p", type=int, default=16, help="log2 points (config 5: 16)")
     ap.add_argument("--surface-method", default="tc", choices=["tc", "fp32"])
+    ap.add_argument("--no-peak-search", action="store_true", help="surface: skip the DE peak search")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
