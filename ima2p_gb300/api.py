@@ -33,7 +33,8 @@ REJECT_IS = -1000000000.0
 EXPORTS = [
     "ima_gpu_create", "ima_gpu_destroy", "ima_gpu_error", "ima_gpu_synchronize",
     "ima_gpu_add_locus_is", "ima_gpu_add_locus_hky", "ima_gpu_add_locus_sw", "ima_gpu_set_chains",
-    "ima_gpu_set_genealogy", "ima_gpu_set_genealogies", "ima_gpu_set_pi", "ima_gpu_set_alleles", "ima_gpu_likelihoodIS",
+    "ima_gpu_set_genealogy", "ima_gpu_set_genealogies", "ima_gpu_set_pi", "ima_gpu_set_alleles",
+    "ima_gpu_set_allele_edits", "ima_gpu_likelihoodIS",
     "ima_gpu_likelihoodHKY", "ima_gpu_copyfraclike", "ima_gpu_storescalefactors",
     "ima_gpu_restorescalefactors", "ima_gpu_likelihoodSW", "ima_gpu_get_dlikeA", "ima_gpu_eval",
     "ima_gpu_commit", "ima_gpu_batch_create", "ima_gpu_batch_run", "ima_gpu_batch_results",
@@ -128,6 +129,7 @@ def _declare(L):
         "ima_gpu_surface_load": (I, [P, I, I, P, I, I, I, P]),
         "ima_gpu_surface_eval": (I, [P, I, P, I, I, P, P]),
         "ima_gpu_jointp": (I, [P, P, I, P, P]),
+        "ima_gpu_set_allele_edits": (I, [P, I, P, P, P, P, P]),
         "ima_gpu_surface_info": (I, [P, C.POINTER(I), C.POINTER(I), C.POINTER(I), C.POINTER(I)]),
         "ima_mt19937_seed": (None, [P, C.c_uint32]),
         "ima_mt19937_uniform": (D, [P]),
@@ -239,6 +241,13 @@ class Context:
 
     def set_alleles(self, ci, li, A, ai=0):
         self._ck(self.lib.ima_gpu_set_alleles(self.h, int(ci), int(li), int(ai), _ptr(_i32(A))))
+
+    def set_allele_edits(self, ci, li, node, A, ai=None):
+        """Edit list of single allele states (ima_gpu_set_allele_edits)."""
+        ci, li, node, A = _i32(ci), _i32(li), _i32(node), _i32(A)
+        ai = _i32(np.zeros(len(ci)) if ai is None else ai)
+        self._ck(self.lib.ima_gpu_set_allele_edits(self.h, len(ci), _ptr(ci), _ptr(li), _ptr(ai), _ptr(node),
+                                                   _ptr(A)))
 
     def flush_genealogies(self):
         self._ck(self.lib.ima_gpu_flush_genealogies(self.h))

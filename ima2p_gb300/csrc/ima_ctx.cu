@@ -632,6 +632,28 @@ extern "C" int ima_gpu_set_alleles(ima_ctx *c, int ci, int li, int ai, const int
   return IMA_OK;
 }
 
+extern "C" int ima_gpu_set_allele_edits(ima_ctx *c, int n, const int *ci, const int *li, const int *ai,
+                                        const int *node, const int32_t *A)
+{
+  if (!c || n < 0 || (n > 0 && (!ci || !li || !ai || !node || !A))) return IMA_ERR_ARG;
+  // validate the whole list before applying any edit
+  for (int k = 0; k < n; k++) {
+    if (!c->valid(ci[k], li[k])) return c->fail(IMA_ERR_ARG, "edit %d: chain %d locus %d out of range", k, ci[k], li[k]);
+    const LocusDev &L = c->loci[li[k]].d;
+    if (L.model != IMA_MODEL_SW || ai[k] < 0 || ai[k] >= L.nlinked)
+      return c->fail(IMA_ERR_ARG, "edit %d: locus %d marker %d is not stepwise", k, li[k], ai[k]);
+    const ItemDev &it = c->items[c->item_of(ci[k], li[k])];
+    if (node[k] < 0 || node[k] >= 2 * it.n - 1) return c->fail(IMA_ERR_ARG, "edit %d: node %d out of range", k, node[k]);
+  }
+  for (int k = 0; k < n; k++) {
+    const int item = c->item_of(ci[k], li[k]);
+    const ItemDev &it = c->items[item];
+    c->h_al[it.al_off + (size_t)ai[k] * (2 * it.n - 1) + node[k]] = A[k];
+    mark(c, item);
+  }
+  return IMA_OK;
+}
+
 static int flush_times(ima_ctx *c)
 {
   if (c->tdirty_hi < 0) return IMA_OK;

@@ -97,6 +97,15 @@ int ima_gpu_set_genealogies(ima_ctx *ctx, int npairs, const int32_t *ci, const i
 int ima_gpu_set_pi(ima_ctx *ctx, int ci, int li, const double *pi4);
 /* Allele states of linked marker ai on every node (gtree[i].A[ai]). */
 int ima_gpu_set_alleles(ima_ctx *ctx, int ci, int li, int ai, const int32_t *A);
+/* Edit list of single allele states: gtree[node[k]].A[ai[k]] = A[k] on chain
+ * ci[k], locus li[k], for k < n -- the state finishSWupdateA
+ * (update_gtree_common.cpp:2219-2362) proposes for the moved node.  The
+ * proposal itself (geometric step, bitran sign, Hastings term Aterm) stays on
+ * the host; the likelihood change likeadj - oldlikeadj is the difference of
+ * the batched SW evaluations after and before the edits.  The whole list is
+ * validated first; nothing is applied when any entry is invalid. */
+int ima_gpu_set_allele_edits(ima_ctx *ctx, int n, const int *ci, const int *li, const int *ai,
+                             const int *node, const int32_t *A);
 
 /* --------------------------------------------- per-call reference mirrors
  * Same names, argument meaning, return values and side effects as the

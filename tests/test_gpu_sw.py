@@ -82,3 +82,39 @@ def test_sw_bessel_edge_terms():
             assert st[k] == api.EVAL_SW_ZERO
         else:
             assert abs(res[k] - want) <= 1e-9 * max(1.0, abs(want)), (d, x, res[k], want)
+
+
+@pytest.mark.parametrize("prec", [api.PREC_FAST, api.PREC_FP64])
+def test_sw_allele_edit_list_gives_update_delta(prec):
+    """finishSWupdateA (update_gtree_common.cpp:2219-2362) proposes a new
+    allele for one internal node and returns likeadj - oldlikeadj, the change
+    of the branch terms that touch it.  Shipped as an edit list, the change is
+    the difference of the batched evaluations after and before the edits; it
+    must equal the oracle's difference of full likelihoods."""
+    rng = np.random.default_rng(23)
+    nloci, nch = 3, 8
+    ctx = ctx_with([("sw", 40, 1)] * nloci, 1, nch)
+    trees_, alle, ci, li, u = {}, {}, [], [], []
+    for c in range(nch):
+        for l in range(nloci):
+            t = synth.three_pop_tree(rng, [14, 13, 13], theta=4.0, mig=0.05)
+            A = synth.sw_alleles(rng, t, 1.0)
+            ctx.set_genealogy(c, l, t)
+            ctx.set_alleles(c, l, A)
+            trees_[c, l], alle[c, l] = t, A
+            ci.append(c), li.append(l), u.append(float(rng.lognormal(0, 0.3)))
+    before, _ = ctx.eval(ci, li, u, precision=prec)
+    # one moved node per chain-locus: an internal node, its allele stepped by -3..3
+    node = [int(rng.integers(40, 79)) for _ in ci]
+    newA = [int(alle[c, l][v] + rng.integers(-3, 4)) for c, l, v in zip(ci, li, node)]
+    ctx.set_allele_edits(ci, li, node, newA)
+    after, _ = ctx.eval(ci, li, u, precision=prec)
+    tol = 2 * SW_FAST_ATOL if prec == api.PREC_FAST else 1e-10
+    for k, (c, l) in enumerate(zip(ci, li)):
+        A2 = alle[c, l].copy()
+        A2[node[k]] = newA[k]
+        want = O.sw_likelihood(A2, trees_[c, l], u[k])[0] - O.sw_likelihood(alle[c, l], trees_[c, l], u[k])[0]
+        assert abs((after[k] - before[k]) - want) <= tol, (k, after[k] - before[k], want)
+    # an invalid entry rejects the whole list
+    with pytest.raises(api.ImaError):
+        ctx.set_allele_edits([0, 0], [0, 0], [40, 999], [20, 20])
