@@ -190,9 +190,12 @@ def run_ours(args):
     units = len(ci)
     prec = api.PREC_FAST
     batch = ctx.batch_create(ci, li, u, par, precision=prec)
-    # warm-up (also initialises per-locus constants)
+    # warm-up (also initialises per-locus constants), then the launch-shape
+    # autotuner on the batch's own requests
     for _ in range(args.warmup):
         batch.run(use_graph=True)
+    tuned = batch.autotune(reps=5)
+    batch.run(use_graph=True)
     ctx.synchronize()
     res_fast, st_fast = batch.results()
 
@@ -278,6 +281,10 @@ def run_ours(args):
                           "max_rel": float((err / np.abs(res64[ok])).max()) if len(err) else None},
         "gpu_launches": int(n_launch),
         "clocks": clk.summary(),
+        "autotune": {"hky_variant": tuned[0], "sw_variant": tuned[1],
+                     "variants": "hky: 0 = 128 threads, 1 = 64, 2 = 256, 3 = 128 without the shared-memory "
+                                 "cache, 4 = 128 with registers for 8 CTAs/SM; sw: 0 = 8 chain-loci per CTA, "
+                                 "1 = 4, 2 = 16"},
     }
     # MC3 swap sweeps of every run on the resident sums (the reference's
     # default swaptries = max(1, chains / 10)), committed likelihoods as pdg

@@ -43,6 +43,7 @@ EXPORTS = [
     "ima_gpu_swapchains", "ima_gpu_get_swapcounts", "ima_gpu_surface_load",
     "ima_gpu_surface_eval", "ima_gpu_jointp", "ima_gpu_surface_fp64_noalloc", "ima_gpu_tc_selftest",
     "ima_gpu_surface_info", "ima_mt19937_seed", "ima_mt19937_uniform", "ima_gpu_modelloop",
+    "ima_gpu_batch_autotune", "ima_gpu_batch_set_variants",
     "ima_gpu_timer_begin", "ima_gpu_timer_end",
     "ima_gpu_set_profiling", "ima_gpu_kernel_stats", "ima_gpu_launch_count", "ima_gpu_flush_l2",
     "ima_gpu_memory",
@@ -129,6 +130,8 @@ def _declare(L):
         "ima_gpu_surface_load": (I, [P, I, I, P, I, I, I, P]),
         "ima_gpu_surface_eval": (I, [P, I, P, I, I, P, P]),
         "ima_gpu_jointp": (I, [P, P, I, P, P]),
+        "ima_gpu_batch_autotune": (I, [P, I, I, C.POINTER(I), C.POINTER(I)]),
+        "ima_gpu_batch_set_variants": (I, [P, I, I, I]),
         "ima_gpu_set_allele_edits": (I, [P, I, P, P, P, P, P]),
         "ima_gpu_surface_info": (I, [P, C.POINTER(I), C.POINTER(I), C.POINTER(I), C.POINTER(I)]),
         "ima_mt19937_seed": (None, [P, C.c_uint32]),
@@ -456,6 +459,15 @@ class Batch:
 
     def __init__(self, ctx, handle, n):
         self.ctx, self.handle, self.n = ctx, handle, n
+
+    def autotune(self, reps=5):
+        """ima_gpu_batch_autotune: returns the chosen (hky, sw) launch variants."""
+        h, w = I(), I()
+        self.ctx._ck(self.ctx.lib.ima_gpu_batch_autotune(self.ctx.h, self.handle, int(reps), C.byref(h), C.byref(w)))
+        return h.value, w.value
+
+    def set_variants(self, hky=0, sw=0):
+        self.ctx._ck(self.ctx.lib.ima_gpu_batch_set_variants(self.ctx.h, self.handle, int(hky), int(sw)))
 
     def run(self, use_graph=True):
         self.ctx._ck(self.ctx.lib.ima_gpu_batch_run(self.ctx.h, self.handle, int(use_graph)))

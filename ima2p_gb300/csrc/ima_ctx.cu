@@ -40,6 +40,7 @@ struct Batch {
   cudaGraphExec_t graph = nullptr;
   int maxn_is = 0, maxs_is = 0, maxn_hky = 0, maxs_hky = 0, maxn_sw = 0;
   int cap = 0;  // capacity of the device buffers
+  int hky_variant = 0, sw_variant = 0;  // launch shapes (ima_gpu_batch_autotune)
 };
 
 struct PendingTiming {
@@ -835,7 +836,7 @@ static void enqueue(ima_ctx *c, Batch &b)
     if (b.prec == IMA_PREC_FP64)
       c->launch(IMA_K_HKY_FP64, hky_bytes(c, b), [&] { launch_hky_fp64(P, r, b.nhky, b.maxn_hky, b.d_res + b.nis, b.d_st + b.nis, st); });
     else
-      c->launch(IMA_K_HKY_FAST, hky_bytes(c, b), [&] { launch_hky_fast(P, r, b.nhky, b.maxn_hky, b.maxs_hky, b.d_res + b.nis, b.d_st + b.nis, st); });
+      c->launch(IMA_K_HKY_FAST, hky_bytes(c, b), [&] { launch_hky_fast(P, r, b.nhky, b.maxn_hky, b.maxs_hky, b.hky_variant, b.d_res + b.nis, b.d_st + b.nis, st); });
   }
   if (b.nsw) {
     const ReqDev *r = b.d_req + b.nis + b.nhky;
@@ -843,7 +844,7 @@ static void enqueue(ima_ctx *c, Batch &b)
     if (b.prec == IMA_PREC_FP64)
       c->launch(IMA_K_SW_FP64, sw_bytes(c, b), [&] { launch_sw_fp64(P, r, b.nsw, b.d_res + off, b.d_st + off, st); });
     else
-      c->launch(IMA_K_SW_FAST, sw_bytes(c, b), [&] { launch_sw_fast(P, r, b.nsw, b.maxn_sw, b.d_res + off, b.d_st + off, st); });
+      c->launch(IMA_K_SW_FAST, sw_bytes(c, b), [&] { launch_sw_fast(P, r, b.nsw, b.maxn_sw, b.sw_variant, b.d_res + off, b.d_st + off, st); });
   }
 }
 
@@ -973,6 +974,84 @@ extern "C" int ima_gpu_batch_run(ima_ctx *c, int batch, int use_graph)
   r = c->cuda(cudaGraphLaunch(b.graph, c->st), "graph launch");
   c->launches += (b.nis ? 1 : 0) + (b.nhky ? 1 : 0) + (b.nsw ? 1 : 0);
   return r;
+}
+
+// Launch-shape autotuner: each variant of a kind's kernel runs `reps` times
+// on the batch's own requests (after one untimed run); the fastest is kept
+// unless the default is within 2% of it.  The kernels write only the fresh
+// partial slots and the batch results, so the repeats leave no trace.
+extern "C" int ima_gpu_batch_autotune(ima_ctx *c, int batch, int reps, int *hky_variant, int *sw_variant)
+{
+  if (!c || batch < 0 || batch >= (int)c->batches.size() || !c->batches[batch].live) return IMA_ERR_ARG;
+  Batch &b = c->batches[batch];
+  int r = flush(c);
+  r = r ? r : init_sumlogk(c, b);
+  if (r) return r;
+  if (reps < 1) reps = 1;
+  if (b.prec == IMA_PREC_FAST && (b.nhky || b.nsw)) {
+    Pools P = c->pools();
+    cudaStream_t st = c->st;
+    cudaEvent_t e0 = c->ev(), e1 = c->ev();
+    auto timed = [&](auto launch) -> float {
+      launch();
+      cudaEventRecord(e0, st);
+      for (int k = 0; k < reps; k++) launch();
+      cudaEventRecord(e1, st);
+      float ms = 0.f;
+      if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) return -1.f;
+      c->launches += reps + 1;
+      return ms / reps;
+    };
+    auto pick = [&](int nvar, auto launch_v) -> int {
+      std::vector<float> t(nvar);
+      for (int v = 0; v < nvar; v++) t[v] = timed([&] { launch_v(v); });
+      int best = 0;
+      for (int v = 1; v < nvar; v++)
+        if (t[v] >= 0.f && t[v] < t[best]) best = v;
+      return (t[0] >= 0.f && t[0] <= 1.02f * t[best]) ? 0 : best;
+    };
+    if (b.nhky) {
+      const ReqDev *rq = b.d_req + b.nis;
+      b.hky_variant = pick(HKY_FAST_VARIANTS, [&](int v) {
+        launch_hky_fast(P, rq, b.nhky, b.maxn_hky, b.maxs_hky, v, b.d_res + b.nis, b.d_st + b.nis, st);
+      });
+    }
+    if (b.nsw) {
+      const ReqDev *rq = b.d_req + b.nis + b.nhky;
+      const int off = b.nis + b.nhky;
+      b.sw_variant = pick(SW_FAST_VARIANTS, [&](int v) {
+        launch_sw_fast(P, rq, b.nsw, b.maxn_sw, v, b.d_res + off, b.d_st + off, st);
+      });
+    }
+    c->event_pool.push_back(e0);
+    c->event_pool.push_back(e1);
+    r = c->cuda(cudaGetLastError(), "autotune");
+    if (r) return r;
+    if (b.graph) {  // re-captured with the chosen shapes on the next run
+      cudaStreamSynchronize(c->st);
+      cudaGraphExecDestroy(b.graph);
+      b.graph = nullptr;
+    }
+  }
+  if (hky_variant) *hky_variant = b.hky_variant;
+  if (sw_variant) *sw_variant = b.sw_variant;
+  return IMA_OK;
+}
+
+extern "C" int ima_gpu_batch_set_variants(ima_ctx *c, int batch, int hky_variant, int sw_variant)
+{
+  if (!c || batch < 0 || batch >= (int)c->batches.size() || !c->batches[batch].live) return IMA_ERR_ARG;
+  if (hky_variant < 0 || hky_variant >= HKY_FAST_VARIANTS || sw_variant < 0 || sw_variant >= SW_FAST_VARIANTS)
+    return c->fail(IMA_ERR_ARG, "launch variants out of range (%d, %d)", hky_variant, sw_variant);
+  Batch &b = c->batches[batch];
+  b.hky_variant = hky_variant;
+  b.sw_variant = sw_variant;
+  if (b.graph) {
+    cudaStreamSynchronize(c->st);
+    cudaGraphExecDestroy(b.graph);
+    b.graph = nullptr;
+  }
+  return IMA_OK;
 }
 
 extern "C" int ima_gpu_batch_results(ima_ctx *c, int batch, double *result, int32_t *status)

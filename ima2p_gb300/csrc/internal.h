@@ -75,13 +75,17 @@ void launch_is_sumlogk(const Pools &P, int item, int locus, int maxn, int maxS, 
                        cudaStream_t st);
 void launch_is(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int maxS, double *result,
                int32_t *status, int32_t *site_node, cudaStream_t st);
-void launch_hky_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int maxS,
+// variant: launch shape chosen by the batch autotuner (0 is the default)
+constexpr int HKY_FAST_VARIANTS = 5;  // 128 threads, 64, 256, 128 without the shared-memory cache,
+                                      // 128 with registers for 8 CTAs per SM instead of 12
+constexpr int SW_FAST_VARIANTS = 3;   // 8 chain-loci per CTA, 4, 16
+void launch_hky_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int maxS, int variant,
                      double *result, int32_t *status, cudaStream_t st);
 void launch_hky_fp64(const Pools &P, const ReqDev *reqs, int nreq, int maxn, double *result,
                      int32_t *status, cudaStream_t st);
 void launch_hky_commit(const Pools &P, const int32_t *items, const uint8_t *accept, int n,
                        cudaStream_t st);
-void launch_sw_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, double *result,
+void launch_sw_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int variant, double *result,
                     int32_t *status, cudaStream_t st);
 void launch_sw_fp64(const Pools &P, const ReqDev *reqs, int nreq, double *result,
                     int32_t *status, cudaStream_t st);

@@ -166,13 +166,14 @@ __device__ __forceinline__ int expo_of(float m)  // floor(log2(m)) for normal m 
 }
 
 // ------------------------------------------------------------------ FP32
-// Thread mapping: with S <= HKY_BS patterns, HKY_BS / S nodes of a level are
+// Thread mapping: with S <= BS patterns, BS / S nodes of a level are
 // processed at once (pattern = tid % S), so no division runs per work item;
 // wider loci loop over pattern blocks.  With CACHE, the partials this launch
 // computes are also kept in shared memory ([internal node][pattern]) and
 // daughters are read from there instead of making an L2 round trip per level.
-template <bool CACHE>
-__global__ void __launch_bounds__(HKY_BS, 12) k_hky_fast(Pools P, const ReqDev *reqs,
+// BS threads per CTA, registers for MINB resident CTAs per SM
+template <bool CACHE, int BS, int MINB>
+__global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *reqs,
                                                      double *result, int32_t *status, int maxnl,
                                                      int cache_S)
 {
@@ -192,20 +193,20 @@ __global__ void __launch_bounds__(HKY_BS, 12) k_hky_fast(Pools P, const ReqDev *
   T.order = reinterpret_cast<int16_t *>(smem + lay.order);
   float4 *cpart = reinterpret_cast<float4 *>(smem + lay.total);         // [nint][cache_S]
   int32_t *cexp = reinterpret_cast<int32_t *>(cpart + (size_t)(maxnl / 2) * cache_S);
-  __shared__ double red_d[HKY_BS / 32];
-  __shared__ long long red_e[HKY_BS / 32];
+  __shared__ double red_d[BS / 32];
+  __shared__ long long red_e[BS / 32];
   __shared__ float spi[4];
   __shared__ float smu;
 
   const int tid = threadIdx.x;
   const bool full = (R.e[0] == -1);
-  for (int k = tid; k < nl; k += HKY_BS) {
+  for (int k = tid; k < nl; k += BS) {
     T.nd[k] = P.nodes[it.node_off + k];
     T.slot[k] = P.slot32[it.node_off + k];
     T.dirty[k] = 0;
     T.fresh[k] = full ? 1 : 0;
   }
-  for (int k = tid; k < nint + nlev + 1; k += HKY_BS) T.order[k] = P.sched[it.sched_off + k];
+  for (int k = tid; k < nint + nlev + 1; k += BS) T.order[k] = P.sched[it.sched_off + k];
   T.lstart = T.order + nint;
   if (tid == 0) {
     const double *pid = P.pi + 4 * (size_t)R.item;
@@ -226,7 +227,7 @@ __global__ void __launch_bounds__(HKY_BS, 12) k_hky_fast(Pools P, const ReqDev *
   if (!full) __syncthreads();
   const float2 *tff = P.tff + it.node_off;
   const float kpa = (float)(R.par - 1.0);
-  for (int c = tid; c < nl; c += HKY_BS) {
+  for (int c = tid; c < nl; c += BS) {
     int d = T.nd[c].down;
     if (d < 0 || !T.fresh[d]) continue;
     float pil[4] = {spi[0], spi[1], spi[2], spi[3]};
@@ -239,11 +240,11 @@ __global__ void __launch_bounds__(HKY_BS, 12) k_hky_fast(Pools P, const ReqDev *
   int32_t *pexp = P.pexp + it.part_off;
   const int8_t *seq = P.seq + L.seq_off;
   // (node slot, pattern) of this thread
-  const bool narrow = S <= HKY_BS;
-  const int jstep = narrow ? HKY_BS / S : 1;
+  const bool narrow = S <= BS;
+  const int jstep = narrow ? BS / S : 1;
   const int js = narrow ? tid / S : 0;
   const int is = narrow ? tid - js * S : tid;
-  const int istep = narrow ? S : HKY_BS;  // narrow: one pattern per thread
+  const int istep = narrow ? S : BS;  // narrow: one pattern per thread
   const bool active = !narrow || js < jstep;
   for (int lv = 0; lv < nlev; lv++) {
     const int beg = T.lstart[lv], cnt = T.lstart[lv + 1] - beg;
@@ -322,7 +323,7 @@ __global__ void __launch_bounds__(HKY_BS, 12) k_hky_fast(Pools P, const ReqDev *
   const int32_t *mult = P.mult + L.mult_off;
   double acc = 0.0;
   long long acce = 0;
-  for (int i = tid; i < S; i += HKY_BS) {
+  for (int i = tid; i < S; i += BS) {
     float4 Lr;
     int er;
     if (CACHE && T.fresh[root]) {
@@ -351,12 +352,12 @@ __global__ void __launch_bounds__(HKY_BS, 12) k_hky_fast(Pools P, const ReqDev *
     red_e[tid >> 5] = acce;
   }
   // recomputed marks for the commit step
-  for (int k = tid; k < nl; k += HKY_BS) P.fresh32[it.node_off + k] = (k >= n) ? T.fresh[k] : 0;
+  for (int k = tid; k < nl; k += BS) P.fresh32[it.node_off + k] = (k >= n) ? T.fresh[k] : 0;
   __syncthreads();
   if (tid == 0) {
     double s = 0.0;
     long long se = 0;
-    for (int w = 0; w < HKY_BS / 32; w++) { s += red_d[w]; se += red_e[w]; }
+    for (int w = 0; w < BS / 32; w++) { s += red_d[w]; se += red_e[w]; }
     result[blockIdx.x] = s + (double)se * LN2;
     P.pdg_new[R.item] = result[blockIdx.x];
     status[blockIdx.x] = IMA_EVAL_OK;
@@ -506,22 +507,35 @@ size_t hky_smem(int maxn, size_t elem) { return hky_layout(2 * maxn - 1, elem).t
 // fits in this budget (keeps >= 3 CTAs per SM).
 constexpr size_t HKY_CACHE_BUDGET = 64 * 1024;
 
-void launch_hky_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int maxS,
+template <int BS, int MINB>
+static void hky_fast_bs(const Pools &P, const ReqDev *reqs, int nreq, int maxnl, int maxS, bool cache_ok,
+                        double *result, int32_t *status, cudaStream_t st)
+{
+  size_t base = hky_smem((maxnl + 1) / 2, sizeof(float));
+  size_t cache = (size_t)(maxnl / 2) * maxS * (sizeof(float4) + sizeof(int32_t));
+  if (cache_ok && cache <= HKY_CACHE_BUDGET) {
+    size_t sm = base + cache;
+    if (sm > 48 * 1024)
+      cudaFuncSetAttribute(k_hky_fast<true, BS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_hky_fast<true, BS, MINB><<<nreq, BS, sm, st>>>(P, reqs, result, status, maxnl, maxS);
+  } else {
+    if (base > 48 * 1024)
+      cudaFuncSetAttribute(k_hky_fast<false, BS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)base);
+    k_hky_fast<false, BS, MINB><<<nreq, BS, base, st>>>(P, reqs, result, status, maxnl, 0);
+  }
+}
+
+void launch_hky_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int maxS, int variant,
                      double *result, int32_t *status, cudaStream_t st)
 {
   if (nreq <= 0) return;
   const int maxnl = 2 * maxn - 1;
-  size_t base = hky_smem(maxn, sizeof(float));
-  size_t cache = (size_t)(maxnl / 2) * maxS * (sizeof(float4) + sizeof(int32_t));
-  if (cache <= HKY_CACHE_BUDGET) {
-    size_t sm = base + cache;
-    if (sm > 48 * 1024)
-      cudaFuncSetAttribute(k_hky_fast<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_hky_fast<true><<<nreq, HKY_BS, sm, st>>>(P, reqs, result, status, maxnl, maxS);
-  } else {
-    if (base > 48 * 1024)
-      cudaFuncSetAttribute(k_hky_fast<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)base);
-    k_hky_fast<false><<<nreq, HKY_BS, base, st>>>(P, reqs, result, status, maxnl, 0);
+  switch (variant) {
+    case 1: hky_fast_bs<64, 24>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
+    case 2: hky_fast_bs<256, 6>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
+    case 3: hky_fast_bs<128, 12>(P, reqs, nreq, maxnl, maxS, false, result, status, st); break;
+    case 4: hky_fast_bs<128, 8>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
+    default: hky_fast_bs<128, 12>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
   }
 }
 

@@ -192,8 +192,6 @@ __device__ __forceinline__ ff warp_sum_ff(ff v)
   return v;
 }
 
-constexpr int SW_IPC = 8;        // chain-loci per CTA (one warp reduces each)
-constexpr int SW_FAST_BS = 256;
 // branch terms (float2) and the |d| >= 2 queue (int16) live in dynamic shared
 // memory sized for the batch's largest chain-locus
 
@@ -201,7 +199,9 @@ constexpr int SW_FAST_BS = 256;
 // branch-free core, with |d| >= 2 branches queued; (B) the queued Miller
 // recurrences, packed onto consecutive threads; (C) one warp per chain-locus
 // sums its branch terms in float-float.
-__global__ void __launch_bounds__(SW_FAST_BS) k_sw_fast(Pools P, const ReqDev *reqs, int nreq,
+// IPC chain-loci per CTA of 32 * IPC threads (one warp reduces each)
+template <int IPC>
+__global__ void __launch_bounds__(32 * IPC) k_sw_fast(Pools P, const ReqDev *reqs, int nreq,
                                                         double *result, int32_t *status, int maxb)
 {
   __shared__ SwTables T;
@@ -209,11 +209,11 @@ __global__ void __launch_bounds__(SW_FAST_BS) k_sw_fast(Pools P, const ReqDev *r
   float2 *vals = reinterpret_cast<float2 *>(sw_smem);
   int16_t *queue = reinterpret_cast<int16_t *>(vals + maxb);
   __shared__ int qn;
-  __shared__ int bstart[SW_IPC + 1];
-  __shared__ int zero[SW_IPC];
-  __shared__ float2 uff[SW_IPC], trff[SW_IPC];
-  const int r0 = blockIdx.x * SW_IPC;
-  const int nit = min(SW_IPC, nreq - r0);
+  __shared__ int bstart[IPC + 1];
+  __shared__ int zero[IPC];
+  __shared__ float2 uff[IPC], trff[IPC];
+  const int r0 = blockIdx.x * IPC;
+  const int nit = min(IPC, nreq - r0);
   const int tid = threadIdx.x;
   if (tid < 36) {
     int t = tid / 9, k = tid % 9;
@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(SW_FAST_BS) k_sw_fast(Pools P, const ReqDev *r
   __syncthreads();
   const int total = bstart[nit];
   // ---- phase A
-  for (int b = tid; b < total; b += SW_FAST_BS) {
+  for (int b = tid; b < total; b += (32 * IPC)) {
     int i = 0;
     while (b >= bstart[i + 1]) i++;
     const ReqDev &R = reqs[r0 + i];
@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(SW_FAST_BS) k_sw_fast(Pools P, const ReqDev *r
   }
   __syncthreads();
   // ---- phase B: |d| >= 2
-  for (int q = tid; q < qn; q += SW_FAST_BS) {
+  for (int q = tid; q < qn; q += (32 * IPC)) {
     const int b = queue[q];
     int i = 0;
     while (b >= bstart[i + 1]) i++;
@@ -408,15 +408,25 @@ int sw_init_tables()
   return 0;
 }
 
-void launch_sw_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, double *result,
+template <int IPC>
+static void sw_fast_ipc(const Pools &P, const ReqDev *reqs, int nreq, int maxn, double *result, int32_t *status,
+                        cudaStream_t st)
+{
+  const int maxb = IPC * (2 * maxn - 1);  // queue entries are int16: IPC * (2 maxn - 1) < 32768
+  const size_t sm = (size_t)maxb * (sizeof(float2) + sizeof(int16_t));
+  if (sm > 48 * 1024)
+    cudaFuncSetAttribute(k_sw_fast<IPC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_sw_fast<IPC><<<(nreq + IPC - 1) / IPC, 32 * IPC, sm, st>>>(P, reqs, nreq, result, status, maxb);
+}
+
+void launch_sw_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int variant, double *result,
                     int32_t *status, cudaStream_t st)
 {
   if (nreq <= 0) return;
-  const int maxb = SW_IPC * (2 * maxn - 1);
-  const size_t sm = (size_t)maxb * (sizeof(float2) + sizeof(int16_t));
-  if (sm > 48 * 1024)
-    cudaFuncSetAttribute(k_sw_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_sw_fast<<<(nreq + SW_IPC - 1) / SW_IPC, SW_FAST_BS, sm, st>>>(P, reqs, nreq, result, status, maxb);
+  // wide variants only while the branch queue indexes fit int16
+  if (variant == 2 && 16 * (2 * maxn - 1) < 32768) sw_fast_ipc<16>(P, reqs, nreq, maxn, result, status, st);
+  else if (variant == 1) sw_fast_ipc<4>(P, reqs, nreq, maxn, result, status, st);
+  else sw_fast_ipc<8>(P, reqs, nreq, maxn, result, status, st);
 }
 
 void launch_sw_fp64(const Pools &P, const ReqDev *reqs, int nreq, double *result,

@@ -160,6 +160,17 @@ int ima_gpu_batch_create(ima_ctx *ctx, int npairs, const int32_t *ci, const int3
                          const double *u, const double *kappa, const int32_t *edits,
                          const int32_t *ai, int precision, int *batch);
 int ima_gpu_batch_run(ima_ctx *ctx, int batch, int use_graph);
+/* Launch-shape autotuner for a batch's FP32 kernels: times each variant on
+ * the batch's own requests (reps timed runs after one untimed) and keeps the
+ * fastest -- HKY: 128 threads per chain-locus (0, the default), 64 (1), 256
+ * (2), 128 without the shared-memory partial cache (3), 128 with registers
+ * for 8 resident CTAs per SM instead of 12 (4); SW: 8 chain-loci per CTA
+ * (0), 4 (1), 16 (2).  The default stays unless another variant is more
+ * than 2% faster.  Every variant gives the same likelihoods up to the order
+ * of the final FP64 reduction.  Out (may be NULL): the chosen variants. */
+int ima_gpu_batch_autotune(ima_ctx *ctx, int batch, int reps, int *hky_variant, int *sw_variant);
+/* Pins a batch's launch variants (numbering as above). */
+int ima_gpu_batch_set_variants(ima_ctx *ctx, int batch, int hky_variant, int sw_variant);
 int ima_gpu_batch_results(ima_ctx *ctx, int batch, double *result, int32_t *status);
 int ima_gpu_batch_destroy(ima_ctx *ctx, int batch);
 /* Copy every staged genealogy edit to the device now (normally implicit). */

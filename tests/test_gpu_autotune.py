@@ -1,0 +1,58 @@
+"""The batch autotuner (ima_gpu_batch_autotune) on a small config-4-shaped
+mixed workload: every launch variant of the FP32 kernels gives the plain FP64
+form's likelihoods (HKY within 2e-6 relative, SW within 1e-9 per locus) and
+the variants agree with one another up to the order of the final FP64
+reduction; the tuned batch replays as a graph with the chosen shapes."""
+import numpy as np
+import pytest
+
+from ima2p_gb300 import api, workloads
+from tests._gpu import ctx_with
+
+pytestmark = pytest.mark.gpu
+
+HKY_VARIANTS, SW_VARIANTS = 5, 3
+
+
+def _mixed_ctx():
+    wl = workloads.make_mixed(seed=9, n_hky=12, n_sw=6, nruns=2, cpr=8)
+    ctx = ctx_with(wl.loci, wl.nruns, wl.cpr)
+    wl.upload(ctx)
+    ci, li = wl.pairs()
+    return wl, ctx, ci, li, wl.u.ravel(), wl.par.ravel()
+
+
+def _check(res, ref, is_hky):
+    np.testing.assert_allclose(res[is_hky], ref[is_hky], rtol=2e-6)
+    assert np.max(np.abs(res[~is_hky] - ref[~is_hky])) <= 1e-9
+
+
+def test_every_variant_matches_fp64_and_autotune_picks_one():
+    wl, ctx, ci, li, u, par = _mixed_ctx()
+    is_hky = li < 12
+    ref_b = ctx.batch_create(ci, li, u, par, precision=api.PREC_FP64)
+    ref_b.run(use_graph=False)
+    ref = ref_b.results()[0]
+    b = ctx.batch_create(ci, li, u, par, precision=api.PREC_FAST)
+    outs = []
+    for v in range(HKY_VARIANTS):
+        b.set_variants(v, v % SW_VARIANTS)
+        b.run(use_graph=True)
+        r = b.results()[0]
+        _check(r, ref, is_hky)
+        outs.append(r)
+    for r in outs[1:]:
+        np.testing.assert_allclose(r, outs[0], rtol=1e-12)
+    hv, sv = b.autotune(reps=3)
+    assert 0 <= hv < HKY_VARIANTS and 0 <= sv < SW_VARIANTS
+    b.run(use_graph=True)
+    np.testing.assert_allclose(b.results()[0], outs[0], rtol=1e-12)
+
+
+def test_variants_out_of_range_are_rejected():
+    wl, ctx, ci, li, u, par = _mixed_ctx()
+    b = ctx.batch_create(ci, li, u, par, precision=api.PREC_FAST)
+    with pytest.raises(api.ImaError):
+        b.set_variants(HKY_VARIANTS, 0)
+    with pytest.raises(api.ImaError):
+        b.set_variants(0, SW_VARIANTS)
