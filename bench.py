@@ -516,6 +516,29 @@ def run_surface(args):
     dt = time.perf_counter() - t0
     out["cpu_baseline"] = {"value": round(n / dt, 3), "unit": "points/s", "cores": 1, "kind": "port",
                            "sample": "%d points, exact log-sum-exp over all %d genealogies" % (n, G)}
+    # 1-D marginal densities (fillvec): 13 parameters x GRIDSIZE 1000 grid
+    # points, each a sum over all G genealogies, FP64 as the reference sums it
+    pmin, pmax = np.zeros(13), np.array([20.0] * 5 + [2.0] * 8)
+    ctx.fillvec(pmin, pmax, 1000)
+    ctx.set_profiling(True)
+    m0 = ctx.kernel_stats(api.K_MARGIN)
+    t0 = time.perf_counter()
+    xs_m, ys_m = ctx.fillvec(pmin, pmax, 1000)
+    wall_m = time.perf_counter() - t0
+    m1 = ctx.kernel_stats(api.K_MARGIN)
+    ctx.set_profiling(False)
+    dev_m = (m1[1] - m0[1]) / max(1, m1[0] - m0[0])
+    t0 = time.perf_counter()
+    nm_cpu = 0
+    while time.perf_counter() - t0 < max(0.5, args.cpu_seconds / 4) or nm_cpu == 0:
+        O.margincalc(rows, 5, 8, nm_cpu % 13, xs_m[nm_cpu % 13, (nm_cpu * 37) % 1000])
+        nm_cpu += 1
+    cpu_m = nm_cpu / (time.perf_counter() - t0)
+    out["marginals"] = {"grid_points": 13000, "ms_device": round(dev_m, 3), "ms_e2e": round(1e3 * wall_m, 3),
+                        "points_per_s": round(13000 / (dev_m / 1e3), 1),
+                        "terms_per_s": round(13000 * G / (dev_m / 1e3), 1),
+                        "cpu_points_per_s_1core": round(cpu_m, 3),
+                        "note": "fillvec: margincalc on every parameter's grid, FP64 sums without a shift"}
     if not args.no_peak_search:
         # the L-mode peak search (modelloop) on this surface: differential
         # evolution with 100 x 13 trial points per generation, each generation

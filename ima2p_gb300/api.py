@@ -24,7 +24,7 @@ PREC_FAST, PREC_FP64 = 0, 1
 EVAL_OK, EVAL_IS_REJECT, EVAL_IS_FAIL, EVAL_SW_ZERO = 0, 1, 2, 3
 SURF_FAST, SURF_FP64, SURF_COMPAT, SURF_TC = 0, 1, 2, 3
 K_IS, K_IS_SUMLOGK, K_HKY_FAST, K_HKY_FP64, K_SW_FAST, K_SW_FP64, K_SWAP, K_SURF_FAST, \
-    K_SURF_FP64, K_SURF_COMPAT, K_SURF_TC = range(11)
+    K_SURF_FP64, K_SURF_COMPAT, K_SURF_TC, K_MARGIN = range(12)
 KERNEL_NAMES = ["is", "is_sumlogk", "hky_fast", "hky_fp64", "sw_fast", "sw_fp64", "swap",
                 "surf_fast", "surf_fp64", "surf_compat", "surf_tc"]
 REJECT_IS = -1000000000.0
@@ -43,7 +43,7 @@ EXPORTS = [
     "ima_gpu_swapchains", "ima_gpu_get_swapcounts", "ima_gpu_surface_load",
     "ima_gpu_surface_eval", "ima_gpu_jointp", "ima_gpu_surface_fp64_noalloc", "ima_gpu_tc_selftest",
     "ima_gpu_surface_info", "ima_mt19937_seed", "ima_mt19937_uniform", "ima_gpu_modelloop",
-    "ima_gpu_batch_autotune", "ima_gpu_batch_set_variants",
+    "ima_gpu_batch_autotune", "ima_gpu_batch_set_variants", "ima_gpu_margincalc", "ima_gpu_fillvec",
     "ima_gpu_timer_begin", "ima_gpu_timer_end",
     "ima_gpu_set_profiling", "ima_gpu_kernel_stats", "ima_gpu_launch_count", "ima_gpu_flush_l2",
     "ima_gpu_memory",
@@ -131,6 +131,8 @@ def _declare(L):
         "ima_gpu_surface_eval": (I, [P, I, P, I, I, P, P]),
         "ima_gpu_jointp": (I, [P, P, I, P, P]),
         "ima_gpu_batch_autotune": (I, [P, I, I, C.POINTER(I), C.POINTER(I)]),
+        "ima_gpu_margincalc": (I, [P, I, P, P, D, I, P, P]),
+        "ima_gpu_fillvec": (I, [P, I, P, P, P, P, P]),
         "ima_gpu_batch_set_variants": (I, [P, I, I, I]),
         "ima_gpu_set_allele_edits": (I, [P, I, P, P, P, P, P]),
         "ima_gpu_surface_info": (I, [P, C.POINTER(I), C.POINTER(I), C.POINTER(I), C.POINTER(I)]),
@@ -383,6 +385,23 @@ class Context:
         e = np.zeros(1)
         self._ck(self.lib.ima_gpu_jointp(self.h, _ptr(_f64(x)), int(calc_ess), _ptr(e), _ptr(q)))
         return float(q[0]), float(e[0])
+
+    def margincalc(self, param, x, yadjust=0.0, logi=0, expo_mean=None):
+        param, x = _i32(np.atleast_1d(param)), _f64(np.atleast_1d(x))
+        out = np.zeros(len(x))
+        em = _f64(expo_mean) if expo_mean is not None else None
+        self._ck(self.lib.ima_gpu_margincalc(self.h, len(x), _ptr(param), _ptr(x), float(yadjust), int(logi),
+                                             _ptr(em) if em is not None else None, _ptr(out)))
+        return out
+
+    def fillvec(self, pmin, pmax, gridsize=1000, expo_mean=None):
+        n = len(pmin)
+        xs = np.zeros((n, gridsize))
+        ys = np.zeros((n, gridsize))
+        em = _f64(expo_mean) if expo_mean is not None else None
+        self._ck(self.lib.ima_gpu_fillvec(self.h, int(gridsize), _ptr(_f64(pmin)), _ptr(_f64(pmax)),
+                                          _ptr(em) if em is not None else None, _ptr(xs), _ptr(ys)))
+        return xs, ys
 
     def surface_info(self):
         G, np_, nm, npops = I(), I(), I(), I()

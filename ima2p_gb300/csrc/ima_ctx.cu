@@ -141,6 +141,8 @@ struct ima_ctx {
   double *d_lognorm = nullptr;
   void *d_sscratch = nullptr;
   size_t sscratch_cap = 0;
+  void *d_mscratch = nullptr;  // marginal densities: points, partial sums
+  size_t mscratch_cap = 0;
   // row-derived surface operands held in the scratch: 0 none, 1 FP32 (split
   // precision screen), 2 FP32 + bf16 planes (tensor-core screen); for the
   // model type srows_model
@@ -299,7 +301,8 @@ extern "C" void ima_gpu_destroy(ima_ctx *c)
                   c->d_slot32, c->d_fresh32, c->d_slot64, c->d_fresh64, c->d_pdg, c->d_pdg_new,
                   c->d_beta, c->d_allbetas, c->d_probg, c->d_S, c->d_swapcount, c->d_tempcount,
                   c->d_used, c->d_swap0ok, c->d_ctr, c->d_uni, c->d_rows, c->d_lognorm,
-                  c->d_sscratch, c->d_sx, c->d_sq, c->d_sess, c->d_citems, c->d_cacc, c->d_flush};
+                  c->d_sscratch, c->d_sx, c->d_sq, c->d_sess, c->d_citems, c->d_cacc, c->d_flush,
+                  c->d_mscratch};
   for (void *p : devs)
     if (p) cudaFree(p);
   void *hosts[] = {c->h_nodes, c->h_t64, c->h_tff, c->h_sched, c->h_nlev, c->h_len, c->h_pi, c->h_al};
@@ -1339,6 +1342,110 @@ extern "C" int ima_gpu_surface_info(ima_ctx *c, int *G, int *np, int *nm, int *n
   if (np) *np = c->snp;
   if (nm) *nm = c->snm;
   if (npops) *npops = c->snpops;
+  return IMA_OK;
+}
+
+// ---------------------------------------------------------- 1-D marginals
+static int margin_run(ima_ctx *c, int n, const int32_t *param, const double *x, double yadjust, int logi,
+                      const double *expo_mean, double *out)
+{
+  const int npar = c->snp + c->snm;
+  for (int k = 0; k < n; k++) {
+    if (param[k] < 0 || param[k] >= npar) return c->fail(IMA_ERR_ARG, "point %d: parameter %d out of range", k, param[k]);
+    if (!(x[k] > 0.0)) return c->fail(IMA_ERR_ARG, "point %d: x must be > 0", k);
+  }
+  if (expo_mean)
+    for (int i = 0; i < c->snm; i++)
+      if (!(expo_mean[i] > 0.0)) return c->fail(IMA_ERR_ARG, "exponential prior mean %d must be > 0", i);
+  const int nchunks = margin_chunks(c->sG, n);
+  // one device block: param | x | means | out | partials
+  const size_t bytes = 256 * 5 + (size_t)n * 4 + (size_t)n * 8 + 64 * 8 + (size_t)n * 8 + (size_t)n * nchunks * 8;
+  if (bytes > c->mscratch_cap) {
+    cudaFree(c->d_mscratch);
+    c->d_mscratch = dev_alloc<char>(bytes, c->dev_bytes, c->st);
+    if (!c->d_mscratch) return c->fail(IMA_ERR_NOMEM, "marginal scratch (%zu bytes)", bytes);
+    c->mscratch_cap = bytes;
+  }
+  char *p = static_cast<char *>(c->d_mscratch);
+  auto take = [&](size_t b) {
+    char *q = p;
+    p += (b + 255) / 256 * 256;
+    return q;
+  };
+  int32_t *d_param = reinterpret_cast<int32_t *>(take((size_t)n * 4));
+  double *d_x = reinterpret_cast<double *>(take((size_t)n * 8));
+  double *d_mean = reinterpret_cast<double *>(take(64 * 8));
+  double *d_out = reinterpret_cast<double *>(take((size_t)n * 8));
+  double *d_part = reinterpret_cast<double *>(take((size_t)n * nchunks * 8));
+  MarginArgs a;
+  a.G = c->sG;
+  a.rowlen = c->srowlen;
+  a.np = c->snp;
+  a.nm = c->snm;
+  a.n = n;
+  a.logi = logi;
+  a.yadjust = yadjust;
+  a.ccp = 0;  // gsampinf layout (initialize.cpp:709-718)
+  a.fcp = a.ccp + a.np;
+  a.hccp = a.fcp + a.np;
+  a.mcp = a.hccp + a.np;
+  a.fmp = a.mcp + a.nm;
+  a.qip = a.fmp + a.nm;
+  a.mip = a.qip + a.np;
+  a.rows = c->d_rows;
+  a.param = d_param;
+  a.x = d_x;
+  a.expo_mean = expo_mean ? d_mean : nullptr;
+  int r = c->cuda(cudaMemcpyAsync(d_param, param, (size_t)n * 4, cudaMemcpyHostToDevice, c->st), "marginal points");
+  r = r ? r : c->cuda(cudaMemcpyAsync(d_x, x, (size_t)n * 8, cudaMemcpyHostToDevice, c->st), "marginal points");
+  if (expo_mean) r = r ? r : c->cuda(cudaMemcpyAsync(d_mean, expo_mean, (size_t)c->snm * 8, cudaMemcpyHostToDevice, c->st), "means");
+  if (r) return r;
+  int lr = 0;
+  c->launch(IMA_K_MARGIN, (double)c->sG * c->srowlen * 4, [&] { lr = launch_margin(a, d_part, nchunks, d_out, c->st); });
+  c->launches += 1;  // pass + merge
+  if (lr) return c->fail(IMA_ERR_ARG, "marginal: unsupported shape (%d)", lr);
+  r = c->cuda(cudaGetLastError(), "marginal launch");
+  r = r ? r : c->cuda(cudaMemcpyAsync(out, d_out, (size_t)n * 8, cudaMemcpyDeviceToHost, c->st), "marginal values");
+  return r ? r : c->cuda(cudaStreamSynchronize(c->st), "marginal");
+}
+
+extern "C" int ima_gpu_margincalc(ima_ctx *c, int n, const int32_t *param, const double *x, double yadjust, int logi,
+                                  const double *expo_mean, double *out)
+{
+  if (!c || n < 1 || !param || !x || !out) return IMA_ERR_ARG;
+  if (!c->d_rows) return c->fail(IMA_ERR_STATE, "call ima_gpu_surface_load first");
+  cudaSetDevice(c->device);
+  return margin_run(c, n, param, x, yadjust, logi, expo_mean, out);
+}
+
+extern "C" int ima_gpu_fillvec(ima_ctx *c, int gridsize, const double *pmin, const double *pmax,
+                               const double *expo_mean, double *x_out, double *y_out)
+{
+  if (!c || gridsize < 1 || !pmin || !pmax || !y_out) return IMA_ERR_ARG;
+  if (!c->d_rows) return c->fail(IMA_ERR_STATE, "call ima_gpu_surface_load first");
+  cudaSetDevice(c->device);
+  const int npar = c->snp + c->snm;
+  std::vector<int32_t> param;
+  std::vector<double> x;
+  std::vector<int> where;  // y_out index of each request
+  for (int p = 0; p < npar; p++) {
+    for (int j = 0; j < gridsize; j++) {
+      // the grids of setup_iparams / setimigarray (initialize.cpp:189-194, :236-241)
+      const double xj = pmin[p] + ((j + 0.5) * (pmax[p] - pmin[p])) / gridsize;
+      if (x_out) x_out[(size_t)p * gridsize + j] = xj;
+      y_out[(size_t)p * gridsize + j] = 0.0;
+      // fillvec skips migration rates whose prior is (near) zero (MPRIORMIN)
+      if (p >= c->snp && !(pmax[p] > 0.000001)) continue;
+      param.push_back(p);
+      x.push_back(xj);
+      where.push_back(p * gridsize + j);
+    }
+  }
+  if (param.empty()) return IMA_OK;
+  std::vector<double> y(param.size());
+  int r = margin_run(c, (int)param.size(), param.data(), x.data(), 0.0, 0, expo_mean, y.data());
+  if (r) return r;
+  for (size_t k = 0; k < param.size(); k++) y_out[where[k]] = y[k];
   return IMA_OK;
 }
 

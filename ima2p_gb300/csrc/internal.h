@@ -128,3 +128,16 @@ int launch_surface_tc(const SurfArgs &a, void *scratch, size_t scratch_bytes, in
 size_t surface_tc_scratch_bytes(int G, int npoints);
 int tc_selftest(cudaStream_t st, void *scratch, size_t bytes, int *h_bad, float *h_maxerr);
 size_t surface_fp64_scratch_bytes(int G, int npoints);
+
+// 1-D marginal densities (margincalc)
+struct MarginArgs {
+  int G, rowlen, np, nm, n, logi;
+  int ccp, fcp, hccp, mcp, fmp, qip, mip;  // gsampinf column offsets
+  const float *rows;        // [G][rowlen]
+  const int32_t *param;     // [n] parameter index (population sizes first)
+  const double *x;          // [n]
+  const double *expo_mean;  // [nm] or null
+  double yadjust;
+};
+int margin_chunks(int G, int n);
+int launch_margin(const MarginArgs &a, double *part, int nchunks, double *out, cudaStream_t st);

@@ -225,6 +225,23 @@ int ima_gpu_tc_selftest(ima_ctx *ctx, int *mismatches, float *max_abs_err);
 
 /* jointp (jointfind.cpp:885-1047) at one point, reference semantics. */
 int ima_gpu_jointp(ima_ctx *ctx, const double *x, int calc_ess, double *effective_n, double *q);
+/* margincalc (surface_call_functions.cpp:119-175) at n points over the
+ * loaded genealogies: out[k] = (logi ? log s (LOWLOG -1e200 when s <= 0) : s)
+ * - yadjust, where s = (1/G) sum_g exp(term_g) is the marginal posterior
+ * density of parameter param[k] (population sizes first, then migration
+ * rates) at x[k] > 0, summed in FP64 without a shift as the reference sums
+ * it.  expo_mean: NULL, or the prior mean of every migration parameter when
+ * the migration prior is exponential (EXPOMIGRATIONPRIOR).  The peak and 95%
+ * searches (marginalopt, margin95) call it from the host. */
+int ima_gpu_margincalc(ima_ctx *ctx, int n, const int32_t *param, const double *x, double yadjust, int logi,
+                       const double *expo_mean, double *out);
+/* fillvec (histograms.cpp:82-99): every parameter's marginal density on its
+ * grid x_j = pmin + (j + 0.5)(pmax - pmin) / gridsize (initialize.cpp:189-194,
+ * :236-241; GRIDSIZE is 1000).  x_out (may be NULL) and y_out are
+ * [np+nm][gridsize]; migration rates whose prior maximum is at most
+ * MPRIORMIN (1e-6) are skipped, as fillvec skips them, with y = 0. */
+int ima_gpu_fillvec(ima_ctx *ctx, int gridsize, const double *pmin, const double *pmax,
+                    const double *expo_mean, double *x_out, double *y_out);
 /* The loaded surface's shape (any pointer may be NULL). */
 int ima_gpu_surface_info(ima_ctx *ctx, int *G, int *numpopsizeparams, int *nummigrateparams, int *npops);
 
@@ -300,7 +317,8 @@ int ima_gpu_kernel_stats(ima_ctx *ctx, int kind, long long *launches, double *ms
 #define IMA_K_SURF_FP64 8
 #define IMA_K_SURF_COMPAT 9
 #define IMA_K_SURF_TC 10
-#define IMA_K_COUNT 11
+#define IMA_K_MARGIN 11
+#define IMA_K_COUNT 12
 /* Total kernel launches issued by this library on the context. */
 int ima_gpu_launch_count(ima_ctx *ctx, long long *n);
 /* Write a device buffer larger than L2 (evicts resident data). */

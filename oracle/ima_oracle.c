@@ -803,3 +803,36 @@ int ora_modelloop(int G, int rowlen, const float *g, int np, int nm, int npops,
   free(lo); free(hi); free(pop); free(trial); free(full); free(bestv);
   return gens;
 }
+
+/* ======================================================================
+ * 1-D marginal densities (surface_call_functions.cpp:119-175)
+ * ==================================================================== */
+static long ora_intround(double v) { return v >= 0 ? (long)(v + 0.5) : (long)(v - 0.5); } /* INTEGERROUND */
+
+double ora_margincalc(int G, int rowlen, const float *g, int np, int nm, int pi,
+                      double x, double yadjust, int logi, const double *expo_mean)
+{
+  int ccp, fcp, hccp, mcp, fmp, qip, mip, pdgp, probgp;
+  ora_gsamp_offsets(np, nm, &ccp, &fcp, &hccp, &mcp, &fmp, &qip, &mip, &pdgp, &probgp);
+  double meani = 0.0;
+  if (expo_mean && pi >= np && pi < np + nm) meani = 1.0 / expo_mean[pi - np];
+  double sum = 0.0;
+  for (int e = 0; e < G; e++) {
+    const float *r = g + (size_t)e * rowlen;
+    if (pi < np) {
+      int p = pi;
+      double hval = r[hccp + p];
+      double temp = -r[qip + p] + ora_intround(r[ccp + p]) * (ORA_LOG2 - log(x)) - hval - 2 * r[fcp + p] / x;
+      sum += exp(temp);
+    } else {
+      int p = pi - np;
+      if (expo_mean)
+        sum += exp(-r[mip + p] + log(meani) - x * meani + ora_intround(r[mcp + p]) * log(x) - r[fmp + p] * x);
+      else
+        sum += exp(-r[mip + p] + ora_intround(r[mcp + p]) * log(x) - r[fmp + p] * x);
+    }
+  }
+  sum /= G;
+  if (logi) sum = (sum <= 0) ? -1e200 : log(sum);
+  return sum - yadjust;
+}

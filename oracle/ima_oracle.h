@@ -114,6 +114,15 @@ double ora_jointp_compat(int G, int rowlen, const float *g, int np, int nm,
                          const double *x, double *ess);
 void ora_eexp(double x, double *m, int *z);
 
+/* margincalc (surface_call_functions.cpp:119-175): the marginal posterior
+ * density of parameter pi (population sizes first, then migration rates) at
+ * x, (1/G) sum_g exp(term_g), summed in genealogy order without a shift, then
+ * log'd when logi (LOWLOG -1e200 for a sum <= 0), less yadjust.  expo_mean:
+ * NULL, or the prior means of the migration parameters when their prior is
+ * exponential (EXPOMIGRATIONPRIOR). */
+double ora_margincalc(int G, int rowlen, const float *g, int np, int nm, int pi,
+                      double x, double yadjust, int logi, const double *expo_mean);
+
 /* L-mode peak search: modelloop (jointfind.cpp:746-812) with startpop
  * (:658-702), nextgen (:594-656), difeloop (:705-720) and copybest
  * (:723-738), for one model type, or a nested model given by xmap (nested > 0

@@ -68,6 +68,8 @@ def _declare(L):
     for f in ("ora_jointp_exact", "ora_jointp_compat"):
         getattr(L, f).argtypes = [I, I, P, I, I, I, I, P, P, P]
         getattr(L, f).restype = D
+    L.ora_margincalc.argtypes = [I, I, P, I, I, I, D, D, I, P]
+    L.ora_margincalc.restype = D
     L.ora_mt_seed.argtypes = [P, C.c_uint32]
     L.ora_mt_seed.restype = None
     L.ora_mt_uniform.argtypes = [P]
@@ -332,3 +334,25 @@ def ref_de(rows, np_, nm, npops, upper, modeltype=0, multiplier=100, seed=1234, 
         elif ln.startswith("ESS"):
             ess = float(ln.split()[1])
     return best, ess
+
+
+# ------------------------------------------------------------ 1-D marginals
+def margincalc(rows, np_, nm, pi, x, yadjust=0.0, logi=0, expo_mean=None):
+    G, rl = rows.shape
+    rows = np.ascontiguousarray(rows, np.float32)
+    return lib().ora_margincalc(G, rl, _p(rows), np_, nm, int(pi), float(x), float(yadjust), int(logi),
+                                _p(_f64(expo_mean)) if expo_mean is not None else None)
+
+
+def ref_margincalc(rows, np_, nm, points, expo_mean=None):
+    """The reference's margincalc through oracle/_ref/imaref (this container
+    only); points: (pi, x, logi, yadjust) tuples."""
+    G, rl = rows.shape
+    lines = ["%d %d %d %d %d" % (G, rl, np_, nm, 1 if expo_mean is not None else 0),
+             " ".join("%.9g" % v for v in np.asarray(rows, np.float32).ravel())]
+    if expo_mean is not None:
+        lines.append(" ".join("%.17g" % v for v in expo_mean))
+    lines.append(str(len(points)))
+    lines += ["%d %.17g %d %.17g" % (int(p), x, int(lg), ya) for p, x, lg, ya in points]
+    out = run_ref("margin", "\n".join(lines) + "\n")
+    return np.array([float(v) for v in out.split()])

@@ -12,7 +12,7 @@
  * ref_access_cpd.cpp and ref_access_jf.cpp include those two reference
  * sources to reach them.  The other reference objects are linked unchanged.
  *
- * Usage:  imaref is|hky|sw|swap|jointp|de <input.txt>   (results on stdout)
+ * Usage:  imaref is|hky|sw|swap|jointp|de|margin <input.txt>   (results on stdout)
  */
 #undef GLOBVARS
 #include "imamp.hpp"
@@ -262,9 +262,39 @@ static void run_de()
   printf("\nESS %.17g\n", ess);
 }
 
+/* MARGIN: G rowlen np nm expo rows[G*rowlen] [mean[nm] when expo] npts
+ *         then per point: pi x logi yadjust   -> margincalc value per point */
+static void run_margin()
+{
+  int G = rd_i(), rowlen = rd_i(), np = rd_i(), nm = rd_i(), expo = rd_i();
+  load_gsampinf(G, rowlen, np, nm, 2);
+  gsamp_ccp = 0;  // as setup_iparams (initialize.cpp:709-718) sets them
+  gsamp_fcp = gsamp_ccp + np;
+  gsamp_hccp = gsamp_fcp + np;
+  gsamp_mcp = gsamp_hccp + np;
+  gsamp_fmp = gsamp_mcp + nm;
+  gsamp_qip = gsamp_fmp + nm;
+  gsamp_mip = gsamp_qip + np;
+  gsamp_pdgp = gsamp_mip + nm;
+  gsamp_probgp = gsamp_pdgp + 1;
+  gsamp_tp = gsamp_probgp + 1;
+  modeloptions[EXPOMIGRATIONPRIOR] = expo;
+  imig = static_cast<struct i_param *>(calloc(nm > 0 ? nm : 1, sizeof(struct i_param)));
+  if (expo)
+    for (int i = 0; i < nm; i++) imig[i].pr.mean = rd_d();
+  int npts = rd_i();
+  for (int k = 0; k < npts; k++) {
+    int pi = rd_i();
+    double x = rd_d();
+    int logi = rd_i();
+    double ya = rd_d();
+    printf("%.17g\n", margincalc(x, ya, pi, logi));
+  }
+}
+
 int main(int argc, char **argv)
 {
-  if (argc != 3) { fprintf(stderr, "usage: imaref is|hky|sw|swap|jointp|de <input>\n"); return 2; }
+  if (argc != 3) { fprintf(stderr, "usage: imaref is|hky|sw|swap|jointp|de|margin <input>\n"); return 2; }
   g_in = fopen(argv[2], "r");
   if (!g_in) { perror(argv[2]); return 2; }
   std::string mode = argv[1];
@@ -274,6 +304,7 @@ int main(int argc, char **argv)
   else if (mode == "swap") run_swap();
   else if (mode == "jointp") run_jointp();
   else if (mode == "de") run_de();
+  else if (mode == "margin") run_margin();
   else { fprintf(stderr, "unknown mode\n"); return 2; }
   fclose(g_in);
   return 0;

@@ -17,8 +17,11 @@ Fixtures:
   golden_de.npz     modelloop (the L-mode differential-evolution peak search,
                     MT19937 seeded) for the full model, theta-only and
                     migration-only model types and a nested model
+  golden_margin.npz margincalc (1-D marginal densities) on fillvec's grids,
+                    plain and log'd with yadjust, uniform and exponential
+                    migration priors
 
-Run with fixture names (is hky sw swap jointp de) to regenerate only those.
+Run with fixture names (is hky sw swap jointp de margin) to regenerate only those.
 """
 from __future__ import annotations
 
@@ -339,11 +342,30 @@ def golden_de():
     np.savez_compressed(os.path.join(OUT, "golden_de.npz"), **out)
 
 
+def golden_margin():
+    rng = np.random.default_rng(1007)
+    rows, _, off = synth.surface_stats(rng, 300, 3, 2, 1)
+    pmax = np.array([20.0, 15.0, 25.0, 2.0, 5.0])
+    grid = 40  # points per parameter on fillvec's grid (GRIDSIZE is 1000 in the reference)
+    pts = []
+    for p in range(5):
+        for j in range(grid):
+            pts.append((p, ((j + 0.5) * pmax[p]) / grid, 0, 0.0))
+    for p in range(5):  # log'd with a y adjustment, as margin95's root search calls it
+        for x in (0.05, 1.0, 4.0):
+            pts.append((p, x, 1, 1.92))
+    out = {"rows": rows, "pmax": pmax, "grid": np.array(grid), "points": np.array(pts)}
+    out["ref"] = O.ref_margincalc(rows, 3, 2, pts)
+    out["expo_mean"] = np.array([0.8, 1.7])
+    out["ref_expo"] = O.ref_margincalc(rows, 3, 2, pts, expo_mean=out["expo_mean"])
+    np.savez_compressed(os.path.join(OUT, "golden_margin.npz"), **out)
+
+
 if __name__ == "__main__":
     if not O.ref_available():
         sys.exit("build the reference harness first: make -C oracle ref")
     gens = {"is": golden_is, "hky": golden_hky, "sw": golden_sw, "swap": golden_swap,
-            "jointp": golden_jointp, "de": golden_de}
+            "jointp": golden_jointp, "de": golden_de, "margin": golden_margin}
     for name in (sys.argv[1:] or list(gens)):
         gens[name]()
     for f in sorted(os.listdir(OUT)):

@@ -127,3 +127,16 @@ def test_de_rejects_nested_migration_model():
     best, ess, gens, runs, _ = O.modelloop(d["rows"], 3, 2, 3, d["upper"], 2, 30, 1, xmap=np.array([0.0, 0, 0, 0, 1]),
                                            nested=2)
     assert gens == -1
+
+
+@pytest.mark.parametrize("expo", [False, True])
+def test_margincalc_matches_reference_bit_exact(expo):
+    """margincalc (surface_call_functions.cpp:119-175): plain sums on
+    fillvec's grid and log'd values less yadjust, uniform and exponential
+    migration priors."""
+    d = load("golden_margin.npz")
+    em = d["expo_mean"] if expo else None
+    want = d["ref_expo"] if expo else d["ref"]
+    got = np.array([O.margincalc(d["rows"], 3, 2, int(p), x, ya, int(lg), expo_mean=em)
+                    for p, x, lg, ya in d["points"]])
+    assert np.array_equal(got, want)
