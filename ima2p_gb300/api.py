@@ -44,10 +44,46 @@ EXPORTS = [
     "ima_gpu_surface_eval", "ima_gpu_jointp", "ima_gpu_surface_fp64_noalloc", "ima_gpu_tc_selftest",
     "ima_gpu_surface_info", "ima_mt19937_seed", "ima_mt19937_uniform", "ima_gpu_modelloop",
     "ima_gpu_batch_autotune", "ima_gpu_batch_set_variants", "ima_gpu_margincalc", "ima_gpu_fillvec",
+    "ima_ti_read", "ima_ti_write_binary", "ima_ti_read_binary",
     "ima_gpu_timer_begin", "ima_gpu_timer_end",
     "ima_gpu_set_profiling", "ima_gpu_kernel_stats", "ima_gpu_launch_count", "ima_gpu_flush_l2",
     "ima_gpu_memory",
 ]
+
+
+def _ck_free(code, what):
+    if code != IMA_OK:
+        raise ImaError(code, what)
+
+
+def ti_read(paths, rowlen, maxload=0):
+    """Rows of the reference's .ti files (ima_ti_read): (rows [G][rowlen]
+    float32, total genealogies in the files)."""
+    lib = load_library()
+    arr = (C.c_char_p * len(paths))(*[os.fsencode(p) for p in paths])
+    loaded, total = I(), I()
+    _ck_free(lib.ima_ti_read(len(paths), C.cast(arr, P), int(rowlen), int(maxload), None, 0,
+                             C.byref(loaded), C.byref(total)), "ti_read (count)")
+    rows = np.zeros((loaded.value, rowlen), np.float32)
+    _ck_free(lib.ima_ti_read(len(paths), C.cast(arr, P), int(rowlen), int(maxload), _ptr(rows), loaded.value,
+                             C.byref(loaded), C.byref(total)), "ti_read")
+    return rows, total.value
+
+
+def ti_write_binary(path, rows):
+    rows = np.ascontiguousarray(rows, np.float32)
+    _ck_free(load_library().ima_ti_write_binary(os.fsencode(path), rows.shape[0], rows.shape[1], _ptr(rows)),
+             "ti_write_binary")
+
+
+def ti_read_binary(path):
+    lib = load_library()
+    G, rl = I(), I()
+    _ck_free(lib.ima_ti_read_binary(os.fsencode(path), C.byref(G), C.byref(rl), None, 0), "ti_read_binary")
+    rows = np.zeros((G.value, rl.value), np.float32)
+    _ck_free(lib.ima_ti_read_binary(os.fsencode(path), C.byref(G), C.byref(rl), _ptr(rows), G.value),
+             "ti_read_binary")
+    return rows
 
 
 class MT19937(C.Structure):
@@ -131,6 +167,9 @@ def _declare(L):
         "ima_gpu_surface_eval": (I, [P, I, P, I, I, P, P]),
         "ima_gpu_jointp": (I, [P, P, I, P, P]),
         "ima_gpu_batch_autotune": (I, [P, I, I, C.POINTER(I), C.POINTER(I)]),
+        "ima_ti_read": (I, [I, P, I, I, P, I, C.POINTER(I), C.POINTER(I)]),
+        "ima_ti_write_binary": (I, [C.c_char_p, I, I, P]),
+        "ima_ti_read_binary": (I, [C.c_char_p, C.POINTER(I), C.POINTER(I), P, I]),
         "ima_gpu_margincalc": (I, [P, I, P, P, D, I, P, P]),
         "ima_gpu_fillvec": (I, [P, I, P, P, P, P, P]),
         "ima_gpu_batch_set_variants": (I, [P, I, I, I]),

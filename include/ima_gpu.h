@@ -245,6 +245,24 @@ int ima_gpu_fillvec(ima_ctx *ctx, int gridsize, const double *pmin, const double
 /* The loaded surface's shape (any pointer may be NULL). */
 int ima_gpu_surface_info(ima_ctx *ctx, int *G, int *numpopsizeparams, int *nummigrateparams, int *npops);
 
+/* ------------------------------------------ saved genealogies (.ti files)
+ * Host functions, no context.  ima_ti_read parses the reference's text
+ * format (loadgenealogyvalues, ima_main_mpi.cpp:3216-3440): header lines up
+ * to one containing VALUESSTART, then one line of `rowlen` (gsampinflength)
+ * values per genealogy.  Files are taken in the order given (the reference
+ * takes them in directory order).  When more genealogies are present than
+ * min(maxload (0 = no limit), MAXGENEALOGIESTOSAVE = 300000), lines are kept
+ * by the reference's running-fraction rule.  rows == NULL: counts only (*loaded
+ * and *total).  Otherwise rows [rows_cap][rowlen] receives the kept rows, to
+ * be passed to ima_gpu_surface_load.  IMA_ERR_DATA: no VALUESSTART line, or a
+ * line with too few or too many values. */
+int ima_ti_read(int nfiles, const char *const *paths, int rowlen, int maxload, float *rows, int rows_cap,
+                int *loaded, int *total);
+/* Binary side-car of loaded rows, reloaded without parsing. */
+int ima_ti_write_binary(const char *path, int G, int rowlen, const float *rows);
+/* rows == NULL: header only (*G, *rowlen). */
+int ima_ti_read_binary(const char *path, int *G, int *rowlen, float *rows, int rows_cap);
+
 /* ---------------------------------------------------- L-mode peak search
  * MT19937 generator state (utilities.cpp:323-427, Matsumoto & Nishimura):
  * the reference's global generator, carried by the caller so that a peak

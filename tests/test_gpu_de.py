@@ -92,3 +92,25 @@ def test_bad_arguments():
         ctx.modelloop(d["upper"], 2, xmap=np.array([0.0, 0, 0, 0, 1]), nested=2)
     with pytest.raises(api.ImaError):  # a nested index beyond the nested model
         ctx.modelloop(d["upper"], 0, xmap=np.array([0.0, 1, 2, 3, 4]), nested=3)
+
+
+def test_lmode_pipeline_from_ti_file(tmp_path):
+    """.ti file -> resident surface -> peak search -> marginal densities, the
+    whole L-mode path, against the oracle on the rows the reference's reader
+    would load."""
+    from tests.test_ti_io import parsed, write_ti
+    d = load("golden_de.npz")
+    path = str(tmp_path / "run.ti")
+    write_ti(path, d["rows"])
+    rows, total = api.ti_read([path], d["rows"].shape[1])
+    assert total == len(d["rows"]) and np.array_equal(rows, parsed(d["rows"]))
+    ctx = ctx_with([("sw", 2, 1)])
+    ctx.surface_load(rows, 3, 2, 2)
+    best, ess, gens, runs, _ = ctx.modelloop(d["upper"], 0, seed=77, multiplier=30, method=api.SURF_COMPAT)
+    ob, oe, og, orr, _ = O.modelloop(rows, 3, 2, 2, d["upper"], 0, 30, 77, compat=True)
+    np.testing.assert_allclose(best, ob, rtol=1e-9)
+    xs, ys = ctx.fillvec(np.zeros(5), d["upper"], 200)
+    for p in range(5):
+        for j in (0, 77, 199):
+            want = O.margincalc(rows, 3, 2, p, xs[p, j])
+            assert abs(ys[p, j] - want) <= 1e-12 * abs(want)
