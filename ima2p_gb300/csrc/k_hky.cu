@@ -65,30 +65,53 @@ __device__ __forceinline__ void hky_p(const T *pi, T kpa, T b, T *P)
   }
 }
 
-// The same matrix for FP32, rewritten with E1 = 1 - exp(-b), E2 = 1 - exp(-bA)
-// taken from expm1 so that short branches do not cancel:
+// The same matrix for FP32 as five coefficients per branch.  With
+// E1 = 1 - exp(-b) and E2_c = 1 - exp(-b A_c), A_c = 1 + Pi_c (kappa - 1),
+// both taken from expm1 so that short branches do not cancel, the entries are
 //   transversion  pi_k E1
-//   transition    (pi_k / Pi_k) (E2 - E1 (1 - Pi_k))
-//   identity      1 - E1 pi_k (1 - Pi_k) / Pi_k - E2 (Pi_k - pi_k) / Pi_k
-__device__ __forceinline__ void hky_p_fast(const float *pi, float kpa, float b, float *P)
+//   transition    (pi_k / Pi_c) (E2_c - E1 (1 - Pi_c))
+//   identity      the transition value plus 1 - E2_c
+// and with the states ordered A, C, G, T (purines R = {A, G}, pyrimidines
+// Y = {C, T}) the product of P(b) with a partial L is, for j in class c and
+// the other class o,
+//   v_j = E1 S_o + b_c S_c + d_c L_j,   S_c = sum_{k in c} pi_k L_k,
+//   b_c = (E2_c - E1 (1 - Pi_c)) / Pi_c,   d_c = 1 - E2_c.
+// K = {E1, b_R, b_Y, d_R, d_Y}.
+__device__ __forceinline__ void hky_coef_fast(const float *pi, float kpa, float b, float *K)
 {
-  float E1 = -expm1f(-b);
-  float PR = pi[0] + pi[2], PY = pi[1] + pi[3];
-  float ER = -expm1f(-b * (1.0f + PR * kpa)), EY = -expm1f(-b * (1.0f + PY * kpa));
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    float Pk = (k == 0 || k == 2) ? PR : PY;
-    float E2 = (k == 0 || k == 2) ? ER : EY;
-    float r = pi[k] / Pk;
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      float v;
-      if (j == k) v = 1.0f - E1 * r * (1.0f - Pk) - E2 * (1.0f - r);
-      else if (j + k == 2 || j + k == 4) v = r * (E2 - E1 * (1.0f - Pk));
-      else v = pi[k] * E1;
-      P[j * 4 + k] = v;
-    }
-  }
+  const float E1 = -expm1f(-b);
+  const float PR = pi[0] + pi[2], PY = pi[1] + pi[3];
+  const float ER = -expm1f(-b * (1.0f + PR * kpa)), EY = -expm1f(-b * (1.0f + PY * kpa));
+  K[0] = E1;
+  K[1] = (ER - E1 * (1.0f - PR)) / PR;
+  K[2] = (EY - E1 * (1.0f - PY)) / PY;
+  K[3] = 1.0f - ER;
+  K[4] = 1.0f - EY;
+}
+
+// P(b) L for one child at one pattern: a tip observed in state st, or an
+// internal node's partial Lc
+struct HkyCoef {
+  float a, bR, bY, dR, dY;
+};
+__device__ __forceinline__ void hky_apply_tip(const HkyCoef &K, const float *pi, int st, float *v)
+{
+  const float p = pi[st];
+  const bool isR = (st & 1) == 0;
+  const float tR = (isR ? K.bR : K.a) * p, tY = (isR ? K.a : K.bY) * p;
+  v[0] = tR + (st == 0 ? K.dR : 0.0f);
+  v[2] = tR + (st == 2 ? K.dR : 0.0f);
+  v[1] = tY + (st == 1 ? K.dY : 0.0f);
+  v[3] = tY + (st == 3 ? K.dY : 0.0f);
+}
+__device__ __forceinline__ void hky_apply(const HkyCoef &K, const float *pi, float4 L, float *v)
+{
+  const float SR = fmaf(pi[2], L.z, pi[0] * L.x), SY = fmaf(pi[3], L.w, pi[1] * L.y);
+  const float tR = fmaf(K.bR, SR, K.a * SY), tY = fmaf(K.bY, SY, K.a * SR);
+  v[0] = fmaf(K.dR, L.x, tR);
+  v[2] = fmaf(K.dR, L.z, tR);
+  v[1] = fmaf(K.dY, L.y, tY);
+  v[3] = fmaf(K.dY, L.w, tY);
 }
 
 // Shared-memory carve-up, identical on host (sizing) and device.
@@ -166,12 +189,14 @@ __device__ __forceinline__ int expo_of(float m)  // floor(log2(m)) for normal m 
 }
 
 // ------------------------------------------------------------------ FP32
-// Thread mapping: with S <= BS patterns, BS / S nodes of a level are
-// processed at once (pattern = tid % S), so no division runs per work item;
-// wider loci loop over pattern blocks.  With CACHE, the partials this launch
-// computes are also kept in shared memory ([internal node][pattern]) and
-// daughters are read from there instead of making an L2 round trip per level.
-// BS threads per CTA, registers for MINB resident CTAs per SM
+// One CTA per chain-locus, internal nodes level by level.  Each branch gets
+// the five coefficients of hky_coef_fast (in place of a 4 x 4 matrix), and a
+// warp works on one node and 32 of its patterns at a time, so the children's
+// coefficients are warp-uniform and no warp mixes tip and internal children.
+// With CACHE, the partials this launch computes are also kept in shared
+// memory ([internal node][pattern]) and daughters are read from there instead
+// of making an L2 round trip per level.  BS threads per CTA, registers for
+// MINB resident CTAs per SM.
 template <bool CACHE, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *reqs,
                                                      double *result, int32_t *status, int maxnl,
@@ -184,7 +209,7 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
   const int n = it.n, nl = 2 * n - 1, S = L.nsites, nint = n - 1;
   const int nlev = P.nlev[R.item];
   const HkyLayout lay = hky_layout(maxnl, sizeof(float));
-  float *Pm = reinterpret_cast<float *>(smem);               // [maxnl][16]
+  float *Pm = reinterpret_cast<float *>(smem);               // [maxnl][16]: 5 coefficients per branch
   Tree T;
   T.nd = reinterpret_cast<NodeRec *>(smem + lay.nd);
   T.fresh = reinterpret_cast<uint8_t *>(smem + lay.fresh);
@@ -231,7 +256,7 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
     int d = T.nd[c].down;
     if (d < 0 || !T.fresh[d]) continue;
     float pil[4] = {spi[0], spi[1], spi[2], spi[3]};
-    hky_p_fast(pil, kpa, smu * branch_ff(T.nd, tff, c), Pm + 16 * c);
+    hky_coef_fast(pil, kpa, smu * branch_ff(T.nd, tff, c), Pm + 16 * c);
   }
   __syncthreads();
 
@@ -239,79 +264,67 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
   float4 *part = P.part + it.part_off;
   int32_t *pexp = P.pexp + it.part_off;
   const int8_t *seq = P.seq + L.seq_off;
-  // (node slot, pattern) of this thread
-  const bool narrow = S <= BS;
-  const int jstep = narrow ? BS / S : 1;
-  const int js = narrow ? tid / S : 0;
-  const int is = narrow ? tid - js * S : tid;
-  const int istep = narrow ? S : BS;  // narrow: one pattern per thread
-  const bool active = !narrow || js < jstep;
+  const float pi4[4] = {spi[0], spi[1], spi[2], spi[3]};
+  // warps take (node, 32-pattern chunk) pairs of a level in turn, so a warp
+  // works on one node at a time and its children's coefficients stay in
+  // registers; lanes are patterns
+  constexpr int NW = BS / 32;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int nch = (S + 31) >> 5;
   for (int lv = 0; lv < nlev; lv++) {
-    const int beg = T.lstart[lv], cnt = T.lstart[lv + 1] - beg;
-    if (active) {
-      for (int jj = js; jj < cnt; jj += jstep) {
-        const int node = T.order[beg + jj];
-        if (!T.fresh[node]) continue;
-        const int c0 = T.nd[node].up0, c1 = T.nd[node].up1;
-        const float4 *P0 = reinterpret_cast<const float4 *>(Pm + 16 * c0);
-        const float4 *P1 = reinterpret_cast<const float4 *>(Pm + 16 * c1);
-        for (int i = is; i < S; i += istep) {
-          float v[2][4];
-          int e = 0;
+    const int beg = T.lstart[lv], total = (T.lstart[lv + 1] - beg) * nch;
+    for (int q = warp; q < total; q += NW) {
+      const int jj = q / nch, i = (q - jj * nch) * 32 + lane;
+      const int node = T.order[beg + jj];
+      if (!T.fresh[node] || i >= S) continue;
+      const int cc[2] = {T.nd[node].up0, T.nd[node].up1};
+      float v[2][4];
+      int e = 0;
 #pragma unroll
-          for (int h = 0; h < 2; h++) {
-            const int c = h ? c1 : c0;
-            const float4 *Pc = h ? P1 : P0;
-            if (c < n) {
-              int st = seq[(size_t)c * S + i];
-              const float *Pf = reinterpret_cast<const float *>(Pc);
-#pragma unroll
-              for (int j = 0; j < 4; j++) v[h][j] = Pf[j * 4 + st];
-            } else {
-              float4 Lc;
-              if (CACHE && T.fresh[c]) {
-                size_t ci = (size_t)(c - n) * cache_S + i;
-                Lc = cpart[ci];
-                e += cexp[ci];
-              } else {
-                int rs = T.fresh[c] ? 1 - T.slot[c] : T.slot[c];
-                size_t idx = rs * slot_stride + (size_t)(c - n) * S + i;
-                Lc = part[idx];
-                e += pexp[idx];
-              }
-#pragma unroll
-              for (int j = 0; j < 4; j++) {
-                float4 pr = Pc[j];
-                v[h][j] = pr.x * Lc.x + pr.y * Lc.y + pr.z * Lc.z + pr.w * Lc.w;
-              }
-            }
+      for (int h = 0; h < 2; h++) {
+        const int c = cc[h];
+        const float *Kp = Pm + 16 * c;
+        const HkyCoef K = {Kp[0], Kp[1], Kp[2], Kp[3], Kp[4]};
+        if (c < n) {
+          hky_apply_tip(K, pi4, seq[(size_t)c * S + i], v[h]);
+        } else {
+          float4 Lc;
+          if (CACHE && T.fresh[c]) {
+            const size_t ci = (size_t)(c - n) * cache_S + i;
+            Lc = cpart[ci];
+            e += cexp[ci];
+          } else {
+            const int rs = T.fresh[c] ? 1 - T.slot[c] : T.slot[c];
+            const size_t idx = rs * slot_stride + (size_t)(c - n) * S + i;
+            Lc = part[idx];
+            e += pexp[idx];
           }
-          float4 ov = make_float4(v[0][0] * v[1][0], v[0][1] * v[1][1], v[0][2] * v[1][2],
-                                  v[0][3] * v[1][3]);
-          // rescale by an exact 2^40 only when the largest entry drops below
-          // 2^-40: products of two daughters then stay above 2^-80 (normal)
-          const float m = fmaxf(fmaxf(ov.x, ov.y), fmaxf(ov.z, ov.w));
-          if (m < 9.094947e-13f) {
-            const float up = 1.0995116e12f;  // 2^40
-            ov.x *= up; ov.y *= up; ov.z *= up; ov.w *= up;
-            e -= 40;
-            if (m * up < 9.094947e-13f) {  // very small value: normalise exactly
-              const float mm = m * up;
-              const int k = (mm > 0.f) ? expo_of(mm) : 0;
-              const float sc = pow2f(-k);
-              ov.x *= sc; ov.y *= sc; ov.z *= sc; ov.w *= sc;
-              e += k;
-            }
-          }
-          const size_t widx = (1 - T.slot[node]) * slot_stride + (size_t)(node - n) * S + i;
-          part[widx] = ov;
-          pexp[widx] = e;
-          if (CACHE) {
-            size_t ci = (size_t)(node - n) * cache_S + i;
-            cpart[ci] = ov;
-            cexp[ci] = e;
-          }
+          hky_apply(K, pi4, Lc, v[h]);
         }
+      }
+      float4 ov = make_float4(v[0][0] * v[1][0], v[0][1] * v[1][1], v[0][2] * v[1][2], v[0][3] * v[1][3]);
+      // rescale by an exact 2^40 only when the largest entry drops below
+      // 2^-40: products of two daughters then stay above 2^-80 (normal)
+      const float m = fmaxf(fmaxf(ov.x, ov.y), fmaxf(ov.z, ov.w));
+      if (m < 9.094947e-13f) {
+        const float up = 1.0995116e12f;  // 2^40
+        ov.x *= up; ov.y *= up; ov.z *= up; ov.w *= up;
+        e -= 40;
+        if (m * up < 9.094947e-13f) {  // very small value: normalise exactly
+          const float mm = m * up;
+          const int k = (mm > 0.f) ? expo_of(mm) : 0;
+          const float sc = pow2f(-k);
+          ov.x *= sc; ov.y *= sc; ov.z *= sc; ov.w *= sc;
+          e += k;
+        }
+      }
+      const size_t widx = (1 - T.slot[node]) * slot_stride + (size_t)(node - n) * S + i;
+      part[widx] = ov;
+      pexp[widx] = e;
+      if (CACHE) {
+        const size_t ci = (size_t)(node - n) * cache_S + i;
+        cpart[ci] = ov;
+        cexp[ci] = e;
       }
     }
     __syncthreads();
