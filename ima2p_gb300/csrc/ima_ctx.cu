@@ -15,6 +15,11 @@
 #include <new>
 #include <string>
 #include <vector>
+#include <memory>
+#include <functional>
+#include <condition_variable>
+#include <mutex>
+#include <thread>
 
 #include "internal.h"
 
@@ -41,6 +46,71 @@ struct Batch {
   int maxn_is = 0, maxs_is = 0, maxn_hky = 0, maxs_hky = 0, maxn_sw = 0;
   int cap = 0;  // capacity of the device buffers
   int hky_variant = 0, sw_variant = 0;  // launch shapes (ima_gpu_batch_autotune)
+};
+
+// A small persistent pool of host threads for per-genealogy packing: run(n,
+// f) calls f(0) .. f(n-1) on the pool and the calling thread and returns
+// when every call has finished.
+class HostPool {
+ public:
+  explicit HostPool(int nthreads)
+  {
+    for (int i = 0; i < nthreads; i++) th_.emplace_back([this] { loop(); });
+  }
+  ~HostPool()
+  {
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (auto &t : th_) t.join();
+  }
+  int size() const { return (int)th_.size() + 1; }
+  void run(int n, const std::function<void(int)> &f)
+  {
+    std::unique_lock<std::mutex> lk(m_);
+    job_ = &f;
+    njobs_ = n;
+    next_ = 0;
+    finished_ = 0;
+    gen_++;
+    cv_.notify_all();
+    work(lk);
+    done_.wait(lk, [&] { return finished_ == njobs_; });
+    job_ = nullptr;
+  }
+
+ private:
+  void work(std::unique_lock<std::mutex> &lk)
+  {
+    while (job_ && next_ < njobs_) {
+      const int j = next_++;
+      const std::function<void(int)> *f = job_;
+      lk.unlock();
+      (*f)(j);
+      lk.lock();
+      if (++finished_ == njobs_) done_.notify_all();
+    }
+  }
+  void loop()
+  {
+    uint64_t seen = 0;
+    std::unique_lock<std::mutex> lk(m_);
+    for (;;) {
+      cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+      if (stop_) return;
+      seen = gen_;
+      work(lk);
+    }
+  }
+  std::vector<std::thread> th_;
+  std::mutex m_;
+  std::condition_variable cv_, done_;
+  const std::function<void(int)> *job_ = nullptr;
+  int njobs_ = 0, next_ = 0, finished_ = 0;
+  uint64_t gen_ = 0;
+  bool stop_ = false;
 };
 
 struct PendingTiming {
@@ -122,6 +192,10 @@ struct ima_ctx {
   double *d_dlike = nullptr;
   std::vector<uint8_t> dl_fast;  // per item x marker: last SW evaluation was float-float
   std::vector<uint8_t> has_tree; // per item: a genealogy was uploaded
+  std::unique_ptr<HostPool> pool;  // host threads for set_genealogies (made on first use)
+  std::vector<int> pair_stamp;     // set_genealogies: repeated-pair check
+  std::vector<size_t> pair_off;    // set_genealogies: node offset of each pair
+  int stamp_gen = 0;
   float4 *d_part = nullptr;
   int32_t *d_pexp = nullptr;
   double *d_part64 = nullptr, *d_psf64 = nullptr;
@@ -153,6 +227,13 @@ struct ima_ctx {
   // batches
   std::vector<Batch> batches;
   Batch evb;  // buffers of ima_gpu_eval
+  // the request list evb holds: a call with byte-identical arrays reuses it
+  struct EvalKey {
+    bool valid = false;
+    int n = 0, prec = 0;
+    std::vector<int32_t> ci, li, edits, ai;
+    std::vector<double> u, kappa;
+  } evkey;
   int32_t *d_citems = nullptr;
   uint8_t *d_cacc = nullptr;
   size_t ccap = 0;
@@ -329,6 +410,7 @@ extern "C" int ima_gpu_synchronize(ima_ctx *c)
 static int add_locus(ima_ctx *c, int model, int n, int S, int tots, const int8_t *seq,
                      const int32_t *mult, int nlinked, int *li)
 {
+  c->evkey.valid = false;
   if (!c || !li) return IMA_ERR_ARG;
   if (c->nchains) return c->fail(IMA_ERR_STATE, "loci must be added before ima_gpu_set_chains");
   if (n < 2 || n > 16000) return c->fail(IMA_ERR_ARG, "numgenes %d out of range", n);
@@ -373,6 +455,7 @@ extern "C" int ima_gpu_add_locus_sw(ima_ctx *c, int numgenes, int nlinked, int *
 
 extern "C" int ima_gpu_set_chains(ima_ctx *c, int nruns, int chains_per_run)
 {
+  if (c) c->evkey.valid = false;
   if (!c) return IMA_ERR_ARG;
   if (c->nchains) return c->fail(IMA_ERR_STATE, "chains already set");
   if (nruns < 1 || chains_per_run < 1 || c->loci.empty())
@@ -494,13 +577,29 @@ static void mark(ima_ctx *c, int item)
   c->dirty_hi = std::max(c->dirty_hi, item);
 }
 
-extern "C" int ima_gpu_set_genealogy(ima_ctx *c, int ci, int li, const int32_t *up0, const int32_t *up1,
-                                     const int32_t *down, const double *time, double length)
+// What one genealogy upload changed: dirty item ranges (topology and times
+// only) and the error, kept per worker so that uploads can run in parallel.
+struct SetOut {
+  int lo = INT32_MAX, hi = -1, tlo = INT32_MAX, thi = -1;
+  int code = IMA_OK;
+  char msg[256] = {0};
+  int fail(int c, const char *fmt, ...)
+  {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(msg, sizeof(msg), fmt, ap);
+    va_end(ap);
+    code = c;
+    return c;
+  }
+  void merge_into(ima_ctx *c) const;  // the dirty ranges (the caller reports the error)
+};
+
+// writes genealogy data of one item into the pinned mirrors; touches only
+// that item's entries (and thread_local scratch)
+static int set_one(ima_ctx *c, int item, const int32_t *up0, const int32_t *up1, const int32_t *down,
+                   const double *time, double length, SetOut &o)
 {
-  if (!c || !up0 || !up1 || !down || !time) return IMA_ERR_ARG;
-  if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
-  if (!c->valid(ci, li)) return c->fail(IMA_ERR_ARG, "chain %d locus %d out of range", ci, li);
-  const int item = c->item_of(ci, li);
   const ItemDev &it = c->items[item];
   const int n = it.n, nl = 2 * n - 1;
   NodeRec *rec = c->h_nodes + it.node_off;
@@ -518,27 +617,27 @@ extern "C" int ima_gpu_set_genealogy(ima_ctx *c, int ci, int li, const int32_t *
       if (down[k] >= 0) L += (up0[k] < 0) ? t : t - time[up0[k]];
     }
     c->h_len[item] = (length >= 0.0) ? length : L;
-    c->tdirty_lo = std::min(c->tdirty_lo, item);
-    c->tdirty_hi = std::max(c->tdirty_hi, item);
+    o.tlo = std::min(o.tlo, item);
+    o.thi = std::max(o.thi, item);
     return IMA_OK;
   }
   // validate the topology: tips have no daughters, internal nodes two, one root
   int root = -1;
   for (int k = 0; k < nl; k++) {
     bool tip = k < n;
-    if (tip != (up0[k] < 0) || tip != (up1[k] < 0)) return c->fail(IMA_ERR_ARG, "node %d: daughters do not match tip/internal numbering", k);
+    if (tip != (up0[k] < 0) || tip != (up1[k] < 0)) return o.fail(IMA_ERR_ARG, "node %d: daughters do not match tip/internal numbering", k);
     if (!tip) {
-      if (up0[k] >= nl || up1[k] >= nl || up0[k] == up1[k]) return c->fail(IMA_ERR_ARG, "node %d: bad daughters", k);
-      if (down[up0[k]] != k || down[up1[k]] != k) return c->fail(IMA_ERR_ARG, "node %d: parent links disagree", k);
+      if (up0[k] >= nl || up1[k] >= nl || up0[k] == up1[k]) return o.fail(IMA_ERR_ARG, "node %d: bad daughters", k);
+      if (down[up0[k]] != k || down[up1[k]] != k) return o.fail(IMA_ERR_ARG, "node %d: parent links disagree", k);
     }
     if (down[k] < 0) {
-      if (root >= 0) return c->fail(IMA_ERR_ARG, "two roots (%d, %d)", root, k);
+      if (root >= 0) return o.fail(IMA_ERR_ARG, "two roots (%d, %d)", root, k);
       root = k;
     } else if (down[k] < n || down[k] >= nl) {
-      return c->fail(IMA_ERR_ARG, "node %d: bad parent %d", k, down[k]);
+      return o.fail(IMA_ERR_ARG, "node %d: bad parent %d", k, down[k]);
     }
   }
-  if (root < n) return c->fail(IMA_ERR_ARG, "no internal root");
+  if (root < n) return o.fail(IMA_ERR_ARG, "no internal root");
   // heights by an explicit post-order from the root; levels = heights 1..H
   thread_local std::vector<int> height, stack, cnt, pos;
   thread_local std::vector<uint8_t> seen;
@@ -558,14 +657,14 @@ extern "C" int ima_gpu_set_genealogy(ima_ctx *c, int ci, int li, const int32_t *
       seen[v] = 1;
       stack.push_back(up0[v]);
       stack.push_back(up1[v]);
-      if (stack.size() > (size_t)4 * nl) return c->fail(IMA_ERR_ARG, "genealogy has a cycle");
+      if (stack.size() > (size_t)4 * nl) return o.fail(IMA_ERR_ARG, "genealogy has a cycle");
       continue;
     }
     stack.pop_back();
     height[v] = 1 + std::max(height[up0[v]], height[up1[v]]);
     visited++;
   }
-  if (visited != nl) return c->fail(IMA_ERR_ARG, "genealogy is not connected");
+  if (visited != nl) return o.fail(IMA_ERR_ARG, "genealogy is not connected");
   int H = height[root];
   cnt.assign(H + 2, 0);
   for (int k = n; k < nl; k++) cnt[height[k]]++;
@@ -591,8 +690,30 @@ extern "C" int ima_gpu_set_genealogy(ima_ctx *c, int ci, int li, const int32_t *
   }
   c->h_len[item] = (length >= 0.0) ? length : L;
   c->has_tree[item] = 1;
-  mark(c, item);
+  o.lo = std::min(o.lo, item);
+  o.hi = std::max(o.hi, item);
   return IMA_OK;
+}
+
+void SetOut::merge_into(ima_ctx *c) const
+{
+  c->dirty_lo = std::min(c->dirty_lo, lo);
+  c->dirty_hi = std::max(c->dirty_hi, hi);
+  c->tdirty_lo = std::min(c->tdirty_lo, tlo);
+  c->tdirty_hi = std::max(c->tdirty_hi, thi);
+}
+
+extern "C" int ima_gpu_set_genealogy(ima_ctx *c, int ci, int li, const int32_t *up0, const int32_t *up1,
+                                     const int32_t *down, const double *time, double length)
+{
+  if (!c || !up0 || !up1 || !down || !time) return IMA_ERR_ARG;
+  if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
+  if (!c->valid(ci, li)) return c->fail(IMA_ERR_ARG, "chain %d locus %d out of range", ci, li);
+  SetOut o;
+  int r = set_one(c, c->item_of(ci, li), up0, up1, down, time, length, o);
+  o.merge_into(c);
+  if (r) c->err = o.msg;
+  return r;
 }
 
 extern "C" int ima_gpu_set_genealogies(ima_ctx *c, int n, const int32_t *ci, const int32_t *li,
@@ -600,16 +721,56 @@ extern "C" int ima_gpu_set_genealogies(ima_ctx *c, int n, const int32_t *ci, con
                                        const double *time, const double *length)
 {
   if (!c || n < 0 || (n > 0 && (!ci || !li || !up0 || !up1 || !down || !time))) return IMA_ERR_ARG;
-  size_t off = 0;
+  if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
+  // offsets of each pair's nodes, and whether a pair repeats (then the list
+  // is applied in order on one thread)
+  // node offset of each pair (a context vector: the pool's threads read it)
+  std::vector<size_t> &off = c->pair_off;
+  off.resize((size_t)n + 1);
+  off[0] = 0;
+  bool repeat = false;
+  if ((int)c->pair_stamp.size() != c->nitems) c->pair_stamp.assign(c->nitems, -1);
+  const int gen = ++c->stamp_gen;
   for (int k = 0; k < n; k++) {
     if (!c->valid(ci[k], li[k])) return c->fail(IMA_ERR_ARG, "pair %d: chain %d locus %d out of range", k, ci[k], li[k]);
-    int nl = 2 * c->loci[li[k]].d.n - 1;
-    int r = ima_gpu_set_genealogy(c, ci[k], li[k], up0 + off, up1 + off, down + off, time + off,
-                                  length ? length[k] : -1.0);
-    if (r) return r;
-    off += nl;
+    const int item = c->item_of(ci[k], li[k]);
+    if (c->pair_stamp[item] == gen) repeat = true;
+    c->pair_stamp[item] = gen;
+    off[k + 1] = off[k] + 2 * c->loci[li[k]].d.n - 1;
   }
-  return IMA_OK;
+  const size_t *offp = off.data();
+  auto apply = [c, ci, li, up0, up1, down, time, length, offp](int k0, int k1, SetOut &o) {
+    for (int k = k0; k < k1; k++) {
+      const size_t f = offp[k];
+      if (set_one(c, c->item_of(ci[k], li[k]), up0 + f, up1 + f, down + f, time + f, length ? length[k] : -1.0, o))
+        return;
+    }
+  };
+  if (repeat || n < 256) {
+    SetOut o;
+    apply(0, n, o);
+    o.merge_into(c);
+    if (o.code) c->err = o.msg;
+    return o.code;
+  }
+  if (!c->pool) {
+    const unsigned hw = std::thread::hardware_concurrency();
+    c->pool.reset(new HostPool((int)std::max(1u, std::min(hw, 16u)) - 1));
+  }
+  const int nchunk = std::min(n / 64, 4 * c->pool->size());
+  std::vector<SetOut> outs(nchunk);
+  c->pool->run(nchunk, [&](int j) {
+    apply((int)((long long)n * j / nchunk), (int)((long long)n * (j + 1) / nchunk), outs[j]);
+  });
+  int r = IMA_OK;
+  for (int j = 0; j < nchunk; j++) {  // the first failing chunk names the error
+    outs[j].merge_into(c);
+    if (!r && outs[j].code) {
+      r = outs[j].code;
+      c->err = outs[j].msg;
+    }
+  }
+  return r;
 }
 
 extern "C" int ima_gpu_set_pi(ima_ctx *c, int ci, int li, const double *pi4)
@@ -917,7 +1078,35 @@ extern "C" int ima_gpu_eval(ima_ctx *c, int n, const int32_t *ci, const int32_t 
 {
   if (!c) return IMA_ERR_ARG;
   Batch &b = c->evb;  // reused request buffers: no allocation per call
-  int r = build_batch(c, b, n, ci, li, u, kappa, edits, ai, precision);
+  // the same request list as the last call (the changet_RY1 pattern: new
+  // genealogies, same chain-loci and rates) reuses the staged requests
+  auto same = [&](const auto &v, const auto *p, size_t cnt) {
+    return p ? (v.size() == cnt && memcmp(v.data(), p, cnt * sizeof(*p)) == 0) : v.empty();
+  };
+  ima_ctx::EvalKey &K = c->evkey;
+  const bool hit = K.valid && K.n == n && K.prec == precision && n > 0 && same(K.ci, ci, n) &&
+                   same(K.li, li, n) && same(K.u, u, n) && same(K.kappa, kappa, n) &&
+                   same(K.edits, edits, 4 * (size_t)n) && same(K.ai, ai, n);
+  int r = IMA_OK;
+  if (!hit) {
+    K.valid = false;
+    r = build_batch(c, b, n, ci, li, u, kappa, edits, ai, precision);
+    if (!r) {
+      auto keep = [&](auto &v, const auto *p, size_t cnt) {
+        if (p) v.assign(p, p + cnt);
+        else v.clear();
+      };
+      keep(K.ci, ci, n);
+      keep(K.li, li, n);
+      keep(K.u, u, n);
+      keep(K.kappa, kappa, n);
+      keep(K.edits, edits, 4 * (size_t)n);
+      keep(K.ai, ai, n);
+      K.n = n;
+      K.prec = precision;
+      K.valid = true;
+    }
+  }
   r = r ? r : flush(c);
   r = r ? r : init_sumlogk(c, b);
   if (!r) enqueue(c, b);

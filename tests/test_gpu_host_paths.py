@@ -1,0 +1,80 @@
+"""Host paths of the boundary on the GPU: set_genealogies splits long lists
+over host threads (results must be those of one-by-one uploads, bitwise), and
+ima_gpu_eval reuses its staged requests when a call repeats the previous
+request arrays (new genealogies must still be seen, changed rates must not be
+missed)."""
+import numpy as np
+import pytest
+
+from ima2p_gb300 import api, workloads
+from tests._gpu import ctx_with
+
+pytestmark = pytest.mark.gpu
+
+
+def _hky_ctx(wl):
+    ctx = ctx_with(wl.loci, wl.nruns, wl.cpr)
+    return ctx
+
+
+def test_parallel_upload_matches_one_by_one():
+    wl = workloads.make_hky(seed=31, nloci=12, nch=32, ncopies=10, nbases=300)   # 384 pairs: parallel path
+    ci, li = wl.pairs()
+    pci, pli, up0, up1, down, tm = wl.packed()
+    u, par = wl.u.ravel(), wl.par.ravel()
+    a = _hky_ctx(wl)
+    wl.upload(a)  # set_genealogies over all 384 pairs at once
+    b = _hky_ctx(wl)
+    for (c, l), p in wl.pi.items():
+        b.set_pi(c, l, p)
+    for c, l in zip(pci, pli):
+        b.set_genealogy(int(c), int(l), wl.tree(int(c), int(l)))
+    ra, _ = a.eval(ci, li, u, par)
+    rb, _ = b.eval(ci, li, u, par)
+    assert np.array_equal(ra, rb)
+    # re-timed (topology kept) and re-shaped lists go through the same path
+    scaled = np.where(tm > 0, tm * 1.01, tm)
+    a.set_genealogies(pci, pli, up0, up1, down, scaled)
+    off = 0
+    for k, (c, l) in enumerate(zip(pci, pli)):
+        g = wl.tree(int(c), int(l)).copy()
+        nl = len(g.up0)
+        g.time = scaled[off:off + nl].copy()
+        off += nl
+        b.set_genealogy(int(c), int(l), g)
+    assert np.array_equal(a.eval(ci, li, u, par)[0], b.eval(ci, li, u, par)[0])
+
+
+def test_parallel_upload_rejects_a_bad_genealogy():
+    wl = workloads.make_hky(seed=32, nloci=10, nch=32, ncopies=10, nbases=200)
+    pci, pli, up0, up1, down, tm = wl.packed()
+    ctx = _hky_ctx(wl)
+    bad_down = down.copy()
+    nl = 2 * 20 - 1
+    k = 150 * nl + nl - 1  # the root of pair 150 gets a parent: two parents link to it
+    bad_down[k] = 21
+    with pytest.raises(api.ImaError):
+        ctx.set_genealogies(pci, pli, up0, up1, bad_down, tm)
+
+
+def test_eval_reuses_requests_but_sees_new_data():
+    wl = workloads.make_hky(seed=33, nloci=8, nch=32, ncopies=10, nbases=300)
+    ci, li = wl.pairs()
+    pci, pli, up0, up1, down, tm = wl.packed()
+    u, par = wl.u.ravel().copy(), wl.par.ravel()
+    ctx = _hky_ctx(wl)
+    wl.upload(ctx)
+    r0 = ctx.eval(ci, li, u, par)[0]
+    # new genealogy times, identical request arrays: the cached requests see them
+    scaled = np.where(tm > 0, tm * 1.2, tm)
+    ctx.set_genealogies(pci, pli, up0, up1, down, scaled)
+    r1 = ctx.eval(ci, li, u, par)[0]
+    fresh = _hky_ctx(wl)
+    wl.upload(fresh)
+    fresh.set_genealogies(pci, pli, up0, up1, down, scaled)
+    assert np.array_equal(r1, fresh.eval(ci, li, u, par)[0])
+    assert not np.array_equal(r0, r1)
+    # one changed rate is a different request list
+    u[7] *= 1.5
+    r2 = ctx.eval(ci, li, u, par)[0]
+    assert r2[7] != r1[7] and np.array_equal(np.delete(r2, 7), np.delete(r1, 7))
