@@ -130,6 +130,147 @@ def sim_im_genealogy(rng, samples, theta, mig, splits, theta_anc=None):
     return Genealogy(up0, up1, down, time, int(root))
 
 
+@dataclasses.dataclass
+class LabelledGenealogy:
+    """A genealogy with the population labels treeweight reads
+    (update_gtree_common.cpp:1680-1937): ``pop[i]`` is the population at the
+    lower end of edge ``i`` (the sampled population at a tip, the population
+    of the coalescence otherwise) and ``mig[i]`` the migration events along
+    the edge, oldest last, as (time, population moved to going back in time)
+    pairs -- the reference's ``gtree[i].mig[]`` list (imamp.hpp:601-605).
+    Population changes at splits are implicit, as in the reference."""
+    g: Genealogy
+    pop: np.ndarray
+    mig: list
+
+    @property
+    def mignum(self) -> int:
+        return sum(len(m) for m in self.mig)
+
+    def packed_mig(self):
+        """CSR form: per-node offsets (len nodes+1), times, destination pops."""
+        off = np.zeros(len(self.mig) + 1, np.int32)
+        off[1:] = np.cumsum([len(m) for m in self.mig])
+        t = np.array([e[0] for m in self.mig for e in m], np.float64)
+        p = np.array([e[1] for m in self.mig for e in m], np.int32)
+        return off, t, p
+
+
+def sim_im_labeled(rng, samples, theta, mig, splits):
+    """The structured coalescent of sim_im_genealogy, recording where each
+    lineage is: the population of every coalescence and every migration event
+    with its time and destination.  ``splits`` as in sim_im_genealogy, with
+    ``new_pop`` the ancestral population id of the reference's tree string
+    (the split forming population npops+k happens at the k-th split time)."""
+    n = int(sum(samples))
+    nl = 2 * n - 1
+    up0 = np.full(nl, -1, np.int32)
+    up1 = np.full(nl, -1, np.int32)
+    down = np.full(nl, -1, np.int32)
+    time = np.zeros(nl, np.float64)
+    pop = np.zeros(nl, np.int32)
+    migs = [[] for _ in range(nl)]
+    lin = []  # [node, current pop, events on the edge so far]
+    k = 0
+    for p, s in enumerate(samples):
+        for _ in range(s):
+            lin.append([k, p, []])
+            pop[k] = p
+            k += 1
+    active = set(range(len(samples)))
+    nxt = n
+    t = 0.0
+    si = 0
+    while len(lin) > 1:
+        counts = {}
+        for _, p, _e in lin:
+            counts[p] = counts.get(p, 0) + 1
+        crate = {p: c * (c - 1) / theta[p] for p, c in counts.items() if c > 1}
+        mrate = mig * len(lin) if len(active) > 1 else 0.0
+        total = sum(crate.values()) + mrate
+        wait = rng.exponential(1.0 / total) if total > 0 else np.inf
+        tsplit = splits[si][0] if si < len(splits) else np.inf
+        if t + wait >= tsplit:
+            t = tsplit
+            _, a, b, new = splits[si]
+            for l in lin:
+                if l[1] in (a, b):
+                    l[1] = new
+            active.discard(a)
+            active.discard(b)
+            active.add(new)
+            si += 1
+            continue
+        t += wait
+        r = rng.uniform(0, total)
+        if r < mrate:
+            li = int(rng.integers(len(lin)))
+            others = sorted(active - {lin[li][1]})
+            dest = int(others[rng.integers(len(others))])
+            lin[li][1] = dest
+            lin[li][2].append((t, dest))
+            continue
+        r -= mrate
+        pops = list(crate)
+        p = pops[-1]
+        for q in pops:
+            if r < crate[q]:
+                p = q
+                break
+            r -= crate[q]
+        idx = [i for i, l in enumerate(lin) if l[1] == p]
+        i, j = rng.choice(idx, 2, replace=False)
+        a, b = lin[i][0], lin[j][0]
+        migs[a], migs[b] = lin[i][2], lin[j][2]
+        node = nxt
+        nxt += 1
+        up0[node], up1[node] = a, b
+        down[a] = down[b] = node
+        time[a] = time[b] = t
+        pop[node] = p
+        for x in sorted((i, j), reverse=True):
+            lin.pop(x)
+        lin.append([node, p, []])
+    root = lin[0][0]
+    time[root] = -1.0
+    return LabelledGenealogy(Genealogy(up0, up1, down, time, int(root)), pop, migs)
+
+
+def splits_from_treestring(s: str, npops: int):
+    """(daughter a, daughter b, ancestor) per split of an IMa2p population
+    tree string such as "((0,1):3,2):4", ordered by ancestor id: the
+    ancestor numbered npops+k forms at the k-th split time
+    (build_poptree.cpp:508-629)."""
+    pos = 0
+
+    def node():
+        nonlocal pos
+        if s[pos] == "(":
+            pos += 1
+            a = node()
+            assert s[pos] == ","
+            pos += 1
+            b = node()
+            assert s[pos] == ")" and s[pos + 1] == ":"
+            pos += 2
+            j = pos
+            while pos < len(s) and s[pos].isdigit():
+                pos += 1
+            anc = int(s[j:pos])
+            out.append((a, b, anc))
+            return anc
+        j = pos
+        while pos < len(s) and s[pos].isdigit():
+            pos += 1
+        return int(s[j:pos])
+
+    out = []
+    node()
+    out.sort(key=lambda x: x[2])
+    assert [x[2] for x in out] == list(range(npops, 2 * npops - 1))
+    return out
+
+
 def two_pop_tree(rng, n1, n2, theta=5.0, mig=0.1, tsplit=1.0):
     return sim_im_genealogy(rng, [n1, n2], [theta, theta, theta], mig,
                             [(tsplit, 0, 1, 2)])

@@ -836,3 +836,484 @@ double ora_margincalc(int G, int rowlen, const float *g, int np, int nm, int pi,
   if (logi) sum = (sum <= 0) ? -1e200 : log(sum);
   return sum - yadjust;
 }
+
+/* ======================================================================
+ * Genealogy weights.  treeweight (update_gtree_common.cpp:1680-1937): every
+ * coalescence (internal node, at the time of its daughters' tops), every
+ * migration (with the population it leaves, found by following the edge's
+ * population through the splits, :1770-1790) and every split younger than
+ * the root becomes an event; the events are visited in time order and, over
+ * each interval, each population of the current period accumulates
+ * n(n-1)*dt/(2h) (fc) and n*dt (fm, the same for every partner); counts
+ * (cc, mc) and the lineage numbers change at each event.
+ * ==================================================================== */
+int ora_tw_sizes(int npops, int *T, int *M)
+{
+  int m = 0;
+  for (int k = 0; k < npops - 1; k++) m += (npops - k) * (npops - k);
+  *T = npops * (npops + 1) / 2;
+  *M = m;
+  return 0;
+}
+
+static int tw_toff(int npops, int k) { return k * npops - k * (k - 1) / 2; }
+static int tw_moff(int npops, int k)
+{
+  int m = 0;
+  for (int j = 0; j < k; j++) m += (npops - j) * (npops - j);
+  return m;
+}
+
+typedef struct { double t; int cmt, pop, topop, ord; } tw_event;
+
+static int tw_cmp(const void *a, const void *b)
+{
+  const tw_event *x = (const tw_event *)a, *y = (const tw_event *)b;
+  if (x->t < y->t) return -1;
+  if (x->t > y->t) return 1;
+  return x->ord - y->ord;
+}
+
+static int tw_period(const double *tvals, int nsplit, double t) /* findperiod, :1626 */
+{
+  int k = 0;
+  while (k < nsplit && tvals[k] <= t) k++;
+  return k;
+}
+
+int ora_treeweight(int npops, const int *plist, const int *droppops, const int *addpop,
+                   const int *pop_e, const int *pop_down, const double *tvals, int nomig,
+                   int ng, const int *samppop, double hval, const int *up0,
+                   const double *time, const int *pop, const int *mig_off,
+                   const double *mig_t, const int *mig_p, int *cc, double *hcc,
+                   double *fc, int *mc, double *fm, double *out3, int *mignum)
+{
+  int T, M, nl = 2 * ng - 1, nsplit = npops - 1, ntp = 2 * npops - 1;
+  ora_tw_sizes(npops, &T, &M);
+  memset(cc, 0, sizeof(int) * (size_t)T);
+  memset(hcc, 0, sizeof(double) * (size_t)T);
+  memset(fc, 0, sizeof(double) * (size_t)T);
+  memset(mc, 0, sizeof(int) * (size_t)M);
+  memset(fm, 0, sizeof(double) * (size_t)M);
+  if (npops < 2) return 1;
+  int nmig = mig_off[nl];
+  /* roottime: the root's coalescence, the latest of all */
+  double roottime = 0.0;
+  for (int i = ng; i < nl; i++)
+    if (time[up0[i]] > roottime) roottime = time[up0[i]];
+  int kroot = tw_period(tvals, nsplit, roottime);
+  int ne = (ng - 1) + nmig + kroot;
+  tw_event *ev = (tw_event *)malloc(sizeof(tw_event) * (size_t)(ne > 0 ? ne : 1));
+  int e = 0;
+  for (int i = 0; i < nl; i++) {
+    int nowpop = pop[i];
+    if (nowpop < 0 || nowpop >= ntp) { free(ev); return 1; }
+    if (i >= ng) {
+      ev[e].t = time[up0[i]];
+      ev[e].cmt = 0;
+      ev[e].pop = nowpop;
+      ev[e].topop = -1;
+      ev[e].ord = e;
+      e++;
+    }
+    for (int j = mig_off[i]; j < mig_off[i + 1]; j++) {
+      int per = tw_period(tvals, nsplit, mig_t[j]);
+      while (pop_e[nowpop] <= per && pop_e[nowpop] != -1) nowpop = pop_down[nowpop];
+      ev[e].t = mig_t[j];
+      ev[e].cmt = 1;
+      ev[e].pop = nowpop;
+      ev[e].topop = mig_p[j];
+      ev[e].ord = e;
+      if (mig_p[j] == nowpop || mig_p[j] < 0 || mig_p[j] >= ntp) { free(ev); return 1; }
+      nowpop = mig_p[j];
+      e++;
+    }
+  }
+  for (int i = 0; i < kroot; i++) {
+    ev[e].t = tvals[i];
+    ev[e].cmt = -1;
+    ev[e].pop = ev[e].topop = -1;
+    ev[e].ord = e;
+    e++;
+  }
+  qsort(ev, (size_t)ne, sizeof(tw_event), tw_cmp);
+
+  int n[2 * 10 - 1];
+  for (int i = 0; i < ntp; i++) n[i] = 0;
+  for (int i = 0; i < npops; i++) n[i] = samppop[i];
+  int nsum = ng, k = 0, bad = 0;
+  double lasttime = 0.0, length = 0.0, tlength = 0.0;
+  double h2term = 1 / (2 * hval);
+  double lastsplitt = tvals[nsplit - 1];
+  for (int j = 0; j < ne && !bad; j++) {
+    const tw_event *s = &ev[j];
+    double dt = s->t - lasttime;
+    double tadd = nsum * dt;
+    length += tadd;
+    if (s->t < lastsplitt) tlength += tadd;
+    else if (lasttime < lastsplitt) tlength += nsum * (lastsplitt - lasttime);
+    lasttime = s->t;
+    for (int ii = 0; ii < npops - k; ii++) {
+      int ip = plist[k * npops + ii];
+      double nn1 = (double)n[ip] * ((double)n[ip] - 1);
+      fc[tw_toff(npops, k) + ii] += nn1 * dt * h2term;
+      if (!nomig && k < nsplit) {
+        double fmtemp = n[ip] * dt;
+        for (int jj = 0; jj < npops - k; jj++)
+          if (jj != ii) fm[tw_moff(npops, k) + ii * (npops - k) + jj] += fmtemp;
+      }
+    }
+    if (s->cmt == 0) {
+      int ii = 0;
+      while (ii < npops - k && plist[k * npops + ii] != s->pop) ii++;
+      if (ii == npops - k || n[s->pop] < 2) { bad = 1; break; }
+      cc[tw_toff(npops, k) + ii]++;
+      n[s->pop]--;
+      nsum--;
+    } else if (s->cmt == 1) {
+      int ii = 0, jj = 0;
+      while (ii < npops - k && plist[k * npops + ii] != s->pop) ii++;
+      while (jj < npops - k && plist[k * npops + jj] != s->topop) jj++;
+      if (ii == npops - k || jj == npops - k || n[s->pop] < 1 || k >= nsplit) { bad = 1; break; }
+      mc[tw_moff(npops, k) + ii * (npops - k) + jj]++;
+      n[s->pop]--;
+      n[s->topop]++;
+    } else {
+      k++;
+      n[addpop[k]] = n[droppops[2 * k]] + n[droppops[2 * k + 1]];
+      n[droppops[2 * k]] = n[droppops[2 * k + 1]] = 0;
+    }
+  }
+  free(ev);
+  if (bad || nsum != 1) return 1;
+  double hlog = log(hval);
+  if (hlog != 0.0)
+    for (int i = 0; i < T; i++) hcc[i] += hlog * cc[i];
+  out3[0] = length;
+  out3[1] = tlength;
+  *mignum = nmig;
+  return 0;
+}
+
+/* ======================================================================
+ * p(G) integrals.  The reference's incomplete gamma functions
+ * (utilities.cpp:808-1130; Numerical Recipes series and Lentz continued
+ * fraction, EPS 3e-7, ITMAX 1000; expint with MAXIT 100 and its own
+ * truncated Euler constant) return logs; logfact[i] is the running sum
+ * log(1)+...+log(i) (setlogfact, utilities.cpp:1406-1415).  A stop the
+ * reference would take through IM_err sets *st.
+ * ==================================================================== */
+#define IG_EPS 3.0e-7
+#define IG_ITMAX 1000
+#define IG_FPMIN 1.0e-30
+#define EI_MAXIT 100
+#define EI_EULER 0.5772156649
+#define LD_CUT 7.0978271289338397e+02
+#define ORA_MPRIORMIN 0.000001 /* imamp.hpp:137 */
+
+static double *lf_tab;
+static int lf_n;
+static double lf(int i, int *st)
+{
+  if (i < 0) { *st = 3; return 0.0; }
+  if (i >= lf_n) {
+    int nn = lf_n ? lf_n : 1024;
+    while (nn <= i) nn *= 2;
+    double *t = (double *)realloc(lf_tab, sizeof(double) * (size_t)nn);
+    if (!t) { *st = 3; return 0.0; }
+    if (lf_n == 0) t[0] = 0.0;
+    for (int k = lf_n ? lf_n : 1; k < nn; k++) t[k] = t[k - 1] + log((double)k);
+    lf_tab = t;
+    lf_n = nn;
+  }
+  return lf_tab[i];
+}
+
+static double ig_gser(int a, double x, double *gln, int lg, int *st) /* gser / gserlog */
+{
+  *gln = lf(a - 1, st);
+  if (x <= 0.0) {
+    if (x < 0.0) *st = 3;
+    return 0.0;
+  }
+  double ap = a, del = 1.0 / a, sum = del;
+  for (int n = 1; n <= IG_ITMAX; n++) {
+    ++ap;
+    del *= x / ap;
+    sum += del;
+    if (fabs(del) < fabs(sum) * IG_EPS)
+      return lg ? log(sum) + (-x + a * log(x) - (*gln)) : sum * exp(-x + a * log(x) - (*gln));
+  }
+  *st = 2;
+  return 0.0;
+}
+
+static double ig_gcf(double a, double x, double *gln, int lg, int *st) /* gcf / gcflog */
+{
+  *gln = lf((int)a - 1, st);
+  double b = x + 1.0 - a, c = 1.0 / IG_FPMIN, d = 1.0 / b, h = d, an, del;
+  int i;
+  for (i = 1; i <= IG_ITMAX; i++) {
+    an = -i * (i - a);
+    b += 2.0;
+    d = an * d + b;
+    if (fabs(d) < IG_FPMIN) d = IG_FPMIN;
+    c = b + an / c;
+    if (fabs(c) < IG_FPMIN) c = IG_FPMIN;
+    d = 1.0 / d;
+    del = d * c;
+    h *= del;
+    if (fabs(del - 1.0) < IG_EPS) break;
+  }
+  if (i > IG_ITMAX) *st = 2;
+  return lg ? (-x + a * log(x) - (*gln)) + log(h) : exp(-x + a * log(x) - (*gln)) * h;
+}
+
+static double ig_expint1(double x, int *islog, int *st) /* expint(1, x) */
+{
+  *islog = 0;
+  if (x <= 0.0) { *st = 3; return 0.0; }
+  if (x > 1.0) {
+    double b = x + 1, c = 1.0 / IG_FPMIN, d = 1.0 / b, h = d, a, del;
+    for (int i = 1; i <= EI_MAXIT; i++) {
+      a = -i * i;
+      b += 2.0;
+      d = 1.0 / (a * d + b);
+      c = b + a / c;
+      del = c * d;
+      h *= del;
+      if (fabs(del - 1.0) < IG_EPS) {
+        *islog = 1;
+        return log(h) - x;
+      }
+    }
+    *st = 2;
+    return 0.0;
+  }
+  double ans = -log(x) - EI_EULER, fact = 1.0, del;
+  for (int i = 1; i <= EI_MAXIT; i++) {
+    fact *= -x / i;
+    del = -fact / i;
+    ans += del;
+    if (fabs(del) < fabs(ans) * IG_EPS) return ans;
+  }
+  *st = 2;
+  return ans;
+}
+
+static double ig_upper(int a, double x, int *st) /* uppergamma, :1068 */
+{
+  double p, gln;
+  if (x < 0.0 || a < 0) { *st = 3; return 0.0; }
+  if (a == 0) {
+    int islog;
+    double t = ig_expint1(x, &islog, st);
+    p = islog ? t : log(t);
+  } else if (x < (a + 1.0)) {
+    double g = ig_gser(a, x, &gln, 0, st);
+    p = gln + log(1.0 - g);
+  } else {
+    double g = ig_gcf((double)a, x, &gln, 1, st);
+    p = gln + g;
+  }
+  if (p < -1e200) p = -1e200;
+  return p;
+}
+
+static double ig_lower(int a, double x, int *st) /* lowergamma, :1104 */
+{
+  double p, gln;
+  if (x < 0.0 || a <= 0) { *st = 3; return 0.0; }
+  if (x < (a + 1.0)) {
+    double g = ig_gser(a, x, &gln, 1, st);
+    p = gln + g;
+  } else {
+    double g = ig_gcf((double)a, x, &gln, 0, st);
+    p = gln + log(1 - g);
+  }
+  if (p < -1e200) p = -1e200;
+  return p;
+}
+
+/* LogDiff (imamp.hpp:257-262): log(exp(a) - exp(b)), a > b required */
+static double ld(double a, double b, int *st)
+{
+  if (a <= b) { *st = 1; return 0.0; }
+  return (a - b < LD_CUT) ? b + log(exp(a - b) - 1.0) : a;
+}
+
+static double it_coal(int cc, double fc, double hcc, double max, double min, int *st)
+{
+  double p;
+  if (cc > 0) {
+    if (!(fc > 0)) { *st = 3; return 0.0; }
+    if (min == 0) {
+      double ug = ig_upper(cc - 1, 2 * fc / max, st);
+      if (cc > 1) {
+        double fullg = lf(cc - 2, st);
+        if (fullg - ug < 1e-15 || fullg - ug > LD_CUT) {
+          double lg = ig_lower(cc - 1, 2 * fc / max, st);
+          if (fullg > lg) {
+            double ugalt = ld(fullg, lg, st);
+            if (fabs(ugalt - ug) > 1e-10) ug = ugalt;
+          }
+        }
+      }
+      p = ug + ORA_LOG2 - hcc + (1 - cc) * log(fc);
+    } else {
+      double a = ig_upper(cc - 1, 2 * fc / max, st), b = ig_upper(cc - 1, 2 * fc / min, st);
+      p = ld(a, b, st);
+      p += (ORA_LOG2 - hcc + (1 - cc) * log(fc));
+    }
+  } else if (2 * fc / max > 0) {
+    if (min == 0) {
+      double a = log(max) - 2.0 * fc / max;
+      double b = ORA_LOG2 + log(fc) + ig_upper(0, 2.0 * fc / max, st);
+      p = ld(a, b, st);
+    } else {
+      double a = ig_upper(0, 2 * fc / max, st), b = ig_upper(0, 2 * fc / min, st);
+      double c = ld(a, b, st);
+      c += ORA_LOG2 + log(fc);
+      a = log(max) - 2.0 * fc / max;
+      b = log(min) - 2.0 * fc / min;
+      double d = ld(a, b, st);
+      p = ld(d, c, st);
+    }
+  } else {
+    p = log(max - min);
+  }
+  return p;
+}
+
+static double it_mig(int cm, double fm, double max, double min, int *st)
+{
+  double p;
+  if (cm > 0) {
+    if (!(fm > 0)) { *st = 3; return 0.0; }
+    if (min == 0) {
+      double lg = ig_lower(cm + 1, fm * max, st);
+      double fullg = lf(cm, st);
+      if (fullg - lg < 1e-15 || fullg - lg > LD_CUT) {
+        double ug = ig_upper(cm + 1, fm * max, st);
+        if (fullg > ug) {
+          double lgalt = ld(fullg, ug, st);
+          if (fabs(lgalt - lg) > 1e-12) lg = lgalt;
+        }
+      }
+      p = (-1 - cm) * log(fm) + lg;
+    } else {
+      double a = ig_upper(cm + 1, fm * min, st), b = ig_upper(cm + 1, fm * max, st);
+      double c = ld(a, b, st);
+      p = (-1 - cm) * log(fm) + c;
+    }
+  } else if (fm > ORA_MPRIORMIN) {
+    if (min == 0) {
+      if (max == ORA_MPRIORMIN) {
+        p = 0;
+      } else {
+        double c = ld(0.0, -fm * max, st);
+        p = c - log(fm);
+      }
+    } else {
+      double c = ld(-fm * min, -fm * max, st);
+      p = c - log(fm);
+    }
+  } else {
+    p = log(max - min);
+  }
+  return p;
+}
+
+static double it_mig_expo(int cm, double fm, double mean, int *st)
+{
+  return -log(mean) + (-(cm + 1) * log(fm + 1.0 / mean)) + lf(cm, st);
+}
+
+double ora_iterm(int kind, int c, double f, double h, double max, double min, int *status)
+{
+  int st = 0;
+  double v = kind == 0 ? it_coal(c, f, h, max, min, &st)
+           : kind == 1 ? it_mig(c, f, max, min, &st) : it_mig_expo(c, f, max, &st);
+  *status = st;
+  return v;
+}
+
+int ora_tree_prob(int nomig, int expo, const int *cc, const double *hcc, const double *fc,
+                  const int *mc, const double *fm, int nth, const int *th_off,
+                  const int *th_idx, const double *th_max, const double *th_min, int nmg,
+                  const int *mg_off, const int *mg_idx, const double *mg_max,
+                  const double *mg_min, const double *mg_mean, int nchk, const int *chk_idx,
+                  double *probg, double *q, double *m)
+{
+  int st = 0;
+  if (!nomig)
+    for (int i = 0; i < nchk; i++)
+      if (mc[chk_idx[i]] != 0) {
+        *probg = -DBL_MAX; /* MYDBL_MAX, imamp.hpp */
+        return 0;
+      }
+  double psum = 0;
+  for (int i = 0; i < nth; i++) {
+    int c = 0;
+    double f = 0.0, hc = 0.0;
+    for (int j = th_off[i]; j < th_off[i + 1]; j++) {
+      c += cc[th_idx[j]];
+      f += fc[th_idx[j]];
+      hc += hcc[th_idx[j]];
+    }
+    q[i] = it_coal(c, f, hc, th_max[i], th_min[i], &st);
+    psum += q[i];
+  }
+  if (!nomig)
+    for (int i = 0; i < nmg; i++) {
+      int c = 0;
+      double f = 0.0;
+      for (int j = mg_off[i]; j < mg_off[i + 1]; j++) {
+        c += mc[mg_idx[j]];
+        f += fm[mg_idx[j]];
+      }
+      m[i] = expo ? it_mig_expo(c, f, mg_mean[i], &st) : it_mig(c, f, mg_max[i], mg_min[i], &st);
+      psum += m[i];
+    }
+  *probg = psum;
+  return st;
+}
+
+void ora_gsamp_row(int nomig, const int *cc, const double *hcc, const double *fc,
+                   const int *mc, const double *fm, int nth, const int *th_off,
+                   const int *th_idx, int nmg, const int *mg_off, const int *mg_idx,
+                   const double *q, const double *m, double pdg, double probg,
+                   int nsplit, const double *tvals, float *row)
+{
+  int nmg_eff = nomig ? 0 : nmg;
+  int ccp = 0, fcp = nth, hccp = 2 * nth, mcp = 3 * nth, fmp = mcp + nmg_eff;
+  int qip = fmp + nmg_eff, mip = qip + nth, pdgp = mip + nmg_eff, probgp = pdgp + 1,
+      tp = probgp + 1;
+  for (int i = 0; i < nth; i++) {
+    int c = 0;
+    float f = 0.0f, hc = 0.0f;
+    for (int j = th_off[i]; j < th_off[i + 1]; j++) {
+      c += cc[th_idx[j]];
+      f += (float)fc[th_idx[j]];
+      hc += (float)hcc[th_idx[j]];
+    }
+    row[ccp + i] = (float)c;
+    row[fcp + i] = f;
+    row[hccp + i] = hc;
+  }
+  for (int i = 0; i < nmg_eff; i++) {
+    int c = 0;
+    float f = 0.0f;
+    for (int j = mg_off[i]; j < mg_off[i + 1]; j++) {
+      c += mc[mg_idx[j]];
+      f += (float)fm[mg_idx[j]];
+    }
+    row[mcp + i] = (float)c;
+    row[fmp + i] = f;
+  }
+  for (int i = 0; i < nth; i++) row[qip + i] = (float)q[i];
+  for (int i = 0; i < nmg_eff; i++) row[mip + i] = (float)m[i];
+  row[pdgp] = (float)pdg;
+  row[probgp] = (float)probg;
+  for (int i = 0; i < nsplit; i++) row[tp + i] = (float)tvals[i];
+}

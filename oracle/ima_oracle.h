@@ -140,6 +140,56 @@ int ora_modelloop(int G, int rowlen, const float *g, int np, int nm, int npops,
                   int nested, ora_mt *rng, double *best, double *ess,
                   int *restarts);
 
+/* ---- genealogy weights and p(G) (update_gtree_common.cpp:108-304,
+ *      :1680-2134; ginfo.cpp:209-244, :318-377) ---------------------------
+ * Weight layout for npops sampled populations (numsplittimes = npops-1):
+ *   T = npops(npops+1)/2 entries for cc/hcc/fc: period k, position ii in the
+ *       period's population list at  k*npops - k(k-1)/2 + ii;
+ *   M = sum_{k<npops-1} (npops-k)^2 entries for mc/fm: period k, positions
+ *       (ii, jj) at  moff(k) + ii*(npops-k) + jj.
+ * Population model tables, as fillplist (build_poptree.cpp:391-450) leaves
+ * them: plist[k*npops+ii], droppops[k*2+{0,1}], addpop[k] (k = 1..npops-1),
+ * pop_e[p] / pop_down[p] for the 2npops-1 tree populations.  */
+int ora_tw_sizes(int npops, int *T, int *M);
+/* treeweight restated (update_gtree_common.cpp:1680-1937) for one genealogy
+ * whose weights start at zero.  up0/time/pop per node (2ng-1), migration
+ * events per node in CSR form (mig_off[2ng], times, destination pops).
+ * out3 = {length, tlength}; *mignum.  Returns 0, or 1 for a genealogy the
+ * model cannot hold (a coalescence or migration in a population that does
+ * not exist in that period, or a count going negative). */
+int ora_treeweight(int npops, const int *plist, const int *droppops, const int *addpop,
+                   const int *pop_e, const int *pop_down, const double *tvals, int nomig,
+                   int ng, const int *samppop, double hval, const int *up0,
+                   const double *time, const int *pop, const int *mig_off,
+                   const double *mig_t, const int *mig_p, int *cc, double *hcc,
+                   double *fc, int *mc, double *fm, double *out3, int *mignum);
+/* The integral terms (update_gtree_common.cpp:108-304, MORESTABLE form) on
+ * the reference's incomplete gamma functions (utilities.cpp:808-1130).
+ * kind 0: integrate_coalescent_term(c, f, h, max, min); 1:
+ * integrate_migration_term(c, f, max, min); 2:
+ * integrate_migration_term_expo_prior(c, f, mean = max).  *status 0 ok,
+ * else the reference would stop with IM_err (LogDiff order, iteration
+ * limit, bad argument). */
+double ora_iterm(int kind, int c, double f, double h, double max, double min, int *status);
+/* initialize_integrate_tree_prob restated (:2089-2134) on weights already
+ * summed over loci.  Theta parameter i sums the T entries th_idx[th_off[i] ..
+ * th_off[i+1]) in order, migration parameter i the M entries mg_idx[...];
+ * chk_idx: M entries that must hold no migration (nomigrationchecklist).
+ * Returns 0, or the term's status. */
+int ora_tree_prob(int nomig, int expo, const int *cc, const double *hcc, const double *fc,
+                  const int *mc, const double *fm, int nth, const int *th_off,
+                  const int *th_idx, const double *th_max, const double *th_min, int nmg,
+                  const int *mg_off, const int *mg_idx, const double *mg_max,
+                  const double *mg_min, const double *mg_mean, int nchk, const int *chk_idx,
+                  double *probg, double *q, double *m);
+/* savegsampinf restated (ginfo.cpp:318-377): one gsampinf row (float) from
+ * summed weights, integrals, pdg and split times. */
+void ora_gsamp_row(int nomig, const int *cc, const double *hcc, const double *fc,
+                   const int *mc, const double *fm, int nth, const int *th_off,
+                   const int *th_idx, int nmg, const int *mg_off, const int *mg_idx,
+                   const double *q, const double *m, double pdg, double probg,
+                   int nsplit, const double *tvals, float *row);
+
 #ifdef __cplusplus
 }
 #endif

@@ -76,6 +76,14 @@ def _declare(L):
     L.ora_mt_uniform.restype = D
     L.ora_modelloop.argtypes = [I, I, P, I, I, I, P, I, I, P, I, P, I, P, P, P, P]
     L.ora_modelloop.restype = I
+    L.ora_treeweight.argtypes = [I, P, P, P, P, P, P, I, I, P, D, P, P, P, P, P, P, P, P, P, P, P, P, P]
+    L.ora_treeweight.restype = I
+    L.ora_iterm.argtypes = [I, I, D, D, D, D, P]
+    L.ora_iterm.restype = D
+    L.ora_tree_prob.argtypes = [I, I, P, P, P, P, P, I, P, P, P, P, I, P, P, P, P, P, I, P, P, P, P]
+    L.ora_tree_prob.restype = I
+    L.ora_gsamp_row.argtypes = [I, P, P, P, P, P, I, P, P, I, P, P, P, P, D, D, I, P, P]
+    L.ora_gsamp_row.restype = None
 
 
 def _p(a):
@@ -356,3 +364,129 @@ def ref_margincalc(rows, np_, nm, points, expo_mean=None):
     lines += ["%d %.17g %d %.17g" % (int(p), x, int(lg), ya) for p, x, lg, ya in points]
     out = run_ref("margin", "\n".join(lines) + "\n")
     return np.array([float(v) for v in out.split()])
+
+
+# ------------------------------------------------- treeweight + p(G) integral
+def ref_tw(npops, treestr, loci, tvals, gens, thetaprior, mprior, expo=False, nomig=False):
+    """The reference's treeweight, sum_treeinfo and
+    initialize_integrate_tree_prob through oracle/_ref/imaref (this container
+    only).  loci: (numgenes, hval, samppop) per locus; tvals: split times per
+    chain; gens[ci][li]: LabelledGenealogy.  Returns a dict with the
+    parameter maps ("theta": [(wp, max, min)], "mig": [(wp, max, min, mean)]),
+    per chain-locus weights ("gw") and per chain integrals ("pg")."""
+    nch, nl = len(gens), len(loci)
+    t = ["%d %d %d %d %d" % (npops, nch, nl, int(expo), int(nomig)), treestr,
+         "%.17g %.17g" % (thetaprior, mprior)]
+    for ng, h, sp in loci:
+        t.append("%d %.17g %s" % (ng, h, " ".join(map(str, sp))))
+    for tv in tvals:
+        t.append(" ".join("%.17g" % v for v in tv) if len(tv) else "")
+    for ci in range(nch):
+        for li in range(nl):
+            lg = gens[ci][li]
+            t.append(str(len(lg.pop)))
+            t.append(_tree_txt(lg.g) + " ".join(map(str, lg.pop)))
+            for m in lg.mig:
+                t.append(" ".join([str(len(m))] + ["%.17g %d" % (mt, mp) for mt, mp in m]))
+    out = run_ref("tw", "\n".join(t) + "\n")
+    T = npops * (npops + 1) // 2
+    M = 0 if nomig else sum((npops - k) ** 2 for k in range(npops - 1))
+    res = {"theta": [], "mig": [], "gw": {}, "pg": {}}
+    for ln in out.splitlines():
+        f = ln.split()
+        if f[0] == "TH":
+            n = int(f[2])
+            wp = [(int(f[3 + 2 * j]), int(f[4 + 2 * j])) for j in range(n)]
+            res["theta"].append((wp, float(f[3 + 2 * n]), float(f[4 + 2 * n])))
+        elif f[0] == "MG":
+            n = int(f[2])
+            wp = [(int(f[3 + 3 * j]), int(f[4 + 3 * j]), int(f[5 + 3 * j])) for j in range(n)]
+            res["mig"].append((wp, float(f[3 + 3 * n]), float(f[4 + 3 * n]), float(f[5 + 3 * n])))
+        elif f[0] == "GW":
+            v = f[3:]
+            o = 0
+            d = {"mignum": int(v[0]), "length": float(v[1]), "tlength": float(v[2])}
+            o = 3
+            d["cc"] = np.array([int(x) for x in v[o:o + T]]); o += T
+            d["hcc"] = np.array([float(x) for x in v[o:o + T]]); o += T
+            d["fc"] = np.array([float(x) for x in v[o:o + T]]); o += T
+            d["mc"] = np.array([int(x) for x in v[o:o + M]], dtype=np.int64); o += M
+            d["fm"] = np.array([float(x) for x in v[o:o + M]]); o += M
+            res["gw"][(int(f[1]), int(f[2]))] = d
+        elif f[0] == "PG":
+            res["pg"][int(f[1])] = np.array([float(x) for x in f[2:]])
+    return res
+
+
+def ref_iterm(lines):
+    """Reference integral terms; lines: (kind, c, f, h, max, min) with kind 0
+    coalescent, 1 migration, 2 migration under the exponential prior (max is
+    then the prior mean)."""
+    t = [str(len(lines))] + ["%d %d %.17g %.17g %.17g %.17g" % tuple(x) for x in lines]
+    return np.array([float(v) for v in run_ref("iterm", "\n".join(t) + "\n").split()])
+
+
+def treeweight(pm, tvals, lg, samppop, hval):
+    """ora_treeweight on one LabelledGenealogy; returns (status, dict)."""
+    T, M = pm.T, pm.M
+    g = lg.g
+    ng = g.n
+    off, mt, mp = lg.packed_mig()
+    cc = np.zeros(T, np.int32); hcc = np.zeros(T); fc = np.zeros(T)
+    mc = np.zeros(max(M, 1), np.int32); fm = np.zeros(max(M, 1))
+    out3 = np.zeros(2); mn = np.zeros(1, np.int32)
+    st = lib().ora_treeweight(pm.npops, _p(_i32(pm.plist)), _p(_i32(pm.droppops)), _p(_i32(pm.addpop)),
+                              _p(_i32(pm.pop_e)), _p(_i32(pm.pop_down)), _p(_f64(tvals)), int(pm.nomig),
+                              ng, _p(_i32(samppop)), float(hval), _p(_i32(g.up0)), _p(_f64(g.time)),
+                              _p(_i32(lg.pop)), _p(_i32(off)), _p(_f64(mt if len(mt) else np.zeros(1))),
+                              _p(_i32(mp if len(mp) else np.zeros(1))), _p(cc), _p(hcc), _p(fc),
+                              _p(mc), _p(fm), _p(out3), _p(mn))
+    return st, {"cc": cc, "hcc": hcc, "fc": fc, "mc": mc[:M], "fm": fm[:M],
+                "length": float(out3[0]), "tlength": float(out3[1]), "mignum": int(mn[0])}
+
+
+def iterm(kind, c, f, h, mx, mn):
+    st = np.zeros(1, np.int32)
+    v = lib().ora_iterm(int(kind), int(c), float(f), float(h), float(mx), float(mn), _p(st))
+    return v, int(st[0])
+
+
+def sum_weights(ws, pm):
+    """sum_treeinfo (ginfo.cpp:209-244) over loci in order, from zero."""
+    tot = {"cc": np.zeros(pm.T, np.int32), "hcc": np.zeros(pm.T), "fc": np.zeros(pm.T),
+           "mc": np.zeros(pm.M, np.int32), "fm": np.zeros(pm.M)}
+    for w in ws:
+        for k in tot:
+            tot[k] = tot[k] + w[k]
+    return tot
+
+
+def tree_prob(pm, w, th_max, th_min, mg_max, mg_min, mg_mean, expo=False, chk=()):
+    tho, thi = pm.th_csr()
+    mgo, mgi = pm.mg_csr()
+    nth, nmg = len(pm.th_cells), len(pm.mg_cells)
+    q = np.zeros(max(nth, 1)); m = np.zeros(max(nmg, 1)); pg = np.zeros(1)
+    chk = _i32(np.asarray(chk if len(chk) else [0]))
+    st = lib().ora_tree_prob(int(pm.nomig), int(expo), _p(_i32(w["cc"])), _p(_f64(w["hcc"])), _p(_f64(w["fc"])),
+                             _p(_i32(w["mc"] if pm.M else np.zeros(1))), _p(_f64(w["fm"] if pm.M else np.zeros(1))),
+                             nth, _p(tho), _p(thi if len(thi) else np.zeros(1, np.int32)),
+                             _p(_f64(th_max)), _p(_f64(th_min)),
+                             nmg, _p(mgo), _p(mgi if len(mgi) else np.zeros(1, np.int32)),
+                             _p(_f64(mg_max if nmg else np.zeros(1))), _p(_f64(mg_min if nmg else np.zeros(1))),
+                             _p(_f64(mg_mean if nmg else np.zeros(1))), len(chk) if chk[0] or len(chk) > 1 else 0,
+                             _p(chk), _p(pg), _p(q), _p(m))
+    return st, float(pg[0]), q[:nth], m[:nmg]
+
+
+def gsamp_row(pm, w, q, m, pdg, probg, tvals):
+    tho, thi = pm.th_csr()
+    mgo, mgi = pm.mg_csr()
+    nth, nmg = len(pm.th_cells), len(pm.mg_cells)
+    nm_eff = 0 if pm.nomig else nmg
+    row = np.zeros(3 * nth + 2 * nm_eff + nth + nm_eff + 2 + pm.npops - 1, np.float32)
+    lib().ora_gsamp_row(int(pm.nomig), _p(_i32(w["cc"])), _p(_f64(w["hcc"])), _p(_f64(w["fc"])),
+                        _p(_i32(w["mc"] if pm.M else np.zeros(1))), _p(_f64(w["fm"] if pm.M else np.zeros(1))),
+                        nth, _p(tho), _p(thi), nmg, _p(mgo), _p(mgi if len(mgi) else np.zeros(1, np.int32)),
+                        _p(_f64(q)), _p(_f64(m if len(m) else np.zeros(1))), float(pdg), float(probg),
+                        pm.npops - 1, _p(_f64(tvals)), _p(row))
+    return row

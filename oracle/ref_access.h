@@ -6,4 +6,8 @@ void refacc_jointp_setup(int nparams_total, int modeltype);
 double refacc_jointp(double *x, double *ess);
 void refacc_modelloop(int nparams_total, int modeltype, const double *upper, int multiplier,
                       const double *xmap, int nested_params, double *best_out, double *ess_out);
+double refacc_icoal(int cc, double fc, double hcc, double max, double min);
+double refacc_imig(int cm, double fm, double max, double min);
+double refacc_imig_expo(int cm, double fm, double mean);
+void refacc_setup_iparams(void);
 #endif

@@ -12,7 +12,7 @@
  * ref_access_cpd.cpp and ref_access_jf.cpp include those two reference
  * sources to reach them.  The other reference objects are linked unchanged.
  *
- * Usage:  imaref is|hky|sw|swap|jointp|de|margin <input.txt>   (results on stdout)
+ * Usage:  imaref is|hky|sw|swap|jointp|de|margin|tw|iterm <input.txt>   (results on stdout)
  */
 #undef GLOBVARS
 #include "imamp.hpp"
@@ -292,9 +292,121 @@ static void run_margin()
   }
 }
 
+/* TW: npops nchains nloci expo nomig treestring thetaprior mprior
+ *     per locus: numgenes hval samppop[npops]
+ *     per chain: tvals[npops-1]
+ *     per chain, per locus: nlines up0[] up1[] down[] time[] pop[], then per
+ *       node: nm {mt mp}*nm
+ *   -> "PARAMS np nm", "TH i n {p r}*n max min", "MG i n {p r c}*n max min mean",
+ *      per chain·locus "GW ci li mignum length tlength cc.. hcc.. fc.. mc.. fm..",
+ *      per chain "PG ci probg q.. m.."
+ * treeweight (update_gtree_common.cpp:1680-1937) per chain·locus, summed per
+ * chain by sum_treeinfo (ginfo.cpp:209) in locus order, then
+ * initialize_integrate_tree_prob (:2089-2134), as finish_setup_C does. */
+extern "C" void init_gtreecommon(void);  /* C linkage, as update_gtree_common.hpp declares it */
+static void run_tw()
+{
+  int npp = rd_i(), nch = rd_i(), nl = rd_i(), expo = rd_i(), nomig = rd_i();
+  char treestr[POPTREESTRINGLENGTHMAX];
+  if (fscanf(g_in, "%255s", treestr) != 1) { fprintf(stderr, "short input\n"); exit(3); }
+  thetaprior = rd_d();
+  mprior = rd_d();
+  npops = npp;
+  numtreepops = 2 * npops - 1;
+  lastperiodnumber = numsplittimes = npops - 1;
+  modeloptions[EXPOMIGRATIONPRIOR] = expo;
+  modeloptions[NOMIGRATION] = nomig;
+  alloc_chains(nch, nl);
+  for (int li = 0; li < nl; li++) {
+    L[li].numgenes = rd_i();
+    L[li].hval = rd_d();
+    for (int p = 0; p < npops; p++) L[li].samppop[p] = rd_i();
+  }
+  setlogfact();
+  init_gtreecommon();
+  init_treeweight();
+  for (int ci = 0; ci < nch; ci++) {
+    setup_poptree(ci, treestr);
+    C[ci]->tvals = (double *)calloc((size_t)npops, sizeof(double));
+    for (int k = 0; k < npops - 1; k++) C[ci]->tvals[k] = rd_d();
+  }
+  refacc_setup_iparams();
+  printf("PARAMS %d %d\n", numpopsizeparams, nummigrateparams);
+  for (int i = 0; i < numpopsizeparams; i++) {
+    printf("TH %d %d", i, itheta[i].wp.n);
+    for (int j = 0; j < itheta[i].wp.n; j++) printf(" %d %d", itheta[i].wp.p[j], itheta[i].wp.r[j]);
+    printf(" %.17g %.17g\n", itheta[i].pr.max, itheta[i].pr.min);
+  }
+  for (int i = 0; i < nummigrateparams; i++) {
+    printf("MG %d %d", i, imig[i].wp.n);
+    for (int j = 0; j < imig[i].wp.n; j++) printf(" %d %d %d", imig[i].wp.p[j], imig[i].wp.r[j], imig[i].wp.c[j]);
+    printf(" %.17g %.17g %.17g\n", imig[i].pr.max, imig[i].pr.min, imig[i].pr.mean);
+  }
+  for (int ci = 0; ci < nch; ci++) {
+    init_genealogy_weights(&C[ci]->allgweight);
+    init_probcalc(&C[ci]->allpcalc);
+    for (int li = 0; li < nl; li++) {
+      int nlines = rd_i();
+      struct genealogy *G = &C[ci]->G[li];
+      G->gtree = alloc_tree(nlines);
+      read_tree(G->gtree, nlines);
+      for (int i = 0; i < nlines; i++) G->gtree[i].pop = rd_i();
+      for (int i = 0; i < nlines; i++) {
+        int nm = rd_i();
+        G->gtree[i].mig = (struct migstruct *)calloc((size_t)nm + 1, sizeof(struct migstruct));
+        for (int j = 0; j < nm; j++) {
+          G->gtree[i].mig[j].mt = rd_d();
+          G->gtree[i].mig[j].mp = rd_i();
+        }
+        G->gtree[i].mig[nm].mt = -1.0;
+      }
+      G->root = find_root(G->gtree, nlines);
+      G->roottime = G->gtree[G->gtree[G->root].up[0]].time;
+      init_genealogy_weights(&G->gweight);
+      treeweight(ci, li);
+      sum_treeinfo(&C[ci]->allgweight, &G->gweight);
+      struct genealogy_weights *w = &G->gweight;
+      printf("GW %d %d %d %.17g %.17g", ci, li, G->mignum, G->length, G->tlength);
+      for (int k = 0; k < npops; k++) for (int i = 0; i < npops - k; i++) printf(" %d", w->cc[k][i]);
+      for (int k = 0; k < npops; k++) for (int i = 0; i < npops - k; i++) printf(" %.17g", w->hcc[k][i]);
+      for (int k = 0; k < npops; k++) for (int i = 0; i < npops - k; i++) printf(" %.17g", w->fc[k][i]);
+      if (!nomig) {
+        for (int k = 0; k < lastperiodnumber; k++)
+          for (int i = 0; i < npops - k; i++) for (int j = 0; j < npops - k; j++) printf(" %d", w->mc[k][i][j]);
+        for (int k = 0; k < lastperiodnumber; k++)
+          for (int i = 0; i < npops - k; i++) for (int j = 0; j < npops - k; j++) printf(" %.17g", w->fm[k][i][j]);
+      }
+      printf("\n");
+    }
+    total_numgenes = 0;
+    for (int li = 0; li < nl; li++) total_numgenes += L[li].numgenes;
+    initialize_integrate_tree_prob(ci, &C[ci]->allgweight, &C[ci]->allpcalc);
+    printf("PG %d %.17g", ci, C[ci]->allpcalc.probg);
+    for (int i = 0; i < numpopsizeparams; i++) printf(" %.17g", C[ci]->allpcalc.qintegrate[i]);
+    if (!nomig)
+      for (int i = 0; i < nummigrateparams; i++) printf(" %.17g", C[ci]->allpcalc.mintegrate[i]);
+    printf("\n");
+  }
+}
+
+/* ITERM: n, then per line: kind(0 coal, 1 mig, 2 mig expo) c f h max min
+ *   -> the reference integral term per line (update_gtree_common.cpp:108-304) */
+static void run_iterm()
+{
+  setlogfact();
+  int n = rd_i();
+  for (int k = 0; k < n; k++) {
+    int kind = rd_i(), c = rd_i();
+    double f = rd_d(), h = rd_d(), mx = rd_d(), mn = rd_d();
+    double v = kind == 0 ? refacc_icoal(c, f, h, mx, mn)
+             : kind == 1 ? refacc_imig(c, f, mx, mn) : refacc_imig_expo(c, f, mx);
+    printf("%.17g\n", v);
+  }
+}
+
 int main(int argc, char **argv)
 {
-  if (argc != 3) { fprintf(stderr, "usage: imaref is|hky|sw|swap|jointp|de|margin <input>\n"); return 2; }
+  if (argc != 3) { fprintf(stderr, "usage: imaref is|hky|sw|swap|jointp|de|margin|tw|iterm <input>\n"); return 2; }
   g_in = fopen(argv[2], "r");
   if (!g_in) { perror(argv[2]); return 2; }
   std::string mode = argv[1];
@@ -305,6 +417,8 @@ int main(int argc, char **argv)
   else if (mode == "jointp") run_jointp();
   else if (mode == "de") run_de();
   else if (mode == "margin") run_margin();
+  else if (mode == "tw") run_tw();
+  else if (mode == "iterm") run_iterm();
   else { fprintf(stderr, "unknown mode\n"); return 2; }
   fclose(g_in);
   return 0;

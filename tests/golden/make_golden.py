@@ -20,8 +20,13 @@ Fixtures:
   golden_margin.npz margincalc (1-D marginal densities) on fillvec's grids,
                     plain and log'd with yadjust, uniform and exponential
                     migration priors
+  golden_tw.npz     treeweight (genealogy weights), sum_treeinfo and
+                    initialize_integrate_tree_prob (p(G) integrals) on
+                    population-labelled IM genealogies for 2-5 population
+                    trees, with the reference's own parameter maps
+                    (setup_iparams), and the integral terms on edge cases
 
-Run with fixture names (is hky sw swap jointp de margin) to regenerate only those.
+Run with fixture names (is hky sw swap jointp de margin tw) to regenerate only those.
 """
 from __future__ import annotations
 
@@ -361,11 +366,100 @@ def golden_margin():
     np.savez_compressed(os.path.join(OUT, "golden_margin.npz"), **out)
 
 
+TW_CASES = [
+    # (npops, tree string, chains, loci, migration rate, expo prior, no migration)
+    (2, "(0,1):2", 4, 5, 0.5, False, False),
+    (3, "((0,1):3,2):4", 4, 6, 0.3, True, False),
+    (4, "((0,1):4,(2,3):5):6", 3, 4, 0.3, False, False),
+    (3, "((0,2):3,1):4", 3, 4, 0.0, False, True),
+    (5, "(((0,1):5,2):6,(3,4):7):8", 2, 3, 0.2, False, False),
+]
+
+
+def tw_case(rng, npops, ts, nch, nl, mrate, expo, nomig):
+    from ima2p_gb300 import popmodel
+    sp = popmodel.parse_treestring(ts, npops)
+    loci = []
+    for li in range(nl):
+        samp = [int(v) for v in rng.integers(2, 13, npops)]
+        loci.append((int(sum(samp)), float([1.0, 0.25, 0.75, 1.0][li % 4]), samp))
+    # one chain has splits older than most roots, the others younger
+    tvals = [np.sort(rng.uniform(0.2, 1.5 if ci else 6.0, npops - 1)) for ci in range(nch)]
+    gens = []
+    for ci in range(nch):
+        row = []
+        for ng, h, samp in loci:
+            splits = [(tvals[ci][k], a, b, anc) for k, (a, b, anc) in enumerate(sp)]
+            theta = list(rng.uniform(1.0, 6.0, 2 * npops - 1))
+            row.append(synth.sim_im_labeled(rng, samp, theta, mrate, splits))
+        gens.append(row)
+    return loci, tvals, gens
+
+
+def golden_tw():
+    rng = np.random.default_rng(1010)
+    out = {}
+    for c, (npops, ts, nch, nl, mrate, expo, nomig) in enumerate(TW_CASES):
+        loci, tvals, gens = tw_case(rng, npops, ts, nch, nl, mrate, expo, nomig)
+        thetaprior, mprior = 12.0, 1.5
+        r = O.ref_tw(npops, ts, loci, tvals, gens, thetaprior, mprior, expo=expo, nomig=nomig)
+        k = "c%d_" % c
+        out[k + "meta"] = np.array([npops, nch, nl, int(expo), int(nomig)])
+        out[k + "tree"] = np.array(ts)
+        out[k + "priors"] = np.array([thetaprior, mprior])
+        out[k + "loci"] = np.array([[ng, h] + samp for ng, h, samp in loci], np.float64)
+        out[k + "tvals"] = np.array(tvals)
+        flat = [gens[ci][li] for ci in range(nch) for li in range(nl)]
+        out[k + "node_off"] = np.concatenate([[0], np.cumsum([len(g.pop) for g in flat])]).astype(np.int32)
+        for f in ("up0", "up1", "down", "time"):
+            out[k + f] = np.concatenate([getattr(g.g, f) for g in flat])
+        out[k + "pop"] = np.concatenate([g.pop for g in flat]).astype(np.int32)
+        counts = [len(m) for g in flat for m in g.mig]
+        out[k + "mig_off"] = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+        out[k + "mig_t"] = np.array([e[0] for g in flat for m in g.mig for e in m], np.float64)
+        out[k + "mig_p"] = np.array([e[1] for g in flat for m in g.mig for e in m], np.int32)
+        gw = [r["gw"][(ci, li)] for ci in range(nch) for li in range(nl)]
+        for f in ("cc", "hcc", "fc", "mc", "fm"):
+            out[k + f] = np.array([w[f] for w in gw])
+        out[k + "scal"] = np.array([[w["mignum"], w["length"], w["tlength"]] for w in gw])
+        out[k + "pg"] = np.array([r["pg"][ci] for ci in range(nch)])
+        out[k + "th_wp"] = np.array([len(wp) for wp, _, _ in r["theta"]] + [v for wp, _, _ in r["theta"] for pr in wp for v in pr], np.int32)
+        out[k + "mg_wp"] = np.array([len(wp) for wp, _, _, _ in r["mig"]] + [v for wp, _, _, _ in r["mig"] for pr in wp for v in pr], np.int32)
+        out[k + "th_pr"] = np.array([[mx, mn] for _, mx, mn in r["theta"]])
+        out[k + "mg_pr"] = np.array([[mx, mn, mean] for _, mx, mn, mean in r["mig"]]).reshape(-1, 3)
+    out["ncases"] = np.array(len(TW_CASES))
+    lines, errs = [], []
+    for cc in (0, 1, 2, 3, 7, 30, 150, 900):
+        for fc in (1e-3, 0.05, 0.7, 3.0, 40.0, 900.0, 2e4):
+            for mx, mn in ((10.0, 0.0), (50.0, 0.0), (10.0, 0.5), (3.0, 1.0)):
+                h = float(rng.choice([0.0, -0.6931471805599453, 1.3]) * cc)
+                (errs if O.iterm(0, cc, fc, h, mx, mn)[1] else lines).append((0, cc, fc, h, mx, mn))
+    for cm in (0, 1, 2, 5, 40, 300):
+        for fm in (1e-7, 1e-3, 0.3, 2.0, 25.0, 400.0):
+            for mx, mn in ((2.0, 0.0), (10.0, 0.0), (0.000001, 0.0), (5.0, 0.2)):
+                if cm > 0 and mx == 0.000001:
+                    continue
+                (errs if O.iterm(1, cm, fm, 0.0, mx, mn)[1] else lines).append((1, cm, fm, 0.0, mx, mn))
+            lines.append((2, cm, fm, 0.0, 1.7, 0.0))
+    out["iterm_lines"] = np.array(lines)
+    out["iterm_ref"] = O.ref_iterm(lines)
+    stopped = []
+    for l in errs:  # the reference stops (IM_err) on each of these
+        try:
+            O.ref_iterm([l])
+        except Exception:
+            stopped.append(l)
+    assert len(stopped) == len(errs)
+    out["iterm_stop"] = np.array(errs)
+    np.savez_compressed(os.path.join(OUT, "golden_tw.npz"), **out)
+
+
 if __name__ == "__main__":
     if not O.ref_available():
         sys.exit("build the reference harness first: make -C oracle ref")
     gens = {"is": golden_is, "hky": golden_hky, "sw": golden_sw, "swap": golden_swap,
-            "jointp": golden_jointp, "de": golden_de, "margin": golden_margin}
+            "jointp": golden_jointp, "de": golden_de, "margin": golden_margin,
+            "tw": golden_tw}
     for name in (sys.argv[1:] or list(gens)):
         gens[name]()
     for f in sorted(os.listdir(OUT)):
