@@ -24,7 +24,7 @@ PREC_FAST, PREC_FP64 = 0, 1
 EVAL_OK, EVAL_IS_REJECT, EVAL_IS_FAIL, EVAL_SW_ZERO = 0, 1, 2, 3
 SURF_FAST, SURF_FP64, SURF_COMPAT, SURF_TC = 0, 1, 2, 3
 K_IS, K_IS_SUMLOGK, K_HKY_FAST, K_HKY_FP64, K_SW_FAST, K_SW_FP64, K_SWAP, K_SURF_FAST, \
-    K_SURF_FP64, K_SURF_COMPAT, K_SURF_TC, K_MARGIN = range(12)
+    K_SURF_FP64, K_SURF_COMPAT, K_SURF_TC, K_MARGIN, K_TREEWEIGHT, K_TREE_PROB = range(14)
 KERNEL_NAMES = ["is", "is_sumlogk", "hky_fast", "hky_fp64", "sw_fast", "sw_fp64", "swap",
                 "surf_fast", "surf_fp64", "surf_compat", "surf_tc"]
 REJECT_IS = -1000000000.0
@@ -47,7 +47,7 @@ EXPORTS = [
     "ima_ti_read", "ima_ti_write_binary", "ima_ti_read_binary",
     "ima_gpu_timer_begin", "ima_gpu_timer_end",
     "ima_gpu_set_profiling", "ima_gpu_kernel_stats", "ima_gpu_launch_count", "ima_gpu_flush_l2",
-    "ima_gpu_memory",
+    "ima_gpu_memory", "ima_gpu_set_popmodel", "ima_gpu_treeweight", "ima_gpu_tree_prob",
 ]
 
 
@@ -171,6 +171,9 @@ def _declare(L):
         "ima_ti_write_binary": (I, [C.c_char_p, I, I, P]),
         "ima_ti_read_binary": (I, [C.c_char_p, C.POINTER(I), C.POINTER(I), P, I]),
         "ima_gpu_margincalc": (I, [P, I, P, P, D, I, P, P]),
+        "ima_gpu_set_popmodel": (I, [P, I, I, I, P, P, P, P, P, I, P, P, P, P, I, P, P, P, P, P, I, P]),
+        "ima_gpu_treeweight": (I, [P, I, P, P, P, P, P, P, P, P, P, I, P, P, I, P, P, P, P, P, P, P, P]),
+        "ima_gpu_tree_prob": (I, [P, I, P, P, P, P, P, P, P]),
         "ima_gpu_fillvec": (I, [P, I, P, P, P, P, P]),
         "ima_gpu_batch_set_variants": (I, [P, I, I, I]),
         "ima_gpu_set_allele_edits": (I, [P, I, P, P, P, P, P]),
@@ -433,6 +436,66 @@ class Context:
                                              _ptr(em) if em is not None else None, _ptr(out)))
         return out
 
+    # ------------------------------------- genealogy weights and p(G)
+    def set_popmodel(self, pm, th_max, th_min=None, mg_max=None, mg_min=None, mg_mean=None, expo=False,
+                     chk=()):
+        """Load a population model (ima2p_gb300.popmodel.PopModel) with the
+        priors of its parameters (itheta[].pr, imig[].pr)."""
+        nth, nmg = len(pm.th_cells), len(pm.mg_cells)
+        tho, thi = pm.th_csr()
+        mgo, mgi = pm.mg_csr()
+        th_max = _f64(np.broadcast_to(np.asarray(th_max, np.float64), (nth,)))
+        th_min = _f64(np.zeros(nth) if th_min is None else np.broadcast_to(np.asarray(th_min, np.float64), (nth,)))
+        z = np.zeros(max(nmg, 1))
+        mg_max = _f64(z if mg_max is None else np.broadcast_to(np.asarray(mg_max, np.float64), (nmg,)))
+        mg_min = _f64(z if mg_min is None else np.broadcast_to(np.asarray(mg_min, np.float64), (nmg,)))
+        mg_mean = _f64(z if mg_mean is None else np.broadcast_to(np.asarray(mg_mean, np.float64), (nmg,)))
+        chk = _i32(np.asarray(chk, np.int32) if len(chk) else np.zeros(1, np.int32))
+        keep = [_i32(pm.plist.ravel()), _i32(pm.droppops.ravel()), _i32(pm.addpop), _i32(pm.pop_e),
+                _i32(pm.pop_down), tho, _i32(thi if len(thi) else np.zeros(1)), mgo,
+                _i32(mgi if len(mgi) else np.zeros(1))]
+        self._ck(self.lib.ima_gpu_set_popmodel(
+            self.h, pm.npops, int(pm.nomig), int(expo), *(_ptr(a) for a in keep[:5]), nth, _ptr(keep[5]),
+            _ptr(keep[6]), _ptr(th_max), _ptr(th_min), nmg, _ptr(keep[7]), _ptr(keep[8]), _ptr(mg_max),
+            _ptr(mg_min), _ptr(mg_mean), len(chk) if len(chk) > 1 or chk[0] else 0, _ptr(chk)))
+        self._tw_pm = pm
+
+    def treeweight(self, packed, gen_locus, gen_tv, hval, samppop, tvals):
+        """treeweight for many genealogies.  packed: (node_off, up0, time, pop,
+        mig_off, mig_t, mig_p) as pack_labelled() makes them.  Returns a dict
+        of cc, hcc, fc [ngen][T], mc, fm [ngen][M], lens [ngen][2], mignum."""
+        pm = self._tw_pm
+        node_off, up0, time, pop, mig_off, mig_t, mig_p = packed
+        ngen = len(node_off) - 1
+        T, M = pm.T, pm.M
+        out = {"cc": np.zeros((ngen, T), np.int32), "hcc": np.zeros((ngen, T)), "fc": np.zeros((ngen, T)),
+               "mc": np.zeros((ngen, M), np.int32), "fm": np.zeros((ngen, M)), "lens": np.zeros((ngen, 2)),
+               "mignum": np.zeros(ngen, np.int32)}
+        ins = [_i32(node_off), _i32(up0), _f64(time), _i32(pop), _i32(mig_off),
+               _f64(mig_t if len(mig_t) else np.zeros(1)), _i32(mig_p if len(mig_p) else np.zeros(1)),
+               _i32(gen_locus), _i32(gen_tv)]
+        hval, samppop, tvals = _f64(np.atleast_1d(hval)), _i32(samppop), _f64(np.atleast_2d(tvals))
+        self._ck(self.lib.ima_gpu_treeweight(
+            self.h, ngen, *(_ptr(a) for a in ins), len(hval), _ptr(hval), _ptr(samppop), len(tvals),
+            _ptr(tvals), *(_ptr(out[k]) for k in ("cc", "hcc", "fc", "mc", "fm", "lens", "mignum"))))
+        return out
+
+    def tree_prob(self, group_off, pdg=None, group_tv=None, rows=False):
+        """p(G) per chain over the genealogies of the last treeweight call:
+        returns (probg, q [ngroups][nth], m [ngroups][nmg], rows or None)."""
+        pm = self._tw_pm
+        group_off = _i32(group_off)
+        G = len(group_off) - 1
+        nth, nmg = len(pm.th_cells), 0 if pm.nomig else len(pm.mg_cells)
+        probg, q, m = np.zeros(G), np.zeros((G, nth)), np.zeros((G, max(nmg, 1)))
+        rowbuf = np.zeros((G, 4 * nth + 3 * nmg + 2 + pm.npops - 1), np.float32) if rows else None
+        pdg = _f64(pdg) if pdg is not None else None
+        gtv = _i32(group_tv) if group_tv is not None else None
+        self._ck(self.lib.ima_gpu_tree_prob(self.h, G, _ptr(group_off), _ptr(pdg) if pdg is not None else None,
+                                            _ptr(gtv) if gtv is not None else None, _ptr(probg), _ptr(q),
+                                            _ptr(m), _ptr(rowbuf) if rows else None))
+        return probg, q, m[:, :nmg], rowbuf
+
     def fillvec(self, pmin, pmax, gridsize=1000, expo_mean=None):
         n = len(pmin)
         xs = np.zeros((n, gridsize))
@@ -540,3 +603,19 @@ class Batch:
         if self.handle is not None:
             self.ctx._ck(self.ctx.lib.ima_gpu_batch_destroy(self.ctx.h, self.handle))
             self.handle = None
+
+
+def pack_labelled(gens):
+    """CSR arrays of ima_gpu_treeweight from a list of LabelledGenealogy:
+    (node_off, up0, time, pop, mig_off, mig_t, mig_p)."""
+    node_off = np.zeros(len(gens) + 1, np.int32)
+    node_off[1:] = np.cumsum([len(g.pop) for g in gens])
+    up0 = np.concatenate([g.g.up0 for g in gens]).astype(np.int32)
+    time = np.concatenate([g.g.time for g in gens]).astype(np.float64)
+    pop = np.concatenate([g.pop for g in gens]).astype(np.int32)
+    counts = [len(m) for g in gens for m in g.mig]
+    mig_off = np.zeros(len(counts) + 1, np.int32)
+    mig_off[1:] = np.cumsum(counts)
+    mig_t = np.array([e[0] for g in gens for m in g.mig for e in m], np.float64)
+    mig_p = np.array([e[1] for g in gens for m in g.mig for e in m], np.int32)
+    return node_off, up0, time, pop, mig_off, mig_t, mig_p

@@ -18,6 +18,10 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libima2p_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# k_treeweight.cu restates the reference's FP64 sums term by term: without
+# FMA contraction its adds and multiplies round as the host's do
+NOFMAD_FILES = {"k_treeweight.cu"}
+NOFMAD = ["-fmad=false"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
 
 
@@ -47,7 +51,8 @@ def build_library(verbose: bool = False, force: bool = False) -> str:
         o = os.path.join(BUILD, os.path.basename(s)[:-3] + ".o")
         objs.append(o)
         if force or _stale(s, o, deps):
-            jobs.append([exe] + ARCH + FLAGS + ["-c", s, "-o", o])
+            extra = NOFMAD if os.path.basename(s) in NOFMAD_FILES else []
+            jobs.append([exe] + ARCH + FLAGS + extra + ["-c", s, "-o", o])
 
     def run(cmd):
         p = subprocess.run(cmd, capture_output=True, text=True)

@@ -224,6 +224,19 @@ struct ima_ctx {
   double *d_sx = nullptr, *d_sq = nullptr, *d_sess = nullptr;
   size_t spts_cap = 0;
 
+  // genealogy weights: the population model, the inputs and weights of the
+  // last ima_gpu_treeweight (kept for ima_gpu_tree_prob), logfact
+  TwModel h_tw{};
+  TwModel *d_tw = nullptr;
+  bool tw_ready = false;
+  double *d_logfact = nullptr;
+  int32_t *d_twerr = nullptr;
+  void *d_twin = nullptr, *d_twout = nullptr, *d_tpbuf = nullptr;
+  size_t twin_cap = 0, twout_cap = 0, tpbuf_cap = 0;
+  int tw_ngen = 0, tw_ntv = 0;
+  int32_t *tw_cc = nullptr, *tw_mc = nullptr;
+  double *tw_hcc = nullptr, *tw_fc = nullptr, *tw_fm = nullptr, *tw_tvals = nullptr;
+
   // batches
   std::vector<Batch> batches;
   Batch evb;  // buffers of ima_gpu_eval
@@ -383,7 +396,7 @@ extern "C" void ima_gpu_destroy(ima_ctx *c)
                   c->d_beta, c->d_allbetas, c->d_probg, c->d_S, c->d_swapcount, c->d_tempcount,
                   c->d_used, c->d_swap0ok, c->d_ctr, c->d_uni, c->d_rows, c->d_lognorm,
                   c->d_sscratch, c->d_sx, c->d_sq, c->d_sess, c->d_citems, c->d_cacc, c->d_flush,
-                  c->d_mscratch};
+                  c->d_mscratch, c->d_tw, c->d_logfact, c->d_twerr, c->d_twin, c->d_twout, c->d_tpbuf};
   for (void *p : devs)
     if (p) cudaFree(p);
   void *hosts[] = {c->h_nodes, c->h_t64, c->h_tff, c->h_sched, c->h_nlev, c->h_len, c->h_pi, c->h_al};
@@ -1826,4 +1839,374 @@ extern "C" int ima_gpu_memory(ima_ctx *c, size_t *bytes)
   if (!c || !bytes) return IMA_ERR_ARG;
   *bytes = c->dev_bytes;
   return IMA_OK;
+}
+
+// ======================================================================
+// genealogy weights and p(G) integrals
+namespace {
+int grow(ima_ctx *c, void **buf, size_t *cap, size_t bytes, const char *what)
+{
+  if (bytes <= *cap) return IMA_OK;
+  cudaStreamSynchronize(c->st);
+  cudaFree(*buf);
+  *buf = nullptr;
+  *cap = 0;
+  size_t n = bytes + bytes / 4;
+  *buf = dev_alloc<char>(n, c->dev_bytes, c->st);
+  if (!*buf) return c->fail(IMA_ERR_NOMEM, "%s (%zu bytes)", what, n);
+  *cap = n;
+  return IMA_OK;
+}
+
+struct Carve {
+  char *p;
+  template <typename T>
+  T *take(size_t count)
+  {
+    T *q = reinterpret_cast<T *>(p);
+    p += (count * sizeof(T) + 255) / 256 * 256;
+    return q;
+  }
+};
+
+size_t carve_size(std::initializer_list<size_t> bytes)
+{
+  size_t s = 0;
+  for (size_t b : bytes) s += (b + 255) / 256 * 256;
+  return s;
+}
+}  // namespace
+
+extern "C" int ima_gpu_set_popmodel(ima_ctx *c, int npops, int nomig, int expo, const int32_t *plist,
+                                    const int32_t *droppops, const int32_t *addpop, const int32_t *pop_e,
+                                    const int32_t *pop_down, int nth, const int32_t *th_off,
+                                    const int32_t *th_idx, const double *th_max, const double *th_min,
+                                    int nmg, const int32_t *mg_off, const int32_t *mg_idx, const double *mg_max,
+                                    const double *mg_min, const double *mg_mean, int nchk,
+                                    const int32_t *chk_idx)
+{
+  if (!c) return IMA_ERR_ARG;
+  if (npops < 2 || npops > TW_MAXPOPS) return c->fail(IMA_ERR_ARG, "npops must be in 2..%d", TW_MAXPOPS);
+  if (!plist || !droppops || !addpop || !pop_e || !pop_down || !th_off || !th_max || !th_min)
+    return c->fail(IMA_ERR_ARG, "population model: null table");
+  const int ntp = 2 * npops - 1, nsplit = npops - 1;
+  TwModel h;
+  memset(&h, 0, sizeof(h));
+  h.npops = npops;
+  h.nomig = nomig ? 1 : 0;
+  h.expo = expo ? 1 : 0;
+  h.T = npops * (npops + 1) / 2;
+  int mm = 0;
+  for (int k = 0; k <= npops; k++) {
+    h.toff[k] = (int16_t)(k * npops - k * (k - 1) / 2);
+    h.moff[k] = (int16_t)mm;
+    if (k < nsplit) mm += (npops - k) * (npops - k);
+  }
+  h.M = mm;
+  memset(h.plist, -1, sizeof(h.plist));
+  memset(h.pos, -1, sizeof(h.pos));
+  for (int k = 0; k < npops; k++)
+    for (int ii = 0; ii < npops - k; ii++) {
+      const int p = plist[k * npops + ii];
+      if (p < 0 || p >= ntp || (ii > 0 && p <= plist[k * npops + ii - 1]))
+        return c->fail(IMA_ERR_ARG, "plist[%d][%d] = %d: populations of a period must be distinct ids "
+                                    "below %d in increasing order", k, ii, p, ntp);
+      h.plist[k][ii] = (int8_t)p;
+      h.pos[k][p] = (int8_t)ii;
+    }
+  for (int k = 1; k < npops; k++) {
+    const int d0 = droppops[2 * k], d1 = droppops[2 * k + 1], ad = addpop[k];
+    if (d0 < 0 || d0 >= ntp || d1 < 0 || d1 >= ntp || ad < 0 || ad >= ntp || h.pos[k - 1][d0] < 0 ||
+        h.pos[k - 1][d1] < 0 || h.pos[k][ad] < 0 || h.pos[k - 1][ad] >= 0)
+      return c->fail(IMA_ERR_ARG, "split %d (%d, %d -> %d) does not match plist", k, d0, d1, ad);
+    h.droppops[k][0] = (int8_t)d0;
+    h.droppops[k][1] = (int8_t)d1;
+    h.addpop[k] = (int8_t)ad;
+  }
+  for (int p = 0; p < ntp; p++) {
+    if (pop_e[p] < -1 || pop_e[p] == 0 || pop_e[p] > nsplit || pop_down[p] < -1 || pop_down[p] >= ntp)
+      return c->fail(IMA_ERR_ARG, "pop_e/pop_down of population %d out of range", p);
+    h.pop_e[p] = (int8_t)pop_e[p];
+    h.pop_down[p] = (int8_t)pop_down[p];
+  }
+  if (nth < 1 || nth > TW_MAXTH || th_off[0] != 0 || th_off[nth] > TW_MAXT || (th_off[nth] > 0 && !th_idx))
+    return c->fail(IMA_ERR_ARG, "theta parameter map: nth %d", nth);
+  h.nth = nth;
+  for (int i = 0; i <= nth; i++) {
+    if (i > 0 && th_off[i] < th_off[i - 1]) return c->fail(IMA_ERR_ARG, "th_off must not decrease");
+    h.th_off[i] = (int16_t)th_off[i];
+  }
+  for (int j = 0; j < th_off[nth]; j++) {
+    if (th_idx[j] < 0 || th_idx[j] >= h.T) return c->fail(IMA_ERR_ARG, "th_idx[%d] out of range", j);
+    h.th_idx[j] = (int16_t)th_idx[j];
+  }
+  for (int i = 0; i < nth; i++) {
+    if (!(th_max[i] > th_min[i]) || th_min[i] < 0) return c->fail(IMA_ERR_ARG, "theta prior %d", i);
+    h.th_max[i] = th_max[i];
+    h.th_min[i] = th_min[i];
+  }
+  if (!nomig) {
+    if (nmg < 0 || nmg > TW_MAXMG || (nmg > 0 && (!mg_off || !mg_max || !mg_min))) return c->fail(IMA_ERR_ARG, "migration parameter map: nmg %d", nmg);
+    if (nmg > 0 && (mg_off[0] != 0 || mg_off[nmg] > TW_MAXM || (mg_off[nmg] > 0 && !mg_idx)))
+      return c->fail(IMA_ERR_ARG, "migration parameter map offsets");
+    h.nmg = nmg;
+    for (int i = 0; i <= nmg && nmg > 0; i++) {
+      if (i > 0 && mg_off[i] < mg_off[i - 1]) return c->fail(IMA_ERR_ARG, "mg_off must not decrease");
+      h.mg_off[i] = (int16_t)mg_off[i];
+    }
+    for (int j = 0; nmg > 0 && j < mg_off[nmg]; j++) {
+      if (mg_idx[j] < 0 || mg_idx[j] >= h.M) return c->fail(IMA_ERR_ARG, "mg_idx[%d] out of range", j);
+      h.mg_idx[j] = (int16_t)mg_idx[j];
+    }
+    for (int i = 0; i < nmg; i++) {
+      if (expo && (!mg_mean || !(mg_mean[i] > 0))) return c->fail(IMA_ERR_ARG, "migration prior mean %d", i);
+      if (!expo && (!(mg_max[i] > mg_min[i]) || mg_min[i] < 0)) return c->fail(IMA_ERR_ARG, "migration prior %d", i);
+      h.mg_max[i] = mg_max[i];
+      h.mg_min[i] = mg_min[i];
+      h.mg_mean[i] = mg_mean ? mg_mean[i] : 0.0;
+    }
+    if (nchk < 0 || nchk > TW_MAXM || (nchk > 0 && !chk_idx)) return c->fail(IMA_ERR_ARG, "nchk %d", nchk);
+    h.nchk = nchk;
+    for (int i = 0; i < nchk; i++) {
+      if (chk_idx[i] < 0 || chk_idx[i] >= h.M) return c->fail(IMA_ERR_ARG, "chk_idx[%d] out of range", i);
+      h.chk_idx[i] = (int16_t)chk_idx[i];
+    }
+  }
+  cudaSetDevice(c->device);
+  if (!c->d_tw) {
+    c->d_tw = dev_alloc<TwModel>(1, c->dev_bytes, c->st);
+    c->d_twerr = dev_alloc<int32_t>(2, c->dev_bytes, c->st);
+    c->d_logfact = dev_alloc<double>(TW_LF_N, c->dev_bytes, c->st);
+    if (!c->d_tw || !c->d_twerr || !c->d_logfact) return c->fail(IMA_ERR_NOMEM, "population model");
+    // logfact[i] = log(1) + ... + log(i) accumulated as setlogfact does
+    // (utilities.cpp:1406-1415), so the device table holds the host's values
+    std::vector<double> lf(TW_LF_N);
+    lf[0] = 0;
+    for (int i = 1; i < TW_LF_N; i++) lf[i] = lf[i - 1] + log((double)i);
+    int r = c->cuda(cudaMemcpyAsync(c->d_logfact, lf.data(), sizeof(double) * TW_LF_N, cudaMemcpyHostToDevice, c->st), "logfact");
+    r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "logfact");
+    if (r) return r;
+  }
+  c->h_tw = h;
+  int r = c->cuda(cudaMemcpyAsync(c->d_tw, &c->h_tw, sizeof(TwModel), cudaMemcpyHostToDevice, c->st), "population model");
+  r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "population model");
+  if (r) return r;
+  c->tw_ready = true;
+  c->tw_ngen = 0;
+  return IMA_OK;
+}
+
+static int tw_check_err(ima_ctx *c, const char *what)
+{
+  int32_t e[2] = {0, 0};
+  int r = c->cuda(cudaMemcpyAsync(e, c->d_twerr, sizeof(e), cudaMemcpyDeviceToHost, c->st), what);
+  r = r ? r : c->cuda(cudaStreamSynchronize(c->st), what);
+  if (r) return r;
+  static const char *why[] = {"", "a population that does not exist in that period (or a migration to the same "
+                                  "population)", "a lineage count below zero", "more events than planned",
+                              "an integral term the reference rejects (LogDiff order or iteration limit)",
+                              "a count beyond the logfact table"};
+  if (e[0]) return c->fail(IMA_ERR_DATA, "%s: item %d: %s", what, e[1], why[e[0] < 6 ? e[0] : 0]);
+  return IMA_OK;
+}
+
+extern "C" int ima_gpu_treeweight(ima_ctx *c, int ngen, const int32_t *node_off, const int32_t *up0,
+                                  const double *time, const int32_t *pop, const int32_t *mig_off,
+                                  const double *mig_t, const int32_t *mig_p, const int32_t *gen_locus,
+                                  const int32_t *gen_tv, int nloci, const double *hval, const int32_t *samppop,
+                                  int ntv, const double *tvals, int32_t *cc, double *hcc, double *fc,
+                                  int32_t *mc, double *fm, double *lens, int32_t *mignum)
+{
+  if (!c) return IMA_ERR_ARG;
+  if (!c->tw_ready) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_popmodel first");
+  if (ngen < 1 || !node_off || !up0 || !time || !pop || !mig_off || !gen_locus || !gen_tv || nloci < 1 ||
+      !hval || !samppop || ntv < 1 || !tvals)
+    return c->fail(IMA_ERR_ARG, "treeweight: bad argument");
+  const TwModel &h = c->h_tw;
+  const int npops = h.npops, nsplit = npops - 1;
+  if (node_off[0] != 0) return c->fail(IMA_ERR_ARG, "node_off[0] must be 0");
+  for (int li = 0; li < nloci; li++)
+    if (!(hval[li] > 0)) return c->fail(IMA_ERR_ARG, "hval[%d] must be > 0", li);
+  long long Emax = 0;
+  for (int g = 0; g < ngen; g++) {
+    const int a0 = node_off[g], nl = node_off[g + 1] - a0;
+    if (nl < 1 || !(nl & 1)) return c->fail(IMA_ERR_ARG, "genealogy %d: %d nodes (need 2n-1)", g, nl);
+    const int li = gen_locus[g], tv = gen_tv[g];
+    if (li < 0 || li >= nloci || tv < 0 || tv >= ntv) return c->fail(IMA_ERR_ARG, "genealogy %d: locus or tvals row", g);
+    int ns = 0;
+    for (int p = 0; p < npops; p++) ns += samppop[(size_t)li * npops + p];
+    if (ns != (nl + 1) / 2) return c->fail(IMA_ERR_ARG, "genealogy %d: %d genes, samppop of locus %d sums to %d", g, (nl + 1) / 2, li, ns);
+    const long long E = (nl - 1) / 2 + (long long)(mig_off[a0 + nl] - mig_off[a0]) + nsplit;
+    if (E > Emax) Emax = E;
+  }
+  const size_t N = (size_t)node_off[ngen];
+  if (mig_off[0] != 0) return c->fail(IMA_ERR_ARG, "mig_off[0] must be 0");
+  for (size_t i = 0; i < N; i++)
+    if (mig_off[i + 1] < mig_off[i]) return c->fail(IMA_ERR_ARG, "mig_off must not decrease (node %zu)", i);
+  const size_t Nm = (size_t)mig_off[N];
+  if (Nm > 0 && (!mig_t || !mig_p)) return c->fail(IMA_ERR_ARG, "migration events without mig_t/mig_p");
+  int P = 32;
+  while (P < Emax) P <<= 1;
+  if (P > (1 << 20) || tw_smem_per_warp(P, h) > 200 * 1024)
+    return c->fail(IMA_ERR_TOO_LARGE, "a genealogy has %lld events; at most %d fit", Emax,
+                   (int)((200 * 1024 - (h.T + h.M) * 12) / 12));
+  cudaSetDevice(c->device);
+  const size_t T = h.T, MM = h.M;
+  const size_t inb = carve_size({(ngen + 1) * 4ul, N * 4, N * 4, (N + 1) * 4, Nm * 4, ngen * 4ul, ngen * 4ul,
+                                 (size_t)nloci * npops * 4, N * 8, Nm * 8, (size_t)ntv * nsplit * 8,
+                                 (size_t)nloci * 8, (size_t)nloci * 8});
+  const size_t outb = carve_size({ngen * T * 4, ngen * MM * 4, ngen * 4ul, ngen * T * 8, ngen * T * 8,
+                                  ngen * MM * 8, 2 * ngen * 8ul});
+  int r = grow(c, &c->d_twin, &c->twin_cap, inb, "treeweight inputs");
+  r = r ? r : grow(c, &c->d_twout, &c->twout_cap, outb, "treeweight weights");
+  if (r) return r;
+  Carve ci{static_cast<char *>(c->d_twin)}, co{static_cast<char *>(c->d_twout)};
+  TwArgs a;
+  a.ngen = ngen;
+  a.P = P;
+  a.model = c->d_tw;
+  int32_t *d_node_off = ci.take<int32_t>(ngen + 1), *d_up0 = ci.take<int32_t>(N), *d_pop = ci.take<int32_t>(N),
+          *d_mig_off = ci.take<int32_t>(N + 1), *d_mig_p = ci.take<int32_t>(Nm),
+          *d_gl = ci.take<int32_t>(ngen), *d_gt = ci.take<int32_t>(ngen),
+          *d_sp = ci.take<int32_t>((size_t)nloci * npops);
+  double *d_time = ci.take<double>(N), *d_mig_t = ci.take<double>(Nm), *d_tv = ci.take<double>((size_t)ntv * nsplit),
+         *d_hlog = ci.take<double>(nloci), *d_h2 = ci.take<double>(nloci);
+  std::vector<double> hl(nloci), h2(nloci);
+  for (int li = 0; li < nloci; li++) {
+    hl[li] = log(hval[li]);           // treeweight: hlog = log (L[li].hval)
+    h2[li] = 1 / (2 * hval[li]);      // h2term = 1 / (2 * L[li].hval)
+  }
+  auto up = [&](void *dst, const void *src, size_t bytes) {
+    if (!r && bytes) r = c->cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->st), "treeweight inputs");
+  };
+  up(d_node_off, node_off, (ngen + 1) * 4ul);
+  up(d_up0, up0, N * 4);
+  up(d_pop, pop, N * 4);
+  up(d_mig_off, mig_off, (N + 1) * 4);
+  up(d_mig_p, mig_p, Nm * 4);
+  up(d_gl, gen_locus, ngen * 4ul);
+  up(d_gt, gen_tv, ngen * 4ul);
+  up(d_sp, samppop, (size_t)nloci * npops * 4);
+  up(d_time, time, N * 8);
+  up(d_mig_t, mig_t, Nm * 8);
+  up(d_tv, tvals, (size_t)ntv * nsplit * 8);
+  up(d_hlog, hl.data(), (size_t)nloci * 8);
+  up(d_h2, h2.data(), (size_t)nloci * 8);
+  if (r) return r;
+  a.node_off = d_node_off;
+  a.up0 = d_up0;
+  a.pop = d_pop;
+  a.mig_off = d_mig_off;
+  a.mig_p = d_mig_p;
+  a.gen_locus = d_gl;
+  a.gen_tv = d_gt;
+  a.samppop = d_sp;
+  a.time = d_time;
+  a.mig_t = d_mig_t;
+  a.tvals = d_tv;
+  a.hlog = d_hlog;
+  a.h2term = d_h2;
+  a.cc = co.take<int32_t>(ngen * T);
+  a.mc = co.take<int32_t>(ngen * MM);
+  a.mignum = co.take<int32_t>(ngen);
+  a.hcc = co.take<double>(ngen * T);
+  a.fc = co.take<double>(ngen * T);
+  a.fm = co.take<double>(ngen * MM);
+  a.lens = co.take<double>(2 * (size_t)ngen);
+  a.err = c->d_twerr;
+  r = c->cuda(cudaMemsetAsync(c->d_twerr, 0, 8, c->st), "treeweight");
+  if (r) return r;
+  c->tw_ngen = 0;
+  int lr = 0;
+  c->launch(IMA_K_TREEWEIGHT, (double)N * 20 + (double)Nm * 12 + (double)ngen * (T * 20 + MM * 12 + 20),
+            [&] { lr = launch_treeweight(a, h, c->st); });
+  if (lr) return c->fail(IMA_ERR_TOO_LARGE, "treeweight: shared memory for %d events", P);
+  r = c->cuda(cudaGetLastError(), "treeweight launch");
+  if (r) return r;
+  r = tw_check_err(c, "treeweight");
+  if (r) return r;
+  c->tw_ngen = ngen;
+  c->tw_ntv = ntv;
+  c->tw_cc = a.cc;
+  c->tw_mc = a.mc;
+  c->tw_hcc = a.hcc;
+  c->tw_fc = a.fc;
+  c->tw_fm = a.fm;
+  c->tw_tvals = d_tv;
+  auto down = [&](void *dst, const void *src, size_t bytes) {
+    if (!r && dst && bytes) r = c->cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->st), "treeweight outputs");
+  };
+  down(cc, a.cc, ngen * T * 4);
+  down(mc, a.mc, ngen * MM * 4);
+  down(mignum, a.mignum, ngen * 4ul);
+  down(hcc, a.hcc, ngen * T * 8);
+  down(fc, a.fc, ngen * T * 8);
+  down(fm, a.fm, ngen * MM * 8);
+  down(lens, a.lens, 2 * ngen * 8ul);
+  return r ? r : c->cuda(cudaStreamSynchronize(c->st), "treeweight");
+}
+
+extern "C" int ima_gpu_tree_prob(ima_ctx *c, int ngroups, const int32_t *group_off, const double *pdg,
+                                 const int32_t *group_tv, double *probg, double *q, double *m, float *rows)
+{
+  if (!c) return IMA_ERR_ARG;
+  if (!c->tw_ready || c->tw_ngen < 1) return c->fail(IMA_ERR_STATE, "call ima_gpu_treeweight first");
+  if (ngroups < 1 || !group_off) return c->fail(IMA_ERR_ARG, "tree_prob: bad argument");
+  const TwModel &h = c->h_tw;
+  for (int i = 0; i < ngroups; i++)
+    if (group_off[i] < 0 || group_off[i + 1] < group_off[i] || group_off[i + 1] > c->tw_ngen)
+      return c->fail(IMA_ERR_ARG, "group_off[%d..%d] outside the %d genealogies", i, i + 1, c->tw_ngen);
+  if (group_tv)
+    for (int i = 0; i < ngroups; i++)
+      if (group_tv[i] < 0 || group_tv[i] >= c->tw_ntv) return c->fail(IMA_ERR_ARG, "group_tv[%d] out of range", i);
+  const int nth = h.nth, nmg = h.nomig ? 0 : h.nmg;
+  const int rowlen = 4 * nth + 3 * nmg + 2 + h.npops - 1;  // cc fc hcc mc fm qi mi pdg probg t
+  cudaSetDevice(c->device);
+  const size_t G = ngroups;
+  const size_t b = carve_size({(G + 1) * 4, G * 4, G * 8, G * 8, G * nth * 8, G * (nmg ? nmg : 1) * 8,
+                               rows ? G * rowlen * 4 : 4});
+  int r = grow(c, &c->d_tpbuf, &c->tpbuf_cap, b, "tree_prob buffers");
+  if (r) return r;
+  Carve cv{static_cast<char *>(c->d_tpbuf)};
+  TwProbArgs a;
+  a.ngroups = ngroups;
+  a.model = c->d_tw;
+  int32_t *d_off = cv.take<int32_t>(G + 1), *d_tv = cv.take<int32_t>(G);
+  double *d_pdg = cv.take<double>(G);
+  a.group_off = d_off;
+  a.group_tv = d_tv;
+  a.pdg = pdg ? d_pdg : nullptr;
+  a.probg = cv.take<double>(G);
+  a.q = cv.take<double>(G * nth);
+  a.m = cv.take<double>(G * (nmg ? nmg : 1));
+  a.rows = rows ? cv.take<float>(G * rowlen) : nullptr;
+  a.rowlen = rowlen;
+  a.cc = c->tw_cc;
+  a.mc = c->tw_mc;
+  a.hcc = c->tw_hcc;
+  a.fc = c->tw_fc;
+  a.fm = c->tw_fm;
+  a.tvals = c->tw_tvals;
+  a.logfact = c->d_logfact;
+  a.err = c->d_twerr;
+  r = c->cuda(cudaMemcpyAsync(d_off, group_off, (G + 1) * 4, cudaMemcpyHostToDevice, c->st), "tree_prob groups");
+  if (group_tv)
+    r = r ? r : c->cuda(cudaMemcpyAsync(d_tv, group_tv, G * 4, cudaMemcpyHostToDevice, c->st), "tree_prob groups");
+  else
+    r = r ? r : c->cuda(cudaMemsetAsync(d_tv, 0, G * 4, c->st), "tree_prob groups");
+  if (pdg) r = r ? r : c->cuda(cudaMemcpyAsync(d_pdg, pdg, G * 8, cudaMemcpyHostToDevice, c->st), "tree_prob pdg");
+  r = r ? r : c->cuda(cudaMemsetAsync(c->d_twerr, 0, 8, c->st), "tree_prob");
+  if (r) return r;
+  c->launch(IMA_K_TREE_PROB, (double)c->tw_ngen * (h.T * 20 + h.M * 12), [&] { launch_tree_prob(a, c->st); });
+  r = c->cuda(cudaGetLastError(), "tree_prob launch");
+  r = r ? r : tw_check_err(c, "tree_prob");
+  if (r) return r;
+  auto down = [&](void *dst, const void *src, size_t bytes) {
+    if (!r && dst && bytes) r = c->cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->st), "tree_prob outputs");
+  };
+  down(probg, a.probg, G * 8);
+  down(q, a.q, G * nth * 8);
+  if (nmg) down(m, a.m, G * nmg * 8);
+  if (rows) down(rows, a.rows, G * rowlen * 4);
+  return r ? r : c->cuda(cudaStreamSynchronize(c->st), "tree_prob");
 }

@@ -141,3 +141,49 @@ struct MarginArgs {
 };
 int margin_chunks(int G, int n);
 int launch_margin(const MarginArgs &a, double *part, int nchunks, double *out, cudaStream_t st);
+
+// genealogy weights (treeweight) and p(G) integrals (initialize_integrate_tree_prob)
+#define TW_MAXPOPS 10                      // MAXPOPS, imamp.hpp:122
+#define TW_MAXTP (2 * TW_MAXPOPS - 1)
+#define TW_MAXT (TW_MAXPOPS * (TW_MAXPOPS + 1) / 2)
+#define TW_MAXM 384                        // sum_{k<9} (10-k)^2
+#define TW_MAXTH TW_MAXTP
+#define TW_MAXMG (2 * (TW_MAXPOPS - 1) * (TW_MAXPOPS - 1))
+#define TW_LF_N (1 << 17)                  // logfact entries on the device
+struct TwModel {                           // tables of fillplist and setup_iparams
+  int npops, nomig, expo, T, M, nth, nmg, nchk;
+  int8_t plist[TW_MAXPOPS][TW_MAXPOPS];    // period k: populations in id order
+  int8_t pos[TW_MAXPOPS][TW_MAXTP];        // position of population p in period k, -1 absent
+  int8_t droppops[TW_MAXPOPS][2], addpop[TW_MAXPOPS];
+  int8_t pop_e[TW_MAXTP], pop_down[TW_MAXTP];
+  int16_t toff[TW_MAXPOPS + 1], moff[TW_MAXPOPS + 1];
+  int16_t th_off[TW_MAXTH + 1], th_idx[TW_MAXT];
+  int16_t mg_off[TW_MAXMG + 1], mg_idx[TW_MAXM], chk_idx[TW_MAXM];
+  double th_max[TW_MAXTH], th_min[TW_MAXTH];
+  double mg_max[TW_MAXMG], mg_min[TW_MAXMG], mg_mean[TW_MAXMG];
+};
+struct TwArgs {
+  int ngen, P;                             // genealogies; sort size (power of 2 >= events)
+  const TwModel *model;
+  const int32_t *node_off, *up0, *pop, *mig_off, *mig_p, *gen_locus, *gen_tv;
+  const double *time, *mig_t, *tvals;      // tvals [rows][npops-1]
+  const double *hlog, *h2term;             // per locus, from the host's log
+  const int32_t *samppop;                  // [loci][npops]
+  int32_t *cc, *mc, *mignum;               // [ngen][T], [ngen][M], [ngen]
+  double *hcc, *fc, *fm, *lens;            // [ngen][T], [ngen][T], [ngen][M], [ngen][2]
+  int32_t *err;                            // {code, genealogy}: first failure
+};
+struct TwProbArgs {
+  int ngroups;
+  const TwModel *model;
+  const int32_t *group_off, *group_tv;     // genealogy ranges summed in order
+  const int32_t *cc, *mc;
+  const double *hcc, *fc, *fm, *tvals, *pdg, *logfact;
+  double *probg, *q, *m;                   // [ngroups], [ngroups][nth], [ngroups][nmg]
+  float *rows;                             // [ngroups][rowlen] or null
+  int rowlen;
+  int32_t *err;
+};
+size_t tw_smem_per_warp(int P, const TwModel &h);
+int launch_treeweight(const TwArgs &a, const TwModel &h, cudaStream_t st);
+int launch_tree_prob(const TwProbArgs &a, cudaStream_t st);

@@ -1,0 +1,664 @@
+// k_treeweight.cu -- genealogy weights and p(G) integrals on the device.
+//
+// k_treeweight restates treeweight (update_gtree_common.cpp:1680-1937): one
+// warp per genealogy.  The warp lays the genealogy's events out in shared
+// memory -- a coalescence per internal node at its daughters' time, every
+// migration with the population it leaves (the edge's population carried
+// through the splits, :1770-1790) and every split younger than the root --
+// sorts them by (time, position) with a bitonic network and sweeps them in
+// time order.  Lane l owns population l of the current period: its lineage
+// count, its fc accumulator (n(n-1) dt / 2h) and its fm accumulator (n dt;
+// the reference adds the same n dt to every partner cell, :1861-1867).  At a
+// split the lanes flush their period and take the counts of their new
+// population from the daughters' lanes by shuffle.  Every accumulator
+// receives the reference's terms in the reference's order, so with FMA
+// contraction off (this file is compiled with -fmad=false) the weights are
+// the reference's bit for bit.
+//
+// k_tree_prob restates sum_treeinfo (ginfo.cpp:209-244) over a chain's loci
+// in locus order, initialize_integrate_tree_prob (update_gtree_common.cpp:
+// 2089-2134) with the integral terms (:108-304, MORESTABLE) on the
+// reference's incomplete gamma functions (utilities.cpp:808-1130), and
+// optionally savegsampinf (ginfo.cpp:318-377): one warp per chain, a lane per
+// weight cell and then a lane per parameter.  The integrals use the device's
+// log/exp, so they agree with the host's to rounding, not bit for bit.
+#include "internal.h"
+
+#include <cfloat>
+
+namespace {
+
+constexpr int TW_WPB = 4;  // genealogies (warps) per block
+enum { EV_COAL = 0, EV_MIG = 1, EV_SPLIT = 2, EV_PAD = 3 };
+enum { TW_E_POP = 1, TW_E_COUNT = 2, TW_E_SIZE = 3, TW_E_TERM = 4, TW_E_LF = 5 };
+constexpr uint32_t POS_MASK = 0xFFFFFu;  // event position: 20 bits
+
+__device__ __forceinline__ uint32_t ev_pack(int type, int pop, int topop, int pos)
+{
+  return ((uint32_t)type << 30) | ((uint32_t)(topop & 31) << 25) | ((uint32_t)(pop & 31) << 20) |
+         ((uint32_t)pos & POS_MASK);
+}
+
+// findperiod (update_gtree_common.cpp:1626)
+__device__ __forceinline__ int tw_period(const double *tv, int nsplit, double t)
+{
+  int k = 0;
+  while (k < nsplit && tv[k] <= t) k++;
+  return k;
+}
+
+__device__ void tw_fail(int32_t *err, int code, int who)
+{
+  if (atomicCAS(&err[0], 0, code) == 0) atomicExch(&err[1], who);
+}
+
+__global__ void __launch_bounds__(32 * TW_WPB) k_treeweight(TwArgs a, int wpb, int warp_bytes)
+{
+  extern __shared__ __align__(16) unsigned char sm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = blockIdx.x * wpb + warp;
+  if (g >= a.ngen) return;  // whole warps only
+  const TwModel &M = *a.model;
+  const int npops = M.npops, nsplit = npops - 1, ntp = 2 * npops - 1, T = M.T, MM = M.M;
+  unsigned char *base = sm + (size_t)warp * warp_bytes;
+  double *ev_t = reinterpret_cast<double *>(base);
+  uint32_t *ev_c = reinterpret_cast<uint32_t *>(base + (size_t)a.P * 8);
+  double *fc_s = reinterpret_cast<double *>(base + (size_t)a.P * 12);
+  double *fm_s = fc_s + T;
+  int *cc_s = reinterpret_cast<int *>(fm_s + MM);
+  int *mc_s = cc_s + T;
+  for (int i = lane; i < T; i += 32) {
+    fc_s[i] = 0.0;
+    cc_s[i] = 0;
+  }
+  for (int i = lane; i < MM; i += 32) {
+    fm_s[i] = 0.0;
+    mc_s[i] = 0;
+  }
+
+  const int a0 = a.node_off[g], nl = a.node_off[g + 1] - a0, ng = (nl + 1) >> 1;
+  const double *tv = a.tvals + (size_t)a.gen_tv[g] * nsplit;
+  const int loc = a.gen_locus[g];
+  const int32_t *up0 = a.up0 + a0, *pp = a.pop + a0, *mo = a.mig_off + a0;
+  const double *tm = a.time + a0;
+  const int nmig = mo[nl] - mo[0];
+
+  // roottime: the root's coalescence, the latest one
+  int bad = 0;
+  double rt = 0.0;
+  for (int i = ng + lane; i < nl; i += 32) {
+    const int u = up0[i];
+    if ((unsigned)u >= (unsigned)nl) bad = TW_E_POP;
+    else rt = fmax(rt, tm[u]);
+  }
+  for (int d = 16; d; d >>= 1) rt = fmax(rt, __shfl_xor_sync(~0u, rt, d));
+  const int kroot = tw_period(tv, nsplit, rt);
+  const int E = (ng - 1) + nmig + kroot;
+  if (__any_sync(~0u, bad) || E > a.P) {
+    if (lane == 0) tw_fail(a.err, E > a.P ? TW_E_SIZE : TW_E_POP, g);
+    return;
+  }
+
+  // events: node i's coalescence first, then its migrations in edge order
+  int run = 0;
+  for (int b0 = 0; b0 < nl; b0 += 32) {
+    const int i = b0 + lane;
+    int cnt = 0, m0 = 0, m1 = 0;
+    if (i < nl) {
+      m0 = mo[i];
+      m1 = mo[i + 1];
+      cnt = (i >= ng) + (m1 - m0);
+    }
+    int inc = cnt;
+    for (int d = 1; d < 32; d <<= 1) {
+      const int v = __shfl_up_sync(~0u, inc, d);
+      if (lane >= d) inc += v;
+    }
+    int e = run + inc - cnt;
+    run += __shfl_sync(~0u, inc, 31);
+    if (i < nl) {
+      int nowpop = pp[i];
+      if ((unsigned)nowpop >= (unsigned)ntp || m1 < m0 || e + cnt > E) {
+        bad = TW_E_POP;
+      } else {
+        if (i >= ng) {
+          ev_t[e] = tm[up0[i]];
+          ev_c[e] = ev_pack(EV_COAL, nowpop, 0, e);
+          e++;
+        }
+        for (int j = m0; j < m1; j++) {
+          const double t = a.mig_t[j];
+          const int per = tw_period(tv, nsplit, t);
+          while (M.pop_e[nowpop] <= per && M.pop_e[nowpop] != -1) nowpop = M.pop_down[nowpop];
+          const int to = a.mig_p[j];
+          if ((unsigned)to >= (unsigned)ntp || to == nowpop) {
+            bad = TW_E_POP;
+            break;
+          }
+          ev_t[e] = t;
+          ev_c[e] = ev_pack(EV_MIG, nowpop, to, e);
+          e++;
+          nowpop = to;
+        }
+      }
+    }
+  }
+  if (lane < kroot) {
+    ev_t[run + lane] = tv[lane];
+    ev_c[run + lane] = ev_pack(EV_SPLIT, 0, 0, run + lane);
+  }
+  int Pg = 1;
+  while (Pg < E) Pg <<= 1;
+  for (int i = E + lane; i < Pg; i += 32) {
+    ev_t[i] = __longlong_as_double(0x7ff0000000000000LL);  // +inf: after every event
+    ev_c[i] = ev_pack(EV_PAD, 0, 0, i);
+  }
+  if (__any_sync(~0u, bad)) {
+    if (lane == 0) tw_fail(a.err, TW_E_POP, g);
+    return;
+  }
+  __syncwarp();
+
+  // bitonic sort on (time, position): the positions are distinct, so the
+  // order is total and ties in time keep the order the events were listed in
+  for (int size = 2; size <= Pg; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = lane; i < (Pg >> 1); i += 32) {
+        const int lo = ((i & ~(stride - 1)) << 1) | (i & (stride - 1));
+        const int hi = lo + stride;
+        const double tl = ev_t[lo], th = ev_t[hi];
+        const uint32_t cl = ev_c[lo], ch = ev_c[hi];
+        const bool gt = tl > th || (tl == th && (cl & POS_MASK) > (ch & POS_MASK));
+        if (gt == ((lo & size) == 0)) {
+          ev_t[lo] = th;
+          ev_t[hi] = tl;
+          ev_c[lo] = ch;
+          ev_c[hi] = cl;
+        }
+      }
+      __syncwarp();
+    }
+  }
+
+  // the sweep (update_gtree_common.cpp:1827-1927)
+  const double h2 = a.h2term[loc], hl = a.hlog[loc];
+  const double lastsplitt = tv[nsplit - 1];
+  int k = 0, nsum = ng, nmine = lane < npops ? a.samppop[(size_t)loc * npops + lane] : 0, ccm = 0;
+  double accfc = 0.0, accfm = 0.0, last = 0.0, len = 0.0, tlen = 0.0;
+  auto flush = [&](int kk) {
+    const int w = npops - kk;
+    if (lane < w) {
+      fc_s[M.toff[kk] + lane] = accfc;
+      cc_s[M.toff[kk] + lane] = ccm;
+      if (!M.nomig && kk < nsplit)
+        for (int jj = 0; jj < w; jj++)
+          if (jj != lane) fm_s[M.moff[kk] + lane * w + jj] = accfm;
+    }
+  };
+  for (int j = 0; j < E; j++) {
+    const double t = ev_t[j];
+    const uint32_t c = ev_c[j];
+    const double dt = t - last;
+    const double tadd = nsum * dt;
+    len += tadd;
+    if (t < lastsplitt)
+      tlen += tadd;
+    else if (last < lastsplitt)
+      tlen += nsum * (lastsplitt - last);
+    last = t;
+    const int w = npops - k;
+    if (lane < w) {
+      const double dn = (double)nmine;
+      accfc += dn * (dn - 1) * dt * h2;
+      if (!M.nomig && k < nsplit) accfm += nmine * dt;
+    }
+    const int type = (int)(c >> 30);
+    int lbad = 0;
+    if (type == EV_COAL) {
+      const int o = M.pos[k][(c >> 20) & 31];
+      if (o < 0) {
+        bad = TW_E_POP;
+      } else if (lane == o) {
+        lbad = nmine < 2;
+        nmine--;
+        ccm++;
+      }
+      nsum--;
+    } else if (type == EV_MIG) {
+      const int op = M.pos[k][(c >> 20) & 31], oq = M.pos[k][(c >> 25) & 31];
+      if (op < 0 || oq < 0 || k >= nsplit) {
+        bad = TW_E_POP;
+      } else {
+        if (lane == op) {
+          lbad = nmine < 1;
+          nmine--;
+          mc_s[M.moff[k] + op * w + oq]++;
+        }
+        if (lane == oq) nmine++;
+      }
+    } else {  // a split: the period ends
+      if (k >= nsplit || nsum < 2) {
+        bad = TW_E_COUNT;
+      } else {
+        flush(k);
+        const int k1 = k + 1;
+        int s0 = 0, s1 = -1;
+        if (lane < npops - k1) {
+          const int np1 = M.plist[k1][lane];
+          if (np1 == M.addpop[k1]) {
+            s0 = M.pos[k][M.droppops[k1][0]];
+            s1 = M.pos[k][M.droppops[k1][1]];
+          } else {
+            s0 = M.pos[k][np1];
+          }
+        }
+        const int v0 = __shfl_sync(~0u, nmine, s0 < 0 ? 0 : s0);
+        const int v1 = __shfl_sync(~0u, nmine, s1 < 0 ? 0 : s1);
+        nmine = lane < npops - k1 ? v0 + (s1 >= 0 ? v1 : 0) : 0;
+        k = k1;
+        accfc = accfm = 0.0;
+        ccm = 0;
+      }
+    }
+    if (__any_sync(~0u, lbad)) bad = TW_E_COUNT;
+    if (bad) break;
+  }
+  if (!bad && nsum != 1) bad = TW_E_COUNT;
+  if (bad) {
+    if (lane == 0) tw_fail(a.err, bad, g);
+    return;
+  }
+  flush(k);
+  __syncwarp();
+  const size_t oT = (size_t)g * T, oM = (size_t)g * MM;
+  for (int i = lane; i < T; i += 32) {
+    a.cc[oT + i] = cc_s[i];
+    a.fc[oT + i] = fc_s[i];
+    a.hcc[oT + i] = hl != 0.0 ? 0.0 + hl * cc_s[i] : 0.0;
+  }
+  for (int i = lane; i < MM; i += 32) {
+    a.mc[oM + i] = mc_s[i];
+    a.fm[oM + i] = fm_s[i];
+  }
+  if (lane == 0) {
+    a.lens[2 * (size_t)g] = len;
+    a.lens[2 * (size_t)g + 1] = tlen;
+    a.mignum[g] = nmig;
+  }
+}
+
+// ---------------------------------------------------------------- p(G)
+// The reference's incomplete gamma functions, restated from the published
+// Numerical Recipes methods it uses (series, Lentz continued fraction, E1
+// series / continued fraction) with its constants: EPS 3e-7, ITMAX 1000,
+// FPMIN 1e-30, expint's MAXIT 100 and Euler constant 0.5772156649.
+constexpr double IG_EPS = 3.0e-7, IG_FPMIN = 1.0e-30, EI_EULER = 0.5772156649;
+constexpr int IG_ITMAX = 1000, EI_MAXIT = 100;
+constexpr double LD_CUT = 7.0978271289338397e+02, MPRIORMIN = 0.000001;
+constexpr double LOG2 = 0.69314718055994530941723212146;
+
+struct Ig {
+  const double *lft;
+  int st;
+  __device__ double lf(int i)
+  {
+    if (i < 0 || i >= TW_LF_N) {
+      st = TW_E_LF;
+      return 0.0;
+    }
+    return lft[i];
+  }
+  __device__ double gser(int a, double x, double *gln, bool lg)
+  {
+    *gln = lf(a - 1);
+    if (x <= 0.0) {
+      if (x < 0.0) st = TW_E_TERM;
+      return 0.0;
+    }
+    double ap = a, del = 1.0 / a, sum = del;
+    for (int n = 1; n <= IG_ITMAX; n++) {
+      ++ap;
+      del *= x / ap;
+      sum += del;
+      if (fabs(del) < fabs(sum) * IG_EPS)
+        return lg ? log(sum) + (-x + a * log(x) - (*gln)) : sum * exp(-x + a * log(x) - (*gln));
+    }
+    st = TW_E_TERM;
+    return 0.0;
+  }
+  __device__ double gcf(double a, double x, double *gln, bool lg)
+  {
+    *gln = lf((int)a - 1);
+    double b = x + 1.0 - a, c = 1.0 / IG_FPMIN, d = 1.0 / b, h = d;
+    int i;
+    for (i = 1; i <= IG_ITMAX; i++) {
+      const double an = -i * (i - a);
+      b += 2.0;
+      d = an * d + b;
+      if (fabs(d) < IG_FPMIN) d = IG_FPMIN;
+      c = b + an / c;
+      if (fabs(c) < IG_FPMIN) c = IG_FPMIN;
+      d = 1.0 / d;
+      const double del = d * c;
+      h *= del;
+      if (fabs(del - 1.0) < IG_EPS) break;
+    }
+    if (i > IG_ITMAX) st = TW_E_TERM;
+    return lg ? (-x + a * log(x) - (*gln)) + log(h) : exp(-x + a * log(x) - (*gln)) * h;
+  }
+  __device__ double expint1(double x, bool *islog)
+  {
+    *islog = false;
+    if (x <= 0.0) {
+      st = TW_E_TERM;
+      return 0.0;
+    }
+    if (x > 1.0) {
+      double b = x + 1, c = 1.0 / IG_FPMIN, d = 1.0 / b, h = d;
+      for (int i = 1; i <= EI_MAXIT; i++) {
+        const double an = -i * i;
+        b += 2.0;
+        d = 1.0 / (an * d + b);
+        c = b + an / c;
+        const double del = c * d;
+        h *= del;
+        if (fabs(del - 1.0) < IG_EPS) {
+          *islog = true;
+          return log(h) - x;
+        }
+      }
+      st = TW_E_TERM;
+      return 0.0;
+    }
+    double ans = -log(x) - EI_EULER, fact = 1.0;
+    for (int i = 1; i <= EI_MAXIT; i++) {
+      fact *= -x / i;
+      const double del = -fact / i;
+      ans += del;
+      if (fabs(del) < fabs(ans) * IG_EPS) return ans;
+    }
+    st = TW_E_TERM;
+    return ans;
+  }
+  __device__ double upper(int a, double x)  // uppergamma: log Gamma(a, x)
+  {
+    double p, gln;
+    if (x < 0.0 || a < 0) {
+      st = TW_E_TERM;
+      return 0.0;
+    }
+    if (a == 0) {
+      bool islog;
+      const double t = expint1(x, &islog);
+      p = islog ? t : log(t);
+    } else if (x < (a + 1.0)) {
+      const double gs = gser(a, x, &gln, false);
+      p = gln + log(1.0 - gs);
+    } else {
+      p = gln_plus_gcf(a, x, true);
+    }
+    return p < -1e200 ? -1e200 : p;
+  }
+  __device__ double gln_plus_gcf(int a, double x, bool lg)
+  {
+    double gln;
+    const double v = gcf((double)a, x, &gln, lg);
+    return lg ? gln + v : gln + log(1 - v);
+  }
+  __device__ double lower(int a, double x)  // lowergamma: log gamma(a, x)
+  {
+    double p, gln;
+    if (x < 0.0 || a <= 0) {
+      st = TW_E_TERM;
+      return 0.0;
+    }
+    if (x < (a + 1.0)) {
+      const double gs = gser(a, x, &gln, true);
+      p = gln + gs;
+    } else {
+      p = gln_plus_gcf(a, x, false);
+    }
+    return p < -1e200 ? -1e200 : p;
+  }
+  __device__ double logdiff(double a, double b)  // LogDiff, imamp.hpp:257-262
+  {
+    if (a <= b) {
+      st = TW_E_TERM;
+      return 0.0;
+    }
+    return (a - b < LD_CUT) ? b + log(exp(a - b) - 1.0) : a;
+  }
+  __device__ double coal(int cc, double fc, double hcc, double max, double min)
+  {
+    double p;
+    if (cc > 0) {
+      if (!(fc > 0)) {
+        st = TW_E_TERM;
+        return 0.0;
+      }
+      if (min == 0) {
+        double ug = upper(cc - 1, 2 * fc / max);
+        if (cc > 1) {
+          const double fullg = lf(cc - 2);
+          if (fullg - ug < 1e-15 || fullg - ug > LD_CUT) {
+            const double lg = lower(cc - 1, 2 * fc / max);
+            if (fullg > lg) {
+              const double ugalt = logdiff(fullg, lg);
+              if (fabs(ugalt - ug) > 1e-10) ug = ugalt;
+            }
+          }
+        }
+        p = ug + LOG2 - hcc + (1 - cc) * log(fc);
+      } else {
+        const double aa = upper(cc - 1, 2 * fc / max), bb = upper(cc - 1, 2 * fc / min);
+        p = logdiff(aa, bb);
+        p += (LOG2 - hcc + (1 - cc) * log(fc));
+      }
+    } else if (2 * fc / max > 0) {
+      if (min == 0) {
+        const double aa = log(max) - 2.0 * fc / max;
+        const double bb = LOG2 + log(fc) + upper(0, 2.0 * fc / max);
+        p = logdiff(aa, bb);
+      } else {
+        double aa = upper(0, 2 * fc / max), bb = upper(0, 2 * fc / min);
+        double c = logdiff(aa, bb);
+        c += LOG2 + log(fc);
+        aa = log(max) - 2.0 * fc / max;
+        bb = log(min) - 2.0 * fc / min;
+        const double d = logdiff(aa, bb);
+        p = logdiff(d, c);
+      }
+    } else {
+      p = log(max - min);
+    }
+    return p;
+  }
+  __device__ double mig(int cm, double fm, double max, double min)
+  {
+    double p;
+    if (cm > 0) {
+      if (!(fm > 0)) {
+        st = TW_E_TERM;
+        return 0.0;
+      }
+      if (min == 0) {
+        double lg = lower(cm + 1, fm * max);
+        const double fullg = lf(cm);
+        if (fullg - lg < 1e-15 || fullg - lg > LD_CUT) {
+          const double ug = upper(cm + 1, fm * max);
+          if (fullg > ug) {
+            const double lgalt = logdiff(fullg, ug);
+            if (fabs(lgalt - lg) > 1e-12) lg = lgalt;
+          }
+        }
+        p = (-1 - cm) * log(fm) + lg;
+      } else {
+        const double aa = upper(cm + 1, fm * min), bb = upper(cm + 1, fm * max);
+        p = (-1 - cm) * log(fm) + logdiff(aa, bb);
+      }
+    } else if (fm > MPRIORMIN) {
+      if (min == 0) {
+        p = (max == MPRIORMIN) ? 0 : logdiff(0.0, -fm * max) - log(fm);
+      } else {
+        p = logdiff(-fm * min, -fm * max) - log(fm);
+      }
+    } else {
+      p = log(max - min);
+    }
+    return p;
+  }
+  __device__ double mig_expo(int cm, double fm, double mean)
+  {
+    return -log(mean) + (-(cm + 1) * log(fm + 1.0 / mean)) + lf(cm);
+  }
+};
+
+constexpr int TP_WPB = 4;
+
+__global__ void __launch_bounds__(32 * TP_WPB) k_tree_prob(TwProbArgs a)
+{
+  __shared__ int s_cc[TP_WPB][TW_MAXT], s_mc[TP_WPB][TW_MAXM];
+  __shared__ double s_fc[TP_WPB][TW_MAXT], s_hcc[TP_WPB][TW_MAXT], s_fm[TP_WPB][TW_MAXM];
+  __shared__ double s_q[TP_WPB][TW_MAXTH], s_m[TP_WPB][TW_MAXMG];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int grp = blockIdx.x * TP_WPB + warp;
+  if (grp >= a.ngroups) return;
+  const TwModel &M = *a.model;
+  const int T = M.T, MM = M.M, nth = M.nth, nmg = M.nomig ? 0 : M.nmg;
+  const int g0 = a.group_off[grp], g1 = a.group_off[grp + 1];
+  // sum_treeinfo over the chain's genealogies, in order, from zero
+  for (int i = lane; i < T; i += 32) {
+    int c = 0;
+    double f = 0.0, h = 0.0;
+    for (int g = g0; g < g1; g++) {
+      c += a.cc[(size_t)g * T + i];
+      f += a.fc[(size_t)g * T + i];
+      h += a.hcc[(size_t)g * T + i];
+    }
+    s_cc[warp][i] = c;
+    s_fc[warp][i] = f;
+    s_hcc[warp][i] = h;
+  }
+  if (!M.nomig)
+    for (int i = lane; i < MM; i += 32) {
+      int c = 0;
+      double f = 0.0;
+      for (int g = g0; g < g1; g++) {
+        c += a.mc[(size_t)g * MM + i];
+        f += a.fm[(size_t)g * MM + i];
+      }
+      s_mc[warp][i] = c;
+      s_fm[warp][i] = f;
+    }
+  __syncwarp();
+  Ig ig{a.logfact, 0};
+  for (int i = lane; i < nth; i += 32) {
+    int c = 0;
+    double f = 0.0, hc = 0.0;
+    for (int j = M.th_off[i]; j < M.th_off[i + 1]; j++) {
+      c += s_cc[warp][M.th_idx[j]];
+      f += s_fc[warp][M.th_idx[j]];
+      hc += s_hcc[warp][M.th_idx[j]];
+    }
+    s_q[warp][i] = ig.coal(c, f, hc, M.th_max[i], M.th_min[i]);
+  }
+  for (int i = lane; i < nmg; i += 32) {
+    int c = 0;
+    double f = 0.0;
+    for (int j = M.mg_off[i]; j < M.mg_off[i + 1]; j++) {
+      c += s_mc[warp][M.mg_idx[j]];
+      f += s_fm[warp][M.mg_idx[j]];
+    }
+    s_m[warp][i] = M.expo ? ig.mig_expo(c, f, M.mg_mean[i]) : ig.mig(c, f, M.mg_max[i], M.mg_min[i]);
+  }
+  if (__any_sync(~0u, ig.st != 0)) {
+    const int code = __reduce_max_sync(~0u, ig.st);
+    if (lane == 0) tw_fail(a.err, code, grp);
+    return;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    bool checkm = true;
+    if (!M.nomig)
+      for (int i = 0; i < M.nchk && checkm; i++) checkm = s_mc[warp][M.chk_idx[i]] == 0;
+    double psum = 0;
+    if (!checkm) {
+      psum = -DBL_MAX;  // the reference's rejection value (MYDBL_MAX)
+    } else {
+      for (int i = 0; i < nth; i++) psum += s_q[warp][i];
+      for (int i = 0; i < nmg; i++) psum += s_m[warp][i];
+    }
+    a.probg[grp] = psum;
+  }
+  for (int i = lane; i < nth; i += 32) a.q[(size_t)grp * nth + i] = s_q[warp][i];
+  for (int i = lane; i < nmg; i += 32) a.m[(size_t)grp * nmg + i] = s_m[warp][i];
+  if (a.rows) {  // savegsampinf: float sums in parameter order
+    float *row = a.rows + (size_t)grp * a.rowlen;
+    const int ccp = 0, fcp = nth, hccp = 2 * nth, mcp = 3 * nth, fmp = mcp + nmg, qip = fmp + nmg,
+              mip = qip + nth, pdgp = mip + nmg, probgp = pdgp + 1, tp = probgp + 1;
+    for (int i = lane; i < nth; i += 32) {
+      int c = 0;
+      float f = 0.0f, hc = 0.0f;
+      for (int j = M.th_off[i]; j < M.th_off[i + 1]; j++) {
+        c += s_cc[warp][M.th_idx[j]];
+        f += (float)s_fc[warp][M.th_idx[j]];
+        hc += (float)s_hcc[warp][M.th_idx[j]];
+      }
+      row[ccp + i] = (float)c;
+      row[fcp + i] = f;
+      row[hccp + i] = hc;
+      row[qip + i] = (float)s_q[warp][i];
+    }
+    for (int i = lane; i < nmg; i += 32) {
+      int c = 0;
+      float f = 0.0f;
+      for (int j = M.mg_off[i]; j < M.mg_off[i + 1]; j++) {
+        c += s_mc[warp][M.mg_idx[j]];
+        f += (float)s_fm[warp][M.mg_idx[j]];
+      }
+      row[mcp + i] = (float)c;
+      row[fmp + i] = f;
+      row[mip + i] = (float)s_m[warp][i];
+    }
+    __syncwarp();
+    if (lane == 0) {
+      row[pdgp] = a.pdg ? (float)a.pdg[grp] : 0.0f;
+      row[probgp] = (float)a.probg[grp];
+    }
+    const double *tv = a.tvals + (size_t)a.group_tv[grp] * (M.npops - 1);
+    for (int i = lane; i < M.npops - 1; i += 32) row[tp + i] = (float)tv[i];
+  }
+}
+
+}  // namespace
+
+size_t tw_smem_per_warp(int P, const TwModel &h)
+{
+  const size_t b = (size_t)P * 12 + (size_t)(h.T + h.M) * 12;
+  return (b + 15) / 16 * 16;
+}
+
+int launch_treeweight(const TwArgs &a, const TwModel &h, cudaStream_t st)
+{
+  if (a.ngen < 1) return 0;
+  const size_t per = tw_smem_per_warp(a.P, h);
+  const size_t cap = 200 * 1024;
+  if (per > cap) return 1;
+  int wpb = (int)(cap / per);
+  wpb = wpb < 1 ? 1 : (wpb > TW_WPB ? TW_WPB : wpb);
+  const size_t smem = per * wpb;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_treeweight, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return 2;
+  }
+  const int grid = (a.ngen + wpb - 1) / wpb;
+  k_treeweight<<<grid, 32 * wpb, smem, st>>>(a, wpb, (int)per);
+  return 0;
+}
+
+int launch_tree_prob(const TwProbArgs &a, cudaStream_t st)
+{
+  if (a.ngroups < 1) return 0;
+  k_tree_prob<<<(a.ngroups + TP_WPB - 1) / TP_WPB, 32 * TP_WPB, 0, st>>>(a);
+  return 0;
+}

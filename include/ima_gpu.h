@@ -245,6 +245,63 @@ int ima_gpu_fillvec(ima_ctx *ctx, int gridsize, const double *pmin, const double
 /* The loaded surface's shape (any pointer may be NULL). */
 int ima_gpu_surface_info(ima_ctx *ctx, int *G, int *numpopsizeparams, int *nummigrateparams, int *npops);
 
+/* ------------------------------- genealogy weights and p(G) integrals
+ * The population model: the tables fillplist leaves in the reference's
+ * chain (build_poptree.cpp:391-450) and the parameter maps of setup_iparams
+ * (initialize.cpp:202-727).  npops in 2..10 sampled populations;
+ * numtreepops = 2npops-1; numsplittimes = npops-1.
+ *   plist[k*npops + ii]   population ii of period k (ids ascending; npops-k used)
+ *   droppops[2k + {0,1}], addpop[k]   the k-th split (k = 1..npops-1; row 0 unused)
+ *   pop_e[p], pop_down[p]   the period at which population p ends (-1 root), its ancestor
+ * Weight cells, for every genealogy and chain: T = npops(npops+1)/2
+ * coalescent cells (cc/hcc/fc of period k, position ii at
+ * k*npops - k(k-1)/2 + ii) and M = sum_{k<npops-1} (npops-k)^2 migration
+ * cells (mc/fm of period k, positions (ii, jj) at moff(k) + ii(npops-k) + jj,
+ * moff(k) = sum_{j<k} (npops-j)^2).  Theta parameter i sums the T cells
+ * th_idx[th_off[i] .. th_off[i+1]) in that order (itheta[i].wp); migration
+ * parameter i the M cells mg_idx[...] (imig[i].wp); their priors are
+ * th_max/th_min (itheta[i].pr) and mg_max/mg_min/mg_mean (imig[i].pr).
+ * chk_idx: M cells that must hold no migration (nomigrationchecklist).
+ * nomig, expo: modeloptions[NOMIGRATION], modeloptions[EXPOMIGRATIONPRIOR]. */
+int ima_gpu_set_popmodel(ima_ctx *ctx, int npops, int nomig, int expo, const int32_t *plist,
+                         const int32_t *droppops, const int32_t *addpop, const int32_t *pop_e,
+                         const int32_t *pop_down, int nth, const int32_t *th_off, const int32_t *th_idx,
+                         const double *th_max, const double *th_min, int nmg, const int32_t *mg_off,
+                         const int32_t *mg_idx, const double *mg_max, const double *mg_min,
+                         const double *mg_mean, int nchk, const int32_t *chk_idx);
+/* treeweight (update_gtree_common.cpp:1680-1937) for ngen genealogies at
+ * once, each from zero weights (the reference zeroes G->gweight first).
+ * Genealogy g holds nodes node_off[g] .. node_off[g+1] (2n-1 of them, local
+ * ids as in struct edge); per node: up0, time (as everywhere in this ABI) and
+ * pop = gtree[i].pop; its migration events, oldest last, are mig_t/mig_p
+ * [mig_off[node] .. mig_off[node+1]) over the global node index
+ * (gtree[i].mig[].mt/.mp).  gen_locus[g] picks the locus row of hval
+ * (L[li].hval) and samppop[npops] (L[li].samppop); gen_tv[g] the row of
+ * tvals[ntv][npops-1] (C[ci]->tvals).  Outputs (each may be NULL):
+ * cc/hcc/fc [ngen][T], mc/fm [ngen][M], lens [ngen][2] = {G->length,
+ * G->tlength}, mignum [ngen] = G->mignum.  The weights stay on the device
+ * for ima_gpu_tree_prob.  IMA_ERR_DATA: a genealogy the model cannot hold
+ * (the reference asserts): a population outside its period, a count below
+ * zero.  Weights equal the reference's bit for bit. */
+int ima_gpu_treeweight(ima_ctx *ctx, int ngen, const int32_t *node_off, const int32_t *up0,
+                       const double *time, const int32_t *pop, const int32_t *mig_off,
+                       const double *mig_t, const int32_t *mig_p, const int32_t *gen_locus,
+                       const int32_t *gen_tv, int nloci, const double *hval, const int32_t *samppop,
+                       int ntv, const double *tvals, int32_t *cc, double *hcc, double *fc, int32_t *mc,
+                       double *fm, double *lens, int32_t *mignum);
+/* sum_treeinfo (ginfo.cpp:209-244) of each chain's genealogies from the
+ * last ima_gpu_treeweight (group i = genealogies group_off[i] ..
+ * group_off[i+1], summed in that order, i.e. locus order) followed by
+ * initialize_integrate_tree_prob (update_gtree_common.cpp:2089-2134):
+ * probg[ngroups] (C[ci]->allpcalc.probg), q [ngroups][nth] (qintegrate),
+ * m [ngroups][nmg] (mintegrate).  rows (may be NULL): the gsampinf row
+ * savegsampinf (ginfo.cpp:318-377) writes, [ngroups][4nth + 3nmg + 2 +
+ * npops-1] floats, with pdg[i] (may be NULL: 0) and the split times of
+ * tvals row group_tv[i] (may be NULL: row 0).  IMA_ERR_DATA where the
+ * reference stops in an integral term (LogDiff order, iteration limit). */
+int ima_gpu_tree_prob(ima_ctx *ctx, int ngroups, const int32_t *group_off, const double *pdg,
+                      const int32_t *group_tv, double *probg, double *q, double *m, float *rows);
+
 /* ------------------------------------------ saved genealogies (.ti files)
  * Host functions, no context.  ima_ti_read parses the reference's text
  * format (loadgenealogyvalues, ima_main_mpi.cpp:3216-3440): header lines up
@@ -336,7 +393,9 @@ int ima_gpu_kernel_stats(ima_ctx *ctx, int kind, long long *launches, double *ms
 #define IMA_K_SURF_COMPAT 9
 #define IMA_K_SURF_TC 10
 #define IMA_K_MARGIN 11
-#define IMA_K_COUNT 12
+#define IMA_K_TREEWEIGHT 12
+#define IMA_K_TREE_PROB 13
+#define IMA_K_COUNT 14
 /* Total kernel launches issued by this library on the context. */
 int ima_gpu_launch_count(ima_ctx *ctx, long long *n);
 /* Write a device buffer larger than L2 (evicts resident data). */
