@@ -34,6 +34,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "chain-locus likelihood evals/s"
 SURF_METRIC = "L-mode grid points/s"
+TW_METRIC = "genealogy weights (treeweight) per second"
 
 
 def measured_peaks():
@@ -557,13 +558,135 @@ def run_surface(args):
     ctx.close()
 
 
+def tw_workload(nloci=300, nchains=128, nbase=60, seed=1011):
+    """Config-4-shaped genealogy-weight workload: 3 populations
+    ((0,1):3,2):4, per-population samples U(4,60), IM genealogies with their
+    population labels and migrations (theta 2-6, m 0.3); nbase distinct loci
+    cycled over nloci, the same genealogies in every chain (one split-time
+    row).  Returns (popmodel, packed inputs, gen_locus, gen_tv, hval,
+    samppop, tvals, labelled base genealogies, base index per genealogy)."""
+    from ima2p_gb300 import api, popmodel, synth
+    rng = np.random.default_rng(seed)
+    pm = popmodel.build("((0,1):3,2):4", 3)
+    tv = np.array([[0.6, 1.4]])
+    base, samp = [], []
+    for b in range(nbase):
+        s = [int(v) for v in rng.integers(4, 61, 3)]
+        theta = list(rng.uniform(2.0, 6.0, 5))
+        base.append(synth.sim_im_labeled(rng, s, theta, 0.3, [(0.6, 0, 1, 3), (1.4, 3, 2, 4)]))
+        samp.append(s)
+    bp = [api.pack_labelled([g]) for g in base]
+    seq = np.tile(np.arange(nloci) % nbase, nchains)
+    nn = np.array([len(bp[b][1]) for b in range(nbase)])
+    nm = np.array([int(bp[b][4][-1]) for b in range(nbase)])
+    node_off = np.zeros(len(seq) + 1, np.int32)
+    node_off[1:] = np.cumsum(nn[seq])
+    up0 = np.concatenate([bp[b][1] for b in seq])
+    time_ = np.concatenate([bp[b][2] for b in seq])
+    pop = np.concatenate([bp[b][3] for b in seq])
+    mbase = np.concatenate([[0], np.cumsum(nm[seq])])
+    mig_off = np.concatenate([bp[b][4][:-1] + mbase[i] for i, b in enumerate(seq)] + [[mbase[-1]]]).astype(np.int32)
+    mig_t = np.concatenate([bp[b][5] for b in seq])
+    mig_p = np.concatenate([bp[b][6] for b in seq]).astype(np.int32)
+    packed = (node_off, up0, time_, pop, mig_off, mig_t, mig_p)
+    gen_locus = np.tile(np.arange(nloci), nchains).astype(np.int32)
+    gen_tv = np.zeros(len(seq), np.int32)
+    hval = np.ones(nloci)
+    samppop = np.array([samp[li % nbase] for li in range(nloci)], np.int32)
+    return pm, packed, gen_locus, gen_tv, hval, samppop, tv, base, seq
+
+
+def run_treeweight(args):
+    """treeweight for every chain-locus of a config-4-sized chain set (128
+    chains x 300 loci) and the per-chain p(G) integrals: one step = the
+    weights of all genealogies and all chains' integrals, as a split-time
+    update (changet) needs them."""
+    from ima2p_gb300 import api
+    from oracle import pyoracle as O
+    nloci, nch = 300, 128
+    pm, packed, gl, gt, hval, samp, tv, base, seq = tw_workload(nloci, nch)
+    ngen = len(gl)
+    ctx = api.Context(0)
+    nth, nmg = len(pm.th_cells), len(pm.mg_cells)
+    ctx.set_popmodel(pm, 15.0, 0.0, 2.0, 0.0, 1.0)
+    goff = (np.arange(nch + 1) * nloci).astype(np.int32)
+    for _ in range(args.warmup):
+        w = ctx.treeweight(packed, gl, gt, hval, samp, tv)
+        probg, q, m, _ = ctx.tree_prob(goff)
+    ctx.set_profiling(True)
+    k0, p0 = ctx.kernel_stats(api.K_TREEWEIGHT), ctx.kernel_stats(api.K_TREE_PROB)
+    n0 = ctx.launch_count()
+    wall = []
+    with Clocks(0) as clk:
+        for _ in range(args.steps):
+            ctx.flush_l2()
+            t0 = time.perf_counter()
+            w = ctx.treeweight(packed, gl, gt, hval, samp, tv)
+            probg, q, m, _ = ctx.tree_prob(goff)
+            wall.append(time.perf_counter() - t0)
+    k1, p1 = ctx.kernel_stats(api.K_TREEWEIGHT), ctx.kernel_stats(api.K_TREE_PROB)
+    n_timed = ctx.launch_count() - n0
+    ctx.set_profiling(False)
+    nk = max(1, k1[0] - k0[0])
+    tw_ms = (k1[1] - k0[1]) / nk
+    tp_ms = (p1[1] - p0[1]) / max(1, p1[0] - p0[0])
+    dev_ms = tw_ms + tp_ms
+    value = ngen / (dev_ms / 1e3)
+    e2e = ngen / statistics.median(wall)
+    node_off, up0, time_, pop, mig_off, mig_t, mig_p = packed
+    N, Nm = len(up0), len(mig_t)
+    T, M = pm.T, pm.M
+    h2d = (ngen + 1) * 4 + N * 20 + 4 + Nm * 12 + ngen * 8 + samp.size * 4 + tv.size * 8 + nloci * 16 + (nch + 1) * 4
+    d2h = ngen * (T * 20 + M * 12 + 20) + nch * 8 * (1 + nth + nmg)
+    # algorithmic bytes of one treeweight launch: node records, migrations,
+    # weights written
+    algo = N * 20 + Nm * 12 + ngen * (T * 20 + M * 12 + 20)
+    hbm, _, src = measured_peaks()
+    gbs = algo / (tw_ms / 1e3) / 1e9
+    events = int((ngen - len(seq)) + sum(int((len(base[b].pop) - 1) // 2) for b in seq)) + int(Nm) + 2 * ngen
+    out = {
+        "metric": TW_METRIC, "value": round(value, 1), "unit": "genealogies/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic population-labelled IM genealogies",
+        "config": {"workload": "config4-treeweight: %d chains x %d loci, 3 populations ((0,1):3,2):4, "
+                               "samples U(4,60) per population, %d genealogies, %d nodes, %d migrations"
+                               % (nch, nloci, ngen, N, Nm),
+                   "global_batch": ngen, "l2": "flushed between timed steps"},
+        "e2e": {"value": round(e2e, 1), "unit": "genealogies/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "kernels_ms": {"treeweight": round(tw_ms, 4), "tree_prob": round(tp_ms, 4)},
+        "events_per_s": round(events / (tw_ms / 1e3), 1),
+        "roofline": {"kernel": "k_treeweight", "bound": "hbm", "achieved": round(gbs, 1), "peak": hbm,
+                     "unit": "GB/s", "frac": round(gbs / hbm, 5), "peak_source": src, "traffic": None,
+                     "note": "a serial event sweep per genealogy: latency and FP64-issue bound, far from HBM"},
+        "gpu_launches": int(n_timed), "clocks": clk.summary(),
+    }
+    # CPU: the oracle's treeweight (C) over whole chains of the same inputs, one core
+    sub = nloci * 8  # eight chains per call
+    spk = (node_off[:sub + 1], up0[:node_off[sub]], time_[:node_off[sub]], pop[:node_off[sub]],
+           mig_off[:node_off[sub] + 1], mig_t[:mig_off[node_off[sub]]], mig_p[:mig_off[node_off[sub]]])
+    t0 = time.perf_counter()
+    n = 0
+    while time.perf_counter() - t0 < args.cpu_seconds or n == 0:
+        bad, ow = O.treeweight_batch(pm, spk, gl[:sub], gt[:sub], hval, samp, tv)
+        n += sub
+    dt = time.perf_counter() - t0
+    assert bad == 0 and np.array_equal(ow["fc"], w["fc"][:sub]) and np.array_equal(ow["mc"], w["mc"][:sub])
+    out["cpu_baseline"] = {"value": round(n / dt, 1), "unit": "genealogies/s", "cores": 1, "kind": "port",
+                           "sample": "%d genealogies (8 chains x %d loci per call) through the oracle's "
+                                     "treeweight in C" % (n, nloci)}
+    print(json.dumps(out), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3000)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="hky", choices=["hky", "sw", "is", "mixed", "surface"])
+    ap.add_argument("--workload", default="hky", choices=["hky", "sw", "is", "mixed", "surface", "treeweight"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-cap", type=int, default=4096)
     ap.add_argument("--surface-log2g", type=int, default=21, help="log2 genealogies (config 5: 21)")
@@ -577,6 +700,8 @@ def main():
         run_reference(args)
     elif args.workload == "surface":
         run_surface(args)
+    elif args.workload == "treeweight":
+        run_treeweight(args)
     else:
         run_ours(args)
 

@@ -2028,6 +2028,7 @@ extern "C" int ima_gpu_treeweight(ima_ctx *c, int ngen, const int32_t *node_off,
   for (int li = 0; li < nloci; li++)
     if (!(hval[li] > 0)) return c->fail(IMA_ERR_ARG, "hval[%d] must be > 0", li);
   long long Emax = 0;
+  std::vector<int32_t> ev(ngen);
   for (int g = 0; g < ngen; g++) {
     const int a0 = node_off[g], nl = node_off[g + 1] - a0;
     if (nl < 1 || !(nl & 1)) return c->fail(IMA_ERR_ARG, "genealogy %d: %d nodes (need 2n-1)", g, nl);
@@ -2038,6 +2039,7 @@ extern "C" int ima_gpu_treeweight(ima_ctx *c, int ngen, const int32_t *node_off,
     if (ns != (nl + 1) / 2) return c->fail(IMA_ERR_ARG, "genealogy %d: %d genes, samppop of locus %d sums to %d", g, (nl + 1) / 2, li, ns);
     const long long E = (nl - 1) / 2 + (long long)(mig_off[a0 + nl] - mig_off[a0]) + nsplit;
     if (E > Emax) Emax = E;
+    ev[g] = (int32_t)(E < (1 << 21) ? E : (1 << 21));
   }
   const size_t N = (size_t)node_off[ngen];
   if (mig_off[0] != 0) return c->fail(IMA_ERR_ARG, "mig_off[0] must be 0");
@@ -2047,12 +2049,18 @@ extern "C" int ima_gpu_treeweight(ima_ctx *c, int ngen, const int32_t *node_off,
   if (Nm > 0 && (!mig_t || !mig_p)) return c->fail(IMA_ERR_ARG, "migration events without mig_t/mig_p");
   int P = 32;
   while (P < Emax) P <<= 1;
-  if (P > (1 << 20) || tw_smem_per_warp(P, h) > 200 * 1024)
+  if (P > (1 << 20) || tw_group_width(P, h) == 0)
     return c->fail(IMA_ERR_TOO_LARGE, "a genealogy has %lld events; at most %d fit", Emax,
                    (int)((200 * 1024 - (h.T + h.M) * 12) / 12));
+  // processing order: most events first (counting sort), so that the
+  // genealogies sharing a warp sweep about as many events
+  std::vector<int32_t> perm(ngen), cnt((size_t)Emax + 2, 0);
+  for (int g = 0; g < ngen; g++) cnt[(size_t)(Emax - ev[g])]++;
+  for (size_t i = 1; i < cnt.size(); i++) cnt[i] += cnt[i - 1];
+  for (int g = ngen - 1; g >= 0; g--) perm[--cnt[(size_t)(Emax - ev[g])]] = g;
   cudaSetDevice(c->device);
   const size_t T = h.T, MM = h.M;
-  const size_t inb = carve_size({(ngen + 1) * 4ul, N * 4, N * 4, (N + 1) * 4, Nm * 4, ngen * 4ul, ngen * 4ul,
+  const size_t inb = carve_size({ngen * 4ul, (ngen + 1) * 4ul, N * 4, N * 4, (N + 1) * 4, Nm * 4, ngen * 4ul, ngen * 4ul,
                                  (size_t)nloci * npops * 4, N * 8, Nm * 8, (size_t)ntv * nsplit * 8,
                                  (size_t)nloci * 8, (size_t)nloci * 8});
   const size_t outb = carve_size({ngen * T * 4, ngen * MM * 4, ngen * 4ul, ngen * T * 8, ngen * T * 8,
@@ -2065,6 +2073,7 @@ extern "C" int ima_gpu_treeweight(ima_ctx *c, int ngen, const int32_t *node_off,
   a.ngen = ngen;
   a.P = P;
   a.model = c->d_tw;
+  int32_t *d_perm = ci.take<int32_t>(ngen);
   int32_t *d_node_off = ci.take<int32_t>(ngen + 1), *d_up0 = ci.take<int32_t>(N), *d_pop = ci.take<int32_t>(N),
           *d_mig_off = ci.take<int32_t>(N + 1), *d_mig_p = ci.take<int32_t>(Nm),
           *d_gl = ci.take<int32_t>(ngen), *d_gt = ci.take<int32_t>(ngen),
@@ -2079,6 +2088,7 @@ extern "C" int ima_gpu_treeweight(ima_ctx *c, int ngen, const int32_t *node_off,
   auto up = [&](void *dst, const void *src, size_t bytes) {
     if (!r && bytes) r = c->cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->st), "treeweight inputs");
   };
+  up(d_perm, perm.data(), ngen * 4ul);
   up(d_node_off, node_off, (ngen + 1) * 4ul);
   up(d_up0, up0, N * 4);
   up(d_pop, pop, N * 4);
@@ -2093,6 +2103,7 @@ extern "C" int ima_gpu_treeweight(ima_ctx *c, int ngen, const int32_t *node_off,
   up(d_hlog, hl.data(), (size_t)nloci * 8);
   up(d_h2, h2.data(), (size_t)nloci * 8);
   if (r) return r;
+  a.perm = d_perm;
   a.node_off = d_node_off;
   a.up0 = d_up0;
   a.pop = d_pop;

@@ -165,6 +165,7 @@ struct TwModel {                           // tables of fillplist and setup_ipar
 struct TwArgs {
   int ngen, P;                             // genealogies; sort size (power of 2 >= events)
   const TwModel *model;
+  const int32_t *perm;                     // genealogies in processing order
   const int32_t *node_off, *up0, *pop, *mig_off, *mig_p, *gen_locus, *gen_tv;
   const double *time, *mig_t, *tvals;      // tvals [rows][npops-1]
   const double *hlog, *h2term;             // per locus, from the host's log
@@ -184,6 +185,7 @@ struct TwProbArgs {
   int rowlen;
   int32_t *err;
 };
-size_t tw_smem_per_warp(int P, const TwModel &h);
+size_t tw_smem_per_genealogy(int P, const TwModel &h);
+int tw_group_width(int P, const TwModel &h);  // 0: does not fit
 int launch_treeweight(const TwArgs &a, const TwModel &h, cudaStream_t st);
 int launch_tree_prob(const TwProbArgs &a, cudaStream_t st);

@@ -1,19 +1,23 @@
 // k_treeweight.cu -- genealogy weights and p(G) integrals on the device.
 //
-// k_treeweight restates treeweight (update_gtree_common.cpp:1680-1937): one
-// warp per genealogy.  The warp lays the genealogy's events out in shared
-// memory -- a coalescence per internal node at its daughters' time, every
-// migration with the population it leaves (the edge's population carried
-// through the splits, :1770-1790) and every split younger than the root --
-// sorts them by (time, position) with a bitonic network and sweeps them in
-// time order.  Lane l owns population l of the current period: its lineage
-// count, its fc accumulator (n(n-1) dt / 2h) and its fm accumulator (n dt;
-// the reference adds the same n dt to every partner cell, :1861-1867).  At a
+// k_treeweight restates treeweight (update_gtree_common.cpp:1680-1937) with
+// a group of lanes per genealogy (as many as the populations, rounded up to
+// a power of two: 4 lanes for 3 populations, 8 genealogies per warp).  The
+// group lays the genealogy's events out in shared memory -- a coalescence
+// per internal node at its daughters' time, every migration with the
+// population it leaves (the edge's population carried through the splits,
+// :1770-1790) and every split younger than the root -- sorts them by (time,
+// position) with a bitonic network and sweeps them in time order.  Lane l of
+// the group owns population l of the current period: its lineage count, its
+// fc accumulator (n(n-1) dt / 2h) and its fm accumulator (n dt; the
+// reference adds the same n dt to every partner cell, :1861-1867).  At a
 // split the lanes flush their period and take the counts of their new
 // population from the daughters' lanes by shuffle.  Every accumulator
 // receives the reference's terms in the reference's order, so with FMA
 // contraction off (this file is compiled with -fmad=false) the weights are
-// the reference's bit for bit.
+// the reference's bit for bit.  The sweep is FP64-issue bound (GB300 runs
+// FP64 at 1/64 of the FP32 rate), which is why genealogies share warps
+// rather than each taking a warp of mostly idle lanes.
 //
 // k_tree_prob restates sum_treeinfo (ginfo.cpp:209-244) over a chain's loci
 // in locus order, initialize_integrate_tree_prob (update_gtree_common.cpp:
@@ -52,26 +56,36 @@ __device__ void tw_fail(int32_t *err, int code, int who)
   if (atomicCAS(&err[0], 0, code) == 0) atomicExch(&err[1], who);
 }
 
-__global__ void __launch_bounds__(32 * TW_WPB) k_treeweight(TwArgs a, int wpb, int warp_bytes)
+// One group of GW lanes per genealogy (GW = the smallest power of two >=
+// npops, or wider when a genealogy's events need more shared memory), 32/GW
+// genealogies per warp.  Lane l of a group owns population l of the current
+// period.  Genealogies are taken in the order perm gives (longest event list
+// first) so that a warp's groups sweep about as many events each.
+template <int GW>
+__global__ void __launch_bounds__(32 * TW_WPB) k_treeweight(TwArgs a, int wpb, int gbytes)
 {
   extern __shared__ __align__(16) unsigned char sm[];
+  constexpr int GPW = 32 / GW;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int g = blockIdx.x * wpb + warp;
-  if (g >= a.ngen) return;  // whole warps only
+  const int grp = lane / GW, gl = lane % GW;
+  const unsigned gmask = GW == 32 ? 0xffffffffu : ((1u << GW) - 1) << (grp * GW);
+  const int slot = (blockIdx.x * wpb + warp) * GPW + grp;
+  if (slot >= a.ngen) return;  // whole groups only
+  const int g = a.perm[slot];
   const TwModel &M = *a.model;
   const int npops = M.npops, nsplit = npops - 1, ntp = 2 * npops - 1, T = M.T, MM = M.M;
-  unsigned char *base = sm + (size_t)warp * warp_bytes;
+  unsigned char *base = sm + (size_t)(warp * GPW + grp) * gbytes;
   double *ev_t = reinterpret_cast<double *>(base);
   uint32_t *ev_c = reinterpret_cast<uint32_t *>(base + (size_t)a.P * 8);
   double *fc_s = reinterpret_cast<double *>(base + (size_t)a.P * 12);
   double *fm_s = fc_s + T;
   int *cc_s = reinterpret_cast<int *>(fm_s + MM);
   int *mc_s = cc_s + T;
-  for (int i = lane; i < T; i += 32) {
+  for (int i = gl; i < T; i += GW) {
     fc_s[i] = 0.0;
     cc_s[i] = 0;
   }
-  for (int i = lane; i < MM; i += 32) {
+  for (int i = gl; i < MM; i += GW) {
     fm_s[i] = 0.0;
     mc_s[i] = 0;
   }
@@ -83,26 +97,27 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_treeweight(TwArgs a, int wpb, i
   const double *tm = a.time + a0;
   const int nmig = mo[nl] - mo[0];
 
-  // roottime: the root's coalescence, the latest one
+  // roottime: the root's coalescence, the latest one (times are >= 0, so
+  // their bit patterns order as the values do)
   int bad = 0;
-  double rt = 0.0;
-  for (int i = ng + lane; i < nl; i += 32) {
+  long long rtb = 0;
+  for (int i = ng + gl; i < nl; i += GW) {
     const int u = up0[i];
     if ((unsigned)u >= (unsigned)nl) bad = TW_E_POP;
-    else rt = fmax(rt, tm[u]);
+    else rtb = max(rtb, __double_as_longlong(tm[u]));
   }
-  for (int d = 16; d; d >>= 1) rt = fmax(rt, __shfl_xor_sync(~0u, rt, d));
-  const int kroot = tw_period(tv, nsplit, rt);
+  for (int d = GW >> 1; d; d >>= 1) rtb = max(rtb, __shfl_xor_sync(gmask, rtb, d, GW));
+  const int kroot = tw_period(tv, nsplit, __longlong_as_double(rtb));
   const int E = (ng - 1) + nmig + kroot;
-  if (__any_sync(~0u, bad) || E > a.P) {
-    if (lane == 0) tw_fail(a.err, E > a.P ? TW_E_SIZE : TW_E_POP, g);
+  if (__any_sync(gmask, bad) || E > a.P) {
+    if (gl == 0) tw_fail(a.err, E > a.P ? TW_E_SIZE : TW_E_POP, g);
     return;
   }
 
   // events: node i's coalescence first, then its migrations in edge order
   int run = 0;
-  for (int b0 = 0; b0 < nl; b0 += 32) {
-    const int i = b0 + lane;
+  for (int b0 = 0; b0 < nl; b0 += GW) {
+    const int i = b0 + gl;
     int cnt = 0, m0 = 0, m1 = 0;
     if (i < nl) {
       m0 = mo[i];
@@ -110,12 +125,12 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_treeweight(TwArgs a, int wpb, i
       cnt = (i >= ng) + (m1 - m0);
     }
     int inc = cnt;
-    for (int d = 1; d < 32; d <<= 1) {
-      const int v = __shfl_up_sync(~0u, inc, d);
-      if (lane >= d) inc += v;
+    for (int d = 1; d < GW; d <<= 1) {
+      const int v = __shfl_up_sync(gmask, inc, d, GW);
+      if (gl >= d) inc += v;
     }
     int e = run + inc - cnt;
-    run += __shfl_sync(~0u, inc, 31);
+    run += __shfl_sync(gmask, inc, GW - 1, GW);
     if (i < nl) {
       int nowpop = pp[i];
       if ((unsigned)nowpop >= (unsigned)ntp || m1 < m0 || e + cnt > E) {
@@ -143,56 +158,56 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_treeweight(TwArgs a, int wpb, i
       }
     }
   }
-  if (lane < kroot) {
-    ev_t[run + lane] = tv[lane];
-    ev_c[run + lane] = ev_pack(EV_SPLIT, 0, 0, run + lane);
+  if (gl < kroot) {
+    ev_t[run + gl] = tv[gl];
+    ev_c[run + gl] = ev_pack(EV_SPLIT, 0, 0, run + gl);
   }
   int Pg = 1;
   while (Pg < E) Pg <<= 1;
-  for (int i = E + lane; i < Pg; i += 32) {
+  for (int i = E + gl; i < Pg; i += GW) {
     ev_t[i] = __longlong_as_double(0x7ff0000000000000LL);  // +inf: after every event
     ev_c[i] = ev_pack(EV_PAD, 0, 0, i);
   }
-  if (__any_sync(~0u, bad)) {
-    if (lane == 0) tw_fail(a.err, TW_E_POP, g);
+  if (__any_sync(gmask, bad)) {
+    if (gl == 0) tw_fail(a.err, TW_E_POP, g);
     return;
   }
-  __syncwarp();
+  __syncwarp(gmask);
 
-  // bitonic sort on (time, position): the positions are distinct, so the
-  // order is total and ties in time keep the order the events were listed in
+  // bitonic sort on (time, position), compared as integers: the positions
+  // are distinct, so the order is total and ties in time keep list order
   for (int size = 2; size <= Pg; size <<= 1) {
     for (int stride = size >> 1; stride > 0; stride >>= 1) {
-      for (int i = lane; i < (Pg >> 1); i += 32) {
+      for (int i = gl; i < (Pg >> 1); i += GW) {
         const int lo = ((i & ~(stride - 1)) << 1) | (i & (stride - 1));
         const int hi = lo + stride;
-        const double tl = ev_t[lo], th = ev_t[hi];
+        const long long tl = __double_as_longlong(ev_t[lo]), th = __double_as_longlong(ev_t[hi]);
         const uint32_t cl = ev_c[lo], ch = ev_c[hi];
         const bool gt = tl > th || (tl == th && (cl & POS_MASK) > (ch & POS_MASK));
         if (gt == ((lo & size) == 0)) {
-          ev_t[lo] = th;
-          ev_t[hi] = tl;
+          ev_t[lo] = __longlong_as_double(th);
+          ev_t[hi] = __longlong_as_double(tl);
           ev_c[lo] = ch;
           ev_c[hi] = cl;
         }
       }
-      __syncwarp();
+      __syncwarp(gmask);
     }
   }
 
   // the sweep (update_gtree_common.cpp:1827-1927)
   const double h2 = a.h2term[loc], hl = a.hlog[loc];
   const double lastsplitt = tv[nsplit - 1];
-  int k = 0, nsum = ng, nmine = lane < npops ? a.samppop[(size_t)loc * npops + lane] : 0, ccm = 0;
+  int k = 0, nsum = ng, nmine = gl < npops ? a.samppop[(size_t)loc * npops + gl] : 0, ccm = 0;
   double accfc = 0.0, accfm = 0.0, last = 0.0, len = 0.0, tlen = 0.0;
   auto flush = [&](int kk) {
     const int w = npops - kk;
-    if (lane < w) {
-      fc_s[M.toff[kk] + lane] = accfc;
-      cc_s[M.toff[kk] + lane] = ccm;
+    if (gl < w) {
+      fc_s[M.toff[kk] + gl] = accfc;
+      cc_s[M.toff[kk] + gl] = ccm;
       if (!M.nomig && kk < nsplit)
         for (int jj = 0; jj < w; jj++)
-          if (jj != lane) fm_s[M.moff[kk] + lane * w + jj] = accfm;
+          if (jj != gl) fm_s[M.moff[kk] + gl * w + jj] = accfm;
     }
   };
   for (int j = 0; j < E; j++) {
@@ -207,9 +222,10 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_treeweight(TwArgs a, int wpb, i
       tlen += nsum * (lastsplitt - last);
     last = t;
     const int w = npops - k;
-    if (lane < w) {
-      const double dn = (double)nmine;
-      accfc += dn * (dn - 1) * dt * h2;
+    if (gl < w) {
+      // n(n-1) is exact in an int and in a double, so converting the
+      // product equals the reference's (double)n * ((double)n - 1)
+      accfc += (double)(nmine * (nmine - 1)) * dt * h2;
       if (!M.nomig && k < nsplit) accfm += nmine * dt;
     }
     const int type = (int)(c >> 30);
@@ -218,7 +234,7 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_treeweight(TwArgs a, int wpb, i
       const int o = M.pos[k][(c >> 20) & 31];
       if (o < 0) {
         bad = TW_E_POP;
-      } else if (lane == o) {
+      } else if (gl == o) {
         lbad = nmine < 2;
         nmine--;
         ccm++;
@@ -229,12 +245,12 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_treeweight(TwArgs a, int wpb, i
       if (op < 0 || oq < 0 || k >= nsplit) {
         bad = TW_E_POP;
       } else {
-        if (lane == op) {
+        if (gl == op) {
           lbad = nmine < 1;
           nmine--;
           mc_s[M.moff[k] + op * w + oq]++;
         }
-        if (lane == oq) nmine++;
+        if (gl == oq) nmine++;
       }
     } else {  // a split: the period ends
       if (k >= nsplit || nsum < 2) {
@@ -243,8 +259,8 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_treeweight(TwArgs a, int wpb, i
         flush(k);
         const int k1 = k + 1;
         int s0 = 0, s1 = -1;
-        if (lane < npops - k1) {
-          const int np1 = M.plist[k1][lane];
+        if (gl < npops - k1) {
+          const int np1 = M.plist[k1][gl];
           if (np1 == M.addpop[k1]) {
             s0 = M.pos[k][M.droppops[k1][0]];
             s1 = M.pos[k][M.droppops[k1][1]];
@@ -252,35 +268,35 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_treeweight(TwArgs a, int wpb, i
             s0 = M.pos[k][np1];
           }
         }
-        const int v0 = __shfl_sync(~0u, nmine, s0 < 0 ? 0 : s0);
-        const int v1 = __shfl_sync(~0u, nmine, s1 < 0 ? 0 : s1);
-        nmine = lane < npops - k1 ? v0 + (s1 >= 0 ? v1 : 0) : 0;
+        const int v0 = __shfl_sync(gmask, nmine, s0 < 0 ? 0 : s0, GW);
+        const int v1 = __shfl_sync(gmask, nmine, s1 < 0 ? 0 : s1, GW);
+        nmine = gl < npops - k1 ? v0 + (s1 >= 0 ? v1 : 0) : 0;
         k = k1;
         accfc = accfm = 0.0;
         ccm = 0;
       }
     }
-    if (__any_sync(~0u, lbad)) bad = TW_E_COUNT;
+    if (__any_sync(gmask, lbad)) bad = TW_E_COUNT;
     if (bad) break;
   }
   if (!bad && nsum != 1) bad = TW_E_COUNT;
   if (bad) {
-    if (lane == 0) tw_fail(a.err, bad, g);
+    if (gl == 0) tw_fail(a.err, bad, g);
     return;
   }
   flush(k);
-  __syncwarp();
+  __syncwarp(gmask);
   const size_t oT = (size_t)g * T, oM = (size_t)g * MM;
-  for (int i = lane; i < T; i += 32) {
+  for (int i = gl; i < T; i += GW) {
     a.cc[oT + i] = cc_s[i];
     a.fc[oT + i] = fc_s[i];
     a.hcc[oT + i] = hl != 0.0 ? 0.0 + hl * cc_s[i] : 0.0;
   }
-  for (int i = lane; i < MM; i += 32) {
+  for (int i = gl; i < MM; i += GW) {
     a.mc[oM + i] = mc_s[i];
     a.fm[oM + i] = fm_s[i];
   }
-  if (lane == 0) {
+  if (gl == 0) {
     a.lens[2 * (size_t)g] = len;
     a.lens[2 * (size_t)g + 1] = tlen;
     a.mignum[g] = nmig;
@@ -632,28 +648,49 @@ __global__ void __launch_bounds__(32 * TP_WPB) k_tree_prob(TwProbArgs a)
 
 }  // namespace
 
-size_t tw_smem_per_warp(int P, const TwModel &h)
+size_t tw_smem_per_genealogy(int P, const TwModel &h)
 {
   const size_t b = (size_t)P * 12 + (size_t)(h.T + h.M) * 12;
   return (b + 15) / 16 * 16;
 }
 
+int tw_group_width(int P, const TwModel &h)
+{
+  int gw = 2;
+  while (gw < h.npops) gw <<= 1;
+  while (gw < 32 && (32 / gw) * tw_smem_per_genealogy(P, h) > 200 * 1024) gw <<= 1;
+  return (32 / gw) * tw_smem_per_genealogy(P, h) > 200 * 1024 ? 0 : gw;
+}
+
+template <int GW>
+static int launch_tw(const TwArgs &a, const TwModel &h, cudaStream_t st)
+{
+  const size_t per = tw_smem_per_genealogy(a.P, h);
+  const size_t warp_bytes = per * (32 / GW);
+  int wpb = (int)((200 * 1024) / warp_bytes);
+  wpb = wpb < 1 ? 1 : (wpb > TW_WPB ? TW_WPB : wpb);
+  const size_t smem = warp_bytes * wpb;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_treeweight<GW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return 2;
+  }
+  const int per_block = wpb * (32 / GW);
+  const int grid = (a.ngen + per_block - 1) / per_block;
+  k_treeweight<GW><<<grid, 32 * wpb, smem, st>>>(a, wpb, (int)per);
+  return 0;
+}
+
 int launch_treeweight(const TwArgs &a, const TwModel &h, cudaStream_t st)
 {
   if (a.ngen < 1) return 0;
-  const size_t per = tw_smem_per_warp(a.P, h);
-  const size_t cap = 200 * 1024;
-  if (per > cap) return 1;
-  int wpb = (int)(cap / per);
-  wpb = wpb < 1 ? 1 : (wpb > TW_WPB ? TW_WPB : wpb);
-  const size_t smem = per * wpb;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_treeweight, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return 2;
+  switch (tw_group_width(a.P, h)) {
+    case 2: return launch_tw<2>(a, h, st);
+    case 4: return launch_tw<4>(a, h, st);
+    case 8: return launch_tw<8>(a, h, st);
+    case 16: return launch_tw<16>(a, h, st);
+    case 32: return launch_tw<32>(a, h, st);
+    default: return 1;
   }
-  const int grid = (a.ngen + wpb - 1) / wpb;
-  k_treeweight<<<grid, 32 * wpb, smem, st>>>(a, wpb, (int)per);
-  return 0;
 }
 
 int launch_tree_prob(const TwProbArgs &a, cudaStream_t st)

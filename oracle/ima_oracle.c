@@ -1317,3 +1317,27 @@ void ora_gsamp_row(int nomig, const int *cc, const double *hcc, const double *fc
   row[probgp] = (float)probg;
   for (int i = 0; i < nsplit; i++) row[tp + i] = (float)tvals[i];
 }
+
+int ora_treeweight_batch(int npops, const int *plist, const int *droppops, const int *addpop,
+                         const int *pop_e, const int *pop_down, int nomig, int ngen, const int *node_off,
+                         const int *up0, const double *time, const int *pop, const int *mig_off,
+                         const double *mig_t, const int *mig_p, const int *gen_locus, const int *gen_tv,
+                         const double *hval, const int *samppop, const double *tvals, int *cc, double *hcc,
+                         double *fc, int *mc, double *fm, double *lens, int *mignum)
+{
+  int T, M, bad = 0;
+  ora_tw_sizes(npops, &T, &M);
+  int *moff = (int *)malloc(sizeof(int) * (size_t)(node_off[ngen] + 1));
+  for (int g = 0; g < ngen; g++) {
+    const int a0 = node_off[g], nl = node_off[g + 1] - a0, li = gen_locus[g];
+    for (int i = 0; i <= nl; i++) moff[i] = mig_off[a0 + i] - mig_off[a0];
+    const int mb = mig_off[a0];
+    if (ora_treeweight(npops, plist, droppops, addpop, pop_e, pop_down, tvals + (size_t)gen_tv[g] * (npops - 1),
+                       nomig, (nl + 1) / 2, samppop + (size_t)li * npops, hval[li], up0 + a0, time + a0, pop + a0,
+                       moff, mig_t + mb, mig_p + mb, cc + (size_t)g * T, hcc + (size_t)g * T, fc + (size_t)g * T,
+                       mc + (size_t)g * M, fm + (size_t)g * M, lens + 2 * (size_t)g, mignum + g))
+      bad++;
+  }
+  free(moff);
+  return bad;
+}

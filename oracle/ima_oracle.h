@@ -163,6 +163,15 @@ int ora_treeweight(int npops, const int *plist, const int *droppops, const int *
                    const double *time, const int *pop, const int *mig_off,
                    const double *mig_t, const int *mig_p, int *cc, double *hcc,
                    double *fc, int *mc, double *fm, double *out3, int *mignum);
+/* ora_treeweight over ngen genealogies in the CSR layout of
+ * ima_gpu_treeweight (the CPU baseline of that call); returns the number
+ * of genealogies the model could not hold. */
+int ora_treeweight_batch(int npops, const int *plist, const int *droppops, const int *addpop,
+                         const int *pop_e, const int *pop_down, int nomig, int ngen, const int *node_off,
+                         const int *up0, const double *time, const int *pop, const int *mig_off,
+                         const double *mig_t, const int *mig_p, const int *gen_locus, const int *gen_tv,
+                         const double *hval, const int *samppop, const double *tvals, int *cc, double *hcc,
+                         double *fc, int *mc, double *fm, double *lens, int *mignum);
 /* The integral terms (update_gtree_common.cpp:108-304, MORESTABLE form) on
  * the reference's incomplete gamma functions (utilities.cpp:808-1130).
  * kind 0: integrate_coalescent_term(c, f, h, max, min); 1:

@@ -78,6 +78,8 @@ def _declare(L):
     L.ora_modelloop.restype = I
     L.ora_treeweight.argtypes = [I, P, P, P, P, P, P, I, I, P, D, P, P, P, P, P, P, P, P, P, P, P, P, P]
     L.ora_treeweight.restype = I
+    L.ora_treeweight_batch.argtypes = [I, P, P, P, P, P, I, I] + [P] * 19
+    L.ora_treeweight_batch.restype = I
     L.ora_iterm.argtypes = [I, I, D, D, D, D, P]
     L.ora_iterm.restype = D
     L.ora_tree_prob.argtypes = [I, I, P, P, P, P, P, I, P, P, P, P, I, P, P, P, P, P, I, P, P, P, P]
@@ -490,3 +492,22 @@ def gsamp_row(pm, w, q, m, pdg, probg, tvals):
                         _p(_f64(q)), _p(_f64(m if len(m) else np.zeros(1))), float(pdg), float(probg),
                         pm.npops - 1, _p(_f64(tvals)), _p(row))
     return row
+
+
+def treeweight_batch(pm, packed, gen_locus, gen_tv, hval, samppop, tvals):
+    """ora_treeweight_batch over the CSR inputs of ima_gpu_treeweight;
+    returns (number rejected, dict of outputs)."""
+    node_off, up0, time, pop, mig_off, mig_t, mig_p = packed
+    ngen = len(node_off) - 1
+    T, M = pm.T, pm.M
+    out = {"cc": np.zeros((ngen, T), np.int32), "hcc": np.zeros((ngen, T)), "fc": np.zeros((ngen, T)),
+           "mc": np.zeros((ngen, M), np.int32), "fm": np.zeros((ngen, M)), "lens": np.zeros((ngen, 2)),
+           "mignum": np.zeros(ngen, np.int32)}
+    keep = [_i32(node_off), _i32(up0), _f64(time), _i32(pop), _i32(mig_off),
+            _f64(mig_t if len(mig_t) else np.zeros(1)), _i32(mig_p if len(mig_p) else np.zeros(1)),
+            _i32(gen_locus), _i32(gen_tv), _f64(hval), _i32(samppop), _f64(tvals)]
+    bad = lib().ora_treeweight_batch(pm.npops, _p(_i32(pm.plist)), _p(_i32(pm.droppops)), _p(_i32(pm.addpop)),
+                                     _p(_i32(pm.pop_e)), _p(_i32(pm.pop_down)), int(pm.nomig), ngen,
+                                     *(_p(a) for a in keep),
+                                     *(_p(out[k]) for k in ("cc", "hcc", "fc", "mc", "fm", "lens", "mignum")))
+    return bad, out
