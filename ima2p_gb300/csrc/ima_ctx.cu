@@ -2049,7 +2049,7 @@ extern "C" int ima_gpu_treeweight(ima_ctx *c, int ngen, const int32_t *node_off,
   if (Nm > 0 && (!mig_t || !mig_p)) return c->fail(IMA_ERR_ARG, "migration events without mig_t/mig_p");
   int P = 32;
   while (P < Emax) P <<= 1;
-  if (P > (1 << 20) || tw_group_width(P, h) == 0)
+  if (P > (1 << 20) || !tw_fits(P))
     return c->fail(IMA_ERR_TOO_LARGE, "a genealogy has %lld events; at most %d fit", Emax,
                    (int)((200 * 1024 - (h.T + h.M) * 12) / 12));
   // processing order: most events first (counting sort), so that the
@@ -2058,11 +2058,16 @@ extern "C" int ima_gpu_treeweight(ima_ctx *c, int ngen, const int32_t *node_off,
   for (int g = 0; g < ngen; g++) cnt[(size_t)(Emax - ev[g])]++;
   for (size_t i = 1; i < cnt.size(); i++) cnt[i] += cnt[i - 1];
   for (int g = ngen - 1; g >= 0; g--) perm[--cnt[(size_t)(Emax - ev[g])]] = g;
+  std::vector<long long> evoff(ngen + 1);
+  evoff[0] = 0;
+  for (int g = 0; g < ngen; g++) evoff[g + 1] = evoff[g] + ev[g];
+  const size_t Etot = (size_t)evoff[ngen];
   cudaSetDevice(c->device);
   const size_t T = h.T, MM = h.M;
   const size_t inb = carve_size({ngen * 4ul, (ngen + 1) * 4ul, N * 4, N * 4, (N + 1) * 4, Nm * 4, ngen * 4ul, ngen * 4ul,
                                  (size_t)nloci * npops * 4, N * 8, Nm * 8, (size_t)ntv * nsplit * 8,
-                                 (size_t)nloci * 8, (size_t)nloci * 8});
+                                 (size_t)nloci * 8, (size_t)nloci * 8, (ngen + 1) * 8ul, Etot * 8, Etot * 4,
+                                 ngen * 4ul});
   const size_t outb = carve_size({ngen * T * 4, ngen * MM * 4, ngen * 4ul, ngen * T * 8, ngen * T * 8,
                                   ngen * MM * 8, 2 * ngen * 8ul});
   int r = grow(c, &c->d_twin, &c->twin_cap, inb, "treeweight inputs");
@@ -2080,6 +2085,11 @@ extern "C" int ima_gpu_treeweight(ima_ctx *c, int ngen, const int32_t *node_off,
           *d_sp = ci.take<int32_t>((size_t)nloci * npops);
   double *d_time = ci.take<double>(N), *d_mig_t = ci.take<double>(Nm), *d_tv = ci.take<double>((size_t)ntv * nsplit),
          *d_hlog = ci.take<double>(nloci), *d_h2 = ci.take<double>(nloci);
+  long long *d_evoff = ci.take<long long>(ngen + 1);
+  a.ev_t = ci.take<double>(Etot);
+  a.ev_c = ci.take<uint32_t>(Etot);
+  a.ev_n = ci.take<int32_t>(ngen);
+  a.ev_off = d_evoff;
   std::vector<double> hl(nloci), h2(nloci);
   for (int li = 0; li < nloci; li++) {
     hl[li] = log(hval[li]);           // treeweight: hlog = log (L[li].hval)
@@ -2102,6 +2112,7 @@ extern "C" int ima_gpu_treeweight(ima_ctx *c, int ngen, const int32_t *node_off,
   up(d_tv, tvals, (size_t)ntv * nsplit * 8);
   up(d_hlog, hl.data(), (size_t)nloci * 8);
   up(d_h2, h2.data(), (size_t)nloci * 8);
+  up(d_evoff, evoff.data(), (ngen + 1) * 8ul);
   if (r) return r;
   a.perm = d_perm;
   a.node_off = d_node_off;
@@ -2131,6 +2142,7 @@ extern "C" int ima_gpu_treeweight(ima_ctx *c, int ngen, const int32_t *node_off,
   int lr = 0;
   c->launch(IMA_K_TREEWEIGHT, (double)N * 20 + (double)Nm * 12 + (double)ngen * (T * 20 + MM * 12 + 20),
             [&] { lr = launch_treeweight(a, h, c->st); });
+  c->launches += 1;  // event sort + sweep
   if (lr) return c->fail(IMA_ERR_TOO_LARGE, "treeweight: shared memory for %d events", P);
   r = c->cuda(cudaGetLastError(), "treeweight launch");
   if (r) return r;

@@ -173,6 +173,10 @@ struct TwArgs {
   int32_t *cc, *mc, *mignum;               // [ngen][T], [ngen][M], [ngen]
   double *hcc, *fc, *fm, *lens;            // [ngen][T], [ngen][T], [ngen][M], [ngen][2]
   int32_t *err;                            // {code, genealogy}: first failure
+  const long long *ev_off;                 // [ngen+1] event-list offsets (an upper bound each)
+  double *ev_t;                            // sorted event times (pass 1 -> pass 2)
+  uint32_t *ev_c;                          // sorted event codes
+  int32_t *ev_n;                           // [ngen] events, -1 when rejected
 };
 struct TwProbArgs {
   int ngroups;
@@ -185,7 +189,6 @@ struct TwProbArgs {
   int rowlen;
   int32_t *err;
 };
-size_t tw_smem_per_genealogy(int P, const TwModel &h);
-int tw_group_width(int P, const TwModel &h);  // 0: does not fit
+bool tw_fits(int P);                       // P events fit one warp's shared memory
 int launch_treeweight(const TwArgs &a, const TwModel &h, cudaStream_t st);
 int launch_tree_prob(const TwProbArgs &a, cudaStream_t st);

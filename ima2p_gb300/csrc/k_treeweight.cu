@@ -56,43 +56,23 @@ __device__ void tw_fail(int32_t *err, int code, int who)
   if (atomicCAS(&err[0], 0, code) == 0) atomicExch(&err[1], who);
 }
 
-// One group of GW lanes per genealogy (GW = the smallest power of two >=
-// npops, or wider when a genealogy's events need more shared memory), 32/GW
-// genealogies per warp.  Lane l of a group owns population l of the current
-// period.  Genealogies are taken in the order perm gives (longest event list
-// first) so that a warp's groups sweep about as many events each.
-template <int GW>
-__global__ void __launch_bounds__(32 * TW_WPB) k_treeweight(TwArgs a, int wpb, int gbytes)
+// Pass 1, one warp per genealogy: lay out the events in shared memory, sort
+// them and write the sorted list to ev_t/ev_c at the genealogy's offset;
+// ev_n[g] = the number of events, or -1 for a genealogy the model cannot hold.
+__global__ void __launch_bounds__(32 * TW_WPB) k_tw_events(TwArgs a, int wpb)
 {
   extern __shared__ __align__(16) unsigned char sm[];
-  constexpr int GPW = 32 / GW;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int grp = lane / GW, gl = lane % GW;
-  const unsigned gmask = GW == 32 ? 0xffffffffu : ((1u << GW) - 1) << (grp * GW);
-  const int slot = (blockIdx.x * wpb + warp) * GPW + grp;
-  if (slot >= a.ngen) return;  // whole groups only
-  const int g = a.perm[slot];
+  const int g = blockIdx.x * wpb + warp;
+  if (g >= a.ngen) return;  // whole warps only
   const TwModel &M = *a.model;
-  const int npops = M.npops, nsplit = npops - 1, ntp = 2 * npops - 1, T = M.T, MM = M.M;
-  unsigned char *base = sm + (size_t)(warp * GPW + grp) * gbytes;
+  const int npops = M.npops, nsplit = npops - 1, ntp = 2 * npops - 1;
+  unsigned char *base = sm + (size_t)warp * a.P * 12;
   double *ev_t = reinterpret_cast<double *>(base);
   uint32_t *ev_c = reinterpret_cast<uint32_t *>(base + (size_t)a.P * 8);
-  double *fc_s = reinterpret_cast<double *>(base + (size_t)a.P * 12);
-  double *fm_s = fc_s + T;
-  int *cc_s = reinterpret_cast<int *>(fm_s + MM);
-  int *mc_s = cc_s + T;
-  for (int i = gl; i < T; i += GW) {
-    fc_s[i] = 0.0;
-    cc_s[i] = 0;
-  }
-  for (int i = gl; i < MM; i += GW) {
-    fm_s[i] = 0.0;
-    mc_s[i] = 0;
-  }
 
   const int a0 = a.node_off[g], nl = a.node_off[g + 1] - a0, ng = (nl + 1) >> 1;
   const double *tv = a.tvals + (size_t)a.gen_tv[g] * nsplit;
-  const int loc = a.gen_locus[g];
   const int32_t *up0 = a.up0 + a0, *pp = a.pop + a0, *mo = a.mig_off + a0;
   const double *tm = a.time + a0;
   const int nmig = mo[nl] - mo[0];
@@ -101,23 +81,26 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_treeweight(TwArgs a, int wpb, i
   // their bit patterns order as the values do)
   int bad = 0;
   long long rtb = 0;
-  for (int i = ng + gl; i < nl; i += GW) {
+  for (int i = ng + lane; i < nl; i += 32) {
     const int u = up0[i];
     if ((unsigned)u >= (unsigned)nl) bad = TW_E_POP;
     else rtb = max(rtb, __double_as_longlong(tm[u]));
   }
-  for (int d = GW >> 1; d; d >>= 1) rtb = max(rtb, __shfl_xor_sync(gmask, rtb, d, GW));
+  for (int d = 16; d; d >>= 1) rtb = max(rtb, __shfl_xor_sync(~0u, rtb, d));
   const int kroot = tw_period(tv, nsplit, __longlong_as_double(rtb));
   const int E = (ng - 1) + nmig + kroot;
-  if (__any_sync(gmask, bad) || E > a.P) {
-    if (gl == 0) tw_fail(a.err, E > a.P ? TW_E_SIZE : TW_E_POP, g);
+  if (__any_sync(~0u, bad) || E > a.P || a.ev_off[g] + E > a.ev_off[g + 1]) {
+    if (lane == 0) {
+      a.ev_n[g] = -1;
+      tw_fail(a.err, bad ? TW_E_POP : TW_E_SIZE, g);
+    }
     return;
   }
 
   // events: node i's coalescence first, then its migrations in edge order
   int run = 0;
-  for (int b0 = 0; b0 < nl; b0 += GW) {
-    const int i = b0 + gl;
+  for (int b0 = 0; b0 < nl; b0 += 32) {
+    const int i = b0 + lane;
     int cnt = 0, m0 = 0, m1 = 0;
     if (i < nl) {
       m0 = mo[i];
@@ -125,12 +108,12 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_treeweight(TwArgs a, int wpb, i
       cnt = (i >= ng) + (m1 - m0);
     }
     int inc = cnt;
-    for (int d = 1; d < GW; d <<= 1) {
-      const int v = __shfl_up_sync(gmask, inc, d, GW);
-      if (gl >= d) inc += v;
+    for (int d = 1; d < 32; d <<= 1) {
+      const int v = __shfl_up_sync(~0u, inc, d);
+      if (lane >= d) inc += v;
     }
     int e = run + inc - cnt;
-    run += __shfl_sync(gmask, inc, GW - 1, GW);
+    run += __shfl_sync(~0u, inc, 31);
     if (i < nl) {
       int nowpop = pp[i];
       if ((unsigned)nowpop >= (unsigned)ntp || m1 < m0 || e + cnt > E) {
@@ -158,27 +141,30 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_treeweight(TwArgs a, int wpb, i
       }
     }
   }
-  if (gl < kroot) {
-    ev_t[run + gl] = tv[gl];
-    ev_c[run + gl] = ev_pack(EV_SPLIT, 0, 0, run + gl);
+  if (lane < kroot) {
+    ev_t[run + lane] = tv[lane];
+    ev_c[run + lane] = ev_pack(EV_SPLIT, 0, 0, run + lane);
   }
   int Pg = 1;
   while (Pg < E) Pg <<= 1;
-  for (int i = E + gl; i < Pg; i += GW) {
+  for (int i = E + lane; i < Pg; i += 32) {
     ev_t[i] = __longlong_as_double(0x7ff0000000000000LL);  // +inf: after every event
     ev_c[i] = ev_pack(EV_PAD, 0, 0, i);
   }
-  if (__any_sync(gmask, bad)) {
-    if (gl == 0) tw_fail(a.err, TW_E_POP, g);
+  if (__any_sync(~0u, bad)) {
+    if (lane == 0) {
+      a.ev_n[g] = -1;
+      tw_fail(a.err, TW_E_POP, g);
+    }
     return;
   }
-  __syncwarp(gmask);
+  __syncwarp();
 
   // bitonic sort on (time, position), compared as integers: the positions
   // are distinct, so the order is total and ties in time keep list order
   for (int size = 2; size <= Pg; size <<= 1) {
     for (int stride = size >> 1; stride > 0; stride >>= 1) {
-      for (int i = gl; i < (Pg >> 1); i += GW) {
+      for (int i = lane; i < (Pg >> 1); i += 32) {
         const int lo = ((i & ~(stride - 1)) << 1) | (i & (stride - 1));
         const int hi = lo + stride;
         const long long tl = __double_as_longlong(ev_t[lo]), th = __double_as_longlong(ev_t[hi]);
@@ -191,15 +177,60 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_treeweight(TwArgs a, int wpb, i
           ev_c[hi] = cl;
         }
       }
-      __syncwarp(gmask);
+      __syncwarp();
     }
   }
+  const long long off = a.ev_off[g];
+  for (int j = lane; j < E; j += 32) {
+    a.ev_t[off + j] = ev_t[j];
+    a.ev_c[off + j] = ev_c[j];
+  }
+  if (lane == 0) a.ev_n[g] = E;
+}
 
-  // the sweep (update_gtree_common.cpp:1827-1927)
+// Pass 2, the sweep (update_gtree_common.cpp:1827-1927): one group of GW
+// lanes per genealogy (GW = the smallest power of two >= npops), 32/GW
+// genealogies per warp, taken in the order perm gives (most events first) so
+// that a warp's groups sweep about as many events each.  Lane l of a group
+// owns population l of the current period.
+template <int GW>
+__global__ void __launch_bounds__(32 * TW_WPB) k_tw_sweep(TwArgs a, int wpb, int gbytes)
+{
+  extern __shared__ __align__(16) unsigned char sm[];
+  constexpr int GPW = 32 / GW;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int grp = lane / GW, gl = lane % GW;
+  const unsigned gmask = GW == 32 ? 0xffffffffu : ((1u << GW) - 1) << (grp * GW);
+  const int slot = (blockIdx.x * wpb + warp) * GPW + grp;
+  if (slot >= a.ngen) return;  // whole groups only
+  const int g = a.perm[slot];
+  const int E = a.ev_n[g];
+  if (E < 0) return;  // pass 1 rejected it
+  const TwModel &M = *a.model;
+  const int npops = M.npops, nsplit = npops - 1, T = M.T, MM = M.M;
+  double *fc_s = reinterpret_cast<double *>(sm + (size_t)(warp * GPW + grp) * gbytes);
+  double *fm_s = fc_s + T;
+  int *cc_s = reinterpret_cast<int *>(fm_s + MM);
+  int *mc_s = cc_s + T;
+  for (int i = gl; i < T; i += GW) {
+    fc_s[i] = 0.0;
+    cc_s[i] = 0;
+  }
+  for (int i = gl; i < MM; i += GW) {
+    fm_s[i] = 0.0;
+    mc_s[i] = 0;
+  }
+  const int a0 = a.node_off[g], nl = a.node_off[g + 1] - a0, ng = (nl + 1) >> 1;
+  const double *tv = a.tvals + (size_t)a.gen_tv[g] * nsplit;
+  const int loc = a.gen_locus[g];
+  const double *et = a.ev_t + a.ev_off[g];
+  const uint32_t *ec = a.ev_c + a.ev_off[g];
   const double h2 = a.h2term[loc], hl = a.hlog[loc];
   const double lastsplitt = tv[nsplit - 1];
-  int k = 0, nsum = ng, nmine = gl < npops ? a.samppop[(size_t)loc * npops + gl] : 0, ccm = 0;
+  const long long lsb = __double_as_longlong(lastsplitt);  // times >= 0: compare bit patterns
+  int k = 0, nsum = ng, nmine = gl < npops ? a.samppop[(size_t)loc * npops + gl] : 0, ccm = 0, bad = 0;
   double accfc = 0.0, accfm = 0.0, last = 0.0, len = 0.0, tlen = 0.0;
+  __syncwarp(gmask);
   auto flush = [&](int kk) {
     const int w = npops - kk;
     if (gl < w) {
@@ -210,15 +241,21 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_treeweight(TwArgs a, int wpb, i
           if (jj != gl) fm_s[M.moff[kk] + gl * w + jj] = accfm;
     }
   };
+  double tn = E > 0 ? et[0] : 0.0;
+  uint32_t cn = E > 0 ? ec[0] : 0u;
   for (int j = 0; j < E; j++) {
-    const double t = ev_t[j];
-    const uint32_t c = ev_c[j];
+    const double t = tn;
+    const uint32_t c = cn;
+    if (j + 1 < E) {  // the next event's load overlaps this one's arithmetic
+      tn = et[j + 1];
+      cn = ec[j + 1];
+    }
     const double dt = t - last;
     const double tadd = nsum * dt;
     len += tadd;
-    if (t < lastsplitt)
+    if (__double_as_longlong(t) < lsb)
       tlen += tadd;
-    else if (last < lastsplitt)
+    else if (__double_as_longlong(last) < lsb)
       tlen += nsum * (lastsplitt - last);
     last = t;
     const int w = npops - k;
@@ -299,7 +336,7 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_treeweight(TwArgs a, int wpb, i
   if (gl == 0) {
     a.lens[2 * (size_t)g] = len;
     a.lens[2 * (size_t)g + 1] = tlen;
-    a.mignum[g] = nmig;
+    a.mignum[g] = a.mig_off[a0 + nl] - a.mig_off[a0];
   }
 }
 
@@ -546,6 +583,7 @@ __global__ void __launch_bounds__(32 * TP_WPB) k_tree_prob(TwProbArgs a)
   for (int i = lane; i < T; i += 32) {
     int c = 0;
     double f = 0.0, h = 0.0;
+#pragma unroll 8
     for (int g = g0; g < g1; g++) {
       c += a.cc[(size_t)g * T + i];
       f += a.fc[(size_t)g * T + i];
@@ -559,6 +597,7 @@ __global__ void __launch_bounds__(32 * TP_WPB) k_tree_prob(TwProbArgs a)
     for (int i = lane; i < MM; i += 32) {
       int c = 0;
       double f = 0.0;
+#pragma unroll 8
       for (int g = g0; g < g1; g++) {
         c += a.mc[(size_t)g * MM + i];
         f += a.fm[(size_t)g * MM + i];
@@ -568,24 +607,28 @@ __global__ void __launch_bounds__(32 * TP_WPB) k_tree_prob(TwProbArgs a)
     }
   __syncwarp();
   Ig ig{a.logfact, 0};
-  for (int i = lane; i < nth; i += 32) {
-    int c = 0;
-    double f = 0.0, hc = 0.0;
-    for (int j = M.th_off[i]; j < M.th_off[i + 1]; j++) {
-      c += s_cc[warp][M.th_idx[j]];
-      f += s_fc[warp][M.th_idx[j]];
-      hc += s_hcc[warp][M.th_idx[j]];
+  // one lane per parameter: theta parameters, then migration rates
+  for (int p = lane; p < nth + nmg; p += 32) {
+    if (p < nth) {
+      const int i = p;
+      int c = 0;
+      double f = 0.0, hc = 0.0;
+      for (int j = M.th_off[i]; j < M.th_off[i + 1]; j++) {
+        c += s_cc[warp][M.th_idx[j]];
+        f += s_fc[warp][M.th_idx[j]];
+        hc += s_hcc[warp][M.th_idx[j]];
+      }
+      s_q[warp][i] = ig.coal(c, f, hc, M.th_max[i], M.th_min[i]);
+    } else {
+      const int i = p - nth;
+      int c = 0;
+      double f = 0.0;
+      for (int j = M.mg_off[i]; j < M.mg_off[i + 1]; j++) {
+        c += s_mc[warp][M.mg_idx[j]];
+        f += s_fm[warp][M.mg_idx[j]];
+      }
+      s_m[warp][i] = M.expo ? ig.mig_expo(c, f, M.mg_mean[i]) : ig.mig(c, f, M.mg_max[i], M.mg_min[i]);
     }
-    s_q[warp][i] = ig.coal(c, f, hc, M.th_max[i], M.th_min[i]);
-  }
-  for (int i = lane; i < nmg; i += 32) {
-    int c = 0;
-    double f = 0.0;
-    for (int j = M.mg_off[i]; j < M.mg_off[i + 1]; j++) {
-      c += s_mc[warp][M.mg_idx[j]];
-      f += s_fm[warp][M.mg_idx[j]];
-    }
-    s_m[warp][i] = M.expo ? ig.mig_expo(c, f, M.mg_mean[i]) : ig.mig(c, f, M.mg_max[i], M.mg_min[i]);
   }
   if (__any_sync(~0u, ig.st != 0)) {
     const int code = __reduce_max_sync(~0u, ig.st);
@@ -648,49 +691,44 @@ __global__ void __launch_bounds__(32 * TP_WPB) k_tree_prob(TwProbArgs a)
 
 }  // namespace
 
-size_t tw_smem_per_genealogy(int P, const TwModel &h)
-{
-  const size_t b = (size_t)P * 12 + (size_t)(h.T + h.M) * 12;
-  return (b + 15) / 16 * 16;
-}
+size_t tw_stage_bytes(const TwModel &h) { return ((size_t)(h.T + h.M) * 12 + 15) / 16 * 16; }
 
-int tw_group_width(int P, const TwModel &h)
-{
-  int gw = 2;
-  while (gw < h.npops) gw <<= 1;
-  while (gw < 32 && (32 / gw) * tw_smem_per_genealogy(P, h) > 200 * 1024) gw <<= 1;
-  return (32 / gw) * tw_smem_per_genealogy(P, h) > 200 * 1024 ? 0 : gw;
-}
+bool tw_fits(int P) { return (size_t)P * 12 <= 200 * 1024; }
 
 template <int GW>
-static int launch_tw(const TwArgs &a, const TwModel &h, cudaStream_t st)
+static void launch_sweep(const TwArgs &a, const TwModel &h, cudaStream_t st)
 {
-  const size_t per = tw_smem_per_genealogy(a.P, h);
-  const size_t warp_bytes = per * (32 / GW);
-  int wpb = (int)((200 * 1024) / warp_bytes);
-  wpb = wpb < 1 ? 1 : (wpb > TW_WPB ? TW_WPB : wpb);
-  const size_t smem = warp_bytes * wpb;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_treeweight<GW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return 2;
-  }
+  const size_t per = tw_stage_bytes(h);
+  const int wpb = TW_WPB;
+  const size_t smem = per * (32 / GW) * wpb;
   const int per_block = wpb * (32 / GW);
-  const int grid = (a.ngen + per_block - 1) / per_block;
-  k_treeweight<GW><<<grid, 32 * wpb, smem, st>>>(a, wpb, (int)per);
-  return 0;
+  k_tw_sweep<GW><<<(a.ngen + per_block - 1) / per_block, 32 * wpb, smem, st>>>(a, wpb, (int)per);
 }
 
 int launch_treeweight(const TwArgs &a, const TwModel &h, cudaStream_t st)
 {
   if (a.ngen < 1) return 0;
-  switch (tw_group_width(a.P, h)) {
-    case 2: return launch_tw<2>(a, h, st);
-    case 4: return launch_tw<4>(a, h, st);
-    case 8: return launch_tw<8>(a, h, st);
-    case 16: return launch_tw<16>(a, h, st);
-    case 32: return launch_tw<32>(a, h, st);
-    default: return 1;
+  if (!tw_fits(a.P)) return 1;
+  // pass 1: a warp per genealogy, P events of shared memory per warp
+  const size_t wbytes = (size_t)a.P * 12;
+  int wpb = (int)((200 * 1024) / wbytes);
+  wpb = wpb < 1 ? 1 : (wpb > TW_WPB ? TW_WPB : wpb);
+  const size_t smem = wbytes * wpb;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_tw_events, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return 2;
   }
+  k_tw_events<<<(a.ngen + wpb - 1) / wpb, 32 * wpb, smem, st>>>(a, wpb);
+  // pass 2: lane groups
+  int gw = 2;
+  while (gw < h.npops) gw <<= 1;
+  switch (gw) {
+    case 2: launch_sweep<2>(a, h, st); break;
+    case 4: launch_sweep<4>(a, h, st); break;
+    case 8: launch_sweep<8>(a, h, st); break;
+    default: launch_sweep<16>(a, h, st); break;
+  }
+  return 0;
 }
 
 int launch_tree_prob(const TwProbArgs &a, cudaStream_t st)
