@@ -2220,7 +2220,8 @@ extern "C" int ima_gpu_tree_prob(ima_ctx *c, int ngroups, const int32_t *group_o
   if (pdg) r = r ? r : c->cuda(cudaMemcpyAsync(d_pdg, pdg, G * 8, cudaMemcpyHostToDevice, c->st), "tree_prob pdg");
   r = r ? r : c->cuda(cudaMemsetAsync(c->d_twerr, 0, 8, c->st), "tree_prob");
   if (r) return r;
-  c->launch(IMA_K_TREE_PROB, (double)c->tw_ngen * (h.T * 20 + h.M * 12), [&] { launch_tree_prob(a, c->st); });
+  c->launch(IMA_K_TREE_PROB, (double)c->tw_ngen * (h.T * 20 + h.M * 12), [&] { launch_tree_prob(a, h, c->st); });
+  c->launches += 1;  // parameters + final
   r = c->cuda(cudaGetLastError(), "tree_prob launch");
   r = r ? r : tw_check_err(c, "tree_prob");
   if (r) return r;

@@ -191,4 +191,4 @@ struct TwProbArgs {
 };
 bool tw_fits(int P);                       // P events fit one warp's shared memory
 int launch_treeweight(const TwArgs &a, const TwModel &h, cudaStream_t st);
-int launch_tree_prob(const TwProbArgs &a, cudaStream_t st);
+int launch_tree_prob(const TwProbArgs &a, const TwModel &h, cudaStream_t st);

@@ -19,13 +19,15 @@
 // FP64 at 1/64 of the FP32 rate), which is why genealogies share warps
 // rather than each taking a warp of mostly idle lanes.
 //
-// k_tree_prob restates sum_treeinfo (ginfo.cpp:209-244) over a chain's loci
-// in locus order, initialize_integrate_tree_prob (update_gtree_common.cpp:
-// 2089-2134) with the integral terms (:108-304, MORESTABLE) on the
-// reference's incomplete gamma functions (utilities.cpp:808-1130), and
-// optionally savegsampinf (ginfo.cpp:318-377): one warp per chain, a lane per
-// weight cell and then a lane per parameter.  The integrals use the device's
-// log/exp, so they agree with the host's to rounding, not bit for bit.
+// k_tp_params / k_tp_final restate sum_treeinfo (ginfo.cpp:209-244) over a
+// chain's loci in locus order, initialize_integrate_tree_prob
+// (update_gtree_common.cpp:2089-2134) with the integral terms (:108-304,
+// MORESTABLE) on the reference's incomplete gamma functions
+// (utilities.cpp:808-1130), and optionally savegsampinf (ginfo.cpp:318-377):
+// a warp per (chain, parameter) sums that parameter's cells and evaluates
+// its integral, then a lane per chain adds the integrals in parameter order.
+// The integrals use the device's log/exp, so they agree with the host's to
+// rounding, not bit for bit.
 #include "internal.h"
 
 #include <cfloat>
@@ -193,7 +195,14 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_tw_events(TwArgs a, int wpb)
 // genealogies per warp, taken in the order perm gives (most events first) so
 // that a warp's groups sweep about as many events each.  Lane l of a group
 // owns population l of the current period.
-template <int GW>
+//
+// With MERGE (npops < GW: a group lane without a population), lane npops
+// carries G->length and G->tlength through the same two multiply-adds the
+// population lanes use for fc and fm -- length += (nsum * dt) * 1.0 and
+// tlength += nsum * d with d = dt before the last split, lastsplitt - lasttime
+// across it and 0 after it, each factor exact -- so the FP64 pipe does 8
+// operations per event instead of 12, with the reference's values.
+template <int GW, bool MERGE>
 __global__ void __launch_bounds__(32 * TW_WPB) k_tw_sweep(TwArgs a, int wpb, int gbytes)
 {
   extern __shared__ __align__(16) unsigned char sm[];
@@ -233,7 +242,7 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_tw_sweep(TwArgs a, int wpb, int
   __syncwarp(gmask);
   auto flush = [&](int kk) {
     const int w = npops - kk;
-    if (gl < w) {
+    if (gl < w && !(MERGE && gl == npops)) {
       fc_s[M.toff[kk] + gl] = accfc;
       cc_s[M.toff[kk] + gl] = ccm;
       if (!M.nomig && kk < nsplit)
@@ -241,6 +250,7 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_tw_sweep(TwArgs a, int wpb, int
           if (jj != gl) fm_s[M.moff[kk] + gl * w + jj] = accfm;
     }
   };
+  const bool lenlane = MERGE && gl == npops;
   double tn = E > 0 ? et[0] : 0.0;
   uint32_t cn = E > 0 ? ec[0] : 0u;
   for (int j = 0; j < E; j++) {
@@ -251,20 +261,36 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_tw_sweep(TwArgs a, int wpb, int
       cn = ec[j + 1];
     }
     const double dt = t - last;
-    const double tadd = nsum * dt;
-    len += tadd;
-    if (__double_as_longlong(t) < lsb)
-      tlen += tadd;
-    else if (__double_as_longlong(last) < lsb)
-      tlen += nsum * (lastsplitt - last);
-    last = t;
+    const bool before = __double_as_longlong(t) < lsb, lbefore = __double_as_longlong(last) < lsb;
     const int w = npops - k;
-    if (gl < w) {
+    if constexpr (MERGE) {
       // n(n-1) is exact in an int and in a double, so converting the
       // product equals the reference's (double)n * ((double)n - 1)
-      accfc += (double)(nmine * (nmine - 1)) * dt * h2;
-      if (!M.nomig && k < nsplit) accfm += nmine * dt;
+      if (gl < w || lenlane) {
+        double d2;
+        if (lenlane) {
+          d2 = before ? dt : 0.0;
+          if (!before && lbefore) d2 = lastsplitt - last;
+        } else {
+          d2 = (!M.nomig && k < nsplit) ? dt : 0.0;
+        }
+        const int x1 = lenlane ? nsum : nmine * (nmine - 1), x2 = lenlane ? nsum : nmine;
+        accfc += (double)x1 * dt * (lenlane ? 1.0 : h2);  // lenlane: length
+        accfm += (double)x2 * d2;                         // lenlane: tlength
+      }
+    } else {
+      const double tadd = nsum * dt;
+      len += tadd;
+      if (before)
+        tlen += tadd;
+      else if (lbefore)
+        tlen += nsum * (lastsplitt - last);
+      if (gl < w) {
+        accfc += (double)(nmine * (nmine - 1)) * dt * h2;
+        if (!M.nomig && k < nsplit) accfm += nmine * dt;
+      }
     }
+    last = t;
     const int type = (int)(c >> 30);
     int lbad = 0;
     if (type == EV_COAL) {
@@ -309,8 +335,10 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_tw_sweep(TwArgs a, int wpb, int
         const int v1 = __shfl_sync(gmask, nmine, s1 < 0 ? 0 : s1, GW);
         nmine = gl < npops - k1 ? v0 + (s1 >= 0 ? v1 : 0) : 0;
         k = k1;
-        accfc = accfm = 0.0;
-        ccm = 0;
+        if (!lenlane) {
+          accfc = accfm = 0.0;
+          ccm = 0;
+        }
       }
     }
     if (__any_sync(gmask, lbad)) bad = TW_E_COUNT;
@@ -323,6 +351,10 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_tw_sweep(TwArgs a, int wpb, int
   }
   flush(k);
   __syncwarp(gmask);
+  if (lenlane) {
+    len = accfc;
+    tlen = accfm;
+  }
   const size_t oT = (size_t)g * T, oM = (size_t)g * MM;
   for (int i = gl; i < T; i += GW) {
     a.cc[oT + i] = cc_s[i];
@@ -333,7 +365,7 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_tw_sweep(TwArgs a, int wpb, int
     a.mc[oM + i] = mc_s[i];
     a.fm[oM + i] = fm_s[i];
   }
-  if (gl == 0) {
+  if (gl == (MERGE ? npops : 0)) {
     a.lens[2 * (size_t)g] = len;
     a.lens[2 * (size_t)g + 1] = tlen;
     a.mignum[g] = a.mig_off[a0 + nl] - a.mig_off[a0];
@@ -568,124 +600,112 @@ struct Ig {
 
 constexpr int TP_WPB = 4;
 
-__global__ void __launch_bounds__(32 * TP_WPB) k_tree_prob(TwProbArgs a)
+// Pass 1 of p(G): one warp per (chain, parameter).  Lane 3j+q sums quantity q
+// (counts, then f, then h for theta; counts, then f for migration) of the
+// parameter's j-th cell over the chain's genealogies in order -- sum_treeinfo's
+// order for that cell -- and lane 0 adds the cells in the parameter's order
+// and evaluates its integral; it also writes the parameter's entries of the
+// gsampinf row (float sums, as savegsampinf makes them).
+__global__ void __launch_bounds__(32 * TP_WPB) k_tp_params(TwProbArgs a)
 {
-  __shared__ int s_cc[TP_WPB][TW_MAXT], s_mc[TP_WPB][TW_MAXM];
-  __shared__ double s_fc[TP_WPB][TW_MAXT], s_hcc[TP_WPB][TW_MAXT], s_fm[TP_WPB][TW_MAXM];
-  __shared__ double s_q[TP_WPB][TW_MAXTH], s_m[TP_WPB][TW_MAXMG];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int grp = blockIdx.x * TP_WPB + warp;
+  const TwModel &M = *a.model;
+  const int nth = M.nth, nmg = M.nomig ? 0 : M.nmg, npar = nth + nmg;
+  const long long wid = (long long)blockIdx.x * TP_WPB + warp;
+  if (wid >= (long long)a.ngroups * npar) return;
+  const int grp = (int)(wid / npar), p = (int)(wid % npar);
+  const bool th = p < nth;
+  const int i = th ? p : p - nth;
+  const int c0 = th ? M.th_off[i] : M.mg_off[i], nc = (th ? M.th_off[i + 1] : M.mg_off[i + 1]) - c0;
+  const int T = M.T, MM = M.M;
+  const int g0 = a.group_off[grp], g1 = a.group_off[grp + 1];
+  // lanes: cell j = lane / 3, quantity q = lane % 3 (0 count, 1 f, 2 h)
+  const int j = lane / 3, q = lane % 3;
+  int csum = 0;
+  double dsum = 0.0;
+  if (j < nc && (th || q < 2)) {
+    const int cell = th ? M.th_idx[c0 + j] : M.mg_idx[c0 + j];
+    if (q == 0) {
+      const int32_t *src = (th ? a.cc + cell : a.mc + cell);
+      const int stride = th ? T : MM;
+#pragma unroll 8
+      for (int g = g0; g < g1; g++) csum += src[(size_t)g * stride];
+    } else {
+      const double *src = th ? (q == 1 ? a.fc : a.hcc) + cell : a.fm + cell;
+      const int stride = th ? T : MM;
+#pragma unroll 8
+      for (int g = g0; g < g1; g++) dsum += src[(size_t)g * stride];
+    }
+  }
+  // lane 0 gathers the cells in the parameter's order
+  int c = 0;
+  double f = 0.0, hc = 0.0;
+  float ff = 0.0f, hf = 0.0f;
+  for (int jj = 0; jj < nc; jj++) {
+    const int cj = __shfl_sync(~0u, csum, 3 * jj);
+    const double fj = __shfl_sync(~0u, dsum, 3 * jj + 1);
+    const double hj = __shfl_sync(~0u, dsum, 3 * jj + 2);
+    c += cj;
+    f += fj;
+    hc += hj;
+    ff += (float)fj;
+    hf += (float)hj;
+  }
+  if (lane != 0) return;
+  Ig ig{a.logfact, 0};
+  const double v = th ? ig.coal(c, f, hc, M.th_max[i], M.th_min[i])
+                      : (M.expo ? ig.mig_expo(c, f, M.mg_mean[i]) : ig.mig(c, f, M.mg_max[i], M.mg_min[i]));
+  if (ig.st) tw_fail(a.err, ig.st, grp);
+  if (th)
+    a.q[(size_t)grp * nth + i] = v;
+  else
+    a.m[(size_t)grp * nmg + i] = v;
+  if (a.rows) {  // ccp 0, fcp nth, hccp 2nth, mcp 3nth, fmp mcp+nmg, qip fmp+nmg, mip qip+nth
+    float *row = a.rows + (size_t)grp * a.rowlen;
+    if (th) {
+      row[i] = (float)c;
+      row[nth + i] = ff;
+      row[2 * nth + i] = hf;
+      row[3 * nth + 2 * nmg + i] = (float)v;
+    } else {
+      row[3 * nth + i] = (float)c;
+      row[3 * nth + nmg + i] = ff;
+      row[4 * nth + 2 * nmg + i] = (float)v;
+    }
+  }
+}
+
+// Pass 2 of p(G): one lane per chain.  probg = the integrals added in
+// parameter order (initialize_integrate_tree_prob), or -DBL_MAX when a
+// cell of nomigrationchecklist holds a migration; the rest of the row.
+__global__ void __launch_bounds__(128) k_tp_final(TwProbArgs a)
+{
+  const int grp = blockIdx.x * blockDim.x + threadIdx.x;
   if (grp >= a.ngroups) return;
   const TwModel &M = *a.model;
-  const int T = M.T, MM = M.M, nth = M.nth, nmg = M.nomig ? 0 : M.nmg;
-  const int g0 = a.group_off[grp], g1 = a.group_off[grp + 1];
-  // sum_treeinfo over the chain's genealogies, in order, from zero
-  for (int i = lane; i < T; i += 32) {
-    int c = 0;
-    double f = 0.0, h = 0.0;
-#pragma unroll 8
-    for (int g = g0; g < g1; g++) {
-      c += a.cc[(size_t)g * T + i];
-      f += a.fc[(size_t)g * T + i];
-      h += a.hcc[(size_t)g * T + i];
-    }
-    s_cc[warp][i] = c;
-    s_fc[warp][i] = f;
-    s_hcc[warp][i] = h;
-  }
+  const int nth = M.nth, nmg = M.nomig ? 0 : M.nmg;
+  bool checkm = true;
   if (!M.nomig)
-    for (int i = lane; i < MM; i += 32) {
-      int c = 0;
-      double f = 0.0;
-#pragma unroll 8
-      for (int g = g0; g < g1; g++) {
-        c += a.mc[(size_t)g * MM + i];
-        f += a.fm[(size_t)g * MM + i];
-      }
-      s_mc[warp][i] = c;
-      s_fm[warp][i] = f;
+    for (int i = 0; i < M.nchk && checkm; i++) {
+      int cnt = 0;
+      for (int g = a.group_off[grp]; g < a.group_off[grp + 1]; g++) cnt += a.mc[(size_t)g * M.M + M.chk_idx[i]];
+      checkm = cnt == 0;
     }
-  __syncwarp();
-  Ig ig{a.logfact, 0};
-  // one lane per parameter: theta parameters, then migration rates
-  for (int p = lane; p < nth + nmg; p += 32) {
-    if (p < nth) {
-      const int i = p;
-      int c = 0;
-      double f = 0.0, hc = 0.0;
-      for (int j = M.th_off[i]; j < M.th_off[i + 1]; j++) {
-        c += s_cc[warp][M.th_idx[j]];
-        f += s_fc[warp][M.th_idx[j]];
-        hc += s_hcc[warp][M.th_idx[j]];
-      }
-      s_q[warp][i] = ig.coal(c, f, hc, M.th_max[i], M.th_min[i]);
-    } else {
-      const int i = p - nth;
-      int c = 0;
-      double f = 0.0;
-      for (int j = M.mg_off[i]; j < M.mg_off[i + 1]; j++) {
-        c += s_mc[warp][M.mg_idx[j]];
-        f += s_fm[warp][M.mg_idx[j]];
-      }
-      s_m[warp][i] = M.expo ? ig.mig_expo(c, f, M.mg_mean[i]) : ig.mig(c, f, M.mg_max[i], M.mg_min[i]);
-    }
+  double psum = 0;
+  if (!checkm) {
+    psum = -DBL_MAX;  // the reference's rejection value (MYDBL_MAX)
+  } else {
+    for (int i = 0; i < nth; i++) psum += a.q[(size_t)grp * nth + i];
+    for (int i = 0; i < nmg; i++) psum += a.m[(size_t)grp * nmg + i];
   }
-  if (__any_sync(~0u, ig.st != 0)) {
-    const int code = __reduce_max_sync(~0u, ig.st);
-    if (lane == 0) tw_fail(a.err, code, grp);
-    return;
-  }
-  __syncwarp();
-  if (lane == 0) {
-    bool checkm = true;
-    if (!M.nomig)
-      for (int i = 0; i < M.nchk && checkm; i++) checkm = s_mc[warp][M.chk_idx[i]] == 0;
-    double psum = 0;
-    if (!checkm) {
-      psum = -DBL_MAX;  // the reference's rejection value (MYDBL_MAX)
-    } else {
-      for (int i = 0; i < nth; i++) psum += s_q[warp][i];
-      for (int i = 0; i < nmg; i++) psum += s_m[warp][i];
-    }
-    a.probg[grp] = psum;
-  }
-  for (int i = lane; i < nth; i += 32) a.q[(size_t)grp * nth + i] = s_q[warp][i];
-  for (int i = lane; i < nmg; i += 32) a.m[(size_t)grp * nmg + i] = s_m[warp][i];
-  if (a.rows) {  // savegsampinf: float sums in parameter order
+  a.probg[grp] = psum;
+  if (a.rows) {
     float *row = a.rows + (size_t)grp * a.rowlen;
-    const int ccp = 0, fcp = nth, hccp = 2 * nth, mcp = 3 * nth, fmp = mcp + nmg, qip = fmp + nmg,
-              mip = qip + nth, pdgp = mip + nmg, probgp = pdgp + 1, tp = probgp + 1;
-    for (int i = lane; i < nth; i += 32) {
-      int c = 0;
-      float f = 0.0f, hc = 0.0f;
-      for (int j = M.th_off[i]; j < M.th_off[i + 1]; j++) {
-        c += s_cc[warp][M.th_idx[j]];
-        f += (float)s_fc[warp][M.th_idx[j]];
-        hc += (float)s_hcc[warp][M.th_idx[j]];
-      }
-      row[ccp + i] = (float)c;
-      row[fcp + i] = f;
-      row[hccp + i] = hc;
-      row[qip + i] = (float)s_q[warp][i];
-    }
-    for (int i = lane; i < nmg; i += 32) {
-      int c = 0;
-      float f = 0.0f;
-      for (int j = M.mg_off[i]; j < M.mg_off[i + 1]; j++) {
-        c += s_mc[warp][M.mg_idx[j]];
-        f += (float)s_fm[warp][M.mg_idx[j]];
-      }
-      row[mcp + i] = (float)c;
-      row[fmp + i] = f;
-      row[mip + i] = (float)s_m[warp][i];
-    }
-    __syncwarp();
-    if (lane == 0) {
-      row[pdgp] = a.pdg ? (float)a.pdg[grp] : 0.0f;
-      row[probgp] = (float)a.probg[grp];
-    }
+    const int pdgp = 4 * nth + 3 * nmg, probgp = pdgp + 1, tp = probgp + 1;
+    row[pdgp] = a.pdg ? (float)a.pdg[grp] : 0.0f;
+    row[probgp] = (float)psum;
     const double *tv = a.tvals + (size_t)a.group_tv[grp] * (M.npops - 1);
-    for (int i = lane; i < M.npops - 1; i += 32) row[tp + i] = (float)tv[i];
+    for (int i = 0; i < M.npops - 1; i++) row[tp + i] = (float)tv[i];
   }
 }
 
@@ -695,14 +715,14 @@ size_t tw_stage_bytes(const TwModel &h) { return ((size_t)(h.T + h.M) * 12 + 15)
 
 bool tw_fits(int P) { return (size_t)P * 12 <= 200 * 1024; }
 
-template <int GW>
+template <int GW, bool MERGE>
 static void launch_sweep(const TwArgs &a, const TwModel &h, cudaStream_t st)
 {
   const size_t per = tw_stage_bytes(h);
   const int wpb = TW_WPB;
   const size_t smem = per * (32 / GW) * wpb;
   const int per_block = wpb * (32 / GW);
-  k_tw_sweep<GW><<<(a.ngen + per_block - 1) / per_block, 32 * wpb, smem, st>>>(a, wpb, (int)per);
+  k_tw_sweep<GW, MERGE><<<(a.ngen + per_block - 1) / per_block, 32 * wpb, smem, st>>>(a, wpb, (int)per);
 }
 
 int launch_treeweight(const TwArgs &a, const TwModel &h, cudaStream_t st)
@@ -722,18 +742,23 @@ int launch_treeweight(const TwArgs &a, const TwModel &h, cudaStream_t st)
   // pass 2: lane groups
   int gw = 2;
   while (gw < h.npops) gw <<= 1;
+  // a spare lane (npops < gw) takes the length sums: fewer FP64 operations
+  // per event; with none, every lane computes them alongside
+  const bool merge = h.npops < gw;
   switch (gw) {
-    case 2: launch_sweep<2>(a, h, st); break;
-    case 4: launch_sweep<4>(a, h, st); break;
-    case 8: launch_sweep<8>(a, h, st); break;
-    default: launch_sweep<16>(a, h, st); break;
+    case 2: launch_sweep<2, false>(a, h, st); break;
+    case 4: merge ? launch_sweep<4, true>(a, h, st) : launch_sweep<4, false>(a, h, st); break;
+    case 8: merge ? launch_sweep<8, true>(a, h, st) : launch_sweep<8, false>(a, h, st); break;
+    default: merge ? launch_sweep<16, true>(a, h, st) : launch_sweep<16, false>(a, h, st); break;
   }
   return 0;
 }
 
-int launch_tree_prob(const TwProbArgs &a, cudaStream_t st)
+int launch_tree_prob(const TwProbArgs &a, const TwModel &h, cudaStream_t st)
 {
   if (a.ngroups < 1) return 0;
-  k_tree_prob<<<(a.ngroups + TP_WPB - 1) / TP_WPB, 32 * TP_WPB, 0, st>>>(a);
+  const long long warps = (long long)a.ngroups * (h.nth + (h.nomig ? 0 : h.nmg));
+  k_tp_params<<<(unsigned)((warps + TP_WPB - 1) / TP_WPB), 32 * TP_WPB, 0, st>>>(a);
+  k_tp_final<<<(a.ngroups + 127) / 128, 128, 0, st>>>(a);
   return 0;
 }
