@@ -48,6 +48,7 @@ EXPORTS = [
     "ima_gpu_timer_begin", "ima_gpu_timer_end",
     "ima_gpu_set_profiling", "ima_gpu_kernel_stats", "ima_gpu_launch_count", "ima_gpu_flush_l2",
     "ima_gpu_memory", "ima_gpu_set_popmodel", "ima_gpu_treeweight", "ima_gpu_tree_prob",
+    "ima_gpu_surface_append_tree_rows", "ima_gpu_surface_get_rows",
 ]
 
 
@@ -174,6 +175,8 @@ def _declare(L):
         "ima_gpu_set_popmodel": (I, [P, I, I, I, P, P, P, P, P, I, P, P, P, P, I, P, P, P, P, P, I, P]),
         "ima_gpu_treeweight": (I, [P, I, P, P, P, P, P, P, P, P, P, I, P, P, I, P, P, P, P, P, P, P, P]),
         "ima_gpu_tree_prob": (I, [P, I, P, P, P, P, P, P, P]),
+        "ima_gpu_surface_append_tree_rows": (I, [P, I, P]),
+        "ima_gpu_surface_get_rows": (I, [P, I, I, I, P]),
         "ima_gpu_fillvec": (I, [P, I, P, P, P, P, P]),
         "ima_gpu_batch_set_variants": (I, [P, I, I, I]),
         "ima_gpu_set_allele_edits": (I, [P, I, P, P, P, P, P]),
@@ -495,6 +498,24 @@ class Context:
                                             _ptr(gtv) if gtv is not None else None, _ptr(probg), _ptr(q),
                                             _ptr(m), _ptr(rowbuf) if rows else None))
         return probg, q, m[:, :nmg], rowbuf
+
+    def surface_append_tree_rows(self, groups):
+        """Append the gsampinf rows of these chains (last tree_prob) to the
+        resident surface."""
+        groups = _i32(np.atleast_1d(groups))
+        self._ck(self.lib.ima_gpu_surface_append_tree_rows(self.h, len(groups), _ptr(groups)))
+        _, np_, nm, _ = self.surface_info()
+        self.surf_npar = np_ + nm
+
+    def surface_get_rows(self, start=0, count=None, rowlen=None):
+        """Surface rows [start, start+count) ([count][rowlen]; rowlen defaults
+        to gsampinf's 4np + 3nm + 2 + npops-1)."""
+        G, np_, nm, npops = self.surface_info()
+        count = G - start if count is None else count
+        rowlen = 4 * np_ + 3 * nm + 2 + npops - 1 if rowlen is None else rowlen
+        out = np.zeros((count, rowlen), np.float32)
+        self._ck(self.lib.ima_gpu_surface_get_rows(self.h, int(start), int(count), int(rowlen), _ptr(out)))
+        return out
 
     def fillvec(self, pmin, pmax, gridsize=1000, expo_mean=None):
         n = len(pmin)

@@ -234,6 +234,9 @@ struct ima_ctx {
   void *d_twin = nullptr, *d_twout = nullptr, *d_tpbuf = nullptr;
   size_t twin_cap = 0, twout_cap = 0, tpbuf_cap = 0;
   int tw_ngen = 0, tw_ntv = 0;
+  float *tp_rows = nullptr;  // gsampinf rows of the last ima_gpu_tree_prob
+  int tp_ngroups = 0, tp_rowlen = 0;
+  size_t s_cap = 0;          // surface row capacity (rows appended on the device)
   int32_t *tw_cc = nullptr, *tw_mc = nullptr;
   double *tw_hcc = nullptr, *tw_fc = nullptr, *tw_fm = nullptr, *tw_tvals = nullptr;
 
@@ -1526,6 +1529,7 @@ extern "C" int ima_gpu_surface_load(ima_ctx *c, int G, int rowlen, const float *
     if (!c->d_lognorm) return c->fail(IMA_ERR_NOMEM, "surface normalisers");
   }
   c->srows_state = 0;
+  c->s_cap = (size_t)G;
   c->sG = G;
   c->srowlen = rowlen;
   c->snp = np;
@@ -2187,7 +2191,7 @@ extern "C" int ima_gpu_tree_prob(ima_ctx *c, int ngroups, const int32_t *group_o
   cudaSetDevice(c->device);
   const size_t G = ngroups;
   const size_t b = carve_size({(G + 1) * 4, G * 4, G * 8, G * 8, G * nth * 8, G * (nmg ? nmg : 1) * 8,
-                               rows ? G * rowlen * 4 : 4});
+                               G * rowlen * 4});
   int r = grow(c, &c->d_tpbuf, &c->tpbuf_cap, b, "tree_prob buffers");
   if (r) return r;
   Carve cv{static_cast<char *>(c->d_tpbuf)};
@@ -2202,7 +2206,7 @@ extern "C" int ima_gpu_tree_prob(ima_ctx *c, int ngroups, const int32_t *group_o
   a.probg = cv.take<double>(G);
   a.q = cv.take<double>(G * nth);
   a.m = cv.take<double>(G * (nmg ? nmg : 1));
-  a.rows = rows ? cv.take<float>(G * rowlen) : nullptr;
+  a.rows = cv.take<float>(G * rowlen);  // kept for ima_gpu_surface_append_tree_rows
   a.rowlen = rowlen;
   a.cc = c->tw_cc;
   a.mc = c->tw_mc;
@@ -2220,11 +2224,15 @@ extern "C" int ima_gpu_tree_prob(ima_ctx *c, int ngroups, const int32_t *group_o
   if (pdg) r = r ? r : c->cuda(cudaMemcpyAsync(d_pdg, pdg, G * 8, cudaMemcpyHostToDevice, c->st), "tree_prob pdg");
   r = r ? r : c->cuda(cudaMemsetAsync(c->d_twerr, 0, 8, c->st), "tree_prob");
   if (r) return r;
+  c->tp_ngroups = 0;
   c->launch(IMA_K_TREE_PROB, (double)c->tw_ngen * (h.T * 20 + h.M * 12), [&] { launch_tree_prob(a, h, c->st); });
   c->launches += 1;  // parameters + final
   r = c->cuda(cudaGetLastError(), "tree_prob launch");
   r = r ? r : tw_check_err(c, "tree_prob");
   if (r) return r;
+  c->tp_rows = a.rows;
+  c->tp_ngroups = ngroups;
+  c->tp_rowlen = rowlen;
   auto down = [&](void *dst, const void *src, size_t bytes) {
     if (!r && dst && bytes) r = c->cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->st), "tree_prob outputs");
   };
@@ -2233,4 +2241,68 @@ extern "C" int ima_gpu_tree_prob(ima_ctx *c, int ngroups, const int32_t *group_o
   if (nmg) down(m, a.m, G * nmg * 8);
   if (rows) down(rows, a.rows, G * rowlen * 4);
   return r ? r : c->cuda(cudaStreamSynchronize(c->st), "tree_prob");
+}
+
+extern "C" int ima_gpu_surface_append_tree_rows(ima_ctx *c, int n, const int32_t *groups)
+{
+  if (!c || n < 1 || !groups) return IMA_ERR_ARG;
+  if (c->tp_ngroups < 1) return c->fail(IMA_ERR_STATE, "call ima_gpu_tree_prob first");
+  for (int i = 0; i < n; i++)
+    if (groups[i] < 0 || groups[i] >= c->tp_ngroups)
+      return c->fail(IMA_ERR_ARG, "groups[%d] = %d: the last tree_prob had %d chains", i, groups[i], c->tp_ngroups);
+  const TwModel &h = c->h_tw;
+  const int np = h.nth, nm = h.nomig ? 0 : h.nmg, rowlen = c->tp_rowlen;
+  if (np + nm > 32 || rowlen > 64)
+    return c->fail(IMA_ERR_ARG, "a surface holds at most 32 parameters and 64 columns (here %d, %d)", np + nm, rowlen);
+  if (c->d_rows && (c->srowlen != rowlen || c->snp != np || c->snm != nm || c->snpops != h.npops))
+    return c->fail(IMA_ERR_STATE, "the resident surface holds rows of another model; load or append to a new context");
+  if (c->d_lognorm) return c->fail(IMA_ERR_STATE, "the resident surface has per-genealogy normalisers; rows cannot be added");
+  cudaSetDevice(c->device);
+  const size_t need = (size_t)(c->d_rows ? c->sG : 0) + n;
+  if (need >= (size_t)(1 << 24)) return c->fail(IMA_ERR_TOO_LARGE, "surface rows beyond 2^24");
+  if (!c->d_rows || need > c->s_cap) {
+    size_t cap = c->s_cap ? c->s_cap * 2 : 1024;
+    while (cap < need) cap *= 2;
+    float *nr = dev_alloc<float>(cap * rowlen, c->dev_bytes, c->st);
+    if (!nr) return c->fail(IMA_ERR_NOMEM, "surface rows (%zu)", cap);
+    if (c->d_rows) {
+      int r = c->cuda(cudaMemcpyAsync(nr, c->d_rows, (size_t)c->sG * rowlen * 4, cudaMemcpyDeviceToDevice, c->st), "surface grow");
+      if (r) return r;
+      cudaStreamSynchronize(c->st);
+      cudaFree(c->d_rows);
+    } else {
+      c->sG = 0;
+    }
+    c->d_rows = nr;
+    c->s_cap = cap;
+    c->srowlen = rowlen;
+    c->snp = np;
+    c->snm = nm;
+    c->snpops = h.npops;
+  }
+  int32_t *d_groups = nullptr;
+  int r = c->cuda(cudaMallocAsync((void **)&d_groups, (size_t)n * 4, c->st), "append groups");
+  r = r ? r : c->cuda(cudaMemcpyAsync(d_groups, groups, (size_t)n * 4, cudaMemcpyHostToDevice, c->st), "append groups");
+  if (r) return r;
+  launch_gather_rows(c->tp_rows, rowlen, d_groups, n, c->d_rows + (size_t)c->sG * rowlen, c->st);
+  c->launches += 1;
+  r = c->cuda(cudaGetLastError(), "append rows");
+  cudaFreeAsync(d_groups, c->st);
+  r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "append rows");
+  if (r) return r;
+  c->sG += n;
+  c->srows_state = 0;  // row-derived surface operands are stale
+  return IMA_OK;
+}
+
+extern "C" int ima_gpu_surface_get_rows(ima_ctx *c, int start, int count, int rowlen, float *rows)
+{
+  if (!c || !rows || start < 0 || count < 0) return IMA_ERR_ARG;
+  if (!c->d_rows) return c->fail(IMA_ERR_STATE, "no surface rows");
+  if (rowlen != c->srowlen) return c->fail(IMA_ERR_ARG, "rowlen %d: the surface's rows hold %d values", rowlen, c->srowlen);
+  if (start + count > c->sG) return c->fail(IMA_ERR_ARG, "rows %d..%d beyond the %d held", start, start + count, c->sG);
+  cudaSetDevice(c->device);
+  int r = c->cuda(cudaMemcpyAsync(rows, c->d_rows + (size_t)start * c->srowlen, (size_t)count * c->srowlen * 4,
+                                  cudaMemcpyDeviceToHost, c->st), "surface rows");
+  return r ? r : c->cuda(cudaStreamSynchronize(c->st), "surface rows");
 }

@@ -192,3 +192,4 @@ struct TwProbArgs {
 bool tw_fits(int P);                       // P events fit one warp's shared memory
 int launch_treeweight(const TwArgs &a, const TwModel &h, cudaStream_t st);
 int launch_tree_prob(const TwProbArgs &a, const TwModel &h, cudaStream_t st);
+int launch_gather_rows(const float *rows, int rowlen, const int32_t *groups, int n, float *dst, cudaStream_t st);

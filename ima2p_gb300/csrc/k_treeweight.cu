@@ -709,7 +709,24 @@ __global__ void __launch_bounds__(128) k_tp_final(TwProbArgs a)
   }
 }
 
+// rows[groups[i]] -> dst + i * rowlen (a warp per row)
+__global__ void __launch_bounds__(128) k_gather_rows(const float *rows, int rowlen, const int32_t *groups, int n,
+                                                     float *dst)
+{
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= n) return;
+  const float *src = rows + (size_t)groups[w] * rowlen;
+  for (int k = lane; k < rowlen; k += 32) dst[(size_t)w * rowlen + k] = src[k];
+}
+
 }  // namespace
+
+int launch_gather_rows(const float *rows, int rowlen, const int32_t *groups, int n, float *dst, cudaStream_t st)
+{
+  if (n < 1) return 0;
+  k_gather_rows<<<(n + 3) / 4, 128, 0, st>>>(rows, rowlen, groups, n, dst);
+  return 0;
+}
 
 size_t tw_stage_bytes(const TwModel &h) { return ((size_t)(h.T + h.M) * 12 + 15) / 16 * 16; }
 

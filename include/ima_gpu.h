@@ -301,6 +301,21 @@ int ima_gpu_treeweight(ima_ctx *ctx, int ngen, const int32_t *node_off, const in
  * reference stops in an integral term (LogDiff order, iteration limit). */
 int ima_gpu_tree_prob(ima_ctx *ctx, int ngroups, const int32_t *group_off, const double *pdg,
                       const int32_t *group_tv, double *probg, double *q, double *m, float *rows);
+/* The M-mode sampling step on the device: append the gsampinf rows of the
+ * chains groups[0..n) from the last ima_gpu_tree_prob (its rows are kept on
+ * the device whether or not they were copied out) to the resident surface,
+ * as savegsampinf appends the cold chain's row to gsampinf
+ * (savegenealogyinfo, ima_main_mpi.cpp:3096-3117).  The first append on a context without
+ * surface rows starts one with this model's shape (numpopsizeparams = nth,
+ * nummigrateparams = nmg); later appends must match it.  The surface
+ * functions (ima_gpu_surface_eval, ima_gpu_modelloop, ima_gpu_fillvec, ...)
+ * then see every appended row.  IMA_ERR_STATE: the resident surface has
+ * another shape or per-genealogy normalisers. */
+int ima_gpu_surface_append_tree_rows(ima_ctx *ctx, int n, const int32_t *groups);
+/* Copy surface rows start .. start+count to the host ([count][rowlen]), e.g.
+ * to write them with ima_ti_write_binary.  rowlen must be the surface's
+ * (IMA_ERR_ARG otherwise). */
+int ima_gpu_surface_get_rows(ima_ctx *ctx, int start, int count, int rowlen, float *rows);
 
 /* ------------------------------------------ saved genealogies (.ti files)
  * Host functions, no context.  ima_ti_read parses the reference's text

@@ -120,3 +120,45 @@ def test_genealogy_the_model_cannot_hold_is_rejected():
         ctx.treeweight(packed, gl, gt, hval, samp + 1, cs.tvals)
     with pytest.raises(api.ImaError):  # groups beyond the genealogies
         ctx.tree_prob(np.array([0, len(gl) + 1], np.int32))
+
+
+def test_mmode_rows_feed_the_resident_surface():
+    """Sampling steps on the device: each step's gsampinf rows (one per
+    chain here) are appended to the resident surface, which the L-mode
+    functions then read -- against the oracle's jointp and margincalc on the
+    same rows copied to the host."""
+    cs = CASES[1]  # 3 populations: 5 theta, 8 migration parameters, rowlen 48
+    ctx = api.Context(0)
+    _load(ctx, cs)
+    packed, gl, gt, hval, samp = _inputs(cs)
+    off = np.arange(cs.nch + 1, dtype=np.int32) * cs.nl
+    host_rows = []
+    for step in range(3):
+        ctx.treeweight(packed, gl, gt, hval, samp, cs.tvals)
+        pdg = np.linspace(-250.0, -210.0, cs.nch) - step
+        _, _, _, rows = ctx.tree_prob(off, pdg=pdg, group_tv=np.arange(cs.nch), rows=True)
+        order = [3, 0, 2, 1] if step == 1 else list(range(cs.nch))
+        ctx.surface_append_tree_rows(order[:2])
+        ctx.surface_append_tree_rows(order[2:])
+        host_rows += [rows[i] for i in order]
+    host_rows = np.array(host_rows, np.float32)
+    G, np_, nm, npops = ctx.surface_info()
+    assert (G, np_, nm, npops) == (len(host_rows), 5, 8, 3)
+    assert np.array_equal(ctx.surface_get_rows(), host_rows)
+    rng = np.random.default_rng(6)
+    pts = np.column_stack([rng.uniform(0.5, 10.0, (6, 5)), rng.uniform(0.05, 1.5, (6, 8))])
+    q, _ = ctx.surface_eval(pts, method=api.SURF_FP64)
+    want = np.array([O.jointp(host_rows, 5, 8, 3, x)[0] for x in pts])
+    np.testing.assert_allclose(q, want, rtol=1e-12)
+    for p_, x in ((0, 2.5), (4, 7.0), (7, 0.4)):
+        assert abs(ctx.margincalc(p_, x)[0] - O.margincalc(host_rows, 5, 8, p_, x)) <= 1e-12 * abs(O.margincalc(host_rows, 5, 8, p_, x))
+    with pytest.raises(api.ImaError):  # the caller's row width must be the surface's
+        ctx.surface_get_rows(rowlen=47)
+    # rows of a model with another shape are refused
+    other = CASES[0]
+    _load(ctx, other)
+    p2, gl2, gt2, hv2, sp2 = _inputs(other)
+    ctx.treeweight(p2, gl2, gt2, hv2, sp2, other.tvals)
+    ctx.tree_prob(np.arange(other.nch + 1, dtype=np.int32) * other.nl)
+    with pytest.raises(api.ImaError):
+        ctx.surface_append_tree_rows([0])
