@@ -2190,8 +2190,9 @@ extern "C" int ima_gpu_tree_prob(ima_ctx *c, int ngroups, const int32_t *group_o
   const int rowlen = 4 * nth + 3 * nmg + 2 + h.npops - 1;  // cc fc hcc mc fm qi mi pdg probg t
   cudaSetDevice(c->device);
   const size_t G = ngroups;
+  const size_t MMc = h.nomig ? 0 : h.M;
   const size_t b = carve_size({(G + 1) * 4, G * 4, G * 8, G * 8, G * nth * 8, G * (nmg ? nmg : 1) * 8,
-                               G * rowlen * 4});
+                               G * rowlen * 4, G * (h.T + MMc) * 4, G * (2 * h.T + MMc) * 8});
   int r = grow(c, &c->d_tpbuf, &c->tpbuf_cap, b, "tree_prob buffers");
   if (r) return r;
   Carve cv{static_cast<char *>(c->d_tpbuf)};
@@ -2207,6 +2208,8 @@ extern "C" int ima_gpu_tree_prob(ima_ctx *c, int ngroups, const int32_t *group_o
   a.q = cv.take<double>(G * nth);
   a.m = cv.take<double>(G * (nmg ? nmg : 1));
   a.rows = cv.take<float>(G * rowlen);  // kept for ima_gpu_surface_append_tree_rows
+  a.sc = cv.take<int32_t>(G * (h.T + MMc));
+  a.sd = cv.take<double>(G * (2 * h.T + MMc));
   a.rowlen = rowlen;
   a.cc = c->tw_cc;
   a.mc = c->tw_mc;
@@ -2226,7 +2229,7 @@ extern "C" int ima_gpu_tree_prob(ima_ctx *c, int ngroups, const int32_t *group_o
   if (r) return r;
   c->tp_ngroups = 0;
   c->launch(IMA_K_TREE_PROB, (double)c->tw_ngen * (h.T * 20 + h.M * 12), [&] { launch_tree_prob(a, h, c->st); });
-  c->launches += 1;  // parameters + final
+  c->launches += 2;  // cells, parameters, final
   r = c->cuda(cudaGetLastError(), "tree_prob launch");
   r = r ? r : tw_check_err(c, "tree_prob");
   if (r) return r;

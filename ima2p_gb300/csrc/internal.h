@@ -188,6 +188,8 @@ struct TwProbArgs {
   float *rows;                             // [ngroups][rowlen] or null
   int rowlen;
   int32_t *err;
+  int32_t *sc;                             // [ngroups][T+M] summed counts (cc, mc)
+  double *sd;                              // [ngroups][2T+M] summed fc, hcc, fm
 };
 bool tw_fits(int P);                       // P events fit one warp's shared memory
 int launch_treeweight(const TwArgs &a, const TwModel &h, cudaStream_t st);

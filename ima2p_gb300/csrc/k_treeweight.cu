@@ -24,8 +24,9 @@
 // (update_gtree_common.cpp:2089-2134) with the integral terms (:108-304,
 // MORESTABLE) on the reference's incomplete gamma functions
 // (utilities.cpp:808-1130), and optionally savegsampinf (ginfo.cpp:318-377):
-// a warp per (chain, parameter) sums that parameter's cells and evaluates
-// its integral, then a lane per chain adds the integrals in parameter order.
+// a thread per (chain, weight cell) sums the cell over the chain's loci, a
+// thread per (parameter, chain) evaluates the integral, then a thread per
+// chain adds the integrals in parameter order.
 // The integrals use the device's log/exp, so they agree with the host's to
 // rounding, not bit for bit.
 #include "internal.h"
@@ -598,68 +599,98 @@ struct Ig {
   }
 };
 
-constexpr int TP_WPB = 4;
+constexpr int TP_BS = 128;
 
-// Pass 1 of p(G): one warp per (chain, parameter).  Lane 3j+q sums quantity q
-// (counts, then f, then h for theta; counts, then f for migration) of the
-// parameter's j-th cell over the chain's genealogies in order -- sum_treeinfo's
-// order for that cell -- and lane 0 adds the cells in the parameter's order
-// and evaluates its integral; it also writes the parameter's entries of the
-// gsampinf row (float sums, as savegsampinf makes them).
-__global__ void __launch_bounds__(32 * TP_WPB) k_tp_params(TwProbArgs a)
+// p(G) runs on the FP64 pipe, which GB300 issues at 1/64 of the FP32 rate:
+// the work is packed densely into lanes so that every FP64 instruction
+// carries 32 useful operations.
+//
+// Pass 1: a thread per (chain, summed quantity): the chain's weights added
+// over its genealogies in order -- sum_treeinfo's order for that cell.
+// Doubles (fc, hcc, fm cells) first, then the counts (cc, mc).
+__global__ void __launch_bounds__(TP_BS) k_tp_cells(TwProbArgs a)
 {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const TwModel &M = *a.model;
-  const int nth = M.nth, nmg = M.nomig ? 0 : M.nmg, npar = nth + nmg;
-  const long long wid = (long long)blockIdx.x * TP_WPB + warp;
-  if (wid >= (long long)a.ngroups * npar) return;
-  const int grp = (int)(wid / npar), p = (int)(wid % npar);
-  const bool th = p < nth;
-  const int i = th ? p : p - nth;
-  const int c0 = th ? M.th_off[i] : M.mg_off[i], nc = (th ? M.th_off[i + 1] : M.mg_off[i + 1]) - c0;
-  const int T = M.T, MM = M.M;
-  const int g0 = a.group_off[grp], g1 = a.group_off[grp + 1];
-  // lanes: cell j = lane / 3, quantity q = lane % 3 (0 count, 1 f, 2 h)
-  const int j = lane / 3, q = lane % 3;
-  int csum = 0;
-  double dsum = 0.0;
-  if (j < nc && (th || q < 2)) {
-    const int cell = th ? M.th_idx[c0 + j] : M.mg_idx[c0 + j];
-    if (q == 0) {
-      const int32_t *src = (th ? a.cc + cell : a.mc + cell);
-      const int stride = th ? T : MM;
-#pragma unroll 8
-      for (int g = g0; g < g1; g++) csum += src[(size_t)g * stride];
+  const int T = M.T, MM = M.nomig ? 0 : M.M;
+  const int Qd = 2 * T + MM, Qi = T + MM;
+  const long long tid = (long long)blockIdx.x * TP_BS + threadIdx.x;
+  const long long nd = (long long)a.ngroups * Qd, ni = (long long)a.ngroups * Qi;
+  if (tid < nd) {
+    const int grp = (int)(tid / Qd), q = (int)(tid % Qd);
+    const double *src;
+    int stride;
+    if (q < T) {
+      src = a.fc + q;
+      stride = T;
+    } else if (q < 2 * T) {
+      src = a.hcc + (q - T);
+      stride = T;
     } else {
-      const double *src = th ? (q == 1 ? a.fc : a.hcc) + cell : a.fm + cell;
-      const int stride = th ? T : MM;
-#pragma unroll 8
-      for (int g = g0; g < g1; g++) dsum += src[(size_t)g * stride];
+      src = a.fm + (q - 2 * T);
+      stride = M.M;
     }
+    double sum = 0.0;
+    const int g1 = a.group_off[grp + 1];
+#pragma unroll 8
+    for (int g = a.group_off[grp]; g < g1; g++) sum += src[(size_t)g * stride];
+    a.sd[(size_t)grp * Qd + q] = sum;
+  } else if (tid < nd + ni) {
+    const long long t2 = tid - nd;
+    const int grp = (int)(t2 / Qi), q = (int)(t2 % Qi);
+    const int32_t *src = q < T ? a.cc + q : a.mc + (q - T);
+    const int stride = q < T ? T : M.M;
+    int sum = 0;
+    const int g1 = a.group_off[grp + 1];
+#pragma unroll 8
+    for (int g = a.group_off[grp]; g < g1; g++) sum += src[(size_t)g * stride];
+    a.sc[(size_t)grp * Qi + q] = sum;
   }
-  // lane 0 gathers the cells in the parameter's order
+}
+
+// Pass 2: a thread per (parameter, chain), parameter-major so that a warp's
+// lanes evaluate one parameter for 32 chains (similar arguments, similar
+// series lengths): the cells added in the parameter's order, the integral,
+// and the parameter's entries of the gsampinf row (float sums, as
+// savegsampinf makes them).
+__global__ void __launch_bounds__(TP_BS) k_tp_params(TwProbArgs a)
+{
+  const TwModel &M = *a.model;
+  const int nth = M.nth, nmg = M.nomig ? 0 : M.nmg, G = a.ngroups;
+  const int T = M.T, MM = M.nomig ? 0 : M.M, Qd = 2 * T + MM, Qi = T + MM;
+  const long long tid = (long long)blockIdx.x * TP_BS + threadIdx.x;
+  if (tid >= (long long)G * (nth + nmg)) return;
+  const bool th = tid < (long long)G * nth;
+  const long long t2 = th ? tid : tid - (long long)G * nth;
+  const int i = (int)(t2 / G), grp = (int)(t2 % G);
+  const double *sd = a.sd + (size_t)grp * Qd;
+  const int32_t *sc = a.sc + (size_t)grp * Qi;
   int c = 0;
   double f = 0.0, hc = 0.0;
   float ff = 0.0f, hf = 0.0f;
-  for (int jj = 0; jj < nc; jj++) {
-    const int cj = __shfl_sync(~0u, csum, 3 * jj);
-    const double fj = __shfl_sync(~0u, dsum, 3 * jj + 1);
-    const double hj = __shfl_sync(~0u, dsum, 3 * jj + 2);
-    c += cj;
-    f += fj;
-    hc += hj;
-    ff += (float)fj;
-    hf += (float)hj;
-  }
-  if (lane != 0) return;
   Ig ig{a.logfact, 0};
-  const double v = th ? ig.coal(c, f, hc, M.th_max[i], M.th_min[i])
-                      : (M.expo ? ig.mig_expo(c, f, M.mg_mean[i]) : ig.mig(c, f, M.mg_max[i], M.mg_min[i]));
-  if (ig.st) tw_fail(a.err, ig.st, grp);
-  if (th)
+  double v;
+  if (th) {
+    for (int j = M.th_off[i]; j < M.th_off[i + 1]; j++) {
+      const int cell = M.th_idx[j];
+      c += sc[cell];
+      f += sd[cell];
+      hc += sd[T + cell];
+      ff += (float)sd[cell];
+      hf += (float)sd[T + cell];
+    }
+    v = ig.coal(c, f, hc, M.th_max[i], M.th_min[i]);
     a.q[(size_t)grp * nth + i] = v;
-  else
+  } else {
+    for (int j = M.mg_off[i]; j < M.mg_off[i + 1]; j++) {
+      const int cell = M.mg_idx[j];
+      c += sc[T + cell];
+      f += sd[2 * T + cell];
+      ff += (float)sd[2 * T + cell];
+    }
+    v = M.expo ? ig.mig_expo(c, f, M.mg_mean[i]) : ig.mig(c, f, M.mg_max[i], M.mg_min[i]);
     a.m[(size_t)grp * nmg + i] = v;
+  }
+  if (ig.st) tw_fail(a.err, ig.st, grp);
   if (a.rows) {  // ccp 0, fcp nth, hccp 2nth, mcp 3nth, fmp mcp+nmg, qip fmp+nmg, mip qip+nth
     float *row = a.rows + (size_t)grp * a.rowlen;
     if (th) {
@@ -774,8 +805,11 @@ int launch_treeweight(const TwArgs &a, const TwModel &h, cudaStream_t st)
 int launch_tree_prob(const TwProbArgs &a, const TwModel &h, cudaStream_t st)
 {
   if (a.ngroups < 1) return 0;
-  const long long warps = (long long)a.ngroups * (h.nth + (h.nomig ? 0 : h.nmg));
-  k_tp_params<<<(unsigned)((warps + TP_WPB - 1) / TP_WPB), 32 * TP_WPB, 0, st>>>(a);
+  const int MM = h.nomig ? 0 : h.M;
+  const long long cells = (long long)a.ngroups * ((2 * h.T + MM) + (h.T + MM));
+  const long long params = (long long)a.ngroups * (h.nth + (h.nomig ? 0 : h.nmg));
+  k_tp_cells<<<(unsigned)((cells + TP_BS - 1) / TP_BS), TP_BS, 0, st>>>(a);
+  k_tp_params<<<(unsigned)((params + TP_BS - 1) / TP_BS), TP_BS, 0, st>>>(a);
   k_tp_final<<<(a.ngroups + 127) / 128, 128, 0, st>>>(a);
   return 0;
 }
