@@ -2009,8 +2009,8 @@ static int tw_check_err(ima_ctx *c, const char *what)
   static const char *why[] = {"", "a population that does not exist in that period (or a migration to the same "
                                   "population)", "a lineage count below zero", "more events than planned",
                               "an integral term the reference rejects (LogDiff order or iteration limit)",
-                              "a count beyond the logfact table"};
-  if (e[0]) return c->fail(IMA_ERR_DATA, "%s: item %d: %s", what, e[1], why[e[0] < 6 ? e[0] : 0]);
+                              "a count beyond the logfact table", "mig_off decreasing within the genealogy"};
+  if (e[0]) return c->fail(e[0] == 6 ? IMA_ERR_ARG : IMA_ERR_DATA, "%s: item %d: %s", what, e[1], why[e[0] < 7 ? e[0] : 0]);
   return IMA_OK;
 }
 
@@ -2046,9 +2046,11 @@ extern "C" int ima_gpu_treeweight(ima_ctx *c, int ngen, const int32_t *node_off,
     ev[g] = (int32_t)(E < (1 << 21) ? E : (1 << 21));
   }
   const size_t N = (size_t)node_off[ngen];
+  // per genealogy here; node by node in the kernel, before any event is read
   if (mig_off[0] != 0) return c->fail(IMA_ERR_ARG, "mig_off[0] must be 0");
-  for (size_t i = 0; i < N; i++)
-    if (mig_off[i + 1] < mig_off[i]) return c->fail(IMA_ERR_ARG, "mig_off must not decrease (node %zu)", i);
+  for (int g = 0; g < ngen; g++)
+    if (mig_off[node_off[g + 1]] < mig_off[node_off[g]])
+      return c->fail(IMA_ERR_ARG, "mig_off must not decrease (genealogy %d)", g);
   const size_t Nm = (size_t)mig_off[N];
   if (Nm > 0 && (!mig_t || !mig_p)) return c->fail(IMA_ERR_ARG, "migration events without mig_t/mig_p");
   int P = 32;

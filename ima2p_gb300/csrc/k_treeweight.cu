@@ -37,7 +37,7 @@ namespace {
 
 constexpr int TW_WPB = 4;  // genealogies (warps) per block
 enum { EV_COAL = 0, EV_MIG = 1, EV_SPLIT = 2, EV_PAD = 3 };
-enum { TW_E_POP = 1, TW_E_COUNT = 2, TW_E_SIZE = 3, TW_E_TERM = 4, TW_E_LF = 5 };
+enum { TW_E_POP = 1, TW_E_COUNT = 2, TW_E_SIZE = 3, TW_E_TERM = 4, TW_E_LF = 5, TW_E_MIGOFF = 6 };
 constexpr uint32_t POS_MASK = 0xFFFFFu;  // event position: 20 bits
 
 __device__ __forceinline__ uint32_t ev_pack(int type, int pop, int topop, int pos)
@@ -119,7 +119,9 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_tw_events(TwArgs a, int wpb)
     run += __shfl_sync(~0u, inc, 31);
     if (i < nl) {
       int nowpop = pp[i];
-      if ((unsigned)nowpop >= (unsigned)ntp || m1 < m0 || e + cnt > E) {
+      if (m1 < m0 || m0 < mo[0] || m1 > mo[nl]) {
+        bad = TW_E_MIGOFF;  // checked before any migration is read
+      } else if ((unsigned)nowpop >= (unsigned)ntp || e < 0 || e + cnt > E) {
         bad = TW_E_POP;
       } else {
         if (i >= ng) {
@@ -155,9 +157,10 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_tw_events(TwArgs a, int wpb)
     ev_c[i] = ev_pack(EV_PAD, 0, 0, i);
   }
   if (__any_sync(~0u, bad)) {
+    const int code = __reduce_max_sync(~0u, bad);
     if (lane == 0) {
       a.ev_n[g] = -1;
-      tw_fail(a.err, TW_E_POP, g);
+      tw_fail(a.err, code, g);
     }
     return;
   }

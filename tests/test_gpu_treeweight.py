@@ -118,6 +118,14 @@ def test_genealogy_the_model_cannot_hold_is_rejected():
     assert np.array_equal(w["fc"], cs.ref["fc"])
     with pytest.raises(api.ImaError):  # samppop that does not match the genealogy
         ctx.treeweight(packed, gl, gt, hval, samp + 1, cs.tvals)
+    # migration offsets that decrease inside a genealogy (its end points intact):
+    # node j of genealogy 0 gets a negative count
+    j = next(i for i in range(node_off[0] + 1, node_off[1] - 1) if mig_off[i] > mig_off[node_off[0]])
+    bad_off = mig_off.copy()
+    bad_off[j + 1] = mig_off[j] - 1
+    with pytest.raises(api.ImaError):
+        ctx.treeweight((node_off, up0, time, pop, bad_off, mig_t, mig_p), gl, gt, hval, samp, cs.tvals)
+    assert np.array_equal(ctx.treeweight(packed, gl, gt, hval, samp, cs.tvals)["fc"], cs.ref["fc"])
     with pytest.raises(api.ImaError):  # groups beyond the genealogies
         ctx.tree_prob(np.array([0, len(gl) + 1], np.int32))
 
