@@ -511,3 +511,41 @@ def treeweight_batch(pm, packed, gen_locus, gen_tv, hval, samppop, tvals):
                                      *(_p(a) for a in keep),
                                      *(_p(out[k]) for k in ("cc", "hcc", "fc", "mc", "fm", "lens", "mignum")))
     return bad, out
+
+
+def ref_ry(npops, treestr, tprior, loci, chains, gens, steps, seed, thetaprior, mprior, expo=False):
+    """The reference's split-time update changet_RY1 through
+    oracle/_ref/imaref (this container only).  loci: (numgenes, hval,
+    samppop, u, seq[n][S]) per infinite-sites locus; chains: (tvals, beta);
+    gens[ci][li]: LabelledGenealogy; steps: (ci, period) in order.  Returns
+    (per step (accepted, tval, probg, pdg), times[ci][li], migration
+    times[ci][li])."""
+    nch, nl = len(chains), len(loci)
+    t = ["%d %d %d %d %d %d" % (npops, nch, nl, seed, len(steps), int(expo)), treestr,
+         "%.17g %.17g" % (thetaprior, mprior)]
+    t += ["%.17g %.17g" % tuple(p) for p in tprior]
+    for ng, h, sp, u, seq in loci:
+        seq = np.asarray(seq)
+        t.append("%d %.17g %s %.17g %d" % (ng, h, " ".join(map(str, sp)), u, seq.shape[1]))
+        t.append(" ".join(map(str, seq.ravel())))
+    for tv, b in chains:
+        t.append(" ".join("%.17g" % v for v in tv) + " %.17g" % b)
+    for ci in range(nch):
+        for li in range(nl):
+            lg = gens[ci][li]
+            t.append(str(len(lg.pop)))
+            t.append(_tree_txt(lg.g) + " ".join(map(str, lg.pop)))
+            for m in lg.mig:
+                t.append(" ".join([str(len(m))] + ["%.17g %d" % (mt, mp) for mt, mp in m]))
+    t += ["%d %d" % s for s in steps]
+    out = run_ref("ry", "\n".join(t) + "\n")
+    res, times, migt = [], {}, {}
+    for ln in out.splitlines():
+        f = ln.split()
+        if f[0] == "STEP":
+            res.append((int(f[1]), float(f[2]), float(f[3]), float(f[4])))
+        elif f[0] == "TIMES":
+            times[(int(f[1]), int(f[2]))] = np.array([float(v) for v in f[3:]])
+        elif f[0] == "MIGT":
+            migt[(int(f[1]), int(f[2]))] = np.array([float(v) for v in f[3:]])
+    return res, times, migt

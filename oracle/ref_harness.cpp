@@ -12,7 +12,7 @@
  * ref_access_cpd.cpp and ref_access_jf.cpp include those two reference
  * sources to reach them.  The other reference objects are linked unchanged.
  *
- * Usage:  imaref is|hky|sw|swap|jointp|de|margin|tw|iterm <input.txt>   (results on stdout)
+ * Usage:  imaref is|hky|sw|swap|jointp|de|margin|tw|iterm|ry <input.txt>   (results on stdout)
  */
 #undef GLOBVARS
 #include "imamp.hpp"
@@ -389,6 +389,119 @@ static void run_tw()
   }
 }
 
+/* RY: npops nchains nloci seed nsteps expo treestring thetaprior mprior
+ *     per period k: tmin tmax                         (T[k].pr)
+ *     per locus: numgenes hval samppop[npops] u numsites seq[numgenes*numsites]
+ *     per chain: tvals[npops-1] beta
+ *     per chain, per locus: nlines up0[] up1[] down[] time[] pop[], then per
+ *       node: nm {mt mp}*nm
+ *     per step: ci period
+ *   -> per step "STEP accepted tval probg pdg", then per chain-locus
+ *      "TIMES ci li time[nlines]" and "MIGT ci li mt..." (all events in
+ *      node order)
+ * The split-time update changet_RY1 (update_t_RY.cpp:223-518) on infinite-
+ * sites loci, after the chain state is set up as finish_setup_C does it
+ * (treeweight, likelihoodIS, sum_treeinfo, initialize_integrate_tree_prob). */
+static void run_ry()
+{
+  int npp = rd_i(), nch = rd_i(), nl = rd_i(), seed = rd_i(), nsteps = rd_i(), expo = rd_i();
+  char treestr[POPTREESTRINGLENGTHMAX];
+  if (fscanf(g_in, "%255s", treestr) != 1) { fprintf(stderr, "short input\n"); exit(3); }
+  thetaprior = rd_d();
+  mprior = rd_d();
+  npops = npp;
+  numtreepops = 2 * npops - 1;
+  lastperiodnumber = numsplittimes = npops - 1;
+  modeloptions[EXPOMIGRATIONPRIOR] = expo;
+  gbeta = 1.0;
+  T = (struct chainstate_record_updates_and_values *)calloc((size_t)lastperiodnumber, sizeof(*T));
+  for (int k = 0; k < lastperiodnumber; k++) {
+    T[k].pr.min = rd_d();
+    T[k].pr.max = rd_d();
+  }
+  alloc_chains(nch, nl);
+  nurates = nl;
+  std::vector<double> us(nl);
+  std::vector<std::vector<int>> seqs(nl);
+  for (int li = 0; li < nl; li++) {
+    L[li].numgenes = rd_i();
+    L[li].numlines = 2 * L[li].numgenes - 1;
+    L[li].hval = rd_d();
+    for (int p = 0; p < npops; p++) L[li].samppop[p] = rd_i();
+    us[li] = rd_d();
+    L[li].numsites = rd_i();
+    L[li].model = INFINITESITES;
+    L[li].nlinked = 1;
+    L[li].uii[0] = li;
+    seqs[li].resize((size_t)L[li].numgenes * L[li].numsites);
+    for (auto &v : seqs[li]) v = rd_i();
+    L[li].seq = (int **)malloc(sizeof(int *) * L[li].numgenes);
+    for (int i = 0; i < L[li].numgenes; i++) L[li].seq[i] = &seqs[li][(size_t)i * L[li].numsites];
+  }
+  total_numgenes = 0;
+  for (int li = 0; li < nl; li++) total_numgenes += L[li].numgenes;
+  setlogfact();
+  init_gtreecommon();
+  init_treeweight();
+  for (int ci = 0; ci < nch; ci++) {
+    setup_poptree(ci, treestr);
+    C[ci]->tvals = (double *)calloc((size_t)npops, sizeof(double));
+    for (int k = 0; k < npops - 1; k++) C[ci]->tvals[k] = rd_d();
+    C[ci]->tvals[lastperiodnumber] = TIMEMAX;
+    beta[ci] = rd_d();
+  }
+  refacc_setup_iparams();
+  for (int ci = 0; ci < nch; ci++) {
+    init_genealogy_weights(&C[ci]->allgweight);
+    init_probcalc(&C[ci]->allpcalc);
+    C[ci]->allpcalc.pdg = 0;
+    for (int li = 0; li < nl; li++) {
+      int nlines = rd_i();
+      struct genealogy *G = &C[ci]->G[li];
+      G->gtree = alloc_tree(nlines);
+      read_tree(G->gtree, nlines);
+      for (int i = 0; i < nlines; i++) G->gtree[i].pop = rd_i();
+      for (int i = 0; i < nlines; i++) {
+        int nm = rd_i();
+        G->gtree[i].mig = (struct migstruct *)calloc((size_t)ABSMIGMAX, sizeof(struct migstruct));
+        for (int j = 0; j < nm; j++) {
+          G->gtree[i].mig[j].mt = rd_d();
+          G->gtree[i].mig[j].mp = rd_i();
+        }
+        G->gtree[i].mig[nm].mt = -1.0;
+      }
+      G->root = find_root(G->gtree, nlines);
+      G->roottime = G->gtree[G->gtree[G->root].up[0]].time;
+      G->uvals = (double *)malloc(sizeof(double));
+      G->uvals[0] = us[li];
+      G->pdg_a = (double *)malloc(sizeof(double));
+      init_genealogy_weights(&G->gweight);
+      treeweight(ci, li);
+      sum_treeinfo(&C[ci]->allgweight, &G->gweight);
+      G->pdg = G->pdg_a[0] = likelihoodIS(ci, li, us[li]);
+      C[ci]->allpcalc.pdg += G->pdg;
+    }
+    initialize_integrate_tree_prob(ci, &C[ci]->allgweight, &C[ci]->allpcalc);
+  }
+  init_t_RY();
+  setseeds(seed);
+  for (int s = 0; s < nsteps; s++) {
+    int ci = rd_i(), k = rd_i();
+    int acc = changet_RY1(ci, k);
+    printf("STEP %d %.17g %.17g %.17g\n", acc, C[ci]->tvals[k], C[ci]->allpcalc.probg, C[ci]->allpcalc.pdg);
+  }
+  for (int ci = 0; ci < nch; ci++)
+    for (int li = 0; li < nl; li++) {
+      struct genealogy *G = &C[ci]->G[li];
+      printf("TIMES %d %d", ci, li);
+      for (int i = 0; i < L[li].numlines; i++) printf(" %.17g", G->gtree[i].time);
+      printf("\nMIGT %d %d", ci, li);
+      for (int i = 0; i < L[li].numlines; i++)
+        for (int j = 0; G->gtree[i].mig[j].mt > -0.5; j++) printf(" %.17g", G->gtree[i].mig[j].mt);
+      printf("\n");
+    }
+}
+
 /* ITERM: n, then per line: kind(0 coal, 1 mig, 2 mig expo) c f h max min
  *   -> the reference integral term per line (update_gtree_common.cpp:108-304) */
 static void run_iterm()
@@ -406,7 +519,7 @@ static void run_iterm()
 
 int main(int argc, char **argv)
 {
-  if (argc != 3) { fprintf(stderr, "usage: imaref is|hky|sw|swap|jointp|de|margin|tw|iterm <input>\n"); return 2; }
+  if (argc != 3) { fprintf(stderr, "usage: imaref is|hky|sw|swap|jointp|de|margin|tw|iterm|ry <input>\n"); return 2; }
   g_in = fopen(argv[2], "r");
   if (!g_in) { perror(argv[2]); return 2; }
   std::string mode = argv[1];
@@ -419,6 +532,7 @@ int main(int argc, char **argv)
   else if (mode == "margin") run_margin();
   else if (mode == "tw") run_tw();
   else if (mode == "iterm") run_iterm();
+  else if (mode == "ry") run_ry();
   else { fprintf(stderr, "unknown mode\n"); return 2; }
   fclose(g_in);
   return 0;

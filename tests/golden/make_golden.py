@@ -25,8 +25,12 @@ Fixtures:
                     population-labelled IM genealogies for 2-5 population
                     trees, with the reference's own parameter maps
                     (setup_iparams), and the integral terms on edge cases
+  golden_ry.npz     the split-time update changet_RY1 (MT19937 seeded) on
+                    three chains of four infinite-sites loci, 3 populations
+                    with migration: decisions, split times, probg and pdg
+                    per step, final node and migration times
 
-Run with fixture names (is hky sw swap jointp de margin tw) to regenerate only those.
+Run with fixture names (is hky sw swap jointp de margin tw ry) to regenerate only those.
 """
 from __future__ import annotations
 
@@ -454,12 +458,48 @@ def golden_tw():
     np.savez_compressed(os.path.join(OUT, "golden_tw.npz"), **out)
 
 
+def golden_ry():
+    from ima2p_gb300 import popmodel
+    rng = np.random.default_rng(1011)
+    npops, ts = 3, "((0,1):3,2):4"
+    sp = popmodel.parse_treestring(ts, npops)
+    nl, nch, tv0 = 4, 3, [0.45, 1.1]
+    samps = [[int(v) for v in rng.integers(3, 7, npops)] for _ in range(nl)]
+    splits = [(tv0[k], a, b, anc) for k, (a, b, anc) in enumerate(sp)]
+    base = [synth.sim_im_labeled(rng, samps[li], list(rng.uniform(1.0, 3.0, 5)), 0.5, splits) for li in range(nl)]
+    seqs = [synth.is_data(rng, base[li].g, 1.0, min_sites=4) for li in range(nl)]
+    us = [0.8, 1.0, 1.2, 1.0]
+    loci = [(sum(samps[li]), 1.0, samps[li], us[li], seqs[li]) for li in range(nl)]
+    gens = [[base[li] for li in range(nl)] for _ in range(nch)]
+    betas = [1.0, 0.7, 0.45]
+    tprior = [(0.0, 3.0), (0.0, 5.0)]
+    steps = [(s % nch, int(rng.integers(0, npops - 1))) for s in range(90)]
+    res, times, migt = O.ref_ry(npops, ts, tprior, loci, [(tv0, b) for b in betas], gens, steps, 4321, 10.0, 1.0)
+    out = {"npops": np.array(npops), "tree": np.array(ts), "tv0": np.array(tv0), "betas": np.array(betas),
+           "tprior": np.array(tprior), "steps": np.array(steps), "seed": np.array(4321),
+           "priors": np.array([10.0, 1.0]), "samps": np.array(samps), "us": np.array(us),
+           "seq_off": np.concatenate([[0], np.cumsum([q.size for q in seqs])]),
+           "seq_shape": np.array([q.shape for q in seqs]), "seqs": np.concatenate([q.ravel() for q in seqs]),
+           "res": np.array(res)}
+    packed_base = [b for b in base]
+    out["node_off"] = np.concatenate([[0], np.cumsum([len(g.pop) for g in packed_base])]).astype(np.int32)
+    for f in ("up0", "up1", "down", "time"):
+        out[f] = np.concatenate([getattr(g.g, f) for g in packed_base])
+    out["pop"] = np.concatenate([g.pop for g in packed_base]).astype(np.int32)
+    out["mig_off"] = np.concatenate([[0], np.cumsum([len(m) for g in packed_base for m in g.mig])]).astype(np.int32)
+    out["mig_t"] = np.array([e[0] for g in packed_base for m in g.mig for e in m])
+    out["mig_p"] = np.array([e[1] for g in packed_base for m in g.mig for e in m], np.int32)
+    out["times"] = np.concatenate([times[(ci, li)] for ci in range(nch) for li in range(nl)])
+    out["migt"] = np.concatenate([migt[(ci, li)] for ci in range(nch) for li in range(nl)])
+    np.savez_compressed(os.path.join(OUT, "golden_ry.npz"), **out)
+
+
 if __name__ == "__main__":
     if not O.ref_available():
         sys.exit("build the reference harness first: make -C oracle ref")
     gens = {"is": golden_is, "hky": golden_hky, "sw": golden_sw, "swap": golden_swap,
             "jointp": golden_jointp, "de": golden_de, "margin": golden_margin,
-            "tw": golden_tw}
+            "tw": golden_tw, "ry": golden_ry}
     for name in (sys.argv[1:] or list(gens)):
         gens[name]()
     for f in sorted(os.listdir(OUT)):
