@@ -163,3 +163,162 @@ class DeviceBackend:
         r, st = self.ctx.eval(np.full(nl, ci, np.int32), np.arange(nl, dtype=np.int32), self.u,
                               np.ones(nl), precision=self.prec)
         return r
+
+
+class ChainSet:
+    """Every chain's state packed for a batched sweep: the labelled
+    genealogies of chains 0..nch-1 x loci 0..nl-1 (chain-major) as one CSR
+    (api.pack_labelled order), split times [nch][npops-1], heats, per-locus
+    likelihoods [nch][nl] and their sums, p(G) per chain."""
+
+    def __init__(self, gens, tvals, betas):
+        self.nch, self.nl = len(gens), len(gens[0])
+        flat = [lg for row in gens for lg in row]
+        (self.node_off, self.up0, self.time, self.pop, self.mig_off, self.mig_t,
+         self.mig_p) = api.pack_labelled(flat)
+        self.up1 = np.concatenate([lg.g.up1 for lg in flat]).astype(np.int32)
+        self.down = np.concatenate([lg.g.down for lg in flat]).astype(np.int32)
+        self.tvals = np.array(tvals, np.float64).reshape(self.nch, -1).copy()
+        self.beta = np.asarray(betas, np.float64).copy()
+        nn = np.diff(self.node_off)
+        self.node_chain = np.repeat(np.arange(self.nch * self.nl) // self.nl, nn)
+        self.edge = self.down != -1
+        counts = np.diff(self.mig_off)
+        self.mig_chain = np.repeat(self.node_chain, counts)
+        self.pdg = np.zeros((self.nch, self.nl))
+        self.pdgsum = np.zeros(self.nch)
+        self.probg = np.zeros(self.nch)
+
+    def packed(self):
+        return self.node_off, self.up0, self.time, self.pop, self.mig_off, self.mig_t, self.mig_p
+
+
+def _band(period, last, oldt, newt, t_u, t_d, t, sel_lo, sel_hi):
+    """beforesplit on sel_lo, aftersplit on sel_hi; oldt..t_d per element."""
+    out = t.copy()
+    first = sel_lo & (period == 0)
+    rest = sel_lo & (period != 0)
+    out[first] = t[first] * newt[first] / oldt[first]
+    out[rest] = t_u[rest] + (t[rest] - t_u[rest]) * (newt[rest] - t_u[rest]) / (oldt[rest] - t_u[rest])
+    top = sel_hi & (period == last - 1)
+    mid = sel_hi & (period != last - 1)
+    out[top] = t[top] + newt[top] - oldt[top]
+    out[mid] = t_d[mid] - (t_d[mid] - newt[mid]) * (t_d[mid] - t[mid]) / (t_d[mid] - oldt[mid])
+    return out
+
+
+class SweepBackend:
+    """Device work of a batched sweep: weights and p(G) of every chain in one
+    ima_gpu_treeweight + ima_gpu_tree_prob, likelihoods of every chain-locus
+    in one ima_gpu_set_genealogies + ima_gpu_eval.  ctx holds the loci, nch
+    chains in one run (ima_gpu_set_chains(1, nch)) and the population
+    model."""
+
+    def __init__(self, ctx, loci_hval, loci_samppop, u, kappa=None, precision=api.PREC_FP64):
+        self.ctx = ctx
+        self.hval = np.asarray(loci_hval, np.float64)
+        self.samp = np.asarray(loci_samppop, np.int32)
+        self.u = np.asarray(u, np.float64)
+        self.kappa = np.ones(len(self.u)) if kappa is None else np.asarray(kappa, np.float64)
+        self.prec = precision
+
+    def weights(self, cs: ChainSet):
+        n = cs.nch * cs.nl
+        gl = np.tile(np.arange(cs.nl, dtype=np.int32), cs.nch)
+        gt = np.repeat(np.arange(cs.nch, dtype=np.int32), cs.nl)
+        w = self.ctx.treeweight(cs.packed(), gl, gt, self.hval, self.samp, cs.tvals)
+        probg, _, _, _ = self.ctx.tree_prob((np.arange(cs.nch + 1) * cs.nl).astype(np.int32))
+        return w["lens"], probg
+
+    def likelihoods(self, cs: ChainSet, lens):
+        n = cs.nch * cs.nl
+        ci = np.repeat(np.arange(cs.nch, dtype=np.int32), cs.nl)
+        li = np.tile(np.arange(cs.nl, dtype=np.int32), cs.nch)
+        self.ctx.set_genealogies(ci, li, cs.up0, cs.up1, cs.down, cs.time, length=lens[:, 0].copy())
+        r, _ = self.ctx.eval(ci, li, np.tile(self.u, cs.nch), np.tile(self.kappa, cs.nch), precision=self.prec)
+        return r.reshape(cs.nch, cs.nl)
+
+    def decide(self, cs: ChainSet, accept):
+        """Commit the accepted chains' evaluations, revert the others'."""
+        ci = np.repeat(np.arange(cs.nch, dtype=np.int32), cs.nl)
+        li = np.tile(np.arange(cs.nl, dtype=np.int32), cs.nch)
+        self.ctx.commit(ci, li, np.repeat(np.asarray(accept, np.uint8), cs.nl))
+
+
+def setup_chainset(cs: ChainSet, backend):
+    """The state finish_setup_C leaves: weights, p(G), likelihoods and
+    their per-chain sums in locus order."""
+    lens, probg = backend.weights(cs)
+    pdg = np.asarray(backend.likelihoods(cs, lens), np.float64)
+    backend.decide(cs, np.ones(cs.nch, bool))
+    cs.pdg = pdg
+    s = np.zeros(cs.nch)
+    for li in range(cs.nl):
+        s = s + pdg[:, li]
+    cs.pdgsum = s
+    cs.probg = np.asarray(probg, np.float64)
+
+
+def changet_ry1_sweep(cs: ChainSet, periods, rng, tprior, npops, backend, gbeta=1.0):
+    """One changet_RY1 per chain, chains in order, with the device work of
+    all chains batched.  The generator draws are the sequential run's (for
+    chain 0: getnewt's uniform, then the acceptance uniform; then chain 1,
+    ...), since no draw depends on another chain.  Returns the accept flags."""
+    nch, last = cs.nch, npops - 1
+    periods = np.asarray(periods, np.int64)
+    oldt = cs.tvals[np.arange(nch), periods].copy()
+    t_u = np.where(periods == 0, 0.0, cs.tvals[np.arange(nch), np.maximum(periods - 1, 0)])
+    t_d = np.where(periods == last - 1, TIMEMAX, cs.tvals[np.arange(nch), np.minimum(periods + 1, last - 1)])
+    newt = np.zeros(nch)
+    logU = np.zeros(nch)
+    for c in range(nch):
+        k = int(periods[c])
+        t_d_prior = min(tprior[k][1], float(t_d[c]))
+        t_u_prior = max(tprior[k][0], float(t_u[c]))
+        newt[c] = getnewt(rng, k, t_u_prior, t_d_prior, float(oldt[c]), cs.nl, npops)
+        logU[c] = math.log(rng.uniform())
+    # the rubber band on every node and migration time, per chain's parameters
+    nc, mc = cs.node_chain, cs.mig_chain
+
+    def move(o, n, t, chain, edge):
+        P, tu, td, ot, nt = periods[chain], t_u[chain], t_d[chain], o[chain], n[chain]
+        lo = edge & (t <= ot) & (t > tu)
+        hi = edge & ~lo & (t > ot) & (t < td)
+        return _band(P, last, ot, nt, tu, td, t, lo, hi), lo, hi
+
+    old_time, old_mig = cs.time.copy(), cs.mig_t.copy()
+    cs.time, lo, hi = move(oldt, newt, cs.time, nc, cs.edge)
+    ecu = np.bincount(nc[lo], minlength=nch) // 2
+    ecd = np.bincount(nc[hi], minlength=nch) // 2
+    medge = np.repeat(cs.edge, np.diff(cs.mig_off))
+    cs.mig_t, mlo, mhi = move(oldt, newt, cs.mig_t, mc, medge)
+    emu = np.bincount(mc[mlo], minlength=nch)
+    emd = np.bincount(mc[mhi], minlength=nch)
+    cs.tvals[np.arange(nch), periods] = newt
+    lens, probg_new = backend.weights(cs)
+    pdg_new = np.asarray(backend.likelihoods(cs, lens), np.float64)
+    pdgnewsum = np.zeros(nch)
+    for li in range(cs.nl):
+        pdgnewsum = pdgnewsum + pdg_new[:, li]
+    accept = np.zeros(nch, bool)
+    for c in range(nch):
+        t_u_hterm = (newt[c] - t_u[c]) / (oldt[c] - t_u[c])
+        t_d_hterm = 1.0 if periods[c] == last - 1 else (t_d[c] - newt[c]) / (t_d[c] - oldt[c])
+        tpw = gbeta * (float(pdgnewsum[c]) - float(cs.pdgsum[c]))
+        tpw += float(probg_new[c]) - float(cs.probg[c])
+        mh = (float(cs.beta[c]) * tpw + int(ecd[c] + emd[c]) * math.log(t_d_hterm)
+              + int(ecu[c] + emu[c]) * math.log(t_u_hterm))
+        accept[c] = logU[c] < min(1.0, mh)
+    backend.decide(cs, accept)
+    cs.pdg[accept] = pdg_new[accept]
+    cs.pdgsum[accept] = pdgnewsum[accept]
+    cs.probg[accept] = np.asarray(probg_new, np.float64)[accept]
+    rej = ~accept
+    if rej.any():
+        # rejected chains: the inverse maps, as the reference moves them back
+        cs.tvals[np.arange(nch)[rej], periods[rej]] = oldt[rej]
+        back_t, _, _ = move(newt, oldt, cs.time, nc, cs.edge & rej[nc])
+        back_m, _, _ = move(newt, oldt, cs.mig_t, mc, medge & rej[mc])
+        cs.time = np.where(rej[nc], back_t, cs.time)
+        cs.mig_t = np.where(rej[mc], back_m, cs.mig_t)
+    return accept

@@ -106,3 +106,55 @@ def final_times(case, states):
     t = np.concatenate([lg.g.time for st in states for lg in st.gens])
     m = np.array([e[0] for st in states for lg in st.gens for mm in lg.mig for e in mm])
     return t, m
+
+
+class OracleSweepBackend:
+    """The batched sweep's backend on the oracle."""
+
+    def __init__(self, case):
+        self.c = case
+        self.one = OracleBackend(case)
+
+    def _gens(self, cs):
+        from ima2p_gb300.synth import Genealogy, LabelledGenealogy
+        out = []
+        for i in range(cs.nch * cs.nl):
+            a, b = int(cs.node_off[i]), int(cs.node_off[i + 1])
+            root = int(np.flatnonzero(cs.down[a:b] == -1)[0])
+            g = Genealogy(cs.up0[a:b], cs.up1[a:b], cs.down[a:b], cs.time[a:b], root)
+            mig = [[(float(cs.mig_t[e]), int(cs.mig_p[e])) for e in range(cs.mig_off[j], cs.mig_off[j + 1])]
+                   for j in range(a, b)]
+            out.append(LabelledGenealogy(g, cs.pop[a:b], mig))
+        return out
+
+    def weights(self, cs):
+        gens = self._gens(cs)
+        lens, probg = [], []
+        for ci in range(cs.nch):
+            l_, p_ = self.one.weights(ci, gens[ci * cs.nl:(ci + 1) * cs.nl], cs.tvals[ci])
+            lens.append(l_)
+            probg.append(p_)
+        return np.concatenate(lens), np.array(probg)
+
+    def likelihoods(self, cs, lens):
+        gens = self._gens(cs)
+        return np.array([self.one.likelihoods(ci, gens[ci * cs.nl:(ci + 1) * cs.nl], lens[ci * cs.nl:(ci + 1) * cs.nl])
+                         for ci in range(cs.nch)])
+
+    def decide(self, cs, accept):
+        pass
+
+
+def run_sweeps(case, backend, rng):
+    """The fixture's steps as sweeps: chains 0, 1, 2 in order, 30 times."""
+    from ima2p_gb300 import splittime
+    cs = splittime.ChainSet(case.fresh_gens(), [case.d["tv0"]] * case.nch, case.betas)
+    splittime.setup_chainset(cs, backend)
+    res = []
+    for s0 in range(0, len(case.steps), case.nch):
+        periods = [case.steps[s0 + c][1] for c in range(case.nch)]
+        assert [case.steps[s0 + c][0] for c in range(case.nch)] == list(range(case.nch))
+        acc = splittime.changet_ry1_sweep(cs, periods, rng, case.tprior, case.npops, backend)
+        for c in range(case.nch):
+            res.append((int(acc[c]), float(cs.tvals[c, periods[c]]), float(cs.probg[c]), float(cs.pdgsum[c])))
+    return np.array(res), cs

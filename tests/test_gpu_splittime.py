@@ -38,3 +38,26 @@ def test_device_driven_update_follows_the_reference():
     assert np.array_equal(t[~root], case.times[~root])
     assert np.array_equal(m, case.migt)
     ctx.close()
+
+
+def test_batched_sweep_follows_the_reference():
+    """changet_ry1_sweep: every chain's proposal in one ima_gpu_treeweight /
+    ima_gpu_tree_prob / ima_gpu_set_genealogies / ima_gpu_eval round; the
+    generator draws in the sequential run's order."""
+    from tests._splittime import run_sweeps
+    case = RyCase()
+    ctx = api.Context(0)
+    for q in case.seqs:
+        ctx.add_locus_is(q)
+    ctx.set_chains(1, case.nch)
+    ctx.set_popmodel(case.pm, *case.priors())
+    backend = splittime.SweepBackend(ctx, np.ones(case.nl), case.samps, case.us)
+    res, cs = run_sweeps(case, backend, api.MT19937(case.seed))
+    ref = case.res
+    assert np.array_equal(res[:, 0], ref[:, 0])
+    assert np.array_equal(res[:, 1], ref[:, 1])
+    np.testing.assert_allclose(res[:, 2], ref[:, 2], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(res[:, 3], ref[:, 3], rtol=1e-12)
+    assert np.array_equal(cs.time[cs.edge], case.times[cs.edge])
+    assert np.array_equal(cs.mig_t, case.migt)
+    ctx.close()
