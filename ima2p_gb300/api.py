@@ -49,6 +49,8 @@ EXPORTS = [
     "ima_gpu_set_profiling", "ima_gpu_kernel_stats", "ima_gpu_launch_count", "ima_gpu_flush_l2",
     "ima_gpu_memory", "ima_gpu_set_popmodel", "ima_gpu_treeweight", "ima_gpu_tree_prob",
     "ima_gpu_surface_append_tree_rows", "ima_gpu_surface_get_rows",
+    "ima_gpu_set_locus_pops", "ima_gpu_set_labels", "ima_gpu_get_times", "ima_gpu_rubber_band",
+    "ima_gpu_chain_weights",
 ]
 
 
@@ -177,6 +179,11 @@ def _declare(L):
         "ima_gpu_tree_prob": (I, [P, I, P, P, P, P, P, P, P]),
         "ima_gpu_surface_append_tree_rows": (I, [P, I, P]),
         "ima_gpu_surface_get_rows": (I, [P, I, I, I, P]),
+        "ima_gpu_set_locus_pops": (I, [P, P, P]),
+        "ima_gpu_set_labels": (I, [P, I, P, P, P, P, P, P]),
+        "ima_gpu_get_times": (I, [P, I, I, P, P, P]),
+        "ima_gpu_rubber_band": (I, [P, I, P, P, P, P, P, P, I, P]),
+        "ima_gpu_chain_weights": (I, [P, I, P, P, P, P, P]),
         "ima_gpu_fillvec": (I, [P, I, P, P, P, P, P]),
         "ima_gpu_batch_set_variants": (I, [P, I, I, I]),
         "ima_gpu_set_allele_edits": (I, [P, I, P, P, P, P, P]),
@@ -498,6 +505,60 @@ class Context:
                                             _ptr(gtv) if gtv is not None else None, _ptr(probg), _ptr(q),
                                             _ptr(m), _ptr(rowbuf) if rows else None))
         return probg, q, m[:, :nmg], rowbuf
+
+    # -------------------- resident labels and the split-time update
+    def set_locus_pops(self, hval, samppop):
+        """L[li].hval and L[li].samppop of every locus, for the resident
+        weights."""
+        hval, samppop = _f64(hval), _i32(samppop)
+        self._ck(self.lib.ima_gpu_set_locus_pops(self.h, _ptr(hval), _ptr(samppop)))
+
+    def set_labels(self, ci, li, gens):
+        """Population labels and migration events (LabelledGenealogy) of the
+        chain-loci (ci[k], li[k]), kept on the device."""
+        ci, li = _i32(np.atleast_1d(ci)), _i32(np.atleast_1d(li))
+        pop = _i32(np.concatenate([g.pop for g in gens]))
+        moff = []
+        for g in gens:
+            o = np.zeros(len(g.mig) + 1, np.int32)
+            o[1:] = np.cumsum([len(m) for m in g.mig])
+            moff.append(o)
+        moff = _i32(np.concatenate(moff))
+        mt = _f64(np.array([e[0] for g in gens for m in g.mig for e in m] or [0.0]))
+        mp = _i32(np.array([e[1] for g in gens for m in g.mig for e in m] or [0]))
+        self._ck(self.lib.ima_gpu_set_labels(self.h, len(ci), _ptr(ci), _ptr(li), _ptr(pop), _ptr(moff),
+                                             _ptr(mt), _ptr(mp)))
+
+    def get_times(self, ci, li, nlines):
+        """Device node times and migration times (node order) of a chain-locus."""
+        t = np.zeros(nlines)
+        n = I()
+        self._ck(self.lib.ima_gpu_get_times(self.h, int(ci), int(li), _ptr(t), C.byref(n), None))
+        m = np.zeros(max(n.value, 1))
+        self._ck(self.lib.ima_gpu_get_times(self.h, int(ci), int(li), _ptr(t), C.byref(n), _ptr(m)))
+        return t, m[:n.value]
+
+    def rubber_band(self, chains, period, oldt, newt, t_u, t_d, inverse=False):
+        """changet_RY1's time moves on every locus of the chains; returns
+        [nch][4] = (ecd, ecu, emd, emu) going forward (node counts per edge)."""
+        chains, period = _i32(chains), _i32(period)
+        arrs = [_f64(v) for v in (oldt, newt, t_u, t_d)]
+        counts = np.zeros((len(chains), 4), np.int32)
+        self._ck(self.lib.ima_gpu_rubber_band(self.h, len(chains), _ptr(chains), _ptr(period),
+                                              *(_ptr(v) for v in arrs), int(inverse), _ptr(counts)))
+        return counts
+
+    def chain_weights(self, chains, tvals):
+        """Resident weights of every locus of the chains (lengths updated on
+        the device) and their p(G): (probg, q, m)."""
+        pm = self._tw_pm
+        chains = _i32(chains)
+        tvals = _f64(np.asarray(tvals, np.float64).reshape(len(chains), -1))
+        nth, nmg = len(pm.th_cells), 0 if pm.nomig else len(pm.mg_cells)
+        probg, q, m = np.zeros(len(chains)), np.zeros((len(chains), nth)), np.zeros((len(chains), max(nmg, 1)))
+        self._ck(self.lib.ima_gpu_chain_weights(self.h, len(chains), _ptr(chains), _ptr(tvals), _ptr(probg),
+                                                _ptr(q), _ptr(m)))
+        return probg, q, m[:, :nmg]
 
     def surface_append_tree_rows(self, groups):
         """Append the gsampinf rows of these chains (last tree_prob) to the

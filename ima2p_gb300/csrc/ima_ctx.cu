@@ -234,6 +234,22 @@ struct ima_ctx {
   void *d_twin = nullptr, *d_twout = nullptr, *d_tpbuf = nullptr;
   size_t twin_cap = 0, twout_cap = 0, tpbuf_cap = 0;
   int tw_ngen = 0, tw_ntv = 0;
+  // resident population labels for the split-time update: per node pop,
+  // per item nl+1 relative migration offsets (at node_off + item), events in
+  // a pool (item events from mbase[item]), split-time rows per chain
+  int32_t *d_pop = nullptr, *d_moff = nullptr, *d_inode_off = nullptr, *d_gl = nullptr, *d_gt = nullptr;
+  int32_t *d_moff_start = nullptr, *d_bcnt = nullptr, *d_mig_p = nullptr, *d_rsamp = nullptr;
+  long long *d_mbase = nullptr;
+  double *d_mig_t = nullptr, *d_tvr = nullptr, *d_len_hold = nullptr, *d_rhlog = nullptr, *d_rh2 = nullptr;
+  size_t mig_cap = 0, mig_used = 0;
+  std::vector<long long> h_mbase;
+  std::vector<int32_t> h_mcnt, h_mcap;
+  std::vector<uint8_t> has_labels;
+  std::vector<double> h_tvr;
+  bool locus_pops = false;
+  void *d_rsel = nullptr;
+  size_t rsel_cap = 0;
+  int dev_lo = INT32_MAX, dev_hi = -1;  // items whose device times/lengths are newer than the mirror
   float *tp_rows = nullptr;  // gsampinf rows of the last ima_gpu_tree_prob
   int tp_ngroups = 0, tp_rowlen = 0;
   size_t s_cap = 0;          // surface row capacity (rows appended on the device)
@@ -399,7 +415,10 @@ extern "C" void ima_gpu_destroy(ima_ctx *c)
                   c->d_beta, c->d_allbetas, c->d_probg, c->d_S, c->d_swapcount, c->d_tempcount,
                   c->d_used, c->d_swap0ok, c->d_ctr, c->d_uni, c->d_rows, c->d_lognorm,
                   c->d_sscratch, c->d_sx, c->d_sq, c->d_sess, c->d_citems, c->d_cacc, c->d_flush,
-                  c->d_mscratch, c->d_tw, c->d_logfact, c->d_twerr, c->d_twin, c->d_twout, c->d_tpbuf};
+                  c->d_mscratch, c->d_tw, c->d_logfact, c->d_twerr, c->d_twin, c->d_twout, c->d_tpbuf,
+                  c->d_pop, c->d_moff, c->d_inode_off, c->d_gl, c->d_gt, c->d_moff_start, c->d_bcnt,
+                  c->d_mig_p, c->d_rsamp, c->d_mbase, c->d_mig_t, c->d_tvr, c->d_len_hold, c->d_rhlog,
+                  c->d_rh2, c->d_rsel};
   for (void *p : devs)
     if (p) cudaFree(p);
   void *hosts[] = {c->h_nodes, c->h_t64, c->h_tff, c->h_sched, c->h_nlev, c->h_len, c->h_pi, c->h_al};
@@ -587,8 +606,29 @@ extern "C" int ima_gpu_set_chains(ima_ctx *c, int nruns, int chains_per_run)
 
 // ======================================================================
 // genealogies
+
+// Device-side updates (the split-time rubber band, resident weights) leave
+// times and lengths newer on the device than in the pinned mirror; every
+// host write into the mirror first copies them back, so that a later range
+// upload never carries stale values.
+static int sync_mirror(ima_ctx *c)
+{
+  if (c->dev_hi < 0) return IMA_OK;
+  const ItemDev &a = c->items[c->dev_lo], &b = c->items[c->dev_hi];
+  const size_t n0 = a.node_off, n1 = (size_t)b.node_off + 2 * b.n - 1;
+  int r = c->cuda(cudaMemcpyAsync(c->h_t64 + n0, c->d_t64 + n0, (n1 - n0) * sizeof(double), cudaMemcpyDeviceToHost, c->st), "mirror");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->h_tff + n0, c->d_tff + n0, (n1 - n0) * sizeof(float2), cudaMemcpyDeviceToHost, c->st), "mirror");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->h_len + c->dev_lo, c->d_len + c->dev_lo, (size_t)(c->dev_hi - c->dev_lo + 1) * sizeof(double),
+                                      cudaMemcpyDeviceToHost, c->st), "mirror");
+  r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "mirror");
+  c->dev_lo = INT32_MAX;
+  c->dev_hi = -1;
+  return r;
+}
+
 static void mark(ima_ctx *c, int item)
 {
+  sync_mirror(c);
   c->dirty_lo = std::min(c->dirty_lo, item);
   c->dirty_hi = std::max(c->dirty_hi, item);
 }
@@ -725,8 +765,10 @@ extern "C" int ima_gpu_set_genealogy(ima_ctx *c, int ci, int li, const int32_t *
   if (!c || !up0 || !up1 || !down || !time) return IMA_ERR_ARG;
   if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
   if (!c->valid(ci, li)) return c->fail(IMA_ERR_ARG, "chain %d locus %d out of range", ci, li);
+  int r = sync_mirror(c);
+  if (r) return r;
   SetOut o;
-  int r = set_one(c, c->item_of(ci, li), up0, up1, down, time, length, o);
+  r = set_one(c, c->item_of(ci, li), up0, up1, down, time, length, o);
   o.merge_into(c);
   if (r) c->err = o.msg;
   return r;
@@ -738,6 +780,7 @@ extern "C" int ima_gpu_set_genealogies(ima_ctx *c, int n, const int32_t *ci, con
 {
   if (!c || n < 0 || (n > 0 && (!ci || !li || !up0 || !up1 || !down || !time))) return IMA_ERR_ARG;
   if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
+  if (int rs = sync_mirror(c)) return rs;
   // offsets of each pair's nodes, and whether a pair repeats (then the list
   // is applied in order on one thread)
   // node offset of each pair (a context vector: the pool's threads read it)
@@ -2080,10 +2123,14 @@ extern "C" int ima_gpu_treeweight(ima_ctx *c, int ngen, const int32_t *node_off,
   r = r ? r : grow(c, &c->d_twout, &c->twout_cap, outb, "treeweight weights");
   if (r) return r;
   Carve ci{static_cast<char *>(c->d_twin)}, co{static_cast<char *>(c->d_twout)};
-  TwArgs a;
+  TwArgs a{};
   a.ngen = ngen;
   a.P = P;
   a.model = c->d_tw;
+  a.nodes = nullptr;  // host-packed genealogies
+  a.moff_start = nullptr;
+  a.mbase = nullptr;
+  a.len_out = nullptr;
   int32_t *d_perm = ci.take<int32_t>(ngen);
   int32_t *d_node_off = ci.take<int32_t>(ngen + 1), *d_up0 = ci.take<int32_t>(N), *d_pop = ci.take<int32_t>(N),
           *d_mig_off = ci.take<int32_t>(N + 1), *d_mig_p = ci.take<int32_t>(Nm),
@@ -2175,16 +2222,20 @@ extern "C" int ima_gpu_treeweight(ima_ctx *c, int ngen, const int32_t *node_off,
   return r ? r : c->cuda(cudaStreamSynchronize(c->st), "treeweight");
 }
 
-extern "C" int ima_gpu_tree_prob(ima_ctx *c, int ngroups, const int32_t *group_off, const double *pdg,
-                                 const int32_t *group_tv, double *probg, double *q, double *m, float *rows)
+// p(G) of groups of the last weights: group i = genealogies group_off[i] ..
+// group_end[i] (group_end null: group_off[i+1])
+static int tree_prob_run(ima_ctx *c, int ngroups, const int32_t *group_off, const int32_t *group_end,
+                         const double *pdg, const int32_t *group_tv, double *probg, double *q, double *m,
+                         float *rows)
 {
-  if (!c) return IMA_ERR_ARG;
   if (!c->tw_ready || c->tw_ngen < 1) return c->fail(IMA_ERR_STATE, "call ima_gpu_treeweight first");
   if (ngroups < 1 || !group_off) return c->fail(IMA_ERR_ARG, "tree_prob: bad argument");
   const TwModel &h = c->h_tw;
-  for (int i = 0; i < ngroups; i++)
-    if (group_off[i] < 0 || group_off[i + 1] < group_off[i] || group_off[i + 1] > c->tw_ngen)
-      return c->fail(IMA_ERR_ARG, "group_off[%d..%d] outside the %d genealogies", i, i + 1, c->tw_ngen);
+  for (int i = 0; i < ngroups; i++) {
+    const int e = group_end ? group_end[i] : group_off[i + 1];
+    if (group_off[i] < 0 || e < group_off[i] || e > c->tw_ngen)
+      return c->fail(IMA_ERR_ARG, "group %d (%d..%d) outside the %d genealogies", i, group_off[i], e, c->tw_ngen);
+  }
   if (group_tv)
     for (int i = 0; i < ngroups; i++)
       if (group_tv[i] < 0 || group_tv[i] >= c->tw_ntv) return c->fail(IMA_ERR_ARG, "group_tv[%d] out of range", i);
@@ -2194,12 +2245,13 @@ extern "C" int ima_gpu_tree_prob(ima_ctx *c, int ngroups, const int32_t *group_o
   const size_t G = ngroups;
   const size_t MMc = h.nomig ? 0 : h.M;
   const size_t b = carve_size({(G + 1) * 4, G * 4, G * 8, G * 8, G * nth * 8, G * (nmg ? nmg : 1) * 8,
-                               G * rowlen * 4, G * (h.T + MMc) * 4, G * (2 * h.T + MMc) * 8});
+                               G * rowlen * 4, G * (h.T + MMc) * 4, G * (2 * h.T + MMc) * 8, G * 4});
   int r = grow(c, &c->d_tpbuf, &c->tpbuf_cap, b, "tree_prob buffers");
   if (r) return r;
   Carve cv{static_cast<char *>(c->d_tpbuf)};
-  TwProbArgs a;
+  TwProbArgs a{};
   a.ngroups = ngroups;
+  a.group_end = nullptr;
   a.model = c->d_tw;
   int32_t *d_off = cv.take<int32_t>(G + 1), *d_tv = cv.take<int32_t>(G);
   double *d_pdg = cv.take<double>(G);
@@ -2212,6 +2264,7 @@ extern "C" int ima_gpu_tree_prob(ima_ctx *c, int ngroups, const int32_t *group_o
   a.rows = cv.take<float>(G * rowlen);  // kept for ima_gpu_surface_append_tree_rows
   a.sc = cv.take<int32_t>(G * (h.T + MMc));
   a.sd = cv.take<double>(G * (2 * h.T + MMc));
+  int32_t *d_end = cv.take<int32_t>(G);
   a.rowlen = rowlen;
   a.cc = c->tw_cc;
   a.mc = c->tw_mc;
@@ -2221,7 +2274,11 @@ extern "C" int ima_gpu_tree_prob(ima_ctx *c, int ngroups, const int32_t *group_o
   a.tvals = c->tw_tvals;
   a.logfact = c->d_logfact;
   a.err = c->d_twerr;
-  r = c->cuda(cudaMemcpyAsync(d_off, group_off, (G + 1) * 4, cudaMemcpyHostToDevice, c->st), "tree_prob groups");
+  r = c->cuda(cudaMemcpyAsync(d_off, group_off, (group_end ? G : G + 1) * 4, cudaMemcpyHostToDevice, c->st), "tree_prob groups");
+  if (group_end) {
+    r = r ? r : c->cuda(cudaMemcpyAsync(d_end, group_end, G * 4, cudaMemcpyHostToDevice, c->st), "tree_prob groups");
+    a.group_end = d_end;
+  }
   if (group_tv)
     r = r ? r : c->cuda(cudaMemcpyAsync(d_tv, group_tv, G * 4, cudaMemcpyHostToDevice, c->st), "tree_prob groups");
   else
@@ -2246,6 +2303,13 @@ extern "C" int ima_gpu_tree_prob(ima_ctx *c, int ngroups, const int32_t *group_o
   if (nmg) down(m, a.m, G * nmg * 8);
   if (rows) down(rows, a.rows, G * rowlen * 4);
   return r ? r : c->cuda(cudaStreamSynchronize(c->st), "tree_prob");
+}
+
+extern "C" int ima_gpu_tree_prob(ima_ctx *c, int ngroups, const int32_t *group_off, const double *pdg,
+                                 const int32_t *group_tv, double *probg, double *q, double *m, float *rows)
+{
+  if (!c) return IMA_ERR_ARG;
+  return tree_prob_run(c, ngroups, group_off, nullptr, pdg, group_tv, probg, q, m, rows);
 }
 
 extern "C" int ima_gpu_surface_append_tree_rows(ima_ctx *c, int n, const int32_t *groups)
@@ -2310,4 +2374,359 @@ extern "C" int ima_gpu_surface_get_rows(ima_ctx *c, int start, int count, int ro
   int r = c->cuda(cudaMemcpyAsync(rows, c->d_rows + (size_t)start * c->srowlen, (size_t)count * c->srowlen * 4,
                                   cudaMemcpyDeviceToHost, c->st), "surface rows");
   return r ? r : c->cuda(cudaStreamSynchronize(c->st), "surface rows");
+}
+
+// ======================================================================
+// resident population labels and the split-time update
+static int labels_alloc(ima_ctx *c)
+{
+  if (c->d_pop) return IMA_OK;
+  if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
+  const int ni = c->nitems;
+  const size_t nn = c->nnodes;
+  size_t &B = c->dev_bytes;
+  c->d_pop = dev_alloc<int32_t>(nn, B, c->st);
+  c->d_moff = dev_alloc<int32_t>(nn + ni, B, c->st);
+  c->d_inode_off = dev_alloc<int32_t>(ni + 1, B, c->st);
+  c->d_gl = dev_alloc<int32_t>(ni, B, c->st);
+  c->d_gt = dev_alloc<int32_t>(ni, B, c->st);
+  c->d_moff_start = dev_alloc<int32_t>(ni, B, c->st);
+  c->d_bcnt = dev_alloc<int32_t>(4 * (size_t)c->nchains, B, c->st);
+  c->d_mbase = dev_alloc<long long>(ni, B, c->st);
+  c->d_len_hold = dev_alloc<double>(ni, B, c->st);
+  if (!c->d_pop || !c->d_moff || !c->d_inode_off || !c->d_gl || !c->d_gt || !c->d_moff_start || !c->d_bcnt ||
+      !c->d_mbase || !c->d_len_hold)
+    return c->fail(IMA_ERR_NOMEM, "population labels");
+  std::vector<int32_t> off(ni + 1), gl(ni), gt(ni), ms(ni);
+  for (int i = 0; i < ni; i++) {
+    off[i] = c->items[i].node_off;
+    gl[i] = i % c->nloci;
+    gt[i] = i / c->nloci;
+    ms[i] = c->items[i].node_off + i;
+    if (i > 0 && off[i] != off[i - 1] + 2 * c->items[i - 1].n - 1)
+      return c->fail(IMA_ERR_STATE, "node pool is not in item order");
+  }
+  off[ni] = c->items[ni - 1].node_off + 2 * c->items[ni - 1].n - 1;
+  int r = c->cuda(cudaMemcpyAsync(c->d_inode_off, off.data(), (ni + 1) * 4ul, cudaMemcpyHostToDevice, c->st), "labels");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_gl, gl.data(), ni * 4ul, cudaMemcpyHostToDevice, c->st), "labels");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_gt, gt.data(), ni * 4ul, cudaMemcpyHostToDevice, c->st), "labels");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_moff_start, ms.data(), ni * 4ul, cudaMemcpyHostToDevice, c->st), "labels");
+  r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "labels");
+  if (r) return r;
+  c->h_mbase.assign(ni, 0);
+  c->h_mcnt.assign(ni, 0);
+  c->h_mcap.assign(ni, 0);
+  c->has_labels.assign(ni, 0);
+  return IMA_OK;
+}
+
+extern "C" int ima_gpu_set_locus_pops(ima_ctx *c, const double *hval, const int32_t *samppop)
+{
+  if (!c || !hval || !samppop) return IMA_ERR_ARG;
+  if (!c->tw_ready) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_popmodel first");
+  if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
+  const int npops = c->h_tw.npops, nl = c->nloci;
+  std::vector<double> hl(nl), h2(nl);
+  for (int li = 0; li < nl; li++) {
+    if (!(hval[li] > 0)) return c->fail(IMA_ERR_ARG, "hval[%d] must be > 0", li);
+    int ns = 0;
+    for (int p = 0; p < npops; p++) ns += samppop[(size_t)li * npops + p];
+    if (ns != c->loci[li].d.n) return c->fail(IMA_ERR_ARG, "locus %d: samppop sums to %d, not %d genes", li, ns, c->loci[li].d.n);
+    hl[li] = log(hval[li]);
+    h2[li] = 1 / (2 * hval[li]);
+  }
+  cudaSetDevice(c->device);
+  if (!c->d_rhlog) {
+    c->d_rhlog = dev_alloc<double>(nl, c->dev_bytes, c->st);
+    c->d_rh2 = dev_alloc<double>(nl, c->dev_bytes, c->st);
+    c->d_rsamp = dev_alloc<int32_t>((size_t)nl * TW_MAXPOPS, c->dev_bytes, c->st);
+    c->d_tvr = dev_alloc<double>((size_t)c->nchains * TW_MAXPOPS, c->dev_bytes, c->st);
+    if (!c->d_rhlog || !c->d_rh2 || !c->d_rsamp || !c->d_tvr) return c->fail(IMA_ERR_NOMEM, "locus populations");
+  }
+  int r = c->cuda(cudaMemcpyAsync(c->d_rhlog, hl.data(), nl * 8ul, cudaMemcpyHostToDevice, c->st), "locus pops");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_rh2, h2.data(), nl * 8ul, cudaMemcpyHostToDevice, c->st), "locus pops");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_rsamp, samppop, (size_t)nl * npops * 4, cudaMemcpyHostToDevice, c->st), "locus pops");
+  r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "locus pops");
+  if (r) return r;
+  c->h_tvr.assign((size_t)c->nchains * (npops - 1), 0.0);
+  c->locus_pops = true;
+  return IMA_OK;
+}
+
+extern "C" int ima_gpu_set_labels(ima_ctx *c, int n, const int32_t *ci, const int32_t *li, const int32_t *pop,
+                                  const int32_t *mig_off, const double *mig_t, const int32_t *mig_p)
+{
+  if (!c || n < 1 || !ci || !li || !pop || !mig_off) return IMA_ERR_ARG;
+  if (!c->tw_ready) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_popmodel first");
+  cudaSetDevice(c->device);
+  int r = labels_alloc(c);
+  if (r) return r;
+  const int ntp = 2 * c->h_tw.npops - 1;
+  size_t noff = 0, moff = 0, ev = 0;
+  for (int k = 0; k < n; k++) {
+    if (!c->valid(ci[k], li[k])) return c->fail(IMA_ERR_ARG, "pair %d: chain %d locus %d out of range", k, ci[k], li[k]);
+    const int item = c->item_of(ci[k], li[k]);
+    const int nl = 2 * c->items[item].n - 1;
+    const int32_t *mo = mig_off + moff;
+    if (mo[0] != 0) return c->fail(IMA_ERR_ARG, "pair %d: mig_off must start at 0", k);
+    for (int i = 0; i < nl; i++) {
+      if (pop[noff + i] < 0 || pop[noff + i] >= ntp) return c->fail(IMA_ERR_ARG, "pair %d node %d: population %d", k, i, pop[noff + i]);
+      if (mo[i + 1] < mo[i]) return c->fail(IMA_ERR_ARG, "pair %d: mig_off decreases at node %d", k, i);
+    }
+    const int cnt = mo[nl];
+    if (cnt > 0 && (!mig_t || !mig_p)) return c->fail(IMA_ERR_ARG, "migration events without mig_t/mig_p");
+    for (int j = 0; j < cnt; j++)
+      if (mig_p[ev + j] < 0 || mig_p[ev + j] >= ntp) return c->fail(IMA_ERR_ARG, "pair %d: migration to population %d", k, mig_p[ev + j]);
+    // room for the item's events: its own range, or a new one at the end of the pool
+    if (cnt > c->h_mcap[item]) {
+      if (c->mig_used + cnt > c->mig_cap) {
+        size_t cap = c->mig_cap ? c->mig_cap * 2 : 4096;
+        while (cap < c->mig_used + cnt) cap *= 2;
+        double *nt = dev_alloc<double>(cap, c->dev_bytes, c->st);
+        int32_t *np_ = dev_alloc<int32_t>(cap, c->dev_bytes, c->st);
+        if (!nt || !np_) return c->fail(IMA_ERR_NOMEM, "migration events (%zu)", cap);
+        if (c->mig_used) {
+          r = c->cuda(cudaMemcpyAsync(nt, c->d_mig_t, c->mig_used * 8, cudaMemcpyDeviceToDevice, c->st), "events");
+          r = r ? r : c->cuda(cudaMemcpyAsync(np_, c->d_mig_p, c->mig_used * 4, cudaMemcpyDeviceToDevice, c->st), "events");
+          if (r) return r;
+        }
+        cudaStreamSynchronize(c->st);
+        cudaFree(c->d_mig_t);
+        cudaFree(c->d_mig_p);
+        c->d_mig_t = nt;
+        c->d_mig_p = np_;
+        c->mig_cap = cap;
+      }
+      c->h_mbase[item] = (long long)c->mig_used;
+      c->h_mcap[item] = cnt;
+      c->mig_used += cnt;
+    }
+    c->h_mcnt[item] = cnt;
+    const size_t no = c->items[item].node_off;
+    r = c->cuda(cudaMemcpyAsync(c->d_pop + no, pop + noff, nl * 4ul, cudaMemcpyHostToDevice, c->st), "labels");
+    r = r ? r : c->cuda(cudaMemcpyAsync(c->d_moff + no + item, mo, (nl + 1) * 4ul, cudaMemcpyHostToDevice, c->st), "labels");
+    r = r ? r : c->cuda(cudaMemcpyAsync(c->d_mbase + item, &c->h_mbase[item], 8, cudaMemcpyHostToDevice, c->st), "labels");
+    if (cnt) {
+      r = r ? r : c->cuda(cudaMemcpyAsync(c->d_mig_t + c->h_mbase[item], mig_t + ev, cnt * 8ul, cudaMemcpyHostToDevice, c->st), "labels");
+      r = r ? r : c->cuda(cudaMemcpyAsync(c->d_mig_p + c->h_mbase[item], mig_p + ev, cnt * 4ul, cudaMemcpyHostToDevice, c->st), "labels");
+    }
+    if (r) return r;
+    c->has_labels[item] = 1;
+    noff += nl;
+    moff += nl + 1;
+    ev += cnt;
+  }
+  return c->cuda(cudaStreamSynchronize(c->st), "labels");
+}
+
+extern "C" int ima_gpu_get_times(ima_ctx *c, int ci, int li, double *time, int32_t *nmig, double *mig_t)
+{
+  if (!c || !time) return IMA_ERR_ARG;
+  if (!c->valid(ci, li)) return c->fail(IMA_ERR_ARG, "chain %d locus %d out of range", ci, li);
+  const int item = c->item_of(ci, li);
+  const ItemDev &it = c->items[item];
+  cudaSetDevice(c->device);
+  int r = c->cuda(cudaMemcpyAsync(time, c->d_t64 + it.node_off, (2 * it.n - 1) * 8ul, cudaMemcpyDeviceToHost, c->st), "times");
+  const int cnt = (c->d_pop && c->has_labels[item]) ? c->h_mcnt[item] : 0;
+  if (nmig) *nmig = cnt;
+  if (mig_t && cnt)
+    r = r ? r : c->cuda(cudaMemcpyAsync(mig_t, c->d_mig_t + c->h_mbase[item], cnt * 8ul, cudaMemcpyDeviceToHost, c->st), "times");
+  return r ? r : c->cuda(cudaStreamSynchronize(c->st), "times");
+}
+
+// also uploads pending host edits: the resident functions read the device pools
+static int chains_ready(ima_ctx *c, int nch, const int32_t *chains)
+{
+  if (!c->d_pop || !c->locus_pops) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_labels and ima_gpu_set_locus_pops first");
+  cudaSetDevice(c->device);
+  if (int r = flush(c)) return r;
+  for (int k = 0; k < nch; k++) {
+    if (chains[k] < 0 || chains[k] >= c->nchains) return c->fail(IMA_ERR_ARG, "chain %d out of range", chains[k]);
+    for (int l = 0; l < k; l++)
+      if (chains[l] == chains[k]) return c->fail(IMA_ERR_ARG, "chain %d listed twice", chains[k]);
+    for (int li = 0; li < c->nloci; li++)
+      if (!c->has_labels[c->item_of(chains[k], li)] || !c->has_tree[c->item_of(chains[k], li)])
+        return c->fail(IMA_ERR_STATE, "chain %d locus %d has no genealogy or labels", chains[k], li);
+  }
+  return IMA_OK;
+}
+
+static void* rsel(ima_ctx *c, size_t bytes)
+{
+  if (bytes > c->rsel_cap) {
+    cudaStreamSynchronize(c->st);
+    cudaFree(c->d_rsel);
+    c->d_rsel = dev_alloc<char>(bytes, c->dev_bytes, c->st);
+    c->rsel_cap = c->d_rsel ? bytes : 0;
+  }
+  return c->d_rsel;
+}
+
+static void dev_newer(ima_ctx *c, int nch, const int32_t *chains)
+{
+  for (int k = 0; k < nch; k++) {
+    c->dev_lo = std::min(c->dev_lo, chains[k] * c->nloci);
+    c->dev_hi = std::max(c->dev_hi, chains[k] * c->nloci + c->nloci - 1);
+  }
+}
+
+extern "C" int ima_gpu_rubber_band(ima_ctx *c, int nch, const int32_t *chains, const int32_t *period,
+                                   const double *oldt, const double *newt, const double *t_u, const double *t_d,
+                                   int inverse, int32_t *counts)
+{
+  if (!c || nch < 1 || !chains || !period || !oldt || !newt || !t_u || !t_d) return IMA_ERR_ARG;
+  if (!c->tw_ready) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_popmodel first");
+  int r = chains_ready(c, nch, chains);
+  if (r) return r;
+  const int last = c->h_tw.npops - 1;
+  std::vector<double> prm(5 * (size_t)nch);
+  for (int k = 0; k < nch; k++) {
+    if (period[k] < 0 || period[k] >= last) return c->fail(IMA_ERR_ARG, "period %d out of range", period[k]);
+    if (!(oldt[k] > t_u[k]) || !(newt[k] > t_u[k]) || !(oldt[k] < t_d[k]) || !(newt[k] < t_d[k]))
+      return c->fail(IMA_ERR_ARG, "chain %d: split times must lie inside (t_u, t_d)", chains[k]);
+    prm[5 * k + 0] = period[k];
+    prm[5 * k + 1] = inverse ? newt[k] : oldt[k];  // going back: from newt to oldt
+    prm[5 * k + 2] = inverse ? oldt[k] : newt[k];
+    prm[5 * k + 3] = t_u[k];
+    prm[5 * k + 4] = t_d[k];
+  }
+  cudaSetDevice(c->device);
+  char *buf = static_cast<char *>(rsel(c, 256 + nch * 4ul + 256 + 40ul * nch));
+  if (!buf) return c->fail(IMA_ERR_NOMEM, "band buffers");
+  int32_t *d_ch = reinterpret_cast<int32_t *>(buf);
+  double *d_prm = reinterpret_cast<double *>(buf + (nch * 4 + 255) / 256 * 256 + 256);
+  r = c->cuda(cudaMemcpyAsync(d_ch, chains, nch * 4ul, cudaMemcpyHostToDevice, c->st), "band");
+  r = r ? r : c->cuda(cudaMemcpyAsync(d_prm, prm.data(), prm.size() * 8, cudaMemcpyHostToDevice, c->st), "band");
+  r = r ? r : c->cuda(cudaMemsetAsync(c->d_bcnt, 0, 16ul * nch, c->st), "band");
+  if (r) return r;
+  BandArgs a{};
+  a.items = c->d_items;
+  a.nodes = c->d_nodes;
+  a.t64 = c->d_t64;
+  a.tff = c->d_tff;
+  a.moff = c->d_moff;
+  a.mbase = c->d_mbase;
+  a.mig_t = c->d_mig_t;
+  a.chains = d_ch;
+  a.prm = d_prm;
+  a.nch = nch;
+  a.nloci = c->nloci;
+  a.last = last;
+  a.inverse = inverse ? 1 : 0;
+  a.counts = c->d_bcnt;
+  a.len = c->d_len;
+  a.len_hold = c->d_len_hold;
+  c->launch(IMA_K_TREEWEIGHT, 0.0, [&] { launch_band(a, c->st); });
+  r = c->cuda(cudaGetLastError(), "band launch");
+  if (!r && counts && !inverse) r = c->cuda(cudaMemcpyAsync(counts, c->d_bcnt, 16ul * nch, cudaMemcpyDeviceToHost, c->st), "band counts");
+  r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "band");
+  if (!r) dev_newer(c, nch, chains);
+  return r;
+}
+
+extern "C" int ima_gpu_chain_weights(ima_ctx *c, int nch, const int32_t *chains, const double *tvals,
+                                     double *probg, double *q, double *m)
+{
+  if (!c || nch < 1 || !chains || !tvals) return IMA_ERR_ARG;
+  if (!c->tw_ready) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_popmodel first");
+  int r = chains_ready(c, nch, chains);
+  if (r) return r;
+  const TwModel &h = c->h_tw;
+  const int npops = h.npops, nsplit = npops - 1, nl = c->nloci, ni = c->nitems;
+  for (int k = 0; k < nch; k++)
+    for (int s = 0; s < nsplit; s++) c->h_tvr[(size_t)chains[k] * nsplit + s] = tvals[(size_t)k * nsplit + s];
+  // the chains' genealogies, most events first; event scratch per item
+  std::vector<int32_t> ev(ni, 0), sel;
+  long long Emax = 0;
+  for (int k = 0; k < nch; k++)
+    for (int li = 0; li < nl; li++) {
+      const int item = c->item_of(chains[k], li);
+      const long long E = c->items[item].n - 1 + (long long)c->h_mcnt[item] + nsplit;
+      ev[item] = (int32_t)E;
+      Emax = std::max(Emax, E);
+      sel.push_back(item);
+    }
+  int P = 32;
+  while (P < Emax) P <<= 1;
+  if (P > (1 << 20) || !tw_fits(P)) return c->fail(IMA_ERR_TOO_LARGE, "a genealogy has %lld events", Emax);
+  std::vector<int32_t> perm(sel.size()), cnt((size_t)Emax + 2, 0);
+  for (int item : sel) cnt[(size_t)(Emax - ev[item])]++;
+  for (size_t i = 1; i < cnt.size(); i++) cnt[i] += cnt[i - 1];
+  for (int k = (int)sel.size() - 1; k >= 0; k--) perm[--cnt[(size_t)(Emax - ev[sel[k]])]] = sel[k];
+  std::vector<long long> evoff(ni + 1, 0);
+  for (int i = 0; i < ni; i++) evoff[i + 1] = evoff[i] + ev[i];
+  const size_t Etot = (size_t)evoff[ni], ns = sel.size(), T = h.T, MM = h.M;
+  cudaSetDevice(c->device);
+  const size_t inb = carve_size({ns * 4, (ni + 1) * 8ul, Etot * 8, Etot * 4, ni * 4ul});
+  const size_t outb = carve_size({ni * T * 4, ni * MM * 4, ni * 4ul, ni * T * 8, ni * T * 8, ni * MM * 8, 2ul * ni * 8});
+  r = grow(c, &c->d_twin, &c->twin_cap, inb, "treeweight scratch");
+  r = r ? r : grow(c, &c->d_twout, &c->twout_cap, outb, "treeweight weights");
+  if (r) return r;
+  Carve ci_{static_cast<char *>(c->d_twin)}, co{static_cast<char *>(c->d_twout)};
+  TwArgs a{};
+  a.ngen = (int)ns;
+  a.P = P;
+  a.model = c->d_tw;
+  int32_t *d_perm = ci_.take<int32_t>(ns);
+  long long *d_evoff = ci_.take<long long>(ni + 1);
+  a.perm = d_perm;
+  a.ev_off = d_evoff;
+  a.ev_t = ci_.take<double>(Etot);
+  a.ev_c = ci_.take<uint32_t>(Etot);
+  a.ev_n = ci_.take<int32_t>(ni);
+  a.node_off = c->d_inode_off;
+  a.up0 = nullptr;
+  a.nodes = c->d_nodes;
+  a.time = c->d_t64;
+  a.pop = c->d_pop;
+  a.mig_off = c->d_moff;
+  a.moff_start = c->d_moff_start;
+  a.mbase = c->d_mbase;
+  a.mig_t = c->d_mig_t;
+  a.mig_p = c->d_mig_p;
+  a.gen_locus = c->d_gl;
+  a.gen_tv = c->d_gt;
+  a.tvals = c->d_tvr;
+  a.hlog = c->d_rhlog;
+  a.h2term = c->d_rh2;
+  a.samppop = c->d_rsamp;
+  a.cc = co.take<int32_t>(ni * T);
+  a.mc = co.take<int32_t>(ni * MM);
+  a.mignum = co.take<int32_t>(ni);
+  a.hcc = co.take<double>(ni * T);
+  a.fc = co.take<double>(ni * T);
+  a.fm = co.take<double>(ni * MM);
+  a.lens = co.take<double>(2ul * ni);
+  a.len_out = c->d_len;
+  a.err = c->d_twerr;
+  r = c->cuda(cudaMemcpyAsync(d_perm, perm.data(), ns * 4, cudaMemcpyHostToDevice, c->st), "weights");
+  r = r ? r : c->cuda(cudaMemcpyAsync(d_evoff, evoff.data(), (ni + 1) * 8ul, cudaMemcpyHostToDevice, c->st), "weights");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_tvr, c->h_tvr.data(), c->h_tvr.size() * 8, cudaMemcpyHostToDevice, c->st), "weights");
+  r = r ? r : c->cuda(cudaMemsetAsync(c->d_twerr, 0, 8, c->st), "weights");
+  if (r) return r;
+  c->tw_ngen = 0;
+  int lr = 0;
+  c->launch(IMA_K_TREEWEIGHT, 0.0, [&] { lr = launch_treeweight(a, h, c->st); });
+  if (lr < 0) return c->fail(IMA_ERR_TOO_LARGE, "treeweight: shared memory for %d events", P);
+  c->launches += lr - 1;
+  r = c->cuda(cudaGetLastError(), "weights launch");
+  r = r ? r : tw_check_err(c, "chain weights");
+  if (r) return r;
+  dev_newer(c, nch, chains);  // the lengths of these items changed on the device
+  c->tw_ngen = ni;
+  c->tw_ntv = c->nchains;
+  c->tw_cc = a.cc;
+  c->tw_mc = a.mc;
+  c->tw_hcc = a.hcc;
+  c->tw_fc = a.fc;
+  c->tw_fm = a.fm;
+  c->tw_tvals = c->d_tvr;
+  std::vector<int32_t> goff(nch), gend(nch);
+  for (int k = 0; k < nch; k++) {
+    goff[k] = chains[k] * nl;
+    gend[k] = chains[k] * nl + nl;
+  }
+  std::vector<double> pg(nch);
+  r = tree_prob_run(c, nch, goff.data(), gend.data(), nullptr, chains, probg ? probg : pg.data(), q, m, nullptr);
+  return r;
 }

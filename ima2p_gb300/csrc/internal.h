@@ -177,6 +177,13 @@ struct TwArgs {
   double *ev_t;                            // sorted event times (pass 1 -> pass 2)
   uint32_t *ev_c;                          // sorted event codes
   int32_t *ev_n;                           // [ngen] events, -1 when rejected
+  // resident genealogies (null for host-packed inputs): up0 from the node
+  // records, migration offsets of genealogy g at mig_off + moff_start[g]
+  // (relative to its events, which start at mig_t/mig_p + mbase[g])
+  const NodeRec *nodes;
+  const int32_t *moff_start;
+  const long long *mbase;
+  double *len_out;                         // [ngen] G->length also written here, or null
 };
 struct TwProbArgs {
   int ngroups;
@@ -190,7 +197,24 @@ struct TwProbArgs {
   int32_t *err;
   int32_t *sc;                             // [ngroups][T+M] summed counts (cc, mc)
   double *sd;                              // [ngroups][2T+M] summed fc, hcc, fm
+  const int32_t *group_end;                // group i ends at group_end[i] (null: group_off[i+1])
 };
+// the split-time update's rubber band (changet_RY1) on resident genealogies
+struct BandArgs {
+  const ItemDev *items;
+  const NodeRec *nodes;
+  double *t64;
+  float2 *tff;
+  const int32_t *moff;                     // per item: nl+1 relative offsets at node_off + item
+  const long long *mbase;                  // per item: first migration event
+  double *mig_t;
+  const int32_t *chains;                   // [nch]
+  const double *prm;                       // [nch][5]: period, o, n, t_u, t_d
+  int nch, nloci, last, inverse;
+  int32_t *counts;                         // [nch][4]: ecd, ecu, emd, emu (forward)
+  double *len, *len_hold;                  // per item: saved going forward, restored on the way back
+};
+int launch_band(const BandArgs &a, cudaStream_t st);
 bool tw_fits(int P);                       // P events fit one warp's shared memory
 int launch_treeweight(const TwArgs &a, const TwModel &h, cudaStream_t st);
 int launch_tree_prob(const TwProbArgs &a, const TwModel &h, cudaStream_t st);

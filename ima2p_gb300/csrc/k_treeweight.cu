@@ -76,16 +76,19 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_tw_events(TwArgs a, int wpb)
 
   const int a0 = a.node_off[g], nl = a.node_off[g + 1] - a0, ng = (nl + 1) >> 1;
   const double *tv = a.tvals + (size_t)a.gen_tv[g] * nsplit;
-  const int32_t *up0 = a.up0 + a0, *pp = a.pop + a0, *mo = a.mig_off + a0;
+  const int32_t *up0 = a.nodes ? nullptr : a.up0 + a0, *pp = a.pop + a0;
+  const int32_t *mo = a.mig_off + (a.moff_start ? a.moff_start[g] : a0);
+  const long long mb = a.mbase ? a.mbase[g] : 0;
   const double *tm = a.time + a0;
   const int nmig = mo[nl] - mo[0];
+  auto daughter = [&](int i) { return a.nodes ? (int)a.nodes[a0 + i].up0 : up0[i]; };
 
   // roottime: the root's coalescence, the latest one (times are >= 0, so
   // their bit patterns order as the values do)
   int bad = 0;
   long long rtb = 0;
   for (int i = ng + lane; i < nl; i += 32) {
-    const int u = up0[i];
+    const int u = daughter(i);
     if ((unsigned)u >= (unsigned)nl) bad = TW_E_POP;
     else rtb = max(rtb, __double_as_longlong(tm[u]));
   }
@@ -125,15 +128,15 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_tw_events(TwArgs a, int wpb)
         bad = TW_E_POP;
       } else {
         if (i >= ng) {
-          ev_t[e] = tm[up0[i]];
+          ev_t[e] = tm[daughter(i)];
           ev_c[e] = ev_pack(EV_COAL, nowpop, 0, e);
           e++;
         }
         for (int j = m0; j < m1; j++) {
-          const double t = a.mig_t[j];
+          const double t = a.mig_t[mb + j];
           const int per = tw_period(tv, nsplit, t);
           while (M.pop_e[nowpop] <= per && M.pop_e[nowpop] != -1) nowpop = M.pop_down[nowpop];
-          const int to = a.mig_p[j];
+          const int to = a.mig_p[mb + j];
           if ((unsigned)to >= (unsigned)ntp || to == nowpop) {
             bad = TW_E_POP;
             break;
@@ -370,9 +373,11 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_tw_sweep(TwArgs a, int wpb, int
     a.fm[oM + i] = fm_s[i];
   }
   if (gl == (MERGE ? npops : 0)) {
+    const int32_t *mo = a.mig_off + (a.moff_start ? a.moff_start[g] : a0);
     a.lens[2 * (size_t)g] = len;
     a.lens[2 * (size_t)g + 1] = tlen;
-    a.mignum[g] = a.mig_off[a0 + nl] - a.mig_off[a0];
+    a.mignum[g] = mo[nl] - mo[0];
+    if (a.len_out) a.len_out[g] = len;
   }
 }
 
@@ -633,7 +638,7 @@ __global__ void __launch_bounds__(TP_BS) k_tp_cells(TwProbArgs a)
       stride = M.M;
     }
     double sum = 0.0;
-    const int g1 = a.group_off[grp + 1];
+    const int g1 = a.group_end ? a.group_end[grp] : a.group_off[grp + 1];
 #pragma unroll 8
     for (int g = a.group_off[grp]; g < g1; g++) sum += src[(size_t)g * stride];
     a.sd[(size_t)grp * Qd + q] = sum;
@@ -643,7 +648,7 @@ __global__ void __launch_bounds__(TP_BS) k_tp_cells(TwProbArgs a)
     const int32_t *src = q < T ? a.cc + q : a.mc + (q - T);
     const int stride = q < T ? T : M.M;
     int sum = 0;
-    const int g1 = a.group_off[grp + 1];
+    const int g1 = a.group_end ? a.group_end[grp] : a.group_off[grp + 1];
 #pragma unroll 8
     for (int g = a.group_off[grp]; g < g1; g++) sum += src[(size_t)g * stride];
     a.sc[(size_t)grp * Qi + q] = sum;
@@ -722,7 +727,8 @@ __global__ void __launch_bounds__(128) k_tp_final(TwProbArgs a)
   if (!M.nomig)
     for (int i = 0; i < M.nchk && checkm; i++) {
       int cnt = 0;
-      for (int g = a.group_off[grp]; g < a.group_off[grp + 1]; g++) cnt += a.mc[(size_t)g * M.M + M.chk_idx[i]];
+      const int g1 = a.group_end ? a.group_end[grp] : a.group_off[grp + 1];
+      for (int g = a.group_off[grp]; g < g1; g++) cnt += a.mc[(size_t)g * M.M + M.chk_idx[i]];
       checkm = cnt == 0;
     }
   double psum = 0;
@@ -743,6 +749,71 @@ __global__ void __launch_bounds__(128) k_tp_final(TwProbArgs a)
   }
 }
 
+// The rubber band of changet_RY1 (update_t_RY.cpp:59-86, 279-335 going
+// forward, 444-491 back) on every locus of the listed chains, a block per
+// chain-locus: node times of non-root edges in (t_u, o] go through
+// beforesplit, those in (o, t_d) through aftersplit, with o -> n; migration
+// times alike.  The float-float copy of each moved time follows it.  Going
+// forward the chain's counts are added up (each node time twice, once per
+// daughter edge, as the reference counts them) and the item's length is
+// saved; going back (o and n exchanged by the caller) the length is restored.
+__global__ void __launch_bounds__(128) k_band(BandArgs a)
+{
+  const int c = blockIdx.x / a.nloci, li = blockIdx.x % a.nloci;
+  const int item = a.chains[c] * a.nloci + li;
+  const ItemDev it = a.items[item];
+  const int nl = 2 * it.n - 1, off = it.node_off;
+  const double *P = a.prm + 5 * (size_t)c;
+  const int period = (int)P[0];
+  const double o = P[1], n = P[2], tu = P[3], td = P[4];
+  auto band = [&](double t, int *lo, int *hi) -> double {
+    if (t <= o && t > tu) {
+      (*lo)++;
+      return period == 0 ? t * n / o : tu + (t - tu) * (n - tu) / (o - tu);
+    }
+    if (t > o && t < td) {
+      (*hi)++;
+      return period == a.last - 1 ? t + n - o : td - (td - n) * (td - t) / (td - o);
+    }
+    return t;
+  };
+  int lo = 0, hi = 0, mlo = 0, mhi = 0;
+  const int32_t *mo = a.moff + off + item;
+  const long long mb = a.mbase[item];
+  for (int k = threadIdx.x; k < nl; k += blockDim.x) {
+    if (a.nodes[off + k].down == -1) continue;
+    const double t = a.t64[off + k];
+    const int moved = lo + hi;
+    const double tn = band(t, &lo, &hi);
+    if (lo + hi != moved) {
+      a.t64[off + k] = tn;
+      const float h = (float)tn;
+      a.tff[off + k] = make_float2(h, (float)(tn - (double)h));
+    }
+    for (int j = mo[k]; j < mo[k + 1]; j++) a.mig_t[mb + j] = band(a.mig_t[mb + j], &mlo, &mhi);
+  }
+  if (!a.inverse) {
+    for (int d = 16; d; d >>= 1) {
+      lo += __shfl_xor_sync(~0u, lo, d);
+      hi += __shfl_xor_sync(~0u, hi, d);
+      mlo += __shfl_xor_sync(~0u, mlo, d);
+      mhi += __shfl_xor_sync(~0u, mhi, d);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      if (hi) atomicAdd(&a.counts[4 * c + 0], hi);
+      if (lo) atomicAdd(&a.counts[4 * c + 1], lo);
+      if (mhi) atomicAdd(&a.counts[4 * c + 2], mhi);
+      if (mlo) atomicAdd(&a.counts[4 * c + 3], mlo);
+    }
+  }
+  if (threadIdx.x == 0) {
+    if (a.inverse)
+      a.len[item] = a.len_hold[item];
+    else
+      a.len_hold[item] = a.len[item];
+  }
+}
+
 // rows[groups[i]] -> dst + i * rowlen (a warp per row)
 __global__ void __launch_bounds__(128) k_gather_rows(const float *rows, int rowlen, const int32_t *groups, int n,
                                                      float *dst)
@@ -754,6 +825,13 @@ __global__ void __launch_bounds__(128) k_gather_rows(const float *rows, int rowl
 }
 
 }  // namespace
+
+int launch_band(const BandArgs &a, cudaStream_t st)
+{
+  if (a.nch < 1) return 0;
+  k_band<<<a.nch * a.nloci, 128, 0, st>>>(a);
+  return 0;
+}
 
 int launch_gather_rows(const float *rows, int rowlen, const int32_t *groups, int n, float *dst, cudaStream_t st)
 {

@@ -322,3 +322,89 @@ def changet_ry1_sweep(cs: ChainSet, periods, rng, tprior, npops, backend, gbeta=
         cs.time = np.where(rej[nc], back_t, cs.time)
         cs.mig_t = np.where(rej[mc], back_m, cs.mig_t)
     return accept
+
+
+class ResidentChainSet:
+    """Every chain's state resident in a context for device sweeps: the
+    genealogies and their population labels stay on the GPU and the rubber
+    band moves their times there (ima_gpu_rubber_band); weights, p(G) and
+    likelihoods are computed in place (ima_gpu_chain_weights, ima_gpu_eval);
+    only the generator draws, the per-chain counts and sums and the
+    decisions pass through the host.  ctx: the loci added, ima_gpu_set_chains
+    (1, nch) and the population model set."""
+
+    def __init__(self, ctx, gens, tvals, betas, hval, samppop, u, kappa=None, precision=api.PREC_FP64):
+        self.ctx = ctx
+        self.nch, self.nl = len(gens), len(gens[0])
+        self.tvals = np.array(tvals, np.float64).reshape(self.nch, -1).copy()
+        self.beta = np.asarray(betas, np.float64).copy()
+        self.u = np.asarray(u, np.float64)
+        self.kappa = np.ones(self.nl) if kappa is None else np.asarray(kappa, np.float64)
+        self.prec = precision
+        self.ci = np.repeat(np.arange(self.nch, dtype=np.int32), self.nl)
+        self.li = np.tile(np.arange(self.nl, dtype=np.int32), self.nch)
+        flat = [lg for row in gens for lg in row]
+        ctx.set_genealogies(self.ci, self.li, np.concatenate([g.g.up0 for g in flat]),
+                            np.concatenate([g.g.up1 for g in flat]), np.concatenate([g.g.down for g in flat]),
+                            np.concatenate([g.g.time for g in flat]), length=np.full(len(flat), -1.0))
+        ctx.set_labels(self.ci, self.li, flat)
+        ctx.set_locus_pops(hval, samppop)
+        self.chains = np.arange(self.nch, dtype=np.int32)
+        self.probg, _, _ = ctx.chain_weights(self.chains, self.tvals)
+        self.pdg = self._eval()
+        ctx.commit(self.ci, self.li, np.ones(len(self.ci), np.uint8))
+        self.pdgsum = self._sums(self.pdg)
+
+    def _eval(self):
+        r, _ = self.ctx.eval(self.ci, self.li, np.tile(self.u, self.nch), np.tile(self.kappa, self.nch),
+                             precision=self.prec)
+        return r.reshape(self.nch, self.nl)
+
+    def _sums(self, pdg):
+        s = np.zeros(self.nch)
+        for li in range(self.nl):
+            s = s + pdg[:, li]
+        return s
+
+    def sweep(self, periods, rng, tprior, npops, gbeta=1.0):
+        """One changet_RY1 per chain, chains in order (draws as in the
+        sequential run); returns the accept flags."""
+        nch, last = self.nch, npops - 1
+        periods = np.asarray(periods, np.int64)
+        rows = np.arange(nch)
+        oldt = self.tvals[rows, periods].copy()
+        t_u = np.where(periods == 0, 0.0, self.tvals[rows, np.maximum(periods - 1, 0)])
+        t_d = np.where(periods == last - 1, TIMEMAX, self.tvals[rows, np.minimum(periods + 1, last - 1)])
+        newt, logU = np.zeros(nch), np.zeros(nch)
+        for c in range(nch):
+            k = int(periods[c])
+            newt[c] = getnewt(rng, k, max(tprior[k][0], float(t_u[c])), min(tprior[k][1], float(t_d[c])),
+                              float(oldt[c]), self.nl, npops)
+            logU[c] = math.log(rng.uniform())
+        counts = self.ctx.rubber_band(self.chains, periods, oldt, newt, t_u, t_d)
+        tv_new = self.tvals.copy()
+        tv_new[rows, periods] = newt
+        probg_new, _, _ = self.ctx.chain_weights(self.chains, tv_new)
+        pdg_new = self._eval()
+        pdgnewsum = self._sums(pdg_new)
+        accept = np.zeros(nch, bool)
+        for c in range(nch):
+            ecd, ecu, emd, emu = (int(v) for v in counts[c])
+            ecd //= 2
+            ecu //= 2
+            t_u_hterm = (newt[c] - t_u[c]) / (oldt[c] - t_u[c])
+            t_d_hterm = 1.0 if periods[c] == last - 1 else (t_d[c] - newt[c]) / (t_d[c] - oldt[c])
+            tpw = gbeta * (float(pdgnewsum[c]) - float(self.pdgsum[c]))
+            tpw += float(probg_new[c]) - float(self.probg[c])
+            mh = float(self.beta[c]) * tpw + (ecd + emd) * math.log(t_d_hterm) + (ecu + emu) * math.log(t_u_hterm)
+            accept[c] = logU[c] < min(1.0, mh)
+        self.ctx.commit(self.ci, self.li, np.repeat(accept.astype(np.uint8), self.nl))
+        self.pdg[accept] = pdg_new[accept]
+        self.pdgsum[accept] = pdgnewsum[accept]
+        self.probg[accept] = probg_new[accept]
+        self.tvals[rows[accept], periods[accept]] = newt[accept]
+        rej = np.flatnonzero(~accept)
+        if len(rej):
+            self.ctx.rubber_band(self.chains[rej], periods[rej], oldt[rej], newt[rej], t_u[rej], t_d[rej],
+                                 inverse=True)
+        return accept

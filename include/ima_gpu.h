@@ -312,6 +312,46 @@ int ima_gpu_tree_prob(ima_ctx *ctx, int ngroups, const int32_t *group_off, const
  * then see every appended row.  IMA_ERR_STATE: the resident surface has
  * another shape or per-genealogy normalisers. */
 int ima_gpu_surface_append_tree_rows(ima_ctx *ctx, int n, const int32_t *groups);
+/* ------------------------- resident labels and the split-time update
+ * For device-resident chains: the population labels and migration events of
+ * every chain-locus stay on the device with its genealogy, and the
+ * split-time update changet_RY1 (update_t_RY.cpp:223-518) moves their times
+ * there.  The host keeps the generator draws and the Metropolis-Hastings
+ * decision.  Host genealogy uploads (ima_gpu_set_genealogy(ies), set_pi,
+ * set_alleles) after device moves first copy the device's times back, so
+ * the two never overwrite each other.
+ *
+ * L[li].hval and L[li].samppop[npops] of every locus (after
+ * ima_gpu_set_popmodel and ima_gpu_set_chains). */
+int ima_gpu_set_locus_pops(ima_ctx *ctx, const double *hval, const int32_t *samppop);
+/* gtree[].pop and gtree[].mig[] of the chain-loci (ci[k], li[k]); packed per
+ * pair: pop[2n-1], mig_off[2n] (the pair's events, node by node, from 0),
+ * mig_t/mig_p (times, destination populations). */
+int ima_gpu_set_labels(ima_ctx *ctx, int n, const int32_t *ci, const int32_t *li, const int32_t *pop,
+                       const int32_t *mig_off, const double *mig_t, const int32_t *mig_p);
+/* The device's node times [2n-1] and (mig_t may be NULL) migration times of
+ * a chain-locus; *nmig = its number of events. */
+int ima_gpu_get_times(ima_ctx *ctx, int ci, int li, double *time, int32_t *nmig, double *mig_t);
+/* changet_RY1's moves (update_t_RY.cpp:279-335; beforesplit/aftersplit
+ * :59-86) on every locus of the nch chains: node times of non-root edges and
+ * migration times in (t_u, oldt] and (oldt, t_d) of chain k's period
+ * period[k] go to their image under oldt -> newt.  counts (may be NULL)
+ * [nch][4] = ecd, ecu, emd, emu as the reference counts them (node times
+ * once per daughter edge).  inverse = 1 moves them back (:444-491) and
+ * restores the genealogies' lengths. */
+int ima_gpu_rubber_band(ima_ctx *ctx, int nch, const int32_t *chains, const int32_t *period,
+                        const double *oldt, const double *newt, const double *t_u, const double *t_d,
+                        int inverse, int32_t *counts);
+/* treeweight of every locus of the nch chains from the resident genealogies
+ * and labels, with split times tvals [nch][npops-1] (C[ci]->tvals); the
+ * genealogies' lengths (G->length) are updated on the device for the
+ * likelihoods; then sum_treeinfo and initialize_integrate_tree_prob per chain:
+ * probg [nch], q [nch][nth], m [nch][nmg] (q, m may be NULL).  The weights
+ * stay available to ima_gpu_tree_prob (genealogy index = chain * nloci +
+ * locus). */
+int ima_gpu_chain_weights(ima_ctx *ctx, int nch, const int32_t *chains, const double *tvals,
+                          double *probg, double *q, double *m);
+
 /* Copy surface rows start .. start+count to the host ([count][rowlen]), e.g.
  * to write them with ima_ti_write_binary.  rowlen must be the surface's
  * (IMA_ERR_ARG otherwise). */

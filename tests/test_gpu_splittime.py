@@ -61,3 +61,65 @@ def test_batched_sweep_follows_the_reference():
     assert np.array_equal(cs.time[cs.edge], case.times[cs.edge])
     assert np.array_equal(cs.mig_t, case.migt)
     ctx.close()
+
+
+def test_resident_sweep_follows_the_reference():
+    """ResidentChainSet: genealogies, labels and times stay on the GPU; the
+    rubber band moves them there (ima_gpu_rubber_band), the weights are
+    computed in place (ima_gpu_chain_weights).  Same decisions and times as
+    the reference's changet_RY1; then a host upload of one genealogy leaves
+    every other chain-locus as the device had it."""
+    case = RyCase()
+    ctx = api.Context(0)
+    for q in case.seqs:
+        ctx.add_locus_is(q)
+    ctx.set_chains(1, case.nch)
+    ctx.set_popmodel(case.pm, *case.priors())
+    cs = splittime.ResidentChainSet(ctx, case.fresh_gens(), [case.d["tv0"]] * case.nch, case.betas,
+                                    np.ones(case.nl), case.samps, case.us)
+    rng = api.MT19937(case.seed)
+    res = []
+    for s0 in range(0, len(case.steps), case.nch):
+        periods = [case.steps[s0 + c][1] for c in range(case.nch)]
+        acc = cs.sweep(periods, rng, case.tprior, case.npops)
+        for c in range(case.nch):
+            res.append((int(acc[c]), float(cs.tvals[c, periods[c]]), float(cs.probg[c]), float(cs.pdgsum[c])))
+    res, ref = np.array(res), case.res
+    assert np.array_equal(res[:, 0], ref[:, 0])
+    assert np.array_equal(res[:, 1], ref[:, 1])
+    np.testing.assert_allclose(res[:, 2], ref[:, 2], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(res[:, 3], ref[:, 3], rtol=1e-12)
+    base = case.fresh_gens()
+    off = 0
+    moff = 0
+    for ci in range(case.nch):
+        for li in range(case.nl):
+            g = base[ci][li]
+            nl = len(g.pop)
+            t, m = ctx.get_times(ci, li, nl)
+            edge = g.g.down != -1
+            assert np.array_equal(t[edge], case.times[off:off + nl][edge])
+            assert np.array_equal(m, case.migt[moff:moff + len(m)])
+            off += nl
+            moff += len(m)
+    # a host upload of the first and last chain-locus after device moves:
+    # the range upload spans every other one, which must keep the device's
+    # times and lengths
+    before = cs._eval()
+    ends = [(0, 0), (case.nch - 1, case.nl - 1)]
+    gs = []
+    for ci, li in ends:
+        t_, _ = ctx.get_times(ci, li, len(base[ci][li].pop))
+        g = base[ci][li].g.copy()
+        g.time = t_
+        gs.append(g)
+    ctx.set_genealogies(np.array([e[0] for e in ends]), np.array([e[1] for e in ends]),
+                        np.concatenate([g.up0 for g in gs]), np.concatenate([g.up1 for g in gs]),
+                        np.concatenate([g.down for g in gs]), np.concatenate([g.time for g in gs]),
+                        length=np.full(2, -1.0))
+    after = cs._eval()
+    mask = np.ones_like(before, bool)
+    for ci, li in ends:
+        mask[ci, li] = False
+    assert np.array_equal(before[mask], after[mask])
+    ctx.close()
