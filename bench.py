@@ -676,8 +676,74 @@ def run_treeweight(args):
     out["cpu_baseline"] = {"value": round(n / dt, 1), "unit": "genealogies/s", "cores": 1, "kind": "port",
                            "sample": "%d genealogies (8 chains x %d loci per call) through the oracle's "
                                      "treeweight in C" % (n, nloci)}
+    out["splittime_sweep"] = splittime_sweep(pm, packed, samp, tv, base, seq, nloci, nch, args)
     print(json.dumps(out), flush=True)
     ctx.close()
+
+
+def splittime_sweep(pm, packed, samp, tv, base, seq, nloci, nch, args):
+    """The device-resident split-time update (changet_RY1) on the same
+    chain set, loci with infinite-sites data simulated on their genealogies:
+    one update of every chain per sweep (ima2p_gb300.splittime.
+    ResidentChainSet), timed on the host clock around whole sweeps."""
+    import copy
+    from ima2p_gb300 import api, splittime, synth
+    from oracle import pyoracle as O
+    rng = np.random.default_rng(1012)
+    nbase = len(base)
+    seqs = [synth.is_data(rng, base[b].g, 1.0, min_sites=2) for b in range(nbase)]
+    ctx = api.Context(0)
+    for li in range(nloci):
+        ctx.add_locus_is(seqs[li % nbase])
+    ctx.set_chains(1, nch)
+    nth, nmg = len(pm.th_cells), len(pm.mg_cells)
+    ctx.set_popmodel(pm, [15.0] * nth, [0.0] * nth, [2.0] * nmg, [0.0] * nmg, [1.0] * nmg)
+    gens = [[copy.deepcopy(base[li % nbase]) for li in range(nloci)] for _ in range(nch)]
+    t0 = time.perf_counter()
+    cs = splittime.ResidentChainSet(ctx, gens, np.repeat(tv, nch, axis=0), np.linspace(1.0, 0.5, nch),
+                                    np.ones(nloci), samp, np.ones(nloci))
+    setup_s = time.perf_counter() - t0
+    mt = api.MT19937(99)
+    prng = np.random.default_rng(3)
+    tprior = [(0.0, 3.0), (0.0, 6.0)]
+    for _ in range(args.warmup):
+        cs.sweep(prng.integers(0, 2, nch), mt, tprior, 3)
+    ctx.synchronize()
+    nsw = 10
+    acc = 0
+    t0 = time.perf_counter()
+    for _ in range(nsw):
+        acc += int(cs.sweep(prng.integers(0, 2, nch), mt, tprior, 3).sum())
+    ctx.synchronize()
+    wall = time.perf_counter() - t0
+    # one core: the same update of one chain on the oracle's C functions
+    # (rubber band in numpy, treeweight, p(G), likelihoodIS)
+    node_off, up0, time_, pop, mig_off, mig_t, mig_p = packed
+    one = (node_off[:nloci + 1], up0[:node_off[nloci]], time_[:node_off[nloci]].copy(), pop[:node_off[nloci]],
+           mig_off[:node_off[nloci] + 1], mig_t[:mig_off[node_off[nloci]]].copy(), mig_p[:mig_off[node_off[nloci]]])
+    gl = np.arange(nloci, dtype=np.int32)
+    slk = [O.is_sumlogk(seqs[li % nbase], base[li % nbase].g)[1] for li in range(nloci)]
+    t0 = time.perf_counter()
+    ncpu = 0
+    while time.perf_counter() - t0 < max(1.0, args.cpu_seconds / 2) or ncpu == 0:
+        t = one[2]
+        lo = (t > 0) & (t <= tv[0, 0])
+        t[lo] = t[lo] * (tv[0, 0] * 1.0001) / tv[0, 0]
+        bad, w = O.treeweight_batch(pm, one, gl, np.zeros(nloci, np.int32), np.ones(nloci), samp, tv)
+        tot = O.sum_weights([{k: w[k][i] for k in ("cc", "hcc", "fc", "mc", "fm")} for i in range(nloci)], pm)
+        O.tree_prob(pm, tot, [15.0] * nth, [0.0] * nth, [2.0] * nmg, [0.0] * nmg, [1.0] * nmg)
+        for li in range(nloci):
+            O.is_likelihood(seqs[li % nbase], base[li % nbase].g, w["lens"][li, 0], 1.0, slk[li])
+        ncpu += 1
+    cpu = ncpu / (time.perf_counter() - t0)
+    ctx.close()
+    return {"chain_updates_per_s": round(nsw * nch / wall, 1), "ms_per_sweep": round(1e3 * wall / nsw, 3),
+            "chains": nch, "loci": nloci, "accept_rate": round(acc / (nsw * nch), 3),
+            "setup_s": round(setup_s, 2),
+            "cpu_chain_updates_per_s_1core": round(cpu, 2),
+            "note": "resident genealogies, labels and times; per sweep: MT19937 draws and MH decisions on "
+                    "the host, rubber band, weights, p(G), infinite-sites likelihoods and commits on the GPU; "
+                    "CPU: one chain's update on the oracle's C functions"}
 
 
 def main():
