@@ -26,7 +26,7 @@ SURF_FAST, SURF_FP64, SURF_COMPAT, SURF_TC = 0, 1, 2, 3
 K_IS, K_IS_SUMLOGK, K_HKY_FAST, K_HKY_FP64, K_SW_FAST, K_SW_FP64, K_SWAP, K_SURF_FAST, \
     K_SURF_FP64, K_SURF_COMPAT, K_SURF_TC, K_MARGIN, K_TREEWEIGHT, K_TREE_PROB = range(14)
 KERNEL_NAMES = ["is", "is_sumlogk", "hky_fast", "hky_fp64", "sw_fast", "sw_fp64", "swap",
-                "surf_fast", "surf_fp64", "surf_compat", "surf_tc"]
+                "surf_fast", "surf_fp64", "surf_compat", "surf_tc", "margin", "treeweight", "tree_prob"]
 REJECT_IS = -1000000000.0
 
 # every symbol the header declares (checked by tests/test_abi.py)
@@ -50,7 +50,7 @@ EXPORTS = [
     "ima_gpu_memory", "ima_gpu_set_popmodel", "ima_gpu_treeweight", "ima_gpu_tree_prob",
     "ima_gpu_surface_append_tree_rows", "ima_gpu_surface_get_rows",
     "ima_gpu_set_locus_pops", "ima_gpu_set_labels", "ima_gpu_get_times", "ima_gpu_rubber_band",
-    "ima_gpu_chain_weights",
+    "ima_gpu_chain_weights", "ima_gpu_changet_ry1_sweep",
 ]
 
 
@@ -184,6 +184,7 @@ def _declare(L):
         "ima_gpu_get_times": (I, [P, I, I, P, P, P]),
         "ima_gpu_rubber_band": (I, [P, I, P, P, P, P, P, P, I, P]),
         "ima_gpu_chain_weights": (I, [P, I, P, P, P, P, P]),
+        "ima_gpu_changet_ry1_sweep": (I, [P, I, P, P, P, P, P, P, P, P, P, D, P, P, P, I, P, P, P]),
         "ima_gpu_fillvec": (I, [P, I, P, P, P, P, P]),
         "ima_gpu_batch_set_variants": (I, [P, I, I, I]),
         "ima_gpu_set_allele_edits": (I, [P, I, P, P, P, P, P]),
@@ -559,6 +560,21 @@ class Context:
         self._ck(self.lib.ima_gpu_chain_weights(self.h, len(chains), _ptr(chains), _ptr(tvals), _ptr(probg),
                                                 _ptr(q), _ptr(m)))
         return probg, q, m[:, :nmg]
+
+    def changet_ry1_sweep(self, chains, period, oldt, newt, t_u, t_d, log_hu, log_hd, logU, tvals, u,
+                          kappa=None, gbeta=1.0, precision=PREC_FP64):
+        """One device-decided changet_RY1 per chain: returns (accept,
+        pdgsum, probg) after the decisions."""
+        chains, period = _i32(chains), _i32(period)
+        f = [_f64(v) for v in (oldt, newt, t_u, t_d, log_hu, log_hd, logU)]
+        tvals, u = _f64(tvals), _f64(u)
+        kap = _f64(kappa) if kappa is not None else None
+        n = len(chains)
+        acc, pdgsum, probg = np.zeros(n, np.uint8), np.zeros(n), np.zeros(n)
+        self._ck(self.lib.ima_gpu_changet_ry1_sweep(
+            self.h, n, _ptr(chains), _ptr(period), *(_ptr(v) for v in f), float(gbeta), _ptr(tvals), _ptr(u),
+            _ptr(kap) if kap is not None else None, int(precision), _ptr(acc), _ptr(pdgsum), _ptr(probg)))
+        return acc.astype(bool), pdgsum, probg
 
     def surface_append_tree_rows(self, groups):
         """Append the gsampinf rows of these chains (last tree_prob) to the

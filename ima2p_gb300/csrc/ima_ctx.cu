@@ -2226,7 +2226,7 @@ extern "C" int ima_gpu_treeweight(ima_ctx *c, int ngen, const int32_t *node_off,
 // group_end[i] (group_end null: group_off[i+1])
 static int tree_prob_run(ima_ctx *c, int ngroups, const int32_t *group_off, const int32_t *group_end,
                          const double *pdg, const int32_t *group_tv, double *probg, double *q, double *m,
-                         float *rows)
+                         float *rows, double **d_probg = nullptr)
 {
   if (!c->tw_ready || c->tw_ngen < 1) return c->fail(IMA_ERR_STATE, "call ima_gpu_treeweight first");
   if (ngroups < 1 || !group_off) return c->fail(IMA_ERR_ARG, "tree_prob: bad argument");
@@ -2295,6 +2295,7 @@ static int tree_prob_run(ima_ctx *c, int ngroups, const int32_t *group_off, cons
   c->tp_rows = a.rows;
   c->tp_ngroups = ngroups;
   c->tp_rowlen = rowlen;
+  if (d_probg) *d_probg = a.probg;
   auto down = [&](void *dst, const void *src, size_t bytes) {
     if (!r && dst && bytes) r = c->cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->st), "tree_prob outputs");
   };
@@ -2570,14 +2571,13 @@ static void dev_newer(ima_ctx *c, int nch, const int32_t *chains)
   }
 }
 
-extern "C" int ima_gpu_rubber_band(ima_ctx *c, int nch, const int32_t *chains, const int32_t *period,
-                                   const double *oldt, const double *newt, const double *t_u, const double *t_d,
-                                   int inverse, int32_t *counts)
+// the band on the device; counts stay in d_bcnt, the chain list in
+// *d_chains (the caller's chains, device copy) when asked for
+static int band_run(ima_ctx *c, int nch, const int32_t *chains, const int32_t *period, const double *oldt,
+                    const double *newt, const double *t_u, const double *t_d, int inverse, int32_t *counts,
+                    bool sync, int32_t **d_chains = nullptr)
 {
-  if (!c || nch < 1 || !chains || !period || !oldt || !newt || !t_u || !t_d) return IMA_ERR_ARG;
-  if (!c->tw_ready) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_popmodel first");
-  int r = chains_ready(c, nch, chains);
-  if (r) return r;
+  int r = IMA_OK;
   const int last = c->h_tw.npops - 1;
   std::vector<double> prm(5 * (size_t)nch);
   for (int k = 0; k < nch; k++) {
@@ -2619,18 +2619,29 @@ extern "C" int ima_gpu_rubber_band(ima_ctx *c, int nch, const int32_t *chains, c
   c->launch(IMA_K_TREEWEIGHT, 0.0, [&] { launch_band(a, c->st); });
   r = c->cuda(cudaGetLastError(), "band launch");
   if (!r && counts && !inverse) r = c->cuda(cudaMemcpyAsync(counts, c->d_bcnt, 16ul * nch, cudaMemcpyDeviceToHost, c->st), "band counts");
+  // the parameter block is host memory of this call: wait for its copy
   r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "band");
   if (!r) dev_newer(c, nch, chains);
+  if (d_chains) *d_chains = d_ch;
+  (void)sync;
   return r;
 }
 
-extern "C" int ima_gpu_chain_weights(ima_ctx *c, int nch, const int32_t *chains, const double *tvals,
-                                     double *probg, double *q, double *m)
+extern "C" int ima_gpu_rubber_band(ima_ctx *c, int nch, const int32_t *chains, const int32_t *period,
+                                   const double *oldt, const double *newt, const double *t_u, const double *t_d,
+                                   int inverse, int32_t *counts)
 {
-  if (!c || nch < 1 || !chains || !tvals) return IMA_ERR_ARG;
+  if (!c || nch < 1 || !chains || !period || !oldt || !newt || !t_u || !t_d) return IMA_ERR_ARG;
   if (!c->tw_ready) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_popmodel first");
   int r = chains_ready(c, nch, chains);
   if (r) return r;
+  return band_run(c, nch, chains, period, oldt, newt, t_u, t_d, inverse, counts, true);
+}
+
+static int chain_weights_run(ima_ctx *c, int nch, const int32_t *chains, const double *tvals, double *probg,
+                             double *q, double *m, double **d_probg)
+{
+  int r = IMA_OK;
   const TwModel &h = c->h_tw;
   const int npops = h.npops, nsplit = npops - 1, nl = c->nloci, ni = c->nitems;
   for (int k = 0; k < nch; k++)
@@ -2727,6 +2738,117 @@ extern "C" int ima_gpu_chain_weights(ima_ctx *c, int nch, const int32_t *chains,
     gend[k] = chains[k] * nl + nl;
   }
   std::vector<double> pg(nch);
-  r = tree_prob_run(c, nch, goff.data(), gend.data(), nullptr, chains, probg ? probg : pg.data(), q, m, nullptr);
+  return tree_prob_run(c, nch, goff.data(), gend.data(), nullptr, chains, probg ? probg : pg.data(), q, m, nullptr,
+                       d_probg);
+}
+
+extern "C" int ima_gpu_chain_weights(ima_ctx *c, int nch, const int32_t *chains, const double *tvals,
+                                     double *probg, double *q, double *m)
+{
+  if (!c || nch < 1 || !chains || !tvals) return IMA_ERR_ARG;
+  if (!c->tw_ready) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_popmodel first");
+  int r = chains_ready(c, nch, chains);
+  if (r) return r;
+  return chain_weights_run(c, nch, chains, tvals, probg, q, m, nullptr);
+}
+
+extern "C" int ima_gpu_changet_ry1_sweep(ima_ctx *c, int nch, const int32_t *chains, const int32_t *period,
+                                         const double *oldt, const double *newt, const double *t_u, const double *t_d,
+                                         const double *log_hu, const double *log_hd, const double *logU, double gbeta,
+                                         const double *tvals, const double *u, const double *kappa, int precision,
+                                         uint8_t *accept, double *pdgsum, double *probg)
+{
+  if (!c || nch < 1 || !chains || !period || !oldt || !newt || !t_u || !t_d || !log_hu || !log_hd || !logU ||
+      !tvals || !u || !accept)
+    return IMA_ERR_ARG;
+  if (!c->tw_ready) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_popmodel first");
+  int r = chains_ready(c, nch, chains);
+  if (r) return r;
+  const int nl = c->nloci;
+  int32_t *d_ch = nullptr;
+  r = band_run(c, nch, chains, period, oldt, newt, t_u, t_d, 0, nullptr, false, &d_ch);
+  double *d_pgnew = nullptr;
+  r = r ? r : chain_weights_run(c, nch, chains, tvals, nullptr, nullptr, nullptr, &d_pgnew);
+  if (r) return r;
+  // the chains' likelihoods (writes the per-item pdg_new pool)
+  std::vector<int32_t> ci((size_t)nch * nl), li((size_t)nch * nl), st((size_t)nch * nl);
+  std::vector<double> kap((size_t)nch * nl, 1.0), res((size_t)nch * nl);
+  for (int k = 0; k < nch; k++)
+    for (int l = 0; l < nl; l++) {
+      ci[(size_t)k * nl + l] = chains[k];
+      li[(size_t)k * nl + l] = l;
+      if (kappa) kap[(size_t)k * nl + l] = kappa[(size_t)k * nl + l];
+    }
+  r = ima_gpu_eval(c, nch * nl, ci.data(), li.data(), u, kap.data(), nullptr, nullptr, precision, res.data(), st.data());
+  if (r) return r;
+  for (size_t k = 0; k < st.size(); k++)
+    if (st[k] == IMA_EVAL_IS_FAIL)
+      return c->fail(IMA_ERR_DATA, "chain %d locus %d: data incompatible with the genealogy", ci[k], li[k]);
+  // the decisions, on the device
+  char *buf = static_cast<char *>(rsel(c, carve_size({nch * 4ul, 40ul * nch, 24ul * nch, 8ul * nch, nch * 1ul, 8ul * nch})));
+  if (!buf) return c->fail(IMA_ERR_NOMEM, "decision buffers");
+  Carve cv{buf};
+  int32_t *d_ch2 = cv.take<int32_t>(nch);
+  cv.take<double>(5 * (size_t)nch);  // the band's parameter block (same buffer)
+  double *d_logs = cv.take<double>(3 * (size_t)nch);
+  double *d_sum = cv.take<double>(nch);
+  uint8_t *d_acc = cv.take<uint8_t>(nch);
+  (void)d_ch;
+  std::vector<double> logs(3 * (size_t)nch);
+  for (int k = 0; k < nch; k++) {
+    logs[k] = log_hu[k];
+    logs[nch + k] = log_hd[k];
+    logs[2 * nch + k] = logU[k];
+  }
+  r = c->cuda(cudaMemcpyAsync(d_ch2, chains, nch * 4ul, cudaMemcpyHostToDevice, c->st), "decide");
+  r = r ? r : c->cuda(cudaMemcpyAsync(d_logs, logs.data(), logs.size() * 8, cudaMemcpyHostToDevice, c->st), "decide");
+  if (r) return r;
+  RyArgs a{};
+  a.nch = nch;
+  a.nloci = nl;
+  a.chains = d_ch2;
+  a.counts = c->d_bcnt;
+  a.lhu = d_logs;
+  a.lhd = d_logs + nch;
+  a.logU = d_logs + 2 * nch;
+  a.probg_new = d_pgnew;
+  a.gbeta = gbeta;
+  a.beta = c->d_beta;
+  a.probg = c->d_probg;
+  a.pdg = c->d_pdg;
+  a.pdg_new = c->d_pdg_new;
+  a.accept = d_acc;
+  a.pdgsum = d_sum;
+  launch_ry_decide(a, c->st);
+  c->launches++;
+  r = c->cuda(cudaGetLastError(), "decide launch");
+  r = r ? r : c->cuda(cudaMemcpyAsync(accept, d_acc, nch, cudaMemcpyDeviceToHost, c->st), "decisions");
+  if (pdgsum) r = r ? r : c->cuda(cudaMemcpyAsync(pdgsum, d_sum, nch * 8ul, cudaMemcpyDeviceToHost, c->st), "decisions");
+  r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "decisions");
+  if (r) return r;
+  // commit the accepted chains' evaluations, move the others back
+  std::vector<uint8_t> acc_items((size_t)nch * nl);
+  std::vector<int32_t> rc, rp;
+  std::vector<double> ro, rn, ru, rd;
+  for (int k = 0; k < nch; k++) {
+    for (int l = 0; l < nl; l++) acc_items[(size_t)k * nl + l] = accept[k];
+    if (!accept[k]) {
+      rc.push_back(chains[k]);
+      rp.push_back(period[k]);
+      ro.push_back(oldt[k]);
+      rn.push_back(newt[k]);
+      ru.push_back(t_u[k]);
+      rd.push_back(t_d[k]);
+    }
+  }
+  r = commit(c, nch * nl, ci.data(), li.data(), acc_items.data(), true, true);
+  if (!r && !rc.empty())
+    r = band_run(c, (int)rc.size(), rc.data(), rp.data(), ro.data(), rn.data(), ru.data(), rd.data(), 1, nullptr, true);
+  if (!r && probg) {  // the resident p(G) of each chain after the decision
+    std::vector<double> all(c->nchains);
+    r = c->cuda(cudaMemcpyAsync(all.data(), c->d_probg, c->nchains * 8ul, cudaMemcpyDeviceToHost, c->st), "probg");
+    r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "probg");
+    for (int k = 0; !r && k < nch; k++) probg[k] = all[chains[k]];
+  }
   return r;
 }

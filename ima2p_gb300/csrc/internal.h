@@ -215,6 +215,21 @@ struct BandArgs {
   double *len, *len_hold;                  // per item: saved going forward, restored on the way back
 };
 int launch_band(const BandArgs &a, cudaStream_t st);
+// changet_RY1's Metropolis-Hastings decision (update_t_RY.cpp:394-410), a
+// thread per chain, on the device's weights and likelihoods
+struct RyArgs {
+  int nch, nloci;
+  const int32_t *chains, *counts;          // counts [nch][4] from the band
+  const double *lhu, *lhd, *logU;          // [nch] host logs of the Hastings ratios, log U
+  const double *probg_new;                 // [nch]
+  double gbeta;
+  const double *beta;                      // per chain (resident)
+  double *probg;                           // per chain (resident): updated on acceptance
+  const double *pdg, *pdg_new;             // per item: committed, last evaluation
+  uint8_t *accept;                         // [nch]
+  double *pdgsum;                          // [nch] the chain's likelihood sum after the decision
+};
+int launch_ry_decide(const RyArgs &a, cudaStream_t st);
 bool tw_fits(int P);                       // P events fit one warp's shared memory
 int launch_treeweight(const TwArgs &a, const TwModel &h, cudaStream_t st);
 int launch_tree_prob(const TwProbArgs &a, const TwModel &h, cudaStream_t st);

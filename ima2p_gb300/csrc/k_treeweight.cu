@@ -814,6 +814,33 @@ __global__ void __launch_bounds__(128) k_band(BandArgs a)
   }
 }
 
+// changet_RY1's decision: likelihood sums in locus order (allpcalc.pdg is
+// that sum), tpw = gbeta (new - old) + probg_new - probg_old, the MH term
+// beta tpw + (ecd + emd) log(t_d ratio) + (ecu + emu) log(t_u ratio) with
+// the node counts halved, and log U < DMIN(1, term) -- NaN rejects, as the
+// reference's comparison does.
+__global__ void k_ry_decide(RyArgs a)
+{
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.nch) return;
+  const int ci = a.chains[c];
+  double snew = 0.0, sold = 0.0;
+  for (int li = 0; li < a.nloci; li++) {
+    snew += a.pdg_new[(size_t)ci * a.nloci + li];
+    sold += a.pdg[(size_t)ci * a.nloci + li];
+  }
+  const int ecd = a.counts[4 * c] / 2, ecu = a.counts[4 * c + 1] / 2, emd = a.counts[4 * c + 2],
+            emu = a.counts[4 * c + 3];
+  double tpw = a.gbeta * (snew - sold);
+  tpw += a.probg_new[c] - a.probg[ci];
+  const double mh = a.beta[ci] * tpw + (ecd + emd) * a.lhd[c] + (ecu + emu) * a.lhu[c];
+  const double lim = (1.0 < mh) ? 1.0 : mh;
+  const bool acc = a.logU[c] < lim;
+  a.accept[c] = acc;
+  a.pdgsum[c] = acc ? snew : sold;
+  if (acc) a.probg[ci] = a.probg_new[c];
+}
+
 // rows[groups[i]] -> dst + i * rowlen (a warp per row)
 __global__ void __launch_bounds__(128) k_gather_rows(const float *rows, int rowlen, const int32_t *groups, int n,
                                                      float *dst)
@@ -830,6 +857,13 @@ int launch_band(const BandArgs &a, cudaStream_t st)
 {
   if (a.nch < 1) return 0;
   k_band<<<a.nch * a.nloci, 128, 0, st>>>(a);
+  return 0;
+}
+
+int launch_ry_decide(const RyArgs &a, cudaStream_t st)
+{
+  if (a.nch < 1) return 0;
+  k_ry_decide<<<(a.nch + 127) / 128, 128, 0, st>>>(a);
   return 0;
 }
 

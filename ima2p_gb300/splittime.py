@@ -354,6 +354,8 @@ class ResidentChainSet:
         self.pdg = self._eval()
         ctx.commit(self.ci, self.li, np.ones(len(self.ci), np.uint8))
         self.pdgsum = self._sums(self.pdg)
+        ctx.set_betas(self.beta)     # resident heats and p(G) for the device decisions
+        ctx.set_probg(self.probg)
 
     def _eval(self):
         r, _ = self.ctx.eval(self.ci, self.li, np.tile(self.u, self.nch), np.tile(self.kappa, self.nch),
@@ -408,3 +410,31 @@ class ResidentChainSet:
             self.ctx.rubber_band(self.chains[rej], periods[rej], oldt[rej], newt[rej], t_u[rej], t_d[rej],
                                  inverse=True)
         return accept
+
+    def sweep_device(self, periods, rng, tprior, npops, gbeta=1.0):
+        """sweep() with the decisions on the device (ima_gpu_changet_ry1_sweep):
+        one call per sweep; the host draws and takes the two logs of the
+        Hastings ratios, as the reference computes them."""
+        nch, last = self.nch, npops - 1
+        periods = np.asarray(periods, np.int64)
+        rows = np.arange(nch)
+        oldt = self.tvals[rows, periods].copy()
+        t_u = np.where(periods == 0, 0.0, self.tvals[rows, np.maximum(periods - 1, 0)])
+        t_d = np.where(periods == last - 1, TIMEMAX, self.tvals[rows, np.minimum(periods + 1, last - 1)])
+        newt, logU, lhu, lhd = np.zeros(nch), np.zeros(nch), np.zeros(nch), np.zeros(nch)
+        for c in range(nch):
+            k = int(periods[c])
+            newt[c] = getnewt(rng, k, max(tprior[k][0], float(t_u[c])), min(tprior[k][1], float(t_d[c])),
+                              float(oldt[c]), self.nl, npops)
+            logU[c] = math.log(rng.uniform())
+            lhu[c] = math.log((newt[c] - t_u[c]) / (oldt[c] - t_u[c]))
+            lhd[c] = 0.0 if k == last - 1 else math.log((t_d[c] - newt[c]) / (t_d[c] - oldt[c]))
+        tv_new = self.tvals.copy()
+        tv_new[rows, periods] = newt
+        acc, pdgsum, probg = self.ctx.changet_ry1_sweep(
+            self.chains, periods, oldt, newt, t_u, t_d, lhu, lhd, logU, tv_new,
+            np.tile(self.u, nch), np.tile(self.kappa, nch), gbeta, self.prec)
+        self.tvals[rows[acc], periods[acc]] = newt[acc]
+        self.pdgsum = pdgsum
+        self.probg = probg
+        return acc

@@ -352,6 +352,25 @@ int ima_gpu_rubber_band(ima_ctx *ctx, int nch, const int32_t *chains, const int3
 int ima_gpu_chain_weights(ima_ctx *ctx, int nch, const int32_t *chains, const double *tvals,
                           double *probg, double *q, double *m);
 
+/* One changet_RY1 of each of the nch chains, decided on the device: the
+ * band forward, the chains' weights and p(G), their likelihoods (u, kappa
+ * [nch][nloci]; kappa may be NULL), then per chain the reference's
+ * Metropolis-Hastings term (update_t_RY.cpp:394-410) from the likelihood
+ * sums in locus order, p(G) against the resident p(G) (ima_gpu_set_probg),
+ * the resident heat (ima_gpu_set_betas), gbeta, the counts and the host's
+ * log_hu = log((newt - t_u)/(oldt - t_u)), log_hd = log((t_d - newt)/
+ * (t_d - oldt)) (0 for the last period), against logU = log(U).  Accepted
+ * chains are committed (likelihoods, p(G)); the others moved back.  tvals
+ * [nch][npops-1]: the proposed split times.  accept [nch]; pdgsum and probg
+ * (may be NULL) [nch]: each chain's likelihood sum and p(G) after the
+ * decision.  The caller draws newt and U in the reference's order (getnewt's
+ * uniform, then the acceptance uniform, chain by chain). */
+int ima_gpu_changet_ry1_sweep(ima_ctx *ctx, int nch, const int32_t *chains, const int32_t *period,
+                              const double *oldt, const double *newt, const double *t_u, const double *t_d,
+                              const double *log_hu, const double *log_hd, const double *logU, double gbeta,
+                              const double *tvals, const double *u, const double *kappa, int precision,
+                              uint8_t *accept, double *pdgsum, double *probg);
+
 /* Copy surface rows start .. start+count to the host ([count][rowlen]), e.g.
  * to write them with ima_ti_write_binary.  rowlen must be the surface's
  * (IMA_ERR_ARG otherwise). */

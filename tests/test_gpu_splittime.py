@@ -123,3 +123,41 @@ def test_resident_sweep_follows_the_reference():
         mask[ci, li] = False
     assert np.array_equal(before[mask], after[mask])
     ctx.close()
+
+
+def test_device_decided_sweep_follows_the_reference():
+    """ima_gpu_changet_ry1_sweep: band, weights, likelihoods and the MH
+    decision on the device in one call per sweep -- the reference's
+    decisions and times again."""
+    case = RyCase()
+    ctx = api.Context(0)
+    for q in case.seqs:
+        ctx.add_locus_is(q)
+    ctx.set_chains(1, case.nch)
+    ctx.set_popmodel(case.pm, *case.priors())
+    cs = splittime.ResidentChainSet(ctx, case.fresh_gens(), [case.d["tv0"]] * case.nch, case.betas,
+                                    np.ones(case.nl), case.samps, case.us)
+    rng = api.MT19937(case.seed)
+    res = []
+    for s0 in range(0, len(case.steps), case.nch):
+        periods = [case.steps[s0 + c][1] for c in range(case.nch)]
+        acc = cs.sweep_device(periods, rng, case.tprior, case.npops)
+        for c in range(case.nch):
+            res.append((int(acc[c]), float(cs.tvals[c, periods[c]]), float(cs.probg[c]), float(cs.pdgsum[c])))
+    res, ref = np.array(res), case.res
+    assert np.array_equal(res[:, 0], ref[:, 0])
+    assert np.array_equal(res[:, 1], ref[:, 1])
+    np.testing.assert_allclose(res[:, 2], ref[:, 2], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(res[:, 3], ref[:, 3], rtol=1e-12)
+    base = case.fresh_gens()
+    off = moff = 0
+    for ci in range(case.nch):
+        for li in range(case.nl):
+            nl = len(base[ci][li].pop)
+            t, m = ctx.get_times(ci, li, nl)
+            edge = base[ci][li].g.down != -1
+            assert np.array_equal(t[edge], case.times[off:off + nl][edge])
+            assert np.array_equal(m, case.migt[moff:moff + len(m)])
+            off += nl
+            moff += len(m)
+    ctx.close()
