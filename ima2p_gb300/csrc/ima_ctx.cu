@@ -19,6 +19,8 @@
 #include <functional>
 #include <condition_variable>
 #include <mutex>
+#include <atomic>
+#include <chrono>
 #include <thread>
 
 #include "internal.h"
@@ -50,7 +52,10 @@ struct Batch {
 
 // A small persistent pool of host threads for per-genealogy packing: run(n,
 // f) calls f(0) .. f(n-1) on the pool and the calling thread and returns
-// when every call has finished.
+// when every call has finished.  Jobs are claimed under the mutex; between
+// calls the workers spin (yielding) for a short while before they block, and
+// the caller spins on the completion count, so that a call does not pay a
+// condition-variable wake-up on each side (tens of microseconds per call).
 class HostPool {
  public:
   explicit HostPool(int nthreads)
@@ -61,7 +66,8 @@ class HostPool {
   {
     {
       std::lock_guard<std::mutex> lk(m_);
-      stop_ = true;
+      stop_.store(true);
+      gen_.fetch_add(1);
     }
     cv_.notify_all();
     for (auto &t : th_) t.join();
@@ -69,19 +75,26 @@ class HostPool {
   int size() const { return (int)th_.size() + 1; }
   void run(int n, const std::function<void(int)> &f)
   {
-    std::unique_lock<std::mutex> lk(m_);
-    job_ = &f;
-    njobs_ = n;
-    next_ = 0;
-    finished_ = 0;
-    gen_++;
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      job_ = &f;
+      njobs_ = n;
+      next_ = 0;
+      finished_.store(0);
+      gen_.fetch_add(1, std::memory_order_release);
+    }
     cv_.notify_all();
-    work(lk);
-    done_.wait(lk, [&] { return finished_ == njobs_; });
+    {
+      std::unique_lock<std::mutex> lk(m_);
+      work(lk);
+    }
+    while (finished_.load(std::memory_order_acquire) < n) std::this_thread::yield();
+    std::lock_guard<std::mutex> lk(m_);
     job_ = nullptr;
   }
 
  private:
+  static constexpr auto kSpin = std::chrono::microseconds(200);
   void work(std::unique_lock<std::mutex> &lk)
   {
     while (job_ && next_ < njobs_) {
@@ -90,27 +103,31 @@ class HostPool {
       lk.unlock();
       (*f)(j);
       lk.lock();
-      if (++finished_ == njobs_) done_.notify_all();
+      finished_.fetch_add(1, std::memory_order_release);
     }
   }
   void loop()
   {
     uint64_t seen = 0;
-    std::unique_lock<std::mutex> lk(m_);
     for (;;) {
-      cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
-      if (stop_) return;
-      seen = gen_;
+      const auto t0 = std::chrono::steady_clock::now();
+      while (gen_.load(std::memory_order_acquire) == seen && std::chrono::steady_clock::now() - t0 < kSpin)
+        std::this_thread::yield();
+      std::unique_lock<std::mutex> lk(m_);
+      cv_.wait(lk, [&] { return stop_.load() || gen_.load() != seen; });
+      if (stop_.load()) return;
+      seen = gen_.load();
       work(lk);
     }
   }
   std::vector<std::thread> th_;
   std::mutex m_;
-  std::condition_variable cv_, done_;
+  std::condition_variable cv_;
   const std::function<void(int)> *job_ = nullptr;
-  int njobs_ = 0, next_ = 0, finished_ = 0;
-  uint64_t gen_ = 0;
-  bool stop_ = false;
+  int njobs_ = 0, next_ = 0;
+  std::atomic<int> finished_{0};
+  std::atomic<uint64_t> gen_{0};
+  std::atomic<bool> stop_{false};
 };
 
 struct PendingTiming {
@@ -805,7 +822,7 @@ extern "C" int ima_gpu_set_genealogies(ima_ctx *c, int n, const int32_t *ci, con
         return;
     }
   };
-  if (repeat || n < 256) {
+  if (repeat || n < 128) {  // below this, waking the pool costs more than it saves
     SetOut o;
     apply(0, n, o);
     o.merge_into(c);
@@ -816,7 +833,7 @@ extern "C" int ima_gpu_set_genealogies(ima_ctx *c, int n, const int32_t *ci, con
     const unsigned hw = std::thread::hardware_concurrency();
     c->pool.reset(new HostPool((int)std::max(1u, std::min(hw, 16u)) - 1));
   }
-  const int nchunk = std::min(n / 64, 4 * c->pool->size());
+  const int nchunk = std::min(std::max(2, n / 64), 4 * c->pool->size());
   std::vector<SetOut> outs(nchunk);
   c->pool->run(nchunk, [&](int j) {
     apply((int)((long long)n * j / nchunk), (int)((long long)n * (j + 1) / nchunk), outs[j]);
