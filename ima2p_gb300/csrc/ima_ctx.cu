@@ -255,7 +255,7 @@ struct ima_ctx {
   // per item nl+1 relative migration offsets (at node_off + item), events in
   // a pool (item events from mbase[item]), split-time rows per chain
   int32_t *d_pop = nullptr, *d_moff = nullptr, *d_inode_off = nullptr, *d_gl = nullptr, *d_gt = nullptr;
-  int32_t *d_moff_start = nullptr, *d_bcnt = nullptr, *d_mig_p = nullptr, *d_rsamp = nullptr;
+  int32_t *d_moff_start = nullptr, *d_bcnt = nullptr, *d_bicnt = nullptr, *d_mig_p = nullptr, *d_rsamp = nullptr;
   long long *d_mbase = nullptr;
   double *d_mig_t = nullptr, *d_tvr = nullptr, *d_len_hold = nullptr, *d_rhlog = nullptr, *d_rh2 = nullptr;
   size_t mig_cap = 0, mig_used = 0;
@@ -433,7 +433,7 @@ extern "C" void ima_gpu_destroy(ima_ctx *c)
                   c->d_used, c->d_swap0ok, c->d_ctr, c->d_uni, c->d_rows, c->d_lognorm,
                   c->d_sscratch, c->d_sx, c->d_sq, c->d_sess, c->d_citems, c->d_cacc, c->d_flush,
                   c->d_mscratch, c->d_tw, c->d_logfact, c->d_twerr, c->d_twin, c->d_twout, c->d_tpbuf,
-                  c->d_pop, c->d_moff, c->d_inode_off, c->d_gl, c->d_gt, c->d_moff_start, c->d_bcnt,
+                  c->d_pop, c->d_moff, c->d_inode_off, c->d_gl, c->d_gt, c->d_moff_start, c->d_bcnt, c->d_bicnt,
                   c->d_mig_p, c->d_rsamp, c->d_mbase, c->d_mig_t, c->d_tvr, c->d_len_hold, c->d_rhlog,
                   c->d_rh2, c->d_rsel};
   for (void *p : devs)
@@ -2410,9 +2410,10 @@ static int labels_alloc(ima_ctx *c)
   c->d_gt = dev_alloc<int32_t>(ni, B, c->st);
   c->d_moff_start = dev_alloc<int32_t>(ni, B, c->st);
   c->d_bcnt = dev_alloc<int32_t>(4 * (size_t)c->nchains, B, c->st);
+  c->d_bicnt = dev_alloc<int32_t>(4 * (size_t)ni, B, c->st);
   c->d_mbase = dev_alloc<long long>(ni, B, c->st);
   c->d_len_hold = dev_alloc<double>(ni, B, c->st);
-  if (!c->d_pop || !c->d_moff || !c->d_inode_off || !c->d_gl || !c->d_gt || !c->d_moff_start || !c->d_bcnt ||
+  if (!c->d_pop || !c->d_moff || !c->d_inode_off || !c->d_gl || !c->d_gt || !c->d_moff_start || !c->d_bcnt || !c->d_bicnt ||
       !c->d_mbase || !c->d_len_hold)
     return c->fail(IMA_ERR_NOMEM, "population labels");
   std::vector<int32_t> off(ni + 1), gl(ni), gt(ni), ms(ni);
@@ -2631,9 +2632,12 @@ static int band_run(ima_ctx *c, int nch, const int32_t *chains, const int32_t *p
   a.last = last;
   a.inverse = inverse ? 1 : 0;
   a.counts = c->d_bcnt;
+  a.item_counts = c->d_bicnt;
   a.len = c->d_len;
   a.len_hold = c->d_len_hold;
-  c->launch(IMA_K_TREEWEIGHT, 0.0, [&] { launch_band(a, c->st); });
+  int nk = 1;
+  c->launch(IMA_K_TREEWEIGHT, 0.0, [&] { nk = launch_band(a, c->st); });
+  c->launches += nk - 1;
   r = c->cuda(cudaGetLastError(), "band launch");
   if (!r && counts && !inverse) r = c->cuda(cudaMemcpyAsync(counts, c->d_bcnt, 16ul * nch, cudaMemcpyDeviceToHost, c->st), "band counts");
   // the parameter block is host memory of this call: wait for its copy

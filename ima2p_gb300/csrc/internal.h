@@ -212,9 +212,10 @@ struct BandArgs {
   const double *prm;                       // [nch][5]: period, o, n, t_u, t_d
   int nch, nloci, last, inverse;
   int32_t *counts;                         // [nch][4]: ecd, ecu, emd, emu (forward)
+  int32_t *item_counts;                    // [nch * nloci][4] per chain-locus counts (forward)
   double *len, *len_hold;                  // per item: saved going forward, restored on the way back
 };
-int launch_band(const BandArgs &a, cudaStream_t st);
+int launch_band(const BandArgs &a, cudaStream_t st);  // returns the kernels launched
 // changet_RY1's Metropolis-Hastings decision (update_t_RY.cpp:394-410), a
 // thread per chain, on the device's weights and likelihoods
 struct RyArgs {

@@ -750,16 +750,21 @@ __global__ void __launch_bounds__(128) k_tp_final(TwProbArgs a)
 }
 
 // The rubber band of changet_RY1 (update_t_RY.cpp:59-86, 279-335 going
-// forward, 444-491 back) on every locus of the listed chains, a block per
+// forward, 444-491 back) on every locus of the listed chains, a warp per
 // chain-locus: node times of non-root edges in (t_u, o] go through
 // beforesplit, those in (o, t_d) through aftersplit, with o -> n; migration
 // times alike.  The float-float copy of each moved time follows it.  Going
 // forward the chain's counts are added up (each node time twice, once per
 // daughter edge, as the reference counts them) and the item's length is
 // saved; going back (o and n exchanged by the caller) the length is restored.
-__global__ void __launch_bounds__(128) k_band(BandArgs a)
+constexpr int BAND_WPB = 8;  // chain-loci (warps) per block
+
+__global__ void __launch_bounds__(32 * BAND_WPB) k_band(BandArgs a)
 {
-  const int c = blockIdx.x / a.nloci, li = blockIdx.x % a.nloci;
+  const int lane = threadIdx.x & 31;
+  const int slot = blockIdx.x * BAND_WPB + (threadIdx.x >> 5);
+  if (slot >= a.nch * a.nloci) return;  // whole warps only
+  const int c = slot / a.nloci, li = slot % a.nloci;
   const int item = a.chains[c] * a.nloci + li;
   const ItemDev it = a.items[item];
   const int nl = 2 * it.n - 1, off = it.node_off;
@@ -780,7 +785,7 @@ __global__ void __launch_bounds__(128) k_band(BandArgs a)
   int lo = 0, hi = 0, mlo = 0, mhi = 0;
   const int32_t *mo = a.moff + off + item;
   const long long mb = a.mbase[item];
-  for (int k = threadIdx.x; k < nl; k += blockDim.x) {
+  for (int k = lane; k < nl; k += 32) {
     if (a.nodes[off + k].down == -1) continue;
     const double t = a.t64[off + k];
     const int moved = lo + hi;
@@ -792,26 +797,38 @@ __global__ void __launch_bounds__(128) k_band(BandArgs a)
     }
     for (int j = mo[k]; j < mo[k + 1]; j++) a.mig_t[mb + j] = band(a.mig_t[mb + j], &mlo, &mhi);
   }
-  if (!a.inverse) {
+  if (!a.inverse) {  // the chain-locus's counts in its own slot (no atomics)
     for (int d = 16; d; d >>= 1) {
       lo += __shfl_xor_sync(~0u, lo, d);
       hi += __shfl_xor_sync(~0u, hi, d);
       mlo += __shfl_xor_sync(~0u, mlo, d);
       mhi += __shfl_xor_sync(~0u, mhi, d);
     }
-    if ((threadIdx.x & 31) == 0) {
-      if (hi) atomicAdd(&a.counts[4 * c + 0], hi);
-      if (lo) atomicAdd(&a.counts[4 * c + 1], lo);
-      if (mhi) atomicAdd(&a.counts[4 * c + 2], mhi);
-      if (mlo) atomicAdd(&a.counts[4 * c + 3], mlo);
+    if (lane == 0) {
+      int32_t *ic = a.item_counts + 4 * (size_t)slot;
+      ic[0] = hi;
+      ic[1] = lo;
+      ic[2] = mhi;
+      ic[3] = mlo;
     }
   }
-  if (threadIdx.x == 0) {
+  if (lane == 0) {
     if (a.inverse)
       a.len[item] = a.len_hold[item];
     else
       a.len_hold[item] = a.len[item];
   }
+}
+
+// per-chain counts: the chain-loci's slots summed (a thread per chain and count)
+__global__ void k_band_sum(const int32_t *item_counts, int nch, int nloci, int32_t *counts)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 4 * nch) return;
+  const int c = t >> 2, q = t & 3;
+  int v = 0;
+  for (int li = 0; li < nloci; li++) v += item_counts[4 * ((size_t)c * nloci + li) + q];
+  counts[t] = v;
 }
 
 // changet_RY1's decision: likelihood sums in locus order (allpcalc.pdg is
@@ -856,8 +873,10 @@ __global__ void __launch_bounds__(128) k_gather_rows(const float *rows, int rowl
 int launch_band(const BandArgs &a, cudaStream_t st)
 {
   if (a.nch < 1) return 0;
-  k_band<<<a.nch * a.nloci, 128, 0, st>>>(a);
-  return 0;
+  const int slots = a.nch * a.nloci;
+  k_band<<<(slots + BAND_WPB - 1) / BAND_WPB, 32 * BAND_WPB, 0, st>>>(a);
+  if (!a.inverse) k_band_sum<<<(4 * a.nch + 127) / 128, 128, 0, st>>>(a.item_counts, a.nch, a.nloci, a.counts);
+  return a.inverse ? 1 : 2;
 }
 
 int launch_ry_decide(const RyArgs &a, cudaStream_t st)
