@@ -50,7 +50,8 @@ EXPORTS = [
     "ima_gpu_memory", "ima_gpu_set_popmodel", "ima_gpu_treeweight", "ima_gpu_tree_prob",
     "ima_gpu_surface_append_tree_rows", "ima_gpu_surface_get_rows",
     "ima_gpu_set_locus_pops", "ima_gpu_set_labels", "ima_gpu_get_times", "ima_gpu_rubber_band",
-    "ima_gpu_chain_weights", "ima_gpu_changet_ry1_sweep",
+    "ima_gpu_chain_weights", "ima_gpu_changet_ry1_sweep", "ima_gpu_get_probg", "ima_gpu_get_split_times",
+    "ima_gpu_checkpoint_write", "ima_gpu_checkpoint_read",
 ]
 
 
@@ -164,6 +165,10 @@ def _declare(L):
         "ima_gpu_set_pdg": (I, [P, P]),
         "ima_gpu_get_pdg": (I, [P, P]),
         "ima_gpu_set_probg": (I, [P, P]),
+        "ima_gpu_get_probg": (I, [P, P]),
+        "ima_gpu_get_split_times": (I, [P, P]),
+        "ima_gpu_checkpoint_write": (I, [P, C.c_char_p, P]),
+        "ima_gpu_checkpoint_read": (I, [P, C.c_char_p, P]),
         "ima_gpu_swapchains": (I, [P, I, I, P, I, C.c_uint64, P, P]),
         "ima_gpu_get_swapcounts": (I, [P, I, P, P]),
         "ima_gpu_surface_load": (I, [P, I, I, P, I, I, I, P]),
@@ -392,6 +397,11 @@ class Context:
     def set_probg(self, probg):
         self._ck(self.lib.ima_gpu_set_probg(self.h, _ptr(_f64(probg))))
 
+    def get_probg(self):
+        out = np.zeros(self.nchains)
+        self._ck(self.lib.ima_gpu_get_probg(self.h, _ptr(out)))
+        return out
+
     def swapchains(self, swaptries, include_probg=True, uniforms=None, seed=0):
         """uniforms: [nruns, stride] per-run streams, or None for Philox."""
         used = np.zeros(self.nruns, np.int32)
@@ -575,6 +585,24 @@ class Context:
             self.h, n, _ptr(chains), _ptr(period), *(_ptr(v) for v in f), float(gbeta), _ptr(tvals), _ptr(u),
             _ptr(kap) if kap is not None else None, int(precision), _ptr(acc), _ptr(pdgsum), _ptr(probg)))
         return acc.astype(bool), pdgsum, probg
+
+    def get_split_times(self):
+        """The split times the resident labels follow, [nchains][npops-1]."""
+        out = np.zeros((self.nchains, self._tw_pm.npops - 1))
+        self._ck(self.lib.ima_gpu_get_split_times(self.h, _ptr(out)))
+        return out
+
+    def checkpoint_write(self, path, rng=None):
+        """The resident chain state (and the generator, if given) to a file."""
+        self._ck(self.lib.ima_gpu_checkpoint_write(self.h, os.fsencode(path),
+                                                   C.byref(rng) if rng is not None else None))
+
+    def checkpoint_read(self, path, rng=None):
+        """Restore a checkpoint_write file into this context (same loci and
+        chains; the population model set first when the file holds labels);
+        rng, if given, takes the saved generator state."""
+        self._ck(self.lib.ima_gpu_checkpoint_read(self.h, os.fsencode(path),
+                                                  C.byref(rng) if rng is not None else None))
 
     def surface_append_tree_rows(self, groups):
         """Append the gsampinf rows of these chains (last tree_prob) to the

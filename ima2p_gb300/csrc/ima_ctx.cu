@@ -262,7 +262,8 @@ struct ima_ctx {
   std::vector<long long> h_mbase;
   std::vector<int32_t> h_mcnt, h_mcap;
   std::vector<uint8_t> has_labels;
-  std::vector<double> h_tvr;
+  std::vector<double> h_tvr, h_hval;
+  std::vector<int32_t> h_samp;
   bool locus_pops = false;
   void *d_rsel = nullptr;
   size_t rsel_cap = 0;
@@ -1506,6 +1507,10 @@ extern "C" int ima_gpu_set_probg(ima_ctx *c, const double *probg)
 {
   return copy_dev(c, c ? c->d_probg : nullptr, probg, c ? c->nchains * 8 : 0, cudaMemcpyHostToDevice, "probg");
 }
+extern "C" int ima_gpu_get_probg(ima_ctx *c, double *probg)
+{
+  return copy_dev(c, probg, c ? c->d_probg : nullptr, c ? c->nchains * 8 : 0, cudaMemcpyDeviceToHost, "probg");
+}
 
 extern "C" int ima_gpu_swapchains(ima_ctx *c, int swaptries, int include_probg, const double *uniforms,
                                   int stride, uint64_t seed, int32_t *used, int32_t *swap0ok)
@@ -2468,6 +2473,8 @@ extern "C" int ima_gpu_set_locus_pops(ima_ctx *c, const double *hval, const int3
   r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "locus pops");
   if (r) return r;
   c->h_tvr.assign((size_t)c->nchains * (npops - 1), 0.0);
+  c->h_hval.assign(hval, hval + nl);
+  c->h_samp.assign(samppop, samppop + (size_t)nl * npops);
   c->locus_pops = true;
   return IMA_OK;
 }
@@ -2608,6 +2615,9 @@ static int band_run(ima_ctx *c, int nch, const int32_t *chains, const int32_t *p
     prm[5 * k + 3] = t_u[k];
     prm[5 * k + 4] = t_d[k];
   }
+  const int nsplit = last;
+  if (c->h_tvr.size() == (size_t)c->nchains * nsplit)  // the split times the labels follow from here on
+    for (int k = 0; k < nch; k++) c->h_tvr[(size_t)chains[k] * nsplit + period[k]] = inverse ? oldt[k] : newt[k];
   cudaSetDevice(c->device);
   char *buf = static_cast<char *>(rsel(c, 256 + nch * 4ul + 256 + 40ul * nch));
   if (!buf) return c->fail(IMA_ERR_NOMEM, "band buffers");
@@ -2872,4 +2882,250 @@ extern "C" int ima_gpu_changet_ry1_sweep(ima_ctx *c, int nch, const int32_t *cha
     for (int k = 0; !r && k < nch; k++) probg[k] = all[chains[k]];
   }
   return r;
+}
+
+// ======================================================================
+// checkpoints of the resident chain state (resume a run, with the caller's
+// generator state, as the reference's .mcf files and seed do)
+namespace {
+const char CKP_MAGIC[8] = {'I', 'M', 'A', 'C', 'K', 'P', '0', '1'};
+
+struct CkpHeader {
+  char magic[8];
+  int32_t version, nloci, nchains, nitems;
+  int64_t nnodes, nsched, nal;
+  int32_t npops, has_labels, locus_pops, has_rng;
+  int64_t nmig;
+};
+
+struct CkpFile {
+  FILE *f = nullptr;
+  bool ok = true;
+  ~CkpFile() { if (f) fclose(f); }
+  void put(const void *p, size_t bytes) { if (ok && bytes && fwrite(p, 1, bytes, f) != bytes) ok = false; }
+  void get(void *p, size_t bytes) { if (ok && bytes && fread(p, 1, bytes, f) != bytes) ok = false; }
+};
+
+int dev_to_host(ima_ctx *c, void *dst, const void *src, size_t bytes)
+{
+  if (!bytes) return IMA_OK;
+  return c->cuda(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost), "checkpoint");
+}
+int host_to_dev(ima_ctx *c, void *dst, const void *src, size_t bytes)
+{
+  if (!bytes) return IMA_OK;
+  return c->cuda(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice), "checkpoint");
+}
+}  // namespace
+
+extern "C" int ima_gpu_checkpoint_write(ima_ctx *c, const char *path, const ima_mt19937 *rng)
+{
+  if (!c || !path) return IMA_ERR_ARG;
+  if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
+  cudaSetDevice(c->device);
+  int r = c->cuda(cudaStreamSynchronize(c->st), "checkpoint");
+  r = r ? r : sync_mirror(c);
+  if (r) return r;
+  const size_t ni = c->nitems, nn = c->nnodes;
+  CkpHeader h;
+  memset(&h, 0, sizeof(h));
+  memcpy(h.magic, CKP_MAGIC, 8);
+  h.version = 1;
+  h.nloci = c->nloci;
+  h.nchains = c->nchains;
+  h.nitems = c->nitems;
+  h.nnodes = (int64_t)nn;
+  h.nsched = (int64_t)c->nsched;
+  h.nal = (int64_t)c->nal;
+  h.npops = c->tw_ready ? c->h_tw.npops : 0;
+  h.has_labels = c->d_pop ? 1 : 0;
+  h.locus_pops = c->locus_pops ? 1 : 0;
+  h.has_rng = rng ? 1 : 0;
+  if (h.has_labels)
+    for (size_t i = 0; i < ni; i++) h.nmig += c->h_mcnt[i];
+  std::vector<double> pdg(ni), probg(c->nchains), beta(c->nchains);
+  r = dev_to_host(c, pdg.data(), c->d_pdg, ni * 8);
+  r = r ? r : dev_to_host(c, probg.data(), c->d_probg, c->nchains * 8ul);
+  r = r ? r : dev_to_host(c, beta.data(), c->d_beta, c->nchains * 8ul);
+  if (r) return r;
+  CkpFile F;
+  F.f = fopen(path, "wb");
+  if (!F.f) return c->fail(IMA_ERR_ARG, "cannot write %s", path);
+  F.put(&h, sizeof(h));
+  for (int li = 0; li < c->nloci; li++) {  // the loci, to check a restore against
+    const int32_t sig[3] = {c->loci[li].d.model, c->loci[li].d.n, c->loci[li].d.nsites};
+    F.put(sig, sizeof(sig));
+  }
+  F.put(c->h_nodes, nn * sizeof(NodeRec));
+  F.put(c->h_t64, nn * 8);
+  F.put(c->h_tff, nn * sizeof(float2));
+  F.put(c->h_sched, c->nsched * sizeof(int16_t));
+  F.put(c->h_nlev, ni * 4);
+  F.put(c->h_len, ni * 8);
+  F.put(c->h_pi, 4 * ni * 8);
+  F.put(c->h_al, c->nal * 4);
+  F.put(c->has_tree.data(), ni);
+  F.put(pdg.data(), ni * 8);
+  F.put(probg.data(), c->nchains * 8ul);
+  F.put(beta.data(), c->nchains * 8ul);
+  if (h.has_labels) {
+    std::vector<int32_t> pop(nn), moff(nn + ni);
+    std::vector<double> mt(c->mig_used);
+    std::vector<int32_t> mp(c->mig_used);
+    r = dev_to_host(c, pop.data(), c->d_pop, nn * 4);
+    r = r ? r : dev_to_host(c, moff.data(), c->d_moff, (nn + ni) * 4);
+    r = r ? r : dev_to_host(c, mt.data(), c->d_mig_t, c->mig_used * 8);
+    r = r ? r : dev_to_host(c, mp.data(), c->d_mig_p, c->mig_used * 4);
+    if (r) return r;
+    F.put(pop.data(), nn * 4);
+    F.put(moff.data(), (nn + ni) * 4);
+    F.put(c->h_mcnt.data(), ni * 4);
+    F.put(c->has_labels.data(), ni);
+    for (size_t i = 0; i < ni; i++) {  // each item's events, compacted in item order
+      F.put(mt.data() + c->h_mbase[i], (size_t)c->h_mcnt[i] * 8);
+      F.put(mp.data() + c->h_mbase[i], (size_t)c->h_mcnt[i] * 4);
+    }
+  }
+  if (h.locus_pops) {
+    F.put(c->h_hval.data(), c->nloci * 8ul);
+    F.put(c->h_samp.data(), c->h_samp.size() * 4);
+    F.put(c->h_tvr.data(), c->h_tvr.size() * 8);
+  }
+  if (rng) F.put(rng, sizeof(ima_mt19937));
+  if (!F.ok) return c->fail(IMA_ERR_ARG, "writing %s failed", path);
+  return IMA_OK;
+}
+
+extern "C" int ima_gpu_checkpoint_read(ima_ctx *c, const char *path, ima_mt19937 *rng)
+{
+  if (!c || !path) return IMA_ERR_ARG;
+  if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first (the same loci and chains)");
+  cudaSetDevice(c->device);
+  CkpFile F;
+  F.f = fopen(path, "rb");
+  if (!F.f) return c->fail(IMA_ERR_ARG, "cannot read %s", path);
+  CkpHeader h;
+  F.get(&h, sizeof(h));
+  const size_t ni = c->nitems, nn = c->nnodes;
+  if (!F.ok || memcmp(h.magic, CKP_MAGIC, 8) || h.version != 1)
+    return c->fail(IMA_ERR_DATA, "%s is not a checkpoint of this library", path);
+  if (h.nloci != c->nloci || h.nchains != c->nchains || h.nitems != c->nitems || h.nnodes != (int64_t)nn ||
+      h.nsched != (int64_t)c->nsched || h.nal != (int64_t)c->nal)
+    return c->fail(IMA_ERR_STATE, "checkpoint of %d loci x %d chains does not match this context", h.nloci, h.nchains);
+  for (int li = 0; li < c->nloci; li++) {
+    int32_t sig[3];
+    F.get(sig, sizeof(sig));
+    if (!F.ok || sig[0] != c->loci[li].d.model || sig[1] != c->loci[li].d.n || sig[2] != c->loci[li].d.nsites)
+      return c->fail(IMA_ERR_STATE, "checkpoint locus %d does not match this context's", li);
+  }
+  if ((h.has_labels || h.locus_pops) && (!c->tw_ready || c->h_tw.npops != h.npops))
+    return c->fail(IMA_ERR_STATE, "set the population model (%d populations) before restoring", h.npops);
+  if (h.nmig < 0 || h.npops < 0 || h.npops > TW_MAXPOPS) return c->fail(IMA_ERR_DATA, "%s: bad header", path);
+  {  // the whole file must be there before any state is replaced
+    size_t want = sizeof(h) + 12ul * c->nloci + nn * (sizeof(NodeRec) + 8 + sizeof(float2)) + c->nsched * 2 +
+                  ni * (4 + 8 + 32 + 1 + 8) + c->nal * 4 + c->nchains * 16ul;
+    if (h.has_labels) want += nn * 4 + (nn + ni) * 4 + ni * 5 + (size_t)h.nmig * 12;
+    if (h.locus_pops) want += c->nloci * (8ul + 4ul * h.npops) + c->nchains * 8ul * (h.npops - 1);
+    if (h.has_rng) want += sizeof(ima_mt19937);
+    const long here = ftell(F.f);
+    if (here < 0 || fseek(F.f, 0, SEEK_END) != 0) return c->fail(IMA_ERR_DATA, "%s: cannot size", path);
+    const long end = ftell(F.f);
+    if (end < 0 || (size_t)end != want || fseek(F.f, here, SEEK_SET) != 0)
+      return c->fail(IMA_ERR_DATA, "%s holds %ld bytes, this context's checkpoint %zu", path, end, want);
+  }
+  int r = c->cuda(cudaStreamSynchronize(c->st), "checkpoint");
+  if (r) return r;
+  F.get(c->h_nodes, nn * sizeof(NodeRec));
+  F.get(c->h_t64, nn * 8);
+  F.get(c->h_tff, nn * sizeof(float2));
+  F.get(c->h_sched, c->nsched * sizeof(int16_t));
+  F.get(c->h_nlev, ni * 4);
+  F.get(c->h_len, ni * 8);
+  F.get(c->h_pi, 4 * ni * 8);
+  F.get(c->h_al, c->nal * 4);
+  F.get(c->has_tree.data(), ni);
+  std::vector<double> pdg(ni), probg(c->nchains), beta(c->nchains);
+  F.get(pdg.data(), ni * 8);
+  F.get(probg.data(), c->nchains * 8ul);
+  F.get(beta.data(), c->nchains * 8ul);
+  if (!F.ok) return c->fail(IMA_ERR_DATA, "%s is truncated", path);
+  c->dev_lo = INT32_MAX;  // the file is authoritative now
+  c->dev_hi = -1;
+  c->dirty_lo = 0;        // upload everything with the next flush
+  c->dirty_hi = (int)ni - 1;
+  c->tdirty_lo = INT32_MAX;
+  c->tdirty_hi = -1;
+  c->evkey.valid = false;
+  r = flush(c);
+  r = r ? r : host_to_dev(c, c->d_pdg, pdg.data(), ni * 8);
+  r = r ? r : host_to_dev(c, c->d_probg, probg.data(), c->nchains * 8ul);
+  r = r ? r : host_to_dev(c, c->d_beta, beta.data(), c->nchains * 8ul);
+  if (r) return r;
+  if (h.has_labels) {
+    r = labels_alloc(c);
+    if (r) return r;
+    std::vector<int32_t> pop(nn), moff(nn + ni), cnt(ni);
+    std::vector<uint8_t> has(ni);
+    F.get(pop.data(), nn * 4);
+    F.get(moff.data(), (nn + ni) * 4);
+    F.get(cnt.data(), ni * 4);
+    F.get(has.data(), ni);
+    std::vector<double> mt((size_t)h.nmig);
+    std::vector<int32_t> mp((size_t)h.nmig);
+    std::vector<long long> base(ni);
+    size_t used = 0;
+    for (size_t i = 0; i < ni; i++) {
+      if (cnt[i] < 0 || used + cnt[i] > (size_t)h.nmig) return c->fail(IMA_ERR_DATA, "%s: bad event counts", path);
+      F.get(mt.data() + used, (size_t)cnt[i] * 8);
+      F.get(mp.data() + used, (size_t)cnt[i] * 4);
+      base[i] = (long long)used;
+      used += cnt[i];
+    }
+    if (!F.ok) return c->fail(IMA_ERR_DATA, "%s is truncated", path);
+    if (used > c->mig_cap) {
+      cudaFree(c->d_mig_t);
+      cudaFree(c->d_mig_p);
+      c->d_mig_t = dev_alloc<double>(used, c->dev_bytes, c->st);
+      c->d_mig_p = dev_alloc<int32_t>(used, c->dev_bytes, c->st);
+      if (!c->d_mig_t || !c->d_mig_p) return c->fail(IMA_ERR_NOMEM, "migration events");
+      c->mig_cap = used;
+    }
+    r = host_to_dev(c, c->d_pop, pop.data(), nn * 4);
+    r = r ? r : host_to_dev(c, c->d_moff, moff.data(), (nn + ni) * 4);
+    r = r ? r : host_to_dev(c, c->d_mbase, base.data(), ni * 8);
+    r = r ? r : host_to_dev(c, c->d_mig_t, mt.data(), used * 8);
+    r = r ? r : host_to_dev(c, c->d_mig_p, mp.data(), used * 4);
+    if (r) return r;
+    c->mig_used = used;
+    c->h_mbase = base;
+    c->h_mcnt = cnt;
+    c->h_mcap = cnt;
+    c->has_labels = has;
+  }
+  if (h.locus_pops) {
+    std::vector<double> hval(c->nloci), tvr((size_t)c->nchains * (h.npops - 1));
+    std::vector<int32_t> samp((size_t)c->nloci * h.npops);
+    F.get(hval.data(), hval.size() * 8);
+    F.get(samp.data(), samp.size() * 4);
+    F.get(tvr.data(), tvr.size() * 8);
+    if (!F.ok) return c->fail(IMA_ERR_DATA, "%s is truncated", path);
+    r = ima_gpu_set_locus_pops(c, hval.data(), samp.data());
+    if (r) return r;
+    c->h_tvr = tvr;
+  }
+  if (h.has_rng) {
+    ima_mt19937 g;
+    F.get(&g, sizeof(g));
+    if (!F.ok) return c->fail(IMA_ERR_DATA, "%s is truncated", path);
+    if (rng) *rng = g;
+  }
+  return c->cuda(cudaDeviceSynchronize(), "checkpoint");
+}
+
+extern "C" int ima_gpu_get_split_times(ima_ctx *c, double *tvals)
+{
+  if (!c || !tvals) return IMA_ERR_ARG;
+  if (!c->tw_ready || c->h_tvr.empty()) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_locus_pops first");
+  memcpy(tvals, c->h_tvr.data(), c->h_tvr.size() * 8);
+  return IMA_OK;
 }

@@ -357,6 +357,32 @@ class ResidentChainSet:
         ctx.set_betas(self.beta)     # resident heats and p(G) for the device decisions
         ctx.set_probg(self.probg)
 
+    @classmethod
+    def resume(cls, ctx, path, u, kappa=None, precision=api.PREC_FP64, rng=None):
+        """The chain set a checkpoint_write file holds, restored into ctx (the
+        loci added, ima_gpu_set_chains and the population model set as when
+        it was written); rng (may be None) takes the saved generator state.
+        Split times, heats and p(G) come from the context; one full
+        evaluation rebuilds the partial likelihoods the file does not hold
+        and gives back the saved G.pdg."""
+        self = cls.__new__(cls)
+        ctx.checkpoint_read(path, rng)
+        self.ctx = ctx
+        self.nch, self.nl = ctx.nchains, len(ctx.loci)
+        self.u = np.asarray(u, np.float64)
+        self.kappa = np.ones(self.nl) if kappa is None else np.asarray(kappa, np.float64)
+        self.prec = precision
+        self.ci = np.repeat(np.arange(self.nch, dtype=np.int32), self.nl)
+        self.li = np.tile(np.arange(self.nl, dtype=np.int32), self.nch)
+        self.chains = np.arange(self.nch, dtype=np.int32)
+        self.tvals = ctx.get_split_times()
+        self.beta = ctx.get_betas()
+        self.probg = ctx.get_probg()
+        self.pdg = self._eval()
+        ctx.commit(self.ci, self.li, np.ones(len(self.ci), np.uint8))
+        self.pdgsum = self._sums(self.pdg)
+        return self
+
     def _eval(self):
         r, _ = self.ctx.eval(self.ci, self.li, np.tile(self.u, self.nch), np.tile(self.kappa, self.nch),
                              precision=self.prec)

@@ -186,6 +186,7 @@ int ima_gpu_set_betas(ima_ctx *ctx, const double *beta);
 int ima_gpu_set_pdg(ima_ctx *ctx, const double *pdg);
 int ima_gpu_get_pdg(ima_ctx *ctx, double *pdg);
 int ima_gpu_set_probg(ima_ctx *ctx, const double *probg);
+int ima_gpu_get_probg(ima_ctx *ctx, double *probg);
 /* swapchains (swapchains.cpp:526-653) with swapbetasonly = 1 in every run.
  * Uniform source: if uniforms != NULL, run r consumes uniforms[r*stride ...]
  * in the reference's order (ci, cj rejection loop, then U only when w < 1)
@@ -375,6 +376,11 @@ int ima_gpu_changet_ry1_sweep(ima_ctx *ctx, int nch, const int32_t *chains, cons
  * to write them with ima_ti_write_binary.  rowlen must be the surface's
  * (IMA_ERR_ARG otherwise). */
 int ima_gpu_surface_get_rows(ima_ctx *ctx, int start, int count, int rowlen, float *rows);
+/* The split times the resident labels follow, [nchains][npops-1]: the last
+ * tvals given to ima_gpu_chain_weights, moved by ima_gpu_rubber_band (to
+ * newt, and back to oldt with inverse = 1) and by the rejections of
+ * ima_gpu_changet_ry1_sweep.  After ima_gpu_set_locus_pops. */
+int ima_gpu_get_split_times(ima_ctx *ctx, double *tvals);
 
 /* ------------------------------------------ saved genealogies (.ti files)
  * Host functions, no context.  ima_ti_read parses the reference's text
@@ -424,6 +430,27 @@ double ima_mt19937_uniform(ima_mt19937 *rng);
 int ima_gpu_modelloop(ima_ctx *ctx, int modeltype, const double *upper, int popsizemultiplier,
                       const double *xmap, int nested, int method, ima_mt19937 *rng, double *best,
                       double *ess, int *generations, int *restarts);
+
+/* ------------------------------------------------ checkpoint and restart
+ * The resident chain state to a file and back, for the restart the
+ * reference makes from its .mcf file (writemcf / readmcf, mcmcfile.cpp:
+ * 204-292 / 310-442, called at ima_main_mpi.cpp:1778, 2146, 4176): every
+ * chain-locus's genealogy (nodes, times, level schedule, length, base
+ * frequencies, alleles), its likelihood G.pdg, population labels and
+ * migration events (after ima_gpu_set_labels), the chains' p(G), heats and
+ * split times (after ima_gpu_set_locus_pops), each locus's hval and samppop,
+ * and (rng may be NULL) the caller's generator.  ima_gpu_checkpoint_read
+ * restores it into a context with the same loci and number of chains (the
+ * reference also fills more chains than the file holds by rereading it;
+ * here the counts must agree) and, when the
+ * file holds labels, the same population model already set -- IMA_ERR_STATE
+ * otherwise, IMA_ERR_DATA for a file that is not one or is truncated.  HKY
+ * partial likelihoods are not saved: the first evaluation after a restore
+ * is a full one (edits NULL), which gives the same G.pdg.  The reference's
+ * .mcf also carries its burn-in and sampling counters and the running
+ * tables of the host program; those stay with the caller. */
+int ima_gpu_checkpoint_write(ima_ctx *ctx, const char *path, const ima_mt19937 *rng);
+int ima_gpu_checkpoint_read(ima_ctx *ctx, const char *path, ima_mt19937 *rng);
 
 /* No counterpart in the reference.  The FP64 surface of ima_gpu_surface_eval
  * (IMA_SURF_FP64) for callers that cannot allocate device memory -- code

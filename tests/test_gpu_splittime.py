@@ -161,3 +161,91 @@ def test_device_decided_sweep_follows_the_reference():
             off += nl
             moff += len(m)
     ctx.close()
+
+
+def _resident_context(case):
+    ctx = api.Context(0)
+    for q in case.seqs:
+        ctx.add_locus_is(q)
+    ctx.set_chains(1, case.nch)
+    ctx.set_popmodel(case.pm, *case.priors())
+    return ctx
+
+
+def _run(cs, case, rng, sweeps):
+    res = []
+    for s0 in sweeps:
+        periods = [case.steps[s0 + c][1] for c in range(case.nch)]
+        acc = cs.sweep_device(periods, rng, case.tprior, case.npops)
+        for c in range(case.nch):
+            res.append((int(acc[c]), float(cs.tvals[c, periods[c]]), float(cs.probg[c]), float(cs.pdgsum[c])))
+    return res
+
+
+def test_checkpoint_resume_continues_the_run(tmp_path):
+    """ima_gpu_checkpoint_write after 12 sweeps, then ima_gpu_checkpoint_read
+    into a fresh context with the saved generator: the remaining 18 sweeps
+    make the uninterrupted run's decisions, split times, p(G) and likelihood
+    sums bit for bit (and so the reference's), and leave the same times on
+    the device.  A file for other chains, a truncated file and a file that
+    is not a checkpoint are refused."""
+    case = RyCase()
+    starts = list(range(0, len(case.steps), case.nch))
+    ctx = _resident_context(case)
+    cs = splittime.ResidentChainSet(ctx, case.fresh_gens(), [case.d["tv0"]] * case.nch, case.betas,
+                                    np.ones(case.nl), case.samps, case.us)
+    whole = _run(cs, case, api.MT19937(case.seed), starts)
+    base = case.fresh_gens()
+    want_t = [ctx.get_times(ci, li, len(base[ci][li].pop)) for ci in range(case.nch) for li in range(case.nl)]
+    ctx.close()
+
+    path = tmp_path / "chains.ckp"
+    ctx = _resident_context(case)
+    cs = splittime.ResidentChainSet(ctx, case.fresh_gens(), [case.d["tv0"]] * case.nch, case.betas,
+                                    np.ones(case.nl), case.samps, case.us)
+    rng = api.MT19937(case.seed)
+    first = _run(cs, case, rng, starts[:12])
+    ctx.checkpoint_write(path, rng)
+    saved_tv, saved_pdg, saved_pg = cs.tvals.copy(), ctx.get_pdg(), ctx.get_probg()
+    ctx.close()
+
+    ctx = _resident_context(case)
+    rng2 = api.MT19937(1)
+    cs2 = splittime.ResidentChainSet.resume(ctx, path, case.us, rng=rng2)
+    assert np.array_equal(cs2.tvals, saved_tv)
+    assert np.array_equal(cs2.pdg, saved_pdg)
+    assert np.array_equal(cs2.probg, saved_pg)
+    assert np.array_equal(np.frombuffer(bytes(rng2), np.uint8), np.frombuffer(bytes(rng), np.uint8))
+    rest = _run(cs2, case, rng2, starts[12:])
+    assert first + rest == whole
+    res, ref = np.array(whole), case.res
+    assert np.array_equal(res[:, 0], ref[:, 0])
+    assert np.array_equal(res[:, 1], ref[:, 1])
+    k = 0
+    for ci in range(case.nch):
+        for li in range(case.nl):
+            t, m = ctx.get_times(ci, li, len(base[ci][li].pop))
+            edge = base[ci][li].g.down != -1
+            assert np.array_equal(t[edge], want_t[k][0][edge])
+            assert np.array_equal(m, want_t[k][1])
+            k += 1
+    ctx.close()
+
+    other = api.Context(0)  # one chain fewer
+    for q in case.seqs:
+        other.add_locus_is(q)
+    other.set_chains(1, case.nch - 1)
+    other.set_popmodel(case.pm, *case.priors())
+    with pytest.raises(api.ImaError):
+        other.checkpoint_read(path)
+    other.close()
+    data = path.read_bytes()
+    short = tmp_path / "short.ckp"
+    short.write_bytes(data[:len(data) // 2])
+    junk = tmp_path / "junk.ckp"
+    junk.write_bytes(b"not a checkpoint" * 64)
+    ctx = _resident_context(case)
+    for bad in (short, junk):
+        with pytest.raises(api.ImaError):
+            ctx.checkpoint_read(bad)
+    ctx.close()
