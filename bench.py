@@ -35,6 +35,7 @@ sys.path.insert(0, ROOT)
 METRIC = "chain-locus likelihood evals/s"
 SURF_METRIC = "L-mode grid points/s"
 TW_METRIC = "genealogy weights (treeweight) per second"
+PM_METRIC = "2NM density terms (points x genealogies) per second"
 
 
 def measured_peaks():
@@ -401,9 +402,9 @@ def run_reference(args):
         return
     from ima2p_gb300 import workloads
 
-    if args.workload == "surface":
-        print(json.dumps({"impl": "reference", "unavailable": "surface reference arm not provided; "
-                          "see cpu_baseline of the surface line"}))
+    if args.workload in ("surface", "treeweight", "popmig"):
+        print(json.dumps({"impl": "reference", "unavailable": "%s reference arm not provided; "
+                          "see cpu_baseline of the %s line" % (args.workload, args.workload)}))
         return
     cores = os.cpu_count() or 1
     wl = workloads.make(args.workload)
@@ -754,19 +755,112 @@ def splittime_sweep(pm, packed, samp, tv, base, seq, nloci, nch, args):
                     "decisions taken in Python); CPU: one chain's update on the oracle's C functions"}
 
 
+def run_popmig(args):
+    """The 2NM curves of print_populationmigrationrate_histograms for a
+    3-population model (5 population sizes, 8 migration rates; its 8 default
+    2NM terms) over G = 300,000 saved genealogies (MAXGENEALOGIESTOSAVE):
+    one step = every term's range scan and its curve of GRIDSIZE 1000
+    points, every point a sum over all G genealogies of calc_popmig's
+    incomplete-gamma term.  The metric counts the curve terms (points x
+    genealogies); the scan is overhead in both implementations."""
+    from ima2p_gb300 import api, popmodel, synth
+    from oracle import pyoracle as O
+
+    G, grid = args.popmig_g, 1000
+    rng = np.random.default_rng(1013)
+    rows, _, off = synth.surface_stats(rng, G, 5, 8, 2)
+    pm = popmodel.build("((0,1):3,2):4", 3)
+    terms = popmodel.popmig_terms(pm)
+    tlist = [(t, m) for t, m, _ in terms]
+    qmax, mmax = np.full(5, 20.0), np.full(8, 2.0)
+    ctx = api.Context(0)
+    ctx.surface_load(rows, 5, 8, 3)
+    for _ in range(args.warmup):
+        xs, ys, mx = ctx.popmig_curves(tlist, qmax, mmax, gridsize=grid)
+    ctx.set_profiling(True)
+    k0 = ctx.kernel_stats(api.K_POPMIG)
+    n0 = ctx.launch_count()
+    wall = []
+    with Clocks(0) as clk:
+        for _ in range(args.steps):
+            ctx.flush_l2()
+            t0 = time.perf_counter()
+            xs, ys, mx = ctx.popmig_curves(tlist, qmax, mmax, gridsize=grid)
+            wall.append(time.perf_counter() - t0)
+    k1 = ctx.kernel_stats(api.K_POPMIG)
+    n_timed = ctx.launch_count() - n0
+    ctx.set_profiling(False)
+    nk = max(1, k1[0] - k0[0])
+    # scan points per step: each term scans down from the top in batches of
+    # 32, 128, 512, ... points until a density above 1e-9
+    nscan = 0
+    for (t, m), v in zip(tlist, mx):
+        pmmax = qmax[t] * mmax[m] / 2.0
+        need = grid - int(round(v * grid / pmmax - 0.5)) if v < pmmax else grid
+        b, left = 32, grid
+        while need > 0 and left > 0:
+            nscan += min(b, left)
+            need -= b
+            left -= b
+            b *= 4
+    launch_ms = (k1[1] - k0[1]) / nk
+    dev_ms = launch_ms * nk / args.steps
+    pts = len(tlist) * grid  # curve points; the top-down scan for each term's range is overhead
+    units = pts * G
+    value = units / (dev_ms / 1e3)
+    e2e = units / statistics.median(wall)
+    hbm, _, src = measured_peaks()
+    algo = G * rows.shape[1] * 4 + len(tlist) * grid * 8 * 3  # rows once, points and partials per launch
+    gbs = algo / (launch_ms / 1e3) / 1e9
+    out = {
+        "metric": PM_METRIC, "value": round(value, 1), "unit": "terms/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic gsampinf rows (cc ~ Poisson(8), fc ~ Gamma(4,1), mc ~ Poisson(1), fm ~ Gamma(2,1))",
+        "config": {"workload": "popmig-curves: G=%d genealogies, 3 populations (5 theta, 8 m), %d 2NM terms, "
+                               "curves of %d points each after the top-down range scan, posterior form"
+                               % (G, len(tlist), grid),
+                   "global_batch": pts, "l2": "flushed between timed steps (rows 57.6 MB; L2-resident within a step)"},
+        "e2e": {"value": round(e2e, 1), "unit": "terms/s", "h2d_bytes_per_step": int(pts * 40 + nscan * 40),
+                "d2h_bytes_per_step": int(pts * 16 + nscan * 8)},
+        "scan_points_per_step": nscan,
+        "curve_points_per_s": round(pts / (dev_ms / 1e3), 1),
+        "roofline": {"kernel": "k_popmig", "bound": "hbm", "achieved": round(gbs, 2), "peak": hbm, "unit": "GB/s",
+                     "frac": round(gbs / hbm, 6), "peak_source": src, "traffic": None,
+                     "note": "FP64-issue bound: one or two incomplete gamma series / continued fractions per "
+                             "(point, genealogy); HBM is not the limit"},
+        "gpu_launches": int(n_timed), "clocks": clk.summary(),
+    }
+    # CPU: the oracle's calc_popmig (C) over all G genealogies, one core
+    t0 = time.perf_counter()
+    n = 0
+    while time.perf_counter() - t0 < args.cpu_seconds or n == 0:
+        t, m = tlist[n % len(tlist)]
+        O.popmig(rows, 5, 8, t, m, xs[n % len(tlist), (n * 37) % grid], qmax[t], mmax[m])
+        n += 1
+    dt = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": round(n * G / dt, 1), "unit": "terms/s", "cores": 1, "kind": "port",
+                           "sample": "%d curve points over all %d genealogies through the oracle's "
+                                     "calc_popmig in C" % (n, G)}
+    print(json.dumps(out), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3000)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="hky", choices=["hky", "sw", "is", "mixed", "surface", "treeweight"])
+    ap.add_argument("--workload", default="hky", choices=["hky", "sw", "is", "mixed", "surface", "treeweight",
+                                                        "popmig"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-cap", type=int, default=4096)
     ap.add_argument("--surface-log2g", type=int, default=21, help="log2 genealogies (config 5: 21)")
     ap.add_argument("--surface-log2p", type=int, default=16, help="log2 points (config 5: 16)")
     ap.add_argument("--surface-method", default="tc", choices=["tc", "fp32"])
     ap.add_argument("--no-peak-search", action="store_true", help="surface: skip the DE peak search")
+    ap.add_argument("--popmig-g", type=int, default=300000, help="popmig: saved genealogies")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -776,6 +870,8 @@ def main():
         run_surface(args)
     elif args.workload == "treeweight":
         run_treeweight(args)
+    elif args.workload == "popmig":
+        run_popmig(args)
     else:
         run_ours(args)
 

@@ -24,9 +24,10 @@ PREC_FAST, PREC_FP64 = 0, 1
 EVAL_OK, EVAL_IS_REJECT, EVAL_IS_FAIL, EVAL_SW_ZERO = 0, 1, 2, 3
 SURF_FAST, SURF_FP64, SURF_COMPAT, SURF_TC = 0, 1, 2, 3
 K_IS, K_IS_SUMLOGK, K_HKY_FAST, K_HKY_FP64, K_SW_FAST, K_SW_FP64, K_SWAP, K_SURF_FAST, \
-    K_SURF_FP64, K_SURF_COMPAT, K_SURF_TC, K_MARGIN, K_TREEWEIGHT, K_TREE_PROB = range(14)
+    K_SURF_FP64, K_SURF_COMPAT, K_SURF_TC, K_MARGIN, K_TREEWEIGHT, K_TREE_PROB, K_POPMIG = range(15)
 KERNEL_NAMES = ["is", "is_sumlogk", "hky_fast", "hky_fp64", "sw_fast", "sw_fp64", "swap",
-                "surf_fast", "surf_fp64", "surf_compat", "surf_tc", "margin", "treeweight", "tree_prob"]
+                "surf_fast", "surf_fp64", "surf_compat", "surf_tc", "margin", "treeweight", "tree_prob",
+                "popmig"]
 REJECT_IS = -1000000000.0
 
 # every symbol the header declares (checked by tests/test_abi.py)
@@ -51,7 +52,7 @@ EXPORTS = [
     "ima_gpu_surface_append_tree_rows", "ima_gpu_surface_get_rows",
     "ima_gpu_set_locus_pops", "ima_gpu_set_labels", "ima_gpu_get_times", "ima_gpu_rubber_band",
     "ima_gpu_chain_weights", "ima_gpu_changet_ry1_sweep", "ima_gpu_get_probg", "ima_gpu_get_split_times",
-    "ima_gpu_checkpoint_write", "ima_gpu_checkpoint_read",
+    "ima_gpu_checkpoint_write", "ima_gpu_checkpoint_read", "ima_gpu_popmig", "ima_gpu_popmig_curves",
 ]
 
 
@@ -169,6 +170,8 @@ def _declare(L):
         "ima_gpu_get_split_times": (I, [P, P]),
         "ima_gpu_checkpoint_write": (I, [P, C.c_char_p, P]),
         "ima_gpu_checkpoint_read": (I, [P, C.c_char_p, P]),
+        "ima_gpu_popmig": (I, [P, I, P, P, P, P, P, P, I, P]),
+        "ima_gpu_popmig_curves": (I, [P, I, P, P, I, P, P, P, I, P, P, P]),
         "ima_gpu_swapchains": (I, [P, I, I, P, I, C.c_uint64, P, P]),
         "ima_gpu_get_swapcounts": (I, [P, I, P, P]),
         "ima_gpu_surface_load": (I, [P, I, I, P, I, I, I, P]),
@@ -621,6 +624,34 @@ class Context:
         out = np.zeros((count, rowlen), np.float32)
         self._ck(self.lib.ima_gpu_surface_get_rows(self.h, int(start), int(count), int(rowlen), _ptr(out)))
         return out
+
+    def popmig(self, thetai, mi, x, theta_max, mig_max, mig_mean=None, prob_or_like=0):
+        """calc_popmig (calc_pop_expomig with mig_mean) at the points: term
+        (thetai[k], mi[k]) at x[k]."""
+        x = _f64(np.atleast_1d(x))
+        n = len(x)
+        th = _i32(np.broadcast_to(np.asarray(thetai), (n,)).copy())
+        mi = _i32(np.broadcast_to(np.asarray(mi), (n,)).copy())
+        q, m = _f64(theta_max), _f64(mig_max)
+        mean = _f64(mig_mean) if mig_mean is not None else None
+        y = np.zeros(n)
+        self._ck(self.lib.ima_gpu_popmig(self.h, n, _ptr(th), _ptr(mi), _ptr(x), _ptr(q), _ptr(m),
+                                         _ptr(mean) if mean is not None else None, int(prob_or_like), _ptr(y)))
+        return y
+
+    def popmig_curves(self, terms, theta_max, mig_max, mig_mean=None, prob_or_like=0, gridsize=1000):
+        """The 2NM curves of the (thetai, mi) terms: (x [nt][gridsize],
+        y [nt][gridsize], maxx [nt])."""
+        terms = np.asarray(terms, np.int32).reshape(-1, 2)
+        nt = len(terms)
+        th, mi = _i32(terms[:, 0]), _i32(terms[:, 1])
+        q, m = _f64(theta_max), _f64(mig_max)
+        mean = _f64(mig_mean) if mig_mean is not None else None
+        xs, ys, mx = np.zeros((nt, gridsize)), np.zeros((nt, gridsize)), np.zeros(nt)
+        self._ck(self.lib.ima_gpu_popmig_curves(self.h, nt, _ptr(th), _ptr(mi), int(gridsize), _ptr(q), _ptr(m),
+                                                _ptr(mean) if mean is not None else None, int(prob_or_like),
+                                                _ptr(xs), _ptr(ys), _ptr(mx)))
+        return xs, ys, mx
 
     def fillvec(self, pmin, pmax, gridsize=1000, expo_mean=None):
         n = len(pmin)

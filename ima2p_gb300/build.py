@@ -20,7 +20,7 @@ LIB = os.path.join(HERE, "libima2p_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # k_treeweight.cu restates the reference's FP64 sums term by term: without
 # FMA contraction its adds and multiplies round as the host's do
-NOFMAD_FILES = {"k_treeweight.cu"}
+NOFMAD_FILES = {"k_treeweight.cu", "k_popmig.cu"}
 NOFMAD = ["-fmad=false"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
 

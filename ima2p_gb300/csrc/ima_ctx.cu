@@ -1680,6 +1680,186 @@ static int margin_run(ima_ctx *c, int n, const int32_t *param, const double *x, 
   return r ? r : c->cuda(cudaStreamSynchronize(c->st), "marginal");
 }
 
+static int ensure_logfact(ima_ctx *c);
+constexpr double EXPOMIGPLOTSCALE = 20;  // the 2NM plot scale in prior means (imamp.hpp:156)
+
+// calc_popmig / calc_pop_expomig at n points (term k: thetai[k], mi[k], x[k])
+static int popmig_run(ima_ctx *c, int n, const int32_t *thetai, const int32_t *mi, const double *x,
+                      const double *theta_max, const double *mig_max, const double *mig_mean, int prob_or_like,
+                      double *out)
+{
+  for (int k = 0; k < n; k++) {
+    if (thetai[k] < 0 || thetai[k] >= c->snp || mi[k] < 0 || mi[k] >= c->snm)
+      return c->fail(IMA_ERR_ARG, "point %d: term (%d, %d) out of range", k, thetai[k], mi[k]);
+    if (!(x[k] > 0.0)) return c->fail(IMA_ERR_ARG, "point %d: x must be > 0", k);
+  }
+  for (int i = 0; i < c->snp; i++)
+    if (!(theta_max[i] > 0.0)) return c->fail(IMA_ERR_ARG, "theta prior maximum %d must be > 0", i);
+  for (int i = 0; i < c->snm; i++) {
+    if (!(mig_max[i] > 0.0)) return c->fail(IMA_ERR_ARG, "migration prior maximum %d must be > 0", i);
+    if (mig_mean && !(mig_mean[i] > 0.0)) return c->fail(IMA_ERR_ARG, "exponential prior mean %d must be > 0", i);
+  }
+  if (int r0 = ensure_logfact(c)) return r0;
+  const int nchunks = popmig_chunks(c->sG, n);
+  std::vector<double> hq(n), hm(n), hmean(mig_mean ? n : 0);
+  for (int k = 0; k < n; k++) {
+    hq[k] = theta_max[thetai[k]];
+    hm[k] = mig_max[mi[k]];
+    if (mig_mean) hmean[k] = mig_mean[mi[k]];
+  }
+  // one device block: thetai | mi | x | qmax | mmax | mmean | out | error | partials
+  const size_t bytes = 256 * 9 + (size_t)n * (4 + 4 + 8 * 5) + 8 + (size_t)n * nchunks * 16;
+  if (bytes > c->mscratch_cap) {
+    cudaFree(c->d_mscratch);
+    c->d_mscratch = dev_alloc<char>(bytes, c->dev_bytes, c->st);
+    if (!c->d_mscratch) {
+      c->mscratch_cap = 0;
+      return c->fail(IMA_ERR_NOMEM, "2NM scratch (%zu bytes)", bytes);
+    }
+    c->mscratch_cap = bytes;
+  }
+  char *p = static_cast<char *>(c->d_mscratch);
+  auto take = [&](size_t b) {
+    char *q = p;
+    p += (b + 255) / 256 * 256;
+    return q;
+  };
+  int32_t *d_th = reinterpret_cast<int32_t *>(take((size_t)n * 4));
+  int32_t *d_mi = reinterpret_cast<int32_t *>(take((size_t)n * 4));
+  double *d_x = reinterpret_cast<double *>(take((size_t)n * 8));
+  double *d_q = reinterpret_cast<double *>(take((size_t)n * 8));
+  double *d_m = reinterpret_cast<double *>(take((size_t)n * 8));
+  double *d_mean = reinterpret_cast<double *>(take((size_t)n * 8));
+  double *d_out = reinterpret_cast<double *>(take((size_t)n * 8));
+  int32_t *d_err = reinterpret_cast<int32_t *>(take(8));
+  double *d_part = reinterpret_cast<double *>(take((size_t)n * nchunks * 16));
+  PopmigArgs a{};
+  a.G = c->sG;
+  a.rowlen = c->srowlen;
+  a.n = n;
+  a.expo = mig_mean ? 1 : 0;
+  a.prob_or_like = prob_or_like ? 1 : 0;
+  a.ccp = 0;  // gsampinf layout (initialize.cpp:709-718)
+  a.fcp = a.ccp + c->snp;
+  a.hccp = a.fcp + c->snp;
+  a.mcp = a.hccp + c->snp;
+  a.fmp = a.mcp + c->snm;
+  a.qip = a.fmp + c->snm;
+  a.mip = a.qip + c->snp;
+  a.rows = c->d_rows;
+  a.thetai = d_th;
+  a.mi = d_mi;
+  a.x = d_x;
+  a.qmax = d_q;
+  a.mmax = d_m;
+  a.mmean = mig_mean ? d_mean : nullptr;
+  a.logfact = c->d_logfact;
+  a.err = d_err;
+  int r = c->cuda(cudaMemcpyAsync(d_th, thetai, (size_t)n * 4, cudaMemcpyHostToDevice, c->st), "2NM points");
+  r = r ? r : c->cuda(cudaMemcpyAsync(d_mi, mi, (size_t)n * 4, cudaMemcpyHostToDevice, c->st), "2NM points");
+  r = r ? r : c->cuda(cudaMemcpyAsync(d_x, x, (size_t)n * 8, cudaMemcpyHostToDevice, c->st), "2NM points");
+  r = r ? r : c->cuda(cudaMemcpyAsync(d_q, hq.data(), (size_t)n * 8, cudaMemcpyHostToDevice, c->st), "2NM priors");
+  r = r ? r : c->cuda(cudaMemcpyAsync(d_m, hm.data(), (size_t)n * 8, cudaMemcpyHostToDevice, c->st), "2NM priors");
+  if (mig_mean) r = r ? r : c->cuda(cudaMemcpyAsync(d_mean, hmean.data(), (size_t)n * 8, cudaMemcpyHostToDevice, c->st), "2NM priors");
+  r = r ? r : c->cuda(cudaMemsetAsync(d_err, 0, 4, c->st), "2NM status");
+  if (r) return r;
+  int lr = 0;
+  c->launch(IMA_K_POPMIG, (double)c->sG * c->srowlen * 4, [&] { lr = launch_popmig(a, d_part, nchunks, d_out, c->st); });
+  c->launches += 1;  // pass + merge
+  if (lr) return c->fail(IMA_ERR_ARG, "2NM densities: unsupported shape (%d)", lr);
+  int32_t err = 0;
+  r = c->cuda(cudaGetLastError(), "2NM launch");
+  r = r ? r : c->cuda(cudaMemcpyAsync(out, d_out, (size_t)n * 8, cudaMemcpyDeviceToHost, c->st), "2NM values");
+  r = r ? r : c->cuda(cudaMemcpyAsync(&err, d_err, 4, cudaMemcpyDeviceToHost, c->st), "2NM status");
+  r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "2NM");
+  if (!r && err)
+    return c->fail(IMA_ERR_DATA, "2NM density: %s", err == 5 ? "a count beyond the logfact table"
+                                                             : "an incomplete gamma series or fraction did not converge");
+  return r;
+}
+
+extern "C" int ima_gpu_popmig(ima_ctx *c, int n, const int32_t *thetai, const int32_t *mi, const double *x,
+                              const double *theta_max, const double *mig_max, const double *mig_mean,
+                              int prob_or_like, double *y)
+{
+  if (!c || n < 1 || !thetai || !mi || !x || !theta_max || !mig_max || !y) return IMA_ERR_ARG;
+  if (!c->d_rows) return c->fail(IMA_ERR_STATE, "call ima_gpu_surface_load first");
+  if (c->snm < 1) return c->fail(IMA_ERR_STATE, "the loaded surface has no migration parameters");
+  cudaSetDevice(c->device);
+  return popmig_run(c, n, thetai, mi, x, theta_max, mig_max, mig_mean, prob_or_like, y);
+}
+
+extern "C" int ima_gpu_popmig_curves(ima_ctx *c, int nterms, const int32_t *thetai, const int32_t *mi, int gridsize,
+                                     const double *theta_max, const double *mig_max, const double *mig_mean,
+                                     int prob_or_like, double *x_out, double *y_out, double *maxx)
+{
+  if (!c || nterms < 1 || !thetai || !mi || gridsize < 1 || !theta_max || !mig_max || !x_out || !y_out)
+    return IMA_ERR_ARG;
+  if (!c->d_rows) return c->fail(IMA_ERR_STATE, "call ima_gpu_surface_load first");
+  if (c->snm < 1) return c->fail(IMA_ERR_STATE, "the loaded surface has no migration parameters");
+  for (int t = 0; t < nterms; t++)
+    if (thetai[t] < 0 || thetai[t] >= c->snp || mi[t] < 0 || mi[t] >= c->snm)
+      return c->fail(IMA_ERR_ARG, "term %d: (%d, %d) out of range", t, thetai[t], mi[t]);
+  cudaSetDevice(c->device);
+  // pass 1: every term's scale grid (j + 0.5) pmmax / gridsize, scanned from
+  // the top for the first density above 1e-9 as the reference scans it; the
+  // points go to the device in batches from the top (32 per term, then 4x
+  // more each round) so that a scan that stops early costs little
+  const size_t npts = (size_t)nterms * gridsize;
+  if (npts > (size_t)INT32_MAX) return c->fail(IMA_ERR_ARG, "too many points");
+  std::vector<double> pmmax(nterms), mx(nterms, 0.0);
+  std::vector<int> top(nterms, gridsize - 1);  // highest index not yet scanned
+  for (int t = 0; t < nterms; t++)
+    pmmax[t] = mig_mean ? EXPOMIGPLOTSCALE * mig_mean[mi[t]] : theta_max[thetai[t]] * mig_max[mi[t]] / 2.0;
+  int r = IMA_OK;
+  for (long long batch = 32;; batch *= 4) {
+    std::vector<int32_t> th, mm, who;
+    std::vector<double> x;
+    for (int t = 0; t < nterms; t++) {
+      if (top[t] < 0) continue;
+      for (long long j = top[t]; j >= 0 && j > top[t] - batch; j--) {
+        th.push_back(thetai[t]);
+        mm.push_back(mi[t]);
+        who.push_back(t);
+        x.push_back((j + 0.5) * pmmax[t] / gridsize);
+      }
+    }
+    if (x.empty()) break;
+    std::vector<double> y(x.size());
+    r = popmig_run(c, (int)x.size(), th.data(), mm.data(), x.data(), theta_max, mig_max, mig_mean, prob_or_like, y.data());
+    if (r) return r;
+    for (size_t k = 0; k < x.size();) {  // each term's points, top down
+      const int t = who[k];
+      size_t e = k;
+      while (e < x.size() && who[e] == t) e++;
+      for (size_t q = k; q < e && top[t] >= 0; q++) {
+        if (y[q] > 1e-9) {
+          mx[t] = x[q];
+          top[t] = -1;
+        } else if (--top[t] < 0) {
+          mx[t] = pmmax[t];  // no point above 1e-9
+        }
+      }
+      k = e;
+    }
+  }
+  std::vector<int32_t> th(npts), mm(npts);
+  std::vector<double> x(npts);
+  for (int t = 0; t < nterms; t++) {
+    if (maxx) maxx[t] = mx[t];
+    for (int j = 0; j < gridsize; j++) {
+      th[(size_t)t * gridsize + j] = thetai[t];
+      mm[(size_t)t * gridsize + j] = mi[t];
+      x[(size_t)t * gridsize + j] = (j + 0.5) * mx[t] / gridsize;
+    }
+  }
+  // pass 2: the curves on [0, maxx]
+  r = popmig_run(c, (int)npts, th.data(), mm.data(), x.data(), theta_max, mig_max, mig_mean, prob_or_like, y_out);
+  if (r) return r;
+  memcpy(x_out, x.data(), npts * 8);
+  return IMA_OK;
+}
+
 extern "C" int ima_gpu_margincalc(ima_ctx *c, int n, const int32_t *param, const double *x, double yadjust, int logi,
                                   const double *expo_mean, double *out)
 {
@@ -1946,6 +2126,26 @@ size_t carve_size(std::initializer_list<size_t> bytes)
 }
 }  // namespace
 
+// logfact[i] = log(1) + ... + log(i) accumulated as setlogfact does
+// (utilities.cpp:1406-1415), so the device table holds the host's values;
+// read by the incomplete gamma functions (p(G) integrals, 2NM densities)
+static int ensure_logfact(ima_ctx *c)
+{
+  if (c->d_logfact) return IMA_OK;
+  c->d_logfact = dev_alloc<double>(TW_LF_N, c->dev_bytes, c->st);
+  if (!c->d_logfact) return c->fail(IMA_ERR_NOMEM, "logfact table");
+  std::vector<double> lf(TW_LF_N);
+  lf[0] = 0;
+  for (int i = 1; i < TW_LF_N; i++) lf[i] = lf[i - 1] + log((double)i);
+  int r = c->cuda(cudaMemcpyAsync(c->d_logfact, lf.data(), sizeof(double) * TW_LF_N, cudaMemcpyHostToDevice, c->st), "logfact");
+  r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "logfact");
+  if (r) {
+    cudaFree(c->d_logfact);
+    c->d_logfact = nullptr;
+  }
+  return r;
+}
+
 extern "C" int ima_gpu_set_popmodel(ima_ctx *c, int npops, int nomig, int expo, const int32_t *plist,
                                     const int32_t *droppops, const int32_t *addpop, const int32_t *pop_e,
                                     const int32_t *pop_down, int nth, const int32_t *th_off,
@@ -2045,17 +2245,9 @@ extern "C" int ima_gpu_set_popmodel(ima_ctx *c, int npops, int nomig, int expo, 
   if (!c->d_tw) {
     c->d_tw = dev_alloc<TwModel>(1, c->dev_bytes, c->st);
     c->d_twerr = dev_alloc<int32_t>(2, c->dev_bytes, c->st);
-    c->d_logfact = dev_alloc<double>(TW_LF_N, c->dev_bytes, c->st);
-    if (!c->d_tw || !c->d_twerr || !c->d_logfact) return c->fail(IMA_ERR_NOMEM, "population model");
-    // logfact[i] = log(1) + ... + log(i) accumulated as setlogfact does
-    // (utilities.cpp:1406-1415), so the device table holds the host's values
-    std::vector<double> lf(TW_LF_N);
-    lf[0] = 0;
-    for (int i = 1; i < TW_LF_N; i++) lf[i] = lf[i - 1] + log((double)i);
-    int r = c->cuda(cudaMemcpyAsync(c->d_logfact, lf.data(), sizeof(double) * TW_LF_N, cudaMemcpyHostToDevice, c->st), "logfact");
-    r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "logfact");
-    if (r) return r;
+    if (!c->d_tw || !c->d_twerr) return c->fail(IMA_ERR_NOMEM, "population model");
   }
+  if (int r0 = ensure_logfact(c)) return r0;
   c->h_tw = h;
   int r = c->cuda(cudaMemcpyAsync(c->d_tw, &c->h_tw, sizeof(TwModel), cudaMemcpyHostToDevice, c->st), "population model");
   r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "population model");

@@ -142,6 +142,19 @@ struct MarginArgs {
 int margin_chunks(int G, int n);
 int launch_margin(const MarginArgs &a, double *part, int nchunks, double *out, cudaStream_t st);
 
+// 2NM densities (calc_popmig / calc_pop_expomig) at n requested points
+struct PopmigArgs {
+  int G, rowlen, n, expo, prob_or_like;
+  int ccp, fcp, hccp, mcp, fmp, qip, mip;  // gsampinf column offsets
+  const float *rows;                       // [G][rowlen]
+  const int32_t *thetai, *mi;              // [n] parameter indices of each point's term
+  const double *x, *qmax, *mmax, *mmean;   // [n]; mmean only under the exponential prior
+  const double *logfact;                   // [TW_LF_N]
+  int32_t *err;                            // first failing series / fraction (0 = none)
+};
+int popmig_chunks(int G, int n);
+int launch_popmig(const PopmigArgs &a, double *part, int nchunks, double *out, cudaStream_t st);
+
 // genealogy weights (treeweight) and p(G) integrals (initialize_integrate_tree_prob)
 #define TW_MAXPOPS 10                      // MAXPOPS, imamp.hpp:122
 #define TW_MAXTP (2 * TW_MAXPOPS - 1)

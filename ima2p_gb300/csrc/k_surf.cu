@@ -21,6 +21,7 @@
 #include <mutex>
 
 #include "internal.h"
+#include "eexp.cuh"
 
 namespace {
 
@@ -165,28 +166,6 @@ __global__ void k_surf_merge(SurfArgs a, int nchunks, const double *part)
 
 // -------------------------------------------------------------- compat
 constexpr int CP_BS = 256;
-
-__device__ void eexp_dev(double x, double *m, int *z)
-{
-  const double inv_fact[10] = {1.0, 0.5, 0.16666666666666666666666666667,
-                               0.04166666666666666666666666667, 0.00833333333333333333333333333,
-                               0.001388888888888888888888888889, 0.000198412698412698412698412698,
-                               0.000024801587301587301587301587301,
-                               2.75573192239858906525573192239859e-6,
-                               2.75573192239858906525573192239e-7};
-  const double log10_2 = 0.30102999566398119521;
-  int n = (int)floor(x / LOG2);
-  double zr = log10_2 * (double)n;
-  *z = (int)zr;
-  zr -= (double)*z;
-  double u = x - ((double)n) * LOG2;
-  double t = inv_fact[9];
-  for (int k = 8; k >= 0; k--) t = inv_fact[k] + u * t;
-  t = 1 + u * t;
-  *m = t * pow(10.0, zr);
-  if (fabs(*m) > 10) { *m = *m / 10.0; *z = *z + 1; }
-  if (fabs(*m) < 1) { *m = *m * 10.0; *z = *z - 1; }
-}
 
 template <typename T, typename Op>
 __device__ T block_reduce(T v, Op op, T *sh)

@@ -33,6 +33,8 @@
 
 #include <cfloat>
 
+#include "igamma.cuh"
+
 namespace {
 
 constexpr int TW_WPB = 4;  // genealogies (warps) per block
@@ -382,146 +384,9 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_tw_sweep(TwArgs a, int wpb, int
 }
 
 // ---------------------------------------------------------------- p(G)
-// The reference's incomplete gamma functions, restated from the published
-// Numerical Recipes methods it uses (series, Lentz continued fraction, E1
-// series / continued fraction) with its constants: EPS 3e-7, ITMAX 1000,
-// FPMIN 1e-30, expint's MAXIT 100 and Euler constant 0.5772156649.
-constexpr double IG_EPS = 3.0e-7, IG_FPMIN = 1.0e-30, EI_EULER = 0.5772156649;
-constexpr int IG_ITMAX = 1000, EI_MAXIT = 100;
-constexpr double LD_CUT = 7.0978271289338397e+02, MPRIORMIN = 0.000001;
-constexpr double LOG2 = 0.69314718055994530941723212146;
-
-struct Ig {
-  const double *lft;
-  int st;
-  __device__ double lf(int i)
-  {
-    if (i < 0 || i >= TW_LF_N) {
-      st = TW_E_LF;
-      return 0.0;
-    }
-    return lft[i];
-  }
-  __device__ double gser(int a, double x, double *gln, bool lg)
-  {
-    *gln = lf(a - 1);
-    if (x <= 0.0) {
-      if (x < 0.0) st = TW_E_TERM;
-      return 0.0;
-    }
-    double ap = a, del = 1.0 / a, sum = del;
-    for (int n = 1; n <= IG_ITMAX; n++) {
-      ++ap;
-      del *= x / ap;
-      sum += del;
-      if (fabs(del) < fabs(sum) * IG_EPS)
-        return lg ? log(sum) + (-x + a * log(x) - (*gln)) : sum * exp(-x + a * log(x) - (*gln));
-    }
-    st = TW_E_TERM;
-    return 0.0;
-  }
-  __device__ double gcf(double a, double x, double *gln, bool lg)
-  {
-    *gln = lf((int)a - 1);
-    double b = x + 1.0 - a, c = 1.0 / IG_FPMIN, d = 1.0 / b, h = d;
-    int i;
-    for (i = 1; i <= IG_ITMAX; i++) {
-      const double an = -i * (i - a);
-      b += 2.0;
-      d = an * d + b;
-      if (fabs(d) < IG_FPMIN) d = IG_FPMIN;
-      c = b + an / c;
-      if (fabs(c) < IG_FPMIN) c = IG_FPMIN;
-      d = 1.0 / d;
-      const double del = d * c;
-      h *= del;
-      if (fabs(del - 1.0) < IG_EPS) break;
-    }
-    if (i > IG_ITMAX) st = TW_E_TERM;
-    return lg ? (-x + a * log(x) - (*gln)) + log(h) : exp(-x + a * log(x) - (*gln)) * h;
-  }
-  __device__ double expint1(double x, bool *islog)
-  {
-    *islog = false;
-    if (x <= 0.0) {
-      st = TW_E_TERM;
-      return 0.0;
-    }
-    if (x > 1.0) {
-      double b = x + 1, c = 1.0 / IG_FPMIN, d = 1.0 / b, h = d;
-      for (int i = 1; i <= EI_MAXIT; i++) {
-        const double an = -i * i;
-        b += 2.0;
-        d = 1.0 / (an * d + b);
-        c = b + an / c;
-        const double del = c * d;
-        h *= del;
-        if (fabs(del - 1.0) < IG_EPS) {
-          *islog = true;
-          return log(h) - x;
-        }
-      }
-      st = TW_E_TERM;
-      return 0.0;
-    }
-    double ans = -log(x) - EI_EULER, fact = 1.0;
-    for (int i = 1; i <= EI_MAXIT; i++) {
-      fact *= -x / i;
-      const double del = -fact / i;
-      ans += del;
-      if (fabs(del) < fabs(ans) * IG_EPS) return ans;
-    }
-    st = TW_E_TERM;
-    return ans;
-  }
-  __device__ double upper(int a, double x)  // uppergamma: log Gamma(a, x)
-  {
-    double p, gln;
-    if (x < 0.0 || a < 0) {
-      st = TW_E_TERM;
-      return 0.0;
-    }
-    if (a == 0) {
-      bool islog;
-      const double t = expint1(x, &islog);
-      p = islog ? t : log(t);
-    } else if (x < (a + 1.0)) {
-      const double gs = gser(a, x, &gln, false);
-      p = gln + log(1.0 - gs);
-    } else {
-      p = gln_plus_gcf(a, x, true);
-    }
-    return p < -1e200 ? -1e200 : p;
-  }
-  __device__ double gln_plus_gcf(int a, double x, bool lg)
-  {
-    double gln;
-    const double v = gcf((double)a, x, &gln, lg);
-    return lg ? gln + v : gln + log(1 - v);
-  }
-  __device__ double lower(int a, double x)  // lowergamma: log gamma(a, x)
-  {
-    double p, gln;
-    if (x < 0.0 || a <= 0) {
-      st = TW_E_TERM;
-      return 0.0;
-    }
-    if (x < (a + 1.0)) {
-      const double gs = gser(a, x, &gln, true);
-      p = gln + gs;
-    } else {
-      p = gln_plus_gcf(a, x, false);
-    }
-    return p < -1e200 ? -1e200 : p;
-  }
-  __device__ double logdiff(double a, double b)  // LogDiff, imamp.hpp:257-262
-  {
-    if (a <= b) {
-      st = TW_E_TERM;
-      return 0.0;
-    }
-    return (a - b < LD_CUT) ? b + log(exp(a - b) - 1.0) : a;
-  }
+// The incomplete gamma functions (IgBase) are shared with the 2NM densities
+// (igamma.cuh); Ig adds the integral terms of initialize_integrate_tree_prob.
+struct Ig : IgBase {
   __device__ double coal(int cc, double fc, double hcc, double max, double min)
   {
     double p;
@@ -675,7 +540,7 @@ __global__ void __launch_bounds__(TP_BS) k_tp_params(TwProbArgs a)
   int c = 0;
   double f = 0.0, hc = 0.0;
   float ff = 0.0f, hf = 0.0f;
-  Ig ig{a.logfact, 0};
+  Ig ig{{a.logfact, 0}};
   double v;
   if (th) {
     for (int j = M.th_off[i]; j < M.th_off[i + 1]; j++) {

@@ -188,3 +188,18 @@ def build(treestring: str, npops: int, nomig: bool = False) -> PopModel:
                         mg_names.append("m%d>%d" % (src, dst))
     return PopModel(npops, plist, droppops, addpop, pop_e, pop_down, bool(nomig),
                     th_cells, mg_cells, th_names, mg_names)
+
+
+def popmig_terms(pm: PopModel):
+    """The 2NM terms print_populationmigrationrate_histograms draws for the
+    default parameterisation (histograms.cpp:754-773): for every population
+    but the root (thetai < numtreepops - 1), each migration parameter whose
+    name starts with that population ("m<thetai>>..."), in (thetai, mi)
+    order; returns [(thetai, mi, label)] with the reference's "2N<i>m<i>><j>"
+    labels."""
+    out = []
+    for ti in range(2 * pm.npops - 2):
+        for mi, name in enumerate(pm.mg_names):
+            if int(name[1:].split(">")[0]) == ti:
+                out.append((ti, mi, "2N%d%s" % (ti, name)))
+    return out

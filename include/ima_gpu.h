@@ -243,6 +243,34 @@ int ima_gpu_margincalc(ima_ctx *ctx, int n, const int32_t *param, const double *
  * MPRIORMIN (1e-6) are skipped, as fillvec skips them, with y = 0. */
 int ima_gpu_fillvec(ima_ctx *ctx, int gridsize, const double *pmin, const double *pmax,
                     const double *expo_mean, double *x_out, double *y_out);
+/* calc_popmig (popmig.cpp:9-91), or calc_pop_expomig (:96-172) when
+ * mig_mean != NULL (EXPOMIGRATIONPRIOR): the posterior density of the
+ * population migration rate 2N_i m_j of the term (thetai[k], mi[k]) at
+ * x[k] > 0, over the loaded genealogies; prob_or_like = 1 divides it by the
+ * prior density of 2NM (the likelihood curve).  theta_max [np] and mig_max
+ * [nm] are the priors' maxima (itheta[].pr.max, imig[].pr.max), mig_mean
+ * [nm] the exponential priors' means.  The terms follow the reference's
+ * branches and operation order, including its quirks (counts truncated, a
+ * genealogy whose two gamma terms do not separate adds exp(0)); the sum over
+ * genealogies is in FP64, chunked, so it agrees with the reference's to
+ * rounding.  IMA_ERR_DATA where the reference's series or fraction would
+ * not converge. */
+int ima_gpu_popmig(ima_ctx *ctx, int n, const int32_t *thetai, const int32_t *mi, const double *x,
+                   const double *theta_max, const double *mig_max, const double *mig_mean, int prob_or_like,
+                   double *y);
+/* The 2NM curves print_populationmigrationrate_histograms computes for the
+ * default parameterisation (histograms.cpp:755-805): for each term t, the
+ * grid (j + 0.5) pmmax / gridsize (pmmax = theta_max * mig_max / 2, or
+ * EXPOMIGPLOTSCALE (20) * mig_mean under the exponential prior) is scanned
+ * from the top for the first density above 1e-9, which sets maxx[t] (pmmax
+ * when there is none); then x_out[t][j] = (j + 0.5) maxx[t] / gridsize and
+ * y_out[t][j] the density there (GRIDSIZE is 1000).  Each pass is one launch
+ * over every term.  maxx may be NULL.  The caller picks the terms (thetai
+ * below numtreepops - 1, each migration parameter whose first population is
+ * thetai), as the reference does from the parameter names. */
+int ima_gpu_popmig_curves(ima_ctx *ctx, int nterms, const int32_t *thetai, const int32_t *mi, int gridsize,
+                          const double *theta_max, const double *mig_max, const double *mig_mean,
+                          int prob_or_like, double *x_out, double *y_out, double *maxx);
 /* The loaded surface's shape (any pointer may be NULL). */
 int ima_gpu_surface_info(ima_ctx *ctx, int *G, int *numpopsizeparams, int *nummigrateparams, int *npops);
 
@@ -496,7 +524,8 @@ int ima_gpu_kernel_stats(ima_ctx *ctx, int kind, long long *launches, double *ms
 #define IMA_K_MARGIN 11
 #define IMA_K_TREEWEIGHT 12
 #define IMA_K_TREE_PROB 13
-#define IMA_K_COUNT 14
+#define IMA_K_POPMIG 14
+#define IMA_K_COUNT 15
 /* Total kernel launches issued by this library on the context. */
 int ima_gpu_launch_count(ima_ctx *ctx, long long *n);
 /* Write a device buffer larger than L2 (evicts resident data). */

@@ -1341,3 +1341,115 @@ int ora_treeweight_batch(int npops, const int *plist, const int *droppops, const
   free(moff);
   return bad;
 }
+
+/* ======================================================================
+ * 2NM densities.  calc_popmig (popmig.cpp:9-91): the posterior density of
+ * the population migration rate 2N_i m_j at x, a sum over the saved
+ * genealogies of exp(temp1 + temp2) with one or two incomplete gamma terms
+ * per genealogy (terms outside +-700 skipped); calc_pop_expomig (:96-172)
+ * the same under an exponential migration prior, its terms summed as eexp
+ * mantissa / decimal-exponent pairs rescaled to the largest exponent.
+ * prob_or_like = 1 divides by the prior density of 2NM.  Counts are
+ * truncated as the reference's (int) casts truncate them.
+ * ==================================================================== */
+static void popmig_cols(int np, int nm, int thetai, int mi, int *c)
+{
+  int ccp, fcp, hccp, mcp, fmp, qip, mip, pdgp, probgp;
+  ora_gsamp_offsets(np, nm, &ccp, &fcp, &hccp, &mcp, &fmp, &qip, &mip, &pdgp, &probgp);
+  c[0] = ccp + thetai; c[1] = fcp + thetai; c[2] = hccp + thetai; c[3] = mcp + mi;
+  c[4] = fmp + mi; c[5] = qip + thetai; c[6] = mip + mi;
+}
+
+double ora_popmig(int G, int rowlen, const float *g, int np, int nm, int thetai, int mi, double x,
+                  double qmax, double mmax, int prob_or_like, int *st)
+{
+  int c[7];
+  popmig_cols(np, nm, thetai, mi, c);
+  double sum = 0.0;
+  for (int e = 0; e < G; e++) {
+    const float *r = g + (size_t)e * rowlen;
+    int cc = (int)r[c[0]], mc = (int)r[c[3]];
+    double fc = r[c[1]], hc = r[c[2]], fm = r[c[4]], qintg = r[c[5]], mintg = r[c[6]];
+    double temp1, temp2;
+    if (fc == 0 && cc == 0 && fm > 0) {
+      temp1 = ORA_LOG2 - (mc * log(fm)) - hc - qintg - mintg;
+      temp2 = log(exp(ig_upper(mc, 2 * fm * x / qmax, st)) - exp(ig_upper(mc, mmax * fm, st)));
+    } else if (fm == 0 && mc == 0 && fc > 0) {
+      temp1 = ORA_LOG2 - (cc * log(fc)) - hc - qintg - mintg;
+      temp2 = log(exp(ig_upper(cc, 2 * fc / qmax, st)) - exp(ig_upper(cc, fc * mmax / x, st)));
+    } else if (fc == 0 && cc == 0 && mc == 0 && fm == 0) {
+      temp1 = log(2 * log(mmax * qmax / (2 * x))) - hc - qintg - mintg;
+      temp2 = 0;
+    } else {
+      temp1 = ORA_LOG2 + (mc * log(x)) - ((cc + mc) * log(fc + fm * x)) - hc - qintg - mintg;
+      double a = ig_upper(cc + mc, 2 * (fc + fm * x) / qmax, st);
+      double b = ig_upper(cc + mc, mmax * (fm + fc / x), st);
+      if (a == b) {
+        b = ig_lower(cc + mc, 2 * (fc + fm * x) / qmax, st);
+        a = ig_lower(cc + mc, mmax * (fm + fc / x), st);
+      }
+      if (a > b) {
+        temp2 = ld(a, b, st);
+      } else {
+        temp1 = temp2 = 0.0;
+      }
+    }
+    if ((temp1 + temp2 < 700) && (temp1 + temp2 > -700)) sum += exp(temp1 + temp2);
+  }
+  sum /= G;
+  if (prob_or_like) {
+    double temp = 2 * (log(qmax) + log(mmax) - log(2 * x)) / (qmax * mmax);
+    sum /= temp;
+  }
+  return sum;
+}
+
+double ora_pop_expomig(int G, int rowlen, const float *g, int np, int nm, int thetai, int mi, double x,
+                       double qmax, double mmean, int prob_or_like, int *st)
+{
+  int c[7];
+  popmig_cols(np, nm, thetai, mi, c);
+  double *mm = (double *)malloc(sizeof(double) * (size_t)(G > 0 ? G : 1));
+  int *zz = (int *)malloc(sizeof(int) * (size_t)(G > 0 ? G : 1));
+  if (!mm || !zz) { free(mm); free(zz); *st = 3; return 0.0; }
+  int maxz = -1000000000;
+  for (int e = 0; e < G; e++) {
+    const float *r = g + (size_t)e * rowlen;
+    int cc = (int)r[c[0]], mc = (int)r[c[3]];
+    double fc = r[c[1]], hc = r[c[2]], fm = r[c[4]], qintg = r[c[5]], mintg = r[c[6]];
+    double temp1 = x + fc * mmean + fm * mmean * x;
+    double temp2 = ORA_LOG2 - hc - log(mmean) - qintg - mintg;
+    double temp3 = 2 * temp1 / (mmean * qmax);
+    if (mc == 0 && cc == 0) {
+      temp3 = ig_upper(0, temp3, st);
+      temp2 += temp3;
+    } else if (cc == 0) {
+      temp3 = ig_upper(mc, temp3, st);
+      temp2 += temp3 - mc * log(fm + 1 / mmean);
+    } else if (mc == 0) {
+      temp3 = ig_upper(cc, temp3, st);
+      temp2 += temp3 + -cc * log(fc + x * (fm + 1 / mmean));
+    } else {
+      temp3 = ig_upper(mc + cc, temp3, st);
+      temp2 += temp3 - cc * log(x) + (cc + mc) * log(mmean * x / temp1);
+    }
+    ora_eexp(temp2, &mm[e], &zz[e]);
+    if (zz[e] > maxz) maxz = zz[e];
+  }
+  double acumm = 0.0;
+  for (int e = 0; e < G; e++) {
+    int zadj = zz[e] - (maxz - 10);
+    mm[e] *= pow(10.0, (double)zadj);
+    acumm += mm[e];
+  }
+  free(mm);
+  free(zz);
+  double sum = log(acumm) + (maxz - 10) * ORA_LOG10;
+  sum -= log((double)G);
+  sum = exp(sum);
+  if (prob_or_like) {
+    double temp = 2 * exp(ig_upper(0, 2 * x / (mmean * qmax), st)) / (qmax * mmean);
+    sum /= temp;
+  }
+  return sum;
+}

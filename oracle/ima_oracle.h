@@ -198,6 +198,15 @@ void ora_gsamp_row(int nomig, const int *cc, const double *hcc, const double *fc
                    const int *th_idx, int nmg, const int *mg_off, const int *mg_idx,
                    const double *q, const double *m, double pdg, double probg,
                    int nsplit, const double *tvals, float *row);
+/* calc_popmig (popmig.cpp:9-91) and calc_pop_expomig (:96-172): the
+ * posterior density (prob_or_like = 0) or likelihood (1) of 2N_i m_j at x
+ * for theta parameter thetai and migration parameter mi over G gsampinf
+ * rows; qmax / mmax the priors' maxima, mmean the exponential prior's mean.
+ * *st is set where the reference would stop in an incomplete gamma term. */
+double ora_popmig(int G, int rowlen, const float *g, int np, int nm, int thetai, int mi, double x,
+                  double qmax, double mmax, int prob_or_like, int *st);
+double ora_pop_expomig(int G, int rowlen, const float *g, int np, int nm, int thetai, int mi, double x,
+                       double qmax, double mmean, int prob_or_like, int *st);
 
 #ifdef __cplusplus
 }

@@ -70,6 +70,9 @@ def _declare(L):
         getattr(L, f).restype = D
     L.ora_margincalc.argtypes = [I, I, P, I, I, I, D, D, I, P]
     L.ora_margincalc.restype = D
+    for f in ("ora_popmig", "ora_pop_expomig"):
+        getattr(L, f).argtypes = [I, I, P, I, I, I, I, D, D, D, I, P]
+        getattr(L, f).restype = D
     L.ora_mt_seed.argtypes = [P, C.c_uint32]
     L.ora_mt_seed.restype = None
     L.ora_mt_uniform.argtypes = [P]
@@ -365,6 +368,39 @@ def ref_margincalc(rows, np_, nm, points, expo_mean=None):
     lines.append(str(len(points)))
     lines += ["%d %.17g %d %.17g" % (int(p), x, int(lg), ya) for p, x, lg, ya in points]
     out = run_ref("margin", "\n".join(lines) + "\n")
+    return np.array([float(v) for v in out.split()])
+
+
+# ------------------------------------------------------------- 2NM densities
+def popmig(rows, np_, nm, thetai, mi, x, qmax, mmax, mmean=None, prob_or_like=0):
+    """calc_popmig (calc_pop_expomig when mmean is given) at x; raises
+    ValueError where the reference would stop in an incomplete gamma term."""
+    G, rl = rows.shape
+    rows = np.ascontiguousarray(rows, np.float32)
+    st = C.c_int(0)
+    if mmean is None:
+        v = lib().ora_popmig(G, rl, _p(rows), np_, nm, int(thetai), int(mi), float(x), float(qmax),
+                             float(mmax), int(prob_or_like), C.byref(st))
+    else:
+        v = lib().ora_pop_expomig(G, rl, _p(rows), np_, nm, int(thetai), int(mi), float(x), float(qmax),
+                                  float(mmean), int(prob_or_like), C.byref(st))
+    if st.value:
+        raise ValueError("incomplete gamma term failed (%d)" % st.value)
+    return v
+
+
+def ref_popmig(rows, np_, nm, qmax, mmax, points, mmean=None):
+    """The reference's calc_popmig / calc_pop_expomig through
+    oracle/_ref/imaref (this container only); points: (thetai, mi, x,
+    prob_or_like) tuples; qmax [np], mmax [nm], mmean [nm] or None."""
+    G, rl = rows.shape
+    lines = ["%d %d %d %d %d" % (G, rl, np_, nm, 1 if mmean is not None else 0),
+             " ".join("%.9g" % v for v in np.asarray(rows, np.float32).ravel()),
+             " ".join("%.17g" % v for v in qmax), " ".join("%.17g" % v for v in mmax),
+             " ".join("%.17g" % v for v in (mmean if mmean is not None else np.zeros(nm)))]
+    lines.append(str(len(points)))
+    lines += ["%d %d %.17g %d" % (int(t), int(m), x, int(pl)) for t, m, x, pl in points]
+    out = run_ref("popmig", "\n".join(lines) + "\n")
     return np.array([float(v) for v in out.split()])
 
 

@@ -292,6 +292,36 @@ static void run_margin()
   }
 }
 
+/* POPMIG: G rowlen np nm expo rows[G*rowlen] qmax[np] mmax[nm] mmean[nm] npts
+ *         then per point: thetai mi x prob_or_like -> calc_popmig (calc_pop_expomig
+ *         when expo) per point */
+static void run_popmig()
+{
+  int G = rd_i(), rowlen = rd_i(), np = rd_i(), nm = rd_i(), expo = rd_i();
+  load_gsampinf(G, rowlen, np, nm, 2);
+  setlogfact();
+  gsamp_ccp = 0;  // as setup_iparams (initialize.cpp:709-718) sets them
+  gsamp_fcp = gsamp_ccp + np;
+  gsamp_hccp = gsamp_fcp + np;
+  gsamp_mcp = gsamp_hccp + np;
+  gsamp_fmp = gsamp_mcp + nm;
+  gsamp_qip = gsamp_fmp + nm;
+  gsamp_mip = gsamp_qip + np;
+  modeloptions[EXPOMIGRATIONPRIOR] = expo;
+  itheta = static_cast<struct i_param *>(calloc(np, sizeof(struct i_param)));
+  imig = static_cast<struct i_param *>(calloc(nm, sizeof(struct i_param)));
+  for (int i = 0; i < np; i++) itheta[i].pr.max = rd_d();
+  for (int i = 0; i < nm; i++) imig[i].pr.max = rd_d();
+  for (int i = 0; i < nm; i++) imig[i].pr.mean = rd_d();
+  int npts = rd_i();
+  for (int k = 0; k < npts; k++) {
+    int ti = rd_i(), mi = rd_i();
+    double x = rd_d();
+    int pl = rd_i();
+    printf("%.17g\n", expo ? calc_pop_expomig(ti, mi, x, pl) : calc_popmig(ti, mi, x, pl));
+  }
+}
+
 /* TW: npops nchains nloci expo nomig treestring thetaprior mprior
  *     per locus: numgenes hval samppop[npops]
  *     per chain: tvals[npops-1]
@@ -519,7 +549,7 @@ static void run_iterm()
 
 int main(int argc, char **argv)
 {
-  if (argc != 3) { fprintf(stderr, "usage: imaref is|hky|sw|swap|jointp|de|margin|tw|iterm|ry <input>\n"); return 2; }
+  if (argc != 3) { fprintf(stderr, "usage: imaref is|hky|sw|swap|jointp|de|margin|tw|iterm|ry|popmig <input>\n"); return 2; }
   g_in = fopen(argv[2], "r");
   if (!g_in) { perror(argv[2]); return 2; }
   std::string mode = argv[1];
@@ -533,6 +563,7 @@ int main(int argc, char **argv)
   else if (mode == "tw") run_tw();
   else if (mode == "iterm") run_iterm();
   else if (mode == "ry") run_ry();
+  else if (mode == "popmig") run_popmig();
   else { fprintf(stderr, "unknown mode\n"); return 2; }
   fclose(g_in);
   return 0;

@@ -30,7 +30,12 @@ Fixtures:
                     with migration: decisions, split times, probg and pdg
                     per step, final node and migration times
 
-Run with fixture names (is hky sw swap jointp de margin tw ry) to regenerate only those.
+  golden_popmig.npz calc_popmig and calc_pop_expomig (2NM densities) over
+                    gsampinf rows that reach every branch of the terms
+                    (no coalescences, no migrations, neither), posterior
+                    and likelihood forms, and a 2NM curve grid
+
+Run with fixture names (is hky sw swap jointp de margin tw ry popmig) to regenerate only those.
 """
 from __future__ import annotations
 
@@ -494,12 +499,45 @@ def golden_ry():
     np.savez_compressed(os.path.join(OUT, "golden_ry.npz"), **out)
 
 
+def popmig_rows():
+    """gsampinf rows (3 population sizes, 2 migration rates) with every
+    branch of calc_popmig's term present: cc = fc = 0 (rows 0-19, theta 0),
+    mc = fm = 0 (rows 20-39, migration 0), all four zero (rows 40-49, theta
+    1 / migration 1)."""
+    rng = np.random.default_rng(2024)
+    rows, _, off = synth.surface_stats(rng, 200, 3, 2, 1)
+    rows[0:20, off["cc"] + 0] = 0
+    rows[0:20, off["fc"] + 0] = 0
+    rows[20:40, off["mc"] + 0] = 0
+    rows[20:40, off["fm"] + 0] = 0
+    for c in ("cc", "fc"):
+        rows[40:50, off[c] + 1] = 0
+    for c in ("mc", "fm"):
+        rows[40:50, off[c] + 1] = 0
+    return rows
+
+
+def golden_popmig():
+    rows = popmig_rows()
+    qmax, mmax, mean = np.array([20.0, 15.0, 25.0]), np.array([2.0, 5.0]), np.array([0.8, 1.7])
+    pts = [(t, m, x, pl) for (t, m) in ((0, 0), (1, 1), (0, 1), (2, 0))
+           for x in (0.01, 0.05, 0.7, 3.0, 9.0, 14.9, 40.0) for pl in (0, 1)]
+    # a curve: the 2NM grid of term (1, 1) at 50 points on (0, qmax mmax / 2]
+    grid = 50
+    pmmax = qmax[1] * mmax[1] / 2.0
+    pts += [(1, 1, (j + 0.5) * pmmax / grid, 0) for j in range(grid)]
+    out = {"rows": rows, "qmax": qmax, "mmax": mmax, "mean": mean, "points": np.array(pts), "grid": np.array(grid)}
+    out["ref"] = O.ref_popmig(rows, 3, 2, qmax, mmax, pts)
+    out["ref_expo"] = O.ref_popmig(rows, 3, 2, qmax, mmax, pts, mmean=mean)
+    np.savez_compressed(os.path.join(OUT, "golden_popmig.npz"), **out)
+
+
 if __name__ == "__main__":
     if not O.ref_available():
         sys.exit("build the reference harness first: make -C oracle ref")
     gens = {"is": golden_is, "hky": golden_hky, "sw": golden_sw, "swap": golden_swap,
             "jointp": golden_jointp, "de": golden_de, "margin": golden_margin,
-            "tw": golden_tw, "ry": golden_ry}
+            "tw": golden_tw, "ry": golden_ry, "popmig": golden_popmig}
     for name in (sys.argv[1:] or list(gens)):
         gens[name]()
     for f in sorted(os.listdir(OUT)):
