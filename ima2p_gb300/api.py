@@ -53,6 +53,7 @@ EXPORTS = [
     "ima_gpu_set_locus_pops", "ima_gpu_set_labels", "ima_gpu_get_times", "ima_gpu_rubber_band",
     "ima_gpu_chain_weights", "ima_gpu_changet_ry1_sweep", "ima_gpu_get_probg", "ima_gpu_get_split_times",
     "ima_gpu_checkpoint_write", "ima_gpu_checkpoint_read", "ima_gpu_popmig", "ima_gpu_popmig_curves",
+    "ima_gpu_findmarginpeaks",
 ]
 
 
@@ -172,6 +173,7 @@ def _declare(L):
         "ima_gpu_checkpoint_read": (I, [P, C.c_char_p, P]),
         "ima_gpu_popmig": (I, [P, I, P, P, P, P, P, P, I, P]),
         "ima_gpu_popmig_curves": (I, [P, I, P, P, I, P, P, P, I, P, P, P]),
+        "ima_gpu_findmarginpeaks": (I, [P, P, P, P, P, P, I, P, P, P, P, P, P, P, P, P, P, P, C.POINTER(I)]),
         "ima_gpu_swapchains": (I, [P, I, I, P, I, C.c_uint64, P, P]),
         "ima_gpu_get_swapcounts": (I, [P, I, P, P]),
         "ima_gpu_surface_load": (I, [P, I, I, P, I, I, I, P]),
@@ -652,6 +654,31 @@ class Context:
                                                 _ptr(mean) if mean is not None else None, int(prob_or_like),
                                                 _ptr(xs), _ptr(ys), _ptr(mx)))
         return xs, ys, mx
+
+    def findmarginpeaks(self, theta_min, theta_max, mig_min, mig_max, mig_mean=None, terms=()):
+        """findmarginpeaks' numbers: dict of mlval, peakloc ([3][np+nm]),
+        migtest, lo95, hi95, pm_mlval, pm_peakloc ([3][nterms]), pm_test,
+        holdpeakloc and rounds; terms = [(thetai, mi)] 2NM terms."""
+        _, np_, nm, _ = self.surface_info()
+        terms = np.asarray(terms, np.int32).reshape(-1, 2)
+        nt = len(terms)
+        mpop, mterm = _i32(terms[:, 0]), _i32(terms[:, 1])
+        f = lambda v: _f64(v) if v is not None else None  # noqa: E731
+        tmin, tmax, mmin, mmax, mean = f(theta_min), f(theta_max), f(mig_min), f(mig_max), f(mig_mean)
+        o = {"mlval": np.zeros((3, np_ + nm)), "peakloc": np.zeros((3, np_ + nm)), "migtest": np.zeros(max(nm, 1)),
+             "lo95": np.zeros(np_ + nm), "hi95": np.zeros(np_ + nm), "pm_mlval": np.zeros((3, max(nt, 1))),
+             "pm_peakloc": np.zeros((3, max(nt, 1))), "pm_test": np.zeros(max(nt, 1)),
+             "holdpeakloc": np.zeros(np_ + nm, np.float32)}
+        rounds = I()
+        self._ck(self.lib.ima_gpu_findmarginpeaks(
+            self.h, _ptr(tmin), _ptr(tmax), _ptr(mmin), _ptr(mmax), _ptr(mean), nt, _ptr(mpop), _ptr(mterm),
+            _ptr(o["mlval"]), _ptr(o["peakloc"]), _ptr(o["migtest"]), _ptr(o["lo95"]), _ptr(o["hi95"]),
+            _ptr(o["pm_mlval"]) if nt else None, _ptr(o["pm_peakloc"]) if nt else None,
+            _ptr(o["pm_test"]) if nt else None, _ptr(o["holdpeakloc"]), C.byref(rounds)))
+        o["migtest"] = o["migtest"][:nm]
+        o["pm_mlval"], o["pm_peakloc"], o["pm_test"] = o["pm_mlval"][:, :nt], o["pm_peakloc"][:, :nt], o["pm_test"][:nt]
+        o["rounds"] = rounds.value
+        return o
 
     def fillvec(self, pmin, pmax, gridsize=1000, expo_mean=None):
         n = len(pmin)

@@ -1617,18 +1617,25 @@ extern "C" int ima_gpu_surface_info(ima_ctx *c, int *G, int *np, int *nm, int *n
 }
 
 // ---------------------------------------------------------- 1-D marginals
+// genealogies [lo, hi) summed and divided by div; raw_cc as marginp reads cc
+struct GRange {
+  int lo, hi;
+  double div;
+  int raw_cc;
+};
+
 static int margin_run(ima_ctx *c, int n, const int32_t *param, const double *x, double yadjust, int logi,
-                      const double *expo_mean, double *out)
+                      const double *expo_mean, double *out, const GRange *rg = nullptr)
 {
   const int npar = c->snp + c->snm;
   for (int k = 0; k < n; k++) {
     if (param[k] < 0 || param[k] >= npar) return c->fail(IMA_ERR_ARG, "point %d: parameter %d out of range", k, param[k]);
-    if (!(x[k] > 0.0)) return c->fail(IMA_ERR_ARG, "point %d: x must be > 0", k);
+    if (!(x[k] > 0.0) && !(rg && x[k] >= 0.0)) return c->fail(IMA_ERR_ARG, "point %d: x must be > 0", k);
   }
   if (expo_mean)
     for (int i = 0; i < c->snm; i++)
       if (!(expo_mean[i] > 0.0)) return c->fail(IMA_ERR_ARG, "exponential prior mean %d must be > 0", i);
-  const int nchunks = margin_chunks(c->sG, n);
+  const int nchunks = margin_chunks(rg ? rg->hi - rg->lo : c->sG, n);
   // one device block: param | x | means | out | partials
   const size_t bytes = 256 * 5 + (size_t)n * 4 + (size_t)n * 8 + 64 * 8 + (size_t)n * 8 + (size_t)n * nchunks * 8;
   if (bytes > c->mscratch_cap) {
@@ -1648,8 +1655,12 @@ static int margin_run(ima_ctx *c, int n, const int32_t *param, const double *x, 
   double *d_mean = reinterpret_cast<double *>(take(64 * 8));
   double *d_out = reinterpret_cast<double *>(take((size_t)n * 8));
   double *d_part = reinterpret_cast<double *>(take((size_t)n * nchunks * 8));
-  MarginArgs a;
+  MarginArgs a{};
   a.G = c->sG;
+  a.g_lo = rg ? rg->lo : 0;
+  a.g_hi = rg ? rg->hi : c->sG;
+  a.div = rg ? rg->div : c->sG;
+  a.raw_cc = rg ? rg->raw_cc : 0;
   a.rowlen = c->srowlen;
   a.np = c->snp;
   a.nm = c->snm;
@@ -1686,12 +1697,12 @@ constexpr double EXPOMIGPLOTSCALE = 20;  // the 2NM plot scale in prior means (i
 // calc_popmig / calc_pop_expomig at n points (term k: thetai[k], mi[k], x[k])
 static int popmig_run(ima_ctx *c, int n, const int32_t *thetai, const int32_t *mi, const double *x,
                       const double *theta_max, const double *mig_max, const double *mig_mean, int prob_or_like,
-                      double *out)
+                      double *out, const GRange *rg = nullptr)
 {
   for (int k = 0; k < n; k++) {
     if (thetai[k] < 0 || thetai[k] >= c->snp || mi[k] < 0 || mi[k] >= c->snm)
       return c->fail(IMA_ERR_ARG, "point %d: term (%d, %d) out of range", k, thetai[k], mi[k]);
-    if (!(x[k] > 0.0)) return c->fail(IMA_ERR_ARG, "point %d: x must be > 0", k);
+    if (!(x[k] > 0.0) && !(rg && x[k] >= 0.0)) return c->fail(IMA_ERR_ARG, "point %d: x must be > 0", k);
   }
   for (int i = 0; i < c->snp; i++)
     if (!(theta_max[i] > 0.0)) return c->fail(IMA_ERR_ARG, "theta prior maximum %d must be > 0", i);
@@ -1700,7 +1711,7 @@ static int popmig_run(ima_ctx *c, int n, const int32_t *thetai, const int32_t *m
     if (mig_mean && !(mig_mean[i] > 0.0)) return c->fail(IMA_ERR_ARG, "exponential prior mean %d must be > 0", i);
   }
   if (int r0 = ensure_logfact(c)) return r0;
-  const int nchunks = popmig_chunks(c->sG, n);
+  const int nchunks = popmig_chunks(rg ? rg->hi - rg->lo : c->sG, n);
   std::vector<double> hq(n), hm(n), hmean(mig_mean ? n : 0);
   for (int k = 0; k < n; k++) {
     hq[k] = theta_max[thetai[k]];
@@ -1735,6 +1746,9 @@ static int popmig_run(ima_ctx *c, int n, const int32_t *thetai, const int32_t *m
   double *d_part = reinterpret_cast<double *>(take((size_t)n * nchunks * 16));
   PopmigArgs a{};
   a.G = c->sG;
+  a.g_lo = rg ? rg->lo : 0;
+  a.g_hi = rg ? rg->hi : c->sG;
+  a.div = rg ? rg->div : c->sG;
   a.rowlen = c->srowlen;
   a.n = n;
   a.expo = mig_mean ? 1 : 0;
@@ -1858,6 +1872,97 @@ extern "C" int ima_gpu_popmig_curves(ima_ctx *c, int nterms, const int32_t *thet
   if (r) return r;
   memcpy(x_out, x.data(), npts * 8);
   return IMA_OK;
+}
+
+extern "C" int ima_gpu_findmarginpeaks(ima_ctx *c, const double *theta_min, const double *theta_max,
+                                       const double *mig_min, const double *mig_max, const double *mig_mean,
+                                       int nterms, const int32_t *mpop, const int32_t *mterm, double *mlval,
+                                       double *peakloc, double *migtest, double *lo95, double *hi95,
+                                       double *pm_mlval, double *pm_peakloc, double *pm_test, float *holdpeakloc,
+                                       int *rounds)
+{
+  if (!c || !theta_min || !theta_max || !mlval || !peakloc || !lo95 || !hi95 || !holdpeakloc) return IMA_ERR_ARG;
+  if (!c->d_rows) return c->fail(IMA_ERR_STATE, "call ima_gpu_surface_load first");
+  const int np = c->snp, nm = c->snm;
+  if (nm > 0 && (!mig_min || !mig_max || !migtest)) return IMA_ERR_ARG;
+  if (nterms < 0 || (nterms > 0 && (!mpop || !mterm || !pm_mlval || !pm_peakloc || !pm_test))) return IMA_ERR_ARG;
+  for (int t = 0; t < nterms; t++)
+    if (mpop[t] < 0 || mpop[t] >= np || mterm[t] < 0 || mterm[t] >= nm)
+      return c->fail(IMA_ERR_ARG, "2NM term %d: (%d, %d) out of range", t, mpop[t], mterm[t]);
+  for (int i = 0; i < np; i++)
+    if (!(theta_max[i] > 0.0)) return c->fail(IMA_ERR_ARG, "theta prior maximum %d must be > 0", i);
+  for (int i = 0; i < nm; i++) {
+    if (!(mig_max[i] > 0.0)) return c->fail(IMA_ERR_ARG, "migration prior maximum %d must be > 0", i);
+    if (mig_mean && !(mig_mean[i] > 0.0)) return c->fail(IMA_ERR_ARG, "exponential prior mean %d must be > 0", i);
+  }
+  cudaSetDevice(c->device);
+  MarginPeaksIn in;
+  in.G = c->sG;
+  in.np = np;
+  in.nm = nm;
+  in.nterms = nterms;
+  in.theta_min = theta_min;
+  in.theta_max = theta_max;
+  in.mig_min = mig_min;
+  in.mig_max = mig_max;
+  in.mig_mean = mig_mean;
+  in.mpop = mpop;
+  in.mterm = mterm;
+  MarginPeaksOut out;
+  out.mlval = mlval;
+  out.peakloc = peakloc;
+  out.migtest = migtest;
+  out.lo95 = lo95;
+  out.hi95 = hi95;
+  out.pm_mlval = pm_mlval;
+  out.pm_peakloc = pm_peakloc;
+  out.pm_test = pm_test;
+  out.holdpeakloc = holdpeakloc;
+  // one batched launch per (kind, genealogy range) of a round
+  MarginPeaksEval eval = [&](const std::vector<MarginPeaksReq> &reqs, std::vector<double> &v) -> int {
+    std::vector<char> used(reqs.size(), 0);
+    for (size_t k0 = 0; k0 < reqs.size(); k0++) {
+      if (used[k0]) continue;
+      const MarginPeaksReq &q0 = reqs[k0];
+      std::vector<size_t> grp;
+      for (size_t k = k0; k < reqs.size(); k++)
+        if (!used[k] && reqs[k].kind == q0.kind && reqs[k].lo == q0.lo && reqs[k].hi == q0.hi) {
+          used[k] = 1;
+          grp.push_back(k);
+        }
+      const int n = (int)grp.size();
+      std::vector<int32_t> idx(n), th(n), mi(n);
+      std::vector<double> x(n), y(n);
+      for (int k = 0; k < n; k++) {
+        idx[k] = reqs[grp[k]].idx;
+        x[k] = reqs[grp[k]].x;
+      }
+      GRange rg;
+      rg.lo = q0.lo;
+      rg.hi = q0.hi;
+      rg.div = (double)(q0.hi - q0.lo + (q0.lo == 0));
+      rg.raw_cc = q0.kind == 0;
+      int r;
+      if (q0.kind >= 2) {
+        for (int k = 0; k < n; k++) {
+          th[k] = mpop[idx[k]];
+          mi[k] = mterm[idx[k]];
+        }
+        r = popmig_run(c, n, th.data(), mi.data(), x.data(), theta_max, mig_max, q0.kind == 2 ? mig_mean : nullptr,
+                       0, y.data(), &rg);
+      } else {
+        if (q0.kind == 1) rg.div = (double)(q0.hi - q0.lo);  // margincalc divides by the count
+        r = margin_run(c, n, idx.data(), x.data(), 0.0, q0.kind == 1, mig_mean, y.data(), &rg);
+      }
+      if (r) return r;
+      for (int k = 0; k < n; k++) v[grp[k]] = y[k];
+    }
+    return IMA_OK;
+  };
+  const int r = findmarginpeaks_run(in, eval, out);
+  if (rounds) *rounds = out.rounds;
+  if (r == -1) return c->fail(IMA_ERR_DATA, "a peak search did not end in 20000 rounds");
+  return r;
 }
 
 extern "C" int ima_gpu_margincalc(ima_ctx *c, int n, const int32_t *param, const double *x, double yadjust, int logi,

@@ -3,6 +3,8 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <functional>
+#include <vector>
 
 #include "../../include/ima_gpu.h"
 
@@ -132,6 +134,9 @@ size_t surface_fp64_scratch_bytes(int G, int npoints);
 // 1-D marginal densities (margincalc)
 struct MarginArgs {
   int G, rowlen, np, nm, n, logi;
+  int g_lo, g_hi;           // genealogies [g_lo, g_hi) are summed
+  int raw_cc;               // marginp: the theta term takes cc as stored, not rounded
+  double div;               // the sum is divided by this (G for margincalc)
   int ccp, fcp, hccp, mcp, fmp, qip, mip;  // gsampinf column offsets
   const float *rows;        // [G][rowlen]
   const int32_t *param;     // [n] parameter index (population sizes first)
@@ -145,6 +150,8 @@ int launch_margin(const MarginArgs &a, double *part, int nchunks, double *out, c
 // 2NM densities (calc_popmig / calc_pop_expomig) at n requested points
 struct PopmigArgs {
   int G, rowlen, n, expo, prob_or_like;
+  int g_lo, g_hi;                          // genealogies [g_lo, g_hi) are summed
+  double div;                              // the sum is divided by this (G for calc_popmig)
   int ccp, fcp, hccp, mcp, fmp, qip, mip;  // gsampinf column offsets
   const float *rows;                       // [G][rowlen]
   const int32_t *thetai, *mi;              // [n] parameter indices of each point's term
@@ -154,6 +161,36 @@ struct PopmigArgs {
 };
 int popmig_chunks(int G, int n);
 int launch_popmig(const PopmigArgs &a, double *part, int nchunks, double *out, cudaStream_t st);
+
+// findmarginpeaks' numeric core (margin_peaks.cu, host): the searches run
+// together, their function values evaluated in batches by `eval`
+struct MarginPeaksIn {
+  int G, np, nm, nterms;
+  const double *theta_min, *theta_max, *mig_min, *mig_max;
+  const double *mig_mean;      // null: uniform migration priors
+  const int32_t *mpop, *mterm; // [nterms] the 2NM terms
+};
+struct MarginPeaksOut {
+  int too_few = 0, rounds = 0;
+  double *mlval, *peakloc;       // [NUMTREEINT + 1 = 3][np+nm]
+  double *migtest;               // [nm]
+  double *lo95, *hi95;           // [np+nm]
+  double *pm_mlval, *pm_peakloc; // [3][nterms]
+  double *pm_test;               // [nterms]
+  float *holdpeakloc;            // [np+nm]
+};
+// kind 0: marginp's density (cc as stored) of parameter idx; 1: margincalc's
+// log density (cc rounded); 2: the 2NM density of term idx under the run's
+// migration prior; 3: the same under the uniform prior (marginpopmig);
+// summed over genealogies [lo, hi), divided by hi - lo + (lo == 0)
+// (margincalc: by hi - lo)
+struct MarginPeaksReq {
+  int kind, idx, lo, hi;
+  double x;
+};
+using MarginPeaksEval = std::function<int(const std::vector<MarginPeaksReq> &, std::vector<double> &)>;
+// returns 0, eval's error, or -1 when a search runs past 20000 rounds
+int findmarginpeaks_run(const MarginPeaksIn &in, const MarginPeaksEval &eval, MarginPeaksOut &out);
 
 // genealogy weights (treeweight) and p(G) integrals (initialize_integrate_tree_prob)
 #define TW_MAXPOPS 10                      // MAXPOPS, imamp.hpp:122

@@ -7,6 +7,9 @@
 //                       (+ ln(1/mean) - x / mean under an exponential prior)
 // summed in FP64 without a shift, as the reference sums it (the values span
 // hundreds of orders of magnitude and the reference returns them as they are).
+// marginp (surface_call_functions.cpp:25-80), the peak searches' form, sums a
+// range of genealogies, takes the theta term's cc as stored and divides by
+// the range's length (+1 when it starts at genealogy 0).
 //
 // One thread per requested (parameter, x) and genealogy chunk; tiles of whole
 // gsampinf rows are staged in shared memory with coalesced loads, and every
@@ -53,7 +56,7 @@ __global__ void __launch_bounds__(MG_BS) k_margin(MarginArgs a, int chunk, doubl
     const int p = pi - a.np;
     c0 = a.mip + p; c1 = a.mcp + p; c2 = a.fmp + p; c3 = c2;
   }
-  const int g0 = blockIdx.y * chunk, g1 = min(a.G, g0 + chunk);
+  const int g0 = a.g_lo + blockIdx.y * chunk, g1 = min(a.g_hi, g0 + chunk);
   double sum = 0.0;
   for (int t0 = g0; t0 < g1; t0 += MG_TG) {
     const int nt = min(MG_TG, g1 - t0);
@@ -66,7 +69,8 @@ __global__ void __launch_bounds__(MG_BS) k_margin(MarginArgs a, int chunk, doubl
       const float *r = tile + j * a.rowlen;
       double temp;
       if (theta)
-        temp = -(double)r[c0] + intround(r[c1]) * lx - (double)r[c2] - 2.0 * (double)r[c3] * ix;
+        temp = -(double)r[c0] + (a.raw_cc ? (double)r[c1] : intround(r[c1])) * lx - (double)r[c2] -
+               2.0 * (double)r[c3] * ix;
       else
         temp = -(double)r[c0] + cst - x * slope + intround(r[c1]) * lx - (double)r[c2] * x;
       sum += exp(temp);
@@ -81,7 +85,7 @@ __global__ void k_margin_merge(MarginArgs a, int nchunks, const double *part, do
   if (k >= a.n) return;
   double s = 0.0;
   for (int c = 0; c < nchunks; c++) s += part[(size_t)k * nchunks + c];
-  s /= a.G;
+  s /= a.div;
   if (a.logi) s = (s <= 0.0) ? -1e200 : log(s);  // LOWLOG
   out[k] = s - a.yadjust;
 }
@@ -100,8 +104,10 @@ int margin_chunks(int G, int n)
 int launch_margin(const MarginArgs &a, double *part, int nchunks, double *out, cudaStream_t st)
 {
   if (a.rowlen > MG_MAXROW || a.n < 1) return 2;
-  const int chunk = ((a.G + nchunks - 1) / nchunks + MG_TG - 1) / MG_TG * MG_TG;
-  nchunks = (a.G + chunk - 1) / chunk;
+  const int ng = a.g_hi - a.g_lo;
+  if (ng < 1) return 2;
+  const int chunk = ((ng + nchunks - 1) / nchunks + MG_TG - 1) / MG_TG * MG_TG;
+  nchunks = (ng + chunk - 1) / chunk;
   k_margin<<<dim3((a.n + MG_BS - 1) / MG_BS, nchunks), MG_BS, 0, st>>>(a, chunk, part);
   k_margin_merge<<<(a.n + 127) / 128, 128, 0, st>>>(a, nchunks, part, out);
   return 0;

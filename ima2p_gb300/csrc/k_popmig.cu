@@ -18,7 +18,9 @@
 // calc_pop_expomig's eexp mantissa / decimal-exponent terms are kept per
 // chunk rescaled to the chunk's largest exponent.  The merge kernel adds the
 // chunks in chunk order, rescales them to the overall largest exponent, and
-// divides by G and, for likelihoods, by the prior density of 2NM.
+// divides by G and, for likelihoods, by the prior density of 2NM.  The peak
+// search's forms (marginpopmig, marginpop_expomig; :181-351) sum a range of
+// genealogies and divide by its length (+1 when it starts at genealogy 0).
 //
 // The terms are written with the reference's operation order and this file
 // is compiled with -fmad=false; log, exp and pow are the device's.
@@ -100,7 +102,7 @@ __global__ void __launch_bounds__(PM_BS) k_popmig(PopmigArgs a, int chunk, doubl
   IgBase ig{a.logfact, 0};
   double sum = 0.0;        // calc_popmig: sum of exp; expo: sum of m 10^(z - (maxz - OCUTOFF))
   int maxz = -1000000000;  // expo: the chunk's largest decimal exponent
-  const int g0 = blockIdx.y * chunk, g1 = min(a.G, g0 + chunk);
+  const int g0 = a.g_lo + blockIdx.y * chunk, g1 = min(a.g_hi, g0 + chunk);
   for (int g = g0; g < g1; g++) {
     const size_t o = (size_t)g * a.rowlen;
     const int cc = (int)__ldg(c_cc + o), mc = (int)__ldg(c_mc + o);
@@ -136,7 +138,7 @@ __global__ void k_popmig_merge(PopmigArgs a, int nchunks, const double *part, do
   double sum = 0.0;
   if (!a.expo) {
     for (int c = 0; c < nchunks; c++) sum += w[2 * c];
-    sum /= a.G;
+    sum /= a.div;
     if (a.prob_or_like) {
       const double temp = 2 * (log(qmax) + log(mmax) - log(2 * x)) / (qmax * mmax);
       sum /= temp;
@@ -149,7 +151,7 @@ __global__ void k_popmig_merge(PopmigArgs a, int nchunks, const double *part, do
     for (int c = 0; c < nchunks; c++)
       if (w[2 * c] != 0.0) acumm += w[2 * c] * pow(10.0, (double)((int)w[2 * c + 1] - maxz));
     sum = log(acumm) + (maxz - OCUTOFF) * LOG10;
-    sum -= log((double)a.G);
+    sum -= log(a.div);
     sum = exp(sum);
     if (a.prob_or_like) {
       IgBase ig{a.logfact, 0};
@@ -177,9 +179,10 @@ int popmig_chunks(int G, int n)
 
 int launch_popmig(const PopmigArgs &a, double *part, int nchunks, double *out, cudaStream_t st)
 {
-  if (a.n < 1 || a.G < 1) return 2;
-  const int chunk = (a.G + nchunks - 1) / nchunks;
-  nchunks = (a.G + chunk - 1) / chunk;
+  const int ng = a.g_hi - a.g_lo;
+  if (a.n < 1 || ng < 1) return 2;
+  const int chunk = (ng + nchunks - 1) / nchunks;
+  nchunks = (ng + chunk - 1) / chunk;
   k_popmig<<<dim3((a.n + PM_BS - 1) / PM_BS, nchunks), PM_BS, 0, st>>>(a, chunk, part);
   k_popmig_merge<<<(a.n + 127) / 128, 128, 0, st>>>(a, nchunks, part, out);
   return 0;

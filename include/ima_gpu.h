@@ -271,6 +271,37 @@ int ima_gpu_popmig(ima_ctx *ctx, int n, const int32_t *thetai, const int32_t *mi
 int ima_gpu_popmig_curves(ima_ctx *ctx, int nterms, const int32_t *thetai, const int32_t *mi, int gridsize,
                           const double *theta_max, const double *mig_max, const double *mig_mean,
                           int prob_or_like, double *x_out, double *y_out, double *maxx);
+/* The numbers of findmarginpeaks (surface_call_functions.cpp:316-734) over
+ * the loaded genealogies, G clamped to MAXGENEALOGIESTOSAVE - 1 as there:
+ *   mlval, peakloc [3][np+nm]: marginalopt (:178-266) of every parameter
+ *     over the first half of the genealogies, the second (starting one past
+ *     the first's end, as the reference steps), and all of them; the peak
+ *     of marginp's density (:25-80: cc as stored, the genealogy range's
+ *     length + 1 when it starts at 0) by two mnbrakmod brackets and
+ *     goldenmod (surface_search_functions.cpp:42-200); peakloc -1 (mlval
+ *     NaN) where the brackets do not overlap;
+ *   migtest [nm]: 2 log(density at the peak / density at MINPARAMVAL);
+ *   lo95, hi95 [np+nm]: margin95 (:268-292), bisection (marginbis, 40
+ *     steps, tolerance 1e-4) of margincalc's log density 1.92 below the
+ *     peak; DBL_MIN where no crossing, DBL_MAX where the bisection did not
+ *     end; NaN for parameters without a peak;
+ *   pm_mlval, pm_peakloc [3][nterms], pm_test [nterms]: the same for the
+ *     2NM terms (mpop[t], mterm[t]) -- marginalopt_popmig (popmig.cpp:361-428,
+ *     a 100-point scan then goldenmod on marginpopmig / marginpop_expomig)
+ *     and its test; nterms = 0 skips them (POPMIGPARAMHIST off);
+ *   holdpeakloc [np+nm]: the all-genealogy peaks (MINPARAMVAL where none),
+ *     -1 everywhere when 10 or fewer genealogies are loaded.
+ * theta_min/max, mig_min/max: the priors (itheta[].pr, imig[].pr);
+ * mig_mean: NULL, or the exponential priors' means (EXPOMIGRATIONPRIOR).
+ * Every search follows the reference's sequence of points given its values;
+ * the searches of all parameters, terms and genealogy ranges advance
+ * together, each round's points evaluated in one batched launch per kind
+ * of density and range.  *rounds (may be NULL): the number of rounds. */
+int ima_gpu_findmarginpeaks(ima_ctx *ctx, const double *theta_min, const double *theta_max,
+                            const double *mig_min, const double *mig_max, const double *mig_mean,
+                            int nterms, const int32_t *mpop, const int32_t *mterm, double *mlval,
+                            double *peakloc, double *migtest, double *lo95, double *hi95, double *pm_mlval,
+                            double *pm_peakloc, double *pm_test, float *holdpeakloc, int *rounds);
 /* The loaded surface's shape (any pointer may be NULL). */
 int ima_gpu_surface_info(ima_ctx *ctx, int *G, int *numpopsizeparams, int *nummigrateparams, int *npops);
 

@@ -1360,42 +1360,104 @@ static void popmig_cols(int np, int nm, int thetai, int mi, int *c)
   c[4] = fmp + mi; c[5] = qip + thetai; c[6] = mip + mi;
 }
 
+/* calc_popmig's term of one genealogy (popmig.cpp:33-84): temp1 + temp2 */
+static double pm_term(const float *r, const int *c, double x, double qmax, double mmax, int *st)
+{
+  int cc = (int)r[c[0]], mc = (int)r[c[3]];
+  double fc = r[c[1]], hc = r[c[2]], fm = r[c[4]], qintg = r[c[5]], mintg = r[c[6]];
+  double temp1, temp2;
+  if (fc == 0 && cc == 0 && fm > 0) {
+    temp1 = ORA_LOG2 - (mc * log(fm)) - hc - qintg - mintg;
+    temp2 = log(exp(ig_upper(mc, 2 * fm * x / qmax, st)) - exp(ig_upper(mc, mmax * fm, st)));
+  } else if (fm == 0 && mc == 0 && fc > 0) {
+    temp1 = ORA_LOG2 - (cc * log(fc)) - hc - qintg - mintg;
+    temp2 = log(exp(ig_upper(cc, 2 * fc / qmax, st)) - exp(ig_upper(cc, fc * mmax / x, st)));
+  } else if (fc == 0 && cc == 0 && mc == 0 && fm == 0) {
+    temp1 = log(2 * log(mmax * qmax / (2 * x))) - hc - qintg - mintg;
+    temp2 = 0;
+  } else {
+    temp1 = ORA_LOG2 + (mc * log(x)) - ((cc + mc) * log(fc + fm * x)) - hc - qintg - mintg;
+    double a = ig_upper(cc + mc, 2 * (fc + fm * x) / qmax, st);
+    double b = ig_upper(cc + mc, mmax * (fm + fc / x), st);
+    if (a == b) {
+      b = ig_lower(cc + mc, 2 * (fc + fm * x) / qmax, st);
+      a = ig_lower(cc + mc, mmax * (fm + fc / x), st);
+    }
+    if (a > b) {
+      temp2 = ld(a, b, st);
+    } else {
+      temp1 = temp2 = 0.0;
+    }
+  }
+  return temp1 + temp2;
+}
+
+/* calc_pop_expomig's log term of one genealogy (popmig.cpp:114-147) */
+static double pe_term(const float *r, const int *c, double x, double qmax, double mmean, int *st)
+{
+  int cc = (int)r[c[0]], mc = (int)r[c[3]];
+  double fc = r[c[1]], hc = r[c[2]], fm = r[c[4]], qintg = r[c[5]], mintg = r[c[6]];
+  double temp1 = x + fc * mmean + fm * mmean * x;
+  double temp2 = ORA_LOG2 - hc - log(mmean) - qintg - mintg;
+  double temp3 = 2 * temp1 / (mmean * qmax);
+  if (mc == 0 && cc == 0) {
+    temp3 = ig_upper(0, temp3, st);
+    temp2 += temp3;
+  } else if (cc == 0) {
+    temp3 = ig_upper(mc, temp3, st);
+    temp2 += temp3 - mc * log(fm + 1 / mmean);
+  } else if (mc == 0) {
+    temp3 = ig_upper(cc, temp3, st);
+    temp2 += temp3 + -cc * log(fc + x * (fm + 1 / mmean));
+  } else {
+    temp3 = ig_upper(mc + cc, temp3, st);
+    temp2 += temp3 - cc * log(x) + (cc + mc) * log(mmean * x / temp1);
+  }
+  return temp2;
+}
+
+/* sum over genealogies [ft, lt) of exp(term) (terms outside +-700 skipped) */
+static double pm_sum(const float *g, int rowlen, const int *c, int ft, int lt, double x, double qmax, double mmax,
+                     int *st)
+{
+  double sum = 0.0;
+  for (int e = ft; e < lt; e++) {
+    double t = pm_term(g + (size_t)e * rowlen, c, x, qmax, mmax, st);
+    if ((t < 700) && (t > -700)) sum += exp(t);
+  }
+  return sum;
+}
+
+/* log of the eexp-rescaled sum over genealogies [ft, lt) (popmig.cpp:148-160) */
+static double pe_logsum(const float *g, int rowlen, const int *c, int ft, int lt, double x, double qmax,
+                        double mmean, int *st)
+{
+  int n = lt - ft;
+  double *mm = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+  int *zz = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+  if (!mm || !zz) { free(mm); free(zz); *st = 3; return 0.0; }
+  int maxz = -1000000000;
+  for (int e = 0; e < n; e++) {
+    ora_eexp(pe_term(g + (size_t)(ft + e) * rowlen, c, x, qmax, mmean, st), &mm[e], &zz[e]);
+    if (zz[e] > maxz) maxz = zz[e];
+  }
+  double acumm = 0.0;
+  for (int e = 0; e < n; e++) {
+    int zadj = zz[e] - (maxz - 10);
+    mm[e] *= pow(10.0, (double)zadj);
+    acumm += mm[e];
+  }
+  free(mm);
+  free(zz);
+  return log(acumm) + (maxz - 10) * ORA_LOG10;
+}
+
 double ora_popmig(int G, int rowlen, const float *g, int np, int nm, int thetai, int mi, double x,
                   double qmax, double mmax, int prob_or_like, int *st)
 {
   int c[7];
   popmig_cols(np, nm, thetai, mi, c);
-  double sum = 0.0;
-  for (int e = 0; e < G; e++) {
-    const float *r = g + (size_t)e * rowlen;
-    int cc = (int)r[c[0]], mc = (int)r[c[3]];
-    double fc = r[c[1]], hc = r[c[2]], fm = r[c[4]], qintg = r[c[5]], mintg = r[c[6]];
-    double temp1, temp2;
-    if (fc == 0 && cc == 0 && fm > 0) {
-      temp1 = ORA_LOG2 - (mc * log(fm)) - hc - qintg - mintg;
-      temp2 = log(exp(ig_upper(mc, 2 * fm * x / qmax, st)) - exp(ig_upper(mc, mmax * fm, st)));
-    } else if (fm == 0 && mc == 0 && fc > 0) {
-      temp1 = ORA_LOG2 - (cc * log(fc)) - hc - qintg - mintg;
-      temp2 = log(exp(ig_upper(cc, 2 * fc / qmax, st)) - exp(ig_upper(cc, fc * mmax / x, st)));
-    } else if (fc == 0 && cc == 0 && mc == 0 && fm == 0) {
-      temp1 = log(2 * log(mmax * qmax / (2 * x))) - hc - qintg - mintg;
-      temp2 = 0;
-    } else {
-      temp1 = ORA_LOG2 + (mc * log(x)) - ((cc + mc) * log(fc + fm * x)) - hc - qintg - mintg;
-      double a = ig_upper(cc + mc, 2 * (fc + fm * x) / qmax, st);
-      double b = ig_upper(cc + mc, mmax * (fm + fc / x), st);
-      if (a == b) {
-        b = ig_lower(cc + mc, 2 * (fc + fm * x) / qmax, st);
-        a = ig_lower(cc + mc, mmax * (fm + fc / x), st);
-      }
-      if (a > b) {
-        temp2 = ld(a, b, st);
-      } else {
-        temp1 = temp2 = 0.0;
-      }
-    }
-    if ((temp1 + temp2 < 700) && (temp1 + temp2 > -700)) sum += exp(temp1 + temp2);
-  }
+  double sum = pm_sum(g, rowlen, c, 0, G, x, qmax, mmax, st);
   sum /= G;
   if (prob_or_like) {
     double temp = 2 * (log(qmax) + log(mmax) - log(2 * x)) / (qmax * mmax);
@@ -1409,42 +1471,7 @@ double ora_pop_expomig(int G, int rowlen, const float *g, int np, int nm, int th
 {
   int c[7];
   popmig_cols(np, nm, thetai, mi, c);
-  double *mm = (double *)malloc(sizeof(double) * (size_t)(G > 0 ? G : 1));
-  int *zz = (int *)malloc(sizeof(int) * (size_t)(G > 0 ? G : 1));
-  if (!mm || !zz) { free(mm); free(zz); *st = 3; return 0.0; }
-  int maxz = -1000000000;
-  for (int e = 0; e < G; e++) {
-    const float *r = g + (size_t)e * rowlen;
-    int cc = (int)r[c[0]], mc = (int)r[c[3]];
-    double fc = r[c[1]], hc = r[c[2]], fm = r[c[4]], qintg = r[c[5]], mintg = r[c[6]];
-    double temp1 = x + fc * mmean + fm * mmean * x;
-    double temp2 = ORA_LOG2 - hc - log(mmean) - qintg - mintg;
-    double temp3 = 2 * temp1 / (mmean * qmax);
-    if (mc == 0 && cc == 0) {
-      temp3 = ig_upper(0, temp3, st);
-      temp2 += temp3;
-    } else if (cc == 0) {
-      temp3 = ig_upper(mc, temp3, st);
-      temp2 += temp3 - mc * log(fm + 1 / mmean);
-    } else if (mc == 0) {
-      temp3 = ig_upper(cc, temp3, st);
-      temp2 += temp3 + -cc * log(fc + x * (fm + 1 / mmean));
-    } else {
-      temp3 = ig_upper(mc + cc, temp3, st);
-      temp2 += temp3 - cc * log(x) + (cc + mc) * log(mmean * x / temp1);
-    }
-    ora_eexp(temp2, &mm[e], &zz[e]);
-    if (zz[e] > maxz) maxz = zz[e];
-  }
-  double acumm = 0.0;
-  for (int e = 0; e < G; e++) {
-    int zadj = zz[e] - (maxz - 10);
-    mm[e] *= pow(10.0, (double)zadj);
-    acumm += mm[e];
-  }
-  free(mm);
-  free(zz);
-  double sum = log(acumm) + (maxz - 10) * ORA_LOG10;
+  double sum = pe_logsum(g, rowlen, c, 0, G, x, qmax, mmean, st);
   sum -= log((double)G);
   sum = exp(sum);
   if (prob_or_like) {
@@ -1452,4 +1479,274 @@ double ora_pop_expomig(int G, int rowlen, const float *g, int np, int nm, int th
     sum /= temp;
   }
   return sum;
+}
+
+/* ======================================================================
+ * findmarginpeaks' numbers (surface_call_functions.cpp:316-734).  marginp
+ * (:25-80) is margincalc's density over genealogies [ft, lt) with cc as
+ * stored, divided by lt - ft + (ft == 0), negated, and OFFSCALEVAL (1)
+ * outside the prior; marginpopmig / marginpop_expomig (popmig.cpp:181-351)
+ * the same for 2NM.  The searches: mnbrakmod and goldenmod
+ * (surface_search_functions.cpp:42-200), marginalopt (:178-266),
+ * marginbis / margin95 (:86-113, :268-292), marginalopt_popmig
+ * (popmig.cpp:361-428).
+ * ==================================================================== */
+#define PK_MINPARAMVAL 0.0000001
+typedef struct {
+  int G, rowlen, np, nm, expo, uniform2nm, kind, idx, ft, lt;
+  const float *g;
+  const double *thmin, *thmax, *mgmin, *mgmax, *mgmean;
+  const int *mpop, *mterm;
+  double yadjust;
+  int st;
+} PkCtx;
+
+static double pk_marginp(PkCtx *k, double x)
+{
+  int p = k->idx, np = k->np, ccp, fcp, hccp, mcp, fmp, qip, mip, pdgp, probgp;
+  double max = p < np ? k->thmax[p] : k->mgmax[p - np], min = p < np ? k->thmin[p] : k->mgmin[p - np];
+  if (x < min || x > max) return 1;
+  ora_gsamp_offsets(np, k->nm, &ccp, &fcp, &hccp, &mcp, &fmp, &qip, &mip, &pdgp, &probgp);
+  double meani = (k->expo && p >= np) ? 1.0 / k->mgmean[p - np] : 0.0, sumtemp = 0.0;
+  for (int e = k->ft; e < k->lt; e++) {
+    const float *r = k->g + (size_t)e * k->rowlen;
+    double temp;
+    if (p < np) {
+      temp = -r[qip + p] + r[ccp + p] * (ORA_LOG2 - log(x)) - r[hccp + p] - 2 * r[fcp + p] / x;
+    } else {
+      int q = p - np;
+      if (k->expo)
+        temp = -r[mip + q] + log(meani) - x * meani + ora_intround(r[mcp + q]) * log(x) - r[fmp + q] * x;
+      else
+        temp = -r[mip + q] + ora_intround(r[mcp + q]) * log(x) - r[fmp + q] * x;
+    }
+    sumtemp += exp(temp);
+  }
+  sumtemp /= (k->lt - k->ft + (k->ft == 0));
+  return -sumtemp;
+}
+
+static double pk_marginpopmig(PkCtx *k, double x)
+{
+  int t = k->idx, th = k->mpop[t], mi = k->mterm[t], c[7];
+  int expo = k->expo && !k->uniform2nm;
+  double qmax = k->thmax[th], max = expo ? 20.0 * k->mgmean[mi] : qmax * k->mgmax[mi] / 2.0;
+  if (x < 0 || x > max) return 1.0;
+  popmig_cols(k->np, k->nm, th, mi, c);
+  if (!expo) {
+    double sum = pm_sum(k->g, k->rowlen, c, k->ft, k->lt, x, qmax, k->mgmax[mi], &k->st);
+    sum /= (k->lt - k->ft + (k->ft == 0));
+    return -sum;
+  }
+  double sum = pe_logsum(k->g, k->rowlen, c, k->ft, k->lt, x, qmax, k->mgmean[mi], &k->st);
+  sum -= log((double)k->lt - k->ft + (k->ft == 0));
+  return -exp(sum);
+}
+
+static double pk_f(PkCtx *k, double x)
+{
+  if (k->kind == 0) return pk_marginp(k, x);
+  if (k->kind == 1) return ora_margincalc(k->lt, k->rowlen, k->g, k->np, k->nm, k->idx, x, k->yadjust, 1,
+                                          k->expo ? k->mgmean : NULL);
+  return pk_marginpopmig(k, x);
+}
+
+static double pk_sign(double a, double b) { return b > 0.0 ? fabs(a) : -fabs(a); }
+
+static void pk_mnbrak(PkCtx *k, double *ax, double *bx, double *cx, double *fa, double *fb, double *fc)
+{
+  const double gold = 1.618034, glimit = 100.0, tiny = 1.0e-20;
+  double ulim, u, rr, q, fu, dum;
+  *fa = pk_f(k, *ax);
+  *fb = pk_f(k, *bx);
+  if (*fb > *fa) {
+    dum = *ax; *ax = *bx; *bx = dum;
+    dum = *fb; *fb = *fa; *fa = dum;
+  }
+  *cx = fabs(*bx + gold * (*bx - *ax));
+  *fc = pk_f(k, *cx);
+  while (*fb >= *fc && *fb > -DBL_MAX && !(*fb == 0 && *fc == 0)) {
+    rr = (*bx - *ax) * (*fb - *fc);
+    q = (*bx - *cx) * (*fb - *fa);
+    float m1 = (float)fabs(q - rr), m2 = (float)tiny; /* FMAX's float variables */
+    u = (double)*bx - ((*bx - *cx) * q - (*bx - *ax) * rr) / (2.0 * pk_sign(m1 > m2 ? m1 : m2, q - rr));
+    ulim = *bx + glimit * (*cx - *bx);
+    if ((*bx - u) * (u - *cx) > 0.0) {
+      fu = pk_f(k, u);
+      if (fu < *fc) { *ax = *bx; *fa = *fb; *bx = u; *fb = fu; continue; }
+      if (fu > *fb) { *cx = u; *fc = fu; continue; }
+      u = *cx + gold * (*cx - *bx);
+      fu = pk_f(k, u);
+    } else if ((*cx - u) * (u - ulim) > 0.0) {
+      fu = pk_f(k, u);
+      if (fu < *fc) {
+        *bx = *cx; *cx = u; u = *cx + gold * (*cx - *bx);
+        *fb = *fc; *fc = fu; fu = pk_f(k, u);
+      }
+    } else if ((u - ulim) * (ulim - *cx) >= 0.0) {
+      u = ulim;
+      fu = pk_f(k, u);
+    } else {
+      u = *cx + gold * (*cx - *bx);
+      fu = pk_f(k, u);
+    }
+    *ax = *bx; *bx = *cx; *cx = u;
+    *fa = *fb; *fb = *fc; *fc = fu;
+  }
+}
+
+static double pk_golden(PkCtx *k, double ax, double bx, double cx, double tol, double *xmin)
+{
+  const double r = 0.61803399, c = 1.0 - r;
+  double f1, f2, x0 = ax, x1, x2, x3 = cx;
+  if (fabs(cx - bx) > fabs(bx - ax)) { x1 = bx; x2 = bx + c * (cx - bx); }
+  else { x2 = bx; x1 = bx - c * (bx - ax); }
+  f1 = pk_f(k, x1);
+  f2 = pk_f(k, x2);
+  while (fabs(x3 - x0) > tol * (fabs(x1) + fabs(x2)) && (x3 > -DBL_MAX)) {
+    if (f2 < f1) {
+      x0 = x1; x1 = x2; x2 = r * x1 + c * x3; f1 = f2; f2 = pk_f(k, x2);
+      continue;
+    }
+    x3 = x2; x2 = x1; x1 = r * x2 + c * x0; f2 = f1; f1 = pk_f(k, x1);
+  }
+  if (f1 < f2) { *xmin = x1; return f1; }
+  *xmin = x2;
+  return f2;
+}
+
+static double pk_bis(PkCtx *k, double x1, double x2)
+{
+  double dx, f, fmid, xmid, rtb;
+  f = pk_f(k, x1);
+  fmid = pk_f(k, x2);
+  if (f * fmid >= 0.0) return DBL_MIN;
+  rtb = f < 0.0 ? (dx = x2 - x1, x1) : (dx = x1 - x2, x2);
+  for (int j = 1; j <= 40; j++) {
+    fmid = pk_f(k, xmid = rtb + (dx *= 0.5));
+    if (fmid <= 0.0) rtb = xmid;
+    if (fabs(dx) < 1e-4 || fmid == 0.0) return rtb;
+  }
+  return DBL_MAX;
+}
+
+static void pk_marginalopt(PkCtx *k, double *mlval, double *peakloc)
+{
+  int npar = k->np + k->nm;
+  double ax, bx, cx, fa, fb, fc, axt, bxt, cxt, prior, xmax;
+  double max0 = 0, min0 = 0, max1 = 0, min1 = 0; /* the reference leaves them unset */
+  k->kind = 0;
+  for (int i = 0; i < npar; i++) {
+    k->idx = i;
+    prior = i < k->np ? k->thmax[i] : k->mgmax[i - k->np];
+    ax = prior; bx = prior / 2;
+    pk_mnbrak(k, &ax, &bx, &cx, &fa, &fb, &fc);
+    axt = ax; bxt = bx; cxt = cx;
+    bx = prior / 2; ax = PK_MINPARAMVAL;
+    pk_mnbrak(k, &ax, &bx, &cx, &fa, &fb, &fc);
+    if (axt < bxt && axt < cxt) min0 = axt;
+    if (bxt < axt && bxt < cxt) min0 = bxt;
+    if (cxt < axt && cxt < bxt) min0 = cxt;
+    if (axt > bxt && axt > cxt) { if (axt > prior) axt = prior; max0 = axt; }
+    if (bxt > axt && bxt > cxt) { if (bxt > prior) bxt = prior; max0 = bxt; }
+    if (cxt > axt && cxt > bxt) { if (cxt > prior) cxt = prior; max0 = cxt; }
+    if (ax < bx && ax < cx) min1 = ax;
+    if (bx < ax && bx < cx) min1 = bx;
+    if (cx < ax && cx < bx) min1 = cx;
+    if (ax > bx && ax > cx) max1 = ax;
+    { if (ax > prior) ax = prior; max1 = ax; } /* unconditional, as in the reference */
+    if (bx > ax && bx > cx) { if (bx > prior) bx = prior; max1 = bx; }
+    if (cx > ax && cx > bx) { if (cx > prior) cx = prior; max1 = cx; }
+    if (max0 <= min1 || max1 <= min0) {
+      peakloc[i] = -1;
+      mlval[i] = NAN;
+    } else {
+      mlval[i] = -pk_golden(k, ax, bx, cx, 1e-7, &xmax);
+      peakloc[i] = xmax;
+    }
+  }
+}
+
+static void pk_marginalopt_popmig(PkCtx *k, int nt, double *mlval, double *peakloc)
+{
+  double ax, bx, cx, fa, xmax, ub, maxf;
+  int maxj;
+  k->kind = 2;
+  k->uniform2nm = 0;
+  for (int i = 0; i < nt; i++) {
+    k->idx = i;
+    ub = k->expo ? 20.0 * k->mgmean[k->mterm[i]] : k->thmax[k->mpop[i]] * k->mgmax[k->mterm[i]] / 2.0;
+    maxf = 1e100;
+    maxj = -1;
+    for (int j = 0; j < 100; j++) {
+      ax = PK_MINPARAMVAL + j * (ub / (double)100);
+      fa = pk_f(k, ax);
+      if (fa < maxf) { maxf = fa; maxj = j; }
+    }
+    if (maxj == 0) {
+      ax = PK_MINPARAMVAL; cx = PK_MINPARAMVAL + ub / (double)100; bx = (ax + cx) / 2.0;
+    } else if (maxj == 100 - 1) {
+      ax = PK_MINPARAMVAL + ((double)100 - 1) * (ub / (double)100);
+      bx = PK_MINPARAMVAL + ((double)100 - 2) * (ub / (double)100);
+      cx = ub;
+    } else {
+      bx = PK_MINPARAMVAL + ((double)maxj - 1) * (ub / (double)100);
+      cx = PK_MINPARAMVAL + ((double)maxj + 1) * (ub / (double)100);
+      ax = PK_MINPARAMVAL + ((double)maxj) * (ub / (double)100);
+    }
+    mlval[i] = -pk_golden(k, ax, bx, cx, 1e-7, &xmax);
+    peakloc[i] = xmax;
+  }
+}
+
+int ora_findmarginpeaks(int G, int rowlen, const float *g, int np, int nm, const double *thmin,
+                        const double *thmax, const double *mgmin, const double *mgmax, const double *mgmean,
+                        int nt, const int *mpop, const int *mterm, double *mlval, double *peakloc,
+                        double *migtest, double *lo95, double *hi95, double *pm_mlval, double *pm_peakloc,
+                        double *pm_test)
+{
+  PkCtx k;
+  memset(&k, 0, sizeof(k));
+  k.G = G; k.rowlen = rowlen; k.g = g; k.np = np; k.nm = nm; k.expo = mgmean != NULL;
+  k.thmin = thmin; k.thmax = thmax; k.mgmin = mgmin; k.mgmax = mgmax; k.mgmean = mgmean;
+  k.mpop = mpop; k.mterm = mterm;
+  int Gs = G < 300000 - 1 ? G : 300000 - 1, npar = np + nm, ft, lt, j;
+  if (Gs <= 10) return -1;
+  for (ft = 0, lt = Gs / 2, j = 0; j < 2; j++) {
+    k.ft = ft; k.lt = lt;
+    pk_marginalopt(&k, mlval + (size_t)j * npar, peakloc + (size_t)j * npar);
+    if (nt) pk_marginalopt_popmig(&k, nt, pm_mlval + (size_t)j * nt, pm_peakloc + (size_t)j * nt);
+    ft = lt + 1;
+    lt += Gs / 2;
+    if (lt > Gs) lt = Gs;
+  }
+  k.ft = 0; k.lt = Gs;
+  double *pk = peakloc + 2 * (size_t)npar, *ml = mlval + 2 * (size_t)npar;
+  pk_marginalopt(&k, ml, pk);
+  k.kind = 0;
+  for (int i = 0; i < nm; i++) {
+    k.idx = np + i;
+    double maxp = -pk_f(&k, pk[np + i]), max0p = -pk_f(&k, PK_MINPARAMVAL);
+    migtest[i] = 2 * log(maxp / max0p);
+  }
+  k.kind = 1;
+  for (int i = 0; i < npar; i++) {
+    lo95[i] = hi95[i] = NAN;
+    if (!(pk[i] >= 0)) continue;
+    k.idx = i;
+    k.yadjust = log(ml[i]) - 1.92;
+    lo95[i] = pk_bis(&k, PK_MINPARAMVAL, pk[i]);
+    hi95[i] = pk_bis(&k, pk[i], i < np ? thmax[i] : mgmax[i - np]);
+  }
+  if (nt) {
+    pk_marginalopt_popmig(&k, nt, pm_mlval + 2 * (size_t)nt, pm_peakloc + 2 * (size_t)nt);
+    k.kind = 2;
+    k.uniform2nm = 1; /* the test calls marginpopmig whatever the prior */
+    for (int t = 0; t < nt; t++) {
+      k.idx = t;
+      double maxp = -pk_f(&k, pm_peakloc[2 * (size_t)nt + t]), max0p = -pk_f(&k, PK_MINPARAMVAL);
+      pm_test[t] = 2 * log(maxp / max0p);
+    }
+  }
+  return k.st;
 }

@@ -207,6 +207,18 @@ double ora_popmig(int G, int rowlen, const float *g, int np, int nm, int thetai,
                   double qmax, double mmax, int prob_or_like, int *st);
 double ora_pop_expomig(int G, int rowlen, const float *g, int np, int nm, int thetai, int mi, double x,
                        double qmax, double mmean, int prob_or_like, int *st);
+/* findmarginpeaks' numbers (surface_call_functions.cpp:316-734): mlval,
+ * peakloc [3][np+nm] over the first half, the second half and all of the
+ * genealogies (G clamped to 299,999), migtest [nm], lo95 / hi95 [np+nm]
+ * (NaN where no peak), and for the nt 2NM terms (mpop, mterm) pm_mlval,
+ * pm_peakloc [3][nt], pm_test [nt].  mgmean NULL: uniform migration
+ * priors.  Returns -1 for 10 or fewer genealogies, else an incomplete-gamma
+ * status (0 = fine). */
+int ora_findmarginpeaks(int G, int rowlen, const float *g, int np, int nm, const double *thmin,
+                        const double *thmax, const double *mgmin, const double *mgmax, const double *mgmean,
+                        int nt, const int *mpop, const int *mterm, double *mlval, double *peakloc,
+                        double *migtest, double *lo95, double *hi95, double *pm_mlval, double *pm_peakloc,
+                        double *pm_test);
 
 #ifdef __cplusplus
 }

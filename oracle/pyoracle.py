@@ -70,6 +70,8 @@ def _declare(L):
         getattr(L, f).restype = D
     L.ora_margincalc.argtypes = [I, I, P, I, I, I, D, D, I, P]
     L.ora_margincalc.restype = D
+    L.ora_findmarginpeaks.argtypes = [I, I, P, I, I, P, P, P, P, P, I, P, P, P, P, P, P, P, P, P, P]
+    L.ora_findmarginpeaks.restype = I
     for f in ("ora_popmig", "ora_pop_expomig"):
         getattr(L, f).argtypes = [I, I, P, I, I, I, I, D, D, D, I, P]
         getattr(L, f).restype = D
@@ -402,6 +404,73 @@ def ref_popmig(rows, np_, nm, qmax, mmax, points, mmean=None):
     lines += ["%d %d %.17g %d" % (int(t), int(m), x, int(pl)) for t, m, x, pl in points]
     out = run_ref("popmig", "\n".join(lines) + "\n")
     return np.array([float(v) for v in out.split()])
+
+
+# ------------------------------------------------------ findmarginpeaks
+def _parse_peaks(out, nt):
+    d = {}
+    for ln in out.splitlines():
+        f = ln.split()
+        if not f:
+            continue
+        if f[0] == "TOOFEW":
+            return None
+        if f[0] in ("ML", "PK", "PML", "PPK"):
+            d.setdefault(f[0], []).append([float(v) for v in f[2:]])
+        else:
+            d[f[0]] = [float(v) for v in f[1:]]
+    o = {"mlval": np.array(d["ML"]), "peakloc": np.array(d["PK"]), "migtest": np.array(d["MT"]),
+         "lo95": np.array(d["LO"]), "hi95": np.array(d["HI"])}
+    if nt:
+        o["pm_mlval"], o["pm_peakloc"], o["pm_test"] = np.array(d["PML"]), np.array(d["PPK"]), np.array(d["PT"])
+    return o
+
+
+def findmarginpeaks(rows, np_, nm, th_min, th_max, mg_min, mg_max, mg_mean=None, terms=()):
+    """The oracle's findmarginpeaks numbers (same dict as ref_findmarginpeaks);
+    None for 10 or fewer genealogies."""
+    G, rl = rows.shape
+    rows = np.ascontiguousarray(rows, np.float32)
+    terms = np.asarray(list(terms), np.int32).reshape(-1, 2)
+    nt, npar = len(terms), np_ + nm
+    mpop, mterm = np.ascontiguousarray(terms[:, 0]), np.ascontiguousarray(terms[:, 1])
+    o = {"mlval": np.zeros((3, npar)), "peakloc": np.zeros((3, npar)), "migtest": np.zeros(max(nm, 1)),
+         "lo95": np.zeros(npar), "hi95": np.zeros(npar), "pm_mlval": np.zeros((3, max(nt, 1))),
+         "pm_peakloc": np.zeros((3, max(nt, 1))), "pm_test": np.zeros(max(nt, 1))}
+    f = [_f64(v) for v in (th_min, th_max, mg_min, mg_max)]
+    mean = _f64(mg_mean) if mg_mean is not None else None
+    st = lib().ora_findmarginpeaks(G, rl, _p(rows), np_, nm, *(_p(v) for v in f), _p(mean) if mean is not None else None,
+                                   nt, _p(mpop), _p(mterm), *(_p(o[k]) for k in ("mlval", "peakloc", "migtest",
+                                                                                  "lo95", "hi95", "pm_mlval",
+                                                                                  "pm_peakloc", "pm_test")))
+    if st == -1:
+        return None
+    if st:
+        raise ValueError("incomplete gamma term failed (%d)" % st)
+    o["migtest"] = o["migtest"][:nm]
+    if nt:
+        o["pm_mlval"], o["pm_peakloc"], o["pm_test"] = o["pm_mlval"][:, :nt], o["pm_peakloc"][:, :nt], o["pm_test"][:nt]
+    else:
+        for k in ("pm_mlval", "pm_peakloc", "pm_test"):
+            del o[k]
+    return o
+
+
+def ref_findmarginpeaks(rows, np_, nm, th_min, th_max, mg_min, mg_max, mg_mean=None, terms=()):
+    """The reference's findmarginpeaks numbers (marginalopt over the two
+    halves and all genealogies, the migration tests, margin95, and for the
+    2NM terms marginalopt_popmig and its test) through oracle/_ref/imaref
+    (this container only)."""
+    G, rl = rows.shape
+    terms = list(terms)
+    lines = ["%d %d %d %d %d" % (G, rl, np_, nm, 1 if mg_mean is not None else 0),
+             " ".join("%.9g" % v for v in np.asarray(rows, np.float32).ravel())]
+    for arr in (th_min, th_max, mg_min, mg_max, mg_mean if mg_mean is not None else np.zeros(nm)):
+        lines.append(" ".join("%.17g" % v for v in arr))
+    lines.append(str(len(terms)))
+    lines.append(" ".join(str(t[0]) for t in terms))
+    lines.append(" ".join(str(t[1]) for t in terms))
+    return _parse_peaks(run_ref("peaks", "\n".join(lines) + "\n"), len(terms))
 
 
 # ------------------------------------------------- treeweight + p(G) integral

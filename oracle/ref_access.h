@@ -10,4 +10,5 @@ double refacc_icoal(int cc, double fc, double hcc, double max, double min);
 double refacc_imig(int cm, double fm, double max, double min);
 double refacc_imig_expo(int cm, double fm, double mean);
 void refacc_setup_iparams(void);
+double refacc_marginp(int param, int firsttree, int lasttree, double x);
 #endif

@@ -322,6 +322,90 @@ static void run_popmig()
   }
 }
 
+/* PEAKS: G rowlen np nm expo rows[G*rowlen] thmin[np] thmax[np] mgmin[nm] mgmax[nm]
+ *        mgmean[nm] nterms mpop[nterms] mterm[nterms]
+ *   -> findmarginpeaks' numbers (surface_call_functions.cpp:433-470, :596-652):
+ *      "ML j" / "PK j" per range j = 0..2, "MT" migtest, "LO" / "HI" (margin95 where
+ *      the peak exists, else nan), and with terms "PML j" / "PPK j", "PT" */
+static void run_peaks()
+{
+  int G = rd_i(), rowlen = rd_i(), np = rd_i(), nm = rd_i(), expo = rd_i();
+  load_gsampinf(G, rowlen, np, nm, 2);
+  setlogfact();
+  gsamp_ccp = 0;
+  gsamp_fcp = gsamp_ccp + np;
+  gsamp_hccp = gsamp_fcp + np;
+  gsamp_mcp = gsamp_hccp + np;
+  gsamp_fmp = gsamp_mcp + nm;
+  gsamp_qip = gsamp_fmp + nm;
+  gsamp_mip = gsamp_qip + np;
+  modeloptions[EXPOMIGRATIONPRIOR] = expo;
+  itheta = static_cast<struct i_param *>(calloc(np, sizeof(struct i_param)));
+  imig = static_cast<struct i_param *>(calloc(nm > 0 ? nm : 1, sizeof(struct i_param)));
+  for (int i = 0; i < np; i++) itheta[i].pr.min = rd_d();
+  for (int i = 0; i < np; i++) itheta[i].pr.max = rd_d();
+  for (int i = 0; i < nm; i++) imig[i].pr.min = rd_d();
+  for (int i = 0; i < nm; i++) imig[i].pr.max = rd_d();
+  for (int i = 0; i < nm; i++) imig[i].pr.mean = rd_d();
+  int nt = rd_i();
+  std::vector<int> mpop(nt > 0 ? nt : 1), mterm(nt > 0 ? nt : 1);
+  for (int t = 0; t < nt; t++) mpop[t] = rd_i();
+  for (int t = 0; t < nt; t++) mterm[t] = rd_i();
+  const int p = np + nm, NT = 2;
+  genealogiessaved = IMIN(MAXGENEALOGIESTOSAVE - 1, genealogiessaved);
+  if (genealogiessaved <= 10) {
+    printf("TOOFEW\n");
+    return;
+  }
+  std::vector<std::vector<double>> ml(NT + 1, std::vector<double>(p, NAN)), pk(NT + 1, std::vector<double>(p, NAN));
+  std::vector<std::vector<double>> pml(NT + 1, std::vector<double>(nm > 0 ? nm : 1, NAN)),
+      ppk(NT + 1, std::vector<double>(nm > 0 ? nm : 1, NAN));
+  int firsttree, lasttree, j;
+  for (firsttree = 0, lasttree = (int)genealogiessaved / NT, j = 0; j < NT; j++) {
+    marginalopt(firsttree, lasttree, ml[j].data(), pk[j].data());
+    if (nt) marginalopt_popmig(firsttree, lasttree, pml[j].data(), ppk[j].data(), mpop.data(), mterm.data());
+    firsttree = lasttree + 1;
+    lasttree += (int)genealogiessaved / NT;
+    if (lasttree > genealogiessaved) lasttree = genealogiessaved;
+  }
+  marginalopt(0, genealogiessaved, ml[NT].data(), pk[NT].data());
+  for (j = 0; j <= NT; j++) {
+    printf("ML %d", j);
+    for (int i = 0; i < p; i++) printf(" %.17g", pk[j][i] < 0 ? NAN : ml[j][i]);
+    printf("\nPK %d", j);
+    for (int i = 0; i < p; i++) printf(" %.17g", pk[j][i]);
+    printf("\n");
+  }
+  printf("MT");
+  for (int i = 0; i < nm; i++) {
+    double maxp = -refacc_marginp(i + np, 0, genealogiessaved, pk[NT][i + np]);
+    double max0p = -refacc_marginp(i + np, 0, genealogiessaved, MINPARAMVAL);
+    printf(" %.17g", 2 * log(maxp / max0p));
+  }
+  printf("\nLO");
+  for (int i = 0; i < p; i++) printf(" %.17g", pk[NT][i] >= 0 ? margin95(ml[NT].data(), pk[NT].data(), i, 0) : NAN);
+  printf("\nHI");
+  for (int i = 0; i < p; i++) printf(" %.17g", pk[NT][i] >= 0 ? margin95(ml[NT].data(), pk[NT].data(), i, 1) : NAN);
+  printf("\n");
+  if (nt) {
+    marginalopt_popmig(0, genealogiessaved, pml[NT].data(), ppk[NT].data(), mpop.data(), mterm.data());
+    for (j = 0; j <= NT; j++) {
+      printf("PML %d", j);
+      for (int t = 0; t < nt; t++) printf(" %.17g", pml[j][t]);
+      printf("\nPPK %d", j);
+      for (int t = 0; t < nt; t++) printf(" %.17g", ppk[j][t]);
+      printf("\n");
+    }
+    printf("PT");
+    for (int t = 0; t < nt; t++) {
+      double maxp = -marginpopmig(mterm[t], 0, genealogiessaved, ppk[NT][t], mpop[t]);
+      double max0p = -marginpopmig(mterm[t], 0, genealogiessaved, MINPARAMVAL, mpop[t]);
+      printf(" %.17g", 2 * log(maxp / max0p));
+    }
+    printf("\n");
+  }
+}
+
 /* TW: npops nchains nloci expo nomig treestring thetaprior mprior
  *     per locus: numgenes hval samppop[npops]
  *     per chain: tvals[npops-1]
@@ -549,7 +633,7 @@ static void run_iterm()
 
 int main(int argc, char **argv)
 {
-  if (argc != 3) { fprintf(stderr, "usage: imaref is|hky|sw|swap|jointp|de|margin|tw|iterm|ry|popmig <input>\n"); return 2; }
+  if (argc != 3) { fprintf(stderr, "usage: imaref is|hky|sw|swap|jointp|de|margin|tw|iterm|ry|popmig|peaks <input>\n"); return 2; }
   g_in = fopen(argv[2], "r");
   if (!g_in) { perror(argv[2]); return 2; }
   std::string mode = argv[1];
@@ -564,6 +648,7 @@ int main(int argc, char **argv)
   else if (mode == "iterm") run_iterm();
   else if (mode == "ry") run_ry();
   else if (mode == "popmig") run_popmig();
+  else if (mode == "peaks") run_peaks();
   else { fprintf(stderr, "unknown mode\n"); return 2; }
   fclose(g_in);
   return 0;

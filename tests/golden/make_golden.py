@@ -35,7 +35,13 @@ Fixtures:
                     (no coalescences, no migrations, neither), posterior
                     and likelihood forms, and a 2NM curve grid
 
-Run with fixture names (is hky sw swap jointp de margin tw ry popmig) to regenerate only those.
+  golden_peaks.npz  findmarginpeaks' numbers (marginalopt peaks over both
+                    halves and all genealogies, migration tests, margin95
+                    limits, marginalopt_popmig peaks and tests) on the
+                    popmig rows and on rows whose peaks lie inside the
+                    priors, uniform and exponential migration priors
+
+Run with fixture names (is hky sw swap jointp de margin tw ry popmig peaks) to regenerate only those.
 """
 from __future__ import annotations
 
@@ -532,12 +538,46 @@ def golden_popmig():
     np.savez_compressed(os.path.join(OUT, "golden_popmig.npz"), **out)
 
 
+def interior_rows(G=2000, seed=2025):
+    """gsampinf rows (3 population sizes, 2 migration rates) whose marginal
+    peaks lie inside the priors: cc ~ Poisson(15) with fc / cc ~ U(1, 5)
+    (theta peaks 2-10 of 20), mc ~ Poisson(4) with mc / fm ~ U(0.3, 2)
+    (migration peaks inside 2 and 5), integrals ~ N(0, 1)."""
+    rng = np.random.default_rng(seed)
+    off = synth.gsamp_layout(3, 2, 1)
+    rows = np.zeros((G, off["rowlen"]), np.float32)
+    cc = rng.poisson(15.0, (G, 3))
+    rows[:, off["cc"]:off["cc"] + 3] = cc
+    rows[:, off["fc"]:off["fc"] + 3] = cc * rng.uniform(1.0, 5.0, (G, 3))
+    mc = rng.poisson(4.0, (G, 2))
+    rows[:, off["mc"]:off["mc"] + 2] = mc
+    rows[:, off["fm"]:off["fm"] + 2] = np.maximum(mc, 0.5) / rng.uniform(0.3, 2.0, (G, 2))
+    rows[:, off["qi"]:off["qi"] + 3] = rng.normal(0.0, 1.0, (G, 3))
+    rows[:, off["mi"]:off["mi"] + 2] = rng.normal(0.0, 1.0, (G, 2))
+    rows[:, off["t"]] = rng.uniform(0.1, 3.0, G)
+    return rows
+
+
+def golden_peaks():
+    qmax, mmax, mean = np.array([20.0, 15.0, 25.0]), np.array([2.0, 5.0]), np.array([0.8, 1.7])
+    terms = [(0, 0), (1, 1)]
+    out = {"qmax": qmax, "mmax": mmax, "mean": mean, "terms": np.array(terms)}
+    for name, rows in (("branch", popmig_rows()), ("interior", interior_rows())):
+        out[name + "_rows"] = rows
+        for tag, m in (("", None), ("_expo", mean)):
+            r = O.ref_findmarginpeaks(rows, 3, 2, np.zeros(3), qmax, np.zeros(2), mmax, mg_mean=m, terms=terms)
+            for k, v in r.items():
+                out["%s%s_%s" % (name, tag, k)] = v
+    np.savez_compressed(os.path.join(OUT, "golden_peaks.npz"), **out)
+
+
 if __name__ == "__main__":
     if not O.ref_available():
         sys.exit("build the reference harness first: make -C oracle ref")
     gens = {"is": golden_is, "hky": golden_hky, "sw": golden_sw, "swap": golden_swap,
             "jointp": golden_jointp, "de": golden_de, "margin": golden_margin,
-            "tw": golden_tw, "ry": golden_ry, "popmig": golden_popmig}
+            "tw": golden_tw, "ry": golden_ry, "popmig": golden_popmig,
+            "peaks": golden_peaks}
     for name in (sys.argv[1:] or list(gens)):
         gens[name]()
     for f in sorted(os.listdir(OUT)):
