@@ -768,7 +768,7 @@ def run_popmig(args):
 
     G, grid = args.popmig_g, 1000
     rng = np.random.default_rng(1013)
-    rows, _, off = synth.surface_stats(rng, G, 5, 8, 2)
+    rows = synth.peaked_stats(rng, G, 5, 8, 2)
     pm = popmodel.build("((0,1):3,2):4", 3)
     terms = popmodel.popmig_terms(pm)
     tlist = [(t, m) for t, m, _ in terms]
@@ -816,7 +816,8 @@ def run_popmig(args):
         "metric": PM_METRIC, "value": round(value, 1), "unit": "terms/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic gsampinf rows (cc ~ Poisson(8), fc ~ Gamma(4,1), mc ~ Poisson(1), fm ~ Gamma(2,1))",
+        "data": "synthetic gsampinf rows with interior peaks (cc ~ Poisson(15), fc/cc ~ U(1,5), mc ~ Poisson(4), "
+                "mc/fm ~ U(0.3,2), log integrals ~ N(0,1))",
         "config": {"workload": "popmig-curves: G=%d genealogies, 3 populations (5 theta, 8 m), %d 2NM terms, "
                                "curves of %d points each after the top-down range scan, posterior form"
                                % (G, len(tlist), grid),
@@ -842,6 +843,24 @@ def run_popmig(args):
     out["cpu_baseline"] = {"value": round(n * G / dt, 1), "unit": "terms/s", "cores": 1, "kind": "port",
                            "sample": "%d curve points over all %d genealogies through the oracle's "
                                      "calc_popmig in C" % (n, G)}
+    # findmarginpeaks on the same genealogies: 13 parameters x 3 genealogy
+    # ranges of bracket + golden-section searches, the migration tests, the
+    # 95% limits, and the 8 2NM terms' scans, searches and tests
+    tmin, mmin = np.zeros(5), np.zeros(8)
+    t0 = time.perf_counter()
+    pk = ctx.findmarginpeaks(tmin, qmax, mmin, mmax, terms=tlist)
+    pk_s = time.perf_counter() - t0
+    # the oracle's findmarginpeaks in C on a genealogy sample, scaled per genealogy
+    gs = args.peaks_cpu_g
+    t0 = time.perf_counter()
+    O.findmarginpeaks(rows[:gs], 5, 8, tmin, qmax, mmin, mmax, terms=tlist)
+    cpu_s = (time.perf_counter() - t0) * G / gs
+    out["marginal_peaks"] = {"seconds": round(pk_s, 3), "rounds": pk["rounds"],
+                             "cpu_seconds_1core_scaled": round(cpu_s, 1),
+                             "cpu_sample": "the oracle's findmarginpeaks on the first %d genealogies, "
+                                           "scaled by %d/%d" % (gs, G, gs),
+                             "note": "all searches advance together; each round one batched launch per density "
+                                     "kind and genealogy range"}
     print(json.dumps(out), flush=True)
     ctx.close()
 
@@ -861,6 +880,7 @@ def main():
     ap.add_argument("--surface-method", default="tc", choices=["tc", "fp32"])
     ap.add_argument("--no-peak-search", action="store_true", help="surface: skip the DE peak search")
     ap.add_argument("--popmig-g", type=int, default=300000, help="popmig: saved genealogies")
+    ap.add_argument("--peaks-cpu-g", type=int, default=6000, help="popmig: genealogies in the CPU peaks sample")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -456,6 +456,25 @@ def surface_stats(rng, G, np_=5, nm=8, nsplit=2):
     return rows, lognorm, off
 
 
+def peaked_stats(rng, G, np_=5, nm=8, nsplit=2):
+    """Synthetic gsampinf rows whose marginal densities peak inside priors of
+    theta <= 20 and m <= 2: cc ~ Poisson(15) with fc / cc ~ U(1, 5) (theta
+    peaks near 2 fc / cc), mc ~ Poisson(4) with mc / fm ~ U(0.3, 2) (m peaks
+    near mc / fm), log integrals ~ N(0, 1)."""
+    off = gsamp_layout(np_, nm, nsplit)
+    rows = np.zeros((G, off["rowlen"]), np.float32)
+    cc = rng.poisson(15.0, (G, np_))
+    rows[:, off["cc"]:off["cc"] + np_] = cc
+    rows[:, off["fc"]:off["fc"] + np_] = cc * rng.uniform(1.0, 5.0, (G, np_))
+    mc = rng.poisson(4.0, (G, nm))
+    rows[:, off["mc"]:off["mc"] + nm] = mc
+    rows[:, off["fm"]:off["fm"] + nm] = np.maximum(mc, 0.5) / rng.uniform(0.3, 2.0, (G, nm))
+    rows[:, off["qi"]:off["qi"] + np_] = rng.normal(0.0, 1.0, (G, np_))
+    rows[:, off["mi"]:off["mi"] + nm] = rng.normal(0.0, 1.0, (G, nm))
+    rows[:, off["t"]:off["t"] + nsplit] = rng.uniform(0.1, 3.0, (G, nsplit))
+    return rows
+
+
 def surface_points(rng, P, np_=5, nm=8, theta_hi=20.0, m_hi=2.0):
     th = rng.uniform(0.1, theta_hi, (P, np_))
     m = rng.uniform(1e-7, m_hi, (P, nm))
