@@ -200,7 +200,7 @@ __device__ __forceinline__ int expo_of(float m)  // floor(log2(m)) for normal m 
 template <bool CACHE, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *reqs,
                                                      double *result, int32_t *status, int maxnl,
-                                                     int cache_S)
+                                                     int cache_S, int tip_cap)
 {
   extern __shared__ __align__(16) char smem[];
   const ReqDev R = reqs[blockIdx.x];
@@ -216,7 +216,12 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
   T.dirty = T.fresh + maxnl;
   T.slot = T.dirty + maxnl;
   T.order = reinterpret_cast<int16_t *>(smem + lay.order);
-  float4 *cpart = reinterpret_cast<float4 *>(smem + lay.total);         // [nint][cache_S]
+  // the tips' states [n][S] when they fit in tip_cap bytes: the level loop
+  // then reads no global memory when the partials are cached too
+  int8_t *stip = reinterpret_cast<int8_t *>(smem + lay.total);
+  const size_t tipb = ((size_t)tip_cap + 15) & ~size_t(15);
+  const bool tips = n * S <= tip_cap;
+  float4 *cpart = reinterpret_cast<float4 *>(smem + lay.total + tipb);  // [nint][cache_S]
   int32_t *cexp = reinterpret_cast<int32_t *>(cpart + (size_t)(maxnl / 2) * cache_S);
   __shared__ double red_d[BS / 32];
   __shared__ long long red_e[BS / 32];
@@ -233,6 +238,10 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
   }
   for (int k = tid; k < nint + nlev + 1; k += BS) T.order[k] = P.sched[it.sched_off + k];
   T.lstart = T.order + nint;
+  if (tips) {
+    const int8_t *sq = P.seq + L.seq_off;
+    for (int k = tid; k < n * S; k += BS) stip[k] = sq[k];
+  }
   if (tid == 0) {
     const double *pid = P.pi + 4 * (size_t)R.item;
     smu = (float)(R.u / ((double)L.totsites * standfactor(pid, R.par)));
@@ -286,7 +295,7 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
         const float *Kp = Pm + 16 * c;
         const HkyCoef K = {Kp[0], Kp[1], Kp[2], Kp[3], Kp[4]};
         if (c < n) {
-          hky_apply_tip(K, pi4, seq[(size_t)c * S + i], v[h]);
+          hky_apply_tip(K, pi4, tips ? stip[c * S + i] : seq[(size_t)c * S + i], v[h]);
         } else {
           float4 Lc;
           if (CACHE && T.fresh[c]) {
@@ -519,22 +528,27 @@ size_t hky_smem(int maxn, size_t elem) { return hky_layout(2 * maxn - 1, elem).t
 // Partials stay in shared memory when the largest chain-locus of the batch
 // fits in this budget (keeps >= 3 CTAs per SM).
 constexpr size_t HKY_CACHE_BUDGET = 64 * 1024;
+constexpr size_t HKY_TIP_BUDGET = 8 * 1024;
 
 template <int BS, int MINB>
 static void hky_fast_bs(const Pools &P, const ReqDev *reqs, int nreq, int maxnl, int maxS, bool cache_ok,
                         double *result, int32_t *status, cudaStream_t st)
 {
-  size_t base = hky_smem((maxnl + 1) / 2, sizeof(float));
+  // tip states staged in shared memory when the largest locus's fit in
+  // HKY_TIP_BUDGET bytes (a few KB: occupancy is unchanged)
+  const size_t maxn = (size_t)(maxnl + 1) / 2;
+  const int tip_cap = (maxn * maxS <= HKY_TIP_BUDGET) ? (int)(maxn * maxS) : 0;
+  size_t base = hky_smem((int)maxn, sizeof(float)) + (((size_t)tip_cap + 15) & ~size_t(15));
   size_t cache = (size_t)(maxnl / 2) * maxS * (sizeof(float4) + sizeof(int32_t));
   if (cache_ok && cache <= HKY_CACHE_BUDGET) {
     size_t sm = base + cache;
     if (sm > 48 * 1024)
       cudaFuncSetAttribute(k_hky_fast<true, BS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_hky_fast<true, BS, MINB><<<nreq, BS, sm, st>>>(P, reqs, result, status, maxnl, maxS);
+    k_hky_fast<true, BS, MINB><<<nreq, BS, sm, st>>>(P, reqs, result, status, maxnl, maxS, tip_cap);
   } else {
     if (base > 48 * 1024)
       cudaFuncSetAttribute(k_hky_fast<false, BS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)base);
-    k_hky_fast<false, BS, MINB><<<nreq, BS, base, st>>>(P, reqs, result, status, maxnl, 0);
+    k_hky_fast<false, BS, MINB><<<nreq, BS, base, st>>>(P, reqs, result, status, maxnl, 0, tip_cap);
   }
 }
 
