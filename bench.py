@@ -855,6 +855,35 @@ def run_popmig(args):
     t0 = time.perf_counter()
     O.findmarginpeaks(rows[:gs], 5, 8, tmin, qmax, mmin, mmax, terms=tlist)
     cpu_s = (time.perf_counter() - t0) * G / gs
+    # the saved genealogies as a .ti file (the reference's "%.6f" tab-separated
+    # text), loaded by the library's parser and by the reference's value loop
+    import tempfile
+    tdir = tempfile.mkdtemp()
+    tpath = os.path.join(tdir, "popmig.ti")
+    with open(tpath, "w") as f:
+        f.write("IMa2p-style header\nVALUESSTART\n")
+        np.savetxt(f, rows, fmt="%.6f", delimiter="\t")
+    mb = os.path.getsize(tpath) / 1e6
+    t0 = time.perf_counter()
+    lrows, _ = api.ti_read([tpath], rows.shape[1])
+    ti_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    orows = O.ti_load(tpath, rows.shape[1], G)
+    ti_cpu = time.perf_counter() - t0
+    bpath = os.path.join(tdir, "popmig.tib")
+    api.ti_write_binary(bpath, lrows)
+    t0 = time.perf_counter()
+    brows = api.ti_read_binary(bpath)
+    tib_s = time.perf_counter() - t0
+    assert np.array_equal(lrows, orows) and np.array_equal(brows, lrows)
+    for fp in (tpath, bpath):
+        os.unlink(fp)
+    os.rmdir(tdir)
+    out["ti_load"] = {"genealogies": int(len(lrows)), "mb": round(mb, 1), "seconds": round(ti_s, 3),
+                      "mb_per_s": round(mb / ti_s, 1), "binary_seconds": round(tib_s, 4),
+                      "cpu_seconds_1core": round(ti_cpu, 3),
+                      "cpu": "the reference's loop (fgets per genealogy, sscanf per value) in the oracle, one core",
+                      "rows_equal": True}
     out["marginal_peaks"] = {"seconds": round(pk_s, 3), "rounds": pk["rounds"],
                              "cpu_seconds_1core_scaled": round(cpu_s, 1),
                              "cpu_sample": "the oracle's findmarginpeaks on the first %d genealogies, "

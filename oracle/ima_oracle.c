@@ -12,6 +12,8 @@
  */
 #include "ima_oracle.h"
 #include <float.h>
+#include <ctype.h>
+#include <stdio.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -1749,4 +1751,36 @@ int ora_findmarginpeaks(int G, int rowlen, const float *g, int np, int nm, const
     }
   }
   return k.st;
+}
+
+/* ======================================================================
+ * .ti loading, the reference's way (loadgenealogyvalues,
+ * ima_main_mpi.cpp:3370-3400): lines up to VALUESSTART skipped, then one
+ * fgets per genealogy (a buffer of rowlen * 20 characters) and one
+ * sscanf("%f") per value, stepping to the next whitespace; every genealogy
+ * kept.  Returns the number of rows read (at most cap), or -1 when the file
+ * cannot be opened.  Used as the one-core baseline of the library's parser.
+ * ==================================================================== */
+int ora_ti_load(const char *path, int rowlen, float *rows, int cap)
+{
+  FILE *f = fopen(path, "r");
+  if (!f) return -1;
+  char head[300];
+  while (fgets(head, sizeof(head), f) && strstr(head, "VALUESSTART") == NULL && !feof(f)) {
+  }
+  size_t blen = (size_t)rowlen * 20;
+  char *line = (char *)malloc(blen);
+  int loaded = 0;
+  while (line && loaded < cap && fgets(line, (int)blen, f) && !feof(f)) {
+    char *c = line;
+    for (int i = 0; i < rowlen; i++) {
+      sscanf(c, "%f", &rows[(size_t)loaded * rowlen + i]);
+      while (*c && isspace((unsigned char)*c)) c++; /* nextwhite: past this value */
+      while (*c && !isspace((unsigned char)*c)) c++;
+    }
+    loaded++;
+  }
+  free(line);
+  fclose(f);
+  return loaded;
 }

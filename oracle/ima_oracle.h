@@ -219,6 +219,9 @@ int ora_findmarginpeaks(int G, int rowlen, const float *g, int np, int nm, const
                         int nt, const int *mpop, const int *mterm, double *mlval, double *peakloc,
                         double *migtest, double *lo95, double *hi95, double *pm_mlval, double *pm_peakloc,
                         double *pm_test);
+/* .ti loading the reference's way (fgets per genealogy, sscanf("%f") per
+ * value; ima_main_mpi.cpp:3370-3400), every genealogy kept, at most cap. */
+int ora_ti_load(const char *path, int rowlen, float *rows, int cap);
 
 #ifdef __cplusplus
 }

@@ -70,6 +70,8 @@ def _declare(L):
         getattr(L, f).restype = D
     L.ora_margincalc.argtypes = [I, I, P, I, I, I, D, D, I, P]
     L.ora_margincalc.restype = D
+    L.ora_ti_load.argtypes = [C.c_char_p, I, P, I]
+    L.ora_ti_load.restype = I
     L.ora_findmarginpeaks.argtypes = [I, I, P, I, I, P, P, P, P, P, I, P, P, P, P, P, P, P, P, P, P]
     L.ora_findmarginpeaks.restype = I
     for f in ("ora_popmig", "ora_pop_expomig"):
@@ -424,6 +426,15 @@ def _parse_peaks(out, nt):
     if nt:
         o["pm_mlval"], o["pm_peakloc"], o["pm_test"] = np.array(d["PML"]), np.array(d["PPK"]), np.array(d["PT"])
     return o
+
+
+def ti_load(path, rowlen, cap):
+    """The reference's .ti value loop on one core: rows [n][rowlen] float32."""
+    rows = np.zeros((cap, rowlen), np.float32)
+    n = lib().ora_ti_load(os.fsencode(str(path)), int(rowlen), _p(rows), int(cap))
+    if n < 0:
+        raise OSError("cannot open %s" % path)
+    return rows[:n]
 
 
 def findmarginpeaks(rows, np_, nm, th_min, th_max, mg_min, mg_max, mg_mean=None, terms=()):
