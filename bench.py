@@ -708,6 +708,7 @@ def splittime_sweep(pm, packed, samp, tv, base, seq, nloci, nch, args):
     prng = np.random.default_rng(3)
     tprior = [(0.0, 3.0), (0.0, 6.0)]
     for _ in range(args.warmup):
+        cs.sweep_device_mt(prng.integers(0, 2, nch), mt, tprior)
         cs.sweep_device(prng.integers(0, 2, nch), mt, tprior, 3)
         cs.sweep(prng.integers(0, 2, nch), mt, tprior, 3)
     ctx.synchronize()
@@ -715,9 +716,14 @@ def splittime_sweep(pm, packed, samp, tv, base, seq, nloci, nch, args):
     acc = 0
     t0 = time.perf_counter()
     for _ in range(nsw):
-        acc += int(cs.sweep_device(prng.integers(0, 2, nch), mt, tprior, 3).sum())
+        acc += int(cs.sweep_device_mt(prng.integers(0, 2, nch), mt, tprior).sum())
     ctx.synchronize()
     wall = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for _ in range(nsw):
+        cs.sweep_device(prng.integers(0, 2, nch), mt, tprior, 3)
+    ctx.synchronize()
+    wall_pydraws = time.perf_counter() - t0
     t0 = time.perf_counter()
     for _ in range(nsw):
         cs.sweep(prng.integers(0, 2, nch), mt, tprior, 3)
@@ -745,14 +751,16 @@ def splittime_sweep(pm, packed, samp, tv, base, seq, nloci, nch, args):
     cpu = ncpu / (time.perf_counter() - t0)
     ctx.close()
     return {"chain_updates_per_s": round(nsw * nch / wall, 1), "ms_per_sweep": round(1e3 * wall / nsw, 3),
+            "ms_per_sweep_python_draws": round(1e3 * wall_pydraws / nsw, 3),
             "ms_per_sweep_host_decisions": round(1e3 * wall_host / nsw, 3),
             "chains": nch, "loci": nloci, "accept_rate": round(acc / (nsw * nch), 3),
             "setup_s": round(setup_s, 2),
             "cpu_chain_updates_per_s_1core": round(cpu, 2),
-            "note": "resident genealogies, labels and times; per sweep one ima_gpu_changet_ry1_sweep: MT19937 "
-                    "draws and the Hastings logs on the host; rubber band, weights, p(G), infinite-sites "
-                    "likelihoods, MH decisions and commits on the GPU (host_decisions: the same with the "
-                    "decisions taken in Python); CPU: one chain's update on the oracle's C functions"}
+            "note": "resident genealogies, labels and times; per sweep one ima_gpu_changet_ry1_sweep_mt: MT19937 "
+                    "draws (getnewt, acceptance) and the Hastings logs in the library; rubber band, weights, "
+                    "p(G), infinite-sites likelihoods, MH decisions and commits on the GPU (python_draws: the "
+                    "draws in Python; host_decisions: the decisions taken in Python too); CPU: one chain's "
+                    "update on the oracle's C functions"}
 
 
 def run_popmig(args):

@@ -53,7 +53,7 @@ EXPORTS = [
     "ima_gpu_set_locus_pops", "ima_gpu_set_labels", "ima_gpu_get_times", "ima_gpu_rubber_band",
     "ima_gpu_chain_weights", "ima_gpu_changet_ry1_sweep", "ima_gpu_get_probg", "ima_gpu_get_split_times",
     "ima_gpu_checkpoint_write", "ima_gpu_checkpoint_read", "ima_gpu_popmig", "ima_gpu_popmig_curves",
-    "ima_gpu_findmarginpeaks",
+    "ima_gpu_findmarginpeaks", "ima_gpu_changet_ry1_sweep_mt",
 ]
 
 
@@ -173,6 +173,7 @@ def _declare(L):
         "ima_gpu_checkpoint_read": (I, [P, C.c_char_p, P]),
         "ima_gpu_popmig": (I, [P, I, P, P, P, P, P, P, I, P]),
         "ima_gpu_popmig_curves": (I, [P, I, P, P, I, P, P, P, I, P, P, P]),
+        "ima_gpu_changet_ry1_sweep_mt": (I, [P, I, P, P, P, P, P, D, P, P, I, P, P, P, P]),
         "ima_gpu_findmarginpeaks": (I, [P, P, P, P, P, P, I, P, P, P, P, P, P, P, P, P, P, P, C.POINTER(I)]),
         "ima_gpu_swapchains": (I, [P, I, I, P, I, C.c_uint64, P, P]),
         "ima_gpu_get_swapcounts": (I, [P, I, P, P]),
@@ -608,6 +609,23 @@ class Context:
         rng, if given, takes the saved generator state."""
         self._ck(self.lib.ima_gpu_checkpoint_read(self.h, os.fsencode(path),
                                                   C.byref(rng) if rng is not None else None))
+
+    def changet_ry1_sweep_mt(self, chains, period, tprior, rng, u, kappa=None, gbeta=1.0, precision=PREC_FP64):
+        """changet_ry1_sweep with getnewt's and the acceptance draws made in
+        the library from rng (MT19937); tprior [(lo, hi)] per split.
+        Returns (accept, pdgsum, probg, newt)."""
+        chains, period = _i32(chains), _i32(period)
+        tp = np.asarray(tprior, np.float64).reshape(-1, 2)
+        lo, hi = _f64(tp[:, 0]), _f64(tp[:, 1])
+        u = _f64(u)
+        kap = _f64(kappa) if kappa is not None else None
+        n = len(chains)
+        acc, pdgsum, probg, newt = np.zeros(n, np.uint8), np.zeros(n), np.zeros(n), np.zeros(n)
+        self._ck(self.lib.ima_gpu_changet_ry1_sweep_mt(
+            self.h, n, _ptr(chains), _ptr(period), _ptr(lo), _ptr(hi), C.byref(rng), float(gbeta), _ptr(u),
+            _ptr(kap) if kap is not None else None, int(precision), _ptr(acc), _ptr(pdgsum), _ptr(probg),
+            _ptr(newt)))
+        return acc.astype(bool), pdgsum, probg, newt
 
     def surface_append_tree_rows(self, groups):
         """Append the gsampinf rows of these chains (last tree_prob) to the

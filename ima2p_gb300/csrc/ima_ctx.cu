@@ -3181,6 +3181,53 @@ extern "C" int ima_gpu_changet_ry1_sweep(ima_ctx *c, int nch, const int32_t *cha
   return r;
 }
 
+// changet_RY1's draws in the library: for each chain in order, getnewt
+// (update_gtree_common.cpp:2501-2519: one uniform, a window over the prior
+// range inside the neighbouring split times, reflected at its ends) and the
+// acceptance uniform, from the caller's MT19937, as the reference draws
+// them; the split times come from the context (ima_gpu_get_split_times).
+extern "C" int ima_gpu_changet_ry1_sweep_mt(ima_ctx *c, int nch, const int32_t *chains, const int32_t *period,
+                                            const double *tprior_lo, const double *tprior_hi, ima_mt19937 *rng,
+                                            double gbeta, const double *u, const double *kappa, int precision,
+                                            uint8_t *accept, double *pdgsum, double *probg, double *newt_out)
+{
+  if (!c || nch < 1 || !chains || !period || !tprior_lo || !tprior_hi || !rng || !u || !accept) return IMA_ERR_ARG;
+  if (!c->tw_ready) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_popmodel first");
+  const int npops = c->h_tw.npops, nsplit = npops - 1, last = nsplit;
+  if (c->h_tvr.size() != (size_t)c->nchains * nsplit) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_locus_pops first");
+  const double TIMEMAX = 1000000.0;  // imamp.hpp:129
+  std::vector<double> oldt(nch), newt(nch), tu(nch), td(nch), lhu(nch), lhd(nch), logU(nch), tv((size_t)nch * nsplit);
+  for (int k = 0; k < nch; k++) {
+    if (chains[k] < 0 || chains[k] >= c->nchains) return c->fail(IMA_ERR_ARG, "chain %d out of range", chains[k]);
+    if (period[k] < 0 || period[k] >= last) return c->fail(IMA_ERR_ARG, "period %d out of range", period[k]);
+  }
+  for (int k = 0; k < nch; k++) {
+    const int p = period[k];
+    const double *row = &c->h_tvr[(size_t)chains[k] * nsplit];
+    oldt[k] = row[p];
+    tu[k] = p == 0 ? 0.0 : row[p - 1];
+    td[k] = p == last - 1 ? TIMEMAX : row[p + 1];
+    const double tup = std::max(tprior_lo[p], tu[k]), tdp = std::min(tprior_hi[p], td[k]);
+    const double twin = (tdp - tup) / (log(static_cast<double>(c->nloci) + 1) * (npops - p));
+    const double U = ima_mt19937_uniform(rng);
+    double nt = (oldt[k] - twin / 2) + U * twin;
+    if (nt >= tdp)
+      nt = 2.0 * tdp - nt;
+    else if (nt <= tup)
+      nt = 2.0 * tup - nt;
+    newt[k] = nt;
+    logU[k] = log(ima_mt19937_uniform(rng));
+    lhu[k] = log((nt - tu[k]) / (oldt[k] - tu[k]));
+    lhd[k] = p == last - 1 ? 0.0 : log((td[k] - nt) / (td[k] - oldt[k]));
+    for (int q = 0; q < nsplit; q++) tv[(size_t)k * nsplit + q] = row[q];
+    tv[(size_t)k * nsplit + p] = nt;
+  }
+  if (newt_out) memcpy(newt_out, newt.data(), nch * 8ul);
+  return ima_gpu_changet_ry1_sweep(c, nch, chains, period, oldt.data(), newt.data(), tu.data(), td.data(), lhu.data(),
+                                   lhd.data(), logU.data(), gbeta, tv.data(), u, kappa, precision, accept, pdgsum,
+                                   probg);
+}
+
 // ======================================================================
 // checkpoints of the resident chain state (resume a run, with the caller's
 // generator state, as the reference's .mcf files and seed do)

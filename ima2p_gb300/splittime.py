@@ -437,6 +437,20 @@ class ResidentChainSet:
                                  inverse=True)
         return accept
 
+    def sweep_device_mt(self, periods, rng, tprior, gbeta=1.0):
+        """sweep_device with the draws in the library
+        (ima_gpu_changet_ry1_sweep_mt): rng is the api.MT19937 the
+        reference's uniform() would draw from."""
+        nch = self.nch
+        periods = np.asarray(periods, np.int64)
+        acc, pdgsum, probg, newt = self.ctx.changet_ry1_sweep_mt(
+            self.chains, periods, tprior, rng, np.tile(self.u, nch), np.tile(self.kappa, nch), gbeta, self.prec)
+        rows = np.arange(nch)
+        self.tvals[rows[acc], periods[acc]] = newt[acc]
+        self.pdgsum = pdgsum
+        self.probg = probg
+        return acc
+
     def sweep_device(self, periods, rng, tprior, npops, gbeta=1.0):
         """sweep() with the decisions on the device (ima_gpu_changet_ry1_sweep):
         one call per sweep; the host draws and takes the two logs of the

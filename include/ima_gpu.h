@@ -511,6 +511,17 @@ int ima_gpu_modelloop(ima_ctx *ctx, int modeltype, const double *upper, int pops
 int ima_gpu_checkpoint_write(ima_ctx *ctx, const char *path, const ima_mt19937 *rng);
 int ima_gpu_checkpoint_read(ima_ctx *ctx, const char *path, ima_mt19937 *rng);
 
+/* ima_gpu_changet_ry1_sweep with the draws made here: for each chain k in
+ * order, getnewt (update_gtree_common.cpp:2501-2519) on period[k] with the
+ * prior range [tprior_lo[p], tprior_hi[p]] inside the neighbouring split
+ * times (the context's, ima_gpu_get_split_times; TIMEMAX above the last
+ * one), then the acceptance uniform, both from *rng, as the reference draws
+ * them; then the sweep.  newt_out [nch] (may be NULL): the proposed times. */
+int ima_gpu_changet_ry1_sweep_mt(ima_ctx *ctx, int nch, const int32_t *chains, const int32_t *period,
+                                 const double *tprior_lo, const double *tprior_hi, ima_mt19937 *rng, double gbeta,
+                                 const double *u, const double *kappa, int precision, uint8_t *accept,
+                                 double *pdgsum, double *probg, double *newt_out);
+
 /* No counterpart in the reference.  The FP64 surface of ima_gpu_surface_eval
  * (IMA_SURF_FP64) for callers that cannot allocate device memory -- code
  * running inside a CUDA graph capture or under a host framework that owns

@@ -125,6 +125,40 @@ def test_resident_sweep_follows_the_reference():
     ctx.close()
 
 
+def test_library_drawn_sweep_follows_the_reference():
+    """ima_gpu_changet_ry1_sweep_mt: getnewt's and the acceptance draws made
+    in the library from the caller's MT19937, split times from the context --
+    the reference's decisions and times again, and the generator left where
+    the reference leaves it."""
+    case = RyCase()
+    ctx = api.Context(0)
+    for q in case.seqs:
+        ctx.add_locus_is(q)
+    ctx.set_chains(1, case.nch)
+    ctx.set_popmodel(case.pm, *case.priors())
+    cs = splittime.ResidentChainSet(ctx, case.fresh_gens(), [case.d["tv0"]] * case.nch, case.betas,
+                                    np.ones(case.nl), case.samps, case.us)
+    rng = api.MT19937(case.seed)
+    res = []
+    for s0 in range(0, len(case.steps), case.nch):
+        periods = [case.steps[s0 + c][1] for c in range(case.nch)]
+        acc = cs.sweep_device_mt(periods, rng, case.tprior)
+        for c in range(case.nch):
+            res.append((int(acc[c]), float(cs.tvals[c, periods[c]]), float(cs.probg[c]), float(cs.pdgsum[c])))
+    res, ref = np.array(res), case.res
+    assert np.array_equal(res[:, 0], ref[:, 0])
+    assert np.array_equal(res[:, 1], ref[:, 1])
+    np.testing.assert_allclose(res[:, 2], ref[:, 2], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(res[:, 3], ref[:, 3], rtol=1e-12)
+    assert np.array_equal(ctx.get_split_times(), cs.tvals)
+    # two draws per chain and step: the Python-driven run leaves the same state
+    rng2 = api.MT19937(case.seed)
+    for _ in range(2 * len(case.steps)):
+        rng2.uniform()
+    assert rng.uniform() == rng2.uniform()
+    ctx.close()
+
+
 def test_device_decided_sweep_follows_the_reference():
     """ima_gpu_changet_ry1_sweep: band, weights, likelihoods and the MH
     decision on the device in one call per sweep -- the reference's
