@@ -223,6 +223,8 @@ struct ima_ctx {
   double *d_beta = nullptr, *d_allbetas = nullptr, *d_probg = nullptr, *d_S = nullptr;
   int32_t *d_swapcount = nullptr, *d_tempcount = nullptr, *d_used = nullptr, *d_swap0ok = nullptr;
   unsigned long long *d_ctr = nullptr;
+  int32_t *d_is_site = nullptr;  // IS per-site mutation branches, valid while the topology is
+  uint8_t *d_is_valid = nullptr;
   double *d_uni = nullptr;
   size_t uni_cap = 0;
 
@@ -330,6 +332,8 @@ struct ima_ctx {
     P.alleles = d_al;
     P.dlike = d_dlike;
     P.sumlogk = d_sumlogk;
+    P.is_site = d_is_site;
+    P.is_valid = d_is_valid;
     P.pdg_new = d_pdg_new;
     P.part = d_part;
     P.pexp = d_pexp;
@@ -436,7 +440,7 @@ extern "C" void ima_gpu_destroy(ima_ctx *c)
                   c->d_mscratch, c->d_tw, c->d_logfact, c->d_twerr, c->d_twin, c->d_twout, c->d_tpbuf,
                   c->d_pop, c->d_moff, c->d_inode_off, c->d_gl, c->d_gt, c->d_moff_start, c->d_bcnt, c->d_bicnt,
                   c->d_mig_p, c->d_rsamp, c->d_mbase, c->d_mig_t, c->d_tvr, c->d_len_hold, c->d_rhlog,
-                  c->d_rh2, c->d_rsel};
+                  c->d_rh2, c->d_rsel, c->d_is_site, c->d_is_valid};
   for (void *p : devs)
     if (p) cudaFree(p);
   void *hosts[] = {c->h_nodes, c->h_t64, c->h_tff, c->h_sched, c->h_nlev, c->h_len, c->h_pi, c->h_al};
@@ -532,7 +536,7 @@ extern "C" int ima_gpu_set_chains(ima_ctx *c, int nruns, int chains_per_run)
   }
   // placement of every chain-locus
   c->items.resize(c->nitems);
-  size_t nodes = 0, sched = 0, al = 0, part = 0, part64 = 0;
+  size_t nodes = 0, sched = 0, al = 0, part = 0, part64 = 0, iss = 0;
   for (int ci = 0; ci < c->nchains; ci++)
     for (int li = 0; li < c->nloci; li++) {
       const LocusDev &L = ld[li];
@@ -546,6 +550,8 @@ extern "C" int ima_gpu_set_chains(ima_ctx *c, int nruns, int chains_per_run)
       it.dl_off = (int)al;
       it.part_off = (long long)part;
       it.part64_off = (long long)part64;
+      it.is_off = (long long)iss;
+      if (L.model == IMA_MODEL_IS) iss += (size_t)L.nsites;
       nodes += nl;
       sched += 2 * L.n + 2;
       if (L.model == IMA_MODEL_SW) al += (size_t)L.nlinked * nl;
@@ -591,13 +597,16 @@ extern "C" int ima_gpu_set_chains(ima_ctx *c, int nruns, int chains_per_run)
   c->d_used = dev_alloc<int32_t>(c->nruns, B, c->st);
   c->d_swap0ok = dev_alloc<int32_t>(c->nruns, B, c->st);
   c->d_ctr = dev_alloc<unsigned long long>(c->nruns, B, c->st);
+  c->d_is_site = dev_alloc<int32_t>(iss > 0 ? iss : 1, B, c->st);
+  c->d_is_valid = dev_alloc<uint8_t>(c->nitems, B, c->st);
   void *chk[] = {c->d_loci, c->d_seq, c->d_mult, c->d_sumlogk, c->d_items, c->d_nodes, c->d_t64,
                  c->d_tff, c->d_slot32, c->d_fresh32, c->d_sched, c->d_nlev, c->d_len, c->d_pi,
                  c->d_al, c->d_dlike, c->d_part, c->d_pexp, c->d_pdg, c->d_pdg_new, c->d_beta,
                  c->d_allbetas, c->d_probg, c->d_S, c->d_swapcount, c->d_tempcount, c->d_used,
-                 c->d_swap0ok, c->d_ctr};
+                 c->d_swap0ok, c->d_ctr, c->d_is_site, c->d_is_valid};
   for (void *p : chk)
     if (!p) return c->fail(IMA_ERR_NOMEM, "device allocation failed (%zu bytes so far)", B);
+  if (int r0 = c->cuda(cudaMemsetAsync(c->d_is_valid, 0, c->nitems, c->st), "IS site cache")) return r0;
   c->h_nodes = host_alloc<NodeRec>(nodes);
   c->h_t64 = host_alloc<double>(nodes);
   c->h_tff = host_alloc<float2>(nodes);
@@ -938,6 +947,8 @@ static int flush(ima_ctx *c)
   r = r ? r : c->cuda(cudaMemcpyAsync(c->d_len + lo, c->h_len + lo, (hi - lo + 1) * sizeof(double), cudaMemcpyHostToDevice, st), "length");
   r = r ? r : c->cuda(cudaMemcpyAsync(c->d_pi + 4 * (size_t)lo, c->h_pi + 4 * (size_t)lo, 4 * (hi - lo + 1) * sizeof(double), cudaMemcpyHostToDevice, st), "pi");
   if (a1 > a0) r = r ? r : c->cuda(cudaMemcpyAsync(c->d_al + a0, c->h_al + a0, (a1 - a0) * sizeof(int32_t), cudaMemcpyHostToDevice, st), "alleles");
+  // topologies may have changed: the IS site caches of the range are stale
+  r = r ? r : c->cuda(cudaMemsetAsync(c->d_is_valid + lo, 0, hi - lo + 1, st), "IS site cache");
   c->dirty_lo = INT32_MAX;
   c->dirty_hi = -1;
   return r;

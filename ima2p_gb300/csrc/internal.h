@@ -36,6 +36,7 @@ struct ItemDev {
   long long part64_off;    // HKY FP64: double index (x4 per pattern) of slot 0
   int al_off;              // SW: int32 [nlinked][2n-1] alleles
   int dl_off;              // SW: double [nlinked][2n-1] dlikeA
+  long long is_off;        // IS: int32 [S] per-site mutation branch cache
 };
 
 // One evaluation request (a chain-locus with its parameters).
@@ -63,6 +64,9 @@ struct Pools {
   const int32_t *alleles;
   double *dlike;            // SW per-branch terms
   double *sumlogk;          // IS per-locus constant
+  int32_t *is_site;         // IS: per item and site, (mutation node << 8) | branch (0 first daughter,
+                            // 1 second, 2 both at the root); node -1 none, -2 two
+  uint8_t *is_valid;        // IS: the item's site cache matches its topology
   double *pdg_new;          // last evaluated log P(D|G) per item
   // HKY state
   float4 *part;             // FP32 partials

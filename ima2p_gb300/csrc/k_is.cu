@@ -9,7 +9,10 @@
 // branch that carries the mutation.  Labels live in shared memory, laid out
 // [node][thread] so the walks of a warp hit distinct banks.  log(t*u) is
 // formed per site in FP64; the site terms are then added in site order by one
-// thread, so the FP64 sum has the reference's association.
+// thread, so the FP64 sum has the reference's association.  Each site's
+// mutation branch is cached per chain-locus and reused while its topology is
+// unchanged (the context clears the cache of every item whose topology it
+// uploads), so re-timing updates skip the labelling.
 #include "internal.h"
 
 namespace {
@@ -108,8 +111,24 @@ __global__ void __launch_bounds__(IS_BS) k_is(Pools P, const ReqDev *reqs, doubl
   __syncthreads();
   const int8_t *seq = P.seq + L.seq_off;
   int8_t *mut = s.mut + threadIdx.x;
+  // the labelling depends on the topology and the data only: while the
+  // item's topology is unchanged each site's mutation branch is read back
+  const bool cached = P.is_valid[R.item] != 0;
+  int32_t *cache = P.is_site + it.is_off;
   for (int site = threadIdx.x; site < S; site += IS_BS) {
-    int hit = label_site(s.nd, seq, n, S, site, mut);
+    int hit, br = 0;
+    if (cached) {
+      const int32_t code = cache[site];
+      hit = code >> 8;
+      br = code & 0xff;
+    } else {
+      hit = label_site(s.nd, seq, n, S, site, mut);
+      if (hit >= 0) {
+        const int a = s.nd[hit].up0, dn = s.nd[hit].down;
+        br = (dn < 0) ? 2 : (mut[dn * IS_BS] == mut[a * IS_BS]) ? 1 : 0;
+      }
+      cache[site] = (int32_t)(hit * 256 + br);
+    }
     int8_t st = SITE_OK;
     double v = 0.0;
     if (hit == -2) {
@@ -117,11 +136,10 @@ __global__ void __launch_bounds__(IS_BS) k_is(Pools P, const ReqDev *reqs, doubl
     } else if (hit == -1) {
       st = SITE_FAIL;
     } else {
-      int a = s.nd[hit].up0, b = s.nd[hit].up1;
+      const int a = s.nd[hit].up0, b = s.nd[hit].up1;
       double t;
-      int dn = s.nd[hit].down;
-      if (dn < 0) t = branch64(s.nd, s.t, a) + branch64(s.nd, s.t, b);
-      else if (mut[dn * IS_BS] == mut[a * IS_BS]) t = branch64(s.nd, s.t, b);
+      if (br == 2) t = branch64(s.nd, s.t, a) + branch64(s.nd, s.t, b);
+      else if (br == 1) t = branch64(s.nd, s.t, b);
       else t = branch64(s.nd, s.t, a);
       v = log(t * R.u);
     }
@@ -131,6 +149,7 @@ __global__ void __launch_bounds__(IS_BS) k_is(Pools P, const ReqDev *reqs, doubl
   }
   __syncthreads();
   if (threadIdx.x == 0) {
+    if (!cached) P.is_valid[R.item] = 1;  // every site's entry is written (barrier above)
     double p = -P.length[R.item] * R.u;
     int code = IMA_EVAL_OK;
     for (int site = 0; site < S; site++) {

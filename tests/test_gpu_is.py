@@ -68,3 +68,38 @@ def test_is_incompatible_data_raises():
     with pytest.raises(api.ImaError) as e:
         ctx.likelihoodIS(0, 0, 1.0)
     assert e.value.code == api.IMA_ERR_DATA
+
+
+def test_site_cache_follows_topology_changes():
+    """Each site's mutation branch is cached per chain-locus while its
+    topology is unchanged: re-timed uploads reuse it, a new topology (single
+    or batched upload) replaces it.  Every evaluation of a sequence of
+    uploads -- same topology, new topologies (some incompatible with the
+    data), and back -- equals the oracle's labelling from scratch."""
+    rng = np.random.default_rng(11)
+    g0 = synth.two_pop_tree(rng, 8, 8, theta=5.0, mig=0.1, tsplit=1.0)
+    seq = synth.is_data(rng, g0, 1.5, min_sites=4)
+    others = [synth.two_pop_tree(rng, 8, 8, theta=5.0, mig=0.1, tsplit=1.0) for _ in range(3)]
+    seqs = [g0, synth.jitter_times(rng, g0, 0.3), others[0], synth.jitter_times(rng, others[0], 0.2),
+            synth.jitter_times(rng, g0, 0.2), others[1], others[2], synth.jitter_times(rng, g0, 0.1)]
+    ctx = ctx_with([("is", seq)], 1, 2)
+    _, slk, _ = O.is_sumlogk(seq, g0)
+    statuses = set()
+    for step, t in enumerate(seqs):
+        if step % 2 == 0:
+            ctx.set_genealogy(0, 0, t)
+            ctx.set_genealogy(1, 0, t)
+        else:
+            ctx.set_genealogies(np.array([0, 1]), np.array([0, 0]), np.concatenate([t.up0, t.up0]),
+                                np.concatenate([t.up1, t.up1]), np.concatenate([t.down, t.down]),
+                                np.concatenate([t.time, t.time]))
+        res, st = ctx.eval(np.array([0, 1]), np.array([0, 0]), np.array([1.0, 0.7]), precision=api.PREC_FP64)
+        for k, u in enumerate((1.0, 0.7)):
+            v, status, _ = O.is_likelihood(seq, t, t.length(), u, slk)
+            assert st[k] == status, (step, k)
+            statuses.add(int(status))
+            if status == 0:
+                assert abs(res[k] - v) <= 1e-13 * abs(v), (step, k)
+            elif res[k] == res[k]:  # rejected: the reject value; failed: NaN
+                assert res[k] == v
+    assert 0 in statuses
