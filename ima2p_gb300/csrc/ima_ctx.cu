@@ -2554,9 +2554,11 @@ extern "C" int ima_gpu_treeweight(ima_ctx *c, int ngen, const int32_t *node_off,
 
 // p(G) of groups of the last weights: group i = genealogies group_off[i] ..
 // group_end[i] (group_end null: group_off[i+1])
+// defer: no error check, no copies back and no synchronisation here (the
+// caller checks the error word after a later synchronisation)
 static int tree_prob_run(ima_ctx *c, int ngroups, const int32_t *group_off, const int32_t *group_end,
                          const double *pdg, const int32_t *group_tv, double *probg, double *q, double *m,
-                         float *rows, double **d_probg = nullptr)
+                         float *rows, double **d_probg = nullptr, bool defer = false)
 {
   if (!c->tw_ready || c->tw_ngen < 1) return c->fail(IMA_ERR_STATE, "call ima_gpu_treeweight first");
   if (ngroups < 1 || !group_off) return c->fail(IMA_ERR_ARG, "tree_prob: bad argument");
@@ -2614,13 +2616,13 @@ static int tree_prob_run(ima_ctx *c, int ngroups, const int32_t *group_off, cons
   else
     r = r ? r : c->cuda(cudaMemsetAsync(d_tv, 0, G * 4, c->st), "tree_prob groups");
   if (pdg) r = r ? r : c->cuda(cudaMemcpyAsync(d_pdg, pdg, G * 8, cudaMemcpyHostToDevice, c->st), "tree_prob pdg");
-  r = r ? r : c->cuda(cudaMemsetAsync(c->d_twerr, 0, 8, c->st), "tree_prob");
+  if (!defer) r = r ? r : c->cuda(cudaMemsetAsync(c->d_twerr, 0, 8, c->st), "tree_prob");
   if (r) return r;
   c->tp_ngroups = 0;
   c->launch(IMA_K_TREE_PROB, (double)c->tw_ngen * (h.T * 20 + h.M * 12), [&] { launch_tree_prob(a, h, c->st); });
   c->launches += 2;  // cells, parameters, final
   r = c->cuda(cudaGetLastError(), "tree_prob launch");
-  r = r ? r : tw_check_err(c, "tree_prob");
+  if (!defer) r = r ? r : tw_check_err(c, "tree_prob");
   if (r) return r;
   c->tp_rows = a.rows;
   c->tp_ngroups = ngroups;
@@ -2633,6 +2635,7 @@ static int tree_prob_run(ima_ctx *c, int ngroups, const int32_t *group_off, cons
   down(q, a.q, G * nth * 8);
   if (nmg) down(m, a.m, G * nmg * 8);
   if (rows) down(rows, a.rows, G * rowlen * 4);
+  if (defer) return r;
   return r ? r : c->cuda(cudaStreamSynchronize(c->st), "tree_prob");
 }
 
@@ -2978,7 +2981,7 @@ extern "C" int ima_gpu_rubber_band(ima_ctx *c, int nch, const int32_t *chains, c
 }
 
 static int chain_weights_run(ima_ctx *c, int nch, const int32_t *chains, const double *tvals, double *probg,
-                             double *q, double *m, double **d_probg)
+                             double *q, double *m, double **d_probg, bool defer = false)
 {
   int r = IMA_OK;
   const TwModel &h = c->h_tw;
@@ -3060,7 +3063,7 @@ static int chain_weights_run(ima_ctx *c, int nch, const int32_t *chains, const d
   if (lr < 0) return c->fail(IMA_ERR_TOO_LARGE, "treeweight: shared memory for %d events", P);
   c->launches += lr - 1;
   r = c->cuda(cudaGetLastError(), "weights launch");
-  r = r ? r : tw_check_err(c, "chain weights");
+  if (!defer) r = r ? r : tw_check_err(c, "chain weights");
   if (r) return r;
   dev_newer(c, nch, chains);  // the lengths of these items changed on the device
   c->tw_ngen = ni;
@@ -3077,8 +3080,8 @@ static int chain_weights_run(ima_ctx *c, int nch, const int32_t *chains, const d
     gend[k] = chains[k] * nl + nl;
   }
   std::vector<double> pg(nch);
-  return tree_prob_run(c, nch, goff.data(), gend.data(), nullptr, chains, probg ? probg : pg.data(), q, m, nullptr,
-                       d_probg);
+  return tree_prob_run(c, nch, goff.data(), gend.data(), nullptr, chains, (probg || defer) ? probg : pg.data(), q, m,
+                       nullptr, d_probg, defer);
 }
 
 extern "C" int ima_gpu_chain_weights(ima_ctx *c, int nch, const int32_t *chains, const double *tvals,
@@ -3107,7 +3110,9 @@ extern "C" int ima_gpu_changet_ry1_sweep(ima_ctx *c, int nch, const int32_t *cha
   int32_t *d_ch = nullptr;
   r = band_run(c, nch, chains, period, oldt, newt, t_u, t_d, 0, nullptr, false, &d_ch);
   double *d_pgnew = nullptr;
-  r = r ? r : chain_weights_run(c, nch, chains, tvals, nullptr, nullptr, nullptr, &d_pgnew);
+  // weights and p(G) run on while the host stages the likelihood requests;
+  // their error word is read once the likelihoods have synchronised
+  r = r ? r : chain_weights_run(c, nch, chains, tvals, nullptr, nullptr, nullptr, &d_pgnew, true);
   if (r) return r;
   // the chains' likelihoods (writes the per-item pdg_new pool)
   std::vector<int32_t> ci((size_t)nch * nl), li((size_t)nch * nl), st((size_t)nch * nl);
@@ -3119,6 +3124,7 @@ extern "C" int ima_gpu_changet_ry1_sweep(ima_ctx *c, int nch, const int32_t *cha
       if (kappa) kap[(size_t)k * nl + l] = kappa[(size_t)k * nl + l];
     }
   r = ima_gpu_eval(c, nch * nl, ci.data(), li.data(), u, kap.data(), nullptr, nullptr, precision, res.data(), st.data());
+  r = r ? r : tw_check_err(c, "chain weights / p(G)");
   if (r) return r;
   for (size_t k = 0; k < st.size(); k++)
     if (st[k] == IMA_EVAL_IS_FAIL)
