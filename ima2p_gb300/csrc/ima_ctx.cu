@@ -20,6 +20,7 @@
 #include <condition_variable>
 #include <mutex>
 #include <atomic>
+#include <exception>
 #include <chrono>
 #include <thread>
 
@@ -1970,7 +1971,12 @@ extern "C" int ima_gpu_findmarginpeaks(ima_ctx *c, const double *theta_min, cons
     }
     return IMA_OK;
   };
-  const int r = findmarginpeaks_run(in, eval, out);
+  int r;
+  try {
+    r = findmarginpeaks_run(in, eval, out);
+  } catch (const std::exception &e) {  // host allocation of the search state
+    return c->fail(IMA_ERR_NOMEM, "findmarginpeaks: %s", e.what());
+  }
   if (rounds) *rounds = out.rounds;
   if (r == -1) return c->fail(IMA_ERR_DATA, "a peak search did not end in 20000 rounds");
   return r;
