@@ -623,6 +623,7 @@ __global__ void __launch_bounds__(128) k_tp_final(TwProbArgs a)
 // daughter edge, as the reference counts them) and the item's length is
 // saved; going back (o and n exchanged by the caller) the length is restored.
 constexpr int BAND_WPB = 8;  // chain-loci (warps) per block
+constexpr int RY_STAGE_MAX = 3000;  // loci staged in shared memory (48 KB of rows)
 
 __global__ void __launch_bounds__(32 * BAND_WPB) k_band(BandArgs a)
 {
@@ -701,15 +702,31 @@ __global__ void k_band_sum(const int32_t *item_counts, int nch, int nloci, int32
 // beta tpw + (ecd + emd) log(t_d ratio) + (ecu + emu) log(t_u ratio) with
 // the node counts halved, and log U < DMIN(1, term) -- NaN rejects, as the
 // reference's comparison does.
+// One block per chain: the chain's old and new likelihood rows are staged in
+// shared memory with coalesced loads, then one thread adds them in locus
+// order (the reference's association) and decides.
 __global__ void k_ry_decide(RyArgs a)
 {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  extern __shared__ double rowbuf[];  // [2][nloci] when staged
+  const int c = blockIdx.x;
   if (c >= a.nch) return;
   const int ci = a.chains[c];
+  const double *pn = a.pdg_new + (size_t)ci * a.nloci, *po = a.pdg + (size_t)ci * a.nloci;
+  const bool staged = a.nloci <= RY_STAGE_MAX;
+  if (staged) {
+    for (int li = threadIdx.x; li < a.nloci; li += blockDim.x) {
+      rowbuf[li] = pn[li];
+      rowbuf[a.nloci + li] = po[li];
+    }
+    __syncthreads();
+    pn = rowbuf;
+    po = rowbuf + a.nloci;
+  }
+  if (threadIdx.x != 0) return;
   double snew = 0.0, sold = 0.0;
   for (int li = 0; li < a.nloci; li++) {
-    snew += a.pdg_new[(size_t)ci * a.nloci + li];
-    sold += a.pdg[(size_t)ci * a.nloci + li];
+    snew += pn[li];
+    sold += po[li];
   }
   const int ecd = a.counts[4 * c] / 2, ecu = a.counts[4 * c + 1] / 2, emd = a.counts[4 * c + 2],
             emu = a.counts[4 * c + 3];
@@ -747,7 +764,8 @@ int launch_band(const BandArgs &a, cudaStream_t st)
 int launch_ry_decide(const RyArgs &a, cudaStream_t st)
 {
   if (a.nch < 1) return 0;
-  k_ry_decide<<<(a.nch + 127) / 128, 128, 0, st>>>(a);
+  const size_t sm = a.nloci <= RY_STAGE_MAX ? 2 * sizeof(double) * (size_t)a.nloci : 0;
+  k_ry_decide<<<a.nch, 128, sm, st>>>(a);
   return 0;
 }
 
