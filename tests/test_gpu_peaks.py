@@ -67,3 +67,26 @@ def test_too_few_genealogies_and_no_terms():
     with pytest.raises(api.ImaError):  # a term outside the parameters
         ctx.findmarginpeaks(np.zeros(3), GOLD["qmax"], np.zeros(2), GOLD["mmax"], terms=[(0, 2)])
     ctx.close()
+
+
+def test_prior_minima_against_the_oracle():
+    """Non-zero prior minima: marginp is off-scale below them as above the
+    maxima, which moves the brackets; the device's searches against the
+    oracle's (pinned to the reference on the golden cases)."""
+    from oracle import pyoracle as O
+    rows = GOLD["interior_rows"]
+    tmin, mmin = np.array([0.5, 1.0, 2.0]), np.array([0.05, 0.3])
+    want = O.findmarginpeaks(rows, 3, 2, tmin, GOLD["qmax"], mmin, GOLD["mmax"], terms=GOLD["terms"])
+    ctx = api.Context(0)
+    ctx.surface_load(rows, 3, 2, 2)
+    got = ctx.findmarginpeaks(tmin, GOLD["qmax"], mmin, GOLD["mmax"], terms=GOLD["terms"])
+    ctx.close()
+    assert np.array_equal(got["peakloc"] < 0, want["peakloc"] < 0)
+    ok = want["peakloc"] >= 0
+    np.testing.assert_allclose(got["peakloc"][ok], want["peakloc"][ok], rtol=1e-5)
+    np.testing.assert_allclose(got["mlval"][ok], want["mlval"][ok], rtol=1e-9)
+    np.testing.assert_allclose(got["migtest"], want["migtest"], rtol=0, atol=1e-6)
+    fin = ~np.isnan(want["lo95"])
+    np.testing.assert_allclose(got["lo95"][fin], want["lo95"][fin], rtol=0, atol=1e-4)
+    np.testing.assert_allclose(got["hi95"][fin], want["hi95"][fin], rtol=0, atol=1e-4)
+    np.testing.assert_allclose(got["pm_peakloc"], want["pm_peakloc"], rtol=1e-5)

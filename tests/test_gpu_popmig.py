@@ -110,3 +110,19 @@ def test_bad_requests_are_refused():
     y = ctx.popmig([0], [0], [0.7], GOLD["qmax"], GOLD["mmax"])  # still usable
     assert np.isfinite(y[0])
     ctx.close()
+
+
+def test_likelihood_curves_under_both_priors():
+    """popmig_curves with prob_or_like = 1 (each density divided by the prior
+    density of 2NM), uniform and exponential migration priors, against the
+    oracle on the curve the device chose."""
+    rows = GOLD["rows"]
+    ctx = _ctx(rows)
+    q, m, mean = GOLD["qmax"], GOLD["mmax"], GOLD["mean"]
+    for mig_mean in (None, mean):
+        xs, ys, mx = ctx.popmig_curves([(0, 0), (2, 1)], q, m, mig_mean=mig_mean, prob_or_like=1, gridsize=40)
+        for t, (ti, mj) in enumerate([(0, 0), (2, 1)]):
+            ref = [O.popmig(rows, 3, 2, ti, mj, v, q[ti], m[mj], mmean=None if mig_mean is None else mean[mj],
+                            prob_or_like=1) for v in xs[t]]
+            np.testing.assert_allclose(ys[t], ref, rtol=RTOL_GRID)
+    ctx.close()
