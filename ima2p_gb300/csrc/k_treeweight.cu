@@ -68,8 +68,9 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_tw_events(TwArgs a, int wpb)
 {
   extern __shared__ __align__(16) unsigned char sm[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int g = blockIdx.x * wpb + warp;
-  if (g >= a.ngen) return;  // whole warps only
+  const int slot = blockIdx.x * wpb + warp;
+  if (slot >= a.ngen) return;  // whole warps only
+  const int g = a.perm[slot];  // the selected genealogies, most events first
   const TwModel &M = *a.model;
   const int npops = M.npops, nsplit = npops - 1, ntp = 2 * npops - 1;
   unsigned char *base = sm + (size_t)warp * a.P * 12;

@@ -283,3 +283,22 @@ def test_checkpoint_resume_continues_the_run(tmp_path):
         with pytest.raises(api.ImaError):
             ctx.checkpoint_read(bad)
     ctx.close()
+
+
+def test_chain_weights_on_a_subset_of_chains():
+    """ima_gpu_chain_weights on chains given in any order and any subset:
+    each chain's p(G) and integrals equal the all-chain call's."""
+    case = RyCase()
+    ctx = _resident_context(case)
+    splittime.ResidentChainSet(ctx, case.fresh_gens(), [case.d["tv0"]] * case.nch, case.betas,
+                               np.ones(case.nl), case.samps, case.us)
+    tv = np.array([case.d["tv0"]] * case.nch, np.float64).reshape(case.nch, -1)
+    allc = np.arange(case.nch, dtype=np.int32)
+    p_all, q_all, m_all = ctx.chain_weights(allc, tv)
+    for sub in ([case.nch - 1], [2, 0], [1]):
+        sub = np.array(sub, np.int32)
+        p, q, m = ctx.chain_weights(sub, tv[sub])
+        assert np.array_equal(p, p_all[sub])
+        assert np.array_equal(q, q_all[sub])
+        assert np.array_equal(m, m_all[sub])
+    ctx.close()
