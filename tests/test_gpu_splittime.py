@@ -302,3 +302,53 @@ def test_chain_weights_on_a_subset_of_chains():
         assert np.array_equal(q, q_all[sub])
         assert np.array_equal(m, m_all[sub])
     ctx.close()
+
+
+def test_library_drawn_sweep_of_one_chain():
+    """ima_gpu_changet_ry1_sweep_mt on a subset of the chains (chain 1 alone,
+    12 updates): each decision, split time, p(G) and likelihood sum equals the
+    oracle-driven changet_RY1 of that chain with the same generator, the
+    chain's final node and migration times are the oracle's, and the other
+    chains' genealogies and split times are untouched."""
+    from tests._splittime import OracleBackend
+    case = RyCase()
+    ctx = _resident_context(case)
+    splittime.ResidentChainSet(ctx, case.fresh_gens(), [case.d["tv0"]] * case.nch, case.betas,
+                               np.ones(case.nl), case.samps, case.us)
+    base = case.fresh_gens()
+    before = {(ci, li): ctx.get_times(ci, li, len(base[ci][li].pop)) for ci in range(case.nch) for li in range(case.nl)}
+    tv0 = ctx.get_split_times().copy()
+    backend = OracleBackend(case)
+    g0 = case.fresh_gens()[0]  # sum log k! comes from chain 0's genealogies, evaluated first
+    backend.likelihoods(0, g0, backend.weights(0, g0, np.array(case.d["tv0"], np.float64))[0])
+    gens = case.fresh_gens()[1]
+    tv = np.array(case.d["tv0"], np.float64)
+    lens, probg = backend.weights(1, gens, tv)
+    pdg = np.asarray(backend.likelihoods(1, gens, lens), np.float64)
+    s = 0.0
+    for v in pdg:
+        s += float(v)
+    state = splittime.ChainState(tv, float(case.betas[1]), gens, pdg, s, probg)
+    rng_o, rng_g = api.MT19937(case.seed), api.MT19937(case.seed)
+    periods = [k for ci, k in case.steps if ci == 1][:12]
+    for k in periods:
+        acc_o = splittime.changet_ry1(state, 1, k, rng_o, case.tprior, case.nl, case.npops, backend)
+        acc, pdgsum, pg, newt = ctx.changet_ry1_sweep_mt(np.array([1], np.int32), np.array([k]), case.tprior, rng_g,
+                                                       np.asarray(case.us, np.float64))
+        assert bool(acc[0]) == acc_o
+        assert ctx.get_split_times()[1, k] == state.tvals[k]
+        assert abs(pg[0] - state.probg) <= 1e-10
+        assert abs(pdgsum[0] - state.pdgsum) <= 1e-12 * abs(state.pdgsum)
+    tv_now = ctx.get_split_times()
+    assert np.array_equal(np.delete(tv_now, 1, axis=0), np.delete(tv0, 1, axis=0))
+    for ci in range(case.nch):
+        for li in range(case.nl):
+            t, m = ctx.get_times(ci, li, len(base[ci][li].pop))
+            edge = base[ci][li].g.down != -1
+            if ci == 1:
+                lg = state.gens[li]
+                assert np.array_equal(t[edge], lg.g.time[edge])
+                assert np.array_equal(m, np.array([e[0] for mm in lg.mig for e in mm]))
+            else:
+                assert np.array_equal(t, before[(ci, li)][0]) and np.array_equal(m, before[(ci, li)][1])
+    ctx.close()
