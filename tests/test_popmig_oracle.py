@@ -33,3 +33,20 @@ def test_fixture_reaches_every_branch():
     assert ((mc0 == 0) & (fm0 == 0) & (fc0 > 0)).any()          # no migrations
     assert ((rows[:, 1] == 0) & (rows[:, 4] == 0) & (rows[:, 10] == 0) & (rows[:, 12] == 0)).any()  # neither
     assert (GOLD["ref"] < 0).any()  # x beyond theta_max * m_max / 2: the likelihood's prior term turns negative
+
+
+def test_popmig_terms_follow_the_parameter_names():
+    """popmodel.popmig_terms: for every population but the root, each
+    migration parameter whose name starts with it, in (thetai, mi) order, as
+    print_populationmigrationrate_histograms picks them
+    (histograms.cpp:754-773)."""
+    from ima2p_gb300 import popmodel
+    pm = popmodel.build("(0,1):2", 2)
+    assert [(t, m) for t, m, _ in popmodel.popmig_terms(pm)] == [(0, 0), (1, 1)]
+    pm = popmodel.build("((0,1):3,2):4", 3)
+    terms = popmodel.popmig_terms(pm)
+    assert [(t, m) for t, m, _ in terms] == [(0, 0), (0, 2), (1, 1), (1, 4), (2, 3), (2, 5), (2, 6), (3, 7)]
+    for t, m, label in terms:
+        src = int(pm.mg_names[m][1:].split(">")[0])
+        assert src == t and t < 2 * pm.npops - 2 and label == "2N%d%s" % (t, pm.mg_names[m])
+    assert all(any(m == mm for _, mm, _ in terms) for m in range(len(pm.mg_names)))
