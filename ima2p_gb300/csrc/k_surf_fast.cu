@@ -11,10 +11,13 @@
 // float-float phi) and enter an online log-sum-exp whose sum is kept in
 // float-float.  A skipped term weighs < e^-MARGIN of the maximum.
 //
-// The per-point threshold is shared by every thread of the CTA (shared-memory
-// atomicMax of the running maxima) and seeded with the exact maximum over a
-// sample of genealogies, so it is tight from the first tile; candidates of a
-// warp are drained with a ballot loop, one per lane per pass.
+// The per-point threshold is shared by every thread of the CTA and seeded
+// with the exact maximum over a sample of genealogies, so it is tight from
+// the first tile; candidates of a warp are drained with a ballot loop, one per
+// lane per pass.  Maxima found during a tile go to a second array that is
+// folded into the thresholds between tiles, so a tile's thresholds depend
+// only on the earlier tiles: the candidate set, each thread's fold order and
+// so the result are the same on every run.
 //
 // Screens: FP32 FMA on CUDA cores (this file) and a bf16 tcgen05 GEMM
 // (k_surf_tc.cu).  Partial (max, sum) per point and genealogy chunk are
@@ -44,7 +47,8 @@ __global__ void __launch_bounds__(BS) k_surf_screen_fp32(SurfPrep S, int npoints
   __shared__ __align__(16) float sS[SURF_KP][TG];      // statistics, genealogy-contiguous
   __shared__ __align__(16) float2 sPff[TP][SURF_K + 1];
   __shared__ float sOff[TP];                           // margin + screening error bound
-  __shared__ unsigned sBest[TP];                       // best known maximum per point
+  __shared__ unsigned sBest[TP];                       // best known maximum per point (this tile's thresholds)
+  __shared__ unsigned sBestNext[TP];                   // maxima found during the current tile
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int p0 = blockIdx.x * TP;
   const int g0 = blockIdx.y * chunk, g1 = min(S.G, g0 + chunk);
@@ -60,6 +64,7 @@ __global__ void __launch_bounds__(BS) k_surf_screen_fp32(SurfPrep S, int npoints
     bool ok = p0 + p < npoints;
     sOff[p] = ok ? FP32_SCREEN_ERR * S.mag[p0 + p] + SURF_MARGIN : 0.f;
     sBest[p] = f2ord(ok ? S.seed[p0 + p] : -INFINITY);
+    sBestNext[p] = sBest[p];
   }
   __syncthreads();
   LseState st[4];
@@ -68,6 +73,8 @@ __global__ void __launch_bounds__(BS) k_surf_screen_fp32(SurfPrep S, int npoints
   for (int t0 = g0; t0 < g1; t0 += TG) {
     const int nt = min(TG, g1 - t0);
     __syncthreads();
+    // every drain of the previous tile is done: its maxima become thresholds
+    for (int p = tid; p < TP; p += BS) sBest[p] = sBestNext[p];
     for (int k = tid; k < SURF_KP * TG; k += BS) {
       int kk = k / TG, g = k % TG;
       sS[kk][g] = (g < nt) ? S.sT[(size_t)kk * S.Gpad + t0 + g] : 0.0f;
@@ -112,7 +119,7 @@ __global__ void __launch_bounds__(BS) k_surf_screen_fp32(SurfPrep S, int npoints
           if (jj == j) {
             float before = st[jj].m.hi;
             st[jj].add(y);
-            if (st[jj].m.hi > before) atomicMax(&sBest[pl], f2ord(st[jj].m.hi));
+            if (st[jj].m.hi > before) atomicMax(&sBestNext[pl], f2ord(st[jj].m.hi));
           }
       }
     }

@@ -9,28 +9,36 @@
 // significant bits per product, so few terms reach the exact recomputation.
 //
 // One CTA owns 128 points (the A operand, loaded once) and streams tiles of
-// 128 genealogies (the B operand) through an 8-stage shared-memory ring
+// 256 genealogies (the B operand) through a 4-stage shared-memory ring
 // filled by 1-D bulk copies (the TMA engine; the prepared operand is already
 // in the tile layout, so one copy per tile).  Warp roles:
 //   warp 0     one thread issues the bulk copies;
-//   warp 1     one thread issues six K=16 MMAs per tile into one of four
-//              128-column TMEM accumulators, so it can run three tiles ahead
-//              of the slowest draining warp;
+//   warp 1     one thread issues six K=16 MMAs per tile into one of two
+//              256-column TMEM accumulators;
 //   warps 4-19 drain the accumulators with tcgen05.ld -- warp w reads TMEM
-//              lane quarter w % 4 (32 points, one per thread) and 32
-//              genealogy columns -- and a max tree over each thread's 32
-//              values decides whether any lies within MARGIN + screen error
-//              of the point's best maximum; such candidates go to a ring;
+//              lane quarter w % 4 (32 points, one per thread) and 64
+//              genealogy columns -- and a max tree over each thread's values
+//              decides whether any lies within MARGIN + screen error of the
+//              point's lower bound; such candidates go to a ring;
 //   warps 2-3  take the rings' candidates 32 at a time, recompute them
 //              exactly (phi of every point is staged in shared memory) and
-//              fold them into per-point log-sum-exp states.
-// The drain never waits for the exact recomputation, so one warp's
-// candidates do not hold the accumulator.  The threshold is a lower bound on
-// the point's maximum less MARGIN and the screen error: a screened value less
-// its error bound is such a lower bound, so the threshold is tight from the
-// first tile without any exact work, and exact values raise it further.  The
-// bound is shared by the warps of the CTA (shared memory) and by all
-// genealogy chunks of the point (global memory).
+//              add exp(p - ref) to the point's sums.
+//
+// Results are bit-for-bit reproducible.  Two things would otherwise follow
+// timing: which terms pass the screen, and the order in which they are added.
+//   * The set: a drain warp's threshold is the point's lower bound from the
+//     max-only pre-pass (a maximum over a fixed set of values, so fixed) raised
+//     only by the screened maxima of the warp's own earlier tiles.  Nothing
+//     another warp or chunk found moves it, so every warp screens the same
+//     terms on every run.
+//   * The order: each term's weight w = exp(p - ref), with ref the pre-pass
+//     bound, is added as a 192-bit fixed-point integer (w * 2^64) by 64-bit
+//     shared-memory atomics with exact carries.  Integer addition is
+//     associative, so the sum does not depend on arrival order; the chunk
+//     sums are merged in chunk order.
+// A term with w >= 2^48 (the pre-pass bound more than 33 nats below the
+// term) would leave the fixed-point range: the point is flagged and its log
+// density is taken again in FP64 over every genealogy (k_surf_tc_exact).
 //
 // Every wait is bounded: a wait that runs out sets the error word, the CTA
 // stops issuing work, waits (bounded) for the copies and MMAs it started,
@@ -86,11 +94,63 @@ struct TcSmem {
   int epi_done;                       // epilogue warps that have finished
   unsigned head[REF_WARPS];           // slots reserved so far in each ring
   int ring[REF_WARPS][RING];          // candidates: genealogy << 7 | point; -1 = free
-  float2 res[REF_WARPS][32];          // exact values of one batch
-  SurfPart lse[TC_M];                 // log-sum-exp state per point
-  unsigned best[TC_M];                // best lower bound on the point's maximum (ordered bits)
+  unsigned long long sum[TC_M][3];    // sum of w * 2^64, w = exp(p - ref), 192-bit fixed point
+  unsigned long long sum2[TC_M][3];   // sum of w^2 * 2^64
+  float ref[TC_M];                    // the point's lower bound after the pre-pass
+  int ovf[TC_M];                      // a term left the fixed-point range
   float2 phi[TC_M * PHI_STRIDE];      // float-float phi of the CTA's points
 };
+
+// w >= 2^48 (33.27 nats above ref) leaves the range the sums are sized for:
+// 2^24 genealogies of w^2 * 2^64 < 2^96 * 2^64 stay below 2^184
+constexpr double OVF_NATS = 33.0;
+
+// w * 2^64 as a 192-bit integer, truncated (0 <= w < 2^128)
+__device__ __forceinline__ void fix192(double w, unsigned long long o[3])
+{
+  o[0] = o[1] = o[2] = 0ull;
+  const unsigned long long b = (unsigned long long)__double_as_longlong(w);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (!(w > 0.0) || e == 0) return;  // zero or subnormal: nothing at this scale
+  const unsigned long long m = (b & 0xfffffffffffffull) | (1ull << 52);
+  const int s = e - 1023 - 52 + 64;  // w * 2^64 = m * 2^s
+  if (s <= -53) return;
+  if (s < 0) {
+    o[0] = m >> (-s);
+    return;
+  }
+  const int wd = s >> 6, bit = s & 63;
+  if (wd < 3) o[wd] = m << bit;
+  if (bit && wd + 1 < 3) o[wd + 1] = m >> (64 - bit);
+}
+
+// acc += x on a 192-bit integer in shared memory, word by word with 64-bit
+// atomics; a word that wraps carries one into the next.  Every wrap is seen
+// by exactly one atomic, so the sum is exact whatever the interleaving.
+__device__ __forceinline__ void atomic_add192(unsigned long long *acc, const unsigned long long x[3])
+{
+  unsigned long long carry = 0ull;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    unsigned long long out = 0ull;
+    if (x[i]) {
+      const unsigned long long old = atomicAdd(&acc[i], x[i]);
+      out += (old + x[i] < old) ? 1ull : 0ull;
+    }
+    if (carry) {
+      const unsigned long long old = atomicAdd(&acc[i], carry);
+      out += (old + carry < old) ? 1ull : 0ull;
+    }
+    carry = out;
+  }
+}
+
+__device__ __forceinline__ double fix192_to_double(const unsigned long long w[3])
+{
+  // 2^128, 2^64 and 2^-64 are exact; the order of the two additions is fixed
+  return ((double)w[2] * 3.4028236692093846e38 + (double)w[1] * 18446744073709551616.0 + (double)w[0]) *
+         5.421010862427522e-20;
+}
 
 __device__ __forceinline__ void set_err(int *err_shared, int *err_global, int code)
 {
@@ -116,11 +176,9 @@ __device__ __forceinline__ void push_candidate(TcSmem &sh, int *gerr, int pl, in
 }
 
 // Refine warp r: takes its ring's candidates 32 at a time, recomputes each
-// exactly (one per lane) and folds it into its point's log-sum-exp state --
-// lanes holding the same point form a group whose lowest lane folds the
-// group's values.  It stops when every epilogue warp has finished and the
-// ring is drained.
-__device__ void refine_loop(const SurfPrep &S, TcSmem &sh, int *gerr, int r, int lane, int ptile, int npoints)
+// exactly (one per lane) and adds its weight to its point's sums.  It stops
+// when every epilogue warp has finished and the ring is drained.
+__device__ void refine_loop(const SurfPrep &S, TcSmem &sh, int *gerr, int r, int lane)
 {
   for (unsigned next = 0;; next += 32) {
     const unsigned slot = next + lane;
@@ -138,44 +196,32 @@ __device__ void refine_loop(const SurfPrep &S, TcSmem &sh, int *gerr, int r, int
       __nanosleep(64);
     }
     const bool have = e != -1;
-    int owner = TC_M + lane;  // unique dummy for idle lanes
     if (have) {
       *src = -1;
-      owner = e & (TC_M - 1);
-      const int g = e >> 7;
-      ff y = surf_exact(S, g, S.sT + g, S.Gpad, &sh.phi[owner * PHI_STRIDE]);
-      sh.res[r][lane] = make_float2(y.hi, y.lo);
-    }
-    __syncwarp();
-    const unsigned grp = __match_any_sync(0xffffffffu, owner);
-    if (have && lane == __ffs(grp) - 1) {
-      LseState L;
-      L.unpack(sh.lse[owner]);
-      const float b0 = ord2f(*(volatile unsigned *)&sh.best[owner]);
-      float b = b0;
-      for (unsigned m = grp; m; m &= m - 1) {
-        const float2 v = sh.res[r][__ffs(m) - 1];
-        L.add(ff_make(v.x, v.y));
-        b = fmaxf(b, v.x);
-      }
-      sh.lse[owner] = L.pack();
-      // publish an improved maximum to the drain and the other chunks
-      if (b > b0) {
-        atomicMax(&sh.best[owner], f2ord(b));
-        atomicMax(&S.best[ptile * TC_M + owner], f2ord(b));
+      const int pl = e & (TC_M - 1), g = e >> 7;
+      const ff y = surf_exact(S, g, S.sT + g, S.Gpad, &sh.phi[pl * PHI_STRIDE]);
+      const double d = ((double)y.hi - (double)sh.ref[pl]) + (double)y.lo;
+      if (d > OVF_NATS) {
+        sh.ovf[pl] = 1;
+      } else {
+        const double w = exp(d);
+        unsigned long long x[3];
+        fix192(w, x);
+        atomic_add192(sh.sum[pl], x);
+        fix192(w * w, x);
+        atomic_add192(sh.sum2[pl], x);
       }
     }
-    __syncwarp();
     if (!__any_sync(0xffffffffu, have)) break;
   }
-  (void)npoints;
 }
 
 // stride > 0: max-only pass over genealogy tiles 0, stride, 2 stride, ...
-// that only raises the shared per-point lower bounds (no candidates, no
-// partials); stride == 0: the full pass over every tile.
+// that only raises the per-point lower bounds S.best (no candidates, no
+// partials); stride == 0: the full pass over every tile, which reads S.best
+// and leaves it unchanged.
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    k_surf_tc(SurfPrep S, int npoints, int tiles_per_chunk, int stride, SurfPart *part, int *gerr)
+    k_surf_tc(SurfPrep S, int npoints, int tiles_per_chunk, int stride, double2 *part, int *gerr)
 {
   extern __shared__ __align__(1024) char smem[];
   char *bufA = smem;
@@ -208,11 +254,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   }
   for (int i = threadIdx.x; i < REF_WARPS * RING; i += TC_THREADS) (&sh.ring[0][0])[i] = -1;
   for (int pl = threadIdx.x; pl < TC_M; pl += TC_THREADS) {
-    LseState L;
-    L.init();
-    sh.lse[pl] = L.pack();
+    for (int w = 0; w < 3; w++) sh.sum[pl][w] = sh.sum2[pl][w] = 0ull;
     const int p = ptile * TC_M + pl;
-    sh.best[pl] = p < npoints ? S.best[p] : f2ord(-INFINITY);
+    sh.ref[pl] = p < npoints ? ord2f(S.best[p]) : -INFINITY;
+    sh.ovf[pl] = 0;
   }
   if (warp == 1) {
     tc::tmem_alloc(&sh.tmem, 512);
@@ -280,7 +325,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (ndone > 0) tc::mbar_wait(&sh.done[(ndone - 1) % TC_STAGES], ((ndone - 1) / TC_STAGES) & 1, WAIT_LIMIT);
   } else if ((warp == 2 || warp == 3) && !maxonly) {
     // ------------------------------------------------------------ refine
-    refine_loop(S, sh, gerr, warp - 2, lane, ptile, npoints);
+    refine_loop(S, sh, gerr, warp - 2, lane);
   } else if (warp >= 4) {
     // ---------------------------------------------------------- epilogue
     const int ew = warp - 4;            // epilogue warp
@@ -291,11 +336,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const bool live = p < npoints;
     const float err = live ? BF16_SCREEN_ERR * S.mag[p] : 0.f;  // screen error bound
     const float off = err + SURF_MARGIN;
-    // lb: a lower bound on the point's maximum -- exact values, and screened
-    // values less their error bound, from any warp of this CTA or any chunk
-    // (the global bound is read one tile ahead)
-    float lb = -INFINITY, published = -INFINITY;
-    unsigned pending = live ? *(volatile unsigned *)&S.best[p] : 0u;
+    // lb: a lower bound on the point's maximum -- the pre-pass bound raised
+    // by this warp's own screened values less their error bound, in tile
+    // order, so the threshold of every tile is the same on every run
+    float lb = live ? sh.ref[pl] : -INFINITY;
     for (int i = 0; i < ntiles; i++) {
       const int a = i % NACC;
       if (!tc::mbar_wait(&sh.done[i % TC_STAGES], (i / TC_STAGES) & 1, WAIT_LIMIT)) {
@@ -303,11 +347,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         break;
       }
       tc::fence_after_sync();
-      if (live) {
-        lb = fmaxf(lb, ord2f(pending));
-        pending = *(volatile unsigned *)&S.best[p];
-        lb = fmaxf(lb, ord2f(*(volatile unsigned *)&sh.best[pl]));
-      }
       const int gbase = (t0 + i) * step * TC_N + cg * GROUP_COLS;
       const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * TC_N + cg * GROUP_COLS);
       float mxv;
@@ -350,11 +389,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       if (gbase + GROUP_COLS <= S.G) lb = fmaxf(lb, mxv - err);
       const float thr = lb - off;
       const bool hit = live && !maxonly && mxv > thr;
-      if (live && lb > published) {
-        published = lb;
-        atomicMax(&sh.best[pl], f2ord(lb));
-        atomicMax(&S.best[p], f2ord(lb));
-      }
       if (__any_sync(0xffffffffu, hit)) {
 #pragma unroll 1
         for (int c = 0; c < GROUP_COLS / 32; c++) {
@@ -373,6 +407,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&sh.accempty[a]);
     }
+    // the pre-pass publishes its bound once: a maximum, whatever the order
+    if (maxonly && live) atomicMax(&S.best[p], f2ord(lb));
     __syncwarp();
     if (lane == 0) {
       __threadfence_block();
@@ -387,7 +423,73 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   }
   if (threadIdx.x < TC_M && !maxonly) {
     const int p = ptile * TC_M + threadIdx.x;
-    if (p < npoints) part[(size_t)p * gridDim.y + blockIdx.y] = sh.lse[threadIdx.x];
+    if (p < npoints)
+      part[(size_t)p * gridDim.y + blockIdx.y] =
+          make_double2(sh.ovf[threadIdx.x] ? -1.0 : fix192_to_double(sh.sum[threadIdx.x]),
+                       fix192_to_double(sh.sum2[threadIdx.x]));
+  }
+}
+
+// Chunk sums added in chunk order: q = ln G - (ref + ln sum).  A point with
+// a flagged chunk is left to k_surf_tc_exact.
+__global__ void k_surf_tc_merge(SurfArgs a, SurfPrep S, const double2 *part, int nchunks, int *flag)
+{
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.npoints) return;
+  const double2 *w = part + (size_t)p * nchunks;
+  double s = 0.0, s2 = 0.0;
+  int ovf = 0;
+  for (int c = 0; c < nchunks; c++) {
+    if (w[c].x < 0.0) ovf = 1;
+    s += w[c].x;
+    s2 += w[c].y;
+  }
+  flag[p] = ovf;
+  if (ovf) return;
+  const double ref = (double)ord2f(S.best[p]);
+  a.q[p] = log((double)a.G) - (ref + log(s));
+  if (a.ess) a.ess[p] = s * s / s2;
+}
+
+// The flagged points in FP64 over every genealogy, a warp per point: the
+// maximum, then the sums of exp(p - max), lanes over genealogies and a fixed
+// shuffle tree, so these too are reproducible.
+__global__ void k_surf_tc_exact(SurfArgs a, SurfPrep S, const int *flag)
+{
+  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (p >= a.npoints || !flag[p]) return;  // warp-uniform
+  double phi[SURF_K];
+#pragma unroll
+  for (int k = 0; k < SURF_K; k++) {
+    const float2 f = S.phiff[(size_t)p * SURF_K + k];
+    phi[k] = (double)f.x + (double)f.y;
+  }
+  auto term = [&](int g) {
+    const float2 b = S.biasff[g];
+    double v = (double)b.x + (double)b.y;
+#pragma unroll
+    for (int k = 0; k < SURF_K; k++)
+      if (k < S.K) v = fma((double)S.sT[(size_t)k * S.Gpad + g], phi[k], v);
+    return v;
+  };
+  double m = -INFINITY;
+  for (int g = lane; g < a.G; g += 32) m = fmax(m, term(g));
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  double s = 0.0, s2 = 0.0;
+  for (int g = lane; g < a.G; g += 32) {
+    const double e = exp(term(g) - m);
+    s += e;
+    s2 += e * e;
+  }
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    s += __shfl_xor_sync(0xffffffffu, s, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  }
+  if (lane == 0) {
+    a.q[p] = log((double)a.G) - (m + log(s));
+    if (a.ess) a.ess[p] = s * s / s2;
   }
 }
 
@@ -491,8 +593,9 @@ __global__ void k_tc_selftest_check(const float *D, int *bad, float *maxerr)
 // ---------------------------------------------------------------- host
 size_t surface_tc_scratch_bytes(int G, int npoints)
 {
-  const int nchunks = SURF_MAX_CHUNKS;
-  return surf_prep_bytes(G, npoints) + (size_t)npoints * nchunks * sizeof(SurfPart) + 1024;
+  // prepared operands | chunk sums (double2 per point and chunk) | flags
+  return surf_prep_bytes(G, npoints) + (size_t)npoints * SURF_MAX_CHUNKS * sizeof(double2) +
+         (size_t)npoints * sizeof(int) + 1024;
 }
 
 namespace {
@@ -531,7 +634,8 @@ int launch_surface_tc(const SurfArgs &a, void *scratch, size_t scratch_bytes, in
   if (scratch_bytes < surface_tc_scratch_bytes(a.G, a.npoints)) return 3;
   if (a.G >= (1 << 24)) return 4;  // candidate entries pack the genealogy index into 24 bits
   SurfPrep S;
-  SurfPart *part = surf_prep_carve(&S, static_cast<char *>(scratch), a.G, a.npoints);
+  double2 *part = reinterpret_cast<double2 *>(surf_prep_carve(&S, static_cast<char *>(scratch), a.G, a.npoints));
+  int *flag = reinterpret_cast<int *>(part + (size_t)a.npoints * SURF_MAX_CHUNKS);
   surf_prep(a, S, true, rows_ready, st);
   surf_seed(S, a.npoints, SEED_TC, st);
   const int ntiles = S.Gpad / TC_N;
@@ -553,8 +657,10 @@ int launch_surface_tc(const SurfArgs &a, void *scratch, size_t scratch_bytes, in
   if (pre) k_surf_tc<<<dim3(ptiles, nchunks), TC_THREADS, sm, st>>>(S, a.npoints, per, PRE_STRIDE, part, d_err);
   nchunks = surf_tc_chunks(ptiles, ntiles, nsm, &per);
   k_surf_tc<<<dim3(ptiles, nchunks), TC_THREADS, sm, st>>>(S, a.npoints, per, 0, part, d_err);
-  surf_merge(a, part, nchunks, st);
-  *nkernels = (rows_ready ? 0 : 1) + 4 + (pre ? 1 : 0);  // rows, points, seed, pre-pass, pass, merge
+  k_surf_tc_merge<<<(a.npoints + 127) / 128, 128, 0, st>>>(a, S, part, nchunks, flag);
+  k_surf_tc_exact<<<(a.npoints * 32 + 255) / 256, 256, 0, st>>>(a, S, flag);
+  // rows, points, seed, pre-pass, pass, merge, FP64 retake of flagged points
+  *nkernels = (rows_ready ? 0 : 1) + 5 + (pre ? 1 : 0);
   return 0;
 }
 

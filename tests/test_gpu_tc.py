@@ -39,11 +39,8 @@ def test_surface_tensor_core_screen_vs_oracle(mt):
 def test_surface_row_operands_reused_across_evaluations():
     """The row-derived operands are prepared once per (rows, model type) and
     reused; switching model type, method or point count, or reloading rows,
-    must give what a fresh context gives.  Two runs agree to ~4e-10, not
-    bitwise: the order in which candidates are folded depends on timing, and
-    each term's weight is an FP32 exponential taken against the running
-    maximum at that moment.  Stale operands would be off by far more than
-    the 1e-8 allowed here."""
+    must give what a fresh context gives, bit for bit: the screened candidate
+    set and the sums do not depend on timing."""
     rng = np.random.default_rng(77)
     rows, lognorm, off = synth.surface_stats(rng, 20000, 5, 8, 2)
     pts = synth.surface_points(rng, 400)
@@ -59,7 +56,7 @@ def test_surface_row_operands_reused_across_evaluations():
            (1, api.SURF_FP64, 50), (1, api.SURF_TC, 400), (2, api.SURF_FAST, 200), (1, api.SURF_TC, 100)]
     for mt, method, n in seq:
         q = ctx.surface_eval(pts[:n], modeltype=mt, method=method)[0]
-        np.testing.assert_allclose(q, fresh(mt, method, n), rtol=0, atol=1e-8, err_msg=str((mt, method, n)))
+        np.testing.assert_array_equal(q, fresh(mt, method, n), err_msg=str((mt, method, n)))
     # reloading other rows invalidates the prepared operands
     rows2 = rows.copy()
     rows2[:, off["fc"]] *= 1.5
@@ -67,4 +64,53 @@ def test_surface_row_operands_reused_across_evaluations():
     q = ctx.surface_eval(pts, modeltype=1, method=api.SURF_TC)[0]
     c2 = ctx_with([("sw", 2, 1)])
     c2.surface_load(rows2, 5, 8, 3, lognorm=None)
-    np.testing.assert_allclose(q, c2.surface_eval(pts, modeltype=1, method=api.SURF_TC)[0], rtol=0, atol=1e-8)
+    np.testing.assert_array_equal(q, c2.surface_eval(pts, modeltype=1, method=api.SURF_TC)[0])
+
+
+@pytest.mark.parametrize("method", [api.SURF_TC, api.SURF_FAST])
+def test_surface_repeat_calls_bitwise(method):
+    """The same points evaluated again give the same bits (densities and
+    effective sample sizes): neither which terms pass the screen nor the order
+    of their sums follows timing.  Enough genealogies for several chunks and
+    the max-only pre-pass.  With the points in another order each point's
+    density is unchanged."""
+    rng = np.random.default_rng(5)
+    rows, lognorm, _ = synth.surface_stats(rng, 70000, 5, 8, 2)
+    pts = synth.surface_points(rng, 700)
+    ctx = ctx_with([("sw", 2, 1)])
+    ctx.surface_load(rows, 5, 8, 3, lognorm=lognorm)
+    q0, e0 = ctx.surface_eval(pts, modeltype=0, method=method)
+    for _ in range(3):
+        q1, e1 = ctx.surface_eval(pts, modeltype=0, method=method)
+        np.testing.assert_array_equal(q1, q0)
+        np.testing.assert_array_equal(e1, e0)
+    perm = rng.permutation(len(pts))
+    q2, _ = ctx.surface_eval(pts[perm], modeltype=0, method=method)
+    # a point's terms and sums do not depend on the other points of its tile
+    np.testing.assert_allclose(q2, q0[perm], rtol=1e-12, atol=0)
+
+
+def test_surface_tc_term_far_above_prepass_bound():
+    """One genealogy 150 nats above every other, in a tile the max-only
+    pre-pass skips and away from the seed samples: its weight relative to the
+    pre-pass bound leaves the fixed-point range, the point is flagged and taken
+    again in FP64 over every genealogy.  Points on either side agree with the
+    FP64 form and the oracle."""
+    rng = np.random.default_rng(8)
+    G = 40000
+    rows, lognorm, _ = synth.surface_stats(rng, G, 5, 8, 2)
+    lognorm = lognorm.copy()
+    g_star = 256 * 3 + 17   # tile 3 (the pre-pass reads tiles 0, 8, ...); seeds sample multiples of G/32
+    lognorm[g_star] += 150.0
+    pts = synth.surface_points(rng, 200)
+    ctx = ctx_with([("sw", 2, 1)])
+    ctx.surface_load(rows, 5, 8, 3, lognorm=lognorm)
+    q, ess = ctx.surface_eval(pts, modeltype=0, method=api.SURF_TC)
+    q64, ess64 = ctx.surface_eval(pts, modeltype=0, method=api.SURF_FP64)
+    assert np.all(np.abs(q - q64) <= 2e-9 * np.abs(q64) + 3e-7), np.max(np.abs(q - q64))
+    np.testing.assert_allclose(ess, ess64, rtol=1e-4)
+    for k in range(0, len(pts), 37):
+        qo, _ = O.jointp(rows, 5, 8, 3, pts[k], modeltype=0, lognorm=lognorm)
+        assert abs(q[k] - qo) <= 2e-9 * abs(qo) + 3e-7, (k, q[k], qo)
+    q2, _ = ctx.surface_eval(pts, modeltype=0, method=api.SURF_TC)
+    np.testing.assert_array_equal(q2, q)
