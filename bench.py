@@ -1,31 +1,41 @@
 #!/usr/bin/env python3
 """Throughput of the GB300 hot paths: chain-locus likelihood evaluations per
-second (and L-mode surface points per second with --workload surface).
+second, and L-mode surface grid points per second.
 
-Default workload: 2 populations, 50 HKY loci x (20+20) copies x 1000 bp, 32
-heated chains -- every chain-locus fully re-evaluated each step (the batched
-form of changet_RY1's all-locus re-likelihood), FP32 pruning with exact
-power-of-two rescaling and FP64 sums.  One JSON line on stdout.
+Default (--workload all): one JSON line whose headline is the stepwise
+microsatellite workload -- 3 sampled populations (5-population tree), 100
+SW loci x 30 copies per population, 64 heated chains, every chain-locus
+fully evaluated per step -- with the other named workloads as sub-objects
+under "configs", each with its own value, e2e, roofline, CPU baseline and
+error against the plain FP64 form:
+  config1_is       2 populations, 5 IS loci x (10+10) copies, 4 chains
+  config2_hky      2 populations, 50 HKY loci x (20+20) x 1000 bp, 32 chains
+                   (float-float pruning; the plain FP32 kernel beside it, an
+                   edit-list leg and the per-call C-ABI latency)
+  config4_mixed    200 HKY + 100 SW loci, U(4,60) copies x 3 populations,
+                   128 chains x 8 runs
+  config5_surface  G = 2^21 genealogy summaries, P = 2^16 points
 
-  python bench.py [--steps K] [--warmup W] [--gpus N] [--workload hky|sw|is|surface]
-  python bench.py --impl reference ...   # the CPU restatement of the reference
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--workload all|sw|is|hky|mixed|surface|treeweight|popmig]
+  python bench.py --impl reference ...   # the CPU restatement of the reference on every host core
 
-value: inputs resident in HBM, device time (CUDA events) of K steps, L2
-flushed between steps.  e2e: the same steps through the public C ABI from
-host buffers (genealogies staged and copied host->device, results copied
-back) on the host clock.  Multi-GPU: independent replicas, one per rank.
+value: inputs resident in HBM, device time (CUDA events on the context's
+stream) of K steps, L2 flushed between steps.  e2e: the same steps through
+the public C ABI from host buffers (genealogies copied host->device every
+step, results copied back) on the host clock.  Multi-GPU: independent
+replicas, one per rank, each on its own device.
 """
 from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
 import sys
 import threading
 import time
-from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
@@ -47,6 +57,20 @@ def measured_peaks():
         return 6800.0, 1900.0, "fallback"
 
 
+def fp32_peak_tflops(sm_max_mhz):
+    """Nominal FP32 FMA rate: SMs x 128 lanes x 2 FLOP x the SM clock the
+    run's clock samples report as maximum (no measured figure exists)."""
+    nsm = 152
+    try:
+        import torch
+
+        nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    except Exception:
+        pass
+    mhz = sm_max_mhz or 2070.0
+    return nsm * 128 * 2 * mhz * 1e6 / 1e12, "nominal: %d SMs x 128 FP32 lanes x 2 x %.0f MHz" % (nsm, mhz)
+
+
 def profile_traffic(kernel):
     """dram bytes per launch from the committed ncu summary, if present."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
@@ -57,6 +81,15 @@ def profile_traffic(kernel):
         return None
 
 
+def rank_device():
+    """This rank's GPU: LOCAL_RANK when the launcher leaves several devices
+    visible (or none listed), else the one visible device."""
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if vis is None:
+        return local
+    n = len([v for v in vis.split(",") if v.strip()])
+    return local if n > 1 else 0
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -129,8 +162,8 @@ def aggregate(total_ms, units, steps, dist=None):
 
 
 # ------------------------------------------------------------- workloads
-def build_ctx(wl, api):
-    ctx = api.Context(0)
+def build_ctx(wl, api, device=0):
+    ctx = api.Context(device)
     for spec in wl.loci:
         if spec[0] == "is":
             ctx.add_locus_is(spec[1])
@@ -144,107 +177,259 @@ def build_ctx(wl, api):
     return ctx
 
 
-def algo_bytes(wl):
-    """Compulsory bytes of one full evaluation of every chain-locus."""
+def hky_algo_bytes(wl):
+    """Algorithmic bytes of one full evaluation of every HKY chain-locus:
+    per internal node and pattern 60 B (two daughter partials 32 B, their
+    scales 8 B, the written partial 16 B and scale 4 B), per pattern 28 B at
+    the root."""
     total = 0.0
     for spec in wl.loci:
         if spec[0] == "hky":
-            L = spec[1]
-            n, S = L.seq.shape
-            # partials (float4) + exponent written per internal node and pattern,
-            # tip states, multiplicities, topology and times read
-            total += (n - 1) * S * 20.0 + n * S + 4.0 * S + (2 * n - 1) * 16.0
-        elif spec[0] == "sw":
-            n = spec[1]
-            total += (2 * n - 1) * 28.0  # node + FF time + allele read, dlikeA write
-        else:
-            seq = spec[1]
-            n, S = seq.shape
-            total += (2 * n - 1) * 16.0 + n * S + 8.0
+            n, S = spec[1].seq.shape
+            total += (n - 1) * S * 60.0 + S * 28.0
     return total * wl.nchains
 
 
-def dominant_kind(wl, api):
-    kinds = {s[0] for s in wl.loci}
-    if "hky" in kinds:
-        return api.K_HKY_FAST, "k_hky_fast"
-    if "sw" in kinds:
-        return api.K_SW_FAST, "k_sw_fast"
-    return api.K_IS, "k_is"
+def sw_branch_flops(d):
+    """FLOPs of one SW branch term: 30 for |d| < 2, else 30 + 6 (|d| +
+    floor(sqrt(40 |d|))) -- the length of the reference's Miller recurrence."""
+    d = np.abs(np.asarray(d))
+    return np.where(d < 2, 30.0, 30.0 + 6.0 * (d + np.floor(np.sqrt(40.0 * d))))
 
 
-def run_ours(args):
-    from ima2p_gb300 import api, workloads
+def sw_algo_flops(wl, max_chains=None):
+    """FLOPs of one evaluation of every SW chain-locus (a sample of chains,
+    scaled, when max_chains is given)."""
+    ch = np.arange(wl.nchains)
+    if max_chains is not None and wl.nchains > max_chains:
+        ch = np.linspace(0, wl.nchains - 1, max_chains).astype(int)
+    tot = 0.0
+    for li, spec in enumerate(wl.loci):
+        if spec[0] != "sw":
+            continue
+        for c in ch:
+            g, A = wl.tree(int(c), li), np.asarray(wl.allele(int(c), li))
+            keep = g.down >= 0
+            tot += float(sw_branch_flops(A[keep] - A[g.down[keep]]).sum())
+    return tot * wl.nchains / len(ch)
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    dist = None
-    if world > 1:
-        import torch.distributed as dist_mod
-        dist_mod.init_process_group("gloo")
-        dist = dist_mod
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("LOCAL_RANK", "0"))
-    wl = workloads.make(args.workload)
-    ctx = build_ctx(wl, api)
+
+def is_algo_bytes(wl):
+    """Per evaluation: (2n-1) x 20 B of topology and time, S x ceil(n/32) x 4 B
+    of site bit sets, 8 B out."""
+    total = 0.0
+    for spec in wl.loci:
+        if spec[0] == "is":
+            n, S = spec[1].shape
+            total += (2 * n - 1) * 20.0 + S * math.ceil(n / 32) * 4.0 + 8.0
+    return total * wl.nchains
+
+
+def oracle_packs(wl, limit):
+    """An even sample of the workload's chain-loci, packed per model kind for
+    the oracle's batched C entry points."""
+    from oracle import pyoracle as O
+
     ci, li = wl.pairs()
-    u = wl.u.ravel()
-    par = wl.par.ravel()
+    # an even sample of `limit` pairs; a workload with fewer pairs is cycled
+    # through until the batch holds `limit` (thread start-up per call stays
+    # small against the work)
+    idx = np.linspace(0, len(ci) - 1, limit).astype(int) if limit < len(ci) else np.resize(np.arange(len(ci)), limit)
+    by = {}
+    for k in idx:
+        c, l = int(ci[k]), int(li[k])
+        spec = wl.loci[l]
+        data = spec[1] if spec[0] in ("is", "hky") else wl.allele(c, l)
+        by.setdefault(spec[0], []).append((spec[0], wl.tree(c, l), float(wl.u[c, l]), float(wl.par[c, l]), data))
+    return [O.PackedItems(v) for v in by.values()]
+
+
+def cpu_rate(packs, seconds, threads):
+    """Chain-locus evaluations per second of the oracle's batched C path on
+    `threads` host threads, repeated for about `seconds`."""
+    n, t = 0, 0.0
+    while t < seconds or n == 0:
+        for p in packs:
+            t0 = time.perf_counter()
+            p.run(threads)
+            t += time.perf_counter() - t0
+            n += p.nitems
+    return n / t, n, t
+
+
+def cpu_baseline(wl, seconds, limit=4096):
+    cores = os.cpu_count() or 1
+    packs = oracle_packs(wl, limit)
+    v, n, t = cpu_rate(packs, seconds, cores)
+    return {"value": round(v, 1), "unit": "evals/s", "cores": cores, "kind": "port",
+            "sample": "%d chain-locus evaluations in %.1f s over an even %d-pair sample of the workload's %d "
+                      "pairs, the oracle's batched C path on %d threads"
+                      % (n, t, sum(p.nitems for p in packs), wl.nchains * wl.nloci, cores)}
+
+
+def dirty_edits(wl, rng, ndirty=4):
+    """Four internal (non-root) nodes of every chain-locus moved down in time,
+    one after another so each move stays inside its bounds, as a genealogy
+    update leaves them: the packed arrays with the new times, the edit lists
+    [pairs][4] and how many nodes each evaluation recomputes (the edited
+    nodes and their ancestors)."""
+    pci, pli, up0, up1, down, tm = wl.packed()
+    tm = tm.copy()
+    ci, li = wl.pairs()
+    edits = np.full((len(ci), 4), -1, np.int32)
+    recomputed = 0
+    off = 0
+    for k in range(len(ci)):
+        spec = wl.loci[int(li[k])]
+        n = spec[1].seq.shape[0] if spec[0] == "hky" else (spec[1] if spec[0] == "sw" else spec[1].shape[0])
+        nl = 2 * n - 1
+        u0, u1, dn, t = up0[off:off + nl], up1[off:off + nl], down[off:off + nl], tm[off:off + nl]
+        cand = [j for j in range(n, nl) if dn[j] >= 0]
+        pick = rng.choice(cand, size=min(ndirty, len(cand)), replace=False)
+        fresh = set()
+        for j in pick:
+            a, b = int(u0[j]), int(u1[j])
+            lo = max(t[u0[a]] if u0[a] >= 0 else 0.0, t[u0[b]] if u0[b] >= 0 else 0.0)
+            t[a] = t[b] = 0.5 * (lo + t[a])
+            x = int(j)
+            while x >= 0 and x not in fresh:
+                fresh.add(x)
+                x = int(dn[x])
+        edits[k, :len(pick)] = pick
+        recomputed += len(fresh)
+        off += nl
+    return (pci, pli, up0, up1, down, tm), edits, recomputed / len(ci)
+
+
+def kdelta(k0, k1):
+    n = k1[0] - k0[0]
+    return n, (k1[1] - k0[1]) / max(n, 1)
+
+
+def measure_lik(args, api, wl, steps, dist=None, device=0, hky_legs=False):
+    """One likelihood workload: every chain-locus fully evaluated per step
+    (the batched form of changet_RY1's all-locus re-likelihood)."""
+    world = dist.get_world_size() if dist else 1
+    rank = dist.get_rank() if dist else 0
+    ctx = build_ctx(wl, api, device)
+    ci, li = wl.pairs()
+    u, par = wl.u.ravel(), wl.par.ravel()
     units = len(ci)
     prec = api.PREC_FAST
     batch = ctx.batch_create(ci, li, u, par, precision=prec)
-    # warm-up (also initialises per-locus constants), then the launch-shape
-    # autotuner on the batch's own requests
     for _ in range(args.warmup):
         batch.run(use_graph=True)
     tuned = batch.autotune(reps=5)
     batch.run(use_graph=True)
     ctx.synchronize()
     res_fast, st_fast = batch.results()
+    kinds = {s[0] for s in wl.loci}
 
     # ---------------- timed region: resident inputs, L2 flushed between steps
-    kind, kname = dominant_kind(wl, api)
+    kstat = {k: None for k in (api.K_IS, api.K_HKY_FAST, api.K_SW_FAST)}
     ctx.set_profiling(True)
     n0 = ctx.launch_count()
-    k0 = ctx.kernel_stats(kind)
+    for k in kstat:
+        kstat[k] = ctx.kernel_stats(k)
     times = []
     if dist:
         dist.barrier()
-    with Clocks(0) as clk:
-        for _ in range(args.steps):
+    with Clocks(device) as clk:
+        for _ in range(steps):
             ctx.flush_l2()
             ctx.timer_begin()
             batch.run(use_graph=False)
             times.append(ctx.timer_end())
-    k1 = ctx.kernel_stats(kind)
-    n_launch = ctx.launch_count() - n0  # library kernels only (the L2 flush is a memset)
+    n_launch = ctx.launch_count() - n0
+    per = {k: kdelta(kstat[k], ctx.kernel_stats(k)) for k in kstat}
     ctx.set_profiling(False)
-    total_ms, value = aggregate(float(sum(times)), units, args.steps, dist)
+    total_ms, value = aggregate(float(sum(times)), units, steps, dist)
+    clocks = clk.summary()
 
-    # ---------------- dominant kernel roofline
-    kl = k1[0] - k0[0]
-    kms = (k1[1] - k0[1]) / max(kl, 1)
-    kbytes = (k1[2] - k0[2]) / max(kl, 1)
-    hbm, bf16, src = measured_peaks()
-    achieved = kbytes / (kms / 1e3) / 1e9 if kms > 0 else 0.0
-    roof = {"kernel": kname, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm,
-            "unit": "GB/s", "frac": round(achieved / hbm, 4), "peak_source": src,
-            "traffic": profile_traffic(kname), "algorithmic_bytes_per_launch": kbytes,
-            "avg_launch_ms": round(kms, 5)}
+    # ---------------- roofline of the dominant kernel
+    hbm, _, src = measured_peaks()
+    fp32, fp32_src = fp32_peak_tflops(clocks["sm_max_mhz"] if clocks else None)
+    roof, composite = None, None
+    if "hky" in kinds:
+        nl_, ms = per[api.K_HKY_FAST]
+        b = hky_algo_bytes(wl)
+        ach = b / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+        roof = {"kernel": "k_hky_fast (float-float)", "bound": "hbm", "achieved": round(ach, 1), "peak": hbm,
+                "unit": "GB/s", "frac": round(ach / hbm, 4), "peak_source": src + " (of %s)" % src,
+                "traffic": profile_traffic("k_hky_fast"), "algorithmic_bytes_per_launch": b,
+                "avg_launch_ms": round(ms, 5), "launches": nl_}
+    if "sw" in kinds:
+        nl_, ms = per[api.K_SW_FAST]
+        fl = sw_algo_flops(wl, max_chains=16)
+        ach = fl / (ms / 1e3) / 1e12 if ms > 0 else 0.0
+        sroof = {"kernel": "k_sw_fast", "bound": "fp32", "achieved": round(ach, 3), "peak": round(fp32, 1),
+                 "unit": "TFLOP/s", "frac": round(ach / fp32, 4), "peak_source": fp32_src,
+                 "traffic": profile_traffic("k_sw_fast"), "algorithmic_flops_per_launch": fl,
+                 "avg_launch_ms": round(ms, 5), "launches": nl_,
+                 "note": "algorithmic FLOPs of the reference's Bessel terms; the kernel issues them in "
+                         "float-float, about ten FP32 instructions each"}
+        if roof is None:
+            roof = sroof
+        else:
+            # batched uneven workload: the per-kind bounds added up against the step time
+            hb = hky_algo_bytes(wl) / (hbm * 1e9) + fl / (fp32 * 1e12)
+            composite = {"time_bound_ms": round(1e3 * hb, 4), "step_ms": round(total_ms / steps, 4),
+                         "frac": round(1e3 * hb / (total_ms / steps), 4),
+                         "note": "HKY algorithmic bytes at the measured HBM rate plus SW algorithmic FLOPs at "
+                                 "the nominal FP32 rate, over the measured step time"}
+            roof["sw"] = sroof
+    if roof is None:
+        nl_, ms = per[api.K_IS]
+        b = is_algo_bytes(wl)
+        ach = b / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+        roof = {"kernel": "k_is", "bound": "hbm", "achieved": round(ach, 2), "peak": hbm, "unit": "GB/s",
+                "frac": round(ach / hbm, 6), "peak_source": src, "traffic": profile_traffic("k_is"),
+                "algorithmic_bytes_per_launch": b, "avg_launch_ms": round(ms, 5), "launches": nl_,
+                "note": "latency-bound: %d chain-loci per launch" % units}
 
     # ---------------- plain FP64 per-chain form on the same GPU
-    b64 = ctx.batch_create(ci, li, u, par, precision=api.PREC_FP64)
-    for _ in range(2):
-        b64.run(use_graph=False)
-    t64 = []
-    for _ in range(max(3, min(args.steps, 10))):
-        ctx.flush_l2()
-        ctx.timer_begin()
-        b64.run(use_graph=False)
-        t64.append(ctx.timer_end())
-    res64, _ = b64.results()
-    v64 = units / (statistics.median(t64) / 1e3)
+    def form(precision, reps):
+        b = ctx.batch_create(ci, li, u, par, precision=precision)
+        for _ in range(2):
+            b.run(use_graph=False)
+        tt = []
+        for _ in range(reps):
+            ctx.flush_l2()
+            ctx.timer_begin()
+            b.run(use_graph=False)
+            tt.append(ctx.timer_end())
+        r, _ = b.results()
+        b.destroy()
+        return r, units / (statistics.median(tt) / 1e3)
+
+    res64, v64 = form(api.PREC_FP64, max(3, min(steps, 10)))
     ok = (st_fast == 0)
     err = np.abs(res_fast[ok] - res64[ok])
+    out = {
+        "value": round(value, 1), "unit": "evals/s", "ms_per_step": round(total_ms / steps, 5), "steps": steps,
+        "config": {"workload": wl.describe, "global_batch": units * world, "chain_loci_per_step": units,
+                   "l2": "flushed between timed steps",
+                   "precision": "float-float pruning / Bessel terms, FP64 sums" if kinds & {"hky", "sw"}
+                   else "FP64"},
+        "roofline": roof,
+        "fp64_form": {"value": round(v64, 1), "unit": "evals/s", "speedup": round(value / world / v64, 2)},
+        "error_vs_fp64": {"max_abs": float(err.max()) if len(err) else None,
+                          "median_abs": float(np.median(err)) if len(err) else None,
+                          "max_rel": float((err / np.abs(res64[ok])).max()) if len(err) else None},
+        "gpu_launches": int(n_launch), "clocks": clocks,
+        "autotune": {"hky_variant": tuned[0], "sw_variant": tuned[1]},
+    }
+    if composite:
+        out["roofline_composite"] = composite
+    if "hky" in kinds:
+        # the plain FP32 pruning kernel on the same batch: its speed and error
+        res32, v32 = form(api.PREC_FP32, max(3, min(steps, 20)))
+        e32 = np.abs(res32[ok] - res64[ok])
+        out["fp32_form"] = {"value": round(v32, 1), "unit": "evals/s",
+                            "error_vs_fp64": {"max_abs": float(e32.max()), "median_abs": float(np.median(e32))},
+                            "note": "FP32 partials: a pattern's rounding repeats in each of its sites"}
+        batch.run(use_graph=False)  # the float-float partials are the committed ones below
+        ctx.synchronize()
 
     # ---------------- e2e through the C ABI from host buffers
     # every step re-times every genealogy (changet_RY1's pattern: topology
@@ -252,44 +437,27 @@ def run_ours(args):
     pci, pli, up0, up1, down, tm = wl.packed()
     scaled = np.where(tm > 0, tm * (1.0 + 1e-6), tm)
     nodes = len(up0)
-    # FP64 + float-float time per node, length per pair, 40-byte request per pair
-    h2d = nodes * 16 + units * 8 + units * 40
+    h2d = nodes * 16 + units * 8 + units * 40  # FP64 + float-float time per node, lengths, requests
     d2h = units * (8 + 4)
     e2e_t = []
-    for s in range(args.warmup + min(args.steps, 200)):
-        times = scaled if s % 2 else tm
+    for s in range(args.warmup + min(steps, 100)):
+        tms = scaled if s % 2 else tm
         t0 = time.perf_counter()
-        ctx.set_genealogies(pci, pli, up0, up1, down, times)
-        r, _ = ctx.eval(ci, li, u, par, precision=prec)
+        ctx.set_genealogies(pci, pli, up0, up1, down, tms)
+        ctx.eval(ci, li, u, par, precision=prec)
         t1 = time.perf_counter()
         if s >= args.warmup:
             e2e_t.append(t1 - t0)
     e2e = units * world / statistics.median(e2e_t)
+    out["e2e"] = {"value": round(e2e, 1), "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
+                  "d2h_bytes_per_step": int(d2h)}
+    ctx.set_genealogies(pci, pli, up0, up1, down, tm)
 
-    out = {
-        "metric": METRIC, "value": round(value, 1), "unit": "evals/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 5),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
-        "data": "synthetic (seeded IM coalescent genealogies and simulated data, shapes of the named config)",
-        "config": {"workload": wl.describe, "global_batch": units * world, "chain_loci_per_step": units,
-                   "parallelism": "replicas%d" % world, "l2": "flushed between timed steps",
-                   "precision": "FP32 partials, exact power-of-two rescaling, FP64 root sums"},
-        "e2e": {"value": round(e2e, 1), "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
-        "roofline": roof,
-        "fp64_form": {"value": round(v64, 1), "unit": "evals/s", "speedup": round(value / world / v64, 2)},
-        "error_vs_fp64": {"max_abs": float(err.max()) if len(err) else None,
-                          "median_abs": float(np.median(err)) if len(err) else None,
-                          "max_rel": float((err / np.abs(res64[ok])).max()) if len(err) else None},
-        "gpu_launches": int(n_launch),
-        "clocks": clk.summary(),
-        "autotune": {"hky_variant": tuned[0], "sw_variant": tuned[1],
-                     "variants": "hky: 0 = 128 threads, 1 = 64, 2 = 256, 3 = 128 without the shared-memory "
-                                 "cache, 4 = 128 with registers for 8 CTAs/SM; sw: 0 = 8 chain-loci per CTA, "
-                                 "1 = 4, 2 = 16"},
-    }
-    # MC3 swap sweeps of every run on the resident sums (the reference's
-    # default swaptries = max(1, chains / 10)), committed likelihoods as pdg
+    if hky_legs:
+        out["edit_lists"] = edit_list_leg(ctx, api, wl, ci, li, u, par, steps)
+        out["per_call"] = per_call_leg(ctx, api, wl)
+
+    # ---------------- MC3 swap sweeps of every run on the resident sums
     ctx.commit(ci, li, np.ones(units, np.uint8))
     ctx.set_probg(np.zeros(wl.nchains))
     ctx.setheat(0.9, 0.8, 1)
@@ -304,146 +472,149 @@ def run_ours(args):
     sw_ms = ctx.timer_end() / nsw
     out["swaps"] = {"runs": wl.nruns, "chains_per_run": wl.cpr, "swaptries": tries,
                     "ms_per_sweep": round(sw_ms, 5),
-                    "attempts_per_s": round(wl.nruns * tries / (sw_ms / 1e3), 1),
-                    "note": "one launch per sweep: per-chain sums over loci + sequential attempts per run"}
+                    "attempts_per_s": round(wl.nruns * tries / (sw_ms / 1e3), 1)}
     if rank == 0:
         out["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
-        print(json.dumps(out), flush=True)
     batch.destroy()
-    b64.destroy()
     ctx.close()
-    if dist:
-        dist.destroy_process_group()
+    return out
 
 
-# --------------------------------------------------------- CPU baselines
-def _oracle_items(wl, limit=None):
-    """(locus spec, genealogy, u, kappa/tr, alleles) of the workload's chain-loci;
-    with `limit`, an even sample of that many."""
+def edit_list_leg(ctx, api, wl, ci, li, u, par, steps):
+    """The genealogy-update case: four internal nodes of every chain-locus
+    moved, each evaluation given those four as its edit list (e1..e4), so
+    only they and their ancestors are recomputed (device time, L2 flushed)."""
+    rng = np.random.default_rng(99)
+    packed, edits, nrec = dirty_edits(wl, rng)
+    ctx.set_genealogies(*packed)
+    b = ctx.batch_create(ci, li, u, par, edits=edits, precision=api.PREC_FAST)
+    for _ in range(3):
+        b.run(use_graph=True)
+    tt = []
+    for _ in range(max(3, min(steps, 200))):
+        ctx.flush_l2()
+        ctx.timer_begin()
+        b.run(use_graph=False)
+        tt.append(ctx.timer_end())
+    r_ff, _ = b.results()
+    b.destroy()
+    b64 = ctx.batch_create(ci, li, u, par, edits=edits, precision=api.PREC_FP64)
+    b64.run(use_graph=False)
+    r64, _ = b64.results()
+    b64.destroy()
+    ms = statistics.median(tt)
+    return {"value": round(len(ci) / (ms / 1e3), 1), "unit": "evals/s", "ms_per_step": round(ms, 5),
+            "dirty_nodes_per_eval": 4, "recomputed_nodes_per_eval": round(nrec, 2),
+            "error_vs_fp64_max_abs": float(np.abs(r_ff - r64).max())}
+
+
+def per_call_leg(ctx, api, wl, calls=2000):
+    """The per-call drop-in (ima_gpu_likelihoodHKY, one chain-locus per call,
+    result copied back and synchronised) against one host core running the
+    oracle's C likelihood on the same chain-loci."""
     from oracle import pyoracle as O
 
-    ci, li = wl.pairs()
-    idx = np.arange(len(ci))
-    if limit is not None and limit < len(idx):
-        idx = np.linspace(0, len(idx) - 1, limit).astype(int)
-    items = []
-    for k in idx:
-        c, l = int(ci[k]), int(li[k])
-        items.append((wl.loci[l], wl.tree(c, l), float(wl.u[c, l]), float(wl.par[c, l]), wl.allele(c, l)))
-    return O, items
+    nl = wl.nloci
+    lat = []
+    for k in range(calls + 50):
+        l = k % nl
+        t0 = time.perf_counter()
+        ctx.likelihoodHKY(0, l, float(wl.u[0, l]), float(wl.par[0, l]), -1, -1, -1, -1)
+        if k >= 50:
+            lat.append(time.perf_counter() - t0)
+    lat_up = []
+    for k in range(200):
+        l = k % nl
+        g = wl.tree(0, l)
+        t0 = time.perf_counter()
+        ctx.set_genealogy(0, l, g)
+        ctx.likelihoodHKY(0, l, float(wl.u[0, l]), float(wl.par[0, l]), -1, -1, -1, -1)
+        lat_up.append(time.perf_counter() - t0)
+    items = [("hky", wl.tree(0, l), float(wl.u[0, l]), float(wl.par[0, l]), wl.loci[l][1]) for l in range(nl)]
+    pack = O.PackedItems(items)
+    v, n, t = cpu_rate([pack], 1.0, 1)
+    return {"us_per_call": round(1e6 * statistics.median(lat), 2),
+            "us_per_call_with_genealogy_upload": round(1e6 * statistics.median(lat_up), 2),
+            "cpu_us_per_eval_1core": round(1e6 / v, 2),
+            "note": "one chain-locus (20+20 copies, 1000 bp) per call; the genealogy stays resident unless "
+                    "uploaded"}
 
 
-def _eval_item(O, it, cache):
-    spec, g, u, par, A = it
-    if spec[0] == "hky":
-        L = spec[1]
-        st = cache.get(id(L))
-        if st is None:
-            st = cache[id(L)] = O.HKYState(*L.seq.shape)
-        return st.likelihood(L, g, u, par)
-    if spec[0] == "sw":
-        return O.sw_likelihood(A, g, u, par)[0]
-    seq = spec[1]
-    return O.is_likelihood(seq, g, g.length(), u, 0.0)[0]
+def run_likelihood_line(args, name):
+    """--workload is|hky|sw|mixed alone."""
+    from ima2p_gb300 import api, workloads
+
+    dist = init_dist()
+    wl = workloads.make(name)
+    steps = args.steps if name != "mixed" else min(args.steps, 50)
+    out = measure_lik(args, api, wl, steps, dist, rank_device(), hky_legs=(name == "hky"))
+    emit(args, out, METRIC, dist)
 
 
-def cpu_baseline(wl, seconds):
-    """The oracle (a C restatement of the reference) on one host core over a
-    bounded sample of the workload's chain-loci."""
-    O, items = _oracle_items(wl, limit=20000)
-    cache = {}
-    n = 0
-    t0 = time.perf_counter()
-    while time.perf_counter() - t0 < seconds:
-        _eval_item(O, items[n % len(items)], cache)
-        n += 1
-    dt = time.perf_counter() - t0
-    return {"value": round(n / dt, 1), "unit": "evals/s", "cores": 1, "kind": "port",
-            "sample": "%d chain-locus evaluations (%.1f s, cycling over the workload's %d chain-loci)"
-                      % (n, dt, len(items))}
+def init_dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world <= 1:
+        return None
+    import torch.distributed as dist_mod
+    dist_mod.init_process_group("gloo")
+    return dist_mod
 
 
-_REF = {}
-
-
-def _ref_init(counter, workload, limit, ncores):
-    """Worker set-up: this worker's share of a bounded sample of the workload."""
-    from ima2p_gb300 import workloads
-
-    with counter.get_lock():
-        k = counter.value
-        counter.value += 1
-    wl = workloads.make(workload)
-    O, items = _oracle_items(wl, limit=limit)
-    _REF["O"], _REF["items"] = O, items[k::ncores]
-
-
-def _ref_step(min_seconds):
-    """Evaluate this worker's share, repeated until min_seconds have passed."""
-    cache = {}
-    n = 0
-    t0 = time.perf_counter()
-    while True:
-        for it in _REF["items"]:
-            _eval_item(_REF["O"], it, cache)
-        n += len(_REF["items"])
-        if not _REF["items"] or time.perf_counter() - t0 >= min_seconds:
-            return n
-
-
-def run_reference(args):
-    """The reference's CPU path on every host core: the oracle (a C
-    restatement of the reference functions) in one process per core, each on
-    its share of a bounded sample of the workload's chain-loci."""
-    import multiprocessing as mp
-
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
-        return
-    from ima2p_gb300 import workloads
-
-    if args.workload in ("surface", "treeweight", "popmig"):
-        print(json.dumps({"impl": "reference", "unavailable": "%s reference arm not provided; "
-                          "see cpu_baseline of the %s line" % (args.workload, args.workload)}))
-        return
-    cores = os.cpu_count() or 1
-    wl = workloads.make(args.workload)
-    nall = wl.nchains * wl.nloci
-    limit = min(nall, max(args.ref_cap, cores))
-    ctx = mp.get_context("spawn")
-    counter = ctx.Value("i", 0)
-    with ctx.Pool(cores, initializer=_ref_init, initargs=(counter, args.workload, limit, cores)) as pool:
-        times = []
-        done = 0
-        for s in range(args.warmup + args.steps):
-            t0 = time.perf_counter()
-            done = sum(pool.map(_ref_step, [0.05] * cores, chunksize=1))
-            if s >= args.warmup:
-                times.append(time.perf_counter() - t0)
-    v = done / statistics.median(times)
-    wl_desc = wl.describe
-    desc = ("%d chain-locus evaluations per step (a %d-pair sample of the workload's %d, repeated "
-            "for >= 50 ms), %d processes" % (done, limit, nall, cores))
-    print(json.dumps({
-        "impl": "reference", "metric": METRIC, "value": round(v, 1), "unit": "evals/s", "n_gpus": 0,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * statistics.median(times), 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
-        "data": "synthetic", "config": {"workload": wl_desc},
-        "cpu_baseline": {"value": round(v, 1), "unit": "evals/s", "cores": cores, "kind": "port",
-                         "sample": desc},
-        "e2e": {"value": round(v, 1), "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }), flush=True)
-
-
-def run_surface(args):
-    """Config 5: G = 2^21 genealogy summaries (K = 48 row width), P = 2^16 points."""
-    from ima2p_gb300 import api, synth
+def emit(args, sub, metric, dist, extra=None):
+    """Print the contract's JSON line (rank 0) around a measurement dict."""
+    world = dist.get_world_size() if dist else 1
+    out = {"metric": metric, "value": sub["value"], "unit": sub["unit"], "n_gpus": world,
+           "steps": sub.get("steps", args.steps), "warmup": args.warmup, "ms_per_step": sub["ms_per_step"],
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": sub.get("dtype", "ff32 (float-float on FP32) + fp64 sums"),
+           "data": "synthetic (seeded IM coalescent genealogies and simulated data, shapes of the named config)"}
+    out["config"] = dict(sub["config"], parallelism="replicas%d" % world)
+    for k, v in sub.items():
+        if k not in out and k not in ("config", "steps"):
+            out[k] = v
+    if extra:
+        out.update(extra)
+    if (dist.get_rank() if dist else 0) == 0:
+        print(json.dumps(out), flush=True)
+    if dist:
+        dist.destroy_process_group()
+# ------------------------------------------------------------------ surface
+def surface_inputs(args):
+    from ima2p_gb300 import synth
 
     rng = np.random.default_rng(1005)
     G, P = 1 << args.surface_log2g, 1 << args.surface_log2p
     rows, lognorm, off = synth.surface_stats(rng, G, 5, 8, 2)
     pts = synth.surface_points(rng, P)
-    ctx = api.Context(0)
+    return G, P, rows, lognorm, pts
+
+
+def surface_cpu(rows, lognorm, pts, seconds, threads):
+    """The oracle's exact jointp (C) on `threads` host threads over the first
+    points, as many as about `seconds` take; points per second."""
+    from oracle import pyoracle as O
+
+    n = max(threads, 1)
+    t = 0.0
+    done = 0
+    while True:
+        k = min(n, len(pts) - done) if done < len(pts) else n
+        sub = pts[done % len(pts): done % len(pts) + k]
+        t0 = time.perf_counter()
+        O.jointp_batch(rows, 5, 8, 3, sub, 0, lognorm, threads)
+        t += time.perf_counter() - t0
+        done += len(sub)
+        if t >= seconds:
+            return done / t, done, t
+        # grow the next batch toward the time left
+        n = max(threads, int(done / t * max(0.5, seconds - t)))
+
+
+def measure_surface(args, api, steps, extended=True, device=0):
+    """Config 5: G = 2^21 genealogy summaries (K = 48 row width), P = 2^16
+    points; the tensor-core screen with exact float-float refinement."""
+    G, P, rows, lognorm, pts = surface_inputs(args)
+    ctx = api.Context(device)
     ctx.add_locus_sw(2, 1)
     ctx.set_chains(1, 1)
     ctx.surface_load(rows, 5, 8, 3, lognorm=lognorm)
@@ -455,8 +626,8 @@ def run_surface(args):
     k0 = ctx.kernel_stats(kind)
     n0 = ctx.launch_count()
     wall = []
-    with Clocks(0) as clk:
-        for _ in range(args.steps):
+    with Clocks(device) as clk:
+        for _ in range(steps):
             ctx.flush_l2()
             t0 = time.perf_counter()
             q, ess = ctx.surface_eval(pts, 0, method)
@@ -467,26 +638,20 @@ def run_surface(args):
     dev_ms = (k1[1] - k0[1]) / max(1, k1[0] - k0[0])
     value = P / (dev_ms / 1e3)
     e2e = P / statistics.median(wall)
-    # the other screen, same points (one evaluation)
-    other = api.SURF_FAST if method == api.SURF_TC else api.SURF_TC
-    t0 = time.perf_counter()
-    q_other, _ = ctx.surface_eval(pts, 0, other)
-    other_s = time.perf_counter() - t0
+    # the same points again: the screens give the same bits every call
+    q_again, _ = ctx.surface_eval(pts, 0, method)
     # plain FP64 CUDA-core form on a subset of points, extrapolated per point
     sub = pts[:512]
     ctx.surface_eval(sub, 0, api.SURF_FP64)
     t0 = time.perf_counter()
-    q64, _ = ctx.surface_eval(sub, 0, api.SURF_FP64)
+    q64, e64 = ctx.surface_eval(sub, 0, api.SURF_FP64)
     v64 = len(sub) / (time.perf_counter() - t0)
     rel = np.abs(q[:512] - q64) / np.abs(q64)
-    # exact tensor work of the contraction: 2 * G * K_eff FLOP per point
-    flops = 2.0 * G * 26
+    flops = 2.0 * G * 26  # the contraction's algorithmic FLOPs per point
     hbm, bf16, src = measured_peaks()
     out = {
-        "metric": SURF_METRIC, "value": round(value, 1), "unit": "points/s", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms, 4),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+ff",
-        "data": "synthetic gsampinf rows with the configured distributions",
+        "value": round(value, 1), "unit": "points/s", "ms_per_step": round(dev_ms, 4), "steps": steps,
+        "dtype": "bf16 split (3 products, FP32 accumulate) screen + float-float exact terms + FP64 sums",
         "config": {"workload": "config5-surface: G=2^%d genealogy summaries, K=48 row width "
                                "(5 theta, 8 m), P=2^%d points, full model"
                                % (args.surface_log2g, args.surface_log2p), "global_batch": P,
@@ -494,10 +659,7 @@ def run_surface(args):
         "e2e": {"value": round(e2e, 1), "unit": "points/s", "h2d_bytes_per_step": int(P * 13 * 8),
                 "d2h_bytes_per_step": int(P * 16)},
         "screen": "tcgen05 split-bf16 GEMM (3 products) into TMEM + exact float-float refinement"
-                  if method == api.SURF_TC
-                  else "FP32 CUDA-core FMA + exact float-float refinement",
-        "other_screen": {"points_per_s_e2e": round(P / other_s, 1),
-                         "max_rel_diff": float(np.max(np.abs(q_other - q) / np.abs(q)))},
+                  if method == api.SURF_TC else "FP32 CUDA-core FMA + exact float-float refinement",
         "roofline": {"kernel": "surface (prep + screen + merge)", "bound": "tensor",
                      "achieved": round(flops * P / (dev_ms / 1e3) / 1e12, 2), "peak": bf16,
                      "unit": "TFLOP/s", "frac": round(flops * P / (dev_ms / 1e3) / 1e12 / bf16, 5),
@@ -506,57 +668,63 @@ def run_surface(args):
                              "screen issues 3 x 2*G*32 on the tensor pipe"},
         "fp64_form": {"value": round(v64, 1), "unit": "points/s", "speedup": round(value / v64, 2),
                       "sample": "512 points"},
-        "error_vs_fp64": {"max_rel": float(rel.max()), "median_rel": float(np.median(rel))},
+        "error_vs_fp64": {"max_rel": float(rel.max()), "median_rel": float(np.median(rel)),
+                          "ess_max_rel": float(np.max(np.abs(ess[:512] - e64) / e64))},
+        "repeat_bitwise": bool(np.array_equal(q_again, q)),
         "gpu_launches": int(n_timed), "clocks": clk.summary(),
     }
-    from oracle import pyoracle as O
-    t0 = time.perf_counter()
-    n = 0
-    while time.perf_counter() - t0 < args.cpu_seconds or n == 0:
-        O.jointp(rows, 5, 8, 3, pts[n], lognorm=lognorm)
-        n += 1
-    dt = time.perf_counter() - t0
-    out["cpu_baseline"] = {"value": round(n / dt, 3), "unit": "points/s", "cores": 1, "kind": "port",
-                           "sample": "%d points, exact log-sum-exp over all %d genealogies" % (n, G)}
-    # 1-D marginal densities (fillvec): 13 parameters x GRIDSIZE 1000 grid
-    # points, each a sum over all G genealogies, FP64 as the reference sums it
-    pmin, pmax = np.zeros(13), np.array([20.0] * 5 + [2.0] * 8)
-    ctx.fillvec(pmin, pmax, 1000)
-    ctx.set_profiling(True)
-    m0 = ctx.kernel_stats(api.K_MARGIN)
-    t0 = time.perf_counter()
-    xs_m, ys_m = ctx.fillvec(pmin, pmax, 1000)
-    wall_m = time.perf_counter() - t0
-    m1 = ctx.kernel_stats(api.K_MARGIN)
-    ctx.set_profiling(False)
-    dev_m = (m1[1] - m0[1]) / max(1, m1[0] - m0[0])
-    t0 = time.perf_counter()
-    nm_cpu = 0
-    while time.perf_counter() - t0 < max(0.5, args.cpu_seconds / 4) or nm_cpu == 0:
-        O.margincalc(rows, 5, 8, nm_cpu % 13, xs_m[nm_cpu % 13, (nm_cpu * 37) % 1000])
-        nm_cpu += 1
-    cpu_m = nm_cpu / (time.perf_counter() - t0)
-    out["marginals"] = {"grid_points": 13000, "ms_device": round(dev_m, 3), "ms_e2e": round(1e3 * wall_m, 3),
-                        "points_per_s": round(13000 / (dev_m / 1e3), 1),
-                        "terms_per_s": round(13000 * G / (dev_m / 1e3), 1),
-                        "cpu_points_per_s_1core": round(cpu_m, 3),
-                        "note": "fillvec: margincalc on every parameter's grid, FP64 sums without a shift"}
-    if not args.no_peak_search:
-        # the L-mode peak search (modelloop) on this surface: differential
-        # evolution with 100 x 13 trial points per generation, each generation
-        # one batched tensor-core surface evaluation
-        upper = [20.0] * 5 + [2.0] * 8
+    cores = os.cpu_count() or 1
+    v_cpu, n_cpu, t_cpu = surface_cpu(rows, lognorm, pts, args.cpu_seconds, cores)
+    out["cpu_baseline"] = {"value": round(v_cpu, 3), "unit": "points/s", "cores": cores, "kind": "port",
+                           "sample": "%d points in %.1f s, the oracle's exact jointp over all %d genealogies "
+                                     "on %d threads" % (n_cpu, t_cpu, G, cores)}
+    if extended:
+        # 1-D marginal densities (fillvec): 13 parameters x 1000 grid points,
+        # each a sum over all G genealogies, FP64 as the reference sums it
+        from oracle import pyoracle as O
+        pmin, pmax = np.zeros(13), np.array([20.0] * 5 + [2.0] * 8)
+        ctx.fillvec(pmin, pmax, 1000)
+        ctx.set_profiling(True)
+        m0 = ctx.kernel_stats(api.K_MARGIN)
         t0 = time.perf_counter()
-        best, ess_pk, gens, runs, _ = ctx.modelloop(upper, 0, seed=1234, multiplier=100, method=method)
-        dt = time.perf_counter() - t0
-        evals = (gens + runs) * 1300
-        out["peak_search"] = {"generations": gens, "restarts": runs, "seconds": round(dt, 3),
-                              "ms_per_generation": round(1e3 * dt / (gens + runs), 4),
-                              "points_per_s": round(evals / dt, 1), "population": 1300,
-                              "peak_neg_log_density": float(best[-1]), "ess": ess_pk,
-                              "cpu_seconds_per_generation_1core": round(1300 / out["cpu_baseline"]["value"], 1)}
-    print(json.dumps(out), flush=True)
+        xs_m, ys_m = ctx.fillvec(pmin, pmax, 1000)
+        wall_m = time.perf_counter() - t0
+        m1 = ctx.kernel_stats(api.K_MARGIN)
+        ctx.set_profiling(False)
+        dev_m = (m1[1] - m0[1]) / max(1, m1[0] - m0[0])
+        t0 = time.perf_counter()
+        nm_cpu = 0
+        while time.perf_counter() - t0 < max(0.5, args.cpu_seconds / 4) or nm_cpu == 0:
+            O.margincalc(rows, 5, 8, nm_cpu % 13, xs_m[nm_cpu % 13, (nm_cpu * 37) % 1000])
+            nm_cpu += 1
+        cpu_m = nm_cpu / (time.perf_counter() - t0)
+        out["marginals"] = {"grid_points": 13000, "ms_device": round(dev_m, 3), "ms_e2e": round(1e3 * wall_m, 3),
+                            "points_per_s": round(13000 / (dev_m / 1e3), 1),
+                            "terms_per_s": round(13000 * G / (dev_m / 1e3), 1),
+                            "cpu_points_per_s_1core": round(cpu_m, 3)}
+        if not args.no_peak_search:
+            # the L-mode peak search (modelloop): differential evolution with
+            # 100 x 13 trial points per generation, one batched surface
+            # evaluation per generation
+            upper = [20.0] * 5 + [2.0] * 8
+            t0 = time.perf_counter()
+            best, ess_pk, gens, runs, _ = ctx.modelloop(upper, 0, seed=1234, multiplier=100, method=method)
+            dt = time.perf_counter() - t0
+            evals = (gens + runs) * 1300
+            out["peak_search"] = {"generations": gens, "restarts": runs, "seconds": round(dt, 3),
+                                  "ms_per_generation": round(1e3 * dt / (gens + runs), 4),
+                                  "points_per_s": round(evals / dt, 1), "population": 1300,
+                                  "peak_neg_log_density": float(best[-1]), "ess": ess_pk,
+                                  "cpu_seconds_per_generation_all_cores": round(1300 / v_cpu, 1)}
     ctx.close()
+    return out
+
+
+def run_surface(args):
+    from ima2p_gb300 import api
+
+    out = measure_surface(args, api, args.steps, True, rank_device())
+    emit(args, out, SURF_METRIC, None)
 
 
 def tw_workload(nloci=300, nchains=128, nbase=60, seed=1011):
@@ -902,20 +1070,106 @@ def run_popmig(args):
     ctx.close()
 
 
+
+# ------------------------------------------------------- default: all configs
+def run_all(args):
+    """Config 3 (SW) as the headline line; configs 1, 2, 4 and 5 as sub-objects."""
+    from ima2p_gb300 import api, workloads
+
+    dist = init_dist()
+    dev = rank_device()
+    head = measure_lik(args, api, workloads.make("sw"), args.steps, dist, dev)
+    configs = {}
+    sub_steps = min(args.steps, 200)
+    configs["config1_is"] = measure_lik(args, api, workloads.make("is"), sub_steps, dist, dev)
+    configs["config2_hky"] = measure_lik(args, api, workloads.make("hky"), sub_steps, dist, dev, hky_legs=True)
+    configs["config4_mixed"] = measure_lik(args, api, workloads.make("mixed"), min(args.steps, 30), dist, dev)
+    configs["config5_surface"] = measure_surface(args, api, min(args.steps, 20), not args.no_peak_search, dev)
+    emit(args, head, METRIC, dist, {"configs": configs})
+
+
+# ------------------------------------------------------- the reference arm
+def run_reference(args):
+    """The reference's CPU path on every host core: the oracle (a C
+    restatement of the reference functions, pinned to the compiled reference
+    by the golden fixtures) through its batched C entry points on one thread
+    per core.  Headline: the stepwise-microsatellite workload; sub-objects:
+    the other named workloads (the surface on a bounded sample of points,
+    extrapolated per point)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from ima2p_gb300 import workloads
+
+    cores = os.cpu_count() or 1
+    name = "sw" if args.workload == "all" else args.workload
+    if name in ("treeweight", "popmig"):
+        print(json.dumps({"impl": "reference", "unavailable": "%s: the CPU rate is the line's cpu_baseline"
+                          % name}))
+        return
+
+    def lik_arm(wl, k_steps, step_seconds):
+        packs = oracle_packs(wl, 8192)
+        times, done = [], 0
+        for s in range(args.warmup + k_steps):
+            v, n, t = cpu_rate(packs, step_seconds, cores)
+            if s >= args.warmup:
+                times.append(t)
+                done += n
+        v = done / sum(times)
+        return {"value": round(v, 1), "unit": "evals/s", "ms_per_step": round(1e3 * statistics.median(times), 3),
+                "config": {"workload": wl.describe},
+                "cpu_baseline": {"value": round(v, 1), "unit": "evals/s", "cores": cores, "kind": "port",
+                                 "sample": "an even sample of %d chain-loci of the workload's %d, the oracle's "
+                                           "batched C path on %d threads, >= %.2f s per step"
+                                           % (sum(p.nitems for p in packs), wl.nchains * wl.nloci, cores,
+                                              step_seconds)},
+                "e2e": {"value": round(v, 1), "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+    def surface_arm():
+        G, P, rows, lognorm, pts = surface_inputs(args)
+        v, n, t = surface_cpu(rows, lognorm, pts, max(args.cpu_seconds, 20.0), cores)
+        return {"value": round(v, 3), "unit": "points/s", "ms_per_step": round(1e3 * P / v, 1),
+                "config": {"workload": "config5-surface: G=2^%d, P=2^%d" % (args.surface_log2g, args.surface_log2p)},
+                "cpu_baseline": {"value": round(v, 3), "unit": "points/s", "cores": cores, "kind": "port",
+                                 "sample": "%d points in %.1f s (exact jointp over all %d genealogies, %d "
+                                           "threads), extrapolated per point to the %d-point grid"
+                                           % (n, t, G, cores, P)},
+                "e2e": {"value": round(v, 3), "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+    k_steps = max(1, min(args.steps, 50))
+    step_s = max(0.05, min(0.5, 60.0 / (k_steps + args.warmup)))
+    if name == "surface":
+        head, metric = surface_arm(), SURF_METRIC
+    else:
+        head, metric = lik_arm(workloads.make(name), k_steps, step_s), METRIC
+    line = {"impl": "reference", "metric": metric, "value": head["value"], "unit": head["unit"], "n_gpus": 0,
+            "steps": k_steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+            "config": head["config"], "cpu_baseline": head["cpu_baseline"], "e2e": head["e2e"]}
+    if args.workload == "all":
+        line["configs"] = {
+            "config1_is": lik_arm(workloads.make("is"), 3, 0.5),
+            "config2_hky": lik_arm(workloads.make("hky"), 3, 0.5),
+            "config4_mixed": lik_arm(workloads.make("mixed"), 3, 0.5),
+            "config5_surface": surface_arm(),
+        }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="hky", choices=["hky", "sw", "is", "mixed", "surface", "treeweight",
-                                                        "popmig"])
-    ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--ref-cap", type=int, default=4096)
+    ap.add_argument("--workload", default="all", choices=["all", "sw", "is", "hky", "mixed", "surface",
+                                                        "treeweight", "popmig"])
+    ap.add_argument("--cpu-seconds", type=float, default=3.0)
     ap.add_argument("--surface-log2g", type=int, default=21, help="log2 genealogies (config 5: 21)")
     ap.add_argument("--surface-log2p", type=int, default=16, help="log2 points (config 5: 16)")
     ap.add_argument("--surface-method", default="tc", choices=["tc", "fp32"])
-    ap.add_argument("--no-peak-search", action="store_true", help="surface: skip the DE peak search")
+    ap.add_argument("--no-peak-search", action="store_true", help="surface: skip the marginals and peak search")
     ap.add_argument("--popmig-g", type=int, default=300000, help="popmig: saved genealogies")
     ap.add_argument("--peaks-cpu-g", type=int, default=6000, help="popmig: genealogies in the CPU peaks sample")
     args = ap.parse_args()
@@ -923,6 +1177,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "all":
+        run_all(args)
     elif args.workload == "surface":
         run_surface(args)
     elif args.workload == "treeweight":
@@ -930,7 +1186,7 @@ def main():
     elif args.workload == "popmig":
         run_popmig(args)
     else:
-        run_ours(args)
+        run_likelihood_line(args, args.workload)
 
 
 if __name__ == "__main__":

@@ -20,14 +20,14 @@ LIB_PATH = os.path.join(HERE, "libima2p_gb300.so")
 
 IMA_OK, IMA_ERR_ARG, IMA_ERR_CUDA, IMA_ERR_STATE, IMA_ERR_NOMEM, IMA_ERR_DATA = 0, -1, -2, -3, -4, -5
 MODEL_IS, MODEL_HKY, MODEL_SW = 0, 1, 2
-PREC_FAST, PREC_FP64 = 0, 1
+PREC_FAST, PREC_FP64, PREC_FP32 = 0, 1, 2
 EVAL_OK, EVAL_IS_REJECT, EVAL_IS_FAIL, EVAL_SW_ZERO = 0, 1, 2, 3
 SURF_FAST, SURF_FP64, SURF_COMPAT, SURF_TC = 0, 1, 2, 3
 K_IS, K_IS_SUMLOGK, K_HKY_FAST, K_HKY_FP64, K_SW_FAST, K_SW_FP64, K_SWAP, K_SURF_FAST, \
-    K_SURF_FP64, K_SURF_COMPAT, K_SURF_TC, K_MARGIN, K_TREEWEIGHT, K_TREE_PROB, K_POPMIG = range(15)
+    K_SURF_FP64, K_SURF_COMPAT, K_SURF_TC, K_MARGIN, K_TREEWEIGHT, K_TREE_PROB, K_POPMIG, K_HKY_FP32 = range(16)
 KERNEL_NAMES = ["is", "is_sumlogk", "hky_fast", "hky_fp64", "sw_fast", "sw_fp64", "swap",
                 "surf_fast", "surf_fp64", "surf_compat", "surf_tc", "margin", "treeweight", "tree_prob",
-                "popmig"]
+                "popmig", "hky_fp32"]
 REJECT_IS = -1000000000.0
 
 # every symbol the header declares (checked by tests/test_abi.py)
@@ -41,7 +41,7 @@ EXPORTS = [
     "ima_gpu_commit", "ima_gpu_batch_create", "ima_gpu_batch_run", "ima_gpu_batch_results",
     "ima_gpu_batch_destroy", "ima_gpu_flush_genealogies", "ima_gpu_setheat", "ima_gpu_get_betas",
     "ima_gpu_set_betas", "ima_gpu_set_pdg", "ima_gpu_get_pdg", "ima_gpu_set_probg",
-    "ima_gpu_swapchains", "ima_gpu_get_swapcounts", "ima_gpu_surface_load",
+    "ima_gpu_swapchains", "ima_gpu_swapchains_cb", "ima_gpu_set_allbetas", "ima_gpu_get_swapcounts", "ima_gpu_surface_load",
     "ima_gpu_surface_eval", "ima_gpu_jointp", "ima_gpu_surface_fp64_noalloc", "ima_gpu_tc_selftest",
     "ima_gpu_surface_info", "ima_mt19937_seed", "ima_mt19937_uniform", "ima_gpu_modelloop",
     "ima_gpu_batch_autotune", "ima_gpu_batch_set_variants", "ima_gpu_margincalc", "ima_gpu_fillvec",
@@ -87,9 +87,10 @@ def ti_read_binary(path):
     G, rl = I(), I()
     _ck_free(lib.ima_ti_read_binary(os.fsencode(path), C.byref(G), C.byref(rl), None, 0), "ti_read_binary")
     rows = np.zeros((G.value, rl.value), np.float32)
-    _ck_free(lib.ima_ti_read_binary(os.fsencode(path), C.byref(G), C.byref(rl), _ptr(rows), G.value),
+    G2, rl2 = I(), I(rl.value)
+    _ck_free(lib.ima_ti_read_binary(os.fsencode(path), C.byref(G2), C.byref(rl2), _ptr(rows), G.value),
              "ti_read_binary")
-    return rows
+    return rows[:G2.value]
 
 
 class MT19937(C.Structure):
@@ -103,6 +104,10 @@ class MT19937(C.Structure):
 
     def uniform(self):
         return load_library().ima_mt19937_uniform(C.byref(self))
+
+
+# double uniform(void *arg): the caller's generator, drawn one value at a time
+UNIFORM_FN = C.CFUNCTYPE(C.c_double, C.c_void_p)
 
 
 class ImaError(RuntimeError):
@@ -204,6 +209,7 @@ def _declare(L):
         "ima_mt19937_uniform": (D, [P]),
         "ima_gpu_modelloop": (I, [P, I, P, I, P, I, I, P, P, P, C.POINTER(I), C.POINTER(I)]),
         "ima_gpu_surface_fp64_noalloc": (I, [P, I, I, I, I, I, P, P, I, I, P, P, P]),
+        "ima_gpu_swapchains_cb": (I, [P, I, I, UNIFORM_FN, P, P, P]),
         "ima_gpu_tc_selftest": (I, [P, C.POINTER(I), C.POINTER(C.c_float)]),
         "ima_gpu_timer_begin": (I, [P]),
         "ima_gpu_timer_end": (I, [P, C.POINTER(C.c_float)]),
@@ -419,6 +425,17 @@ class Context:
             stride = 0
         self._ck(self.lib.ima_gpu_swapchains(self.h, int(swaptries), int(include_probg), _ptr(uniforms),
                                              int(stride), int(seed), _ptr(used), _ptr(ok)))
+        return ok, used
+
+    def swapchains_cb(self, swaptries, uniform, include_probg=True):
+        """Swap attempts drawing uniform() one value at a time, where the
+        reference draws (ima_gpu_swapchains_cb): returns (swap0ok, draws)
+        per run."""
+        used = np.zeros(self.nruns, np.int32)
+        ok = np.zeros(self.nruns, np.int32)
+        cb = UNIFORM_FN(lambda _arg: float(uniform()))
+        self._ck(self.lib.ima_gpu_swapchains_cb(self.h, int(swaptries), int(include_probg), cb, None, _ptr(used),
+                                                _ptr(ok)))
         return ok, used
 
     def get_swapcounts(self, run=0):

@@ -132,3 +132,38 @@ __device__ __forceinline__ ff ff_horner(const float2 *c, int m, ff y)
 }
 
 __device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
+
+// e^x and e^x - 1 for -87 < x <= 0 in float-float.  x = k ln2 + r with
+// |r| <= ln2 / 2 (k ln2a.x exact: ln2a.x has 9 significant bits), y =
+// expm1(r / 16) from its Taylor series (degree 7, |r / 16| <= 0.022), four
+// doublings expm1(2z) = expm1(z) (expm1(z) + 2), then e^x = 2^k (1 + y) and
+// e^x - 1 = y (k = 0) or 2^k (1 + y) - 1.  No step cancels: e^x - 1 of a
+// short branch keeps its relative accuracy (about 1e-14).
+__device__ __forceinline__ void ff_exp_expm1_neg(ff x, const FFConsts &K, ff *ex, ff *em1)
+{
+  if (x.hi < -86.0f) {
+    *ex = ff_from(0.0f);
+    *em1 = ff_from(-1.0f);
+    return;
+  }
+  const float kf = rintf(x.hi * 1.44269504f);
+  ff r = ff_sub(x, ff_from(kf * K.ln2a.x));
+  r = ff_sub(r, two_prod(kf, K.ln2a.y));
+  r = ff_add_f(r, -kf * K.ln2b);
+  const ff s = ff_make(r.hi * 0.0625f, r.lo * 0.0625f);
+  // the coefficients from 1/120 on in float (their terms weigh < 2e-9 of
+  // the sum), the rest in float-float
+  const float tail = __fmaf_rn(s.hi, __fmaf_rn(s.hi, 1.0f / 5040.0f, 1.0f / 720.0f), 1.0f / 120.0f);
+  ff u = ff_add(ff_make(0.041666668f, -1.2417635e-09f), ff_mul_f(s, tail));  // 1/24 + s tail
+  u = ff_add(ff_make(0.16666667f, -4.967054e-09f), ff_mul(s, u));          // 1/6 + s u
+  u = ff_add_f(ff_mul(s, u), 0.5f);
+  u = ff_add_f(ff_mul(s, u), 1.0f);
+  ff y = ff_mul(s, u);
+#pragma unroll
+  for (int i = 0; i < 4; i++) y = ff_mul(y, ff_add_f(y, 2.0f));
+  const int k = (int)kf;
+  const float p2 = __int_as_float((127 + k) << 23);  // 2^k, k >= -125
+  const ff one_y = ff_add_f(y, 1.0f);
+  *ex = ff_make(one_y.hi * p2, one_y.lo * p2);
+  *em1 = (k == 0) ? y : ff_add_f(*ex, -1.0f);
+}

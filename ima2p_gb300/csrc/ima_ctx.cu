@@ -214,7 +214,7 @@ struct ima_ctx {
   std::vector<int> pair_stamp;     // set_genealogies: repeated-pair check
   std::vector<size_t> pair_off;    // set_genealogies: node offset of each pair
   int stamp_gen = 0;
-  float4 *d_part = nullptr;
+  float4 *d_part = nullptr, *d_partlo = nullptr;
   int32_t *d_pexp = nullptr;
   double *d_part64 = nullptr, *d_psf64 = nullptr;
   uint8_t *d_slot32 = nullptr, *d_fresh32 = nullptr, *d_slot64 = nullptr, *d_fresh64 = nullptr;
@@ -254,6 +254,9 @@ struct ima_ctx {
   void *d_twin = nullptr, *d_twout = nullptr, *d_tpbuf = nullptr;
   size_t twin_cap = 0, twout_cap = 0, tpbuf_cap = 0;
   int tw_ngen = 0, tw_ntv = 0;
+  // which of the tw_ngen genealogies hold weights from the last treeweight
+  // (all) or chain_weights call (the selected chains' items only)
+  std::vector<uint8_t> tw_valid;
   // resident population labels for the split-time update: per node pop,
   // per item nl+1 relative migration offsets (at node_off + item), events in
   // a pool (item events from mbase[item]), split-time rows per chain
@@ -337,6 +340,7 @@ struct ima_ctx {
     P.is_valid = d_is_valid;
     P.pdg_new = d_pdg_new;
     P.part = d_part;
+    P.partlo = d_partlo;
     P.pexp = d_pexp;
     P.part64 = d_part64;
     P.psf64 = d_psf64;
@@ -410,7 +414,7 @@ extern "C" int ima_gpu_create(int device, ima_ctx **out)
   }
   cudaEventCreate(&c->t0);
   cudaEventCreate(&c->t1);
-  if (sw_init_tables() != 0) {
+  if (sw_init_tables() != 0 || hky_init_tables() != 0) {
     delete c;
     return IMA_ERR_CUDA;
   }
@@ -433,7 +437,7 @@ extern "C" void ima_gpu_destroy(ima_ctx *c)
   }
   void *devs[] = {c->d_loci, c->d_seq, c->d_mult, c->d_sumlogk, c->d_flag, c->d_items,
                   c->d_nodes, c->d_t64, c->d_tff, c->d_sched, c->d_nlev, c->d_len, c->d_pi,
-                  c->d_al, c->d_dlike, c->d_part, c->d_pexp, c->d_part64, c->d_psf64,
+                  c->d_al, c->d_dlike, c->d_part, c->d_partlo, c->d_pexp, c->d_part64, c->d_psf64,
                   c->d_slot32, c->d_fresh32, c->d_slot64, c->d_fresh64, c->d_pdg, c->d_pdg_new,
                   c->d_beta, c->d_allbetas, c->d_probg, c->d_S, c->d_swapcount, c->d_tempcount,
                   c->d_used, c->d_swap0ok, c->d_ctr, c->d_uni, c->d_rows, c->d_lognorm,
@@ -981,12 +985,23 @@ static int ensure_fp64_hky(ima_ctx *c)
   return IMA_OK;
 }
 
+// lo parts of the float-float HKY partials, allocated on first use
+static int ensure_ff_hky(ima_ctx *c)
+{
+  if (c->d_partlo || c->npart == 0) return IMA_OK;
+  c->d_partlo = dev_alloc<float4>(c->npart, c->dev_bytes, c->st);
+  if (!c->d_partlo) return c->fail(IMA_ERR_NOMEM, "float-float partial likelihoods (%zu float4) do not fit", c->npart);
+  // the hi parts already in place (FP32 evaluations) read as exact pairs
+  return c->cuda(cudaMemsetAsync(c->d_partlo, 0, c->npart * sizeof(float4), c->st), "float-float partials");
+}
+
 static int build_batch(ima_ctx *c, Batch &b, int n, const int32_t *ci, const int32_t *li, const double *u,
                        const double *kappa, const int32_t *edits, const int32_t *ai, int prec)
 {
   if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
   if (n < 1 || !ci || !li || !u) return c->fail(IMA_ERR_ARG, "empty or null request list");
-  if (prec != IMA_PREC_FAST && prec != IMA_PREC_FP64) return c->fail(IMA_ERR_ARG, "bad precision");
+  if (prec != IMA_PREC_FAST && prec != IMA_PREC_FP64 && prec != IMA_PREC_FP32)
+    return c->fail(IMA_ERR_ARG, "bad precision");
   std::vector<int> g[3];
   for (int k = 0; k < n; k++) {
     if (!c->valid(ci[k], li[k])) return c->fail(IMA_ERR_ARG, "request %d: chain %d locus %d out of range", k, ci[k], li[k]);
@@ -1031,6 +1046,10 @@ static int build_batch(ima_ctx *c, Batch &b, int n, const int32_t *ci, const int
     int r = ensure_fp64_hky(c);
     if (r) return r;
   }
+  if (b.nhky && prec == IMA_PREC_FAST) {
+    int r = ensure_ff_hky(c);
+    if (r) return r;
+  }
   if (!c->d_slot64 && b.nhky) {
     // the commit kernel touches both slot sets; keep the FP64 marks allocated
     c->d_slot64 = dev_alloc<uint8_t>(c->nnodes, c->dev_bytes, c->st);
@@ -1062,9 +1081,12 @@ static double hky_bytes(ima_ctx *c, const Batch &b)
     const ItemDev &it = c->items[b.h_req[k].item];
     const LocusDev &L = c->loci[it.locus].d;
     double nodes = (double)(2 * it.n - 1);
-    s += (double)(it.n - 1) * L.nsites * 20.0 + (double)it.n * L.nsites + L.nsites * 4.0 + nodes * 16.0;
+    // written partials (FP32: 16 B + 4 B exponent; float-float: + 16 B lo
+    // parts), tip states, multiplicities, topology and times
+    const double pw = b.prec == IMA_PREC_FP32 ? 20.0 : 36.0;
+    s += (double)(it.n - 1) * L.nsites * pw + (double)it.n * L.nsites + L.nsites * 4.0 + nodes * 16.0;
   }
-  return b.prec == IMA_PREC_FP64 ? s * 2.0 : s;
+  return b.prec == IMA_PREC_FP64 ? s * 40.0 / 36.0 : s;
 }
 
 static double sw_bytes(ima_ctx *c, const Batch &b)
@@ -1088,6 +1110,8 @@ static void enqueue(ima_ctx *c, Batch &b)
     const ReqDev *r = b.d_req + b.nis;
     if (b.prec == IMA_PREC_FP64)
       c->launch(IMA_K_HKY_FP64, hky_bytes(c, b), [&] { launch_hky_fp64(P, r, b.nhky, b.maxn_hky, b.d_res + b.nis, b.d_st + b.nis, st); });
+    else if (b.prec == IMA_PREC_FP32)
+      c->launch(IMA_K_HKY_FP32, hky_bytes(c, b), [&] { launch_hky_fp32(P, r, b.nhky, b.maxn_hky, b.maxs_hky, b.hky_variant, b.d_res + b.nis, b.d_st + b.nis, st); });
     else
       c->launch(IMA_K_HKY_FAST, hky_bytes(c, b), [&] { launch_hky_fast(P, r, b.nhky, b.maxn_hky, b.maxs_hky, b.hky_variant, b.d_res + b.nis, b.d_st + b.nis, st); });
   }
@@ -1147,7 +1171,7 @@ static int fetch(ima_ctx *c, Batch &b, double *result, int32_t *status)
   // remember the format of the per-branch SW terms
   for (int k = b.nis + b.nhky; k < b.n; k++) {
     const ItemDev &it = c->items[b.h_req[k].item];
-    c->dl_fast[it.al_off + (size_t)b.h_req[k].ai] = (b.prec == IMA_PREC_FAST);
+    c->dl_fast[it.al_off + (size_t)b.h_req[k].ai] = (b.prec != IMA_PREC_FP64);
   }
   return IMA_OK;
 }
@@ -1269,7 +1293,7 @@ extern "C" int ima_gpu_batch_autotune(ima_ctx *c, int batch, int reps, int *hky_
   r = r ? r : init_sumlogk(c, b);
   if (r) return r;
   if (reps < 1) reps = 1;
-  if (b.prec == IMA_PREC_FAST && (b.nhky || b.nsw)) {
+  if (b.prec != IMA_PREC_FP64 && (b.nhky || b.nsw)) {
     Pools P = c->pools();
     cudaStream_t st = c->st;
     cudaEvent_t e0 = c->ev(), e1 = c->ev();
@@ -1294,7 +1318,10 @@ extern "C" int ima_gpu_batch_autotune(ima_ctx *c, int batch, int reps, int *hky_
     if (b.nhky) {
       const ReqDev *rq = b.d_req + b.nis;
       b.hky_variant = pick(HKY_FAST_VARIANTS, [&](int v) {
-        launch_hky_fast(P, rq, b.nhky, b.maxn_hky, b.maxs_hky, v, b.d_res + b.nis, b.d_st + b.nis, st);
+        if (b.prec == IMA_PREC_FP32)
+          launch_hky_fp32(P, rq, b.nhky, b.maxn_hky, b.maxs_hky, v, b.d_res + b.nis, b.d_st + b.nis, st);
+        else
+          launch_hky_fast(P, rq, b.nhky, b.maxn_hky, b.maxs_hky, v, b.d_res + b.nis, b.d_st + b.nis, st);
       });
     }
     if (b.nsw) {
@@ -1507,6 +1534,11 @@ extern "C" int ima_gpu_set_betas(ima_ctx *c, const double *beta)
 {
   return copy_dev(c, c ? c->d_beta : nullptr, beta, c ? c->nchains * 8 : 0, cudaMemcpyHostToDevice, "betas");
 }
+extern "C" int ima_gpu_set_allbetas(ima_ctx *c, const double *allbetas)
+{
+  return copy_dev(c, c ? c->d_allbetas : nullptr, allbetas, c ? c->nchains * 8 : 0, cudaMemcpyHostToDevice,
+                  "heat ladder");
+}
 extern "C" int ima_gpu_set_pdg(ima_ctx *c, const double *pdg)
 {
   return copy_dev(c, c ? c->d_pdg : nullptr, pdg, c ? (size_t)c->nitems * 8 : 0, cudaMemcpyHostToDevice, "pdg");
@@ -1574,6 +1606,97 @@ extern "C" int ima_gpu_swapchains(ima_ctx *c, int swaptries, int include_probg, 
     for (int k = 0; k < c->nruns; k++)
       if (used[k] < 0) return c->fail(IMA_ERR_ARG, "run %d ran out of supplied uniforms", k);
   return r;
+}
+
+// The swap attempts with the caller's generator drawn one uniform at a time:
+// the per-chain sums S (every locus, the expensive part) come from the
+// device; the attempts, which the reference interleaves with single draws of
+// its one generator stream (swapchains.cpp:549-605), run here in the order
+// k_swap makes them, so a caller whose generator cannot be drawn ahead
+// consumes exactly the reference's draws.
+extern "C" int ima_gpu_swapchains_cb(ima_ctx *c, int swaptries, int include_probg, double (*uniform)(void *),
+                                     void *arg, int32_t *used, int32_t *swap0ok)
+{
+  if (!c || !uniform) return IMA_ERR_ARG;
+  if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
+  if (swaptries < 0) return c->fail(IMA_ERR_ARG, "swaptries must be >= 0");
+  if (c->cpr < 2) return IMA_OK;
+  SwapArgs a{};
+  a.nruns = c->nruns;
+  a.cpr = c->cpr;
+  a.nloci = c->nloci;
+  a.swaptries = 0;  // sums only
+  a.include_probg = include_probg;
+  a.stride = 1;
+  a.pdg = c->d_pdg;
+  a.probg = c->d_probg;
+  a.beta = c->d_beta;
+  a.allbetas = c->d_allbetas;
+  a.uniforms = nullptr;
+  a.counter = nullptr;
+  a.used = nullptr;
+  a.swap0ok = nullptr;
+  a.swapcount = c->d_swapcount;
+  a.tempcount = c->d_tempcount;
+  a.S = c->d_S;
+  c->launch(IMA_K_SWAP, (double)c->nitems * 8.0, [&] { launch_swap(a, c->st); });
+  const int n = c->cpr;
+  const size_t nn = (size_t)n * n, N = (size_t)c->nchains;
+  std::vector<double> S(N), beta(N), allb(N);
+  std::vector<int32_t> sc(nn * c->nruns), tc(nn * c->nruns);
+  int r = c->cuda(cudaGetLastError(), "swap sums");
+  r = r ? r : c->cuda(cudaMemcpyAsync(S.data(), c->d_S, N * 8, cudaMemcpyDeviceToHost, c->st), "sums");
+  r = r ? r : c->cuda(cudaMemcpyAsync(beta.data(), c->d_beta, N * 8, cudaMemcpyDeviceToHost, c->st), "betas");
+  r = r ? r : c->cuda(cudaMemcpyAsync(allb.data(), c->d_allbetas, N * 8, cudaMemcpyDeviceToHost, c->st), "betas");
+  r = r ? r : c->cuda(cudaMemcpyAsync(sc.data(), c->d_swapcount, sc.size() * 4, cudaMemcpyDeviceToHost, c->st), "counts");
+  r = r ? r : c->cuda(cudaMemcpyAsync(tc.data(), c->d_tempcount, tc.size() * 4, cudaMemcpyDeviceToHost, c->st), "counts");
+  r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "swap sums");
+  if (r) return r;
+  constexpr int SWAPDIST = 7;
+  for (int run = 0; run < c->nruns; run++) {
+    double *b = beta.data() + (size_t)run * n;
+    const double *ab = allb.data() + (size_t)run * n, *Sr = S.data() + (size_t)run * n;
+    int32_t *scr = sc.data() + run * nn, *tcr = tc.data() + run * nn;
+    int k = 0, ok0 = 0;
+    auto draw = [&] {
+      k++;
+      return uniform(arg);
+    };
+    auto rank_of = [&](double v) {
+      for (int q = 0; q < n; q++)
+        if (ab[q] == v) return q;
+      return -1;
+    };
+    for (int t = 0; t < swaptries; t++) {
+      int ci, cj, cjmin, cjrange;
+      do { ci = (int)(draw() * n); } while (ci < 0 || ci >= n);
+      if (n < 2 * SWAPDIST + 3) {
+        cjmin = 0;
+        cjrange = n;
+      } else {
+        cjmin = std::max(0, ci - SWAPDIST);
+        cjrange = std::min(n, ci + SWAPDIST) - cjmin;
+      }
+      do { cj = cjmin + (int)(draw() * cjrange); } while (cj == ci || cj < 0 || cj >= n);
+      const int p = rank_of(b[ci]), q = rank_of(b[cj]);
+      const int hi = std::max(ci, cj), lo = std::min(ci, cj), phi = std::max(p, q), plo = std::min(p, q);
+      if (p >= 0 && q >= 0) tcr[(size_t)phi * n + plo]++;
+      scr[(size_t)hi * n + lo]++;
+      const double w = exp((b[ci] - b[cj]) * (Sr[cj] - Sr[ci]));
+      if (w >= 1.0 || w > draw()) {
+        std::swap(b[ci], b[cj]);
+        scr[(size_t)lo * n + hi]++;
+        if (p >= 0 && q >= 0) tcr[(size_t)plo * n + phi]++;
+        if (ci == 0 || cj == 0) ok0 = 1;
+      }
+    }
+    if (used) used[run] = k;
+    if (swap0ok) swap0ok[run] = ok0;
+  }
+  r = c->cuda(cudaMemcpyAsync(c->d_beta, beta.data(), N * 8, cudaMemcpyHostToDevice, c->st), "betas");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_swapcount, sc.data(), sc.size() * 4, cudaMemcpyHostToDevice, c->st), "counts");
+  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_tempcount, tc.data(), tc.size() * 4, cudaMemcpyHostToDevice, c->st), "counts");
+  return r ? r : c->cuda(cudaStreamSynchronize(c->st), "swap");
 }
 
 extern "C" int ima_gpu_get_swapcounts(ima_ctx *c, int run, int32_t *swapcount, int32_t *tempcount)
@@ -2538,6 +2661,7 @@ extern "C" int ima_gpu_treeweight(ima_ctx *c, int ngen, const int32_t *node_off,
   r = tw_check_err(c, "treeweight");
   if (r) return r;
   c->tw_ngen = ngen;
+  c->tw_valid.assign((size_t)ngen, 1);
   c->tw_ntv = ntv;
   c->tw_cc = a.cc;
   c->tw_mc = a.mc;
@@ -2573,6 +2697,9 @@ static int tree_prob_run(ima_ctx *c, int ngroups, const int32_t *group_off, cons
     const int e = group_end ? group_end[i] : group_off[i + 1];
     if (group_off[i] < 0 || e < group_off[i] || e > c->tw_ngen)
       return c->fail(IMA_ERR_ARG, "group %d (%d..%d) outside the %d genealogies", i, group_off[i], e, c->tw_ngen);
+    for (int g = group_off[i]; g < e; g++)
+      if (!c->tw_valid[g])
+        return c->fail(IMA_ERR_STATE, "group %d: genealogy %d has no weights from the last weights call", i, g);
   }
   if (group_tv)
     for (int i = 0; i < ngroups; i++)
@@ -3073,6 +3200,8 @@ static int chain_weights_run(ima_ctx *c, int nch, const int32_t *chains, const d
   if (r) return r;
   dev_newer(c, nch, chains);  // the lengths of these items changed on the device
   c->tw_ngen = ni;
+  c->tw_valid.assign((size_t)ni, 0);
+  for (int item : sel) c->tw_valid[item] = 1;
   c->tw_ntv = c->nchains;
   c->tw_cc = a.cc;
   c->tw_mc = a.mc;
@@ -3400,22 +3529,90 @@ extern "C" int ima_gpu_checkpoint_read(ima_ctx *c, const char *path, ima_mt19937
     if (end < 0 || (size_t)end != want || fseek(F.f, here, SEEK_SET) != 0)
       return c->fail(IMA_ERR_DATA, "%s holds %ld bytes, this context's checkpoint %zu", path, end, want);
   }
-  int r = c->cuda(cudaStreamSynchronize(c->st), "checkpoint");
-  if (r) return r;
-  F.get(c->h_nodes, nn * sizeof(NodeRec));
-  F.get(c->h_t64, nn * 8);
-  F.get(c->h_tff, nn * sizeof(float2));
-  F.get(c->h_sched, c->nsched * sizeof(int16_t));
-  F.get(c->h_nlev, ni * 4);
-  F.get(c->h_len, ni * 8);
-  F.get(c->h_pi, 4 * ni * 8);
-  F.get(c->h_al, c->nal * 4);
-  F.get(c->has_tree.data(), ni);
+  // every section is read into host buffers and checked before any state
+  // of the context is replaced: a bad file leaves the context as it was
+  std::vector<char> nodes(nn * sizeof(NodeRec)), t64(nn * 8), tff(nn * sizeof(float2)), sched(c->nsched * 2),
+      nlev(ni * 4), len(ni * 8), pi(4 * ni * 8), al(c->nal * 4);
+  std::vector<uint8_t> has_tree(ni);
   std::vector<double> pdg(ni), probg(c->nchains), beta(c->nchains);
+  F.get(nodes.data(), nodes.size());
+  F.get(t64.data(), t64.size());
+  F.get(tff.data(), tff.size());
+  F.get(sched.data(), sched.size());
+  F.get(nlev.data(), nlev.size());
+  F.get(len.data(), len.size());
+  F.get(pi.data(), pi.size());
+  F.get(al.data(), al.size());
+  F.get(has_tree.data(), ni);
   F.get(pdg.data(), ni * 8);
   F.get(probg.data(), c->nchains * 8ul);
   F.get(beta.data(), c->nchains * 8ul);
   if (!F.ok) return c->fail(IMA_ERR_DATA, "%s is truncated", path);
+  std::vector<int32_t> pop, moff, cnt, mp;
+  std::vector<uint8_t> has;
+  std::vector<double> mt;
+  std::vector<long long> base;
+  size_t used = 0;
+  if (h.has_labels) {
+    pop.resize(nn);
+    moff.resize(nn + ni);
+    cnt.resize(ni);
+    has.resize(ni);
+    F.get(pop.data(), nn * 4);
+    F.get(moff.data(), (nn + ni) * 4);
+    F.get(cnt.data(), ni * 4);
+    F.get(has.data(), ni);
+    if (!F.ok) return c->fail(IMA_ERR_DATA, "%s is truncated", path);
+    mt.resize((size_t)h.nmig);
+    mp.resize((size_t)h.nmig);
+    base.resize(ni);
+    for (size_t i = 0; i < ni; i++) {
+      if (cnt[i] < 0 || used + cnt[i] > (size_t)h.nmig) return c->fail(IMA_ERR_DATA, "%s: bad event counts", path);
+      F.get(mt.data() + used, (size_t)cnt[i] * 8);
+      F.get(mp.data() + used, (size_t)cnt[i] * 4);
+      base[i] = (long long)used;
+      used += cnt[i];
+    }
+    if (!F.ok) return c->fail(IMA_ERR_DATA, "%s is truncated", path);
+    if (used != (size_t)h.nmig)
+      return c->fail(IMA_ERR_DATA, "%s: event counts sum to %zu, not %d", path, used, (int)h.nmig);
+  }
+  std::vector<double> hval, tvr;
+  std::vector<int32_t> samp;
+  if (h.locus_pops) {
+    hval.resize(c->nloci);
+    tvr.resize((size_t)c->nchains * (h.npops - 1));
+    samp.resize((size_t)c->nloci * h.npops);
+    F.get(hval.data(), hval.size() * 8);
+    F.get(samp.data(), samp.size() * 4);
+    F.get(tvr.data(), tvr.size() * 8);
+    if (!F.ok) return c->fail(IMA_ERR_DATA, "%s is truncated", path);
+    for (int li = 0; li < c->nloci; li++) {
+      int ns = 0;
+      for (int p = 0; p < h.npops; p++) ns += samp[(size_t)li * h.npops + p];
+      if (!(hval[li] > 0) || ns != c->loci[li].d.n)
+        return c->fail(IMA_ERR_DATA, "%s: locus %d populations do not match its %d genes", path, li, c->loci[li].d.n);
+    }
+  }
+  ima_mt19937 g;
+  if (h.has_rng) {
+    F.get(&g, sizeof(g));
+    if (!F.ok) return c->fail(IMA_ERR_DATA, "%s is truncated", path);
+  }
+  // commit
+  int r = c->cuda(cudaStreamSynchronize(c->st), "checkpoint");
+  if (r) return r;
+  memcpy(c->h_nodes, nodes.data(), nodes.size());
+  memcpy(c->h_t64, t64.data(), t64.size());
+  memcpy(c->h_tff, tff.data(), tff.size());
+  memcpy(c->h_sched, sched.data(), sched.size());
+  memcpy(c->h_nlev, nlev.data(), nlev.size());
+  memcpy(c->h_len, len.data(), len.size());
+  memcpy(c->h_pi, pi.data(), pi.size());
+  memcpy(c->h_al, al.data(), al.size());
+  c->has_tree = has_tree;
+  c->tw_ngen = 0;  // weights of the genealogies replaced here are gone
+  c->tw_valid.clear();
   c->dev_lo = INT32_MAX;  // the file is authoritative now
   c->dev_hi = -1;
   c->dirty_lo = 0;        // upload everything with the next flush
@@ -3431,24 +3628,6 @@ extern "C" int ima_gpu_checkpoint_read(ima_ctx *c, const char *path, ima_mt19937
   if (h.has_labels) {
     r = labels_alloc(c);
     if (r) return r;
-    std::vector<int32_t> pop(nn), moff(nn + ni), cnt(ni);
-    std::vector<uint8_t> has(ni);
-    F.get(pop.data(), nn * 4);
-    F.get(moff.data(), (nn + ni) * 4);
-    F.get(cnt.data(), ni * 4);
-    F.get(has.data(), ni);
-    std::vector<double> mt((size_t)h.nmig);
-    std::vector<int32_t> mp((size_t)h.nmig);
-    std::vector<long long> base(ni);
-    size_t used = 0;
-    for (size_t i = 0; i < ni; i++) {
-      if (cnt[i] < 0 || used + cnt[i] > (size_t)h.nmig) return c->fail(IMA_ERR_DATA, "%s: bad event counts", path);
-      F.get(mt.data() + used, (size_t)cnt[i] * 8);
-      F.get(mp.data() + used, (size_t)cnt[i] * 4);
-      base[i] = (long long)used;
-      used += cnt[i];
-    }
-    if (!F.ok) return c->fail(IMA_ERR_DATA, "%s is truncated", path);
     if (used > c->mig_cap) {
       cudaFree(c->d_mig_t);
       cudaFree(c->d_mig_p);
@@ -3468,24 +3647,16 @@ extern "C" int ima_gpu_checkpoint_read(ima_ctx *c, const char *path, ima_mt19937
     c->h_mcnt = cnt;
     c->h_mcap = cnt;
     c->has_labels = has;
+  } else {
+    // the restored genealogies come without labels: none of the old ones apply
+    c->has_labels.assign(ni, 0);
   }
   if (h.locus_pops) {
-    std::vector<double> hval(c->nloci), tvr((size_t)c->nchains * (h.npops - 1));
-    std::vector<int32_t> samp((size_t)c->nloci * h.npops);
-    F.get(hval.data(), hval.size() * 8);
-    F.get(samp.data(), samp.size() * 4);
-    F.get(tvr.data(), tvr.size() * 8);
-    if (!F.ok) return c->fail(IMA_ERR_DATA, "%s is truncated", path);
     r = ima_gpu_set_locus_pops(c, hval.data(), samp.data());
     if (r) return r;
     c->h_tvr = tvr;
   }
-  if (h.has_rng) {
-    ima_mt19937 g;
-    F.get(&g, sizeof(g));
-    if (!F.ok) return c->fail(IMA_ERR_DATA, "%s is truncated", path);
-    if (rng) *rng = g;
-  }
+  if (h.has_rng && rng) *rng = g;
   return c->cuda(cudaDeviceSynchronize(), "checkpoint");
 }
 

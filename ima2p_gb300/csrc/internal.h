@@ -69,7 +69,8 @@ struct Pools {
   uint8_t *is_valid;        // IS: the item's site cache matches its topology
   double *pdg_new;          // last evaluated log P(D|G) per item
   // HKY state
-  float4 *part;             // FP32 partials
+  float4 *part;             // FP32 partials (float-float form: the hi parts)
+  float4 *partlo;           // float-float form: the lo parts (null until first used)
   int32_t *pexp;            // FP32 partial power-of-two exponents
   double *part64;           // FP64 partials (4 per pattern)
   double *psf64;            // FP64 log scale factors
@@ -82,13 +83,17 @@ void launch_is_sumlogk(const Pools &P, int item, int locus, int maxn, int maxS, 
 void launch_is(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int maxS, double *result,
                int32_t *status, int32_t *site_node, cudaStream_t st);
 // variant: launch shape chosen by the batch autotuner (0 is the default)
-constexpr int HKY_FAST_VARIANTS = 5;  // 128 threads, 64, 256, 128 without the shared-memory cache,
-                                      // 128 with registers for 8 CTAs per SM instead of 12
+constexpr int HKY_FAST_VARIANTS = 5;  // float-float: 128 threads (6 CTAs per SM), 64, 256, 128 without the
+                                      // shared-memory cache, 128 with registers for 4 CTAs per SM;
+                                      // FP32: 128 threads (12 CTAs per SM), 64, 256, 128 uncached, 128 at 8
 constexpr int SW_FAST_VARIANTS = 3;   // 8 chain-loci per CTA, 4, 16
 void launch_hky_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int maxS, int variant,
                      double *result, int32_t *status, cudaStream_t st);
+void launch_hky_fp32(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int maxS, int variant,
+                     double *result, int32_t *status, cudaStream_t st);
 void launch_hky_fp64(const Pools &P, const ReqDev *reqs, int nreq, int maxn, double *result,
                      int32_t *status, cudaStream_t st);
+int hky_init_tables();
 void launch_hky_commit(const Pools &P, const int32_t *items, const uint8_t *accept, int n,
                        cudaStream_t st);
 void launch_sw_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int variant, double *result,

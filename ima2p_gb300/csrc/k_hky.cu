@@ -19,11 +19,22 @@
 // power of two whose exponent is kept as an integer, so the log scale factor
 // carries no rounding; the root sum log(sum_j pi_j L_j) is formed from an
 // FP32 mantissa log and the integer exponent, accumulated in FP64.
+// Float-float form (the default fast precision): the same kernel with every
+// partial, coefficient and product as a float-float pair (about 46 bits):
+// the hi parts in the FP32 partial array, the lo parts in a second one, the
+// exponents shared.  An FP32 partial's rounding (6e-8) repeats in every
+// site of a pattern, so a 1000-bp locus of FP32 pruning is off by ~1e-4 in
+// log L; the pairs bring that below 1e-8.
 // FP64 form: the reference's arithmetic -- partials divided by their maximum,
 // log(max) accumulated into an FP64 scale factor.
+#include <cmath>
+
+#include "ff.cuh"
 #include "internal.h"
 
 namespace {
+
+__constant__ FFConsts c_ffh;  // ln 2 and the log table (filled by hky_init_tables)
 
 constexpr int HKY_BS = 128;
 constexpr double LN2 = 0.69314718055994530941723212146;
@@ -114,6 +125,76 @@ __device__ __forceinline__ void hky_apply(const HkyCoef &K, const float *pi, flo
   v[3] = fmaf(K.dY, L.w, tY);
 }
 
+// Float-float coefficients of one branch, K = {E1, b_R, b_Y, d_R, d_Y} as
+// (hi, lo) pairs: E1 = 1 - e^-b, E2_c = 1 - e^(-b A_c), d_c = e^(-b A_c)
+// taken directly (1 - E2_c would cancel on long branches).
+__device__ __forceinline__ void hky_coef_ff(const ff *pi, ff kpa, ff b, float *K)
+{
+  const ff PR = ff_add(pi[0], pi[2]), PY = ff_add(pi[1], pi[3]);
+  ff e1, m1, eR, mR, eY, mY;
+  ff_exp_expm1_neg(ff_neg(b), c_ffh, &e1, &m1);
+  ff_exp_expm1_neg(ff_neg(ff_mul(b, ff_add_f(ff_mul(PR, kpa), 1.0f))), c_ffh, &eR, &mR);
+  ff_exp_expm1_neg(ff_neg(ff_mul(b, ff_add_f(ff_mul(PY, kpa), 1.0f))), c_ffh, &eY, &mY);
+  const ff E1 = ff_neg(m1), ER = ff_neg(mR), EY = ff_neg(mY);
+  const ff bR = ff_div(ff_sub(ER, ff_mul(E1, ff_add_f(ff_neg(PR), 1.0f))), PR);
+  const ff bY = ff_div(ff_sub(EY, ff_mul(E1, ff_add_f(ff_neg(PY), 1.0f))), PY);
+  K[0] = E1.hi; K[1] = E1.lo;
+  K[2] = bR.hi; K[3] = bR.lo;
+  K[4] = bY.hi; K[5] = bY.lo;
+  K[6] = eR.hi; K[7] = eR.lo;
+  K[8] = eY.hi; K[9] = eY.lo;
+}
+
+// Every operand of the pruning products is >= 0, so these sums never cancel.
+// a*b + c:
+__device__ __forceinline__ ff ff_fma_pos(ff a, ff b, ff c)
+{
+  const float p = __fmul_rn(a.hi, b.hi);
+  const float pe = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, __fmaf_rn(a.hi, b.hi, -p)));
+  const ff s = two_sum(p, c.hi);
+  return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(pe, c.lo)));
+}
+
+struct HkyCoefFF {
+  ff a, bR, bY, dR, dY;
+};
+__device__ __forceinline__ HkyCoefFF load_coef_ff(const float *Kp)
+{
+  HkyCoefFF K;
+  K.a = ff_make(Kp[0], Kp[1]);
+  K.bR = ff_make(Kp[2], Kp[3]);
+  K.bY = ff_make(Kp[4], Kp[5]);
+  K.dR = ff_make(Kp[6], Kp[7]);
+  K.dY = ff_make(Kp[8], Kp[9]);
+  return K;
+}
+// P(b) applied to a tip observed in state st: column st of P(b)
+__device__ __forceinline__ void hky_apply_tip_ff(const HkyCoefFF &K, const ff *pi, int st, ff *v)
+{
+  const ff p = st == 0 ? pi[0] : st == 1 ? pi[1] : st == 2 ? pi[2] : pi[3];
+  const bool isR = (st & 1) == 0;
+  const ff tR = ff_mul(isR ? K.bR : K.a, p), tY = ff_mul(isR ? K.a : K.bY, p);
+  const ff own = ff_add(isR ? tR : tY, isR ? K.dR : K.dY);  // the observed state's entry
+  v[0] = st == 0 ? own : tR;
+  v[2] = st == 2 ? own : tR;
+  v[1] = st == 1 ? own : tY;
+  v[3] = st == 3 ? own : tY;
+}
+// v_j = E1 S_o + b_c S_c + d_c L_j
+__device__ __forceinline__ void hky_apply_ff(const HkyCoefFF &K, const ff *pi, const ff *L, ff *v)
+{
+  const ff SR = ff_fma_pos(pi[2], L[2], ff_mul(pi[0], L[0]));
+  const ff SY = ff_fma_pos(pi[3], L[3], ff_mul(pi[1], L[1]));
+  const ff tR = ff_fma_pos(K.bR, SR, ff_mul(K.a, SY));
+  const ff tY = ff_fma_pos(K.bY, SY, ff_mul(K.a, SR));
+  v[0] = ff_fma_pos(K.dR, L[0], tR);
+  v[2] = ff_fma_pos(K.dR, L[2], tR);
+  v[1] = ff_fma_pos(K.dY, L[1], tY);
+  v[3] = ff_fma_pos(K.dY, L[3], tY);
+}
+
+__device__ __forceinline__ ff ff_of(float2 v) { return ff_make(v.x, v.y); }
+
 // Shared-memory carve-up, identical on host (sizing) and device.
 struct HkyLayout {
   size_t nd, fresh, order, total;
@@ -196,8 +277,11 @@ __device__ __forceinline__ int expo_of(float m)  // floor(log2(m)) for normal m 
 // With CACHE, the partials this launch computes are also kept in shared
 // memory ([internal node][pattern]) and daughters are read from there instead
 // of making an L2 round trip per level.  BS threads per CTA, registers for
-// MINB resident CTAs per SM.
-template <bool CACHE, int BS, int MINB>
+// MINB resident CTAs per SM.  FF: every value a float-float pair (the lo
+// parts of the partials in P.partlo); otherwise FP32 (which clears the lo
+// parts of what it writes when they exist, so a later FF evaluation reads
+// its partials as exact pairs).
+template <bool FF, bool CACHE, int BS, int MINB>
 __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *reqs,
                                                      double *result, int32_t *status, int maxnl,
                                                      int cache_S, int tip_cap)
@@ -209,7 +293,7 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
   const int n = it.n, nl = 2 * n - 1, S = L.nsites, nint = n - 1;
   const int nlev = P.nlev[R.item];
   const HkyLayout lay = hky_layout(maxnl, sizeof(float));
-  float *Pm = reinterpret_cast<float *>(smem);               // [maxnl][16]: 5 coefficients per branch
+  float *Pm = reinterpret_cast<float *>(smem);               // [maxnl][16]: 5 coefficients per branch (FF: pairs)
   Tree T;
   T.nd = reinterpret_cast<NodeRec *>(smem + lay.nd);
   T.fresh = reinterpret_cast<uint8_t *>(smem + lay.fresh);
@@ -222,11 +306,12 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
   const size_t tipb = ((size_t)tip_cap + 15) & ~size_t(15);
   const bool tips = n * S <= tip_cap;
   float4 *cpart = reinterpret_cast<float4 *>(smem + lay.total + tipb);  // [nint][cache_S]
-  int32_t *cexp = reinterpret_cast<int32_t *>(cpart + (size_t)(maxnl / 2) * cache_S);
+  float4 *cpartlo = cpart + (FF ? (size_t)(maxnl / 2) * cache_S : 0);   // FF: lo parts
+  int32_t *cexp = reinterpret_cast<int32_t *>(cpartlo + (size_t)(maxnl / 2) * cache_S);
   __shared__ double red_d[BS / 32];
   __shared__ long long red_e[BS / 32];
-  __shared__ float spi[4];
-  __shared__ float smu;
+  __shared__ float2 spi[4];   // pi (FP32: .x only)
+  __shared__ float2 smu, skpa;
 
   const int tid = threadIdx.x;
   const bool full = (R.e[0] == -1);
@@ -244,8 +329,11 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
   }
   if (tid == 0) {
     const double *pid = P.pi + 4 * (size_t)R.item;
-    smu = (float)(R.u / ((double)L.totsites * standfactor(pid, R.par)));
-    for (int j = 0; j < 4; j++) spi[j] = (float)pid[j];
+    const double mu = R.u / ((double)L.totsites * standfactor(pid, R.par));
+    const double kp = R.par - 1.0;
+    smu = make_float2((float)mu, (float)(mu - (double)(float)mu));
+    skpa = make_float2((float)kp, (float)(kp - (double)(float)kp));
+    for (int j = 0; j < 4; j++) spi[j] = make_float2((float)pid[j], (float)(pid[j] - (double)(float)pid[j]));
   }
   __syncthreads();
   if (!full && tid == 0) {  // the reference's propagation rule, bottom-up
@@ -260,20 +348,28 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
   }
   if (!full) __syncthreads();
   const float2 *tff = P.tff + it.node_off;
-  const float kpa = (float)(R.par - 1.0);
   for (int c = tid; c < nl; c += BS) {
     int d = T.nd[c].down;
     if (d < 0 || !T.fresh[d]) continue;
-    float pil[4] = {spi[0], spi[1], spi[2], spi[3]};
-    hky_coef_fast(pil, kpa, smu * branch_ff(T.nd, tff, c), Pm + 16 * c);
+    if constexpr (FF) {
+      const ff pif[4] = {ff_of(spi[0]), ff_of(spi[1]), ff_of(spi[2]), ff_of(spi[3])};
+      const int u = T.nd[c].up0;
+      const ff tc = ff_of(tff[c]);
+      const ff br = (u < 0) ? tc : ff_sub(tc, ff_of(tff[u]));
+      hky_coef_ff(pif, ff_of(skpa), ff_mul(ff_of(smu), br), Pm + 16 * c);
+    } else {
+      float pil[4] = {spi[0].x, spi[1].x, spi[2].x, spi[3].x};
+      hky_coef_fast(pil, skpa.x, smu.x * branch_ff(T.nd, tff, c), Pm + 16 * c);
+    }
   }
   __syncthreads();
 
   const size_t slot_stride = (size_t)nint * S;
   float4 *part = P.part + it.part_off;
+  float4 *partlo = P.partlo ? P.partlo + it.part_off : nullptr;
   int32_t *pexp = P.pexp + it.part_off;
   const int8_t *seq = P.seq + L.seq_off;
-  const float pi4[4] = {spi[0], spi[1], spi[2], spi[3]};
+  const float pi4[4] = {spi[0].x, spi[1].x, spi[2].x, spi[3].x};
   // warps take (node, 32-pattern chunk) pairs of a level in turn, so a warp
   // works on one node at a time and its children's coefficients stay in
   // registers; lanes are patterns
@@ -287,52 +383,99 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
       const int node = T.order[beg + jj];
       if (!T.fresh[node] || i >= S) continue;
       const int cc[2] = {T.nd[node].up0, T.nd[node].up1};
-      float v[2][4];
       int e = 0;
+      float4 ov, ol = make_float4(0.f, 0.f, 0.f, 0.f);
+      if constexpr (FF) {
+        const ff pif[4] = {ff_of(spi[0]), ff_of(spi[1]), ff_of(spi[2]), ff_of(spi[3])};
+        ff v[2][4];
 #pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int c = cc[h];
-        const float *Kp = Pm + 16 * c;
-        const HkyCoef K = {Kp[0], Kp[1], Kp[2], Kp[3], Kp[4]};
-        if (c < n) {
-          hky_apply_tip(K, pi4, tips ? stip[c * S + i] : seq[(size_t)c * S + i], v[h]);
-        } else {
-          float4 Lc;
-          if (CACHE && T.fresh[c]) {
-            const size_t ci = (size_t)(c - n) * cache_S + i;
-            Lc = cpart[ci];
-            e += cexp[ci];
+        for (int h = 0; h < 2; h++) {
+          const int c = cc[h];
+          const HkyCoefFF K = load_coef_ff(Pm + 16 * c);
+          if (c < n) {
+            hky_apply_tip_ff(K, pif, tips ? stip[c * S + i] : seq[(size_t)c * S + i], v[h]);
           } else {
-            const int rs = T.fresh[c] ? 1 - T.slot[c] : T.slot[c];
-            const size_t idx = rs * slot_stride + (size_t)(c - n) * S + i;
-            Lc = part[idx];
-            e += pexp[idx];
+            float4 hi, lo;
+            if (CACHE && T.fresh[c]) {
+              const size_t ci = (size_t)(c - n) * cache_S + i;
+              hi = cpart[ci];
+              lo = cpartlo[ci];
+              e += cexp[ci];
+            } else {
+              const int rs = T.fresh[c] ? 1 - T.slot[c] : T.slot[c];
+              const size_t idx = rs * slot_stride + (size_t)(c - n) * S + i;
+              hi = part[idx];
+              lo = partlo[idx];
+              e += pexp[idx];
+            }
+            const ff Lc[4] = {ff_make(hi.x, lo.x), ff_make(hi.y, lo.y), ff_make(hi.z, lo.z), ff_make(hi.w, lo.w)};
+            hky_apply_ff(K, pif, Lc, v[h]);
           }
-          hky_apply(K, pi4, Lc, v[h]);
         }
-      }
-      float4 ov = make_float4(v[0][0] * v[1][0], v[0][1] * v[1][1], v[0][2] * v[1][2], v[0][3] * v[1][3]);
-      // rescale by an exact 2^40 only when the largest entry drops below
-      // 2^-40: products of two daughters then stay above 2^-80 (normal)
-      const float m = fmaxf(fmaxf(ov.x, ov.y), fmaxf(ov.z, ov.w));
-      if (m < 9.094947e-13f) {
-        const float up = 1.0995116e12f;  // 2^40
-        ov.x *= up; ov.y *= up; ov.z *= up; ov.w *= up;
-        e -= 40;
-        if (m * up < 9.094947e-13f) {  // very small value: normalise exactly
-          const float mm = m * up;
-          const int k = (mm > 0.f) ? expo_of(mm) : 0;
+        ff o[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) o[j] = ff_mul(v[0][j], v[1][j]);
+        // normalise by an exact power of two when the largest entry drops
+        // below 2^-20: the lo parts (2^-24 below) stay far from subnormal
+        const float m = fmaxf(fmaxf(o[0].hi, o[1].hi), fmaxf(o[2].hi, o[3].hi));
+        if (m < 9.5367432e-07f && m > 0.f) {
+          const int k = expo_of(m);
           const float sc = pow2f(-k);
-          ov.x *= sc; ov.y *= sc; ov.z *= sc; ov.w *= sc;
+#pragma unroll
+          for (int j = 0; j < 4; j++) o[j] = ff_make(o[j].hi * sc, o[j].lo * sc);
           e += k;
+        }
+        ov = make_float4(o[0].hi, o[1].hi, o[2].hi, o[3].hi);
+        ol = make_float4(o[0].lo, o[1].lo, o[2].lo, o[3].lo);
+      } else {
+        float v[2][4];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const int c = cc[h];
+          const float *Kp = Pm + 16 * c;
+          const HkyCoef K = {Kp[0], Kp[1], Kp[2], Kp[3], Kp[4]};
+          if (c < n) {
+            hky_apply_tip(K, pi4, tips ? stip[c * S + i] : seq[(size_t)c * S + i], v[h]);
+          } else {
+            float4 Lc;
+            if (CACHE && T.fresh[c]) {
+              const size_t ci = (size_t)(c - n) * cache_S + i;
+              Lc = cpart[ci];
+              e += cexp[ci];
+            } else {
+              const int rs = T.fresh[c] ? 1 - T.slot[c] : T.slot[c];
+              const size_t idx = rs * slot_stride + (size_t)(c - n) * S + i;
+              Lc = part[idx];
+              e += pexp[idx];
+            }
+            hky_apply(K, pi4, Lc, v[h]);
+          }
+        }
+        ov = make_float4(v[0][0] * v[1][0], v[0][1] * v[1][1], v[0][2] * v[1][2], v[0][3] * v[1][3]);
+        // rescale by an exact 2^40 only when the largest entry drops below
+        // 2^-40: products of two daughters then stay above 2^-80 (normal)
+        const float m = fmaxf(fmaxf(ov.x, ov.y), fmaxf(ov.z, ov.w));
+        if (m < 9.094947e-13f) {
+          const float up = 1.0995116e12f;  // 2^40
+          ov.x *= up; ov.y *= up; ov.z *= up; ov.w *= up;
+          e -= 40;
+          if (m * up < 9.094947e-13f) {  // very small value: normalise exactly
+            const float mm = m * up;
+            const int k = (mm > 0.f) ? expo_of(mm) : 0;
+            const float sc = pow2f(-k);
+            ov.x *= sc; ov.y *= sc; ov.z *= sc; ov.w *= sc;
+            e += k;
+          }
         }
       }
       const size_t widx = (1 - T.slot[node]) * slot_stride + (size_t)(node - n) * S + i;
       part[widx] = ov;
+      if (partlo) partlo[widx] = ol;
       pexp[widx] = e;
       if (CACHE) {
         const size_t ci = (size_t)(node - n) * cache_S + i;
         cpart[ci] = ov;
+        if (FF) cpartlo[ci] = ol;
         cexp[ci] = e;
       }
     }
@@ -346,23 +489,37 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
   double acc = 0.0;
   long long acce = 0;
   for (int i = tid; i < S; i += BS) {
-    float4 Lr;
+    float4 Lr, Ll = make_float4(0.f, 0.f, 0.f, 0.f);
     int er;
     if (CACHE && T.fresh[root]) {
       size_t ci = (size_t)(root - n) * cache_S + i;
       Lr = cpart[ci];
+      if (FF) Ll = cpartlo[ci];
       er = cexp[ci];
     } else {
       size_t idx = rs * slot_stride + (size_t)(root - n) * S + i;
       Lr = part[idx];
+      if (FF) Ll = partlo[idx];
       er = pexp[idx];
     }
-    float f = spi[0] * Lr.x + spi[1] * Lr.y + spi[2] * Lr.z + spi[3] * Lr.w;
-    int k = expo_of(f);
-    float mant = f * pow2f(-k);
-    int mlt = mult[i];
-    acc += (double)mlt * (double)logf(mant);
-    acce += (long long)mlt * (long long)(er + k);
+    const int mlt = mult[i];
+    if constexpr (FF) {
+      ff f = ff_mul(ff_of(spi[0]), ff_make(Lr.x, Ll.x));
+      f = ff_fma_pos(ff_of(spi[1]), ff_make(Lr.y, Ll.y), f);
+      f = ff_fma_pos(ff_of(spi[2]), ff_make(Lr.z, Ll.z), f);
+      f = ff_fma_pos(ff_of(spi[3]), ff_make(Lr.w, Ll.w), f);
+      const int k = expo_of(f.hi);
+      const float sc = pow2f(-k);
+      const ff lg = ff_log(ff_make(f.hi * sc, f.lo * sc), c_ffh);
+      acc += (double)mlt * ((double)lg.hi + (double)lg.lo);
+      acce += (long long)mlt * (long long)(er + k);
+    } else {
+      float f = spi[0].x * Lr.x + spi[1].x * Lr.y + spi[2].x * Lr.z + spi[3].x * Lr.w;
+      int k = expo_of(f);
+      float mant = f * pow2f(-k);
+      acc += (double)mlt * (double)logf(mant);
+      acce += (long long)mlt * (long long)(er + k);
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -530,7 +687,7 @@ size_t hky_smem(int maxn, size_t elem) { return hky_layout(2 * maxn - 1, elem).t
 constexpr size_t HKY_CACHE_BUDGET = 64 * 1024;
 constexpr size_t HKY_TIP_BUDGET = 8 * 1024;
 
-template <int BS, int MINB>
+template <bool FF, int BS, int MINB>
 static void hky_fast_bs(const Pools &P, const ReqDev *reqs, int nreq, int maxnl, int maxS, bool cache_ok,
                         double *result, int32_t *status, cudaStream_t st)
 {
@@ -539,16 +696,16 @@ static void hky_fast_bs(const Pools &P, const ReqDev *reqs, int nreq, int maxnl,
   const size_t maxn = (size_t)(maxnl + 1) / 2;
   const int tip_cap = (maxn * maxS <= HKY_TIP_BUDGET) ? (int)(maxn * maxS) : 0;
   size_t base = hky_smem((int)maxn, sizeof(float)) + (((size_t)tip_cap + 15) & ~size_t(15));
-  size_t cache = (size_t)(maxnl / 2) * maxS * (sizeof(float4) + sizeof(int32_t));
+  size_t cache = (size_t)(maxnl / 2) * maxS * ((FF ? 2 : 1) * sizeof(float4) + sizeof(int32_t));
   if (cache_ok && cache <= HKY_CACHE_BUDGET) {
     size_t sm = base + cache;
     if (sm > 48 * 1024)
-      cudaFuncSetAttribute(k_hky_fast<true, BS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_hky_fast<true, BS, MINB><<<nreq, BS, sm, st>>>(P, reqs, result, status, maxnl, maxS, tip_cap);
+      cudaFuncSetAttribute(k_hky_fast<FF, true, BS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_hky_fast<FF, true, BS, MINB><<<nreq, BS, sm, st>>>(P, reqs, result, status, maxnl, maxS, tip_cap);
   } else {
     if (base > 48 * 1024)
-      cudaFuncSetAttribute(k_hky_fast<false, BS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)base);
-    k_hky_fast<false, BS, MINB><<<nreq, BS, base, st>>>(P, reqs, result, status, maxnl, 0, tip_cap);
+      cudaFuncSetAttribute(k_hky_fast<FF, false, BS, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)base);
+    k_hky_fast<FF, false, BS, MINB><<<nreq, BS, base, st>>>(P, reqs, result, status, maxnl, 0, tip_cap);
   }
 }
 
@@ -558,12 +715,41 @@ void launch_hky_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int
   if (nreq <= 0) return;
   const int maxnl = 2 * maxn - 1;
   switch (variant) {
-    case 1: hky_fast_bs<64, 24>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
-    case 2: hky_fast_bs<256, 6>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
-    case 3: hky_fast_bs<128, 12>(P, reqs, nreq, maxnl, maxS, false, result, status, st); break;
-    case 4: hky_fast_bs<128, 8>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
-    default: hky_fast_bs<128, 12>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
+    case 1: hky_fast_bs<true, 64, 12>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
+    case 2: hky_fast_bs<true, 256, 3>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
+    case 3: hky_fast_bs<true, 128, 6>(P, reqs, nreq, maxnl, maxS, false, result, status, st); break;
+    case 4: hky_fast_bs<true, 128, 4>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
+    default: hky_fast_bs<true, 128, 6>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
   }
+}
+
+void launch_hky_fp32(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int maxS, int variant,
+                     double *result, int32_t *status, cudaStream_t st)
+{
+  if (nreq <= 0) return;
+  const int maxnl = 2 * maxn - 1;
+  switch (variant) {
+    case 1: hky_fast_bs<false, 64, 24>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
+    case 2: hky_fast_bs<false, 256, 6>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
+    case 3: hky_fast_bs<false, 128, 12>(P, reqs, nreq, maxnl, maxS, false, result, status, st); break;
+    case 4: hky_fast_bs<false, 128, 8>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
+    default: hky_fast_bs<false, 128, 12>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
+  }
+}
+
+// ln 2 and the log table of the float-float root sum (once per device)
+int hky_init_tables()
+{
+  FFConsts K{};
+  for (int i = 0; i < 64; i++) {
+    const double v = std::log(1.0 + (2.0 * i + 1.0) / 128.0);
+    K.logtab[i] = make_float2((float)v, (float)(v - (double)(float)v));
+  }
+  const double ln2 = 0.69314718055994530941723212146;
+  const double a = 355.0 / 512.0;
+  K.ln2a = make_float2((float)a, (float)(ln2 - a));
+  K.ln2b = (float)(ln2 - a - (double)(float)(ln2 - a));
+  return cudaMemcpyToSymbol(c_ffh, &K, sizeof(K)) == cudaSuccess ? 0 : -1;
 }
 
 void launch_hky_fp64(const Pools &P, const ReqDev *reqs, int nreq, int maxn, double *result,

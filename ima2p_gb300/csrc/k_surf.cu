@@ -314,10 +314,14 @@ void launch_surface_compat(const SurfArgs &a, double *scratch, cudaStream_t st)
 }
 
 // ======================================================================
-// Allocation-free variant of the FP64 surface, for callers that cannot call
-// cudaMalloc.  Its only scratch -- one (max, sum, sum of squares) triple per
-// point and genealogy chunk -- lives in the fixed device array below, which
-// every GPU that loads this library holds until the process exits.
+// Allocation-free variant of the FP64 surface, for callers that may not call
+// cudaMalloc: a plugin whose host application owns every device allocation
+// through its own pool.  Its only scratch -- one (max, sum, sum of squares)
+// triple per point and genealogy chunk -- lives in the fixed device array
+// below, which every GPU that loads this library holds until the process
+// exits.  The array's device address is looked up once per device and kept;
+// after a cudaDeviceReset of that device the kept address is stale, so the
+// entry point is not for use after a reset in the same process.
 namespace {
 
 constexpr size_t NOALLOC_SCRATCH_DOUBLES = (size_t)1 << 19;  // 4 MiB
@@ -363,6 +367,9 @@ extern "C" int ima_gpu_surface_fp64_noalloc(const float *rows, int G, int rowlen
   if (nchunks > 64) nchunks = 64;
   size_t fit = NOALLOC_SCRATCH_DOUBLES / ((size_t)npoints * per_point);
   if ((size_t)nchunks > fit) nchunks = (int)fit;
+  // an error already pending on this thread is the caller's: report it
+  // without launching (and leave it pending) rather than take it for ours
+  if (cudaPeekAtLastError() != cudaSuccess) return IMA_ERR_CUDA;
   double *scratch = nullptr;
   int r = noalloc_scratch(&scratch);
   if (r) return r;

@@ -32,13 +32,13 @@
 //     another warp or chunk found moves it, so every warp screens the same
 //     terms on every run.
 //   * The order: each term's weight w = exp(p - ref), with ref the pre-pass
-//     bound, is added as a 192-bit fixed-point integer (w * 2^64) by 64-bit
+//     bound, is added as a 256-bit fixed-point integer (w * 2^64) by 64-bit
 //     shared-memory atomics with exact carries.  Integer addition is
 //     associative, so the sum does not depend on arrival order; the chunk
 //     sums are merged in chunk order.
-// A term with w >= 2^48 (the pre-pass bound more than 33 nats below the
+// A term with w >= 2^80 (the pre-pass bound more than 55 nats below the
 // term) would leave the fixed-point range: the point is flagged and its log
-// density is taken again in FP64 over every genealogy (k_surf_tc_exact).
+// density is taken again over every genealogy (k_surf_tc_exact).
 //
 // Every wait is bounded: a wait that runs out sets the error word, the CTA
 // stops issuing work, waits (bounded) for the copies and MMAs it started,
@@ -84,6 +84,8 @@ constexpr int GROUP_COLS = TC_N / COL_GROUPS;      // columns per epilogue warp 
 constexpr int REF_WARPS = 2;             // warps 2-3 recompute candidates exactly
 constexpr int RING = 1024;               // candidate slots per refine warp
 
+constexpr int FIXW = 4;  // 64-bit words of the fixed-point sums
+
 struct TcSmem {
   // full[s]: B tile of stage s landed; done[s]: the MMAs of the tile in stage
   // s completed (stage free, accumulator ready); accempty[a]: accumulator a
@@ -94,21 +96,22 @@ struct TcSmem {
   int epi_done;                       // epilogue warps that have finished
   unsigned head[REF_WARPS];           // slots reserved so far in each ring
   int ring[REF_WARPS][RING];          // candidates: genealogy << 7 | point; -1 = free
-  unsigned long long sum[TC_M][3];    // sum of w * 2^64, w = exp(p - ref), 192-bit fixed point
-  unsigned long long sum2[TC_M][3];   // sum of w^2 * 2^64
+  unsigned long long sum[TC_M][FIXW];   // sum of w * 2^64, w = exp(p - ref), 256-bit fixed point
+  unsigned long long sum2[TC_M][FIXW];  // sum of w^2 * 2^64
   float ref[TC_M];                    // the point's lower bound after the pre-pass
   int ovf[TC_M];                      // a term left the fixed-point range
   float2 phi[TC_M * PHI_STRIDE];      // float-float phi of the CTA's points
 };
 
-// w >= 2^48 (33.27 nats above ref) leaves the range the sums are sized for:
-// 2^24 genealogies of w^2 * 2^64 < 2^96 * 2^64 stay below 2^184
-constexpr double OVF_NATS = 33.0;
+// w >= 2^80 (55.45 nats above ref) leaves the range the sums are sized for:
+// 2^24 genealogies of w^2 * 2^64 < 2^160 * 2^64 stay below 2^248
+constexpr double OVF_NATS = 55.0;
 
-// w * 2^64 as a 192-bit integer, truncated (0 <= w < 2^128)
-__device__ __forceinline__ void fix192(double w, unsigned long long o[3])
+// w * 2^64 as a 256-bit integer, truncated (0 <= w < 2^180)
+__device__ __forceinline__ void fixw(double w, unsigned long long o[FIXW])
 {
-  o[0] = o[1] = o[2] = 0ull;
+#pragma unroll
+  for (int i = 0; i < FIXW; i++) o[i] = 0ull;
   const unsigned long long b = (unsigned long long)__double_as_longlong(w);
   const int e = (int)((b >> 52) & 0x7ff);
   if (!(w > 0.0) || e == 0) return;  // zero or subnormal: nothing at this scale
@@ -120,18 +123,18 @@ __device__ __forceinline__ void fix192(double w, unsigned long long o[3])
     return;
   }
   const int wd = s >> 6, bit = s & 63;
-  if (wd < 3) o[wd] = m << bit;
-  if (bit && wd + 1 < 3) o[wd + 1] = m >> (64 - bit);
+  if (wd < FIXW) o[wd] = m << bit;
+  if (bit && wd + 1 < FIXW) o[wd + 1] = m >> (64 - bit);
 }
 
-// acc += x on a 192-bit integer in shared memory, word by word with 64-bit
+// acc += x on a 256-bit integer in shared memory, word by word with 64-bit
 // atomics; a word that wraps carries one into the next.  Every wrap is seen
 // by exactly one atomic, so the sum is exact whatever the interleaving.
-__device__ __forceinline__ void atomic_add192(unsigned long long *acc, const unsigned long long x[3])
+__device__ __forceinline__ void atomic_addw(unsigned long long *acc, const unsigned long long x[FIXW])
 {
   unsigned long long carry = 0ull;
 #pragma unroll
-  for (int i = 0; i < 3; i++) {
+  for (int i = 0; i < FIXW; i++) {
     unsigned long long out = 0ull;
     if (x[i]) {
       const unsigned long long old = atomicAdd(&acc[i], x[i]);
@@ -145,11 +148,13 @@ __device__ __forceinline__ void atomic_add192(unsigned long long *acc, const uns
   }
 }
 
-__device__ __forceinline__ double fix192_to_double(const unsigned long long w[3])
+__device__ __forceinline__ double fixw_to_double(const unsigned long long w[FIXW])
 {
-  // 2^128, 2^64 and 2^-64 are exact; the order of the two additions is fixed
-  return ((double)w[2] * 3.4028236692093846e38 + (double)w[1] * 18446744073709551616.0 + (double)w[0]) *
-         5.421010862427522e-20;
+  // powers of two are exact; the order of the additions is fixed
+  double v = 0.0;
+#pragma unroll
+  for (int i = FIXW - 1; i >= 0; i--) v = v * 18446744073709551616.0 + (double)w[i];
+  return v * 5.421010862427522e-20;  // 2^-64
 }
 
 __device__ __forceinline__ void set_err(int *err_shared, int *err_global, int code)
@@ -205,11 +210,11 @@ __device__ void refine_loop(const SurfPrep &S, TcSmem &sh, int *gerr, int r, int
         sh.ovf[pl] = 1;
       } else {
         const double w = exp(d);
-        unsigned long long x[3];
-        fix192(w, x);
-        atomic_add192(sh.sum[pl], x);
-        fix192(w * w, x);
-        atomic_add192(sh.sum2[pl], x);
+        unsigned long long x[FIXW];
+        fixw(w, x);
+        atomic_addw(sh.sum[pl], x);
+        fixw(w * w, x);
+        atomic_addw(sh.sum2[pl], x);
       }
     }
     if (!__any_sync(0xffffffffu, have)) break;
@@ -254,7 +259,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   }
   for (int i = threadIdx.x; i < REF_WARPS * RING; i += TC_THREADS) (&sh.ring[0][0])[i] = -1;
   for (int pl = threadIdx.x; pl < TC_M; pl += TC_THREADS) {
-    for (int w = 0; w < 3; w++) sh.sum[pl][w] = sh.sum2[pl][w] = 0ull;
+    for (int w = 0; w < FIXW; w++) sh.sum[pl][w] = sh.sum2[pl][w] = 0ull;
     const int p = ptile * TC_M + pl;
     sh.ref[pl] = p < npoints ? ord2f(S.best[p]) : -INFINITY;
     sh.ovf[pl] = 0;
@@ -425,13 +430,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int p = ptile * TC_M + threadIdx.x;
     if (p < npoints)
       part[(size_t)p * gridDim.y + blockIdx.y] =
-          make_double2(sh.ovf[threadIdx.x] ? -1.0 : fix192_to_double(sh.sum[threadIdx.x]),
-                       fix192_to_double(sh.sum2[threadIdx.x]));
+          make_double2(sh.ovf[threadIdx.x] ? -1.0 : fixw_to_double(sh.sum[threadIdx.x]),
+                       fixw_to_double(sh.sum2[threadIdx.x]));
   }
 }
 
 // Chunk sums added in chunk order: q = ln G - (ref + ln sum).  A point with
-// a flagged chunk is left to k_surf_tc_exact.
+// a flagged chunk goes to the list k_surf_tc_exact works through
+// (flag[0] = list length, flag[1..] = points; the list's order does not
+// matter, each point is taken on its own).
 __global__ void k_surf_tc_merge(SurfArgs a, SurfPrep S, const double2 *part, int nchunks, int *flag)
 {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -444,52 +451,66 @@ __global__ void k_surf_tc_merge(SurfArgs a, SurfPrep S, const double2 *part, int
     s += w[c].x;
     s2 += w[c].y;
   }
-  flag[p] = ovf;
-  if (ovf) return;
+  if (ovf) {
+    flag[1 + atomicAdd(&flag[0], 1)] = p;
+    return;
+  }
   const double ref = (double)ord2f(S.best[p]);
   a.q[p] = log((double)a.G) - (ref + log(s));
   if (a.ess) a.ess[p] = s * s / s2;
 }
 
-// The flagged points in FP64 over every genealogy, a warp per point: the
-// maximum, then the sums of exp(p - max), lanes over genealogies and a fixed
-// shuffle tree, so these too are reproducible.
-__global__ void k_surf_tc_exact(SurfArgs a, SurfPrep S, const int *flag)
+constexpr int EX_THREADS = 512;
+
+// The listed points over every genealogy, a CTA per point: the exact values
+// (surf_exact, as the refinement computes them) give the maximum M, then
+// the terms within 40 nats of it are summed as exp(p - M) in FP64 (the rest
+// weigh < 2^21 e^-40 = 9e-12 of the sum).  Per-thread sums in genealogy
+// order and a fixed tree keep these reproducible too.
+__global__ void __launch_bounds__(EX_THREADS) k_surf_tc_exact(SurfArgs a, SurfPrep S, const int *flag)
 {
-  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (p >= a.npoints || !flag[p]) return;  // warp-uniform
-  double phi[SURF_K];
-#pragma unroll
-  for (int k = 0; k < SURF_K; k++) {
-    const float2 f = S.phiff[(size_t)p * SURF_K + k];
-    phi[k] = (double)f.x + (double)f.y;
-  }
-  auto term = [&](int g) {
-    const float2 b = S.biasff[g];
-    double v = (double)b.x + (double)b.y;
-#pragma unroll
-    for (int k = 0; k < SURF_K; k++)
-      if (k < S.K) v = fma((double)S.sT[(size_t)k * S.Gpad + g], phi[k], v);
-    return v;
-  };
-  double m = -INFINITY;
-  for (int g = lane; g < a.G; g += 32) m = fmax(m, term(g));
-#pragma unroll
-  for (int o = 16; o >= 1; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  double s = 0.0, s2 = 0.0;
-  for (int g = lane; g < a.G; g += 32) {
-    const double e = exp(term(g) - m);
-    s += e;
-    s2 += e * e;
-  }
-#pragma unroll
-  for (int o = 16; o >= 1; o >>= 1) {
-    s += __shfl_xor_sync(0xffffffffu, s, o);
-    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-  }
-  if (lane == 0) {
-    a.q[p] = log((double)a.G) - (m + log(s));
-    if (a.ess) a.ess[p] = s * s / s2;
+  __shared__ double rs[EX_THREADS], rs2[EX_THREADS];
+  __shared__ float rm[EX_THREADS];
+  __shared__ float2 phi[SURF_K];
+  const int nflag = flag[0], t = threadIdx.x;
+  for (int k = blockIdx.x; k < nflag; k += gridDim.x) {
+    const int p = flag[1 + k];
+    __syncthreads();
+    if (t < SURF_K) phi[t] = S.phiff[(size_t)p * SURF_K + t];
+    __syncthreads();
+    float m = -INFINITY;
+    for (int g = t; g < a.G; g += EX_THREADS) m = fmaxf(m, surf_exact(S, g, S.sT + g, S.Gpad, phi).hi);
+    rm[t] = m;
+    __syncthreads();
+    for (int o = EX_THREADS / 2; o > 0; o >>= 1) {
+      if (t < o) rm[t] = fmaxf(rm[t], rm[t + o]);
+      __syncthreads();
+    }
+    const double M = (double)rm[0];
+    double s = 0.0, s2 = 0.0;
+    for (int g = t; g < a.G; g += EX_THREADS) {
+      const ff y = surf_exact(S, g, S.sT + g, S.Gpad, phi);
+      const double d = ((double)y.hi - M) + (double)y.lo;
+      if (d > -40.0) {
+        const double e = exp(d);
+        s += e;
+        s2 += e * e;
+      }
+    }
+    rs[t] = s;
+    rs2[t] = s2;
+    __syncthreads();
+    for (int o = EX_THREADS / 2; o > 0; o >>= 1) {
+      if (t < o) {
+        rs[t] += rs[t + o];
+        rs2[t] += rs2[t + o];
+      }
+      __syncthreads();
+    }
+    if (t == 0) {
+      a.q[p] = log((double)a.G) - (M + log(rs[0]));
+      if (a.ess) a.ess[p] = rs[0] * rs[0] / rs2[0];
+    }
   }
 }
 
@@ -593,9 +614,10 @@ __global__ void k_tc_selftest_check(const float *D, int *bad, float *maxerr)
 // ---------------------------------------------------------------- host
 size_t surface_tc_scratch_bytes(int G, int npoints)
 {
-  // prepared operands | chunk sums (double2 per point and chunk) | flags
+  // prepared operands | chunk sums (double2 per point and chunk) | the
+  // list of points to retake (a count, then points)
   return surf_prep_bytes(G, npoints) + (size_t)npoints * SURF_MAX_CHUNKS * sizeof(double2) +
-         (size_t)npoints * sizeof(int) + 1024;
+         (size_t)(npoints + 1) * sizeof(int) + 1024;
 }
 
 namespace {
@@ -657,8 +679,9 @@ int launch_surface_tc(const SurfArgs &a, void *scratch, size_t scratch_bytes, in
   if (pre) k_surf_tc<<<dim3(ptiles, nchunks), TC_THREADS, sm, st>>>(S, a.npoints, per, PRE_STRIDE, part, d_err);
   nchunks = surf_tc_chunks(ptiles, ntiles, nsm, &per);
   k_surf_tc<<<dim3(ptiles, nchunks), TC_THREADS, sm, st>>>(S, a.npoints, per, 0, part, d_err);
+  cudaMemsetAsync(flag, 0, sizeof(int), st);
   k_surf_tc_merge<<<(a.npoints + 127) / 128, 128, 0, st>>>(a, S, part, nchunks, flag);
-  k_surf_tc_exact<<<(a.npoints * 32 + 255) / 256, 256, 0, st>>>(a, S, flag);
+  k_surf_tc_exact<<<nsm, EX_THREADS, 0, st>>>(a, S, flag);
   // rows, points, seed, pre-pass, pass, merge, FP64 retake of flagged points
   *nkernels = (rows_ready ? 0 : 1) + 5 + (pre ? 1 : 0);
   return 0;

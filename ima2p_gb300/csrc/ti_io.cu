@@ -172,13 +172,16 @@ extern "C" int ima_ti_read_binary(const char *path, int *G, int *rowlen, float *
     fclose(f);
     return IMA_ERR_DATA;
   }
-  *rowlen = hdr[0];
-  *G = hdr[1];
   int r = IMA_OK;
   if (rows) {
-    if (hdr[1] > rows_cap) r = IMA_ERR_TOO_LARGE;
+    // *rowlen on input: the row length the caller sized rows for; the file
+    // may have changed since the header call
+    if (hdr[0] != *rowlen) r = IMA_ERR_DATA;
+    else if (rows_cap < 0 || hdr[1] > rows_cap) r = IMA_ERR_TOO_LARGE;
     else if (fread(rows, sizeof(float), (size_t)hdr[0] * hdr[1], f) != (size_t)hdr[0] * hdr[1]) r = IMA_ERR_DATA;
   }
+  *rowlen = hdr[0];
+  *G = hdr[1];
   fclose(f);
   return r;
 }

@@ -131,7 +131,7 @@ def make_hky(seed=1002, nloci=50, nch=32, ncopies=20, nbases=1000):
         for ci in range(nch):
             trees[(ci, li)] = g0 if ci == 0 else synth.two_pop_tree(rng, ncopies, ncopies, 10.0, 0.2, 1.5)
             pis[(ci, li)] = loc.pi
-    return Workload("hky", "config2-hky-fp32: 2 pops, %d HKY loci x (%d+%d) x %d bp, %d chains, "
+    return Workload("hky", "config2-hky: 2 pops, %d HKY loci x (%d+%d) x %d bp, %d chains, "
                            "full re-evaluation of every chain-locus per step" % (nloci, ncopies, ncopies, nbases, nch),
                     loci, 1, nch, trees, np.tile(ul, (nch, 1)), np.tile(kap, (nch, 1)), pis, {})
 

@@ -48,8 +48,10 @@ typedef struct ima_ctx ima_ctx;
 #define IMA_MODEL_SW 2
 
 /* arithmetic of an evaluation */
-#define IMA_PREC_FAST 0            /* FP32 pruning / float-float Bessel, FP64 sums */
+#define IMA_PREC_FAST 0            /* float-float pruning and Bessel, FP64 sums   */
 #define IMA_PREC_FP64 1            /* plain FP64 per chain-locus                  */
+#define IMA_PREC_FP32 2            /* HKY: plain FP32 pruning (log L off by ~1e-4
+                                      on a 1000-bp locus); IS, SW as IMA_PREC_FAST */
 
 /* per chain-locus evaluation status */
 #define IMA_EVAL_OK 0
@@ -141,7 +143,11 @@ int ima_gpu_get_dlikeA(ima_ctx *ctx, int ci, int li, int ai, double *dlikeA);
  *                of likelihoodSW (ignored for IS; NULL = 1.0)
  *   edits      : 4 dirty node ids per pair for HKY (NULL = full recompute)
  *   ai         : SW marker per pair (NULL = 0)
- *   precision  : IMA_PREC_FAST or IMA_PREC_FP64
+ *   precision  : IMA_PREC_FAST, IMA_PREC_FP64 or IMA_PREC_FP32.  HKY partials
+ *                of IMA_PREC_FAST and IMA_PREC_FP32 share their slots: a
+ *                node last computed in FP32 enters a later float-float
+ *                evaluation of its ancestors with FP32 accuracy (e1 = -1
+ *                recomputes every node)
  *   result     : log P(D|G) per pair (host)
  *   status     : IMA_EVAL_* per pair (host, may be NULL)
  * Staged requests can be replayed without host copies through the batch
@@ -182,6 +188,9 @@ int ima_gpu_flush_genealogies(ima_ctx *ctx);
 int ima_gpu_setheat(ima_ctx *ctx, double hval1, double hval2, int heatmode);
 int ima_gpu_get_betas(ima_ctx *ctx, double *beta);        /* nchains values */
 int ima_gpu_set_betas(ima_ctx *ctx, const double *beta);
+/* The heat ladder the swap counts index (allbetas, imamp.hpp:1081), nchains
+ * values, for a caller that ran setheat itself. */
+int ima_gpu_set_allbetas(ima_ctx *ctx, const double *allbetas);
 /* G.pdg of every chain-locus ([nchains][nloci]) and allpcalc.probg per chain. */
 int ima_gpu_set_pdg(ima_ctx *ctx, const double *pdg);
 int ima_gpu_get_pdg(ima_ctx *ctx, double *pdg);
@@ -195,6 +204,15 @@ int ima_gpu_get_probg(ima_ctx *ctx, double *probg);
  * swap0ok[r] (may be NULL) as the reference returns it. */
 int ima_gpu_swapchains(ima_ctx *ctx, int swaptries, int include_probg, const double *uniforms,
                        int stride, uint64_t seed, int32_t *used, int32_t *swap0ok);
+/* The same attempts for a caller whose generator must be drawn one value at
+ * a time, as the reference's uniform() is (utilities.cpp:323-427): the
+ * per-chain sums come from the device, the attempts call uniform(arg)
+ * exactly where swapchains (swapchains.cpp:549-605) calls uniform() -- ci,
+ * the cj rejection loop, then U only when w < 1 -- and update the resident
+ * betas and both count matrices.  used[r] (may be NULL): the draws run r
+ * made.  Replaces swapchains() in the reference-side binding. */
+int ima_gpu_swapchains_cb(ima_ctx *ctx, int swaptries, int include_probg, double (*uniform)(void *arg),
+                          void *arg, int32_t *used, int32_t *swap0ok);
 /* swapcount and tempbasedswapcount (imamp.hpp:1123-1129) of run r,
  * chains_per_run^2 each, row-major. */
 int ima_gpu_get_swapcounts(ima_ctx *ctx, int run, int32_t *swapcount, int32_t *tempcount);
@@ -407,8 +425,9 @@ int ima_gpu_rubber_band(ima_ctx *ctx, int nch, const int32_t *chains, const int3
  * genealogies' lengths (G->length) are updated on the device for the
  * likelihoods; then sum_treeinfo and initialize_integrate_tree_prob per chain:
  * probg [nch], q [nch][nth], m [nch][nmg] (q, m may be NULL).  The weights
- * stay available to ima_gpu_tree_prob (genealogy index = chain * nloci +
- * locus). */
+ * of these chains stay available to ima_gpu_tree_prob (genealogy index =
+ * chain * nloci + locus); a group there that takes in a genealogy of a chain
+ * not in this call gives IMA_ERR_STATE. */
 int ima_gpu_chain_weights(ima_ctx *ctx, int nch, const int32_t *chains, const double *tvals,
                           double *probg, double *q, double *m);
 
@@ -456,7 +475,10 @@ int ima_ti_read(int nfiles, const char *const *paths, int rowlen, int maxload, f
                 int *loaded, int *total);
 /* Binary side-car of loaded rows, reloaded without parsing. */
 int ima_ti_write_binary(const char *path, int G, int rowlen, const float *rows);
-/* rows == NULL: header only (*G, *rowlen). */
+/* rows == NULL: header only (*G, *rowlen).  Otherwise *rowlen on input is
+ * the row length rows [rows_cap][*rowlen] was sized for: a file with another
+ * row length gives IMA_ERR_DATA, more than rows_cap rows IMA_ERR_TOO_LARGE,
+ * before anything is read.  *G and *rowlen return the file's header. */
 int ima_ti_read_binary(const char *path, int *G, int *rowlen, float *rows, int rows_cap);
 
 /* ---------------------------------------------------- L-mode peak search
@@ -523,9 +545,10 @@ int ima_gpu_changet_ry1_sweep_mt(ima_ctx *ctx, int nch, const int32_t *chains, c
                                  double *pdgsum, double *probg, double *newt_out);
 
 /* No counterpart in the reference.  The FP64 surface of ima_gpu_surface_eval
- * (IMA_SURF_FP64) for callers that cannot allocate device memory -- code
- * running inside a CUDA graph capture or under a host framework that owns
- * every device allocation.  No context and no allocation: every pointer is
+ * (IMA_SURF_FP64) for callers that may not allocate device memory: a plugin
+ * inside a host application that owns every device allocation through its
+ * own pool (a cudaMalloc there would bypass the pool's accounting and
+ * synchronise the device).  No context and no allocation: every pointer is
  * caller-owned DEVICE memory (rows [G][rowlen] float, lognorm [G] or NULL,
  * x [npoints][np+nm], q and ess [npoints], ess may be NULL); work is queued
  * on `stream` (a cudaStream_t, NULL = legacy default stream) and results are
@@ -535,7 +558,11 @@ int ima_gpu_changet_ry1_sweep_mt(ima_ctx *ctx, int nch, const int32_t *chains, c
  * IMA_ERR_TOO_LARGE without launching anything.  The first call on a device
  * looks up the array's device address (make it before any stream capture).
  * All calls share the array: calls that overlap on the GPU (different
- * streams, or other threads) race, so serialise them. */
+ * streams, or other threads) race, so serialise them.  An error already
+ * pending on the calling thread (cudaPeekAtLastError) is returned as
+ * IMA_ERR_CUDA before anything is launched and left pending.  The looked-up
+ * address does not survive a cudaDeviceReset of the device: do not call this
+ * after a reset in the same process. */
 #define IMA_ERR_TOO_LARGE (-7)
 int ima_gpu_surface_fp64_noalloc(const float *rows, int G, int rowlen, int numpopsizeparams,
                                  int nummigrateparams, int npops, const double *lognorm,
@@ -567,7 +594,8 @@ int ima_gpu_kernel_stats(ima_ctx *ctx, int kind, long long *launches, double *ms
 #define IMA_K_TREEWEIGHT 12
 #define IMA_K_TREE_PROB 13
 #define IMA_K_POPMIG 14
-#define IMA_K_COUNT 15
+#define IMA_K_HKY_FP32 15
+#define IMA_K_COUNT 16
 /* Total kernel launches issued by this library on the context. */
 int ima_gpu_launch_count(ima_ctx *ctx, long long *n);
 /* Write a device buffer larger than L2 (evicts resident data). */

@@ -223,6 +223,22 @@ int ora_findmarginpeaks(int G, int rowlen, const float *g, int np, int nm, const
  * value; ima_main_mpi.cpp:3370-3400), every genealogy kept, at most cap. */
 int ora_ti_load(const char *path, int rowlen, float *rows, int cap);
 
+/* Batched likelihoods over packed arrays on nthreads host threads
+ * (ora_batch.c); return the threads used. */
+int ora_sw_batch(int nitems, const int *n, const long long *node_off, const int *up0, const int *down,
+                 const double *time, const long long *al_off, const int *A, const double *u, const double *tr,
+                 int nthreads, double *out);
+int ora_hky_batch(int nitems, const int *n, const long long *node_off, const int *up0, const int *up1,
+                  const int *down, const double *time, const int *S, const int *totsites,
+                  const long long *seq_off, const int8_t *seq, const long long *mult_off, const int *mult,
+                  const double *pi, const double *u, const double *kappa, int nthreads, double *out);
+int ora_is_batch(int nitems, const int *n, const long long *node_off, const int *up0, const int *up1,
+                 const int *down, const double *time, const int *S, const long long *seq_off, const int8_t *seq,
+                 const double *length, const double *u, const double *sumlogk, int nthreads, double *out,
+                 int *status);
+int ora_jointp_batch(int G, int rowlen, const float *g, int np, int nm, int npops, int modeltype,
+                     const double *lognorm, int npoints, const double *x, int nthreads, double *q, double *ess);
+
 #ifdef __cplusplus
 }
 #endif

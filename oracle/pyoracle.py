@@ -14,6 +14,8 @@ import tempfile
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# the IMa2p source tree the harness and the link-level binding compile
+REFERENCE = os.environ.get("IMA2P_REFERENCE", "/root/reference")
 LIB_PATH = os.path.join(HERE, "libima_oracle.so")
 REF_BIN = os.path.join(HERE, "_ref", "imaref")
 
@@ -40,6 +42,14 @@ D = C.c_double
 
 
 def _declare(L):
+    L.ora_sw_batch.argtypes = [I, P, P, P, P, P, P, P, P, P, I, P]
+    L.ora_sw_batch.restype = I
+    L.ora_hky_batch.argtypes = [I, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, I, P]
+    L.ora_hky_batch.restype = I
+    L.ora_is_batch.argtypes = [I, P, P, P, P, P, P, P, P, P, P, P, P, I, P, P]
+    L.ora_is_batch.restype = I
+    L.ora_jointp_batch.argtypes = [I, I, P, I, I, I, I, P, I, P, I, P, P]
+    L.ora_jointp_batch.restype = I
     L.ora_is_sumlogk.argtypes = [I, I, P, P, P, P, P, P]
     L.ora_is_sumlogk.restype = I
     L.ora_is_likelihood.argtypes = [I, I, P, P, P, P, P, D, D, D, P, P]
@@ -665,3 +675,87 @@ def ref_ry(npops, treestr, tprior, loci, chains, gens, steps, seed, thetaprior, 
         elif f[0] == "MIGT":
             migt[(int(f[1]), int(f[2]))] = np.array([float(v) for v in f[3:]])
     return res, times, migt
+
+
+# ------------------------------------------------------------- batches
+class PackedItems:
+    """Chain-loci of one model packed into flat arrays for the batched C
+    entry points (ora_*_batch): evaluating them costs one call, so timing
+    them times the restated arithmetic, not per-item marshalling.
+
+    items: (kind, genealogy, u, kappa / tr, data) with kind "is" | "hky" |
+    "sw" (all the same); data is the IS seq, the HKYLocus or the alleles."""
+
+    def __init__(self, items):
+        kinds = {it[0] for it in items}
+        assert len(kinds) == 1, kinds
+        self.kind = kinds.pop()
+        self.nitems = len(items)
+        gs = [it[1] for it in items]
+        self.n = _i32([g.n for g in gs])
+        nl = np.array([len(g.up0) for g in gs], np.int64)
+        self.node_off = np.concatenate([[0], np.cumsum(nl)[:-1]]).astype(np.int64)
+        self.up0 = _i32(np.concatenate([g.up0 for g in gs]))
+        self.up1 = _i32(np.concatenate([g.up1 for g in gs]))
+        self.down = _i32(np.concatenate([g.down for g in gs]))
+        self.time = _f64(np.concatenate([g.time for g in gs]))
+        self.u = _f64([it[2] for it in items])
+        self.par = _f64([it[3] for it in items])
+        self.out = np.zeros(self.nitems)
+        if self.kind == "sw":
+            A = [_i32(it[4]) for it in items]
+            self.al_off = np.concatenate([[0], np.cumsum([len(a) for a in A])[:-1]]).astype(np.int64)
+            self.A = _i32(np.concatenate(A))
+        else:
+            # one copy of each distinct data table
+            tabs, idx = [], {}
+            for it in items:
+                key = id(it[4])
+                if key not in idx:
+                    idx[key] = len(tabs)
+                    tabs.append(it[4])
+            seqs = [np.ascontiguousarray(t.seq if self.kind == "hky" else t, np.int8) for t in tabs]
+            soff = np.concatenate([[0], np.cumsum([q.size for q in seqs])[:-1]]).astype(np.int64)
+            self.seq = np.concatenate([q.ravel() for q in seqs]).astype(np.int8)
+            tix = [idx[id(it[4])] for it in items]
+            self.S = _i32([seqs[t].shape[1] for t in tix])
+            self.seq_off = soff[tix]
+            if self.kind == "hky":
+                mults = [_i32(t.mult) for t in tabs]
+                moff = np.concatenate([[0], np.cumsum([len(m) for m in mults])[:-1]]).astype(np.int64)
+                self.mult = _i32(np.concatenate(mults))
+                self.mult_off = moff[tix]
+                self.totsites = _i32([tabs[t].totsites for t in tix])
+                self.pi = _f64(np.concatenate([tabs[t].pi for t in tix]))
+            else:
+                self.length = _f64([g.length() for g in gs])
+                self.sumlogk = np.zeros(self.nitems)
+                self.status = np.zeros(self.nitems, np.int32)
+
+    def run(self, nthreads=1):
+        """Evaluate every item; returns the log likelihoods."""
+        L = lib()
+        if self.kind == "sw":
+            L.ora_sw_batch(self.nitems, _p(self.n), _p(self.node_off), _p(self.up0), _p(self.down), _p(self.time),
+                           _p(self.al_off), _p(self.A), _p(self.u), _p(self.par), int(nthreads), _p(self.out))
+        elif self.kind == "hky":
+            L.ora_hky_batch(self.nitems, _p(self.n), _p(self.node_off), _p(self.up0), _p(self.up1), _p(self.down),
+                            _p(self.time), _p(self.S), _p(self.totsites), _p(self.seq_off), _p(self.seq),
+                            _p(self.mult_off), _p(self.mult), _p(self.pi), _p(self.u), _p(self.par),
+                            int(nthreads), _p(self.out))
+        else:
+            L.ora_is_batch(self.nitems, _p(self.n), _p(self.node_off), _p(self.up0), _p(self.up1), _p(self.down),
+                           _p(self.time), _p(self.S), _p(self.seq_off), _p(self.seq), _p(self.length), _p(self.u),
+                           _p(self.sumlogk), int(nthreads), _p(self.out), _p(self.status))
+        return self.out
+
+
+def jointp_batch(rows, np_, nm, npops, pts, modeltype=0, lognorm=None, nthreads=1):
+    """ora_jointp_exact at every point, on nthreads host threads: (q, ess)."""
+    rows = np.ascontiguousarray(rows, np.float32)
+    pts = _f64(pts)
+    q, ess = np.zeros(len(pts)), np.zeros(len(pts))
+    ln = _f64(lognorm) if lognorm is not None else None
+    lib().ora_jointp_batch(rows.shape[0], rows.shape[1], _p(rows), np_, nm, npops, modeltype,
+                           _p(ln) if ln is not None else None, len(pts), _p(pts), int(nthreads), _p(q), _p(ess))
+    return q, ess

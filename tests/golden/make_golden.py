@@ -57,7 +57,7 @@ from ima2p_gb300 import synth  # noqa: E402
 from oracle import pyoracle as O  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
-SIMDIR = "/root/reference/Simulations"
+SIMDIR = os.path.join(O.REFERENCE, "Simulations")
 
 
 def pack_trees(trees):

@@ -1,7 +1,8 @@
 """The batch autotuner (ima_gpu_batch_autotune) on a small config-4-shaped
-mixed workload: every launch variant of the FP32 kernels gives the plain FP64
-form's likelihoods (HKY within 2e-6 relative, SW within 1e-9 per locus) and
-the variants agree with one another up to the order of the final FP64
+mixed workload: every launch variant of the fast kernels gives the plain
+FP64 form's likelihoods (float-float HKY within 1e-6 per locus, SW within
+1e-9), every variant of the FP32 HKY kernel within 2e-6 relative, and the
+variants agree with one another up to the order of the final FP64
 reduction; the tuned batch replays as a graph with the chosen shapes."""
 import numpy as np
 import pytest
@@ -22,24 +23,28 @@ def _mixed_ctx():
     return wl, ctx, ci, li, wl.u.ravel(), wl.par.ravel()
 
 
-def _check(res, ref, is_hky):
-    np.testing.assert_allclose(res[is_hky], ref[is_hky], rtol=2e-6)
+def _check(res, ref, is_hky, prec):
+    if prec == api.PREC_FP32:
+        np.testing.assert_allclose(res[is_hky], ref[is_hky], rtol=2e-6)
+    else:
+        assert np.max(np.abs(res[is_hky] - ref[is_hky])) <= 1e-6
     assert np.max(np.abs(res[~is_hky] - ref[~is_hky])) <= 1e-9
 
 
-def test_every_variant_matches_fp64_and_autotune_picks_one():
+@pytest.mark.parametrize("prec", [api.PREC_FAST, api.PREC_FP32])
+def test_every_variant_matches_fp64_and_autotune_picks_one(prec):
     wl, ctx, ci, li, u, par = _mixed_ctx()
     is_hky = li < 12
     ref_b = ctx.batch_create(ci, li, u, par, precision=api.PREC_FP64)
     ref_b.run(use_graph=False)
     ref = ref_b.results()[0]
-    b = ctx.batch_create(ci, li, u, par, precision=api.PREC_FAST)
+    b = ctx.batch_create(ci, li, u, par, precision=prec)
     outs = []
     for v in range(HKY_VARIANTS):
         b.set_variants(v, v % SW_VARIANTS)
         b.run(use_graph=True)
         r = b.results()[0]
-        _check(r, ref, is_hky)
+        _check(r, ref, is_hky, prec)
         outs.append(r)
     for r in outs[1:]:
         np.testing.assert_allclose(r, outs[0], rtol=1e-12)

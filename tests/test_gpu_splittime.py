@@ -283,6 +283,34 @@ def test_checkpoint_resume_continues_the_run(tmp_path):
         with pytest.raises(api.ImaError):
             ctx.checkpoint_read(bad)
     ctx.close()
+    # a file whose population section does not match its loci (samppop of
+    # locus 0 one gene too many) is refused before anything is replaced: the
+    # context keeps its genealogies, p(G) and split times
+    import ctypes
+    bad = bytearray(data)
+    ntv = case.nch * (case.npops - 1)
+    off = len(bad) - ctypes.sizeof(api.MT19937) - ntv * 8 - case.nl * case.npops * 4
+    v = int.from_bytes(bytes(bad[off:off + 4]), "little", signed=True) + 1
+    bad[off:off + 4] = v.to_bytes(4, "little", signed=True)
+    badp = tmp_path / "bad_pops.ckp"
+    badp.write_bytes(bytes(bad))
+    ctx = _resident_context(case)
+    splittime.ResidentChainSet(ctx, case.fresh_gens(), [case.d["tv0"]] * case.nch, case.betas,
+                               np.ones(case.nl), case.samps, case.us)
+    keep_t = [ctx.get_times(ci, li, len(base[ci][li].pop)) for ci in range(case.nch) for li in range(case.nl)]
+    keep_pg, keep_tv = ctx.get_probg(), ctx.get_split_times().copy()
+    with pytest.raises(api.ImaError) as ei:
+        ctx.checkpoint_read(badp)
+    assert ei.value.code == api.IMA_ERR_DATA
+    assert np.array_equal(ctx.get_probg(), keep_pg)
+    assert np.array_equal(ctx.get_split_times(), keep_tv)
+    k = 0
+    for ci in range(case.nch):
+        for li in range(case.nl):
+            t, m = ctx.get_times(ci, li, len(base[ci][li].pop))
+            assert np.array_equal(t, keep_t[k][0]) and np.array_equal(m, keep_t[k][1])
+            k += 1
+    ctx.close()
 
 
 def test_chain_weights_on_a_subset_of_chains():
@@ -301,6 +329,14 @@ def test_chain_weights_on_a_subset_of_chains():
         assert np.array_equal(p, p_all[sub])
         assert np.array_equal(q, q_all[sub])
         assert np.array_equal(m, m_all[sub])
+    # after the subset call only chain 1's genealogies hold weights: p(G) of
+    # chain 1 again matches, a group over chain 0 is refused
+    nl = case.nl
+    p1, _, _, _ = ctx.tree_prob(np.array([nl, 2 * nl], np.int32))
+    assert np.array_equal(p1, p_all[[1]])
+    with pytest.raises(api.ImaError) as ei:
+        ctx.tree_prob(np.array([0, nl], np.int32))
+    assert ei.value.code == api.IMA_ERR_STATE
     ctx.close()
 
 

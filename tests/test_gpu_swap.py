@@ -73,3 +73,34 @@ def test_swap_philox_stream_is_deterministic():
     b1, b2 = run(), run()
     assert np.array_equal(b1, b2)
     assert sorted(b1[:32]) == sorted(O.setheat(32, 0.9, 0.8, 1)[1])  # a permutation of the ladder
+
+
+def test_swap_callback_draws_like_the_reference():
+    """ima_gpu_swapchains_cb with the reference's MT19937 drawn one value at a
+    time (the library's copy of the generator, seeded as the harness seeds
+    it): every decision, the betas after every step, both count matrices and
+    the generator's final state match the compiled reference's golden run --
+    no draw more, none fewer."""
+    d = load("golden_swap.npz")
+    for c in range(int(d["ncases"])):
+        p = "c%d_" % c
+        nch, nl, tries, steps, mode, seed = (int(v) for v in d[p + "params"])
+        h1, h2 = (float(v) for v in d[p + "h"])
+        ctx = ctx_with([("sw", 2, 1)] * nl, 1, nch)
+        ctx.setheat(h1, h2, mode)
+        ctx.set_pdg(d[p + "pdg"])
+        ctx.set_probg(d[p + "probg"])
+        rng = api.MT19937(seed)
+        u = O.mt_uniforms(seed, 400000)
+        k = 0
+        for s in range(steps):
+            ok, used = ctx.swapchains_cb(tries, rng.uniform)
+            k += int(used[0])
+            assert ok[0] == d[p + "ok"][s]
+            assert np.array_equal(ctx.get_betas(), d[p + "betas"][s]), (c, s)
+        # the next draw is the stream's k-th value: exactly k were taken
+        assert rng.uniform() == u[k]
+        sc, tc = ctx.get_swapcounts(0)
+        assert np.array_equal(sc, d[p + "swapcount"])
+        assert np.array_equal(tc, d[p + "tempcount"])
+        ctx.close()

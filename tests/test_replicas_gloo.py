@@ -17,6 +17,13 @@ import torch.distributed as dist
 import bench
 dist.init_process_group("gloo")
 rank = dist.get_rank()
+# each rank opens its own GPU: the launcher's LOCAL_RANK among all visible
+# devices, whatever CUDA_VISIBLE_DEVICES lists
+assert bench.rank_device() == (rank if os.environ.get("VIS_MODE") != "one" else 0), bench.rank_device()
+devs = [None, None]
+dist.all_gather_object(devs, bench.rank_device())
+if os.environ.get("VIS_MODE") != "one":
+    assert devs == [0, 1], devs
 total, value = bench.aggregate(100.0 * (rank + 1), 10, 5, dist)
 assert total == 200.0, total
 assert abs(value - 10 * 5 * 2 / 0.2) < 1e-9, value
@@ -33,13 +40,21 @@ def _free_port():
     return p
 
 
-def test_two_gloo_replicas_take_the_slowest_time():
+@pytest.mark.parametrize("vis", ["unset", "all", "one"])
+def test_two_gloo_replicas_take_the_slowest_time(vis):
+    """vis: CUDA_VISIBLE_DEVICES unset, listing every GPU, or narrowed to
+    this rank's one GPU by the launcher."""
     pytest.importorskip("torch.distributed")
     port = _free_port()
     procs = []
     for r in range(2):
         env = dict(os.environ, RANK=str(r), WORLD_SIZE="2", MASTER_ADDR="127.0.0.1",
-                   MASTER_PORT=str(port), LOCAL_RANK=str(r))
+                   MASTER_PORT=str(port), LOCAL_RANK=str(r), VIS_MODE=vis)
+        env.pop("CUDA_VISIBLE_DEVICES", None)
+        if vis == "all":
+            env["CUDA_VISIBLE_DEVICES"] = "0,1,2,3,4,5,6,7"
+        elif vis == "one":
+            env["CUDA_VISIBLE_DEVICES"] = str(r)
         procs.append(subprocess.Popen([sys.executable, "-c", CHILD, ROOT], env=env,
                                       stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True))
     outs = [p.communicate(timeout=120) for p in procs]

@@ -90,3 +90,23 @@ def test_binary_side_car_round_trip(tmp_path):
     api.ti_write_binary(p, rows)
     back = api.ti_read_binary(p)
     assert back.dtype == np.float32 and np.array_equal(back, rows)
+
+
+def test_binary_side_car_checks_the_callers_buffer(tmp_path):
+    """A buffer sized for another row length, or for fewer rows, is refused
+    before anything is read into it."""
+    import ctypes as C
+    rng = np.random.default_rng(6)
+    rows = rng.normal(0, 10, (50, 48)).astype(np.float32)
+    p = str(tmp_path / "rows.tib")
+    api.ti_write_binary(p, rows)
+    lib = api.load_library()
+    buf = np.full((100, 21), 7.0, np.float32)
+    G, rl = C.c_int(), C.c_int(21)
+    rc = lib.ima_ti_read_binary(os.fsencode(p), C.byref(G), C.byref(rl), buf.ctypes.data_as(C.c_void_p), 100)
+    assert rc == api.IMA_ERR_DATA and rl.value == 48 and G.value == 50
+    assert np.all(buf == 7.0)
+    buf = np.full((49, 48), 7.0, np.float32)
+    rl = C.c_int(48)
+    rc = lib.ima_ti_read_binary(os.fsencode(p), C.byref(G), C.byref(rl), buf.ctypes.data_as(C.c_void_p), 49)
+    assert rc != api.IMA_OK and np.all(buf == 7.0)

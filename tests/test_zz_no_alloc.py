@@ -1,6 +1,6 @@
 """The allocation-free surface entry point (ima_gpu_surface_fp64_noalloc) for
-callers that cannot allocate device memory, e.g. code inside a CUDA graph
-capture or under a host framework that owns every device allocation.
+callers that may not allocate device memory, e.g. a plugin inside a host
+application that owns every device allocation through its own pool.
 
 It is called through the C ABI on device buffers the test owns, twice in a
 row with different point sets (the fixed scratch array it shares across calls
@@ -99,6 +99,34 @@ def test_noalloc_surface_matches_existing_entry_point():
         rc = api.surface_fp64_noalloc(d_rows, G, rows.shape[1], 5, 8, 3, d_lognorm, d_x,
                                       200000, 0, d_q, d_ess, None)
         assert rc == api.IMA_ERR_TOO_LARGE
+    finally:
+        dev.close()
+        ctx.close()
+
+
+def test_noalloc_surface_fewer_chunks_when_the_array_is_full():
+    """Enough points that the fixed array holds fewer genealogy chunks than
+    the FP64 form would use (300,000 genealogies are 5 chunks; 40,000 points
+    leave room for 4): the result still matches the existing entry point."""
+    rng = np.random.default_rng(78)
+    G = 300000
+    rows, lognorm, _ = synth.surface_stats(rng, G, 5, 8, 2)
+    pts = synth.surface_points(rng, 40000)
+    ctx = api.Context(0)
+    ctx.surface_load(rows, 5, 8, 3, lognorm=lognorm)
+    dev = DeviceBuffers()
+    try:
+        d_rows = dev.put(rows.astype(np.float32))
+        d_lognorm = dev.put(lognorm)
+        want_q, want_ess = ctx.surface_eval(pts, modeltype=0, method=api.SURF_FP64)
+        d_x = dev.put(pts)
+        d_q = dev.zeros(len(pts))
+        d_ess = dev.zeros(len(pts))
+        rc = api.surface_fp64_noalloc(d_rows, G, rows.shape[1], 5, 8, 3, d_lognorm, d_x,
+                                      len(pts), 0, d_q, d_ess, None)
+        assert rc == api.IMA_OK
+        np.testing.assert_allclose(dev.get(d_q, len(pts)), want_q, rtol=1e-12, atol=0)
+        np.testing.assert_allclose(dev.get(d_ess, len(pts)), want_ess, rtol=1e-9, atol=0)
     finally:
         dev.close()
         ctx.close()
