@@ -439,18 +439,24 @@ def measure_lik(args, api, wl, steps, dist=None, device=0, hky_legs=False):
     nodes = len(up0)
     h2d = nodes * 16 + units * 8 + units * 40  # FP64 + float-float time per node, lengths, requests
     d2h = units * (8 + 4)
-    e2e_t = []
+    e2e_t, set_t = [], []
     for s in range(args.warmup + min(steps, 100)):
         tms = scaled if s % 2 else tm
         t0 = time.perf_counter()
         ctx.set_genealogies(pci, pli, up0, up1, down, tms)
+        tm1 = time.perf_counter()
         ctx.eval(ci, li, u, par, precision=prec)
         t1 = time.perf_counter()
         if s >= args.warmup:
             e2e_t.append(t1 - t0)
+            set_t.append(tm1 - t0)
     e2e = units * world / statistics.median(e2e_t)
     out["e2e"] = {"value": round(e2e, 1), "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
-                  "d2h_bytes_per_step": int(d2h)}
+                  "d2h_bytes_per_step": int(d2h),
+                  "ms_per_step": round(1e3 * statistics.median(e2e_t), 4),
+                  "ms_set_genealogies": round(1e3 * statistics.median(set_t), 4),
+                  "note": "every step re-times every genealogy on the host (set_genealogies: checks and "
+                          "staging), then ima_gpu_eval copies the changed times, runs and copies results back"}
     ctx.set_genealogies(pci, pli, up0, up1, down, tm)
 
     if hky_legs:
@@ -638,6 +644,7 @@ def measure_surface(args, api, steps, extended=True, device=0):
     dev_ms = (k1[1] - k0[1]) / max(1, k1[0] - k0[0])
     value = P / (dev_ms / 1e3)
     e2e = P / statistics.median(wall)
+    retaken = ctx.surface_retaken() if method == api.SURF_TC else 0
     # the same points again: the screens give the same bits every call
     q_again, _ = ctx.surface_eval(pts, 0, method)
     # plain FP64 CUDA-core form on a subset of points, extrapolated per point
@@ -671,6 +678,7 @@ def measure_surface(args, api, steps, extended=True, device=0):
         "error_vs_fp64": {"max_rel": float(rel.max()), "median_rel": float(np.median(rel)),
                           "ess_max_rel": float(np.max(np.abs(ess[:512] - e64) / e64))},
         "repeat_bitwise": bool(np.array_equal(q_again, q)),
+        "points_retaken": int(retaken),
         "gpu_launches": int(n_timed), "clocks": clk.summary(),
     }
     cores = os.cpu_count() or 1

@@ -41,7 +41,7 @@ EXPORTS = [
     "ima_gpu_commit", "ima_gpu_batch_create", "ima_gpu_batch_run", "ima_gpu_batch_results",
     "ima_gpu_batch_destroy", "ima_gpu_flush_genealogies", "ima_gpu_setheat", "ima_gpu_get_betas",
     "ima_gpu_set_betas", "ima_gpu_set_pdg", "ima_gpu_get_pdg", "ima_gpu_set_probg",
-    "ima_gpu_swapchains", "ima_gpu_swapchains_cb", "ima_gpu_set_allbetas", "ima_gpu_get_swapcounts", "ima_gpu_surface_load",
+    "ima_gpu_swapchains", "ima_gpu_swapchains_cb", "ima_gpu_set_allbetas", "ima_gpu_surface_retaken", "ima_gpu_get_swapcounts", "ima_gpu_surface_load",
     "ima_gpu_surface_eval", "ima_gpu_jointp", "ima_gpu_surface_fp64_noalloc", "ima_gpu_tc_selftest",
     "ima_gpu_surface_info", "ima_mt19937_seed", "ima_mt19937_uniform", "ima_gpu_modelloop",
     "ima_gpu_batch_autotune", "ima_gpu_batch_set_variants", "ima_gpu_margincalc", "ima_gpu_fillvec",
@@ -210,6 +210,7 @@ def _declare(L):
         "ima_gpu_modelloop": (I, [P, I, P, I, P, I, I, P, P, P, C.POINTER(I), C.POINTER(I)]),
         "ima_gpu_surface_fp64_noalloc": (I, [P, I, I, I, I, I, P, P, I, I, P, P, P]),
         "ima_gpu_swapchains_cb": (I, [P, I, I, UNIFORM_FN, P, P, P]),
+        "ima_gpu_surface_retaken": (I, [P, C.POINTER(I)]),
         "ima_gpu_tc_selftest": (I, [P, C.POINTER(I), C.POINTER(C.c_float)]),
         "ima_gpu_timer_begin": (I, [P]),
         "ima_gpu_timer_end": (I, [P, C.POINTER(C.c_float)]),
@@ -426,6 +427,12 @@ class Context:
         self._ck(self.lib.ima_gpu_swapchains(self.h, int(swaptries), int(include_probg), _ptr(uniforms),
                                              int(stride), int(seed), _ptr(used), _ptr(ok)))
         return ok, used
+
+    def surface_retaken(self):
+        """Points the last tensor-core surface evaluation took a second time."""
+        n = I()
+        self._ck(self.lib.ima_gpu_surface_retaken(self.h, C.byref(n)))
+        return n.value
 
     def swapchains_cb(self, swaptries, uniform, include_probg=True):
         """Swap attempts drawing uniform() one value at a time, where the

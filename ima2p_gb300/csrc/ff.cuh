@@ -133,13 +133,22 @@ __device__ __forceinline__ ff ff_horner(const float2 *c, int m, ff y)
 
 __device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
 
-// e^x and e^x - 1 for -87 < x <= 0 in float-float.  x = k ln2 + r with
-// |r| <= ln2 / 2 (k ln2a.x exact: ln2a.x has 9 significant bits), y =
-// expm1(r / 16) from its Taylor series (degree 7, |r / 16| <= 0.022), four
-// doublings expm1(2z) = expm1(z) (expm1(z) + 2), then e^x = 2^k (1 + y) and
-// e^x - 1 = y (k = 0) or 2^k (1 + y) - 1.  No step cancels: e^x - 1 of a
-// short branch keeps its relative accuracy (about 1e-14).
-__device__ __forceinline__ void ff_exp_expm1_neg(ff x, const FFConsts &K, ff *ex, ff *em1)
+// ln 2 = LN2_A + LN2_B + LN2_C: LN2_A = 355/512 (9 significant bits, so k
+// LN2_A is exact for |k| < 2^15), LN2_B and LN2_C the next two float parts
+constexpr float LN2_A = 0.693359375f;
+constexpr float LN2_B = -2.121944417e-04f;
+constexpr float LN2_C = 1.646571768e-12f;
+// ln 2 as a normalised float-float pair
+constexpr float LN2_HI = 6.931471825e-01f;
+constexpr float LN2_LO = -1.904654212e-09f;
+
+// e^x and e^x - 1 for -86 < x < 88 in float-float.  x = k ln2 + r with
+// |r| <= ln2 / 2, y = expm1(r / 16) from its Taylor series (degree 7,
+// |r / 16| <= 0.022), four doublings expm1(2z) = expm1(z) (expm1(z) + 2),
+// then e^x = 2^k (1 + y) and e^x - 1 = y (k = 0) or 2^k (1 + y) - 1.  No
+// step cancels: e^x - 1 of a short branch keeps its relative accuracy
+// (about 1e-14).
+__device__ __forceinline__ void ff_exp_expm1(ff x, ff *ex, ff *em1)
 {
   if (x.hi < -86.0f) {
     *ex = ff_from(0.0f);
@@ -147,9 +156,9 @@ __device__ __forceinline__ void ff_exp_expm1_neg(ff x, const FFConsts &K, ff *ex
     return;
   }
   const float kf = rintf(x.hi * 1.44269504f);
-  ff r = ff_sub(x, ff_from(kf * K.ln2a.x));
-  r = ff_sub(r, two_prod(kf, K.ln2a.y));
-  r = ff_add_f(r, -kf * K.ln2b);
+  ff r = ff_sub(x, ff_from(kf * LN2_A));
+  r = ff_sub(r, two_prod(kf, LN2_B));
+  r = ff_add_f(r, -kf * LN2_C);
   const ff s = ff_make(r.hi * 0.0625f, r.lo * 0.0625f);
   // the coefficients from 1/120 on in float (their terms weigh < 2e-9 of
   // the sum), the rest in float-float
@@ -162,7 +171,7 @@ __device__ __forceinline__ void ff_exp_expm1_neg(ff x, const FFConsts &K, ff *ex
 #pragma unroll
   for (int i = 0; i < 4; i++) y = ff_mul(y, ff_add_f(y, 2.0f));
   const int k = (int)kf;
-  const float p2 = __int_as_float((127 + k) << 23);  // 2^k, k >= -125
+  const float p2 = __int_as_float((127 + k) << 23);  // 2^k, -125 <= k <= 127
   const ff one_y = ff_add_f(y, 1.0f);
   *ex = ff_make(one_y.hi * p2, one_y.lo * p2);
   *em1 = (k == 0) ? y : ff_add_f(*ex, -1.0f);

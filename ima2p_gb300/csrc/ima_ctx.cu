@@ -254,6 +254,7 @@ struct ima_ctx {
   void *d_twin = nullptr, *d_twout = nullptr, *d_tpbuf = nullptr;
   size_t twin_cap = 0, twout_cap = 0, tpbuf_cap = 0;
   int tw_ngen = 0, tw_ntv = 0;
+  int surf_retaken = 0;  // points the last tensor-core surface took a second time
   // which of the tw_ngen genealogies hold weights from the last treeweight
   // (all) or chain_weights call (the selected chains' items only)
   std::vector<uint8_t> tw_valid;
@@ -1699,6 +1700,13 @@ extern "C" int ima_gpu_swapchains_cb(ima_ctx *c, int swaptries, int include_prob
   return r ? r : c->cuda(cudaStreamSynchronize(c->st), "swap");
 }
 
+extern "C" int ima_gpu_surface_retaken(ima_ctx *c, int *n)
+{
+  if (!c || !n) return IMA_ERR_ARG;
+  *n = c->surf_retaken;
+  return IMA_OK;
+}
+
 extern "C" int ima_gpu_get_swapcounts(ima_ctx *c, int run, int32_t *swapcount, int32_t *tempcount)
 {
   if (!c || run < 0 || run >= c->nruns) return IMA_ERR_ARG;
@@ -2217,7 +2225,9 @@ extern "C" int ima_gpu_surface_eval(ima_ctx *c, int npoints, const double *x, in
     if (r) return r;
     c->launch(IMA_K_SURF_TC, (double)a.G * 32 * 2 + (double)npoints * 27 * 8,
               [&] { lr = launch_surface_tc(a, c->d_sscratch, c->sscratch_cap, c->d_flag,
-                                           c->srows_state == 2 && c->srows_model == modeltype, &nk, c->st); });
+                                           c->srows_state == 2 && c->srows_model == modeltype, &nk,
+                                           &c->surf_retaken, c->st); });
+    if (lr == 5) return c->cuda(cudaGetLastError(), "tensor-core surface");
     if (lr) return c->fail(IMA_ERR_ARG, "tensor-core surface: unsupported shape (%d)", lr);
     c->launches += nk - 1;
     c->srows_state = 2;

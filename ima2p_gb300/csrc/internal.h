@@ -83,8 +83,8 @@ void launch_is_sumlogk(const Pools &P, int item, int locus, int maxn, int maxS, 
 void launch_is(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int maxS, double *result,
                int32_t *status, int32_t *site_node, cudaStream_t st);
 // variant: launch shape chosen by the batch autotuner (0 is the default)
-constexpr int HKY_FAST_VARIANTS = 5;  // float-float: 128 threads (6 CTAs per SM), 64, 256, 128 without the
-                                      // shared-memory cache, 128 with registers for 4 CTAs per SM;
+constexpr int HKY_FAST_VARIANTS = 5;  // float-float: 128 threads with registers for 8 CTAs per SM, 64 threads
+                                      // (16 CTAs), 256 (4), 128 at 10 CTAs, 128 at 6;
                                       // FP32: 128 threads (12 CTAs per SM), 64, 256, 128 uncached, 128 at 8
 constexpr int SW_FAST_VARIANTS = 3;   // 8 chain-loci per CTA, 4, 16
 void launch_hky_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int maxS, int variant,
@@ -134,8 +134,9 @@ constexpr int SURF_COMPAT_CONCURRENT = 64;  // points per launch of the compat s
 int launch_surface_fast(const SurfArgs &a, void *scratch, size_t scratch_bytes, bool rows_ready, int *nkernels,
                         cudaStream_t st);
 size_t surface_fast_scratch_bytes(int G, int npoints);
+// *nretaken: points whose terms left the fixed-point sums and were taken again
 int launch_surface_tc(const SurfArgs &a, void *scratch, size_t scratch_bytes, int *d_err, bool rows_ready,
-                      int *nkernels, cudaStream_t st);
+                      int *nkernels, int *nretaken, cudaStream_t st);
 size_t surface_tc_scratch_bytes(int G, int npoints);
 int tc_selftest(cudaStream_t st, void *scratch, size_t bytes, int *h_bad, float *h_maxerr);
 size_t surface_fp64_scratch_bytes(int G, int npoints);

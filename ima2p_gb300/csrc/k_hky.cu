@@ -132,9 +132,9 @@ __device__ __forceinline__ void hky_coef_ff(const ff *pi, ff kpa, ff b, float *K
 {
   const ff PR = ff_add(pi[0], pi[2]), PY = ff_add(pi[1], pi[3]);
   ff e1, m1, eR, mR, eY, mY;
-  ff_exp_expm1_neg(ff_neg(b), c_ffh, &e1, &m1);
-  ff_exp_expm1_neg(ff_neg(ff_mul(b, ff_add_f(ff_mul(PR, kpa), 1.0f))), c_ffh, &eR, &mR);
-  ff_exp_expm1_neg(ff_neg(ff_mul(b, ff_add_f(ff_mul(PY, kpa), 1.0f))), c_ffh, &eY, &mY);
+  ff_exp_expm1(ff_neg(b), &e1, &m1);
+  ff_exp_expm1(ff_neg(ff_mul(b, ff_add_f(ff_mul(PR, kpa), 1.0f))), &eR, &mR);
+  ff_exp_expm1(ff_neg(ff_mul(b, ff_add_f(ff_mul(PY, kpa), 1.0f))), &eY, &mY);
   const ff E1 = ff_neg(m1), ER = ff_neg(mR), EY = ff_neg(mY);
   const ff bR = ff_div(ff_sub(ER, ff_mul(E1, ff_add_f(ff_neg(PR), 1.0f))), PR);
   const ff bY = ff_div(ff_sub(EY, ff_mul(E1, ff_add_f(ff_neg(PY), 1.0f))), PY);
@@ -180,17 +180,35 @@ __device__ __forceinline__ void hky_apply_tip_ff(const HkyCoefFF &K, const ff *p
   v[1] = st == 1 ? own : tY;
   v[3] = st == 3 ? own : tY;
 }
+// The same steps leaving the pair unnormalised (|lo| may reach a few
+// ulp(hi)), for intermediate values: the next step's TwoSum is exact
+// whatever lo is, so only the values that leave the apply are renormalised.
+__device__ __forceinline__ ff ff_mul_u(ff a, ff b)
+{
+  const float p = __fmul_rn(a.hi, b.hi);
+  return ff_make(p, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, __fmaf_rn(a.hi, b.hi, -p))));
+}
+__device__ __forceinline__ ff ff_fma_pos_u(ff a, ff b, ff c)
+{
+  const float p = __fmul_rn(a.hi, b.hi);
+  const float pe = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, __fmaf_rn(a.hi, b.hi, -p)));
+  const ff s = two_sum(p, c.hi);
+  return ff_make(s.hi, __fadd_rn(s.lo, __fadd_rn(pe, c.lo)));
+}
+
 // v_j = E1 S_o + b_c S_c + d_c L_j
 __device__ __forceinline__ void hky_apply_ff(const HkyCoefFF &K, const ff *pi, const ff *L, ff *v)
 {
-  const ff SR = ff_fma_pos(pi[2], L[2], ff_mul(pi[0], L[0]));
-  const ff SY = ff_fma_pos(pi[3], L[3], ff_mul(pi[1], L[1]));
-  const ff tR = ff_fma_pos(K.bR, SR, ff_mul(K.a, SY));
-  const ff tY = ff_fma_pos(K.bY, SY, ff_mul(K.a, SR));
-  v[0] = ff_fma_pos(K.dR, L[0], tR);
-  v[2] = ff_fma_pos(K.dR, L[2], tR);
-  v[1] = ff_fma_pos(K.dY, L[1], tY);
-  v[3] = ff_fma_pos(K.dY, L[3], tY);
+  const ff SR = ff_fma_pos_u(pi[2], L[2], ff_mul_u(pi[0], L[0]));
+  const ff SY = ff_fma_pos_u(pi[3], L[3], ff_mul_u(pi[1], L[1]));
+  const ff tR = ff_fma_pos_u(K.bR, SR, ff_mul_u(K.a, SY));
+  const ff tY = ff_fma_pos_u(K.bY, SY, ff_mul_u(K.a, SR));
+  const ff w0 = ff_fma_pos_u(K.dR, L[0], tR), w2 = ff_fma_pos_u(K.dR, L[2], tR);
+  const ff w1 = ff_fma_pos_u(K.dY, L[1], tY), w3 = ff_fma_pos_u(K.dY, L[3], tY);
+  v[0] = fast_two_sum(w0.hi, w0.lo);
+  v[1] = fast_two_sum(w1.hi, w1.lo);
+  v[2] = fast_two_sum(w2.hi, w2.lo);
+  v[3] = fast_two_sum(w3.hi, w3.lo);
 }
 
 __device__ __forceinline__ ff ff_of(float2 v) { return ff_make(v.x, v.y); }
@@ -715,11 +733,11 @@ void launch_hky_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int
   if (nreq <= 0) return;
   const int maxnl = 2 * maxn - 1;
   switch (variant) {
-    case 1: hky_fast_bs<true, 64, 12>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
-    case 2: hky_fast_bs<true, 256, 3>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
-    case 3: hky_fast_bs<true, 128, 6>(P, reqs, nreq, maxnl, maxS, false, result, status, st); break;
-    case 4: hky_fast_bs<true, 128, 4>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
-    default: hky_fast_bs<true, 128, 6>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
+    case 1: hky_fast_bs<true, 64, 16>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
+    case 2: hky_fast_bs<true, 256, 4>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
+    case 3: hky_fast_bs<true, 128, 10>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
+    case 4: hky_fast_bs<true, 128, 6>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
+    default: hky_fast_bs<true, 128, 8>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
   }
 }
 

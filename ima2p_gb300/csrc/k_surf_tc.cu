@@ -37,8 +37,10 @@
 //     associative, so the sum does not depend on arrival order; the chunk
 //     sums are merged in chunk order.
 // A term with w >= 2^80 (the pre-pass bound more than 55 nats below the
-// term) would leave the fixed-point range: the point is flagged and its log
-// density is taken again over every genealogy (k_surf_tc_exact).
+// term) would leave the fixed-point range: the point is flagged.  The pass
+// also keeps each point's largest exact value, a maximum and so the same on
+// every run; the flagged points are then taken again by a second pass over
+// just them, with that value as the reference, where no term can exceed it.
 //
 // Every wait is bounded: a wait that runs out sets the error word, the CTA
 // stops issuing work, waits (bounded) for the copies and MMAs it started,
@@ -99,6 +101,7 @@ struct TcSmem {
   unsigned long long sum[TC_M][FIXW];   // sum of w * 2^64, w = exp(p - ref), 256-bit fixed point
   unsigned long long sum2[TC_M][FIXW];  // sum of w^2 * 2^64
   float ref[TC_M];                    // the point's lower bound after the pre-pass
+  unsigned xmax[TC_M];                // largest exact value refined (ordered bits)
   int ovf[TC_M];                      // a term left the fixed-point range
   float2 phi[TC_M * PHI_STRIDE];      // float-float phi of the CTA's points
 };
@@ -205,11 +208,17 @@ __device__ void refine_loop(const SurfPrep &S, TcSmem &sh, int *gerr, int r, int
       *src = -1;
       const int pl = e & (TC_M - 1), g = e >> 7;
       const ff y = surf_exact(S, g, S.sT + g, S.Gpad, &sh.phi[pl * PHI_STRIDE]);
-      const double d = ((double)y.hi - (double)sh.ref[pl]) + (double)y.lo;
-      if (d > OVF_NATS) {
+      atomicMax(&sh.xmax[pl], f2ord(y.hi));
+      const ff d = ff_sub(y, ff_from(sh.ref[pl]));
+      if (d.hi > (float)OVF_NATS) {
         sh.ovf[pl] = 1;
       } else {
-        const double w = exp(d);
+        // w = e^d in float-float (FP32 pipes: GB300 runs FP64 at 1/64 of
+        // the FP32 rate); hi + lo is exact in a double, and w^2 (up to 2^160,
+        // beyond FP32's range) is squared there
+        ff e, em1;
+        ff_exp_expm1(d, &e, &em1);
+        const double w = (double)e.hi + (double)e.lo;
         unsigned long long x[FIXW];
         fixw(w, x);
         atomic_addw(sh.sum[pl], x);
@@ -262,6 +271,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     for (int w = 0; w < FIXW; w++) sh.sum[pl][w] = sh.sum2[pl][w] = 0ull;
     const int p = ptile * TC_M + pl;
     sh.ref[pl] = p < npoints ? ord2f(S.best[p]) : -INFINITY;
+    sh.xmax[pl] = f2ord(-INFINITY);
     sh.ovf[pl] = 0;
   }
   if (warp == 1) {
@@ -428,6 +438,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   }
   if (threadIdx.x < TC_M && !maxonly) {
     const int p = ptile * TC_M + threadIdx.x;
+    if (p < npoints) atomicMax(&S.xmax[p], sh.xmax[threadIdx.x]);
     if (p < npoints)
       part[(size_t)p * gridDim.y + blockIdx.y] =
           make_double2(sh.ovf[threadIdx.x] ? -1.0 : fixw_to_double(sh.sum[threadIdx.x]),
@@ -436,9 +447,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 }
 
 // Chunk sums added in chunk order: q = ln G - (ref + ln sum).  A point with
-// a flagged chunk goes to the list k_surf_tc_exact works through
-// (flag[0] = list length, flag[1..] = points; the list's order does not
-// matter, each point is taken on its own).
+// a flagged chunk goes to the list of points to take again (flag[0] = list
+// length, flag[1..] = points; the list's order does not matter, each point
+// is taken on its own).
 __global__ void k_surf_tc_merge(SurfArgs a, SurfPrep S, const double2 *part, int nchunks, int *flag)
 {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -460,58 +471,31 @@ __global__ void k_surf_tc_merge(SurfArgs a, SurfPrep S, const double2 *part, int
   if (a.ess) a.ess[p] = s * s / s2;
 }
 
-constexpr int EX_THREADS = 512;
-
-// The listed points over every genealogy, a CTA per point: the exact values
-// (surf_exact, as the refinement computes them) give the maximum M, then
-// the terms within 40 nats of it are summed as exp(p - M) in FP64 (the rest
-// weigh < 2^21 e^-40 = 9e-12 of the sum).  Per-thread sums in genealogy
-// order and a fixed tree keep these reproducible too.
-__global__ void __launch_bounds__(EX_THREADS) k_surf_tc_exact(SurfArgs a, SurfPrep S, const int *flag)
+// The flagged points as a problem of their own: their coordinates and, as
+// the reference, the largest exact value the first pass met.
+__global__ void k_surf_tc_gather(const double *x, int npar, const unsigned *xmax, const int *flag, double *xs,
+                                 unsigned *refs)
 {
-  __shared__ double rs[EX_THREADS], rs2[EX_THREADS];
-  __shared__ float rm[EX_THREADS];
-  __shared__ float2 phi[SURF_K];
-  const int nflag = flag[0], t = threadIdx.x;
-  for (int k = blockIdx.x; k < nflag; k += gridDim.x) {
-    const int p = flag[1 + k];
-    __syncthreads();
-    if (t < SURF_K) phi[t] = S.phiff[(size_t)p * SURF_K + t];
-    __syncthreads();
-    float m = -INFINITY;
-    for (int g = t; g < a.G; g += EX_THREADS) m = fmaxf(m, surf_exact(S, g, S.sT + g, S.Gpad, phi).hi);
-    rm[t] = m;
-    __syncthreads();
-    for (int o = EX_THREADS / 2; o > 0; o >>= 1) {
-      if (t < o) rm[t] = fmaxf(rm[t], rm[t + o]);
-      __syncthreads();
-    }
-    const double M = (double)rm[0];
-    double s = 0.0, s2 = 0.0;
-    for (int g = t; g < a.G; g += EX_THREADS) {
-      const ff y = surf_exact(S, g, S.sT + g, S.Gpad, phi);
-      const double d = ((double)y.hi - M) + (double)y.lo;
-      if (d > -40.0) {
-        const double e = exp(d);
-        s += e;
-        s2 += e * e;
-      }
-    }
-    rs[t] = s;
-    rs2[t] = s2;
-    __syncthreads();
-    for (int o = EX_THREADS / 2; o > 0; o >>= 1) {
-      if (t < o) {
-        rs[t] += rs[t + o];
-        rs2[t] += rs2[t + o];
-      }
-      __syncthreads();
-    }
-    if (t == 0) {
-      a.q[p] = log((double)a.G) - (M + log(rs[0]));
-      if (a.ess) a.ess[p] = rs[0] * rs[0] / rs2[0];
-    }
-  }
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= flag[0]) return;
+  const int p = flag[1 + k];
+  for (int j = 0; j < npar; j++) xs[(size_t)k * npar + j] = x[(size_t)p * npar + j];
+  refs[k] = xmax[p];
+}
+
+__global__ void k_surf_tc_setref(unsigned *best, unsigned *xmax, const unsigned *refs, int n)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) best[k] = xmax[k] = refs[k];
+}
+
+__global__ void k_surf_tc_scatter(const int *flag, const double *qs, const double *es, double *q, double *ess)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= flag[0]) return;
+  const int p = flag[1 + k];
+  q[p] = qs[k];
+  if (ess) ess[p] = es[k];
 }
 
 // ------------------------------------------------------------ self-test
@@ -614,10 +598,12 @@ __global__ void k_tc_selftest_check(const float *D, int *bad, float *maxerr)
 // ---------------------------------------------------------------- host
 size_t surface_tc_scratch_bytes(int G, int npoints)
 {
-  // prepared operands | chunk sums (double2 per point and chunk) | the
-  // list of points to retake (a count, then points)
-  return surf_prep_bytes(G, npoints) + (size_t)npoints * SURF_MAX_CHUNKS * sizeof(double2) +
-         (size_t)(npoints + 1) * sizeof(int) + 1024;
+  // prepared operands | chunk sums (double2 per point and chunk) | the list
+  // of points to retake (a count, then points) | their coordinates,
+  // references, densities, sample sizes and the retake's own list
+  const size_t np = (size_t)npoints;
+  return surf_prep_bytes(G, npoints) + np * SURF_MAX_CHUNKS * sizeof(double2) + 2 * (np + 1) * sizeof(int) +
+         np * (SURF_K / 2) * sizeof(double) + np * sizeof(unsigned) + 2 * np * sizeof(double) + 4096;
 }
 
 namespace {
@@ -649,41 +635,82 @@ int surf_tc_chunks(int ptiles, int ntiles, int nsm, int *per)
 
 }  // namespace
 
+// One evaluation of the points of `a` on prepared operands S: the optional
+// max-only pre-pass, the full pass and the merge; returns the kernels queued.
+static int tc_passes(const SurfArgs &a, const SurfPrep &S, double2 *part, int *flag, int *d_err, int nsm, bool pre,
+                     cudaStream_t st)
+{
+  const int ntiles = S.Gpad / TC_N;
+  const int ptiles = (a.npoints + TC_M - 1) / TC_M;
+  int per = 0, nk = 0;
+  if (pre) {
+    const int nch = surf_tc_chunks(ptiles, (ntiles + PRE_STRIDE - 1) / PRE_STRIDE, nsm, &per);
+    k_surf_tc<<<dim3(ptiles, nch), TC_THREADS, TC_SMEM, st>>>(S, a.npoints, per, PRE_STRIDE, part, d_err);
+    nk++;
+  }
+  const int nchunks = surf_tc_chunks(ptiles, ntiles, nsm, &per);
+  k_surf_tc<<<dim3(ptiles, nchunks), TC_THREADS, TC_SMEM, st>>>(S, a.npoints, per, 0, part, d_err);
+  cudaMemsetAsync(flag, 0, sizeof(int), st);
+  k_surf_tc_merge<<<(a.npoints + 127) / 128, 128, 0, st>>>(a, S, part, nchunks, flag);
+  return nk + 2;
+}
+
 int launch_surface_tc(const SurfArgs &a, void *scratch, size_t scratch_bytes, int *d_err, bool rows_ready,
-                      int *nkernels, cudaStream_t st)
+                      int *nkernels, int *nretaken, cudaStream_t st)
 {
   if (a.np + a.nm > SURF_K / 2) return 2;
   if (scratch_bytes < surface_tc_scratch_bytes(a.G, a.npoints)) return 3;
   if (a.G >= (1 << 24)) return 4;  // candidate entries pack the genealogy index into 24 bits
+  const size_t np = (size_t)a.npoints;
+  const int npar = a.np + a.nm;
+  char *base = static_cast<char *>(scratch);
   SurfPrep S;
-  double2 *part = reinterpret_cast<double2 *>(surf_prep_carve(&S, static_cast<char *>(scratch), a.G, a.npoints));
-  int *flag = reinterpret_cast<int *>(part + (size_t)a.npoints * SURF_MAX_CHUNKS);
-  surf_prep(a, S, true, rows_ready, st);
-  surf_seed(S, a.npoints, SEED_TC, st);
-  const int ntiles = S.Gpad / TC_N;
-  const int ptiles = (a.npoints + TC_M - 1) / TC_M;
+  double2 *part = reinterpret_cast<double2 *>(surf_prep_carve(&S, base, a.G, a.npoints));
+  // the retake's buffers sit past everything the first evaluation uses
+  int *flag = reinterpret_cast<int *>(part + np * SURF_MAX_CHUNKS);
+  double *xs = reinterpret_cast<double *>(
+      (reinterpret_cast<uintptr_t>(flag + np + 1) + 255) & ~static_cast<uintptr_t>(255));
+  unsigned *refs = reinterpret_cast<unsigned *>(xs + np * (SURF_K / 2));
+  double *qs = reinterpret_cast<double *>((reinterpret_cast<uintptr_t>(refs + np) + 255) & ~static_cast<uintptr_t>(255));
+  double *es = qs + np;
+  int *flag2 = reinterpret_cast<int *>(es + np);  // the retake's own list (always empty)
   static_assert(A_BYTES + TC_STAGES * B_BYTES + sizeof(TcSmem) + 1024 <= TC_SMEM, "smem");
-  const size_t sm = TC_SMEM;
-  cudaFuncSetAttribute(k_surf_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cudaFuncSetAttribute(k_surf_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
   int nsm = 152;
   {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   }
-  // max-only pre-pass over every PRE_STRIDE-th tile: every point starts the
-  // full pass with a lower bound near its maximum
-  int per = 0;
-  int nchunks = surf_tc_chunks(ptiles, (ntiles + PRE_STRIDE - 1) / PRE_STRIDE, nsm, &per);
-  const bool pre = ntiles >= 4 * PRE_STRIDE;
-  if (pre) k_surf_tc<<<dim3(ptiles, nchunks), TC_THREADS, sm, st>>>(S, a.npoints, per, PRE_STRIDE, part, d_err);
-  nchunks = surf_tc_chunks(ptiles, ntiles, nsm, &per);
-  k_surf_tc<<<dim3(ptiles, nchunks), TC_THREADS, sm, st>>>(S, a.npoints, per, 0, part, d_err);
-  cudaMemsetAsync(flag, 0, sizeof(int), st);
-  k_surf_tc_merge<<<(a.npoints + 127) / 128, 128, 0, st>>>(a, S, part, nchunks, flag);
-  k_surf_tc_exact<<<nsm, EX_THREADS, 0, st>>>(a, S, flag);
-  // rows, points, seed, pre-pass, pass, merge, FP64 retake of flagged points
-  *nkernels = (rows_ready ? 0 : 1) + 5 + (pre ? 1 : 0);
+  surf_prep(a, S, true, rows_ready, st);
+  surf_seed(S, a.npoints, SEED_TC, st);
+  // a max-only pre-pass over every PRE_STRIDE-th tile gives every point a
+  // lower bound near its maximum before the full pass
+  const bool pre = S.Gpad / TC_N >= 4 * PRE_STRIDE;
+  int nk = (rows_ready ? 0 : 1) + 2 + tc_passes(a, S, part, flag, d_err, nsm, pre, st);
+  // points whose terms left the fixed-point range: a second evaluation of
+  // just them, referenced to their exact maxima
+  int nflag = 0;
+  if (cudaMemcpyAsync(&nflag, flag, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return 5;
+  *nretaken = nflag;
+  if (nflag > 0) {
+    k_surf_tc_gather<<<(nflag + 127) / 128, 128, 0, st>>>(a.x, npar, S.xmax, flag, xs, refs);
+    SurfArgs b = a;
+    b.npoints = nflag;
+    b.x = xs;
+    b.q = qs;
+    b.ess = a.ess ? es : nullptr;
+    SurfPrep S2;
+    double2 *part2 = reinterpret_cast<double2 *>(surf_prep_carve(&S2, base, a.G, nflag));
+    surf_prep(b, S2, true, true, st);
+    k_surf_tc_setref<<<(nflag + 127) / 128, 128, 0, st>>>(S2.best, S2.xmax, refs, nflag);
+    nk += 3 + tc_passes(b, S2, part2, flag2, d_err, nsm, false, st);
+    k_surf_tc_scatter<<<(nflag + 127) / 128, 128, 0, st>>>(flag, qs, es, a.q, a.ess);
+    nk++;
+  }
+  *nkernels = nk;
   return 0;
 }
 

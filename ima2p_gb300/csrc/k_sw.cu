@@ -8,10 +8,15 @@
 // |d| >= 2.  A zero Bessel value makes the branch term -1e100 and the locus
 // total -DBL_MAX.  There is no pruning: internal alleles are chain state.
 //
-// Fast form: every branch term is evaluated in the log domain in float-float
-// arithmetic (ff.cuh), so the exp(x) of the large-x polynomials cancels
-// against -x analytically and no FP64 instruction is issued per branch; the
-// float-float terms are summed per chain-locus and converted to FP64 once.
+// Fast form: every branch term is evaluated in the log domain, so the
+// exp(x) of the large-x polynomials cancels against -x analytically and no
+// FP64 instruction is issued per branch; the terms are summed per
+// chain-locus in float-float and converted to FP64 once.  Short branches
+// (x <= 0.375, y = (x / 3.75)^2 <= 0.01: 81% of them in the 100-locus
+// benchmark) take a cheaper form: bessi0 = 1 + u0(y), bessi1 = x (1 + u1(y))
+// / 2 with u(y) <= 0.036 and log(1 + u) from its series, the leading terms
+// in float-float and the rest in FP32.  Longer branches use the float-float
+// core (A&S polynomial and table log).  Both keep about 1e-11 per branch.
 // Branches outside the float-float range (x below 1e-15 with |d| >= 2, or a
 // Miller value the reference would take below 1e-300) take the FP64 path.
 // FP64 form: the reference algorithm in FP64, one thread per branch.
@@ -27,6 +32,9 @@ constexpr double BESSI_MIN = -1e+100;  // imamp.hpp:173
 
 __constant__ FFConsts c_ff;
 __constant__ double c_i0s[7], c_i0l[9], c_i1s[7], c_i1l[9];
+__constant__ float c_cheap[2][7];  // A&S 9.8.1 / 9.8.3 coefficients over their constant term
+__constant__ float2 c_cheap1[2];   // the first of them as float-float
+constexpr float SW_CHEAP_Y = 0.01f;
 
 // ---------------------------------------------------------------- FP64
 __device__ __forceinline__ double horner64(const double *c, int m, double y)
@@ -134,6 +142,29 @@ __device__ __forceinline__ ff sw_core(ff x, int d01, const SwTables &T)
   return ff_add(lp, tail);
 }
 
+// log(bessi_d01(x)) - x for a short branch (y = (x / 3.75)^2 <= SW_CHEAP_Y):
+// with the polynomial written as c0 (1 + u), u = c1' y + y^2 (c2' + c3' y +
+// ...), c_k' = c_k / c0, log(1 + u) (|u| <= 0.036) from its series: u and
+// u - u^2/2 in float-float, u^3 (1/3 - u/4 + ... - u^5/8) in FP32 (its
+// weight is below 1.6e-5, the first term left out below 1.2e-14).  About
+// 1e-11 per branch, like the float-float core, at a quarter of its work.
+__device__ __forceinline__ ff sw_cheap(ff x, ff y, int d01)
+{
+  const float *c = c_cheap[d01];
+  float t = c[6];
+#pragma unroll
+  for (int k = 5; k >= 2; k--) t = __fmaf_rn(t, y.hi, c[k]);
+  const ff u = ff_add_f(ff_mul(ffc(c_cheap1[d01]), y), y.hi * y.hi * t);
+  const ff u2 = ff_mul(u, u);
+  const float h = u.hi;
+  const float s3 = h * h * h *
+                   (0.33333334f + h * (-0.25f + h * (0.2f + h * (-0.16666667f + h * (0.14285715f + h * -0.125f)))));
+  const ff l = ff_add_f(ff_sub(u, ff_make(0.5f * u2.hi, 0.5f * u2.lo)), s3);
+  ff v = ff_sub(l, x);
+  if (d01) v = ff_add(v, ff_sub(ff_log(x, c_ff), ff_make(LN2_HI, LN2_LO)));  // + log(x / 2)
+  return v;
+}
+
 // log(ans / bi) of the reference's Miller recurrence and its 1e10 rescaling
 // count; false when the value must come from the FP64 path.
 __device__ bool sw_miller(int n, ff x, ff *out)
@@ -207,8 +238,9 @@ __global__ void __launch_bounds__(32 * IPC) k_sw_fast(Pools P, const ReqDev *req
   __shared__ SwTables T;
   extern __shared__ __align__(16) char sw_smem[];
   float2 *vals = reinterpret_cast<float2 *>(sw_smem);
-  int16_t *queue = reinterpret_cast<int16_t *>(vals + maxb);
-  __shared__ int qn;
+  int16_t *queue = reinterpret_cast<int16_t *>(vals + maxb);   // |d| >= 2: the Miller recurrence
+  int16_t *gqueue = queue + maxb;                              // longer branches: the float-float core
+  __shared__ int qn, gn;
   __shared__ int bstart[IPC + 1];
   __shared__ int zero[IPC];
   __shared__ float2 uff[IPC], trff[IPC];
@@ -225,6 +257,7 @@ __global__ void __launch_bounds__(32 * IPC) k_sw_fast(Pools P, const ReqDev *req
   }
   if (tid == 0) {
     qn = 0;
+    gn = 0;
     int b = 0;
     for (int i = 0; i < nit; i++) {
       bstart[i] = b;
@@ -261,12 +294,36 @@ __global__ void __launch_bounds__(32 * IPC) k_sw_fast(Pools P, const ReqDev *req
         zero[i] = 1;
         v = ff_make(-INFINITY, 0.f);
       } else {
-        v = sw_core(x, n == 1 ? 1 : 0, T);
+        const ff xq = ff_mul(x, ffc(c_ff.inv375));  // x / 3.75
+        const ff y = ff_mul(xq, xq);
+        if (y.hi <= SW_CHEAP_Y) {
+          v = sw_cheap(x, y, n == 1 ? 1 : 0);
+        } else {
+          gqueue[atomicAdd(&gn, 1)] = (int16_t)b;  // phase A2
+          v = ff_from(0.0f);
+        }
         if (n >= 2) queue[atomicAdd(&qn, 1)] = (int16_t)b;
       }
       out = make_float2(v.hi, v.lo);
     }
     vals[b] = out;
+  }
+  __syncthreads();
+  // ---- phase A2: longer branches through the float-float core, packed onto
+  // consecutive threads
+  for (int q = tid; q < gn; q += (32 * IPC)) {
+    const int b = gqueue[q];
+    int i = 0;
+    while (b >= bstart[i + 1]) i++;
+    const ReqDev &R = reqs[r0 + i];
+    const ItemDev it = P.items[R.item];
+    const int nl = 2 * it.n - 1, c = b - bstart[i];
+    const NodeRec nd = P.nodes[it.node_off + c];
+    const int32_t *A = P.alleles + it.al_off + (size_t)R.ai * nl;
+    const int n = abs(A[c] - A[nd.down]);
+    const ff x = ff_mul(branch_len_ff(nd, P.tff + it.node_off, c, ffc(trff[i])), ffc(uff[i]));
+    const ff v = sw_core(x, n == 1 ? 1 : 0, T);
+    vals[b] = make_float2(v.hi, v.lo);
   }
   __syncthreads();
   // ---- phase B: |d| >= 2
@@ -405,6 +462,14 @@ int sw_init_tables()
   if (cudaMemcpyToSymbol(c_i0l, AS_I0L, sizeof(AS_I0L)) != cudaSuccess) return -1;
   if (cudaMemcpyToSymbol(c_i1s, AS_I1S, sizeof(AS_I1S)) != cudaSuccess) return -1;
   if (cudaMemcpyToSymbol(c_i1l, AS_I1L, sizeof(AS_I1L)) != cudaSuccess) return -1;
+  float cheap[2][7];
+  for (int k = 0; k < 7; k++) {
+    cheap[0][k] = (float)(AS_I0S[k] / AS_I0S[0]);
+    cheap[1][k] = (float)(AS_I1S[k] / AS_I1S[0]);
+  }
+  if (cudaMemcpyToSymbol(c_cheap, cheap, sizeof(cheap)) != cudaSuccess) return -1;
+  const float2 c1[2] = {split(AS_I0S[1] / AS_I0S[0]), split(AS_I1S[1] / AS_I1S[0])};
+  if (cudaMemcpyToSymbol(c_cheap1, c1, sizeof(c1)) != cudaSuccess) return -1;
   return 0;
 }
 
@@ -413,7 +478,7 @@ static void sw_fast_ipc(const Pools &P, const ReqDev *reqs, int nreq, int maxn, 
                         cudaStream_t st)
 {
   const int maxb = IPC * (2 * maxn - 1);  // queue entries are int16: IPC * (2 maxn - 1) < 32768
-  const size_t sm = (size_t)maxb * (sizeof(float2) + sizeof(int16_t));
+  const size_t sm = (size_t)maxb * (sizeof(float2) + 2 * sizeof(int16_t));
   if (sm > 48 * 1024)
     cudaFuncSetAttribute(k_sw_fast<IPC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k_sw_fast<IPC><<<(nreq + IPC - 1) / IPC, 32 * IPC, sm, st>>>(P, reqs, nreq, result, status, maxb);

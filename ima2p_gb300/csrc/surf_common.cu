@@ -144,6 +144,7 @@ size_t surf_prep_bytes(int G, int npoints)
   b += align256(sizeof(float) * npad);
   b += align256(sizeof(float) * npad);
   b += align256(sizeof(unsigned) * npad);
+  b += align256(sizeof(unsigned) * npad);
   b += align256(sizeof(unsigned) * SURF_KP);
   b += align256(2 * sizeof(uint16_t) * SURF_KP * Gpad);
   b += align256(2 * sizeof(uint16_t) * SURF_KP * npad);
@@ -173,6 +174,7 @@ SurfPart *surf_prep_carve(SurfPrep *S, char *base, int G, int npoints)
   S->mag = reinterpret_cast<float *>(take(sizeof(float) * npad));
   S->seed = reinterpret_cast<float *>(take(sizeof(float) * npad));
   S->best = reinterpret_cast<unsigned *>(take(sizeof(unsigned) * npad));
+  S->xmax = reinterpret_cast<unsigned *>(take(sizeof(unsigned) * npad));
   S->pbf = reinterpret_cast<uint16_t *>(take(2 * sizeof(uint16_t) * SURF_KP * npad));
   return reinterpret_cast<SurfPart *>(base + o);
 }
@@ -215,6 +217,7 @@ __global__ void k_surf_seed(SurfPrep S, int npoints, int samples)
   if (lane == 0) {
     S.seed[p] = best;
     S.best[p] = f2ord(best);
+    S.xmax[p] = f2ord(best);
   }
 }
 

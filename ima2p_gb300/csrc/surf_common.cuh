@@ -26,6 +26,7 @@ struct SurfPrep {
   float *mag;       // [npoints] sum_k colmax_k |phi_k|: scale of screening errors
   float *seed;      // [npoints] exact max over a sample of genealogies
   unsigned *best;   // [npoints] best exact maximum found so far (ordered bits), shared by chunks
+  unsigned *xmax;   // [npoints] largest exact value the refinement met (ordered bits; tensor-core screen)
   unsigned *colmax; // [SURF_KP] max |column| as float bits
   uint16_t *sbf;    // bf16 statistics, hi and lo planes of 256-row MMA tiles (tensor-core screen)
   uint16_t *pbf;    // bf16 phi, hi and lo planes of 128-row MMA tiles (tensor-core screen)

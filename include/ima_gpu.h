@@ -213,6 +213,12 @@ int ima_gpu_swapchains(ima_ctx *ctx, int swaptries, int include_probg, const dou
  * made.  Replaces swapchains() in the reference-side binding. */
 int ima_gpu_swapchains_cb(ima_ctx *ctx, int swaptries, int include_probg, double (*uniform)(void *arg),
                           void *arg, int32_t *used, int32_t *swap0ok);
+/* How many points the last IMA_SURF_TC evaluation took a second time: its
+ * sums are fixed-point numbers relative to a first bound on each point's
+ * maximum, and points with a term more than 55 nats above that bound are
+ * evaluated again relative to their exact maximum (same results, more
+ * time). */
+int ima_gpu_surface_retaken(ima_ctx *ctx, int *n);
 /* swapcount and tempbasedswapcount (imamp.hpp:1123-1129) of run r,
  * chains_per_run^2 each, row-major. */
 int ima_gpu_get_swapcounts(ima_ctx *ctx, int run, int32_t *swapcount, int32_t *tempcount);

@@ -29,6 +29,9 @@ Fixtures:
                     three chains of four infinite-sites loci, 3 populations
                     with migration: decisions, split times, probg and pdg
                     per step, final node and migration times
+  golden_ks.npz     long runs of the same update on chain 0 for six seeds:
+                    thinned split times of both periods (the statistical
+                    comparison of the device-resident sampler)
 
   golden_popmig.npz calc_popmig and calc_pop_expomig (2NM densities) over
                     gsampinf rows that reach every branch of the terms
@@ -41,7 +44,7 @@ Fixtures:
                     popmig rows and on rows whose peaks lie inside the
                     priors, uniform and exponential migration priors
 
-Run with fixture names (is hky sw swap jointp de margin tw ry popmig peaks) to regenerate only those.
+Run with fixture names (is hky sw swap jointp de margin tw ry ks popmig peaks) to regenerate only those.
 """
 from __future__ import annotations
 
@@ -523,6 +526,32 @@ def popmig_rows():
     return rows
 
 
+# long runs of the split-time update for the statistical comparison
+KS_SEEDS, KS_STEPS, KS_THIN = (101, 102, 103, 104, 105, 106), 4000, 10
+
+
+def golden_ks():
+    """The reference's changet_RY1 run for KS_STEPS updates on chain 0 of the
+    golden_ry case (periods alternating), for each of KS_SEEDS: every
+    KS_THIN-th split time of each period after its update."""
+    sys.path.insert(0, ROOT)
+    from tests._splittime import RyCase
+    c = RyCase()
+    loci = [(int(c.samps[li].sum()), 1.0, [int(v) for v in c.samps[li]], float(c.us[li]), c.seqs[li])
+            for li in range(c.nl)]
+    tv0 = [float(v) for v in c.d["tv0"]]
+    out = {"seeds": np.array(KS_SEEDS), "steps": np.array(KS_STEPS), "thin": np.array(KS_THIN)}
+    for seed in KS_SEEDS:
+        steps = [(0, k % 2) for k in range(KS_STEPS)]
+        res, _, _ = O.ref_ry(c.npops, c.tree, c.tprior, loci, [(tv0, b) for b in c.betas], c.fresh_gens(), steps,
+                             seed, c.thetaprior, c.mprior)
+        tv = np.array([r[1] for r in res])
+        for k in range(2):
+            out["t%d_%d" % (k, seed)] = tv[k::2][::KS_THIN]
+        out["acc_%d" % seed] = np.array([r[0] for r in res], np.int8)
+    np.savez_compressed(os.path.join(OUT, "golden_ks.npz"), **out)
+
+
 def golden_popmig():
     rows = popmig_rows()
     qmax, mmax, mean = np.array([20.0, 15.0, 25.0]), np.array([2.0, 5.0]), np.array([0.8, 1.7])
@@ -576,7 +605,7 @@ if __name__ == "__main__":
         sys.exit("build the reference harness first: make -C oracle ref")
     gens = {"is": golden_is, "hky": golden_hky, "sw": golden_sw, "swap": golden_swap,
             "jointp": golden_jointp, "de": golden_de, "margin": golden_margin,
-            "tw": golden_tw, "ry": golden_ry, "popmig": golden_popmig,
+            "tw": golden_tw, "ry": golden_ry, "ks": golden_ks, "popmig": golden_popmig,
             "peaks": golden_peaks}
     for name in (sys.argv[1:] or list(gens)):
         gens[name]()

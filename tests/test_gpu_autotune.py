@@ -1,7 +1,7 @@
 """The batch autotuner (ima_gpu_batch_autotune) on a small config-4-shaped
 mixed workload: every launch variant of the fast kernels gives the plain
 FP64 form's likelihoods (float-float HKY within 1e-6 per locus, SW within
-1e-9), every variant of the FP32 HKY kernel within 2e-6 relative, and the
+1e-8), every variant of the FP32 HKY kernel within 2e-6 relative, and the
 variants agree with one another up to the order of the final FP64
 reduction; the tuned batch replays as a graph with the chosen shapes."""
 import numpy as np
@@ -28,7 +28,7 @@ def _check(res, ref, is_hky, prec):
         np.testing.assert_allclose(res[is_hky], ref[is_hky], rtol=2e-6)
     else:
         assert np.max(np.abs(res[is_hky] - ref[is_hky])) <= 1e-6
-    assert np.max(np.abs(res[~is_hky] - ref[~is_hky])) <= 1e-9
+    assert np.max(np.abs(res[~is_hky] - ref[~is_hky])) <= 1e-8
 
 
 @pytest.mark.parametrize("prec", [api.PREC_FAST, api.PREC_FP32])

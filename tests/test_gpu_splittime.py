@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 from ima2p_gb300 import api, splittime
+from tests._golden import load
 from tests._splittime import RyCase, final_times, run_chain_set
 
 pytestmark = pytest.mark.gpu
@@ -388,3 +389,50 @@ def test_library_drawn_sweep_of_one_chain():
             else:
                 assert np.array_equal(t, before[(ci, li)][0]) and np.array_equal(m, before[(ci, li)][1])
     ctx.close()
+
+
+def test_long_runs_match_reference_marginals():
+    """Statistical parity of whole runs: the device-resident split-time
+    sampler (changet_ry1_sweep_mt: band, weights, p(G), likelihoods and the
+    decision on the GPU) run for 4000 updates on chain 0 of the golden case,
+    periods alternating, under six seeds of its own, against the compiled
+    reference's runs of the same length under six other seeds: the thinned
+    split times of each period pass a two-sample Kolmogorov-Smirnov test
+    (p > 1e-3), their means agree within four standard errors of the
+    difference (from per-seed means), and so do the acceptance rates."""
+    stats = pytest.importorskip("scipy.stats")
+    d = load("golden_ks.npz")
+    steps, thin = int(d["steps"]), int(d["thin"])
+    ref = {k: np.concatenate([d["t%d_%d" % (k, s)] for s in d["seeds"]]) for k in range(2)}
+    ref_acc = np.array([d["acc_%d" % s].mean() for s in d["seeds"]])
+    case = RyCase()
+    ours = {0: [], 1: []}
+    per_seed = {0: [], 1: []}
+    acc_rate = []
+    for seed in (201, 202, 203, 204, 205, 206):
+        ctx = _resident_context(case)
+        splittime.ResidentChainSet(ctx, case.fresh_gens(), [case.d["tv0"]] * case.nch, case.betas,
+                                   np.ones(case.nl), case.samps, case.us)
+        rng = api.MT19937(seed)
+        tv = {0: [], 1: []}
+        nacc = 0
+        for k in range(steps):
+            acc, _, _, _ = ctx.changet_ry1_sweep_mt(np.array([0], np.int32), np.array([k % 2]), case.tprior, rng,
+                                                    np.asarray(case.us, np.float64))
+            nacc += int(acc[0])
+            tv[k % 2].append(float(ctx.get_split_times()[0, k % 2]))
+        for p in range(2):
+            x = np.array(tv[p])[::thin]
+            ours[p].append(x)
+            per_seed[p].append(x.mean())
+        acc_rate.append(nacc / steps)
+        ctx.close()
+    for p in range(2):
+        a, b = np.concatenate(ours[p]), ref[p]
+        assert stats.ks_2samp(a, b).pvalue > 1e-3, (p, a.mean(), b.mean())
+        rm = np.array([d["t%d_%d" % (p, s)].mean() for s in d["seeds"]])
+        om = np.array(per_seed[p])
+        se = np.sqrt(rm.var(ddof=1) / len(rm) + om.var(ddof=1) / len(om))
+        assert abs(om.mean() - rm.mean()) <= 4 * se, (p, om.mean(), rm.mean(), se)
+    se = np.sqrt(np.var(acc_rate, ddof=1) / 6 + ref_acc.var(ddof=1) / 6)
+    assert abs(np.mean(acc_rate) - ref_acc.mean()) <= 4 * se + 1e-3, (np.mean(acc_rate), ref_acc.mean())

@@ -1,8 +1,10 @@
 """Stepwise-mutation likelihood on the GPU against the reference's golden
 values: per-locus totals and per-branch dlikeA, including a zero Bessel term
-(total -DBL_MAX) and x > 700.  The float-float form must stay within
-SW_FAST_ATOL of the reference per locus (the 1e-6 target, with margin); the
-FP64 form within 1e-12 relative."""
+(total -DBL_MAX) and x > 700.  The fast form must stay within SW_FAST_ATOL of
+the reference per locus (the 1e-6 target, with margin) and SW_BRANCH_ATOL
+per branch (float-float terms, about 1e-11 each; short branches take the
+series of log(1 + u) with its tail in FP32); the FP64 form within 1e-12
+relative."""
 import numpy as np
 import pytest
 
@@ -13,7 +15,8 @@ from tests._gpu import ctx_with
 
 pytestmark = pytest.mark.gpu
 
-SW_FAST_ATOL = 1e-9      # per-locus |log L - reference|
+SW_FAST_ATOL = 1e-8      # per-locus |log L - reference|
+SW_BRANCH_ATOL = 2e-10   # per-branch |dlikeA - reference|
 DBLMAX = np.finfo(np.float64).max
 
 
@@ -36,7 +39,10 @@ def test_sw_golden(prec):
         else:
             assert abs(res[ci] - r[0]) <= 1e-12 * abs(r[0])
         dl = ctx.get_dlikeA(ci, 0)
-        np.testing.assert_allclose(dl, r[1:], rtol=1e-11 if prec == api.PREC_FP64 else 1e-9, atol=1e-11)
+        if prec == api.PREC_FP64:
+            np.testing.assert_allclose(dl, r[1:], rtol=1e-11, atol=1e-11)
+        else:
+            np.testing.assert_allclose(dl, r[1:], rtol=0, atol=SW_BRANCH_ATOL)
 
 
 def test_sw_config3_shape_vs_oracle():
@@ -81,7 +87,7 @@ def test_sw_bessel_edge_terms():
         if want <= -1e99:
             assert st[k] == api.EVAL_SW_ZERO
         else:
-            assert abs(res[k] - want) <= 1e-9 * max(1.0, abs(want)), (d, x, res[k], want)
+            assert abs(res[k] - want) <= 2 * SW_BRANCH_ATOL + 1e-9 * abs(want), (d, x, res[k], want)
 
 
 @pytest.mark.parametrize("prec", [api.PREC_FAST, api.PREC_FP64])

@@ -91,21 +91,22 @@ def test_surface_repeat_calls_bitwise(method):
 
 
 def test_surface_tc_term_far_above_prepass_bound():
-    """One genealogy 150 nats above every other, in a tile the max-only
+    """One genealogy 300 nats above every other, in a tile the max-only
     pre-pass skips and away from the seed samples: its weight relative to the
-    pre-pass bound leaves the fixed-point range, the point is flagged and taken
-    again in FP64 over every genealogy.  Points on either side agree with the
-    FP64 form and the oracle."""
+    pre-pass bound leaves the fixed-point range, so every point is taken a
+    second time relative to its exact maximum.  The densities agree with the
+    FP64 form and the oracle, and repeat bit for bit."""
     rng = np.random.default_rng(8)
     G = 40000
     rows, lognorm, _ = synth.surface_stats(rng, G, 5, 8, 2)
     lognorm = lognorm.copy()
     g_star = 256 * 3 + 17   # tile 3 (the pre-pass reads tiles 0, 8, ...); seeds sample multiples of G/32
-    lognorm[g_star] += 150.0
+    lognorm[g_star] = lognorm.max() + 300.0
     pts = synth.surface_points(rng, 200)
     ctx = ctx_with([("sw", 2, 1)])
     ctx.surface_load(rows, 5, 8, 3, lognorm=lognorm)
     q, ess = ctx.surface_eval(pts, modeltype=0, method=api.SURF_TC)
+    assert ctx.surface_retaken() == len(pts)
     q64, ess64 = ctx.surface_eval(pts, modeltype=0, method=api.SURF_FP64)
     assert np.all(np.abs(q - q64) <= 2e-9 * np.abs(q64) + 3e-7), np.max(np.abs(q - q64))
     np.testing.assert_allclose(ess, ess64, rtol=1e-4)
@@ -114,3 +115,25 @@ def test_surface_tc_term_far_above_prepass_bound():
         assert abs(q[k] - qo) <= 2e-9 * abs(qo) + 3e-7, (k, q[k], qo)
     q2, _ = ctx.surface_eval(pts, modeltype=0, method=api.SURF_TC)
     np.testing.assert_array_equal(q2, q)
+
+
+@pytest.mark.parametrize("lead", [20.0, 40.0, 46.0, 50.0, 54.0, 60.0])
+def test_surface_tc_dominant_genealogy_sample_size(lead):
+    """One genealogy `lead` nats above every other (in a tile the max-only
+    pre-pass skips): terms up to 55 nats above the pre-pass bound stay in the
+    first pass's fixed-point sums, larger ones send the point to the second
+    pass.  Either way the densities and the effective sample sizes (here
+    close to 1) agree with the FP64 form -- the squared weights of the
+    largest terms exceed FP32's range and must still be counted."""
+    rng = np.random.default_rng(9)
+    G = 40000
+    rows, lognorm, _ = synth.surface_stats(rng, G, 5, 8, 2)
+    lognorm = lognorm.copy()
+    lognorm[256 * 3 + 17] = lognorm.max() + lead
+    pts = synth.surface_points(rng, 100)
+    ctx = ctx_with([("sw", 2, 1)])
+    ctx.surface_load(rows, 5, 8, 3, lognorm=lognorm)
+    q, ess = ctx.surface_eval(pts, modeltype=0, method=api.SURF_TC)
+    q64, ess64 = ctx.surface_eval(pts, modeltype=0, method=api.SURF_FP64)
+    assert np.all(np.abs(q - q64) <= 2e-9 * np.abs(q64) + 3e-7), np.max(np.abs(q - q64))
+    np.testing.assert_allclose(ess, ess64, rtol=1e-4)
