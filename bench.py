@@ -269,10 +269,11 @@ def cpu_baseline(wl, seconds, limit=4096):
 
 def dirty_edits(wl, rng, ndirty=4):
     """Four internal (non-root) nodes of every chain-locus moved down in time,
-    one after another so each move stays inside its bounds, as a genealogy
-    update leaves them: the packed arrays with the new times, the edit lists
-    [pairs][4] and how many nodes each evaluation recomputes (the edited
-    nodes and their ancestors)."""
+    one after another, each inside the bounds its daughters and parent set
+    at that moment, as a genealogy update leaves them: the packed arrays with
+    the new times, the edit lists [pairs][4] (the moved nodes: their
+    daughters' branches changed) and how many nodes each evaluation
+    recomputes (the moved nodes and their ancestors)."""
     pci, pli, up0, up1, down, tm = wl.packed()
     tm = tm.copy()
     ci, li = wl.pairs()
@@ -288,9 +289,8 @@ def dirty_edits(wl, rng, ndirty=4):
         pick = rng.choice(cand, size=min(ndirty, len(cand)), replace=False)
         fresh = set()
         for j in pick:
-            a, b = int(u0[j]), int(u1[j])
-            lo = max(t[u0[a]] if u0[a] >= 0 else 0.0, t[u0[b]] if u0[b] >= 0 else 0.0)
-            t[a] = t[b] = 0.5 * (lo + t[a])
+            lo = max(t[u0[j]], t[u1[j]])
+            t[j] = 0.5 * (lo + t[j])   # below its old time, above both daughters
             x = int(j)
             while x >= 0 and x not in fresh:
                 fresh.add(x)
@@ -437,13 +437,15 @@ def measure_lik(args, api, wl, steps, dist=None, device=0, hky_legs=False):
     pci, pli, up0, up1, down, tm = wl.packed()
     scaled = np.where(tm > 0, tm * (1.0 + 1e-6), tm)
     nodes = len(up0)
-    h2d = nodes * 16 + units * 8 + units * 40  # FP64 + float-float time per node, lengths, requests
+    # FP64 time per node and a length per chain-locus; the request list
+    # repeats, so ima_gpu_eval keeps the staged one
+    h2d = nodes * 8 + units * 8
     d2h = units * (8 + 4)
     e2e_t, set_t = [], []
     for s in range(args.warmup + min(steps, 100)):
         tms = scaled if s % 2 else tm
         t0 = time.perf_counter()
-        ctx.set_genealogies(pci, pli, up0, up1, down, tms)
+        ctx.set_times(pci, pli, tms)
         tm1 = time.perf_counter()
         ctx.eval(ci, li, u, par, precision=prec)
         t1 = time.perf_counter()
@@ -454,9 +456,10 @@ def measure_lik(args, api, wl, steps, dist=None, device=0, hky_legs=False):
     out["e2e"] = {"value": round(e2e, 1), "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
                   "d2h_bytes_per_step": int(d2h),
                   "ms_per_step": round(1e3 * statistics.median(e2e_t), 4),
-                  "ms_set_genealogies": round(1e3 * statistics.median(set_t), 4),
-                  "note": "every step re-times every genealogy on the host (set_genealogies: checks and "
-                          "staging), then ima_gpu_eval copies the changed times, runs and copies results back"}
+                  "ms_set_times": round(1e3 * statistics.median(set_t), 4),
+                  "note": "every step re-times every genealogy (ima_gpu_set_times: FP64 times staged, "
+                          "lengths summed on the host threads), then ima_gpu_eval copies the times, makes "
+                          "their float-float form on the device, runs and copies results back"}
     ctx.set_genealogies(pci, pli, up0, up1, down, tm)
 
     if hky_legs:
@@ -479,11 +482,42 @@ def measure_lik(args, api, wl, steps, dist=None, device=0, hky_legs=False):
     out["swaps"] = {"runs": wl.nruns, "chains_per_run": wl.cpr, "swaptries": tries,
                     "ms_per_sweep": round(sw_ms, 5),
                     "attempts_per_s": round(wl.nruns * tries / (sw_ms / 1e3), 1)}
+    if wl.nruns > 1:
+        out["sweep"] = sweep_leg(ctx, api, ci, li, u, par, prec, tuned, tries, steps)
     if rank == 0:
         out["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
     batch.destroy()
     ctx.close()
     return out
+
+
+def sweep_leg(ctx, api, ci, li, u, par, prec, tuned, tries, steps):
+    """One MC3 sweep of every run: every chain-locus evaluated, committed,
+    then each run's swap attempts -- as one graph launch
+    (ima_gpu_batch_sweep) and as separate launches, device time per sweep."""
+    b = ctx.batch_create(ci, li, u, par, precision=prec)
+    b.set_variants(*tuned)
+    k = max(3, min(steps, 30))
+
+    def timed(graph):
+        for _ in range(3):
+            b.sweep(tries, seed=5, use_graph=graph)
+        ctx.synchronize()
+        n0 = ctx.launch_count()
+        ctx.timer_begin()
+        for _ in range(k):
+            b.sweep(tries, seed=5, use_graph=graph)
+        ms = ctx.timer_end() / k
+        return ms, (ctx.launch_count() - n0) / k
+
+    ms_g, kern = timed(True)
+    ms_l, _ = timed(False)
+    b.destroy()
+    return {"ms_per_sweep_graph": round(ms_g, 4), "ms_per_sweep_launches": round(ms_l, 4),
+            "kernels_per_sweep": kern, "graph_launches_per_sweep": 1,
+            "chain_locus_evals_per_s": round(len(ci) / (ms_g / 1e3), 1),
+            "note": "every (run, chain, locus) evaluated, accepted and committed, then swapchains of every run "
+                    "(%d attempts, Philox stream) -- all kernels of a sweep in one CUDA graph" % tries}
 
 
 def edit_list_leg(ctx, api, wl, ci, li, u, par, steps):
@@ -492,7 +526,13 @@ def edit_list_leg(ctx, api, wl, ci, li, u, par, steps):
     only they and their ancestors are recomputed (device time, L2 flushed)."""
     rng = np.random.default_rng(99)
     packed, edits, nrec = dirty_edits(wl, rng)
-    ctx.set_genealogies(*packed)
+    # the partials of the unmoved genealogies, committed: the clean nodes'
+    # partials the edit-list evaluations start from
+    ctx.set_genealogies(*wl.packed())
+    full = ctx.batch_create(ci, li, u, par, precision=api.PREC_FAST)
+    full.run(use_graph=False)
+    ctx.commit(ci, li, np.ones(len(ci), np.uint8))
+    ctx.set_times(packed[0], packed[1], packed[5])
     b = ctx.batch_create(ci, li, u, par, edits=edits, precision=api.PREC_FAST)
     for _ in range(3):
         b.run(use_graph=True)
@@ -504,13 +544,19 @@ def edit_list_leg(ctx, api, wl, ci, li, u, par, steps):
         tt.append(ctx.timer_end())
     r_ff, _ = b.results()
     b.destroy()
-    b64 = ctx.batch_create(ci, li, u, par, edits=edits, precision=api.PREC_FP64)
+    # the same genealogies evaluated in full: the float-float form gives the
+    # same bits, the FP64 form the error
+    full.run(use_graph=False)
+    r_full, _ = full.results()
+    full.destroy()
+    b64 = ctx.batch_create(ci, li, u, par, precision=api.PREC_FP64)
     b64.run(use_graph=False)
     r64, _ = b64.results()
     b64.destroy()
     ms = statistics.median(tt)
     return {"value": round(len(ci) / (ms / 1e3), 1), "unit": "evals/s", "ms_per_step": round(ms, 5),
             "dirty_nodes_per_eval": 4, "recomputed_nodes_per_eval": round(nrec, 2),
+            "same_bits_as_full_evaluation": bool(np.array_equal(r_ff, r_full)),
             "error_vs_fp64_max_abs": float(np.abs(r_ff - r64).max())}
 
 
@@ -536,10 +582,20 @@ def per_call_leg(ctx, api, wl, calls=2000):
         ctx.set_genealogy(0, l, g)
         ctx.likelihoodHKY(0, l, float(wl.u[0, l]), float(wl.par[0, l]), -1, -1, -1, -1)
         lat_up.append(time.perf_counter() - t0)
+    # the kernel's own time per call (CUDA events around each launch, in a
+    # separate loop: recording them costs host time)
+    ctx.set_profiling(True)
+    k0 = ctx.kernel_stats(api.K_HKY_FAST)
+    for k in range(200):
+        l = k % nl
+        ctx.likelihoodHKY(0, l, float(wl.u[0, l]), float(wl.par[0, l]), -1, -1, -1, -1)
+    nk, kms = kdelta(k0, ctx.kernel_stats(api.K_HKY_FAST))
+    ctx.set_profiling(False)
     items = [("hky", wl.tree(0, l), float(wl.u[0, l]), float(wl.par[0, l]), wl.loci[l][1]) for l in range(nl)]
     pack = O.PackedItems(items)
     v, n, t = cpu_rate([pack], 1.0, 1)
     return {"us_per_call": round(1e6 * statistics.median(lat), 2),
+            "kernel_us_per_call": round(1e3 * kms, 2),
             "us_per_call_with_genealogy_upload": round(1e6 * statistics.median(lat_up), 2),
             "cpu_us_per_eval_1core": round(1e6 / v, 2),
             "note": "one chain-locus (20+20 copies, 1000 bp) per call; the genealogy stays resident unless "

@@ -41,7 +41,8 @@ EXPORTS = [
     "ima_gpu_commit", "ima_gpu_batch_create", "ima_gpu_batch_run", "ima_gpu_batch_results",
     "ima_gpu_batch_destroy", "ima_gpu_flush_genealogies", "ima_gpu_setheat", "ima_gpu_get_betas",
     "ima_gpu_set_betas", "ima_gpu_set_pdg", "ima_gpu_get_pdg", "ima_gpu_set_probg",
-    "ima_gpu_swapchains", "ima_gpu_swapchains_cb", "ima_gpu_set_allbetas", "ima_gpu_surface_retaken", "ima_gpu_get_swapcounts", "ima_gpu_surface_load",
+    "ima_gpu_swapchains", "ima_gpu_swapchains_cb", "ima_gpu_set_allbetas", "ima_gpu_surface_retaken",
+    "ima_gpu_batch_sweep", "ima_gpu_set_times", "ima_gpu_get_swapcounts", "ima_gpu_surface_load",
     "ima_gpu_surface_eval", "ima_gpu_jointp", "ima_gpu_surface_fp64_noalloc", "ima_gpu_tc_selftest",
     "ima_gpu_surface_info", "ima_mt19937_seed", "ima_mt19937_uniform", "ima_gpu_modelloop",
     "ima_gpu_batch_autotune", "ima_gpu_batch_set_variants", "ima_gpu_margincalc", "ima_gpu_fillvec",
@@ -211,6 +212,8 @@ def _declare(L):
         "ima_gpu_surface_fp64_noalloc": (I, [P, I, I, I, I, I, P, P, I, I, P, P, P]),
         "ima_gpu_swapchains_cb": (I, [P, I, I, UNIFORM_FN, P, P, P]),
         "ima_gpu_surface_retaken": (I, [P, C.POINTER(I)]),
+        "ima_gpu_batch_sweep": (I, [P, I, P, I, I, C.c_uint64, I]),
+        "ima_gpu_set_times": (I, [P, I, P, P, P, P]),
         "ima_gpu_tc_selftest": (I, [P, C.POINTER(I), C.POINTER(C.c_float)]),
         "ima_gpu_timer_begin": (I, [P]),
         "ima_gpu_timer_end": (I, [P, C.POINTER(C.c_float)]),
@@ -311,6 +314,12 @@ class Context:
         self._ck(self.lib.ima_gpu_set_genealogies(
             self.h, len(ci), _ptr(ci), _ptr(li), _ptr(_i32(up0)), _ptr(_i32(up1)), _ptr(_i32(down)),
             _ptr(_f64(time)), _ptr(_f64(length))))
+
+    def set_times(self, ci, li, time, length=None):
+        """New node times of genealogies whose topology is unchanged (packed as in set_genealogies)."""
+        ci, li = _i32(ci), _i32(li)
+        self._ck(self.lib.ima_gpu_set_times(self.h, len(ci), _ptr(ci), _ptr(li), _ptr(_f64(time)),
+                                            _ptr(_f64(length))))
 
     def set_pi(self, ci, li, pi):
         self._ck(self.lib.ima_gpu_set_pi(self.h, int(ci), int(li), _ptr(_f64(pi))))
@@ -818,6 +827,14 @@ class Batch:
 
     def run(self, use_graph=True):
         self.ctx._ck(self.ctx.lib.ima_gpu_batch_run(self.ctx.h, self.handle, int(use_graph)))
+
+    def sweep(self, swaptries, accept=None, include_probg=True, seed=0, use_graph=True):
+        """ima_gpu_batch_sweep: every request evaluated, the accepted ones
+        (all when accept is None) committed, then every run's swap attempts on
+        the device's Philox stream -- one graph launch with use_graph."""
+        acc = None if accept is None else np.ascontiguousarray(accept, np.uint8)
+        self.ctx._ck(self.ctx.lib.ima_gpu_batch_sweep(self.ctx.h, self.handle, _ptr(acc), int(swaptries),
+                                                      int(include_probg), int(seed), int(use_graph)))
 
     def results(self):
         res = np.zeros(self.n)

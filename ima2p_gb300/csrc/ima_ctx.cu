@@ -44,11 +44,21 @@ struct Batch {
   ReqDev *d_req = nullptr;
   double *d_res = nullptr;
   int32_t *d_st = nullptr;
+  double *h_res = nullptr;   // pinned: results and status come back by DMA
+  int32_t *h_st = nullptr;
+  ReqDev *h_reqpin = nullptr;  // pinned staging of h_req for its upload
   std::vector<ReqDev> h_req;
   cudaGraphExec_t graph = nullptr;
   int maxn_is = 0, maxs_is = 0, maxn_hky = 0, maxs_hky = 0, maxn_sw = 0;
   int cap = 0;  // capacity of the device buffers
   int hky_variant = 0, sw_variant = 0;  // launch shapes (ima_gpu_batch_autotune)
+  // MC3 sweep of the batch (ima_gpu_batch_sweep): its items and accept mask
+  // on the device, and the graph of evaluation, commit and swaps
+  int32_t *d_items = nullptr;
+  uint8_t *d_acc = nullptr;
+  cudaGraphExec_t sgraph = nullptr;
+  int s_tries = -1, s_probg = -1;
+  uint64_t s_seed = 0;
 };
 
 // A small persistent pool of host threads for per-genealogy packing: run(n,
@@ -190,7 +200,6 @@ struct ima_ctx {
   // host mirrors (pinned)
   NodeRec *h_nodes = nullptr;
   double *h_t64 = nullptr;
-  float2 *h_tff = nullptr;
   int16_t *h_sched = nullptr;
   int32_t *h_nlev = nullptr;
   double *h_len = nullptr;
@@ -255,6 +264,7 @@ struct ima_ctx {
   size_t twin_cap = 0, twout_cap = 0, tpbuf_cap = 0;
   int tw_ngen = 0, tw_ntv = 0;
   int surf_retaken = 0;  // points the last tensor-core surface took a second time
+  long long graph_launches = 0;  // graph replays of MC3 sweeps
   // which of the tw_ngen genealogies hold weights from the last treeweight
   // (all) or chain_weights call (the selected chains' items only)
   std::vector<uint8_t> tw_valid;
@@ -432,9 +442,15 @@ extern "C" void ima_gpu_destroy(ima_ctx *c)
   c->batches.push_back(c->evb);
   for (auto &b : c->batches) {
     if (b.graph) cudaGraphExecDestroy(b.graph);
+    if (b.sgraph) cudaGraphExecDestroy(b.sgraph);
     cudaFree(b.d_req);
     cudaFree(b.d_res);
     cudaFree(b.d_st);
+    cudaFree(b.d_items);
+    cudaFree(b.d_acc);
+    cudaFreeHost(b.h_res);
+    cudaFreeHost(b.h_st);
+    cudaFreeHost(b.h_reqpin);
   }
   void *devs[] = {c->d_loci, c->d_seq, c->d_mult, c->d_sumlogk, c->d_flag, c->d_items,
                   c->d_nodes, c->d_t64, c->d_tff, c->d_sched, c->d_nlev, c->d_len, c->d_pi,
@@ -449,7 +465,7 @@ extern "C" void ima_gpu_destroy(ima_ctx *c)
                   c->d_rh2, c->d_rsel, c->d_is_site, c->d_is_valid};
   for (void *p : devs)
     if (p) cudaFree(p);
-  void *hosts[] = {c->h_nodes, c->h_t64, c->h_tff, c->h_sched, c->h_nlev, c->h_len, c->h_pi, c->h_al};
+  void *hosts[] = {c->h_nodes, c->h_t64, c->h_sched, c->h_nlev, c->h_len, c->h_pi, c->h_al};
   for (void *p : hosts)
     if (p) cudaFreeHost(p);
   for (auto &p : c->pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
@@ -615,13 +631,12 @@ extern "C" int ima_gpu_set_chains(ima_ctx *c, int nruns, int chains_per_run)
   if (int r0 = c->cuda(cudaMemsetAsync(c->d_is_valid, 0, c->nitems, c->st), "IS site cache")) return r0;
   c->h_nodes = host_alloc<NodeRec>(nodes);
   c->h_t64 = host_alloc<double>(nodes);
-  c->h_tff = host_alloc<float2>(nodes);
   c->h_sched = host_alloc<int16_t>(sched);
   c->h_nlev = host_alloc<int32_t>(c->nitems);
   c->h_len = host_alloc<double>(c->nitems);
   c->h_pi = host_alloc<double>(4 * (size_t)c->nitems);
   c->h_al = host_alloc<int32_t>(al);
-  if (!c->h_nodes || !c->h_t64 || !c->h_tff || !c->h_sched || !c->h_nlev || !c->h_len || !c->h_pi || !c->h_al)
+  if (!c->h_nodes || !c->h_t64 || !c->h_sched || !c->h_nlev || !c->h_len || !c->h_pi || !c->h_al)
     return c->fail(IMA_ERR_NOMEM, "pinned host allocation failed");
   for (int i = 0; i < c->nitems; i++)
     for (int j = 0; j < 4; j++) c->h_pi[4 * (size_t)i + j] = 0.25;
@@ -650,7 +665,6 @@ static int sync_mirror(ima_ctx *c)
   const ItemDev &a = c->items[c->dev_lo], &b = c->items[c->dev_hi];
   const size_t n0 = a.node_off, n1 = (size_t)b.node_off + 2 * b.n - 1;
   int r = c->cuda(cudaMemcpyAsync(c->h_t64 + n0, c->d_t64 + n0, (n1 - n0) * sizeof(double), cudaMemcpyDeviceToHost, c->st), "mirror");
-  r = r ? r : c->cuda(cudaMemcpyAsync(c->h_tff + n0, c->d_tff + n0, (n1 - n0) * sizeof(float2), cudaMemcpyDeviceToHost, c->st), "mirror");
   r = r ? r : c->cuda(cudaMemcpyAsync(c->h_len + c->dev_lo, c->d_len + c->dev_lo, (size_t)(c->dev_hi - c->dev_lo + 1) * sizeof(double),
                                       cudaMemcpyDeviceToHost, c->st), "mirror");
   r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "mirror");
@@ -701,8 +715,6 @@ static int set_one(ima_ctx *c, int item, const int32_t *up0, const int32_t *up1,
     for (int k = 0; k < nl; k++) {
       double t = time[k];
       c->h_t64[it.node_off + k] = t;
-      float hi = (float)t;
-      c->h_tff[it.node_off + k] = make_float2(hi, (float)(t - (double)hi));
       if (down[k] >= 0) L += (up0[k] < 0) ? t : t - time[up0[k]];
     }
     c->h_len[item] = (length >= 0.0) ? length : L;
@@ -773,8 +785,6 @@ static int set_one(ima_ctx *c, int item, const int32_t *up0, const int32_t *up1,
     r.pad = 0;
     double t = time[k];
     c->h_t64[it.node_off + k] = t;
-    float hi = (float)t;
-    c->h_tff[it.node_off + k] = make_float2(hi, (float)(t - (double)hi));
     if (down[k] >= 0) L += (up0[k] < 0) ? t : t - time[up0[k]];
   }
   c->h_len[item] = (length >= 0.0) ? length : L;
@@ -865,6 +875,75 @@ extern "C" int ima_gpu_set_genealogies(ima_ctx *c, int n, const int32_t *ci, con
   return r;
 }
 
+// Re-timings with the topology kept (the moves of changet_RY1 and of a
+// rubber band): only the node times, and the length, go to the mirror.
+static void set_times_one(ima_ctx *c, int item, const double *time, double length)
+{
+  const ItemDev &it = c->items[item];
+  const int nl = 2 * it.n - 1;
+  double *t64 = c->h_t64 + it.node_off;
+  memcpy(t64, time, nl * sizeof(double));
+  if (length >= 0.0) {
+    c->h_len[item] = length;
+    return;
+  }
+  const NodeRec *rec = c->h_nodes + it.node_off;
+  double L = 0.0;
+  for (int k = 0; k < nl; k++)
+    if (rec[k].down >= 0) L += (rec[k].up0 < 0) ? time[k] : time[k] - time[rec[k].up0];
+  c->h_len[item] = L;
+}
+
+extern "C" int ima_gpu_set_times(ima_ctx *c, int n, const int32_t *ci, const int32_t *li, const double *time,
+                                 const double *length)
+{
+  if (!c || n < 0 || (n > 0 && (!ci || !li || !time))) return IMA_ERR_ARG;
+  if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
+  if (int rs = sync_mirror(c)) return rs;
+  std::vector<size_t> &off = c->pair_off;
+  off.resize((size_t)n + 1);
+  off[0] = 0;
+  int lo = INT32_MAX, hi = -1;
+  for (int k = 0; k < n; k++) {
+    if (!c->valid(ci[k], li[k])) return c->fail(IMA_ERR_ARG, "pair %d: chain %d locus %d out of range", k, ci[k], li[k]);
+    const int item = c->item_of(ci[k], li[k]);
+    if (!c->has_tree[item]) return c->fail(IMA_ERR_STATE, "pair %d: chain %d locus %d has no genealogy", k, ci[k], li[k]);
+    off[k + 1] = off[k] + 2 * c->loci[li[k]].d.n - 1;
+    lo = std::min(lo, item);
+    hi = std::max(hi, item);
+  }
+  const size_t *offp = off.data();
+  // a pair given twice keeps its later times only when the list is applied
+  // in order on one thread
+  bool repeat = false;
+  if ((int)c->pair_stamp.size() != c->nitems) c->pair_stamp.assign(c->nitems, -1);
+  const int gen = ++c->stamp_gen;
+  for (int k = 0; k < n; k++) {
+    const int item = c->item_of(ci[k], li[k]);
+    if (c->pair_stamp[item] == gen) repeat = true;
+    c->pair_stamp[item] = gen;
+  }
+  auto apply = [c, ci, li, time, length, offp](int k0, int k1) {
+    for (int k = k0; k < k1; k++)
+      set_times_one(c, c->item_of(ci[k], li[k]), time + offp[k], length ? length[k] : -1.0);
+  };
+  if (repeat || n < 128) {
+    apply(0, n);
+  } else {
+    if (!c->pool) {
+      const unsigned hw = std::thread::hardware_concurrency();
+      c->pool.reset(new HostPool((int)std::max(1u, std::min(hw, 16u)) - 1));
+    }
+    const int nchunk = std::min(std::max(2, n / 64), 4 * c->pool->size());
+    c->pool->run(nchunk, [&](int j) { apply((int)((long long)n * j / nchunk), (int)((long long)n * (j + 1) / nchunk)); });
+  }
+  if (hi >= 0) {
+    c->tdirty_lo = std::min(c->tdirty_lo, lo);
+    c->tdirty_hi = std::max(c->tdirty_hi, hi);
+  }
+  return IMA_OK;
+}
+
 extern "C" int ima_gpu_set_pi(ima_ctx *c, int ci, int li, const double *pi4)
 {
   if (!c || !pi4) return IMA_ERR_ARG;
@@ -911,6 +990,25 @@ extern "C" int ima_gpu_set_allele_edits(ima_ctx *c, int n, const int *ci, const 
   return IMA_OK;
 }
 
+// the float-float copy of uploaded FP64 node times, made on the device (the
+// same two roundings the host mirror makes), so a re-timing copies 8 bytes
+// per node instead of 16
+__global__ void k_split_times(const double *t64, float2 *tff, size_t n)
+{
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double t = t64[i];
+  const float hi = (float)t;
+  tff[i] = make_float2(hi, (float)(t - (double)hi));
+}
+
+static void split_times(ima_ctx *c, size_t n0, size_t n1)
+{
+  if (n1 <= n0) return;
+  const size_t n = n1 - n0;
+  k_split_times<<<(unsigned)((n + 255) / 256), 256, 0, c->st>>>(c->d_t64 + n0, c->d_tff + n0, n);
+}
+
 static int flush_times(ima_ctx *c)
 {
   if (c->tdirty_hi < 0) return IMA_OK;
@@ -920,7 +1018,7 @@ static int flush_times(ima_ctx *c)
   cudaStream_t st = c->st;
   int r = IMA_OK;
   r = r ? r : c->cuda(cudaMemcpyAsync(c->d_t64 + n0, c->h_t64 + n0, (n1 - n0) * sizeof(double), cudaMemcpyHostToDevice, st), "times");
-  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_tff + n0, c->h_tff + n0, (n1 - n0) * sizeof(float2), cudaMemcpyHostToDevice, st), "times");
+  if (!r) split_times(c, n0, n1);
   r = r ? r : c->cuda(cudaMemcpyAsync(c->d_len + lo, c->h_len + lo, (hi - lo + 1) * sizeof(double), cudaMemcpyHostToDevice, st), "length");
   c->tdirty_lo = INT32_MAX;
   c->tdirty_hi = -1;
@@ -947,7 +1045,7 @@ static int flush(ima_ctx *c)
   int r = IMA_OK;
   r = r ? r : c->cuda(cudaMemcpyAsync(c->d_nodes + n0, c->h_nodes + n0, (n1 - n0) * sizeof(NodeRec), cudaMemcpyHostToDevice, st), "nodes");
   r = r ? r : c->cuda(cudaMemcpyAsync(c->d_t64 + n0, c->h_t64 + n0, (n1 - n0) * sizeof(double), cudaMemcpyHostToDevice, st), "times");
-  r = r ? r : c->cuda(cudaMemcpyAsync(c->d_tff + n0, c->h_tff + n0, (n1 - n0) * sizeof(float2), cudaMemcpyHostToDevice, st), "times");
+  if (!r) split_times(c, n0, n1);
   r = r ? r : c->cuda(cudaMemcpyAsync(c->d_sched + s0, c->h_sched + s0, (s1 - s0) * sizeof(int16_t), cudaMemcpyHostToDevice, st), "sched");
   r = r ? r : c->cuda(cudaMemcpyAsync(c->d_nlev + lo, c->h_nlev + lo, (hi - lo + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, st), "levels");
   r = r ? r : c->cuda(cudaMemcpyAsync(c->d_len + lo, c->h_len + lo, (hi - lo + 1) * sizeof(double), cudaMemcpyHostToDevice, st), "length");
@@ -1062,17 +1160,26 @@ static int build_batch(ima_ctx *c, Batch &b, int n, const int32_t *ci, const int
     cudaFree(b.d_req);
     cudaFree(b.d_res);
     cudaFree(b.d_st);
+    cudaFreeHost(b.h_res);
+    cudaFreeHost(b.h_st);
+    cudaFreeHost(b.h_reqpin);
     size_t &B = c->dev_bytes;
     b.d_req = dev_alloc<ReqDev>(n, B, c->st);
     b.d_res = dev_alloc<double>(n, B, c->st);
     b.d_st = dev_alloc<int32_t>(n, B, c->st);
-    if (!b.d_req || !b.d_res || !b.d_st) {
+    b.h_res = host_alloc<double>(n);
+    b.h_st = host_alloc<int32_t>(n);
+    b.h_reqpin = host_alloc<ReqDev>(n);
+    if (!b.d_req || !b.d_res || !b.d_st || !b.h_res || !b.h_st || !b.h_reqpin) {
       b.cap = 0;
       return c->fail(IMA_ERR_NOMEM, "batch buffers");
     }
     b.cap = n;
   }
-  return c->cuda(cudaMemcpyAsync(b.d_req, b.h_req.data(), n * sizeof(ReqDev), cudaMemcpyHostToDevice, c->st), "requests");
+  // an earlier upload from the staging buffer may still be queued
+  if (int r = c->cuda(cudaStreamSynchronize(c->st), "requests")) return r;
+  memcpy(b.h_reqpin, b.h_req.data(), n * sizeof(ReqDev));
+  return c->cuda(cudaMemcpyAsync(b.d_req, b.h_reqpin, n * sizeof(ReqDev), cudaMemcpyHostToDevice, c->st), "requests");
 }
 
 static double hky_bytes(ima_ctx *c, const Batch &b)
@@ -1159,15 +1266,13 @@ static int init_sumlogk(ima_ctx *c, Batch &b)
 
 static int fetch(ima_ctx *c, Batch &b, double *result, int32_t *status)
 {
-  std::vector<double> res(b.n);
-  std::vector<int32_t> sts(b.n);
-  int r = c->cuda(cudaMemcpyAsync(res.data(), b.d_res, b.n * sizeof(double), cudaMemcpyDeviceToHost, c->st), "results");
-  r = r ? r : c->cuda(cudaMemcpyAsync(sts.data(), b.d_st, b.n * sizeof(int32_t), cudaMemcpyDeviceToHost, c->st), "status");
+  int r = c->cuda(cudaMemcpyAsync(b.h_res, b.d_res, b.n * sizeof(double), cudaMemcpyDeviceToHost, c->st), "results");
+  r = r ? r : c->cuda(cudaMemcpyAsync(b.h_st, b.d_st, b.n * sizeof(int32_t), cudaMemcpyDeviceToHost, c->st), "status");
   r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "evaluation");
   if (r) return r;
   for (int k = 0; k < b.n; k++) {
-    if (result) result[b.order[k]] = res[k];
-    if (status) status[b.order[k]] = sts[k];
+    if (result) result[b.order[k]] = b.h_res[k];
+    if (status) status[b.order[k]] = b.h_st[k];
   }
   // remember the format of the per-branch SW terms
   for (int k = b.nis + b.nhky; k < b.n; k++) {
@@ -1180,9 +1285,15 @@ static int fetch(ima_ctx *c, Batch &b, double *result, int32_t *status)
 static void free_batch(Batch &b)
 {
   if (b.graph) cudaGraphExecDestroy(b.graph);
+  if (b.sgraph) cudaGraphExecDestroy(b.sgraph);
   cudaFree(b.d_req);
   cudaFree(b.d_res);
   cudaFree(b.d_st);
+  cudaFree(b.d_items);
+  cudaFree(b.d_acc);
+  cudaFreeHost(b.h_res);
+  cudaFreeHost(b.h_st);
+  cudaFreeHost(b.h_reqpin);
   b = Batch();
 }
 
@@ -1336,6 +1447,10 @@ extern "C" int ima_gpu_batch_autotune(ima_ctx *c, int batch, int reps, int *hky_
     c->event_pool.push_back(e1);
     r = c->cuda(cudaGetLastError(), "autotune");
     if (r) return r;
+    if (b.sgraph) {
+      cudaGraphExecDestroy(b.sgraph);
+      b.sgraph = nullptr;
+    }
     if (b.graph) {  // re-captured with the chosen shapes on the next run
       cudaStreamSynchronize(c->st);
       cudaGraphExecDestroy(b.graph);
@@ -1355,12 +1470,115 @@ extern "C" int ima_gpu_batch_set_variants(ima_ctx *c, int batch, int hky_variant
   Batch &b = c->batches[batch];
   b.hky_variant = hky_variant;
   b.sw_variant = sw_variant;
+  if (b.graph || b.sgraph) cudaStreamSynchronize(c->st);
   if (b.graph) {
-    cudaStreamSynchronize(c->st);
     cudaGraphExecDestroy(b.graph);
     b.graph = nullptr;
   }
+  if (b.sgraph) {
+    cudaGraphExecDestroy(b.sgraph);
+    b.sgraph = nullptr;
+  }
   return IMA_OK;
+}
+
+// the swap sweep of every run on the committed sums, Philox stream
+static void enqueue_swap(ima_ctx *c, int swaptries, int include_probg, uint64_t seed)
+{
+  SwapArgs a{};
+  a.nruns = c->nruns;
+  a.cpr = c->cpr;
+  a.nloci = c->nloci;
+  a.swaptries = swaptries;
+  a.include_probg = include_probg;
+  a.stride = 1;
+  a.pdg = c->d_pdg;
+  a.probg = c->d_probg;
+  a.beta = c->d_beta;
+  a.allbetas = c->d_allbetas;
+  a.uniforms = nullptr;
+  a.seed = seed;
+  a.counter = c->d_ctr;
+  a.used = c->d_used;
+  a.swap0ok = c->d_swap0ok;
+  a.swapcount = c->d_swapcount;
+  a.tempcount = c->d_tempcount;
+  a.S = c->d_S;
+  c->launch(IMA_K_SWAP, (double)c->nitems * 8.0, [&] { launch_swap(a, c->st); });
+}
+
+// One MC3 sweep of a batch: every request evaluated, the accepted ones
+// committed (partial likelihoods and pdg), then the swap attempts of every
+// run on the committed sums -- every kernel of the sweep in one graph launch
+// when use_graph is set (captured on the first call, kept while swaptries,
+// include_probg and seed are unchanged; the Philox counters advance on the
+// device, so each replay draws new uniforms).
+extern "C" int ima_gpu_batch_sweep(ima_ctx *c, int batch, const uint8_t *accept, int swaptries, int include_probg,
+                                   uint64_t seed, int use_graph)
+{
+  if (!c || batch < 0 || batch >= (int)c->batches.size() || !c->batches[batch].live) return IMA_ERR_ARG;
+  if (swaptries < 0) return c->fail(IMA_ERR_ARG, "swaptries must be >= 0");
+  Batch &b = c->batches[batch];
+  int r = flush(c);
+  r = r ? r : init_sumlogk(c, b);
+  if (r) return r;
+  if (!b.d_items) {
+    std::vector<int32_t> items(b.n);
+    for (int k = 0; k < b.n; k++) items[k] = b.h_req[k].item;
+    b.d_items = dev_alloc<int32_t>(b.n, c->dev_bytes, c->st);
+    b.d_acc = dev_alloc<uint8_t>(b.n, c->dev_bytes, c->st);
+    if (!b.d_items || !b.d_acc) return c->fail(IMA_ERR_NOMEM, "sweep buffers");
+    r = c->cuda(cudaMemcpyAsync(b.d_items, items.data(), b.n * 4, cudaMemcpyHostToDevice, c->st), "sweep items");
+    r = r ? r : c->cuda(cudaMemsetAsync(b.d_acc, 1, b.n, c->st), "sweep mask");
+    r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "sweep items");
+    if (r) return r;
+  }
+  if (accept) {  // caller order -> the batch's grouped order
+    std::vector<uint8_t> acc(b.n);
+    for (int k = 0; k < b.n; k++) acc[k] = accept[b.order[k]];
+    r = c->cuda(cudaMemcpyAsync(b.d_acc, acc.data(), b.n, cudaMemcpyHostToDevice, c->st), "sweep mask");
+    r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "sweep mask");
+    if (r) return r;
+  }
+  const bool swap = c->cpr >= 2;
+  auto body = [&] {
+    enqueue(c, b);
+    Pools P = c->pools();
+    launch_hky_commit(P, b.d_items, b.d_acc, b.n, c->st);
+    launch_pdg_commit(b.d_items, b.d_acc, c->d_pdg_new, c->d_pdg, b.n, c->st);
+    c->launches += 2;
+    if (swap) enqueue_swap(c, swaptries, include_probg, seed);
+  };
+  const int nk = (b.nis ? 1 : 0) + (b.nhky ? 1 : 0) + (b.nsw ? 1 : 0) + 2 + (swap ? 1 : 0);
+  if (!use_graph || c->profiling) {
+    body();
+    return c->cuda(cudaGetLastError(), "sweep");
+  }
+  if (b.sgraph && (b.s_tries != swaptries || b.s_probg != include_probg || b.s_seed != seed)) {
+    cudaStreamSynchronize(c->st);
+    cudaGraphExecDestroy(b.sgraph);
+    b.sgraph = nullptr;
+  }
+  if (!b.sgraph) {
+    cudaGraph_t g;
+    r = c->cuda(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal), "capture");
+    if (r) return r;
+    const long long before = c->launches;
+    body();
+    c->launches = before;  // counted when replayed
+    r = c->cuda(cudaStreamEndCapture(c->st, &g), "capture end");
+    if (r) return r;
+    r = c->cuda(cudaGraphInstantiate(&b.sgraph, g, 0), "graph instantiate");
+    cudaGraphDestroy(g);
+    if (r) return r;
+    b.s_tries = swaptries;
+    b.s_probg = include_probg;
+    b.s_seed = seed;
+  }
+  r = c->cuda(cudaGraphLaunch(b.sgraph, c->st), "graph launch");
+  c->launches += nk;
+  c->graph_launches++;
+  return r;
 }
 
 extern "C" int ima_gpu_batch_results(ima_ctx *c, int batch, double *result, int32_t *status)
@@ -3464,7 +3682,14 @@ extern "C" int ima_gpu_checkpoint_write(ima_ctx *c, const char *path, const ima_
   }
   F.put(c->h_nodes, nn * sizeof(NodeRec));
   F.put(c->h_t64, nn * 8);
-  F.put(c->h_tff, nn * sizeof(float2));
+  {  // the float-float copy the device keeps, as the device makes it
+    std::vector<float2> tff(nn);
+    for (size_t k = 0; k < nn; k++) {
+      const float hi = (float)c->h_t64[k];
+      tff[k] = make_float2(hi, (float)(c->h_t64[k] - (double)hi));
+    }
+    F.put(tff.data(), nn * sizeof(float2));
+  }
   F.put(c->h_sched, c->nsched * sizeof(int16_t));
   F.put(c->h_nlev, ni * 4);
   F.put(c->h_len, ni * 8);
@@ -3614,7 +3839,7 @@ extern "C" int ima_gpu_checkpoint_read(ima_ctx *c, const char *path, ima_mt19937
   if (r) return r;
   memcpy(c->h_nodes, nodes.data(), nodes.size());
   memcpy(c->h_t64, t64.data(), t64.size());
-  memcpy(c->h_tff, tff.data(), tff.size());
+  // the float-float times are made again from the FP64 ones at the upload
   memcpy(c->h_sched, sched.data(), sched.size());
   memcpy(c->h_nlev, nlev.data(), nlev.size());
   memcpy(c->h_len, len.data(), len.size());

@@ -196,19 +196,18 @@ __device__ __forceinline__ ff ff_fma_pos_u(ff a, ff b, ff c)
   return ff_make(s.hi, __fadd_rn(s.lo, __fadd_rn(pe, c.lo)));
 }
 
-// v_j = E1 S_o + b_c S_c + d_c L_j
+// v_j = E1 S_o + b_c S_c + d_c L_j, left unnormalised too: its only use is
+// the product of the two daughters, whose ff_mul renormalises
 __device__ __forceinline__ void hky_apply_ff(const HkyCoefFF &K, const ff *pi, const ff *L, ff *v)
 {
   const ff SR = ff_fma_pos_u(pi[2], L[2], ff_mul_u(pi[0], L[0]));
   const ff SY = ff_fma_pos_u(pi[3], L[3], ff_mul_u(pi[1], L[1]));
   const ff tR = ff_fma_pos_u(K.bR, SR, ff_mul_u(K.a, SY));
   const ff tY = ff_fma_pos_u(K.bY, SY, ff_mul_u(K.a, SR));
-  const ff w0 = ff_fma_pos_u(K.dR, L[0], tR), w2 = ff_fma_pos_u(K.dR, L[2], tR);
-  const ff w1 = ff_fma_pos_u(K.dY, L[1], tY), w3 = ff_fma_pos_u(K.dY, L[3], tY);
-  v[0] = fast_two_sum(w0.hi, w0.lo);
-  v[1] = fast_two_sum(w1.hi, w1.lo);
-  v[2] = fast_two_sum(w2.hi, w2.lo);
-  v[3] = fast_two_sum(w3.hi, w3.lo);
+  v[0] = ff_fma_pos_u(K.dR, L[0], tR);
+  v[2] = ff_fma_pos_u(K.dR, L[2], tR);
+  v[1] = ff_fma_pos_u(K.dY, L[1], tY);
+  v[3] = ff_fma_pos_u(K.dY, L[3], tY);
 }
 
 __device__ __forceinline__ ff ff_of(float2 v) { return ff_make(v.x, v.y); }
@@ -310,8 +309,12 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
   const LocusDev L = P.loci[it.locus];
   const int n = it.n, nl = 2 * n - 1, S = L.nsites, nint = n - 1;
   const int nlev = P.nlev[R.item];
-  const HkyLayout lay = hky_layout(maxnl, sizeof(float));
-  float *Pm = reinterpret_cast<float *>(smem);               // [maxnl][16]: 5 coefficients per branch (FF: pairs)
+  // [maxnl][PMS]: 5 coefficients per branch (FF: pairs); FF tip branches
+  // hold instead the columns of P(b) for the four observed states, [4][4]
+  // pairs, so a tip daughter costs four loads
+  constexpr int PMS = FF ? 32 : 16;
+  const HkyLayout lay = hky_layout(maxnl, FF ? 2 * sizeof(float) : sizeof(float));
+  float *Pm = reinterpret_cast<float *>(smem);
   Tree T;
   T.nd = reinterpret_cast<NodeRec *>(smem + lay.nd);
   T.fresh = reinterpret_cast<uint8_t *>(smem + lay.fresh);
@@ -374,10 +377,25 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
       const int u = T.nd[c].up0;
       const ff tc = ff_of(tff[c]);
       const ff br = (u < 0) ? tc : ff_sub(tc, ff_of(tff[u]));
-      hky_coef_ff(pif, ff_of(skpa), ff_mul(ff_of(smu), br), Pm + 16 * c);
+      float Kc[10];
+      hky_coef_ff(pif, ff_of(skpa), ff_mul(ff_of(smu), br), Kc);
+      float *dst = Pm + PMS * c;
+      if (c < n) {
+        const HkyCoefFF K = load_coef_ff(Kc);
+#pragma unroll
+        for (int st = 0; st < 4; st++) {
+          ff v[4];
+          hky_apply_tip_ff(K, pif, st, v);
+#pragma unroll
+          for (int j = 0; j < 4; j++) reinterpret_cast<float2 *>(dst)[4 * st + j] = make_float2(v[j].hi, v[j].lo);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 10; j++) dst[j] = Kc[j];
+      }
     } else {
       float pil[4] = {spi[0].x, spi[1].x, spi[2].x, spi[3].x};
-      hky_coef_fast(pil, skpa.x, smu.x * branch_ff(T.nd, tff, c), Pm + 16 * c);
+      hky_coef_fast(pil, skpa.x, smu.x * branch_ff(T.nd, tff, c), Pm + PMS * c);
     }
   }
   __syncthreads();
@@ -394,10 +412,19 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
   constexpr int NW = BS / 32;
   const int warp = tid >> 5, lane = tid & 31;
   const int nch = (S + 31) >> 5;
+  // a warp's task q = jj * nch + chunk advances by NW: by NW / nch nodes and
+  // NW % nch chunks (no division in the loop)
+  const int jstep = NW / nch, cstep = NW - jstep * nch;
+  const int j0 = warp / nch, c0 = warp - j0 * nch;
   for (int lv = 0; lv < nlev; lv++) {
     const int beg = T.lstart[lv], total = (T.lstart[lv + 1] - beg) * nch;
-    for (int q = warp; q < total; q += NW) {
-      const int jj = q / nch, i = (q - jj * nch) * 32 + lane;
+    int jj = j0, ch = c0;
+    for (int q = warp; q < total; q += NW, jj += jstep, ch += cstep) {
+      if (ch >= nch) {
+        ch -= nch;
+        jj++;
+      }
+      const int i = ch * 32 + lane;
       const int node = T.order[beg + jj];
       if (!T.fresh[node] || i >= S) continue;
       const int cc[2] = {T.nd[node].up0, T.nd[node].up1};
@@ -409,10 +436,16 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
 #pragma unroll
         for (int h = 0; h < 2; h++) {
           const int c = cc[h];
-          const HkyCoefFF K = load_coef_ff(Pm + 16 * c);
           if (c < n) {
-            hky_apply_tip_ff(K, pif, tips ? stip[c * S + i] : seq[(size_t)c * S + i], v[h]);
+            const int st = tips ? stip[c * S + i] : seq[(size_t)c * S + i];
+            const float4 *col = reinterpret_cast<const float4 *>(Pm + PMS * c) + 2 * st;
+            const float4 a = col[0], b = col[1];
+            v[h][0] = ff_make(a.x, a.y);
+            v[h][1] = ff_make(a.z, a.w);
+            v[h][2] = ff_make(b.x, b.y);
+            v[h][3] = ff_make(b.z, b.w);
           } else {
+            const HkyCoefFF K = load_coef_ff(Pm + PMS * c);
             float4 hi, lo;
             if (CACHE && T.fresh[c]) {
               const size_t ci = (size_t)(c - n) * cache_S + i;
@@ -450,7 +483,7 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
 #pragma unroll
         for (int h = 0; h < 2; h++) {
           const int c = cc[h];
-          const float *Kp = Pm + 16 * c;
+          const float *Kp = Pm + PMS * c;
           const HkyCoef K = {Kp[0], Kp[1], Kp[2], Kp[3], Kp[4]};
           if (c < n) {
             hky_apply_tip(K, pi4, tips ? stip[c * S + i] : seq[(size_t)c * S + i], v[h]);
@@ -713,7 +746,7 @@ static void hky_fast_bs(const Pools &P, const ReqDev *reqs, int nreq, int maxnl,
   // HKY_TIP_BUDGET bytes (a few KB: occupancy is unchanged)
   const size_t maxn = (size_t)(maxnl + 1) / 2;
   const int tip_cap = (maxn * maxS <= HKY_TIP_BUDGET) ? (int)(maxn * maxS) : 0;
-  size_t base = hky_smem((int)maxn, sizeof(float)) + (((size_t)tip_cap + 15) & ~size_t(15));
+  size_t base = hky_smem((int)maxn, FF ? 2 * sizeof(float) : sizeof(float)) + (((size_t)tip_cap + 15) & ~size_t(15));
   size_t cache = (size_t)(maxnl / 2) * maxS * ((FF ? 2 : 1) * sizeof(float4) + sizeof(int32_t));
   if (cache_ok && cache <= HKY_CACHE_BUDGET) {
     size_t sm = base + cache;

@@ -20,6 +20,8 @@
 // Branches outside the float-float range (x below 1e-15 with |d| >= 2, or a
 // Miller value the reference would take below 1e-300) take the FP64 path.
 // FP64 form: the reference algorithm in FP64, one thread per branch.
+#include <algorithm>
+#include <atomic>
 #include <cfloat>
 
 #include "ff.cuh"
@@ -226,14 +228,15 @@ __device__ __forceinline__ ff warp_sum_ff(ff v)
 // branch terms (float2) and the |d| >= 2 queue (int16) live in dynamic shared
 // memory sized for the batch's largest chain-locus
 
-// Three phases per CTA of up to 8 chain-loci: (A) every branch through the
-// branch-free core, with |d| >= 2 branches queued; (B) the queued Miller
+// Three phases per CTA of up to MAXI chain-loci: (A) every branch through
+// the branch-free core, with |d| >= 2 branches queued; (B) the queued Miller
 // recurrences, packed onto consecutive threads; (C) one warp per chain-locus
-// sums its branch terms in float-float.
-// IPC chain-loci per CTA of 32 * IPC threads (one warp reduces each)
-template <int IPC>
-__global__ void __launch_bounds__(32 * IPC) k_sw_fast(Pools P, const ReqDev *reqs, int nreq,
-                                                        double *result, int32_t *status, int maxb)
+// sums its branch terms in float-float.  `per` chain-loci go to each CTA:
+// the host picks it so that the whole batch is one wave of resident CTAs.
+constexpr int SW_NT = 256;  // threads per CTA
+template <int MAXI, int MINB>
+__global__ void __launch_bounds__(SW_NT, MINB) k_sw_fast(Pools P, const ReqDev *reqs, int nreq, int per,
+                                                           double *result, int32_t *status, int maxb)
 {
   __shared__ SwTables T;
   extern __shared__ __align__(16) char sw_smem[];
@@ -241,11 +244,15 @@ __global__ void __launch_bounds__(32 * IPC) k_sw_fast(Pools P, const ReqDev *req
   int16_t *queue = reinterpret_cast<int16_t *>(vals + maxb);   // |d| >= 2: the Miller recurrence
   int16_t *gqueue = queue + maxb;                              // longer branches: the float-float core
   __shared__ int qn, gn;
-  __shared__ int bstart[IPC + 1];
-  __shared__ int zero[IPC];
-  __shared__ float2 uff[IPC], trff[IPC];
-  const int r0 = blockIdx.x * IPC;
-  const int nit = min(IPC, nreq - r0);
+  __shared__ int bstart[MAXI + 1];
+  __shared__ int zero[MAXI];
+  __shared__ float2 uff[MAXI], trff[MAXI];
+  // each chain-locus's node base and marker allele base, staged once so a
+  // branch's loads start from shared memory (request -> item -> node would
+  // be two more dependent global loads per branch)
+  __shared__ int s_noff[MAXI], s_alb[MAXI], s_nl[MAXI];
+  const int r0 = blockIdx.x * per;
+  const int nit = min(per, nreq - r0);
   const int tid = threadIdx.x;
   if (tid < 36) {
     int t = tid / 9, k = tid % 9;
@@ -258,35 +265,42 @@ __global__ void __launch_bounds__(32 * IPC) k_sw_fast(Pools P, const ReqDev *req
   if (tid == 0) {
     qn = 0;
     gn = 0;
-    int b = 0;
-    for (int i = 0; i < nit; i++) {
-      bstart[i] = b;
-      b += 2 * P.items[reqs[r0 + i].item].n - 1;
-    }
-    bstart[nit] = b;
   }
   if (tid < nit) {
     const ReqDev R = reqs[r0 + tid];
+    const ItemDev it = P.items[R.item];
+    const int nl = 2 * it.n - 1;
+    s_noff[tid] = it.node_off;
+    s_alb[tid] = it.al_off + R.ai * nl;
+    s_nl[tid] = nl;
     float uh = (float)R.u, th = (float)R.par;
     uff[tid] = make_float2(uh, (float)(R.u - (double)uh));
     trff[tid] = make_float2(th, (float)(R.par - (double)th));
     zero[tid] = 0;
   }
   __syncthreads();
+  if (tid == 0) {
+    int b = 0;
+    for (int i = 0; i < nit; i++) {
+      bstart[i] = b;
+      b += s_nl[i];
+    }
+    bstart[nit] = b;
+  }
+  __syncthreads();
   const int total = bstart[nit];
-  // ---- phase A
-  for (int b = tid; b < total; b += (32 * IPC)) {
-    int i = 0;
+  // ---- phase A (a thread's branches only move forward: its chain-locus
+  // index carries over)
+  int i = 0;
+  for (int b = tid; b < total; b += SW_NT) {
     while (b >= bstart[i + 1]) i++;
-    const ReqDev &R = reqs[r0 + i];
-    const ItemDev it = P.items[R.item];
-    const int nl = 2 * it.n - 1, c = b - bstart[i];
-    const NodeRec nd = P.nodes[it.node_off + c];
+    const int c = b - bstart[i];
+    const NodeRec nd = P.nodes[s_noff[i] + c];
     float2 out = make_float2(0.f, 0.f);
     if (nd.down >= 0) {
-      const int32_t *A = P.alleles + it.al_off + (size_t)R.ai * nl;
+      const int32_t *A = P.alleles + s_alb[i];
       int n = abs(A[c] - A[nd.down]);
-      ff x = ff_mul(branch_len_ff(nd, P.tff + it.node_off, c, ffc(trff[i])), ffc(uff[i]));
+      ff x = ff_mul(branch_len_ff(nd, P.tff + s_noff[i], c, ffc(trff[i])), ffc(uff[i]));
       ff v;
       if (x.hi > 700.0f || (x.hi == 700.0f && x.lo > 0.0f)) {
         v = ff_sub(ffc(c_ff.logmydblmax), x);
@@ -311,40 +325,37 @@ __global__ void __launch_bounds__(32 * IPC) k_sw_fast(Pools P, const ReqDev *req
   __syncthreads();
   // ---- phase A2: longer branches through the float-float core, packed onto
   // consecutive threads
-  for (int q = tid; q < gn; q += (32 * IPC)) {
+  for (int q = tid; q < gn; q += SW_NT) {
     const int b = gqueue[q];
     int i = 0;
     while (b >= bstart[i + 1]) i++;
-    const ReqDev &R = reqs[r0 + i];
-    const ItemDev it = P.items[R.item];
-    const int nl = 2 * it.n - 1, c = b - bstart[i];
-    const NodeRec nd = P.nodes[it.node_off + c];
-    const int32_t *A = P.alleles + it.al_off + (size_t)R.ai * nl;
+    const int c = b - bstart[i];
+    const NodeRec nd = P.nodes[s_noff[i] + c];
+    const int32_t *A = P.alleles + s_alb[i];
     const int n = abs(A[c] - A[nd.down]);
-    const ff x = ff_mul(branch_len_ff(nd, P.tff + it.node_off, c, ffc(trff[i])), ffc(uff[i]));
+    const ff x = ff_mul(branch_len_ff(nd, P.tff + s_noff[i], c, ffc(trff[i])), ffc(uff[i]));
     const ff v = sw_core(x, n == 1 ? 1 : 0, T);
     vals[b] = make_float2(v.hi, v.lo);
   }
   __syncthreads();
   // ---- phase B: |d| >= 2
-  for (int q = tid; q < qn; q += (32 * IPC)) {
+  for (int q = tid; q < qn; q += SW_NT) {
     const int b = queue[q];
     int i = 0;
     while (b >= bstart[i + 1]) i++;
-    const ReqDev &R = reqs[r0 + i];
-    const ItemDev it = P.items[R.item];
-    const int nl = 2 * it.n - 1, c = b - bstart[i];
-    const NodeRec nd = P.nodes[it.node_off + c];
-    const int32_t *A = P.alleles + it.al_off + (size_t)R.ai * nl;
+    const int c = b - bstart[i];
+    const NodeRec nd = P.nodes[s_noff[i] + c];
+    const int32_t *A = P.alleles + s_alb[i];
     const int d = A[c] - A[nd.down];
-    ff x = ff_mul(branch_len_ff(nd, P.tff + it.node_off, c, ffc(trff[i])), ffc(uff[i]));
+    ff x = ff_mul(branch_len_ff(nd, P.tff + s_noff[i], c, ffc(trff[i])), ffc(uff[i]));
     ff r;
     float2 out;
     if (sw_miller(abs(d), x, &r)) {
       ff v = ff_add(ffc(vals[b]), r);
       out = make_float2(v.hi, v.lo);
     } else {  // rare: the reference's FP64 arithmetic
-      const double *t64 = P.t64 + it.node_off;
+      const ReqDev &R = reqs[r0 + i];
+      const double *t64 = P.t64 + s_noff[i];
       double t = (nd.up0 < 0) ? t64[c] * R.par : R.par * (t64[c] - t64[nd.up0]);
       bool z = false;
       double w = term_64(d, t * R.u, &z);
@@ -360,8 +371,8 @@ __global__ void __launch_bounds__(32 * IPC) k_sw_fast(Pools P, const ReqDev *req
   }
   __syncthreads();
   // ---- phase C: per chain-locus sums, dlikeA write-back
-  const int w = tid >> 5, lane = tid & 31;
-  if (w < nit) {
+  const int lane = tid & 31;
+  for (int w = tid >> 5; w < nit; w += SW_NT / 32) {
     const ReqDev &R = reqs[r0 + w];
     const ItemDev it = P.items[R.item];
     const int nl = 2 * it.n - 1;
@@ -473,25 +484,63 @@ int sw_init_tables()
   return 0;
 }
 
-template <int IPC>
-static void sw_fast_ipc(const Pools &P, const ReqDev *reqs, int nreq, int maxn, double *result, int32_t *status,
-                        cudaStream_t st)
+// Chain-loci per CTA that make the batch one wave of resident CTAs (at most
+// MAXI, and few enough that the int16 branch queues index every branch).
+// The occupancy query is remembered per device and shared-memory size.
+template <int MAXI, int MINB>
+static int sw_balanced_per(int nreq, int nlb)
 {
-  const int maxb = IPC * (2 * maxn - 1);  // queue entries are int16: IPC * (2 maxn - 1) < 32768
+  static std::atomic<long long> memo{-1};  // device << 40 | smem bytes << 8 | CTAs per SM
+  int dev = 0, nsm = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int cap = std::min(MAXI, 32767 / nlb);
+  int per = std::max(1, std::min(cap, (nreq + 4 * nsm - 1) / (4 * nsm)));
+  for (int round = 0; round < 3; round++) {
+    const long long sm = (long long)per * nlb * (sizeof(float2) + 2 * sizeof(int16_t));
+    int nb = 0;
+    const long long m = memo.load(std::memory_order_relaxed);
+    if (m >= 0 && (m >> 40) == dev && ((m >> 8) & 0xffffffffLL) == sm) {
+      nb = (int)(m & 0xff);
+    } else {
+      if (sm > 48 * 1024)
+        cudaFuncSetAttribute(k_sw_fast<MAXI, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_sw_fast<MAXI, MINB>, SW_NT, (size_t)sm) != cudaSuccess)
+        nb = 1;
+      nb = std::max(1, std::min(nb, 255));
+      memo.store(((long long)dev << 40) | (sm << 8) | nb, std::memory_order_relaxed);
+    }
+    const long long slots = (long long)nsm * nb;
+    const int want = std::max(1, std::min(cap, (int)((nreq + slots - 1) / slots)));
+    if (want == per) break;
+    per = want;
+  }
+  return per;
+}
+
+template <int MAXI, int MINB>
+static void sw_fast_launch(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int per, double *result,
+                           int32_t *status, cudaStream_t st)
+{
+  const int nlb = 2 * maxn - 1;
+  if (per <= 0) per = sw_balanced_per<MAXI, MINB>(nreq, nlb);
+  per = std::max(1, std::min(per, std::min(MAXI, 32767 / nlb)));
+  const int maxb = per * nlb;
   const size_t sm = (size_t)maxb * (sizeof(float2) + 2 * sizeof(int16_t));
   if (sm > 48 * 1024)
-    cudaFuncSetAttribute(k_sw_fast<IPC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_sw_fast<IPC><<<(nreq + IPC - 1) / IPC, 32 * IPC, sm, st>>>(P, reqs, nreq, result, status, maxb);
+    cudaFuncSetAttribute(k_sw_fast<MAXI, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_sw_fast<MAXI, MINB><<<(nreq + per - 1) / per, SW_NT, sm, st>>>(P, reqs, nreq, per, result, status, maxb);
 }
 
 void launch_sw_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int variant, double *result,
                     int32_t *status, cudaStream_t st)
 {
   if (nreq <= 0) return;
-  // wide variants only while the branch queue indexes fit int16
-  if (variant == 2 && 16 * (2 * maxn - 1) < 32768) sw_fast_ipc<16>(P, reqs, nreq, maxn, result, status, st);
-  else if (variant == 1) sw_fast_ipc<4>(P, reqs, nreq, maxn, result, status, st);
-  else sw_fast_ipc<8>(P, reqs, nreq, maxn, result, status, st);
+  // 0: one wave, registers for 5 CTAs of 256 threads per SM; 1: one wave,
+  // registers for 6; 2: 8 chain-loci per CTA whatever the wave count
+  if (variant == 1) sw_fast_launch<16, 6>(P, reqs, nreq, maxn, 0, result, status, st);
+  else if (variant == 2) sw_fast_launch<8, 5>(P, reqs, nreq, maxn, 8, result, status, st);
+  else sw_fast_launch<16, 5>(P, reqs, nreq, maxn, 0, result, status, st);
 }
 
 void launch_sw_fp64(const Pools &P, const ReqDev *reqs, int nreq, double *result,

@@ -95,6 +95,14 @@ int ima_gpu_set_genealogy(ima_ctx *ctx, int ci, int li, const int32_t *up0, cons
 int ima_gpu_set_genealogies(ima_ctx *ctx, int npairs, const int32_t *ci, const int32_t *li,
                             const int32_t *up0, const int32_t *up1, const int32_t *down,
                             const double *time, const double *length);
+/* New node times for genealogies whose topology is unchanged (the moves of
+ * changet_RY1, update_t_RY.cpp:279-335, and other re-timings): time is
+ * packed per pair as in ima_gpu_set_genealogies, length (may be NULL: the
+ * sum of branch lengths) per pair.  Each pair must already hold a genealogy
+ * (IMA_ERR_STATE).  Only the FP64 times travel: the device makes the
+ * float-float copy. */
+int ima_gpu_set_times(ima_ctx *ctx, int npairs, const int32_t *ci, const int32_t *li, const double *time,
+                      const double *length);
 /* Base frequencies of an HKY chain-locus (C[ci]->G[li].pi). */
 int ima_gpu_set_pi(ima_ctx *ctx, int ci, int li, const double *pi4);
 /* Allele states of linked marker ai on every node (gtree[i].A[ai]). */
@@ -178,6 +186,16 @@ int ima_gpu_batch_autotune(ima_ctx *ctx, int batch, int reps, int *hky_variant, 
 /* Pins a batch's launch variants (numbering as above). */
 int ima_gpu_batch_set_variants(ima_ctx *ctx, int batch, int hky_variant, int sw_variant);
 int ima_gpu_batch_results(ima_ctx *ctx, int batch, double *result, int32_t *status);
+/* One MC3 sweep of a batch (the loop body of ima_main_mpi.cpp:1821-1981 for
+ * the batch's chain-loci): every request evaluated, the accepted ones
+ * committed as copyfraclike does (accept [npairs] in the batch's caller
+ * order, or NULL: all), then swapchains (swapchains.cpp:526) of every run
+ * with swaptries attempts on the committed sums, drawing the device's
+ * per-run Philox stream keyed by seed.  With use_graph every kernel of the
+ * sweep is one CUDA graph launch, captured on the first call and replayed
+ * while swaptries, include_probg and seed stay the same. */
+int ima_gpu_batch_sweep(ima_ctx *ctx, int batch, const uint8_t *accept, int swaptries, int include_probg,
+                        uint64_t seed, int use_graph);
 int ima_gpu_batch_destroy(ima_ctx *ctx, int batch);
 /* Copy every staged genealogy edit to the device now (normally implicit). */
 int ima_gpu_flush_genealogies(ima_ctx *ctx);

@@ -61,3 +61,33 @@ def test_variants_out_of_range_are_rejected():
         b.set_variants(HKY_VARIANTS, 0)
     with pytest.raises(api.ImaError):
         b.set_variants(0, SW_VARIANTS)
+
+
+def test_sweep_graph_matches_separate_calls():
+    """ima_gpu_batch_sweep as one graph launch per sweep (evaluation, commit,
+    swaps) leaves the same betas, committed likelihoods and swap counts as the
+    same sweeps made call by call (batch run, commit, swapchains on the same
+    Philox stream), with an accept mask that changes between sweeps."""
+    out = []
+    for graph in (True, False):
+        wl, ctx, ci, li, u, par = _mixed_ctx()
+        ctx.setheat(0.9, 0.8, 1)
+        ctx.set_probg(np.linspace(-30.0, -20.0, wl.nchains))
+        b = ctx.batch_create(ci, li, u, par, precision=api.PREC_FAST)
+        rng = np.random.default_rng(4)
+        for s in range(6):
+            acc = (rng.uniform(size=len(ci)) < 0.7).astype(np.uint8)
+            if graph:
+                b.sweep(3, accept=acc, seed=11, use_graph=True)
+            else:
+                b.run(use_graph=False)
+                ctx.commit(ci, li, acc)
+                ctx.swapchains(3, True, seed=11)
+        ctx.synchronize()
+        counts = [ctx.get_swapcounts(r) for r in range(wl.nruns)]
+        out.append((ctx.get_betas(), ctx.get_pdg(), counts))
+        ctx.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    for (a, b_), (c, d) in zip(out[0][2], out[1][2]):
+        assert np.array_equal(a, c) and np.array_equal(b_, d)

@@ -45,6 +45,41 @@ def test_parallel_upload_matches_one_by_one():
     assert np.array_equal(a.eval(ci, li, u, par)[0], b.eval(ci, li, u, par)[0])
 
 
+@pytest.mark.parametrize("kind", ["hky", "is"])
+def test_set_times_matches_set_genealogies(kind):
+    """The times-only upload (long lists over the host threads, short ones
+    on the caller's) gives the bits of a full upload with the same times,
+    tree lengths included (the infinite-sites likelihood reads them), and
+    refuses a pair that holds no genealogy."""
+    if kind == "hky":
+        wl = workloads.make_hky(seed=33, nloci=12, nch=32, ncopies=10, nbases=300)   # 384 pairs
+    else:
+        wl = workloads.make_is(seed=34)
+    ci, li = wl.pairs()
+    pci, pli, up0, up1, down, tm = wl.packed()
+    u, par = wl.u.ravel(), wl.par.ravel()
+    a, b = _hky_ctx(wl), _hky_ctx(wl)
+    wl.upload(a)
+    wl.upload(b)
+    a.eval(ci, li, u, par)
+    b.eval(ci, li, u, par)
+    nl = np.array([2 * wl.tree(int(c), int(l)).n - 1 for c, l in zip(pci, pli)])
+    ends = np.cumsum(nl)
+    rng = np.random.default_rng(7)
+    for npairs in (len(pci), 5):
+        f = np.repeat(rng.uniform(0.9, 1.1, size=len(nl)), nl)   # one factor per genealogy keeps the order
+        scaled = np.where(tm > 0, tm * f, tm)
+        sel = slice(0, int(ends[npairs - 1]))
+        a.set_times(pci[:npairs], pli[:npairs], scaled[sel])
+        b.set_genealogies(pci[:npairs], pli[:npairs], up0[sel], up1[sel], down[sel], scaled[sel])
+        ra, sa = a.eval(ci, li, u, par)
+        rb, sb = b.eval(ci, li, u, par)
+        assert np.array_equal(ra, rb) and np.array_equal(sa, sb)
+    fresh = _hky_ctx(wl)
+    with pytest.raises(api.ImaError):
+        fresh.set_times([0], [0], tm[:nl[0]])
+
+
 def test_parallel_upload_rejects_a_bad_genealogy():
     wl = workloads.make_hky(seed=32, nloci=10, nch=32, ncopies=10, nbases=200)
     pci, pli, up0, up1, down, tm = wl.packed()
