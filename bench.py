@@ -452,11 +452,27 @@ def measure_lik(args, api, wl, steps, dist=None, device=0, hky_legs=False):
         if s >= args.warmup:
             e2e_t.append(t1 - t0)
             set_t.append(tm1 - t0)
+    # where an e2e step goes: the host-to-device copy of the staged times
+    # (with the float-float split), and an evaluation with nothing to upload
+    fl_t, ev_t = [], []
+    for s in range(args.warmup + min(steps, 50)):
+        ctx.set_times(pci, pli, scaled if s % 2 else tm)
+        t0 = time.perf_counter()
+        ctx.flush_genealogies()
+        ctx.synchronize()
+        t1 = time.perf_counter()
+        ctx.eval(ci, li, u, par, precision=prec)
+        t2 = time.perf_counter()
+        if s >= args.warmup:
+            fl_t.append(t1 - t0)
+            ev_t.append(t2 - t1)
     e2e = units * world / statistics.median(e2e_t)
     out["e2e"] = {"value": round(e2e, 1), "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
                   "d2h_bytes_per_step": int(d2h),
                   "ms_per_step": round(1e3 * statistics.median(e2e_t), 4),
                   "ms_set_times": round(1e3 * statistics.median(set_t), 4),
+                  "ms_upload": round(1e3 * statistics.median(fl_t), 4),
+                  "ms_eval_resident": round(1e3 * statistics.median(ev_t), 4),
                   "note": "every step re-times every genealogy (ima_gpu_set_times: FP64 times staged, "
                           "lengths summed on the host threads), then ima_gpu_eval copies the times, makes "
                           "their float-float form on the device, runs and copies results back"}

@@ -42,11 +42,14 @@ struct Batch {
   int n = 0, nis = 0, nhky = 0, nsw = 0, prec = IMA_PREC_FAST;
   std::vector<int> order;  // grouped position -> caller index
   ReqDev *d_req = nullptr;
-  double *d_res = nullptr;
+  double *d_res = nullptr;   // results, then the status words (one allocation, one copy back)
   int32_t *d_st = nullptr;
-  double *h_res = nullptr;   // pinned: results and status come back by DMA
+  double *h_res = nullptr;   // pinned, the same layout
   int32_t *h_st = nullptr;
   ReqDev *h_reqpin = nullptr;  // pinned staging of h_req for its upload
+  cudaEvent_t req_ev = nullptr;  // the last upload from h_reqpin
+  double hky_bytes = 0.0, sw_bytes = 0.0;  // algorithmic bytes of one run (launch statistics)
+  std::vector<int> dl_idx;  // SW requests' entries of ima_ctx::dl_fast
   std::vector<ReqDev> h_req;
   cudaGraphExec_t graph = nullptr;
   int maxn_is = 0, maxs_is = 0, maxn_hky = 0, maxs_hky = 0, maxn_sw = 0;
@@ -179,6 +182,7 @@ T *host_alloc(size_t count)
 
 struct ima_ctx {
   int device = 0;
+  int nsm = 152;  // SMs of the device
   cudaStream_t st = nullptr;
   std::string err;
   size_t dev_bytes = 0;
@@ -425,6 +429,7 @@ extern "C" int ima_gpu_create(int device, ima_ctx **out)
   }
   cudaEventCreate(&c->t0);
   cudaEventCreate(&c->t1);
+  cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
   if (sw_init_tables() != 0 || hky_init_tables() != 0) {
     delete c;
     return IMA_ERR_CUDA;
@@ -445,12 +450,11 @@ extern "C" void ima_gpu_destroy(ima_ctx *c)
     if (b.sgraph) cudaGraphExecDestroy(b.sgraph);
     cudaFree(b.d_req);
     cudaFree(b.d_res);
-    cudaFree(b.d_st);
     cudaFree(b.d_items);
     cudaFree(b.d_acc);
     cudaFreeHost(b.h_res);
-    cudaFreeHost(b.h_st);
     cudaFreeHost(b.h_reqpin);
+    if (b.req_ev) cudaEventDestroy(b.req_ev);
   }
   void *devs[] = {c->d_loci, c->d_seq, c->d_mult, c->d_sumlogk, c->d_flag, c->d_items,
                   c->d_nodes, c->d_t64, c->d_tff, c->d_sched, c->d_nlev, c->d_len, c->d_pi,
@@ -659,12 +663,15 @@ extern "C" int ima_gpu_set_chains(ima_ctx *c, int nruns, int chains_per_run)
 // times and lengths newer on the device than in the pinned mirror; every
 // host write into the mirror first copies them back, so that a later range
 // upload never carries stale values.
+// Before the host writes its mirror: values newer on the device (moved or
+// uploaded there) come back into it.
 static int sync_mirror(ima_ctx *c)
 {
+  int r = IMA_OK;
   if (c->dev_hi < 0) return IMA_OK;
   const ItemDev &a = c->items[c->dev_lo], &b = c->items[c->dev_hi];
   const size_t n0 = a.node_off, n1 = (size_t)b.node_off + 2 * b.n - 1;
-  int r = c->cuda(cudaMemcpyAsync(c->h_t64 + n0, c->d_t64 + n0, (n1 - n0) * sizeof(double), cudaMemcpyDeviceToHost, c->st), "mirror");
+  r = c->cuda(cudaMemcpyAsync(c->h_t64 + n0, c->d_t64 + n0, (n1 - n0) * sizeof(double), cudaMemcpyDeviceToHost, c->st), "mirror");
   r = r ? r : c->cuda(cudaMemcpyAsync(c->h_len + c->dev_lo, c->d_len + c->dev_lo, (size_t)(c->dev_hi - c->dev_lo + 1) * sizeof(double),
                                       cudaMemcpyDeviceToHost, c->st), "mirror");
   r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "mirror");
@@ -875,14 +882,52 @@ extern "C" int ima_gpu_set_genealogies(ima_ctx *c, int n, const int32_t *ci, con
   return r;
 }
 
+// the float-float copy of uploaded FP64 node times, made on the device (hi
+// the nearest float, lo the nearest float to the remainder), so a re-timing
+// copies 8 bytes per node instead of 16
+__global__ void k_split_times(const double *t64, float2 *tff, size_t n)
+{
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double t = t64[i];
+  const float hi = (float)t;
+  tff[i] = make_float2(hi, (float)(t - (double)hi));
+}
+
+// Tree lengths of items lo .. lo + n - 1, one thread per item summing its
+// branches in node order: the host's sum, bit for bit.
+__global__ void k_item_lengths(const ItemDev *items, const NodeRec *nodes, const double *t64, double *len, int lo, int n)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const ItemDev it = items[lo + k];
+  const NodeRec *r = nodes + it.node_off;
+  const double *t = t64 + it.node_off;
+  double L = 0.0;
+  for (int j = 0; j < 2 * it.n - 1; j++) {
+    const NodeRec nd = r[j];
+    if (nd.down >= 0) L += (nd.up0 < 0) ? t[j] : t[j] - t[nd.up0];
+  }
+  len[lo + k] = L;
+}
+
+static void split_times(ima_ctx *c, size_t n0, size_t n1)
+{
+  if (n1 <= n0) return;
+  const size_t n = n1 - n0;
+  k_split_times<<<(unsigned)((n + 255) / 256), 256, 0, c->st>>>(c->d_t64 + n0, c->d_tff + n0, n);
+}
+
+static int flush(ima_ctx *c);
+
 // Re-timings with the topology kept (the moves of changet_RY1 and of a
-// rubber band): only the node times, and the length, go to the mirror.
+// rubber band): only the node times, and the length (given, or summed here
+// in node order), go to the mirror.
 static void set_times_one(ima_ctx *c, int item, const double *time, double length)
 {
   const ItemDev &it = c->items[item];
   const int nl = 2 * it.n - 1;
-  double *t64 = c->h_t64 + it.node_off;
-  memcpy(t64, time, nl * sizeof(double));
+  memcpy(c->h_t64 + it.node_off, time, nl * sizeof(double));
   if (length >= 0.0) {
     c->h_len[item] = length;
     return;
@@ -899,11 +944,12 @@ extern "C" int ima_gpu_set_times(ima_ctx *c, int n, const int32_t *ci, const int
 {
   if (!c || n < 0 || (n > 0 && (!ci || !li || !time))) return IMA_ERR_ARG;
   if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
-  if (int rs = sync_mirror(c)) return rs;
+  if (n == 0) return IMA_OK;
   std::vector<size_t> &off = c->pair_off;
   off.resize((size_t)n + 1);
   off[0] = 0;
   int lo = INT32_MAX, hi = -1;
+  bool run = true;  // the pairs are items first, first + 1, ... in order
   for (int k = 0; k < n; k++) {
     if (!c->valid(ci[k], li[k])) return c->fail(IMA_ERR_ARG, "pair %d: chain %d locus %d out of range", k, ci[k], li[k]);
     const int item = c->item_of(ci[k], li[k]);
@@ -911,10 +957,38 @@ extern "C" int ima_gpu_set_times(ima_ctx *c, int n, const int32_t *ci, const int
     off[k + 1] = off[k] + 2 * c->loci[li[k]].d.n - 1;
     lo = std::min(lo, item);
     hi = std::max(hi, item);
+    run = run && item == c->item_of(ci[0], li[0]) + k;
   }
   const size_t *offp = off.data();
-  // a pair given twice keeps its later times only when the list is applied
-  // in order on one thread
+  if (run) {
+    // a contiguous run of items in order: the caller's packed times are the
+    // device layout of the run, so they go to the device in one copy (from
+    // pageable memory: the call returns once the buffer has been read), the
+    // device makes their float-float form and, when no lengths are given,
+    // the lengths (one thread per item, the host's order of additions).
+    // The device then holds the newer values; the mirror is refreshed before
+    // the host next writes it.  Uploads still pending from the mirror go
+    // first.
+    if (int r = flush(c)) return r;
+    const size_t n0 = c->items[lo].node_off, n1 = n0 + offp[n];
+    int r = c->cuda(cudaMemcpyAsync(c->d_t64 + n0, time, (n1 - n0) * sizeof(double), cudaMemcpyHostToDevice, c->st),
+                    "times upload");
+    if (r) return r;
+    split_times(c, n0, n1);
+    if (length)
+      r = c->cuda(cudaMemcpyAsync(c->d_len + lo, length, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->st),
+                  "length");
+    else
+      k_item_lengths<<<(n + 127) / 128, 128, 0, c->st>>>(c->d_items, c->d_nodes, c->d_t64, c->d_len, lo, n);
+    c->dev_lo = std::min(c->dev_lo, lo);
+    c->dev_hi = std::max(c->dev_hi, hi);
+    return r ? r : c->cuda(cudaGetLastError(), "times upload");
+  }
+
+  // any order: staged in the mirror on the host threads (a pair given twice
+  // keeps its later times only when the list is applied in order on one
+  // thread), copied with the next evaluation
+  if (int rs = sync_mirror(c)) return rs;
   bool repeat = false;
   if ((int)c->pair_stamp.size() != c->nitems) c->pair_stamp.assign(c->nitems, -1);
   const int gen = ++c->stamp_gen;
@@ -937,10 +1011,8 @@ extern "C" int ima_gpu_set_times(ima_ctx *c, int n, const int32_t *ci, const int
     const int nchunk = std::min(std::max(2, n / 64), 4 * c->pool->size());
     c->pool->run(nchunk, [&](int j) { apply((int)((long long)n * j / nchunk), (int)((long long)n * (j + 1) / nchunk)); });
   }
-  if (hi >= 0) {
-    c->tdirty_lo = std::min(c->tdirty_lo, lo);
-    c->tdirty_hi = std::max(c->tdirty_hi, hi);
-  }
+  c->tdirty_lo = std::min(c->tdirty_lo, lo);
+  c->tdirty_hi = std::max(c->tdirty_hi, hi);
   return IMA_OK;
 }
 
@@ -988,25 +1060,6 @@ extern "C" int ima_gpu_set_allele_edits(ima_ctx *c, int n, const int *ci, const 
     mark(c, item);
   }
   return IMA_OK;
-}
-
-// the float-float copy of uploaded FP64 node times, made on the device (the
-// same two roundings the host mirror makes), so a re-timing copies 8 bytes
-// per node instead of 16
-__global__ void k_split_times(const double *t64, float2 *tff, size_t n)
-{
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double t = t64[i];
-  const float hi = (float)t;
-  tff[i] = make_float2(hi, (float)(t - (double)hi));
-}
-
-static void split_times(ima_ctx *c, size_t n0, size_t n1)
-{
-  if (n1 <= n0) return;
-  const size_t n = n1 - n0;
-  k_split_times<<<(unsigned)((n + 255) / 256), 256, 0, c->st>>>(c->d_t64 + n0, c->d_tff + n0, n);
 }
 
 static int flush_times(ima_ctx *c)
@@ -1094,6 +1147,9 @@ static int ensure_ff_hky(ima_ctx *c)
   return c->cuda(cudaMemsetAsync(c->d_partlo, 0, c->npart * sizeof(float4), c->st), "float-float partials");
 }
 
+static double hky_bytes(ima_ctx *c, const Batch &b);
+static double sw_bytes(ima_ctx *c, const Batch &b);
+
 static int build_batch(ima_ctx *c, Batch &b, int n, const int32_t *ci, const int32_t *li, const double *u,
                        const double *kappa, const int32_t *edits, const int32_t *ai, int prec)
 {
@@ -1123,6 +1179,9 @@ static int build_batch(ima_ctx *c, Batch &b, int n, const int32_t *ci, const int
   b.nis = (int)g[0].size();
   b.nhky = (int)g[1].size();
   b.nsw = (int)g[2].size();
+  // fewer HKY chain-loci than SMs: each runs alone on its SM, so the
+  // widest CTA (256 threads) shortens the level chain
+  b.hky_variant = (b.nhky > 0 && b.nhky < c->nsm) ? 2 : 0;
   b.order.clear();
   b.h_req.clear();
   b.maxn_is = b.maxs_is = b.maxn_hky = b.maxs_hky = b.maxn_sw = 0;
@@ -1159,27 +1218,33 @@ static int build_batch(ima_ctx *c, Batch &b, int n, const int32_t *ci, const int
     cudaStreamSynchronize(c->st);
     cudaFree(b.d_req);
     cudaFree(b.d_res);
-    cudaFree(b.d_st);
     cudaFreeHost(b.h_res);
-    cudaFreeHost(b.h_st);
     cudaFreeHost(b.h_reqpin);
     size_t &B = c->dev_bytes;
+    const size_t rw = (size_t)n + ((size_t)n + 1) / 2;  // doubles holding n results and n status words
     b.d_req = dev_alloc<ReqDev>(n, B, c->st);
-    b.d_res = dev_alloc<double>(n, B, c->st);
-    b.d_st = dev_alloc<int32_t>(n, B, c->st);
-    b.h_res = host_alloc<double>(n);
-    b.h_st = host_alloc<int32_t>(n);
+    b.d_res = dev_alloc<double>(rw, B, c->st);
+    b.d_st = b.d_res ? reinterpret_cast<int32_t *>(b.d_res + n) : nullptr;
+    b.h_res = host_alloc<double>(rw);
+    b.h_st = b.h_res ? reinterpret_cast<int32_t *>(b.h_res + n) : nullptr;
     b.h_reqpin = host_alloc<ReqDev>(n);
-    if (!b.d_req || !b.d_res || !b.d_st || !b.h_res || !b.h_st || !b.h_reqpin) {
+    if (!b.req_ev) cudaEventCreateWithFlags(&b.req_ev, cudaEventDisableTiming);
+    if (!b.d_req || !b.d_res || !b.h_res || !b.h_reqpin || !b.req_ev) {
       b.cap = 0;
       return c->fail(IMA_ERR_NOMEM, "batch buffers");
     }
     b.cap = n;
   }
+  b.hky_bytes = hky_bytes(c, b);
+  b.sw_bytes = sw_bytes(c, b);
+  b.dl_idx.clear();
+  for (int k = b.nis + b.nhky; k < b.n; k++)
+    b.dl_idx.push_back(c->items[b.h_req[k].item].al_off + b.h_req[k].ai);
   // an earlier upload from the staging buffer may still be queued
-  if (int r = c->cuda(cudaStreamSynchronize(c->st), "requests")) return r;
+  if (int r = c->cuda(cudaEventSynchronize(b.req_ev), "requests")) return r;
   memcpy(b.h_reqpin, b.h_req.data(), n * sizeof(ReqDev));
-  return c->cuda(cudaMemcpyAsync(b.d_req, b.h_reqpin, n * sizeof(ReqDev), cudaMemcpyHostToDevice, c->st), "requests");
+  int r = c->cuda(cudaMemcpyAsync(b.d_req, b.h_reqpin, n * sizeof(ReqDev), cudaMemcpyHostToDevice, c->st), "requests");
+  return r ? r : c->cuda(cudaEventRecord(b.req_ev, c->st), "requests");
 }
 
 static double hky_bytes(ima_ctx *c, const Batch &b)
@@ -1217,19 +1282,19 @@ static void enqueue(ima_ctx *c, Batch &b)
   if (b.nhky) {
     const ReqDev *r = b.d_req + b.nis;
     if (b.prec == IMA_PREC_FP64)
-      c->launch(IMA_K_HKY_FP64, hky_bytes(c, b), [&] { launch_hky_fp64(P, r, b.nhky, b.maxn_hky, b.d_res + b.nis, b.d_st + b.nis, st); });
+      c->launch(IMA_K_HKY_FP64, b.hky_bytes, [&] { launch_hky_fp64(P, r, b.nhky, b.maxn_hky, b.d_res + b.nis, b.d_st + b.nis, st); });
     else if (b.prec == IMA_PREC_FP32)
-      c->launch(IMA_K_HKY_FP32, hky_bytes(c, b), [&] { launch_hky_fp32(P, r, b.nhky, b.maxn_hky, b.maxs_hky, b.hky_variant, b.d_res + b.nis, b.d_st + b.nis, st); });
+      c->launch(IMA_K_HKY_FP32, b.hky_bytes, [&] { launch_hky_fp32(P, r, b.nhky, b.maxn_hky, b.maxs_hky, b.hky_variant, b.d_res + b.nis, b.d_st + b.nis, st); });
     else
-      c->launch(IMA_K_HKY_FAST, hky_bytes(c, b), [&] { launch_hky_fast(P, r, b.nhky, b.maxn_hky, b.maxs_hky, b.hky_variant, b.d_res + b.nis, b.d_st + b.nis, st); });
+      c->launch(IMA_K_HKY_FAST, b.hky_bytes, [&] { launch_hky_fast(P, r, b.nhky, b.maxn_hky, b.maxs_hky, b.hky_variant, b.d_res + b.nis, b.d_st + b.nis, st); });
   }
   if (b.nsw) {
     const ReqDev *r = b.d_req + b.nis + b.nhky;
     int off = b.nis + b.nhky;
     if (b.prec == IMA_PREC_FP64)
-      c->launch(IMA_K_SW_FP64, sw_bytes(c, b), [&] { launch_sw_fp64(P, r, b.nsw, b.d_res + off, b.d_st + off, st); });
+      c->launch(IMA_K_SW_FP64, b.sw_bytes, [&] { launch_sw_fp64(P, r, b.nsw, b.d_res + off, b.d_st + off, st); });
     else
-      c->launch(IMA_K_SW_FAST, sw_bytes(c, b), [&] { launch_sw_fast(P, r, b.nsw, b.maxn_sw, b.sw_variant, b.d_res + off, b.d_st + off, st); });
+      c->launch(IMA_K_SW_FAST, b.sw_bytes, [&] { launch_sw_fast(P, r, b.nsw, b.maxn_sw, b.sw_variant, b.d_res + off, b.d_st + off, st); });
   }
 }
 
@@ -1266,8 +1331,16 @@ static int init_sumlogk(ima_ctx *c, Batch &b)
 
 static int fetch(ima_ctx *c, Batch &b, double *result, int32_t *status)
 {
-  int r = c->cuda(cudaMemcpyAsync(b.h_res, b.d_res, b.n * sizeof(double), cudaMemcpyDeviceToHost, c->st), "results");
-  r = r ? r : c->cuda(cudaMemcpyAsync(b.h_st, b.d_st, b.n * sizeof(int32_t), cudaMemcpyDeviceToHost, c->st), "status");
+  // results and status words lie together in one buffer of capacity
+  // b.cap: two copies when the batch fills less than its capacity
+  int r;
+  if (b.n == b.cap) {
+    r = c->cuda(cudaMemcpyAsync(b.h_res, b.d_res, b.n * (sizeof(double) + sizeof(int32_t)), cudaMemcpyDeviceToHost, c->st),
+                "results");
+  } else {
+    r = c->cuda(cudaMemcpyAsync(b.h_res, b.d_res, b.n * sizeof(double), cudaMemcpyDeviceToHost, c->st), "results");
+    r = r ? r : c->cuda(cudaMemcpyAsync(b.h_st, b.d_st, b.n * sizeof(int32_t), cudaMemcpyDeviceToHost, c->st), "status");
+  }
   r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "evaluation");
   if (r) return r;
   for (int k = 0; k < b.n; k++) {
@@ -1275,10 +1348,8 @@ static int fetch(ima_ctx *c, Batch &b, double *result, int32_t *status)
     if (status) status[b.order[k]] = b.h_st[k];
   }
   // remember the format of the per-branch SW terms
-  for (int k = b.nis + b.nhky; k < b.n; k++) {
-    const ItemDev &it = c->items[b.h_req[k].item];
-    c->dl_fast[it.al_off + (size_t)b.h_req[k].ai] = (b.prec != IMA_PREC_FP64);
-  }
+  const uint8_t fmt = (b.prec != IMA_PREC_FP64);
+  for (int k : b.dl_idx) c->dl_fast[k] = fmt;
   return IMA_OK;
 }
 
@@ -1288,12 +1359,11 @@ static void free_batch(Batch &b)
   if (b.sgraph) cudaGraphExecDestroy(b.sgraph);
   cudaFree(b.d_req);
   cudaFree(b.d_res);
-  cudaFree(b.d_st);
   cudaFree(b.d_items);
   cudaFree(b.d_acc);
   cudaFreeHost(b.h_res);
-  cudaFreeHost(b.h_st);
   cudaFreeHost(b.h_reqpin);
+  if (b.req_ev) cudaEventDestroy(b.req_ev);
   b = Batch();
 }
 

@@ -132,14 +132,17 @@ __device__ __forceinline__ ff sw_core(ff x, int d01, const SwTables &T)
   const ff xs = (x.hi > 0.f) ? x : ff_from(1.0f);
   ff y = ff_mul(x, ffc(c_ff.inv375));
   y = ff_mul(y, y);
-  ff z = ff_div(ff_from(3.75f), xs);
-  ff arg = small ? y : z;
+  // the division (x >= 3.75: 1% of branches) and log x (x >= 3.75 or
+  // |d| = 1) only where a lane needs them
+  ff arg = y;
+  if (!small) arg = ff_div(ff_from(3.75f), xs);
   const float2 *c = T.c[d01 * 2 + (small ? 1 : 0)];
   ff acc = ffc(c[8]);
 #pragma unroll
   for (int k = 7; k >= 0; k--) acc = ff_add_fast(ff_mul(acc, arg), ffc(c[k]));
   ff lp = ff_log(acc, c_ff);
-  ff lx = ff_log(xs, c_ff);
+  ff lx = ff_from(0.0f);
+  if (!small || d01) lx = ff_log(xs, c_ff);
   ff tail = small ? (d01 ? ff_sub(lx, x) : ff_neg(x)) : ff_make(-0.5f * lx.hi, -0.5f * lx.lo);
   return ff_add(lp, tail);
 }
@@ -225,14 +228,19 @@ __device__ __forceinline__ ff warp_sum_ff(ff v)
   return v;
 }
 
-// branch terms (float2) and the |d| >= 2 queue (int16) live in dynamic shared
-// memory sized for the batch's largest chain-locus
-
-// Three phases per CTA of up to MAXI chain-loci: (A) every branch through
-// the branch-free core, with |d| >= 2 branches queued; (B) the queued Miller
-// recurrences, packed onto consecutive threads; (C) one warp per chain-locus
-// sums its branch terms in float-float.  `per` chain-loci go to each CTA:
-// the host picks it so that the whole batch is one wave of resident CTAs.
+// Per CTA of 256 threads, `per` chain-loci (the host picks it so that the
+// batch is one wave of resident CTAs), in three phases:
+//  (A) classify: every branch's x = t tr u (float-float) goes to shared
+//      memory and the branch to one of four task lists, the longest work
+//      first: Miller recurrences (|d| >= 2), the float-float core (y > 0.01),
+//      short branches with |d| = 1 (series plus log x), short branches with
+//      d = 0 (series only);
+//  (T) tasks: warps take 32 consecutive tasks at a time from a shared
+//      counter, so lanes of a warp run the same form and warps that drew
+//      long recurrences take fewer tasks; each task writes its branch's term;
+//  (C) one warp per chain-locus sums its branch terms in float-float.
+// Lists 0 and 1 share one int32 array, filled from its two ends, and lists
+// 2 and 3 another; an entry is the branch (low 16 bits) and min(|d|, 65535).
 constexpr int SW_NT = 256;  // threads per CTA
 template <int MAXI, int MINB>
 __global__ void __launch_bounds__(SW_NT, MINB) k_sw_fast(Pools P, const ReqDev *reqs, int nreq, int per,
@@ -240,10 +248,10 @@ __global__ void __launch_bounds__(SW_NT, MINB) k_sw_fast(Pools P, const ReqDev *
 {
   __shared__ SwTables T;
   extern __shared__ __align__(16) char sw_smem[];
-  float2 *vals = reinterpret_cast<float2 *>(sw_smem);
-  int16_t *queue = reinterpret_cast<int16_t *>(vals + maxb);   // |d| >= 2: the Miller recurrence
-  int16_t *gqueue = queue + maxb;                              // longer branches: the float-float core
-  __shared__ int qn, gn;
+  float2 *vals = reinterpret_cast<float2 *>(sw_smem);          // x, then the branch term
+  int32_t *q01 = reinterpret_cast<int32_t *>(vals + maxb);      // Miller from the front, core from the back
+  int32_t *q23 = q01 + maxb;                                   // |d| = 1 short from the front, d = 0 from the back
+  __shared__ int qn[4], next;
   __shared__ int bstart[MAXI + 1];
   __shared__ int zero[MAXI];
   __shared__ float2 uff[MAXI], trff[MAXI];
@@ -262,10 +270,8 @@ __global__ void __launch_bounds__(SW_NT, MINB) k_sw_fast(Pools P, const ReqDev *
     if (k < m) v = d01 ? (small ? c_ff.i1s[k] : c_ff.i1l[k]) : (small ? c_ff.i0s[k] : c_ff.i0l[k]);
     T.c[t][k] = v;
   }
-  if (tid == 0) {
-    qn = 0;
-    gn = 0;
-  }
+  if (tid < 4) qn[tid] = 0;
+  if (tid == 0) next = 0;
   if (tid < nit) {
     const ReqDev R = reqs[r0 + tid];
     const ItemDev it = P.items[R.item];
@@ -289,89 +295,95 @@ __global__ void __launch_bounds__(SW_NT, MINB) k_sw_fast(Pools P, const ReqDev *
   }
   __syncthreads();
   const int total = bstart[nit];
-  // ---- phase A (a thread's branches only move forward: its chain-locus
-  // index carries over)
-  int i = 0;
-  for (int b = tid; b < total; b += SW_NT) {
-    while (b >= bstart[i + 1]) i++;
-    const int c = b - bstart[i];
-    const NodeRec nd = P.nodes[s_noff[i] + c];
-    float2 out = make_float2(0.f, 0.f);
-    if (nd.down >= 0) {
-      const int32_t *A = P.alleles + s_alb[i];
-      int n = abs(A[c] - A[nd.down]);
-      ff x = ff_mul(branch_len_ff(nd, P.tff + s_noff[i], c, ffc(trff[i])), ffc(uff[i]));
-      ff v;
-      if (x.hi > 700.0f || (x.hi == 700.0f && x.lo > 0.0f)) {
-        v = ff_sub(ffc(c_ff.logmydblmax), x);
-      } else if (n >= 1 && x.hi == 0.0f) {
-        zero[i] = 1;
-        v = ff_make(-INFINITY, 0.f);
-      } else {
-        const ff xq = ff_mul(x, ffc(c_ff.inv375));  // x / 3.75
-        const ff y = ff_mul(xq, xq);
-        if (y.hi <= SW_CHEAP_Y) {
-          v = sw_cheap(x, y, n == 1 ? 1 : 0);
+  // ---- phase A: classify (a thread's branches only move forward: its
+  // chain-locus index carries over)
+  {
+    int i = 0;
+    for (int b = tid; b < total; b += SW_NT) {
+      while (b >= bstart[i + 1]) i++;
+      const int c = b - bstart[i];
+      const NodeRec nd = P.nodes[s_noff[i] + c];
+      float2 out = make_float2(0.f, 0.f);
+      if (nd.down >= 0) {
+        const int32_t *A = P.alleles + s_alb[i];
+        const int n = abs(A[c] - A[nd.down]);
+        const ff x = ff_mul(branch_len_ff(nd, P.tff + s_noff[i], c, ffc(trff[i])), ffc(uff[i]));
+        if (x.hi > 700.0f || (x.hi == 700.0f && x.lo > 0.0f)) {
+          const ff v = ff_sub(ffc(c_ff.logmydblmax), x);
+          out = make_float2(v.hi, v.lo);
+        } else if (n >= 1 && x.hi == 0.0f) {
+          zero[i] = 1;
+          out = make_float2(-INFINITY, 0.f);
         } else {
-          gqueue[atomicAdd(&gn, 1)] = (int16_t)b;  // phase A2
-          v = ff_from(0.0f);
+          out = make_float2(x.hi, x.lo);
+          const ff xq = ff_mul(x, ffc(c_ff.inv375));  // x / 3.75
+          const float yh = ff_mul(xq, xq).hi;
+          const int e = b | (min(n, 65535) << 16);
+          if (n >= 2) q01[atomicAdd(&qn[0], 1)] = e;
+          else if (yh > SW_CHEAP_Y) q01[maxb - 1 - atomicAdd(&qn[1], 1)] = e;
+          else if (n == 1) q23[atomicAdd(&qn[2], 1)] = e;
+          else q23[maxb - 1 - atomicAdd(&qn[3], 1)] = e;
         }
-        if (n >= 2) queue[atomicAdd(&qn, 1)] = (int16_t)b;
       }
-      out = make_float2(v.hi, v.lo);
+      vals[b] = out;
     }
-    vals[b] = out;
   }
   __syncthreads();
-  // ---- phase A2: longer branches through the float-float core, packed onto
-  // consecutive threads
-  for (int q = tid; q < gn; q += SW_NT) {
-    const int b = gqueue[q];
-    int i = 0;
-    while (b >= bstart[i + 1]) i++;
-    const int c = b - bstart[i];
-    const NodeRec nd = P.nodes[s_noff[i] + c];
-    const int32_t *A = P.alleles + s_alb[i];
-    const int n = abs(A[c] - A[nd.down]);
-    const ff x = ff_mul(branch_len_ff(nd, P.tff + s_noff[i], c, ffc(trff[i])), ffc(uff[i]));
-    const ff v = sw_core(x, n == 1 ? 1 : 0, T);
+  // ---- phase T: the four lists as one sequence of tasks
+  const int n0 = qn[0], n1 = n0 + qn[1], n2 = n1 + qn[2], ntask = n2 + qn[3];
+  const int lane = tid & 31;
+  for (;;) {
+    int t0 = 0;
+    if (lane == 0) t0 = atomicAdd(&next, 32);
+    t0 = __shfl_sync(0xffffffffu, t0, 0);
+    if (t0 >= ntask) break;
+    const int t = t0 + lane;
+    if (t >= ntask) continue;
+    const int e = t < n0 ? q01[t] : t < n1 ? q01[maxb - 1 - (t - n0)] : t < n2 ? q23[t - n1] : q23[maxb - 1 - (t - n2)];
+    const int b = e & 0xffff;
+    int n = (int)((unsigned)e >> 16);
+    const float2 xv = vals[b];
+    const ff x = ff_make(xv.x, xv.y);
+    const ff xq = ff_mul(x, ffc(c_ff.inv375));
+    const ff y = ff_mul(xq, xq);
+    ff v;
+    if (t >= n1) {  // short branches
+      v = sw_cheap(x, y, t < n2 ? 1 : 0);
+    } else if (t >= n0) {  // the float-float core, |d| <= 1
+      v = sw_core(x, n, T);
+    } else {  // |d| >= 2: the d = 0 term and the Miller ratio
+      int i = 0;
+      while (b >= bstart[i + 1]) i++;
+      const int c = b - bstart[i];
+      if (n == 65535) {  // the exact difference from the alleles
+        const NodeRec nd = P.nodes[s_noff[i] + c];
+        const int32_t *A = P.alleles + s_alb[i];
+        n = abs(A[c] - A[nd.down]);
+      }
+      const ff base = (y.hi <= SW_CHEAP_Y) ? sw_cheap(x, y, 0) : sw_core(x, 0, T);
+      ff r;
+      if (sw_miller(n, x, &r)) {
+        v = ff_add(base, r);
+      } else {  // rare: the reference's FP64 arithmetic
+        const NodeRec nd = P.nodes[s_noff[i] + c];
+        const ReqDev &R = reqs[r0 + i];
+        const double *t64 = P.t64 + s_noff[i];
+        double tt = (nd.up0 < 0) ? t64[c] * R.par : R.par * (t64[c] - t64[nd.up0]);
+        bool z = false;
+        double w = term_64(n, tt * R.u, &z);
+        if (z) {
+          zero[i] = 1;
+          v = ff_make(-INFINITY, 0.f);
+        } else {
+          float wh = (float)w;
+          v = ff_make(wh, (float)(w - (double)wh));
+        }
+      }
+    }
     vals[b] = make_float2(v.hi, v.lo);
   }
   __syncthreads();
-  // ---- phase B: |d| >= 2
-  for (int q = tid; q < qn; q += SW_NT) {
-    const int b = queue[q];
-    int i = 0;
-    while (b >= bstart[i + 1]) i++;
-    const int c = b - bstart[i];
-    const NodeRec nd = P.nodes[s_noff[i] + c];
-    const int32_t *A = P.alleles + s_alb[i];
-    const int d = A[c] - A[nd.down];
-    ff x = ff_mul(branch_len_ff(nd, P.tff + s_noff[i], c, ffc(trff[i])), ffc(uff[i]));
-    ff r;
-    float2 out;
-    if (sw_miller(abs(d), x, &r)) {
-      ff v = ff_add(ffc(vals[b]), r);
-      out = make_float2(v.hi, v.lo);
-    } else {  // rare: the reference's FP64 arithmetic
-      const ReqDev &R = reqs[r0 + i];
-      const double *t64 = P.t64 + s_noff[i];
-      double t = (nd.up0 < 0) ? t64[c] * R.par : R.par * (t64[c] - t64[nd.up0]);
-      bool z = false;
-      double w = term_64(d, t * R.u, &z);
-      if (z) {
-        zero[i] = 1;
-        out = make_float2(-INFINITY, 0.f);
-      } else {
-        float wh = (float)w;
-        out = make_float2(wh, (float)(w - (double)wh));
-      }
-    }
-    vals[b] = out;
-  }
-  __syncthreads();
   // ---- phase C: per chain-locus sums, dlikeA write-back
-  const int lane = tid & 31;
   for (int w = tid >> 5; w < nit; w += SW_NT / 32) {
     const ReqDev &R = reqs[r0 + w];
     const ItemDev it = P.items[R.item];
@@ -485,7 +497,7 @@ int sw_init_tables()
 }
 
 // Chain-loci per CTA that make the batch one wave of resident CTAs (at most
-// MAXI, and few enough that the int16 branch queues index every branch).
+// MAXI, and few enough that a task entry's 16 bits index every branch).
 // The occupancy query is remembered per device and shared-memory size.
 template <int MAXI, int MINB>
 static int sw_balanced_per(int nreq, int nlb)
@@ -497,7 +509,7 @@ static int sw_balanced_per(int nreq, int nlb)
   const int cap = std::min(MAXI, 32767 / nlb);
   int per = std::max(1, std::min(cap, (nreq + 4 * nsm - 1) / (4 * nsm)));
   for (int round = 0; round < 3; round++) {
-    const long long sm = (long long)per * nlb * (sizeof(float2) + 2 * sizeof(int16_t));
+    const long long sm = (long long)per * nlb * (sizeof(float2) + 2 * sizeof(int32_t));
     int nb = 0;
     const long long m = memo.load(std::memory_order_relaxed);
     if (m >= 0 && (m >> 40) == dev && ((m >> 8) & 0xffffffffLL) == sm) {
@@ -526,7 +538,7 @@ static void sw_fast_launch(const Pools &P, const ReqDev *reqs, int nreq, int max
   if (per <= 0) per = sw_balanced_per<MAXI, MINB>(nreq, nlb);
   per = std::max(1, std::min(per, std::min(MAXI, 32767 / nlb)));
   const int maxb = per * nlb;
-  const size_t sm = (size_t)maxb * (sizeof(float2) + 2 * sizeof(int16_t));
+  const size_t sm = (size_t)maxb * (sizeof(float2) + 2 * sizeof(int32_t));
   if (sm > 48 * 1024)
     cudaFuncSetAttribute(k_sw_fast<MAXI, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k_sw_fast<MAXI, MINB><<<(nreq + per - 1) / per, SW_NT, sm, st>>>(P, reqs, nreq, per, result, status, maxb);

@@ -100,7 +100,11 @@ int ima_gpu_set_genealogies(ima_ctx *ctx, int npairs, const int32_t *ci, const i
  * packed per pair as in ima_gpu_set_genealogies, length (may be NULL: the
  * sum of branch lengths) per pair.  Each pair must already hold a genealogy
  * (IMA_ERR_STATE).  Only the FP64 times travel: the device makes the
- * float-float copy. */
+ * float-float copy.  Pairs that are consecutive chain-loci in order (chain
+ * major, locus minor, as a batch of whole chains lists them) go to the
+ * device in one copy straight from the caller's buffers, with the lengths
+ * summed there; other lists are staged and copied with the next
+ * evaluation.  The buffers may be reused when the call returns. */
 int ima_gpu_set_times(ima_ctx *ctx, int npairs, const int32_t *ci, const int32_t *li, const double *time,
                       const double *length);
 /* Base frequencies of an HKY chain-locus (C[ci]->G[li].pi). */

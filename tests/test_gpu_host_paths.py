@@ -65,16 +65,28 @@ def test_set_times_matches_set_genealogies(kind):
     b.eval(ci, li, u, par)
     nl = np.array([2 * wl.tree(int(c), int(l)).n - 1 for c, l in zip(pci, pli)])
     ends = np.cumsum(nl)
+    starts = ends - nl
     rng = np.random.default_rng(7)
-    for npairs in (len(pci), 5):
+    # every pair in item order (copies started while the host stages), the
+    # first five, every pair shuffled (staged, copied at the evaluation), and
+    # one pair of the first kind followed by a full upload of another
+    for case in ("all", "five", "shuffled", "mixed"):
         f = np.repeat(rng.uniform(0.9, 1.1, size=len(nl)), nl)   # one factor per genealogy keeps the order
         scaled = np.where(tm > 0, tm * f, tm)
-        sel = slice(0, int(ends[npairs - 1]))
-        a.set_times(pci[:npairs], pli[:npairs], scaled[sel])
-        b.set_genealogies(pci[:npairs], pli[:npairs], up0[sel], up1[sel], down[sel], scaled[sel])
+        order = {"all": np.arange(len(pci)), "five": np.arange(5),
+                 "shuffled": rng.permutation(len(pci)), "mixed": np.arange(len(pci))}[case]
+        idx = np.concatenate([np.arange(starts[k], ends[k]) for k in order])
+        a.set_times(pci[order], pli[order], scaled[idx])
+        b.set_genealogies(pci[order], pli[order], up0[idx], up1[idx], down[idx], scaled[idx])
+        if case == "mixed":
+            k = len(pci) // 2
+            g = wl.tree(int(pci[k]), int(pli[k])).copy()
+            g.time = np.where(g.time > 0, g.time * 1.05, g.time)
+            a.set_genealogy(int(pci[k]), int(pli[k]), g)
+            b.set_genealogy(int(pci[k]), int(pli[k]), g)
         ra, sa = a.eval(ci, li, u, par)
         rb, sb = b.eval(ci, li, u, par)
-        assert np.array_equal(ra, rb) and np.array_equal(sa, sb)
+        assert np.array_equal(ra, rb) and np.array_equal(sa, sb), case
     fresh = _hky_ctx(wl)
     with pytest.raises(api.ImaError):
         fresh.set_times([0], [0], tm[:nl[0]])
