@@ -257,7 +257,10 @@ def cpu_rate(packs, seconds, threads):
     return n / t, n, t
 
 
-def cpu_baseline(wl, seconds, limit=4096):
+CPU_SAMPLE = 8192  # chain-loci per batched oracle call, in this line and in the reference arm
+
+
+def cpu_baseline(wl, seconds, limit=CPU_SAMPLE):
     cores = os.cpu_count() or 1
     packs = oracle_packs(wl, limit)
     v, n, t = cpu_rate(packs, seconds, cores)
@@ -1189,7 +1192,7 @@ def run_reference(args):
         return
 
     def lik_arm(wl, k_steps, step_seconds):
-        packs = oracle_packs(wl, 8192)
+        packs = oracle_packs(wl, CPU_SAMPLE)
         times, done = [], 0
         for s in range(args.warmup + k_steps):
             v, n, t = cpu_rate(packs, step_seconds, cores)

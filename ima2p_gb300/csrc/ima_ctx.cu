@@ -894,21 +894,42 @@ __global__ void k_split_times(const double *t64, float2 *tff, size_t n)
   tff[i] = make_float2(hi, (float)(t - (double)hi));
 }
 
-// Tree lengths of items lo .. lo + n - 1, one thread per item summing its
-// branches in node order: the host's sum, bit for bit.
-__global__ void k_item_lengths(const ItemDev *items, const NodeRec *nodes, const double *t64, double *len, int lo, int n)
+// One warp per item of lo .. lo + n - 1: the float-float copy of every node
+// time, and the tree length, its branch terms added in node order (the
+// host's sum, bit for bit: lane k's term is broadcast in turn).
+__global__ void k_split_lengths(const ItemDev *items, const NodeRec *nodes, const double *t64, float2 *tff,
+                                double *len, int lo, int n)
 {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const ItemDev it = items[lo + k];
+  const int w = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (w >= n) return;  // whole warps
+  const ItemDev it = items[lo + w];
+  const int nl = 2 * it.n - 1;
   const NodeRec *r = nodes + it.node_off;
   const double *t = t64 + it.node_off;
+  float2 *f = tff + it.node_off;
   double L = 0.0;
-  for (int j = 0; j < 2 * it.n - 1; j++) {
-    const NodeRec nd = r[j];
-    if (nd.down >= 0) L += (nd.up0 < 0) ? t[j] : t[j] - t[nd.up0];
+  for (int j0 = 0; j0 < nl; j0 += 32) {
+    const int j = j0 + lane;
+    double term = 0.0;
+    bool has = false;
+    if (j < nl) {
+      const double tj = t[j];
+      const float hi = (float)tj;
+      f[j] = make_float2(hi, (float)(tj - (double)hi));
+      const NodeRec nd = r[j];
+      if (nd.down >= 0) {
+        has = true;
+        term = (nd.up0 < 0) ? tj : tj - t[nd.up0];
+      }
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, has);
+    const int cnt = min(32, nl - j0);
+    for (int k = 0; k < cnt; k++) {
+      const double v = __shfl_sync(0xffffffffu, term, k);
+      if ((mask >> k) & 1u) L += v;
+    }
   }
-  len[lo + k] = L;
+  if (lane == 0) len[lo + w] = L;
 }
 
 static void split_times(ima_ctx *c, size_t n0, size_t n1)
@@ -965,7 +986,7 @@ extern "C" int ima_gpu_set_times(ima_ctx *c, int n, const int32_t *ci, const int
     // device layout of the run, so they go to the device in one copy (from
     // pageable memory: the call returns once the buffer has been read), the
     // device makes their float-float form and, when no lengths are given,
-    // the lengths (one thread per item, the host's order of additions).
+    // the lengths (in the host's order of additions).
     // The device then holds the newer values; the mirror is refreshed before
     // the host next writes it.  Uploads still pending from the mirror go
     // first.
@@ -974,12 +995,14 @@ extern "C" int ima_gpu_set_times(ima_ctx *c, int n, const int32_t *ci, const int
     int r = c->cuda(cudaMemcpyAsync(c->d_t64 + n0, time, (n1 - n0) * sizeof(double), cudaMemcpyHostToDevice, c->st),
                     "times upload");
     if (r) return r;
-    split_times(c, n0, n1);
-    if (length)
+    if (length) {
+      split_times(c, n0, n1);
       r = c->cuda(cudaMemcpyAsync(c->d_len + lo, length, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->st),
                   "length");
-    else
-      k_item_lengths<<<(n + 127) / 128, 128, 0, c->st>>>(c->d_items, c->d_nodes, c->d_t64, c->d_len, lo, n);
+    } else {
+      k_split_lengths<<<(unsigned)(((size_t)n * 32 + 127) / 128), 128, 0, c->st>>>(c->d_items, c->d_nodes, c->d_t64,
+                                                                               c->d_tff, c->d_len, lo, n);
+    }
     c->dev_lo = std::min(c->dev_lo, lo);
     c->dev_hi = std::max(c->dev_hi, hi);
     return r ? r : c->cuda(cudaGetLastError(), "times upload");

@@ -21,7 +21,7 @@
 // Miller value the reference would take below 1e-300) take the FP64 path.
 // FP64 form: the reference algorithm in FP64, one thread per branch.
 #include <algorithm>
-#include <atomic>
+#include <mutex>
 #include <cfloat>
 
 #include "ff.cuh"
@@ -498,35 +498,44 @@ int sw_init_tables()
 
 // Chain-loci per CTA that make the batch one wave of resident CTAs (at most
 // MAXI, and few enough that a task entry's 16 bits index every branch).
-// The occupancy query is remembered per device and shared-memory size.
+// The answer is remembered for the last few (device, batch size, branch
+// count): a batch replayed step after step asks the occupancy calculator
+// once.
 template <int MAXI, int MINB>
 static int sw_balanced_per(int nreq, int nlb)
 {
-  static std::atomic<long long> memo{-1};  // device << 40 | smem bytes << 8 | CTAs per SM
-  int dev = 0, nsm = 152;
+  struct Memo {
+    int dev = -1, nreq = 0, nlb = 0, per = 0;
+  };
+  static std::mutex mu;
+  static Memo memo[8];  // the last few shapes, replaced in turn
+  static int turn = 0;
+  int dev = 0;
   cudaGetDevice(&dev);
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    for (const Memo &m : memo)
+      if (m.dev == dev && m.nreq == nreq && m.nlb == nlb) return m.per;
+  }
+  int nsm = 152;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const int cap = std::min(MAXI, 32767 / nlb);
   int per = std::max(1, std::min(cap, (nreq + 4 * nsm - 1) / (4 * nsm)));
   for (int round = 0; round < 3; round++) {
-    const long long sm = (long long)per * nlb * (sizeof(float2) + 2 * sizeof(int32_t));
+    const size_t sm = (size_t)per * nlb * (sizeof(float2) + 2 * sizeof(int32_t));
+    if (sm > 48 * 1024)
+      cudaFuncSetAttribute(k_sw_fast<MAXI, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     int nb = 0;
-    const long long m = memo.load(std::memory_order_relaxed);
-    if (m >= 0 && (m >> 40) == dev && ((m >> 8) & 0xffffffffLL) == sm) {
-      nb = (int)(m & 0xff);
-    } else {
-      if (sm > 48 * 1024)
-        cudaFuncSetAttribute(k_sw_fast<MAXI, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_sw_fast<MAXI, MINB>, SW_NT, (size_t)sm) != cudaSuccess)
-        nb = 1;
-      nb = std::max(1, std::min(nb, 255));
-      memo.store(((long long)dev << 40) | (sm << 8) | nb, std::memory_order_relaxed);
-    }
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_sw_fast<MAXI, MINB>, SW_NT, sm) != cudaSuccess) nb = 1;
+    nb = std::max(1, nb);
     const long long slots = (long long)nsm * nb;
     const int want = std::max(1, std::min(cap, (int)((nreq + slots - 1) / slots)));
     if (want == per) break;
     per = want;
   }
+  std::lock_guard<std::mutex> lk(mu);
+  memo[turn] = Memo{dev, nreq, nlb, per};
+  turn = (turn + 1) % 8;
   return per;
 }
 
