@@ -440,45 +440,69 @@ def measure_lik(args, api, wl, steps, dist=None, device=0, hky_legs=False):
     pci, pli, up0, up1, down, tm = wl.packed()
     scaled = np.where(tm > 0, tm * (1.0 + 1e-6), tm)
     nodes = len(up0)
-    # FP64 time per node and a length per chain-locus; the request list
-    # repeats, so ima_gpu_eval keeps the staged one
-    h2d = nodes * 8 + units * 8
+    # FP64 time per node in, a result and a status per chain-locus out (the
+    # lengths are summed on the device; the request list repeats, so the
+    # staged one is kept)
+    h2d = nodes * 8
     d2h = units * (8 + 4)
-    e2e_t, set_t = [], []
+    assert np.array_equal(pci, ci) and np.array_equal(pli, li)
+    e2e_t = []
     for s in range(args.warmup + min(steps, 100)):
         tms = scaled if s % 2 else tm
         t0 = time.perf_counter()
-        ctx.set_times(pci, pli, tms)
-        tm1 = time.perf_counter()
-        ctx.eval(ci, li, u, par, precision=prec)
+        ctx.eval_times(ci, li, tms, u, par, precision=prec)
         t1 = time.perf_counter()
         if s >= args.warmup:
             e2e_t.append(t1 - t0)
-            set_t.append(tm1 - t0)
-    # where an e2e step goes: the host-to-device copy of the staged times
-    # (with the float-float split), and an evaluation with nothing to upload
-    fl_t, ev_t = [], []
+    # the same step as two calls (ima_gpu_set_times, ima_gpu_eval), and where
+    # its time goes: the upload, and an evaluation with nothing to upload
+    two_t, set_t, fl_t, ev_t = [], [], [], []
     for s in range(args.warmup + min(steps, 50)):
-        ctx.set_times(pci, pli, scaled if s % 2 else tm)
+        tms = scaled if s % 2 else tm
         t0 = time.perf_counter()
-        ctx.flush_genealogies()
-        ctx.synchronize()
+        ctx.set_times(ci, li, tms)
         t1 = time.perf_counter()
         ctx.eval(ci, li, u, par, precision=prec)
         t2 = time.perf_counter()
+        ctx.set_times(ci, li, tm if s % 2 else scaled)
+        t3 = time.perf_counter()
+        ctx.synchronize()
+        t4 = time.perf_counter()
+        ctx.eval(ci, li, u, par, precision=prec)
+        t5 = time.perf_counter()
         if s >= args.warmup:
-            fl_t.append(t1 - t0)
-            ev_t.append(t2 - t1)
+            two_t.append(t2 - t0)
+            set_t.append(t1 - t0)
+            fl_t.append(t4 - t3)
+            ev_t.append(t5 - t4)
+    # device time of the step's kernels (events around each launch, in a
+    # loop of its own: recording them costs host time)
+    ctx.set_profiling(True)
+    kk = [k for k in (api.K_TIMES, api.K_IS, api.K_HKY_FAST, api.K_SW_FAST)]
+    k0 = {k: ctx.kernel_stats(k) for k in kk}
+    nprof = 20
+    for s in range(nprof):
+        ctx.eval_times(ci, li, scaled if s % 2 else tm, u, par, precision=prec)
+    kms = {k: (ctx.kernel_stats(k)[1] - k0[k][1]) / nprof for k in kk}
+    ctx.set_profiling(False)
     e2e = units * world / statistics.median(e2e_t)
     out["e2e"] = {"value": round(e2e, 1), "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
                   "d2h_bytes_per_step": int(d2h),
                   "ms_per_step": round(1e3 * statistics.median(e2e_t), 4),
-                  "ms_set_times": round(1e3 * statistics.median(set_t), 4),
-                  "ms_upload": round(1e3 * statistics.median(fl_t), 4),
-                  "ms_eval_resident": round(1e3 * statistics.median(ev_t), 4),
-                  "note": "every step re-times every genealogy (ima_gpu_set_times: FP64 times staged, "
-                          "lengths summed on the host threads), then ima_gpu_eval copies the times, makes "
-                          "their float-float form on the device, runs and copies results back"}
+                  "api": "ima_gpu_eval_times",
+                  "ms_upload_kernels": round(kms[api.K_TIMES], 4),
+                  "ms_evaluation_kernels": round(sum(kms[k] for k in kk[1:]), 4),
+                  "note": "every step re-times every genealogy (topology kept, as changet_RY1 moves) and "
+                          "evaluates every chain-locus in one call: the device reads the step's FP64 times "
+                          "from the caller's buffer, makes their float-float form and the tree lengths, "
+                          "evaluates, and the results come back",
+                  "two_calls": {"value": round(units * world / statistics.median(two_t), 1),
+                                "ms_per_step": round(1e3 * statistics.median(two_t), 4),
+                                "ms_set_times": round(1e3 * statistics.median(set_t), 4),
+                                "ms_upload_wait": round(1e3 * statistics.median(fl_t), 4),
+                                "ms_eval_resident": round(1e3 * statistics.median(ev_t), 4),
+                                "note": "ima_gpu_set_times (one copy from the caller's buffer) then "
+                                        "ima_gpu_eval"}}
     ctx.set_genealogies(pci, pli, up0, up1, down, tm)
 
     if hky_legs:

@@ -24,7 +24,7 @@ PREC_FAST, PREC_FP64, PREC_FP32 = 0, 1, 2
 EVAL_OK, EVAL_IS_REJECT, EVAL_IS_FAIL, EVAL_SW_ZERO = 0, 1, 2, 3
 SURF_FAST, SURF_FP64, SURF_COMPAT, SURF_TC = 0, 1, 2, 3
 K_IS, K_IS_SUMLOGK, K_HKY_FAST, K_HKY_FP64, K_SW_FAST, K_SW_FP64, K_SWAP, K_SURF_FAST, \
-    K_SURF_FP64, K_SURF_COMPAT, K_SURF_TC, K_MARGIN, K_TREEWEIGHT, K_TREE_PROB, K_POPMIG, K_HKY_FP32 = range(16)
+    K_SURF_FP64, K_SURF_COMPAT, K_SURF_TC, K_MARGIN, K_TREEWEIGHT, K_TREE_PROB, K_POPMIG, K_HKY_FP32, K_TIMES = range(17)
 KERNEL_NAMES = ["is", "is_sumlogk", "hky_fast", "hky_fp64", "sw_fast", "sw_fp64", "swap",
                 "surf_fast", "surf_fp64", "surf_compat", "surf_tc", "margin", "treeweight", "tree_prob",
                 "popmig", "hky_fp32"]
@@ -42,7 +42,7 @@ EXPORTS = [
     "ima_gpu_batch_destroy", "ima_gpu_flush_genealogies", "ima_gpu_setheat", "ima_gpu_get_betas",
     "ima_gpu_set_betas", "ima_gpu_set_pdg", "ima_gpu_get_pdg", "ima_gpu_set_probg",
     "ima_gpu_swapchains", "ima_gpu_swapchains_cb", "ima_gpu_set_allbetas", "ima_gpu_surface_retaken",
-    "ima_gpu_batch_sweep", "ima_gpu_set_times", "ima_gpu_get_swapcounts", "ima_gpu_surface_load",
+    "ima_gpu_batch_sweep", "ima_gpu_set_times", "ima_gpu_eval_times", "ima_gpu_get_swapcounts", "ima_gpu_surface_load",
     "ima_gpu_surface_eval", "ima_gpu_jointp", "ima_gpu_surface_fp64_noalloc", "ima_gpu_tc_selftest",
     "ima_gpu_surface_info", "ima_mt19937_seed", "ima_mt19937_uniform", "ima_gpu_modelloop",
     "ima_gpu_batch_autotune", "ima_gpu_batch_set_variants", "ima_gpu_margincalc", "ima_gpu_fillvec",
@@ -214,6 +214,7 @@ def _declare(L):
         "ima_gpu_surface_retaken": (I, [P, C.POINTER(I)]),
         "ima_gpu_batch_sweep": (I, [P, I, P, I, I, C.c_uint64, I]),
         "ima_gpu_set_times": (I, [P, I, P, P, P, P]),
+        "ima_gpu_eval_times": (I, [P, I, P, P, P, P, P, P, P, I, P, P]),
         "ima_gpu_tc_selftest": (I, [P, C.POINTER(I), C.POINTER(C.c_float)]),
         "ima_gpu_timer_begin": (I, [P]),
         "ima_gpu_timer_end": (I, [P, C.POINTER(C.c_float)]),
@@ -320,6 +321,18 @@ class Context:
         ci, li = _i32(ci), _i32(li)
         self._ck(self.lib.ima_gpu_set_times(self.h, len(ci), _ptr(ci), _ptr(li), _ptr(_f64(time)),
                                             _ptr(_f64(length))))
+
+    def eval_times(self, ci, li, time, u, kappa=None, ai=None, length=None, precision=PREC_FAST):
+        """set_times then eval of the same pairs in one call (full evaluations)."""
+        ci, li, u = _i32(ci), _i32(li), _f64(u)
+        n = len(ci)
+        kappa, ai = _f64(kappa), _i32(ai)
+        time, length = _f64(time), _f64(length)
+        res = np.zeros(n)
+        st = np.zeros(n, np.int32)
+        self._ck(self.lib.ima_gpu_eval_times(self.h, n, _ptr(ci), _ptr(li), _ptr(time), _ptr(length), _ptr(u),
+                                             _ptr(kappa), _ptr(ai), int(precision), _ptr(res), _ptr(st)))
+        return res, st
 
     def set_pi(self, ci, li, pi):
         self._ck(self.lib.ima_gpu_set_pi(self.h, int(ci), int(li), _ptr(_f64(pi))))

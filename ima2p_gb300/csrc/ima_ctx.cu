@@ -183,6 +183,7 @@ T *host_alloc(size_t count)
 struct ima_ctx {
   int device = 0;
   int nsm = 152;  // SMs of the device
+  int pageable_access = 0;  // the device reads pageable host memory (cudaDevAttrPageableMemoryAccess)
   cudaStream_t st = nullptr;
   std::string err;
   size_t dev_bytes = 0;
@@ -289,6 +290,10 @@ struct ima_ctx {
   void *d_rsel = nullptr;
   size_t rsel_cap = 0;
   int dev_lo = INT32_MAX, dev_hi = -1;  // items whose device times/lengths are newer than the mirror
+  // items whose tree lengths are still to be summed from their device times
+  // (re-timings without lengths): done when a reader needs them
+  int lpend_lo = INT32_MAX, lpend_hi = -1;
+  double *d_lterm = nullptr;  // per node: its branch term, for those sums
   float *tp_rows = nullptr;  // gsampinf rows of the last ima_gpu_tree_prob
   int tp_ngroups = 0, tp_rowlen = 0;
   size_t s_cap = 0;          // surface row capacity (rows appended on the device)
@@ -430,6 +435,7 @@ extern "C" int ima_gpu_create(int device, ima_ctx **out)
   cudaEventCreate(&c->t0);
   cudaEventCreate(&c->t1);
   cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
+  cudaDeviceGetAttribute(&c->pageable_access, cudaDevAttrPageableMemoryAccess, device);
   if (sw_init_tables() != 0 || hky_init_tables() != 0) {
     delete c;
     return IMA_ERR_CUDA;
@@ -466,7 +472,7 @@ extern "C" void ima_gpu_destroy(ima_ctx *c)
                   c->d_mscratch, c->d_tw, c->d_logfact, c->d_twerr, c->d_twin, c->d_twout, c->d_tpbuf,
                   c->d_pop, c->d_moff, c->d_inode_off, c->d_gl, c->d_gt, c->d_moff_start, c->d_bcnt, c->d_bicnt,
                   c->d_mig_p, c->d_rsamp, c->d_mbase, c->d_mig_t, c->d_tvr, c->d_len_hold, c->d_rhlog,
-                  c->d_rh2, c->d_rsel, c->d_is_site, c->d_is_valid};
+                  c->d_rh2, c->d_rsel, c->d_is_site, c->d_is_valid, c->d_lterm};
   for (void *p : devs)
     if (p) cudaFree(p);
   void *hosts[] = {c->h_nodes, c->h_t64, c->h_sched, c->h_nlev, c->h_len, c->h_pi, c->h_al};
@@ -665,10 +671,12 @@ extern "C" int ima_gpu_set_chains(ima_ctx *c, int nruns, int chains_per_run)
 // upload never carries stale values.
 // Before the host writes its mirror: values newer on the device (moved or
 // uploaded there) come back into it.
+static int ensure_lengths(ima_ctx *c);
+
 static int sync_mirror(ima_ctx *c)
 {
-  int r = IMA_OK;
-  if (c->dev_hi < 0) return IMA_OK;
+  int r = ensure_lengths(c);
+  if (r || c->dev_hi < 0) return r;
   const ItemDev &a = c->items[c->dev_lo], &b = c->items[c->dev_hi];
   const size_t n0 = a.node_off, n1 = (size_t)b.node_off + 2 * b.n - 1;
   r = c->cuda(cudaMemcpyAsync(c->h_t64 + n0, c->d_t64 + n0, (n1 - n0) * sizeof(double), cudaMemcpyDeviceToHost, c->st), "mirror");
@@ -894,19 +902,64 @@ __global__ void k_split_times(const double *t64, float2 *tff, size_t n)
   tff[i] = make_float2(hi, (float)(t - (double)hi));
 }
 
-// One warp per item of lo .. lo + n - 1: the float-float copy of every node
-// time, and the tree length, its branch terms added in node order (the
-// host's sum, bit for bit: lane k's term is broadcast in turn).
-__global__ void k_split_lengths(const ItemDev *items, const NodeRec *nodes, const double *t64, float2 *tff,
-                                double *len, int lo, int n)
+// Tree lengths of items lo .. lo + n - 1 in two passes.  (1) A warp per
+// item forms every node's branch term (coalesced reads, the daughter's time
+// from L1/L2) into term[]; (2) a thread per item adds its terms in node
+// order -- the host's sum, bit for bit -- with independent loads and one
+// FP64 add per node on one lane each (GB300 issues FP64 at 1/64 of the FP32
+// rate: a warp-wide sequential sum would spend 32 lanes per add).
+__global__ void k_branch_terms(const ItemDev *items, const NodeRec *nodes, const double *t64, double *term, int lo,
+                               int n)
+{
+  const int w = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (w >= n) return;
+  const ItemDev it = items[lo + w];
+  const int nl = 2 * it.n - 1;
+  const NodeRec *r = nodes + it.node_off;
+  const double *t = t64 + it.node_off;
+  double *out = term + it.node_off;
+  for (int j = lane; j < nl; j += 32) {
+    const NodeRec nd = r[j];
+    out[j] = nd.down < 0 ? 0.0 : (nd.up0 < 0 ? t[j] : t[j] - t[nd.up0]);
+  }
+}
+
+__global__ void k_sum_terms(const ItemDev *items, const NodeRec *nodes, const double *term, double *len, int lo,
+                            int n)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const ItemDev it = items[lo + k];
+  const NodeRec *r = nodes + it.node_off;
+  const double *v = term + it.node_off;
+  const int nl = 2 * it.n - 1;
+  double L = 0.0;
+#pragma unroll 8
+  for (int j = 0; j < nl; j++)
+    if (r[j].down >= 0) L += v[j];
+  len[lo + k] = L;
+}
+
+// A short run in one kernel, a warp per item: the times read from src
+// (indexed by node_off - src0: the caller's packed run where the device can
+// read it, or the device times themselves when src == t64), copied into t64,
+// their float-float form, and the tree length -- given (src_len) or its
+// branch terms added in node order, broadcast lane by lane (the host's sum,
+// bit for bit; every lane repeats the FP64 adds, which only a short run can
+// afford on GB300's FP64 pipe).
+constexpr long long SHORT_RUN_NODES = 1 << 16;
+__global__ void k_times_short(const ItemDev *items, const NodeRec *nodes, const double *src, size_t src0,
+                              const double *src_len, double *t64, float2 *tff, double *len, int lo, int n)
 {
   const int w = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
   if (w >= n) return;  // whole warps
   const ItemDev it = items[lo + w];
   const int nl = 2 * it.n - 1;
   const NodeRec *r = nodes + it.node_off;
-  const double *t = t64 + it.node_off;
+  const double *t = src + (it.node_off - src0);
+  double *t_out = t64 + it.node_off;
   float2 *f = tff + it.node_off;
+  const bool copy = (src != t64);
   double L = 0.0;
   for (int j0 = 0; j0 < nl; j0 += 32) {
     const int j = j0 + lane;
@@ -914,14 +967,16 @@ __global__ void k_split_lengths(const ItemDev *items, const NodeRec *nodes, cons
     bool has = false;
     if (j < nl) {
       const double tj = t[j];
+      if (copy) t_out[j] = tj;
       const float hi = (float)tj;
       f[j] = make_float2(hi, (float)(tj - (double)hi));
       const NodeRec nd = r[j];
-      if (nd.down >= 0) {
+      if (!src_len && nd.down >= 0) {
         has = true;
         term = (nd.up0 < 0) ? tj : tj - t[nd.up0];
       }
     }
+    if (src_len) continue;  // uniform across the warp
     const unsigned mask = __ballot_sync(0xffffffffu, has);
     const int cnt = min(32, nl - j0);
     for (int k = 0; k < cnt; k++) {
@@ -929,7 +984,58 @@ __global__ void k_split_lengths(const ItemDev *items, const NodeRec *nodes, cons
       if ((mask >> k) & 1u) L += v;
     }
   }
-  if (lane == 0) len[lo + w] = L;
+  if (lane == 0) len[lo + w] = src_len ? src_len[w] : L;
+}
+
+// The caller's packed times of a run, read where they lie (host memory the
+// device can access), into the device times and their float-float copy:
+// one coalesced pass, grid-stride.
+__global__ void k_pull_times(const double *src, double *t64, float2 *tff, size_t n)
+{
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double t = src[i];
+    t64[i] = t;
+    const float hi = (float)t;
+    tff[i] = make_float2(hi, (float)(t - (double)hi));
+  }
+}
+
+__global__ void k_pull_lengths(const double *src, double *len, int n)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) len[i] = src[i];
+}
+
+// The lengths still pending, summed now (before a reader: the infinite-sites
+// likelihood, the band and the genealogy weights, the mirror).
+static int ensure_lengths(ima_ctx *c)
+{
+  if (c->lpend_hi < 0) return IMA_OK;
+  const int lo = c->lpend_lo, n = c->lpend_hi - lo + 1;
+  c->lpend_lo = INT32_MAX;
+  c->lpend_hi = -1;
+  if (!c->d_lterm) {
+    c->d_lterm = dev_alloc<double>(c->nnodes, c->dev_bytes, c->st);
+    if (!c->d_lterm) return c->fail(IMA_ERR_NOMEM, "branch-length scratch");
+  }
+  c->launch(IMA_K_TIMES, 0.0, [&] {
+    k_branch_terms<<<(unsigned)(((size_t)n * 32 + 127) / 128), 128, 0, c->st>>>(c->d_items, c->d_nodes, c->d_t64,
+                                                                               c->d_lterm, lo, n);
+    k_sum_terms<<<(n + 127) / 128, 128, 0, c->st>>>(c->d_items, c->d_nodes, c->d_lterm, c->d_len, lo, n);
+  });
+  return c->cuda(cudaGetLastError(), "lengths");
+}
+
+// Items lo .. hi get lengths summed later; a range apart from the pending
+// one is summed first (the pending range stays one interval, and items
+// between the two may hold lengths a caller gave).
+static int pend_lengths(ima_ctx *c, int lo, int hi)
+{
+  if (c->lpend_hi >= 0 && (lo > c->lpend_hi + 1 || hi < c->lpend_lo - 1))
+    if (int r = ensure_lengths(c)) return r;
+  c->lpend_lo = std::min(c->lpend_lo, lo);
+  c->lpend_hi = std::max(c->lpend_hi, hi);
+  return IMA_OK;
 }
 
 static void split_times(ima_ctx *c, size_t n0, size_t n1)
@@ -960,9 +1066,14 @@ static void set_times_one(ima_ctx *c, int item, const double *time, double lengt
   c->h_len[item] = L;
 }
 
-extern "C" int ima_gpu_set_times(ima_ctx *c, int n, const int32_t *ci, const int32_t *li, const double *time,
-                                 const double *length)
+// New times of genealogies whose topology is kept.  in_place: a contiguous
+// run may be read by the device from the caller's buffers while the stream
+// runs (the caller synchronises the stream before returning); *read_in_place
+// tells whether that happened.
+static int upload_times(ima_ctx *c, int n, const int32_t *ci, const int32_t *li, const double *time,
+                        const double *length, bool in_place, bool *read_in_place)
 {
+  if (read_in_place) *read_in_place = false;
   if (!c || n < 0 || (n > 0 && (!ci || !li || !time))) return IMA_ERR_ARG;
   if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
   if (n == 0) return IMA_OK;
@@ -992,16 +1103,58 @@ extern "C" int ima_gpu_set_times(ima_ctx *c, int n, const int32_t *ci, const int
     // first.
     if (int r = flush(c)) return r;
     const size_t n0 = c->items[lo].node_off, n1 = n0 + offp[n];
+    if (in_place && c->pageable_access && (long long)(n1 - n0) <= SHORT_RUN_NODES) {
+      // a short run: one kernel reads it in place (times, float-float form,
+      // lengths), nothing left pending
+      if (int r = ensure_lengths(c)) return r;
+      c->launch(IMA_K_TIMES, (double)(n1 - n0) * 16.0, [&] {
+        k_times_short<<<(unsigned)(((size_t)n * 32 + 127) / 128), 128, 0, c->st>>>(
+            c->d_items, c->d_nodes, time, n0, length, c->d_t64, c->d_tff, c->d_len, lo, n);
+      });
+      if (read_in_place) *read_in_place = true;
+      c->dev_lo = std::min(c->dev_lo, lo);
+      c->dev_hi = std::max(c->dev_hi, hi);
+      return c->cuda(cudaGetLastError(), "times upload");
+    }
+    if (in_place && c->pageable_access) {
+      // the device reads the run where it lies (times and their float-float
+      // form in one coalesced pass), no staging copy; the lengths are read
+      // too, or summed from the device times
+      if (length) {
+        if (int r = ensure_lengths(c)) return r;  // pending ones inside the run would overwrite these
+      } else if (int r = pend_lengths(c, lo, hi)) {
+        return r;
+      }
+      c->launch(IMA_K_TIMES, (double)(n1 - n0) * 16.0, [&] {
+        const unsigned g = (unsigned)std::min<size_t>(4 * (size_t)c->nsm, (n1 - n0 + 255) / 256);
+        k_pull_times<<<g, 256, 0, c->st>>>(time, c->d_t64 + n0, c->d_tff + n0, n1 - n0);
+        if (length) k_pull_lengths<<<(n + 255) / 256, 256, 0, c->st>>>(length, c->d_len + lo, n);
+      });
+      if (read_in_place) *read_in_place = true;
+      c->dev_lo = std::min(c->dev_lo, lo);
+      c->dev_hi = std::max(c->dev_hi, hi);
+      return c->cuda(cudaGetLastError(), "times upload");
+    }
     int r = c->cuda(cudaMemcpyAsync(c->d_t64 + n0, time, (n1 - n0) * sizeof(double), cudaMemcpyHostToDevice, c->st),
                     "times upload");
     if (r) return r;
     if (length) {
-      split_times(c, n0, n1);
-      r = c->cuda(cudaMemcpyAsync(c->d_len + lo, length, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->st),
-                  "length");
+      r = ensure_lengths(c);  // pending ones inside the run would overwrite these
+      r = r ? r : c->cuda(cudaMemcpyAsync(c->d_len + lo, length, (size_t)n * sizeof(double), cudaMemcpyHostToDevice,
+                                          c->st), "length");
+    }
+    if (r) return r;
+    if ((long long)(n1 - n0) <= SHORT_RUN_NODES) {  // one kernel, nothing left pending
+      r = ensure_lengths(c);
+      if (!r)
+        c->launch(IMA_K_TIMES, (double)(n1 - n0) * 16.0, [&] {
+          k_times_short<<<(unsigned)(((size_t)n * 32 + 127) / 128), 128, 0, c->st>>>(
+              c->d_items, c->d_nodes, c->d_t64, 0, length ? c->d_len + lo : nullptr, c->d_t64, c->d_tff, c->d_len,
+              lo, n);
+        });
     } else {
-      k_split_lengths<<<(unsigned)(((size_t)n * 32 + 127) / 128), 128, 0, c->st>>>(c->d_items, c->d_nodes, c->d_t64,
-                                                                               c->d_tff, c->d_len, lo, n);
+      c->launch(IMA_K_TIMES, (double)(n1 - n0) * 16.0, [&] { split_times(c, n0, n1); });
+      if (!length) r = pend_lengths(c, lo, hi);
     }
     c->dev_lo = std::min(c->dev_lo, lo);
     c->dev_hi = std::max(c->dev_hi, hi);
@@ -1037,6 +1190,12 @@ extern "C" int ima_gpu_set_times(ima_ctx *c, int n, const int32_t *ci, const int
   c->tdirty_lo = std::min(c->tdirty_lo, lo);
   c->tdirty_hi = std::max(c->tdirty_hi, hi);
   return IMA_OK;
+}
+
+extern "C" int ima_gpu_set_times(ima_ctx *c, int n, const int32_t *ci, const int32_t *li, const double *time,
+                                 const double *length)
+{
+  return upload_times(c, n, ci, li, time, length, false, nullptr);
 }
 
 extern "C" int ima_gpu_set_pi(ima_ctx *c, int ci, int li, const double *pi4)
@@ -1426,10 +1585,31 @@ extern "C" int ima_gpu_eval(ima_ctx *c, int n, const int32_t *ci, const int32_t 
     }
   }
   r = r ? r : flush(c);
+  r = r ? r : (b.nis ? ensure_lengths(c) : IMA_OK);  // the infinite-sites likelihood reads them
   r = r ? r : init_sumlogk(c, b);
   if (!r) enqueue(c, b);
   r = r ? r : c->cuda(cudaGetLastError(), "launch");
   r = r ? r : fetch(c, b, result, status);
+  return r;
+}
+
+// New times of every pair (topologies kept), then their full evaluation:
+// the batched form of a re-timing move followed by the likelihoods of the
+// moved genealogies.  Where the device reads the caller's memory in place,
+// the times go straight from the caller's buffer into the evaluation's
+// stream; the stream is synchronised before returning whatever happens.
+extern "C" int ima_gpu_eval_times(ima_ctx *c, int n, const int32_t *ci, const int32_t *li, const double *time,
+                                  const double *length, const double *u, const double *kappa, const int32_t *ai,
+                                  int precision, double *result, int32_t *status)
+{
+  if (!c) return IMA_ERR_ARG;
+  bool in_place = false;
+  int r = upload_times(c, n, ci, li, time, length, true, &in_place);
+  r = r ? r : ima_gpu_eval(c, n, ci, li, u, kappa, nullptr, ai, precision, result, status);
+  if (in_place) {
+    const int rs = c->cuda(cudaStreamSynchronize(c->st), "evaluation");
+    r = r ? r : rs;
+  }
   return r;
 }
 
@@ -1461,6 +1641,7 @@ extern "C" int ima_gpu_batch_run(ima_ctx *c, int batch, int use_graph)
   if (!c || batch < 0 || batch >= (int)c->batches.size() || !c->batches[batch].live) return IMA_ERR_ARG;
   Batch &b = c->batches[batch];
   int r = flush(c);
+  r = r ? r : (b.nis ? ensure_lengths(c) : IMA_OK);  // the infinite-sites likelihood reads them
   r = r ? r : init_sumlogk(c, b);
   if (r) return r;
   if (!use_graph || c->profiling) {
@@ -1495,6 +1676,7 @@ extern "C" int ima_gpu_batch_autotune(ima_ctx *c, int batch, int reps, int *hky_
   if (!c || batch < 0 || batch >= (int)c->batches.size() || !c->batches[batch].live) return IMA_ERR_ARG;
   Batch &b = c->batches[batch];
   int r = flush(c);
+  r = r ? r : (b.nis ? ensure_lengths(c) : IMA_OK);  // the infinite-sites likelihood reads them
   r = r ? r : init_sumlogk(c, b);
   if (r) return r;
   if (reps < 1) reps = 1;
@@ -1613,6 +1795,7 @@ extern "C" int ima_gpu_batch_sweep(ima_ctx *c, int batch, const uint8_t *accept,
   if (swaptries < 0) return c->fail(IMA_ERR_ARG, "swaptries must be >= 0");
   Batch &b = c->batches[batch];
   int r = flush(c);
+  r = r ? r : (b.nis ? ensure_lengths(c) : IMA_OK);  // the infinite-sites likelihood reads them
   r = r ? r : init_sumlogk(c, b);
   if (r) return r;
   if (!b.d_items) {
@@ -3331,6 +3514,7 @@ static int chains_ready(ima_ctx *c, int nch, const int32_t *chains)
   if (!c->d_pop || !c->locus_pops) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_labels and ima_gpu_set_locus_pops first");
   cudaSetDevice(c->device);
   if (int r = flush(c)) return r;
+  if (int r = ensure_lengths(c)) return r;
   for (int k = 0; k < nch; k++) {
     if (chains[k] < 0 || chains[k] >= c->nchains) return c->fail(IMA_ERR_ARG, "chain %d out of range", chains[k]);
     for (int l = 0; l < k; l++)
@@ -3943,6 +4127,8 @@ extern "C" int ima_gpu_checkpoint_read(ima_ctx *c, const char *path, ima_mt19937
   c->tw_valid.clear();
   c->dev_lo = INT32_MAX;  // the file is authoritative now
   c->dev_hi = -1;
+  c->lpend_lo = INT32_MAX;
+  c->lpend_hi = -1;
   c->dirty_lo = 0;        // upload everything with the next flush
   c->dirty_hi = (int)ni - 1;
   c->tdirty_lo = INT32_MAX;

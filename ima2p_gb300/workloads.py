@@ -105,9 +105,8 @@ def _loci_u(rng, nloci):
     return u / np.exp(np.mean(np.log(u)))  # product of the scalars = 1
 
 
-def make_is(seed=1001):
+def make_is(seed=1001, nloci=5, nch=4):
     rng = np.random.default_rng(seed)
-    nloci, nch = 5, 4
     loci, trees = [], {}
     u = np.tile(_loci_u(rng, nloci), (nch, 1))
     for li in range(nloci):
@@ -115,7 +114,7 @@ def make_is(seed=1001):
         loci.append(("is", synth.is_data(rng, g0, u[0, li] * 1.0, min_sites=3)))
         for ci in range(nch):
             trees[(ci, li)] = g0 if ci == 0 else synth.jitter_times(rng, g0, 0.1)
-    return Workload("is", "config1-is: 2 pops, 5 IS loci x (10+10) copies, 500 bp, 4 chains",
+    return Workload("is", "config1-is: 2 pops, %d IS loci x (10+10) copies, 500 bp, %d chains" % (nloci, nch),
                     loci, 1, nch, trees, u, np.ones((nch, nloci)), {}, {})
 
 

@@ -107,6 +107,16 @@ int ima_gpu_set_genealogies(ima_ctx *ctx, int npairs, const int32_t *ci, const i
  * evaluation.  The buffers may be reused when the call returns. */
 int ima_gpu_set_times(ima_ctx *ctx, int npairs, const int32_t *ci, const int32_t *li, const double *time,
                       const double *length);
+/* ima_gpu_set_times for every pair, then ima_gpu_eval of the same pairs
+ * (full evaluations): a re-timing move of many chains (changet_RY1,
+ * update_t_RY.cpp:223-389, whose loop over loci calls the likelihood of each
+ * re-timed genealogy) in one call.  Where the device can read the caller's
+ * memory (cudaDevAttrPageableMemoryAccess), a contiguous run of pairs is
+ * read in place by the first kernel of the evaluation's stream.  The
+ * buffers may be reused when the call returns. */
+int ima_gpu_eval_times(ima_ctx *ctx, int npairs, const int32_t *ci, const int32_t *li, const double *time,
+                       const double *length, const double *u, const double *kappa, const int32_t *ai,
+                       int precision, double *result, int32_t *status);
 /* Base frequencies of an HKY chain-locus (C[ci]->G[li].pi). */
 int ima_gpu_set_pi(ima_ctx *ctx, int ci, int li, const double *pi4);
 /* Allele states of linked marker ai on every node (gtree[i].A[ai]). */
@@ -623,7 +633,8 @@ int ima_gpu_kernel_stats(ima_ctx *ctx, int kind, long long *launches, double *ms
 #define IMA_K_TREE_PROB 13
 #define IMA_K_POPMIG 14
 #define IMA_K_HKY_FP32 15
-#define IMA_K_COUNT 16
+#define IMA_K_TIMES 16             /* re-timing uploads: float-float copies, lengths, in-place reads */
+#define IMA_K_COUNT 17
 /* Total kernel launches issued by this library on the context. */
 int ima_gpu_launch_count(ima_ctx *ctx, long long *n);
 /* Write a device buffer larger than L2 (evicts resident data). */

@@ -45,7 +45,7 @@ def test_parallel_upload_matches_one_by_one():
     assert np.array_equal(a.eval(ci, li, u, par)[0], b.eval(ci, li, u, par)[0])
 
 
-@pytest.mark.parametrize("kind", ["hky", "is"])
+@pytest.mark.parametrize("kind", ["hky", "is", "is_long"])
 def test_set_times_matches_set_genealogies(kind):
     """The times-only upload (long lists over the host threads, short ones
     on the caller's) gives the bits of a full upload with the same times,
@@ -53,8 +53,10 @@ def test_set_times_matches_set_genealogies(kind):
     refuses a pair that holds no genealogy."""
     if kind == "hky":
         wl = workloads.make_hky(seed=33, nloci=12, nch=32, ncopies=10, nbases=300)   # 384 pairs
-    else:
+    elif kind == "is":
         wl = workloads.make_is(seed=34)
+    else:
+        wl = workloads.make_is(seed=38, nloci=10, nch=200)   # 78,000 nodes: lengths summed later
     ci, li = wl.pairs()
     pci, pli, up0, up1, down, tm = wl.packed()
     u, par = wl.u.ravel(), wl.par.ravel()
@@ -90,6 +92,44 @@ def test_set_times_matches_set_genealogies(kind):
     fresh = _hky_ctx(wl)
     with pytest.raises(api.ImaError):
         fresh.set_times([0], [0], tm[:nl[0]])
+
+
+@pytest.mark.parametrize("kind", ["sw", "is", "is_long"])
+def test_eval_times_matches_set_times_then_eval(kind):
+    """The one-call re-timing and evaluation gives the bits of set_times
+    followed by eval, for a run of pairs in item order (read in place where
+    the device reads host memory) and for a shuffled list, with and without
+    given lengths.  is_long has more nodes than the one-kernel short-run
+    path takes: its lengths are summed later, before the infinite-sites
+    evaluation reads them."""
+    if kind == "sw":
+        wl = workloads.make_sw(seed=35, nloci=10, nch=16, per_pop=10)
+    elif kind == "is":
+        wl = workloads.make_is(seed=36)
+    else:
+        wl = workloads.make_is(seed=37, nloci=10, nch=200)   # 78,000 nodes
+    ci, li = wl.pairs()
+    pci, pli, up0, up1, down, tm = wl.packed()
+    u, par = wl.u.ravel(), wl.par.ravel()
+    a, b = _hky_ctx(wl), _hky_ctx(wl)
+    wl.upload(a)
+    wl.upload(b)
+    nl = np.array([2 * wl.tree(int(c), int(l)).n - 1 for c, l in zip(pci, pli)])
+    ends = np.cumsum(nl)
+    starts = ends - nl
+    rng = np.random.default_rng(8)
+    for case in ("run", "shuffled", "run_lengths"):
+        f = np.repeat(rng.uniform(0.9, 1.1, size=len(nl)), nl)
+        scaled = np.where(tm > 0, tm * f, tm)
+        order = rng.permutation(len(pci)) if case == "shuffled" else np.arange(len(pci))
+        idx = np.concatenate([np.arange(starts[k], ends[k]) for k in order])
+        lengths = rng.uniform(1.0, 3.0, size=len(order)) if case == "run_lengths" else None
+        ra, sa = a.eval_times(pci[order], pli[order], scaled[idx], u[order], par[order], length=lengths)
+        b.set_times(pci[order], pli[order], scaled[idx], length=lengths)
+        rb, sb = b.eval(pci[order], pli[order], u[order], par[order])
+        assert np.array_equal(ra, rb) and np.array_equal(sa, sb), case
+        # and the state left behind is the same
+        assert np.array_equal(a.eval(ci, li, u, par)[0], b.eval(ci, li, u, par)[0]), case
 
 
 def test_parallel_upload_rejects_a_bad_genealogy():
