@@ -234,6 +234,13 @@ def _ptr(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
 
 
+def _addr(a):
+    """The address as an int (cheaper per call than _ptr).  Only for arrays
+    a caller holds in a variable for the duration of the call: unlike _ptr's
+    pointer object, an int keeps no reference to a temporary array."""
+    return None if a is None else a.ctypes.data
+
+
 def _i32(a):
     return None if a is None else np.ascontiguousarray(a, dtype=np.int32)
 
@@ -328,10 +335,10 @@ class Context:
         n = len(ci)
         kappa, ai = _f64(kappa), _i32(ai)
         time, length = _f64(time), _f64(length)
-        res = np.zeros(n)
-        st = np.zeros(n, np.int32)
-        self._ck(self.lib.ima_gpu_eval_times(self.h, n, _ptr(ci), _ptr(li), _ptr(time), _ptr(length), _ptr(u),
-                                             _ptr(kappa), _ptr(ai), int(precision), _ptr(res), _ptr(st)))
+        res = np.empty(n)
+        st = np.empty(n, np.int32)
+        self._ck(self.lib.ima_gpu_eval_times(self.h, n, _addr(ci), _addr(li), _addr(time), _addr(length), _addr(u),
+                                             _addr(kappa), _addr(ai), int(precision), _addr(res), _addr(st)))
         return res, st
 
     def set_pi(self, ci, li, pi):
@@ -388,10 +395,10 @@ class Context:
         n = len(ci)
         kappa, ai = _f64(kappa), _i32(ai)
         edits = None if edits is None else _i32(edits).reshape(n, 4)
-        res = np.zeros(n)
-        st = np.zeros(n, np.int32)
-        self._ck(self.lib.ima_gpu_eval(self.h, n, _ptr(ci), _ptr(li), _ptr(u), _ptr(kappa), _ptr(edits),
-                                       _ptr(ai), int(precision), _ptr(res), _ptr(st)))
+        res = np.empty(n)
+        st = np.empty(n, np.int32)
+        self._ck(self.lib.ima_gpu_eval(self.h, n, _addr(ci), _addr(li), _addr(u), _addr(kappa), _addr(edits),
+                                       _addr(ai), int(precision), _addr(res), _addr(st)))
         return res, st
 
     def commit(self, ci, li, accept):

@@ -1077,21 +1077,18 @@ static int upload_times(ima_ctx *c, int n, const int32_t *ci, const int32_t *li,
   if (!c || n < 0 || (n > 0 && (!ci || !li || !time))) return IMA_ERR_ARG;
   if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
   if (n == 0) return IMA_OK;
-  std::vector<size_t> &off = c->pair_off;
-  off.resize((size_t)n + 1);
-  off[0] = 0;
   int lo = INT32_MAX, hi = -1;
-  bool run = true;  // the pairs are items first, first + 1, ... in order
+  bool run = c->valid(ci[0], li[0]);  // the pairs are items first, first + 1, ... in order
+  const int first = run ? c->item_of(ci[0], li[0]) : 0;
+  const uint8_t *has = c->has_tree.data();
   for (int k = 0; k < n; k++) {
     if (!c->valid(ci[k], li[k])) return c->fail(IMA_ERR_ARG, "pair %d: chain %d locus %d out of range", k, ci[k], li[k]);
     const int item = c->item_of(ci[k], li[k]);
-    if (!c->has_tree[item]) return c->fail(IMA_ERR_STATE, "pair %d: chain %d locus %d has no genealogy", k, ci[k], li[k]);
-    off[k + 1] = off[k] + 2 * c->loci[li[k]].d.n - 1;
+    if (!has[item]) return c->fail(IMA_ERR_STATE, "pair %d: chain %d locus %d has no genealogy", k, ci[k], li[k]);
     lo = std::min(lo, item);
     hi = std::max(hi, item);
-    run = run && item == c->item_of(ci[0], li[0]) + k;
+    run = run && item == first + k;
   }
-  const size_t *offp = off.data();
   if (run) {
     // a contiguous run of items in order: the caller's packed times are the
     // device layout of the run, so they go to the device in one copy (from
@@ -1102,7 +1099,7 @@ static int upload_times(ima_ctx *c, int n, const int32_t *ci, const int32_t *li,
     // the host next writes it.  Uploads still pending from the mirror go
     // first.
     if (int r = flush(c)) return r;
-    const size_t n0 = c->items[lo].node_off, n1 = n0 + offp[n];
+    const size_t n0 = c->items[lo].node_off, n1 = (size_t)c->items[hi].node_off + 2 * c->items[hi].n - 1;
     if (in_place && c->pageable_access && (long long)(n1 - n0) <= SHORT_RUN_NODES) {
       // a short run: one kernel reads it in place (times, float-float form,
       // lengths), nothing left pending
@@ -1164,6 +1161,11 @@ static int upload_times(ima_ctx *c, int n, const int32_t *ci, const int32_t *li,
   // any order: staged in the mirror on the host threads (a pair given twice
   // keeps its later times only when the list is applied in order on one
   // thread), copied with the next evaluation
+  std::vector<size_t> &off = c->pair_off;
+  off.resize((size_t)n + 1);
+  off[0] = 0;
+  for (int k = 0; k < n; k++) off[k + 1] = off[k] + 2 * c->loci[li[k]].d.n - 1;
+  const size_t *offp = off.data();
   if (int rs = sync_mirror(c)) return rs;
   bool repeat = false;
   if ((int)c->pair_stamp.size() != c->nitems) c->pair_stamp.assign(c->nitems, -1);
@@ -1606,10 +1608,9 @@ extern "C" int ima_gpu_eval_times(ima_ctx *c, int n, const int32_t *ci, const in
   bool in_place = false;
   int r = upload_times(c, n, ci, li, time, length, true, &in_place);
   r = r ? r : ima_gpu_eval(c, n, ci, li, u, kappa, nullptr, ai, precision, result, status);
-  if (in_place) {
-    const int rs = c->cuda(cudaStreamSynchronize(c->st), "evaluation");
-    r = r ? r : rs;
-  }
+  // a successful evaluation has synchronised the stream already; a failed
+  // one must not return while a kernel may still read the caller's buffers
+  if (r && in_place) cudaStreamSynchronize(c->st);
   return r;
 }
 
