@@ -518,9 +518,13 @@ class Context:
 
     # ------------------------------------- genealogy weights and p(G)
     def set_popmodel(self, pm, th_max, th_min=None, mg_max=None, mg_min=None, mg_mean=None, expo=False,
-                     chk=()):
+                     chk=None):
         """Load a population model (ima2p_gb300.popmodel.PopModel) with the
-        priors of its parameters (itheta[].pr, imig[].pr)."""
+        priors of its parameters (itheta[].pr, imig[].pr).  chk: the
+        migration cells that must stay empty (default: the model's own,
+        pm.chk_cells)."""
+        if chk is None:
+            chk = getattr(pm, "chk_cells", ())
         nth, nmg = len(pm.th_cells), len(pm.mg_cells)
         tho, thi = pm.th_csr()
         mgo, mgi = pm.mg_csr()

@@ -259,6 +259,38 @@ def run_ref(mode, text):
     return out
 
 
+IPARAM_FLAGS = ("parameters_by_period", "ancestral_sizes_largest_sampled", "one_migration_parameter",
+                "migration_between_sampled", "no_migration_between_nonsisters",
+                "single_migration_both_directions", "no_migration", "expo_migration_prior")
+
+
+def ref_iparams(npops, treestr, flags, thetaprior, mprior, varrank):
+    """The reference's setup_iparams and set_nomigrationchecklist
+    (initialize.cpp:202-809) on a population tree, through oracle/_ref/imaref
+    (this container only).  flags: the IPARAM_FLAGS that are set.  Returns
+    {"theta": [(name, b, e, [(p, r)], max, min)], "mig": [(name, b, e,
+    [(p, r, c)], max, min, mean)], "chk": [(p, r, c)]}."""
+    t = ["%d %s" % (npops, treestr), " ".join("1" if f in flags else "0" for f in IPARAM_FLAGS),
+         "%.17g %.17g" % (thetaprior, mprior), " ".join("%.17g" % v for v in varrank)]
+    out = run_ref("iparams", "\n".join(t) + "\n")
+    res = {"theta": [], "mig": [], "chk": []}
+    for ln in out.splitlines():
+        f = ln.split()
+        if f[0] == "TH":
+            n = int(f[5])
+            wp = [(int(f[6 + 2 * j]), int(f[7 + 2 * j])) for j in range(n)]
+            res["theta"].append((f[2], int(f[3]), int(f[4]), wp, float(f[6 + 2 * n]), float(f[7 + 2 * n])))
+        elif f[0] == "MG":
+            n = int(f[5])
+            wp = [(int(f[6 + 3 * j]), int(f[7 + 3 * j]), int(f[8 + 3 * j])) for j in range(n)]
+            res["mig"].append((f[2], int(f[3]), int(f[4]), wp, float(f[6 + 3 * n]), float(f[7 + 3 * n]),
+                               float(f[8 + 3 * n])))
+        elif f[0] == "CHK":
+            n = int(f[1])
+            res["chk"] = [(int(f[2 + 3 * j]), int(f[3 + 3 * j]), int(f[4 + 3 * j])) for j in range(n)]
+    return res
+
+
 def ref_is(seq, trees, lengths, us):
     n, S = seq.shape
     t = [f"{n} {S}", " ".join(map(str, seq.ravel())), str(len(trees))]

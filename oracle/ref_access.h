@@ -10,5 +10,7 @@ double refacc_icoal(int cc, double fc, double hcc, double max, double min);
 double refacc_imig(int cm, double fm, double max, double min);
 double refacc_imig_expo(int cm, double fm, double mean);
 void refacc_setup_iparams(void);
+void refacc_set_varrank(const double *v, int n);
+void refacc_set_nomigrationchecklist(void);
 double refacc_marginp(int param, int firsttree, int lasttree, double x);
 #endif

@@ -12,7 +12,8 @@
  * ref_access_cpd.cpp and ref_access_jf.cpp include those two reference
  * sources to reach them.  The other reference objects are linked unchanged.
  *
- * Usage:  imaref is|hky|sw|swap|jointp|de|margin|tw|iterm|ry <input.txt>   (results on stdout)
+ * Usage:  imaref is|hky|sw|swap|jointp|de|margin|tw|iterm|ry|popmig|peaks|iparams <input.txt>
+ *         (results on stdout)
  */
 #undef GLOBVARS
 #include "imamp.hpp"
@@ -418,6 +419,52 @@ static void run_peaks()
  * chain by sum_treeinfo (ginfo.cpp:209) in locus order, then
  * initialize_integrate_tree_prob (:2089-2134), as finish_setup_C does. */
 extern "C" void init_gtreecommon(void);  /* C linkage, as update_gtree_common.hpp declares it */
+/* IP: npops treestring flags[8] thetaprior mprior varrank[npops]
+ *   flags: PARAMETERSBYPERIOD ANCESTRALPOPSIZESSETTOLARGESTSAMPLED
+ *          ONEMIGRATIONPARAMETER MIGRATIONBETWEENSAMPLED NOMIGBETWEENNONSISTERS
+ *          SINGLEMIGRATIONBOTHDIRECTIONS NOMIGRATION EXPOMIGRATIONPRIOR
+ *   -> "PARAMS np nm", "TH i str b e n {p r}*n max min",
+ *      "MG i str b e n {p r c}*n max min mean", "CHK n {p r c}*n"
+ * setup_iparams (initialize.cpp:202-727) and set_nomigrationchecklist
+ * (:761-809) on the population tree of chain 0, without a prior file. */
+static void run_iparams()
+{
+  int npp = rd_i();
+  char treestr[POPTREESTRINGLENGTHMAX];
+  if (fscanf(g_in, "%255s", treestr) != 1) { fprintf(stderr, "short input\n"); exit(3); }
+  const int opt[8] = {PARAMETERSBYPERIOD, ANCESTRALPOPSIZESSETTOLARGESTSAMPLED, ONEMIGRATIONPARAMETER,
+                      MIGRATIONBETWEENSAMPLED, NOMIGBETWEENNONSISTERS, SINGLEMIGRATIONBOTHDIRECTIONS, NOMIGRATION,
+                      EXPOMIGRATIONPRIOR};
+  for (int k = 0; k < 8; k++) modeloptions[opt[k]] = rd_i();
+  thetaprior = rd_d();
+  mprior = rd_d();
+  npops = npp;
+  numtreepops = 2 * npops - 1;
+  lastperiodnumber = numsplittimes = npops - 1;
+  double vr[MAXPOPS];
+  for (int p = 0; p < npops; p++) vr[p] = rd_d();
+  refacc_set_varrank(vr, npops);
+  alloc_chains(1, 1);
+  setup_poptree(0, treestr);
+  refacc_setup_iparams();
+  refacc_set_nomigrationchecklist();
+  printf("PARAMS %d %d\n", numpopsizeparams, nummigrateparams);
+  for (int i = 0; i < numpopsizeparams; i++) {
+    printf("TH %d %s %d %d %d", i, itheta[i].str, itheta[i].b, itheta[i].e, itheta[i].wp.n);
+    for (int j = 0; j < itheta[i].wp.n; j++) printf(" %d %d", itheta[i].wp.p[j], itheta[i].wp.r[j]);
+    printf(" %.17g %.17g\n", itheta[i].pr.max, itheta[i].pr.min);
+  }
+  for (int i = 0; i < nummigrateparams; i++) {
+    printf("MG %d %s %d %d %d", i, imig[i].str, imig[i].b, imig[i].e, imig[i].wp.n);
+    for (int j = 0; j < imig[i].wp.n; j++) printf(" %d %d %d", imig[i].wp.p[j], imig[i].wp.r[j], imig[i].wp.c[j]);
+    printf(" %.17g %.17g %.17g\n", imig[i].pr.max, imig[i].pr.min, imig[i].pr.mean);
+  }
+  printf("CHK %d", nomigrationchecklist.n);
+  for (int j = 0; j < nomigrationchecklist.n; j++)
+    printf(" %d %d %d", nomigrationchecklist.p[j], nomigrationchecklist.r[j], nomigrationchecklist.c[j]);
+  printf("\n");
+}
+
 static void run_tw()
 {
   int npp = rd_i(), nch = rd_i(), nl = rd_i(), expo = rd_i(), nomig = rd_i();
@@ -649,6 +696,7 @@ int main(int argc, char **argv)
   else if (mode == "ry") run_ry();
   else if (mode == "popmig") run_popmig();
   else if (mode == "peaks") run_peaks();
+  else if (mode == "iparams") run_iparams();
   else { fprintf(stderr, "unknown mode\n"); return 2; }
   fclose(g_in);
   return 0;

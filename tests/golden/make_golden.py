@@ -600,13 +600,57 @@ def golden_peaks():
     np.savez_compressed(os.path.join(OUT, "golden_peaks.npz"), **out)
 
 
+IPARAM_TREES = [
+    (2, "(0,1):2"),
+    (3, "((0,1):3,2):4"),
+    (3, "((0,2):3,1):4"),
+    (3, "(0,(1,2):3):4"),
+    (4, "((0,1):4,(2,3):5):6"),
+    (4, "(((0,1):4,2):5,3):6"),
+    (4, "((0,(1,2):4):5,3):6"),
+    (5, "(((0,1):5,2):6,(3,4):7):8"),
+    (5, "((0,1):5,((2,3):6,4):7):8"),
+]
+IPARAM_OPTIONS = [
+    (), ("parameters_by_period",), ("ancestral_sizes_largest_sampled",), ("one_migration_parameter",),
+    ("migration_between_sampled",), ("no_migration_between_nonsisters",), ("single_migration_both_directions",),
+    ("no_migration",), ("expo_migration_prior",),
+    ("parameters_by_period", "single_migration_both_directions"),
+    ("parameters_by_period", "one_migration_parameter"),
+    ("parameters_by_period", "migration_between_sampled"),
+    ("parameters_by_period", "no_migration_between_nonsisters"),
+    ("ancestral_sizes_largest_sampled", "no_migration_between_nonsisters"),
+    ("one_migration_parameter", "no_migration_between_nonsisters"),
+    ("one_migration_parameter", "migration_between_sampled"),
+    ("migration_between_sampled", "single_migration_both_directions"),
+    ("no_migration_between_nonsisters", "single_migration_both_directions", "expo_migration_prior"),
+    ("ancestral_sizes_largest_sampled", "no_migration"),
+]
+
+
+def golden_iparams():
+    """The reference's parameter maps and no-migration checklist for every
+    tree of IPARAM_TREES under every option set of IPARAM_OPTIONS (with
+    seeded polymorphism scores for the ancestral-size option, ties
+    included)."""
+    rng = np.random.default_rng(1012)
+    cases = []
+    for npops, ts in IPARAM_TREES:
+        for flags in IPARAM_OPTIONS:
+            vr = rng.integers(0, 4, size=npops).astype(float)  # small integers: ties occur
+            r = O.ref_iparams(npops, ts, flags, 10.0, 5.0, vr)
+            cases.append({"npops": npops, "tree": ts, "flags": list(flags), "varrank": vr.tolist(), "ref": r})
+    import json
+    np.savez_compressed(os.path.join(OUT, "golden_iparams.npz"), cases=np.array(json.dumps(cases)))
+
+
 if __name__ == "__main__":
     if not O.ref_available():
         sys.exit("build the reference harness first: make -C oracle ref")
     gens = {"is": golden_is, "hky": golden_hky, "sw": golden_sw, "swap": golden_swap,
             "jointp": golden_jointp, "de": golden_de, "margin": golden_margin,
             "tw": golden_tw, "ry": golden_ry, "ks": golden_ks, "popmig": golden_popmig,
-            "peaks": golden_peaks}
+            "peaks": golden_peaks, "iparams": golden_iparams}
     for name in (sys.argv[1:] or list(gens)):
         gens[name]()
     for f in sorted(os.listdir(OUT)):

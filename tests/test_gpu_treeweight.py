@@ -72,6 +72,43 @@ def test_weights_bit_exact_and_integrals(c):
         assert np.array_equal(rows[ci], want)
 
 
+OPTION_SETS = [
+    dict(parameters_by_period=True),
+    dict(ancestral_sizes_largest_sampled=True, no_migration_between_nonsisters=True),
+    dict(one_migration_parameter=True),
+    dict(migration_between_sampled=True, single_migration_both_directions=True),
+]
+
+
+@pytest.mark.parametrize("opts", range(len(OPTION_SETS)))
+@pytest.mark.parametrize("c", [c for c in range(len(CASES)) if CASES[c].npops >= 3 and not CASES[c].nomig])
+def test_model_option_integrals(c, opts):
+    """p(G) under the -j model options' maps (popmodel.build, pinned to the
+    reference's setup_iparams by test_popmodel_options) against the oracle,
+    including the chains a forbidden migration cell sends to -DBL_MAX."""
+    from ima2p_gb300 import popmodel
+    cs = CASES[c]
+    opt = popmodel.ModelOptions(**OPTION_SETS[opts])
+    pm = popmodel.build(cs.tree, cs.npops, options=opt, varrank=np.arange(cs.npops)[::-1] * 1.0)
+    pr = popmodel.priors(pm, cs.thetaprior, cs.mprior, cs.expo)
+    ctx = api.Context(0)
+    ctx.set_popmodel(pm, *pr, expo=cs.expo)
+    packed, gl, gt, hval, samp = _inputs(cs)
+    w = ctx.treeweight(packed, gl, gt, hval, samp, cs.tvals)
+    off = np.arange(cs.nch + 1, dtype=np.int32) * cs.nl
+    probg, q, m = ctx.tree_prob(off, group_tv=np.arange(cs.nch))[:3]
+    for ci in range(cs.nch):
+        ws = [dict(cc=w["cc"][i], hcc=w["hcc"][i], fc=w["fc"][i], mc=w["mc"][i], fm=w["fm"][i])
+              for i in range(ci * cs.nl, (ci + 1) * cs.nl)]
+        st, pg, q_o, m_o = O.tree_prob(pm, O.sum_weights(ws, pm), *pr, expo=cs.expo, chk=pm.chk_cells)
+        if pg == -np.finfo(np.float64).max:
+            assert probg[ci] == pg
+            continue
+        np.testing.assert_allclose(probg[ci], pg, rtol=0, atol=ATOL_INT)
+        np.testing.assert_allclose(q[ci], q_o, rtol=0, atol=ATOL_INT)
+        np.testing.assert_allclose(m[ci], m_o, rtol=0, atol=ATOL_INT)
+
+
 def test_many_genealogies_and_long_groups():
     """The 3-population case repeated 400 times (9600 genealogies, 2400 warps'
     worth of blocks): every copy gives the reference's weights, and a chain
