@@ -90,17 +90,24 @@ def test_surface_repeat_calls_bitwise(method):
     np.testing.assert_allclose(q2, q0[perm], rtol=1e-12, atol=0)
 
 
+# Fewer than four 256-genealogy tiles: no max-only pre-pass runs, and a
+# point's reference is the best of its 32 exact seed samples (genealogies
+# floor(i G / 32)), so a term can lie far above it
+G_NO_PREPASS = 700
+G_STAR = 256 + 17  # between the seed samples 262 and 284
+
+
 def test_surface_tc_term_far_above_prepass_bound():
-    """One genealogy 300 nats above every other, in a tile the max-only
-    pre-pass skips and away from the seed samples: its weight relative to the
-    pre-pass bound leaves the fixed-point range, so every point is taken a
-    second time relative to its exact maximum.  The densities agree with the
-    FP64 form and the oracle, and repeat bit for bit."""
+    """One genealogy 300 nats above every other, away from the seed samples,
+    with no pre-pass: its weight relative to the seeds' bound leaves the
+    fixed-point range, so every point is taken a second time relative to its
+    exact maximum.  The densities agree with the FP64 form and the oracle,
+    and repeat bit for bit."""
     rng = np.random.default_rng(8)
-    G = 40000
+    G = G_NO_PREPASS
     rows, lognorm, _ = synth.surface_stats(rng, G, 5, 8, 2)
     lognorm = lognorm.copy()
-    g_star = 256 * 3 + 17   # tile 3 (the pre-pass reads tiles 0, 8, ...); seeds sample multiples of G/32
+    g_star = G_STAR
     lognorm[g_star] = lognorm.max() + 300.0
     pts = synth.surface_points(rng, 200)
     ctx = ctx_with([("sw", 2, 1)])
@@ -119,17 +126,17 @@ def test_surface_tc_term_far_above_prepass_bound():
 
 @pytest.mark.parametrize("lead", [20.0, 40.0, 46.0, 50.0, 54.0, 60.0])
 def test_surface_tc_dominant_genealogy_sample_size(lead):
-    """One genealogy `lead` nats above every other (in a tile the max-only
-    pre-pass skips): terms up to 55 nats above the pre-pass bound stay in the
-    first pass's fixed-point sums, larger ones send the point to the second
-    pass.  Either way the densities and the effective sample sizes (here
-    close to 1) agree with the FP64 form -- the squared weights of the
-    largest terms exceed FP32's range and must still be counted."""
+    """One genealogy `lead` nats above every other, away from the seed
+    samples, with no pre-pass: terms up to 55 nats above the seeds' bound
+    stay in the first pass's fixed-point sums, larger ones send the point to
+    the second pass.  Either way the densities and the effective sample
+    sizes (here close to 1) agree with the FP64 form -- the squared weights
+    of the largest terms exceed FP32's range and must still be counted."""
     rng = np.random.default_rng(9)
-    G = 40000
+    G = G_NO_PREPASS
     rows, lognorm, _ = synth.surface_stats(rng, G, 5, 8, 2)
     lognorm = lognorm.copy()
-    lognorm[256 * 3 + 17] = lognorm.max() + lead
+    lognorm[G_STAR] = lognorm.max() + lead
     pts = synth.surface_points(rng, 100)
     ctx = ctx_with([("sw", 2, 1)])
     ctx.surface_load(rows, 5, 8, 3, lognorm=lognorm)
