@@ -50,6 +50,8 @@ struct Batch {
   cudaEvent_t req_ev = nullptr;  // the last upload from h_reqpin
   double hky_bytes = 0.0, sw_bytes = 0.0;  // algorithmic bytes of one run (launch statistics)
   std::vector<int> dl_idx;  // SW requests' entries of ima_ctx::dl_fast
+  bool in_order = false;    // order is the identity: results copy straight back
+  long long dl_stamp = -1;  // ima_ctx::dl_stamp when this batch last set those entries
   std::vector<ReqDev> h_req;
   cudaGraphExec_t graph = nullptr;
   int maxn_is = 0, maxs_is = 0, maxn_hky = 0, maxs_hky = 0, maxn_sw = 0;
@@ -223,6 +225,14 @@ struct ima_ctx {
   int32_t *d_al = nullptr;
   double *d_dlike = nullptr;
   std::vector<uint8_t> dl_fast;  // per item x marker: last SW evaluation was float-float
+  long long dl_stamp = 0;        // counts the batches that set dl_fast entries
+  // the last list of pairs upload_times checked, and what it found: a list
+  // given again is not walked again (pairs only gain genealogies, except
+  // when a checkpoint is read, which bumps tree_gen)
+  std::vector<int32_t> tk_ci, tk_li;
+  int tk_lo = 0, tk_hi = -1, tk_gen = -1;
+  bool tk_run = false;
+  int tree_gen = 0;
   std::vector<uint8_t> has_tree; // per item: a genealogy was uploaded
   std::unique_ptr<HostPool> pool;  // host threads for set_genealogies (made on first use)
   std::vector<int> pair_stamp;     // set_genealogies: repeated-pair check
@@ -293,6 +303,7 @@ struct ima_ctx {
   // items whose tree lengths are still to be summed from their device times
   // (re-timings without lengths): done when a reader needs them
   int lpend_lo = INT32_MAX, lpend_hi = -1;
+
   double *d_lterm = nullptr;  // per node: its branch term, for those sums
   float *tp_rows = nullptr;  // gsampinf rows of the last ima_gpu_tree_prob
   int tp_ngroups = 0, tp_rowlen = 0;
@@ -382,21 +393,24 @@ struct ima_ctx {
     return e;
   }
   // bracket one kernel launch for accounting
+  // launches by f() on stream on (the context stream by default), counted
+  // and, when profiling, timed by events on that stream
   template <typename F>
-  void launch(int kind, double bytes, F &&f)
+  void launch(int kind, double bytes, F &&f, cudaStream_t on = nullptr)
   {
+    if (!on) on = st;
     cudaEvent_t a = nullptr, b = nullptr;
     if (profiling) {
       a = ev();
       b = ev();
-      cudaEventRecord(a, st);
+      cudaEventRecord(a, on);
     }
     f();
     launches++;
     k_launches[kind]++;
     k_bytes[kind] += bytes;
     if (profiling) {
-      cudaEventRecord(b, st);
+      cudaEventRecord(b, on);
       pending.push_back({kind, a, b, bytes});
     }
   }
@@ -482,6 +496,7 @@ extern "C" void ima_gpu_destroy(ima_ctx *c)
   for (auto e : c->event_pool) cudaEventDestroy(e);
   if (c->t0) cudaEventDestroy(c->t0);
   if (c->t1) cudaEventDestroy(c->t1);
+
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -1066,6 +1081,44 @@ static void set_times_one(ima_ctx *c, int item, const double *time, double lengt
   c->h_len[item] = L;
 }
 
+// The pairs of a re-timing: each a chain-locus holding a genealogy; their
+// item range, and whether they are items first, first + 1, ... in order (a
+// run).  A list given again is not walked again (pairs only gain
+// genealogies, except when a checkpoint is read, which bumps tree_gen).
+static int check_pairs(ima_ctx *c, int n, const int32_t *ci, const int32_t *li, int *lo_, int *hi_, bool *run_)
+{
+  int lo = INT32_MAX, hi = -1;
+  bool run = false;
+  if (c->tk_gen == c->tree_gen && (int)c->tk_ci.size() == n && !memcmp(c->tk_ci.data(), ci, n * sizeof(int32_t)) &&
+      !memcmp(c->tk_li.data(), li, n * sizeof(int32_t))) {
+    lo = c->tk_lo;
+    hi = c->tk_hi;
+    run = c->tk_run;
+  } else {
+    run = c->valid(ci[0], li[0]);
+    const int first = run ? c->item_of(ci[0], li[0]) : 0;
+    const uint8_t *has = c->has_tree.data();
+    for (int k = 0; k < n; k++) {
+      if (!c->valid(ci[k], li[k])) return c->fail(IMA_ERR_ARG, "pair %d: chain %d locus %d out of range", k, ci[k], li[k]);
+      const int item = c->item_of(ci[k], li[k]);
+      if (!has[item]) return c->fail(IMA_ERR_STATE, "pair %d: chain %d locus %d has no genealogy", k, ci[k], li[k]);
+      lo = std::min(lo, item);
+      hi = std::max(hi, item);
+      run = run && item == first + k;
+    }
+    c->tk_ci.assign(ci, ci + n);
+    c->tk_li.assign(li, li + n);
+    c->tk_lo = lo;
+    c->tk_hi = hi;
+    c->tk_run = run;
+    c->tk_gen = c->tree_gen;
+  }
+  *lo_ = lo;
+  *hi_ = hi;
+  *run_ = run;
+  return IMA_OK;
+}
+
 // New times of genealogies whose topology is kept.  in_place: a contiguous
 // run may be read by the device from the caller's buffers while the stream
 // runs (the caller synchronises the stream before returning); *read_in_place
@@ -1078,17 +1131,8 @@ static int upload_times(ima_ctx *c, int n, const int32_t *ci, const int32_t *li,
   if (!c->nchains) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_chains first");
   if (n == 0) return IMA_OK;
   int lo = INT32_MAX, hi = -1;
-  bool run = c->valid(ci[0], li[0]);  // the pairs are items first, first + 1, ... in order
-  const int first = run ? c->item_of(ci[0], li[0]) : 0;
-  const uint8_t *has = c->has_tree.data();
-  for (int k = 0; k < n; k++) {
-    if (!c->valid(ci[k], li[k])) return c->fail(IMA_ERR_ARG, "pair %d: chain %d locus %d out of range", k, ci[k], li[k]);
-    const int item = c->item_of(ci[k], li[k]);
-    if (!has[item]) return c->fail(IMA_ERR_STATE, "pair %d: chain %d locus %d has no genealogy", k, ci[k], li[k]);
-    lo = std::min(lo, item);
-    hi = std::max(hi, item);
-    run = run && item == first + k;
-  }
+  bool run = false;  // the pairs are items first, first + 1, ... in order
+  if (int r = check_pairs(c, n, ci, li, &lo, &hi, &run)) return r;
   if (run) {
     // a contiguous run of items in order: the caller's packed times are the
     // device layout of the run, so they go to the device in one copy (from
@@ -1424,6 +1468,9 @@ static int build_batch(ima_ctx *c, Batch &b, int n, const int32_t *ci, const int
   b.dl_idx.clear();
   for (int k = b.nis + b.nhky; k < b.n; k++)
     b.dl_idx.push_back(c->items[b.h_req[k].item].al_off + b.h_req[k].ai);
+  b.dl_stamp = -1;
+  b.in_order = true;
+  for (int k = 0; k < b.n && b.in_order; k++) b.in_order = (b.order[k] == k);
   // an earlier upload from the staging buffer may still be queued
   if (int r = c->cuda(cudaEventSynchronize(b.req_ev), "requests")) return r;
   memcpy(b.h_reqpin, b.h_req.data(), n * sizeof(ReqDev));
@@ -1456,6 +1503,7 @@ static double sw_bytes(ima_ctx *c, const Batch &b)
   return s;
 }
 
+// kernels of a batch (no host work, graph-capturable once sumlogk is set)
 // kernels of a batch (no host work, graph-capturable once sumlogk is set)
 static void enqueue(ima_ctx *c, Batch &b)
 {
@@ -1527,13 +1575,22 @@ static int fetch(ima_ctx *c, Batch &b, double *result, int32_t *status)
   }
   r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "evaluation");
   if (r) return r;
-  for (int k = 0; k < b.n; k++) {
-    if (result) result[b.order[k]] = b.h_res[k];
-    if (status) status[b.order[k]] = b.h_st[k];
+  if (b.in_order) {
+    if (result) memcpy(result, b.h_res, b.n * sizeof(double));
+    if (status) memcpy(status, b.h_st, b.n * sizeof(int32_t));
+  } else {
+    for (int k = 0; k < b.n; k++) {
+      if (result) result[b.order[k]] = b.h_res[k];
+      if (status) status[b.order[k]] = b.h_st[k];
+    }
   }
-  // remember the format of the per-branch SW terms
-  const uint8_t fmt = (b.prec != IMA_PREC_FP64);
-  for (int k : b.dl_idx) c->dl_fast[k] = fmt;
+  // remember the format of the per-branch SW terms (nothing to do when this
+  // batch was the last to set them: its precision is fixed)
+  if (!b.dl_idx.empty() && b.dl_stamp != c->dl_stamp) {
+    const uint8_t fmt = (b.prec != IMA_PREC_FP64);
+    for (int k : b.dl_idx) c->dl_fast[k] = fmt;
+    b.dl_stamp = ++c->dl_stamp;
+  }
   return IMA_OK;
 }
 
@@ -1551,11 +1608,11 @@ static void free_batch(Batch &b)
   b = Batch();
 }
 
-extern "C" int ima_gpu_eval(ima_ctx *c, int n, const int32_t *ci, const int32_t *li, const double *u,
-                            const double *kappa, const int32_t *edits, const int32_t *ai, int precision,
-                            double *result, int32_t *status)
+// The request list of ima_gpu_eval staged in c->evb (kept when a call
+// repeats the previous arrays).
+static int eval_prepare(ima_ctx *c, int n, const int32_t *ci, const int32_t *li, const double *u,
+                        const double *kappa, const int32_t *edits, const int32_t *ai, int precision)
 {
-  if (!c) return IMA_ERR_ARG;
   Batch &b = c->evb;  // reused request buffers: no allocation per call
   // the same request list as the last call (the changet_RY1 pattern: new
   // genealogies, same chain-loci and rates) reuses the staged requests
@@ -1586,6 +1643,16 @@ extern "C" int ima_gpu_eval(ima_ctx *c, int n, const int32_t *ci, const int32_t 
       K.valid = true;
     }
   }
+  return r;
+}
+
+extern "C" int ima_gpu_eval(ima_ctx *c, int n, const int32_t *ci, const int32_t *li, const double *u,
+                            const double *kappa, const int32_t *edits, const int32_t *ai, int precision,
+                            double *result, int32_t *status)
+{
+  if (!c) return IMA_ERR_ARG;
+  Batch &b = c->evb;
+  int r = eval_prepare(c, n, ci, li, u, kappa, edits, ai, precision);
   r = r ? r : flush(c);
   r = r ? r : (b.nis ? ensure_lengths(c) : IMA_OK);  // the infinite-sites likelihood reads them
   r = r ? r : init_sumlogk(c, b);
@@ -4124,6 +4191,7 @@ extern "C" int ima_gpu_checkpoint_read(ima_ctx *c, const char *path, ima_mt19937
   memcpy(c->h_pi, pi.data(), pi.size());
   memcpy(c->h_al, al.data(), al.size());
   c->has_tree = has_tree;
+  c->tree_gen++;
   c->tw_ngen = 0;  // weights of the genealogies replaced here are gone
   c->tw_valid.clear();
   c->dev_lo = INT32_MAX;  // the file is authoritative now

@@ -94,20 +94,26 @@ def test_set_times_matches_set_genealogies(kind):
         fresh.set_times([0], [0], tm[:nl[0]])
 
 
-@pytest.mark.parametrize("kind", ["sw", "is", "is_long"])
+@pytest.mark.parametrize("kind", ["sw", "is", "is_long", "sw_long", "mixed_long"])
 def test_eval_times_matches_set_times_then_eval(kind):
     """The one-call re-timing and evaluation gives the bits of set_times
     followed by eval, for a run of pairs in item order (read in place where
     the device reads host memory) and for a shuffled list, with and without
     given lengths.  is_long has more nodes than the one-kernel short-run
     path takes: its lengths are summed later, before the infinite-sites
-    evaluation reads them."""
+    evaluation reads them.  sw_long and mixed_long are long enough that the
+    run is read in two parts, each part's evaluation waiting for its own
+    times only."""
     if kind == "sw":
         wl = workloads.make_sw(seed=35, nloci=10, nch=16, per_pop=10)
     elif kind == "is":
         wl = workloads.make_is(seed=36)
-    else:
+    elif kind == "is_long":
         wl = workloads.make_is(seed=37, nloci=10, nch=200)   # 78,000 nodes
+    elif kind == "sw_long":
+        wl = workloads.make_sw(seed=39, nloci=24, nch=64, per_pop=30)   # 275,000 nodes
+    else:
+        wl = workloads.make_mixed(seed=40, n_hky=12, n_sw=8, nruns=2, cpr=64)
     ci, li = wl.pairs()
     pci, pli, up0, up1, down, tm = wl.packed()
     u, par = wl.u.ravel(), wl.par.ravel()
