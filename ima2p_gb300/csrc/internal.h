@@ -83,9 +83,10 @@ void launch_is_sumlogk(const Pools &P, int item, int locus, int maxn, int maxS, 
 void launch_is(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int maxS, double *result,
                int32_t *status, int32_t *site_node, cudaStream_t st);
 // variant: launch shape chosen by the batch autotuner (0 is the default)
-constexpr int HKY_FAST_VARIANTS = 5;  // float-float: 128 threads with registers for 8 CTAs per SM, 64 threads
-                                      // (16 CTAs), 256 (4), 128 at 10 CTAs, 128 at 6;
-                                      // FP32: 128 threads (12 CTAs per SM), 64, 256, 128 uncached, 128 at 8
+constexpr int HKY_FAST_VARIANTS = 6;  // float-float: 128 threads with registers for 8 CTAs per SM, 64 threads
+                                      // (16 CTAs), 256 (4), 128 at 10 CTAs, 128 at 6, 96 at 11;
+                                      // FP32: 128 threads (12 CTAs per SM), 64, 256, 128 uncached, 128 at 8,
+                                      // 96 at 16
 constexpr int SW_FAST_VARIANTS = 3;   // one wave (5 or 6 CTAs per SM), 8 chain-loci per CTA
 void launch_hky_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int maxS, int variant,
                      double *result, int32_t *status, cudaStream_t st);

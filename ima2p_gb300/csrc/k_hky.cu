@@ -770,6 +770,7 @@ void launch_hky_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int
     case 2: hky_fast_bs<true, 256, 4>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
     case 3: hky_fast_bs<true, 128, 10>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
     case 4: hky_fast_bs<true, 128, 6>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
+    case 5: hky_fast_bs<true, 96, 11>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
     default: hky_fast_bs<true, 128, 8>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
   }
 }
@@ -784,6 +785,7 @@ void launch_hky_fp32(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int
     case 2: hky_fast_bs<false, 256, 6>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
     case 3: hky_fast_bs<false, 128, 12>(P, reqs, nreq, maxnl, maxS, false, result, status, st); break;
     case 4: hky_fast_bs<false, 128, 8>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
+    case 5: hky_fast_bs<false, 96, 16>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
     default: hky_fast_bs<false, 128, 12>(P, reqs, nreq, maxnl, maxS, true, result, status, st); break;
   }
 }

@@ -12,7 +12,7 @@ from tests._gpu import ctx_with
 
 pytestmark = pytest.mark.gpu
 
-HKY_VARIANTS, SW_VARIANTS = 5, 3
+HKY_VARIANTS, SW_VARIANTS = 6, 3
 
 
 def _mixed_ctx():
