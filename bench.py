@@ -71,12 +71,13 @@ def fp32_peak_tflops(sm_max_mhz):
     return nsm * 128 * 2 * mhz * 1e6 / 1e12, "nominal: %d SMs x 128 FP32 lanes x 2 x %.0f MHz" % (nsm, mhz)
 
 
-def profile_traffic(kernel):
-    """dram bytes per launch from the committed ncu summary, if present."""
+def profile_traffic(kernel, workload):
+    """DRAM bytes per launch of `kernel` on `workload` from the committed ncu
+    summaries (profiles/traffic.json, keyed "kernel/workload"), if captured."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(p) as f:
-            return json.load(f).get(kernel)
+            return json.load(f).get("%s/%s" % (kernel, workload))
     except Exception:
         return None
 
@@ -359,7 +360,7 @@ def measure_lik(args, api, wl, steps, dist=None, device=0, hky_legs=False):
         ach = b / (ms / 1e3) / 1e9 if ms > 0 else 0.0
         roof = {"kernel": "k_hky_fast (float-float)", "bound": "hbm", "achieved": round(ach, 1), "peak": hbm,
                 "unit": "GB/s", "frac": round(ach / hbm, 4), "peak_source": src + " (of %s)" % src,
-                "traffic": profile_traffic("k_hky_fast"), "algorithmic_bytes_per_launch": b,
+                "traffic": profile_traffic("k_hky_fast", wl.name), "algorithmic_bytes_per_launch": b,
                 "avg_launch_ms": round(ms, 5), "launches": nl_}
     if "sw" in kinds:
         nl_, ms = per[api.K_SW_FAST]
@@ -367,7 +368,7 @@ def measure_lik(args, api, wl, steps, dist=None, device=0, hky_legs=False):
         ach = fl / (ms / 1e3) / 1e12 if ms > 0 else 0.0
         sroof = {"kernel": "k_sw_fast", "bound": "fp32", "achieved": round(ach, 3), "peak": round(fp32, 1),
                  "unit": "TFLOP/s", "frac": round(ach / fp32, 4), "peak_source": fp32_src,
-                 "traffic": profile_traffic("k_sw_fast"), "algorithmic_flops_per_launch": fl,
+                 "traffic": profile_traffic("k_sw_fast", wl.name), "algorithmic_flops_per_launch": fl,
                  "avg_launch_ms": round(ms, 5), "launches": nl_,
                  "note": "algorithmic FLOPs of the reference's Bessel terms; the kernel issues them in "
                          "float-float, about ten FP32 instructions each"}
@@ -386,7 +387,7 @@ def measure_lik(args, api, wl, steps, dist=None, device=0, hky_legs=False):
         b = is_algo_bytes(wl)
         ach = b / (ms / 1e3) / 1e9 if ms > 0 else 0.0
         roof = {"kernel": "k_is", "bound": "hbm", "achieved": round(ach, 2), "peak": hbm, "unit": "GB/s",
-                "frac": round(ach / hbm, 6), "peak_source": src, "traffic": profile_traffic("k_is"),
+                "frac": round(ach / hbm, 6), "peak_source": src, "traffic": profile_traffic("k_is", wl.name),
                 "algorithmic_bytes_per_launch": b, "avg_launch_ms": round(ms, 5), "launches": nl_,
                 "note": "latency-bound: %d chain-loci per launch" % units}
 
