@@ -226,6 +226,14 @@ struct ima_ctx {
   double *d_dlike = nullptr;
   std::vector<uint8_t> dl_fast;  // per item x marker: last SW evaluation was float-float
   long long dl_stamp = 0;        // counts the batches that set dl_fast entries
+  // launch shapes the autotuner chose, by batch shape (counts per kind,
+  // largest loci, precision): a later batch of the same shape, ima_gpu_eval's
+  // own included, starts on them
+  struct Tuned {
+    int key[7];
+    int hky, sw;
+  };
+  std::vector<Tuned> tuned;
   // the last list of pairs upload_times checked, and what it found: a list
   // given again is not walked again (pairs only gain genealogies, except
   // when a checkpoint is read, which bumps tree_gen)
@@ -963,6 +971,10 @@ __global__ void k_sum_terms(const ItemDev *items, const NodeRec *nodes, const do
 // bit for bit; every lane repeats the FP64 adds, which only a short run can
 // afford on GB300's FP64 pipe).
 constexpr long long SHORT_RUN_NODES = 1 << 16;
+// Longer runs are copied by the copy engine: on GB300 a kernel read 9.2 MB
+// of the caller's pageable memory at ~175 GB/s but 478 MB at ~70 GB/s,
+// where one pageable copy ran at ~170 GB/s
+constexpr long long PULL_RUN_NODES = 1 << 22;
 __global__ void k_times_short(const ItemDev *items, const NodeRec *nodes, const double *src, size_t src0,
                               const double *src_len, double *t64, float2 *tff, double *len, int lo, int n)
 {
@@ -1157,7 +1169,7 @@ static int upload_times(ima_ctx *c, int n, const int32_t *ci, const int32_t *li,
       c->dev_hi = std::max(c->dev_hi, hi);
       return c->cuda(cudaGetLastError(), "times upload");
     }
-    if (in_place && c->pageable_access) {
+    if (in_place && c->pageable_access && (long long)(n1 - n0) <= PULL_RUN_NODES) {
       // the device reads the run where it lies (times and their float-float
       // form in one coalesced pass), no staging copy; the lengths are read
       // too, or summed from the device times
@@ -1378,6 +1390,12 @@ static int ensure_ff_hky(ima_ctx *c)
 static double hky_bytes(ima_ctx *c, const Batch &b);
 static double sw_bytes(ima_ctx *c, const Batch &b);
 
+static void batch_shape(const Batch &b, int *k)
+{
+  const int v[7] = {b.nis, b.nhky, b.nsw, b.maxn_hky, b.maxs_hky, b.maxn_sw, b.prec};
+  memcpy(k, v, sizeof(v));
+}
+
 static int build_batch(ima_ctx *c, Batch &b, int n, const int32_t *ci, const int32_t *li, const double *u,
                        const double *kappa, const int32_t *edits, const int32_t *ai, int prec)
 {
@@ -1465,6 +1483,15 @@ static int build_batch(ima_ctx *c, Batch &b, int n, const int32_t *ci, const int
   }
   b.hky_bytes = hky_bytes(c, b);
   b.sw_bytes = sw_bytes(c, b);
+  {
+    int key[7];
+    batch_shape(b, key);
+    for (const auto &t : c->tuned)
+      if (!memcmp(t.key, key, sizeof(key))) {
+        b.hky_variant = t.hky;
+        b.sw_variant = t.sw;
+      }
+  }
   b.dl_idx.clear();
   for (int k = b.nis + b.nhky; k < b.n; k++)
     b.dl_idx.push_back(c->items[b.h_req[k].item].al_off + b.h_req[k].ai);
@@ -1798,6 +1825,27 @@ extern "C" int ima_gpu_batch_autotune(ima_ctx *c, int batch, int reps, int *hky_
       cudaStreamSynchronize(c->st);
       cudaGraphExecDestroy(b.graph);
       b.graph = nullptr;
+    }
+  }
+  {
+    ima_ctx::Tuned t;
+    batch_shape(b, t.key);
+    t.hky = b.hky_variant;
+    t.sw = b.sw_variant;
+    bool found = false;
+    for (auto &u : c->tuned)
+      if (!memcmp(u.key, t.key, sizeof(t.key))) {
+        u = t;
+        found = true;
+      }
+    if (!found) c->tuned.push_back(t);
+    if (c->evb.live || c->evkey.valid) {  // the evaluation buffers take the choice if they hold this shape
+      int k2[7];
+      batch_shape(c->evb, k2);
+      if (!memcmp(k2, t.key, sizeof(k2))) {
+        c->evb.hky_variant = t.hky;
+        c->evb.sw_variant = t.sw;
+      }
     }
   }
   if (hky_variant) *hky_variant = b.hky_variant;

@@ -45,7 +45,7 @@ def test_parallel_upload_matches_one_by_one():
     assert np.array_equal(a.eval(ci, li, u, par)[0], b.eval(ci, li, u, par)[0])
 
 
-@pytest.mark.parametrize("kind", ["hky", "is", "is_long"])
+@pytest.mark.parametrize("kind", ["hky", "is", "is_long", "is_huge"])
 def test_set_times_matches_set_genealogies(kind):
     """The times-only upload (long lists over the host threads, short ones
     on the caller's) gives the bits of a full upload with the same times,
@@ -55,8 +55,10 @@ def test_set_times_matches_set_genealogies(kind):
         wl = workloads.make_hky(seed=33, nloci=12, nch=32, ncopies=10, nbases=300)   # 384 pairs
     elif kind == "is":
         wl = workloads.make_is(seed=34)
-    else:
+    elif kind == "is_long":
         wl = workloads.make_is(seed=38, nloci=10, nch=200)   # 78,000 nodes: lengths summed later
+    else:
+        wl = workloads.make_is(seed=41, nloci=10, nch=12000)   # 4.7 M nodes: the copy engine's path
     ci, li = wl.pairs()
     pci, pli, up0, up1, down, tm = wl.packed()
     u, par = wl.u.ravel(), wl.par.ravel()
@@ -94,7 +96,7 @@ def test_set_times_matches_set_genealogies(kind):
         fresh.set_times([0], [0], tm[:nl[0]])
 
 
-@pytest.mark.parametrize("kind", ["sw", "is", "is_long", "sw_long", "mixed_long"])
+@pytest.mark.parametrize("kind", ["sw", "is", "is_long", "sw_long", "mixed_long", "is_huge"])
 def test_eval_times_matches_set_times_then_eval(kind):
     """The one-call re-timing and evaluation gives the bits of set_times
     followed by eval, for a run of pairs in item order (read in place where
@@ -112,8 +114,10 @@ def test_eval_times_matches_set_times_then_eval(kind):
         wl = workloads.make_is(seed=37, nloci=10, nch=200)   # 78,000 nodes
     elif kind == "sw_long":
         wl = workloads.make_sw(seed=39, nloci=24, nch=64, per_pop=30)   # 275,000 nodes
-    else:
+    elif kind == "mixed_long":
         wl = workloads.make_mixed(seed=40, n_hky=12, n_sw=8, nruns=2, cpr=64)
+    else:
+        wl = workloads.make_is(seed=42, nloci=10, nch=12000)   # 4.7 M nodes: the copy engine's path
     ci, li = wl.pairs()
     pci, pli, up0, up1, down, tm = wl.packed()
     u, par = wl.u.ravel(), wl.par.ravel()
