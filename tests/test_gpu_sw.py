@@ -124,3 +124,45 @@ def test_sw_allele_edit_list_gives_update_delta(prec):
     # an invalid entry rejects the whole list
     with pytest.raises(api.ImaError):
         ctx.set_allele_edits([0, 0], [0, 0], [40, 999], [20, 20])
+
+
+@pytest.mark.parametrize("prec", [api.PREC_FAST, api.PREC_FP64])
+def test_sw_linked_markers(prec):
+    """A locus of three linked stepwise markers (L[li].nlinked = 3): each
+    marker ai has its own allele states on the same genealogy, and
+    likelihoodSW(ci, li, ai, u, tr) evaluates one marker with its own rate.
+    Every (chain, marker) request in one batch, against the oracle; dlikeA per
+    marker; an edit of one marker leaves the others' terms unchanged."""
+    rng = np.random.default_rng(29)
+    nch, nm = 6, 3
+    ctx = ctx_with([("sw", 36, nm)], 1, nch)
+    trees_, alle = {}, {}
+    for c in range(nch):
+        t = synth.three_pop_tree(rng, [12, 12, 12], theta=4.0, mig=0.05)
+        ctx.set_genealogy(c, 0, t)
+        trees_[c] = t
+        for a in range(nm):
+            A = synth.sw_alleles(rng, t, float(rng.lognormal(0, 0.4)))
+            ctx.set_alleles(c, 0, A, ai=a)
+            alle[c, a] = A
+    ci = np.repeat(np.arange(nch), nm)
+    ai = np.tile(np.arange(nm), nch)
+    u = rng.lognormal(0, 0.4, size=len(ci))
+    tr = rng.uniform(0.5, 2.0, size=len(ci))
+    res, st = ctx.eval(ci, np.zeros(len(ci), np.int32), u, tr, ai=ai, precision=prec)
+    tol = SW_FAST_ATOL if prec == api.PREC_FAST else 1e-12
+    for k in range(len(ci)):
+        want, dl_want = O.sw_likelihood(alle[ci[k], ai[k]], trees_[ci[k]], u[k], tr[k])
+        assert abs(res[k] - want) <= tol * (1 if prec == api.PREC_FAST else abs(want)), (k, res[k], want)
+    # dlikeA of the last evaluation of each (chain, marker)
+    for k in range(len(ci)):
+        dl = ctx.get_dlikeA(int(ci[k]), 0, int(ai[k]))
+        dl_want = O.sw_likelihood(alle[ci[k], ai[k]], trees_[ci[k]], u[k], tr[k])[1]
+        np.testing.assert_allclose(dl, dl_want, rtol=0 if prec == api.PREC_FAST else 1e-11,
+                                   atol=SW_BRANCH_ATOL if prec == api.PREC_FAST else 1e-11)
+    # an edit of marker 1 on chain 0 changes only that marker's evaluation
+    node = 40
+    ctx.set_allele_edits([0], [0], [node], [int(alle[0, 1][node]) + 2], ai=[1])
+    res2, _ = ctx.eval(ci, np.zeros(len(ci), np.int32), u, tr, ai=ai, precision=prec)
+    changed = np.flatnonzero(res2 != res)
+    assert list(changed) == [1]
