@@ -1437,6 +1437,19 @@ static int build_batch(ima_ctx *c, Batch &b, int n, const int32_t *ci, const int
       r.item = c->item_of(ci[k], li[k]);
       r.ai = ai ? ai[k] : 0;
       for (int q = 0; q < 4; q++) r.e[q] = edits ? edits[4 * k + q] : -1;
+      {
+        const ItemDev &it = c->items[r.item];
+        const LocusDev &Ld = c->loci[it.locus].d;
+        r.part_off = it.part_off;
+        r.node_off = it.node_off;
+        r.sched_off = it.sched_off;
+        r.n = it.n;
+        r.nsites = Ld.nsites;
+        r.totsites = Ld.totsites;
+        r.seq_off = Ld.seq_off;
+        r.mult_off = Ld.mult_off;
+        r.pad = 0;
+      }
       r.u = u[k];
       r.par = kappa ? kappa[k] : 1.0;
       const LocusDev &L = c->loci[li[k]].d;

@@ -46,6 +46,11 @@ struct ReqDev {
   int e[4];
   double u;
   double par;  // HKY: kappa; SW: branch-time scale tr
+  // the item's and locus's fixed offsets and sizes, copied in when the
+  // request is built, so a kernel's first load brings them (the HKY kernel
+  // otherwise chains request -> item -> locus before its tree loads)
+  long long part_off;
+  int node_off, sched_off, n, nsites, totsites, seq_off, mult_off, pad;
 };
 
 // Everything a kernel may read; passed by value.

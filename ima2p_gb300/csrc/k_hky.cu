@@ -304,11 +304,10 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
                                                      int cache_S, int tip_cap)
 {
   extern __shared__ __align__(16) char smem[];
+  // the request carries the item's offsets and sizes, so the tree loads
+  // below wait on this one load only
   const ReqDev R = reqs[blockIdx.x];
-  const ItemDev it = P.items[R.item];
-  const LocusDev L = P.loci[it.locus];
-  const int n = it.n, nl = 2 * n - 1, S = L.nsites, nint = n - 1;
-  const int nlev = P.nlev[R.item];
+  const int n = R.n, nl = 2 * n - 1, S = R.nsites, nint = n - 1;
   // [maxnl][PMS]: 5 coefficients per branch (FF: pairs); FF tip branches
   // hold instead the columns of P(b) for the four observed states, [4][4]
   // pairs, so a tip daughter costs four loads
@@ -337,20 +336,23 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
   const int tid = threadIdx.x;
   const bool full = (R.e[0] == -1);
   for (int k = tid; k < nl; k += BS) {
-    T.nd[k] = P.nodes[it.node_off + k];
-    T.slot[k] = P.slot32[it.node_off + k];
+    T.nd[k] = P.nodes[R.node_off + k];
+    T.slot[k] = P.slot32[R.node_off + k];
     T.dirty[k] = 0;
     T.fresh[k] = full ? 1 : 0;
   }
-  for (int k = tid; k < nint + nlev + 1; k += BS) T.order[k] = P.sched[it.sched_off + k];
+  // the schedule (n-1 + nlev+1 entries, nlev <= n-1) in its 2n-entry slot,
+  // without waiting for the level count
+  for (int k = tid; k < 2 * n; k += BS) T.order[k] = P.sched[R.sched_off + k];
+  const int nlev = P.nlev[R.item];
   T.lstart = T.order + nint;
   if (tips) {
-    const int8_t *sq = P.seq + L.seq_off;
+    const int8_t *sq = P.seq + R.seq_off;
     for (int k = tid; k < n * S; k += BS) stip[k] = sq[k];
   }
   if (tid == 0) {
     const double *pid = P.pi + 4 * (size_t)R.item;
-    const double mu = R.u / ((double)L.totsites * standfactor(pid, R.par));
+    const double mu = R.u / ((double)R.totsites * standfactor(pid, R.par));
     const double kp = R.par - 1.0;
     smu = make_float2((float)mu, (float)(mu - (double)(float)mu));
     skpa = make_float2((float)kp, (float)(kp - (double)(float)kp));
@@ -368,7 +370,7 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
     }
   }
   if (!full) __syncthreads();
-  const float2 *tff = P.tff + it.node_off;
+  const float2 *tff = P.tff + R.node_off;
   for (int c = tid; c < nl; c += BS) {
     int d = T.nd[c].down;
     if (d < 0 || !T.fresh[d]) continue;
@@ -401,10 +403,10 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
   __syncthreads();
 
   const size_t slot_stride = (size_t)nint * S;
-  float4 *part = P.part + it.part_off;
-  float4 *partlo = P.partlo ? P.partlo + it.part_off : nullptr;
-  int32_t *pexp = P.pexp + it.part_off;
-  const int8_t *seq = P.seq + L.seq_off;
+  float4 *part = P.part + R.part_off;
+  float4 *partlo = P.partlo ? P.partlo + R.part_off : nullptr;
+  int32_t *pexp = P.pexp + R.part_off;
+  const int8_t *seq = P.seq + R.seq_off;
   const float pi4[4] = {spi[0].x, spi[1].x, spi[2].x, spi[3].x};
   // warps take (node, 32-pattern chunk) pairs of a level in turn, so a warp
   // works on one node at a time and its children's coefficients stay in
@@ -536,7 +538,7 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
   // root: sum_i mult_i * (log(sum_j pi_j L_j) + scale_i)
   const int root = T.order[nint - 1];
   const int rs = T.fresh[root] ? 1 - T.slot[root] : T.slot[root];
-  const int32_t *mult = P.mult + L.mult_off;
+  const int32_t *mult = P.mult + R.mult_off;
   double acc = 0.0;
   long long acce = 0;
   for (int i = tid; i < S; i += BS) {
@@ -582,7 +584,7 @@ __global__ void __launch_bounds__(BS, MINB) k_hky_fast(Pools P, const ReqDev *re
     red_e[tid >> 5] = acce;
   }
   // recomputed marks for the commit step
-  for (int k = tid; k < nl; k += BS) P.fresh32[it.node_off + k] = (k >= n) ? T.fresh[k] : 0;
+  for (int k = tid; k < nl; k += BS) P.fresh32[R.node_off + k] = (k >= n) ? T.fresh[k] : 0;
   __syncthreads();
   if (tid == 0) {
     double s = 0.0;
