@@ -24,10 +24,11 @@ PREC_FAST, PREC_FP64, PREC_FP32 = 0, 1, 2
 EVAL_OK, EVAL_IS_REJECT, EVAL_IS_FAIL, EVAL_SW_ZERO = 0, 1, 2, 3
 SURF_FAST, SURF_FP64, SURF_COMPAT, SURF_TC = 0, 1, 2, 3
 K_IS, K_IS_SUMLOGK, K_HKY_FAST, K_HKY_FP64, K_SW_FAST, K_SW_FP64, K_SWAP, K_SURF_FAST, \
-    K_SURF_FP64, K_SURF_COMPAT, K_SURF_TC, K_MARGIN, K_TREEWEIGHT, K_TREE_PROB, K_POPMIG, K_HKY_FP32, K_TIMES = range(17)
+    K_SURF_FP64, K_SURF_COMPAT, K_SURF_TC, K_MARGIN, K_TREEWEIGHT, K_TREE_PROB, K_POPMIG, K_HKY_FP32, K_TIMES, \
+    K_UG = range(18)
 KERNEL_NAMES = ["is", "is_sumlogk", "hky_fast", "hky_fp64", "sw_fast", "sw_fp64", "swap",
                 "surf_fast", "surf_fp64", "surf_compat", "surf_tc", "margin", "treeweight", "tree_prob",
-                "popmig", "hky_fp32"]
+                "popmig", "hky_fp32", "times", "ug"]
 REJECT_IS = -1000000000.0
 
 # every symbol the header declares (checked by tests/test_abi.py)
@@ -54,7 +55,8 @@ EXPORTS = [
     "ima_gpu_set_locus_pops", "ima_gpu_set_labels", "ima_gpu_get_times", "ima_gpu_rubber_band",
     "ima_gpu_chain_weights", "ima_gpu_changet_ry1_sweep", "ima_gpu_get_probg", "ima_gpu_get_split_times",
     "ima_gpu_checkpoint_write", "ima_gpu_checkpoint_read", "ima_gpu_popmig", "ima_gpu_popmig_curves",
-    "ima_gpu_findmarginpeaks", "ima_gpu_changet_ry1_sweep_mt",
+    "ima_gpu_findmarginpeaks", "ima_gpu_changet_ry1_sweep_mt", "ima_ug_rng_seed",
+    "ima_gpu_updategenealogy_sweep", "ima_gpu_get_genealogy",
 ]
 
 
@@ -105,6 +107,17 @@ class MT19937(C.Structure):
 
     def uniform(self):
         return load_library().ima_mt19937_uniform(C.byref(self))
+
+
+class UgRng(C.Structure):
+    """A chain's generators for the genealogy update (ima_ug_rng): the
+    MT19937 of uniform(), normdev's cached deviate and bitran's register."""
+    _fields_ = [("mt", MT19937), ("iset", C.c_int32), ("gset", C.c_double), ("iseed", C.c_uint64)]
+
+    def __init__(self, seed=None):
+        super().__init__()
+        if seed is not None:
+            load_library().ima_ug_rng_seed(C.byref(self), int(seed))
 
 
 # double uniform(void *arg): the caller's generator, drawn one value at a time
@@ -180,6 +193,9 @@ def _declare(L):
         "ima_gpu_popmig": (I, [P, I, P, P, P, P, P, P, I, P]),
         "ima_gpu_popmig_curves": (I, [P, I, P, P, I, P, P, P, I, P, P, P]),
         "ima_gpu_changet_ry1_sweep_mt": (I, [P, I, P, P, P, P, P, D, P, P, I, P, P, P, P]),
+        "ima_ug_rng_seed": (None, [P, C.c_int32]),
+        "ima_gpu_updategenealogy_sweep": (I, [P, I, P, P, I, P, P, D, I, P, P, P, P]),
+        "ima_gpu_get_genealogy": (I, [P, I, I, P, P, P, P, P]),
         "ima_gpu_findmarginpeaks": (I, [P, P, P, P, P, P, I, P, P, P, P, P, P, P, P, P, P, P, C.POINTER(I)]),
         "ima_gpu_swapchains": (I, [P, I, I, P, I, C.c_uint64, P, P]),
         "ima_gpu_get_swapcounts": (I, [P, I, P, P]),
@@ -683,6 +699,32 @@ class Context:
             _ptr(kap) if kap is not None else None, int(precision), _ptr(acc), _ptr(pdgsum), _ptr(probg),
             _ptr(newt)))
         return acc.astype(bool), pdgsum, probg, newt
+
+    def updategenealogy_sweep(self, chains, tvals, nsweeps, rngs, u, kappa=None, gbeta=1.0, precision=PREC_FP64):
+        """nsweeps device genealogy updates of every locus of the chains (the
+        no-migration model); rngs: a UgRng per chain, advanced in place.
+        Returns (accepted, topology changes) [nch][nloci] and p(G) [nch]."""
+        chains = _i32(chains)
+        n, nl = len(chains), len(self.loci)
+        tvals = _f64(np.asarray(tvals, np.float64).reshape(n, -1))
+        u = _f64(np.asarray(u, np.float64).reshape(-1))
+        kap = _f64(np.asarray(kappa, np.float64).reshape(-1)) if kappa is not None else None
+        arr = (UgRng * n)(*rngs)
+        acc, top, probg = np.zeros((n, nl), np.int32), np.zeros((n, nl), np.int32), np.zeros(n)
+        self._ck(self.lib.ima_gpu_updategenealogy_sweep(
+            self.h, n, _ptr(chains), _ptr(tvals), int(nsweeps), _ptr(u), _ptr(kap) if kap is not None else None,
+            float(gbeta), int(precision), C.cast(arr, P), _ptr(acc), _ptr(top), _ptr(probg)))
+        for k in range(n):
+            C.memmove(C.addressof(rngs[k]), C.addressof(arr[k]), C.sizeof(UgRng))
+        return acc, top, probg
+
+    def get_genealogy(self, ci, li, nlines):
+        """The resident genealogy of a chain-locus: (up0, up1, down, time, pop)."""
+        up0, up1, down, pop = (np.zeros(nlines, np.int32) for _ in range(4))
+        t = np.zeros(nlines)
+        self._ck(self.lib.ima_gpu_get_genealogy(self.h, int(ci), int(li), _ptr(up0), _ptr(up1), _ptr(down), _ptr(t),
+                                                _ptr(pop)))
+        return up0, up1, down, t, pop
 
     def surface_append_tree_rows(self, groups):
         """Append the gsampinf rows of these chains (last tree_prob) to the

@@ -18,9 +18,9 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libima2p_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-# k_treeweight.cu restates the reference's FP64 sums term by term: without
-# FMA contraction its adds and multiplies round as the host's do
-NOFMAD_FILES = {"k_treeweight.cu", "k_popmig.cu"}
+# k_treeweight.cu, k_popmig.cu and k_updgen.cu restate the reference's FP64
+# arithmetic term by term: without FMA contraction it rounds as the host's does
+NOFMAD_FILES = {"k_treeweight.cu", "k_popmig.cu", "k_updgen.cu"}
 NOFMAD = ["-fmad=false"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
 

@@ -308,6 +308,11 @@ struct ima_ctx {
   void *d_rsel = nullptr;
   size_t rsel_cap = 0;
   int dev_lo = INT32_MAX, dev_hi = -1;  // items whose device times/lengths are newer than the mirror
+  int topo_lo = INT32_MAX, topo_hi = -1;  // items whose device topology and schedule are newer too
+  // the genealogy update's buffers and per-locus evaluation requests
+  void *d_ug = nullptr;
+  size_t ug_cap = 0;
+  std::vector<Batch> ugb;
   // items whose tree lengths are still to be summed from their device times
   // (re-timings without lengths): done when a reader needs them
   int lpend_lo = INT32_MAX, lpend_hi = -1;
@@ -473,6 +478,7 @@ extern "C" void ima_gpu_destroy(ima_ctx *c)
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->st);
   c->batches.push_back(c->evb);
+  for (auto &b : c->ugb) c->batches.push_back(b);
   for (auto &b : c->batches) {
     if (b.graph) cudaGraphExecDestroy(b.graph);
     if (b.sgraph) cudaGraphExecDestroy(b.sgraph);
@@ -494,7 +500,7 @@ extern "C" void ima_gpu_destroy(ima_ctx *c)
                   c->d_mscratch, c->d_tw, c->d_logfact, c->d_twerr, c->d_twin, c->d_twout, c->d_tpbuf,
                   c->d_pop, c->d_moff, c->d_inode_off, c->d_gl, c->d_gt, c->d_moff_start, c->d_bcnt, c->d_bicnt,
                   c->d_mig_p, c->d_rsamp, c->d_mbase, c->d_mig_t, c->d_tvr, c->d_len_hold, c->d_rhlog,
-                  c->d_rh2, c->d_rsel, c->d_is_site, c->d_is_valid, c->d_lterm};
+                  c->d_rh2, c->d_rsel, c->d_is_site, c->d_is_valid, c->d_lterm, c->d_ug};
   for (void *p : devs)
     if (p) cudaFree(p);
   void *hosts[] = {c->h_nodes, c->h_t64, c->h_sched, c->h_nlev, c->h_len, c->h_pi, c->h_al};
@@ -699,15 +705,30 @@ static int ensure_lengths(ima_ctx *c);
 static int sync_mirror(ima_ctx *c)
 {
   int r = ensure_lengths(c);
+  if (c->topo_hi >= 0) {
+    c->dev_lo = std::min(c->dev_lo, c->topo_lo);
+    c->dev_hi = std::max(c->dev_hi, c->topo_hi);
+  }
   if (r || c->dev_hi < 0) return r;
   const ItemDev &a = c->items[c->dev_lo], &b = c->items[c->dev_hi];
   const size_t n0 = a.node_off, n1 = (size_t)b.node_off + 2 * b.n - 1;
   r = c->cuda(cudaMemcpyAsync(c->h_t64 + n0, c->d_t64 + n0, (n1 - n0) * sizeof(double), cudaMemcpyDeviceToHost, c->st), "mirror");
   r = r ? r : c->cuda(cudaMemcpyAsync(c->h_len + c->dev_lo, c->d_len + c->dev_lo, (size_t)(c->dev_hi - c->dev_lo + 1) * sizeof(double),
                                       cudaMemcpyDeviceToHost, c->st), "mirror");
+  if (c->topo_hi >= 0) {  // genealogies the device changed: topology and level schedules too
+    const ItemDev &ta = c->items[c->topo_lo], &tb = c->items[c->topo_hi];
+    const size_t m0 = ta.node_off, m1 = (size_t)tb.node_off + 2 * tb.n - 1;
+    const size_t s0 = ta.sched_off, s1 = (size_t)tb.sched_off + 2 * tb.n + 2;
+    const size_t l0 = c->topo_lo, l1 = (size_t)c->topo_hi + 1;
+    r = r ? r : c->cuda(cudaMemcpyAsync(c->h_nodes + m0, c->d_nodes + m0, (m1 - m0) * sizeof(NodeRec), cudaMemcpyDeviceToHost, c->st), "mirror");
+    r = r ? r : c->cuda(cudaMemcpyAsync(c->h_sched + s0, c->d_sched + s0, (s1 - s0) * sizeof(int16_t), cudaMemcpyDeviceToHost, c->st), "mirror");
+    r = r ? r : c->cuda(cudaMemcpyAsync(c->h_nlev + l0, c->d_nlev + l0, (l1 - l0) * sizeof(int32_t), cudaMemcpyDeviceToHost, c->st), "mirror");
+  }
   r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "mirror");
   c->dev_lo = INT32_MAX;
   c->dev_hi = -1;
+  c->topo_lo = INT32_MAX;
+  c->topo_hi = -1;
   return r;
 }
 
@@ -3319,9 +3340,16 @@ extern "C" int ima_gpu_treeweight(ima_ctx *c, int ngen, const int32_t *node_off,
 // group_end[i] (group_end null: group_off[i+1])
 // defer: no error check, no copies back and no synchronisation here (the
 // caller checks the error word after a later synchronisation)
+// device copies of tree_prob_run's per-group outputs, valid until the next call
+struct TpDev {
+  int32_t *sc = nullptr;  // [groups][T + M] summed counts
+  double *sd = nullptr;   // [groups][2T + M] summed fc, hcc, fm
+  double *q = nullptr;    // [groups][nth] theta integrals
+};
+
 static int tree_prob_run(ima_ctx *c, int ngroups, const int32_t *group_off, const int32_t *group_end,
                          const double *pdg, const int32_t *group_tv, double *probg, double *q, double *m,
-                         float *rows, double **d_probg = nullptr, bool defer = false)
+                         float *rows, double **d_probg = nullptr, bool defer = false, TpDev *dev = nullptr)
 {
   if (!c->tw_ready || c->tw_ngen < 1) return c->fail(IMA_ERR_STATE, "call ima_gpu_treeweight first");
   if (ngroups < 1 || !group_off) return c->fail(IMA_ERR_ARG, "tree_prob: bad argument");
@@ -3394,6 +3422,11 @@ static int tree_prob_run(ima_ctx *c, int ngroups, const int32_t *group_off, cons
   c->tp_ngroups = ngroups;
   c->tp_rowlen = rowlen;
   if (d_probg) *d_probg = a.probg;
+  if (dev) {
+    dev->sc = a.sc;
+    dev->sd = a.sd;
+    dev->q = a.q;
+  }
   auto down = [&](void *dst, const void *src, size_t bytes) {
     if (!r && dst && bytes) r = c->cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->st), "tree_prob outputs");
   };
@@ -3748,7 +3781,7 @@ extern "C" int ima_gpu_rubber_band(ima_ctx *c, int nch, const int32_t *chains, c
 }
 
 static int chain_weights_run(ima_ctx *c, int nch, const int32_t *chains, const double *tvals, double *probg,
-                             double *q, double *m, double **d_probg, bool defer = false)
+                             double *q, double *m, double **d_probg, bool defer = false, TpDev *dev = nullptr)
 {
   int r = IMA_OK;
   const TwModel &h = c->h_tw;
@@ -3850,7 +3883,7 @@ static int chain_weights_run(ima_ctx *c, int nch, const int32_t *chains, const d
   }
   std::vector<double> pg(nch);
   return tree_prob_run(c, nch, goff.data(), gend.data(), nullptr, chains, (probg || defer) ? probg : pg.data(), q, m,
-                       nullptr, d_probg, defer);
+                       nullptr, d_probg, defer, dev);
 }
 
 extern "C" int ima_gpu_chain_weights(ima_ctx *c, int nch, const int32_t *chains, const double *tvals,
@@ -4012,6 +4045,288 @@ extern "C" int ima_gpu_changet_ry1_sweep_mt(ima_ctx *c, int nch, const int32_t *
   return ima_gpu_changet_ry1_sweep(c, nch, chains, period, oldt.data(), newt.data(), tu.data(), td.data(), lhu.data(),
                                    lhd.data(), logU.data(), gbeta, tv.data(), u, kappa, precision, accept, pdgsum,
                                    probg);
+}
+
+// ======================================================================
+// the genealogy update of the no-migration model (k_updgen.cu)
+extern "C" int ima_gpu_get_genealogy(ima_ctx *c, int ci, int li, int32_t *up0, int32_t *up1, int32_t *down,
+                                     double *time, int32_t *pop)
+{
+  if (!c) return IMA_ERR_ARG;
+  if (!c->valid(ci, li)) return c->fail(IMA_ERR_ARG, "chain %d locus %d out of range", ci, li);
+  const int item = c->item_of(ci, li);
+  if (!c->has_tree[item]) return c->fail(IMA_ERR_STATE, "chain %d locus %d has no genealogy", ci, li);
+  if (pop && !c->has_labels.size()) return c->fail(IMA_ERR_STATE, "no population labels");
+  cudaSetDevice(c->device);
+  const ItemDev &it = c->items[item];
+  const int nl = 2 * it.n - 1;
+  std::vector<NodeRec> nd(nl);
+  int r = c->cuda(cudaMemcpyAsync(nd.data(), c->d_nodes + it.node_off, nl * sizeof(NodeRec), cudaMemcpyDeviceToHost, c->st), "genealogy");
+  if (time) r = r ? r : c->cuda(cudaMemcpyAsync(time, c->d_t64 + it.node_off, nl * 8ul, cudaMemcpyDeviceToHost, c->st), "genealogy");
+  if (pop) r = r ? r : c->cuda(cudaMemcpyAsync(pop, c->d_pop + it.node_off, nl * 4ul, cudaMemcpyDeviceToHost, c->st), "genealogy");
+  r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "genealogy");
+  if (r) return r;
+  for (int k = 0; k < nl; k++) {
+    if (up0) up0[k] = nd[k].up0;
+    if (up1) up1[k] = nd[k].up1;
+    if (down) down[k] = nd[k].down;
+  }
+  return IMA_OK;
+}
+
+extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t *chains, const double *tvals,
+                                             int nsweeps, const double *u, const double *kappa, double gbeta,
+                                             int precision, ima_ug_rng *rng, int32_t *accepted, int32_t *topology,
+                                             double *probg)
+{
+  if (!c || nch < 1 || !chains || !tvals || nsweeps < 0 || !u || !rng) return IMA_ERR_ARG;
+  if (!c->tw_ready) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_popmodel first");
+  const TwModel &h = c->h_tw;
+  if (!h.nomig) return c->fail(IMA_ERR_STATE, "the genealogy update is built for the no-migration model (nomig = 1)");
+  const int nl = c->nloci, nsplit = h.npops - 1, T = h.T, nth = h.nth, ni = c->nitems;
+  int maxn = 0, anyhky = 0;
+  for (int li = 0; li < nl; li++) {
+    const LocusDev &L = c->loci[li].d;
+    if (L.model == IMA_MODEL_SW) return c->fail(IMA_ERR_ARG, "locus %d: the genealogy update takes IS and HKY loci", li);
+    maxn = std::max(maxn, L.n);
+    anyhky |= (L.model == IMA_MODEL_HKY);
+  }
+  int r = chains_ready(c, nch, chains);
+  if (r) return r;
+  for (int k = 0; k < nch; k++)
+    for (int li = 0; li < nl; li++)
+      if (c->h_mcnt[c->item_of(chains[k], li)])
+        return c->fail(IMA_ERR_STATE, "chain %d locus %d holds migration events", chains[k], li);
+  // a full evaluation, committed: the partials and G.pdg of the genealogies
+  // the sweep starts from
+  const size_t np = (size_t)nch * nl;
+  std::vector<int32_t> ci(np), li(np), st(np);
+  std::vector<double> kap(np, 1.0), res(np);
+  for (int k = 0; k < nch; k++)
+    for (int l = 0; l < nl; l++) {
+      ci[(size_t)k * nl + l] = chains[k];
+      li[(size_t)k * nl + l] = l;
+      if (kappa) kap[(size_t)k * nl + l] = kappa[(size_t)k * nl + l];
+    }
+  r = ima_gpu_eval(c, (int)np, ci.data(), li.data(), u, kap.data(), nullptr, nullptr, precision, res.data(), st.data());
+  if (r) return r;
+  for (size_t k = 0; k < np; k++)
+    if (st[k] != IMA_EVAL_OK)
+      return c->fail(IMA_ERR_DATA, "chain %d locus %d: the likelihood rejects the current genealogy", ci[k], li[k]);
+  {
+    std::vector<uint8_t> ones(np, 1);
+    r = commit(c, (int)np, ci.data(), li.data(), ones.data(), true, true);
+    if (r) return r;
+  }
+  // the chains' weights summed afresh and their p(G), made resident
+  TpDev tpd;
+  std::vector<double> pg(nch);
+  r = chain_weights_run(c, nch, chains, tvals, pg.data(), nullptr, nullptr, nullptr, false, &tpd);
+  if (r) return r;
+  {
+    std::vector<double> all(c->nchains);
+    r = c->cuda(cudaMemcpyAsync(all.data(), c->d_probg, c->nchains * 8ul, cudaMemcpyDeviceToHost, c->st), "probg");
+    r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "probg");
+    for (int k = 0; k < nch; k++) all[chains[k]] = pg[k];
+    r = r ? r : c->cuda(cudaMemcpyAsync(c->d_probg, all.data(), c->nchains * 8ul, cudaMemcpyHostToDevice, c->st), "probg");
+    r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "probg");
+    if (r) return r;
+  }
+  // event lists of the proposed genealogies (no migrations: coalescences and splits)
+  std::vector<long long> evoff(ni + 1, 0);
+  long long Emax = 0;
+  {
+    std::vector<int32_t> ev(ni, 0);
+    for (int k = 0; k < nch; k++)
+      for (int l = 0; l < nl; l++) {
+        const int item = c->item_of(chains[k], l);
+        ev[item] = c->items[item].n - 1 + nsplit;
+        Emax = std::max(Emax, (long long)ev[item]);
+      }
+    for (int i = 0; i < ni; i++) evoff[i + 1] = evoff[i] + ev[i];
+  }
+  int P = 32;
+  while (P < Emax) P <<= 1;
+  if (!tw_fits(P)) return c->fail(IMA_ERR_TOO_LARGE, "a genealogy has %lld events", Emax);
+  // the weights kernel writes every migration cell of the model, nomig or not
+  const size_t Etot = (size_t)evoff[ni], M1 = std::max(1, h.M), mx = 2 * (size_t)maxn;
+  const size_t bytes = carve_size({nch * sizeof(ima_ug_rng), nch * 4ul, np * 4, np * 4, nch * mx * sizeof(NodeRec),
+                                   nch * mx * 8, nch * mx * 4, nch * mx * 2, nch * 8ul, nch * 4ul, nch * 8ul, nch * 8ul,
+                                   8, nch * T * 4ul, nch * T * 8ul, nch * T * 8ul, nch * (size_t)nth * 8, np * 4, np * 4,
+                                   ni * T * 4ul, ni * M1 * 4, ni * 4ul, ni * T * 8ul, ni * T * 8ul, ni * M1 * 8,
+                                   2ul * ni * 8, (ni + 1) * 8ul, Etot * 8, Etot * 4, ni * 4ul});
+  r = grow(c, &c->d_ug, &c->ug_cap, bytes, "genealogy update buffers");
+  if (r) return r;
+  Carve cv{static_cast<char *>(c->d_ug)};
+  UgArgs a{};
+  a.nch = nch;
+  a.nloci = nl;
+  a.maxn = maxn;
+  a.nsplit = nsplit;
+  a.rng = cv.take<ima_ug_rng>(nch);
+  int32_t *d_chains = cv.take<int32_t>(nch);
+  int32_t *d_reqof = cv.take<int32_t>(np);
+  int32_t *d_perm = cv.take<int32_t>(np);
+  a.bk_nodes = cv.take<NodeRec>(nch * mx);
+  a.bk_t = cv.take<double>(nch * mx);
+  a.bk_pop = cv.take<int32_t>(nch * mx);
+  a.bk_sched = cv.take<int16_t>(nch * mx);
+  a.bk_len = cv.take<double>(nch);
+  a.bk_nlev = cv.take<int32_t>(nch);
+  a.prop = reinterpret_cast<int32_t *>(cv.take<double>(nch));
+  a.slidew = cv.take<double>(nch);
+  a.err = cv.take<int32_t>(2);
+  a.ag_cc = cv.take<int32_t>(nch * (size_t)T);
+  a.ag_fc = cv.take<double>(nch * (size_t)T);
+  a.ag_hcc = cv.take<double>(nch * (size_t)T);
+  a.qint = cv.take<double>(nch * (size_t)nth);
+  a.nacc = cv.take<int32_t>(np);
+  a.ntopo = cv.take<int32_t>(np);
+  // the proposed genealogies' weights (treeweight's outputs), by item
+  TwArgs w{};
+  w.cc = cv.take<int32_t>(ni * (size_t)T);
+  w.mc = cv.take<int32_t>(ni * M1);
+  w.mignum = cv.take<int32_t>(ni);
+  w.hcc = cv.take<double>(ni * (size_t)T);
+  w.fc = cv.take<double>(ni * (size_t)T);
+  w.fm = cv.take<double>(ni * M1);
+  w.lens = cv.take<double>(2ul * ni);
+  long long *d_evoff = cv.take<long long>(ni + 1);
+  w.ev_t = cv.take<double>(Etot);
+  w.ev_c = cv.take<uint32_t>(Etot);
+  w.ev_n = cv.take<int32_t>(ni);
+  w.ngen = nch;
+  w.P = P;
+  w.model = c->d_tw;
+  w.ev_off = d_evoff;
+  w.node_off = c->d_inode_off;
+  w.nodes = c->d_nodes;
+  w.time = c->d_t64;
+  w.pop = c->d_pop;
+  w.mig_off = c->d_moff;
+  w.moff_start = c->d_moff_start;
+  w.mbase = c->d_mbase;
+  w.mig_t = c->d_mig_t;
+  w.mig_p = c->d_mig_p;
+  w.gen_locus = c->d_gl;
+  w.gen_tv = c->d_gt;
+  w.tvals = c->d_tvr;
+  w.hlog = c->d_rhlog;
+  w.h2term = c->d_rh2;
+  w.samppop = c->d_rsamp;
+  w.len_out = c->d_len;
+  w.err = c->d_twerr;
+  // per-locus evaluation requests: the listed chains, full evaluations whose
+  // HKY edits the proposal fills in
+  if ((int)c->ugb.size() < nl) c->ugb.resize(nl);
+  std::vector<int32_t> reqof(np), perm(np);
+  for (int l = 0; l < nl && !r; l++) {
+    Batch &b = c->ugb[l];
+    std::vector<int32_t> lli(nch, l);
+    std::vector<double> lu(nch), lk(nch);
+    for (int k = 0; k < nch; k++) {
+      lu[k] = u[(size_t)k * nl + l];
+      lk[k] = kap[(size_t)k * nl + l];
+      perm[(size_t)l * nch + k] = c->item_of(chains[k], l);
+    }
+    r = build_batch(c, b, nch, chains, lli.data(), lu.data(), lk.data(), nullptr, nullptr, precision);
+    r = r ? r : init_sumlogk(c, b);
+    for (int k = 0; k < nch && !r; k++) reqof[(size_t)l * nch + b.order[k]] = k;
+  }
+  if (r) return r;
+  r = c->cuda(cudaMemcpyAsync(a.rng, rng, nch * sizeof(ima_ug_rng), cudaMemcpyHostToDevice, c->st), "generators");
+  r = r ? r : c->cuda(cudaMemcpyAsync(d_chains, chains, nch * 4ul, cudaMemcpyHostToDevice, c->st), "chains");
+  r = r ? r : c->cuda(cudaMemcpyAsync(d_reqof, reqof.data(), np * 4, cudaMemcpyHostToDevice, c->st), "requests");
+  r = r ? r : c->cuda(cudaMemcpyAsync(d_perm, perm.data(), np * 4, cudaMemcpyHostToDevice, c->st), "genealogy lists");
+  r = r ? r : c->cuda(cudaMemcpyAsync(d_evoff, evoff.data(), (ni + 1) * 8ul, cudaMemcpyHostToDevice, c->st), "events");
+  r = r ? r : c->cuda(cudaMemsetAsync(a.err, 0, 8, c->st), "errors");
+  r = r ? r : c->cuda(cudaMemsetAsync(c->d_twerr, 0, 8, c->st), "errors");
+  r = r ? r : c->cuda(cudaMemsetAsync(a.nacc, 0, np * 4, c->st), "counts");
+  r = r ? r : c->cuda(cudaMemsetAsync(a.ntopo, 0, np * 4, c->st), "counts");
+  // the chains' summed weights and integrals from the fresh computation
+  // (nomig: [groups][T] counts, [groups][2T] fc then hcc)
+  r = r ? r : c->cuda(cudaMemcpyAsync(a.ag_cc, tpd.sc, nch * (size_t)T * 4, cudaMemcpyDeviceToDevice, c->st), "sums");
+  r = r ? r : c->cuda(cudaMemcpy2DAsync(a.ag_fc, T * 8ul, tpd.sd, 2 * T * 8ul, T * 8ul, nch, cudaMemcpyDeviceToDevice, c->st), "sums");
+  r = r ? r : c->cuda(cudaMemcpy2DAsync(a.ag_hcc, T * 8ul, tpd.sd + T, 2 * T * 8ul, T * 8ul, nch, cudaMemcpyDeviceToDevice, c->st), "sums");
+  r = r ? r : c->cuda(cudaMemcpyAsync(a.qint, tpd.q, nch * (size_t)nth * 8, cudaMemcpyDeviceToDevice, c->st), "sums");
+  if (r) return r;
+  a.chains = d_chains;
+  a.items = c->d_items;
+  a.nodes = c->d_nodes;
+  a.t64 = c->d_t64;
+  a.tff = c->d_tff;
+  a.pop = c->d_pop;
+  a.sched = c->d_sched;
+  a.nlev = c->d_nlev;
+  a.len = c->d_len;
+  a.is_valid = c->d_is_valid;
+  a.model = c->d_tw;
+  a.tvals = c->d_tvr;
+  a.cc = c->tw_cc;
+  a.fc = c->tw_fc;
+  a.hcc = c->tw_hcc;
+  a.ncc = w.cc;
+  a.nfc = w.fc;
+  a.nhcc = w.hcc;
+  a.probg = c->d_probg;
+  a.pdg = c->d_pdg;
+  a.beta = c->d_beta;
+  a.gbeta = gbeta;
+  a.logfact = c->d_logfact;
+  a.slot32 = c->d_slot32;
+  a.fresh32 = c->d_fresh32;
+  a.slot64 = c->d_slot64;
+  a.fresh64 = c->d_fresh64;
+  // the steps: one locus of every listed chain at a time
+  for (int s = 0; s < nsweeps && !r; s++)
+    for (int l = 0; l < nl && !r; l++) {
+      Batch &b = c->ugb[l];
+      a.locus = l;
+      a.hky = c->loci[l].d.model == IMA_MODEL_HKY;
+      a.req = b.d_req;
+      a.req_of = d_reqof + (size_t)l * nch;
+      a.res = b.d_res;
+      a.st = b.d_st;
+      c->launch(IMA_K_UG, 0.0, [&] { launch_ug_propose(a, c->st); });
+      w.perm = d_perm + (size_t)l * nch;
+      int lr = 0;
+      c->launch(IMA_K_TREEWEIGHT, 0.0, [&] { lr = launch_treeweight(w, h, c->st); });
+      if (lr < 0) return c->fail(IMA_ERR_TOO_LARGE, "treeweight: shared memory for %d events", P);
+      c->launches += lr - 1;
+      enqueue(c, b);
+      c->launch(IMA_K_UG, 0.0, [&] { launch_ug_decide(a, c->st); });
+      r = c->cuda(cudaGetLastError(), "genealogy update launch");
+    }
+  // the device's genealogies are newer than the mirror from here on
+  for (int k = 0; k < nch; k++) {
+    c->topo_lo = std::min(c->topo_lo, chains[k] * nl);
+    c->topo_hi = std::max(c->topo_hi, chains[k] * nl + nl - 1);
+  }
+  dev_newer(c, nch, chains);
+  c->tw_ngen = 0;  // the weights of the last weights call no longer describe these genealogies
+  c->tw_valid.clear();
+  if (r) return r;
+  int32_t e[2] = {0, 0};
+  r = c->cuda(cudaMemcpyAsync(e, a.err, 8, cudaMemcpyDeviceToHost, c->st), "genealogy update");
+  r = r ? r : c->cuda(cudaMemcpyAsync(rng, a.rng, nch * sizeof(ima_ug_rng), cudaMemcpyDeviceToHost, c->st), "generators");
+  if (accepted) r = r ? r : c->cuda(cudaMemcpyAsync(accepted, a.nacc, np * 4, cudaMemcpyDeviceToHost, c->st), "counts");
+  if (topology) r = r ? r : c->cuda(cudaMemcpyAsync(topology, a.ntopo, np * 4, cudaMemcpyDeviceToHost, c->st), "counts");
+  r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "genealogy update");
+  r = r ? r : tw_check_err(c, "genealogy update weights");
+  if (r) return r;
+  if (e[0]) {
+    static const char *why[] = {"", "a slide that did not end", "a root time beyond TIMEMAX",
+                                "an IS genealogy with a site no edge can carry", "an integral term the reference rejects",
+                                "a genealogy that is not a tree"};
+    return c->fail(IMA_ERR_DATA, "genealogy update: listed chain %d: %s", e[1], why[e[0] < 6 ? e[0] : 0]);
+  }
+  if (probg) {
+    std::vector<double> all(c->nchains);
+    r = c->cuda(cudaMemcpyAsync(all.data(), c->d_probg, c->nchains * 8ul, cudaMemcpyDeviceToHost, c->st), "probg");
+    r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "probg");
+    for (int k = 0; !r && k < nch; k++) probg[k] = all[chains[k]];
+  }
+  return r;
 }
 
 // ======================================================================
@@ -4257,6 +4572,8 @@ extern "C" int ima_gpu_checkpoint_read(ima_ctx *c, const char *path, ima_mt19937
   c->tw_valid.clear();
   c->dev_lo = INT32_MAX;  // the file is authoritative now
   c->dev_hi = -1;
+  c->topo_lo = INT32_MAX;
+  c->topo_hi = -1;
   c->lpend_lo = INT32_MAX;
   c->lpend_hi = -1;
   c->dirty_lo = 0;        // upload everything with the next flush

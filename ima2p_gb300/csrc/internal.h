@@ -297,6 +297,59 @@ struct RyArgs {
   double *pdgsum;                          // [nch] the chain's likelihood sum after the decision
 };
 int launch_ry_decide(const RyArgs &a, cudaStream_t st);
+// The genealogy update updategenealogy (update_gtree.cpp:723-966) of the
+// no-migration model on resident genealogies, one locus of every listed
+// chain per step (k_updgen.cu): a warp per chain proposes (edge, slide,
+// reattachment), the weights and the likelihood of the proposed genealogies
+// run as batches, and a warp per chain decides, then commits or restores.
+struct UgArgs {
+  int nch, nloci, locus, maxn, nsplit, hky;
+  const int32_t *chains;                   // [nch]
+  const ItemDev *items;
+  NodeRec *nodes;
+  double *t64;
+  float2 *tff;
+  int32_t *pop;
+  int16_t *sched;
+  int32_t *nlev;
+  double *len;
+  uint8_t *is_valid;
+  const TwModel *model;
+  const double *tvals;                     // [nchains][nsplit]
+  ima_ug_rng *rng;                         // [nch] the listed chains' generators
+  ReqDev *req;                             // the locus's evaluation requests
+  const int32_t *req_of;                   // [nch] request of each listed chain
+  // per listed chain: the genealogy before the proposal, for a rejection
+  NodeRec *bk_nodes;                       // [nch][2 maxn]
+  double *bk_t;                            // [nch][2 maxn]
+  int32_t *bk_pop;                         // [nch][2 maxn]
+  int16_t *bk_sched;                       // [nch][2 maxn]
+  double *bk_len;                          // [nch]
+  int32_t *bk_nlev;                        // [nch]
+  int32_t *prop;                           // [nch][2]: topology changed, tmrca changed
+  double *slidew;                          // [nch] the slide's Hastings term
+  int32_t *err;                            // {code, listed chain} of the first failure
+  // the decision
+  const double *res;                       // the batch's results
+  const int32_t *st;                       // and status words
+  const int32_t *ncc;                      // proposed genealogies' weights [items][T]
+  const double *nfc, *nhcc;
+  int32_t *cc;                             // committed weights [items][T]
+  double *fc, *hcc;
+  int32_t *ag_cc;                          // the chains' summed weights [nch][T]
+  double *ag_fc, *ag_hcc;
+  double *qint;                            // [nch][nth] the chains' integrals
+  double *probg;                           // [nchains] resident p(G)
+  double *pdg;                             // [items] resident log P(D|G)
+  const double *beta;                      // [nchains]
+  double gbeta;
+  const double *logfact;
+  uint8_t *slot32, *fresh32, *slot64, *fresh64;
+  int32_t *nacc, *ntopo;                   // [nch][nloci] accepted proposals, accepted topology changes
+};
+enum { UG_E_SLIDE = 1, UG_E_ROOTTIME = 2, UG_E_ISFAIL = 3, UG_E_TERM = 4, UG_E_TREE = 5 };
+void launch_ug_propose(const UgArgs &a, cudaStream_t st);
+void launch_ug_decide(const UgArgs &a, cudaStream_t st);
 bool tw_fits(int P);                       // P events fit one warp's shared memory
 int launch_treeweight(const TwArgs &a, const TwModel &h, cudaStream_t st);
 int launch_tree_prob(const TwProbArgs &a, const TwModel &h, cudaStream_t st);

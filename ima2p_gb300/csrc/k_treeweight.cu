@@ -385,93 +385,7 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_tw_sweep(TwArgs a, int wpb, int
 }
 
 // ---------------------------------------------------------------- p(G)
-// The incomplete gamma functions (IgBase) are shared with the 2NM densities
-// (igamma.cuh); Ig adds the integral terms of initialize_integrate_tree_prob.
-struct Ig : IgBase {
-  __device__ double coal(int cc, double fc, double hcc, double max, double min)
-  {
-    double p;
-    if (cc > 0) {
-      if (!(fc > 0)) {
-        st = TW_E_TERM;
-        return 0.0;
-      }
-      if (min == 0) {
-        double ug = upper(cc - 1, 2 * fc / max);
-        if (cc > 1) {
-          const double fullg = lf(cc - 2);
-          if (fullg - ug < 1e-15 || fullg - ug > LD_CUT) {
-            const double lg = lower(cc - 1, 2 * fc / max);
-            if (fullg > lg) {
-              const double ugalt = logdiff(fullg, lg);
-              if (fabs(ugalt - ug) > 1e-10) ug = ugalt;
-            }
-          }
-        }
-        p = ug + LOG2 - hcc + (1 - cc) * log(fc);
-      } else {
-        const double aa = upper(cc - 1, 2 * fc / max), bb = upper(cc - 1, 2 * fc / min);
-        p = logdiff(aa, bb);
-        p += (LOG2 - hcc + (1 - cc) * log(fc));
-      }
-    } else if (2 * fc / max > 0) {
-      if (min == 0) {
-        const double aa = log(max) - 2.0 * fc / max;
-        const double bb = LOG2 + log(fc) + upper(0, 2.0 * fc / max);
-        p = logdiff(aa, bb);
-      } else {
-        double aa = upper(0, 2 * fc / max), bb = upper(0, 2 * fc / min);
-        double c = logdiff(aa, bb);
-        c += LOG2 + log(fc);
-        aa = log(max) - 2.0 * fc / max;
-        bb = log(min) - 2.0 * fc / min;
-        const double d = logdiff(aa, bb);
-        p = logdiff(d, c);
-      }
-    } else {
-      p = log(max - min);
-    }
-    return p;
-  }
-  __device__ double mig(int cm, double fm, double max, double min)
-  {
-    double p;
-    if (cm > 0) {
-      if (!(fm > 0)) {
-        st = TW_E_TERM;
-        return 0.0;
-      }
-      if (min == 0) {
-        double lg = lower(cm + 1, fm * max);
-        const double fullg = lf(cm);
-        if (fullg - lg < 1e-15 || fullg - lg > LD_CUT) {
-          const double ug = upper(cm + 1, fm * max);
-          if (fullg > ug) {
-            const double lgalt = logdiff(fullg, ug);
-            if (fabs(lgalt - lg) > 1e-12) lg = lgalt;
-          }
-        }
-        p = (-1 - cm) * log(fm) + lg;
-      } else {
-        const double aa = upper(cm + 1, fm * min), bb = upper(cm + 1, fm * max);
-        p = (-1 - cm) * log(fm) + logdiff(aa, bb);
-      }
-    } else if (fm > MPRIORMIN) {
-      if (min == 0) {
-        p = (max == MPRIORMIN) ? 0 : logdiff(0.0, -fm * max) - log(fm);
-      } else {
-        p = logdiff(-fm * min, -fm * max) - log(fm);
-      }
-    } else {
-      p = log(max - min);
-    }
-    return p;
-  }
-  __device__ double mig_expo(int cm, double fm, double mean)
-  {
-    return -log(mean) + (-(cm + 1) * log(fm + 1.0 / mean)) + lf(cm);
-  }
-};
+// The integral terms (Ig) are in igamma.cuh.
 
 constexpr int TP_BS = 128;
 

@@ -582,6 +582,51 @@ int ima_gpu_changet_ry1_sweep_mt(ima_ctx *ctx, int nch, const int32_t *chains, c
                                  const double *u, const double *kappa, int precision, uint8_t *accept,
                                  double *pdgsum, double *probg, double *newt_out);
 
+/* ------------------------------------------------- genealogy update
+ * A chain's generators for the genealogy update, as the reference keeps
+ * them in globals: the MT19937 of uniform() (utilities.cpp:419-426), the
+ * second deviate normdev caches between calls (iset, gset; :476-503) and
+ * bitran's shift register (iseed; :438-455). */
+typedef struct {
+  ima_mt19937 mt;
+  int32_t iset;
+  double gset;
+  uint64_t iseed;
+} ima_ug_rng;
+/* setseeds (utilities.cpp:399-408): init_genrand(seed), iseed =
+ * ULONG_MAX / 2 + seed, no cached deviate */
+void ima_ug_rng_seed(ima_ug_rng *rng, int32_t seed);
+/* updategenealogy (update_gtree.cpp:723-966) of the no-migration model
+ * (slider_nomigration, :79-254) on the resident genealogies of the listed
+ * chains: nsweeps sweeps, each proposing a new genealogy for every locus in
+ * order on every listed chain (chains in parallel, each drawing from its own
+ * rng[k], updated in place), as qupdate calls it (ima_main_mpi.cpp:1821-1841).
+ * A proposal picks an edge (randposint until it is not the root's), slides
+ * its bottom by a normal deviate of sd min(20, roottime / 3) through the
+ * genealogy (bitran at every node), reattaches it, recomputes the locus's
+ * weights, the chain's p(G) from its summed weights (+ new - old) and the
+ * locus's likelihood (IS in full; HKY from the four edited edges, in
+ * `precision`), and accepts with the reference's Metropolis-Hastings term
+ * (heat from ima_gpu_set_betas, gbeta) and one more uniform -- none when the
+ * IS likelihood rejects the genealogy.  A rejection restores the genealogy.
+ * Needs the population model with nomig = 1, labels and locus populations
+ * (ima_gpu_set_labels, ima_gpu_set_locus_pops) and IS or HKY loci (IMA_ERR_ARG
+ * for SW).  tvals [nch][npops-1]: the chains' split times; u [nch * nloci],
+ * kappa [nch * nloci] (may be NULL: 1).  The call starts from a full
+ * evaluation of the chains' loci and their weights summed afresh (what the
+ * reference holds after its set-up or an accepted split-time update), then
+ * carries the sums from proposal to proposal as the reference does.  Out
+ * (each may be NULL): accepted [nch * nloci] and topology [nch * nloci]
+ * accepted proposals and accepted topology changes per chain-locus; probg
+ * [nch] the chains' p(G) at the end.  Resident G.pdg and p(G) are updated. */
+int ima_gpu_updategenealogy_sweep(ima_ctx *ctx, int nch, const int32_t *chains, const double *tvals, int nsweeps,
+                                  const double *u, const double *kappa, double gbeta, int precision,
+                                  ima_ug_rng *rng, int32_t *accepted, int32_t *topology, double *probg);
+/* The resident genealogy of chain ci, locus li: up0, up1, down, time and
+ * the population labels [2n-1] (any may be NULL). */
+int ima_gpu_get_genealogy(ima_ctx *ctx, int ci, int li, int32_t *up0, int32_t *up1, int32_t *down, double *time,
+                          int32_t *pop);
+
 /* No counterpart in the reference.  The FP64 surface of ima_gpu_surface_eval
  * (IMA_SURF_FP64) for callers that may not allocate device memory: a plugin
  * inside a host application that owns every device allocation through its
@@ -634,7 +679,8 @@ int ima_gpu_kernel_stats(ima_ctx *ctx, int kind, long long *launches, double *ms
 #define IMA_K_POPMIG 14
 #define IMA_K_HKY_FP32 15
 #define IMA_K_TIMES 16             /* re-timing uploads: float-float copies, lengths, in-place reads */
-#define IMA_K_COUNT 17
+#define IMA_K_UG 17                /* genealogy update: proposals and decisions */
+#define IMA_K_COUNT 18
 /* Total kernel launches issued by this library on the context. */
 int ima_gpu_launch_count(ima_ctx *ctx, long long *n);
 /* Write a device buffer larger than L2 (evicts resident data). */

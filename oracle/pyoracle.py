@@ -709,6 +709,52 @@ def ref_ry(npops, treestr, tprior, loci, chains, gens, steps, seed, thetaprior, 
     return res, times, migt
 
 
+def ref_ug(npops, treestr, thetaprior, loci, chains, gens, nsweeps):
+    """The reference's genealogy update updategenealogy under the
+    no-migration model through oracle/_ref/imaref (this container only).
+    loci: ("is", numgenes, hval, samppop, u, seq[n][S]) or ("hky", numgenes,
+    hval, samppop, u, HKYLocus, kappa); chains: (tvals, beta, seed);
+    gens[ci][li]: LabelledGenealogy (no migration events).  Each chain runs
+    nsweeps sweeps over its loci from setseeds(seed).  Returns (per proposal
+    (ci, li, accepted, topolchange, tmrcachange, pdg, probg), final trees
+    {(ci, li): (up0, up1, down, time, pop)})."""
+    nch, nl = len(chains), len(loci)
+    t = ["%d %d %d %d" % (npops, nch, nl, nsweeps), treestr, "%.17g" % thetaprior]
+    for loc in loci:
+        kind, ng, h, sp, u = loc[:5]
+        if kind == "is":
+            seq = np.asarray(loc[5])
+            t.append("0 %d %.17g %s %.17g %d" % (ng, h, " ".join(map(str, sp)), u, seq.shape[1]))
+            t.append(" ".join(map(str, seq.ravel())))
+        else:
+            hl, kappa = loc[5], loc[6]
+            t.append("1 %d %.17g %s %.17g %d" % (ng, h, " ".join(map(str, sp)), u, hl.seq.shape[1]))
+            t.append(" ".join(map(str, hl.seq.ravel())))
+            t.append("%d %s %s %.17g" % (hl.totsites, " ".join(map(str, hl.mult)),
+                                         " ".join("%.17g" % p for p in hl.pi), kappa))
+    for tv, b, seed in chains:
+        t.append(" ".join("%.17g" % v for v in tv) + " %.17g %d" % (b, seed))
+    for ci in range(nch):
+        for li in range(nl):
+            lg = gens[ci][li]
+            t.append(str(len(lg.pop)))
+            t.append(_tree_txt(lg.g) + " ".join(map(str, lg.pop)))
+    out = run_ref("ug", "\n".join(t) + "\n")
+    res, trees = [], {}
+    for ln in out.splitlines():
+        f = ln.split()
+        if f[0] == "UG":
+            res.append((int(f[1]), int(f[2]), int(f[3]), int(f[4]), int(f[5]), float(f[6]), float(f[7])))
+        elif f[0] == "TREE":
+            ci, li = int(f[1]), int(f[2])
+            m = (len(f) - 3) // 5
+            v = f[3:]
+            trees[(ci, li)] = (np.array(v[0:m], np.int32), np.array(v[m:2 * m], np.int32),
+                               np.array(v[2 * m:3 * m], np.int32), np.array([float(x) for x in v[3 * m:4 * m]]),
+                               np.array(v[4 * m:5 * m], np.int32))
+    return res, trees
+
+
 # ------------------------------------------------------------- batches
 class PackedItems:
     """Chain-loci of one model packed into flat arrays for the batched C

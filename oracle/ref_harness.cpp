@@ -12,7 +12,7 @@
  * ref_access_cpd.cpp and ref_access_jf.cpp include those two reference
  * sources to reach them.  The other reference objects are linked unchanged.
  *
- * Usage:  imaref is|hky|sw|swap|jointp|de|margin|tw|iterm|ry|popmig|peaks|iparams <input.txt>
+ * Usage:  imaref is|hky|sw|swap|jointp|de|margin|tw|iterm|ry|popmig|peaks|iparams|ug <input.txt>
  *         (results on stdout)
  */
 #undef GLOBVARS
@@ -20,6 +20,7 @@
 #include "ref_access.h"
 #include <string>
 
+#include <array>
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -663,6 +664,138 @@ static void run_ry()
     }
 }
 
+/* UG: npops nchains nloci nsweeps treestring thetaprior
+ *     per locus: model(0 IS, 1 HKY) numgenes hval samppop[npops] u numsites
+ *       seq[numgenes*numsites]; HKY adds totsites mult[numsites] pi[4] kappa
+ *     per chain: tvals[npops-1] beta seed
+ *     per chain, per locus: nlines up0[] up1[] down[] time[] pop[]
+ *   -> per proposal "UG ci li accepted topolchange tmrcachange pdg probg",
+ *      then per chain-locus "TREE ci li" with up0[] up1[] down[] time[] pop[]
+ * The genealogy update updategenealogy (update_gtree.cpp:723-966) of the
+ * no-migration model (slider_nomigration, :79-254), after the chain state is
+ * set up as finish_setup_C does it.  Each chain runs all its sweeps (every
+ * locus in order per sweep) before the next chain, from setseeds(seed) of
+ * its own: with an even number of proposals per chain, normdev's cached
+ * second deviate (utilities.cpp:476-503) is spent before the next chain
+ * starts, so every chain sees a generator of its own. */
+static void run_ug()
+{
+  int npp = rd_i(), nch = rd_i(), nl = rd_i(), nsweeps = rd_i();
+  char treestr[POPTREESTRINGLENGTHMAX];
+  if (fscanf(g_in, "%255s", treestr) != 1) { fprintf(stderr, "short input\n"); exit(3); }
+  thetaprior = rd_d();
+  mprior = 0.0;
+  npops = npp;
+  numtreepops = 2 * npops - 1;
+  lastperiodnumber = numsplittimes = npops - 1;
+  modeloptions[NOMIGRATION] = 1;
+  gbeta = 1.0;
+  alloc_chains(nch, nl);
+  nurates = nl;
+  std::vector<double> us(nl), kappas(nl, 1.0);
+  std::vector<std::vector<int>> seqs(nl), mults(nl);
+  std::vector<std::array<double, 4>> pis(nl);
+  for (int li = 0; li < nl; li++) {
+    const int model = rd_i();
+    L[li].numgenes = rd_i();
+    L[li].numlines = 2 * L[li].numgenes - 1;
+    L[li].hval = rd_d();
+    for (int p = 0; p < npops; p++) L[li].samppop[p] = rd_i();
+    us[li] = rd_d();
+    L[li].numsites = rd_i();
+    L[li].model = model == 1 ? HKY : INFINITESITES;
+    L[li].nlinked = 1;
+    L[li].uii[0] = li;
+    seqs[li].resize((size_t)L[li].numgenes * L[li].numsites);
+    for (auto &v : seqs[li]) v = rd_i();
+    L[li].seq = (int **)malloc(sizeof(int *) * L[li].numgenes);
+    for (int i = 0; i < L[li].numgenes; i++) L[li].seq[i] = &seqs[li][(size_t)i * L[li].numsites];
+    if (model == 1) {
+      L[li].totsites = rd_i();
+      mults[li].resize(L[li].numsites);
+      for (auto &v : mults[li]) v = rd_i();
+      L[li].mult = mults[li].data();
+      for (int j = 0; j < 4; j++) pis[li][j] = rd_d();
+      kappas[li] = rd_d();
+    }
+  }
+  total_numgenes = 0;
+  for (int li = 0; li < nl; li++) total_numgenes += L[li].numgenes;
+  setlogfact();
+  init_gtreecommon();
+  init_treeweight();
+  std::vector<int> seeds(nch);
+  for (int ci = 0; ci < nch; ci++) {
+    setup_poptree(ci, treestr);
+    C[ci]->tvals = (double *)calloc((size_t)npops, sizeof(double));
+    for (int k = 0; k < npops - 1; k++) C[ci]->tvals[k] = rd_d();
+    C[ci]->tvals[lastperiodnumber] = TIMEMAX;
+    beta[ci] = rd_d();
+    seeds[ci] = rd_i();
+  }
+  refacc_setup_iparams();
+  init_updategenealogy();  // its held probcalc is sized by setup_iparams' parameter counts
+  for (int ci = 0; ci < nch; ci++) {
+    init_genealogy_weights(&C[ci]->allgweight);
+    init_probcalc(&C[ci]->allpcalc);
+    C[ci]->allpcalc.pdg = 0;
+    for (int li = 0; li < nl; li++) {
+      int nlines = rd_i();
+      struct genealogy *G = &C[ci]->G[li];
+      G->gtree = alloc_tree(nlines);
+      read_tree(G->gtree, nlines);
+      for (int i = 0; i < nlines; i++) G->gtree[i].pop = rd_i();
+      for (int i = 0; i < nlines; i++) {
+        G->gtree[i].mig = (struct migstruct *)calloc((size_t)ABSMIGMAX, sizeof(struct migstruct));
+        G->gtree[i].cmm = ABSMIGMAX;
+        G->gtree[i].mig[0].mt = -1.0;
+      }
+      G->root = find_root(G->gtree, nlines);
+      G->gtree[G->root].time = TIMEMAX;
+      G->roottime = G->gtree[G->gtree[G->root].up[0]].time;
+      G->uvals = (double *)malloc(sizeof(double));
+      G->uvals[0] = us[li];
+      G->pdg_a = (double *)malloc(sizeof(double));
+      init_genealogy_weights(&G->gweight);
+      treeweight(ci, li);
+      sum_treeinfo(&C[ci]->allgweight, &G->gweight);
+      if (L[li].model == HKY) {
+        alloc_hky(G->gtree, L[li].numgenes, L[li].numsites);
+        for (int j = 0; j < 4; j++) G->pi[j] = pis[li][j];
+        G->kappaval = kappas[li];
+        G->pdg = G->pdg_a[0] = likelihoodHKY(ci, li, us[li], kappas[li], -1, -1, -1, -1);
+        copyfraclike(ci, li);
+        storescalefactors(ci, li);
+      } else {
+        G->pdg = G->pdg_a[0] = likelihoodIS(ci, li, us[li]);
+      }
+      C[ci]->allpcalc.pdg += G->pdg;
+    }
+    initialize_integrate_tree_prob(ci, &C[ci]->allgweight, &C[ci]->allpcalc);
+  }
+  for (int ci = 0; ci < nch; ci++) {
+    setseeds(seeds[ci]);
+    for (int s = 0; s < nsweeps; s++)
+      for (int li = 0; li < nl; li++) {
+        int topol = 0, tmrca = 0;
+        int acc = updategenealogy(ci, li, &topol, &tmrca);
+        printf("UG %d %d %d %d %d %.17g %.17g\n", ci, li, acc, topol, tmrca, C[ci]->G[li].pdg,
+               C[ci]->allpcalc.probg);
+      }
+  }
+  for (int ci = 0; ci < nch; ci++)
+    for (int li = 0; li < nl; li++) {
+      const struct edge *t = C[ci]->G[li].gtree;
+      printf("TREE %d %d", ci, li);
+      for (int i = 0; i < L[li].numlines; i++) printf(" %d", t[i].up[0]);
+      for (int i = 0; i < L[li].numlines; i++) printf(" %d", t[i].up[1]);
+      for (int i = 0; i < L[li].numlines; i++) printf(" %d", t[i].down);
+      for (int i = 0; i < L[li].numlines; i++) printf(" %.17g", t[i].time);
+      for (int i = 0; i < L[li].numlines; i++) printf(" %d", t[i].pop);
+      printf("\n");
+    }
+}
+
 /* ITERM: n, then per line: kind(0 coal, 1 mig, 2 mig expo) c f h max min
  *   -> the reference integral term per line (update_gtree_common.cpp:108-304) */
 static void run_iterm()
@@ -680,7 +813,7 @@ static void run_iterm()
 
 int main(int argc, char **argv)
 {
-  if (argc != 3) { fprintf(stderr, "usage: imaref is|hky|sw|swap|jointp|de|margin|tw|iterm|ry|popmig|peaks <input>\n"); return 2; }
+  if (argc != 3) { fprintf(stderr, "usage: imaref is|hky|sw|swap|jointp|de|margin|tw|iterm|ry|popmig|peaks|iparams|ug <input>\n"); return 2; }
   g_in = fopen(argv[2], "r");
   if (!g_in) { perror(argv[2]); return 2; }
   std::string mode = argv[1];
@@ -697,6 +830,7 @@ int main(int argc, char **argv)
   else if (mode == "popmig") run_popmig();
   else if (mode == "peaks") run_peaks();
   else if (mode == "iparams") run_iparams();
+  else if (mode == "ug") run_ug();
   else { fprintf(stderr, "unknown mode\n"); return 2; }
   fclose(g_in);
   return 0;

@@ -13,7 +13,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared():
     txt = open(os.path.join(ROOT, "include", "ima_gpu.h")).read()
-    return sorted(set(re.findall(r"\b(ima_(?:gpu|mt19937|ti)_\w+)\s*\(", txt)))
+    return sorted(set(re.findall(r"\b(ima_(?:gpu|mt19937|ti|ug_rng)_\w+)\s*\(", txt)))
 
 
 def test_header_and_wrapper_agree():

@@ -1,0 +1,144 @@
+"""The genealogy update of the no-migration model on the device
+(ima_gpu_updategenealogy_sweep) against the reference's own updategenealogy
+(update_gtree.cpp:723-966), run by the harness on 3 chains x 5 loci (IS and
+HKY), 10 sweeps per chain from a seed of its own (golden_ug.npz): the same
+accepted proposals per chain-locus, the same final genealogies (topology and
+population labels exact, times to the last bits of the device's log and
+sqrt in the slide's normal deviate), G.pdg and p(G)."""
+import numpy as np
+import pytest
+
+from ima2p_gb300 import api, popmodel
+from tests._golden import load
+
+pytestmark = pytest.mark.gpu
+
+
+class UgCase:
+    def __init__(self):
+        d = load("golden_ug.npz")
+        self.d = d
+        self.npops = int(d["npops"])
+        self.tree = str(d["tree"])
+        self.pm = popmodel.build(self.tree, self.npops, nomig=True)
+        self.kinds = [str(k) for k in d["kinds"]]
+        self.nl = len(self.kinds)
+        self.us = d["us"]
+        self.kappa = float(d["kappa"])
+        self.betas = d["betas"]
+        self.seeds = [int(s) for s in d["seeds"]]
+        self.nch = len(self.betas)
+        self.nsweeps = int(d["nsweeps"])
+        self.samps = d["samps"].astype(np.int32)
+        self.off = d["node_off"]
+        self.res = d["res"]
+
+    def base(self, li, f):
+        return self.d["base_" + f][self.off[li]:self.off[li + 1]]
+
+    def final(self, ci, li, f):
+        lens = [self.off[k + 1] - self.off[k] for k in range(self.nl)] * self.nch
+        start = sum(lens[:ci * self.nl + li])
+        return self.d["final_" + f][start:start + lens[ci * self.nl + li]]
+
+    def context(self, precision_loci=True):
+        from ima2p_gb300.synth import Genealogy, LabelledGenealogy
+        ctx = api.Context(0)
+        for li, kind in enumerate(self.kinds):
+            if kind == "is":
+                ctx.add_locus_is(self.d["seq_%d" % li])
+            else:
+                ctx.add_locus_hky(self.d["seq_%d" % li], self.d["mult_%d" % li], int(self.d["totsites_%d" % li]))
+        ctx.set_chains(1, self.nch)
+        th_max, th_min, _, _, _ = popmodel.priors(self.pm, float(self.d["thetaprior"]), 0.0)
+        ctx.set_popmodel(self.pm, th_max, th_min)
+        ci = np.repeat(np.arange(self.nch, dtype=np.int32), self.nl)
+        li = np.tile(np.arange(self.nl, dtype=np.int32), self.nch)
+        flat = []
+        for c in range(self.nch):
+            for l in range(self.nl):
+                down = self.base(l, "down").astype(np.int32)
+                g = Genealogy(self.base(l, "up0").astype(np.int32), self.base(l, "up1").astype(np.int32), down,
+                              self.base(l, "time").copy(), int(np.flatnonzero(down == -1)[0]))
+                flat.append(LabelledGenealogy(g, self.base(l, "pop").astype(np.int32), [[] for _ in range(len(down))]))
+        ctx.set_genealogies(ci, li, np.concatenate([g.g.up0 for g in flat]), np.concatenate([g.g.up1 for g in flat]),
+                            np.concatenate([g.g.down for g in flat]), np.concatenate([g.g.time for g in flat]),
+                            length=np.full(len(flat), -1.0))
+        ctx.set_labels(ci, li, flat)
+        ctx.set_locus_pops(np.ones(self.nl), self.samps)
+        for c in range(self.nch):
+            for l, kind in enumerate(self.kinds):
+                if kind == "hky":
+                    ctx.set_pi(c, l, self.d["pi_%d" % l])
+        ctx.set_betas(self.betas)
+        return ctx
+
+    def rates(self):
+        u = np.tile(self.us, self.nch)
+        kap = np.where(np.array([k == "hky" for k in self.kinds] * self.nch), self.kappa, 1.0)
+        return u, kap
+
+
+@pytest.mark.parametrize("precision", [api.PREC_FP64, api.PREC_FAST])
+def test_updategenealogy_follows_the_reference(precision):
+    case = UgCase()
+    ctx = case.context()
+    u, kap = case.rates()
+    rngs = [api.UgRng(s) for s in case.seeds]
+    tv = np.tile(case.d["tv0"], (case.nch, 1))
+    acc, top, probg = ctx.updategenealogy_sweep(np.arange(case.nch), tv, case.nsweeps, rngs, u, kap,
+                                                precision=precision)
+    ref_acc = np.zeros((case.nch, case.nl), np.int64)
+    ref_top = np.zeros((case.nch, case.nl), np.int64)
+    last_pdg = np.zeros((case.nch, case.nl))
+    last_probg = np.zeros(case.nch)
+    for ci, li, a, t, _, pdg, pg in case.res:
+        ci, li = int(ci), int(li)
+        ref_acc[ci, li] += int(a)
+        ref_top[ci, li] += int(a) * int(t)
+        last_pdg[ci, li] = pdg
+        last_probg[ci] = pg
+    assert np.array_equal(acc, ref_acc)
+    assert np.array_equal(top, ref_top)
+    np.testing.assert_allclose(probg, last_probg, rtol=0, atol=1e-9)
+    pdg = ctx.get_pdg().reshape(case.nch, case.nl)
+    tol = 1e-9 if precision == api.PREC_FP64 else 1e-5
+    np.testing.assert_allclose(pdg, last_pdg, rtol=0, atol=tol)
+    for ci in range(case.nch):
+        for li in range(case.nl):
+            nlines = int(case.off[li + 1] - case.off[li])
+            up0, up1, down, t, pop = ctx.get_genealogy(ci, li, nlines)
+            assert np.array_equal(up0, case.final(ci, li, "up0"))
+            assert np.array_equal(up1, case.final(ci, li, "up1"))
+            assert np.array_equal(down, case.final(ci, li, "down"))
+            assert np.array_equal(pop, case.final(ci, li, "pop"))
+            edge = down != -1
+            np.testing.assert_allclose(t[edge], case.final(ci, li, "time")[edge], rtol=1e-12, atol=0)
+    ctx.close()
+
+
+def test_updategenealogy_state_carries_between_calls():
+    """Ten one-sweep calls give the reference's ten-sweep run: the
+    generators, genealogies, partials and p(G) carry over, and an
+    evaluation after the sweeps reads the accepted genealogies."""
+    case = UgCase()
+    ctx = case.context()
+    u, kap = case.rates()
+    rngs = [api.UgRng(s) for s in case.seeds]
+    tv = np.tile(case.d["tv0"], (case.nch, 1))
+    acc = np.zeros((case.nch, case.nl), np.int64)
+    for _ in range(case.nsweeps):
+        a, _, probg = ctx.updategenealogy_sweep(np.arange(case.nch), tv, 1, rngs, u, kap, precision=api.PREC_FP64)
+        acc += a
+    ref_acc = np.zeros((case.nch, case.nl), np.int64)
+    for ci, li, a, *_ in case.res:
+        ref_acc[int(ci), int(li)] += int(a)
+    assert np.array_equal(acc, ref_acc)
+    last_probg = {int(r[0]): r[6] for r in case.res}
+    np.testing.assert_allclose(probg, [last_probg[c] for c in range(case.nch)], rtol=0, atol=1e-9)
+    ci = np.repeat(np.arange(case.nch, dtype=np.int32), case.nl)
+    li = np.tile(np.arange(case.nl, dtype=np.int32), case.nch)
+    r, st = ctx.eval(ci, li, u, kap, precision=api.PREC_FP64)
+    last = {(int(x[0]), int(x[1])): x[5] for x in case.res}
+    np.testing.assert_allclose(r, [last[(int(a), int(b))] for a, b in zip(ci, li)], rtol=0, atol=1e-9)
+    ctx.close()
