@@ -75,6 +75,32 @@ uint32_t ora_mt_u32(ora_mt *s);
 double ora_mt_uniform(ora_mt *s);          /* genrand_real3: (k+0.5)/2^32 */
 void ora_mt_fill_u32(uint32_t seed, int count, uint32_t *out);
 
+/* ---- genealogy update, no-migration model (update_gtree.cpp:723-966) ---- */
+/* a chain's generators: uniform()'s MT19937, normdev's cached deviate,
+ * bitran's register (the layout of the library's ima_ug_rng) */
+typedef struct { ora_mt mt; int32_t iset; double gset; uint64_t iseed; } ora_ug_rng;
+void ora_ug_rng_seed(ora_ug_rng *g, int seed); /* setseeds (utilities.cpp:399-408) */
+/* nsweeps updategenealogy sweeps (every locus in order) of each of nchains
+ * chains, each from its own generator, chains spread over nthreads host
+ * threads.  Genealogies of chain c, locus l at node_off[c*nloci+l] in up0 /
+ * up1 / down / time / pop (updated in place); loci: model 0 IS (seq, S
+ * sites, sumlogk) or 1 HKY (seq patterns, mult, totsites; pi per
+ * chain-locus).  The chain's state starts as finish_setup_C leaves it.  res
+ * [nchains][nsweeps][nloci][3] (accepted, topology changed, tmrca changed)
+ * and resd [...][2] (G.pdg, p(G) after the proposal) may be NULL; pdg_out
+ * [nchains*nloci], probg_out [nchains].  Returns 0, or 1 a slide that did not
+ * end, 2 a genealogy the model cannot hold, 3 an IS site no edge carries, 4
+ * an integral term the reference rejects, 5 no memory. */
+int ora_ug_run(int npops, const int *plist, const int *droppops, const int *addpop, const int *pop_e,
+               const int *pop_down, int nth, const int *th_off, const int *th_idx, const double *th_max,
+               const double *th_min, int nloci, const int *model, const int *n, const int *S, const int *totsites,
+               const long long *seq_off, const long long *mult_off, const int8_t *seq, const int *mult,
+               const double *hval, const int *samppop, const double *sumlogk, int nchains,
+               const long long *node_off, int *up0, int *up1, int *down, double *time, int *pop,
+               const double *tvals, const double *beta, double gbeta, const double *u, const double *kappa,
+               const double *pi, int nsweeps, ora_ug_rng *rng, int nthreads, int *res, double *resd,
+               double *pdg_out, double *probg_out);
+
 /* ---- MC3 (swapchains.cpp:12-178, 526-662) ------------------------------ */
 /* setheat for one process (numprocesses=1): heatmode 0 linear, 1 geometric,
  * 2 even (imamp.hpp heating enum order HLINEAR, HGEOMETRIC, HEVEN). */

@@ -103,6 +103,13 @@ def _declare(L):
     L.ora_tree_prob.restype = I
     L.ora_gsamp_row.argtypes = [I, P, P, P, P, P, I, P, P, I, P, P, P, P, D, D, I, P, P]
     L.ora_gsamp_row.restype = None
+    L.ora_ug_rng_seed.argtypes = [P, I]
+    L.ora_ug_rng_seed.restype = None
+    # model (npops + 5 tables), theta maps (nth + 4), loci (nloci + 11), chains
+    # (nchains + 8), gbeta + 3 rate arrays, nsweeps, rng, nthreads, 4 outputs
+    L.ora_ug_run.argtypes = ([I] + [P] * 5 + [I] + [P] * 4 + [I] + [P] * 11 + [I] + [P] * 8 + [D] + [P] * 3 +
+                             [I, P, I] + [P] * 4)
+    L.ora_ug_run.restype = I
 
 
 def _p(a):
@@ -753,6 +760,75 @@ def ref_ug(npops, treestr, thetaprior, loci, chains, gens, nsweeps):
                                np.array(v[2 * m:3 * m], np.int32), np.array([float(x) for x in v[3 * m:4 * m]]),
                                np.array(v[4 * m:5 * m], np.int32))
     return res, trees
+
+
+class UgRng(C.Structure):
+    """ora_ug_rng: a chain's uniform() MT19937, normdev's cached deviate and
+    bitran's register."""
+    _fields_ = [("mt", C.c_uint32 * 624), ("mti", C.c_int), ("iset", C.c_int32), ("gset", C.c_double),
+                ("iseed", C.c_uint64)]
+
+    def __init__(self, seed=None):
+        super().__init__()
+        if seed is not None:
+            lib().ora_ug_rng_seed(C.byref(self), int(seed))
+
+
+class UgLoci:
+    """The loci of an updategenealogy run packed for ora_ug_run: per locus
+    ("is", seq, sumlogk) or ("hky", HKYLocus-like (seq, mult, totsites))."""
+
+    def __init__(self, loci, hval, samppop):
+        self.nloci = len(loci)
+        self.model = _i32([0 if l[0] == "is" else 1 for l in loci])
+        seqs = [np.ascontiguousarray(l[1].seq if l[0] == "hky" else l[1], np.int8) for l in loci]
+        self.n = _i32([q.shape[0] for q in seqs])
+        self.S = _i32([q.shape[1] for q in seqs])
+        self.totsites = _i32([l[1].totsites if l[0] == "hky" else 0 for l in loci])
+        self.seq_off = np.concatenate([[0], np.cumsum([q.size for q in seqs])[:-1]]).astype(np.int64)
+        self.seq = np.concatenate([q.ravel() for q in seqs]).astype(np.int8)
+        mults = [_i32(l[1].mult) if l[0] == "hky" else np.zeros(1, np.int32) for l in loci]
+        self.mult_off = np.concatenate([[0], np.cumsum([m.size for m in mults])[:-1]]).astype(np.int64)
+        self.mult = np.concatenate(mults).astype(np.int32)
+        self.sumlogk = _f64([l[2] if l[0] == "is" else 0.0 for l in loci])
+        self.hval = _f64(hval)
+        self.samppop = _i32(samppop)
+
+
+def ug_run(pm, th_max, th_min, loci, gens, tvals, betas, u, kappa, pi, nsweeps, rngs, gbeta=1.0, nthreads=1,
+           record=True):
+    """ora_ug_run: nsweeps genealogy updates (no-migration model) of every
+    chain; gens[c][l] LabelledGenealogy (copied, not changed); rngs UgRng per
+    chain (advanced).  Returns (status, res [nch][nsweeps][nloci][3] or None,
+    resd [...][2] or None, pdg [nch][nloci], probg [nch], final genealogies
+    (up0, up1, down, time, pop) flat in chain-locus order)."""
+    nch, nl = len(gens), loci.nloci
+    flat = [lg for row in gens for lg in row]
+    lens = [len(lg.pop) for lg in flat]
+    node_off = np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.int64)
+    up0 = _i32(np.concatenate([lg.g.up0 for lg in flat])).copy()
+    up1 = _i32(np.concatenate([lg.g.up1 for lg in flat])).copy()
+    down = _i32(np.concatenate([lg.g.down for lg in flat])).copy()
+    time = _f64(np.concatenate([lg.g.time for lg in flat])).copy()
+    pop = _i32(np.concatenate([lg.pop for lg in flat])).copy()
+    tho, thi = pm.th_csr()
+    arr = (UgRng * nch)(*rngs)
+    res = np.zeros((nch, nsweeps, nl, 3), np.int32) if record else None
+    resd = np.zeros((nch, nsweeps, nl, 2)) if record else None
+    pdg, probg = np.zeros((nch, nl)), np.zeros(nch)
+    tv = _f64(np.asarray(tvals, np.float64).reshape(nch, -1))
+    st = lib().ora_ug_run(pm.npops, _p(_i32(pm.plist)), _p(_i32(pm.droppops)), _p(_i32(pm.addpop)),
+                          _p(_i32(pm.pop_e)), _p(_i32(pm.pop_down)), len(pm.th_cells), _p(tho), _p(thi),
+                          _p(_f64(th_max)), _p(_f64(th_min)), nl, _p(loci.model), _p(loci.n), _p(loci.S),
+                          _p(loci.totsites), _p(loci.seq_off), _p(loci.mult_off), _p(loci.seq), _p(loci.mult),
+                          _p(loci.hval), _p(loci.samppop), _p(loci.sumlogk), nch, _p(node_off), _p(up0), _p(up1),
+                          _p(down), _p(time), _p(pop), _p(tv), _p(_f64(betas)), float(gbeta),
+                          _p(_f64(np.asarray(u).reshape(-1))), _p(_f64(np.asarray(kappa).reshape(-1))),
+                          _p(_f64(np.asarray(pi).reshape(-1))), int(nsweeps), C.cast(arr, P), int(nthreads),
+                          _p(res), _p(resd), _p(pdg), _p(probg))
+    for k in range(nch):
+        C.memmove(C.addressof(rngs[k]), C.addressof(arr[k]), C.sizeof(UgRng))
+    return st, res, resd, pdg, probg, (up0, up1, down, time, pop)
 
 
 # ------------------------------------------------------------- batches
