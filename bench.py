@@ -16,7 +16,7 @@ error against the plain FP64 form:
                    128 chains x 8 runs
   config5_surface  G = 2^21 genealogy summaries, P = 2^16 points
 
-  python bench.py [--steps K] [--warmup W] [--gpus N] [--workload all|sw|is|hky|mixed|surface|treeweight|popmig]
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--workload all|sw|is|hky|mixed|surface|treeweight|popmig|updgen]
   python bench.py --impl reference ...   # the CPU restatement of the reference on every host core
 
 value: inputs resident in HBM, device time (CUDA events on the context's
@@ -45,6 +45,7 @@ sys.path.insert(0, ROOT)
 METRIC = "chain-locus likelihood evals/s"
 SURF_METRIC = "L-mode grid points/s"
 TW_METRIC = "genealogy weights (treeweight) per second"
+UG_METRIC = "genealogy update proposals/s"
 PM_METRIC = "2NM density terms (points x genealogies) per second"
 
 
@@ -1039,6 +1040,143 @@ def splittime_sweep(pm, packed, samp, tv, base, seq, nloci, nch, args):
                     "update on the oracle's C functions"}
 
 
+def updgen_context(api, w, precision_hky=True):
+    """A context holding the genealogy-update workload: HKY loci, every chain
+    from the locus's coalescent draw, population labels, locus populations,
+    base frequencies, geometric heats."""
+    from ima2p_gb300 import popmodel
+    ctx = api.Context(0)
+    for loc in w.loci:
+        ctx.add_locus_hky(loc.seq, loc.mult, loc.totsites)
+    ctx.set_chains(1, w.nch)
+    pm = popmodel.build(w.tree, w.npops, nomig=True)
+    th_max, th_min, _, _, _ = popmodel.priors(pm, 30.0, 0.0)
+    ctx.set_popmodel(pm, th_max, th_min)
+    nl = len(w.loci)
+    ci = np.repeat(np.arange(w.nch, dtype=np.int32), nl)
+    li = np.tile(np.arange(nl, dtype=np.int32), w.nch)
+    flat = [w.base[l] for _ in range(w.nch) for l in range(nl)]
+    ctx.set_genealogies(ci, li, np.concatenate([g.g.up0 for g in flat]), np.concatenate([g.g.up1 for g in flat]),
+                        np.concatenate([g.g.down for g in flat]), np.concatenate([g.g.time for g in flat]),
+                        length=np.full(len(flat), -1.0))
+    ctx.set_labels(ci, li, flat)
+    ctx.set_locus_pops(np.ones(nl), w.samppop)
+    for c in range(w.nch):
+        for l in range(nl):
+            ctx.set_pi(c, l, w.loci[l].pi)
+    ctx.set_betas(ug_betas(w.nch))
+    return ctx, pm, th_max, th_min
+
+
+def ug_betas(nch):
+    """Linear heating, 1 / (1 + 0.05 k) for chain k of each run of up to
+    128 chains."""
+    return 1.0 / (1.0 + 0.05 * (np.arange(nch) % 128))
+
+
+def updgen_cpu(args, w, pm, th_max, th_min):
+    """The oracle's restatement of updategenealogy (C: treeweight, p(G),
+    FP64 HKY from the edited edges) over every host core: whole sweeps of at
+    least as many chains as cores, the call's set-up timed apart and
+    subtracted."""
+    from oracle import pyoracle as O
+    nl = len(w.loci)
+    cores = os.cpu_count() or 1
+    ul = O.UgLoci([("hky", loc) for loc in w.loci], np.ones(nl), w.samppop)
+    nc = min(w.nch, max(cores, 8))
+    gens = [[w.base[l] for l in range(nl)] for _ in range(nc)]
+    pis = np.array([w.loci[l].pi for _ in range(nc) for l in range(nl)])
+
+    def cpu_run(ns):
+        rr = [O.UgRng(1000 + c) for c in range(nc)]
+        t = time.perf_counter()
+        st = O.ug_run(pm, th_max, th_min, ul, gens, np.tile(w.tvals, (nc, 1)), ug_betas(nc),
+                      np.tile(w.u, nc), np.tile(w.kappa, nc), pis, ns, rr, nthreads=cores, record=False)[0]
+        assert st == 0
+        return time.perf_counter() - t
+
+    t_setup = cpu_run(0)
+    ncpu = 1
+    while True:
+        t_cpu = cpu_run(ncpu) - t_setup
+        if t_cpu > max(1.0, args.cpu_seconds / 2) or ncpu >= 1024:
+            break
+        ncpu *= 2
+    return {"value": round(ncpu * nc * nl / max(t_cpu, 1e-9), 1), "unit": "proposals/s", "cores": cores,
+            "kind": "port",
+            "sample": "%d sweeps of %d chains x %d loci through the oracle's restatement of updategenealogy in C "
+                      "on %d threads, its set-up (%.0f ms) subtracted" % (ncpu, nc, nl, cores, 1e3 * t_setup)}
+
+
+def measure_updgen(args, api, w, sweeps):
+    """The genealogy update (ima_gpu_updategenealogy_sweep) on the whole
+    chain set: one call of `sweeps` sweeps after a warm-up call, timed on the
+    host clock around the call (its set-up -- one full evaluation and the
+    chains' weights -- included), with the device time of its kernels by
+    kind; the oracle's restatement on every host core for the CPU rate."""
+    from oracle import pyoracle as O
+    nl, nch = len(w.loci), w.nch
+    ctx, pm, th_max, th_min = updgen_context(api, w)
+    chains = np.arange(nch, dtype=np.int32)
+    tv = np.tile(w.tvals, (nch, 1))
+    u, kap = np.tile(w.u, nch), np.tile(w.kappa, nch)
+    rngs = [api.UgRng(1000 + c) for c in range(nch)]
+    ctx.updategenealogy_sweep(chains, tv, args.warmup, rngs, u, kap, precision=api.PREC_FAST)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    ctx.updategenealogy_sweep(chains, tv, 0, rngs, u, kap, precision=api.PREC_FAST)
+    setup_s = time.perf_counter() - t0
+    n0 = ctx.launch_count()
+    with Clocks(0) as clk:
+        t0 = time.perf_counter()
+        acc, top, probg = ctx.updategenealogy_sweep(chains, tv, sweeps, rngs, u, kap, precision=api.PREC_FAST)
+        wall = time.perf_counter() - t0
+    n_timed = ctx.launch_count() - n0
+    # where a sweep's device time goes: the same call again with an event pair
+    # around every launch (which slows the call; not the timed one)
+    ctx.set_profiling(True)
+    kinds = {"proposal_and_decision": api.K_UG, "treeweight": api.K_TREEWEIGHT, "hky": api.K_HKY_FAST}
+    k0 = {k: ctx.kernel_stats(v) for k, v in kinds.items()}
+    ctx.updategenealogy_sweep(chains, tv, sweeps, rngs, u, kap, precision=api.PREC_FAST)
+    k1 = {k: ctx.kernel_stats(v) for k, v in kinds.items()}
+    ctx.set_profiling(False)
+    t0 = time.perf_counter()
+    ctx.updategenealogy_sweep(chains, tv, sweeps, rngs, u, kap, precision=api.PREC_FP64)
+    wall64 = time.perf_counter() - t0
+    ctx.close()
+    props = sweeps * nch * nl
+    dev_ms = {k: round((k1[k][1] - k0[k][1]) / sweeps, 4) for k in kinds}
+    cpu = updgen_cpu(args, w, pm, th_max, th_min)
+    return {
+        "metric": UG_METRIC, "value": round(props / wall, 1), "unit": "proposals/s",
+        "ms_per_sweep": round(1e3 * wall / sweeps, 3), "sweeps": sweeps,
+        "config": {"workload": w.describe},
+        "e2e": {"value": round(props / wall, 1), "unit": "proposals/s", "h2d_bytes_per_step": int(nch * 2520 * 2 / sweeps),
+                "d2h_bytes_per_step": int(nch * (nl * 8 + 8) / sweeps),
+                "note": "one ima_gpu_updategenealogy_sweep call of all sweeps, its set-up included (%.1f ms: a "
+                        "full evaluation and the chains' weights summed afresh); the chains' generators go in "
+                        "and come back" % (1e3 * setup_s)},
+        "device_ms_per_sweep": dev_ms,
+        "fp64_form": {"value": round(props / wall64, 1), "unit": "proposals/s"},
+        "accept_rate": round(float(acc.sum()) / props, 3),
+        "topology_changes_accepted": int(top.sum()),
+        "gpu_launches": int(n_timed), "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+
+
+def run_updgen(args):
+    from ima2p_gb300 import api, workloads
+    w = workloads.make_updgen(nch=args.updgen_chains)
+    sub = measure_updgen(args, api, w, max(1, min(args.steps, 20)))
+    line = {"metric": sub.pop("metric"), "value": sub.pop("value"), "unit": sub.pop("unit"), "n_gpus": 1,
+            "steps": sub["sweeps"], "warmup": args.warmup, "ms_per_step": sub["ms_per_sweep"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "ff32 HKY + fp64 weights",
+            "data": "synthetic population-labelled genealogies (no migration) and HKY data"}
+    line.update(sub)
+    print(json.dumps(line), flush=True)
+
+
 def run_popmig(args):
     """The 2NM curves of print_populationmigrationrate_histograms for a
     3-population model (5 population sizes, 8 migration rates; its 8 default
@@ -1193,6 +1331,8 @@ def run_all(args):
     configs["config2_hky"] = measure_lik(args, api, workloads.make("hky"), sub_steps, dist, dev, hky_legs=True)
     configs["config4_mixed"] = measure_lik(args, api, workloads.make("mixed"), min(args.steps, 30), dist, dev)
     configs["config5_surface"] = measure_surface(args, api, min(args.steps, 20), not args.no_peak_search, dev)
+    configs["genealogy_update"] = measure_updgen(args, api, workloads.make_updgen(), 5)
+    configs["genealogy_update_1024_chains"] = measure_updgen(args, api, workloads.make_updgen(nch=1024), 3)
     emit(args, head, METRIC, dist, {"configs": configs})
 
 
@@ -1211,6 +1351,19 @@ def run_reference(args):
 
     cores = os.cpu_count() or 1
     name = "sw" if args.workload == "all" else args.workload
+    if name == "updgen":
+        from ima2p_gb300 import popmodel
+        w = workloads.make_updgen()
+        pm = popmodel.build(w.tree, w.npops, nomig=True)
+        th_max, th_min, _, _, _ = popmodel.priors(pm, 30.0, 0.0)
+        cpu = updgen_cpu(args, w, pm, th_max, th_min)
+        print(json.dumps({"impl": "reference", "metric": UG_METRIC, "value": cpu["value"], "unit": cpu["unit"],
+                          "n_gpus": 0, "steps": 1, "warmup": args.warmup, "ms_per_step": None,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+                          "data": "synthetic", "config": {"workload": w.describe}, "cpu_baseline": cpu,
+                          "e2e": {"value": cpu["value"], "unit": cpu["unit"], "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}), flush=True)
+        return
     if name in ("treeweight", "popmig"):
         print(json.dumps({"impl": "reference", "unavailable": "%s: the CPU rate is the line's cpu_baseline"
                           % name}))
@@ -1262,6 +1415,13 @@ def run_reference(args):
             "config4_mixed": lik_arm(workloads.make("mixed"), 3, 0.5),
             "config5_surface": surface_arm(),
         }
+        from ima2p_gb300 import popmodel
+        w = workloads.make_updgen()
+        pm = popmodel.build(w.tree, w.npops, nomig=True)
+        th_max, th_min, _, _, _ = popmodel.priors(pm, 30.0, 0.0)
+        cpu = updgen_cpu(args, w, pm, th_max, th_min)
+        line["configs"]["genealogy_update"] = {"value": cpu["value"], "unit": cpu["unit"],
+                                               "config": {"workload": w.describe}, "cpu_baseline": cpu}
     print(json.dumps(line), flush=True)
 
 
@@ -1272,7 +1432,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="all", choices=["all", "sw", "is", "hky", "mixed", "surface",
-                                                        "treeweight", "popmig"])
+                                                        "treeweight", "popmig", "updgen"])
     ap.add_argument("--cpu-seconds", type=float, default=3.0)
     ap.add_argument("--surface-log2g", type=int, default=21, help="log2 genealogies (config 5: 21)")
     ap.add_argument("--surface-log2p", type=int, default=16, help="log2 points (config 5: 16)")
@@ -1280,6 +1440,7 @@ def main():
     ap.add_argument("--no-peak-search", action="store_true", help="surface: skip the marginals and peak search")
     ap.add_argument("--popmig-g", type=int, default=300000, help="popmig: saved genealogies")
     ap.add_argument("--peaks-cpu-g", type=int, default=6000, help="popmig: genealogies in the CPU peaks sample")
+    ap.add_argument("--updgen-chains", type=int, default=32, help="updgen: chains (config 2: 32)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -1293,6 +1454,8 @@ def main():
         run_treeweight(args)
     elif args.workload == "popmig":
         run_popmig(args)
+    elif args.workload == "updgen":
+        run_updgen(args)
     else:
         run_likelihood_line(args, args.workload)
 

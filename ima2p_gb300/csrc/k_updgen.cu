@@ -32,18 +32,64 @@ constexpr double SLIDESTDVMAX = 20.0;        // update_gtree.cpp:686
 constexpr double ONEOVERSQRT2PI = 0.3989422803;  // utilities.cpp:461, as the reference writes it
 constexpr int SLIDE_MAX_STEPS = 1 << 20;     // a slide that long is an error, not a loop
 
-// MT19937 (Matsumoto & Nishimura 1998) on a state in global memory
-__device__ uint32_t mt_next(ima_mt19937 *g)
+// The chain's generators for one kernel: MT19937 (Matsumoto & Nishimura
+// 1998) with its 624 words in shared memory (the warp loads them and writes
+// them back only when a twist changed them) and the rest in lane 0's
+// registers, so that a draw costs a shared-memory read, not a dependent
+// round trip to global memory.
+struct LocalRng {
+  uint32_t *mt;
+  int mti, iset;
+  double gset;
+  unsigned long long iseed;
+  bool twisted;
+};
+
+__device__ void rng_load(LocalRng &r, const ima_ug_rng *g, uint32_t *smt, int lane)
+{
+  const uint2 *src = reinterpret_cast<const uint2 *>(g->mt.mt);  // the state is 8-byte aligned
+  uint2 *dst = reinterpret_cast<uint2 *>(smt);
+  for (int k = lane; k < 312; k += 32) dst[k] = src[k];
+  r.mt = smt;
+  r.mti = g->mt.mti;
+  r.iset = g->iset;
+  r.gset = g->gset;
+  r.iseed = g->iseed;
+  r.twisted = false;
+  __syncwarp();
+}
+
+// the warp writes the generator back (lane 0's registers, and the words
+// when lane 0 twisted them)
+__device__ void rng_store(const LocalRng &r, ima_ug_rng *g, int lane)
+{
+  const bool tw = __shfl_sync(~0u, (int)r.twisted, 0) != 0;
+  if (tw) {
+    const uint2 *src = reinterpret_cast<const uint2 *>(r.mt);
+    uint2 *dst = reinterpret_cast<uint2 *>(g->mt.mt);
+    for (int k = lane; k < 312; k += 32) dst[k] = src[k];
+  }
+  if (lane == 0) {
+    g->mt.mti = r.mti;
+    g->iset = r.iset;
+    g->gset = r.gset;
+    g->iseed = r.iseed;
+  }
+}
+
+__device__ uint32_t mt_next(LocalRng &r)
 {
   constexpr int N = 624, M = 397;
-  if (g->mti >= N) {
+  if (r.mti >= N) {
+    uint32_t *mt = r.mt;
     for (int k = 0; k < N; k++) {
-      const uint32_t y = (g->mt[k] & 0x80000000u) | (g->mt[(k + 1) % N] & 0x7fffffffu);
-      g->mt[k] = g->mt[(k + M) % N] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+      const uint32_t y = (mt[k] & 0x80000000u) | (mt[(k + 1) % N] & 0x7fffffffu);
+      mt[k] = mt[(k + M) % N] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
     }
-    g->mti = 0;
+    r.mti = 0;
+    r.twisted = true;
   }
-  uint32_t y = g->mt[g->mti++];
+  uint32_t y = r.mt[r.mti++];
   y ^= y >> 11;
   y ^= (y << 7) & 0x9d2c5680u;
   y ^= (y << 15) & 0xefc60000u;
@@ -52,37 +98,37 @@ __device__ uint32_t mt_next(ima_mt19937 *g)
 }
 
 // uniform() = genrand_real3, in (0, 1)
-__device__ double uniform(ima_ug_rng *g) { return ((double)mt_next(&g->mt) + 0.5) * (1.0 / 4294967296.0); }
+__device__ double uniform(LocalRng &r) { return ((double)mt_next(r) + 0.5) * (1.0 / 4294967296.0); }
 
 // bitran (utilities.cpp:438-455): Press et al.'s irbit2 on its own register
-__device__ int bitran(ima_ug_rng *g)
+__device__ int bitran(LocalRng &r)
 {
-  if (g->iseed & 131072ull) {
-    g->iseed = ((g->iseed ^ 19ull) << 1) | 1ull;
+  if (r.iseed & 131072ull) {
+    r.iseed = ((r.iseed ^ 19ull) << 1) | 1ull;
     return 1;
   }
-  g->iseed <<= 1;
+  r.iseed <<= 1;
   return 0;
 }
 
 // normdev (utilities.cpp:476-503): the polar method, keeping the second
 // deviate for the next call
-__device__ double normdev(ima_ug_rng *g, double mean, double stdev)
+__device__ double normdev(LocalRng &r, double mean, double stdev)
 {
-  if (g->iset == 0) {
+  if (r.iset == 0) {
     double v1, v2, rsq;
     do {
-      v1 = 2.0 * uniform(g) - 1.0;
-      v2 = 2.0 * uniform(g) - 1.0;
+      v1 = 2.0 * uniform(r) - 1.0;
+      v2 = 2.0 * uniform(r) - 1.0;
       rsq = v1 * v1 + v2 * v2;
     } while (rsq >= 1.0 || rsq == 0.0);
     const double fac = sqrt(-2.0 * log(rsq) / rsq);
-    g->gset = v1 * fac;
-    g->iset = 1;
+    r.gset = v1 * fac;
+    r.iset = 1;
     return v2 * fac * stdev + mean;
   }
-  g->iset = 0;
-  return g->gset * stdev + mean;
+  r.iset = 0;
+  return r.gset * stdev + mean;
 }
 
 __device__ double normprob(double mean, double stdev, double val)
@@ -125,6 +171,7 @@ __device__ double findjointime(const TwModel &M, const double *tv, int nsplit, i
 }
 
 struct UgSmem {
+  uint32_t *mt;    // the chain's MT19937 words
   NodeRec *nd;
   double *t;
   int32_t *pop;
@@ -136,7 +183,8 @@ __device__ UgSmem ug_carve(char *base, int maxn)
 {
   const int maxnl = 2 * maxn - 1;
   UgSmem s;
-  s.t = reinterpret_cast<double *>(base);
+  s.mt = reinterpret_cast<uint32_t *>(base);
+  s.t = reinterpret_cast<double *>(base + 624 * 4);
   s.nd = reinterpret_cast<NodeRec *>(s.t + maxnl);
   s.pop = reinterpret_cast<int32_t *>(s.nd + maxnl);
   s.h = s.pop + maxnl;
@@ -144,12 +192,12 @@ __device__ UgSmem ug_carve(char *base, int maxn)
   return s;
 }
 
-// times, nodes and labels [2n-1]; heights [2n-1] then level counts [n+2];
-// the schedule [2n]
+// the generator's words [624]; times, nodes and labels [2n-1]; heights
+// [2n-1] then level counts [n+2]; the schedule [2n]
 size_t ug_smem(int maxn)
 {
   const size_t maxnl = 2 * (size_t)maxn - 1;
-  return maxnl * (8 + 8 + 4) + (maxnl + maxn + 2) * 4 + 2 * (size_t)maxn * 2 + 16;
+  return 624 * 4 + maxnl * (8 + 8 + 4) + (maxnl + maxn + 2) * 4 + 2 * (size_t)maxn * 2 + 16;
 }
 
 __device__ void ug_fail(int32_t *err, int code, int who)
@@ -187,11 +235,11 @@ __global__ void __launch_bounds__(32) k_ug_propose(UgArgs a)
     a.bk_len[w] = a.len[item];
     a.bk_nlev[w] = a.nlev[item];
   }
-  __syncwarp();
+  LocalRng g;
+  rng_load(g, a.rng + w, s.mt, lane);
   if (lane == 0) {
     const TwModel &M = *a.model;
     const double *tv = a.tvals + (size_t)ci * a.nsplit;
-    ima_ug_rng *g = a.rng + w;
     NodeRec *nd = s.nd;
     double *t = s.t;
     int root = -1;
@@ -370,6 +418,7 @@ __global__ void __launch_bounds__(32) k_ug_propose(UgArgs a)
     a.nlev[item] = H;
   }
   __syncwarp();
+  rng_store(g, a.rng + w, lane);
   for (int k = lane; k < nl; k += 32) {
     a.nodes[base + k] = s.nd[k];
     const double t = s.t[k];
@@ -419,36 +468,59 @@ __global__ void __launch_bounds__(32) k_ug_decide(UgArgs a)
     }
   }
   __syncwarp();
+  // the theta integrals, a lane each: count and length summed over the
+  // parameter's cells in order, the last accepted value kept when neither
+  // changed (integrate_tree_prob)
+  const bool decide = !rejectIS && !failed;
+  if (decide)
+    for (int i = lane; i < nth; i += 32) {
+      int c = 0, holdc = 0;
+      double f = 0.0, holdf = 0.0, hc = 0.0;
+      for (int j = M.th_off[i]; j < M.th_off[i + 1]; j++) {
+        const int cell = M.th_idx[j];
+        c += s_cn[cell];
+        holdc += s_c0[cell];
+        f += s_fn[cell];
+        holdf += s_f0[cell];
+        hc += s_hn[cell];
+      }
+      Ig ig{{a.logfact, 0}};
+      s_q[i] = (c == holdc && f == holdf) ? a.qint[(size_t)w * nth + i]
+                                          : ig.coal(c, f, hc, M.th_max[i], M.th_min[i]);
+      if (ig.st) ug_fail(a.err, UG_E_TERM, w);
+    }
+  // the acceptance uniform: one word of the chain's MT19937, or the whole
+  // state staged for a twist
+  int mti = 0;
+  if (decide) mti = a.rng[w].mt.mti;
+  const bool stage = decide && mti >= 624;
+  __shared__ __align__(16) uint32_t s_mt[624];  // read as 8-byte words
+  LocalRng g{};
+  if (stage) rng_load(g, a.rng + w, s_mt, lane);
+  __syncwarp();
   if (lane == 0) {
     int acc = 0;
     if (failed) {
       if (!a.hky && code == IMA_EVAL_IS_FAIL) ug_fail(a.err, UG_E_ISFAIL, w);
     } else if (!rejectIS) {
-      ima_ug_rng *g = a.rng + w;
-      Ig ig{{a.logfact, 0}};
       double psum = 0;
-      for (int i = 0; i < nth; i++) {
-        int c = 0, holdc = 0;
-        double f = 0.0, holdf = 0.0, hc = 0.0;
-        for (int j = M.th_off[i]; j < M.th_off[i + 1]; j++) {
-          const int cell = M.th_idx[j];
-          c += s_cn[cell];
-          holdc += s_c0[cell];
-          f += s_fn[cell];
-          holdf += s_f0[cell];
-          hc += s_hn[cell];
-        }
-        const double qv = (c == holdc && f == holdf) ? a.qint[(size_t)w * nth + i]
-                                                     : ig.coal(c, f, hc, M.th_max[i], M.th_min[i]);
-        s_q[i] = qv;
-        psum += qv;
-      }
-      if (ig.st) ug_fail(a.err, UG_E_TERM, w);
+      for (int i = 0; i < nth; i++) psum += s_q[i];
       double tpw = -a.probg[ci];
       tpw += psum;
       double mh = tpw + a.gbeta * (pdgnew - a.pdg[item]);
       mh = exp(a.beta[ci] * mh + a.slidew[w]);
-      const double U = uniform(g);
+      double U;
+      if (stage) {
+        U = uniform(g);
+      } else {
+        uint32_t y = a.rng[w].mt.mt[mti];
+        y ^= y >> 11;
+        y ^= (y << 7) & 0x9d2c5680u;
+        y ^= (y << 15) & 0xefc60000u;
+        y ^= y >> 18;
+        U = ((double)y + 0.5) * (1.0 / 4294967296.0);
+        a.rng[w].mt.mti = mti + 1;
+      }
       acc = U < dmin(1.0, mh);
       if (acc) {
         a.probg[ci] = psum;
@@ -462,6 +534,7 @@ __global__ void __launch_bounds__(32) k_ug_decide(UgArgs a)
     s_acc = acc;
   }
   __syncwarp();
+  if (stage) rng_store(g, a.rng + w, lane);
   const bool acc = s_acc != 0;
   const size_t base = it.node_off;
   if (acc) {

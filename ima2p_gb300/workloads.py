@@ -7,6 +7,9 @@
   mixed    300 loci (200 HKY of U(200,3000) bp, 100 SW), U(4,60) copies per
            population x 3 populations, 128 chains x 8 runs
   surface  G = 2^21 genealogy summaries, K = 48 row width, P = 2^16 points
+  updgen   the hky shapes (50 HKY loci x (20+20) x 1000 bp) under the
+           no-migration model, population-labelled genealogies, for the
+           genealogy update
 
 Every chain gets its own genealogy per locus: independent coalescent draws
 for the smaller configurations, time-rescaled copies of a per-locus draw
@@ -195,3 +198,39 @@ def make_mixed(seed=1004, n_hky=200, n_sw=100, nruns=8, cpr=128):
 
 def make(name):
     return {"is": make_is, "hky": make_hky, "sw": make_sw, "mixed": make_mixed}[name]()
+
+
+@dataclasses.dataclass
+class UgWorkload:
+    """Population-labelled genealogies and HKY data for the genealogy
+    update: every chain starts from the locus's own coalescent draw."""
+    describe: str
+    tree: str
+    npops: int
+    tvals: list
+    loci: list            # HKYLocus per locus
+    base: list            # synth.LabelledGenealogy per locus
+    samppop: np.ndarray   # [nloci][npops]
+    u: np.ndarray         # [nloci]
+    kappa: np.ndarray     # [nloci]
+    nch: int
+
+
+def make_updgen(seed=1006, nloci=50, nch=32, ncopies=20, nbases=1000, tsplit=1.5, theta=10.0):
+    """The hky workload's shapes under the no-migration model (two
+    populations split at tsplit): kappa ~ U(2, 8), base frequencies ~
+    Dirichlet(5, 5, 5, 5), lognormal(0, 0.5) rate scalars."""
+    rng = np.random.default_rng(seed)
+    ul = _loci_u(rng, nloci)
+    kap = rng.uniform(2.0, 8.0, nloci)
+    splits = [(tsplit, 0, 1, 2)]
+    loci, base = [], []
+    for li in range(nloci):
+        lg = synth.sim_im_labeled(rng, [ncopies, ncopies], [theta] * 3, 0.0, splits)
+        loci.append(synth.hky_data(rng, lg.g, nbases, float(ul[li]), float(kap[li]), rng.dirichlet([5, 5, 5, 5])))
+        base.append(lg)
+    return UgWorkload("genealogy update: 2 pops (no migration, split at %g), %d HKY loci x (%d+%d) x %d bp, "
+                      "%d chains, one proposal per chain-locus per sweep" % (tsplit, nloci, ncopies, ncopies,
+                                                                             nbases, nch),
+                      "(0,1):2", 2, [tsplit], loci, base, np.tile([ncopies, ncopies], (nloci, 1)).astype(np.int32),
+                      ul, kap, nch)
