@@ -313,6 +313,8 @@ struct ima_ctx {
   void *d_ug = nullptr;
   size_t ug_cap = 0;
   std::vector<Batch> ugb;
+  cudaStream_t ug_st = nullptr;  // the weights of a step's HKY proposals run here beside their likelihoods
+  cudaEvent_t ug_fork = nullptr, ug_join = nullptr;
   // items whose tree lengths are still to be summed from their device times
   // (re-timings without lengths): done when a reader needs them
   int lpend_lo = INT32_MAX, lpend_hi = -1;
@@ -511,6 +513,9 @@ extern "C" void ima_gpu_destroy(ima_ctx *c)
   if (c->t0) cudaEventDestroy(c->t0);
   if (c->t1) cudaEventDestroy(c->t1);
 
+  if (c->ug_fork) cudaEventDestroy(c->ug_fork);
+  if (c->ug_join) cudaEventDestroy(c->ug_join);
+  if (c->ug_st) cudaStreamDestroy(c->ug_st);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -4277,7 +4282,16 @@ extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t 
   a.fresh32 = c->d_fresh32;
   a.slot64 = c->d_slot64;
   a.fresh64 = c->d_fresh64;
-  // the steps: one locus of every listed chain at a time
+  if (!c->ug_st) {
+    r = c->cuda(cudaStreamCreateWithFlags(&c->ug_st, cudaStreamNonBlocking), "stream");
+    r = r ? r : c->cuda(cudaEventCreateWithFlags(&c->ug_fork, cudaEventDisableTiming), "events");
+    r = r ? r : c->cuda(cudaEventCreateWithFlags(&c->ug_join, cudaEventDisableTiming), "events");
+    if (r) return r;
+  }
+  // the steps: one locus of every listed chain at a time.  An HKY step runs
+  // the proposed genealogies' weights on a second stream beside their
+  // likelihoods (neither reads the other's output); an IS step runs them
+  // first, as the IS likelihood reads the lengths they write
   for (int s = 0; s < nsweeps && !r; s++)
     for (int l = 0; l < nl && !r; l++) {
       Batch &b = c->ugb[l];
@@ -4289,11 +4303,21 @@ extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t 
       a.st = b.d_st;
       c->launch(IMA_K_UG, 0.0, [&] { launch_ug_propose(a, c->st); });
       w.perm = d_perm + (size_t)l * nch;
+      cudaStream_t tws = c->st;
+      if (a.hky) {
+        cudaEventRecord(c->ug_fork, c->st);
+        cudaStreamWaitEvent(c->ug_st, c->ug_fork, 0);
+        tws = c->ug_st;
+      }
       int lr = 0;
-      c->launch(IMA_K_TREEWEIGHT, 0.0, [&] { lr = launch_treeweight(w, h, c->st); });
+      c->launch(IMA_K_TREEWEIGHT, 0.0, [&] { lr = launch_treeweight(w, h, tws); }, tws);
       if (lr < 0) return c->fail(IMA_ERR_TOO_LARGE, "treeweight: shared memory for %d events", P);
       c->launches += lr - 1;
       enqueue(c, b);
+      if (a.hky) {
+        cudaEventRecord(c->ug_join, c->ug_st);
+        cudaStreamWaitEvent(c->st, c->ug_join, 0);
+      }
       c->launch(IMA_K_UG, 0.0, [&] { launch_ug_decide(a, c->st); });
       r = c->cuda(cudaGetLastError(), "genealogy update launch");
     }

@@ -261,15 +261,8 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_tw_sweep(TwArgs a, int wpb, int
     }
   };
   const bool lenlane = MERGE && gl == npops;
-  double tn = E > 0 ? et[0] : 0.0;
-  uint32_t cn = E > 0 ? ec[0] : 0u;
-  for (int j = 0; j < E; j++) {
-    const double t = tn;
-    const uint32_t c = cn;
-    if (j + 1 < E) {  // the next event's load overlaps this one's arithmetic
-      tn = et[j + 1];
-      cn = ec[j + 1];
-    }
+  // one event: returns true when the genealogy is found bad
+  auto event = [&](const double t, const uint32_t c) -> bool {
     const double dt = t - last;
     const bool before = __double_as_longlong(t) < lsb, lbefore = __double_as_longlong(last) < lsb;
     const int w = npops - k;
@@ -352,7 +345,28 @@ __global__ void __launch_bounds__(32 * TW_WPB) k_tw_sweep(TwArgs a, int wpb, int
       }
     }
     if (__any_sync(gmask, lbad)) bad = TW_E_COUNT;
-    if (bad) break;
+    return bad != 0;
+  };
+  // events four at a time, the next four loaded while these are swept: the
+  // sweep is a dependent chain, and one L2 round trip per event would set
+  // its pace
+  double q0 = 0.0, q1 = 0.0, q2 = 0.0, q3 = 0.0;
+  uint32_t r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+  if (0 < E) { q0 = et[0]; r0 = ec[0]; }
+  if (1 < E) { q1 = et[1]; r1 = ec[1]; }
+  if (2 < E) { q2 = et[2]; r2 = ec[2]; }
+  if (3 < E) { q3 = et[3]; r3 = ec[3]; }
+  for (int j = 0; j < E; j += 4) {
+    const double t0 = q0, t1 = q1, t2 = q2, t3 = q3;
+    const uint32_t c0 = r0, c1 = r1, c2 = r2, c3 = r3;
+    if (j + 4 < E) { q0 = et[j + 4]; r0 = ec[j + 4]; }
+    if (j + 5 < E) { q1 = et[j + 5]; r1 = ec[j + 5]; }
+    if (j + 6 < E) { q2 = et[j + 6]; r2 = ec[j + 6]; }
+    if (j + 7 < E) { q3 = et[j + 7]; r3 = ec[j + 7]; }
+    if (event(t0, c0)) break;
+    if (j + 1 < E && event(t1, c1)) break;
+    if (j + 2 < E && event(t2, c2)) break;
+    if (j + 3 < E && event(t3, c3)) break;
   }
   if (!bad && nsum != 1) bad = TW_E_COUNT;
   if (bad) {
