@@ -41,7 +41,7 @@ class UgCase:
         start = sum(lens[:ci * self.nl + li])
         return self.d["final_" + f][start:start + lens[ci * self.nl + li]]
 
-    def context(self, precision_loci=True):
+    def context(self):
         from ima2p_gb300.synth import Genealogy, LabelledGenealogy
         ctx = api.Context(0)
         for li, kind in enumerate(self.kinds):
@@ -141,4 +141,86 @@ def test_updategenealogy_state_carries_between_calls():
     r, st = ctx.eval(ci, li, u, kap, precision=api.PREC_FP64)
     last = {(int(x[0]), int(x[1])): x[5] for x in case.res}
     np.testing.assert_allclose(r, [last[(int(a), int(b))] for a, b in zip(ci, li)], rtol=0, atol=1e-9)
+    ctx.close()
+
+
+def test_updategenealogy_checkpoint_round_trip(tmp_path):
+    """Four sweeps, ima_gpu_checkpoint_write, a fresh context restored from
+    the file, six more sweeps: the accepted proposals, final genealogies
+    and G.pdg of the uninterrupted ten-sweep run (the file carries the
+    topologies and level schedules the device changed)."""
+    case = UgCase()
+    u, kap = case.rates()
+    tv = np.tile(case.d["tv0"], (case.nch, 1))
+    chains = np.arange(case.nch)
+    ctx = case.context()
+    rngs = [api.UgRng(s) for s in case.seeds]
+    whole, _, pg_whole = ctx.updategenealogy_sweep(chains, tv, 10, rngs, u, kap, precision=api.PREC_FP64)
+    want = [ctx.get_genealogy(ci, li, int(case.off[li + 1] - case.off[li]))
+            for ci in range(case.nch) for li in range(case.nl)]
+    pdg_whole = ctx.get_pdg()
+    ctx.close()
+
+    path = str(tmp_path / "ug.ckp")
+    ctx = case.context()
+    rngs = [api.UgRng(s) for s in case.seeds]
+    first, _, _ = ctx.updategenealogy_sweep(chains, tv, 4, rngs, u, kap, precision=api.PREC_FP64)
+    ctx.checkpoint_write(path)
+    ctx.close()
+    ctx = case.context()
+    ctx.checkpoint_read(path)
+    rest, _, pg = ctx.updategenealogy_sweep(chains, tv, 6, rngs, u, kap, precision=api.PREC_FP64)
+    assert np.array_equal(first + rest, whole)
+    np.testing.assert_allclose(pg, pg_whole, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(ctx.get_pdg(), pdg_whole, rtol=0, atol=1e-9)
+    k = 0
+    for ci in range(case.nch):
+        for li in range(case.nl):
+            got = ctx.get_genealogy(ci, li, int(case.off[li + 1] - case.off[li]))
+            for f in (0, 1, 2, 4):
+                assert np.array_equal(got[f], want[k][f])
+            edge = got[2] != -1
+            assert np.array_equal(got[3][edge], want[k][3][edge])
+            k += 1
+    ctx.close()
+
+
+def test_updategenealogy_refuses_what_it_does_not_model():
+    """SW loci and models with migration stay with the host: IMA_ERR_ARG /
+    IMA_ERR_STATE before anything runs; no sweeps returns the chains' p(G)
+    summed afresh."""
+    case = UgCase()
+    u, kap = case.rates()
+    tv = np.tile(case.d["tv0"], (case.nch, 1))
+    ctx = case.context()
+    rngs = [api.UgRng(s) for s in case.seeds]
+    before = [r.mt.mti for r in rngs]
+    acc, top, pg = ctx.updategenealogy_sweep(np.arange(case.nch), tv, 0, rngs, u, kap, precision=api.PREC_FP64)
+    assert not acc.any() and not top.any()
+    assert [r.mt.mti for r in rngs] == before
+    assert np.all(np.isfinite(pg))
+    ctx.close()
+    # a model with migration
+    ctx = api.Context(0)
+    for li, kind in enumerate(case.kinds):
+        if kind == "is":
+            ctx.add_locus_is(case.d["seq_%d" % li])
+        else:
+            ctx.add_locus_hky(case.d["seq_%d" % li], case.d["mult_%d" % li], int(case.d["totsites_%d" % li]))
+    ctx.set_chains(1, case.nch)
+    pm = popmodel.build(case.tree, case.npops)
+    ctx.set_popmodel(pm, *popmodel.priors(pm, 10.0, 1.0))
+    with pytest.raises(api.ImaError) as e:
+        ctx.updategenealogy_sweep(np.arange(case.nch), tv, 1, rngs, u, kap)
+    assert e.value.code == api.IMA_ERR_STATE
+    ctx.close()
+    # an SW locus
+    ctx = api.Context(0)
+    ctx.add_locus_sw(10, 1)
+    ctx.set_chains(1, 2)
+    pm = popmodel.build(case.tree, case.npops, nomig=True)
+    ctx.set_popmodel(pm, *popmodel.priors(pm, 10.0, 0.0)[:2])
+    with pytest.raises(api.ImaError) as e:
+        ctx.updategenealogy_sweep(np.arange(2), tv[:2], 1, rngs[:2], np.ones(2), None)
+    assert e.value.code == api.IMA_ERR_ARG
     ctx.close()
