@@ -209,6 +209,7 @@ __device__ void ug_fail(int32_t *err, int code, int who)
 __global__ void __launch_bounds__(32) k_ug_propose(UgArgs a)
 {
   extern __shared__ __align__(16) char smem[];
+  __shared__ int s_root;
   const int w = blockIdx.x, lane = threadIdx.x;
   const int ci = a.chains[w], item = ci * a.nloci + a.locus;
   const ItemDev it = a.items[item];
@@ -230,7 +231,8 @@ __global__ void __launch_bounds__(32) k_ug_propose(UgArgs a)
     bkt[k] = t;
     bkp[k] = p;
   }
-  for (int k = lane; k < 2 * n; k += 32) bks[k] = a.sched[it.sched_off + k];
+  if (a.hky)
+    for (int k = lane; k < 2 * n; k += 32) bks[k] = a.sched[it.sched_off + k];
   if (lane == 0) {
     a.bk_len[w] = a.len[item];
     a.bk_nlev[w] = a.nlev[item];
@@ -386,39 +388,67 @@ __global__ void __launch_bounds__(32) k_ug_propose(UgArgs a)
       R.e[2] = oldsis;
       R.e[3] = newsis;
     }
-    // heights (tips 0, a node one above its higher daughter) and the level
-    // schedule, as the genealogy upload builds them
-    int32_t *h = s.h;
-    for (int k = 0; k < nl; k++) h[k] = 0;
-    int16_t *seen = s.sch;  // scratch: daughters done per node
-    for (int k = 0; k < nl; k++) seen[k] = 0;
-    int walked = 0;
-    for (int tip = 0; tip < n; tip++) {
-      int v = nd[tip].down;
-      while (v >= n && v < nl && walked++ < 2 * nl) {  // a genealogy visits each node twice
-        if (++seen[v] < 2) break;
-        const int ha = h[nd[v].up0], hb = h[nd[v].up1];
-        h[v] = 1 + (ha > hb ? ha : hb);
-        v = nd[v].down;
-      }
-    }
-    int H = h[root];
-    if (walked > 2 * nl || H < 1 || H > n - 1) {
-      ug_fail(a.err, UG_E_TREE, w);
-      H = 1;
-      for (int k = n; k < nl; k++) h[k] = 1;
-    }
-    int16_t *order = s.sch, *lstart = s.sch + (n - 1);
-    int32_t *cnt = h + nl;  // H + 2 <= n + 1 entries past the heights
-    for (int k = 0; k <= H + 1; k++) cnt[k] = 0;
-    for (int k = n; k < nl; k++) cnt[h[k] + 1]++;
-    for (int k = 1; k <= H + 1; k++) cnt[k] += cnt[k - 1];
-    for (int k = 1; k <= H + 1; k++) lstart[k - 1] = (int16_t)cnt[k];
-    for (int k = n; k < nl; k++) order[cnt[h[k]]++] = (int16_t)k;
-    a.nlev[item] = H;
+    s_root = root;
   }
   __syncwarp();
   rng_store(g, a.rng + w, lane);
+  if (a.hky) {
+    // heights (tips 0, a node one above its higher daughter) by rounds of
+    // relaxation over the internal nodes: heights only grow, towards the
+    // true ones, and a round that changes nothing ends it (at most n)
+    int32_t *h = s.h;
+    for (int k = lane; k < nl; k += 32) h[k] = 0;
+    __syncwarp();
+    bool done = false;
+    for (int round = 0; round <= n && !done; round++) {
+      bool changed = false;
+      for (int k = n + lane; k < nl; k += 32) {
+        const int ha = h[s.nd[k].up0], hb = h[s.nd[k].up1];
+        const int v = 1 + (ha > hb ? ha : hb);
+        if (v != h[k]) {
+          h[k] = v;
+          changed = true;
+        }
+      }
+      done = !__any_sync(~0u, changed);
+    }
+    __syncwarp();
+    int H = h[s_root];
+    if (!done || H < 1 || H > n - 1) {
+      if (lane == 0) ug_fail(a.err, UG_E_TREE, w);
+      H = 1;
+      __syncwarp();
+      for (int k = n + lane; k < nl; k += 32) h[k] = 1;
+    }
+    // the level schedule as the genealogy upload builds it: internal nodes
+    // by height, in index order within a level
+    int16_t *order = s.sch, *lstart = s.sch + (n - 1);
+    int32_t *cnt = h + nl;  // H + 2 <= n + 1 entries past the heights
+    for (int k = lane; k <= H + 1; k += 32) cnt[k] = 0;
+    __syncwarp();
+    for (int k = n + lane; k < nl; k += 32) atomicAdd(&cnt[h[k] + 1], 1);
+    __syncwarp();
+    if (lane == 0) {
+      for (int k = 1; k <= H + 1; k++) {
+        cnt[k] += cnt[k - 1];
+        lstart[k - 1] = (int16_t)cnt[k];
+      }
+      a.nlev[item] = H;
+    }
+    __syncwarp();
+    for (int b0 = n; b0 < nl; b0 += 32) {
+      const int k = b0 + lane;
+      const int hk = k < nl ? h[k] : -1;
+      const unsigned peers = __match_any_sync(~0u, hk);
+      const int rank = __popc(peers & ((1u << lane) - 1u));
+      if (k < nl) order[cnt[hk] + rank] = (int16_t)k;
+      __syncwarp();
+      if (k < nl && rank == 0) cnt[hk] += __popc(peers);
+      __syncwarp();
+    }
+    __syncwarp();
+    for (int k = lane; k < n + H; k += 32) a.sched[it.sched_off + k] = s.sch[k];  // order, then level starts
+  }
   for (int k = lane; k < nl; k += 32) {
     a.nodes[base + k] = s.nd[k];
     const double t = s.t[k];
@@ -427,7 +457,6 @@ __global__ void __launch_bounds__(32) k_ug_propose(UgArgs a)
     a.tff[base + k] = make_float2(hi, (float)(t - (double)hi));
     a.pop[base + k] = s.pop[k];
   }
-  for (int k = lane; k < 2 * n; k += 32) a.sched[it.sched_off + k] = s.sch[k];
   if (lane == 0) a.is_valid[item] = 0;  // the IS site labels follow daughter order, which moved
 }
 
@@ -561,7 +590,8 @@ __global__ void __launch_bounds__(32) k_ug_decide(UgArgs a)
       a.tff[base + j] = make_float2(hi, (float)(t - (double)hi));
       a.pop[base + j] = bkp[j];
     }
-    for (int j = lane; j < 2 * n; j += 32) a.sched[it.sched_off + j] = bks[j];
+    if (a.hky)
+      for (int j = lane; j < 2 * n; j += 32) a.sched[it.sched_off + j] = bks[j];
     if (lane == 0) {
       a.len[item] = a.bk_len[w];
       a.nlev[item] = a.bk_nlev[w];

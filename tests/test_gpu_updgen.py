@@ -146,9 +146,13 @@ def test_updategenealogy_state_carries_between_calls():
 
 def test_updategenealogy_checkpoint_round_trip(tmp_path):
     """Four sweeps, ima_gpu_checkpoint_write, a fresh context restored from
-    the file, six more sweeps: the accepted proposals, final genealogies
-    and G.pdg of the uninterrupted ten-sweep run (the file carries the
-    topologies and level schedules the device changed)."""
+    the file, six more sweeps: the accepted proposals, final genealogies,
+    p(G) and HKY G.pdg of the uninterrupted ten-sweep run (the file carries
+    the topologies and level schedules the device changed).  An IS locus's
+    G.pdg moves by a constant: the reference takes sum log k! from the first
+    genealogy a process evaluates (calc_prob_data.cpp:760-765), and after a
+    restart that is the restored one; differences of G.pdg, and with them
+    the decisions, do not move."""
     case = UgCase()
     u, kap = case.rates()
     tv = np.tile(case.d["tv0"], (case.nch, 1))
@@ -172,7 +176,8 @@ def test_updategenealogy_checkpoint_round_trip(tmp_path):
     rest, _, pg = ctx.updategenealogy_sweep(chains, tv, 6, rngs, u, kap, precision=api.PREC_FP64)
     assert np.array_equal(first + rest, whole)
     np.testing.assert_allclose(pg, pg_whole, rtol=0, atol=1e-9)
-    np.testing.assert_allclose(ctx.get_pdg(), pdg_whole, rtol=0, atol=1e-9)
+    hky = np.array([k == "hky" for k in case.kinds])
+    np.testing.assert_allclose(ctx.get_pdg()[:, hky], pdg_whole[:, hky], rtol=0, atol=1e-9)
     k = 0
     for ci in range(case.nch):
         for li in range(case.nl):
