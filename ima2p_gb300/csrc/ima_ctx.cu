@@ -313,8 +313,10 @@ struct ima_ctx {
   void *d_ug = nullptr;
   size_t ug_cap = 0;
   std::vector<Batch> ugb;
-  cudaStream_t ug_st = nullptr;  // the weights of a step's HKY proposals run here beside their likelihoods
-  cudaEvent_t ug_fork = nullptr, ug_join = nullptr;
+  // the genealogy update's streams: weights, likelihoods and decisions run
+  // behind the proposals (on st), ordered by per-step events
+  cudaStream_t ug_sw = nullptr, ug_sw2 = nullptr, ug_sh = nullptr, ug_sh2 = nullptr, ug_sd = nullptr;
+  std::vector<cudaEvent_t> ug_ev;  // [4][ring slots]: proposal, weights, likelihood, decision done
   // items whose tree lengths are still to be summed from their device times
   // (re-timings without lengths): done when a reader needs them
   int lpend_lo = INT32_MAX, lpend_hi = -1;
@@ -513,9 +515,9 @@ extern "C" void ima_gpu_destroy(ima_ctx *c)
   if (c->t0) cudaEventDestroy(c->t0);
   if (c->t1) cudaEventDestroy(c->t1);
 
-  if (c->ug_fork) cudaEventDestroy(c->ug_fork);
-  if (c->ug_join) cudaEventDestroy(c->ug_join);
-  if (c->ug_st) cudaStreamDestroy(c->ug_st);
+  for (auto e : c->ug_ev) cudaEventDestroy(e);
+  for (cudaStream_t q : {c->ug_sw, c->ug_sw2, c->ug_sh, c->ug_sh2, c->ug_sd})
+    if (q) cudaStreamDestroy(q);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -1571,28 +1573,28 @@ static double sw_bytes(ima_ctx *c, const Batch &b)
 
 // kernels of a batch (no host work, graph-capturable once sumlogk is set)
 // kernels of a batch (no host work, graph-capturable once sumlogk is set)
-static void enqueue(ima_ctx *c, Batch &b)
+static void enqueue(ima_ctx *c, Batch &b, cudaStream_t on = nullptr)
 {
   Pools P = c->pools();
-  cudaStream_t st = c->st;
+  cudaStream_t st = on ? on : c->st;
   if (b.nis)
-    c->launch(IMA_K_IS, 0.0, [&] { launch_is(P, b.d_req, b.nis, b.maxn_is, b.maxs_is, b.d_res, b.d_st, nullptr, st); });
+    c->launch(IMA_K_IS, 0.0, [&] { launch_is(P, b.d_req, b.nis, b.maxn_is, b.maxs_is, b.d_res, b.d_st, nullptr, st); }, st);
   if (b.nhky) {
     const ReqDev *r = b.d_req + b.nis;
     if (b.prec == IMA_PREC_FP64)
-      c->launch(IMA_K_HKY_FP64, b.hky_bytes, [&] { launch_hky_fp64(P, r, b.nhky, b.maxn_hky, b.d_res + b.nis, b.d_st + b.nis, st); });
+      c->launch(IMA_K_HKY_FP64, b.hky_bytes, [&] { launch_hky_fp64(P, r, b.nhky, b.maxn_hky, b.d_res + b.nis, b.d_st + b.nis, st); }, st);
     else if (b.prec == IMA_PREC_FP32)
-      c->launch(IMA_K_HKY_FP32, b.hky_bytes, [&] { launch_hky_fp32(P, r, b.nhky, b.maxn_hky, b.maxs_hky, b.hky_variant, b.d_res + b.nis, b.d_st + b.nis, st); });
+      c->launch(IMA_K_HKY_FP32, b.hky_bytes, [&] { launch_hky_fp32(P, r, b.nhky, b.maxn_hky, b.maxs_hky, b.hky_variant, b.d_res + b.nis, b.d_st + b.nis, st); }, st);
     else
-      c->launch(IMA_K_HKY_FAST, b.hky_bytes, [&] { launch_hky_fast(P, r, b.nhky, b.maxn_hky, b.maxs_hky, b.hky_variant, b.d_res + b.nis, b.d_st + b.nis, st); });
+      c->launch(IMA_K_HKY_FAST, b.hky_bytes, [&] { launch_hky_fast(P, r, b.nhky, b.maxn_hky, b.maxs_hky, b.hky_variant, b.d_res + b.nis, b.d_st + b.nis, st); }, st);
   }
   if (b.nsw) {
     const ReqDev *r = b.d_req + b.nis + b.nhky;
     int off = b.nis + b.nhky;
     if (b.prec == IMA_PREC_FP64)
-      c->launch(IMA_K_SW_FP64, b.sw_bytes, [&] { launch_sw_fp64(P, r, b.nsw, b.d_res + off, b.d_st + off, st); });
+      c->launch(IMA_K_SW_FP64, b.sw_bytes, [&] { launch_sw_fp64(P, r, b.nsw, b.d_res + off, b.d_st + off, st); }, st);
     else
-      c->launch(IMA_K_SW_FAST, b.sw_bytes, [&] { launch_sw_fast(P, r, b.nsw, b.maxn_sw, b.sw_variant, b.d_res + off, b.d_st + off, st); });
+      c->launch(IMA_K_SW_FAST, b.sw_bytes, [&] { launch_sw_fast(P, r, b.nsw, b.maxn_sw, b.sw_variant, b.d_res + off, b.d_st + off, st); }, st);
   }
 }
 
@@ -4155,8 +4157,13 @@ extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t 
   if (!tw_fits(P)) return c->fail(IMA_ERR_TOO_LARGE, "a genealogy has %lld events", Emax);
   // the weights kernel writes every migration cell of the model, nomig or not
   const size_t Etot = (size_t)evoff[ni], M1 = std::max(1, h.M), mx = 2 * (size_t)maxn;
-  const size_t bytes = carve_size({nch * sizeof(ima_ug_rng), nch * 4ul, np * 4, np * 4, nch * mx * sizeof(NodeRec),
-                                   nch * mx * 8, nch * mx * 4, nch * mx * 2, nch * 8ul, nch * 4ul, nch * 8ul, nch * 8ul,
+  // steps in flight: a ring of per-step buffers (backups, proposal flags,
+  // slide terms, acceptance uniforms); at most one sweep of loci deep, so a
+  // locus's batch and weights are never rewritten before their decision ran
+  const int R = std::min(4, nl);
+  const size_t rn = (size_t)R * nch;
+  const size_t bytes = carve_size({nch * sizeof(ima_ug_rng), nch * 4ul, np * 4, np * 4, rn * mx * sizeof(NodeRec),
+                                   rn * mx * 8, rn * mx * 4, rn * mx * 2, rn * 8, rn * 4, rn * 8, rn * 8, rn * 8,
                                    8, nch * T * 4ul, nch * T * 8ul, nch * T * 8ul, nch * (size_t)nth * 8, np * 4, np * 4,
                                    ni * T * 4ul, ni * M1 * 4, ni * 4ul, ni * T * 8ul, ni * T * 8ul, ni * M1 * 8,
                                    2ul * ni * 8, (ni + 1) * 8ul, Etot * 8, Etot * 4, ni * 4ul});
@@ -4172,14 +4179,15 @@ extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t 
   int32_t *d_chains = cv.take<int32_t>(nch);
   int32_t *d_reqof = cv.take<int32_t>(np);
   int32_t *d_perm = cv.take<int32_t>(np);
-  a.bk_nodes = cv.take<NodeRec>(nch * mx);
-  a.bk_t = cv.take<double>(nch * mx);
-  a.bk_pop = cv.take<int32_t>(nch * mx);
-  a.bk_sched = cv.take<int16_t>(nch * mx);
-  a.bk_len = cv.take<double>(nch);
-  a.bk_nlev = cv.take<int32_t>(nch);
-  a.prop = reinterpret_cast<int32_t *>(cv.take<double>(nch));
-  a.slidew = cv.take<double>(nch);
+  a.bk_nodes = cv.take<NodeRec>(rn * mx);
+  a.bk_t = cv.take<double>(rn * mx);
+  a.bk_pop = cv.take<int32_t>(rn * mx);
+  a.bk_sched = cv.take<int16_t>(rn * mx);
+  a.bk_len = cv.take<double>(rn);
+  a.bk_nlev = cv.take<int32_t>(rn);
+  a.prop = reinterpret_cast<int32_t *>(cv.take<double>(rn));
+  a.slidew = cv.take<double>(rn);
+  a.ustore = cv.take<double>(rn);
   a.err = cv.take<int32_t>(2);
   a.ag_cc = cv.take<int32_t>(nch * (size_t)T);
   a.ag_fc = cv.take<double>(nch * (size_t)T);
@@ -4282,45 +4290,79 @@ extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t 
   a.fresh32 = c->d_fresh32;
   a.slot64 = c->d_slot64;
   a.fresh64 = c->d_fresh64;
-  if (!c->ug_st) {
-    r = c->cuda(cudaStreamCreateWithFlags(&c->ug_st, cudaStreamNonBlocking), "stream");
-    r = r ? r : c->cuda(cudaEventCreateWithFlags(&c->ug_fork, cudaEventDisableTiming), "events");
-    r = r ? r : c->cuda(cudaEventCreateWithFlags(&c->ug_join, cudaEventDisableTiming), "events");
+  if (!c->ug_sd) {
+    for (cudaStream_t *q : {&c->ug_sw, &c->ug_sw2, &c->ug_sh, &c->ug_sh2, &c->ug_sd})
+      r = r ? r : c->cuda(cudaStreamCreateWithFlags(q, cudaStreamNonBlocking), "streams");
     if (r) return r;
   }
-  // the steps: one locus of every listed chain at a time.  An HKY step runs
-  // the proposed genealogies' weights on a second stream beside their
-  // likelihoods (neither reads the other's output); an IS step runs them
-  // first, as the IS likelihood reads the lengths they write
+  while ((int)c->ug_ev.size() < 16) {
+    cudaEvent_t e;
+    r = c->cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "events");
+    if (r) return r;
+    c->ug_ev.push_back(e);
+  }
+  cudaEvent_t *evP = c->ug_ev.data(), *evW = evP + 4, *evH = evP + 8, *evD = evP + 12;
+  // The steps: one locus of every listed chain at a time.  Each chain's
+  // proposals follow one another on st (they share its generator), its
+  // decisions on ug_sd (they share its sums); a step's weights and its
+  // likelihoods (each on two streams used by turns: consecutive steps touch
+  // different loci) wait for its proposal, its decision for both and
+  // for the previous decision.  So proposals, weights and likelihoods of
+  // the next steps run while a decision does, up to R steps ahead.  After an
+  // IS step the next proposal waits for the decision: an IS decision draws
+  // the acceptance uniform only when the likelihood does not reject, so the
+  // generator's position is known only then (an HKY proposal draws it
+  // itself, next in the stream, as the reference always does).
+  const UgArgs a0 = a;
+  long long step = 0;
+  int prev_is = 0;
   for (int s = 0; s < nsweeps && !r; s++)
-    for (int l = 0; l < nl && !r; l++) {
+    for (int l = 0; l < nl && !r; l++, step++) {
+      const int slot = (int)(step % R);
+      const size_t so = (size_t)slot * nch;
       Batch &b = c->ugb[l];
-      a.locus = l;
-      a.hky = c->loci[l].d.model == IMA_MODEL_HKY;
-      a.req = b.d_req;
-      a.req_of = d_reqof + (size_t)l * nch;
-      a.res = b.d_res;
-      a.st = b.d_st;
-      c->launch(IMA_K_UG, 0.0, [&] { launch_ug_propose(a, c->st); });
+      UgArgs u_ = a0;
+      u_.locus = l;
+      u_.hky = c->loci[l].d.model == IMA_MODEL_HKY;
+      u_.predraw = u_.hky;
+      u_.req = b.d_req;
+      u_.req_of = d_reqof + (size_t)l * nch;
+      u_.res = b.d_res;
+      u_.st = b.d_st;
+      u_.bk_nodes = a0.bk_nodes + so * mx;
+      u_.bk_t = a0.bk_t + so * mx;
+      u_.bk_pop = a0.bk_pop + so * mx;
+      u_.bk_sched = a0.bk_sched + so * mx;
+      u_.bk_len = a0.bk_len + so;
+      u_.bk_nlev = a0.bk_nlev + so;
+      u_.prop = a0.prop + 2 * so;
+      u_.slidew = a0.slidew + so;
+      u_.ustore = a0.ustore + so;
+      if (step >= R) cudaStreamWaitEvent(c->st, evD[slot], 0);
+      if (prev_is) cudaStreamWaitEvent(c->st, evD[(step - 1) % R], 0);
+      c->launch(IMA_K_UG, 0.0, [&] { launch_ug_propose(u_, c->st); });
+      cudaEventRecord(evP[slot], c->st);
       w.perm = d_perm + (size_t)l * nch;
-      cudaStream_t tws = c->st;
-      if (a.hky) {
-        cudaEventRecord(c->ug_fork, c->st);
-        cudaStreamWaitEvent(c->ug_st, c->ug_fork, 0);
-        tws = c->ug_st;
-      }
+      cudaStream_t sw = (step & 1) ? c->ug_sw2 : c->ug_sw;
+      cudaStreamWaitEvent(sw, evP[slot], 0);
       int lr = 0;
-      c->launch(IMA_K_TREEWEIGHT, 0.0, [&] { lr = launch_treeweight(w, h, tws); }, tws);
+      c->launch(IMA_K_TREEWEIGHT, 0.0, [&] { lr = launch_treeweight(w, h, sw); }, sw);
       if (lr < 0) return c->fail(IMA_ERR_TOO_LARGE, "treeweight: shared memory for %d events", P);
       c->launches += lr - 1;
-      enqueue(c, b);
-      if (a.hky) {
-        cudaEventRecord(c->ug_join, c->ug_st);
-        cudaStreamWaitEvent(c->st, c->ug_join, 0);
-      }
-      c->launch(IMA_K_UG, 0.0, [&] { launch_ug_decide(a, c->st); });
+      cudaEventRecord(evW[slot], sw);
+      cudaStream_t sh = (step & 1) ? c->ug_sh2 : c->ug_sh;
+      cudaStreamWaitEvent(sh, evP[slot], 0);
+      if (!u_.hky) cudaStreamWaitEvent(sh, evW[slot], 0);  // the IS likelihood reads the new lengths
+      enqueue(c, b, sh);
+      cudaEventRecord(evH[slot], sh);
+      cudaStreamWaitEvent(c->ug_sd, evW[slot], 0);
+      cudaStreamWaitEvent(c->ug_sd, evH[slot], 0);
+      c->launch(IMA_K_UG, 0.0, [&] { launch_ug_decide(u_, c->ug_sd); }, c->ug_sd);
+      cudaEventRecord(evD[slot], c->ug_sd);
+      prev_is = !u_.hky;
       r = c->cuda(cudaGetLastError(), "genealogy update launch");
     }
+  if (step > 0) cudaStreamWaitEvent(c->st, evD[(step - 1) % R], 0);  // st carries on after the last decision
   // the device's genealogies are newer than the mirror from here on
   for (int k = 0; k < nch; k++) {
     c->topo_lo = std::min(c->topo_lo, chains[k] * nl);

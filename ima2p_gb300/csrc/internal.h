@@ -328,6 +328,11 @@ struct UgArgs {
   int32_t *bk_nlev;                        // [nch]
   int32_t *prop;                           // [nch][2]: topology changed, tmrca changed
   double *slidew;                          // [nch] the slide's Hastings term
+  // predraw: the proposal draws the acceptance uniform itself, right after
+  // its own draws, into ustore [nch] (an HKY locus always draws it, so the
+  // stream's order is the reference's); otherwise the decision draws it
+  int predraw;
+  double *ustore;
   int32_t *err;                            // {code, listed chain} of the first failure
   // the decision
   const double *res;                       // the batch's results

@@ -388,6 +388,7 @@ __global__ void __launch_bounds__(32) k_ug_propose(UgArgs a)
       R.e[2] = oldsis;
       R.e[3] = newsis;
     }
+    if (a.predraw) a.ustore[w] = uniform(g);  // the acceptance uniform, next in the stream
     s_root = root;
   }
   __syncwarp();
@@ -521,8 +522,8 @@ __global__ void __launch_bounds__(32) k_ug_decide(UgArgs a)
   // the acceptance uniform: one word of the chain's MT19937, or the whole
   // state staged for a twist
   int mti = 0;
-  if (decide) mti = a.rng[w].mt.mti;
-  const bool stage = decide && mti >= 624;
+  if (decide && !a.predraw) mti = a.rng[w].mt.mti;
+  const bool stage = decide && !a.predraw && mti >= 624;
   __shared__ __align__(16) uint32_t s_mt[624];  // read as 8-byte words
   LocalRng g{};
   if (stage) rng_load(g, a.rng + w, s_mt, lane);
@@ -539,7 +540,9 @@ __global__ void __launch_bounds__(32) k_ug_decide(UgArgs a)
       double mh = tpw + a.gbeta * (pdgnew - a.pdg[item]);
       mh = exp(a.beta[ci] * mh + a.slidew[w]);
       double U;
-      if (stage) {
+      if (a.predraw) {
+        U = a.ustore[w];
+      } else if (stage) {
         U = uniform(g);
       } else {
         uint32_t y = a.rng[w].mt.mt[mti];
