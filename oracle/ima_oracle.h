@@ -84,8 +84,9 @@ void ora_ug_rng_seed(ora_ug_rng *g, int seed); /* setseeds (utilities.cpp:399-40
  * chains, each from its own generator, chains spread over nthreads host
  * threads.  Genealogies of chain c, locus l at node_off[c*nloci+l] in up0 /
  * up1 / down / time / pop (updated in place); loci: model 0 IS (seq, S
- * sites, sumlogk) or 1 HKY (seq patterns, mult, totsites; pi per
- * chain-locus).  The chain's state starts as finish_setup_C leaves it.  res
+ * sites, sumlogk), 1 HKY (seq patterns, mult, totsites; pi per
+ * chain-locus) or 2 SW (one marker: arange[2l], arange[2l+1] its allele
+ * range; the alleles of every node in `alleles`, updated in place).  The chain's state starts as finish_setup_C leaves it.  res
  * [nchains][nsweeps][nloci][3] (accepted, topology changed, tmrca changed)
  * and resd [...][2] (G.pdg, p(G) after the proposal) may be NULL; pdg_out
  * [nchains*nloci], probg_out [nchains].  Returns 0, or 1 a slide that did not
@@ -95,8 +96,8 @@ int ora_ug_run(int npops, const int *plist, const int *droppops, const int *addp
                const int *pop_down, int nth, const int *th_off, const int *th_idx, const double *th_max,
                const double *th_min, int nloci, const int *model, const int *n, const int *S, const int *totsites,
                const long long *seq_off, const long long *mult_off, const int8_t *seq, const int *mult,
-               const double *hval, const int *samppop, const double *sumlogk, int nchains,
-               const long long *node_off, int *up0, int *up1, int *down, double *time, int *pop,
+               const double *hval, const int *samppop, const double *sumlogk, const int *arange, int nchains,
+               const long long *node_off, int *up0, int *up1, int *down, double *time, int *pop, int *alleles,
                const double *tvals, const double *beta, double gbeta, const double *u, const double *kappa,
                const double *pi, int nsweeps, ora_ug_rng *rng, int nthreads, int *res, double *resd,
                double *pdg_out, double *probg_out);

@@ -13,8 +13,14 @@
  * full, ora_hky_likelihood from the four edited edges) and the
  * Metropolis-Hastings decision with one uniform (none when the IS
  * likelihood rejects).  A rejection restores the genealogy, its weights and
- * the HKY scale factors.  Each chain draws from its own generators
- * (ora_ug_rng), as the device form does; chains run on host threads. */
+ * the HKY scale factors.  Stepwise loci (one marker) take finishSWupdateA
+ * (update_gtree_common.cpp:2219-2362) for the likelihood change: a new allele
+ * for the freed node drawn around its neighbours' (geometric, bitran), the
+ * moved branches' terms, and the allele proposal's Hastings term; a
+ * rejection restores them as restoreedges does (:706-825), which leaves the
+ * new sister's term in place when it was 0 before (the root edge's).  Each
+ * chain draws from its own generators (ora_ug_rng), as the device form does;
+ * chains run on host threads. */
 #include <math.h>
 #include <pthread.h>
 #include <stdint.h>
@@ -96,6 +102,8 @@ typedef struct {
   const double *hval;
   const int *samppop;
   const double *sumlogk;
+  const int *arange;   /* SW: [nloci][2] minA, maxA */
+  int *alleles;        /* SW: per node, in place */
   int nchains;
   const long long *node_off;
   int *up0, *up1, *down, *pop;
@@ -134,7 +142,7 @@ static double ug_jointime(const ug_job *J, const double *tv, int slidepop, int s
  * out: e[4] = edge, freed, oldsis, newsis; *topol, *tmrca, *sw; returns 0 or
  * 1 for a slide that did not end / a root beyond TIMEMAX */
 static int ug_propose(const ug_job *J, const double *tv, ora_ug_rng *g, int n, int *up0, int *up1, int *down,
-                      double *t, int *pop, int *e, int *topol, int *tmrca, double *sw)
+                      double *t, int *pop, double *dl, int *e, int *topol, int *tmrca, double *sw)
 {
   const int nl = 2 * n - 1, nsplit = J->npops - 1;
   int root = -1;
@@ -168,6 +176,7 @@ static int ug_propose(const ug_job *J, const double *tv, ora_ug_rng *g, int n, i
       root = oldsis;
       down[oldsis] = -1;
       t[oldsis] = UG_TIMEMAX;
+      if (dl) dl[oldsis] = 0;
       roottime = uptime;
     }
   }
@@ -244,6 +253,7 @@ static int ug_propose(const ug_job *J, const double *tv, ora_ug_rng *g, int n, i
       roottime = curt;
       rootmove = 1;
       if (roottime > UG_TIMEMAX) bad = 1;
+      if (dl) dl[freed] = 0;
     }
     down[freed] = dd;
     int nowpop = pop[newsis];
@@ -267,6 +277,68 @@ static int ug_propose(const ug_job *J, const double *tv, ora_ug_rng *g, int n, i
   e[3] = newsis;
   *topol = (oldsis != newsis);
   return bad;
+}
+
+/* finishSWupdateA (update_gtree_common.cpp:2219-2362) for one marker on the
+ * proposed genealogy; bkA/bkdl/bkdown: the alleles, terms and parents
+ * before the proposal (storeoldedges' copies).  Returns likeadj - oldlikeadj;
+ * *aterm the allele proposal's Hastings term, *holdsis the new sister's
+ * term before the update (restoreedges puts it back only when nonzero). */
+static double ug_sw_update(ora_ug_rng *g, int n, const int *up0, const int *down, const double *t, int *A, double *dl,
+                           int edge, int freed, int oldsis, int newsis, double u, int minA, int maxA,
+                           const int *bkA, const double *bkdl, const int *bkdown, double *aterm, double *holdsis)
+{
+  const int oldA = A[freed];
+  *holdsis = (newsis != oldsis) ? dl[newsis] : 0.0;
+  const double cp2 = bkdown[freed] != -1 ? bkdl[freed] : 0.0;
+  const int holddownA = bkdown[freed] != -1 ? bkA[bkdown[freed]] : -1;
+  const double oldlikeadj = bkdl[edge] + bkdl[oldsis] + cp2 + *holdsis;
+  const int e[3] = {edge, newsis, down[edge]};
+  double tt[3] = {0.0, 0.0, 0.0};
+  for (int i = 0; i < 3; i++) {
+    const double upt = e[i] >= n ? t[up0[e[i]]] : 0.0;
+    if (down[e[i]] != -1) tt[i] = t[e[i]] - upt;
+  }
+  int wsumdiff = 0, j = 0;
+  for (int i = 0; i < 3; i++)
+    if (down[e[i]] != -1) {
+      const int d = (i < 2 ? A[e[i]] : A[down[e[i]]]) - oldA;
+      wsumdiff += abs(d);
+      j++;
+    }
+  double geotermnew = j / ((double)(wsumdiff + j));
+  if (geotermnew > 0.95) geotermnew = 0.95;
+  int dA = (int)ceil(log(ug_uniform(g)) / log(1.0 - geotermnew)) - 1;
+  if (ug_bitran(g)) dA = -dA;
+  int newA;
+  if (dA >= 0) newA = (maxA < oldA + dA) ? maxA : oldA + dA;
+  else newA = (minA > oldA + dA) ? minA : oldA + dA;
+  A[freed] = newA;
+  dA = newA - oldA;
+  if (down[oldsis] != -1 && oldsis != newsis) {
+    const double upt = oldsis >= n ? t[up0[oldsis]] : 0.0;
+    const int d = A[oldsis] - A[down[oldsis]];
+    dl[oldsis] = -(t[oldsis] - upt) * u + log(ora_bessi(d, (t[oldsis] - upt) * u));
+  } else {
+    dl[oldsis] = 0;
+  }
+  double likeadj = dl[oldsis];
+  for (int i = 0; i < 3; i++)
+    if (down[e[i]] != -1) {
+      const int d = (i < 2 ? A[e[i]] : A[down[e[i]]]) - newA;
+      dl[e[i]] = -(tt[i] * u) + log(ora_bessi(d, tt[i] * u));
+      likeadj += dl[e[i]];
+    }
+  wsumdiff = abs(bkA[edge] - newA) + abs(bkA[oldsis] - newA);
+  j = 2;
+  if (bkdown[freed] != -1) {
+    wsumdiff += abs(holddownA - newA);
+    j++;
+  }
+  double geotermold = j / ((double)(wsumdiff + j));
+  if (geotermold > 0.95) geotermold = 0.95;
+  *aterm = (abs(dA) * log(1 - geotermold) + log(geotermold)) - (abs(dA) * log(1 - geotermnew) + log(geotermnew));
+  return likeadj - oldlikeadj;
 }
 
 static int ug_root(int nl, const int *down)
@@ -303,9 +375,12 @@ static int ug_chain(ug_job *J, int c)
   int *bk = (int *)malloc(sizeof(int) * 4 * (size_t)mnl);
   double *bkt = (double *)malloc(sizeof(double) * (size_t)mnl);
   double **frac = (double **)calloc(nl_, sizeof(double *));
+  double **dls = (double **)calloc(nl_, sizeof(double *));  /* SW: the branch terms (dlikeA) */
+  int *bkA = (int *)malloc(sizeof(int) * (size_t)mnl);
+  double *bkdl = (double *)malloc(sizeof(double) * (size_t)mnl);
   int err = 0;
   if (!wcc || !ncc || !wfc || !whc || !nfc || !nhc || !mc || !fm || !agc || !sgc || !agf || !agh || !sgf || !sgh ||
-      !qint || !nq || !len || !pdg || !moff || !bk || !bkt || !frac) {
+      !qint || !nq || !len || !pdg || !moff || !bk || !bkt || !frac || !dls || !bkA || !bkdl) {
     err = 5;
     goto out;
   }
@@ -331,7 +406,11 @@ static int ug_chain(ug_job *J, int c)
     const int8_t *sq = J->seq + J->seq_off[l];
     const double uu = J->u[(size_t)c * nl_ + l];
     int st = 0;
-    if (J->model[l] == 1) {
+    if (J->model[l] == 2) {
+      dls[l] = (double *)calloc((size_t)nl, sizeof(double));
+      if (!dls[l]) { err = 5; break; }
+      pdg[l] = ora_sw_likelihood(n, J->alleles + o, dn, u0, t, uu, 1.0, dls[l]);
+    } else if (J->model[l] == 1) {
       frac[l] = (double *)calloc((size_t)nl * S * 10, sizeof(double));
       if (!frac[l]) { err = 5; break; }
       double *f = frac[l], *nf = f + (size_t)nl * S * 4, *sf = nf + (size_t)nl * S * 4, *osf = sf + (size_t)nl * S;
@@ -365,9 +444,15 @@ static int ug_chain(ug_job *J, int c)
       memcpy(bk + 2 * mnl, dn, sizeof(int) * nl);
       memcpy(bk + 3 * mnl, pp, sizeof(int) * nl);
       memcpy(bkt, t, sizeof(double) * nl);
+      int *A = J->model[l] == 2 ? J->alleles + o : NULL;
+      double *dl = dls[l];
+      if (A) {
+        memcpy(bkA, A, sizeof(int) * nl);
+        memcpy(bkdl, dl, sizeof(double) * nl);
+      }
       int e[4], topol, tmrca, acc = 0;
       double sw;
-      if (ug_propose(J, tv, g, n, u0, u1, dn, t, pp, e, &topol, &tmrca, &sw)) {
+      if (ug_propose(J, tv, g, n, u0, u1, dn, t, pp, dl, e, &topol, &tmrca, &sw)) {
         err = 1;
         break;
       }
@@ -381,10 +466,14 @@ static int ug_chain(ug_job *J, int c)
       }
       const int8_t *sq = J->seq + J->seq_off[l];
       const double uu = J->u[(size_t)c * nl_ + l];
-      double newpdg;
+      double newpdg, aterm = 0.0, holdsis = 0.0;
       int rejectIS = 0, st = 0;
       double *f = NULL, *nf = NULL, *sf = NULL, *osf = NULL;
-      if (J->model[l] == 1) {
+      if (A) {
+        const double dlt = ug_sw_update(g, n, u0, dn, t, A, dl, e[0], e[1], e[2], e[3], uu, J->arange[2 * l],
+                                        J->arange[2 * l + 1], bkA, bkdl, bk + 2 * mnl, &aterm, &holdsis);
+        newpdg = 0.0 + (pdg[l] + dlt);
+      } else if (J->model[l] == 1) {
         f = frac[l];
         nf = f + (size_t)nl * S * 4;
         sf = nf + (size_t)nl * S * 4;
@@ -436,7 +525,7 @@ static int ug_chain(ug_job *J, int c)
         double tpw = -probg;
         tpw += psum;
         double mh = tpw + J->gbeta * (newpdg - pdg[l]);
-        mh = exp(J->beta[c] * mh + sw);
+        mh = exp(J->beta[c] * mh + sw + aterm);
         const double U = ug_uniform(g);
         acc = U < ug_dmin(1.0, mh);
       }
@@ -462,6 +551,14 @@ static int ug_chain(ug_job *J, int c)
         memcpy(pp, bk + 3 * mnl, sizeof(int) * nl);
         memcpy(t, bkt, sizeof(double) * nl);
         if (f) ora_hky_restorescalefactors(n, S, sf, osf);
+        if (A) {  /* restoreedges: the three moved edges from their copies, the new sister only if nonzero */
+          const int freed = e[1], oldsis = e[2], newsis = e[3];
+          A[freed] = bkA[freed];
+          dl[e[0]] = bkdl[e[0]];
+          dl[oldsis] = bkdl[oldsis];
+          dl[freed] = bk[2 * mnl + freed] != -1 ? bkdl[freed] : 0.0;
+          if (holdsis != 0) dl[newsis] = holdsis;
+        }
         topol = tmrca = 0;
       }
       const size_t r = ((size_t)c * J->nsweeps + s) * nl_ + l;
@@ -484,6 +581,11 @@ out:
   if (frac)
     for (int l = 0; l < nl_; l++) free(frac[l]);
   free(frac);
+  if (dls)
+    for (int l = 0; l < nl_; l++) free(dls[l]);
+  free(dls);
+  free(bkA);
+  free(bkdl);
   free(wcc); free(ncc); free(wfc); free(whc); free(nfc); free(nhc); free(mc); free(fm);
   free(agc); free(sgc); free(agf); free(agh); free(sgf); free(sgh); free(qint); free(nq);
   free(len); free(pdg); free(moff); free(bk); free(bkt);
@@ -506,15 +608,16 @@ int ora_ug_run(int npops, const int *plist, const int *droppops, const int *addp
                const int *pop_down, int nth, const int *th_off, const int *th_idx, const double *th_max,
                const double *th_min, int nloci, const int *model, const int *n, const int *S, const int *totsites,
                const long long *seq_off, const long long *mult_off, const int8_t *seq, const int *mult,
-               const double *hval, const int *samppop, const double *sumlogk, int nchains,
-               const long long *node_off, int *up0, int *up1, int *down, double *time, int *pop,
+               const double *hval, const int *samppop, const double *sumlogk, const int *arange, int nchains,
+               const long long *node_off, int *up0, int *up1, int *down, double *time, int *pop, int *alleles,
                const double *tvals, const double *beta, double gbeta, const double *u, const double *kappa,
                const double *pi, int nsweeps, ora_ug_rng *rng, int nthreads, int *res, double *resd,
                double *pdg_out, double *probg_out)
 {
   ug_job J = {npops, plist, droppops, addpop, pop_e, pop_down, nth, th_off, th_idx, th_max, th_min, nloci, model,
-              n, S, totsites, seq_off, mult_off, seq, mult, hval, samppop, sumlogk, nchains, node_off, up0, up1,
-              down, pop, time, tvals, beta, u, kappa, pi, gbeta, nsweeps, rng, res, resd, pdg_out, probg_out, 0, 0};
+              n, S, totsites, seq_off, mult_off, seq, mult, hval, samppop, sumlogk, arange, alleles, nchains,
+              node_off, up0, up1, down, pop, time, tvals, beta, u, kappa, pi, gbeta, nsweeps, rng, res, resd,
+              pdg_out, probg_out, 0, 0};
   if (nthreads < 1) nthreads = 1;
   if (nthreads > nchains) nthreads = nchains;
   if (nthreads == 1) {

@@ -105,9 +105,9 @@ def _declare(L):
     L.ora_gsamp_row.restype = None
     L.ora_ug_rng_seed.argtypes = [P, I]
     L.ora_ug_rng_seed.restype = None
-    # model (npops + 5 tables), theta maps (nth + 4), loci (nloci + 11), chains
-    # (nchains + 8), gbeta + 3 rate arrays, nsweeps, rng, nthreads, 4 outputs
-    L.ora_ug_run.argtypes = ([I] + [P] * 5 + [I] + [P] * 4 + [I] + [P] * 11 + [I] + [P] * 8 + [D] + [P] * 3 +
+    # model (npops + 5 tables), theta maps (nth + 4), loci (nloci + 12), chains
+    # (nchains + 9), gbeta + 3 rate arrays, nsweeps, rng, nthreads, 4 outputs
+    L.ora_ug_run.argtypes = ([I] + [P] * 5 + [I] + [P] * 4 + [I] + [P] * 12 + [I] + [P] * 9 + [D] + [P] * 3 +
                              [I, P, I] + [P] * 4)
     L.ora_ug_run.restype = I
 
@@ -716,20 +716,24 @@ def ref_ry(npops, treestr, tprior, loci, chains, gens, steps, seed, thetaprior, 
     return res, times, migt
 
 
-def ref_ug(npops, treestr, thetaprior, loci, chains, gens, nsweeps):
+def ref_ug(npops, treestr, thetaprior, loci, chains, gens, nsweeps, alleles=None):
     """The reference's genealogy update updategenealogy under the
     no-migration model through oracle/_ref/imaref (this container only).
-    loci: ("is", numgenes, hval, samppop, u, seq[n][S]) or ("hky", numgenes,
-    hval, samppop, u, HKYLocus, kappa); chains: (tvals, beta, seed);
-    gens[ci][li]: LabelledGenealogy (no migration events).  Each chain runs
-    nsweeps sweeps over its loci from setseeds(seed).  Returns (per proposal
-    (ci, li, accepted, topolchange, tmrcachange, pdg, probg), final trees
-    {(ci, li): (up0, up1, down, time, pop)})."""
+    loci: ("is", numgenes, hval, samppop, u, seq[n][S]), ("hky", numgenes,
+    hval, samppop, u, HKYLocus, kappa) or ("sw", numgenes, hval, samppop, u,
+    minA, maxA); chains: (tvals, beta, seed); gens[ci][li]:
+    LabelledGenealogy (no migration events); alleles[(ci, li)]: the SW
+    loci's alleles of every node.  Each chain runs nsweeps sweeps over its
+    loci from setseeds(seed).  Returns (per proposal (ci, li, accepted,
+    topolchange, tmrcachange, pdg, probg), final trees {(ci, li): (up0, up1,
+    down, time, pop[, A])})."""
     nch, nl = len(chains), len(loci)
     t = ["%d %d %d %d" % (npops, nch, nl, nsweeps), treestr, "%.17g" % thetaprior]
     for loc in loci:
         kind, ng, h, sp, u = loc[:5]
-        if kind == "is":
+        if kind == "sw":
+            t.append("2 %d %.17g %s %.17g %d %d" % (ng, h, " ".join(map(str, sp)), u, loc[5], loc[6]))
+        elif kind == "is":
             seq = np.asarray(loc[5])
             t.append("0 %d %.17g %s %.17g %d" % (ng, h, " ".join(map(str, sp)), u, seq.shape[1]))
             t.append(" ".join(map(str, seq.ravel())))
@@ -746,6 +750,8 @@ def ref_ug(npops, treestr, thetaprior, loci, chains, gens, nsweeps):
             lg = gens[ci][li]
             t.append(str(len(lg.pop)))
             t.append(_tree_txt(lg.g) + " ".join(map(str, lg.pop)))
+            if loci[li][0] == "sw":
+                t.append(" ".join(map(str, alleles[(ci, li)])))
     out = run_ref("ug", "\n".join(t) + "\n")
     res, trees = [], {}
     for ln in out.splitlines():
@@ -754,11 +760,15 @@ def ref_ug(npops, treestr, thetaprior, loci, chains, gens, nsweeps):
             res.append((int(f[1]), int(f[2]), int(f[3]), int(f[4]), int(f[5]), float(f[6]), float(f[7])))
         elif f[0] == "TREE":
             ci, li = int(f[1]), int(f[2])
-            m = (len(f) - 3) // 5
+            k = 6 if loci[li][0] == "sw" else 5
+            m = (len(f) - 3) // k
             v = f[3:]
-            trees[(ci, li)] = (np.array(v[0:m], np.int32), np.array(v[m:2 * m], np.int32),
-                               np.array(v[2 * m:3 * m], np.int32), np.array([float(x) for x in v[3 * m:4 * m]]),
-                               np.array(v[4 * m:5 * m], np.int32))
+            tr = (np.array(v[0:m], np.int32), np.array(v[m:2 * m], np.int32),
+                  np.array(v[2 * m:3 * m], np.int32), np.array([float(x) for x in v[3 * m:4 * m]]),
+                  np.array(v[4 * m:5 * m], np.int32))
+            if k == 6:
+                tr = tr + (np.array(v[5 * m:6 * m], np.int32),)
+            trees[(ci, li)] = tr
     return res, trees
 
 
@@ -776,14 +786,17 @@ class UgRng(C.Structure):
 
 class UgLoci:
     """The loci of an updategenealogy run packed for ora_ug_run: per locus
-    ("is", seq, sumlogk) or ("hky", HKYLocus-like (seq, mult, totsites))."""
+    ("is", seq, sumlogk), ("hky", HKYLocus-like (seq, mult, totsites)) or
+    ("sw", numgenes, minA, maxA)."""
 
     def __init__(self, loci, hval, samppop):
         self.nloci = len(loci)
-        self.model = _i32([0 if l[0] == "is" else 1 for l in loci])
-        seqs = [np.ascontiguousarray(l[1].seq if l[0] == "hky" else l[1], np.int8) for l in loci]
+        self.model = _i32([{"is": 0, "hky": 1, "sw": 2}[l[0]] for l in loci])
+        seqs = [np.zeros((l[1], 1), np.int8) if l[0] == "sw" else
+                np.ascontiguousarray(l[1].seq if l[0] == "hky" else l[1], np.int8) for l in loci]
         self.n = _i32([q.shape[0] for q in seqs])
         self.S = _i32([q.shape[1] for q in seqs])
+        self.arange = _i32([[l[2], l[3]] if l[0] == "sw" else [0, 0] for l in loci]).ravel()
         self.totsites = _i32([l[1].totsites if l[0] == "hky" else 0 for l in loci])
         self.seq_off = np.concatenate([[0], np.cumsum([q.size for q in seqs])[:-1]]).astype(np.int64)
         self.seq = np.concatenate([q.ravel() for q in seqs]).astype(np.int8)
@@ -796,12 +809,13 @@ class UgLoci:
 
 
 def ug_run(pm, th_max, th_min, loci, gens, tvals, betas, u, kappa, pi, nsweeps, rngs, gbeta=1.0, nthreads=1,
-           record=True):
+           record=True, alleles=None):
     """ora_ug_run: nsweeps genealogy updates (no-migration model) of every
-    chain; gens[c][l] LabelledGenealogy (copied, not changed); rngs UgRng per
-    chain (advanced).  Returns (status, res [nch][nsweeps][nloci][3] or None,
-    resd [...][2] or None, pdg [nch][nloci], probg [nch], final genealogies
-    (up0, up1, down, time, pop) flat in chain-locus order)."""
+    chain; gens[c][l] LabelledGenealogy (copied, not changed); alleles[(c,
+    l)] the SW loci's alleles of every node; rngs UgRng per chain
+    (advanced).  Returns (status, res [nch][nsweeps][nloci][3] or None, resd
+    [...][2] or None, pdg [nch][nloci], probg [nch], final genealogies (up0,
+    up1, down, time, pop, A) flat in chain-locus order)."""
     nch, nl = len(gens), loci.nloci
     flat = [lg for row in gens for lg in row]
     lens = [len(lg.pop) for lg in flat]
@@ -811,6 +825,15 @@ def ug_run(pm, th_max, th_min, loci, gens, tvals, betas, u, kappa, pi, nsweeps, 
     down = _i32(np.concatenate([lg.g.down for lg in flat])).copy()
     time = _f64(np.concatenate([lg.g.time for lg in flat])).copy()
     pop = _i32(np.concatenate([lg.pop for lg in flat])).copy()
+    A = np.zeros(len(pop), np.int32)
+    if alleles:
+        k = 0
+        for c in range(nch):
+            for l in range(nl):
+                m = len(gens[c][l].pop)
+                if (c, l) in alleles:
+                    A[k:k + m] = alleles[(c, l)]
+                k += m
     tho, thi = pm.th_csr()
     arr = (UgRng * nch)(*rngs)
     res = np.zeros((nch, nsweeps, nl, 3), np.int32) if record else None
@@ -821,14 +844,14 @@ def ug_run(pm, th_max, th_min, loci, gens, tvals, betas, u, kappa, pi, nsweeps, 
                           _p(_i32(pm.pop_e)), _p(_i32(pm.pop_down)), len(pm.th_cells), _p(tho), _p(thi),
                           _p(_f64(th_max)), _p(_f64(th_min)), nl, _p(loci.model), _p(loci.n), _p(loci.S),
                           _p(loci.totsites), _p(loci.seq_off), _p(loci.mult_off), _p(loci.seq), _p(loci.mult),
-                          _p(loci.hval), _p(loci.samppop), _p(loci.sumlogk), nch, _p(node_off), _p(up0), _p(up1),
-                          _p(down), _p(time), _p(pop), _p(tv), _p(_f64(betas)), float(gbeta),
+                          _p(loci.hval), _p(loci.samppop), _p(loci.sumlogk), _p(loci.arange), nch, _p(node_off),
+                          _p(up0), _p(up1), _p(down), _p(time), _p(pop), _p(A), _p(tv), _p(_f64(betas)), float(gbeta),
                           _p(_f64(np.asarray(u).reshape(-1))), _p(_f64(np.asarray(kappa).reshape(-1))),
                           _p(_f64(np.asarray(pi).reshape(-1))), int(nsweeps), C.cast(arr, P), int(nthreads),
                           _p(res), _p(resd), _p(pdg), _p(probg))
     for k in range(nch):
         C.memmove(C.addressof(rngs[k]), C.addressof(arr[k]), C.sizeof(UgRng))
-    return st, res, resd, pdg, probg, (up0, up1, down, time, pop)
+    return st, res, resd, pdg, probg, (up0, up1, down, time, pop, A)
 
 
 # ------------------------------------------------------------- batches

@@ -665,10 +665,12 @@ static void run_ry()
 }
 
 /* UG: npops nchains nloci nsweeps treestring thetaprior
- *     per locus: model(0 IS, 1 HKY) numgenes hval samppop[npops] u numsites
- *       seq[numgenes*numsites]; HKY adds totsites mult[numsites] pi[4] kappa
+ *     per locus: model(0 IS, 1 HKY, 2 SW) numgenes hval samppop[npops] u, then
+ *       IS/HKY: numsites seq[numgenes*numsites]; HKY adds totsites
+ *       mult[numsites] pi[4] kappa; SW (one marker): minA maxA
  *     per chain: tvals[npops-1] beta seed
- *     per chain, per locus: nlines up0[] up1[] down[] time[] pop[]
+ *     per chain, per locus: nlines up0[] up1[] down[] time[] pop[], SW adds
+ *       the alleles A[nlines]
  *   -> per proposal "UG ci li accepted topolchange tmrcachange pdg probg",
  *      then per chain-locus "TREE ci li" with up0[] up1[] down[] time[] pop[]
  * The genealogy update updategenealogy (update_gtree.cpp:723-966) of the
@@ -702,10 +704,17 @@ static void run_ug()
     L[li].hval = rd_d();
     for (int p = 0; p < npops; p++) L[li].samppop[p] = rd_i();
     us[li] = rd_d();
-    L[li].numsites = rd_i();
-    L[li].model = model == 1 ? HKY : INFINITESITES;
     L[li].nlinked = 1;
     L[li].uii[0] = li;
+    if (model == 2) {
+      L[li].model = STEPWISE;
+      L[li].minA[0] = rd_i();
+      L[li].maxA[0] = rd_i();
+      somestepwise = 1;
+      continue;
+    }
+    L[li].numsites = rd_i();
+    L[li].model = model == 1 ? HKY : INFINITESITES;
     seqs[li].resize((size_t)L[li].numgenes * L[li].numsites);
     for (auto &v : seqs[li]) v = rd_i();
     L[li].seq = (int **)malloc(sizeof(int *) * L[li].numgenes);
@@ -750,6 +759,12 @@ static void run_ug()
         G->gtree[i].cmm = ABSMIGMAX;
         G->gtree[i].mig[0].mt = -1.0;
       }
+      if (L[li].model == STEPWISE)
+        for (int i = 0; i < nlines; i++) {
+          G->gtree[i].A = (int *)calloc(MAXLINKED, sizeof(int));
+          G->gtree[i].dlikeA = (double *)calloc(MAXLINKED, sizeof(double));
+          G->gtree[i].A[0] = rd_i();
+        }
       G->root = find_root(G->gtree, nlines);
       G->gtree[G->root].time = TIMEMAX;
       G->roottime = G->gtree[G->gtree[G->root].up[0]].time;
@@ -759,7 +774,9 @@ static void run_ug()
       init_genealogy_weights(&G->gweight);
       treeweight(ci, li);
       sum_treeinfo(&C[ci]->allgweight, &G->gweight);
-      if (L[li].model == HKY) {
+      if (L[li].model == STEPWISE) {
+        G->pdg = G->pdg_a[0] = likelihoodSW(ci, li, 0, us[li], 1.0);
+      } else if (L[li].model == HKY) {
         alloc_hky(G->gtree, L[li].numgenes, L[li].numsites);
         for (int j = 0; j < 4; j++) G->pi[j] = pis[li][j];
         G->kappaval = kappas[li];
@@ -792,6 +809,8 @@ static void run_ug()
       for (int i = 0; i < L[li].numlines; i++) printf(" %d", t[i].down);
       for (int i = 0; i < L[li].numlines; i++) printf(" %.17g", t[i].time);
       for (int i = 0; i < L[li].numlines; i++) printf(" %d", t[i].pop);
+      if (L[li].model == STEPWISE)
+        for (int i = 0; i < L[li].numlines; i++) printf(" %d", t[i].A[0]);
       printf("\n");
     }
 }

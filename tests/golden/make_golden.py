@@ -644,23 +644,22 @@ def golden_iparams():
     np.savez_compressed(os.path.join(OUT, "golden_iparams.npz"), cases=np.array(json.dumps(cases)))
 
 
-def golden_ug():
+def _golden_ug(name, kinds, seed, us):
     """The reference's genealogy update updategenealogy under the
-    no-migration model: 3 chains x 5 loci (IS and HKY alternating), 10 sweeps
-    per chain from seeds of their own; every proposal's decision, G.pdg and
-    p(G), and the final genealogies."""
+    no-migration model: 3 chains x the given loci, 10 sweeps per chain from
+    seeds of their own; every proposal's decision, G.pdg and p(G), and the
+    final genealogies (with the SW loci's alleles)."""
     from ima2p_gb300 import popmodel
-    rng = np.random.default_rng(2031)
+    rng = np.random.default_rng(seed)
     npops, ts = 3, "((0,1):3,2):4"
     sp = popmodel.parse_treestring(ts, npops)
     tv0 = [0.45, 1.1]
     splits = [(tv0[k], a, b, anc) for k, (a, b, anc) in enumerate(sp)]
-    kinds = ["is", "hky", "is", "hky", "is"]
-    us = [1.0, 1.5, 0.8, 1.2, 1.1]
     kappa, pi_sim = 2.0, np.array([0.3, 0.2, 0.2, 0.3])
-    loci, base, samps = [], [], []
+    loci, base, samps, alleles = [], [], [], {}
     out = {"npops": np.array(npops), "tree": np.array(ts), "tv0": np.array(tv0), "kinds": np.array(kinds),
            "us": np.array(us), "kappa": np.array(kappa), "thetaprior": np.array(10.0)}
+    betas, seeds, nsweeps = [1.0, 0.8, 0.5], [11, 12, 13], 10
     for li, kind in enumerate(kinds):
         samp = [int(v) for v in rng.integers(3, 7, npops)]
         lg = synth.sim_im_labeled(rng, samp, list(rng.uniform(1.0, 3.0, 5)), 0.0, splits)
@@ -670,17 +669,24 @@ def golden_ug():
             seq = synth.is_data(rng, lg.g, us[li], min_sites=4)
             loci.append(("is", sum(samp), 1.0, samp, us[li], seq))
             out["seq_%d" % li] = seq
-        else:
+        elif kind == "hky":
             hl = synth.hky_data(rng, lg.g, 300, us[li], kappa, pi_sim)
             loci.append(("hky", sum(samp), 1.0, samp, us[li], hl, kappa))
             out["seq_%d" % li] = hl.seq
             out["mult_%d" % li] = hl.mult
             out["totsites_%d" % li] = np.array(hl.totsites)
             out["pi_%d" % li] = hl.pi
-    betas, seeds, nsweeps = [1.0, 0.8, 0.5], [11, 12, 13], 10
+        else:
+            A = synth.sw_alleles(rng, lg.g, us[li])
+            lo, hi = int(A.min()) - 3, int(A.max()) + 3
+            loci.append(("sw", sum(samp), 1.0, samp, us[li], lo, hi))
+            out["alleles_%d" % li] = A
+            out["arange_%d" % li] = np.array([lo, hi])
+            for ci in range(len(betas)):
+                alleles[(ci, li)] = A
     chains = [(tv0, b, s) for b, s in zip(betas, seeds)]
     gens = [[base[li] for li in range(len(kinds))] for _ in chains]
-    res, trees = O.ref_ug(npops, ts, 10.0, loci, chains, gens, nsweeps)
+    res, trees = O.ref_ug(npops, ts, 10.0, loci, chains, gens, nsweeps, alleles=alleles)
     out.update({"samps": np.array(samps), "betas": np.array(betas), "seeds": np.array(seeds),
                 "nsweeps": np.array(nsweeps), "res": np.array(res)})
     for f in ("up0", "up1", "down", "time", "pop"):
@@ -689,8 +695,20 @@ def golden_ug():
     for k, f in enumerate(("up0", "up1", "down", "time", "pop")):
         out["final_" + f] = np.concatenate([trees[(ci, li)][k] for ci in range(len(chains))
                                             for li in range(len(kinds))])
-    np.savez_compressed(os.path.join(OUT, "golden_ug.npz"), **out)
+    if "sw" in kinds:
+        out["final_A"] = np.concatenate([trees[(ci, li)][5] for ci in range(len(chains))
+                                         for li in range(len(kinds)) if kinds[li] == "sw"])
+    np.savez_compressed(os.path.join(OUT, name), **out)
 
+
+def golden_ug():
+    _golden_ug("golden_ug.npz", ["is", "hky", "is", "hky", "is"], 2031, [1.0, 1.5, 0.8, 1.2, 1.1])
+
+
+def golden_ug_sw():
+    """The same with stepwise loci among them (finishSWupdateA's allele
+    proposal and branch terms, update_gtree_common.cpp:2219-2362)."""
+    _golden_ug("golden_ug_sw.npz", ["sw", "is", "sw", "hky", "sw"], 2032, [2.0, 1.0, 1.5, 1.2, 3.0])
 
 if __name__ == "__main__":
     if not O.ref_available():
@@ -698,7 +716,7 @@ if __name__ == "__main__":
     gens = {"is": golden_is, "hky": golden_hky, "sw": golden_sw, "swap": golden_swap,
             "jointp": golden_jointp, "de": golden_de, "margin": golden_margin,
             "tw": golden_tw, "ry": golden_ry, "ks": golden_ks, "popmig": golden_popmig,
-            "peaks": golden_peaks, "iparams": golden_iparams, "ug": golden_ug}
+            "peaks": golden_peaks, "iparams": golden_iparams, "ug": golden_ug, "ug_sw": golden_ug_sw}
     for name in (sys.argv[1:] or list(gens)):
         gens[name]()
     for f in sorted(os.listdir(OUT)):
