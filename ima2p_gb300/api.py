@@ -56,7 +56,7 @@ EXPORTS = [
     "ima_gpu_chain_weights", "ima_gpu_changet_ry1_sweep", "ima_gpu_get_probg", "ima_gpu_get_split_times",
     "ima_gpu_checkpoint_write", "ima_gpu_checkpoint_read", "ima_gpu_popmig", "ima_gpu_popmig_curves",
     "ima_gpu_findmarginpeaks", "ima_gpu_changet_ry1_sweep_mt", "ima_ug_rng_seed",
-    "ima_gpu_updategenealogy_sweep", "ima_gpu_get_genealogy",
+    "ima_gpu_updategenealogy_sweep", "ima_gpu_get_genealogy", "ima_gpu_get_alleles",
 ]
 
 
@@ -194,8 +194,9 @@ def _declare(L):
         "ima_gpu_popmig_curves": (I, [P, I, P, P, I, P, P, P, I, P, P, P]),
         "ima_gpu_changet_ry1_sweep_mt": (I, [P, I, P, P, P, P, P, D, P, P, I, P, P, P, P]),
         "ima_ug_rng_seed": (None, [P, C.c_int32]),
-        "ima_gpu_updategenealogy_sweep": (I, [P, I, P, P, I, P, P, D, I, P, P, P, P]),
+        "ima_gpu_updategenealogy_sweep": (I, [P, I, P, P, I, P, P, P, D, I, P, P, P, P]),
         "ima_gpu_get_genealogy": (I, [P, I, I, P, P, P, P, P]),
+        "ima_gpu_get_alleles": (I, [P, I, I, I, P]),
         "ima_gpu_findmarginpeaks": (I, [P, P, P, P, P, P, I, P, P, P, P, P, P, P, P, P, P, P, C.POINTER(I)]),
         "ima_gpu_swapchains": (I, [P, I, I, P, I, C.c_uint64, P, P]),
         "ima_gpu_get_swapcounts": (I, [P, I, P, P]),
@@ -362,6 +363,12 @@ class Context:
 
     def set_alleles(self, ci, li, A, ai=0):
         self._ck(self.lib.ima_gpu_set_alleles(self.h, int(ci), int(li), int(ai), _ptr(_i32(A))))
+
+    def get_alleles(self, ci, li, nlines, ai=0):
+        """The resident allele states of a stepwise chain-locus's marker."""
+        A = np.zeros(nlines, np.int32)
+        self._ck(self.lib.ima_gpu_get_alleles(self.h, int(ci), int(li), int(ai), _ptr(A)))
+        return A
 
     def set_allele_edits(self, ci, li, node, A, ai=None):
         """Edit list of single allele states (ima_gpu_set_allele_edits)."""
@@ -700,20 +707,24 @@ class Context:
             _ptr(newt)))
         return acc.astype(bool), pdgsum, probg, newt
 
-    def updategenealogy_sweep(self, chains, tvals, nsweeps, rngs, u, kappa=None, gbeta=1.0, precision=PREC_FP64):
+    def updategenealogy_sweep(self, chains, tvals, nsweeps, rngs, u, kappa=None, gbeta=1.0, precision=PREC_FP64,
+                              allele_range=None):
         """nsweeps device genealogy updates of every locus of the chains (the
-        no-migration model); rngs: a UgRng per chain, advanced in place.
-        Returns (accepted, topology changes) [nch][nloci] and p(G) [nch]."""
+        no-migration model); rngs: a UgRng per chain, advanced in place;
+        allele_range [nloci][2]: the SW loci's (minA, maxA).  Returns
+        (accepted, topology changes) [nch][nloci] and p(G) [nch]."""
         chains = _i32(chains)
         n, nl = len(chains), len(self.loci)
         tvals = _f64(np.asarray(tvals, np.float64).reshape(n, -1))
         u = _f64(np.asarray(u, np.float64).reshape(-1))
         kap = _f64(np.asarray(kappa, np.float64).reshape(-1)) if kappa is not None else None
+        ar = _i32(np.asarray(allele_range).reshape(-1)) if allele_range is not None else None
         arr = (UgRng * n)(*rngs)
         acc, top, probg = np.zeros((n, nl), np.int32), np.zeros((n, nl), np.int32), np.zeros(n)
         self._ck(self.lib.ima_gpu_updategenealogy_sweep(
             self.h, n, _ptr(chains), _ptr(tvals), int(nsweeps), _ptr(u), _ptr(kap) if kap is not None else None,
-            float(gbeta), int(precision), C.cast(arr, P), _ptr(acc), _ptr(top), _ptr(probg)))
+            _ptr(ar) if ar is not None else None, float(gbeta), int(precision), C.cast(arr, P), _ptr(acc), _ptr(top),
+            _ptr(probg)))
         for k in range(n):
             C.memmove(C.addressof(rngs[k]), C.addressof(arr[k]), C.sizeof(UgRng))
         return acc, top, probg

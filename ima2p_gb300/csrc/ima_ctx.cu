@@ -730,6 +730,11 @@ static int sync_mirror(ima_ctx *c)
     r = r ? r : c->cuda(cudaMemcpyAsync(c->h_nodes + m0, c->d_nodes + m0, (m1 - m0) * sizeof(NodeRec), cudaMemcpyDeviceToHost, c->st), "mirror");
     r = r ? r : c->cuda(cudaMemcpyAsync(c->h_sched + s0, c->d_sched + s0, (s1 - s0) * sizeof(int16_t), cudaMemcpyDeviceToHost, c->st), "mirror");
     r = r ? r : c->cuda(cudaMemcpyAsync(c->h_nlev + l0, c->d_nlev + l0, (l1 - l0) * sizeof(int32_t), cudaMemcpyDeviceToHost, c->st), "mirror");
+    // the stepwise alleles the genealogy update drew
+    const LocusDev &Lb = c->loci[tb.locus].d;
+    const size_t a0 = ta.al_off, a1 = (size_t)tb.al_off + (Lb.model == IMA_MODEL_SW ? (size_t)Lb.nlinked * (2 * tb.n - 1) : 0);
+    if (a1 > a0)
+      r = r ? r : c->cuda(cudaMemcpyAsync(c->h_al + a0, c->d_al + a0, (a1 - a0) * sizeof(int32_t), cudaMemcpyDeviceToHost, c->st), "mirror");
   }
   r = r ? r : c->cuda(cudaStreamSynchronize(c->st), "mirror");
   c->dev_lo = INT32_MAX;
@@ -1306,6 +1311,21 @@ extern "C" int ima_gpu_set_alleles(ima_ctx *c, int ci, int li, int ai, const int
   memcpy(c->h_al + it.al_off + (size_t)ai * nl, A, sizeof(int32_t) * nl);
   mark(c, item);
   return IMA_OK;
+}
+
+extern "C" int ima_gpu_get_alleles(ima_ctx *c, int ci, int li, int ai, int32_t *A)
+{
+  if (!c || !A) return IMA_ERR_ARG;
+  if (!c->valid(ci, li)) return c->fail(IMA_ERR_ARG, "chain %d locus %d out of range", ci, li);
+  const LocusDev &L = c->loci[li].d;
+  if (L.model != IMA_MODEL_SW || ai < 0 || ai >= L.nlinked) return c->fail(IMA_ERR_ARG, "locus %d marker %d is not stepwise", li, ai);
+  cudaSetDevice(c->device);
+  if (int r = flush(c)) return r;  // host edits not yet on the device go first
+  const ItemDev &it = c->items[c->item_of(ci, li)];
+  const int nl = 2 * it.n - 1;
+  int r = c->cuda(cudaMemcpyAsync(A, c->d_al + it.al_off + (size_t)ai * nl, nl * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                  c->st), "alleles");
+  return r ? r : c->cuda(cudaStreamSynchronize(c->st), "alleles");
 }
 
 extern "C" int ima_gpu_set_allele_edits(ima_ctx *c, int n, const int *ci, const int *li, const int *ai,
@@ -4082,21 +4102,25 @@ extern "C" int ima_gpu_get_genealogy(ima_ctx *c, int ci, int li, int32_t *up0, i
 }
 
 extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t *chains, const double *tvals,
-                                             int nsweeps, const double *u, const double *kappa, double gbeta,
-                                             int precision, ima_ug_rng *rng, int32_t *accepted, int32_t *topology,
-                                             double *probg)
+                                             int nsweeps, const double *u, const double *kappa,
+                                             const int32_t *allele_range, double gbeta, int precision, ima_ug_rng *rng,
+                                             int32_t *accepted, int32_t *topology, double *probg)
 {
   if (!c || nch < 1 || !chains || !tvals || nsweeps < 0 || !u || !rng) return IMA_ERR_ARG;
   if (!c->tw_ready) return c->fail(IMA_ERR_STATE, "call ima_gpu_set_popmodel first");
   const TwModel &h = c->h_tw;
   if (!h.nomig) return c->fail(IMA_ERR_STATE, "the genealogy update is built for the no-migration model (nomig = 1)");
   const int nl = c->nloci, nsplit = h.npops - 1, T = h.T, nth = h.nth, ni = c->nitems;
-  int maxn = 0, anyhky = 0;
+  int maxn = 0, anysw = 0;
   for (int li = 0; li < nl; li++) {
     const LocusDev &L = c->loci[li].d;
-    if (L.model == IMA_MODEL_SW) return c->fail(IMA_ERR_ARG, "locus %d: the genealogy update takes IS and HKY loci", li);
+    if (L.model == IMA_MODEL_SW) {
+      if (L.nlinked != 1) return c->fail(IMA_ERR_ARG, "locus %d: the genealogy update takes one-marker SW loci", li);
+      if (!allele_range) return c->fail(IMA_ERR_ARG, "locus %d is SW: allele_range is needed", li);
+      if (allele_range[2 * li] > allele_range[2 * li + 1]) return c->fail(IMA_ERR_ARG, "locus %d: empty allele range", li);
+      anysw = 1;
+    }
     maxn = std::max(maxn, L.n);
-    anyhky |= (L.model == IMA_MODEL_HKY);
   }
   int r = chains_ready(c, nch, chains);
   if (r) return r;
@@ -4115,11 +4139,27 @@ extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t 
       li[(size_t)k * nl + l] = l;
       if (kappa) kap[(size_t)k * nl + l] = kappa[(size_t)k * nl + l];
     }
-  r = ima_gpu_eval(c, (int)np, ci.data(), li.data(), u, kap.data(), nullptr, nullptr, precision, res.data(), st.data());
+  // (the SW loci in FP64: their branch terms are the state the update edits)
+  for (int pass = 0; pass < 2 && !r; pass++) {
+    std::vector<int32_t> pc, pl;
+    std::vector<double> pu, pk;
+    for (size_t k = 0; k < np; k++)
+      if ((c->loci[li[k]].d.model == IMA_MODEL_SW) == (pass == 1)) {
+        pc.push_back(ci[k]);
+        pl.push_back(li[k]);
+        pu.push_back(u[k]);
+        pk.push_back(kap[k]);
+      }
+    if (pc.empty()) continue;
+    std::vector<double> pr(pc.size());
+    std::vector<int32_t> ps(pc.size());
+    r = ima_gpu_eval(c, (int)pc.size(), pc.data(), pl.data(), pu.data(), pk.data(), nullptr, nullptr,
+                     pass ? IMA_PREC_FP64 : precision, pr.data(), ps.data());
+    for (size_t k = 0; !r && k < pc.size(); k++)
+      if (ps[k] != IMA_EVAL_OK)
+        return c->fail(IMA_ERR_DATA, "chain %d locus %d: the likelihood rejects the current genealogy", pc[k], pl[k]);
+  }
   if (r) return r;
-  for (size_t k = 0; k < np; k++)
-    if (st[k] != IMA_EVAL_OK)
-      return c->fail(IMA_ERR_DATA, "chain %d locus %d: the likelihood rejects the current genealogy", ci[k], li[k]);
   {
     std::vector<uint8_t> ones(np, 1);
     r = commit(c, (int)np, ci.data(), li.data(), ones.data(), true, true);
@@ -4164,6 +4204,7 @@ extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t 
   const size_t rn = (size_t)R * nch;
   const size_t bytes = carve_size({nch * sizeof(ima_ug_rng), nch * 4ul, np * 4, np * 4, rn * mx * sizeof(NodeRec),
                                    rn * mx * 8, rn * mx * 4, rn * mx * 2, rn * 8, rn * 4, rn * 8, rn * 8, rn * 8,
+                                   rn * 16, rn * mx * 4, rn * mx * 8, rn * 8, rn * 8, rn * 8, np * 8, nl * 8ul,
                                    8, nch * T * 4ul, nch * T * 8ul, nch * T * 8ul, nch * (size_t)nth * 8, np * 4, np * 4,
                                    ni * T * 4ul, ni * M1 * 4, ni * 4ul, ni * T * 8ul, ni * T * 8ul, ni * M1 * 8,
                                    2ul * ni * 8, (ni + 1) * 8ul, Etot * 8, Etot * 4, ni * 4ul});
@@ -4188,6 +4229,14 @@ extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t 
   a.prop = reinterpret_cast<int32_t *>(cv.take<double>(rn));
   a.slidew = cv.take<double>(rn);
   a.ustore = cv.take<double>(rn);
+  a.edges = cv.take<int32_t>(4 * rn);
+  a.bk_A = cv.take<int32_t>(rn * mx);
+  a.bk_dl = cv.take<double>(rn * mx);
+  a.swnew = cv.take<double>(rn);
+  a.aterm = cv.take<double>(rn);
+  a.holdsis = cv.take<double>(rn);
+  double *d_ucl = cv.take<double>(np);
+  int32_t *d_arange = cv.take<int32_t>(2ul * nl);
   a.err = cv.take<int32_t>(2);
   a.ag_cc = cv.take<int32_t>(nch * (size_t)T);
   a.ag_fc = cv.take<double>(nch * (size_t)T);
@@ -4234,13 +4283,14 @@ extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t 
   if ((int)c->ugb.size() < nl) c->ugb.resize(nl);
   std::vector<int32_t> reqof(np), perm(np);
   for (int l = 0; l < nl && !r; l++) {
+    for (int k = 0; k < nch; k++) perm[(size_t)l * nch + k] = c->item_of(chains[k], l);
+    if (c->loci[l].d.model == IMA_MODEL_SW) continue;  // its update runs in k_ug_sw
     Batch &b = c->ugb[l];
     std::vector<int32_t> lli(nch, l);
     std::vector<double> lu(nch), lk(nch);
     for (int k = 0; k < nch; k++) {
       lu[k] = u[(size_t)k * nl + l];
       lk[k] = kap[(size_t)k * nl + l];
-      perm[(size_t)l * nch + k] = c->item_of(chains[k], l);
     }
     r = build_batch(c, b, nch, chains, lli.data(), lu.data(), lk.data(), nullptr, nullptr, precision);
     r = r ? r : init_sumlogk(c, b);
@@ -4252,6 +4302,9 @@ extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t 
   r = r ? r : c->cuda(cudaMemcpyAsync(d_reqof, reqof.data(), np * 4, cudaMemcpyHostToDevice, c->st), "requests");
   r = r ? r : c->cuda(cudaMemcpyAsync(d_perm, perm.data(), np * 4, cudaMemcpyHostToDevice, c->st), "genealogy lists");
   r = r ? r : c->cuda(cudaMemcpyAsync(d_evoff, evoff.data(), (ni + 1) * 8ul, cudaMemcpyHostToDevice, c->st), "events");
+  r = r ? r : c->cuda(cudaMemcpyAsync(d_ucl, u, np * 8, cudaMemcpyHostToDevice, c->st), "rates");
+  if (anysw)
+    r = r ? r : c->cuda(cudaMemcpyAsync(d_arange, allele_range, nl * 8ul, cudaMemcpyHostToDevice, c->st), "ranges");
   r = r ? r : c->cuda(cudaMemsetAsync(a.err, 0, 8, c->st), "errors");
   r = r ? r : c->cuda(cudaMemsetAsync(c->d_twerr, 0, 8, c->st), "errors");
   r = r ? r : c->cuda(cudaMemsetAsync(a.nacc, 0, np * 4, c->st), "counts");
@@ -4290,6 +4343,10 @@ extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t 
   a.fresh32 = c->d_fresh32;
   a.slot64 = c->d_slot64;
   a.fresh64 = c->d_fresh64;
+  a.alleles = c->d_al;
+  a.dlike = c->d_dlike;
+  a.arange = d_arange;
+  a.u_cl = d_ucl;
   if (!c->ug_sd) {
     for (cudaStream_t *q : {&c->ug_sw, &c->ug_sw2, &c->ug_sh, &c->ug_sh2, &c->ug_sd})
       r = r ? r : c->cuda(cudaStreamCreateWithFlags(q, cudaStreamNonBlocking), "streams");
@@ -4324,7 +4381,8 @@ extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t 
       UgArgs u_ = a0;
       u_.locus = l;
       u_.hky = c->loci[l].d.model == IMA_MODEL_HKY;
-      u_.predraw = u_.hky;
+      u_.sw = c->loci[l].d.model == IMA_MODEL_SW;
+      u_.predraw = u_.hky || u_.sw;
       u_.req = b.d_req;
       u_.req_of = d_reqof + (size_t)l * nch;
       u_.res = b.d_res;
@@ -4338,9 +4396,16 @@ extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t 
       u_.prop = a0.prop + 2 * so;
       u_.slidew = a0.slidew + so;
       u_.ustore = a0.ustore + so;
+      u_.edges = a0.edges + 4 * so;
+      u_.bk_A = a0.bk_A + so * mx;
+      u_.bk_dl = a0.bk_dl + so * mx;
+      u_.swnew = a0.swnew + so;
+      u_.aterm = a0.aterm + so;
+      u_.holdsis = a0.holdsis + so;
       if (step >= R) cudaStreamWaitEvent(c->st, evD[slot], 0);
       if (prev_is) cudaStreamWaitEvent(c->st, evD[(step - 1) % R], 0);
       c->launch(IMA_K_UG, 0.0, [&] { launch_ug_propose(u_, c->st); });
+      if (u_.sw) c->launch(IMA_K_UG, 0.0, [&] { launch_ug_sw(u_, c->st); });
       cudaEventRecord(evP[slot], c->st);
       w.perm = d_perm + (size_t)l * nch;
       cudaStream_t sw = (step & 1) ? c->ug_sw2 : c->ug_sw;
@@ -4350,16 +4415,18 @@ extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t 
       if (lr < 0) return c->fail(IMA_ERR_TOO_LARGE, "treeweight: shared memory for %d events", P);
       c->launches += lr - 1;
       cudaEventRecord(evW[slot], sw);
-      cudaStream_t sh = (step & 1) ? c->ug_sh2 : c->ug_sh;
-      cudaStreamWaitEvent(sh, evP[slot], 0);
-      if (!u_.hky) cudaStreamWaitEvent(sh, evW[slot], 0);  // the IS likelihood reads the new lengths
-      enqueue(c, b, sh);
-      cudaEventRecord(evH[slot], sh);
       cudaStreamWaitEvent(c->ug_sd, evW[slot], 0);
-      cudaStreamWaitEvent(c->ug_sd, evH[slot], 0);
+      if (!u_.sw) {  // a stepwise locus's likelihood change came with its proposal
+        cudaStream_t sh = (step & 1) ? c->ug_sh2 : c->ug_sh;
+        cudaStreamWaitEvent(sh, evP[slot], 0);
+        if (!u_.hky) cudaStreamWaitEvent(sh, evW[slot], 0);  // the IS likelihood reads the new lengths
+        enqueue(c, b, sh);
+        cudaEventRecord(evH[slot], sh);
+        cudaStreamWaitEvent(c->ug_sd, evH[slot], 0);
+      }
       c->launch(IMA_K_UG, 0.0, [&] { launch_ug_decide(u_, c->ug_sd); }, c->ug_sd);
       cudaEventRecord(evD[slot], c->ug_sd);
-      prev_is = !u_.hky;
+      prev_is = c->loci[l].d.model == IMA_MODEL_IS;
       r = c->cuda(cudaGetLastError(), "genealogy update launch");
     }
   if (step > 0) cudaStreamWaitEvent(c->st, evD[(step - 1) % R], 0);  // st carries on after the last decision

@@ -333,6 +333,18 @@ struct UgArgs {
   // stream's order is the reference's); otherwise the decision draws it
   int predraw;
   double *ustore;
+  int32_t *edges;                          // [nch][4]: edge, freed, old sister, new sister
+  // stepwise loci (one marker): finishSWupdateA on the proposal (k_ug_sw)
+  int sw;
+  int32_t *alleles;                        // the allele pool (per item at al_off)
+  double *dlike;                           // FP64 branch terms (per item at dl_off)
+  const int32_t *arange;                   // [nloci][2] allele range
+  const double *u_cl;                      // [nch][nloci] mutation rates
+  int32_t *bk_A;                           // [nch][2 maxn] alleles before the proposal
+  double *bk_dl;                           // [nch][2 maxn] branch terms before the proposal
+  double *swnew;                           // [nch] proposed G.pdg
+  double *aterm;                           // [nch] the allele proposal's Hastings term
+  double *holdsis;                         // [nch] the new sister's term before the update
   int32_t *err;                            // {code, listed chain} of the first failure
   // the decision
   const double *res;                       // the batch's results
@@ -354,6 +366,7 @@ struct UgArgs {
 };
 enum { UG_E_SLIDE = 1, UG_E_ROOTTIME = 2, UG_E_ISFAIL = 3, UG_E_TERM = 4, UG_E_TREE = 5 };
 void launch_ug_propose(const UgArgs &a, cudaStream_t st);
+void launch_ug_sw(const UgArgs &a, cudaStream_t st);  // k_sw.cu
 void launch_ug_decide(const UgArgs &a, cudaStream_t st);
 bool tw_fits(int P);                       // P events fit one warp's shared memory
 int launch_treeweight(const TwArgs &a, const TwModel &h, cudaStream_t st);

@@ -26,6 +26,7 @@
 
 #include "ff.cuh"
 #include "internal.h"
+#include "ug_rng.cuh"
 
 namespace {
 
@@ -463,6 +464,100 @@ float2 split(double v)
   return make_float2(h, (float)(v - (double)h));
 }
 
+
+// finishSWupdateA (update_gtree_common.cpp:2219-2362) for a genealogy
+// update's proposal on a stepwise locus (one marker), a warp per chain, lane
+// 0 in the reference's order: the freed node's new allele (geometric around
+// its neighbours' alleles, sign by bitran, clamped to the locus's range), the
+// terms of the old sister and the three moved branches in FP64 with the
+// reference's Bessel functions, the allele proposal's Hastings term, then the
+// acceptance uniform, next in the generator's stream.  Products and sums are
+// rounded one at a time (no contraction), as the reference writes them.
+__global__ void __launch_bounds__(32) k_ug_sw(UgArgs a)
+{
+  __shared__ __align__(16) uint32_t s_mt[624];
+  const int w = blockIdx.x, lane = threadIdx.x;
+  const int ci = a.chains[w], item = ci * a.nloci + a.locus;
+  const ItemDev it = a.items[item];
+  const int n = it.n, maxnl = 2 * a.maxn;
+  LocalRng g;
+  rng_load(g, a.rng + w, s_mt, lane);
+  if (lane == 0) {
+    const NodeRec *nd = a.nodes + it.node_off;
+    const double *t = a.t64 + it.node_off;
+    int32_t *A = a.alleles + it.al_off;
+    double *dl = a.dlike + it.dl_off;
+    const int32_t *bka = a.bk_A + (size_t)w * maxnl;
+    const double *bkd = a.bk_dl + (size_t)w * maxnl;
+    const NodeRec *bkn = a.bk_nodes + (size_t)w * maxnl;
+    const int32_t *eo = a.edges + 4 * (size_t)w;
+    const int edge = eo[0], freed = eo[1], oldsis = eo[2], newsis = eo[3];
+    const double u = a.u_cl[(size_t)w * a.nloci + a.locus];
+    const int minA = a.arange[2 * a.locus], maxA = a.arange[2 * a.locus + 1];
+    const int oldA = A[freed];
+    const double holdsis = (newsis != oldsis) ? dl[newsis] : 0.0;
+    const bool fdown = bkn[freed].down != -1;
+    const double cp2 = fdown ? bkd[freed] : 0.0;
+    const int holddownA = fdown ? bka[bkn[freed].down] : -1;
+    const double oldlikeadj = bkd[edge] + bkd[oldsis] + cp2 + holdsis;
+    const int e[3] = {edge, newsis, nd[edge].down};
+    double tt[3] = {0.0, 0.0, 0.0};
+    for (int i = 0; i < 3; i++) {
+      const double upt = e[i] >= n ? t[nd[e[i]].up0] : 0.0;
+      if (nd[e[i]].down != -1) tt[i] = t[e[i]] - upt;
+    }
+    int wsumdiff = 0, j = 0;
+    for (int i = 0; i < 3; i++)
+      if (nd[e[i]].down != -1) {
+        const int d = (i < 2 ? A[e[i]] : A[nd[e[i]].down]) - oldA;
+        wsumdiff += abs(d);
+        j++;
+      }
+    double geotermnew = j / ((double)(wsumdiff + j));
+    if (geotermnew > 0.95) geotermnew = 0.95;
+    int dA = (int)ceil(log(uniform(g)) / log(1.0 - geotermnew)) - 1;  // geometric(), utilities.cpp:609-617
+    if (bitran(g)) dA = -dA;
+    int newA;
+    if (dA >= 0) newA = (maxA < oldA + dA) ? maxA : oldA + dA;
+    else newA = (minA > oldA + dA) ? minA : oldA + dA;
+    A[freed] = newA;
+    dA = newA - oldA;
+    if (nd[oldsis].down != -1 && oldsis != newsis) {
+      const double upt = oldsis >= n ? t[nd[oldsis].up0] : 0.0;
+      const int d = A[oldsis] - A[nd[oldsis].down];
+      const double x = (t[oldsis] - upt) * u;
+      dl[oldsis] = __dadd_rn(__dmul_rn(-(t[oldsis] - upt), u), log(bessi_64(d, x)));
+    } else {
+      dl[oldsis] = 0.0;
+    }
+    double likeadj = dl[oldsis];
+    for (int i = 0; i < 3; i++)
+      if (nd[e[i]].down != -1) {
+        const int d = (i < 2 ? A[e[i]] : A[nd[e[i]].down]) - newA;
+        const double x = tt[i] * u;
+        dl[e[i]] = __dadd_rn(-x, log(bessi_64(d, x)));
+        likeadj += dl[e[i]];
+      }
+    wsumdiff = abs(bka[edge] - newA) + abs(bka[oldsis] - newA);
+    j = 2;
+    if (fdown) {
+      wsumdiff += abs(holddownA - newA);
+      j++;
+    }
+    double geotermold = j / ((double)(wsumdiff + j));
+    if (geotermold > 0.95) geotermold = 0.95;
+    const double adA = (double)abs(dA);
+    const double at = __dadd_rn(__dmul_rn(adA, log(1 - geotermold)), log(geotermold)) -
+                      __dadd_rn(__dmul_rn(adA, log(1 - geotermnew)), log(geotermnew));
+    a.aterm[w] = at;
+    a.holdsis[w] = holdsis;
+    a.swnew[w] = 0.0 + (a.pdg[item] + __dadd_rn(likeadj, -oldlikeadj));
+    a.ustore[w] = uniform(g);  // the acceptance uniform
+  }
+  __syncwarp();
+  rng_store(g, a.rng + w, lane);
+}
+
 }  // namespace
 
 // Uploads the coefficient and table constants (once per device).
@@ -563,6 +658,8 @@ void launch_sw_fast(const Pools &P, const ReqDev *reqs, int nreq, int maxn, int 
   else if (variant == 2) sw_fast_launch<8, 5>(P, reqs, nreq, maxn, 8, result, status, st);
   else sw_fast_launch<16, 5>(P, reqs, nreq, maxn, 0, result, status, st);
 }
+
+void launch_ug_sw(const UgArgs &a, cudaStream_t st) { k_ug_sw<<<a.nch, 32, 0, st>>>(a); }
 
 void launch_sw_fp64(const Pools &P, const ReqDev *reqs, int nreq, double *result,
                     int32_t *status, cudaStream_t st)

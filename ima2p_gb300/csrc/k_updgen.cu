@@ -24,6 +24,7 @@
 #include <cfloat>
 
 #include "igamma.cuh"
+#include "ug_rng.cuh"
 
 namespace {
 
@@ -31,85 +32,6 @@ constexpr double TIMEMAX = 1000000.0;        // imamp.hpp:129
 constexpr double SLIDESTDVMAX = 20.0;        // update_gtree.cpp:686
 constexpr double ONEOVERSQRT2PI = 0.3989422803;  // utilities.cpp:461, as the reference writes it
 constexpr int SLIDE_MAX_STEPS = 1 << 20;     // a slide that long is an error, not a loop
-
-// The chain's generators for one kernel: MT19937 (Matsumoto & Nishimura
-// 1998) with its 624 words in shared memory (the warp loads them and writes
-// them back only when a twist changed them) and the rest in lane 0's
-// registers, so that a draw costs a shared-memory read, not a dependent
-// round trip to global memory.
-struct LocalRng {
-  uint32_t *mt;
-  int mti, iset;
-  double gset;
-  unsigned long long iseed;
-  bool twisted;
-};
-
-__device__ void rng_load(LocalRng &r, const ima_ug_rng *g, uint32_t *smt, int lane)
-{
-  const uint2 *src = reinterpret_cast<const uint2 *>(g->mt.mt);  // the state is 8-byte aligned
-  uint2 *dst = reinterpret_cast<uint2 *>(smt);
-  for (int k = lane; k < 312; k += 32) dst[k] = src[k];
-  r.mt = smt;
-  r.mti = g->mt.mti;
-  r.iset = g->iset;
-  r.gset = g->gset;
-  r.iseed = g->iseed;
-  r.twisted = false;
-  __syncwarp();
-}
-
-// the warp writes the generator back (lane 0's registers, and the words
-// when lane 0 twisted them)
-__device__ void rng_store(const LocalRng &r, ima_ug_rng *g, int lane)
-{
-  const bool tw = __shfl_sync(~0u, (int)r.twisted, 0) != 0;
-  if (tw) {
-    const uint2 *src = reinterpret_cast<const uint2 *>(r.mt);
-    uint2 *dst = reinterpret_cast<uint2 *>(g->mt.mt);
-    for (int k = lane; k < 312; k += 32) dst[k] = src[k];
-  }
-  if (lane == 0) {
-    g->mt.mti = r.mti;
-    g->iset = r.iset;
-    g->gset = r.gset;
-    g->iseed = r.iseed;
-  }
-}
-
-__device__ uint32_t mt_next(LocalRng &r)
-{
-  constexpr int N = 624, M = 397;
-  if (r.mti >= N) {
-    uint32_t *mt = r.mt;
-    for (int k = 0; k < N; k++) {
-      const uint32_t y = (mt[k] & 0x80000000u) | (mt[(k + 1) % N] & 0x7fffffffu);
-      mt[k] = mt[(k + M) % N] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
-    }
-    r.mti = 0;
-    r.twisted = true;
-  }
-  uint32_t y = r.mt[r.mti++];
-  y ^= y >> 11;
-  y ^= (y << 7) & 0x9d2c5680u;
-  y ^= (y << 15) & 0xefc60000u;
-  y ^= y >> 18;
-  return y;
-}
-
-// uniform() = genrand_real3, in (0, 1)
-__device__ double uniform(LocalRng &r) { return ((double)mt_next(r) + 0.5) * (1.0 / 4294967296.0); }
-
-// bitran (utilities.cpp:438-455): Press et al.'s irbit2 on its own register
-__device__ int bitran(LocalRng &r)
-{
-  if (r.iseed & 131072ull) {
-    r.iseed = ((r.iseed ^ 19ull) << 1) | 1ull;
-    return 1;
-  }
-  r.iseed <<= 1;
-  return 0;
-}
 
 // normdev (utilities.cpp:476-503): the polar method, keeping the second
 // deviate for the next call
@@ -233,6 +155,17 @@ __global__ void __launch_bounds__(32) k_ug_propose(UgArgs a)
   }
   if (a.hky)
     for (int k = lane; k < 2 * n; k += 32) bks[k] = a.sched[it.sched_off + k];
+  double *dl = nullptr;  // stepwise: the branch terms (joinsisdown and splitsisdown zero the new root's)
+  if (a.sw) {
+    const int32_t *A = a.alleles + it.al_off;
+    dl = a.dlike + it.dl_off;
+    int32_t *bka = a.bk_A + (size_t)w * maxnl;
+    double *bkd = a.bk_dl + (size_t)w * maxnl;
+    for (int k = lane; k < nl; k += 32) {
+      bka[k] = A[k];
+      bkd[k] = dl[k];
+    }
+  }
   if (lane == 0) {
     a.bk_len[w] = a.len[item];
     a.bk_nlev[w] = a.nlev[item];
@@ -280,6 +213,7 @@ __global__ void __launch_bounds__(32) k_ug_propose(UgArgs a)
         root = oldsis;
         nd[oldsis].down = -1;
         t[oldsis] = TIMEMAX;
+        if (dl) dl[oldsis] = 0.0;
         roottime = uptime;
       }
     }
@@ -360,6 +294,7 @@ __global__ void __launch_bounds__(32) k_ug_propose(UgArgs a)
         roottime = curt;
         rootmove = 1;
         if (roottime > TIMEMAX) ok = false;
+        if (dl) dl[freed] = 0.0;
       }
       nd[freed].down = (int16_t)dd;
       int nowpop = s.pop[newsis];
@@ -388,7 +323,14 @@ __global__ void __launch_bounds__(32) k_ug_propose(UgArgs a)
       R.e[2] = oldsis;
       R.e[3] = newsis;
     }
-    if (a.predraw) a.ustore[w] = uniform(g);  // the acceptance uniform, next in the stream
+    int32_t *eo = a.edges + 4 * (size_t)w;
+    eo[0] = edge;
+    eo[1] = freed;
+    eo[2] = oldsis;
+    eo[3] = newsis;
+    // the acceptance uniform, next in the stream (a stepwise locus draws its
+    // allele first, in k_ug_sw, and the uniform after it)
+    if (a.predraw && !a.sw) a.ustore[w] = uniform(g);
     s_root = root;
   }
   __syncwarp();
@@ -475,9 +417,10 @@ __global__ void __launch_bounds__(32) k_ug_decide(UgArgs a)
   const int n = it.n, nl = 2 * n - 1, maxnl = 2 * a.maxn;
   const TwModel &M = *a.model;
   const int T = M.T, nth = M.nth;
-  const int k = a.req_of[w];
-  const int code = a.st[k];
-  const double pdgnew = a.res[k];
+  const int k = a.sw ? 0 : a.req_of[w];
+  const int code = a.sw ? IMA_EVAL_OK : a.st[k];
+  const double pdgnew = a.sw ? a.swnew[w] : a.res[k];
+  const double aterm = a.sw ? a.aterm[w] : 0.0;
   const bool rejectIS = !a.hky && code == IMA_EVAL_IS_REJECT;
   const bool failed = (!a.hky && code == IMA_EVAL_IS_FAIL) || a.err[0] != 0;
   if (!rejectIS && !failed) {
@@ -538,7 +481,7 @@ __global__ void __launch_bounds__(32) k_ug_decide(UgArgs a)
       double tpw = -a.probg[ci];
       tpw += psum;
       double mh = tpw + a.gbeta * (pdgnew - a.pdg[item]);
-      mh = exp(a.beta[ci] * mh + a.slidew[w]);
+      mh = exp(a.beta[ci] * mh + a.slidew[w] + aterm);
       double U;
       if (a.predraw) {
         U = a.ustore[w];
@@ -599,6 +542,19 @@ __global__ void __launch_bounds__(32) k_ug_decide(UgArgs a)
       a.len[item] = a.bk_len[w];
       a.nlev[item] = a.bk_nlev[w];
       a.is_valid[item] = 0;  // the site labels cached by the evaluation are the proposal's
+      if (a.sw) {  // restoreedges: the three moved edges from their copies, the new sister only if nonzero
+        const int32_t *eo = a.edges + 4 * (size_t)w;
+        const int edge = eo[0], freed = eo[1], oldsis = eo[2], newsis = eo[3];
+        const int32_t *bka = a.bk_A + (size_t)w * maxnl;
+        const double *bkd = a.bk_dl + (size_t)w * maxnl;
+        double *dl = a.dlike + it.dl_off;
+        a.alleles[it.al_off + freed] = bka[freed];
+        dl[edge] = bkd[edge];
+        dl[oldsis] = bkd[oldsis];
+        dl[freed] = bkn[freed].down != -1 ? bkd[freed] : 0.0;
+        const double hs = a.holdsis[w];
+        if (hs != 0) dl[newsis] = hs;
+      }
     }
   }
   if (a.hky)  // copyfraclike / restorescalefactors: the recomputed nodes' slots

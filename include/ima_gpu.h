@@ -121,6 +121,9 @@ int ima_gpu_eval_times(ima_ctx *ctx, int npairs, const int32_t *ci, const int32_
 int ima_gpu_set_pi(ima_ctx *ctx, int ci, int li, const double *pi4);
 /* Allele states of linked marker ai on every node (gtree[i].A[ai]). */
 int ima_gpu_set_alleles(ima_ctx *ctx, int ci, int li, int ai, const int32_t *A);
+/* The resident allele states of marker ai on every node (after device
+ * updates, e.g. ima_gpu_updategenealogy_sweep's allele proposals). */
+int ima_gpu_get_alleles(ima_ctx *ctx, int ci, int li, int ai, int32_t *A);
 /* Edit list of single allele states: gtree[node[k]].A[ai[k]] = A[k] on chain
  * ci[k], locus li[k], for k < n -- the state finishSWupdateA
  * (update_gtree_common.cpp:2219-2362) proposes for the moved node.  The
@@ -606,13 +609,18 @@ void ima_ug_rng_seed(ima_ug_rng *rng, int32_t seed);
  * genealogy (bitran at every node), reattaches it, recomputes the locus's
  * weights, the chain's p(G) from its summed weights (+ new - old) and the
  * locus's likelihood (IS in full; HKY from the four edited edges, in
- * `precision`), and accepts with the reference's Metropolis-Hastings term
- * (heat from ima_gpu_set_betas, gbeta) and one more uniform -- none when the
- * IS likelihood rejects the genealogy.  A rejection restores the genealogy.
- * Needs the population model with nomig = 1, labels and locus populations
- * (ima_gpu_set_labels, ima_gpu_set_locus_pops) and IS or HKY loci (IMA_ERR_ARG
- * for SW).  tvals [nch][npops-1]: the chains' split times; u [nch * nloci],
- * kappa [nch * nloci] (may be NULL: 1).  The call starts from a full
+ * `precision`; SW by finishSWupdateA, update_gtree_common.cpp:2219-2362: a
+ * new allele for the freed node and the moved branches' terms, in FP64), and
+ * accepts with the reference's Metropolis-Hastings term (heat from
+ * ima_gpu_set_betas, gbeta; the allele proposal's Hastings term for SW) and
+ * one more uniform -- none when the IS likelihood rejects the genealogy.  A
+ * rejection restores the genealogy (and for SW the alleles and terms, as
+ * restoreedges does).  Needs the population model with nomig = 1, labels and
+ * locus populations (ima_gpu_set_labels, ima_gpu_set_locus_pops), and IS,
+ * HKY or one-marker SW loci (IMA_ERR_ARG for more markers).  tvals
+ * [nch][npops-1]: the chains' split times; u [nch * nloci], kappa [nch *
+ * nloci] (may be NULL: 1); allele_range [nloci][2]: each SW locus's minA and
+ * maxA (L[li].minA/maxA; NULL when there is no SW locus).  The call starts from a full
  * evaluation of the chains' loci and their weights summed afresh (what the
  * reference holds after its set-up or an accepted split-time update), then
  * carries the sums from proposal to proposal as the reference does.  Out
@@ -620,8 +628,9 @@ void ima_ug_rng_seed(ima_ug_rng *rng, int32_t seed);
  * accepted proposals and accepted topology changes per chain-locus; probg
  * [nch] the chains' p(G) at the end.  Resident G.pdg and p(G) are updated. */
 int ima_gpu_updategenealogy_sweep(ima_ctx *ctx, int nch, const int32_t *chains, const double *tvals, int nsweeps,
-                                  const double *u, const double *kappa, double gbeta, int precision,
-                                  ima_ug_rng *rng, int32_t *accepted, int32_t *topology, double *probg);
+                                  const double *u, const double *kappa, const int32_t *allele_range, double gbeta,
+                                  int precision, ima_ug_rng *rng, int32_t *accepted, int32_t *topology,
+                                  double *probg);
 /* The resident genealogy of chain ci, locus li: up0, up1, down, time and
  * the population labels [2n-1] (any may be NULL). */
 int ima_gpu_get_genealogy(ima_ctx *ctx, int ci, int li, int32_t *up0, int32_t *up1, int32_t *down, double *time,

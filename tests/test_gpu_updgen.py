@@ -1,7 +1,8 @@
 """The genealogy update of the no-migration model on the device
 (ima_gpu_updategenealogy_sweep) against the reference's own updategenealogy
 (update_gtree.cpp:723-966), run by the harness on 3 chains x 5 loci (IS and
-HKY), 10 sweeps per chain from a seed of its own (golden_ug.npz): the same
+HKY, golden_ug.npz; SW among IS and HKY, golden_ug_sw.npz), 10 sweeps per
+chain from a seed of its own: the same
 accepted proposals per chain-locus, the same final genealogies (topology and
 population labels exact, times to the last bits of the device's log and
 sqrt in the slide's normal deviate), G.pdg and p(G)."""
@@ -15,8 +16,8 @@ pytestmark = pytest.mark.gpu
 
 
 class UgCase:
-    def __init__(self):
-        d = load("golden_ug.npz")
+    def __init__(self, name="golden_ug.npz"):
+        d = load(name)
         self.d = d
         self.npops = int(d["npops"])
         self.tree = str(d["tree"])
@@ -47,8 +48,10 @@ class UgCase:
         for li, kind in enumerate(self.kinds):
             if kind == "is":
                 ctx.add_locus_is(self.d["seq_%d" % li])
-            else:
+            elif kind == "hky":
                 ctx.add_locus_hky(self.d["seq_%d" % li], self.d["mult_%d" % li], int(self.d["totsites_%d" % li]))
+            else:
+                ctx.add_locus_sw(int(self.off[li + 1] - self.off[li] + 1) // 2, 1)
         ctx.set_chains(1, self.nch)
         th_max, th_min, _, _, _ = popmodel.priors(self.pm, float(self.d["thetaprior"]), 0.0)
         ctx.set_popmodel(self.pm, th_max, th_min)
@@ -70,8 +73,16 @@ class UgCase:
             for l, kind in enumerate(self.kinds):
                 if kind == "hky":
                     ctx.set_pi(c, l, self.d["pi_%d" % l])
+                elif kind == "sw":
+                    ctx.set_alleles(c, l, self.d["alleles_%d" % l])
         ctx.set_betas(self.betas)
         return ctx
+
+    def allele_range(self):
+        if "sw" not in self.kinds:
+            return None
+        return np.array([self.d["arange_%d" % l] if k == "sw" else [0, 0] for l, k in enumerate(self.kinds)],
+                        np.int32)
 
     def rates(self):
         u = np.tile(self.us, self.nch)
@@ -80,14 +91,17 @@ class UgCase:
 
 
 @pytest.mark.parametrize("precision", [api.PREC_FP64, api.PREC_FAST])
-def test_updategenealogy_follows_the_reference(precision):
-    case = UgCase()
+@pytest.mark.parametrize("fixture", ["golden_ug.npz", "golden_ug_sw.npz"])
+def test_updategenealogy_follows_the_reference(precision, fixture):
+    """golden_ug_sw.npz puts stepwise loci among them: finishSWupdateA's
+    allele proposals and branch terms, and the final alleles."""
+    case = UgCase(fixture)
     ctx = case.context()
     u, kap = case.rates()
     rngs = [api.UgRng(s) for s in case.seeds]
     tv = np.tile(case.d["tv0"], (case.nch, 1))
     acc, top, probg = ctx.updategenealogy_sweep(np.arange(case.nch), tv, case.nsweeps, rngs, u, kap,
-                                                precision=precision)
+                                                precision=precision, allele_range=case.allele_range())
     ref_acc = np.zeros((case.nch, case.nl), np.int64)
     ref_top = np.zeros((case.nch, case.nl), np.int64)
     last_pdg = np.zeros((case.nch, case.nl))
@@ -114,6 +128,10 @@ def test_updategenealogy_follows_the_reference(precision):
             assert np.array_equal(pop, case.final(ci, li, "pop"))
             edge = down != -1
             np.testing.assert_allclose(t[edge], case.final(ci, li, "time")[edge], rtol=1e-12, atol=0)
+    if "final_A" in case.d.files:
+        got = [ctx.get_alleles(ci, li, int(case.off[li + 1] - case.off[li]))
+               for ci in range(case.nch) for li in range(case.nl) if case.kinds[li] == "sw"]
+        assert np.array_equal(np.concatenate(got), case.d["final_A"])
     ctx.close()
 
 
@@ -191,9 +209,10 @@ def test_updategenealogy_checkpoint_round_trip(tmp_path):
 
 
 def test_updategenealogy_refuses_what_it_does_not_model():
-    """SW loci and models with migration stay with the host: IMA_ERR_ARG /
-    IMA_ERR_STATE before anything runs; no sweeps returns the chains' p(G)
-    summed afresh."""
+    """Models with migration and SW loci of several markers stay with the
+    host: IMA_ERR_STATE / IMA_ERR_ARG before anything runs (an SW locus also
+    needs its allele range); no sweeps returns the chains' p(G) summed
+    afresh."""
     case = UgCase()
     u, kap = case.rates()
     tv = np.tile(case.d["tv0"], (case.nch, 1))
@@ -219,13 +238,14 @@ def test_updategenealogy_refuses_what_it_does_not_model():
         ctx.updategenealogy_sweep(np.arange(case.nch), tv, 1, rngs, u, kap)
     assert e.value.code == api.IMA_ERR_STATE
     ctx.close()
-    # an SW locus
-    ctx = api.Context(0)
-    ctx.add_locus_sw(10, 1)
-    ctx.set_chains(1, 2)
-    pm = popmodel.build(case.tree, case.npops, nomig=True)
-    ctx.set_popmodel(pm, *popmodel.priors(pm, 10.0, 0.0)[:2])
-    with pytest.raises(api.ImaError) as e:
-        ctx.updategenealogy_sweep(np.arange(2), tv[:2], 1, rngs[:2], np.ones(2), None)
-    assert e.value.code == api.IMA_ERR_ARG
-    ctx.close()
+    # an SW locus of two linked markers, and one without its allele range
+    for markers, rng_ in ((2, np.array([[0, 40]], np.int32)), (1, None)):
+        ctx = api.Context(0)
+        ctx.add_locus_sw(10, markers)
+        ctx.set_chains(1, 2)
+        pm = popmodel.build(case.tree, case.npops, nomig=True)
+        ctx.set_popmodel(pm, *popmodel.priors(pm, 10.0, 0.0)[:2])
+        with pytest.raises(api.ImaError) as e:
+            ctx.updategenealogy_sweep(np.arange(2), tv[:2], 1, rngs[:2], np.ones(2), None, allele_range=rng_)
+        assert e.value.code == api.IMA_ERR_ARG
+        ctx.close()
