@@ -1046,8 +1046,11 @@ def updgen_context(api, w, precision_hky=True):
     base frequencies, geometric heats."""
     from ima2p_gb300 import popmodel
     ctx = api.Context(0)
-    for loc in w.loci:
-        ctx.add_locus_hky(loc.seq, loc.mult, loc.totsites)
+    for l, loc in enumerate(w.loci):
+        if w.kind == "sw":
+            ctx.add_locus_sw(len(w.base[l].pop) // 2 + 1, 1)
+        else:
+            ctx.add_locus_hky(loc.seq, loc.mult, loc.totsites)
     ctx.set_chains(1, w.nch)
     pm = popmodel.build(w.tree, w.npops, nomig=True)
     th_max, th_min, _, _, _ = popmodel.priors(pm, 30.0, 0.0)
@@ -1063,7 +1066,10 @@ def updgen_context(api, w, precision_hky=True):
     ctx.set_locus_pops(np.ones(nl), w.samppop)
     for c in range(w.nch):
         for l in range(nl):
-            ctx.set_pi(c, l, w.loci[l].pi)
+            if w.kind == "sw":
+                ctx.set_alleles(c, l, w.alleles[l])
+            else:
+                ctx.set_pi(c, l, w.loci[l].pi)
     ctx.set_betas(ug_betas(w.nch))
     return ctx, pm, th_max, th_min
 
@@ -1082,16 +1088,22 @@ def updgen_cpu(args, w, pm, th_max, th_min):
     from oracle import pyoracle as O
     nl = len(w.loci)
     cores = os.cpu_count() or 1
-    ul = O.UgLoci([("hky", loc) for loc in w.loci], np.ones(nl), w.samppop)
+    if w.kind == "sw":
+        ul = O.UgLoci([("sw", len(w.base[l].pop) // 2 + 1, int(w.arange[l][0]), int(w.arange[l][1]))
+                       for l in range(nl)], np.ones(nl), w.samppop)
+    else:
+        ul = O.UgLoci([("hky", loc) for loc in w.loci], np.ones(nl), w.samppop)
     nc = min(w.nch, max(cores, 8))
     gens = [[w.base[l] for l in range(nl)] for _ in range(nc)]
-    pis = np.array([w.loci[l].pi for _ in range(nc) for l in range(nl)])
+    pis = np.array([np.zeros(4) if w.kind == "sw" else w.loci[l].pi for _ in range(nc) for l in range(nl)])
+    al = {(c, l): w.alleles[l] for c in range(nc) for l in range(nl)} if w.kind == "sw" else None
 
     def cpu_run(ns):
         rr = [O.UgRng(1000 + c) for c in range(nc)]
         t = time.perf_counter()
         st = O.ug_run(pm, th_max, th_min, ul, gens, np.tile(w.tvals, (nc, 1)), ug_betas(nc),
-                      np.tile(w.u, nc), np.tile(w.kappa, nc), pis, ns, rr, nthreads=cores, record=False)[0]
+                      np.tile(w.u, nc), np.tile(w.kappa, nc), pis, ns, rr, nthreads=cores, record=False,
+                      alleles=al)[0]
         assert st == 0
         return time.perf_counter() - t
 
@@ -1121,15 +1133,17 @@ def measure_updgen(args, api, w, sweeps):
     tv = np.tile(w.tvals, (nch, 1))
     u, kap = np.tile(w.u, nch), np.tile(w.kappa, nch)
     rngs = [api.UgRng(1000 + c) for c in range(nch)]
-    ctx.updategenealogy_sweep(chains, tv, args.warmup, rngs, u, kap, precision=api.PREC_FAST)
+    ar = w.arange
+    ctx.updategenealogy_sweep(chains, tv, args.warmup, rngs, u, kap, precision=api.PREC_FAST, allele_range=ar)
     ctx.synchronize()
     t0 = time.perf_counter()
-    ctx.updategenealogy_sweep(chains, tv, 0, rngs, u, kap, precision=api.PREC_FAST)
+    ctx.updategenealogy_sweep(chains, tv, 0, rngs, u, kap, precision=api.PREC_FAST, allele_range=ar)
     setup_s = time.perf_counter() - t0
     n0 = ctx.launch_count()
     with Clocks(0) as clk:
         t0 = time.perf_counter()
-        acc, top, probg = ctx.updategenealogy_sweep(chains, tv, sweeps, rngs, u, kap, precision=api.PREC_FAST)
+        acc, top, probg = ctx.updategenealogy_sweep(chains, tv, sweeps, rngs, u, kap, precision=api.PREC_FAST,
+                                                    allele_range=ar)
         wall = time.perf_counter() - t0
     n_timed = ctx.launch_count() - n0
     # where a sweep's device time goes: the same call again with an event pair
@@ -1137,11 +1151,11 @@ def measure_updgen(args, api, w, sweeps):
     ctx.set_profiling(True)
     kinds = {"proposal_and_decision": api.K_UG, "treeweight": api.K_TREEWEIGHT, "hky": api.K_HKY_FAST}
     k0 = {k: ctx.kernel_stats(v) for k, v in kinds.items()}
-    ctx.updategenealogy_sweep(chains, tv, sweeps, rngs, u, kap, precision=api.PREC_FAST)
+    ctx.updategenealogy_sweep(chains, tv, sweeps, rngs, u, kap, precision=api.PREC_FAST, allele_range=ar)
     k1 = {k: ctx.kernel_stats(v) for k, v in kinds.items()}
     ctx.set_profiling(False)
     t0 = time.perf_counter()
-    ctx.updategenealogy_sweep(chains, tv, sweeps, rngs, u, kap, precision=api.PREC_FP64)
+    ctx.updategenealogy_sweep(chains, tv, sweeps, rngs, u, kap, precision=api.PREC_FP64, allele_range=ar)
     wall64 = time.perf_counter() - t0
     ctx.close()
     props = sweeps * nch * nl
@@ -1167,11 +1181,12 @@ def measure_updgen(args, api, w, sweeps):
 
 def run_updgen(args):
     from ima2p_gb300 import api, workloads
-    w = workloads.make_updgen(nch=args.updgen_chains)
+    w = (workloads.make_updgen_sw if args.updgen_model == "sw" else workloads.make_updgen)(nch=args.updgen_chains)
     sub = measure_updgen(args, api, w, max(1, min(args.steps, 20)))
     line = {"metric": sub.pop("metric"), "value": sub.pop("value"), "unit": sub.pop("unit"), "n_gpus": 1,
             "steps": sub["sweeps"], "warmup": args.warmup, "ms_per_step": sub["ms_per_sweep"],
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "ff32 HKY + fp64 weights",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp64 (SW terms and weights)" if w.kind == "sw" else "ff32 HKY + fp64 weights",
             "data": "synthetic population-labelled genealogies (no migration) and HKY data"}
     line.update(sub)
     print(json.dumps(line), flush=True)
@@ -1333,6 +1348,7 @@ def run_all(args):
     configs["config5_surface"] = measure_surface(args, api, min(args.steps, 20), not args.no_peak_search, dev)
     configs["genealogy_update"] = measure_updgen(args, api, workloads.make_updgen(), 5)
     configs["genealogy_update_1024_chains"] = measure_updgen(args, api, workloads.make_updgen(nch=1024), 3)
+    configs["genealogy_update_sw"] = measure_updgen(args, api, workloads.make_updgen_sw(), 3)
     emit(args, head, METRIC, dist, {"configs": configs})
 
 
@@ -1353,7 +1369,7 @@ def run_reference(args):
     name = "sw" if args.workload == "all" else args.workload
     if name == "updgen":
         from ima2p_gb300 import popmodel
-        w = workloads.make_updgen()
+        w = (workloads.make_updgen_sw if args.updgen_model == "sw" else workloads.make_updgen)()
         pm = popmodel.build(w.tree, w.npops, nomig=True)
         th_max, th_min, _, _, _ = popmodel.priors(pm, 30.0, 0.0)
         cpu = updgen_cpu(args, w, pm, th_max, th_min)
@@ -1416,12 +1432,12 @@ def run_reference(args):
             "config5_surface": surface_arm(),
         }
         from ima2p_gb300 import popmodel
-        w = workloads.make_updgen()
-        pm = popmodel.build(w.tree, w.npops, nomig=True)
-        th_max, th_min, _, _, _ = popmodel.priors(pm, 30.0, 0.0)
-        cpu = updgen_cpu(args, w, pm, th_max, th_min)
-        line["configs"]["genealogy_update"] = {"value": cpu["value"], "unit": cpu["unit"],
-                                               "config": {"workload": w.describe}, "cpu_baseline": cpu}
+        for key, w in (("genealogy_update", workloads.make_updgen()), ("genealogy_update_sw", workloads.make_updgen_sw())):
+            pm = popmodel.build(w.tree, w.npops, nomig=True)
+            th_max, th_min, _, _, _ = popmodel.priors(pm, 30.0, 0.0)
+            cpu = updgen_cpu(args, w, pm, th_max, th_min)
+            line["configs"][key] = {"value": cpu["value"], "unit": cpu["unit"], "config": {"workload": w.describe},
+                                    "cpu_baseline": cpu}
     print(json.dumps(line), flush=True)
 
 
@@ -1440,7 +1456,9 @@ def main():
     ap.add_argument("--no-peak-search", action="store_true", help="surface: skip the marginals and peak search")
     ap.add_argument("--popmig-g", type=int, default=300000, help="popmig: saved genealogies")
     ap.add_argument("--peaks-cpu-g", type=int, default=6000, help="popmig: genealogies in the CPU peaks sample")
-    ap.add_argument("--updgen-chains", type=int, default=32, help="updgen: chains (config 2: 32)")
+    ap.add_argument("--updgen-chains", type=int, default=32, help="updgen: chains (config 2: 32, config 3: 64)")
+    ap.add_argument("--updgen-model", default="hky", choices=["hky", "sw"],
+                    help="updgen: config-2 HKY loci or config-3 SW loci")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -202,18 +202,21 @@ def make(name):
 
 @dataclasses.dataclass
 class UgWorkload:
-    """Population-labelled genealogies and HKY data for the genealogy
-    update: every chain starts from the locus's own coalescent draw."""
+    """Population-labelled genealogies and data for the genealogy update:
+    every chain starts from the locus's own coalescent draw."""
     describe: str
     tree: str
     npops: int
     tvals: list
-    loci: list            # HKYLocus per locus
+    kind: str             # "hky" or "sw"
+    loci: list            # HKYLocus per locus (hky)
     base: list            # synth.LabelledGenealogy per locus
     samppop: np.ndarray   # [nloci][npops]
     u: np.ndarray         # [nloci]
     kappa: np.ndarray     # [nloci]
     nch: int
+    alleles: list = None       # sw: every node's allele per locus
+    arange: np.ndarray = None  # sw: [nloci][2] allele range
 
 
 def make_updgen(seed=1006, nloci=50, nch=32, ncopies=20, nbases=1000, tsplit=1.5, theta=10.0):
@@ -232,5 +235,27 @@ def make_updgen(seed=1006, nloci=50, nch=32, ncopies=20, nbases=1000, tsplit=1.5
     return UgWorkload("genealogy update: 2 pops (no migration, split at %g), %d HKY loci x (%d+%d) x %d bp, "
                       "%d chains, one proposal per chain-locus per sweep" % (tsplit, nloci, ncopies, ncopies,
                                                                              nbases, nch),
-                      "(0,1):2", 2, [tsplit], loci, base, np.tile([ncopies, ncopies], (nloci, 1)).astype(np.int32),
-                      ul, kap, nch)
+                      "(0,1):2", 2, [tsplit], "hky", loci, base,
+                      np.tile([ncopies, ncopies], (nloci, 1)).astype(np.int32), ul, kap, nch)
+
+
+def make_updgen_sw(seed=1007, nloci=100, nch=64, per_pop=30, tvals=(0.8, 1.6), theta=4.0):
+    """The sw workload's shapes under the no-migration model: 3 sampled
+    populations of a 5-population tree, stepwise loci with alleles
+    simulated on each locus's genealogy (root allele 20), lognormal(0, 0.5)
+    rate scalars; each locus's allele range is its alleles' widened by 5."""
+    rng = np.random.default_rng(seed)
+    ul = _loci_u(rng, nloci)
+    splits = [(tvals[0], 0, 1, 3), (tvals[1], 2, 3, 4)]
+    base, alleles, ar = [], [], []
+    for li in range(nloci):
+        lg = synth.sim_im_labeled(rng, [per_pop] * 3, [theta] * 5, 0.0, splits)
+        A = synth.sw_alleles(rng, lg.g, float(ul[li]))
+        base.append(lg)
+        alleles.append(A)
+        ar.append([int(A.min()) - 5, int(A.max()) + 5])
+    return UgWorkload("genealogy update: 3 sampled pops of a 5-pop tree (no migration), %d SW loci x %d copies, "
+                      "%d chains, one proposal per chain-locus per sweep" % (nloci, 3 * per_pop, nch),
+                      "((0,1):3,2):4", 3, list(tvals), "sw", [None] * nloci, base,
+                      np.tile([per_pop] * 3, (nloci, 1)).astype(np.int32), ul, np.ones(nloci), nch, alleles,
+                      np.array(ar, np.int32))
