@@ -1346,9 +1346,11 @@ def run_all(args):
     configs["config2_hky"] = measure_lik(args, api, workloads.make("hky"), sub_steps, dist, dev, hky_legs=True)
     configs["config4_mixed"] = measure_lik(args, api, workloads.make("mixed"), min(args.steps, 30), dist, dev)
     configs["config5_surface"] = measure_surface(args, api, min(args.steps, 20), not args.no_peak_search, dev)
-    configs["genealogy_update"] = measure_updgen(args, api, workloads.make_updgen(), 5)
-    configs["genealogy_update_1024_chains"] = measure_updgen(args, api, workloads.make_updgen(nch=1024), 3)
-    configs["genealogy_update_sw"] = measure_updgen(args, api, workloads.make_updgen_sw(), 3)
+    # 20 sweeps: a timed call of 40-200 ms, long against the clock sampler's
+    # 200 ms queries (one of them in a 100 ms call moved its rate 3x)
+    configs["genealogy_update"] = measure_updgen(args, api, workloads.make_updgen(), 20)
+    configs["genealogy_update_1024_chains"] = measure_updgen(args, api, workloads.make_updgen(nch=1024), 20)
+    configs["genealogy_update_sw"] = measure_updgen(args, api, workloads.make_updgen_sw(), 20)
     emit(args, head, METRIC, dist, {"configs": configs})
 
 
