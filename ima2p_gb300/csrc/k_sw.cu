@@ -482,30 +482,28 @@ __global__ void __launch_bounds__(32) k_ug_sw(UgArgs a)
   const int n = it.n, maxnl = 2 * a.maxn;
   LocalRng g;
   rng_load(g, a.rng + w, s_mt, lane);
+  const NodeRec *nd = a.nodes + it.node_off;
+  const double *t = a.t64 + it.node_off;
+  int32_t *A = a.alleles + it.al_off;
+  double *dl = a.dlike + it.dl_off;
+  const int32_t *bka = a.bk_A + (size_t)w * maxnl;
+  const double *bkd = a.bk_dl + (size_t)w * maxnl;
+  const NodeRec *bkn = a.bk_nodes + (size_t)w * maxnl;
+  const int32_t *eo = a.edges + 4 * (size_t)w;
+  const int edge = eo[0], freed = eo[1], oldsis = eo[2], newsis = eo[3];
+  const double u = a.u_cl[(size_t)w * a.nloci + a.locus];
+  const int e[3] = {edge, newsis, nd[edge].down};
+  // lane 0: the allele draw, in the generator's order
+  int oldA = 0, newA = 0, dA = 0;
+  double holdsis = 0.0, oldlikeadj = 0.0, geotermnew = 0.0;
+  bool fdown = false;
   if (lane == 0) {
-    const NodeRec *nd = a.nodes + it.node_off;
-    const double *t = a.t64 + it.node_off;
-    int32_t *A = a.alleles + it.al_off;
-    double *dl = a.dlike + it.dl_off;
-    const int32_t *bka = a.bk_A + (size_t)w * maxnl;
-    const double *bkd = a.bk_dl + (size_t)w * maxnl;
-    const NodeRec *bkn = a.bk_nodes + (size_t)w * maxnl;
-    const int32_t *eo = a.edges + 4 * (size_t)w;
-    const int edge = eo[0], freed = eo[1], oldsis = eo[2], newsis = eo[3];
-    const double u = a.u_cl[(size_t)w * a.nloci + a.locus];
     const int minA = a.arange[2 * a.locus], maxA = a.arange[2 * a.locus + 1];
-    const int oldA = A[freed];
-    const double holdsis = (newsis != oldsis) ? dl[newsis] : 0.0;
-    const bool fdown = bkn[freed].down != -1;
+    oldA = A[freed];
+    holdsis = (newsis != oldsis) ? dl[newsis] : 0.0;
+    fdown = bkn[freed].down != -1;
     const double cp2 = fdown ? bkd[freed] : 0.0;
-    const int holddownA = fdown ? bka[bkn[freed].down] : -1;
-    const double oldlikeadj = bkd[edge] + bkd[oldsis] + cp2 + holdsis;
-    const int e[3] = {edge, newsis, nd[edge].down};
-    double tt[3] = {0.0, 0.0, 0.0};
-    for (int i = 0; i < 3; i++) {
-      const double upt = e[i] >= n ? t[nd[e[i]].up0] : 0.0;
-      if (nd[e[i]].down != -1) tt[i] = t[e[i]] - upt;
-    }
+    oldlikeadj = bkd[edge] + bkd[oldsis] + cp2 + holdsis;
     int wsumdiff = 0, j = 0;
     for (int i = 0; i < 3; i++)
       if (nd[e[i]].down != -1) {
@@ -513,33 +511,60 @@ __global__ void __launch_bounds__(32) k_ug_sw(UgArgs a)
         wsumdiff += abs(d);
         j++;
       }
-    double geotermnew = j / ((double)(wsumdiff + j));
+    geotermnew = j / ((double)(wsumdiff + j));
     if (geotermnew > 0.95) geotermnew = 0.95;
-    int dA = (int)ceil(log(uniform(g)) / log(1.0 - geotermnew)) - 1;  // geometric(), utilities.cpp:609-617
+    dA = (int)ceil(log(uniform(g)) / log(1.0 - geotermnew)) - 1;  // geometric(), utilities.cpp:609-617
     if (bitran(g)) dA = -dA;
-    int newA;
     if (dA >= 0) newA = (maxA < oldA + dA) ? maxA : oldA + dA;
     else newA = (minA > oldA + dA) ? minA : oldA + dA;
     A[freed] = newA;
     dA = newA - oldA;
+  }
+  newA = __shfl_sync(0xffffffffu, newA, 0);
+  // The four branch terms, one lane each through one code path: lane 0 the
+  // old sister's branch, lane 1 + i the branch above e[i].  A term reads the
+  // alleles as they stand after the draw (the freed node's from newA).
+  // -(len * u) is the reference's (-len) * u exactly: rounding to nearest is
+  // symmetric in sign.
+  auto allele = [&](int v) { return v == freed ? newA : A[v]; };
+  bool has = false;
+  int d = 0;
+  double len = 0.0;
+  if (lane == 0) {
     if (nd[oldsis].down != -1 && oldsis != newsis) {
-      const double upt = oldsis >= n ? t[nd[oldsis].up0] : 0.0;
-      const int d = A[oldsis] - A[nd[oldsis].down];
-      const double x = (t[oldsis] - upt) * u;
-      dl[oldsis] = __dadd_rn(__dmul_rn(-(t[oldsis] - upt), u), log(bessi_64(d, x)));
-    } else {
-      dl[oldsis] = 0.0;
+      len = t[oldsis] - (oldsis >= n ? t[nd[oldsis].up0] : 0.0);
+      d = allele(oldsis) - allele(nd[oldsis].down);
+      has = true;
     }
-    double likeadj = dl[oldsis];
+  } else if (lane < 4) {
+    const int v = lane == 1 ? e[0] : (lane == 2 ? e[1] : e[2]);
+    if (nd[v].down != -1) {
+      len = t[v] - (v >= n ? t[nd[v].up0] : 0.0);
+      d = (lane < 3 ? allele(v) : allele(nd[v].down)) - newA;
+      has = true;
+    }
+  }
+  double term = 0.0;
+  if (has) {
+    const double x = len * u;
+    term = __dadd_rn(-x, log(bessi_64(d, x)));
+  }
+  const unsigned hasm = __ballot_sync(0xffffffffu, has);
+  const double tm0 = __shfl_sync(0xffffffffu, term, 0), tm1 = __shfl_sync(0xffffffffu, term, 1);
+  const double tm2 = __shfl_sync(0xffffffffu, term, 2), tm3 = __shfl_sync(0xffffffffu, term, 3);
+  if (lane == 0) {
+    // written and summed in the reference's order (finishSWupdateA)
+    dl[oldsis] = tm0;
+    double likeadj = tm0;
+    const double tmi[3] = {tm1, tm2, tm3};
     for (int i = 0; i < 3; i++)
-      if (nd[e[i]].down != -1) {
-        const int d = (i < 2 ? A[e[i]] : A[nd[e[i]].down]) - newA;
-        const double x = tt[i] * u;
-        dl[e[i]] = __dadd_rn(-x, log(bessi_64(d, x)));
-        likeadj += dl[e[i]];
+      if ((hasm >> (i + 1)) & 1) {
+        dl[e[i]] = tmi[i];
+        likeadj += tmi[i];
       }
-    wsumdiff = abs(bka[edge] - newA) + abs(bka[oldsis] - newA);
-    j = 2;
+    const int holddownA = fdown ? bka[bkn[freed].down] : -1;
+    int wsumdiff = abs(bka[edge] - newA) + abs(bka[oldsis] - newA);
+    int j = 2;
     if (fdown) {
       wsumdiff += abs(holddownA - newA);
       j++;
