@@ -315,7 +315,7 @@ struct ima_ctx {
   std::vector<Batch> ugb;
   // the genealogy update's streams: weights, likelihoods and decisions run
   // behind the proposals (on st), ordered by per-step events
-  cudaStream_t ug_sw = nullptr, ug_sw2 = nullptr, ug_sh = nullptr, ug_sh2 = nullptr, ug_sd = nullptr;
+  cudaStream_t ug_sw = nullptr, ug_sw2 = nullptr, ug_sw3 = nullptr, ug_sh = nullptr, ug_sh2 = nullptr, ug_sd = nullptr;
   std::vector<cudaEvent_t> ug_ev;  // [4][ring slots]: proposal, weights, likelihood, decision done
   // items whose tree lengths are still to be summed from their device times
   // (re-timings without lengths): done when a reader needs them
@@ -516,7 +516,7 @@ extern "C" void ima_gpu_destroy(ima_ctx *c)
   if (c->t1) cudaEventDestroy(c->t1);
 
   for (auto e : c->ug_ev) cudaEventDestroy(e);
-  for (cudaStream_t q : {c->ug_sw, c->ug_sw2, c->ug_sh, c->ug_sh2, c->ug_sd})
+  for (cudaStream_t q : {c->ug_sw, c->ug_sw2, c->ug_sw3, c->ug_sh, c->ug_sh2, c->ug_sd})
     if (q) cudaStreamDestroy(q);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
@@ -4348,7 +4348,7 @@ extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t 
   a.arange = d_arange;
   a.u_cl = d_ucl;
   if (!c->ug_sd) {
-    for (cudaStream_t *q : {&c->ug_sw, &c->ug_sw2, &c->ug_sh, &c->ug_sh2, &c->ug_sd})
+    for (cudaStream_t *q : {&c->ug_sw, &c->ug_sw2, &c->ug_sw3, &c->ug_sh, &c->ug_sh2, &c->ug_sd})
       r = r ? r : c->cuda(cudaStreamCreateWithFlags(q, cudaStreamNonBlocking), "streams");
     if (r) return r;
   }
@@ -4361,9 +4361,9 @@ extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t 
   cudaEvent_t *evP = c->ug_ev.data(), *evW = evP + 4, *evH = evP + 8, *evD = evP + 12;
   // The steps: one locus of every listed chain at a time.  Each chain's
   // proposals follow one another on st (they share its generator), its
-  // decisions on ug_sd (they share its sums); a step's weights and its
-  // likelihoods (each on two streams used by turns: consecutive steps touch
-  // different loci) wait for its proposal, its decision for both and
+  // decisions on ug_sd (they share its sums); a step's weights (on three
+  // streams used by turns) and its likelihoods (on two; consecutive steps
+  // touch different loci) wait for its proposal, its decision for both and
   // for the previous decision.  So proposals, weights and likelihoods of
   // the next steps run while a decision does, up to R steps ahead.  After an
   // IS step the next proposal waits for the decision: an IS decision draws
@@ -4405,10 +4405,9 @@ extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t 
       if (step >= R) cudaStreamWaitEvent(c->st, evD[slot], 0);
       if (prev_is) cudaStreamWaitEvent(c->st, evD[(step - 1) % R], 0);
       c->launch(IMA_K_UG, 0.0, [&] { launch_ug_propose(u_, c->st); });
-      if (u_.sw) c->launch(IMA_K_UG, 0.0, [&] { launch_ug_sw(u_, c->st); });
       cudaEventRecord(evP[slot], c->st);
       w.perm = d_perm + (size_t)l * nch;
-      cudaStream_t sw = (step & 1) ? c->ug_sw2 : c->ug_sw;
+      cudaStream_t sw = (step % 3 == 0) ? c->ug_sw : (step % 3 == 1 ? c->ug_sw2 : c->ug_sw3);
       cudaStreamWaitEvent(sw, evP[slot], 0);
       int lr = 0;
       c->launch(IMA_K_TREEWEIGHT, 0.0, [&] { lr = launch_treeweight(w, h, sw); }, sw);
@@ -4416,11 +4415,15 @@ extern "C" int ima_gpu_updategenealogy_sweep(ima_ctx *c, int nch, const int32_t 
       c->launches += lr - 1;
       cudaEventRecord(evW[slot], sw);
       cudaStreamWaitEvent(c->ug_sd, evW[slot], 0);
-      if (!u_.sw) {  // a stepwise locus's likelihood change came with its proposal
+      {  // the likelihood: a stepwise locus's branch terms from its proposal's edges and allele
         cudaStream_t sh = (step & 1) ? c->ug_sh2 : c->ug_sh;
         cudaStreamWaitEvent(sh, evP[slot], 0);
-        if (!u_.hky) cudaStreamWaitEvent(sh, evW[slot], 0);  // the IS likelihood reads the new lengths
-        enqueue(c, b, sh);
+        if (u_.sw) {
+          c->launch(IMA_K_UG, 0.0, [&] { launch_ug_sw(u_, sh); }, sh);
+        } else {
+          if (!u_.hky) cudaStreamWaitEvent(sh, evW[slot], 0);  // the IS likelihood reads the new lengths
+          enqueue(c, b, sh);
+        }
         cudaEventRecord(evH[slot], sh);
         cudaStreamWaitEvent(c->ug_sd, evH[slot], 0);
       }

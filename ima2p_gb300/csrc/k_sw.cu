@@ -475,16 +475,13 @@ float2 split(double v)
 // rounded one at a time (no contraction), as the reference writes them.
 __global__ void __launch_bounds__(32) k_ug_sw(UgArgs a)
 {
-  __shared__ __align__(16) uint32_t s_mt[624];
   const int w = blockIdx.x, lane = threadIdx.x;
   const int ci = a.chains[w], item = ci * a.nloci + a.locus;
   const ItemDev it = a.items[item];
   const int n = it.n, maxnl = 2 * a.maxn;
-  LocalRng g;
-  rng_load(g, a.rng + w, s_mt, lane);
   const NodeRec *nd = a.nodes + it.node_off;
   const double *t = a.t64 + it.node_off;
-  int32_t *A = a.alleles + it.al_off;
+  const int32_t *A = a.alleles + it.al_off;
   double *dl = a.dlike + it.dl_off;
   const int32_t *bka = a.bk_A + (size_t)w * maxnl;
   const double *bkd = a.bk_dl + (size_t)w * maxnl;
@@ -493,13 +490,11 @@ __global__ void __launch_bounds__(32) k_ug_sw(UgArgs a)
   const int edge = eo[0], freed = eo[1], oldsis = eo[2], newsis = eo[3];
   const double u = a.u_cl[(size_t)w * a.nloci + a.locus];
   const int e[3] = {edge, newsis, nd[edge].down};
-  // lane 0: the allele draw, in the generator's order
-  int oldA = 0, newA = 0, dA = 0;
+  // the proposal drew the freed node's allele (bka holds the alleles before)
+  const int oldA = bka[freed], newA = A[freed], dA = newA - oldA;
   double holdsis = 0.0, oldlikeadj = 0.0, geotermnew = 0.0;
   bool fdown = false;
   if (lane == 0) {
-    const int minA = a.arange[2 * a.locus], maxA = a.arange[2 * a.locus + 1];
-    oldA = A[freed];
     holdsis = (newsis != oldsis) ? dl[newsis] : 0.0;
     fdown = bkn[freed].down != -1;
     const double cp2 = fdown ? bkd[freed] : 0.0;
@@ -507,26 +502,17 @@ __global__ void __launch_bounds__(32) k_ug_sw(UgArgs a)
     int wsumdiff = 0, j = 0;
     for (int i = 0; i < 3; i++)
       if (nd[e[i]].down != -1) {
-        const int d = (i < 2 ? A[e[i]] : A[nd[e[i]].down]) - oldA;
-        wsumdiff += abs(d);
+        wsumdiff += abs((i < 2 ? bka[e[i]] : bka[nd[e[i]].down]) - oldA);
         j++;
       }
     geotermnew = j / ((double)(wsumdiff + j));
     if (geotermnew > 0.95) geotermnew = 0.95;
-    dA = (int)ceil(log(uniform(g)) / log(1.0 - geotermnew)) - 1;  // geometric(), utilities.cpp:609-617
-    if (bitran(g)) dA = -dA;
-    if (dA >= 0) newA = (maxA < oldA + dA) ? maxA : oldA + dA;
-    else newA = (minA > oldA + dA) ? minA : oldA + dA;
-    A[freed] = newA;
-    dA = newA - oldA;
   }
-  newA = __shfl_sync(0xffffffffu, newA, 0);
   // The four branch terms, one lane each through one code path: lane 0 the
-  // old sister's branch, lane 1 + i the branch above e[i].  A term reads the
-  // alleles as they stand after the draw (the freed node's from newA).
-  // -(len * u) is the reference's (-len) * u exactly: rounding to nearest is
-  // symmetric in sign.
-  auto allele = [&](int v) { return v == freed ? newA : A[v]; };
+  // old sister's branch, lane 1 + i the branch above e[i], from the alleles
+  // after the draw.  -(len * u) is the reference's (-len) * u exactly:
+  // rounding to nearest is symmetric in sign.
+  auto allele = [&](int v) { return A[v]; };
   bool has = false;
   int d = 0;
   double len = 0.0;
@@ -577,10 +563,7 @@ __global__ void __launch_bounds__(32) k_ug_sw(UgArgs a)
     a.aterm[w] = at;
     a.holdsis[w] = holdsis;
     a.swnew[w] = 0.0 + (a.pdg[item] + __dadd_rn(likeadj, -oldlikeadj));
-    a.ustore[w] = uniform(g);  // the acceptance uniform
   }
-  __syncwarp();
-  rng_store(g, a.rng + w, lane);
 }
 
 }  // namespace

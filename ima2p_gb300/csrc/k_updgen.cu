@@ -328,9 +328,31 @@ __global__ void __launch_bounds__(32) k_ug_propose(UgArgs a)
     eo[1] = freed;
     eo[2] = oldsis;
     eo[3] = newsis;
-    // the acceptance uniform, next in the stream (a stepwise locus draws its
-    // allele first, in k_ug_sw, and the uniform after it)
-    if (a.predraw && !a.sw) a.ustore[w] = uniform(g);
+    if (a.sw) {
+      // finishSWupdateA's allele draw (update_gtree_common.cpp:2219-2362):
+      // a geometric step whose parameter comes from the freed node's
+      // neighbours' distances, signed by bitran, clamped to the locus's
+      // range.  k_ug_sw forms the branch terms from the result.
+      int32_t *A = a.alleles + it.al_off;
+      const int oldA = A[freed];
+      const int e3[3] = {edge, newsis, nd[edge].down};
+      int wsumdiff = 0, j = 0;
+      for (int i = 0; i < 3; i++)
+        if (nd[e3[i]].down != -1) {
+          wsumdiff += abs((i < 2 ? A[e3[i]] : A[nd[e3[i]].down]) - oldA);
+          j++;
+        }
+      double geo = j / ((double)(wsumdiff + j));
+      if (geo > 0.95) geo = 0.95;
+      int dA = (int)ceil(log(uniform(g)) / log(1.0 - geo)) - 1;  // geometric(), utilities.cpp:609-617
+      if (bitran(g)) dA = -dA;
+      const int minA = a.arange[2 * a.locus], maxA = a.arange[2 * a.locus + 1];
+      if (dA >= 0) A[freed] = (maxA < oldA + dA) ? maxA : oldA + dA;
+      else A[freed] = (minA > oldA + dA) ? minA : oldA + dA;
+    }
+    // the acceptance uniform, next in the stream (after a stepwise locus's
+    // allele draw)
+    if (a.predraw) a.ustore[w] = uniform(g);
     s_root = root;
   }
   __syncwarp();
