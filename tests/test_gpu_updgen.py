@@ -249,3 +249,85 @@ def test_updategenealogy_refuses_what_it_does_not_model():
             ctx.updategenealogy_sweep(np.arange(2), tv[:2], 1, rngs[:2], np.ones(2), None, allele_range=rng_)
         assert e.value.code == api.IMA_ERR_ARG
         ctx.close()
+
+
+@pytest.mark.parametrize("kind", ["sw", "hky"])
+def test_updategenealogy_matches_the_oracle_on_many_chains(kind):
+    """Many chains and more loci than the ring of step slots, so proposals,
+    weights (three streams by turns), likelihoods (two) and decisions run
+    steps ahead of one another: 48 chains x 9 loci x 3 sweeps on the
+    stepwise workload's shapes (5-population tree, 3 sampled) or the HKY
+    one's (2 populations), against the oracle's restatement run chain by
+    chain.  Accepted proposals per chain-locus, final topologies, population
+    labels and alleles exact; node times and p(G) to the last bits of the
+    device's log and sqrt in the slide's normal deviate."""
+    from ima2p_gb300 import workloads
+    from oracle import pyoracle as O
+
+    nch, nsw = 48, 3
+    if kind == "sw":
+        w = workloads.make_updgen_sw(nloci=9, nch=nch, per_pop=12)
+    else:
+        w = workloads.make_updgen(nloci=9, nch=nch, ncopies=10, nbases=300)
+    nl = len(w.loci)
+    pm = popmodel.build(w.tree, w.npops, nomig=True)
+    th_max, th_min, _, _, _ = popmodel.priors(pm, 30.0, 0.0)
+    ctx = api.Context(0)
+    for l, loc in enumerate(w.loci):
+        if kind == "sw":
+            ctx.add_locus_sw(len(w.base[l].pop) // 2 + 1, 1)
+        else:
+            ctx.add_locus_hky(loc.seq, loc.mult, loc.totsites)
+    ctx.set_chains(1, nch)
+    ctx.set_popmodel(pm, th_max, th_min)
+    ci = np.repeat(np.arange(nch, dtype=np.int32), nl)
+    li = np.tile(np.arange(nl, dtype=np.int32), nch)
+    flat = [w.base[l] for _ in range(nch) for l in range(nl)]
+    ctx.set_genealogies(ci, li, np.concatenate([g.g.up0 for g in flat]), np.concatenate([g.g.up1 for g in flat]),
+                        np.concatenate([g.g.down for g in flat]), np.concatenate([g.g.time for g in flat]),
+                        length=np.full(len(flat), -1.0))
+    ctx.set_labels(ci, li, flat)
+    ctx.set_locus_pops(np.ones(nl), w.samppop)
+    for c in range(nch):
+        for l in range(nl):
+            if kind == "sw":
+                ctx.set_alleles(c, l, w.alleles[l])
+            else:
+                ctx.set_pi(c, l, w.loci[l].pi)
+    betas = 1.0 / (1.0 + 0.05 * np.arange(nch))
+    ctx.set_betas(betas)
+    tv = np.tile(w.tvals, (nch, 1))
+    u, kap = np.tile(w.u, nch), np.tile(w.kappa, nch)
+    rngs = [api.UgRng(500 + c) for c in range(nch)]
+    acc, _, probg = ctx.updategenealogy_sweep(np.arange(nch), tv, nsw, rngs, u, kap, precision=api.PREC_FP64,
+                                              allele_range=w.arange)
+    if kind == "sw":
+        loci = O.UgLoci([("sw", len(w.base[l].pop) // 2 + 1, int(w.arange[l][0]), int(w.arange[l][1]))
+                         for l in range(nl)], np.ones(nl), w.samppop)
+        al = {(c, l): w.alleles[l] for c in range(nch) for l in range(nl)}
+        pis = np.zeros((nch * nl, 4))
+    else:
+        loci = O.UgLoci([("hky", loc) for loc in w.loci], np.ones(nl), w.samppop)
+        al = None
+        pis = np.array([w.loci[l].pi for _ in range(nch) for l in range(nl)])
+    ro = [O.UgRng(500 + c) for c in range(nch)]
+    st, res, _, _, pg, fin = O.ug_run(pm, th_max, th_min, loci, [[w.base[l] for l in range(nl)]] * nch, tv, betas,
+                                      u, kap, pis, nsw, ro, nthreads=8, alleles=al)
+    assert st == 0
+    np.testing.assert_array_equal(acc, res[..., 0].sum(axis=1))
+    assert 0 < acc.sum() < nch * nl * nsw
+    np.testing.assert_allclose(probg, pg, rtol=0, atol=1e-9)
+    o = 0
+    for k in range(nch * nl):
+        c, l = int(ci[k]), int(li[k])
+        nlines = len(flat[k].pop)
+        got = ctx.get_genealogy(c, l, nlines)
+        sl = slice(o, o + nlines)
+        for j in (0, 1, 2, 4):
+            np.testing.assert_array_equal(got[j], fin[j][sl])
+        nonroot = fin[2][sl] != -1
+        np.testing.assert_allclose(got[3][nonroot], fin[3][sl][nonroot], rtol=1e-12)
+        if kind == "sw":
+            np.testing.assert_array_equal(ctx.get_alleles(c, l, nlines), fin[5][sl])
+        o += nlines
+    ctx.close()
