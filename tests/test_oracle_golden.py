@@ -1,6 +1,6 @@
 """The CPU oracle against golden vectors produced by the compiled reference
 (tests/golden/make_golden.py).  This pins the restatement before it is used
-to judge any kernel."""
+to check any kernel."""
 import numpy as np
 import pytest
 
