@@ -26,7 +26,6 @@
 
 #include "ff.cuh"
 #include "internal.h"
-#include "ug_rng.cuh"
 
 namespace {
 

@@ -1,6 +1,6 @@
 // ug_rng.cuh -- a chain's generators for the genealogy-update kernels
-// (k_updgen.cu, k_sw.cu): the reference's uniform() (MT19937, utilities.cpp:
-// 323-427) and bitran (:438-455), staged for one kernel.
+// (k_updgen.cu): the reference's uniform() (MT19937, utilities.cpp:323-427)
+// and bitran (:438-455), staged for one kernel.
 #pragma once
 
 #include "internal.h"
