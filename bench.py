@@ -1179,10 +1179,17 @@ def measure_updgen(args, api, w, sweeps):
     }
 
 
+def updgen_workload(args):
+    """The genealogy-update workload both arms run: the model's (HKY: 32
+    chains, SW: 64) with --updgen-chains chains when given."""
+    from ima2p_gb300 import workloads
+    make = workloads.make_updgen_sw if args.updgen_model == "sw" else workloads.make_updgen
+    return make() if args.updgen_chains is None else make(nch=args.updgen_chains)
+
+
 def run_updgen(args):
-    from ima2p_gb300 import api, workloads
-    w = (workloads.make_updgen_sw if args.updgen_model == "sw" else workloads.make_updgen)(nch=args.updgen_chains)
-    sub = measure_updgen(args, api, w, max(1, min(args.steps, 20)))
+    from ima2p_gb300 import api
+    sub = measure_updgen(args, api, updgen_workload(args), max(1, min(args.steps, 20)))
     line = {"metric": sub.pop("metric"), "value": sub.pop("value"), "unit": sub.pop("unit"), "n_gpus": 1,
             "steps": sub["sweeps"], "warmup": args.warmup, "ms_per_step": sub["ms_per_sweep"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -1371,7 +1378,7 @@ def run_reference(args):
     name = "sw" if args.workload == "all" else args.workload
     if name == "updgen":
         from ima2p_gb300 import popmodel
-        w = (workloads.make_updgen_sw if args.updgen_model == "sw" else workloads.make_updgen)()
+        w = updgen_workload(args)
         pm = popmodel.build(w.tree, w.npops, nomig=True)
         th_max, th_min, _, _, _ = popmodel.priors(pm, 30.0, 0.0)
         cpu = updgen_cpu(args, w, pm, th_max, th_min)
@@ -1458,7 +1465,8 @@ def main():
     ap.add_argument("--no-peak-search", action="store_true", help="surface: skip the marginals and peak search")
     ap.add_argument("--popmig-g", type=int, default=300000, help="popmig: saved genealogies")
     ap.add_argument("--peaks-cpu-g", type=int, default=6000, help="popmig: genealogies in the CPU peaks sample")
-    ap.add_argument("--updgen-chains", type=int, default=32, help="updgen: chains (config 2: 32, config 3: 64)")
+    ap.add_argument("--updgen-chains", type=int, default=None,
+                    help="updgen: chains (default: the model's workload, 32 for hky, 64 for sw)")
     ap.add_argument("--updgen-model", default="hky", choices=["hky", "sw"],
                     help="updgen: config-2 HKY loci or config-3 SW loci")
     args = ap.parse_args()
